@@ -1,0 +1,361 @@
+/*
+ * socgpu.h -- C-ABI of the GB300 two-stream flux path for SOCRATES.
+ *
+ * This is the drop-in boundary a SOCRATES host program binds to (Fortran
+ * through ISO_C_BINDING, Python through ctypes).  Every entry point takes
+ * plain pointers and sizes; no CUDA or C++ type crosses the boundary.
+ *
+ * Conventions (identical to the reference's Fortran):
+ *   - Arrays are column-major with the profile index fastest, exactly as the
+ *     reference's derived types hold them, e.g. atm%p(nd_profile, nd_layer)
+ *     (src/radiance_core/def_atm.F90).  The allocated extent nd_* is passed
+ *     separately from the valid extent n_*.
+ *   - Level arrays run 0..n_layer (level 0 = top of atmosphere), layer
+ *     arrays 1..n_layer (layer i lies between levels i-1 and i).
+ *   - Option identifiers carry the reference's rad_pcf values
+ *     (src/radiance_core/rad_pcf.F90).  Status codes are the reference's
+ *     error codes (rad_pcf.F90:391-405).  No entry point stops the process;
+ *     failures return a status and a message.
+ *   - All arithmetic on the reference path is FP64.  SOCGPU_PRECISION_FP64
+ *     keeps that; SOCGPU_PRECISION_MIXED (no counterpart in the reference)
+ *     runs the bulk in FP32.
+ */
+#ifndef SOCGPU_H
+#define SOCGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SOCGPU_API __attribute__((visibility("default")))
+#else
+#define SOCGPU_API
+#endif
+
+#define SOCGPU_ABI_VERSION 1
+
+/* ---- status codes: rad_pcf.F90:391-405 ------------------------------- */
+#define SOCGPU_I_NORMAL             0
+#define SOCGPU_I_ERR_FATAL          1
+#define SOCGPU_I_ABORT_CALCULATION  2
+#define SOCGPU_I_ERR_IO             4
+#define SOCGPU_I_ERR_RANGE          5
+#define SOCGPU_I_ERR_EXIST          6
+
+/* ---- option identifiers (rad_pcf.F90 values) ------------------------- */
+#define SOCGPU_IP_SOLAR                 1   /* rad_pcf.F90:602 */
+#define SOCGPU_IP_INFRA_RED             2   /* rad_pcf.F90:604 */
+#define SOCGPU_IP_TWO_STREAM            1   /* rad_pcf.F90:176 */
+/* two-stream schemes, rad_pcf.F90:700-722 */
+#define SOCGPU_IP_EDDINGTON             2
+#define SOCGPU_IP_DISCRETE_ORD          4
+#define SOCGPU_IP_IFM                   5
+#define SOCGPU_IP_PIFM85                6
+#define SOCGPU_IP_ZDK_FLUX              7
+#define SOCGPU_IP_KRSCHG_FLUX           8
+#define SOCGPU_IP_COAKLEY_CHYLEK_1      9
+#define SOCGPU_IP_COAKLEY_CHYLEK_2     10
+#define SOCGPU_IP_MEADOR_WEAVER        11
+#define SOCGPU_IP_ELSASSER             12
+#define SOCGPU_IP_2S_TEST              14
+#define SOCGPU_IP_HEMI_MEAN            15
+#define SOCGPU_IP_PIFM80               16
+/* scattering treatment, rad_pcf.F90:539-545 */
+#define SOCGPU_IP_SCATTER_FULL          1
+#define SOCGPU_IP_NO_SCATTER_ABS        2
+#define SOCGPU_IP_NO_SCATTER_EXT        3
+/* direct-beam optical depth, rad_pcf.F90:553-557 */
+#define SOCGPU_IP_DIRECT_NOSCALING      0
+#define SOCGPU_IP_DIRECT_DELTA_SCALING  1
+#define SOCGPU_IP_DIRECT_CSR_SCALING    2
+/* solvers, rad_pcf.F90:566-572 */
+#define SOCGPU_IP_SOLVER_NO_SCAT        2
+#define SOCGPU_IP_SOLVER_HOMOGEN_DIRECT 13
+/* cloud schemes, rad_pcf.F90:313,322 */
+#define SOCGPU_IP_CLOUD_CLEAR           5
+#define SOCGPU_IP_CLOUD_MCICA          10
+/* cloud representation, rad_pcf.F90:238-254 */
+#define SOCGPU_IP_CLOUD_ICE_WATER       2
+/* cloud types, rad_pcf.F90:332-334 */
+#define SOCGPU_IP_CLOUD_TYPE_WATER      1
+#define SOCGPU_IP_CLOUD_TYPE_ICE        2
+/* condensed phases, rad_pcf.F90:494-496 */
+#define SOCGPU_IP_PHASE_WATER           1
+#define SOCGPU_IP_PHASE_ICE             2
+/* condensed-phase parametrizations, rad_pcf.F90:206,486 */
+#define SOCGPU_IP_DROP_PADE_2           5
+#define SOCGPU_IP_ICE_PADE_2_PHF       20
+/* gas overlap, rad_pcf.F90:427 */
+#define SOCGPU_IP_OVERLAP_RANDOM        2
+/* k scaling, rad_pcf.F90:412-416 and 509-515 */
+#define SOCGPU_IP_SCALE_NULL            0
+#define SOCGPU_IP_SCALE_BAND            1
+#define SOCGPU_IP_SCALE_TERM            2
+#define SOCGPU_IP_SCALE_FNC_NULL        0
+#define SOCGPU_IP_SCALE_POWER_LAW       1
+#define SOCGPU_IP_SCALE_POWER_QUAD      2
+#define SOCGPU_IP_SCALE_DOPPLER_QUAD    3
+/* Rayleigh schemes, rad_pcf.F90:729-731 */
+#define SOCGPU_IP_RAYLEIGH_TOTAL        1
+/* McICA overlap (socrates_cloud_gen.F90 ioverlap), rad_pcf.F90:294-300 */
+#define SOCGPU_IP_MAX_RAND              0
+#define SOCGPU_IP_RAND                  1
+#define SOCGPU_IP_EXPONENTIAL           2
+#define SOCGPU_IP_EXPONENTIAL_RAND      3
+/* McICA sampling, def_mcica.F90:22-26 */
+#define SOCGPU_IP_MCICA_FULL_SAMPLING    0
+#define SOCGPU_IP_MCICA_SINGLE_SAMPLING  1
+#define SOCGPU_IP_MCICA_OPTIMAL_SAMPLING 2
+
+/* ---- extensions with no counterpart in the reference ----------------- */
+#define SOCGPU_PRECISION_FP64   0   /* every operation in FP64 */
+#define SOCGPU_PRECISION_MIXED  1   /* FP32 bulk, stable reformulations */
+
+/* McICA random number generator */
+#define SOCGPU_RNG_LCG     0   /* the reference generator, socrates_cloud_gen.F90:48-50 */
+#define SOCGPU_RNG_PHILOX  1   /* counter-based Philox4x32-10 keyed by (seed, column, subcolumn, layer) */
+
+/* Limits of the device path. */
+#define SOCGPU_MAX_LAYER        512
+#define SOCGPU_MAX_BAND          64
+#define SOCGPU_MAX_GPOINT      4096
+#define SOCGPU_MAX_SPECIES       32
+#define SOCGPU_MAX_MODE          16
+#define SOCGPU_MAX_SUBCOL        64
+
+/* ---- spectral file ----------------------------------------------------
+ * A flat view of the reference's StrSpecData (src/radiance_core/
+ * def_spectrum.F90).  Pointers are host memory, Fortran layout, with the
+ * nd_* dimensions of the spectrum type.  NULL marks an absent block.    */
+typedef struct socgpu_spectrum_desc {
+    /* StrSpecDim */
+    int nd_band, nd_species, nd_k_term, nd_scale_variable;
+    int nd_thermal_coeff, nd_drop_type, nd_ice_type, nd_cloud_parameter;
+    /* StrSpecBasic, block 1 */
+    int n_band;
+    const double *wavelength_short;     /* (nd_band) [m] */
+    const double *wavelength_long;      /* (nd_band) [m] */
+    /* StrSpecSolar, blocks 2 and 3 */
+    const double *solar_flux_band;      /* (nd_band) fraction of the solar constant, or NULL */
+    int i_rayleigh_scheme;              /* SOCGPU_IP_RAYLEIGH_TOTAL */
+    const double *rayleigh_coeff;       /* (nd_band) [m2/kg], or NULL */
+    /* StrSpecGas, blocks 0, 4 and 5 */
+    int n_absorb;
+    const int    *type_absorb;          /* (nd_species) */
+    const int    *n_band_absorb;        /* (nd_band) */
+    const int    *index_absorb;         /* (nd_species, nd_band), 1-based species indices */
+    const int    *i_band_k;             /* (nd_band, nd_species) */
+    const int    *i_scale_k;            /* (nd_band, nd_species) */
+    const int    *i_scale_fnc;          /* (nd_band, nd_species) */
+    const double *k;                    /* (nd_k_term, nd_band, nd_species) [m2/kg] */
+    const double *w;                    /* (nd_k_term, nd_band, nd_species) */
+    const double *scale;                /* (nd_scale_variable, nd_k_term, nd_band, nd_species) */
+    const double *p_ref;                /* (nd_species, nd_band) [Pa] */
+    const double *t_ref;                /* (nd_species, nd_band) [K] */
+    const int    *l_doppler;            /* (nd_species) or NULL */
+    const double *doppler_cor;          /* (nd_species) or NULL */
+    /* StrSpecPlanck, block 6 */
+    int n_deg_fit;
+    double t_ref_planck;
+    const double *thermal_coeff;        /* (0:nd_thermal_coeff-1, nd_band) or NULL */
+    /* StrSpecDrop, block 10 */
+    const int    *l_drop_type;          /* (nd_drop_type) or NULL */
+    const int    *i_drop_parm;          /* (nd_drop_type) */
+    const double *drop_parm_list;       /* (nd_cloud_parameter, nd_band, nd_drop_type) */
+    /* StrSpecIce, block 12 */
+    const int    *l_ice_type;           /* (nd_ice_type) or NULL */
+    const int    *i_ice_parm;           /* (nd_ice_type) */
+    const double *ice_parm_list;        /* (nd_cloud_parameter, nd_band, nd_ice_type) */
+} socgpu_spectrum_desc;
+
+typedef int32_t socgpu_spectrum_handle;   /* > 0 when valid */
+
+/* ---- StrCtrl subset (src/radiance_core/def_control.F90) -------------- */
+typedef struct socgpu_control {
+    int isolir;                 /* SOCGPU_IP_SOLAR | SOCGPU_IP_INFRA_RED */
+    int i_angular_integration;  /* SOCGPU_IP_TWO_STREAM only */
+    int i_2stream;              /* two-stream scheme */
+    int i_scatter_method;       /* SOCGPU_IP_SCATTER_FULL | NO_SCATTER_ABS | NO_SCATTER_EXT */
+    int i_solver;               /* SOCGPU_IP_SOLVER_NO_SCAT | SOLVER_HOMOGEN_DIRECT */
+    int i_cloud;                /* SOCGPU_IP_CLOUD_CLEAR | SOCGPU_IP_CLOUD_MCICA */
+    int i_cloud_representation; /* SOCGPU_IP_CLOUD_ICE_WATER with McICA */
+    int i_gas_overlap;          /* SOCGPU_IP_OVERLAP_RANDOM */
+    int i_direct_tau;           /* SOCGPU_IP_DIRECT_DELTA_SCALING (default) | NOSCALING */
+    int l_rescale;              /* delta-rescaling of tau, omega and the phase function */
+    int n_order_forward;        /* order of the forward-scattering term (2: f = g^2) */
+    int l_ir_source_quad;       /* quadratic IR source */
+    int l_rayleigh;
+    int l_gas;
+    int l_aerosol_mode;         /* modal (UKCA-style) aerosol optics */
+    int l_flux_div;             /* accumulate the flux divergence per k-term */
+    int first_band, last_band;  /* 1-based, inclusive */
+    const double *weight_band;  /* (n_band) or NULL (all 1); device memory for
+                                   socgpu_radiance_calc_device */
+    int precision;              /* SOCGPU_PRECISION_* (extension) */
+} socgpu_control;
+
+/* ---- StrDim subset (src/radiance_core/def_dimen.F90) ----------------- */
+typedef struct socgpu_dimen {
+    int nd_profile, nd_layer;
+    int id_cloud_top;           /* first layer that may hold cloud (1-based) */
+    int nd_aerosol_mode;
+    int nd_cloud_component, nd_cloud_type;
+    int nd_subcol_gen, nd_subcol_req;
+} socgpu_dimen;
+
+/* ---- StrAtm (src/radiance_core/def_atm.F90) --------------------------- */
+typedef struct socgpu_atm {
+    int n_profile, n_layer;
+    const double *p;             /* (nd_profile, nd_layer) [Pa] */
+    const double *t;             /* (nd_profile, nd_layer) [K] */
+    const double *p_level;       /* (nd_profile, 0:nd_layer) [Pa] */
+    const double *t_level;       /* (nd_profile, 0:nd_layer) [K] */
+    const double *mass;          /* (nd_profile, nd_layer) [kg/m2] */
+    const double *gas_mix_ratio; /* (nd_profile, nd_layer, nd_species) [kg/kg] */
+} socgpu_atm;
+
+/* ---- StrBound (src/radiance_core/def_bound.F90) ----------------------- */
+typedef struct socgpu_bound {
+    const double *zen_0;         /* (nd_profile) secant of the solar zenith angle */
+    const double *solar_irrad;   /* (nd_profile) [W/m2] */
+    const double *rho_alb;       /* (nd_profile, 2, nd_band): diffuse (1) and direct (2) albedo */
+    const double *t_ground;      /* (nd_profile) [K] */
+} socgpu_bound;
+
+/* ---- StrAer modal part (src/radiance_core/def_aer.F90:36-44) ---------- */
+typedef struct socgpu_aer {
+    int n_mode;
+    const double *mode_mix_ratio;   /* (nd_profile, nd_layer, nd_aerosol_mode) */
+    const double *mode_absorption;  /* (nd_profile, nd_layer, nd_aerosol_mode, nd_band) [m2/kg] */
+    const double *mode_scattering;  /* same */
+    const double *mode_asymmetry;   /* same */
+} socgpu_aer;
+
+/* ---- StrCld with the McICA state (def_cld.F90, def_mcica.F90) --------
+ * Cloudy arrays span layers id_cloud_top..nd_layer.  The McICA arrays are
+ * what set_cld_mcica (socrates_set_cld_mcica.F90:82-228) leaves in cld.   */
+typedef struct socgpu_cld {
+    int n_condensed;
+    const int *type_condensed;        /* (nd_cloud_component) ip_clcmp_* */
+    const int *i_cloud_type;          /* (nd_cloud_component) cloud type of each component */
+    const int *i_condensed_param;     /* (nd_cloud_component) parametrization (ip_drop_pade_2, ip_ice_pade_2_phf) */
+    const int *i_condensed_type;      /* (nd_cloud_component) 1-based drop type (water) or ice type (ice)
+                                         in the spectrum: the parameter set parm_list(:, band, type) */
+    const double *condensed_mix_ratio;/* (nd_profile, id_ct:nd_layer, nd_cloud_component), in-cloud */
+    const double *condensed_dim_char; /* same layout [m] */
+    int n_cloud_type;
+    const double *w_cloud;            /* (nd_profile, id_ct:nd_layer) cloud fraction */
+    const double *frac_cloud;         /* (nd_profile, id_ct:nd_layer, nd_cloud_type), normalised */
+    /* McICA */
+    int n_subcol_gen, n_subcol_req;
+    const double *c_sub;              /* (nd_profile, id_ct:nd_layer, nd_subcol_gen) scaling of cloud water per subcolumn */
+    const double *frac_cloudy;        /* (nd_profile) */
+    const int *n_subcol_cld;          /* (nd_profile) or NULL.  NULL: c_sub is the filled array that
+                                         set_cld_mcica leaves (socrates_set_cld_mcica.F90:206-220).
+                                         Non-NULL: c_sub is cloud_gen's compacted output and
+                                         subcolumns n_subcol_cld+1..min(n_subcol_req, n_subcol_gen)
+                                         read cloudy subcolumn ((j-1) mod n_subcol_cld)+1, which is
+                                         what the fill step copies there. */
+    const int *subcol_k;              /* (nd_band, nd_k_term) of the spectrum */
+    const int *first_subcol_k;        /* (nd_band, nd_k_term+1) of the spectrum */
+    const int *subcol_reorder;        /* (nd_subcol_req) */
+} socgpu_cld;
+
+/* ---- StrOut subset (src/radiance_core/def_out.F90), one channel ------ */
+typedef struct socgpu_radout {
+    double *flux_up;        /* (nd_profile, 0:nd_layer) */
+    double *flux_down;      /* (nd_profile, 0:nd_layer), total (direct+diffuse) in the SW */
+    double *flux_direct;    /* (nd_profile, 0:nd_layer) SW only, else may be NULL */
+    double *flux_div;       /* (nd_profile, nd_layer) when control.l_flux_div, else NULL */
+    double *heating_rate;   /* (nd_profile, nd_layer) [K/day] or NULL (extension) */
+    double *flux_up_band;   /* (nd_profile, 0:nd_layer, nd_band) or NULL */
+    double *flux_down_band; /* (nd_profile, 0:nd_layer, nd_band) or NULL */
+} socgpu_radout;
+
+/* ---- entry points ------------------------------------------------------ */
+
+/* ABI version of the loaded library (compare with SOCGPU_ABI_VERSION). */
+SOCGPU_API int socgpu_abi_version(void);
+
+/* Register a spectral file under a name and keep its tables resident on the
+ * device.  Replaces socrates_set_spectrum's cache by name
+ * (src/interface_core/socrates_set_spectrum.F90:20-23,90-121): registering
+ * a name that already exists returns the existing handle. */
+SOCGPU_API int socgpu_spectrum_register(const char *name, const socgpu_spectrum_desc *desc,
+                             socgpu_spectrum_handle *handle, char *msg, size_t msg_len);
+/* Look a registered spectrum up by name; SOCGPU_I_ERR_EXIST if absent. */
+SOCGPU_API int socgpu_spectrum_lookup(const char *name, socgpu_spectrum_handle *handle);
+/* Number of g-points (k-term products over the bands) of a spectrum. */
+SOCGPU_API int socgpu_spectrum_n_gpoint(socgpu_spectrum_handle handle);
+/* Release a spectrum and its device tables. */
+SOCGPU_API int socgpu_spectrum_release(socgpu_spectrum_handle handle);
+
+/* Replaces radiance_calc (src/radiance_core/radiance_calc.F90:16) for the
+ * two-stream clear-sky and McICA paths.  All pointers are host memory; the
+ * call copies inputs to the device, runs the fused kernels and copies the
+ * outputs back before it returns.  Re-entrant: each host thread has its own
+ * stream and device workspace. */
+SOCGPU_API int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dimen,
+                         socgpu_spectrum_handle spectrum, const socgpu_atm *atm,
+                         const socgpu_cld *cld, const socgpu_aer *aer,
+                         const socgpu_bound *bound, socgpu_radout *radout,
+                         char *msg, size_t msg_len);
+
+/* Same computation with every array pointer in device memory (Fortran
+ * layout, the given nd_* extents).  Enqueued on `stream` (a cudaStream_t,
+ * NULL for the legacy default stream); returns once the work is enqueued. */
+SOCGPU_API int socgpu_radiance_calc_device(const socgpu_control *control, const socgpu_dimen *dimen,
+                                socgpu_spectrum_handle spectrum, const socgpu_atm *atm,
+                                const socgpu_cld *cld, const socgpu_aer *aer,
+                                const socgpu_bound *bound, socgpu_radout *radout,
+                                void *stream, char *msg, size_t msg_len);
+
+/* Replaces cloud_gen (src/interface_core/socrates_cloud_gen.F90:8-470):
+ * stochastic McICA subcolumns.  Arguments keep the reference's meaning;
+ * il1..il2 are 1-based columns, cloud arrays span cloud_top..nd_layer.
+ * rng selects the reference LCG or the counter-based Philox stream.
+ * Host pointers; synchronous. */
+SOCGPU_API int socgpu_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile,
+                     int il1, int il2, int n_subcol, int n1, int n2,
+                     int ipph, int ioverlap, const int *rand_seed,
+                     const double *rlc_cf, const double *rlc_cw,
+                     const double *sigma_qcw, const double *avg_cf,
+                     const double *c_cloud, const double *c_ratio,
+                     const double *zf, const double *xcw,
+                     int *n_subcol_cld, double *c_sub, int rng,
+                     char *msg, size_t msg_len);
+
+/* Device-pointer variant of socgpu_cloud_gen, enqueued on `stream`. */
+SOCGPU_API int socgpu_cloud_gen_device(int nd_layer, int cloud_top, int n_layer, int nd_profile,
+                            int il1, int il2, int n_subcol, int n1, int n2,
+                            int ipph, int ioverlap, const int *rand_seed,
+                            const double *rlc_cf, const double *rlc_cw,
+                            const double *sigma_qcw, const double *avg_cf,
+                            const double *c_cloud, const double *c_ratio,
+                            const double *zf, const double *xcw,
+                            int *n_subcol_cld, double *c_sub, int rng,
+                            void *stream, char *msg, size_t msg_len);
+
+/* Kernel launches made by this thread since the library loaded (profiling
+ * aid, extension). */
+SOCGPU_API long long socgpu_kernel_launch_count(void);
+
+/* Select the CUDA device for this host thread (extension). */
+SOCGPU_API int socgpu_set_device(int device);
+
+/* Fix the tile shape of one kernel family (extension, used by the tuner):
+ * precision SOCGPU_PRECISION_*, mode 0 = infra-red without scattering,
+ * 1 = full scattering, 2 = McICA; lanes_per_solve in {8 (mixed only), 16,
+ * 32} lanes sharing one (column, g-point) solve; warps_per_cta in 1..8.
+ * Zeros restore the built-in choice. */
+SOCGPU_API int socgpu_set_tile_config(int precision, int mode, int lanes_per_solve, int warps_per_cta);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SOCGPU_H */

@@ -1,0 +1,1236 @@
+/*
+ * socrates_oracle.c -- FP64 CPU restatement of the SOCRATES two-stream flux
+ * path (clear sky and McICA).  TEST INFRASTRUCTURE ONLY: the checker for the
+ * CUDA path and the CPU baseline of the benchmark.  Nothing in the product
+ * library links it.
+ *
+ * Each function restates one reference routine and cites it; paths are
+ * relative to the SOCRATES source tree.  Loop order follows the reference
+ * (band -> k-term -> [subcolumn] -> layer -> profile, profile innermost) so
+ * that FP64 results agree to rounding.  Build with -ffp-contract=off: the
+ * reference is compiled without fused multiply-add contraction on x86.
+ *
+ * Parity is unpinned against reference-produced numbers (no Fortran
+ * compiler here; the reference's own fixtures need lookup-table scaling,
+ * continua and k_eqv_scl overlap).  See socrates_oracle.h.
+ */
+#include "socrates_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define EPS_R  DBL_EPSILON   /* EPSILON(1.0_RealK) */
+#define TINY_R DBL_MIN       /* TINY(1.0_RealK) */
+
+/* rad_ccf.F90:44,50,56 */
+static const double seconds_per_day = 8.64e4;
+static const double cp_air_dry = 1.005e3;
+/* diffusivity_factor.F90:16 */
+static const double elsasser_factor = 1.66;
+/* two_coeff_basic.F90:87 */
+static const double root_3 = 1.7320508075688772;
+
+/* Fortran-layout index helpers (1-based in the reference, 0-based here). */
+#define IX2(a, l, i, nd1) ((a)[(size_t)(l) + (size_t)(nd1) * (size_t)(i)])
+#define IX3(a, l, i, j, nd1, nd2) \
+    ((a)[(size_t)(l) + (size_t)(nd1) * ((size_t)(i) + (size_t)(nd2) * (size_t)(j))])
+
+static void set_msg(char *msg, size_t len, const char *text)
+{
+    if (msg && len > 0) {
+        strncpy(msg, text, len - 1);
+        msg[len - 1] = '\0';
+    }
+}
+
+/* --------------------------------------------------------------------- */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the
+ * 4x32 bijection with the published multipliers and Weyl key steps.      */
+void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* --------------------------------------------------------------------- */
+/* Spectral accessors on the flat Fortran arrays of socgpu_spectrum_desc. */
+static int sp_index_absorb(const socgpu_spectrum_desc *d, int j, int b)
+{   /* index_absorb(nd_species, nd_band): 1-based species -> 0-based */
+    return IX2(d->index_absorb, j, b, d->nd_species) - 1;
+}
+static int sp_bg(const int *a, const socgpu_spectrum_desc *d, int b, int g) { return IX2(a, b, g, d->nd_band); }
+static double sp_kw(const double *a, const socgpu_spectrum_desc *d, int k, int b, int g)
+{ return IX3(a, k, b, g, d->nd_k_term, d->nd_band); }
+static const double *sp_scale(const socgpu_spectrum_desc *d, int k, int b, int g)
+{
+    return d->scale + (size_t)d->nd_scale_variable *
+        ((size_t)k + (size_t)d->nd_k_term * ((size_t)b + (size_t)d->nd_band * (size_t)g));
+}
+
+/* --------------------------------------------------------------------- */
+/* scale_absorb (scale_absorb.F90:110-224): pressure/temperature scaling
+ * factor of one absorber for all cells of the segment.                  */
+static int scale_absorb(int n_profile, int n_layer, int ndp_in, int ndp_w,
+                        const double *p, const double *t, double *gfr,
+                        int i_fnc, double p_reference, double t_reference,
+                        const double *sp, int l_doppler, double doppler_correction)
+{
+    double pressure_offset = l_doppler ? doppler_correction : 0.0;
+    if (i_fnc == SOCGPU_IP_SCALE_POWER_LAW) {
+        /* scale_absorb.F90:122-137: ((p+off)/(pref+off))**sp1 * (t/tref)**sp2 */
+        double t_inv = 1.0 / t_reference;
+        double p_ref_off_inv = 1.0 / (p_reference + pressure_offset);
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                double pwk_in = (IX2(p, l, i, ndp_in) + pressure_offset) * p_ref_off_inv;
+                double twk_in = IX2(t, l, i, ndp_in) * t_inv;
+                IX2(gfr, l, i, ndp_w) = pow(pwk_in, sp[0]) * pow(twk_in, sp[1]);
+            }
+    } else if (i_fnc == SOCGPU_IP_SCALE_FNC_NULL) {
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) IX2(gfr, l, i, ndp_w) = 1.0;
+    } else if (i_fnc == SOCGPU_IP_SCALE_POWER_QUAD) {
+        /* scale_absorb.F90:170-186 */
+        double p_ref_off_inv = 1.0 / (p_reference + pressure_offset);
+        double t_inv = 1.0 / t_reference;
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                double pwk = pow((IX2(p, l, i, ndp_in) + pressure_offset) * p_ref_off_inv, sp[0]);
+                double tmp = IX2(t, l, i, ndp_in) * t_inv - 1.0;
+                IX2(gfr, l, i, ndp_w) = pwk * (1.0 + tmp * sp[1] + sp[2] * tmp * tmp);
+            }
+    } else if (i_fnc == SOCGPU_IP_SCALE_DOPPLER_QUAD) {
+        /* scale_absorb.F90:208-224 */
+        double t_inv = 1.0 / t_reference;
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                double pwk = pow((IX2(p, l, i, ndp_in) + sp[1]) / (p_reference + sp[1]), sp[0]);
+                double tmp = IX2(t, l, i, ndp_in) * t_inv - 1.0;
+                IX2(gfr, l, i, ndp_w) = pwk * (1.0 + tmp * sp[2] + sp[3] * tmp * tmp);
+            }
+    } else {
+        return SOCGPU_I_ERR_FATAL;
+    }
+    return SOCGPU_I_NORMAL;
+}
+
+/* planck_flux_band (planck_flux_band_mod.F90:33-48), polynomial branch. */
+static double planck_flux_band(const socgpu_spectrum_desc *d, int b, double temperature)
+{
+    double t_ratio = temperature / d->t_ref_planck;
+    const double *c = d->thermal_coeff + (size_t)d->nd_thermal_coeff * (size_t)b;
+    double f = c[d->n_deg_fit];
+    for (int j = d->n_deg_fit - 1; j >= 0; --j) f = f * t_ratio + c[j];
+    return f;
+}
+
+/* --------------------------------------------------------------------- */
+/* Two-stream coefficients of one cell.                                   */
+
+/* two_coeff_basic (two_coeff_basic.F90:99-160). */
+static int two_coeff_basic(int i_2stream, double omega, double asym, double *sum, double *diff)
+{
+    switch (i_2stream) {
+    case SOCGPU_IP_EDDINGTON:
+        *sum = 1.5 * (1.0 - omega * asym); *diff = 2.0 * (1.0 - omega); break;
+    case SOCGPU_IP_ELSASSER:
+        *sum = elsasser_factor - 1.5 * omega * asym; *diff = elsasser_factor * (1.0 - omega); break;
+    case SOCGPU_IP_DISCRETE_ORD:
+        *sum = root_3 * (1.0 - omega * asym); *diff = root_3 * (1.0 - omega); break;
+    case SOCGPU_IP_PIFM85:
+        *sum = 2.0 - 1.5 * omega * asym; *diff = 2.0 * (1.0 - omega); break;
+    case SOCGPU_IP_2S_TEST:
+        *sum = 1.5 - 1.5 * omega * asym; *diff = 1.5 * (1.0 - omega); break;
+    case SOCGPU_IP_HEMI_MEAN:
+        *sum = 2.0 * (1.0 - omega * asym); *diff = 2.0 * (1.0 - omega); break;
+    case SOCGPU_IP_PIFM80:
+        *sum = 2.0 - 1.5 * omega * asym - 0.5 * omega; *diff = 2.0 * (1.0 - omega); break;
+    default:
+        return SOCGPU_I_ERR_FATAL;
+    }
+    return SOCGPU_I_NORMAL;
+}
+
+typedef struct { double trans, reflect, trans_0, trans_0_dir, sc1, sc2; } coeffs;
+
+/* two_coeff (two_coeff.F90:148-188) -> solar_coefficient_basic
+ * (solar_coefficient_basic.F90:124-219) -> trans_source_coeff
+ * (trans_source_coeff.F90:144-263).  sc1/sc2 are the solar (up, down) or
+ * IR (1d, 2d) source coefficients. */
+static void two_coeff_cell(int isolir, int i_2stream, int i_direct_tau, int l_ir_source_quad,
+                           double asym, double omega, double tau_dir, double tau, double sec_0,
+                           coeffs *o)
+{
+    double sum = 0.0, diff = 0.0;
+    two_coeff_basic(i_2stream, omega, asym, &sum, &diff);
+    double lambda = sqrt(sum * diff);
+    double gamma_up = 0.0, gamma_down = 0.0;
+    if (isolir == SOCGPU_IP_SOLAR) {
+        double tol_perturb = 3.2e1 * EPS_R;
+        if (fabs(lambda - sec_0) < tol_perturb) {
+            sum = (1.0 + tol_perturb) * sum;
+            diff = (1.0 + tol_perturb) * diff;
+            lambda = (1.0 + tol_perturb) * lambda;
+        }
+        double ksi_0 = (i_2stream == SOCGPU_IP_DISCRETE_ORD) ? root_3 * asym / sec_0
+                                                            : 1.5 * asym / sec_0;
+        double factor = 0.5 * omega * sec_0 / ((lambda - sec_0) * (lambda + sec_0));
+        gamma_up = factor * (sum - sec_0 - ksi_0 * (diff - sec_0));
+        gamma_down = factor * (sum + sec_0 + ksi_0 * (diff + sec_0));
+    }
+    double sq_eps_r = sqrt(EPS_R), tol = sqrt(sq_eps_r);
+    double exponential = exp(-lambda * tau);
+    double exponential2 = exponential * exponential;
+    double gamma = (sum - lambda) / (sum + lambda);
+    double gamma2 = gamma * gamma;
+    double tmp_inv = 1.0 / (1.0 - exponential2 * gamma2);
+    o->trans = exponential * (1.0 - gamma2) * tmp_inv;
+    o->reflect = gamma * (1.0 - exponential2) * tmp_inv;
+    o->trans_0 = 0.0; o->trans_0_dir = 0.0; o->sc2 = 0.0;
+    if (isolir == SOCGPU_IP_SOLAR) {
+        o->trans_0 = exp(-tau * sec_0);
+        if (i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING || i_direct_tau == SOCGPU_IP_DIRECT_CSR_SCALING)
+            o->trans_0_dir = exp(-tau_dir * sec_0);
+        o->sc1 = (gamma_up - o->reflect * (1.0 + gamma_down)) - gamma_up * o->trans * o->trans_0;
+        o->sc2 = o->trans_0 * (1.0 + gamma_down - gamma_up * o->reflect) - (1.0 + gamma_down) * o->trans;
+    } else {
+        o->sc1 = (1.0 - o->trans + o->reflect + sq_eps_r) / (sq_eps_r + tau * sum);
+        if (l_ir_source_quad) {
+            double s2;
+            if (tau > tol) s2 = -2.0 * (1.0 - o->trans - o->reflect + sq_eps_r) / (diff * tau + sq_eps_r);
+            else s2 = -2.0 + diff * tau;
+            o->sc2 = -(1.0 + o->reflect + o->trans + s2) / (sum * tau + sq_eps_r);
+        }
+    }
+}
+
+/* two_coeff_fast_lw (two_coeff_fast_lw.F90:112-154). */
+static void two_coeff_fast_lw_cell(int l_ir_source_quad, double tau, coeffs *o)
+{
+    double sq_eps_r = sqrt(EPS_R), tol = sqrt(sq_eps_r);
+    o->trans = exp(-1.66 * tau);
+    o->reflect = 0.0; o->trans_0 = 0.0; o->trans_0_dir = 0.0; o->sc2 = 0.0;
+    o->sc1 = (1.0 - o->trans + sq_eps_r) / (1.66 * tau + sq_eps_r);
+    if (l_ir_source_quad) {
+        if (tau > tol) o->sc2 = -(1.0 + o->trans - 2.0 * o->sc1) / (1.66 * tau + sq_eps_r);
+        else o->sc2 = -(1.0 + o->trans - 2.0 + 1.66 * tau) / (1.66 * tau + sq_eps_r);
+    }
+}
+
+/* single_scattering (single_scattering.F90:119-164), the direct-beam depth
+ * (monochromatic_radiance.F90:459-475) and rescale_tau_omega
+ * (rescale_tau_omega.F90:73-80) for one cell. */
+static void single_scatter_cell(const socgpu_control *c, double k_grey_tot, double k_ext_scat,
+                                double k_gas_abs, double d_mass, double fwd,
+                                double *tau, double *tau_dir, double *omega)
+{
+    int m = c->i_scatter_method;
+    if (m == SOCGPU_IP_SCATTER_FULL) {
+        double k_total = k_grey_tot + k_gas_abs;
+        *tau = k_total * d_mass;
+        *omega = k_ext_scat / (k_total + TINY_R);
+        double cap = 1.0 - 3.2e1 * EPS_R;
+        if (*omega > cap) *omega = cap;
+    } else if (m == SOCGPU_IP_NO_SCATTER_ABS) {
+        *tau = (k_grey_tot + k_gas_abs - k_ext_scat) * d_mass;
+        *omega = 0.0;
+    } else {
+        *tau = (k_grey_tot + k_gas_abs) * d_mass;
+        *omega = 0.0;
+    }
+    *tau_dir = *tau;
+    if (c->l_rescale) {
+        *tau = *tau * (1.0 - *omega * fwd);
+        *omega = *omega * (1.0 - fwd) / (1.0 - *omega * fwd);
+    }
+}
+
+/* --------------------------------------------------------------------- */
+/* Workspace of one column segment.  Work arrays use the segment's own
+ * leading dimension `wp`; caller arrays keep dimen->nd_profile.          */
+typedef struct {
+    int wp, ndl, n_profile, n_layer;
+    double *k_grey_tot, *k_ext_scat, *phase_fnc, *forward_scatter;
+    double *phase_fnc_nc, *forward_scatter_nc;
+    double *k_ext_tot_cc, *k_ext_scat_cc, *phf_cc, *fwd_cc;   /* per cloud component */
+    double *gfr;                                              /* per absorber of the band */
+    double *k_gas_abs;
+    double *planck_flux, *planck_diff, *planck_diff_2, *flux_ground;
+    double *flux_inc_down, *flux_inc_direct, *d_planck_flux_surface;
+    double *sec_0, *alb_diff, *alb_dir;
+    double *tau, *tau_dir, *omega;
+    double *trans, *reflect, *trans_0, *trans_0_dir, *sc1, *sc2;
+    double *trans_clr, *reflect_clr, *trans_0_clr, *trans_0_dir_clr, *sc1_clr, *sc2_clr;
+    double *s_up, *s_down, *source_ground;
+    double *flux_direct, *flux_direct_dir, *flux_total;
+    double *flux_direct_acc, *flux_total_acc, *flux_direct_clear, *flux_total_clear;
+    double *alpha, *s_up_prime, *beta, *gam, *h;
+    double *ty_tau[3], *ty_tau_dir[3], *ty_omega[3], *ty_asym[3];      /* cloud types 1..2 */
+    double *ty_valid[3];
+    int *slot;
+} work;
+
+static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
+
+#define WORK_FIELDS(X) \
+    X(k_grey_tot, pl) X(k_ext_scat, pl) X(phase_fnc, pl) X(forward_scatter, pl) \
+    X(phase_fnc_nc, pl) X(forward_scatter_nc, pl) \
+    X(k_ext_tot_cc, pl * nc) X(k_ext_scat_cc, pl * nc) X(phf_cc, pl * nc) X(fwd_cc, pl * nc) \
+    X(gfr, pl * na) X(k_gas_abs, pl) \
+    X(planck_flux, pl1) X(planck_diff, pl) X(planck_diff_2, pl) X(flux_ground, wp) \
+    X(flux_inc_down, wp) X(flux_inc_direct, wp) X(d_planck_flux_surface, wp) \
+    X(sec_0, wp) X(alb_diff, wp) X(alb_dir, wp) \
+    X(tau, pl) X(tau_dir, pl) X(omega, pl) \
+    X(trans, pl) X(reflect, pl) X(trans_0, pl) X(trans_0_dir, pl) X(sc1, pl) X(sc2, pl) \
+    X(trans_clr, pl) X(reflect_clr, pl) X(trans_0_clr, pl) X(trans_0_dir_clr, pl) X(sc1_clr, pl) X(sc2_clr, pl) \
+    X(s_up, pl) X(s_down, pl) X(source_ground, wp) \
+    X(flux_direct, pl1) X(flux_direct_dir, pl1) X(flux_total, pl2) \
+    X(flux_direct_acc, pl1) X(flux_total_acc, pl2) X(flux_direct_clear, pl1) X(flux_total_clear, pl2) \
+    X(alpha, wp) X(s_up_prime, wp) X(beta, pl) X(gam, pl) X(h, pl)
+
+static void work_init(work *w, int wp, int ndl, int n_profile, int n_layer, int nc, int na)
+{
+    size_t pl = (size_t)wp * ndl, pl1 = (size_t)wp * (ndl + 1), pl2 = (size_t)wp * (2 * ndl + 2);
+    memset(w, 0, sizeof(*w));
+    w->wp = wp; w->ndl = ndl; w->n_profile = n_profile; w->n_layer = n_layer;
+    if (nc < 1) nc = 1;
+    if (na < 1) na = 1;
+#define ALLOC_F(name, n) w->name = zalloc(n);
+    WORK_FIELDS(ALLOC_F)
+#undef ALLOC_F
+    for (int t = 0; t < 3; ++t) {
+        w->ty_tau[t] = zalloc(pl); w->ty_tau_dir[t] = zalloc(pl);
+        w->ty_omega[t] = zalloc(pl); w->ty_asym[t] = zalloc(pl); w->ty_valid[t] = zalloc(pl);
+    }
+    w->slot = (int *)calloc((size_t)wp, sizeof(int));
+}
+
+static void work_free(work *w)
+{
+#define FREE_F(name, n) free(w->name); w->name = NULL;
+    WORK_FIELDS(FREE_F)
+#undef FREE_F
+    for (int t = 0; t < 3; ++t) {
+        free(w->ty_tau[t]); free(w->ty_tau_dir[t]); free(w->ty_omega[t]);
+        free(w->ty_asym[t]); free(w->ty_valid[t]);
+    }
+    free(w->slot);
+}
+
+/* --------------------------------------------------------------------- */
+/* Column solve of one monochromatic problem for all profiles of the
+ * segment: ir_source (ir_source.F90:93-119), solar_source
+ * (solar_source.F90:105-176), column_solver (column_solver.F90:160-243),
+ * solver_homogen_direct (solver_homogen_direct.F90:94-131) and
+ * solver_no_scat (solver_no_scat.F90:75-94).
+ * flux_total(l, m) of the reference is IX2(flux_total, l, m-1, wp). */
+static void column_solve(work *w, const socgpu_control *c, int no_scat)
+{
+    int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp;
+    double *fd = w->flux_direct, *ft = w->flux_total;
+    if (c->isolir == SOCGPU_IP_INFRA_RED) {
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                if (c->l_ir_source_quad) {
+                    IX2(w->s_up, l, i, wp) = IX2(w->sc1, l, i, wp) * IX2(w->planck_diff, l, i, wp)
+                        + IX2(w->sc2, l, i, wp) * IX2(w->planck_diff_2, l, i, wp);
+                    IX2(w->s_down, l, i, wp) = -IX2(w->sc1, l, i, wp) * IX2(w->planck_diff, l, i, wp)
+                        + IX2(w->sc2, l, i, wp) * IX2(w->planck_diff_2, l, i, wp);
+                } else {
+                    IX2(w->s_up, l, i, wp) = IX2(w->sc1, l, i, wp) * IX2(w->planck_diff, l, i, wp);
+                    IX2(w->s_down, l, i, wp) = -IX2(w->s_up, l, i, wp);
+                }
+            }
+        for (int l = 0; l < n_profile; ++l)
+            w->source_ground[l] = (1.0 - w->alb_diff[l]) * w->d_planck_flux_surface[l];
+        for (int i = 0; i <= n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) IX2(fd, l, i, wp) = 0.0;
+    } else {
+        int l_dir = (c->i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING ||
+                     c->i_direct_tau == SOCGPU_IP_DIRECT_CSR_SCALING);
+        for (int l = 0; l < n_profile; ++l) {
+            IX2(fd, l, 0, wp) = w->flux_inc_direct[l];
+            if (l_dir) IX2(w->flux_direct_dir, l, 0, wp) = w->flux_inc_direct[l];
+        }
+        for (int i = 1; i <= n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                IX2(fd, l, i, wp) = IX2(fd, l, i - 1, wp) * IX2(w->trans_0, l, i - 1, wp);
+                IX2(w->s_up, l, i - 1, wp) = IX2(w->sc1, l, i - 1, wp) * IX2(fd, l, i - 1, wp);
+                IX2(w->s_down, l, i - 1, wp) = IX2(w->sc2, l, i - 1, wp) * IX2(fd, l, i - 1, wp);
+            }
+        if (l_dir) {
+            for (int i = 1; i <= n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l)
+                    IX2(w->flux_direct_dir, l, i, wp) =
+                        IX2(w->flux_direct_dir, l, i - 1, wp) * IX2(w->trans_0_dir, l, i - 1, wp);
+            for (int i = 0; i <= n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l)
+                    IX2(fd, l, i, wp) = IX2(w->flux_direct_dir, l, i, wp);
+        }
+        for (int l = 0; l < n_profile; ++l)
+            w->source_ground[l] = (w->alb_dir[l] - w->alb_diff[l]) * IX2(fd, l, n_layer, wp);
+    }
+
+    if (no_scat) {
+        for (int l = 0; l < n_profile; ++l) IX2(ft, l, 1, wp) = w->flux_inc_down[l];
+        for (int i = 1; i <= n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l)
+                IX2(ft, l, 2 * i + 1, wp) = IX2(w->s_down, l, i - 1, wp)
+                    + IX2(w->trans, l, i - 1, wp) * IX2(ft, l, 2 * i - 1, wp);
+        for (int l = 0; l < n_profile; ++l)
+            IX2(ft, l, 2 * n_layer, wp) = (1.0 - w->alb_diff[l]) * w->d_planck_flux_surface[l]
+                + w->alb_diff[l] * IX2(ft, l, 2 * n_layer + 1, wp);
+        for (int i = n_layer; i >= 1; --i)
+            for (int l = 0; l < n_profile; ++l)
+                IX2(ft, l, 2 * i - 2, wp) = IX2(w->s_up, l, i - 1, wp)
+                    + IX2(w->trans, l, i - 1, wp) * IX2(ft, l, 2 * i, wp);
+    } else {
+        for (int l = 0; l < n_profile; ++l) {
+            w->alpha[l] = w->alb_diff[l];
+            w->s_up_prime[l] = w->source_ground[l];
+        }
+        for (int ii = n_layer - 1; ii >= 0; --ii)
+            for (int l = 0; l < n_profile; ++l) {
+                double r = IX2(w->reflect, l, ii, wp), t = IX2(w->trans, l, ii, wp);
+                double beta = 1.0 / (1.0 - w->alpha[l] * r);
+                double gam = w->alpha[l] * t;
+                double h = w->s_up_prime[l] + w->alpha[l] * IX2(w->s_down, l, ii, wp);
+                IX2(w->beta, l, ii, wp) = beta; IX2(w->gam, l, ii, wp) = gam; IX2(w->h, l, ii, wp) = h;
+                w->alpha[l] = r + beta * gam * t;
+                w->s_up_prime[l] = IX2(w->s_up, l, ii, wp) + beta * t * h;
+            }
+        for (int l = 0; l < n_profile; ++l) {
+            IX2(ft, l, 1, wp) = w->flux_inc_down[l];
+            IX2(ft, l, 0, wp) = w->alpha[l] * IX2(ft, l, 1, wp) + w->s_up_prime[l];
+        }
+        for (int i = 1; i <= n_layer; ++i) {
+            int ii = i - 1;
+            for (int l = 0; l < n_profile; ++l) {
+                IX2(ft, l, 2 * i, wp) = IX2(w->beta, l, ii, wp)
+                    * (IX2(w->h, l, ii, wp) + IX2(w->gam, l, ii, wp) * IX2(ft, l, 2 * i - 1, wp));
+                IX2(ft, l, 2 * i + 1, wp) = IX2(w->s_down, l, ii, wp)
+                    + IX2(w->trans, l, ii, wp) * IX2(ft, l, 2 * i - 1, wp)
+                    + IX2(w->reflect, l, ii, wp) * IX2(ft, l, 2 * i, wp);
+            }
+        }
+    }
+}
+
+/* Clear (type 0) optical properties and two-stream coefficients of one
+ * k-term (monochromatic_radiance.F90:429-528, two_stream.F90:166-206 for the
+ * coefficient part). */
+static void clear_coefficients(work *w, const socgpu_control *c, const double *mass, int ndp_in)
+{
+    int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp;
+    int no_scat = (c->i_scatter_method != SOCGPU_IP_SCATTER_FULL);
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < n_profile; ++l) {
+            double tau, tau_dir, om;
+            single_scatter_cell(c, IX2(w->k_grey_tot, l, i, wp), IX2(w->k_ext_scat, l, i, wp),
+                                IX2(w->k_gas_abs, l, i, wp), IX2(mass, l, i, ndp_in),
+                                IX2(w->forward_scatter, l, i, wp), &tau, &tau_dir, &om);
+            IX2(w->tau, l, i, wp) = tau; IX2(w->tau_dir, l, i, wp) = tau_dir; IX2(w->omega, l, i, wp) = om;
+        }
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < n_profile; ++l) {
+            coeffs o;
+            if (no_scat)
+                two_coeff_fast_lw_cell(c->l_ir_source_quad, IX2(w->tau, l, i, wp), &o);
+            else
+                two_coeff_cell(c->isolir, c->i_2stream, c->i_direct_tau, c->l_ir_source_quad,
+                               IX2(w->phase_fnc, l, i, wp), IX2(w->omega, l, i, wp),
+                               IX2(w->tau_dir, l, i, wp), IX2(w->tau, l, i, wp), w->sec_0[l], &o);
+            IX2(w->trans, l, i, wp) = o.trans; IX2(w->reflect, l, i, wp) = o.reflect;
+            IX2(w->trans_0, l, i, wp) = o.trans_0; IX2(w->trans_0_dir, l, i, wp) = o.trans_0_dir;
+            IX2(w->sc1, l, i, wp) = o.sc1; IX2(w->sc2, l, i, wp) = o.sc2;
+        }
+}
+
+/* --------------------------------------------------------------------- */
+/* Grey optical properties of one band (grey_opt_prop.F90:470-920,
+ * 1010-1030, 1390-1450; opt_prop_ukca_aerosol.F90:128-208;
+ * rescale_phase_fnc.F90:120-128 as called at radiance_calc.F90:996-1017).
+ * Cloud-component optics through opt_prop_pade_2
+ * (opt_prop_pade_2_mod.F90:99-140, the rescaled n_order_forward=2 path of
+ * opt_prop_water_cloud.F90:212-219 and opt_prop_ice_cloud.F90:228-236). */
+static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *dm,
+                         const socgpu_spectrum_desc *d, const socgpu_aer *aer,
+                         const socgpu_cld *cld, int b, int l_cloud)
+{
+    int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp, ndl = w->ndl;
+    int ndp = dm->nd_profile;
+    size_t pl = (size_t)wp * ndl;
+    for (size_t q = 0; q < pl; ++q) {
+        w->k_grey_tot[q] = 0.0; w->k_ext_scat[q] = 0.0;
+        w->phase_fnc[q] = 0.0; w->forward_scatter[q] = 0.0;
+    }
+    if (c->l_rayleigh) {
+        if (d->i_rayleigh_scheme != SOCGPU_IP_RAYLEIGH_TOTAL || !d->rayleigh_coeff) return SOCGPU_I_ERR_FATAL;
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) IX2(w->k_ext_scat, l, i, wp) = d->rayleigh_coeff[b];
+    }
+    if (c->l_aerosol_mode && aer && aer->n_mode > 0) {
+        int ndm = dm->nd_aerosol_mode;
+        for (int j = 0; j < aer->n_mode; ++j)
+            for (int i = 0; i < n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l) {
+                    double mmr = IX3(aer->mode_mix_ratio, l, i, j, ndp, ndl);
+                    size_t q4 = (size_t)l + (size_t)ndp * ((size_t)i + (size_t)ndl *
+                                                           ((size_t)j + (size_t)ndm * (size_t)b));
+                    double g = aer->mode_asymmetry[q4];
+                    IX2(w->k_grey_tot, l, i, wp) = IX2(w->k_grey_tot, l, i, wp) + mmr * aer->mode_absorption[q4];
+                    double k_scatter = mmr * aer->mode_scattering[q4];
+                    IX2(w->k_ext_scat, l, i, wp) = IX2(w->k_ext_scat, l, i, wp) + k_scatter;
+                    IX2(w->phase_fnc, l, i, wp) = IX2(w->phase_fnc, l, i, wp) + k_scatter * g;
+                    if (c->l_rescale) {
+                        double ks_phf = k_scatter * g;
+                        if (c->n_order_forward == 1)
+                            IX2(w->forward_scatter, l, i, wp) = IX2(w->forward_scatter, l, i, wp) + ks_phf;
+                        else if (c->n_order_forward == 2)
+                            IX2(w->forward_scatter, l, i, wp) = IX2(w->forward_scatter, l, i, wp) + ks_phf * g;
+                        else
+                            IX2(w->forward_scatter, l, i, wp) = IX2(w->forward_scatter, l, i, wp)
+                                + k_scatter * pow(g, (double)c->n_order_forward);
+                    }
+                }
+    }
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < n_profile; ++l)
+            IX2(w->k_grey_tot, l, i, wp) = IX2(w->k_grey_tot, l, i, wp) + IX2(w->k_ext_scat, l, i, wp);
+
+    if (l_cloud) {
+        memcpy(w->phase_fnc_nc, w->phase_fnc, pl * sizeof(double));
+        memcpy(w->forward_scatter_nc, w->forward_scatter, pl * sizeof(double));
+    }
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < n_profile; ++l) {
+            double ks = IX2(w->k_ext_scat, l, i, wp);
+            if (ks > TINY_R) {
+                if (c->l_rescale) {
+                    double tmp_inv = 1.0 / ks;
+                    IX2(w->forward_scatter, l, i, wp) = IX2(w->forward_scatter, l, i, wp) * tmp_inv;
+                    IX2(w->phase_fnc, l, i, wp) = IX2(w->phase_fnc, l, i, wp) * tmp_inv;
+                } else {
+                    IX2(w->phase_fnc, l, i, wp) = IX2(w->phase_fnc, l, i, wp) / ks;
+                }
+            }
+        }
+    if (c->l_rescale)
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                double f = IX2(w->forward_scatter, l, i, wp);
+                IX2(w->phase_fnc, l, i, wp) = (IX2(w->phase_fnc, l, i, wp) - f) / (1.0 - f);
+            }
+
+    if (l_cloud) {
+        int ict = dm->id_cloud_top - 1, ndc = ndl - ict;
+        for (int k = 0; k < cld->n_condensed; ++k) {
+            const double *cp0;
+            int ity = cld->i_condensed_type[k] - 1;
+            if (cld->type_condensed[k] == SOCGPU_IP_PHASE_WATER) {
+                if (cld->i_condensed_param[k] != SOCGPU_IP_DROP_PADE_2 || !d->drop_parm_list) return SOCGPU_I_ERR_FATAL;
+                cp0 = d->drop_parm_list + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * (size_t)ity);
+            } else {
+                if (cld->i_condensed_param[k] != SOCGPU_IP_ICE_PADE_2_PHF || !d->ice_parm_list) return SOCGPU_I_ERR_FATAL;
+                cp0 = d->ice_parm_list + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * (size_t)ity);
+            }
+            double *kext = w->k_ext_tot_cc + pl * k, *kscat = w->k_ext_scat_cc + pl * k;
+            double *phf = w->phf_cc + pl * k, *fwd = w->fwd_cc + pl * k;
+            for (int i = ict; i < n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l) {
+                    size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
+                    double q = cld->condensed_mix_ratio[qc + (size_t)ndp * ndc * k];
+                    double re = cld->condensed_dim_char[qc + (size_t)ndp * ndc * k];
+                    const double *cp = cp0;
+                    double ke = q * (cp[0] + re * (cp[1] + re * cp[2]))
+                        / (1.0e+00 + re * (cp[3] + re * (cp[4] + re * cp[5])));
+                    double ks = ke * (1.0e+00 - (cp[6] + re * (cp[7] + re * cp[8]))
+                                      / (1.0e+00 + re * (cp[9] + re * cp[10])));
+                    double g = (cp[11] + re * (cp[12] + re * cp[13]))
+                        / (1.0e+00 + re * (cp[14] + re * cp[15]));
+                    IX2(kext, l, i, wp) = ke;
+                    IX2(kscat, l, i, wp) = ks;
+                    IX2(phf, l, i, wp) = ks * g;
+                    IX2(fwd, l, i, wp) = ks * g * g;
+                }
+        }
+    }
+    return SOCGPU_I_NORMAL;
+}
+
+/* --------------------------------------------------------------------- */
+/* McICA: one k-term of one band (mcica_sample.F90:453-925 with
+ * mcica_column.F90:261-602).  Leaves the blended fluxes in flux_direct and
+ * flux_total. */
+static void solve_mcica_term(work *w, const socgpu_control *c, const socgpu_dimen *dm,
+                             const socgpu_spectrum_desc *d, const double *mass,
+                             const socgpu_cld *cld, int b, int iex)
+{
+    int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp, ndl = w->ndl;
+    int ndp = dm->nd_profile;
+    int no_scat = (c->i_scatter_method != SOCGPU_IP_SCATTER_FULL);
+    int ict = dm->id_cloud_top - 1, ndc = ndl - ict;
+    size_t pl = (size_t)wp * ndl, pl1 = (size_t)wp * (ndl + 1), pl2 = (size_t)wp * (2 * ndl + 2);
+    const double eps = EPS_R;   /* mcica_sample.F90:440 */
+    int first = IX2(cld->first_subcol_k, b, iex, d->nd_band);
+    int last = IX2(cld->first_subcol_k, b, iex + 1, d->nd_band) - 1;
+    double subcol_k_inv = 1.0 / (double)IX2(cld->subcol_k, b, iex, d->nd_band);
+
+    /* clear coefficients (type 0): identical for every subcolumn */
+    clear_coefficients(w, c, mass, ndp);
+    memcpy(w->trans_clr, w->trans, pl * sizeof(double));
+    memcpy(w->reflect_clr, w->reflect, pl * sizeof(double));
+    memcpy(w->trans_0_clr, w->trans_0, pl * sizeof(double));
+    memcpy(w->trans_0_dir_clr, w->trans_0_dir, pl * sizeof(double));
+    memcpy(w->sc1_clr, w->sc1, pl * sizeof(double));
+    memcpy(w->sc2_clr, w->sc2, pl * sizeof(double));
+
+    for (int m = first; m <= last; ++m) {
+        int index_subcol = m % cld->n_subcol_req;
+        if (index_subcol == 0) index_subcol = cld->n_subcol_req;
+        index_subcol = cld->subcol_reorder[index_subcol - 1];
+        /* per-profile subcolumn slot, with the fill of set_cld_mcica
+         * (socrates_set_cld_mcica.F90:206-220) applied on the fly when the
+         * compacted cloud_gen output is given */
+        for (int l = 0; l < n_profile; ++l) {
+            int j = index_subcol;
+            if (cld->n_subcol_cld) {
+                int ncld = cld->n_subcol_cld[l];
+                int nfill = cld->n_subcol_req < cld->n_subcol_gen ? cld->n_subcol_req : cld->n_subcol_gen;
+                if (ncld > 0 && j > ncld && j <= nfill) j = (j - 1) % ncld + 1;
+            }
+            w->slot[l] = j - 1;
+        }
+#define CSUB_AT(qc, l) (cld->c_sub[(qc) + (size_t)ndp * ndc * (size_t)w->slot[l]])
+
+        if (m == first) {
+            /* the clear solve (mcica_column.F90:309-327, l_clear) */
+            column_solve(w, c, no_scat);
+            memcpy(w->flux_direct_clear, w->flux_direct, pl1 * sizeof(double));
+            memcpy(w->flux_total_clear, w->flux_total, pl2 * sizeof(double));
+        }
+        /* cloudy-type optics (mcica_sample.F90:472-560) and their optical
+         * depths (single_scattering_all, rescale_tau_omega) */
+        for (int t = 1; t <= 2; ++t)
+            for (size_t q = 0; q < pl; ++q) w->ty_valid[t][q] = 0.0;
+        for (int k = 0; k < cld->n_condensed; ++k) {
+            int t = cld->i_cloud_type[k];
+            const double *kext = w->k_ext_tot_cc + pl * k, *kscat = w->k_ext_scat_cc + pl * k;
+            const double *phf = w->phf_cc + pl * k, *fwdc = w->fwd_cc + pl * k;
+            for (int i = ict; i < n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l) {
+                    size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
+                    if (!(cld->w_cloud[qc] > 0.0)) continue;
+                    double cs = CSUB_AT(qc, l);
+                    double kgt = IX2(w->k_grey_tot, l, i, wp) + IX2(kext, l, i, wp) * cs;
+                    double kes = IX2(w->k_ext_scat, l, i, wp) + IX2(kscat, l, i, wp) * cs;
+                    double fwd, asym;
+                    if (c->l_rescale) {
+                        fwd = IX2(w->forward_scatter_nc, l, i, wp) + IX2(fwdc, l, i, wp) * cs;
+                        double den = kes - fwd;
+                        asym = (IX2(w->phase_fnc_nc, l, i, wp) + IX2(phf, l, i, wp) * cs - fwd)
+                            / (den > eps ? den : eps);
+                        fwd = fwd / (kes > eps ? kes : eps);
+                    } else {
+                        fwd = 0.0;
+                        asym = (IX2(w->phase_fnc_nc, l, i, wp) + IX2(phf, l, i, wp) * cs)
+                            / (kes > eps ? kes : eps);
+                    }
+                    double tau, tau_dir, om;
+                    single_scatter_cell(c, kgt, kes, IX2(w->k_gas_abs, l, i, wp),
+                                        IX2(mass, l, i, ndp), fwd, &tau, &tau_dir, &om);
+                    IX2(w->ty_tau[t], l, i, wp) = tau; IX2(w->ty_tau_dir[t], l, i, wp) = tau_dir;
+                    IX2(w->ty_omega[t], l, i, wp) = om; IX2(w->ty_asym[t], l, i, wp) = asym;
+                    IX2(w->ty_valid[t], l, i, wp) = 1.0;
+                }
+        }
+        /* mcica_column.F90:336-470: clear coefficients, then the cloudy
+         * cells of this subcolumn get the frac_cloud-weighted cloudy ones */
+        memcpy(w->trans, w->trans_clr, pl * sizeof(double));
+        memcpy(w->reflect, w->reflect_clr, pl * sizeof(double));
+        memcpy(w->trans_0, w->trans_0_clr, pl * sizeof(double));
+        memcpy(w->trans_0_dir, w->trans_0_dir_clr, pl * sizeof(double));
+        memcpy(w->sc1, w->sc1_clr, pl * sizeof(double));
+        memcpy(w->sc2, w->sc2_clr, pl * sizeof(double));
+        for (int t = 1; t <= cld->n_cloud_type; ++t)
+            for (int i = ict; i < n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l) {
+                    size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
+                    double fc = cld->frac_cloud[qc + (size_t)ndp * ndc * (size_t)(t - 1)];
+                    if (CSUB_AT(qc, l) * fc > 0.0) {
+                        IX2(w->trans, l, i, wp) = 0.0; IX2(w->reflect, l, i, wp) = 0.0;
+                        IX2(w->sc1, l, i, wp) = 0.0; IX2(w->sc2, l, i, wp) = 0.0;
+                        if (c->isolir == SOCGPU_IP_SOLAR) {
+                            IX2(w->trans_0, l, i, wp) = 0.0; IX2(w->trans_0_dir, l, i, wp) = 0.0;
+                        }
+                    }
+                }
+        for (int t = 1; t <= cld->n_cloud_type; ++t)
+            for (int i = ict; i < n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l) {
+                    size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
+                    double fc = cld->frac_cloud[qc + (size_t)ndp * ndc * (size_t)(t - 1)];
+                    if (!(CSUB_AT(qc, l) * fc > 0.0) || IX2(w->ty_valid[t], l, i, wp) == 0.0) continue;
+                    coeffs o;
+                    if (no_scat)
+                        two_coeff_fast_lw_cell(c->l_ir_source_quad, IX2(w->ty_tau[t], l, i, wp), &o);
+                    else
+                        two_coeff_cell(c->isolir, c->i_2stream, c->i_direct_tau, c->l_ir_source_quad,
+                                       IX2(w->ty_asym[t], l, i, wp), IX2(w->ty_omega[t], l, i, wp),
+                                       IX2(w->ty_tau_dir[t], l, i, wp), IX2(w->ty_tau[t], l, i, wp),
+                                       w->sec_0[l], &o);
+                    IX2(w->trans, l, i, wp) = IX2(w->trans, l, i, wp) + fc * o.trans;
+                    IX2(w->reflect, l, i, wp) = IX2(w->reflect, l, i, wp) + fc * o.reflect;
+                    IX2(w->sc1, l, i, wp) = IX2(w->sc1, l, i, wp) + fc * o.sc1;
+                    if (c->isolir == SOCGPU_IP_SOLAR || c->l_ir_source_quad)
+                        IX2(w->sc2, l, i, wp) = IX2(w->sc2, l, i, wp) + fc * o.sc2;
+                    if (c->isolir == SOCGPU_IP_SOLAR) {
+                        IX2(w->trans_0, l, i, wp) = IX2(w->trans_0, l, i, wp) + fc * o.trans_0;
+                        if (c->i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING ||
+                            c->i_direct_tau == SOCGPU_IP_DIRECT_CSR_SCALING)
+                            IX2(w->trans_0_dir, l, i, wp) = IX2(w->trans_0_dir, l, i, wp) + fc * o.trans_0_dir;
+                    }
+                }
+        column_solve(w, c, no_scat);
+        /* mcica_sample.F90:793-860: accumulate the subcolumn fluxes */
+        if (m == first) {
+            memcpy(w->flux_direct_acc, w->flux_direct, pl1 * sizeof(double));
+            memcpy(w->flux_total_acc, w->flux_total, pl2 * sizeof(double));
+        } else {
+            for (int i = 0; i <= n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l)
+                    IX2(w->flux_direct_acc, l, i, wp) = IX2(w->flux_direct_acc, l, i, wp) + IX2(w->flux_direct, l, i, wp);
+            for (int i = 0; i < 2 * n_layer + 2; ++i)
+                for (int l = 0; l < n_profile; ++l)
+                    IX2(w->flux_total_acc, l, i, wp) = IX2(w->flux_total_acc, l, i, wp) + IX2(w->flux_total, l, i, wp);
+        }
+    }
+#undef CSUB_AT
+    /* mcica_sample.F90:862-925: mean over subcolumns, blend with clear */
+    if (c->isolir == SOCGPU_IP_SOLAR)
+        for (int i = 0; i <= n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                double fc = cld->frac_cloudy[l];
+                double v = IX2(w->flux_direct_acc, l, i, wp) * subcol_k_inv;
+                IX2(w->flux_direct, l, i, wp) = fc * v + ((1.0 - fc) * IX2(w->flux_direct_clear, l, i, wp));
+            }
+    else
+        for (int i = 0; i <= n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) IX2(w->flux_direct, l, i, wp) = 0.0;
+    for (int i = 0; i < 2 * n_layer + 2; ++i)
+        for (int l = 0; l < n_profile; ++l) {
+            double fc = cld->frac_cloudy[l];
+            double v = IX2(w->flux_total_acc, l, i, wp) * subcol_k_inv;
+            IX2(w->flux_total, l, i, wp) = (fc * v) + ((1.0 - fc) * IX2(w->flux_total_clear, l, i, wp));
+        }
+}
+
+/* --------------------------------------------------------------------- */
+static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
+                         const socgpu_atm *atm, const socgpu_dimen *dm, const socgpu_cld *cld,
+                         char *msg, size_t msg_len)
+{
+    if (c->i_angular_integration != SOCGPU_IP_TWO_STREAM) {
+        set_msg(msg, msg_len, "only two-stream angular integration is supported"); return SOCGPU_I_ERR_FATAL; }
+    if (c->isolir != SOCGPU_IP_SOLAR && c->isolir != SOCGPU_IP_INFRA_RED) {
+        set_msg(msg, msg_len, "isolir must be solar or infra-red"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_RANDOM) {
+        set_msg(msg, msg_len, "only random gas overlap is supported"); return SOCGPU_I_ERR_FATAL; }
+    double s, t;
+    if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
+        if (two_coeff_basic(c->i_2stream, 0.5, 0.5, &s, &t) != SOCGPU_I_NORMAL) {
+            set_msg(msg, msg_len, "unrecognised or unimplemented two-stream scheme"); return SOCGPU_I_ERR_FATAL; }
+        if (c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
+            set_msg(msg, msg_len, "scattering requires solver_homogen_direct"); return SOCGPU_I_ERR_FATAL; }
+    } else if (c->i_scatter_method == SOCGPU_IP_NO_SCATTER_ABS || c->i_scatter_method == SOCGPU_IP_NO_SCATTER_EXT) {
+        if (c->i_solver != SOCGPU_IP_SOLVER_NO_SCAT) {
+            set_msg(msg, msg_len, "no-scattering methods require solver_no_scat"); return SOCGPU_I_ERR_FATAL; }
+    } else {
+        set_msg(msg, msg_len, "unsupported scattering method"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA) {
+        set_msg(msg, msg_len, "only clear-sky and McICA cloud schemes are supported"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA && !cld) {
+        set_msg(msg, msg_len, "McICA requires cloud fields"); return SOCGPU_I_ERR_FATAL; }
+    if (c->first_band < 1 || c->last_band > d->n_band || c->first_band > c->last_band) {
+        set_msg(msg, msg_len, "band range outside the spectrum"); return SOCGPU_I_ERR_RANGE; }
+    if (atm->n_profile < 0 || atm->n_profile > dm->nd_profile || atm->n_layer < 1 || atm->n_layer > dm->nd_layer) {
+        set_msg(msg, msg_len, "profile/layer counts exceed their dimensions"); return SOCGPU_I_ERR_RANGE; }
+    if (c->isolir == SOCGPU_IP_INFRA_RED && !d->thermal_coeff) {
+        set_msg(msg, msg_len, "infra-red calculation without Planck data"); return SOCGPU_I_ERR_FATAL; }
+    if (c->isolir == SOCGPU_IP_SOLAR && !d->solar_flux_band) {
+        set_msg(msg, msg_len, "solar calculation without solar spectrum"); return SOCGPU_I_ERR_FATAL; }
+    return SOCGPU_I_NORMAL;
+}
+
+/* radiance_calc (radiance_calc.F90:16-2160) for one column segment.  The
+ * caller's arrays are viewed from profile p0 on; dimen->nd_profile stays
+ * the leading dimension. */
+static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm,
+                                 const socgpu_spectrum_desc *d, const socgpu_atm *atm0,
+                                 const socgpu_cld *cld0, const socgpu_aer *aer0,
+                                 const socgpu_bound *bd, socgpu_radout *out0,
+                                 int p0, int np, char *msg, size_t msg_len)
+{
+    int status = check_options(c, d, atm0, dm, cld0, msg, msg_len);
+    if (status != SOCGPU_I_NORMAL) return status;
+    if (np <= 0) return SOCGPU_I_NORMAL;
+    int ndp = dm->nd_profile, ndl = dm->nd_layer, n_layer = atm0->n_layer;
+    int l_cloud = (c->i_cloud == SOCGPU_IP_CLOUD_MCICA);
+    int ict = dm->id_cloud_top - 1;
+
+    /* views shifted to the first profile of the segment */
+    socgpu_atm atm = *atm0;
+    atm.p += p0; atm.t += p0; atm.t_level += p0; atm.mass += p0; atm.gas_mix_ratio += p0;
+    if (atm.p_level) atm.p_level += p0;
+    socgpu_aer aerv, *aer = NULL;
+    if (aer0) {
+        aerv = *aer0; aer = &aerv;
+        if (aerv.n_mode > 0) {
+            aerv.mode_mix_ratio += p0; aerv.mode_absorption += p0;
+            aerv.mode_scattering += p0; aerv.mode_asymmetry += p0;
+        }
+    }
+    socgpu_cld cldv, *cld = NULL;
+    if (cld0 && l_cloud) {
+        cldv = *cld0; cld = &cldv;
+        cldv.condensed_mix_ratio += p0; cldv.condensed_dim_char += p0;
+        cldv.w_cloud += p0; cldv.frac_cloud += p0; cldv.c_sub += p0; cldv.frac_cloudy += p0;
+        if (cldv.n_subcol_cld) cldv.n_subcol_cld += p0;
+    }
+    socgpu_radout out = *out0;
+    out.flux_up += p0; out.flux_down += p0;
+    if (out.flux_direct) out.flux_direct += p0;
+    if (out.flux_div) out.flux_div += p0;
+    if (out.heating_rate) out.heating_rate += p0;
+    if (out.flux_up_band) out.flux_up_band += p0;
+    if (out.flux_down_band) out.flux_down_band += p0;
+
+    int max_abs = 1;
+    for (int b = c->first_band - 1; b < c->last_band; ++b)
+        if (d->n_band_absorb[b] > max_abs) max_abs = d->n_band_absorb[b];
+    work w;
+    work_init(&w, np, ndl, np, n_layer, cld ? cld->n_condensed : 0, max_abs);
+    int wp = np;
+
+    /* zero the outputs (augment_radiance's l_initial branch is equivalent) */
+    for (int i = 0; i <= n_layer; ++i)
+        for (int l = 0; l < np; ++l) {
+            IX2(out.flux_up, l, i, ndp) = 0.0;
+            IX2(out.flux_down, l, i, ndp) = 0.0;
+            if (out.flux_direct) IX2(out.flux_direct, l, i, ndp) = 0.0;
+        }
+    if (out.flux_div)
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < np; ++l) IX2(out.flux_div, l, i, ndp) = 0.0;
+    for (int b = 0; b < d->n_band; ++b)
+        for (int i = 0; i <= n_layer; ++i)
+            for (int l = 0; l < np; ++l) {
+                if (out.flux_up_band) IX3(out.flux_up_band, l, i, b, ndp, ndl + 1) = 0.0;
+                if (out.flux_down_band) IX3(out.flux_down_band, l, i, b, ndp, ndl + 1) = 0.0;
+            }
+
+    for (int b = c->first_band - 1; b < c->last_band && status == SOCGPU_I_NORMAL; ++b) {
+        double weight_band = c->weight_band ? c->weight_band[b] : 1.0;
+        status = grey_opt_prop(&w, c, dm, d, aer, cld, b, l_cloud);
+        if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "unsupported optical property option"); break; }
+
+        /* gas scaling of each absorber (radiance_calc.F90:1330-1470) */
+        int n_abs = c->l_gas ? d->n_band_absorb[b] : 0;
+        int gas_of[SOCGPU_MAX_SPECIES], nk[SOCGPU_MAX_SPECIES];
+        for (int j = 0; j < n_abs; ++j) {
+            int g = sp_index_absorb(d, j, b);
+            gas_of[j] = g;
+            nk[j] = sp_bg(d->i_band_k, d, b, g);
+            int isk = sp_bg(d->i_scale_k, d, b, g);
+            double *gfr = w.gfr + (size_t)wp * ndl * j;
+            if (isk == SOCGPU_IP_SCALE_BAND) {
+                status = scale_absorb(np, n_layer, ndp, wp, atm.p, atm.t, gfr, sp_bg(d->i_scale_fnc, d, b, g),
+                                      IX2(d->p_ref, g, b, d->nd_species), IX2(d->t_ref, g, b, d->nd_species),
+                                      sp_scale(d, 0, b, g), d->l_doppler ? d->l_doppler[g] : 0,
+                                      d->doppler_cor ? d->doppler_cor[g] : 0.0);
+                for (int i = 0; i < n_layer; ++i)
+                    for (int l = 0; l < np; ++l) {
+                        double v = IX2(gfr, l, i, wp) * IX3(atm.gas_mix_ratio, l, i, g, ndp, ndl);
+                        IX2(gfr, l, i, wp) = v > 0.0 ? v : 0.0;
+                    }
+            } else if (isk == SOCGPU_IP_SCALE_NULL) {
+                for (int i = 0; i < n_layer; ++i)
+                    for (int l = 0; l < np; ++l) IX2(gfr, l, i, wp) = IX3(atm.gas_mix_ratio, l, i, g, ndp, ndl);
+            } else if (isk != SOCGPU_IP_SCALE_TERM) {
+                status = SOCGPU_I_ERR_FATAL;
+            }
+            if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "illegal type of scaling"); break; }
+        }
+        if (status != SOCGPU_I_NORMAL) break;
+
+        /* Planck terms (diff_planck_source_mod.F90:102-136) and boundary
+         * fluxes (solve_band_random_overlap.F90:565-600) */
+        for (int l = 0; l < np; ++l) {
+            w.sec_0[l] = bd->zen_0 ? bd->zen_0[p0 + l] : 1.0;
+            w.alb_diff[l] = IX3(bd->rho_alb, p0 + l, 0, b, ndp, 2);
+            w.alb_dir[l] = IX3(bd->rho_alb, p0 + l, 1, b, ndp, 2);
+        }
+        if (c->isolir == SOCGPU_IP_INFRA_RED) {
+            for (int l = 0; l < np; ++l)
+                IX2(w.planck_flux, l, 0, wp) = planck_flux_band(d, b, IX2(atm.t_level, l, 0, ndp));
+            for (int i = 1; i <= n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    IX2(w.planck_flux, l, i, wp) = planck_flux_band(d, b, IX2(atm.t_level, l, i, ndp));
+                    IX2(w.planck_diff, l, i - 1, wp) = IX2(w.planck_flux, l, i, wp) - IX2(w.planck_flux, l, i - 1, wp);
+                }
+            if (c->l_ir_source_quad)
+                for (int i = 1; i <= n_layer; ++i)
+                    for (int l = 0; l < np; ++l) {
+                        double bt = planck_flux_band(d, b, IX2(atm.t, l, i - 1, ndp));
+                        IX2(w.planck_diff_2, l, i - 1, wp) = 2.0 * (IX2(w.planck_flux, l, i, wp)
+                            + IX2(w.planck_flux, l, i - 1, wp) - 2.0 * bt);
+                    }
+            for (int l = 0; l < np; ++l) {
+                w.flux_ground[l] = planck_flux_band(d, b, bd->t_ground[p0 + l]);
+                w.flux_inc_direct[l] = 0.0;
+                w.flux_inc_down[l] = -IX2(w.planck_flux, l, 0, wp);
+                w.d_planck_flux_surface[l] = w.flux_ground[l] - IX2(w.planck_flux, l, n_layer, wp);
+            }
+        } else {
+            for (int l = 0; l < np; ++l) {
+                double solar_irrad_band = bd->solar_irrad[p0 + l] * d->solar_flux_band[b];
+                w.d_planck_flux_surface[l] = 0.0;
+                w.flux_inc_down[l] = solar_irrad_band / w.sec_0[l];
+                w.flux_inc_direct[l] = solar_irrad_band / w.sec_0[l];
+            }
+        }
+
+        /* k-term products of random overlap (solve_band_random_overlap.F90:533-560) */
+        int n_term = 1;
+        for (int j = 0; j < n_abs; ++j) n_term *= nk[j];
+        for (int kt = 0; kt < n_term; ++kt) {
+            int iex_of[SOCGPU_MAX_SPECIES];
+            double product_weight = 1.0;
+            int step_prod = 1;
+            for (int j = 0; j < n_abs; ++j) {
+                step_prod *= nk[j];
+                int step = n_term / step_prod;
+                iex_of[j] = (kt / step) % nk[j];
+                double wj = sp_kw(d->w, d, iex_of[j], b, gas_of[j]);
+                product_weight = (j == 0) ? wj : product_weight * wj;
+            }
+            if (n_abs > 0 && !(product_weight > 0.0)) continue;
+            if (n_abs == 0) product_weight = 1.0;
+            /* gas_optical_properties (gas_optical_properties.F90:80-95) with
+             * k_abs_layer = k * gas_frac_rescaled (radiance_calc.F90:1386-1470) */
+            for (int i = 0; i < n_layer; ++i)
+                for (int l = 0; l < np; ++l) IX2(w.k_gas_abs, l, i, wp) = 0.0;
+            for (int j = 0; j < n_abs; ++j) {
+                int g = gas_of[j], iex = iex_of[j];
+                double kval = sp_kw(d->k, d, iex, b, g);
+                int isk = sp_bg(d->i_scale_k, d, b, g);
+                const double *gfr = w.gfr + (size_t)wp * ndl * j;
+                for (int i = 0; i < n_layer; ++i)
+                    for (int l = 0; l < np; ++l) {
+                        double kal;
+                        if (isk == SOCGPU_IP_SCALE_TERM) {
+                            /* per-term scaling: computed below */
+                            kal = 0.0;
+                        } else {
+                            kal = kval * IX2(gfr, l, i, wp);
+                        }
+                        if (j == 0) IX2(w.k_gas_abs, l, i, wp) = kal;
+                        else IX2(w.k_gas_abs, l, i, wp) = IX2(w.k_gas_abs, l, i, wp) + kal;
+                    }
+                if (isk == SOCGPU_IP_SCALE_TERM) {
+                    double *tmp = w.beta;   /* scratch */
+                    status = scale_absorb(np, n_layer, ndp, wp, atm.p, atm.t, tmp, sp_bg(d->i_scale_fnc, d, b, g),
+                                          IX2(d->p_ref, g, b, d->nd_species), IX2(d->t_ref, g, b, d->nd_species),
+                                          sp_scale(d, iex, b, g), d->l_doppler ? d->l_doppler[g] : 0,
+                                          d->doppler_cor ? d->doppler_cor[g] : 0.0);
+                    for (int i = 0; i < n_layer; ++i)
+                        for (int l = 0; l < np; ++l) {
+                            double v = IX2(tmp, l, i, wp) * IX3(atm.gas_mix_ratio, l, i, g, ndp, ndl);
+                            double kal = kval * (v > 0.0 ? v : 0.0);
+                            if (j == 0) IX2(w.k_gas_abs, l, i, wp) = kal;
+                            else IX2(w.k_gas_abs, l, i, wp) = IX2(w.k_gas_abs, l, i, wp) + kal;
+                        }
+                }
+            }
+            if (l_cloud) {
+                solve_mcica_term(&w, c, dm, d, atm.mass, cld, b, n_abs > 0 ? iex_of[0] : 0);
+            } else {
+                clear_coefficients(&w, c, atm.mass, ndp);
+                column_solve(&w, c, c->i_scatter_method != SOCGPU_IP_SCATTER_FULL);
+            }
+            /* augment_radiance / augment_channel (augment_channel_mod.F90:158-235) */
+            double wi = weight_band * product_weight;
+            for (int i = 0; i <= n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    IX2(out.flux_up, l, i, ndp) = IX2(out.flux_up, l, i, ndp) + wi * IX2(w.flux_total, l, 2 * i, wp);
+                    IX2(out.flux_down, l, i, ndp) = IX2(out.flux_down, l, i, ndp) + wi * IX2(w.flux_total, l, 2 * i + 1, wp);
+                    if (out.flux_direct && c->isolir == SOCGPU_IP_SOLAR)
+                        IX2(out.flux_direct, l, i, ndp) = IX2(out.flux_direct, l, i, ndp) + wi * IX2(w.flux_direct, l, i, wp);
+                    if (out.flux_up_band)
+                        IX3(out.flux_up_band, l, i, b, ndp, ndl + 1) += wi * IX2(w.flux_total, l, 2 * i, wp);
+                    if (out.flux_down_band)
+                        IX3(out.flux_down_band, l, i, b, ndp, ndl + 1) += wi * IX2(w.flux_total, l, 2 * i + 1, wp);
+                }
+            if (out.flux_div)
+                for (int i = 1; i <= n_layer; ++i)
+                    for (int l = 0; l < np; ++l)
+                        IX2(out.flux_div, l, i - 1, ndp) = IX2(out.flux_div, l, i - 1, ndp) + wi
+                            * (IX2(w.flux_total, l, 2 * i, wp) - IX2(w.flux_total, l, 2 * i - 2, wp)
+                               + IX2(w.flux_total, l, 2 * i - 1, wp) - IX2(w.flux_total, l, 2 * i + 1, wp));
+        }
+        /* adjust_ir_radiance (adjust_ir_radiance.F90:75-95, adjust_ir_channel) */
+        if (c->isolir == SOCGPU_IP_INFRA_RED)
+            for (int i = 0; i <= n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    double bw = IX2(w.planck_flux, l, i, wp) * weight_band;
+                    IX2(out.flux_up, l, i, ndp) = IX2(out.flux_up, l, i, ndp) + bw;
+                    IX2(out.flux_down, l, i, ndp) = IX2(out.flux_down, l, i, ndp) + bw;
+                    if (out.flux_up_band) IX3(out.flux_up_band, l, i, b, ndp, ndl + 1) += bw;
+                    if (out.flux_down_band) IX3(out.flux_down_band, l, i, b, ndp, ndl + 1) += bw;
+                }
+    }
+    /* heating rate (l_run_cdf.F90:1340-1380) */
+    if (status == SOCGPU_I_NORMAL && out.heating_rate)
+        for (int i = 1; i <= n_layer; ++i)
+            for (int l = 0; l < np; ++l) {
+                double hc = IX2(atm.mass, l, i - 1, ndp) * cp_air_dry;
+                double hr;
+                if (c->l_flux_div && out.flux_div) {
+                    hr = seconds_per_day * IX2(out.flux_div, l, i - 1, ndp) / hc;
+                } else {
+                    double fn0 = IX2(out.flux_down, l, i - 1, ndp) - IX2(out.flux_up, l, i - 1, ndp);
+                    double fn1 = IX2(out.flux_down, l, i, ndp) - IX2(out.flux_up, l, i, ndp);
+                    hr = (fn0 - fn1) / hc;
+                    hr = seconds_per_day * hr;
+                }
+                IX2(out.heating_rate, l, i - 1, ndp) = hr;
+            }
+    (void)ict;
+    work_free(&w);
+    return status;
+}
+
+int oracle_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm,
+                         const socgpu_spectrum_desc *d, const socgpu_atm *atm,
+                         const socgpu_cld *cld, const socgpu_aer *aer,
+                         const socgpu_bound *bd, socgpu_radout *out,
+                         char *msg, size_t msg_len)
+{
+    return segment_radiance_calc(c, dm, d, atm, cld, aer, bd, out, 0, atm->n_profile, msg, msg_len);
+}
+
+int oracle_radiance_calc_segmented(const socgpu_control *c, const socgpu_dimen *dm,
+                                   const socgpu_spectrum_desc *d, const socgpu_atm *atm,
+                                   const socgpu_cld *cld, const socgpu_aer *aer,
+                                   const socgpu_bound *bd, socgpu_radout *out,
+                                   int n_threads, char *msg, size_t msg_len)
+{
+    int n = atm->n_profile;
+    int status = check_options(c, d, atm, dm, cld, msg, msg_len);
+    if (status != SOCGPU_I_NORMAL) return status;
+#ifdef _OPENMP
+    if (n_threads <= 0) n_threads = omp_get_max_threads();
+#else
+    n_threads = 1;
+#endif
+    int n_seg = n_threads * 4;
+    if (n_seg > n) n_seg = n > 0 ? n : 1;
+    int worst = SOCGPU_I_NORMAL;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads) reduction(max:worst)
+#endif
+    for (int s = 0; s < n_seg; ++s) {
+        int p0 = (int)((long long)n * s / n_seg), p1 = (int)((long long)n * (s + 1) / n_seg);
+        char m[256] = {0};
+        int st = segment_radiance_calc(c, dm, d, atm, cld, aer, bd, out, p0, p1 - p0, m, sizeof m);
+        if (st > worst) worst = st;
+    }
+    if (worst != SOCGPU_I_NORMAL) set_msg(msg, msg_len, "a column segment failed");
+    return worst;
+}
+
+/* --------------------------------------------------------------------- */
+/* cloud_gen (socrates_cloud_gen.F90:8-470).  Cloud arrays are indexed
+ * (nd_profile, cloud_top:nd_layer); zf and the column seeds by profile.  */
+static const int lcg_m = 86436, lcg_a = 1093, lcg_c = 18257;   /* socrates_cloud_gen.F90:48-50 */
+
+static inline int lcg_next(int x)
+{   /* temp = x*a+c; x = temp - int(real(temp)*rm)*m  (socrates_cloud_gen.F90:180-203) */
+    const double rm = 1.0 / (double)lcg_m;
+    int temp = x * lcg_a + lcg_c;
+    return temp - (int)((double)temp * rm) * lcg_m;
+}
+
+static inline double philox_u01(uint32_t word) { return (double)word * (1.0 / 4294967296.0); }
+
+int oracle_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile,
+                     int il1, int il2, int n_subcol, int n1, int n2,
+                     int ipph, int ioverlap, const int *rand_seed,
+                     const double *rlc_cf, const double *rlc_cw,
+                     const double *sigma_qcw, const double *avg_cf,
+                     const double *c_cloud, const double *c_ratio,
+                     const double *zf, const double *xcw,
+                     int *n_subcol_cld, double *c_sub, int rng)
+{
+    const double rm = 1.0 / (double)lcg_m;
+    const double cut = EPS_R;
+    int ndc = nd_layer - cloud_top + 1;
+    int rand_seed_max = (2147483647 - lcg_c) / lcg_a;
+#define CLD(a, l, k) ((a)[(size_t)((l) - 1) + (size_t)nd_profile * (size_t)((k) - cloud_top)])
+#define CSUB(l, k, s) (c_sub[(size_t)((l) - 1) + (size_t)nd_profile * ((size_t)((k) - cloud_top) + (size_t)ndc * (size_t)((s) - 1))])
+    if (ioverlap < 0 || ioverlap > 3) return SOCGPU_I_ERR_FATAL;
+    for (int il = il1; il <= il2; ++il)
+        for (int k = cloud_top; k <= nd_layer; ++k)
+            for (int s = 1; s <= n_subcol; ++s) CSUB(il, k, s) = 0.0;
+
+    /* first and last cloudy layers over all columns */
+    int k_top = 0, l_top = 0;
+    for (int k = cloud_top; k <= n_layer && !l_top; ++k)
+        for (int il = il1; il <= il2; ++il) { k_top = k; if (CLD(avg_cf, il, k) > cut) l_top = 1; }
+    if (!l_top) k_top = 0;
+    if (k_top == 0) {
+        for (int il = il1; il <= il2; ++il) n_subcol_cld[il - 1] = 0;
+        return SOCGPU_I_NORMAL;
+    }
+    int k_base = 0, l_bot = 0;
+    for (int k = n_layer; k >= cloud_top && !l_bot; --k)
+        for (int il = il1; il <= il2; ++il) { k_base = k; if (CLD(avg_cf, il, k) >= cut) l_bot = 1; }
+
+    double *alpha = zalloc((size_t)(nd_layer + 2)), *rcorr = zalloc((size_t)(nd_layer + 2));
+    int *seed_x = (int *)calloc((size_t)n_subcol, sizeof(int));
+    int *seed_y = (int *)calloc((size_t)n_subcol, sizeof(int));
+    for (int il = il1; il <= il2; ++il) {
+        /* seed streams (socrates_cloud_gen.F90:180-203) */
+        int rd = abs(rand_seed[il - 1]) % rand_seed_max;
+        for (int i = 0; i < n_subcol; ++i) rd = lcg_next(rd);
+        for (int i = 0; i < n_subcol; ++i) { rd = lcg_next(rd); seed_x[i] = rd; }
+        for (int i = 0; i < n_subcol; ++i) { rd = lcg_next(rd); seed_y[i] = rd; }
+        uint32_t key[2] = {(uint32_t)rand_seed[il - 1], 0x534F4352u};
+
+        /* overlap parameters alpha/rcorr (socrates_cloud_gen.F90:338-375) */
+        if (ioverlap >= 1)
+            for (int k = k_top - 1; k <= k_base - 1; ++k) {
+                double a = 0.0, r = 0.0;
+                if (!(ioverlap == 1 || k < cloud_top)) {
+                    if (ioverlap == 2 || CLD(avg_cf, il, k) > 0.0) {
+                        double dz = zf[(size_t)(il - 1) + (size_t)nd_profile * (size_t)(k - 1)]
+                                  - zf[(size_t)(il - 1) + (size_t)nd_profile * (size_t)k];
+                        a = CLD(rlc_cf, il, k) > 0.0 ? exp(dz / CLD(rlc_cf, il, k)) : 0.0;
+                        r = CLD(rlc_cw, il, k) > 0.0 ? exp(dz / CLD(rlc_cw, il, k)) : 0.0;
+                    }
+                }
+                alpha[k] = a; rcorr[k] = r;
+            }
+        int i_loc = 1;
+        /* x and y persist across the subcolumns of a column, as the
+         * reference's per-column arrays x(il), y(il) do */
+        double x = 0.0, y = 0.0, x1, y1;
+        for (int i = 1; i <= n_subcol; ++i) {
+            int int_x = seed_x[i - 1], int_y = seed_y[i - 1];
+            int l_cld = 0;
+            for (int k = k_top; k <= k_base; ++k) {
+                double cf = CLD(avg_cf, il, k);
+                if (!(cf > 0.0)) continue;
+                uint32_t u[4] = {0, 0, 0, 0};
+                if (rng == SOCGPU_RNG_PHILOX) {
+                    uint32_t ctr[4] = {(uint32_t)k, (uint32_t)i, 0u, 0u};
+                    oracle_philox4x32_10(ctr, key, u);
+                }
+                double zcw;
+                if (ioverlap == 0) {
+                    /* maximum-random (socrates_cloud_gen.F90:251-330) */
+                    if (rng == SOCGPU_RNG_PHILOX) { x = philox_u01(u[0]); y = philox_u01(u[1]); }
+                    else {
+                        int_x = lcg_next(int_x); x = (double)int_x * rm;
+                        int_y = lcg_next(int_y); y = (double)int_y * rm;
+                    }
+                    if (k == cloud_top) {
+                        if (rng == SOCGPU_RNG_PHILOX) { x = philox_u01(u[2]); y = philox_u01(u[3]); }
+                        else {
+                            int_x = lcg_next(int_x); x = (double)int_x * rm;
+                            int_y = lcg_next(int_y); y = (double)int_y * rm;
+                        }
+                    } else if (x < (1.0 - CLD(avg_cf, il, k - 1))) {
+                        if (rng == SOCGPU_RNG_PHILOX) { x1 = philox_u01(u[2]); y1 = philox_u01(u[3]); }
+                        else {
+                            int_x = lcg_next(int_x); x1 = (double)int_x * rm;
+                            int_y = lcg_next(int_y); y1 = (double)int_y * rm;
+                        }
+                        x = x1 * (1.0 - CLD(avg_cf, il, k - 1));
+                        y = y1;
+                    }
+                } else {
+                    /* random / exponential / exponential-random (socrates_cloud_gen.F90:376-460) */
+                    if (rng == SOCGPU_RNG_PHILOX) { x1 = philox_u01(u[0]); y1 = philox_u01(u[1]); }
+                    else {
+                        int_x = lcg_next(int_x); x1 = (double)int_x * rm;
+                        int_y = lcg_next(int_y); y1 = (double)int_y * rm;
+                    }
+                    if (x1 >= alpha[k - 1]) {
+                        if (rng == SOCGPU_RNG_PHILOX) x = philox_u01(u[2]);
+                        else { int_x = lcg_next(int_x); x = (double)int_x * rm; }
+                    }
+                    if (y1 >= rcorr[k - 1]) {
+                        if (rng == SOCGPU_RNG_PHILOX) y = philox_u01(u[3]);
+                        else { int_y = lcg_next(int_y); y = (double)int_y * rm; }
+                    }
+                }
+                if (x < cf) {
+                    if (ipph == 0) {
+                        zcw = 1.0;
+                    } else {
+                        double sig = CLD(sigma_qcw, il, k);
+                        double ratio = 1.0;
+                        if (ioverlap != 0) {
+                            if (x < CLD(c_cloud, il, k)) ratio = CLD(c_ratio, il, k);
+                            else {
+                                double cc = CLD(c_cloud, il, k);
+                                ratio = (cc > 0.0 && cc < cf) ? (cf - CLD(c_ratio, il, k) * cc > 0.0 ?
+                                         (cf - CLD(c_ratio, il, k) * cc) : 0.0) / (cf - cc) : 1.0;
+                            }
+                        }
+                        double rind1 = y * (n1 - 1) + 1.0;
+                        int ind1 = (int)rind1; if (ind1 > n1 - 1) ind1 = n1 - 1; if (ind1 < 1) ind1 = 1;
+                        rind1 = rind1 - (double)ind1; if (rind1 > 1.0) rind1 = 1.0; if (rind1 < 0.0) rind1 = 0.0;
+                        double rind2 = 40.0 * sig - 3.0;
+                        int ind2 = (int)rind2; if (ind2 > n2 - 1) ind2 = n2 - 1; if (ind2 < 1) ind2 = 1;
+                        rind2 = rind2 - (double)ind2; if (rind2 > 1.0) rind2 = 1.0; if (rind2 < 0.0) rind2 = 0.0;
+#define XCW(a, b) xcw[(size_t)((a) - 1) + (size_t)n1 * (size_t)((b) - 1)]
+                        zcw = (1.0 - rind1) * (1.0 - rind2) * XCW(ind1, ind2)
+                            + (1.0 - rind1) * rind2 * XCW(ind1, ind2 + 1)
+                            + rind1 * (1.0 - rind2) * XCW(ind1 + 1, ind2)
+                            + rind1 * rind2 * XCW(ind1 + 1, ind2 + 1);
+#undef XCW
+                        zcw = zcw * ratio;
+                    }
+                    l_cld = 1;
+                    CSUB(il, k, i_loc) = zcw;
+                }
+            }
+            if (l_cld) i_loc = i_loc + 1;
+        }
+        n_subcol_cld[il - 1] = i_loc - 1;
+    }
+    free(alpha); free(rcorr); free(seed_x); free(seed_y);
+#undef CLD
+#undef CSUB
+    return SOCGPU_I_NORMAL;
+}

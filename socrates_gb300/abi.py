@@ -1,0 +1,152 @@
+"""ctypes mirror of include/socgpu.h.
+
+The same structures bind the product library (libsocgpu.so) and, in the
+tests, the CPU oracle, so both receive byte-identical argument blocks.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+# status codes (rad_pcf.F90:391-405)
+I_NORMAL, I_ERR_FATAL, I_ABORT_CALCULATION, I_ERR_IO, I_ERR_RANGE, I_ERR_EXIST = 0, 1, 2, 4, 5, 6
+
+# option identifiers (rad_pcf.F90 values)
+IP_SOLAR, IP_INFRA_RED = 1, 2
+IP_TWO_STREAM = 1
+IP_EDDINGTON, IP_DISCRETE_ORD, IP_IFM, IP_PIFM85 = 2, 4, 5, 6
+IP_ELSASSER, IP_2S_TEST, IP_HEMI_MEAN, IP_PIFM80 = 12, 14, 15, 16
+IP_SCATTER_FULL, IP_NO_SCATTER_ABS, IP_NO_SCATTER_EXT = 1, 2, 3
+IP_DIRECT_NOSCALING, IP_DIRECT_DELTA_SCALING, IP_DIRECT_CSR_SCALING = 0, 1, 2
+IP_SOLVER_NO_SCAT, IP_SOLVER_HOMOGEN_DIRECT = 2, 13
+IP_CLOUD_CLEAR, IP_CLOUD_MCICA = 5, 10
+IP_CLOUD_ICE_WATER = 2
+IP_CLOUD_TYPE_WATER, IP_CLOUD_TYPE_ICE = 1, 2
+IP_PHASE_WATER, IP_PHASE_ICE = 1, 2
+IP_CLCMP_ST_WATER, IP_CLCMP_ST_ICE = 1, 2
+IP_DROP_PADE_2, IP_ICE_PADE_2_PHF = 5, 20
+IP_OVERLAP_RANDOM = 2
+IP_SCALE_NULL, IP_SCALE_BAND, IP_SCALE_TERM = 0, 1, 2
+IP_SCALE_FNC_NULL, IP_SCALE_POWER_LAW, IP_SCALE_POWER_QUAD, IP_SCALE_DOPPLER_QUAD = 0, 1, 2, 3
+IP_RAYLEIGH_TOTAL = 1
+IP_MAX_RAND, IP_RAND, IP_EXPONENTIAL, IP_EXPONENTIAL_RAND = 0, 1, 2, 3
+IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0, 1, 2
+
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+RNG_LCG, RNG_PHILOX = 0, 1
+ABI_VERSION = 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class SpectrumDesc(C.Structure):
+    _fields_ = [
+        ("nd_band", C.c_int), ("nd_species", C.c_int), ("nd_k_term", C.c_int), ("nd_scale_variable", C.c_int),
+        ("nd_thermal_coeff", C.c_int), ("nd_drop_type", C.c_int), ("nd_ice_type", C.c_int),
+        ("nd_cloud_parameter", C.c_int),
+        ("n_band", C.c_int),
+        ("wavelength_short", _dp), ("wavelength_long", _dp),
+        ("solar_flux_band", _dp), ("i_rayleigh_scheme", C.c_int), ("rayleigh_coeff", _dp),
+        ("n_absorb", C.c_int), ("type_absorb", _ip), ("n_band_absorb", _ip), ("index_absorb", _ip),
+        ("i_band_k", _ip), ("i_scale_k", _ip), ("i_scale_fnc", _ip),
+        ("k", _dp), ("w", _dp), ("scale", _dp), ("p_ref", _dp), ("t_ref", _dp),
+        ("l_doppler", _ip), ("doppler_cor", _dp),
+        ("n_deg_fit", C.c_int), ("t_ref_planck", C.c_double), ("thermal_coeff", _dp),
+        ("l_drop_type", _ip), ("i_drop_parm", _ip), ("drop_parm_list", _dp),
+        ("l_ice_type", _ip), ("i_ice_parm", _ip), ("ice_parm_list", _dp),
+    ]
+
+
+class Control(C.Structure):
+    _fields_ = [
+        ("isolir", C.c_int), ("i_angular_integration", C.c_int), ("i_2stream", C.c_int),
+        ("i_scatter_method", C.c_int), ("i_solver", C.c_int), ("i_cloud", C.c_int),
+        ("i_cloud_representation", C.c_int), ("i_gas_overlap", C.c_int), ("i_direct_tau", C.c_int),
+        ("l_rescale", C.c_int), ("n_order_forward", C.c_int), ("l_ir_source_quad", C.c_int),
+        ("l_rayleigh", C.c_int), ("l_gas", C.c_int), ("l_aerosol_mode", C.c_int), ("l_flux_div", C.c_int),
+        ("first_band", C.c_int), ("last_band", C.c_int), ("weight_band", _dp), ("precision", C.c_int),
+    ]
+
+
+class Dimen(C.Structure):
+    _fields_ = [
+        ("nd_profile", C.c_int), ("nd_layer", C.c_int), ("id_cloud_top", C.c_int), ("nd_aerosol_mode", C.c_int),
+        ("nd_cloud_component", C.c_int), ("nd_cloud_type", C.c_int), ("nd_subcol_gen", C.c_int),
+        ("nd_subcol_req", C.c_int),
+    ]
+
+
+class Atm(C.Structure):
+    _fields_ = [
+        ("n_profile", C.c_int), ("n_layer", C.c_int),
+        ("p", _dp), ("t", _dp), ("p_level", _dp), ("t_level", _dp), ("mass", _dp), ("gas_mix_ratio", _dp),
+    ]
+
+
+class Bound(C.Structure):
+    _fields_ = [("zen_0", _dp), ("solar_irrad", _dp), ("rho_alb", _dp), ("t_ground", _dp)]
+
+
+class Aer(C.Structure):
+    _fields_ = [
+        ("n_mode", C.c_int), ("mode_mix_ratio", _dp), ("mode_absorption", _dp),
+        ("mode_scattering", _dp), ("mode_asymmetry", _dp),
+    ]
+
+
+class Cld(C.Structure):
+    _fields_ = [
+        ("n_condensed", C.c_int), ("type_condensed", _ip), ("i_cloud_type", _ip), ("i_condensed_param", _ip),
+        ("i_condensed_type", _ip), ("condensed_mix_ratio", _dp), ("condensed_dim_char", _dp),
+        ("n_cloud_type", C.c_int), ("w_cloud", _dp), ("frac_cloud", _dp),
+        ("n_subcol_gen", C.c_int), ("n_subcol_req", C.c_int), ("c_sub", _dp), ("frac_cloudy", _dp),
+        ("n_subcol_cld", _ip), ("subcol_k", _ip), ("first_subcol_k", _ip), ("subcol_reorder", _ip),
+    ]
+
+
+class Radout(C.Structure):
+    _fields_ = [
+        ("flux_up", _dp), ("flux_down", _dp), ("flux_direct", _dp), ("flux_div", _dp),
+        ("heating_rate", _dp), ("flux_up_band", _dp), ("flux_down_band", _dp),
+    ]
+
+
+ABI_FUNCTIONS = (
+    "socgpu_abi_version", "socgpu_spectrum_register", "socgpu_spectrum_lookup", "socgpu_spectrum_n_gpoint",
+    "socgpu_spectrum_release", "socgpu_radiance_calc", "socgpu_radiance_calc_device", "socgpu_cloud_gen",
+    "socgpu_cloud_gen_device", "socgpu_kernel_launch_count", "socgpu_set_device", "socgpu_set_tile_config",
+)
+
+_CALC_ARGS = [C.POINTER(Control), C.POINTER(Dimen), C.c_int, C.POINTER(Atm), C.POINTER(Cld), C.POINTER(Aer),
+              C.POINTER(Bound), C.POINTER(Radout)]
+_GEN_ARGS = [C.c_int] * 11 + [C.c_void_p] + [C.c_void_p] * 8 + [C.c_void_p, C.c_void_p, C.c_int]
+
+
+def declare(lib: C.CDLL) -> C.CDLL:
+    """Attach argument and return types of the ABI to a loaded library."""
+    lib.socgpu_abi_version.restype = C.c_int
+    lib.socgpu_spectrum_register.argtypes = [C.c_char_p, C.POINTER(SpectrumDesc), C.POINTER(C.c_int), C.c_char_p,
+                                             C.c_size_t]
+    lib.socgpu_spectrum_lookup.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+    lib.socgpu_spectrum_n_gpoint.argtypes = [C.c_int]
+    lib.socgpu_spectrum_release.argtypes = [C.c_int]
+    lib.socgpu_radiance_calc.argtypes = _CALC_ARGS + [C.c_char_p, C.c_size_t]
+    lib.socgpu_radiance_calc_device.argtypes = _CALC_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]
+    lib.socgpu_cloud_gen.argtypes = _GEN_ARGS + [C.c_char_p, C.c_size_t]
+    lib.socgpu_cloud_gen_device.argtypes = _GEN_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]
+    lib.socgpu_kernel_launch_count.restype = C.c_longlong
+    lib.socgpu_set_device.argtypes = [C.c_int]
+    lib.socgpu_set_tile_config.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
+    for name in ABI_FUNCTIONS:
+        f = getattr(lib, name)
+        if name != "socgpu_kernel_launch_count":
+            f.restype = C.c_int
+    return lib
+
+
+def header_functions(header: Path) -> list[str]:
+    """Names of the entry points declared in a header (for the export test)."""
+    import re
+    text = header.read_text()
+    return sorted(set(re.findall(r"SOCGPU_API\s+(?:int|long long)\s+(socgpu_\w+)\s*\(", text)))

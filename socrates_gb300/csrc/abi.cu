@@ -1,0 +1,765 @@
+// abi.cu -- the extern "C" boundary of libsocgpu (include/socgpu.h).
+//
+// Host-side work only: spectrum registry keyed by name, option validation
+// with the reference's error codes, per-thread device workspace and
+// stream, host<->device staging for the host-pointer entry points, and
+// the choice of kernel tile shape.  No computation of the flux path runs
+// on the host: an unsupported request returns SOCGPU_I_ERR_FATAL.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "socgpu_internal.h"
+
+namespace socgpu {
+
+int launch_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2,
+                     int n_subcol, int n1, int n2, int ipph, int ioverlap, const int *rand_seed,
+                     const double *rlc_cf, const double *rlc_cw, const double *sigma_qcw,
+                     const double *avg_cf, const double *c_cloud, const double *c_ratio,
+                     const double *zf, const double *xcw, int *n_subcol_cld, double *c_sub, int rng,
+                     int *range_dev, cudaStream_t st, char *msg, size_t len);
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+
+void set_msg(char *msg, size_t len, const char *fmt, ...) {
+  if (!msg || len == 0) return;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(msg, len, fmt, ap);
+  va_end(ap);
+}
+
+#define CUDA_TRY(expr)                                                                  \
+  do {                                                                                  \
+    cudaError_t e_ = (expr);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      set_msg(msg, msg_len, "%s failed: %s", #expr, cudaGetErrorString(e_));            \
+      return SOCGPU_I_ABORT_CALCULATION;                                                \
+    }                                                                                   \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Spectrum registry.
+struct SpectrumEntry {
+  std::string name;
+  SpectrumDev dev{};
+  std::vector<BandInfo> bands_host;
+  std::vector<GPoint> gpoints_host;
+  int device = 0;
+};
+
+std::mutex g_reg_mutex;
+std::map<int, std::unique_ptr<SpectrumEntry>> g_spectra;
+std::map<std::string, int> g_names;
+int g_next_handle = 1;
+
+template <class T>
+T fget2(const T *a, int i, int j, int nd1) { return a[(size_t)i + (size_t)nd1 * (size_t)j]; }
+
+int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, size_t msg_len) {
+  if (d->n_band < 1 || d->n_band > SOCGPU_MAX_BAND || d->n_band > d->nd_band) {
+    set_msg(msg, msg_len, "number of bands %d outside 1..%d", d->n_band, SOCGPU_MAX_BAND);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  if (d->n_absorb > SOCGPU_MAX_SPECIES) {
+    set_msg(msg, msg_len, "too many absorbers (%d)", d->n_absorb);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  if (d->thermal_coeff && (d->n_deg_fit < 0 || d->n_deg_fit + 1 > kMaxPlanckCoeff)) {
+    set_msg(msg, msg_len, "Planck polynomial degree %d unsupported", d->n_deg_fit);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  e.bands_host.assign(d->n_band, BandInfo{});
+  e.gpoints_host.clear();
+  for (int b = 0; b < d->n_band; ++b) {
+    BandInfo &bi = e.bands_host[b];
+    bi.solar_flux_band = d->solar_flux_band ? d->solar_flux_band[b] : 0.0;
+    bi.rayleigh_coeff = d->rayleigh_coeff ? d->rayleigh_coeff[b] : 0.0;
+    if (d->thermal_coeff)
+      for (int j = 0; j <= d->n_deg_fit; ++j) bi.planck[j] = d->thermal_coeff[(size_t)j + (size_t)d->nd_thermal_coeff * b];
+    int n_abs = d->n_band_absorb ? d->n_band_absorb[b] : 0;
+    if (n_abs > kMaxAbsPerBand) {
+      set_msg(msg, msg_len, "band %d has %d absorbers; at most %d supported", b + 1, n_abs, kMaxAbsPerBand);
+      return SOCGPU_I_ERR_RANGE;
+    }
+    bi.n_abs = n_abs;
+    int nk[kMaxAbsPerBand];
+    long long n_term = 1;
+    for (int j = 0; j < n_abs; ++j) {
+      int g = fget2(d->index_absorb, j, b, d->nd_species) - 1;
+      if (g < 0 || g >= d->n_absorb) {
+        set_msg(msg, msg_len, "band %d lists absorber index %d outside the spectrum", b + 1, g + 1);
+        return SOCGPU_I_ERR_RANGE;
+      }
+      BandGas &gs = bi.gas[j];
+      gs.species = g;
+      gs.i_scale_k = fget2(d->i_scale_k, b, g, d->nd_band);
+      gs.i_scale_fnc = fget2(d->i_scale_fnc, b, g, d->nd_band);
+      gs.l_doppler = d->l_doppler ? d->l_doppler[g] : 0;
+      gs.doppler_cor = d->doppler_cor ? d->doppler_cor[g] : 0.0;
+      gs.p_ref = fget2(d->p_ref, g, b, d->nd_species);
+      gs.t_ref = fget2(d->t_ref, g, b, d->nd_species);
+      if (gs.i_scale_k != SOCGPU_IP_SCALE_NULL && gs.i_scale_k != SOCGPU_IP_SCALE_BAND &&
+          gs.i_scale_k != SOCGPU_IP_SCALE_TERM) {
+        set_msg(msg, msg_len, "band %d absorber %d: illegal type of scaling %d", b + 1, g + 1, gs.i_scale_k);
+        return SOCGPU_I_ERR_FATAL;
+      }
+      if (gs.i_scale_k != SOCGPU_IP_SCALE_NULL && gs.i_scale_fnc != SOCGPU_IP_SCALE_FNC_NULL &&
+          gs.i_scale_fnc != SOCGPU_IP_SCALE_POWER_LAW && gs.i_scale_fnc != SOCGPU_IP_SCALE_POWER_QUAD &&
+          gs.i_scale_fnc != SOCGPU_IP_SCALE_DOPPLER_QUAD) {
+        set_msg(msg, msg_len, "band %d absorber %d: scaling function %d is not supported on the device path "
+                "(lookup tables and double power laws are not implemented)", b + 1, g + 1, gs.i_scale_fnc);
+        return SOCGPU_I_ERR_FATAL;
+      }
+      int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
+      for (int v = 0; v < nv; ++v)
+        gs.scale[v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable *
+                                              ((size_t)0 + (size_t)d->nd_k_term * ((size_t)b + (size_t)d->nd_band * g))];
+      nk[j] = fget2(d->i_band_k, b, g, d->nd_band);
+      if (nk[j] < 1 || nk[j] > d->nd_k_term) {
+        set_msg(msg, msg_len, "band %d absorber %d: %d k-terms", b + 1, g + 1, nk[j]);
+        return SOCGPU_I_ERR_RANGE;
+      }
+      n_term *= nk[j];
+    }
+    bi.g_first = (int)e.gpoints_host.size();
+    if (n_abs == 0) n_term = 1;
+    if ((long long)e.gpoints_host.size() + n_term > SOCGPU_MAX_GPOINT) {
+      set_msg(msg, msg_len, "more than %d k-term products", SOCGPU_MAX_GPOINT);
+      return SOCGPU_I_ERR_RANGE;
+    }
+    // k-term products of random overlap (solve_band_random_overlap.F90:533-560)
+    for (long long kt = 0; kt < n_term; ++kt) {
+      GPoint gp{};
+      gp.band = b;
+      gp.n_abs = n_abs;
+      gp.weight = 1.0;
+      long long step_prod = 1;
+      for (int j = 0; j < n_abs; ++j) {
+        step_prod *= nk[j];
+        long long step = n_term / step_prod;
+        int iex = (int)((kt / step) % nk[j]);
+        int g = bi.gas[j].species;
+        size_t q = (size_t)iex + (size_t)d->nd_k_term * ((size_t)b + (size_t)d->nd_band * g);
+        double wj = d->w[q];
+        gp.weight = (j == 0) ? wj : gp.weight * wj;
+        gp.k[j] = d->k[q];
+        if (j == 0) gp.iex_major = iex;
+        int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
+        for (int v = 0; v < nv; ++v) gp.term_scale[j][v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable * q];
+      }
+      if (n_abs > 0 && !(gp.weight > 0.0)) continue;   // n_term_reduced
+      e.gpoints_host.push_back(gp);
+    }
+    bi.g_count = (int)e.gpoints_host.size() - bi.g_first;
+  }
+  SpectrumDev &s = e.dev;
+  s.n_band = d->n_band;
+  s.n_gpoint = (int)e.gpoints_host.size();
+  s.n_species = d->n_absorb;
+  s.n_deg_fit = d->n_deg_fit;
+  s.nd_band = d->nd_band;
+  s.nd_k_term = d->nd_k_term;
+  s.t_ref_planck = d->t_ref_planck;
+  s.has_solar = d->solar_flux_band != nullptr;
+  s.has_planck = d->thermal_coeff != nullptr;
+  s.has_rayleigh = d->rayleigh_coeff != nullptr;
+  for (int b = 0; b < d->n_band; ++b) s.host_first_g[b] = e.bands_host[b].g_first;
+  s.host_first_g[d->n_band] = s.n_gpoint;
+  // cloud parameter sets
+  std::vector<double> drop, ice;
+  s.n_drop_type = (d->drop_parm_list && d->nd_drop_type > 0) ? d->nd_drop_type : 0;
+  s.n_ice_type = (d->ice_parm_list && d->nd_ice_type > 0) ? d->nd_ice_type : 0;
+  if (s.n_drop_type > 0 && d->nd_cloud_parameter < kPadeParm) {
+    set_msg(msg, msg_len, "droplet parameter sets need %d coefficients", kPadeParm);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  drop.assign((size_t)std::max(1, s.n_drop_type) * d->n_band * kPadeParm, 0.0);
+  ice.assign((size_t)std::max(1, s.n_ice_type) * d->n_band * kPadeParm, 0.0);
+  for (int t = 0; t < s.n_drop_type; ++t)
+    for (int b = 0; b < d->n_band; ++b)
+      for (int c = 0; c < kPadeParm; ++c)
+        drop[((size_t)t * d->n_band + b) * kPadeParm + c] =
+            d->drop_parm_list[(size_t)c + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * t)];
+  for (int t = 0; t < s.n_ice_type; ++t)
+    for (int b = 0; b < d->n_band; ++b)
+      for (int c = 0; c < kPadeParm; ++c)
+        ice[((size_t)t * d->n_band + b) * kPadeParm + c] =
+            d->ice_parm_list[(size_t)c + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * t)];
+  cudaGetDevice(&e.device);
+  if (cudaMalloc(&s.bands, sizeof(BandInfo) * s.n_band) != cudaSuccess ||
+      cudaMalloc(&s.gpoints, sizeof(GPoint) * std::max(1, s.n_gpoint)) != cudaSuccess ||
+      cudaMalloc(&s.drop_parm, sizeof(double) * drop.size()) != cudaSuccess ||
+      cudaMalloc(&s.ice_parm, sizeof(double) * ice.size()) != cudaSuccess) {
+    set_msg(msg, msg_len, "device allocation for spectral tables failed");
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  cudaMemcpy(s.bands, e.bands_host.data(), sizeof(BandInfo) * s.n_band, cudaMemcpyHostToDevice);
+  if (s.n_gpoint > 0)
+    cudaMemcpy(s.gpoints, e.gpoints_host.data(), sizeof(GPoint) * s.n_gpoint, cudaMemcpyHostToDevice);
+  cudaMemcpy(s.drop_parm, drop.data(), sizeof(double) * drop.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(s.ice_parm, ice.data(), sizeof(double) * ice.size(), cudaMemcpyHostToDevice);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) {
+    set_msg(msg, msg_len, "upload of spectral tables failed: %s", cudaGetErrorString(err));
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+void free_spectrum(SpectrumEntry &e) {
+  cudaFree(e.dev.bands);
+  cudaFree(e.dev.gpoints);
+  cudaFree(e.dev.drop_parm);
+  cudaFree(e.dev.ice_parm);
+}
+
+SpectrumEntry *find_spectrum(int h) {
+  std::lock_guard<std::mutex> lk(g_reg_mutex);
+  auto it = g_spectra.find(h);
+  return it == g_spectra.end() ? nullptr : it->second.get();
+}
+
+// ---------------------------------------------------------------------------
+// Tile configuration (set by the tuner; 0 = heuristic).
+std::mutex g_tile_mutex;
+int g_tile[2][3][2] = {};   // [precision][mode][lanes, warps]
+
+TileConfig choose_tile(int precision, int mode, int n_layer) {
+  TileConfig t{};
+  {
+    std::lock_guard<std::mutex> lk(g_tile_mutex);
+    t.lanes_per_solve = g_tile[precision][mode][0];
+    t.warps_per_cta = g_tile[precision][mode][1];
+  }
+  if (t.lanes_per_solve <= 0) {
+    if (precision == SOCGPU_PRECISION_MIXED) t.lanes_per_solve = n_layer <= 144 ? 8 : (n_layer <= 256 ? 16 : 32);
+    else t.lanes_per_solve = n_layer <= 256 ? 16 : 32;
+  }
+  // the chunk must cover the column
+  int maxch = (precision == SOCGPU_PRECISION_MIXED && t.lanes_per_solve == 8) ? 18 : 16;
+  while (t.lanes_per_solve < 32 && t.lanes_per_solve * maxch < n_layer) {
+    t.lanes_per_solve *= 2;
+    maxch = 16;
+  }
+  if (t.warps_per_cta <= 0) t.warps_per_cta = 4;
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Validation (mirrors the checks the reference makes before and during
+// radiance_calc; unsupported options are fatal, never a CPU fallback).
+int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntry *sp, const socgpu_atm *atm,
+             const socgpu_cld *cld, const socgpu_aer *aer, const socgpu_bound *bd, const socgpu_radout *out,
+             char *msg, size_t msg_len) {
+  if (!c || !dm || !atm || !bd || !out) { set_msg(msg, msg_len, "null argument"); return SOCGPU_I_ERR_FATAL; }
+  if (!sp) { set_msg(msg, msg_len, "unknown spectrum handle"); return SOCGPU_I_ERR_EXIST; }
+  if (c->i_angular_integration != SOCGPU_IP_TWO_STREAM) {
+    set_msg(msg, msg_len, "only two-stream angular integration is supported"); return SOCGPU_I_ERR_FATAL; }
+  if (c->isolir != SOCGPU_IP_SOLAR && c->isolir != SOCGPU_IP_INFRA_RED) {
+    set_msg(msg, msg_len, "isolir must be solar or infra-red"); return SOCGPU_I_ERR_FATAL; }
+  if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_RANDOM) {
+    set_msg(msg, msg_len, "only random gas overlap is supported"); return SOCGPU_I_ERR_FATAL; }
+  switch (c->i_2stream) {
+    case SOCGPU_IP_EDDINGTON: case SOCGPU_IP_ELSASSER: case SOCGPU_IP_DISCRETE_ORD: case SOCGPU_IP_PIFM85:
+    case SOCGPU_IP_2S_TEST: case SOCGPU_IP_HEMI_MEAN: case SOCGPU_IP_PIFM80: break;
+    default:
+      if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
+        set_msg(msg, msg_len, "unrecognised or unimplemented two-stream scheme %d", c->i_2stream);
+        return SOCGPU_I_ERR_FATAL;
+      }
+  }
+  if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
+    if (c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
+      set_msg(msg, msg_len, "scattering requires solver_homogen_direct"); return SOCGPU_I_ERR_FATAL; }
+  } else if (c->i_scatter_method == SOCGPU_IP_NO_SCATTER_ABS || c->i_scatter_method == SOCGPU_IP_NO_SCATTER_EXT) {
+    if (c->i_solver != SOCGPU_IP_SOLVER_NO_SCAT) {
+      set_msg(msg, msg_len, "no-scattering methods require solver_no_scat"); return SOCGPU_I_ERR_FATAL; }
+    if (c->isolir == SOCGPU_IP_SOLAR) {
+      set_msg(msg, msg_len, "the solar path requires scattering"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA) {
+      set_msg(msg, msg_len, "McICA requires full scattering on the device path"); return SOCGPU_I_ERR_FATAL; }
+  } else {
+    set_msg(msg, msg_len, "unsupported scattering method %d", c->i_scatter_method); return SOCGPU_I_ERR_FATAL; }
+  if (c->isolir == SOCGPU_IP_SOLAR && c->i_direct_tau != SOCGPU_IP_DIRECT_DELTA_SCALING) {
+    set_msg(msg, msg_len, "only delta-scaled direct optical depths (i_direct_tau=1) are supported");
+    return SOCGPU_I_ERR_FATAL;
+  }
+  if (c->l_rescale && c->n_order_forward < 1) {
+    set_msg(msg, msg_len, "n_order_forward must be positive"); return SOCGPU_I_ERR_FATAL; }
+  if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA) {
+    set_msg(msg, msg_len, "only clear-sky and McICA cloud schemes are supported"); return SOCGPU_I_ERR_FATAL; }
+  if (c->precision != SOCGPU_PRECISION_FP64 && c->precision != SOCGPU_PRECISION_MIXED) {
+    set_msg(msg, msg_len, "unknown precision %d", c->precision); return SOCGPU_I_ERR_FATAL; }
+  if (c->first_band < 1 || c->last_band > sp->dev.n_band || c->first_band > c->last_band) {
+    set_msg(msg, msg_len, "band range %d..%d outside the spectrum's 1..%d", c->first_band, c->last_band, sp->dev.n_band);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  if (atm->n_profile < 0 || atm->n_profile > dm->nd_profile) {
+    set_msg(msg, msg_len, "n_profile %d exceeds nd_profile %d", atm->n_profile, dm->nd_profile); return SOCGPU_I_ERR_RANGE; }
+  if (atm->n_layer < 1 || atm->n_layer > dm->nd_layer || atm->n_layer > SOCGPU_MAX_LAYER) {
+    set_msg(msg, msg_len, "n_layer %d outside 1..min(nd_layer=%d, %d)", atm->n_layer, dm->nd_layer, SOCGPU_MAX_LAYER);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  if (c->isolir == SOCGPU_IP_INFRA_RED && !sp->dev.has_planck) {
+    set_msg(msg, msg_len, "infra-red calculation without Planck data"); return SOCGPU_I_ERR_FATAL; }
+  if (c->isolir == SOCGPU_IP_SOLAR && !sp->dev.has_solar) {
+    set_msg(msg, msg_len, "solar calculation without solar spectrum"); return SOCGPU_I_ERR_FATAL; }
+  if (c->l_rayleigh && !sp->dev.has_rayleigh) {
+    set_msg(msg, msg_len, "Rayleigh scattering requested without Rayleigh coefficients"); return SOCGPU_I_ERR_FATAL; }
+  if (c->isolir == SOCGPU_IP_SOLAR && (!bd->zen_0 || !bd->solar_irrad)) {
+    set_msg(msg, msg_len, "solar calculation without zen_0/solar_irrad"); return SOCGPU_I_ERR_FATAL; }
+  if (c->isolir == SOCGPU_IP_INFRA_RED && !bd->t_ground) {
+    set_msg(msg, msg_len, "infra-red calculation without t_ground"); return SOCGPU_I_ERR_FATAL; }
+  if (!bd->rho_alb || !atm->p || !atm->t || !atm->t_level || !atm->mass || (c->l_gas && !atm->gas_mix_ratio)) {
+    set_msg(msg, msg_len, "missing atmospheric or surface field"); return SOCGPU_I_ERR_FATAL; }
+  if (!out->flux_up || !out->flux_down) { set_msg(msg, msg_len, "missing output arrays"); return SOCGPU_I_ERR_FATAL; }
+  if (out->flux_up_band || out->flux_down_band) {
+    set_msg(msg, msg_len, "per-band flux diagnostics are not supported on the device path"); return SOCGPU_I_ERR_FATAL; }
+  if (c->l_aerosol_mode && aer && aer->n_mode > 0) {
+    if (aer->n_mode > SOCGPU_MAX_MODE || aer->n_mode > dm->nd_aerosol_mode) {
+      set_msg(msg, msg_len, "aerosol modes %d exceed limits", aer->n_mode); return SOCGPU_I_ERR_RANGE; }
+    if (!aer->mode_mix_ratio || !aer->mode_absorption || !aer->mode_scattering || !aer->mode_asymmetry) {
+      set_msg(msg, msg_len, "missing aerosol mode fields"); return SOCGPU_I_ERR_FATAL; }
+  }
+  if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA) {
+    if (!cld) { set_msg(msg, msg_len, "McICA requires cloud fields"); return SOCGPU_I_ERR_FATAL; }
+    if (cld->n_condensed < 1 || cld->n_condensed > kMaxCloudComp || cld->n_cloud_type < 1 || cld->n_cloud_type > 2) {
+      set_msg(msg, msg_len, "cloud components/types outside the supported range"); return SOCGPU_I_ERR_RANGE; }
+    if (dm->id_cloud_top < 1 || dm->id_cloud_top > atm->n_layer) {
+      set_msg(msg, msg_len, "id_cloud_top outside the column"); return SOCGPU_I_ERR_RANGE; }
+    if (cld->n_subcol_gen < 1 || cld->n_subcol_gen > SOCGPU_MAX_SUBCOL || cld->n_subcol_req < 1) {
+      set_msg(msg, msg_len, "subcolumn counts outside 1..%d", SOCGPU_MAX_SUBCOL); return SOCGPU_I_ERR_RANGE; }
+    for (int k = 0; k < cld->n_condensed; ++k) {
+      int ph = cld->type_condensed[k], parm = cld->i_condensed_param[k], ty = cld->i_condensed_type[k];
+      if (ph == SOCGPU_IP_PHASE_WATER) {
+        if (parm != SOCGPU_IP_DROP_PADE_2 || ty < 1 || ty > sp->dev.n_drop_type) {
+          set_msg(msg, msg_len, "droplet parametrization %d (type %d) unsupported", parm, ty); return SOCGPU_I_ERR_FATAL; }
+      } else if (ph == SOCGPU_IP_PHASE_ICE) {
+        if (parm != SOCGPU_IP_ICE_PADE_2_PHF || ty < 1 || ty > sp->dev.n_ice_type) {
+          set_msg(msg, msg_len, "ice parametrization %d (type %d) unsupported", parm, ty); return SOCGPU_I_ERR_FATAL; }
+      } else {
+        set_msg(msg, msg_len, "unknown condensed phase %d", ph); return SOCGPU_I_ERR_FATAL; }
+      if (cld->i_cloud_type[k] < 1 || cld->i_cloud_type[k] > cld->n_cloud_type) {
+        set_msg(msg, msg_len, "component cloud type out of range"); return SOCGPU_I_ERR_RANGE; }
+    }
+    if (c->l_rescale && c->n_order_forward != 2) {
+      set_msg(msg, msg_len, "McICA cloud optics need n_order_forward=2 (the Pade path)"); return SOCGPU_I_ERR_FATAL; }
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+// Fill FluxParams from device pointers.
+void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntry *sp,
+                 const socgpu_atm *atm, const socgpu_cld *cld, const socgpu_aer *aer, const socgpu_bound *bd,
+                 socgpu_radout *out, const double *weight_band_dev) {
+  std::memset(&p, 0, sizeof(p));
+  p.isolir = c->isolir; p.i_2stream = c->i_2stream; p.i_scatter_method = c->i_scatter_method;
+  p.i_direct_tau = c->i_direct_tau; p.l_rescale = c->l_rescale; p.n_order_forward = c->n_order_forward;
+  p.l_ir_source_quad = c->l_ir_source_quad; p.l_rayleigh = c->l_rayleigh; p.l_gas = c->l_gas;
+  p.l_aerosol_mode = c->l_aerosol_mode && aer && aer->n_mode > 0; p.l_flux_div = c->l_flux_div;
+  p.first_band = c->first_band; p.last_band = c->last_band;
+  p.mcica = c->i_cloud == SOCGPU_IP_CLOUD_MCICA;
+  p.n_profile = atm->n_profile; p.n_layer = atm->n_layer;
+  p.nd_profile = dm->nd_profile; p.nd_layer = dm->nd_layer;
+  p.id_ct = (p.mcica ? dm->id_cloud_top : 1) - 1;
+  p.g_begin = sp->dev.host_first_g[c->first_band - 1];
+  p.g_end = sp->dev.host_first_g[c->last_band];
+  p.max_abs = 1;
+  for (int b = c->first_band - 1; b < c->last_band; ++b)
+    p.max_abs = std::max(p.max_abs, c->l_gas ? sp->bands_host[b].n_abs : 0);
+  p.bands = sp->dev.bands; p.gpoints = sp->dev.gpoints;
+  p.drop_parm = sp->dev.drop_parm; p.ice_parm = sp->dev.ice_parm;
+  p.n_band = sp->dev.n_band; p.n_deg_fit = sp->dev.n_deg_fit; p.t_ref_planck = sp->dev.t_ref_planck;
+  p.weight_band = weight_band_dev;
+  p.p = atm->p; p.t = atm->t; p.t_level = atm->t_level; p.mass = atm->mass; p.gas_mix_ratio = atm->gas_mix_ratio;
+  p.nd_species = sp->dev.n_species;
+  p.zen_0 = bd->zen_0; p.solar_irrad = bd->solar_irrad; p.rho_alb = bd->rho_alb; p.t_ground = bd->t_ground;
+  if (p.l_aerosol_mode) {
+    p.n_mode = aer->n_mode; p.nd_mode = dm->nd_aerosol_mode;
+    p.mode_mix_ratio = aer->mode_mix_ratio; p.mode_absorption = aer->mode_absorption;
+    p.mode_scattering = aer->mode_scattering; p.mode_asymmetry = aer->mode_asymmetry;
+  }
+  if (p.mcica) {
+    p.n_condensed = cld->n_condensed; p.n_cloud_type = cld->n_cloud_type;
+    for (int k = 0; k < cld->n_condensed; ++k) {
+      p.comp_type[k] = cld->i_cloud_type[k];
+      p.comp_phase[k] = cld->type_condensed[k];
+      p.comp_parm_index[k] = cld->i_condensed_type[k] - 1;
+    }
+    p.condensed_mix_ratio = cld->condensed_mix_ratio; p.condensed_dim_char = cld->condensed_dim_char;
+    p.w_cloud = cld->w_cloud; p.frac_cloud = cld->frac_cloud; p.c_sub = cld->c_sub;
+    p.frac_cloudy = cld->frac_cloudy; p.n_subcol_cld = cld->n_subcol_cld;
+    p.subcol_k = cld->subcol_k; p.first_subcol_k = cld->first_subcol_k; p.subcol_reorder = cld->subcol_reorder;
+    p.n_subcol_gen = cld->n_subcol_gen; p.n_subcol_req = cld->n_subcol_req; p.nd_band_sp = sp->dev.nd_band;
+  }
+  p.flux_up = out->flux_up; p.flux_down = out->flux_down;
+  p.flux_direct = c->isolir == SOCGPU_IP_SOLAR ? out->flux_direct : nullptr;
+  p.flux_div = out->flux_div; p.heating_rate = out->heating_rate;
+}
+
+int mode_index(const socgpu_control *c) {
+  if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA) return 2;
+  return c->i_scatter_method == SOCGPU_IP_SCATTER_FULL ? 1 : 0;
+}
+
+int launch(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *msg, size_t msg_len) {
+  const int mode = mode_index(c);
+  TileConfig t = choose_tile(c->precision, mode, p.n_layer);
+  if (c->precision == SOCGPU_PRECISION_FP64) {
+    if (mode == 0) return launch_flux_fp64_lwns(p, t, st, msg, msg_len);
+    if (mode == 1) return launch_flux_fp64_full(p, t, st, msg, msg_len);
+    return launch_flux_fp64_mcica(p, t, st, msg, msg_len);
+  }
+  if (mode == 0) return launch_flux_mixed_lwns(p, t, st, msg, msg_len);
+  if (mode == 1) return launch_flux_mixed_full(p, t, st, msg, msg_len);
+  return launch_flux_mixed_mcica(p, t, st, msg, msg_len);
+}
+
+// ---------------------------------------------------------------------------
+// Per-thread device workspace for the host-pointer entry points.
+struct Workspace {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  void *buf = nullptr;
+  size_t cap = 0;
+  int *range = nullptr;
+  ~Workspace() {
+    if (buf) cudaFree(buf);
+    if (range) cudaFree(range);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+thread_local Workspace tl_ws;
+
+int ensure_workspace(size_t bytes, char *msg, size_t msg_len) {
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (tl_ws.device != dev) {
+    if (tl_ws.buf) cudaFree(tl_ws.buf);
+    if (tl_ws.range) cudaFree(tl_ws.range);
+    tl_ws.buf = nullptr; tl_ws.cap = 0; tl_ws.range = nullptr;
+    if (tl_ws.stream) cudaStreamDestroy(tl_ws.stream);
+    tl_ws.stream = nullptr;
+    CUDA_TRY(cudaStreamCreateWithFlags(&tl_ws.stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaMalloc(&tl_ws.range, 2 * sizeof(int)));
+    tl_ws.device = dev;
+  }
+  if (bytes > tl_ws.cap) {
+    if (tl_ws.buf) CUDA_TRY(cudaFree(tl_ws.buf));
+    tl_ws.buf = nullptr;
+    size_t want = bytes + bytes / 4;
+    CUDA_TRY(cudaMalloc(&tl_ws.buf, want));
+    tl_ws.cap = want;
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+// A plan of device copies: each host array gets a 256-byte aligned slot.
+struct Slot {
+  const void *host;
+  void *out_host;
+  size_t off, rows, row_bytes, host_pitch, dev_pitch;
+  bool output;
+};
+
+struct Plan {
+  std::vector<Slot> slots;
+  size_t bytes = 0;
+  // Add an array of `rows` rows of `n_valid` elements each, with leading
+  // (Fortran) extent nd in host memory; on the device the same extent is kept.
+  size_t add(const void *host, size_t esize, size_t nd, size_t n_valid, size_t rows, bool output = false,
+             void *out_host = nullptr) {
+    if (!host && !out_host) return (size_t)-1;
+    size_t off = (bytes + 255) & ~(size_t)255;
+    Slot s{host, out_host, off, rows, n_valid * esize, nd * esize, nd * esize, output};
+    slots.push_back(s);
+    bytes = off + nd * esize * rows;
+    return off;
+  }
+};
+
+}  // namespace
+}  // namespace socgpu
+
+using namespace socgpu;
+
+extern "C" {
+
+int socgpu_abi_version(void) { return SOCGPU_ABI_VERSION; }
+
+long long socgpu_kernel_launch_count(void) { return g_launches.load(); }
+
+int socgpu_set_device(int device) { return cudaSetDevice(device) == cudaSuccess ? SOCGPU_I_NORMAL : SOCGPU_I_ERR_FATAL; }
+
+int socgpu_set_tile_config(int precision, int mode, int lanes_per_solve, int warps_per_cta) {
+  if (precision < 0 || precision > 1 || mode < 0 || mode > 2) return SOCGPU_I_ERR_RANGE;
+  if (lanes_per_solve != 0 && lanes_per_solve != 8 && lanes_per_solve != 16 && lanes_per_solve != 32)
+    return SOCGPU_I_ERR_RANGE;
+  if (precision == SOCGPU_PRECISION_FP64 && lanes_per_solve == 8) return SOCGPU_I_ERR_RANGE;
+  if (warps_per_cta < 0 || warps_per_cta > 8) return SOCGPU_I_ERR_RANGE;
+  std::lock_guard<std::mutex> lk(g_tile_mutex);
+  g_tile[precision][mode][0] = lanes_per_solve;
+  g_tile[precision][mode][1] = warps_per_cta;
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_spectrum_register(const char *name, const socgpu_spectrum_desc *desc, socgpu_spectrum_handle *handle,
+                             char *msg, size_t msg_len) {
+  if (!name || !desc || !handle) { set_msg(msg, msg_len, "null argument"); return SOCGPU_I_ERR_FATAL; }
+  {
+    std::lock_guard<std::mutex> lk(g_reg_mutex);
+    auto it = g_names.find(name);
+    if (it != g_names.end()) { *handle = it->second; return SOCGPU_I_NORMAL; }
+  }
+  auto e = std::make_unique<SpectrumEntry>();
+  e->name = name;
+  int st = build_spectrum(desc, *e, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) { free_spectrum(*e); return st; }
+  std::lock_guard<std::mutex> lk(g_reg_mutex);
+  auto it = g_names.find(name);
+  if (it != g_names.end()) { free_spectrum(*e); *handle = it->second; return SOCGPU_I_NORMAL; }
+  int h = g_next_handle++;
+  g_names[name] = h;
+  g_spectra[h] = std::move(e);
+  *handle = h;
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_spectrum_lookup(const char *name, socgpu_spectrum_handle *handle) {
+  if (!name || !handle) return SOCGPU_I_ERR_FATAL;
+  std::lock_guard<std::mutex> lk(g_reg_mutex);
+  auto it = g_names.find(name);
+  if (it == g_names.end()) return SOCGPU_I_ERR_EXIST;
+  *handle = it->second;
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_spectrum_n_gpoint(socgpu_spectrum_handle handle) {
+  SpectrumEntry *e = find_spectrum(handle);
+  return e ? e->dev.n_gpoint : -1;
+}
+
+int socgpu_spectrum_release(socgpu_spectrum_handle handle) {
+  std::unique_ptr<SpectrumEntry> e;
+  {
+    std::lock_guard<std::mutex> lk(g_reg_mutex);
+    auto it = g_spectra.find(handle);
+    if (it == g_spectra.end()) return SOCGPU_I_ERR_EXIST;
+    e = std::move(it->second);
+    g_spectra.erase(it);
+    g_names.erase(e->name);
+  }
+  cudaDeviceSynchronize();
+  free_spectrum(*e);
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_radiance_calc_device(const socgpu_control *control, const socgpu_dimen *dimen,
+                                socgpu_spectrum_handle spectrum, const socgpu_atm *atm, const socgpu_cld *cld,
+                                const socgpu_aer *aer, const socgpu_bound *bound, socgpu_radout *radout,
+                                void *stream, char *msg, size_t msg_len) {
+  SpectrumEntry *sp = find_spectrum(spectrum);
+  int st = validate(control, dimen, sp, atm, cld, aer, bound, radout, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  FluxParams p;
+  fill_params(p, control, dimen, sp, atm, cld, aer, bound, radout, control->weight_band);
+  return launch(p, control, (cudaStream_t)stream, msg, msg_len);
+}
+
+int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dimen, socgpu_spectrum_handle spectrum,
+                         const socgpu_atm *atm, const socgpu_cld *cld, const socgpu_aer *aer,
+                         const socgpu_bound *bound, socgpu_radout *radout, char *msg, size_t msg_len) {
+  SpectrumEntry *sp = find_spectrum(spectrum);
+  int st = validate(control, dimen, sp, atm, cld, aer, bound, radout, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  const size_t ndp = dimen->nd_profile, ndl = dimen->nd_layer, np = atm->n_profile, nl = atm->n_layer;
+  const size_t nb = sp->dev.n_band, ns = std::max(1, sp->dev.n_species);
+  const bool sw = control->isolir == SOCGPU_IP_SOLAR;
+  const bool mc = control->i_cloud == SOCGPU_IP_CLOUD_MCICA;
+  const bool aero = control->l_aerosol_mode && aer && aer->n_mode > 0;
+  Plan plan;
+  const size_t D = sizeof(double);
+  // inputs: (nd_profile, rows) arrays copied with their valid profiles only
+  size_t o_p = plan.add(atm->p, D, ndp, np, nl);
+  size_t o_t = plan.add(atm->t, D, ndp, np, nl);
+  size_t o_tl = plan.add(atm->t_level, D, ndp, np, nl + 1);
+  size_t o_m = plan.add(atm->mass, D, ndp, np, nl);
+  size_t o_g = control->l_gas ? plan.add(atm->gas_mix_ratio, D, ndp, np, ndl * ns) : (size_t)-1;
+  size_t o_z = sw ? plan.add(bound->zen_0, D, ndp, np, 1) : (size_t)-1;
+  size_t o_si = sw ? plan.add(bound->solar_irrad, D, ndp, np, 1) : (size_t)-1;
+  size_t o_alb = plan.add(bound->rho_alb, D, ndp, np, 2 * nb);
+  size_t o_tg = !sw ? plan.add(bound->t_ground, D, ndp, np, 1) : (size_t)-1;
+  size_t o_amr = (size_t)-1, o_aab = (size_t)-1, o_asc = (size_t)-1, o_aas = (size_t)-1;
+  const size_t ndm = dimen->nd_aerosol_mode;
+  if (aero) {
+    o_amr = plan.add(aer->mode_mix_ratio, D, ndp, np, ndl * ndm);
+    o_aab = plan.add(aer->mode_absorption, D, ndp, np, ndl * ndm * nb);
+    o_asc = plan.add(aer->mode_scattering, D, ndp, np, ndl * ndm * nb);
+    o_aas = plan.add(aer->mode_asymmetry, D, ndp, np, ndl * ndm * nb);
+  }
+  size_t o_wb = control->weight_band ? plan.add(control->weight_band, D, nb, nb, 1) : (size_t)-1;
+  size_t o_cmr = (size_t)-1, o_cdc = (size_t)-1, o_wc = (size_t)-1, o_fc = (size_t)-1, o_cs = (size_t)-1;
+  size_t o_fcl = (size_t)-1, o_nsc = (size_t)-1, o_sk = (size_t)-1, o_fsk = (size_t)-1, o_sro = (size_t)-1;
+  if (mc) {
+    const size_t ndc = ndl - (dimen->id_cloud_top - 1);
+    const size_t ncc = std::max(1, dimen->nd_cloud_component), nct = std::max(1, dimen->nd_cloud_type);
+    o_cmr = plan.add(cld->condensed_mix_ratio, D, ndp, np, ndc * ncc);
+    o_cdc = plan.add(cld->condensed_dim_char, D, ndp, np, ndc * ncc);
+    o_wc = plan.add(cld->w_cloud, D, ndp, np, ndc);
+    o_fc = plan.add(cld->frac_cloud, D, ndp, np, ndc * nct);
+    o_cs = plan.add(cld->c_sub, D, ndp, np, ndc * cld->n_subcol_gen);
+    o_fcl = plan.add(cld->frac_cloudy, D, ndp, np, 1);
+    if (cld->n_subcol_cld) o_nsc = plan.add(cld->n_subcol_cld, sizeof(int), ndp, np, 1);
+    const size_t ndb = sp->dev.nd_band, ndk = sp->dev.nd_k_term;
+    o_sk = plan.add(cld->subcol_k, sizeof(int), ndb * ndk, ndb * ndk, 1);
+    o_fsk = plan.add(cld->first_subcol_k, sizeof(int), ndb * (ndk + 1), ndb * (ndk + 1), 1);
+    o_sro = plan.add(cld->subcol_reorder, sizeof(int), cld->n_subcol_req, cld->n_subcol_req, 1);
+  }
+  const size_t n_inputs = plan.slots.size();
+  // outputs
+  size_t o_fu = plan.add(nullptr, D, ndp, np, nl + 1, true, radout->flux_up);
+  size_t o_fd = plan.add(nullptr, D, ndp, np, nl + 1, true, radout->flux_down);
+  size_t o_fdir = (sw && radout->flux_direct) ? plan.add(nullptr, D, ndp, np, nl + 1, true, radout->flux_direct) : (size_t)-1;
+  size_t o_div = radout->flux_div ? plan.add(nullptr, D, ndp, np, nl, true, radout->flux_div) : (size_t)-1;
+  size_t o_hr = radout->heating_rate ? plan.add(nullptr, D, ndp, np, nl, true, radout->heating_rate) : (size_t)-1;
+
+  st = ensure_workspace(plan.bytes, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  char *base = (char *)tl_ws.buf;
+  cudaStream_t s = tl_ws.stream;
+  for (size_t k = 0; k < n_inputs; ++k) {
+    const Slot &sl = plan.slots[k];
+    if (sl.row_bytes == 0) continue;
+    CUDA_TRY(cudaMemcpy2DAsync(base + sl.off, sl.dev_pitch, sl.host, sl.host_pitch, sl.row_bytes, sl.rows,
+                               cudaMemcpyHostToDevice, s));
+  }
+  auto dptr = [&](size_t off) -> void * { return off == (size_t)-1 ? nullptr : (void *)(base + off); };
+  socgpu_atm a2 = *atm;
+  a2.p = (const double *)dptr(o_p); a2.t = (const double *)dptr(o_t); a2.t_level = (const double *)dptr(o_tl);
+  a2.mass = (const double *)dptr(o_m); a2.gas_mix_ratio = (const double *)dptr(o_g); a2.p_level = nullptr;
+  socgpu_bound b2 = *bound;
+  b2.zen_0 = (const double *)dptr(o_z); b2.solar_irrad = (const double *)dptr(o_si);
+  b2.rho_alb = (const double *)dptr(o_alb); b2.t_ground = (const double *)dptr(o_tg);
+  socgpu_aer e2{};
+  if (aero) {
+    e2 = *aer;
+    e2.mode_mix_ratio = (const double *)dptr(o_amr); e2.mode_absorption = (const double *)dptr(o_aab);
+    e2.mode_scattering = (const double *)dptr(o_asc); e2.mode_asymmetry = (const double *)dptr(o_aas);
+  }
+  socgpu_cld c2{};
+  if (mc) {
+    c2 = *cld;
+    c2.condensed_mix_ratio = (const double *)dptr(o_cmr); c2.condensed_dim_char = (const double *)dptr(o_cdc);
+    c2.w_cloud = (const double *)dptr(o_wc); c2.frac_cloud = (const double *)dptr(o_fc);
+    c2.c_sub = (const double *)dptr(o_cs); c2.frac_cloudy = (const double *)dptr(o_fcl);
+    c2.n_subcol_cld = (const int *)dptr(o_nsc);
+    c2.subcol_k = (const int *)dptr(o_sk); c2.first_subcol_k = (const int *)dptr(o_fsk);
+    c2.subcol_reorder = (const int *)dptr(o_sro);
+  }
+  socgpu_radout r2{};
+  r2.flux_up = (double *)dptr(o_fu); r2.flux_down = (double *)dptr(o_fd);
+  r2.flux_direct = (double *)dptr(o_fdir); r2.flux_div = (double *)dptr(o_div);
+  r2.heating_rate = (double *)dptr(o_hr);
+  FluxParams p;
+  fill_params(p, control, dimen, sp, &a2, mc ? &c2 : nullptr, aero ? &e2 : nullptr, &b2, &r2,
+              (const double *)dptr(o_wb));
+  st = launch(p, control, s, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) { cudaStreamSynchronize(s); return st; }
+  for (size_t k = n_inputs; k < plan.slots.size(); ++k) {
+    const Slot &sl = plan.slots[k];
+    if (sl.row_bytes == 0) continue;
+    CUDA_TRY(cudaMemcpy2DAsync(sl.out_host, sl.host_pitch, base + sl.off, sl.dev_pitch, sl.row_bytes, sl.rows,
+                               cudaMemcpyDeviceToHost, s));
+  }
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_cloud_gen_device(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2, int n_subcol,
+                            int n1, int n2, int ipph, int ioverlap, const int *rand_seed, const double *rlc_cf,
+                            const double *rlc_cw, const double *sigma_qcw, const double *avg_cf,
+                            const double *c_cloud, const double *c_ratio, const double *zf, const double *xcw,
+                            int *n_subcol_cld, double *c_sub, int rng, void *stream, char *msg, size_t msg_len) {
+  if (ioverlap < 0 || ioverlap > 3) {
+    set_msg(msg, msg_len, "Choice of overlap not compatible with cloud generator");
+    return SOCGPU_I_ERR_FATAL;
+  }
+  if (rng != SOCGPU_RNG_LCG && rng != SOCGPU_RNG_PHILOX) { set_msg(msg, msg_len, "unknown rng %d", rng); return SOCGPU_I_ERR_FATAL; }
+  if (cloud_top < 1 || n_layer > nd_layer || il1 < 1 || il2 > nd_profile || n_subcol < 1) {
+    set_msg(msg, msg_len, "cloud_gen dimensions out of range"); return SOCGPU_I_ERR_RANGE; }
+  if (ipph != 0 && (!xcw || !sigma_qcw || n1 < 2 || n2 < 2)) {
+    set_msg(msg, msg_len, "ipph needs the xcw table and sigma_qcw"); return SOCGPU_I_ERR_FATAL; }
+  if (!rand_seed || !rlc_cf || !rlc_cw || !avg_cf || !zf || !n_subcol_cld || !c_sub) {
+    set_msg(msg, msg_len, "missing cloud_gen argument"); return SOCGPU_I_ERR_FATAL; }
+  int st = ensure_workspace(1, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  return launch_cloud_gen(nd_layer, cloud_top, n_layer, nd_profile, il1, il2, n_subcol, n1, n2, ipph, ioverlap,
+                          rand_seed, rlc_cf, rlc_cw, sigma_qcw, avg_cf, c_cloud, c_ratio, zf, xcw, n_subcol_cld,
+                          c_sub, rng, tl_ws.range, (cudaStream_t)stream, msg, msg_len);
+}
+
+int socgpu_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2, int n_subcol,
+                     int n1, int n2, int ipph, int ioverlap, const int *rand_seed, const double *rlc_cf,
+                     const double *rlc_cw, const double *sigma_qcw, const double *avg_cf, const double *c_cloud,
+                     const double *c_ratio, const double *zf, const double *xcw, int *n_subcol_cld, double *c_sub,
+                     int rng, char *msg, size_t msg_len) {
+  if (cloud_top < 1 || n_layer > nd_layer || il1 < 1 || il2 > nd_profile || n_subcol < 1 || ioverlap < 0 || ioverlap > 3) {
+    set_msg(msg, msg_len, "cloud_gen arguments out of range"); return SOCGPU_I_ERR_RANGE; }
+  const size_t ndp = nd_profile, ndc = nd_layer - cloud_top + 1, D = sizeof(double);
+  Plan plan;
+  size_t o_seed = plan.add(rand_seed, sizeof(int), ndp, ndp, 1);
+  size_t o_cf = plan.add(rlc_cf, D, ndp, ndp, ndc);
+  size_t o_cw = plan.add(rlc_cw, D, ndp, ndp, ndc);
+  size_t o_sq = sigma_qcw ? plan.add(sigma_qcw, D, ndp, ndp, ndc) : (size_t)-1;
+  size_t o_av = plan.add(avg_cf, D, ndp, ndp, ndc);
+  size_t o_cc = c_cloud ? plan.add(c_cloud, D, ndp, ndp, ndc) : (size_t)-1;
+  size_t o_cr = c_ratio ? plan.add(c_ratio, D, ndp, ndp, ndc) : (size_t)-1;
+  size_t o_zf = plan.add(zf, D, ndp, ndp, nd_layer);
+  size_t o_x = (xcw && ipph != 0) ? plan.add(xcw, D, (size_t)n1, (size_t)n1, (size_t)n2) : (size_t)-1;
+  const size_t n_inputs = plan.slots.size();
+  size_t o_n = plan.add(nullptr, sizeof(int), ndp, ndp, 1, true, n_subcol_cld);
+  size_t o_cs = plan.add(nullptr, D, ndp, ndp, ndc * n_subcol, true, c_sub);
+  int st = ensure_workspace(plan.bytes, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  char *base = (char *)tl_ws.buf;
+  cudaStream_t s = tl_ws.stream;
+  for (size_t k = 0; k < n_inputs; ++k) {
+    const Slot &sl = plan.slots[k];
+    CUDA_TRY(cudaMemcpy2DAsync(base + sl.off, sl.dev_pitch, sl.host, sl.host_pitch, sl.row_bytes, sl.rows,
+                               cudaMemcpyHostToDevice, s));
+  }
+  auto dptr = [&](size_t off) -> void * { return off == (size_t)-1 ? nullptr : (void *)(base + off); };
+  st = socgpu_cloud_gen_device(nd_layer, cloud_top, n_layer, nd_profile, il1, il2, n_subcol, n1, n2, ipph, ioverlap,
+                               (const int *)dptr(o_seed), (const double *)dptr(o_cf), (const double *)dptr(o_cw),
+                               (const double *)dptr(o_sq),
+                               (const double *)dptr(o_av),
+                               (const double *)(o_cc == (size_t)-1 ? nullptr : dptr(o_cc)),
+                               (const double *)(o_cr == (size_t)-1 ? nullptr : dptr(o_cr)),
+                               (const double *)dptr(o_zf), (const double *)dptr(o_x), (int *)dptr(o_n),
+                               (double *)dptr(o_cs), rng, s, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) { cudaStreamSynchronize(s); return st; }
+  for (size_t k = n_inputs; k < plan.slots.size(); ++k) {
+    const Slot &sl = plan.slots[k];
+    CUDA_TRY(cudaMemcpy2DAsync(sl.out_host, sl.host_pitch, base + sl.off, sl.dev_pitch, sl.row_bytes, sl.rows,
+                               cudaMemcpyDeviceToHost, s));
+  }
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return SOCGPU_I_NORMAL;
+}
+
+}  // extern "C"

@@ -1,0 +1,73 @@
+// flux_launch.cuh -- dispatch of the templated flux kernel over the tile
+// shapes (lanes per solve P, layers per lane CH) it is instantiated for.
+#pragma once
+
+#include <cstdio>
+#include "flux_kernel.cuh"
+
+namespace socgpu {
+
+template <int P_, int CH_>
+struct Shape { static constexpr int P = P_, CH = CH_; };
+
+template <class R, bool MIX, bool NOSCAT, bool MCICA, class S>
+int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len,
+               bool &done) {
+  if (done || cfg.lanes_per_solve != S::P || S::P * S::CH < p.n_layer) return 0;
+  // the smallest chunk of this P that covers the column is chosen by the
+  // caller's ordering of shapes (ascending CH)
+  done = true;
+  const int threads = cfg.warps_per_cta * 32;
+  const int n_groups = threads / S::P;
+  int nb = p.last_band - p.first_band + 1;
+  SmemLayout lay = make_layout<R, R>(p.n_layer, nb, p.max_abs, MCICA ? p.n_condensed : 0,
+                                     MCICA ? p.n_subcol_gen : 0, n_groups,
+                                     p.isolir == SOCGPU_IP_INFRA_RED, MCICA);
+  auto kern = flux_kernel<R, MIX, S::P, S::CH, NOSCAT, MCICA>;
+  if (lay.bytes > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.bytes);
+    if (e != cudaSuccess) {
+      snprintf(msg, len, "shared memory request of %zu bytes refused: %s", lay.bytes, cudaGetErrorString(e));
+      return SOCGPU_I_ERR_RANGE;
+    }
+  }
+  if (p.n_profile <= 0) return 0;
+  kern<<<p.n_profile, threads, lay.bytes, st>>>(p);
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(msg, len, "flux kernel launch failed: %s", cudaGetErrorString(e));
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  return 0;
+}
+
+template <class R, bool MIX, bool NOSCAT, bool MCICA, class... Shapes>
+int launch_shapes(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len) {
+  bool done = false;
+  int status = 0;
+  ((status = status ? status : try_launch<R, MIX, NOSCAT, MCICA, Shapes>(p, cfg, st, msg, len, done)), ...);
+  if (!done && status == 0) {
+    snprintf(msg, len, "no kernel instantiated for %d lanes per solve and %d layers", cfg.lanes_per_solve,
+             p.n_layer);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  return status;
+}
+
+// Bytes of shared memory one CTA needs (for the occupancy-aware tuner).
+template <class R>
+size_t smem_bytes(const FluxParams &p, int lanes, int warps, bool mcica) {
+  int nb = p.last_band - p.first_band + 1;
+  return make_layout<R, R>(p.n_layer, nb, p.max_abs, mcica ? p.n_condensed : 0, mcica ? p.n_subcol_gen : 0,
+                           warps * 32 / lanes, p.isolir == SOCGPU_IP_INFRA_RED, mcica).bytes;
+}
+
+}  // namespace socgpu
+
+// Shape lists: ascending CH within each P so the first fit is the tightest.
+#define SOCGPU_SHAPES_FP64 \
+  Shape<16, 4>, Shape<16, 8>, Shape<16, 16>, Shape<32, 4>, Shape<32, 8>, Shape<32, 16>
+#define SOCGPU_SHAPES_MIXED                                                                      \
+  Shape<8, 8>, Shape<8, 13>, Shape<8, 18>, Shape<16, 4>, Shape<16, 8>, Shape<16, 16>, Shape<32, 4>, \
+      Shape<32, 8>, Shape<32, 16>

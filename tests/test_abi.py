@@ -1,0 +1,60 @@
+"""CPU checks of the C-ABI library: it builds, loads without a GPU and
+exports every entry point include/socgpu.h declares; host-only argument
+validation answers with the reference's error codes."""
+import ctypes as C
+from pathlib import Path
+
+import pytest
+
+from socrates_gb300 import abi, build
+from socrates_gb300.spectrum import Spectrum
+from socrates_gb300 import synth
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def lib():
+    path = build.build()
+    return abi.declare(C.CDLL(str(path)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = abi.header_functions(ROOT / "include" / "socgpu.h")
+    assert len(names) >= 12
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(abi.ABI_FUNCTIONS)
+
+
+def test_abi_version(lib):
+    assert lib.socgpu_abi_version() == abi.ABI_VERSION
+
+
+def test_tile_config_validation(lib):
+    assert lib.socgpu_set_tile_config(abi.PRECISION_MIXED, 1, 8, 4) == abi.I_NORMAL
+    assert lib.socgpu_set_tile_config(abi.PRECISION_FP64, 1, 8, 4) == abi.I_ERR_RANGE
+    assert lib.socgpu_set_tile_config(abi.PRECISION_MIXED, 3, 8, 4) == abi.I_ERR_RANGE
+    assert lib.socgpu_set_tile_config(abi.PRECISION_MIXED, 1, 12, 4) == abi.I_ERR_RANGE
+    assert lib.socgpu_set_tile_config(abi.PRECISION_MIXED, 1, 0, 0) == abi.I_NORMAL
+
+
+def test_lookup_of_unknown_spectrum(lib):
+    h = C.c_int(0)
+    assert lib.socgpu_spectrum_lookup(b"no-such-spectrum", C.byref(h)) == abi.I_ERR_EXIST
+
+
+def test_spectral_file_round_trip(tmp_path):
+    for sp in (synth.lw_spectrum(1, 9, clouds=True), synth.sw_spectrum(2, 8, clouds=True)):
+        path = tmp_path / "sp"
+        sp.write_text(path)
+        back = Spectrum.read_text(path)
+        assert back.n_band == sp.n_band and back.n_gpoint == sp.n_gpoint
+        for name in ("k", "w", "p_ref", "t_ref", "i_band_k", "i_scale_fnc", "index_absorb"):
+            a, b = getattr(sp, name), getattr(back, name)
+            assert a.shape == b.shape and (abs(a - b) <= 1e-9 * abs(a) + 1e-300).all(), name
+        if sp.thermal_coeff is not None:
+            assert abs(back.thermal_coeff - sp.thermal_coeff).max() <= 1e-8 * abs(sp.thermal_coeff).max()
+        if sp.solar_flux_band is not None:
+            assert abs(back.solar_flux_band - sp.solar_flux_band).max() < 1e-9
+        assert abs(back.drop_parm_list - sp.drop_parm_list).max() <= 1e-9 * abs(sp.drop_parm_list).max()

@@ -1,0 +1,184 @@
+"""GPU parity: the CUDA path through the C-ABI against the FP64 oracle.
+
+Tolerances (written here, per the path's contract):
+  * FP64 device kernels: fluxes within 1e-10 relative of the oracle (scaled
+    by the column's largest flux), heating rates within 1e-9 of the
+    column's largest magnitude;
+  * mixed FP32/FP64 kernels: fluxes within 0.1 W/m2, heating rates within
+    0.05 K/day;
+  * McICA subcolumn masks: bit-exact.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+import oracle as O
+from golden_cases import CASES
+from socrates_gb300 import abi, synth
+from socrates_gb300 import radiance as R
+
+pytestmark = pytest.mark.gpu
+
+FLUX_KEYS = ("flux_up", "flux_down", "flux_direct")
+
+
+def _gpu(ctl, sp, col, mc=None):
+    return {**R.radiance_calc(ctl, sp, col, mc), "mass": col.mass}
+
+
+def _ora(ctl, sp, col, mc=None):
+    return {**O.radiance_calc(ctl, sp, col, mc), "mass": col.mass}
+
+
+def assert_fp64_parity(gpu, ref, tag="", mass=None):
+    """Fluxes within 1e-10 of the column's largest flux.  The flux
+    divergence and heating rate are differences of fluxes, so their
+    tolerance is that flux tolerance carried through their own formulas
+    (two levels; heating rate = 86400 div / (mass cp))."""
+    fscale = max(np.abs(ref[k]).max(axis=1) for k in FLUX_KEYS if k in ref)[:, None] + 1e-300
+    for k in ref:
+        if k == "mass":
+            continue
+        g, r = gpu[k], ref[k]
+        if k in FLUX_KEYS:
+            err = np.abs(g - r) / fscale
+            assert err.max() <= 1e-10, f"{tag}{k}: max scaled error {err.max():.3e}"
+        elif k == "flux_div":
+            err = np.abs(g - r) / (2e-10 * fscale)
+            assert err.max() <= 1.0, f"{tag}{k}: error {err.max():.3e} x tolerance"
+        elif k == "heating_rate":
+            m = ref.get("mass", mass)
+            tol = 2e-10 * fscale * 8.64e4 / (m * 1.005e3)
+            err = np.abs(g - r) / tol
+            assert err.max() <= 1.0, f"{tag}{k}: error {err.max():.3e} x tolerance"
+
+
+def assert_mixed_tolerance(gpu, ref, tag=""):
+    for k in FLUX_KEYS:
+        if k in ref:
+            err = np.abs(gpu[k] - ref[k]).max()
+            assert err <= 0.1, f"{tag}{k}: max error {err:.4f} W/m2"
+    err = np.abs(gpu["heating_rate"] - ref["heating_rate"]).max()
+    assert err <= 0.05, f"{tag}heating_rate: max error {err:.4f} K/day"
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp64_matches_oracle(gpu_lib, name):
+    gpu = CASES[name](_gpu)
+    ref = CASES[name](_ora)
+    assert_fp64_parity(gpu, ref, f"{name}: ")
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp64_matches_golden_fixture(gpu_lib, name):
+    from pathlib import Path
+    data = np.load(Path(__file__).resolve().parent / "golden" / f"{name}.npz")
+    gpu = CASES[name](_gpu)
+    assert_fp64_parity(gpu, {k: data[k] for k in data.files}, f"{name}: ", mass=gpu["mass"])
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_mixed_within_tolerance(gpu_lib, name):
+    gpu = CASES[name](lambda c, s, col, mc=None: _gpu(_with(c, abi.PRECISION_MIXED), s, col, mc))
+    ref = CASES[name](_ora)
+    assert_mixed_tolerance(gpu, ref, f"{name}: ")
+
+
+def test_results_are_deterministic(gpu_lib):
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        a = CASES["sw_pifm80"](lambda c, s, col, mc=None: _gpu(_with(c, prec), s, col, mc))
+        b = CASES["sw_pifm80"](lambda c, s, col, mc=None: _gpu(_with(c, prec), s, col, mc))
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k])
+
+
+def _with(c, prec):
+    from dataclasses import replace
+    return replace(c, precision=prec)
+
+
+@pytest.mark.parametrize("ioverlap", [abi.IP_MAX_RAND, abi.IP_RAND, abi.IP_EXPONENTIAL, abi.IP_EXPONENTIAL_RAND])
+@pytest.mark.parametrize("rng", [abi.RNG_LCG, abi.RNG_PHILOX])
+def test_cloud_gen_masks_bit_exact(gpu_lib, ioverlap, rng):
+    lw, sw, col = synth.config3(512, 85, seed=7, n_subcol=16)
+    g, gn = R.cloud_gen(col, 16, ioverlap, rng)
+    o, on = R.cloud_gen(col, 16, ioverlap, rng, impl=O.cloud_gen_impl)
+    np.testing.assert_array_equal(gn, on)
+    np.testing.assert_array_equal(g, o)
+    assert gn.max() > 0
+
+
+def test_philox_masks_independent_of_batch(gpu_lib):
+    """A column's Philox subcolumns depend only on its own seed and fields."""
+    lw, sw, col = synth.config3(64, 60, seed=8, n_subcol=16)
+    full, nf = R.cloud_gen(col, 16, abi.IP_EXPONENTIAL_RAND, abi.RNG_PHILOX)
+    sub = _subset(col, np.arange(10, 20))
+    part, npart = R.cloud_gen(sub, 16, abi.IP_EXPONENTIAL_RAND, abi.RNG_PHILOX)
+    np.testing.assert_array_equal(part, full[10:20])
+    np.testing.assert_array_equal(npart, nf[10:20])
+
+
+def _subset(col, idx):
+    c = copy.copy(col)
+    c.n_profile = len(idx)
+    for name in ("p", "t", "p_level", "t_level", "mass", "gas_mix_ratio", "z", "t_ground", "zen_0", "solar_irrad",
+                 "rho_alb"):
+        v = getattr(col, name)
+        if v is not None:
+            setattr(c, name, np.asfortranarray(v[idx]))
+    if col.aer:
+        c.aer = {k: (np.asfortranarray(v[idx]) if isinstance(v, np.ndarray) else v) for k, v in col.aer.items()}
+    if col.cld:
+        c.cld = {k: (np.asfortranarray(v[idx]) if isinstance(v, np.ndarray) and v.ndim >= 1 and v.shape[0] == col.n_profile
+                     else v) for k, v in col.cld.items()}
+    return c
+
+
+def test_full_size_shortwave_properties(gpu_lib):
+    """10 000 columns x 100 layers: FP64 device path against the oracle on a
+    sample of columns, mixed path against FP64 everywhere, energy balance."""
+    sp, col = synth.config2(10000, 100, seed=2)
+    ctl = R.sw_control(l_aerosol_mode=True)
+    g64 = R.radiance_calc(ctl, sp, col)
+    gmx = R.radiance_calc(_with(ctl, abi.PRECISION_MIXED), sp, col)
+    idx = np.random.default_rng(0).choice(col.n_profile, 48, replace=False)
+    ref = O.radiance_calc(ctl, sp, _subset(col, idx))
+    assert_fp64_parity({k: v[idx] for k, v in g64.items()}, ref, "sample: ", mass=col.mass[idx])
+    assert_mixed_tolerance(gmx, g64, "mixed vs fp64: ")
+    # energy: TOA incoming = reflected + absorbed in the column + absorbed at the surface
+    toa_in = col.solar_irrad * sp.solar_flux_band.sum() / col.zen_0
+    np.testing.assert_allclose(g64["flux_down"][:, 0], toa_in, rtol=1e-12)
+    absorbed = g64["flux_div"].sum(axis=1)
+    net_toa = g64["flux_down"][:, 0] - g64["flux_up"][:, 0]
+    net_sfc = g64["flux_down"][:, -1] - g64["flux_up"][:, -1]
+    np.testing.assert_allclose(absorbed, net_toa - net_sfc, rtol=1e-8, atol=1e-8)
+
+
+def test_unsupported_options_return_status(gpu_lib):
+    sp, col = synth.config1(4, 20)
+    bad = [
+        (R.lw_control(i_2stream=abi.IP_IFM), abi.I_ERR_FATAL),
+        (R.lw_control(i_solver=abi.IP_SOLVER_NO_SCAT), abi.I_ERR_FATAL),
+        (R.lw_control(first_band=3, last_band=12), abi.I_ERR_RANGE),
+        (R.lw_control(i_gas_overlap=4), abi.I_ERR_FATAL),
+    ]
+    for ctl, status in bad:
+        with pytest.raises(R.RadianceError) as e:
+            R.radiance_calc(ctl, sp, col)
+        assert e.value.status == status
+    # the library still works afterwards
+    out = R.radiance_calc(R.lw_noscat_control(), sp, col)
+    assert np.isfinite(out["flux_up"]).all()
+
+
+def test_band_subrange_matches_oracle(gpu_lib):
+    sp, col = synth.config2(16, 60, seed=5)
+    ctl = R.sw_control(l_aerosol_mode=True, first_band=2, last_band=4)
+    assert_fp64_parity(R.radiance_calc(ctl, sp, col), O.radiance_calc(ctl, sp, col), "bands 2-4: ", mass=col.mass)
+
+
+def test_kernels_launch_on_device(gpu_lib):
+    before = R.launch_count()
+    CASES["lw_noscat"](_gpu)
+    assert R.launch_count() > before
