@@ -1,0 +1,339 @@
+"""Benchmark of the two-stream flux path on one GB300 (or N replicas).
+
+Workload: shortwave PIFM80 two-stream with delta-Eddington rescaling,
+Rayleigh and one aerosol mode, direct + diffuse solve: 10 000 columns x
+100 layers x 48 g-points (6 bands x 8 k-terms), seeded synthetic inputs
+(socrates_gb300.synth.config2).  A step is one radiance_calc pass over
+the batch.  The headline path is the mixed FP32/FP64 kernel; the plain
+FP64 device path, the mixed-vs-FP64 error and the CPU baseline are
+reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "column·g-pts/s mixed vs FP64 at ≤0.1 W/m² flux error; serve p50/p99 ms"
+UNIT = "column·g-points/s"
+N_COL, N_LAYER, SEED = 10000, 100, 2
+CONFIG = {"workload": "SW PIFM80 delta-Eddington direct+diffuse, Rayleigh + modal aerosol, "
+                      "10000 columns x 100 layers, 6 bands x 8 k-terms (48 g-points)",
+          "columns": N_COL, "layers": N_LAYER, "g_points": 48, "precision": "mixed FP32/FP64",
+          "l2": "256 MiB L2 flush between timed steps; inputs (about 200 MB) exceed the 129 MB L2"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="socgpu", choices=["socgpu", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=N_COL, help="columns of the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU work of the baseline sample")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons (read only)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the flux kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "flux_kernel_sw_mixed_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return None
+    return None
+
+
+def cpu_baseline(n_sample: int, min_seconds: float = 10.0):
+    """The FP64 oracle (a C restatement of the reference) on all host cores
+    over a bounded sample of the workload: n_sample columns, repeated until
+    about min_seconds of CPU work have run."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    from socrates_gb300 import radiance as R
+    from socrates_gb300.synth import config2
+    threads = os.cpu_count() or 1
+    sp_s, col_s = config2(n_sample, N_LAYER, SEED)
+    ctl = R.sw_control(l_aerosol_mode=True)
+    O.radiance_calc(ctl, sp_s, config2(threads, N_LAYER, SEED)[1], threads=threads)   # warm-up
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        O.radiance_calc(ctl, sp_s, col_s, threads=threads)
+        reps += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds or reps >= 1000:
+            break
+    return {"value": reps * n_sample * sp_s.n_gpoint / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "seconds": dt, "sample": f"{reps} passes over {n_sample} of the workload's {N_COL} columns (all 100 layers, "
+                                     f"48 g-points), FP64 C restatement with OpenMP over column segments"}
+
+
+def dist_setup(n: int):
+    rank, world = 0, 1
+    if n > 1 or "RANK" in os.environ:
+        import torch.distributed as dist
+        rank = int(os.environ.get("RANK", 0))
+        world = int(os.environ.get("WORLD_SIZE", n))
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    """CPU reference arm: the oracle port on all host cores, same metric."""
+    rank = int(os.environ.get("RANK", 0))
+    if rank != 0:
+        return
+    from socrates_gb300.synth import config2
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    from socrates_gb300 import radiance as R
+    threads = os.cpu_count() or 1
+    n = args.cpu_sample
+    sp, col = config2(n, N_LAYER, SEED)
+    ctl = R.sw_control(l_aerosol_mode=True)
+    for _ in range(args.warmup):
+        O.radiance_calc(ctl, sp, col, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.radiance_calc(ctl, sp, col, threads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = n * sp.n_gpoint / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox, shapes of the workload)",
+            "config": {**CONFIG, "precision": "FP64", "columns": n},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n} of {N_COL} columns per step, all 100 layers and 48 g-points, FP64 C "
+                                       f"restatement of the reference (no Fortran compiler on the box)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+    rank, world = dist_setup(args.gpus)
+    dev = torch.cuda.current_device()
+    from socrates_gb300 import abi
+    from socrates_gb300 import build as B
+    from socrates_gb300 import radiance as R
+    from socrates_gb300.device import DeviceCase
+    from socrates_gb300.synth import config2
+    if rank == 0:
+        B.build()
+    barrier(world)
+    # each rank solves its own batch of columns (weak scaling, no exchange)
+    sp, col = config2(N_COL, N_LAYER, SEED + rank)
+    g = sp.n_gpoint
+    ctl_mx = R.sw_control(l_aerosol_mode=True, precision=abi.PRECISION_MIXED)
+    ctl_64 = R.sw_control(l_aerosol_mode=True, precision=abi.PRECISION_FP64)
+    case = DeviceCase(ctl_mx, sp, col)
+    case64 = DeviceCase(ctl_64, sp, col)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(c, steps, warm):
+        for _ in range(warm):
+            c.run(stream.cuda_stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        l0 = R.launch_count()
+        t0 = time.perf_counter()
+        for e0, e1 in evs:
+            flush.fill_(1.0)                 # evict L2 between steps (outside the events)
+            e0.record(stream)
+            c.run(stream.cuda_stream)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        wall = time.perf_counter() - t0
+        launches = R.launch_count() - l0
+        ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+        return sum(ms) / steps, launches, wall
+
+    with ClockSampler(dev) as clk:
+        ms_mx, launches, wall = timed(case, args.steps, max(3, args.warmup))
+    ms_64, _, _ = timed(case64, max(3, args.steps // 4), 3)
+    ms_mx = max_over_ranks(ms_mx, world)
+    ms_64 = max_over_ranks(ms_64, world)
+    value = world * N_COL * g / (ms_mx * 1e-3)
+    value_64 = world * N_COL * g / (ms_64 * 1e-3)
+
+    # accuracy of the mixed path against the FP64 path on this batch
+    err_flux = max(float(np.abs(case.output(k) - case64.output(k)).max())
+                   for k in ("flux_up", "flux_down", "flux_direct"))
+    err_hr = float(np.abs(case.output("heating_rate") - case64.output("heating_rate")).max())
+
+    # end to end through the public host-pointer API (pinned host buffers)
+    def pinned_copy(a):
+        t = torch.empty(a.size, dtype=torch.float64).pin_memory()
+        v = t.numpy().reshape(a.shape, order="F")
+        v[...] = a
+        return v, t
+    keep = []
+    for name in ("p", "t", "t_level", "mass", "gas_mix_ratio", "zen_0", "solar_irrad", "rho_alb"):
+        v, t = pinned_copy(np.asfortranarray(getattr(col, name)))
+        keep.append(t)
+        setattr(col, name, v)
+    for k in ("mode_mix_ratio", "mode_absorption", "mode_scattering", "mode_asymmetry"):
+        v, t = pinned_copy(np.asfortranarray(col.aer[k]))
+        keep.append(t)
+        col.aer[k] = v
+    import ctypes as C
+    marsh = R.Marshal(ctl_mx, sp, col)
+    for name in ("flux_up", "flux_down", "flux_direct", "flux_div", "heating_rate"):
+        arr = getattr(marsh, name)
+        v, t = pinned_copy(arr)
+        keep.append(t)
+        setattr(marsh, name, v)
+        setattr(marsh.radout, name, v.ctypes.data_as(C.POINTER(C.c_double)))
+    h = R.register_spectrum(sp)
+    lib = R.load_library()
+    msg = C.create_string_buffer(256)
+    for _ in range(3):
+        lib.socgpu_radiance_calc(*marsh.args(h), msg, 256)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = lib.socgpu_radiance_calc(*marsh.args(h), msg, 256)
+        if st != 0:
+            raise SystemExit(f"radiance_calc failed: {msg.value.decode()}")
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    h2d = case.input_bytes - (8 * N_COL)          # t_ground is not read on the solar path
+    d2h = case.output_bytes
+    e2e = {"value": world * N_COL * g / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+           "path": "socgpu_radiance_calc with pinned host arrays (H2D inputs, kernel, D2H outputs)"}
+
+    peak, peak_kind = measured_peak_hbm()
+    alg_bytes = h2d + d2h
+    achieved = alg_bytes / (ms_mx * 1e-3) / 1e9
+    traffic = profile_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "algorithmic_bytes_per_launch": int(alg_bytes),
+                "note": "compulsory FP64 I/O of the batch over the mixed kernel's time; the fused kernel is bound "
+                        "by FP32/MUFU issue, not HBM"}
+    if rank == 0:
+        cpu = cpu_baseline(args.cpu_sample, args.cpu_seconds)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": max(3, args.warmup), "ms_per_step": ms_mx, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded Philox inputs with the workload's shapes and distributions)",
+                "config": CONFIG, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "fp64_device": {"value": value_64, "ms_per_step": ms_64, "speedup_mixed_over_fp64": ms_64 / ms_mx},
+                "accuracy_vs_fp64": {"max_flux_err_wm2": err_flux, "max_heating_rate_err_kday": err_hr},
+                "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s_timed_region": wall}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -158,6 +158,7 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
         double wj = d->w[q];
         gp.weight = (j == 0) ? wj : gp.weight * wj;
         gp.k[j] = d->k[q];
+        gp.kf[j] = (float)d->k[q];
         if (j == 0) gp.iex_major = iex;
         int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
         for (int v = 0; v < nv; ++v) gp.term_scale[j][v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable * q];
@@ -247,8 +248,10 @@ TileConfig choose_tile(int precision, int mode, int n_layer) {
     t.warps_per_cta = g_tile[precision][mode][1];
   }
   if (t.lanes_per_solve <= 0) {
-    if (precision == SOCGPU_PRECISION_MIXED) t.lanes_per_solve = n_layer <= 144 ? 8 : (n_layer <= 256 ? 16 : 32);
-    else t.lanes_per_solve = n_layer <= 256 ? 16 : 32;
+    // measured on GB300: short chunks (few layers per lane) win over long
+    // ones -- fewer live registers and more resident warps
+    if (precision == SOCGPU_PRECISION_MIXED) t.lanes_per_solve = n_layer <= 64 ? 16 : 32;
+    else t.lanes_per_solve = n_layer <= 128 ? 16 : 32;
   }
   // the chunk must cover the column
   int maxch = (precision == SOCGPU_PRECISION_MIXED && t.lanes_per_solve == 8) ? 18 : 16;
@@ -256,7 +259,7 @@ TileConfig choose_tile(int precision, int mode, int n_layer) {
     t.lanes_per_solve *= 2;
     maxch = 16;
   }
-  if (t.warps_per_cta <= 0) t.warps_per_cta = 4;
+  if (t.warps_per_cta <= 0) t.warps_per_cta = 8;
   return t;
 }
 

@@ -206,7 +206,7 @@ struct FluxKernel {
   // kgt/kes/kabs: grey extinction, scattering, absorption; asym/fwd: g' and f.
   __device__ static __forceinline__ void cell_coef(const FluxParams &p, R kgt, R kes, R kabs, R kgas,
                                                    R dm, R asym, R fwd, R sec0,
-                                                   R &T, R &Rf, R &T0, R &c1, R &c2) {
+                                                   R &T, R &Rf, R &T0, R &c1, R &c2, R &omtr) {
     if constexpr (kFP64) {
       double tau, om;
       if (p.i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
@@ -226,12 +226,12 @@ struct FluxKernel {
       }
       Coef c = NOSCAT ? fast_lw_ref(p.l_ir_source_quad, tau)
                       : two_coeff_ref(p.isolir, p.i_2stream, p.l_ir_source_quad, asym, om, tau, sec0);
-      T = c.T; Rf = c.R; T0 = c.T0; c1 = c.c1; c2 = c.c2;
+      T = c.T; Rf = c.R; T0 = c.T0; c1 = c.c1; c2 = c.c2; omtr = R(0);
     } else {
       float tau, om, omc;
       if (p.i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
         float k_total = kgt + kgas;
-        float inv = 1.0f / k_total;
+        float inv = 1.0f / fmaxf(k_total, 1.0e-30f);
         tau = k_total * dm;
         om = kes * inv;
         omc = (kabs + kgas) * inv;                 // 1 - omega without cancellation
@@ -252,7 +252,7 @@ struct FluxKernel {
       }
       CoefF c = NOSCAT ? fast_lw_mix(p.l_ir_source_quad, tau)
                        : two_coeff_mix(p.isolir, p.i_2stream, p.l_ir_source_quad, asym, om, omc, tau, sec0);
-      T = c.T; Rf = c.R; T0 = c.T0; c1 = c.c1; c2 = c.c2;
+      T = c.T; Rf = c.R; T0 = c.T0; c1 = c.c1; c2 = c.c2; omtr = c.omtr;
     }
   }
 
@@ -483,20 +483,53 @@ struct FluxKernel {
     }
   }
 
-  // Gas absorption of g-point gp at layer i.
-  __device__ static __forceinline__ R gas_k(const FluxParams &p, const GPoint &gp, const BandInfo &bd,
+  // Per-g-point gas data held in registers for the layer loop.
+  struct GasTerm {
+    int n_abs;
+    bool any_term;          // some absorber scaled per term (ip_scale_term)
+    R k[kMaxAbsPerBand];
+  };
+
+  __device__ static __forceinline__ GasTerm load_gas(const GPoint &gp, const BandInfo &bd, int max_abs) {
+    GasTerm t;
+    t.n_abs = min(gp.n_abs, max_abs);
+    t.any_term = false;
+#pragma unroll
+    for (int j = 0; j < kMaxAbsPerBand; ++j) {
+      if (j < t.n_abs) {
+        if constexpr (kFP64) t.k[j] = gp.k[j];
+        else t.k[j] = gp.kf[j];
+        t.any_term |= (bd.gas[j].i_scale_k == SOCGPU_IP_SCALE_TERM);
+      } else {
+        t.k[j] = R(0);
+      }
+    }
+    return t;
+  }
+
+  // Gas absorption of a g-point at layer i (gas_optical_properties.F90:80-95).
+  __device__ static __forceinline__ R gas_k(const GasTerm &gt, const GPoint &gp, const BandInfo &bd,
                                             const R *amt, int L, int i, R pl, R tl) {
     R kg = R(0);
-    for (int j = 0; j < gp.n_abs; ++j) {
+    if (!gt.any_term) {
+#pragma unroll
+      for (int j = 0; j < kMaxAbsPerBand; ++j)
+        if (j < gt.n_abs) {
+          R kal = gt.k[j] * amt[(size_t)j * L + i];
+          kg = (j == 0) ? kal : kg + kal;
+        }
+      return kg;
+    }
+    for (int j = 0; j < gt.n_abs; ++j) {
       R a = amt[(size_t)j * L + i];
       R kal;
       if (bd.gas[j].i_scale_k == SOCGPU_IP_SCALE_TERM) {
         R gf = scale_factor<R>(bd.gas[j].i_scale_fnc, pl, tl, (R)bd.gas[j].p_ref, (R)bd.gas[j].t_ref,
                                gp.term_scale[j], bd.gas[j].l_doppler, (R)bd.gas[j].doppler_cor);
         R v = gf * a;
-        kal = (R)gp.k[j] * (v > R(0) ? v : R(0));
+        kal = gt.k[j] * (v > R(0) ? v : R(0));
       } else {
-        kal = (R)gp.k[j] * a;
+        kal = gt.k[j] * a;
       }
       kg = (j == 0) ? kal : kg + kal;
     }
@@ -513,6 +546,7 @@ struct FluxKernel {
     const BandInfo &bd = p.bands[b];
     const double wb = p.weight_band ? p.weight_band[b] : 1.0;
     const R w_g = (R)(wb * gp.weight);
+    const GasTerm gt = load_gas(gp, bd, max_abs);
     const R *s_p = (const R *)(smem + lay.off_p), *s_t = (const R *)(smem + lay.off_t);
     const R *s_mass = (const R *)(smem + lay.off_mass);
     const R *kgt_b = (const R *)(smem + lay.off_kgt) + (size_t)bi * L;
@@ -544,28 +578,29 @@ struct FluxKernel {
     }
 
     if (!MCICA) {
-      R T[CH], Rf[CH], T0[CH], c1[CH], c2[CH];
+      R T[CH], Rf[CH], T0[CH], c1[CH], c2[CH], om[CH];
 #pragma unroll
       for (int j = 0; j < CH; ++j) {
         const int i = r * CH + j;
         if (i < L) {
-          R kg = p.l_gas ? gas_k(p, gp, bd, amt_b, L, i, s_p[i], s_t[i]) : R(0);
+          R kg = p.l_gas ? gas_k(gt, gp, bd, amt_b, L, i, s_p[i], s_t[i]) : R(0);
           cell_coef(p, kgt_b[i], kes_b[i], kabs_b[i], kg, s_mass[i], asym_b[i], fwd_b[i], sec0,
-                    T[j], Rf[j], T0[j], c1[j], c2[j]);
+                    T[j], Rf[j], T0[j], c1[j], c2[j], om[j]);
         } else {
-          T[j] = R(1); Rf[j] = R(0); T0[j] = R(1); c1[j] = R(0); c2[j] = R(0);
+          T[j] = R(1); Rf[j] = R(0); T0[j] = R(1); c1[j] = R(0); c2[j] = R(0); om[j] = R(0);
         }
       }
-      solve_column(p, T, Rf, T0, c1, c2, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
+      solve_column(p, T, Rf, T0, c1, c2, om, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
                    alb_diff, alb_dir, dB_surf, w_g, acc, active);
     } else {
-      solve_mcica(p, lay, smem, col, gp, bd, bi, b, r, L, lw, sec0, dB_b, dB2_b, f_inc_down, f_inc_dir,
+      solve_mcica(p, lay, smem, col, gp, gt, bd, bi, b, r, L, lw, sec0, dB_b, dB2_b, f_inc_down, f_inc_dir,
                   alb_diff, alb_dir, dB_surf, w_g, acc, max_abs, active);
     }
   }
 
   __device__ static void solve_mcica(const FluxParams &p, const SmemLayout &lay, unsigned char *smem,
-                                     int col, const GPoint &gp, const BandInfo &bd, int bi, int b, int r,
+                                     int col, const GPoint &gp, const GasTerm &gt, const BandInfo &bd,
+                                     int bi, int b, int r,
                                      int L, bool lw, R sec0, const R *dB_b, const R *dB2_b,
                                      R f_inc_down, R f_inc_dir, R alb_diff, R alb_dir, R dB_surf,
                                      R w_g, Acc *acc, int max_abs, bool active) {
@@ -621,12 +656,12 @@ struct FluxKernel {
           use = false;
         }
       }
-      R T[CH], Rf[CH], T0[CH], c1[CH], c2[CH];
+      R T[CH], Rf[CH], T0[CH], c1[CH], c2[CH], om[CH];
 #pragma unroll
       for (int jj = 0; jj < CH; ++jj) {
         const int i = r * CH + jj;
         if (i < L) {
-          R kg = p.l_gas ? gas_k(p, gp, bd, amt_b, L, i, s_p[i], s_t[i]) : R(0);
+          R kg = p.l_gas ? gas_k(gt, gp, bd, amt_b, L, i, s_p[i], s_t[i]) : R(0);
           R cs_i = (slot >= 0) ? cs[(size_t)slot * L + i] : R(0);
           bool cloudy = false;
           if (slot >= 0 && wc[i] > R(0)) {
@@ -634,10 +669,10 @@ struct FluxKernel {
           }
           if (!cloudy) {
             cell_coef(p, kgt_b[i], kes_b[i], kabs_b[i], kg, s_mass[i], asym_b[i], fwd_b[i], sec0,
-                      T[jj], Rf[jj], T0[jj], c1[jj], c2[jj]);
+                      T[jj], Rf[jj], T0[jj], c1[jj], c2[jj], om[jj]);
           } else {
             // mcica_sample.F90:472-560 then mcica_column.F90:336-470
-            R sT = R(0), sR = R(0), sT0 = R(0), s1 = R(0), s2 = R(0);
+            R sT = R(0), sR = R(0), sT0 = R(0), s1 = R(0), s2 = R(0), sO = R(0);
             for (int k = 0; k < nc; ++k) {
               const int t = p.comp_type[k] - 1;
               const R fc = fr[(size_t)t * L + i];
@@ -657,18 +692,18 @@ struct FluxKernel {
                 asym = (phf_nc[i] + c_ph[qk] * cs_i) / (kes > eps ? kes : eps);
                 fwd = R(0);
               }
-              R tT, tR, tT0, t1, t2;
-              cell_coef(p, kgt, kes, kab, kg, s_mass[i], asym, fwd, sec0, tT, tR, tT0, t1, t2);
+              R tT, tR, tT0, t1, t2, tO;
+              cell_coef(p, kgt, kes, kab, kg, s_mass[i], asym, fwd, sec0, tT, tR, tT0, t1, t2, tO);
               sT = sT + fc * tT; sR = sR + fc * tR; sT0 = sT0 + fc * tT0;
-              s1 = s1 + fc * t1; s2 = s2 + fc * t2;
+              s1 = s1 + fc * t1; s2 = s2 + fc * t2; sO = sO + fc * tO;
             }
-            T[jj] = sT; Rf[jj] = sR; T0[jj] = lw ? R(1) : sT0; c1[jj] = s1; c2[jj] = s2;
+            T[jj] = sT; Rf[jj] = sR; T0[jj] = lw ? R(1) : sT0; c1[jj] = s1; c2[jj] = s2; om[jj] = sO;
           }
         } else {
-          T[jj] = R(1); Rf[jj] = R(0); T0[jj] = R(1); c1[jj] = R(0); c2[jj] = R(0);
+          T[jj] = R(1); Rf[jj] = R(0); T0[jj] = R(1); c1[jj] = R(0); c2[jj] = R(0); om[jj] = R(0);
         }
       }
-      solve_column(p, T, Rf, T0, c1, c2, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
+      solve_column(p, T, Rf, T0, c1, c2, om, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
                    alb_diff, alb_dir, dB_surf, clear ? w_clr : w_sub, acc, use);
     }
   }
@@ -676,12 +711,16 @@ struct FluxKernel {
   // Sources, direct beam, solve and accumulation of one monochromatic
   // problem held in the group's registers.
   __device__ static void solve_column(const FluxParams &p, R (&T)[CH], R (&Rf)[CH], R (&T0)[CH],
-                                      R (&c1)[CH], R (&c2)[CH], int r, int L, bool lw,
+                                      R (&c1)[CH], R (&c2)[CH], R (&om)[CH], int r, int L, bool lw,
                                       const R *dB_b, const R *dB2_b, R f_inc_down, R f_inc_dir,
                                       R alb_diff, R alb_dir, R dB_surf, R w, Acc *acc, bool active) {
     // the last level a lane accumulates into: none when the solve is discarded
     const int L_acc = active ? L : -1;
     // --- sources -------------------------------------------------------------
+    // ssum = s_up + s_down of each layer: with om = 1 - T - R it gives the
+    // layer's flux divergence (1-T-R)(F_dn(top) + F_up(bottom)) - ssum, the
+    // form the mixed kernel uses instead of differencing FP32 level fluxes
+    R ssum[CH];
     R fdir_bottom = R(0);
     if (!lw) {
       // direct beam: exclusive product scan of the chunks' transmissions
@@ -704,6 +743,7 @@ struct FluxKernel {
         const int i = r * CH + j;
         R su = c1[j] * fd, sd = c2[j] * fd;   // solar_source.F90:146-155
         c1[j] = su; c2[j] = sd;
+        ssum[j] = su + sd;
         fd = fd * T0[j];
         if (i < L_acc) acc[(size_t)(i + 1) * kNumAcc + 2] += w * fd;
       }
@@ -717,12 +757,14 @@ struct FluxKernel {
           if (p.l_ir_source_quad) {       // ir_source.F90:93-119
             su = c1[j] * dB + c2[j] * dB2_b[i];
             sd = -c1[j] * dB + c2[j] * dB2_b[i];
+            ssum[j] = R(2) * c2[j] * dB2_b[i];
           } else {
             su = c1[j] * dB; sd = -su;
+            ssum[j] = R(0);
           }
           c1[j] = su; c2[j] = sd;
         } else {
-          c1[j] = R(0); c2[j] = R(0);
+          c1[j] = R(0); c2[j] = R(0); ssum[j] = R(0);
         }
       }
     }
@@ -775,7 +817,8 @@ struct FluxKernel {
         if (i < L_acc) {
           acc[(size_t)(i + 1) * kNumAcc + 0] += w * c1[j];
           acc[(size_t)(i + 1) * kNumAcc + 1] += w * fdn;
-          acc[(size_t)i * kNumAcc + 3] += w * (c1[j] - fu_prev + fd - fdn);
+          if constexpr (kFP64) acc[(size_t)i * kNumAcc + 3] += w * (c1[j] - fu_prev + fd - fdn);
+          else acc[(size_t)i * kNumAcc + 3] += w * (om[j] * (fd + c1[j]) - ssum[j]);
         }
         fu_prev = c1[j];
         fd = fdn;
@@ -845,7 +888,8 @@ struct FluxKernel {
       if (i < L_acc) {
         acc[(size_t)(i + 1) * kNumAcc + 0] += w * fu;
         acc[(size_t)(i + 1) * kNumAcc + 1] += w * fd;
-        acc[(size_t)i * kNumAcc + 3] += w * (fu - fup + fdn - fd);
+        if constexpr (kFP64) acc[(size_t)i * kNumAcc + 3] += w * (fu - fup + fdn - fd);
+        else acc[(size_t)i * kNumAcc + 3] += w * (om[j] * (fdn + fu) - ssum[j]);
       }
       fup = fu; fdn = fd;
     }

@@ -46,6 +46,7 @@ struct GPoint {
   float pad;
   double weight;                    // product weight of the term
   double k[kMaxAbsPerBand];         // k of each absorber's term
+  float kf[kMaxAbsPerBand];         // the same in FP32 for the mixed kernels
   double term_scale[kMaxAbsPerBand][4];   // per-term scaling parameters (ip_scale_term)
 };
 

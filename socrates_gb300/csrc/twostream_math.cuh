@@ -11,8 +11,8 @@
 //     catastrophically in FP32 -- 1-omega carried from the absorption
 //     coefficient, 1-gamma = 2 lambda/(sum+lambda), 1-exp via expm1, and
 //     (1-T), (1-T-R) in factored form -- with the FP64 clamps of the
-//     reference kept as constants.  Cells next to the solar singularity
-//     lambda = sec_0 fall back to the FP64 expressions.
+//     reference kept as constants.  Next to the solar singularity
+//     lambda = sec_0 the coefficients are interpolated across it.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -37,7 +37,7 @@ struct Coef {
 };
 struct CoefF {
   float T, R, T0, c1, c2;
-  float one_minus_T;   // accurate 1-T (IR source) -- informational
+  float omtr;          // 1 - T - R, formed without cancellation
 };
 
 // ---- scheme coefficients (two_coeff_basic.F90:99-160) --------------------
@@ -126,8 +126,65 @@ __device__ __forceinline__ Coef fast_lw_ref(int l_quad, double tau) {
 }
 
 // ---- mixed-precision forms -------------------------------------------------
-// Distance to the solar singularity below which the FP64 expressions are used.
-constexpr float kSolarSingularTol = 2.0e-3f;
+// Small-argument helpers, from the Taylor series of exp (nested Horner form;
+// below x = 0.25 the truncation error is under 1e-10 relative).
+// 1 - exp(-x) given e = exp(-x).
+__device__ __forceinline__ float one_minus_exp(float x, float e) {
+  if (x < 0.25f)
+    return x * (1.0f - x * 0.5f * (1.0f - x * (1.0f / 3.0f) * (1.0f - x * 0.25f * (1.0f - x * 0.2f *
+           (1.0f - x * (1.0f / 6.0f) * (1.0f - x * (1.0f / 7.0f) * (1.0f - x * 0.125f)))))));
+  return 1.0f - e;
+}
+// phi(x) = x - (1 - exp(-x)) = x^2/2 - x^3/6 + ...
+__device__ __forceinline__ float phi_exp(float x, float em1) {
+  if (x < 0.25f)
+    return x * x * 0.5f * (1.0f - x * (1.0f / 3.0f) * (1.0f - x * 0.25f * (1.0f - x * 0.2f *
+           (1.0f - x * (1.0f / 6.0f) * (1.0f - x * (1.0f / 7.0f))))));
+  return x - em1;
+}
+// psi(x) = exp(-x) (1 + x) - 1 = -x^2/2 + x^3/3 - x^4/8 + x^5/30 - x^6/144 + x^7/840 - ...
+__device__ __forceinline__ float psi_exp(float x, float e) {
+  if (x < 0.25f)
+    return -x * x * (0.5f - x * ((1.0f / 3.0f) - x * (0.125f - x * ((1.0f / 30.0f) - x * ((1.0f / 144.0f) -
+           x * (1.0f / 840.0f))))));
+  return e * (1.0f + x) - 1.0f;
+}
+
+// Relative distance of lambda from sec_0 inside which the solar
+// coefficients are interpolated across the removable singularity.
+constexpr float kSolarSingularTol = 3.0e-3f;
+
+struct SwEval { float T, R, c1, c2, omt, omtr; };
+
+// Reflection, transmission and solar source coefficients for given
+// (sum, diff, lambda); the expressions of trans_source_coeff.F90:144-263
+// and solar_coefficient_basic.F90:124-219 regrouped around 1-e, 1-gamma,
+// 1-T and 1-T0 so that none cancels.
+__device__ __forceinline__ SwEval sw_eval(int scheme, float sum, float diff, float lambda, float om, float g,
+                                          float tau, float sec0, float T0, float one_m_t0) {
+  SwEval c;
+  const float x = lambda * tau;
+  const float e = __expf(-x);
+  const float em1 = one_minus_exp(x, e);
+  const float inv_sl = 1.0f / (sum + lambda);
+  const float gamma = (sum - lambda) * inv_sl;
+  const float one_m_gamma = 2.0f * lambda * inv_sl;
+  const float eg = e * gamma;
+  const float inv_den = 1.0f / ((em1 + e * one_m_gamma) * (1.0f + eg));   // 1/(1 - e^2 gamma^2)
+  c.T = e * one_m_gamma * (1.0f + gamma) * inv_den;
+  c.R = gamma * em1 * (1.0f + e) * inv_den;
+  c.omt = em1 * (1.0f + eg * gamma) * inv_den;                 // 1 - T
+  c.omtr = em1 * one_m_gamma / (1.0f + eg);                    // 1 - T - R
+  const float ksi0 = ((scheme == SOCGPU_IP_DISCRETE_ORD) ? 1.7320508f : 1.5f) * g / sec0;
+  const float factor = 0.5f * om * sec0 / ((lambda - sec0) * (lambda + sec0));
+  const float gam_up = factor * (sum - sec0 - ksi0 * (diff - sec0));
+  const float gam_dn = factor * (sum + sec0 + ksi0 * (diff + sec0));
+  // c1 = gam_up - R(1+gam_dn) - gam_up T T0, c2 = T0(1+gam_dn-gam_up R) - (1+gam_dn) T,
+  // with 1 - T T0 = (1-T0) + T0 (1-T) and T0 - T = (1-T) - (1-T0)
+  c.c1 = gam_up * (one_m_t0 + T0 * c.omt) - c.R * (1.0f + gam_dn);
+  c.c2 = (1.0f + gam_dn) * (c.omt - one_m_t0) - gam_up * c.R * T0;
+  return c;
+}
 
 __device__ __forceinline__ CoefF two_coeff_mix(int isolir, int scheme, int l_quad,
                                                float g, float om, float one_m_om,
@@ -135,52 +192,54 @@ __device__ __forceinline__ CoefF two_coeff_mix(int isolir, int scheme, int l_qua
   CoefF c;
   float sum, diff;
   sum_diff_mix(scheme, om, one_m_om, g, sum, diff);
-  float lambda = sqrtf(sum * diff);
-  if (isolir == SOCGPU_IP_SOLAR && fabsf(lambda - sec0) < kSolarSingularTol * sec0) {
-    // near lambda = sec_0 the particular solution cancels: FP64 reference form
-    Coef d = two_coeff_ref(isolir, scheme, l_quad, (double)g, 1.0 - (double)one_m_om,
-                           (double)tau, (double)sec0);
-    c.T = (float)d.T; c.R = (float)d.R; c.T0 = (float)d.T0; c.c1 = (float)d.c1; c.c2 = (float)d.c2;
-    c.one_minus_T = (float)(1.0 - d.T);
+  const float lambda = sqrtf(sum * diff);
+  if (isolir == SOCGPU_IP_SOLAR) {
+    const float x0 = tau * sec0;
+    const float T0 = __expf(-x0);
+    const float one_m_t0 = one_minus_exp(x0, T0);
+    SwEval v = sw_eval(scheme, sum, diff, lambda, om, g, tau, sec0, T0, one_m_t0);
+    if (fabsf(lambda - sec0) < kSolarSingularTol * sec0) {
+      // The coefficients are smooth through lambda = sec_0, where the
+      // particular solution's 1/(lambda^2 - sec_0^2) cancels.  Evaluate at
+      // (sum, diff, lambda) scaled by rho_a, rho_b placed a safe distance
+      // either side of the singularity and interpolate linearly to rho = 1
+      // (error ~ tol^2 + FP32 eps / tol).
+      const float ra = sec0 * (1.0f - kSolarSingularTol) / lambda;
+      const float rb = sec0 * (1.0f + kSolarSingularTol) / lambda;
+      SwEval a = sw_eval(scheme, ra * sum, ra * diff, ra * lambda, om, g, tau, sec0, T0, one_m_t0);
+      SwEval b = sw_eval(scheme, rb * sum, rb * diff, rb * lambda, om, g, tau, sec0, T0, one_m_t0);
+      const float w = (1.0f - ra) / (rb - ra);
+      v.c1 = a.c1 + w * (b.c1 - a.c1);
+      v.c2 = a.c2 + w * (b.c2 - a.c2);
+    }
+    c.T = v.T; c.R = v.R; c.T0 = T0; c.c1 = v.c1; c.c2 = v.c2; c.omtr = v.omtr;
     return c;
   }
-  float lt = lambda * tau;
-  float em1 = -expm1f(-lt);                  // 1 - e, accurate for small lambda*tau
-  float e = 1.0f - em1;
-  float inv_sl = 1.0f / (sum + lambda);
-  float gamma = (sum - lambda) * inv_sl;
-  float one_m_gamma = 2.0f * lambda * inv_sl;          // 1 - gamma
-  float one_m_gamma2 = one_m_gamma * (1.0f + gamma);   // 1 - gamma^2
-  float eg = e * gamma;
-  float one_m_eg = em1 + e * one_m_gamma;              // 1 - e*gamma
-  float den = one_m_eg * (1.0f + eg);                  // 1 - e^2 gamma^2
-  float inv_den = 1.0f / den;
-  float one_m_e2 = em1 * (1.0f + e);                   // 1 - e^2
-  c.T = e * one_m_gamma2 * inv_den;
-  c.R = gamma * one_m_e2 * inv_den;
+  // infra-red
+  const float x = lambda * tau;
+  const float e = __expf(-x);
+  const float em1 = one_minus_exp(x, e);
+  const float inv_sl = 1.0f / (sum + lambda);
+  const float gamma = (sum - lambda) * inv_sl;
+  const float one_m_gamma = 2.0f * lambda * inv_sl;
+  const float opg = 1.0f + gamma;
+  const float eg = e * gamma;
+  const float inv_den = 1.0f / ((em1 + e * one_m_gamma) * (1.0f + eg));
+  c.T = e * one_m_gamma * opg * inv_den;
+  c.R = gamma * em1 * (1.0f + e) * inv_den;
   c.T0 = 1.0f;
+  c.omtr = em1 * one_m_gamma / (1.0f + eg);
+  const float one_m_t = em1 * (1.0f + eg * gamma) * inv_den;
+  const float sq = (float)kSqEps64;
+  c.c1 = (one_m_t + c.R + sq) / (sq + tau * sum);
   c.c2 = 0.0f;
-  // 1 - T = (1-e)(1+e gamma^2)/(1-e^2 gamma^2)
-  c.one_minus_T = em1 * (1.0f + eg * gamma) * inv_den;
-  if (isolir == SOCGPU_IP_SOLAR) {
-    float ksi0 = ((scheme == SOCGPU_IP_DISCRETE_ORD) ? 1.7320508f : 1.5f) * g / sec0;
-    float factor = 0.5f * om * sec0 / ((lambda - sec0) * (lambda + sec0));
-    float gam_up = factor * (sum - sec0 - ksi0 * (diff - sec0));
-    float gam_dn = factor * (sum + sec0 + ksi0 * (diff + sec0));
-    c.T0 = __expf(-tau * sec0);
-    c.c1 = (gam_up - c.R * (1.0f + gam_dn)) - gam_up * c.T * c.T0;
-    c.c2 = c.T0 * (1.0f + gam_dn - gam_up * c.R) - (1.0f + gam_dn) * c.T;
-  } else {
-    const float sq = (float)kSqEps64;
-    c.c1 = (c.one_minus_T + c.R + sq) / (sq + tau * sum);
-    if (l_quad) {
-      // 1 - T - R = (1-e)(1-gamma)/(1+e gamma)
-      float one_m_t_m_r = em1 * one_m_gamma / (1.0f + eg);
-      float s2;
-      if (tau > (float)kTolQuad64) s2 = -2.0f * (one_m_t_m_r + sq) / (diff * tau + sq);
-      else s2 = -2.0f + diff * tau;
-      c.c2 = -(1.0f + c.R + c.T + s2) / (sum * tau + sq);
-    }
+  if (l_quad) {
+    // trans_source_coeff.F90:233-257: the numerator 1 + R + T + s2 equals
+    // d tau - (1-T-R) (thin layers) or 2 (d tau - (1-T-R))/(d tau + sq) - (1-T-R);
+    // d tau - (1-T-R) = (1-gamma)(phi(x) + gamma psi(x)) / ((1+gamma)(1+e gamma))
+    const float dmo = one_m_gamma * (phi_exp(x, em1) + gamma * psi_exp(x, e)) / (opg * (1.0f + eg));
+    const float num = (tau > (float)kTolQuad64) ? 2.0f * dmo / (diff * tau + sq) - c.omtr : dmo;
+    c.c2 = -num / (sum * tau + sq);
   }
   return c;
 }
@@ -188,15 +247,18 @@ __device__ __forceinline__ CoefF two_coeff_mix(int isolir, int scheme, int l_qua
 __device__ __forceinline__ CoefF fast_lw_mix(int l_quad, float tau) {
   CoefF c;
   const float sq = (float)kSqEps64;
-  float x = 1.66f * tau;
-  float em1 = -expm1f(-x);     // 1 - T
-  c.T = 1.0f - em1;
-  c.one_minus_T = em1;
+  const float x = 1.66f * tau;
+  const float e = __expf(-x);
+  const float em1 = one_minus_exp(x, e);     // 1 - T
+  c.T = e;
+  c.omtr = em1;
   c.R = 0.0f; c.T0 = 1.0f; c.c2 = 0.0f;
   c.c1 = (em1 + sq) / (x + sq);
   if (l_quad) {
-    if (tau > (float)kTolQuad64) c.c2 = -(2.0f - em1 - 2.0f * c.c1) / (x + sq);
-    else c.c2 = -(x - em1) / (x + sq);
+    // two_coeff_fast_lw.F90:138-152 with 1 + T - 2 c1 = 2 phi(x)/(x + sq) - (1-T)
+    const float ph = phi_exp(x, em1);
+    const float num = (tau > (float)kTolQuad64) ? 2.0f * ph / (x + sq) - em1 : ph;
+    c.c2 = -num / (x + sq);
   }
   return c;
 }

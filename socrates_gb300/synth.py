@@ -16,7 +16,7 @@ No public dataset is named for this path, so the workloads are generated:
     body, Rayleigh coefficient 8.6e-7 m2/kg (lambda/1 um)^-4;
   * aerosol: one mode in the lowest 2 km, tau550 log-uniform 0.01..0.5,
     omega U(0.85, 0.99), g U(0.6, 0.75), Angstrom exponent 1.2;
-  * clouds: 30 % of layers cloudy with fraction U(0, 1); liquid below 6 km
+  * clouds: 30 % of the layers below 100 hPa cloudy with fraction U(0, 1); liquid below 6 km
     (LWC log-normal, median 0.1 g/m3, sigma 1; re U(4, 16) um), ice above
     (IWC log-normal, median 0.02 g/m3, sigma 1; De U(20, 120) um); Pade
     optics with this generator's coefficient sets.
@@ -295,14 +295,15 @@ def add_aerosol(col: Column, sp: Spectrum, seed: int) -> Column:
 
 
 def add_clouds(col: Column, seed: int, n_subcol: int = 16, decorrelation_m: float = 2000.0,
-               cloud_prob: float = 0.3) -> Column:
+               cloud_prob: float = 0.3, p_top: float = 1.0e4) -> Column:
     """Cloud fields as set_cld leaves them for ip_cloud_ice_water
     (socrates_set_cld.F90:500-530, 800-845): normalised phase fractions and
     in-cloud mixing ratios; overlap decorrelation in pressure from the local
-    scale height (dp = p g dz / (R T))."""
+    scale height (dp = p g dz / (R T)).  Cloud is confined to the
+    troposphere (layer pressure above p_top, 100 hPa by default)."""
     st = Stream(seed, 4)
     n, L = col.n_profile, col.n_layer
-    cloudy = st.uniform((n, L)) < cloud_prob
+    cloudy = (st.uniform((n, L)) < cloud_prob) & (col.p > p_top)
     frac = np.where(cloudy, st.uniform((n, L)), 0.0)
     rho = col.p / (R_DRY * col.t)
     liquid = col.z < 6000.0

@@ -36,7 +36,7 @@ def assert_fp64_parity(gpu, ref, tag="", mass=None):
     divergence and heating rate are differences of fluxes, so their
     tolerance is that flux tolerance carried through their own formulas
     (two levels; heating rate = 86400 div / (mass cp))."""
-    fscale = max(np.abs(ref[k]).max(axis=1) for k in FLUX_KEYS if k in ref)[:, None] + 1e-300
+    fscale = np.maximum.reduce([np.abs(ref[k]).max(axis=1) for k in FLUX_KEYS if k in ref])[:, None] + 1e-300
     for k in ref:
         if k == "mass":
             continue
