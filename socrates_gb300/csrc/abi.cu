@@ -90,7 +90,12 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
     bi.solar_flux_band = d->solar_flux_band ? d->solar_flux_band[b] : 0.0;
     bi.rayleigh_coeff = d->rayleigh_coeff ? d->rayleigh_coeff[b] : 0.0;
     if (d->thermal_coeff)
-      for (int j = 0; j <= d->n_deg_fit; ++j) bi.planck[j] = d->thermal_coeff[(size_t)j + (size_t)d->nd_thermal_coeff * b];
+      for (int j = 0; j <= d->n_deg_fit; ++j) {
+        bi.planck[j] = d->thermal_coeff[(size_t)j + (size_t)d->nd_thermal_coeff * b];
+        bi.planck_f[j] = (float)bi.planck[j];
+      }
+    bi.rayleigh_f = (float)bi.rayleigh_coeff;
+    bi.solar_flux_band_f = (float)bi.solar_flux_band;
     int n_abs = d->n_band_absorb ? d->n_band_absorb[b] : 0;
     if (n_abs > kMaxAbsPerBand) {
       set_msg(msg, msg_len, "band %d has %d absorbers; at most %d supported", b + 1, n_abs, kMaxAbsPerBand);
@@ -126,9 +131,14 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
         return SOCGPU_I_ERR_FATAL;
       }
       int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
-      for (int v = 0; v < nv; ++v)
+      for (int v = 0; v < nv; ++v) {
         gs.scale[v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable *
                                               ((size_t)0 + (size_t)d->nd_k_term * ((size_t)b + (size_t)d->nd_band * g))];
+        gs.scale_f[v] = (float)gs.scale[v];
+      }
+      gs.p_ref_f = (float)gs.p_ref;
+      gs.t_ref_f = (float)gs.t_ref;
+      gs.doppler_cor_f = (float)gs.doppler_cor;
       nk[j] = fget2(d->i_band_k, b, g, d->nd_band);
       if (nk[j] < 1 || nk[j] > d->nd_k_term) {
         set_msg(msg, msg_len, "band %d absorber %d: %d k-terms", b + 1, g + 1, nk[j]);
@@ -161,8 +171,12 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
         gp.kf[j] = (float)d->k[q];
         if (j == 0) gp.iex_major = iex;
         int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
-        for (int v = 0; v < nv; ++v) gp.term_scale[j][v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable * q];
+        for (int v = 0; v < nv; ++v) {
+          gp.term_scale[j][v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable * q];
+          gp.term_scale_f[j][v] = (float)gp.term_scale[j][v];
+        }
       }
+      gp.weight_f = (float)gp.weight;
       if (n_abs > 0 && !(gp.weight > 0.0)) continue;   // n_term_reduced
       e.gpoints_host.push_back(gp);
     }
@@ -201,20 +215,26 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
       for (int c = 0; c < kPadeParm; ++c)
         ice[((size_t)t * d->n_band + b) * kPadeParm + c] =
             d->ice_parm_list[(size_t)c + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * t)];
+  std::vector<float> drop_f(drop.begin(), drop.end()), ice_f(ice.begin(), ice.end());
   cudaGetDevice(&e.device);
   if (cudaMalloc(&s.bands, sizeof(BandInfo) * s.n_band) != cudaSuccess ||
       cudaMalloc(&s.gpoints, sizeof(GPoint) * std::max(1, s.n_gpoint)) != cudaSuccess ||
       cudaMalloc(&s.drop_parm, sizeof(double) * drop.size()) != cudaSuccess ||
-      cudaMalloc(&s.ice_parm, sizeof(double) * ice.size()) != cudaSuccess) {
+      cudaMalloc(&s.ice_parm, sizeof(double) * ice.size()) != cudaSuccess ||
+      cudaMalloc(&s.drop_parm_f, sizeof(float) * drop_f.size()) != cudaSuccess ||
+      cudaMalloc(&s.ice_parm_f, sizeof(float) * ice_f.size()) != cudaSuccess) {
     set_msg(msg, msg_len, "device allocation for spectral tables failed");
     return SOCGPU_I_ABORT_CALCULATION;
   }
-  cudaMemcpy(s.bands, e.bands_host.data(), sizeof(BandInfo) * s.n_band, cudaMemcpyHostToDevice);
-  if (s.n_gpoint > 0)
-    cudaMemcpy(s.gpoints, e.gpoints_host.data(), sizeof(GPoint) * s.n_gpoint, cudaMemcpyHostToDevice);
-  cudaMemcpy(s.drop_parm, drop.data(), sizeof(double) * drop.size(), cudaMemcpyHostToDevice);
-  cudaMemcpy(s.ice_parm, ice.data(), sizeof(double) * ice.size(), cudaMemcpyHostToDevice);
-  cudaError_t err = cudaGetLastError();
+  cudaError_t err = cudaMemcpy(s.bands, e.bands_host.data(), sizeof(BandInfo) * s.n_band, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess && s.n_gpoint > 0)
+    err = cudaMemcpy(s.gpoints, e.gpoints_host.data(), sizeof(GPoint) * s.n_gpoint, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(s.drop_parm, drop.data(), sizeof(double) * drop.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(s.ice_parm, ice.data(), sizeof(double) * ice.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(s.drop_parm_f, drop_f.data(), sizeof(float) * drop_f.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(s.ice_parm_f, ice_f.data(), sizeof(float) * ice_f.size(), cudaMemcpyHostToDevice);
   if (err != cudaSuccess) {
     set_msg(msg, msg_len, "upload of spectral tables failed: %s", cudaGetErrorString(err));
     return SOCGPU_I_ABORT_CALCULATION;
@@ -227,6 +247,8 @@ void free_spectrum(SpectrumEntry &e) {
   cudaFree(e.dev.gpoints);
   cudaFree(e.dev.drop_parm);
   cudaFree(e.dev.ice_parm);
+  cudaFree(e.dev.drop_parm_f);
+  cudaFree(e.dev.ice_parm_f);
 }
 
 SpectrumEntry *find_spectrum(int h) {
@@ -387,7 +409,9 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
     p.max_abs = std::max(p.max_abs, c->l_gas ? sp->bands_host[b].n_abs : 0);
   p.bands = sp->dev.bands; p.gpoints = sp->dev.gpoints;
   p.drop_parm = sp->dev.drop_parm; p.ice_parm = sp->dev.ice_parm;
+  p.drop_parm_f = sp->dev.drop_parm_f; p.ice_parm_f = sp->dev.ice_parm_f;
   p.n_band = sp->dev.n_band; p.n_deg_fit = sp->dev.n_deg_fit; p.t_ref_planck = sp->dev.t_ref_planck;
+  p.t_ref_planck_f = (float)sp->dev.t_ref_planck;
   p.weight_band = weight_band_dev;
   p.p = atm->p; p.t = atm->t; p.t_level = atm->t_level; p.mass = atm->mass; p.gas_mix_ratio = atm->gas_mix_ratio;
   p.nd_species = sp->dev.n_species;

@@ -1,16 +1,16 @@
 // flux_kernel.cuh -- fused two-stream flux kernel for sm_103a.
 //
 // One CTA per column.  The CTA first stages the column's per-band grey
-// optics, gas amounts and Planck terms in shared memory (the band loop of
-// radiance_calc.F90:883-1600), then its lanes solve the monochromatic
-// problems of every g-point (k-term product) of the band range:
+// optics, gas amounts, Planck terms and boundary values in shared memory
+// (the band loop of radiance_calc.F90:883-1600), then its lanes solve the
+// monochromatic problems of every g-point (k-term product):
 //
 //   * a "group" of P consecutive lanes owns one (column, g-point) solve;
 //     lane r of the group holds layers [r*CH, r*CH+CH) in registers;
 //   * the per-layer physics (single_scattering, rescale_tau_omega,
 //     two_coeff, sources) is computed for all layers in parallel;
-//   * the direct beam (solar_source.F90:105-176) is a product scan over
-//     the group's lanes, and the adding-method solve
+//   * the direct beam (solar_source.F90:105-176) is a product scan over the
+//     group's lanes, and the adding-method solve
 //     (solver_homogen_direct.F90:94-131) becomes an associative scan of
 //     layer "composites" (reflection/transmission/source of a stack of
 //     layers) down and up the group, followed by the reference's
@@ -19,6 +19,15 @@
 //   * each group accumulates its fluxes in its own shared-memory slice
 //     (augment_channel_mod.F90:158-235); slices are summed in a fixed order
 //     at the end, so results are deterministic.
+//
+// Per-layer shared arrays use a permuted slot order: layer i lives in slot
+// (i % CH) * P + i / CH, so lane r's j-th layer is slot j*P + r and the P
+// lanes of a group touch P consecutive words (no bank conflicts).
+//
+// The mixed-precision instantiation (R = float) does all of its arithmetic
+// in FP32: FP64 inputs are narrowed once while staging (on the integer
+// pipe), table constants come from FP32 copies, and results are widened on
+// the way out.  On GB300 the FP64 pipe runs at 1/64 of FP32.
 //
 // McICA (mcica_sample.F90:453-925, mcica_column.F90:261-602): a group loops
 // over the subcolumns assigned to its g-point plus the clear solve and adds
@@ -32,11 +41,54 @@
 
 namespace socgpu {
 
-constexpr int kNumAcc = 4;   // up, down, direct (per level), divergence (per layer)
+constexpr int kNumAcc = 4;     // up, down, direct (per level), divergence (per layer)
+constexpr int kBandScal = 6;   // f_inc_down, f_inc_dir, alb_diff, alb_dir, dB_surf, weight_band
 
 // Column-major (Fortran) element access with leading extent nd.
 __device__ __forceinline__ double ld2(const double *a, int l, int i, int nd) {
   return __ldg(a + (size_t)l + (size_t)nd * (size_t)i);
+}
+
+// FP64 -> FP32 narrowing with round-to-nearest-even on the integer pipe
+// (the F2F instruction issues on the FP64 pipe).  Results below the FP32
+// normal range flush to zero, as the mixed kernels run with FTZ; NaN stays
+// NaN and overflow gives infinity.
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1FFFFFFFu;
+  unsigned bits = ((unsigned)e << 23) + m;
+  bits += (rem > 0x10000000u) | ((rem == 0x10000000u) & (m & 1u));
+  if (e <= 0) bits = 0u;
+  if (e >= 255) bits = ((hi & 0x7FFFFFFFu) > 0x7FF00000u || ((hi & 0x7FFFFFFFu) == 0x7FF00000u && lo))
+                           ? 0x7FC00000u : 0x7F800000u;
+  return __uint_as_float(sign | bits);
+}
+
+// FP32 -> FP64 widening (exact) on the integer pipe; FP32 subnormals are
+// already flushed.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  unsigned hi, lo;
+  if (e == 0u) { hi = sign; lo = 0u; }
+  else if (e == 255u) { hi = sign | 0x7FF00000u | (m >> 3); lo = m << 29; }
+  else { hi = sign | ((e + 896u) << 20) | (m >> 3); lo = m << 29; }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+template <class R>
+__device__ __forceinline__ R load_in(const double *a) {
+  if constexpr (sizeof(R) == 8) return __ldg(a);
+  else return narrow(__ldg(a));
+}
+template <class R>
+__device__ __forceinline__ double store_out(R v) {
+  if constexpr (sizeof(R) == 8) return v;
+  else return widen(v);
 }
 
 template <class R>
@@ -90,10 +142,12 @@ __device__ __forceinline__ Comp<R> shfl_down_comp(const Comp<R> &c, int d, int w
 }
 
 // ---------------------------------------------------------------------------
-// Shared-memory layout of one column (identical on host and device).
+// Shared-memory layout of one column (identical on host and device).  LP is
+// the padded layer count P*CH; level arrays hold LP+1 entries (slot LP is
+// level 0).
 struct SmemLayout {
-  int L, nb, max_abs, n_comp, n_sub, n_groups;
-  size_t off_p, off_t, off_mass, off_kgt, off_kes, off_kabs, off_asym, off_fwd, off_amt;
+  int LP, nb, max_abs, n_comp, n_sub, n_groups, acc_stride;
+  size_t off_p, off_t, off_mass, off_kgt, off_kes, off_kabs, off_asym, off_fwd, off_amt, off_bscal;
   size_t off_planck, off_dB, off_dB2;
   size_t off_phf_nc, off_fwd_nc, off_c_ke, off_c_ks, off_c_ka, off_c_phf, off_c_fwd;
   size_t off_wcld, off_frac, off_csub;
@@ -101,77 +155,85 @@ struct SmemLayout {
   size_t bytes;
 };
 
-template <class R, class Acc>
-__host__ __device__ inline SmemLayout make_layout(int L, int nb, int max_abs, int n_comp, int n_sub,
+template <class R>
+__host__ __device__ inline SmemLayout make_layout(int LP, int P, int nb, int max_abs, int n_comp, int n_sub,
                                                   int n_groups, bool lw, bool mcica) {
   SmemLayout s{};
-  s.L = L; s.nb = nb; s.max_abs = max_abs; s.n_comp = n_comp; s.n_sub = n_sub; s.n_groups = n_groups;
+  s.LP = LP; s.nb = nb; s.max_abs = max_abs; s.n_comp = n_comp; s.n_sub = n_sub; s.n_groups = n_groups;
   size_t o = 0;
-  auto take = [&](size_t elems, size_t esz) { size_t r = (o + 15) & ~(size_t)15; o = r + elems * esz; return r; };
-  s.off_p = take(L, sizeof(R));
-  s.off_t = take(L, sizeof(R));
-  s.off_mass = take(L, sizeof(R));
-  s.off_kgt = take((size_t)nb * L, sizeof(R));
-  s.off_kes = take((size_t)nb * L, sizeof(R));
-  s.off_kabs = take((size_t)nb * L, sizeof(R));
-  s.off_asym = take((size_t)nb * L, sizeof(R));
-  s.off_fwd = take((size_t)nb * L, sizeof(R));
-  s.off_amt = take((size_t)nb * max_abs * L, sizeof(R));
-  s.off_planck = lw ? take((size_t)nb * (L + 1), sizeof(R)) : o;
-  s.off_dB = lw ? take((size_t)nb * L, sizeof(R)) : o;
-  s.off_dB2 = lw ? take((size_t)nb * L, sizeof(R)) : o;
+  auto take = [&](size_t elems) { size_t r = (o + 15) & ~(size_t)15; o = r + elems * sizeof(R); return r; };
+  s.off_p = take(LP);
+  s.off_t = take(LP);
+  s.off_mass = take(LP);
+  s.off_kgt = take((size_t)nb * LP);
+  s.off_kes = take((size_t)nb * LP);
+  s.off_kabs = take((size_t)nb * LP);
+  s.off_asym = take((size_t)nb * LP);
+  s.off_fwd = take((size_t)nb * LP);
+  s.off_amt = take((size_t)nb * max_abs * LP);
+  s.off_bscal = take((size_t)nb * kBandScal);
+  s.off_planck = lw ? take((size_t)nb * (LP + 1)) : o;
+  s.off_dB = lw ? take((size_t)nb * LP) : o;
+  s.off_dB2 = lw ? take((size_t)nb * LP) : o;
   if (mcica) {
-    s.off_phf_nc = take((size_t)nb * L, sizeof(R));
-    s.off_fwd_nc = take((size_t)nb * L, sizeof(R));
-    s.off_c_ke = take((size_t)nb * n_comp * L, sizeof(R));
-    s.off_c_ks = take((size_t)nb * n_comp * L, sizeof(R));
-    s.off_c_ka = take((size_t)nb * n_comp * L, sizeof(R));
-    s.off_c_phf = take((size_t)nb * n_comp * L, sizeof(R));
-    s.off_c_fwd = take((size_t)nb * n_comp * L, sizeof(R));
-    s.off_wcld = take(L, sizeof(R));
-    s.off_frac = take((size_t)2 * L, sizeof(R));
-    s.off_csub = take((size_t)n_sub * L, sizeof(R));
+    s.off_phf_nc = take((size_t)nb * LP);
+    s.off_fwd_nc = take((size_t)nb * LP);
+    s.off_c_ke = take((size_t)nb * n_comp * LP);
+    s.off_c_ks = take((size_t)nb * n_comp * LP);
+    s.off_c_ka = take((size_t)nb * n_comp * LP);
+    s.off_c_phf = take((size_t)nb * n_comp * LP);
+    s.off_c_fwd = take((size_t)nb * n_comp * LP);
+    s.off_wcld = take(LP);
+    s.off_frac = take((size_t)2 * LP);
+    s.off_csub = take((size_t)n_sub * LP);
   }
-  s.off_acc = take((size_t)n_groups * (L + 1) * kNumAcc, sizeof(Acc));
+  // per-group accumulator slices, offset by P words mod 32 so that the
+  // groups of one warp land on different banks
+  const int words = (int)(sizeof(R) / 4);
+  int stride = kNumAcc * (LP + 1);
+  int rem = (stride * words) % 32;
+  int want = (P * words) % 32;
+  while (rem != want) { ++stride; rem = (stride * words) % 32; }
+  s.acc_stride = stride;
+  s.off_acc = take((size_t)n_groups * stride);
   s.bytes = (o + 15) & ~(size_t)15;
   return s;
 }
 
-// Powers used by scale_absorb (scale_absorb.F90:122-224).
-template <class R>
-__device__ __forceinline__ R scale_factor(int fnc, R p, R t, R p_ref, R t_ref, const double *sp,
-                                          int l_doppler, R dop) {
-  if constexpr (sizeof(R) == 8) {
-    double off = l_doppler ? dop : 0.0;
-    if (fnc == SOCGPU_IP_SCALE_POWER_LAW) {
-      double t_inv = 1.0 / t_ref, p_ref_off_inv = 1.0 / (p_ref + off);
-      return pow((p + off) * p_ref_off_inv, sp[0]) * pow(t * t_inv, sp[1]);
-    } else if (fnc == SOCGPU_IP_SCALE_POWER_QUAD) {
-      double p_ref_off_inv = 1.0 / (p_ref + off), t_inv = 1.0 / t_ref;
-      double pwk = pow((p + off) * p_ref_off_inv, sp[0]);
-      double tmp = t * t_inv - 1.0;
-      return pwk * (1.0 + tmp * sp[1] + sp[2] * tmp * tmp);
-    } else if (fnc == SOCGPU_IP_SCALE_DOPPLER_QUAD) {
-      double pwk = pow((p + sp[1]) / (p_ref + sp[1]), sp[0]);
-      double tmp = t * (1.0 / t_ref) - 1.0;
-      return pwk * (1.0 + tmp * sp[2] + sp[3] * tmp * tmp);
-    }
-    return 1.0;
-  } else {
-    float off = l_doppler ? (float)dop : 0.0f;
-    if (fnc == SOCGPU_IP_SCALE_POWER_LAW) {
-      return exp2f((float)sp[0] * __log2f((p + off) / (p_ref + off)) + (float)sp[1] * __log2f(t / t_ref));
-    } else if (fnc == SOCGPU_IP_SCALE_POWER_QUAD) {
-      float pwk = exp2f((float)sp[0] * __log2f((p + off) / (p_ref + off)));
-      float tmp = t / t_ref - 1.0f;
-      return pwk * (1.0f + tmp * (float)sp[1] + (float)sp[2] * tmp * tmp);
-    } else if (fnc == SOCGPU_IP_SCALE_DOPPLER_QUAD) {
-      float pwk = exp2f((float)sp[0] * __log2f((p + (float)sp[1]) / (p_ref + (float)sp[1])));
-      float tmp = t / t_ref - 1.0f;
-      return pwk * (1.0f + tmp * (float)sp[2] + (float)sp[3] * tmp * tmp);
-    }
-    return 1.0f;
+// Pressure/temperature scaling of a k-term (scale_absorb.F90:110-224).
+__device__ __forceinline__ double scale_factor_ref(int fnc, double p, double t, double p_ref, double t_ref,
+                                                   const double *sp, int l_doppler, double dop) {
+  double off = l_doppler ? dop : 0.0;
+  if (fnc == SOCGPU_IP_SCALE_POWER_LAW) {
+    double t_inv = 1.0 / t_ref, p_ref_off_inv = 1.0 / (p_ref + off);
+    return pow((p + off) * p_ref_off_inv, sp[0]) * pow(t * t_inv, sp[1]);
+  } else if (fnc == SOCGPU_IP_SCALE_POWER_QUAD) {
+    double p_ref_off_inv = 1.0 / (p_ref + off), t_inv = 1.0 / t_ref;
+    double pwk = pow((p + off) * p_ref_off_inv, sp[0]);
+    double tmp = t * t_inv - 1.0;
+    return pwk * (1.0 + tmp * sp[1] + sp[2] * tmp * tmp);
+  } else if (fnc == SOCGPU_IP_SCALE_DOPPLER_QUAD) {
+    double pwk = pow((p + sp[1]) / (p_ref + sp[1]), sp[0]);
+    double tmp = t * (1.0 / t_ref) - 1.0;
+    return pwk * (1.0 + tmp * sp[2] + sp[3] * tmp * tmp);
   }
+  return 1.0;
+}
+__device__ __forceinline__ float scale_factor_mix(int fnc, float p, float t, float p_ref, float t_ref,
+                                                  const float *sp, int l_doppler, float dop) {
+  float off = l_doppler ? dop : 0.0f;
+  if (fnc == SOCGPU_IP_SCALE_POWER_LAW) {
+    return exp2f(sp[0] * __log2f((p + off) / (p_ref + off)) + sp[1] * __log2f(t / t_ref));
+  } else if (fnc == SOCGPU_IP_SCALE_POWER_QUAD) {
+    float pwk = exp2f(sp[0] * __log2f((p + off) / (p_ref + off)));
+    float tmp = t / t_ref - 1.0f;
+    return pwk * (1.0f + tmp * sp[1] + sp[2] * tmp * tmp);
+  } else if (fnc == SOCGPU_IP_SCALE_DOPPLER_QUAD) {
+    float pwk = exp2f(sp[0] * __log2f((p + sp[1]) / (p_ref + sp[1])));
+    float tmp = t / t_ref - 1.0f;
+    return pwk * (1.0f + tmp * sp[2] + sp[3] * tmp * tmp);
+  }
+  return 1.0f;
 }
 
 // Band Planck flux (planck_flux_band_mod.F90:33-48), Horner in T/T_ref.
@@ -180,20 +242,21 @@ __device__ __forceinline__ double planck_ref(const double *c, int n_deg, double 
   for (int j = n_deg - 1; j >= 0; --j) f = f * t_ratio + c[j];
   return f;
 }
-
-// Difference B(t1) - B(t0) of the polynomial without cancellation:
-// t1^j - t0^j = (t1 - t0) * sum_{m<j} t1^m t0^(j-1-m), accumulated in FP32.
-__device__ __forceinline__ float planck_diff_mix(const double *c, int n_deg, float x1, float x0) {
-  float dx = x1 - x0;
-  float d = 0.0f;            // d_j = (x1^j - x0^j) / dx
-  float p0 = 1.0f;           // x0^(j-1)
-  float sum = 0.0f;
+__device__ __forceinline__ float planck_mix(const float *c, int n_deg, float x) {
+  float f = c[n_deg];
+  for (int j = n_deg - 1; j >= 0; --j) f = f * x + c[j];
+  return f;
+}
+// B(x1) - B(x0) without cancellation: x1^j - x0^j = (x1 - x0) d_j with
+// d_j = x1 d_{j-1} + x0^(j-1).
+__device__ __forceinline__ float planck_diff_mix(const float *c, int n_deg, float x1, float x0) {
+  float d = 0.0f, p0 = 1.0f, sum = 0.0f;
   for (int j = 1; j <= n_deg; ++j) {
-    d = x1 * d + p0;         // d_j = x1 d_{j-1} + x0^{j-1}
+    d = x1 * d + p0;
     p0 *= x0;
-    sum += (float)c[j] * d;
+    sum += c[j] * d;
   }
-  return dx * sum;
+  return (x1 - x0) * sum;
 }
 
 // ---------------------------------------------------------------------------
@@ -201,6 +264,11 @@ template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA>
 struct FluxKernel {
   using Acc = R;
   static constexpr bool kFP64 = (sizeof(R) == 8);
+  static constexpr int LP = P * CH;
+
+  __device__ static __forceinline__ int slot(int i) { return (i % CH) * P + i / CH; }
+  __device__ static __forceinline__ int layer_of_slot(int s) { return (s % P) * CH + s / P; }
+  __device__ static __forceinline__ int level_slot(int lev) { return lev == 0 ? LP : slot(lev - 1); }
 
   // Single scattering + delta rescaling + two-stream coefficients of a cell.
   // kgt/kes/kabs: grey extinction, scattering, absorption; asym/fwd: g' and f.
@@ -208,6 +276,7 @@ struct FluxKernel {
                                                    R dm, R asym, R fwd, R sec0,
                                                    R &T, R &Rf, R &T0, R &c1, R &c2, R &omtr) {
     if constexpr (kFP64) {
+      // single_scattering.F90:119-164, rescale_tau_omega.F90:73-80
       double tau, om;
       if (p.i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
         double k_total = kgt + kgas;
@@ -256,230 +325,329 @@ struct FluxKernel {
     }
   }
 
+  struct Smem {
+    R *p, *t, *mass, *kgt, *kes, *kabs, *asym, *fwd, *amt, *bscal, *planck, *dB, *dB2;
+    R *phf_nc, *fwd_nc, *c_ke, *c_ks, *c_ka, *c_phf, *c_fwd, *wcld, *frac, *csub;
+    Acc *acc;
+  };
+
+  __device__ static Smem bind(unsigned char *smem, const SmemLayout &l) {
+    Smem s;
+    s.p = (R *)(smem + l.off_p); s.t = (R *)(smem + l.off_t); s.mass = (R *)(smem + l.off_mass);
+    s.kgt = (R *)(smem + l.off_kgt); s.kes = (R *)(smem + l.off_kes); s.kabs = (R *)(smem + l.off_kabs);
+    s.asym = (R *)(smem + l.off_asym); s.fwd = (R *)(smem + l.off_fwd); s.amt = (R *)(smem + l.off_amt);
+    s.bscal = (R *)(smem + l.off_bscal);
+    s.planck = (R *)(smem + l.off_planck); s.dB = (R *)(smem + l.off_dB); s.dB2 = (R *)(smem + l.off_dB2);
+    s.phf_nc = (R *)(smem + l.off_phf_nc); s.fwd_nc = (R *)(smem + l.off_fwd_nc);
+    s.c_ke = (R *)(smem + l.off_c_ke); s.c_ks = (R *)(smem + l.off_c_ks); s.c_ka = (R *)(smem + l.off_c_ka);
+    s.c_phf = (R *)(smem + l.off_c_phf); s.c_fwd = (R *)(smem + l.off_c_fwd);
+    s.wcld = (R *)(smem + l.off_wcld); s.frac = (R *)(smem + l.off_frac); s.csub = (R *)(smem + l.off_csub);
+    s.acc = (Acc *)(smem + l.off_acc);
+    return s;
+  }
+
   __device__ static void run(const FluxParams &p) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int col = blockIdx.x;
     const int L = p.n_layer;
-    const int nb = p.last_band - p.first_band + 1;
-    const int b0 = p.first_band - 1;
+    const int nb_all = p.last_band - p.first_band + 1;
+    const int nbat = p.band_batch;             // bands staged at a time
     const int nthreads = blockDim.x;
     const int n_groups = nthreads / P;
     const bool lw = (p.isolir == SOCGPU_IP_INFRA_RED);
     const int max_abs = p.max_abs;
-    const SmemLayout lay = make_layout<R, Acc>(L, nb, max_abs, MCICA ? p.n_condensed : 0,
-                                               MCICA ? p.n_subcol_gen : 0, n_groups, lw, MCICA);
-    R *s_p = (R *)(smem + lay.off_p), *s_t = (R *)(smem + lay.off_t), *s_mass = (R *)(smem + lay.off_mass);
-    R *s_kgt = (R *)(smem + lay.off_kgt), *s_kes = (R *)(smem + lay.off_kes);
-    R *s_kabs = (R *)(smem + lay.off_kabs), *s_asym = (R *)(smem + lay.off_asym);
-    R *s_fwd = (R *)(smem + lay.off_fwd), *s_amt = (R *)(smem + lay.off_amt);
-    R *s_planck = (R *)(smem + lay.off_planck), *s_dB2 = (R *)(smem + lay.off_dB2);
-    R *s_dB = (R *)(smem + lay.off_dB);
-    Acc *s_acc = (Acc *)(smem + lay.off_acc);
-    const int ndp = p.nd_profile, ndl = p.nd_layer;
+    const SmemLayout lay = make_layout<R>(LP, P, nbat, max_abs, MCICA ? p.n_condensed : 0,
+                                         MCICA ? p.n_subcol_gen : 0, n_groups, lw, MCICA);
+    const Smem S = bind(smem, lay);
+    const int ndp = p.nd_profile;
 
-    // ---------------- phase 1: stage the column ----------------------------
-    for (int i = threadIdx.x; i < L; i += nthreads) {
-      s_p[i] = (R)ld2(p.p, col, i, ndp);
-      s_t[i] = (R)ld2(p.t, col, i, ndp);
-      s_mass[i] = (R)ld2(p.mass, col, i, ndp);
+    // ---------------- column fields and accumulators ------------------------
+    for (int s = threadIdx.x; s < LP; s += nthreads) {
+      const int i = layer_of_slot(s);
+      if (i < L) {
+        S.p[s] = load_in<R>(p.p + (size_t)col + (size_t)ndp * i);
+        S.t[s] = load_in<R>(p.t + (size_t)col + (size_t)ndp * i);
+        S.mass[s] = load_in<R>(p.mass + (size_t)col + (size_t)ndp * i);
+      }
     }
-    for (size_t q = threadIdx.x; q < (size_t)n_groups * (L + 1) * kNumAcc; q += nthreads) s_acc[q] = Acc(0);
+    for (int q = threadIdx.x; q < n_groups * lay.acc_stride; q += nthreads) S.acc[q] = Acc(0);
+    if (MCICA) stage_cloud_column(p, S, col);
+    const int gid = threadIdx.x / P;
+    const int r = threadIdx.x % P;
+    const R sec0 = p.zen_0 ? load_in<R>(p.zen_0 + col) : R(1);
+    Acc *acc = S.acc + (size_t)gid * lay.acc_stride;
     __syncthreads();
-    for (int q = threadIdx.x; q < nb * L; q += nthreads) {
-      const int bi = q / L, i = q - bi * L, b = b0 + bi;
+
+    for (int bb = 0; bb < nb_all; bb += nbat) {
+      const int nb = min(nbat, nb_all - bb);
+      const int bstart = p.first_band - 1 + bb;
+      stage_bands(p, S, col, bstart, nb, lw);
+      if (MCICA) stage_cloud_bands(p, S, col, bstart, nb);
+      __syncthreads();
+      stage_boundary(p, S, col, bstart, nb, lw);
+      __syncthreads();
+      // g-point solves.  Every group of every warp runs the same number of
+      // rounds so that the full-warp shuffles of the scans always see all
+      // 32 lanes; a group with no g-point left in the last round solves the
+      // first g-point of the batch and discards it.
+      const int g_lo = p.bands[bstart].g_first;
+      const int g_hi = p.bands[bstart + nb - 1].g_first + p.bands[bstart + nb - 1].g_count;
+      const int rounds = (g_hi - g_lo + n_groups - 1) / n_groups;
+      for (int rd = 0; rd < rounds; ++rd) {
+        int g = g_lo + rd * n_groups + gid;
+        const bool active = g < g_hi;
+        if (!active) g = g_lo;
+        solve_gpoint(p, S, col, g, bstart, max_abs, sec0, r, acc, lw, active);
+      }
+      __syncthreads();
+      if (lw) {
+        // adjust_ir_radiance.F90:75-95: add the band Planck flux back, into
+        // the first group's slice
+        for (int s = threadIdx.x; s <= LP; s += nthreads) {
+          const int lev = (s == LP) ? 0 : layer_of_slot(s) + 1;
+          if (lev > L) continue;
+          Acc add = Acc(0);
+          for (int bi = 0; bi < nb; ++bi) add += S.planck[bi * (LP + 1) + s] * S.bscal[bi * kBandScal + 5];
+          S.acc[s] += add;
+          S.acc[(LP + 1) + s] += add;
+        }
+        __syncthreads();
+      }
+    }
+
+    // ---------------- reduce over groups, write ------------------------------
+    for (int lev = threadIdx.x; lev <= L; lev += nthreads) {
+      const int s = level_slot(lev);
+      Acc up = Acc(0), dn = Acc(0), dir = Acc(0);
+      for (int q = 0; q < n_groups; ++q) {
+        const Acc *a = S.acc + (size_t)q * lay.acc_stride;
+        up += a[s]; dn += a[(LP + 1) + s]; dir += a[2 * (LP + 1) + s];
+      }
+      const size_t o = (size_t)col + (size_t)ndp * lev;
+      p.flux_up[o] = store_out<R>(up);
+      p.flux_down[o] = store_out<R>(dn);
+      if (p.flux_direct) p.flux_direct[o] = lw ? 0.0 : store_out<R>(dir);
+      if (lev < L) {
+        // the divergence of layer lev sits at its bottom level's slot
+        Acc dlay = Acc(0);
+        const int sl = slot(lev);
+        for (int q = 0; q < n_groups; ++q) dlay += S.acc[(size_t)q * lay.acc_stride + 3 * (LP + 1) + sl];
+        if (p.flux_div) p.flux_div[(size_t)col + (size_t)ndp * lev] = store_out<R>(dlay);
+        if (p.heating_rate) {
+          // heating rate (l_run_cdf.F90:1340-1380); without l_flux_div the
+          // FP64 rate is filled below from the net fluxes
+          double hr;
+          if constexpr (kFP64) hr = p.l_flux_div ? 8.64e4 * dlay / (ld2(p.mass, col, lev, ndp) * 1.005e3) : 0.0;
+          else hr = store_out<R>(8.64e4f * dlay / (S.mass[sl] * 1.005e3f));
+          p.heating_rate[(size_t)col + (size_t)ndp * lev] = hr;
+        }
+      }
+    }
+    if (kFP64 && p.heating_rate && !p.l_flux_div) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < L; i += nthreads) {
+        double hc = ld2(p.mass, col, i, ndp) * 1.005e3;
+        double fn0 = p.flux_down[(size_t)col + (size_t)ndp * i] - p.flux_up[(size_t)col + (size_t)ndp * i];
+        double fn1 = p.flux_down[(size_t)col + (size_t)ndp * (i + 1)] - p.flux_up[(size_t)col + (size_t)ndp * (i + 1)];
+        p.heating_rate[(size_t)col + (size_t)ndp * i] = 8.64e4 * ((fn0 - fn1) / hc);
+      }
+    }
+  }
+
+  // Grey optics, gas amounts and Planck terms of bands bstart..bstart+nb-1
+  // (radiance_calc.F90:883-1600 band loop; slot order).
+  __device__ static void stage_bands(const FluxParams &p, const Smem &S, int col, int bstart, int nb, bool lw) {
+    const int L = p.n_layer, ndp = p.nd_profile, ndl = p.nd_layer, nthreads = blockDim.x;
+    const int max_abs = p.max_abs;
+    for (int q = threadIdx.x; q < nb * LP; q += nthreads) {
+      const int bi = q / LP, s = q - bi * LP, b = bstart + bi;
+      const int i = layer_of_slot(s);
+      if (i >= L) continue;
       const BandInfo &bd = p.bands[b];
-      // grey optics: grey_opt_prop.F90:470-790 (Rayleigh, modal aerosol),
-      // computed in the kernel's working precision R
-      R kes = p.l_rayleigh ? (R)bd.rayleigh_coeff : R(0);
+      // grey optics: grey_opt_prop.F90:470-790 (Rayleigh, modal aerosol)
+      R kes = p.l_rayleigh ? (kFP64 ? (R)bd.rayleigh_coeff : (R)bd.rayleigh_f) : R(0);
       R kabs = R(0), phf = R(0), fwd = R(0);
       if (p.l_aerosol_mode) {
         for (int j = 0; j < p.n_mode; ++j) {
-          R mmr = (R)__ldg(p.mode_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * j));
+          R mmr = load_in<R>(p.mode_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * j));
           size_t q4 = (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * ((size_t)j + (size_t)p.nd_mode * b));
-          R g = (R)__ldg(p.mode_asymmetry + q4);
-          kabs = kabs + mmr * (R)__ldg(p.mode_absorption + q4);
-          R ks = mmr * (R)__ldg(p.mode_scattering + q4);
+          R g = load_in<R>(p.mode_asymmetry + q4);
+          kabs = kabs + mmr * load_in<R>(p.mode_absorption + q4);
+          R ks = mmr * load_in<R>(p.mode_scattering + q4);
           kes = kes + ks;
           phf = phf + ks * g;
           if (p.l_rescale) {
             R ks_phf = ks * g;
             if (p.n_order_forward == 1) fwd = fwd + ks_phf;
             else if (p.n_order_forward == 2) fwd = fwd + ks_phf * g;
-            else fwd = fwd + ks * (R)pow((double)g, (double)p.n_order_forward);
+            else {
+              R gp = R(1);
+              for (int o = 0; o < p.n_order_forward; ++o) gp *= g;
+              fwd = fwd + ks * gp;
+            }
           }
         }
       }
       R kgt = kabs + kes;     // grey_opt_prop.F90:773-790
-      if (MCICA) {
-        R *s_phf_nc = (R *)(smem + lay.off_phf_nc), *s_fwd_nc = (R *)(smem + lay.off_fwd_nc);
-        s_phf_nc[q] = phf;
-        s_fwd_nc[q] = fwd;
-      }
+      if (MCICA) { S.phf_nc[q] = phf; S.fwd_nc[q] = fwd; }
       R asym = phf, f = fwd;
-      if ((double)kes > kTiny64) {   // normalisation, grey_opt_prop.F90:840-880
+      if (kFP64 ? ((double)kes > kTiny64) : (kes > R(0))) {   // normalisation, grey_opt_prop.F90:840-880
         if (p.l_rescale) { R tinv = R(1) / kes; f = fwd * tinv; asym = phf * tinv; }
         else asym = phf / kes;
       }
       if (p.l_rescale) asym = (asym - f) / (R(1) - f);   // rescale_phase_fnc.F90:120-128
-      s_kgt[q] = kgt; s_kes[q] = kes; s_kabs[q] = kabs;
-      s_asym[q] = asym; s_fwd[q] = f;
+      S.kgt[q] = kgt; S.kes[q] = kes; S.kabs[q] = kabs; S.asym[q] = asym; S.fwd[q] = f;
       // gas amounts (radiance_calc.F90:1330-1470)
       const int n_abs_b = p.l_gas ? min(bd.n_abs, max_abs) : 0;
       for (int j = 0; j < n_abs_b; ++j) {
         const BandGas &gs = bd.gas[j];
-        R mmr = (R)__ldg(p.gas_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * gs.species));
+        R mmr = load_in<R>(p.gas_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * gs.species));
         R amt;
         if (gs.i_scale_k == SOCGPU_IP_SCALE_BAND) {
-          R gf = scale_factor<R>(gs.i_scale_fnc, s_p[i] , s_t[i], (R)gs.p_ref, (R)gs.t_ref, gs.scale,
-                                 gs.l_doppler, (R)gs.doppler_cor);
+          R gf;
+          if constexpr (kFP64)
+            gf = scale_factor_ref(gs.i_scale_fnc, S.p[s], S.t[s], gs.p_ref, gs.t_ref, gs.scale, gs.l_doppler,
+                                  gs.doppler_cor);
+          else
+            gf = scale_factor_mix(gs.i_scale_fnc, S.p[s], S.t[s], gs.p_ref_f, gs.t_ref_f, gs.scale_f,
+                                  gs.l_doppler, gs.doppler_cor_f);
           R v = gf * mmr;
           amt = v > R(0) ? v : R(0);
         } else {
           amt = mmr;   // ip_scale_null, or ip_scale_term (scaled per term below)
         }
-        s_amt[((size_t)bi * max_abs + j) * L + i] = amt;
+        S.amt[((size_t)bi * max_abs + j) * LP + s] = amt;
       }
     }
     if (lw) {
       // diff_planck_source (diff_planck_source_mod.F90:102-136)
-      for (int q = threadIdx.x; q < nb * (L + 1); q += nthreads) {
-        const int bi = q / (L + 1), i = q - bi * (L + 1);
-        const double *c = p.bands[b0 + bi].planck;
-        if constexpr (kFP64) {
-          s_planck[q] = planck_ref(c, p.n_deg_fit, ld2(p.t_level, col, i, ndp) / p.t_ref_planck);
-        } else {
-          float x = (float)(ld2(p.t_level, col, i, ndp) / p.t_ref_planck);
-          float f = (float)c[p.n_deg_fit];
-          for (int j = p.n_deg_fit - 1; j >= 0; --j) f = f * x + (float)c[j];
-          s_planck[q] = f;
-        }
+      for (int q = threadIdx.x; q < nb * (LP + 1); q += nthreads) {
+        const int bi = q / (LP + 1), s = q - bi * (LP + 1);
+        const int lev = (s == LP) ? 0 : layer_of_slot(s) + 1;
+        if (lev > L) continue;
+        const BandInfo &bd = p.bands[bstart + bi];
+        if constexpr (kFP64)
+          S.planck[q] = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_level, col, lev, ndp) / p.t_ref_planck);
+        else
+          S.planck[q] = planck_mix(bd.planck_f, p.n_deg_fit,
+                                   load_in<float>(p.t_level + (size_t)col + (size_t)ndp * lev) / p.t_ref_planck_f);
       }
-      for (int q = threadIdx.x; q < nb * L; q += nthreads) {
-        const int bi = q / L, i = q - bi * L;
-        const double *c = p.bands[b0 + bi].planck;
+      for (int q = threadIdx.x; q < nb * LP; q += nthreads) {
+        const int bi = q / LP, s = q - bi * LP;
+        const int i = layer_of_slot(s);
+        if (i >= L) continue;
+        const BandInfo &bd = p.bands[bstart + bi];
         if constexpr (kFP64) {
-          double b1 = planck_ref(c, p.n_deg_fit, ld2(p.t_level, col, i + 1, ndp) / p.t_ref_planck);
-          double bm = planck_ref(c, p.n_deg_fit, ld2(p.t_level, col, i, ndp) / p.t_ref_planck);
-          s_dB[q] = b1 - bm;
+          double b1 = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_level, col, i + 1, ndp) / p.t_ref_planck);
+          double bm = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_level, col, i, ndp) / p.t_ref_planck);
+          S.dB[q] = b1 - bm;
           if (p.l_ir_source_quad) {
-            double bl = planck_ref(c, p.n_deg_fit, ld2(p.t, col, i, ndp) / p.t_ref_planck);
-            s_dB2[q] = 2.0 * (b1 + bm - 2.0 * bl);
+            double bl = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t, col, i, ndp) / p.t_ref_planck);
+            S.dB2[q] = 2.0 * (b1 + bm - 2.0 * bl);
           }
         } else {
-          // differences of the polynomial without cancellation
-          float x1 = (float)(ld2(p.t_level, col, i + 1, ndp) / p.t_ref_planck);
-          float x0 = (float)(ld2(p.t_level, col, i, ndp) / p.t_ref_planck);
-          s_dB[q] = planck_diff_mix(c, p.n_deg_fit, x1, x0);
+          const float x1 = load_in<float>(p.t_level + (size_t)col + (size_t)ndp * (i + 1)) / p.t_ref_planck_f;
+          const float x0 = load_in<float>(p.t_level + (size_t)col + (size_t)ndp * i) / p.t_ref_planck_f;
+          S.dB[q] = planck_diff_mix(bd.planck_f, p.n_deg_fit, x1, x0);
           if (p.l_ir_source_quad) {
-            float xl = (float)(ld2(p.t, col, i, ndp) / p.t_ref_planck);
-            s_dB2[q] = 2.0f * (planck_diff_mix(c, p.n_deg_fit, x1, xl) + planck_diff_mix(c, p.n_deg_fit, x0, xl));
+            const float xl = S.t[s] / p.t_ref_planck_f;
+            S.dB2[q] = 2.0f * (planck_diff_mix(bd.planck_f, p.n_deg_fit, x1, xl) +
+                               planck_diff_mix(bd.planck_f, p.n_deg_fit, x0, xl));
           }
         }
-      }
-    }
-    if (MCICA) stage_clouds(p, lay, smem, col, nb, b0);
-    __syncthreads();
-
-    // ---------------- phase 2: g-point solves ---------------------------------
-    const int gid = threadIdx.x / P;
-    const int r = threadIdx.x % P;
-    const R sec0 = p.zen_0 ? (R)ld2(p.zen_0, col, 0, ndp) : R(1);
-    Acc *acc = s_acc + (size_t)gid * (L + 1) * kNumAcc;
-    // Every group of every warp runs the same number of rounds so that the
-    // full-warp shuffles of the scans always see all 32 lanes; a group with
-    // no g-point left in the last round solves g_begin and discards it.
-    const int rounds = (p.g_end - p.g_begin + n_groups - 1) / n_groups;
-    for (int rd = 0; rd < rounds; ++rd) {
-      int g = p.g_begin + rd * n_groups + gid;
-      const bool active = g < p.g_end;
-      if (!active) g = p.g_begin;
-      solve_gpoint(p, lay, smem, col, g, b0, max_abs, sec0, r, acc, lw, active);
-    }
-    __syncthreads();
-
-    // ---------------- phase 3: reduce over groups, write ------------------------
-    for (int lev = threadIdx.x; lev <= L; lev += nthreads) {
-      Acc up = Acc(0), dn = Acc(0), dir = Acc(0), dv = Acc(0);
-      for (int q = 0; q < n_groups; ++q) {
-        const Acc *a = s_acc + ((size_t)q * (L + 1) + lev) * kNumAcc;
-        up += a[0]; dn += a[1]; dir += a[2]; dv += a[3];
-      }
-      if (lw) {    // adjust_ir_radiance.F90:75-95
-        for (int bi = 0; bi < nb; ++bi) {
-          Acc wb = p.weight_band ? (Acc)p.weight_band[b0 + bi] : Acc(1);
-          Acc bw = s_planck[bi * (L + 1) + lev] * wb;
-          up += bw; dn += bw;
-        }
-      }
-      size_t o = (size_t)col + (size_t)ndp * lev;
-      p.flux_up[o] = (double)up;
-      p.flux_down[o] = (double)dn;
-      if (p.flux_direct) p.flux_direct[o] = lw ? 0.0 : (double)dir;
-      if (lev < L && p.flux_div) p.flux_div[(size_t)col + (size_t)ndp * lev] = (double)dv;
-    }
-    if (p.heating_rate) {
-      __syncthreads();
-      for (int i = threadIdx.x; i < L; i += nthreads) {
-        double hc = ld2(p.mass, col, i, ndp) * 1.005e3;
-        double hr;
-        if (p.l_flux_div && p.flux_div) {
-          hr = 8.64e4 * p.flux_div[(size_t)col + (size_t)ndp * i] / hc;
-        } else {
-          double fn0 = p.flux_down[(size_t)col + (size_t)ndp * i] - p.flux_up[(size_t)col + (size_t)ndp * i];
-          double fn1 = p.flux_down[(size_t)col + (size_t)ndp * (i + 1)] - p.flux_up[(size_t)col + (size_t)ndp * (i + 1)];
-          hr = 8.64e4 * ((fn0 - fn1) / hc);
-        }
-        p.heating_rate[(size_t)col + (size_t)ndp * i] = hr;
       }
     }
   }
 
-  // Cloud-component optics of every (band, layer) of the column through
-  // opt_prop_pade_2 (opt_prop_pade_2_mod.F90:99-140), plus the column's
-  // cloud fractions and subcolumn scalings.
-  __device__ static void stage_clouds(const FluxParams &p, const SmemLayout &lay, unsigned char *smem,
-                                      int col, int nb, int b0) {
+  // Per-band boundary values (solve_band_random_overlap.F90:565-600,
+  // column_solver.F90): incident fluxes, surface albedos and emission.
+  __device__ static void stage_boundary(const FluxParams &p, const Smem &S, int col, int bstart, int nb, bool lw) {
+    const int L = p.n_layer, ndp = p.nd_profile;
+    for (int bi = threadIdx.x; bi < nb; bi += blockDim.x) {
+      const int b = bstart + bi;
+      const BandInfo &bd = p.bands[b];
+      R *v = S.bscal + bi * kBandScal;
+      v[2] = load_in<R>(p.rho_alb + (size_t)col + (size_t)ndp * (0 + 2 * (size_t)b));
+      v[3] = load_in<R>(p.rho_alb + (size_t)col + (size_t)ndp * (1 + 2 * (size_t)b));
+      v[5] = p.weight_band ? load_in<R>(p.weight_band + b) : R(1);
+      if (lw) {
+        v[0] = -S.planck[bi * (LP + 1) + LP];
+        v[1] = R(0);
+        if constexpr (kFP64) {
+          double bg = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_ground, col, 0, ndp) / p.t_ref_planck);
+          v[4] = bg - S.planck[bi * (LP + 1) + level_slot(L)];
+        } else {
+          v[4] = planck_diff_mix(bd.planck_f, p.n_deg_fit, load_in<float>(p.t_ground + col) / p.t_ref_planck_f,
+                                 load_in<float>(p.t_level + (size_t)col + (size_t)ndp * L) / p.t_ref_planck_f);
+        }
+      } else {
+        if constexpr (kFP64) {
+          double sib = ld2(p.solar_irrad, col, 0, ndp) * bd.solar_flux_band;
+          v[0] = sib / ld2(p.zen_0, col, 0, ndp);
+        } else {
+          v[0] = load_in<float>(p.solar_irrad + col) * bd.solar_flux_band_f / load_in<float>(p.zen_0 + col);
+        }
+        v[1] = v[0];
+        v[4] = R(0);
+      }
+    }
+  }
+
+  // Cloud-component optics of bands bstart..bstart+nb-1 through
+  // opt_prop_pade_2 (opt_prop_pade_2_mod.F90:99-140).
+  __device__ static void stage_cloud_bands(const FluxParams &p, const Smem &S, int col, int bstart, int nb) {
     const int L = p.n_layer, ndp = p.nd_profile, ndl = p.nd_layer, ict = p.id_ct;
     const int ndc = ndl - ict, nc = p.n_condensed;
-    R *ke = (R *)(smem + lay.off_c_ke), *ks = (R *)(smem + lay.off_c_ks), *ka = (R *)(smem + lay.off_c_ka);
-    R *ph = (R *)(smem + lay.off_c_phf), *fw = (R *)(smem + lay.off_c_fwd);
-    R *wc = (R *)(smem + lay.off_wcld), *fr = (R *)(smem + lay.off_frac), *cs = (R *)(smem + lay.off_csub);
-    for (int q = threadIdx.x; q < nb * nc * L; q += blockDim.x) {
-      const int i = q % L, k = (q / L) % nc, bi = q / (L * nc);
-      double vke = 0.0, vks = 0.0, vka = 0.0, vph = 0.0, vfw = 0.0;
-      if (i >= ict) {
-        size_t qc = (size_t)col + (size_t)ndp * (size_t)(i - ict);
-        double w = __ldg(p.w_cloud + qc);
-        if (w > 0.0) {
-          const double *cp = (p.comp_phase[k] == SOCGPU_IP_PHASE_WATER ? p.drop_parm : p.ice_parm)
-                             + ((size_t)p.comp_parm_index[k] * p.n_band + (b0 + bi)) * kPadeParm;
-          double qm = __ldg(p.condensed_mix_ratio + qc + (size_t)ndp * ndc * k);
-          double re = __ldg(p.condensed_dim_char + qc + (size_t)ndp * ndc * k);
-          double kext = qm * (cp[0] + re * (cp[1] + re * cp[2]))
-                        / (1.0e+00 + re * (cp[3] + re * (cp[4] + re * cp[5])));
-          double coalb = (cp[6] + re * (cp[7] + re * cp[8])) / (1.0e+00 + re * (cp[9] + re * cp[10]));
-          double kscat = kext * (1.0e+00 - coalb);
-          double g = (cp[11] + re * (cp[12] + re * cp[13])) / (1.0e+00 + re * (cp[14] + re * cp[15]));
+    for (int q = threadIdx.x; q < nb * nc * LP; q += blockDim.x) {
+      const int s = q % LP, k = (q / LP) % nc, bi = q / (LP * nc);
+      const int i = layer_of_slot(s);
+      R vke = R(0), vks = R(0), vka = R(0), vph = R(0), vfw = R(0);
+      if (i < L && i >= ict) {
+        const size_t qc = (size_t)col + (size_t)ndp * (size_t)(i - ict);
+        if (load_in<R>(p.w_cloud + qc) > R(0)) {
+          const size_t po = ((size_t)p.comp_parm_index[k] * p.n_band + (bstart + bi)) * kPadeParm;
+          R qm = load_in<R>(p.condensed_mix_ratio + qc + (size_t)ndp * ndc * k);
+          R re = load_in<R>(p.condensed_dim_char + qc + (size_t)ndp * ndc * k);
+          R cp[kPadeParm];
+          if constexpr (kFP64) {
+            const double *c = (p.comp_phase[k] == SOCGPU_IP_PHASE_WATER ? p.drop_parm : p.ice_parm) + po;
+            for (int m = 0; m < kPadeParm; ++m) cp[m] = c[m];
+          } else {
+            const float *c = (p.comp_phase[k] == SOCGPU_IP_PHASE_WATER ? p.drop_parm_f : p.ice_parm_f) + po;
+            for (int m = 0; m < kPadeParm; ++m) cp[m] = c[m];
+          }
+          R kext = qm * (cp[0] + re * (cp[1] + re * cp[2])) / (R(1) + re * (cp[3] + re * (cp[4] + re * cp[5])));
+          R coalb = (cp[6] + re * (cp[7] + re * cp[8])) / (R(1) + re * (cp[9] + re * cp[10]));
+          R kscat = kext * (R(1) - coalb);
+          R g = (cp[11] + re * (cp[12] + re * cp[13])) / (R(1) + re * (cp[14] + re * cp[15]));
           vke = kext; vks = kscat; vka = kext * coalb; vph = kscat * g; vfw = kscat * g * g;
         }
       }
-      ke[q] = (R)vke; ks[q] = (R)vks; ka[q] = (R)vka; ph[q] = (R)vph; fw[q] = (R)vfw;
+      S.c_ke[q] = vke; S.c_ks[q] = vks; S.c_ka[q] = vka; S.c_phf[q] = vph; S.c_fwd[q] = vfw;
     }
-    for (int i = threadIdx.x; i < L; i += blockDim.x) {
-      double w = 0.0, f1 = 0.0, f2 = 0.0;
-      if (i >= ict) {
+  }
+
+  // The column's cloud fractions and subcolumn scalings.
+  __device__ static void stage_cloud_column(const FluxParams &p, const Smem &S, int col) {
+    const int L = p.n_layer, ndp = p.nd_profile, ndl = p.nd_layer, ict = p.id_ct;
+    const int ndc = ndl - ict;
+    for (int s = threadIdx.x; s < LP; s += blockDim.x) {
+      const int i = layer_of_slot(s);
+      R w = R(0), f1 = R(0), f2 = R(0);
+      if (i < L && i >= ict) {
         size_t qc = (size_t)col + (size_t)ndp * (size_t)(i - ict);
-        w = __ldg(p.w_cloud + qc);
-        f1 = __ldg(p.frac_cloud + qc);
-        if (p.n_cloud_type > 1) f2 = __ldg(p.frac_cloud + qc + (size_t)ndp * ndc);
+        w = load_in<R>(p.w_cloud + qc);
+        f1 = load_in<R>(p.frac_cloud + qc);
+        if (p.n_cloud_type > 1) f2 = load_in<R>(p.frac_cloud + qc + (size_t)ndp * ndc);
       }
-      wc[i] = (R)w; fr[i] = (R)f1; fr[L + i] = (R)f2;
+      S.wcld[s] = w; S.frac[s] = f1; S.frac[LP + s] = f2;
     }
-    for (int q = threadIdx.x; q < p.n_subcol_gen * L; q += blockDim.x) {
-      const int i = q % L, s = q / L;
-      double v = 0.0;
-      if (i >= ict) v = __ldg(p.c_sub + (size_t)col + (size_t)ndp * ((size_t)(i - ict) + (size_t)ndc * s));
-      cs[q] = (R)v;
+    for (int q = threadIdx.x; q < p.n_subcol_gen * LP; q += blockDim.x) {
+      const int s = q % LP, sub = q / LP;
+      const int i = layer_of_slot(s);
+      R v = R(0);
+      if (i < L && i >= ict) v = load_in<R>(p.c_sub + (size_t)col + (size_t)ndp * ((size_t)(i - ict) + (size_t)ndc * sub));
+      S.csub[q] = v;
     }
   }
 
@@ -507,25 +675,30 @@ struct FluxKernel {
     return t;
   }
 
-  // Gas absorption of a g-point at layer i (gas_optical_properties.F90:80-95).
+  // Gas absorption of a g-point at slot s (gas_optical_properties.F90:80-95).
   __device__ static __forceinline__ R gas_k(const GasTerm &gt, const GPoint &gp, const BandInfo &bd,
-                                            const R *amt, int L, int i, R pl, R tl) {
+                                            const R *amt, int s, R pl, R tl) {
     R kg = R(0);
     if (!gt.any_term) {
 #pragma unroll
       for (int j = 0; j < kMaxAbsPerBand; ++j)
         if (j < gt.n_abs) {
-          R kal = gt.k[j] * amt[(size_t)j * L + i];
+          R kal = gt.k[j] * amt[(size_t)j * LP + s];
           kg = (j == 0) ? kal : kg + kal;
         }
       return kg;
     }
     for (int j = 0; j < gt.n_abs; ++j) {
-      R a = amt[(size_t)j * L + i];
+      R a = amt[(size_t)j * LP + s];
       R kal;
       if (bd.gas[j].i_scale_k == SOCGPU_IP_SCALE_TERM) {
-        R gf = scale_factor<R>(bd.gas[j].i_scale_fnc, pl, tl, (R)bd.gas[j].p_ref, (R)bd.gas[j].t_ref,
-                               gp.term_scale[j], bd.gas[j].l_doppler, (R)bd.gas[j].doppler_cor);
+        R gf;
+        if constexpr (kFP64)
+          gf = scale_factor_ref(bd.gas[j].i_scale_fnc, pl, tl, bd.gas[j].p_ref, bd.gas[j].t_ref, gp.term_scale[j],
+                                bd.gas[j].l_doppler, bd.gas[j].doppler_cor);
+        else
+          gf = scale_factor_mix(bd.gas[j].i_scale_fnc, pl, tl, bd.gas[j].p_ref_f, bd.gas[j].t_ref_f,
+                                gp.term_scale_f[j], bd.gas[j].l_doppler, bd.gas[j].doppler_cor_f);
         R v = gf * a;
         kal = gt.k[j] * (v > R(0) ? v : R(0));
       } else {
@@ -537,54 +710,29 @@ struct FluxKernel {
   }
 
   // One g-point of one column (all its subcolumns under McICA).
-  __device__ static void solve_gpoint(const FluxParams &p, const SmemLayout &lay, unsigned char *smem,
-                                      int col, int g, int b0, int max_abs, R sec0, int r, Acc *acc,
-                                      bool lw, bool active) {
-    const int L = p.n_layer, ndp = p.nd_profile;
+  __device__ static void solve_gpoint(const FluxParams &p, const Smem &S, int col, int g, int bstart, int max_abs,
+                                      R sec0, int r, Acc *acc, bool lw, bool active) {
+    const int L = p.n_layer;
     const GPoint &gp = p.gpoints[g];
-    const int b = gp.band, bi = b - b0;
+    const int b = gp.band, bi = b - bstart;
     const BandInfo &bd = p.bands[b];
-    const double wb = p.weight_band ? p.weight_band[b] : 1.0;
-    const R w_g = (R)(wb * gp.weight);
+    const R *bs = S.bscal + bi * kBandScal;
+    const R w_g = kFP64 ? (R)(bs[5] * gp.weight) : (R)(bs[5] * gp.weight_f);
     const GasTerm gt = load_gas(gp, bd, max_abs);
-    const R *s_p = (const R *)(smem + lay.off_p), *s_t = (const R *)(smem + lay.off_t);
-    const R *s_mass = (const R *)(smem + lay.off_mass);
-    const R *kgt_b = (const R *)(smem + lay.off_kgt) + (size_t)bi * L;
-    const R *kes_b = (const R *)(smem + lay.off_kes) + (size_t)bi * L;
-    const R *kabs_b = (const R *)(smem + lay.off_kabs) + (size_t)bi * L;
-    const R *asym_b = (const R *)(smem + lay.off_asym) + (size_t)bi * L;
-    const R *fwd_b = (const R *)(smem + lay.off_fwd) + (size_t)bi * L;
-    const R *amt_b = (const R *)(smem + lay.off_amt) + (size_t)bi * max_abs * L;
-    const R *planck_b = (const R *)(smem + lay.off_planck) + (size_t)bi * (L + 1);
-    const R *dB2_b = (const R *)(smem + lay.off_dB2) + (size_t)bi * L;
-    const R *dB_b = (const R *)(smem + lay.off_dB) + (size_t)bi * L;
-
-    // boundary conditions (solve_band_random_overlap.F90:565-600, column_solver.F90)
-    R f_inc_down, f_inc_dir, alb_diff, alb_dir, dB_surf = R(0);
-    alb_diff = (R)__ldg(p.rho_alb + (size_t)col + (size_t)ndp * (0 + 2 * (size_t)b));
-    alb_dir = (R)__ldg(p.rho_alb + (size_t)col + (size_t)ndp * (1 + 2 * (size_t)b));
-    if (lw) {
-      f_inc_dir = R(0);
-      f_inc_down = -planck_b[0];
-      double bg = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_ground, col, 0, ndp) / p.t_ref_planck);
-      if constexpr (kFP64) dB_surf = bg - planck_b[L];
-      else dB_surf = (R)planck_diff_mix(bd.planck, p.n_deg_fit,
-                                        (float)(ld2(p.t_ground, col, 0, ndp) / p.t_ref_planck),
-                                        (float)(ld2(p.t_level, col, L, ndp) / p.t_ref_planck));
-    } else {
-      double sib = ld2(p.solar_irrad, col, 0, ndp) * bd.solar_flux_band;
-      f_inc_down = (R)(sib / (double)sec0);
-      f_inc_dir = f_inc_down;
-    }
+    const R *kgt_b = S.kgt + (size_t)bi * LP, *kes_b = S.kes + (size_t)bi * LP;
+    const R *kabs_b = S.kabs + (size_t)bi * LP, *asym_b = S.asym + (size_t)bi * LP;
+    const R *fwd_b = S.fwd + (size_t)bi * LP, *amt_b = S.amt + (size_t)bi * max_abs * LP;
+    const R *dB_b = S.dB + (size_t)bi * LP, *dB2_b = S.dB2 + (size_t)bi * LP;
+    const R f_inc_down = bs[0], f_inc_dir = bs[1], alb_diff = bs[2], alb_dir = bs[3], dB_surf = bs[4];
 
     if (!MCICA) {
       R T[CH], Rf[CH], T0[CH], c1[CH], c2[CH], om[CH];
 #pragma unroll
       for (int j = 0; j < CH; ++j) {
-        const int i = r * CH + j;
+        const int i = r * CH + j, s = j * P + r;
         if (i < L) {
-          R kg = p.l_gas ? gas_k(gt, gp, bd, amt_b, L, i, s_p[i], s_t[i]) : R(0);
-          cell_coef(p, kgt_b[i], kes_b[i], kabs_b[i], kg, s_mass[i], asym_b[i], fwd_b[i], sec0,
+          R kg = p.l_gas ? gas_k(gt, gp, bd, amt_b, s, S.p[s], S.t[s]) : R(0);
+          cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kg, S.mass[s], asym_b[s], fwd_b[s], sec0,
                     T[j], Rf[j], T0[j], c1[j], c2[j], om[j]);
         } else {
           T[j] = R(1); Rf[j] = R(0); T0[j] = R(1); c1[j] = R(0); c2[j] = R(0); om[j] = R(0);
@@ -593,46 +741,36 @@ struct FluxKernel {
       solve_column(p, T, Rf, T0, c1, c2, om, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
                    alb_diff, alb_dir, dB_surf, w_g, acc, active);
     } else {
-      solve_mcica(p, lay, smem, col, gp, gt, bd, bi, b, r, L, lw, sec0, dB_b, dB2_b, f_inc_down, f_inc_dir,
+      solve_mcica(p, S, col, gp, gt, bd, bi, b, r, L, lw, sec0, dB_b, dB2_b, f_inc_down, f_inc_dir,
                   alb_diff, alb_dir, dB_surf, w_g, acc, max_abs, active);
     }
   }
 
-  __device__ static void solve_mcica(const FluxParams &p, const SmemLayout &lay, unsigned char *smem,
-                                     int col, const GPoint &gp, const GasTerm &gt, const BandInfo &bd,
-                                     int bi, int b, int r,
-                                     int L, bool lw, R sec0, const R *dB_b, const R *dB2_b,
-                                     R f_inc_down, R f_inc_dir, R alb_diff, R alb_dir, R dB_surf,
-                                     R w_g, Acc *acc, int max_abs, bool active) {
+  __device__ static void solve_mcica(const FluxParams &p, const Smem &S, int col, const GPoint &gp,
+                                     const GasTerm &gt, const BandInfo &bd, int bi, int b, int r, int L, bool lw,
+                                     R sec0, const R *dB_b, const R *dB2_b, R f_inc_down, R f_inc_dir,
+                                     R alb_diff, R alb_dir, R dB_surf, R w_g, Acc *acc, int max_abs,
+                                     bool active) {
     const int ndp = p.nd_profile, nc = p.n_condensed;
-    const R *s_p = (const R *)(smem + lay.off_p), *s_t = (const R *)(smem + lay.off_t);
-    const R *s_mass = (const R *)(smem + lay.off_mass);
-    const R *kgt_b = (const R *)(smem + lay.off_kgt) + (size_t)bi * L;
-    const R *kes_b = (const R *)(smem + lay.off_kes) + (size_t)bi * L;
-    const R *kabs_b = (const R *)(smem + lay.off_kabs) + (size_t)bi * L;
-    const R *asym_b = (const R *)(smem + lay.off_asym) + (size_t)bi * L;
-    const R *fwd_b = (const R *)(smem + lay.off_fwd) + (size_t)bi * L;
-    const R *amt_b = (const R *)(smem + lay.off_amt) + (size_t)bi * max_abs * L;
-    const R *phf_nc = (const R *)(smem + lay.off_phf_nc) + (size_t)bi * L;
-    const R *fwd_nc = (const R *)(smem + lay.off_fwd_nc) + (size_t)bi * L;
-    const R *c_ke = (const R *)(smem + lay.off_c_ke) + (size_t)bi * nc * L;
-    const R *c_ks = (const R *)(smem + lay.off_c_ks) + (size_t)bi * nc * L;
-    const R *c_ka = (const R *)(smem + lay.off_c_ka) + (size_t)bi * nc * L;
-    const R *c_ph = (const R *)(smem + lay.off_c_phf) + (size_t)bi * nc * L;
-    const R *c_fw = (const R *)(smem + lay.off_c_fwd) + (size_t)bi * nc * L;
-    const R *wc = (const R *)(smem + lay.off_wcld), *fr = (const R *)(smem + lay.off_frac);
-    const R *cs = (const R *)(smem + lay.off_csub);
+    const R *kgt_b = S.kgt + (size_t)bi * LP, *kes_b = S.kes + (size_t)bi * LP;
+    const R *kabs_b = S.kabs + (size_t)bi * LP, *asym_b = S.asym + (size_t)bi * LP;
+    const R *fwd_b = S.fwd + (size_t)bi * LP, *amt_b = S.amt + (size_t)bi * max_abs * LP;
+    const R *phf_nc = S.phf_nc + (size_t)bi * LP, *fwd_nc = S.fwd_nc + (size_t)bi * LP;
+    const R *c_ke = S.c_ke + (size_t)bi * nc * LP, *c_ks = S.c_ks + (size_t)bi * nc * LP;
+    const R *c_ka = S.c_ka + (size_t)bi * nc * LP, *c_ph = S.c_phf + (size_t)bi * nc * LP;
+    const R *c_fw = S.c_fwd + (size_t)bi * nc * LP;
 
     const int iex = gp.iex_major;
     const int first = __ldg(p.first_subcol_k + b + (size_t)p.nd_band_sp * iex);
     const int last = __ldg(p.first_subcol_k + b + (size_t)p.nd_band_sp * (iex + 1)) - 1;
     const int nsub = __ldg(p.subcol_k + b + (size_t)p.nd_band_sp * iex);
-    const R fcl = (R)ld2(p.frac_cloudy, col, 0, ndp);
+    const R fcl = load_in<R>(p.frac_cloudy + col);
     const int ncld = p.n_subcol_cld ? __ldg(p.n_subcol_cld + col) : 0;
     const int nfill = min(p.n_subcol_req, p.n_subcol_gen);
     // blending weights (mcica_sample.F90:862-925)
-    const R w_sub = w_g * fcl / (R)nsub;
+    const R w_sub = w_g * fcl / (R)(nsub > 0 ? nsub : 1);
     const R w_clr = w_g * (R(1) - fcl);
+    (void)ndp;
 
     // Solve index it = 0 is the clear solve, it = 1.. the subcolumns
     // first..last.  The count is made uniform over the warp (all groups
@@ -643,57 +781,57 @@ struct FluxKernel {
       const bool clear = (it == 0);
       const int m = first + it - 1;
       bool use = active && it < n_iter && (clear ? (w_clr != R(0)) : (w_sub != R(0)));
-      int slot = -1;
+      int slot_sub = -1;
       if (!clear) {
         int idx = (it < n_iter ? m : first) % p.n_subcol_req;
         if (idx == 0) idx = p.n_subcol_req;
         int j = __ldg(p.subcol_reorder + (idx - 1));
         if (p.n_subcol_cld && ncld > 0 && j > ncld && j <= nfill) j = (j - 1) % ncld + 1;
-        slot = j - 1;
-        if (slot < 0 || slot >= p.n_subcol_gen) {   // out-of-range table entry: report, solve clear
+        slot_sub = j - 1;
+        if (slot_sub < 0 || slot_sub >= p.n_subcol_gen) {   // out-of-range table entry: report, skip
           if (p.error_flag) atomicOr(p.error_flag, 1);
-          slot = -1;
+          slot_sub = -1;
           use = false;
         }
       }
       R T[CH], Rf[CH], T0[CH], c1[CH], c2[CH], om[CH];
 #pragma unroll
       for (int jj = 0; jj < CH; ++jj) {
-        const int i = r * CH + jj;
+        const int i = r * CH + jj, s = jj * P + r;
         if (i < L) {
-          R kg = p.l_gas ? gas_k(gt, gp, bd, amt_b, L, i, s_p[i], s_t[i]) : R(0);
-          R cs_i = (slot >= 0) ? cs[(size_t)slot * L + i] : R(0);
+          R kg = p.l_gas ? gas_k(gt, gp, bd, amt_b, s, S.p[s], S.t[s]) : R(0);
+          R cs_i = (slot_sub >= 0) ? S.csub[(size_t)slot_sub * LP + s] : R(0);
           bool cloudy = false;
-          if (slot >= 0 && wc[i] > R(0)) {
-            for (int t = 0; t < p.n_cloud_type; ++t) cloudy |= (cs_i * fr[(size_t)t * L + i] > R(0));
+          if (slot_sub >= 0 && S.wcld[s] > R(0)) {
+            for (int t = 0; t < p.n_cloud_type; ++t) cloudy |= (cs_i * S.frac[(size_t)t * LP + s] > R(0));
           }
           if (!cloudy) {
-            cell_coef(p, kgt_b[i], kes_b[i], kabs_b[i], kg, s_mass[i], asym_b[i], fwd_b[i], sec0,
+            cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kg, S.mass[s], asym_b[s], fwd_b[s], sec0,
                       T[jj], Rf[jj], T0[jj], c1[jj], c2[jj], om[jj]);
           } else {
             // mcica_sample.F90:472-560 then mcica_column.F90:336-470
             R sT = R(0), sR = R(0), sT0 = R(0), s1 = R(0), s2 = R(0), sO = R(0);
             for (int k = 0; k < nc; ++k) {
               const int t = p.comp_type[k] - 1;
-              const R fc = fr[(size_t)t * L + i];
+              const R fc = S.frac[(size_t)t * LP + s];
               if (!(cs_i * fc > R(0))) continue;
-              const size_t qk = (size_t)k * L + i;
-              R kgt = kgt_b[i] + c_ke[qk] * cs_i;
-              R kes = kes_b[i] + c_ks[qk] * cs_i;
-              R kab = kabs_b[i] + c_ka[qk] * cs_i;
+              const size_t qk = (size_t)k * LP + s;
+              R kgt = kgt_b[s] + c_ke[qk] * cs_i;
+              R kes = kes_b[s] + c_ks[qk] * cs_i;
+              R kab = kabs_b[s] + c_ka[qk] * cs_i;
               R asym, fwd;
-              const R eps = kFP64 ? (R)kEps64 : (R)kEps64;
+              const R eps = (R)kEps64;
               if (p.l_rescale) {
-                R fw = fwd_nc[i] + c_fw[qk] * cs_i;
+                R fw = fwd_nc[s] + c_fw[qk] * cs_i;
                 R den = kes - fw;
-                asym = (phf_nc[i] + c_ph[qk] * cs_i - fw) / (den > eps ? den : eps);
+                asym = (phf_nc[s] + c_ph[qk] * cs_i - fw) / (den > eps ? den : eps);
                 fwd = fw / (kes > eps ? kes : eps);
               } else {
-                asym = (phf_nc[i] + c_ph[qk] * cs_i) / (kes > eps ? kes : eps);
+                asym = (phf_nc[s] + c_ph[qk] * cs_i) / (kes > eps ? kes : eps);
                 fwd = R(0);
               }
               R tT, tR, tT0, t1, t2, tO;
-              cell_coef(p, kgt, kes, kab, kg, s_mass[i], asym, fwd, sec0, tT, tR, tT0, t1, t2, tO);
+              cell_coef(p, kgt, kes, kab, kg, S.mass[s], asym, fwd, sec0, tT, tR, tT0, t1, t2, tO);
               sT = sT + fc * tT; sR = sR + fc * tR; sT0 = sT0 + fc * tT0;
               s1 = s1 + fc * t1; s2 = s2 + fc * t2; sO = sO + fc * tO;
             }
@@ -714,8 +852,9 @@ struct FluxKernel {
                                       R (&c1)[CH], R (&c2)[CH], R (&om)[CH], int r, int L, bool lw,
                                       const R *dB_b, const R *dB2_b, R f_inc_down, R f_inc_dir,
                                       R alb_diff, R alb_dir, R dB_surf, R w, Acc *acc, bool active) {
-    // the last level a lane accumulates into: none when the solve is discarded
+    // the last layer a lane accumulates into: none when the solve is discarded
     const int L_acc = active ? L : -1;
+    Acc *acc_up = acc, *acc_dn = acc + (LP + 1), *acc_dir = acc + 2 * (LP + 1), *acc_div = acc + 3 * (LP + 1);
     // --- sources -------------------------------------------------------------
     // ssum = s_up + s_down of each layer: with om = 1 - T - R it gives the
     // layer's flux divergence (1-T-R)(F_dn(top) + F_up(bottom)) - ssum, the
@@ -737,7 +876,7 @@ struct FluxKernel {
       if (r == 0) excl = R(1);
       R fd = f_inc_dir * excl;
       fdir_bottom = f_inc_dir * __shfl_sync(0xffffffffu, incl, P - 1, P);
-      if (r == 0 && active) acc[0 * kNumAcc + 2] += w * fd;
+      if (r == 0 && active) acc_dir[LP] += w * fd;
 #pragma unroll
       for (int j = 0; j < CH; ++j) {
         const int i = r * CH + j;
@@ -745,19 +884,19 @@ struct FluxKernel {
         c1[j] = su; c2[j] = sd;
         ssum[j] = su + sd;
         fd = fd * T0[j];
-        if (i < L_acc) acc[(size_t)(i + 1) * kNumAcc + 2] += w * fd;
+        if (i < L_acc) acc_dir[j * P + r] += w * fd;
       }
     } else {
 #pragma unroll
       for (int j = 0; j < CH; ++j) {
-        const int i = r * CH + j;
+        const int i = r * CH + j, s = j * P + r;
         if (i < L) {
-          R dB = dB_b[i];
+          R dB = dB_b[s];
           R su, sd;
           if (p.l_ir_source_quad) {       // ir_source.F90:93-119
-            su = c1[j] * dB + c2[j] * dB2_b[i];
-            sd = -c1[j] * dB + c2[j] * dB2_b[i];
-            ssum[j] = R(2) * c2[j] * dB2_b[i];
+            su = c1[j] * dB + c2[j] * dB2_b[s];
+            sd = -c1[j] * dB + c2[j] * dB2_b[s];
+            ssum[j] = R(2) * c2[j] * dB2_b[s];
           } else {
             su = c1[j] * dB; sd = -su;
             ssum[j] = R(0);
@@ -808,17 +947,17 @@ struct FluxKernel {
         fu = top;
       }
       R fd = fdn_top;
-      if (r == 0 && active) { acc[0] += w * fu; acc[1] += w * fd; }
+      if (r == 0 && active) { acc_up[LP] += w * fu; acc_dn[LP] += w * fd; }
       R fu_prev = fu;
 #pragma unroll
       for (int j = 0; j < CH; ++j) {
-        const int i = r * CH + j;
+        const int i = r * CH + j, s = j * P + r;
         R fdn = c2[j] + T[j] * fd;
         if (i < L_acc) {
-          acc[(size_t)(i + 1) * kNumAcc + 0] += w * c1[j];
-          acc[(size_t)(i + 1) * kNumAcc + 1] += w * fdn;
-          if constexpr (kFP64) acc[(size_t)i * kNumAcc + 3] += w * (c1[j] - fu_prev + fd - fdn);
-          else acc[(size_t)i * kNumAcc + 3] += w * (om[j] * (fd + c1[j]) - ssum[j]);
+          acc_up[s] += w * c1[j];
+          acc_dn[s] += w * fdn;
+          if constexpr (kFP64) acc_div[s] += w * (c1[j] - fu_prev + fd - fdn);
+          else acc_div[s] += w * (om[j] * (fd + c1[j]) - ssum[j]);
         }
         fu_prev = c1[j];
         fd = fdn;
@@ -860,8 +999,7 @@ struct FluxKernel {
       alpha = bx.R1 + bx.Tu * alb_diff * D * bx.Td;
       S = bx.Su + bx.Tu * D * (src_ground + alb_diff * bx.Sd);
     }
-    // elimination inside the chunk (solver_homogen_direct.F90:94-110);
-    // beta, gamma, h overwrite T0, c1 and a copy kept in Rf-sized arrays.
+    // elimination inside the chunk (solver_homogen_direct.F90:94-110)
     R (&beta)[CH] = T0;   // the direct transmission is no longer needed
     R gam[CH];
 #pragma unroll
@@ -878,18 +1016,18 @@ struct FluxKernel {
     R fup = alpha * fdn + S;
     if (r == 0) {
       fdn = f_inc_down; fup = alpha * fdn + S;
-      if (active) { acc[0] += w * fup; acc[1] += w * fdn; }
+      if (active) { acc_up[LP] += w * fup; acc_dn[LP] += w * fdn; }
     }
 #pragma unroll
     for (int j = 0; j < CH; ++j) {
-      const int i = r * CH + j;
+      const int i = r * CH + j, s = j * P + r;
       R fu = beta[j] * (c1[j] + gam[j] * fdn);
       R fd = c2[j] + T[j] * fdn + Rf[j] * fu;
       if (i < L_acc) {
-        acc[(size_t)(i + 1) * kNumAcc + 0] += w * fu;
-        acc[(size_t)(i + 1) * kNumAcc + 1] += w * fd;
-        if constexpr (kFP64) acc[(size_t)i * kNumAcc + 3] += w * (fu - fup + fdn - fd);
-        else acc[(size_t)i * kNumAcc + 3] += w * (om[j] * (fdn + fu) - ssum[j]);
+        acc_up[s] += w * fu;
+        acc_dn[s] += w * fd;
+        if constexpr (kFP64) acc_div[s] += w * (fu - fup + fdn - fd);
+        else acc_div[s] += w * (om[j] * (fdn + fu) - ssum[j]);
       }
       fup = fu; fdn = fd;
     }

@@ -17,22 +17,37 @@ int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char
   // the smallest chunk of this P that covers the column is chosen by the
   // caller's ordering of shapes (ascending CH)
   done = true;
-  const int threads = cfg.warps_per_cta * 32;
-  const int n_groups = threads / S::P;
-  int nb = p.last_band - p.first_band + 1;
-  SmemLayout lay = make_layout<R, R>(p.n_layer, nb, p.max_abs, MCICA ? p.n_condensed : 0,
-                                     MCICA ? p.n_subcol_gen : 0, n_groups,
-                                     p.isolir == SOCGPU_IP_INFRA_RED, MCICA);
+  const int nb = p.last_band - p.first_band + 1;
+  int max_smem = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  // widest band batch (then most warps) whose staging fits in shared memory
+  int warps = cfg.warps_per_cta, batch = nb;
+  SmemLayout lay{};
+  for (;;) {
+    lay = make_layout<R>(S::P * S::CH, S::P, batch, p.max_abs, MCICA ? p.n_condensed : 0,
+                         MCICA ? p.n_subcol_gen : 0, warps * 32 / S::P, p.isolir == SOCGPU_IP_INFRA_RED, MCICA);
+    if ((long long)lay.bytes <= max_smem) break;
+    if (batch > 1) { --batch; continue; }
+    if (warps > 1) { warps /= 2; batch = nb; continue; }
+    snprintf(msg, len, "one band of %d layers needs %zu bytes of shared memory (limit %d)", p.n_layer, lay.bytes,
+             max_smem);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  const int threads = warps * 32;
+  FluxParams q = p;
+  q.band_batch = batch;
   auto kern = flux_kernel<R, MIX, S::P, S::CH, NOSCAT, MCICA>;
   if (lay.bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.bytes);
     if (e != cudaSuccess) {
+      cudaGetLastError();
       snprintf(msg, len, "shared memory request of %zu bytes refused: %s", lay.bytes, cudaGetErrorString(e));
       return SOCGPU_I_ERR_RANGE;
     }
   }
   if (p.n_profile <= 0) return 0;
-  kern<<<p.n_profile, threads, lay.bytes, st>>>(p);
+  kern<<<p.n_profile, threads, lay.bytes, st>>>(q);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -55,13 +70,6 @@ int launch_shapes(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, c
   return status;
 }
 
-// Bytes of shared memory one CTA needs (for the occupancy-aware tuner).
-template <class R>
-size_t smem_bytes(const FluxParams &p, int lanes, int warps, bool mcica) {
-  int nb = p.last_band - p.first_band + 1;
-  return make_layout<R, R>(p.n_layer, nb, p.max_abs, mcica ? p.n_condensed : 0, mcica ? p.n_subcol_gen : 0,
-                           warps * 32 / lanes, p.isolir == SOCGPU_IP_INFRA_RED, mcica).bytes;
-}
 
 }  // namespace socgpu
 

@@ -26,6 +26,7 @@ struct BandGas {
   int l_doppler;
   double p_ref, t_ref, doppler_cor;
   double scale[4]; // band scaling parameters (ip_scale_band)
+  float p_ref_f, t_ref_f, doppler_cor_f, scale_f[4];   // FP32 copies for the mixed kernels
 };
 
 struct BandInfo {
@@ -34,6 +35,8 @@ struct BandInfo {
   double solar_flux_band;     // fraction of the solar constant
   double rayleigh_coeff;      // m2/kg
   double planck[kMaxPlanckCoeff];
+  float rayleigh_f, solar_flux_band_f;
+  float planck_f[kMaxPlanckCoeff];
   BandGas gas[kMaxAbsPerBand];
 };
 
@@ -46,8 +49,10 @@ struct GPoint {
   float pad;
   double weight;                    // product weight of the term
   double k[kMaxAbsPerBand];         // k of each absorber's term
-  float kf[kMaxAbsPerBand];         // the same in FP32 for the mixed kernels
   double term_scale[kMaxAbsPerBand][4];   // per-term scaling parameters (ip_scale_term)
+  float weight_f;                   // FP32 copies for the mixed kernels
+  float kf[kMaxAbsPerBand];
+  float term_scale_f[kMaxAbsPerBand][4];
 };
 
 // Device-resident spectrum.
@@ -61,6 +66,7 @@ struct SpectrumDev {
   GPoint *gpoints;                  // [n_gpoint]
   double *drop_parm;                // [n_drop_type][n_band][16]
   double *ice_parm;                 // [n_ice_type][n_band][16]
+  float *drop_parm_f, *ice_parm_f;  // FP32 copies
   // host copies for validation
   int host_first_g[SOCGPU_MAX_BAND + 1];
 };
@@ -77,12 +83,15 @@ struct FluxParams {
   int n_profile, n_layer, nd_profile, nd_layer, id_ct;  // id_ct 0-based first cloudy layer
   int g_begin, g_end;               // g-point range of the band range
   int max_abs;                      // most absorbers of any band in the range (>= 1)
+  int band_batch;                   // bands staged in shared memory at a time (set by the launcher)
   // spectrum
   const BandInfo *bands;
   const GPoint *gpoints;
   const double *drop_parm, *ice_parm;
+  const float *drop_parm_f, *ice_parm_f;
   int n_band, n_deg_fit;
   double t_ref_planck;
+  float t_ref_planck_f;
   const double *weight_band;        // device copy, [n_band]
   // atm
   const double *p, *t, *t_level, *mass, *gas_mix_ratio;
