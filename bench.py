@@ -37,7 +37,7 @@ CONFIG = {"workload": "SW PIFM80 delta-Eddington direct+diffuse, Rayleigh + moda
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="socgpu", choices=["socgpu", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=N_COL, help="columns of the CPU baseline sample")
@@ -64,6 +64,9 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0:   # first sample before the timed region
+                time.sleep(0.02)
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
@@ -112,15 +115,17 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the flux kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "flux_kernel_sw_mixed_traffic.json"
+def profile_figures():
+    """Per-launch DRAM bytes and warp instructions of the mixed flux kernel,
+    read from the committed ncu summary (lines ``name: value``)."""
+    p = ROOT / "profiles" / "flux_kernel_sw_mixed_10000x100x48.md"
+    out = {}
     if p.exists():
-        try:
-            return json.loads(p.read_text())
-        except ValueError:
-            return None
-    return None
+        for line in p.read_text().splitlines():
+            key, _, val = line.strip().partition(":")
+            if key in ("dram_bytes_per_launch", "warp_instructions_per_launch") and val.strip().isdigit():
+                out[key] = int(val.strip())
+    return out
 
 
 def cpu_baseline(n_sample: int, min_seconds: float = 10.0):
@@ -303,7 +308,8 @@ def main():
         if st != 0:
             raise SystemExit(f"radiance_calc failed: {msg.value.decode()}")
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
-    h2d = case.input_bytes - (8 * N_COL)          # t_ground is not read on the solar path
+    # t_ground and t_level are not read on the solar path
+    h2d = case.input_bytes - case.tensor_bytes("t_ground") - case.tensor_bytes("t_level")
     d2h = case.output_bytes
     e2e = {"value": world * N_COL * g / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
@@ -312,13 +318,23 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     alg_bytes = h2d + d2h
     achieved = alg_bytes / (ms_mx * 1e-3) / 1e9
-    traffic = profile_traffic()
+    prof = profile_figures()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                "traffic": prof.get("dram_bytes_per_launch"),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes_per_launch": int(alg_bytes),
-                "note": "compulsory FP64 I/O of the batch over the mixed kernel's time; the fused kernel is bound "
-                        "by FP32/MUFU issue, not HBM"}
+                "note": "compulsory FP64 I/O of the batch (inputs the solar kernel reads + outputs) over the "
+                        "mixed kernel's CUDA-event time; the kernel is issue-bound, see issue_roofline"}
+    if "warp_instructions_per_launch" in prof:
+        sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+        clk_ghz = (clk.summary()["sm_mhz"] or 2070.0) / 1e3
+        issue_peak = sm_count * 4 * clk_ghz          # warp instructions per ns: 4 schedulers per SM
+        issue_achieved = prof["warp_instructions_per_launch"] / (ms_mx * 1e6)
+        roofline["issue_roofline"] = {
+            "achieved": issue_achieved, "peak": issue_peak, "unit": "G warp-instructions/s",
+            "frac": issue_achieved / issue_peak,
+            "note": "warp instructions per launch from the committed ncu summary over the live CUDA-event "
+                    "time; peak = SMs x 4 issue slots x median SM clock sampled during the timed region"}
     if rank == 0:
         cpu = cpu_baseline(args.cpu_sample, args.cpu_seconds)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -100,6 +100,10 @@ class DeviceCase:
         self.input_bytes = sum(t.numel() * t.element_size() for k, t in self.tensors.items() if not k.startswith("out_"))
         self.output_bytes = sum(t.numel() * t.element_size() for k, t in self.tensors.items() if k.startswith("out_"))
 
+    def tensor_bytes(self, name: str) -> int:
+        t = self.tensors.get(name)
+        return 0 if t is None else t.numel() * t.element_size()
+
     def run(self, stream_ptr: int = 0) -> None:
         msg = C.create_string_buffer(512)
         st = self.lib.socgpu_radiance_calc_device(
