@@ -340,6 +340,38 @@ SOCGPU_API int socgpu_cloud_gen_device(int nd_layer, int cloud_top, int n_layer,
                             int *n_subcol_cld, double *c_sub, int rng,
                             void *stream, char *msg, size_t msg_len);
 
+/* Most cloud layers (n_layer - cloud_top + 1) socgpu_cloud_gen_device_noalloc
+ * accepts: its scratch is a fixed array of 2 * 1024 + 2 ints (8 KB) in the
+ * library's device memory. */
+#define SOCGPU_NOALLOC_MAX_CLOUD_LAYERS 1024
+
+/* Allocation-free variant of socgpu_cloud_gen_device (extension: no
+ * counterpart in the reference, whose cloud_gen keeps its work in automatic
+ * arrays sized on every call, src/interface_core/socrates_cloud_gen.F90:
+ * 108-138).  Same arguments, same results bit for bit.  It makes no
+ * device allocation and no free, for callers that hold a fixed device-memory
+ * budget or whose streams must not meet the device-wide synchronisation of a
+ * free: its scratch (per-layer cloud flags and the batch's cloud layer range)
+ * is a fixed array in the library's device memory.
+ * - The first call on each device looks up that array's address; make it
+ *   once at set-up, outside any time-critical region.
+ * - n_layer - cloud_top + 1 above SOCGPU_NOALLOC_MAX_CLOUD_LAYERS is
+ *   rejected with SOCGPU_I_ERR_RANGE and a message; nothing is enqueued.
+ * - Every call clears the flags it uses on `stream` before use; nothing has to
+ *   be zeroed by the caller.
+ * - All calls on one device share the scratch: calls that overlap in time
+ *   (other streams or host threads, not ordered by the caller) race on it
+ *   and give wrong subcolumns.  Serialise them on one stream. */
+SOCGPU_API int socgpu_cloud_gen_device_noalloc(int nd_layer, int cloud_top, int n_layer, int nd_profile,
+                            int il1, int il2, int n_subcol, int n1, int n2,
+                            int ipph, int ioverlap, const int *rand_seed,
+                            const double *rlc_cf, const double *rlc_cw,
+                            const double *sigma_qcw, const double *avg_cf,
+                            const double *c_cloud, const double *c_ratio,
+                            const double *zf, const double *xcw,
+                            int *n_subcol_cld, double *c_sub, int rng,
+                            void *stream, char *msg, size_t msg_len);
+
 /* Kernel launches made by this thread since the library loaded (profiling
  * aid, extension). */
 SOCGPU_API long long socgpu_kernel_launch_count(void);

@@ -34,6 +34,7 @@ IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0,
 
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RNG_LCG, RNG_PHILOX = 0, 1
+NOALLOC_MAX_CLOUD_LAYERS = 1024   # SOCGPU_NOALLOC_MAX_CLOUD_LAYERS
 ABI_VERSION = 1
 
 _dp = C.POINTER(C.c_double)
@@ -116,6 +117,7 @@ ABI_FUNCTIONS = (
     "socgpu_abi_version", "socgpu_spectrum_register", "socgpu_spectrum_lookup", "socgpu_spectrum_n_gpoint",
     "socgpu_spectrum_release", "socgpu_radiance_calc", "socgpu_radiance_calc_device", "socgpu_cloud_gen",
     "socgpu_cloud_gen_device", "socgpu_kernel_launch_count", "socgpu_set_device", "socgpu_set_tile_config",
+    "socgpu_cloud_gen_device_noalloc",
 )
 
 _CALC_ARGS = [C.POINTER(Control), C.POINTER(Dimen), C.c_int, C.POINTER(Atm), C.POINTER(Cld), C.POINTER(Aer),
@@ -135,6 +137,7 @@ def declare(lib: C.CDLL) -> C.CDLL:
     lib.socgpu_radiance_calc_device.argtypes = _CALC_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]
     lib.socgpu_cloud_gen.argtypes = _GEN_ARGS + [C.c_char_p, C.c_size_t]
     lib.socgpu_cloud_gen_device.argtypes = _GEN_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]
+    lib.socgpu_cloud_gen_device_noalloc.argtypes = _GEN_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]
     lib.socgpu_kernel_launch_count.restype = C.c_longlong
     lib.socgpu_set_device.argtypes = [C.c_int]
     lib.socgpu_set_tile_config.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]

@@ -29,6 +29,12 @@ int launch_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, i
                      const double *avg_cf, const double *c_cloud, const double *c_ratio,
                      const double *zf, const double *xcw, int *n_subcol_cld, double *c_sub, int rng,
                      int *range_dev, cudaStream_t st, char *msg, size_t len);
+int launch_cloud_gen_noalloc(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2,
+                             int n_subcol, int n1, int n2, int ipph, int ioverlap, const int *rand_seed,
+                             const double *rlc_cf, const double *rlc_cw, const double *sigma_qcw,
+                             const double *avg_cf, const double *c_cloud, const double *c_ratio,
+                             const double *zf, const double *xcw, int *n_subcol_cld, double *c_sub, int rng,
+                             cudaStream_t st, char *msg, size_t len);
 
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
@@ -738,6 +744,35 @@ int socgpu_cloud_gen_device(int nd_layer, int cloud_top, int n_layer, int nd_pro
   return launch_cloud_gen(nd_layer, cloud_top, n_layer, nd_profile, il1, il2, n_subcol, n1, n2, ipph, ioverlap,
                           rand_seed, rlc_cf, rlc_cw, sigma_qcw, avg_cf, c_cloud, c_ratio, zf, xcw, n_subcol_cld,
                           c_sub, rng, tl_ws.range, (cudaStream_t)stream, msg, msg_len);
+}
+
+// Same checks as socgpu_cloud_gen_device, then the allocation-free launcher:
+// no workspace, no allocation of any kind on this path.
+int socgpu_cloud_gen_device_noalloc(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2,
+                                    int n_subcol, int n1, int n2, int ipph, int ioverlap, const int *rand_seed,
+                                    const double *rlc_cf, const double *rlc_cw, const double *sigma_qcw,
+                                    const double *avg_cf, const double *c_cloud, const double *c_ratio,
+                                    const double *zf, const double *xcw, int *n_subcol_cld, double *c_sub,
+                                    int rng, void *stream, char *msg, size_t msg_len) {
+  if (ioverlap < 0 || ioverlap > 3) {
+    set_msg(msg, msg_len, "Choice of overlap not compatible with cloud generator");
+    return SOCGPU_I_ERR_FATAL;
+  }
+  if (rng != SOCGPU_RNG_LCG && rng != SOCGPU_RNG_PHILOX) { set_msg(msg, msg_len, "unknown rng %d", rng); return SOCGPU_I_ERR_FATAL; }
+  if (cloud_top < 1 || n_layer > nd_layer || il1 < 1 || il2 > nd_profile || n_subcol < 1) {
+    set_msg(msg, msg_len, "cloud_gen dimensions out of range"); return SOCGPU_I_ERR_RANGE; }
+  if (n_layer - cloud_top + 1 > SOCGPU_NOALLOC_MAX_CLOUD_LAYERS) {
+    set_msg(msg, msg_len, "%d cloud layers exceed the allocation-free limit of %d (SOCGPU_NOALLOC_MAX_CLOUD_LAYERS)",
+            n_layer - cloud_top + 1, SOCGPU_NOALLOC_MAX_CLOUD_LAYERS);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  if (ipph != 0 && (!xcw || !sigma_qcw || n1 < 2 || n2 < 2)) {
+    set_msg(msg, msg_len, "ipph needs the xcw table and sigma_qcw"); return SOCGPU_I_ERR_FATAL; }
+  if (!rand_seed || !rlc_cf || !rlc_cw || !avg_cf || !zf || !n_subcol_cld || !c_sub) {
+    set_msg(msg, msg_len, "missing cloud_gen argument"); return SOCGPU_I_ERR_FATAL; }
+  return launch_cloud_gen_noalloc(nd_layer, cloud_top, n_layer, nd_profile, il1, il2, n_subcol, n1, n2, ipph,
+                                  ioverlap, rand_seed, rlc_cf, rlc_cw, sigma_qcw, avg_cf, c_cloud, c_ratio, zf, xcw,
+                                  n_subcol_cld, c_sub, rng, (cudaStream_t)stream, msg, msg_len);
 }
 
 int socgpu_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2, int n_subcol,

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include "socgpu_internal.h"
 
 namespace socgpu {
@@ -218,6 +219,137 @@ int launch_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, i
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (blocks < 1) blocks = 1;
   cloud_range_kernel<<<blocks, 256, 0, st>>>(a);
+  count_launch();
+  cloud_gen_kernel<<<(ncol + 127) / 128, 128, 0, st>>>(a);
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(msg, len, "cloud_gen launch failed: %s", cudaGetErrorString(e));
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant (socgpu_cloud_gen_device_noalloc).
+//
+// Some callers cannot allocate device memory where they generate subcolumns:
+// a host model that gives the radiation scheme a fixed device-memory budget at
+// start-up and treats any later allocation as an error, or a time step whose
+// concurrent streams must not be serialised by the device-wide
+// synchronisation that cudaFree implies.  This variant keeps its scratch in a
+// fixed array of the library's own device memory instead of the per-thread
+// workspace, and makes no allocation of any kind.
+//
+// Layout of the scratch (ints), n = SOCGPU_NOALLOC_MAX_CLOUD_LAYERS:
+//   [0, n)       layer cloud_top + j holds cloud fraction >  cut in some column
+//   [n, 2n)      layer cloud_top + j holds cloud fraction >= cut in some column
+//   [2n, 2n + 2) k_top, k_base of the batch (read by cloud_gen_kernel)
+// The flags of the call's layers must be zero when cloud_layer_flag_kernel
+// runs: every call clears them itself on its own stream first, so no state
+// carries over from one call to the next.  The range slots are always written
+// by cloud_layer_range_kernel before cloud_gen_kernel reads them.  All calls on
+// one device share this array: calls that overlap in time (different streams
+// or host threads without ordering between them) race on it.
+namespace {
+
+constexpr int kNoAllocLayers = SOCGPU_NOALLOC_MAX_CLOUD_LAYERS;
+static __device__ __align__(256) int g_noalloc_scratch[2 * kNoAllocLayers + 2];
+
+// Which cloud layers hold cloud anywhere in the batch
+// (socrates_cloud_gen.F90:225-250, as flags instead of atomic min/max).
+__global__ void cloud_layer_flag_kernel(GenArgs a, int *flags, int ncl) {
+  const int ncol = a.il2 - a.il1 + 1;
+  const long long total = (long long)ncol * ncl;
+  const double cut = kEps64;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int il = a.il1 + (int)(q % ncol);
+    const int kk = (int)(q / ncol);
+    const double cf = a.avg_cf[(size_t)(il - 1) + (size_t)a.nd_profile * (size_t)kk];
+    if (cf > cut) flags[kk] = 1;
+    if (cf >= cut) flags[kNoAllocLayers + kk] = 1;
+  }
+}
+
+// Reduce the flags to the batch's first and last cloudy layer.
+__global__ void cloud_layer_range_kernel(const int *flags, int ncl, int cloud_top, int n_layer, int *range) {
+  __shared__ int s_top, s_base;
+  if (threadIdx.x == 0) { s_top = n_layer + 1; s_base = cloud_top - 1; }
+  __syncthreads();
+  for (int kk = threadIdx.x; kk < ncl; kk += blockDim.x) {
+    if (flags[kk]) atomicMin(&s_top, cloud_top + kk);
+    if (flags[kNoAllocLayers + kk]) atomicMax(&s_base, cloud_top + kk);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) { range[0] = s_top; range[1] = s_base; }
+}
+
+std::mutex g_noalloc_mutex;
+constexpr int kMaxDevices = 64;
+int *g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the scratch on the current device, looked up once per
+// device (the first call on a device does this setup).
+int noalloc_scratch(int **out, char *msg, size_t len) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    snprintf(msg, len, "no usable CUDA device: %s", cudaGetErrorString(e));
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      snprintf(msg, len, "address of the allocation-free scratch not available: %s", cudaGetErrorString(e));
+      return SOCGPU_I_ABORT_CALCULATION;
+    }
+    g_noalloc_addr[dev] = (int *)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return SOCGPU_I_NORMAL;
+}
+
+}  // namespace
+
+int launch_cloud_gen_noalloc(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2,
+                             int n_subcol, int n1, int n2, int ipph, int ioverlap, const int *rand_seed,
+                             const double *rlc_cf, const double *rlc_cw, const double *sigma_qcw,
+                             const double *avg_cf, const double *c_cloud, const double *c_ratio,
+                             const double *zf, const double *xcw, int *n_subcol_cld, double *c_sub, int rng,
+                             cudaStream_t st, char *msg, size_t len) {
+  const int ncl = n_layer - cloud_top + 1;
+  if (ncl > kNoAllocLayers) {
+    snprintf(msg, len, "%d cloud layers exceed the allocation-free limit of %d (SOCGPU_NOALLOC_MAX_CLOUD_LAYERS)",
+             ncl, kNoAllocLayers);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  int *scratch = nullptr;
+  int stat = noalloc_scratch(&scratch, msg, len);
+  if (stat != SOCGPU_I_NORMAL) return stat;
+  int *range = scratch + 2 * kNoAllocLayers;
+  GenArgs a{nd_layer, cloud_top, n_layer, nd_profile, il1, il2, n_subcol, n1, n2, ipph, ioverlap, rng,
+            rand_seed, rlc_cf, rlc_cw, sigma_qcw, avg_cf, c_cloud, c_ratio, zf, xcw, n_subcol_cld, c_sub,
+            range};
+  const int ncol = il2 - il1 + 1;
+  if (ncol <= 0) return SOCGPU_I_NORMAL;
+  if (ncl > 0) {
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(int) * ncl, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(scratch + kNoAllocLayers, 0, sizeof(int) * ncl, st);
+    if (e != cudaSuccess) {
+      snprintf(msg, len, "clearing the cloud layer flags failed: %s", cudaGetErrorString(e));
+      return SOCGPU_I_ABORT_CALCULATION;
+    }
+    long long cells = (long long)ncol * ncl;
+    int blocks = (int)((cells + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    cloud_layer_flag_kernel<<<blocks, 256, 0, st>>>(a, scratch, ncl);
+    count_launch();
+  }
+  cloud_layer_range_kernel<<<1, 256, 0, st>>>(scratch, ncl > 0 ? ncl : 0, cloud_top, n_layer, range);
   count_launch();
   cloud_gen_kernel<<<(ncol + 127) / 128, 128, 0, st>>>(a);
   count_launch();
