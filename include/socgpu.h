@@ -372,6 +372,58 @@ SOCGPU_API int socgpu_cloud_gen_device_noalloc(int nd_layer, int cloud_top, int 
                             int *n_subcol_cld, double *c_sub, int rng,
                             void *stream, char *msg, size_t msg_len);
 
+/* ---- multi-batch launches (extension) -----------------------------------
+ * Many column batches of different layer counts, spectra, options and
+ * precision in one replay.  The reference has no counterpart: its callers
+ * call radiance_calc once per batch (src/radiance_core/radiance_calc.F90:16),
+ * which socgpu_radiance_calc_device mirrors.  Every pointer of an item is
+ * device memory and must stay valid while the batch exists; the structs
+ * themselves are read at creation.  The batches are grouped into kernel
+ * classes (precision, mode, tile), each class runs as one persistent launch
+ * over all its columns, and the launches are captured in one CUDA graph. */
+typedef struct socgpu_batch_item {
+    const socgpu_control *control;
+    const socgpu_dimen *dimen;
+    socgpu_spectrum_handle spectrum;
+    const socgpu_atm *atm;
+    const socgpu_cld *cld;
+    const socgpu_aer *aer;
+    const socgpu_bound *bound;
+    socgpu_radout *radout;
+} socgpu_batch_item;
+
+typedef struct socgpu_batch_s *socgpu_batch;
+
+/* Validate every item (the checks of socgpu_radiance_calc), group, prepare
+ * and capture.  On error, msg names the failing item. */
+SOCGPU_API int socgpu_batch_create(const socgpu_batch_item *items, int n_items, socgpu_batch *batch,
+                                   char *msg, size_t msg_len);
+
+/* Replay all batches on `stream` (one graph launch). */
+SOCGPU_API int socgpu_batch_run(socgpu_batch batch, void *stream, char *msg, size_t msg_len);
+
+/* Autotuner: for every (precision, mode, layer count) of the batch, time
+ * each built tile (lanes per solve x smallest covering chunk x 4 or 8
+ * warps) on the batch's own data, `reps` timed launches each (<1: 3), keep
+ * the fastest in the library's tile table (used from then on by every entry
+ * point, unless socgpu_set_tile_config overrides it) and recapture.  The
+ * outputs are overwritten. */
+SOCGPU_API int socgpu_batch_tune(socgpu_batch batch, void *stream, int reps, char *msg, size_t msg_len);
+
+/* Kernel classes, columns and column x g-points of a batch. */
+SOCGPU_API int socgpu_batch_info(socgpu_batch batch, int *n_groups, long long *n_columns,
+                                 long long *n_column_gpoints);
+
+SOCGPU_API int socgpu_batch_destroy(socgpu_batch batch);
+
+/* The tile table (extension): read or set the entry for (precision, mode
+ * 0 lwns / 1 full / 2 mcica, n_layer); lanes_per_solve 0 removes it.  Lets
+ * a caller save the tuner's choices and restore them in a later process. */
+SOCGPU_API int socgpu_tune_get(int precision, int mode, int n_layer, int *lanes_per_solve,
+                               int *layers_per_lane, int *warps_per_cta);
+SOCGPU_API int socgpu_tune_set(int precision, int mode, int n_layer, int lanes_per_solve,
+                               int layers_per_lane, int warps_per_cta);
+
 /* Kernel launches made by this thread since the library loaded (profiling
  * aid, extension). */
 SOCGPU_API long long socgpu_kernel_launch_count(void);

@@ -113,11 +113,20 @@ class Radout(C.Structure):
     ]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [
+        ("control", C.POINTER(Control)), ("dimen", C.POINTER(Dimen)), ("spectrum", C.c_int32),
+        ("atm", C.POINTER(Atm)), ("cld", C.POINTER(Cld)), ("aer", C.POINTER(Aer)), ("bound", C.POINTER(Bound)),
+        ("radout", C.POINTER(Radout)),
+    ]
+
+
 ABI_FUNCTIONS = (
     "socgpu_abi_version", "socgpu_spectrum_register", "socgpu_spectrum_lookup", "socgpu_spectrum_n_gpoint",
     "socgpu_spectrum_release", "socgpu_radiance_calc", "socgpu_radiance_calc_device", "socgpu_cloud_gen",
     "socgpu_cloud_gen_device", "socgpu_kernel_launch_count", "socgpu_set_device", "socgpu_set_tile_config",
-    "socgpu_cloud_gen_device_noalloc",
+    "socgpu_cloud_gen_device_noalloc", "socgpu_batch_create", "socgpu_batch_run", "socgpu_batch_tune",
+    "socgpu_batch_info", "socgpu_batch_destroy", "socgpu_tune_get", "socgpu_tune_set",
 )
 
 _CALC_ARGS = [C.POINTER(Control), C.POINTER(Dimen), C.c_int, C.POINTER(Atm), C.POINTER(Cld), C.POINTER(Aer),
@@ -138,6 +147,16 @@ def declare(lib: C.CDLL) -> C.CDLL:
     lib.socgpu_cloud_gen.argtypes = _GEN_ARGS + [C.c_char_p, C.c_size_t]
     lib.socgpu_cloud_gen_device.argtypes = _GEN_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]
     lib.socgpu_cloud_gen_device_noalloc.argtypes = _GEN_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]
+    lib.socgpu_batch_create.argtypes = [C.POINTER(BatchItem), C.c_int, C.POINTER(C.c_void_p), C.c_char_p,
+                                        C.c_size_t]
+    lib.socgpu_batch_run.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]
+    lib.socgpu_batch_tune.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_char_p, C.c_size_t]
+    lib.socgpu_batch_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong),
+                                      C.POINTER(C.c_longlong)]
+    lib.socgpu_batch_destroy.argtypes = [C.c_void_p]
+    lib.socgpu_tune_get.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]
+    lib.socgpu_tune_set.argtypes = [C.c_int] * 6
     lib.socgpu_kernel_launch_count.restype = C.c_longlong
     lib.socgpu_set_device.argtypes = [C.c_int]
     lib.socgpu_set_tile_config.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]

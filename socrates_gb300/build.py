@@ -26,11 +26,29 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 # The generator mirrors the reference's FP64 branch decisions bit for bit:
 # no multiply-add contraction there.
 PER_FILE = {"cloud_gen.cu": ["-fmad=false"]}
+
+# flux_inst.cu is compiled once per (precision, mode, lanes); see its header.
 # The mixed-precision kernels trade IEEE division/square root for the fast
 # hardware forms (a few ulp in FP32); their error budget is set by the
 # flux/heating-rate tolerances, not by last-bit FP32 rounding.
-for _mode in ("lwns", "full", "mcica"):
-    PER_FILE[f"flux_mixed_{_mode}.cu"] = ["-use_fast_math"]
+FLUX_LANES = {0: (16, 32), 1: (8, 16, 32)}
+
+
+def units() -> list[tuple[Path, str, list[str]]]:
+    """(source, object stem, extra flags) of every object of the library."""
+    out = []
+    for src in sorted(CSRC.glob("*.cu")):
+        if src.name == "flux_inst.cu":
+            for prec, lanes_list in FLUX_LANES.items():
+                for mode in (0, 1, 2):
+                    for lanes in lanes_list:
+                        flags = [f"-DSOCGPU_PREC={prec}", f"-DSOCGPU_MODE={mode}", f"-DSOCGPU_LANES={lanes}"]
+                        if prec == 1:
+                            flags.append("-use_fast_math")
+                        out.append((src, f"flux_{prec}_{mode}_{lanes}", flags))
+        else:
+            out.append((src, src.stem, PER_FILE.get(src.name, [])))
+    return out
 
 
 def nvcc() -> str:
@@ -38,10 +56,6 @@ def nvcc() -> str:
         if cand and Path(cand).exists():
             return cand
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libsocgpu")
-
-
-def sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
 
 
 def _stale() -> bool:
@@ -52,12 +66,13 @@ def _stale() -> bool:
     return any(p.stat().st_mtime > t for p in deps)
 
 
-def _compile(src: Path, extra: list[str]) -> Path:
-    obj = BUILD / (src.stem + ".o")
-    cmd = [nvcc(), *ARCH, *COMMON, *PER_FILE.get(src.name, []), *extra, "-c", str(src), "-o", str(obj)]
+def _compile(unit: tuple[Path, str, list[str]], extra: list[str]) -> Path:
+    src, stem, flags = unit
+    obj = BUILD / (stem + ".o")
+    cmd = [nvcc(), *ARCH, *COMMON, *flags, *extra, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
+        raise RuntimeError(f"nvcc failed on {stem}:\n{r.stdout}\n{r.stderr}")
     return obj
 
 
@@ -66,10 +81,12 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if not force and not _stale():
         return LIB
     BUILD.mkdir(exist_ok=True)
-    srcs = sources()
-    jobs = min(len(srcs), os.cpu_count() or 4)
+    todo = units()
+    # the largest objects first, so the slowest compiles start early
+    todo.sort(key=lambda u: 0 if u[1].startswith("flux_") else 1)
+    jobs = min(len(todo), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra or []), srcs))
+        objs = list(ex.map(lambda u: _compile(u, extra or []), todo))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-Xlinker", "-rpath=/usr/local/cuda/lib64",
            *map(str, objs), "-o", str(tmp)]

@@ -17,6 +17,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "socgpu_internal.h"
@@ -264,30 +265,62 @@ SpectrumEntry *find_spectrum(int h) {
 }
 
 // ---------------------------------------------------------------------------
-// Tile configuration (set by the tuner; 0 = heuristic).
+// Kernel variants and tile choice.
+using LaunchFn = int (*)(const FluxParams &, const TileConfig &, cudaStream_t, char *, size_t);
+using PrepareFn = int (*)(BatchGroup &, char *, size_t);
+struct FluxVariant {
+  int precision, mode, lanes;
+  LaunchFn launch;
+  PrepareFn prepare;
+};
+#define SOCGPU_VARIANT(p, m, l) {p, m, l, launch_flux_##p##_##m##_##l, prepare_flux_##p##_##m##_##l}
+const FluxVariant kVariants[] = {
+    SOCGPU_VARIANT(0, 0, 16), SOCGPU_VARIANT(0, 0, 32), SOCGPU_VARIANT(0, 1, 16), SOCGPU_VARIANT(0, 1, 32),
+    SOCGPU_VARIANT(0, 2, 16), SOCGPU_VARIANT(0, 2, 32), SOCGPU_VARIANT(1, 0, 8),  SOCGPU_VARIANT(1, 0, 16),
+    SOCGPU_VARIANT(1, 0, 32), SOCGPU_VARIANT(1, 1, 8),  SOCGPU_VARIANT(1, 1, 16), SOCGPU_VARIANT(1, 1, 32),
+    SOCGPU_VARIANT(1, 2, 8),  SOCGPU_VARIANT(1, 2, 16), SOCGPU_VARIANT(1, 2, 32),
+};
+#undef SOCGPU_VARIANT
+
+const FluxVariant *find_variant(int precision, int mode, int lanes) {
+  for (const FluxVariant &v : kVariants)
+    if (v.precision == precision && v.mode == mode && v.lanes == lanes) return &v;
+  return nullptr;
+}
+
+// Tile overrides (socgpu_set_tile_config) and the tuner's table, keyed by
+// (precision, mode, n_layer).
 std::mutex g_tile_mutex;
 int g_tile[2][3][2] = {};   // [precision][mode][lanes, warps]
+std::map<std::tuple<int, int, int>, TileConfig> g_tuned;
 
 TileConfig choose_tile(int precision, int mode, int n_layer) {
   TileConfig t{};
+  bool tuned = false;
   {
     std::lock_guard<std::mutex> lk(g_tile_mutex);
     t.lanes_per_solve = g_tile[precision][mode][0];
     t.warps_per_cta = g_tile[precision][mode][1];
+    if (t.lanes_per_solve <= 0 && t.warps_per_cta <= 0) {
+      auto it = g_tuned.find(std::make_tuple(precision, mode, n_layer));
+      if (it != g_tuned.end()) { t = it->second; tuned = true; }
+    }
   }
-  if (t.lanes_per_solve <= 0) {
-    // measured on GB300: short chunks (few layers per lane) win over long
-    // ones -- fewer live registers and more resident warps
-    if (precision == SOCGPU_PRECISION_MIXED) t.lanes_per_solve = n_layer <= 64 ? 16 : 32;
-    else t.lanes_per_solve = n_layer <= 128 ? 16 : 32;
+  if (!tuned) {
+    if (t.lanes_per_solve <= 0) {
+      // measured on GB300: short chunks (few layers per lane) win over long
+      // ones -- fewer live registers and more resident warps
+      if (precision == SOCGPU_PRECISION_MIXED) t.lanes_per_solve = n_layer <= 64 ? 16 : 32;
+      else t.lanes_per_solve = n_layer <= 128 ? 16 : 32;
+    }
+    if (t.warps_per_cta <= 0) t.warps_per_cta = 8;
+    t.chunk = 0;
   }
   // the chunk must cover the column
-  int maxch = (precision == SOCGPU_PRECISION_MIXED && t.lanes_per_solve == 8) ? 18 : 16;
-  while (t.lanes_per_solve < 32 && t.lanes_per_solve * maxch < n_layer) {
+  while (t.lanes_per_solve < 32 && smallest_chunk(precision, t.lanes_per_solve, n_layer) == 0)
     t.lanes_per_solve *= 2;
-    maxch = 16;
-  }
-  if (t.warps_per_cta <= 0) t.warps_per_cta = 8;
+  if (t.chunk == 0 || t.lanes_per_solve * t.chunk < n_layer)
+    t.chunk = smallest_chunk(precision, t.lanes_per_solve, n_layer);
   return t;
 }
 
@@ -356,7 +389,9 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     set_msg(msg, msg_len, "solar calculation without zen_0/solar_irrad"); return SOCGPU_I_ERR_FATAL; }
   if (c->isolir == SOCGPU_IP_INFRA_RED && !bd->t_ground) {
     set_msg(msg, msg_len, "infra-red calculation without t_ground"); return SOCGPU_I_ERR_FATAL; }
-  if (!bd->rho_alb || !atm->p || !atm->t || !atm->t_level || !atm->mass || (c->l_gas && !atm->gas_mix_ratio)) {
+  // t_level feeds only the Planck terms of the infra-red
+  if (!bd->rho_alb || !atm->p || !atm->t || !atm->mass || (c->l_gas && !atm->gas_mix_ratio) ||
+      (c->isolir == SOCGPU_IP_INFRA_RED && !atm->t_level)) {
     set_msg(msg, msg_len, "missing atmospheric or surface field"); return SOCGPU_I_ERR_FATAL; }
   if (!out->flux_up || !out->flux_down) { set_msg(msg, msg_len, "missing output arrays"); return SOCGPU_I_ERR_FATAL; }
   if (out->flux_up_band || out->flux_down_band) {
@@ -453,14 +488,12 @@ int mode_index(const socgpu_control *c) {
 int launch(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *msg, size_t msg_len) {
   const int mode = mode_index(c);
   TileConfig t = choose_tile(c->precision, mode, p.n_layer);
-  if (c->precision == SOCGPU_PRECISION_FP64) {
-    if (mode == 0) return launch_flux_fp64_lwns(p, t, st, msg, msg_len);
-    if (mode == 1) return launch_flux_fp64_full(p, t, st, msg, msg_len);
-    return launch_flux_fp64_mcica(p, t, st, msg, msg_len);
+  const FluxVariant *v = find_variant(c->precision, mode, t.lanes_per_solve);
+  if (!v || t.chunk == 0) {
+    set_msg(msg, msg_len, "no kernel built for %d lanes per solve and %d layers", t.lanes_per_solve, p.n_layer);
+    return SOCGPU_I_ERR_RANGE;
   }
-  if (mode == 0) return launch_flux_mixed_lwns(p, t, st, msg, msg_len);
-  if (mode == 1) return launch_flux_mixed_full(p, t, st, msg, msg_len);
-  return launch_flux_mixed_mcica(p, t, st, msg, msg_len);
+  return v->launch(p, t, st, msg, msg_len);
 }
 
 // ---------------------------------------------------------------------------
@@ -530,6 +563,134 @@ struct Plan {
 }  // namespace socgpu
 
 using namespace socgpu;
+
+// ---------------------------------------------------------------------------
+// Multi-batch launches (socgpu_batch_*): the batches are grouped into kernel
+// classes (precision, mode, tile); each class runs as one persistent launch
+// over all its columns, and the launches are captured in one CUDA graph.
+struct socgpu_batch_s {
+  int device = 0;
+  std::vector<FluxParams> params;      // one per batch
+  std::vector<int> precision, mode;
+  std::vector<BatchGroup> groups;
+  std::vector<std::vector<FluxParams>> group_items;
+  std::vector<std::vector<long long>> group_start;
+  std::vector<FluxParams *> d_items;
+  std::vector<long long *> d_start;
+  char *dbuf = nullptr;
+  cudaStream_t capture = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long n_columns = 0, n_colg = 0;
+  ~socgpu_batch_s() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (dbuf) cudaFree(dbuf);
+    if (capture) cudaStreamDestroy(capture);
+  }
+};
+
+namespace {
+
+size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+// One group (kernel class) over the given batches with tile t: items copied,
+// column offsets, then the variant's prepare step.
+int make_group(socgpu_batch_s &b, const std::vector<int> &idx, int precision, int mode, const TileConfig &t,
+               BatchGroup &g, std::vector<FluxParams> &items, std::vector<long long> &start, char *msg,
+               size_t msg_len) {
+  const FluxVariant *v = find_variant(precision, mode, t.lanes_per_solve);
+  if (!v) { set_msg(msg, msg_len, "no kernel built for %d lanes per solve", t.lanes_per_solve); return SOCGPU_I_ERR_RANGE; }
+  items.clear();
+  start.assign(1, 0);
+  for (int i : idx) {
+    items.push_back(b.params[i]);
+    start.push_back(start.back() + b.params[i].n_profile);
+  }
+  g = BatchGroup{};
+  g.precision = precision; g.mode = mode; g.tile = t;
+  g.items = items.data(); g.col_start = start.data();
+  g.n_items = (int)items.size(); g.total = start.back();
+  return v->prepare(g, msg, msg_len);
+}
+
+// Copy groups' tables to one device buffer (device pointers returned per group).
+int upload_groups(std::vector<BatchGroup> &groups, char *&dbuf, std::vector<FluxParams *> &d_items,
+                  std::vector<long long *> &d_start, char *msg, size_t msg_len) {
+  size_t bytes = 0;
+  for (const BatchGroup &g : groups)
+    bytes += align256(sizeof(FluxParams) * g.n_items) + align256(sizeof(long long) * (g.n_items + 1));
+  if (dbuf) { cudaFree(dbuf); dbuf = nullptr; }
+  CUDA_TRY(cudaMalloc(&dbuf, std::max<size_t>(bytes, 256)));
+  size_t off = 0;
+  d_items.clear(); d_start.clear();
+  for (const BatchGroup &g : groups) {
+    FluxParams *di = (FluxParams *)(dbuf + off);
+    off += align256(sizeof(FluxParams) * g.n_items);
+    long long *ds = (long long *)(dbuf + off);
+    off += align256(sizeof(long long) * (g.n_items + 1));
+    CUDA_TRY(cudaMemcpy(di, g.items, sizeof(FluxParams) * g.n_items, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(ds, g.col_start, sizeof(long long) * (g.n_items + 1), cudaMemcpyHostToDevice));
+    d_items.push_back(di);
+    d_start.push_back(ds);
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+// `count`: a real launch (not one recorded into a graph).
+int launch_group(const BatchGroup &g, FluxParams *di, long long *ds, cudaStream_t st, bool count = true) {
+  if (g.total <= 0) return 0;
+  int n_items = g.n_items;
+  long long total = g.total;
+  void *args[] = {&di, &ds, &n_items, &total};
+  cudaError_t e = cudaLaunchKernel(g.kernel, dim3(g.grid), dim3(g.threads), args, g.smem, st);
+  if (count) count_launch();
+  return e == cudaSuccess ? 0 : -1;
+}
+
+// Group the batches by the tile each one is given (tuner table, overrides or
+// heuristic), prepare, upload and capture the graph.
+int build_plan(socgpu_batch_s &b, char *msg, size_t msg_len) {
+  std::map<std::tuple<int, int, int, int, int>, std::vector<int>> classes;
+  for (size_t i = 0; i < b.params.size(); ++i) {
+    TileConfig t = choose_tile(b.precision[i], b.mode[i], b.params[i].n_layer);
+    classes[std::make_tuple(b.precision[i], b.mode[i], t.lanes_per_solve, t.chunk, t.warps_per_cta)].push_back(
+        (int)i);
+  }
+  b.groups.assign(classes.size(), BatchGroup{});
+  b.group_items.assign(classes.size(), {});
+  b.group_start.assign(classes.size(), {});
+  size_t k = 0;
+  for (auto &kv : classes) {
+    TileConfig t{std::get<2>(kv.first), std::get<4>(kv.first), std::get<3>(kv.first)};
+    int st = make_group(b, kv.second, std::get<0>(kv.first), std::get<1>(kv.first), t, b.groups[k],
+                        b.group_items[k], b.group_start[k], msg, msg_len);
+    if (st != SOCGPU_I_NORMAL) return st;
+    ++k;
+  }
+  int st = upload_groups(b.groups, b.dbuf, b.d_items, b.d_start, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  if (b.exec) { cudaGraphExecDestroy(b.exec); b.exec = nullptr; }
+  CUDA_TRY(cudaStreamBeginCapture(b.capture, cudaStreamCaptureModeThreadLocal));
+  int bad = 0;
+  for (size_t g = 0; g < b.groups.size(); ++g) bad |= launch_group(b.groups[g], b.d_items[g], b.d_start[g], b.capture, false);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b.capture, &graph);
+  if (bad || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    set_msg(msg, msg_len, "capture of the batch launches failed: %s", cudaGetErrorString(e));
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  e = cudaGraphInstantiate(&b.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_msg(msg, msg_len, "graph instantiation failed: %s", cudaGetErrorString(e));
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -630,7 +791,7 @@ int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dime
   // inputs: (nd_profile, rows) arrays copied with their valid profiles only
   size_t o_p = plan.add(atm->p, D, ndp, np, nl);
   size_t o_t = plan.add(atm->t, D, ndp, np, nl);
-  size_t o_tl = plan.add(atm->t_level, D, ndp, np, nl + 1);
+  size_t o_tl = !sw ? plan.add(atm->t_level, D, ndp, np, nl + 1) : (size_t)-1;
   size_t o_m = plan.add(atm->mass, D, ndp, np, nl);
   size_t o_g = control->l_gas ? plan.add(atm->gas_mix_ratio, D, ndp, np, ndl * ns) : (size_t)-1;
   size_t o_z = sw ? plan.add(bound->zen_0, D, ndp, np, 1) : (size_t)-1;
@@ -821,6 +982,156 @@ int socgpu_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, i
                                cudaMemcpyDeviceToHost, s));
   }
   CUDA_TRY(cudaStreamSynchronize(s));
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_batch_create(const socgpu_batch_item *items, int n_items, socgpu_batch *batch, char *msg,
+                        size_t msg_len) {
+  if (!items || n_items < 1 || !batch) { set_msg(msg, msg_len, "no batches"); return SOCGPU_I_ERR_FATAL; }
+  std::unique_ptr<socgpu_batch_s> b(new socgpu_batch_s);
+  CUDA_TRY(cudaGetDevice(&b->device));
+  for (int i = 0; i < n_items; ++i) {
+    const socgpu_batch_item &it = items[i];
+    SpectrumEntry *sp = find_spectrum(it.spectrum);
+    char sub[256] = "";
+    int st = validate(it.control, it.dimen, sp, it.atm, it.cld, it.aer, it.bound, it.radout, sub, sizeof(sub));
+    if (st != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "batch %d: %s", i, sub); return st; }
+    FluxParams p;
+    fill_params(p, it.control, it.dimen, sp, it.atm, it.cld, it.aer, it.bound, it.radout, it.control->weight_band);
+    b->params.push_back(p);
+    b->precision.push_back(it.control->precision);
+    b->mode.push_back(mode_index(it.control));
+    b->n_columns += p.n_profile;
+    b->n_colg += (long long)p.n_profile * (p.g_end - p.g_begin);
+  }
+  CUDA_TRY(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking));
+  int st = build_plan(*b, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  *batch = b.release();
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_batch_run(socgpu_batch batch, void *stream, char *msg, size_t msg_len) {
+  if (!batch || !batch->exec) { set_msg(msg, msg_len, "invalid batch"); return SOCGPU_I_ERR_FATAL; }
+  CUDA_TRY(cudaGraphLaunch(batch->exec, (cudaStream_t)stream));
+  for (const BatchGroup &g : batch->groups)
+    if (g.total > 0) count_launch();
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_batch_tune(socgpu_batch batch, void *stream, int reps, char *msg, size_t msg_len) {
+  if (!batch) { set_msg(msg, msg_len, "invalid batch"); return SOCGPU_I_ERR_FATAL; }
+  socgpu_batch_s &b = *batch;
+  if (reps < 1) reps = 3;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::map<std::tuple<int, int, int>, std::vector<int>> keys;
+  for (size_t i = 0; i < b.params.size(); ++i)
+    keys[std::make_tuple(b.precision[i], b.mode[i], b.params[i].n_layer)].push_back((int)i);
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  int status = SOCGPU_I_NORMAL;
+  for (auto &kv : keys) {
+    const int prec = std::get<0>(kv.first), mode = std::get<1>(kv.first), L = std::get<2>(kv.first);
+    float best = 1e30f;
+    TileConfig best_t{};
+    const int lanes_opts[] = {8, 16, 32};
+    for (int lanes : lanes_opts) {
+      const int chunk = smallest_chunk(prec, lanes, L);
+      if (!find_variant(prec, mode, lanes) || chunk == 0) continue;
+      for (int warps : {4, 8}) {
+        TileConfig t{lanes, warps, chunk};
+        std::vector<BatchGroup> one(1);
+        std::vector<FluxParams> items;
+        std::vector<long long> start;
+        char sub[256] = "";
+        if (make_group(b, kv.second, prec, mode, t, one[0], items, start, sub, sizeof(sub)) != SOCGPU_I_NORMAL)
+          continue;   // this tile does not fit (shared memory): not a candidate
+        char *tbuf = nullptr;
+        std::vector<FluxParams *> di;
+        std::vector<long long *> ds;
+        if (upload_groups(one, tbuf, di, ds, sub, sizeof(sub)) != SOCGPU_I_NORMAL) {
+          if (tbuf) cudaFree(tbuf);
+          status = SOCGPU_I_ABORT_CALCULATION;
+          set_msg(msg, msg_len, "tuning upload failed: %s", sub);
+          break;
+        }
+        float ms = 1e30f;
+        int bad = launch_group(one[0], di[0], ds[0], st);    // warm-up
+        for (int r = 0; r < reps && !bad; ++r) {
+          cudaEventRecord(e0, st);
+          bad |= launch_group(one[0], di[0], ds[0], st);
+          cudaEventRecord(e1, st);
+          if (cudaEventSynchronize(e1) != cudaSuccess) { bad = 1; break; }
+          float m = 0.f;
+          cudaEventElapsedTime(&m, e0, e1);
+          ms = std::min(ms, m);
+        }
+        cudaStreamSynchronize(st);
+        cudaFree(tbuf);
+        if (bad) {
+          cudaGetLastError();
+          status = SOCGPU_I_ABORT_CALCULATION;
+          set_msg(msg, msg_len, "tuning launch failed for %d lanes x %d layers, %d warps", lanes, chunk, warps);
+          break;
+        }
+        if (ms < best) { best = ms; best_t = t; }
+      }
+      if (status != SOCGPU_I_NORMAL) break;
+    }
+    if (status != SOCGPU_I_NORMAL) break;
+    if (best_t.lanes_per_solve) {
+      std::lock_guard<std::mutex> lk(g_tile_mutex);
+      g_tuned[kv.first] = best_t;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (status != SOCGPU_I_NORMAL) return status;
+  return build_plan(b, msg, msg_len);
+}
+
+int socgpu_batch_info(socgpu_batch batch, int *n_groups, long long *n_columns, long long *n_column_gpoints) {
+  if (!batch) return SOCGPU_I_ERR_FATAL;
+  if (n_groups) *n_groups = (int)batch->groups.size();
+  if (n_columns) *n_columns = batch->n_columns;
+  if (n_column_gpoints) *n_column_gpoints = batch->n_colg;
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_batch_destroy(socgpu_batch batch) {
+  if (!batch) return SOCGPU_I_NORMAL;
+  cudaStreamSynchronize(batch->capture);
+  cudaDeviceSynchronize();
+  delete batch;
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_tune_get(int precision, int mode, int n_layer, int *lanes_per_solve, int *layers_per_lane,
+                    int *warps_per_cta) {
+  std::lock_guard<std::mutex> lk(g_tile_mutex);
+  auto it = g_tuned.find(std::make_tuple(precision, mode, n_layer));
+  if (it == g_tuned.end()) return SOCGPU_I_ERR_EXIST;
+  if (lanes_per_solve) *lanes_per_solve = it->second.lanes_per_solve;
+  if (layers_per_lane) *layers_per_lane = it->second.chunk;
+  if (warps_per_cta) *warps_per_cta = it->second.warps_per_cta;
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_tune_set(int precision, int mode, int n_layer, int lanes_per_solve, int layers_per_lane,
+                    int warps_per_cta) {
+  if (precision < 0 || precision > 1 || mode < 0 || mode > 2 || n_layer < 1 || n_layer > SOCGPU_MAX_LAYER)
+    return SOCGPU_I_ERR_RANGE;
+  std::lock_guard<std::mutex> lk(g_tile_mutex);
+  if (lanes_per_solve == 0) { g_tuned.erase(std::make_tuple(precision, mode, n_layer)); return SOCGPU_I_NORMAL; }
+  const int *c = nullptr;
+  const int n = chunk_list(precision, lanes_per_solve, &c);
+  bool ok = false;
+  for (int i = 0; i < n; ++i) ok |= (c[i] == layers_per_lane);
+  if (!ok || lanes_per_solve * layers_per_lane < n_layer || warps_per_cta < 1 || warps_per_cta > 8 ||
+      (warps_per_cta * 32) % lanes_per_solve != 0)
+    return SOCGPU_I_ERR_RANGE;
+  g_tuned[std::make_tuple(precision, mode, n_layer)] = TileConfig{lanes_per_solve, warps_per_cta, layers_per_lane};
   return SOCGPU_I_NORMAL;
 }
 

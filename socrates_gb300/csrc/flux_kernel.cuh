@@ -346,9 +346,8 @@ struct FluxKernel {
     return s;
   }
 
-  __device__ static void run(const FluxParams &p) {
+  __device__ static void run(const FluxParams &p, const int col) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int col = blockIdx.x;
     const int L = p.n_layer;
     const int nb_all = p.last_band - p.first_band + 1;
     const int nbat = p.band_batch;             // bands staged at a time
@@ -1036,7 +1035,50 @@ struct FluxKernel {
 
 template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA>
 __global__ void __launch_bounds__(256) flux_kernel(const __grid_constant__ FluxParams p) {
-  FluxKernel<R, MIX, P, CH, NOSCAT, MCICA>::run(p);
+  FluxKernel<R, MIX, P, CH, NOSCAT, MCICA>::run(p, blockIdx.x);
+}
+
+// Persistent form over many column batches: items[i] describes one batch
+// (its own spectrum, layer count, options and arrays); batch i owns the work
+// indices col_start[i] .. col_start[i+1]-1, one per column.  Each CTA strides
+// over the work indices, finds the batch by binary search and keeps the
+// batch's parameters in shared memory while consecutive indices stay in it.
+// Resident CTAs the batched kernel asks the register allocator for: its
+// parameters sit in shared memory, not in the constant bank, so without a
+// bound it keeps about twice the registers of flux_kernel (measured with
+// -Xptxas -v: 3 CTAs of 256 threads fit without spills up to 4 layers per
+// lane).
+constexpr int batched_min_ctas(int ch) { return ch <= 4 ? 3 : (ch <= 9 ? 2 : 1); }
+
+template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA>
+__global__ void __launch_bounds__(256, batched_min_ctas(CH))
+flux_kernel_batched(const FluxParams *__restrict__ items, const long long *__restrict__ col_start, int n_items,
+                    long long total) {
+  __shared__ __align__(16) FluxParams sp;
+  __shared__ int s_item;
+  static_assert(sizeof(FluxParams) % 4 == 0, "FluxParams is copied as words");
+  int cur = -1;
+  for (long long w = blockIdx.x; w < total; w += gridDim.x) {
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = n_items - 1;   // last batch whose first index is <= w
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (col_start[mid] <= w) lo = mid; else hi = mid - 1;
+      }
+      s_item = lo;
+    }
+    __syncthreads();
+    const int it = s_item;
+    if (it != cur) {
+      const int *src = reinterpret_cast<const int *>(items + it);
+      int *dst = reinterpret_cast<int *>(&sp);
+      for (int q = threadIdx.x; q < (int)(sizeof(FluxParams) / 4); q += blockDim.x) dst[q] = src[q];
+      cur = it;
+    }
+    __syncthreads();
+    FluxKernel<R, MIX, P, CH, NOSCAT, MCICA>::run(sp, (int)(w - col_start[it]));
+    __syncthreads();
+  }
 }
 
 }  // namespace socgpu

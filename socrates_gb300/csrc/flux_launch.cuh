@@ -2,6 +2,7 @@
 // shapes (lanes per solve P, layers per lane CH) it is instantiated for.
 #pragma once
 
+#include <algorithm>
 #include <cstdio>
 #include "flux_kernel.cuh"
 
@@ -14,6 +15,7 @@ template <class R, bool MIX, bool NOSCAT, bool MCICA, class S>
 int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len,
                bool &done) {
   if (done || cfg.lanes_per_solve != S::P || S::P * S::CH < p.n_layer) return 0;
+  if (cfg.chunk && cfg.chunk != S::CH) return 0;
   // the smallest chunk of this P that covers the column is chosen by the
   // caller's ordering of shapes (ascending CH)
   done = true;
@@ -57,6 +59,92 @@ int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char
   return 0;
 }
 
+// Prepare one kernel class of a multi-batch launch for shape S: the band
+// batch of every item so that all fit one shared-memory size, the kernel
+// attribute, and a persistent grid of the resident CTAs of every SM.
+template <class R, bool MIX, bool NOSCAT, bool MCICA, class S>
+int try_prepare(BatchGroup &g, char *msg, size_t len, bool &done) {
+  if (done || g.tile.lanes_per_solve != S::P || g.tile.chunk != S::CH) return 0;
+  done = true;
+  int max_smem = 0, dev = 0, n_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  const int warps = g.tile.warps_per_cta;
+  const int n_groups = warps * 32 / S::P;
+  auto bytes_of = [&](const FluxParams &p, int batch) {
+    return make_layout<R>(S::P * S::CH, S::P, batch, p.max_abs, MCICA ? p.n_condensed : 0,
+                          MCICA ? p.n_subcol_gen : 0, n_groups, p.isolir == SOCGPU_IP_INFRA_RED, MCICA).bytes;
+  };
+  auto kern = flux_kernel_batched<R, MIX, S::P, S::CH, NOSCAT, MCICA>;
+  // the kernel's static shared memory (its parameter copy) counts against
+  // the same per-CTA limit
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) {
+    cudaGetLastError();
+    snprintf(msg, len, "attributes of the batched kernel not available");
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  const size_t dyn_cap = (size_t)max_smem > fa.sharedSizeBytes ? (size_t)max_smem - fa.sharedSizeBytes : 0;
+  // the launch's shared memory: the largest whole-spectrum staging of any
+  // item, capped at the device limit; items that need more stage their bands
+  // in batches
+  size_t smem = 0;
+  for (int i = 0; i < g.n_items; ++i) {
+    const FluxParams &p = g.items[i];
+    if (p.n_layer > S::P * S::CH) {
+      snprintf(msg, len, "batch %d has %d layers, more than the %d of its tile", i, p.n_layer, S::P * S::CH);
+      return SOCGPU_I_ERR_RANGE;
+    }
+    smem = std::max(smem, bytes_of(p, p.last_band - p.first_band + 1));
+  }
+  smem = std::min(smem, dyn_cap);
+  for (int i = 0; i < g.n_items; ++i) {
+    FluxParams &p = g.items[i];
+    int batch = p.last_band - p.first_band + 1;
+    while (batch > 1 && bytes_of(p, batch) > smem) --batch;
+    if (bytes_of(p, batch) > smem) {
+      snprintf(msg, len, "batch %d: one band needs %zu bytes of shared memory (limit %zu)", i, bytes_of(p, 1), smem);
+      return SOCGPU_I_ERR_RANGE;
+    }
+    p.band_batch = batch;
+  }
+  const size_t dyn = smem;
+  if (dyn > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      snprintf(msg, len, "shared memory request of %zu bytes refused: %s", dyn, cudaGetErrorString(e));
+      return SOCGPU_I_ERR_RANGE;
+    }
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, dyn);
+  if (e != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    snprintf(msg, len, "no CTA of %d threads and %zu bytes fits an SM", warps * 32, dyn);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  g.kernel = (const void *)kern;
+  g.smem = dyn;
+  g.threads = warps * 32;
+  g.grid = (int)std::min<long long>(g.total, (long long)per_sm * n_sm);
+  return 0;
+}
+
+template <class R, bool MIX, bool NOSCAT, bool MCICA, class... Shapes>
+int prepare_shapes(BatchGroup &g, char *msg, size_t len) {
+  bool done = false;
+  int status = 0;
+  ((status = status ? status : try_prepare<R, MIX, NOSCAT, MCICA, Shapes>(g, msg, len, done)), ...);
+  if (!done && status == 0) {
+    snprintf(msg, len, "no kernel instantiated for %d lanes per solve and %d layers per lane",
+             g.tile.lanes_per_solve, g.tile.chunk);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  return status;
+}
+
 template <class R, bool MIX, bool NOSCAT, bool MCICA, class... Shapes>
 int launch_shapes(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len) {
   bool done = false;
@@ -71,11 +159,14 @@ int launch_shapes(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, c
 }
 
 
-}  // namespace socgpu
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int P, int... CH>
+int launch_chunks(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len) {
+  return launch_shapes<R, MIX, NOSCAT, MCICA, Shape<P, CH>...>(p, cfg, st, msg, len);
+}
 
-// Shape lists: ascending CH within each P so the first fit is the tightest.
-#define SOCGPU_SHAPES_FP64 \
-  Shape<16, 4>, Shape<16, 8>, Shape<16, 16>, Shape<32, 4>, Shape<32, 8>, Shape<32, 16>
-#define SOCGPU_SHAPES_MIXED                                                                      \
-  Shape<8, 8>, Shape<8, 13>, Shape<8, 18>, Shape<16, 4>, Shape<16, 8>, Shape<16, 16>, Shape<32, 4>, \
-      Shape<32, 8>, Shape<32, 16>
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int P, int... CH>
+int prepare_chunks(BatchGroup &g, char *msg, size_t len) {
+  return prepare_shapes<R, MIX, NOSCAT, MCICA, Shape<P, CH>...>(g, msg, len);
+}
+
+}  // namespace socgpu

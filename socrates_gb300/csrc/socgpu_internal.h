@@ -120,18 +120,77 @@ struct FluxParams {
 struct TileConfig {
   int lanes_per_solve;   // P: lanes sharing one (column, g-point) solve
   int warps_per_cta;     // warps per CTA; one CTA per column
+  int chunk;             // CH: layers per lane; 0 = the smallest instantiated chunk that covers the column
 };
 
-// Kernel entry points (defined in the .cu translation units).
-#define SOCGPU_DECL_LAUNCH(name) \
-  int name(const FluxParams &p, const TileConfig &cfg, cudaStream_t s, char *msg, size_t len);
-SOCGPU_DECL_LAUNCH(launch_flux_fp64_lwns)
-SOCGPU_DECL_LAUNCH(launch_flux_fp64_full)
-SOCGPU_DECL_LAUNCH(launch_flux_fp64_mcica)
-SOCGPU_DECL_LAUNCH(launch_flux_mixed_lwns)
-SOCGPU_DECL_LAUNCH(launch_flux_mixed_full)
-SOCGPU_DECL_LAUNCH(launch_flux_mixed_mcica)
-#undef SOCGPU_DECL_LAUNCH
+// One kernel class of a multi-batch launch: the batches that share precision,
+// mode and tile, run by one persistent launch of flux_kernel_batched.
+struct BatchGroup {
+  int precision = 0, mode = 0;
+  TileConfig tile{};
+  FluxParams *items = nullptr;        // host array [n_items] (band_batch filled by the prepare step)
+  long long *col_start = nullptr;     // host array [n_items + 1]
+  int n_items = 0;
+  long long total = 0;                // columns of all batches
+  // filled by the prepare step
+  const void *kernel = nullptr;
+  size_t smem = 0;
+  int threads = 0, grid = 0;
+};
+
+// Layers per lane (CH) instantiated for each precision and lane count P; a
+// kernel covers P * CH layers.  flux_inst.cu is compiled once per
+// (precision, mode, P) and instantiates these chunks.
+#define SOCGPU_CHUNKS_MIXED_8  5, 8, 13, 18
+#define SOCGPU_CHUNKS_MIXED_16 3, 4, 5, 7, 9, 16
+#define SOCGPU_CHUNKS_MIXED_32 3, 4, 5, 8, 16
+#define SOCGPU_CHUNKS_FP64_16  4, 8, 16
+#define SOCGPU_CHUNKS_FP64_32  4, 5, 8, 16
+
+// The chunks of (precision, lanes) in ascending order; returns their count
+// (0 when that lane count is not built for the precision).
+inline int chunk_list(int precision, int lanes, const int **out) {
+  static const int m8[] = {SOCGPU_CHUNKS_MIXED_8}, m16[] = {SOCGPU_CHUNKS_MIXED_16},
+                   m32[] = {SOCGPU_CHUNKS_MIXED_32}, d16[] = {SOCGPU_CHUNKS_FP64_16},
+                   d32[] = {SOCGPU_CHUNKS_FP64_32};
+#define SOCGPU_RET(a) do { *out = a; return (int)(sizeof(a) / sizeof(a[0])); } while (0)
+  if (precision == SOCGPU_PRECISION_MIXED) {
+    if (lanes == 8) SOCGPU_RET(m8);
+    if (lanes == 16) SOCGPU_RET(m16);
+    if (lanes == 32) SOCGPU_RET(m32);
+  } else {
+    if (lanes == 16) SOCGPU_RET(d16);
+    if (lanes == 32) SOCGPU_RET(d32);
+  }
+#undef SOCGPU_RET
+  *out = nullptr;
+  return 0;
+}
+
+// Smallest built chunk of (precision, lanes) covering n_layer, or 0.
+inline int smallest_chunk(int precision, int lanes, int n_layer) {
+  const int *c = nullptr;
+  const int n = chunk_list(precision, lanes, &c);
+  for (int i = 0; i < n; ++i)
+    if (lanes * c[i] >= n_layer) return c[i];
+  return 0;
+}
+
+// Kernel entry points, one pair per (precision 0 fp64 / 1 mixed, mode
+// 0 lwns / 1 full / 2 mcica, lanes), defined by the objects of flux_inst.cu.
+#define SOCGPU_DECL_FLUX(prec, mode, lanes)                                                             \
+  int launch_flux_##prec##_##mode##_##lanes(const FluxParams &p, const TileConfig &cfg, cudaStream_t s, \
+                                            char *msg, size_t len);                                    \
+  int prepare_flux_##prec##_##mode##_##lanes(BatchGroup &g, char *msg, size_t len);
+#define SOCGPU_DECL_FLUX_MODES(prec, lanes) \
+  SOCGPU_DECL_FLUX(prec, 0, lanes) SOCGPU_DECL_FLUX(prec, 1, lanes) SOCGPU_DECL_FLUX(prec, 2, lanes)
+SOCGPU_DECL_FLUX_MODES(0, 16)
+SOCGPU_DECL_FLUX_MODES(0, 32)
+SOCGPU_DECL_FLUX_MODES(1, 8)
+SOCGPU_DECL_FLUX_MODES(1, 16)
+SOCGPU_DECL_FLUX_MODES(1, 32)
+#undef SOCGPU_DECL_FLUX_MODES
+#undef SOCGPU_DECL_FLUX
 
 void count_launch();
 

@@ -28,7 +28,7 @@ class DeviceCase:
     """One radiance_calc problem with every array resident on the GPU."""
 
     def __init__(self, control: Control, spectrum: Spectrum, col, mcica: McicaState | None = None,
-                 id_cloud_top: int = 1):
+                 id_cloud_top: int = 1, keep_host: bool = True):
         import torch
         self.lib = load_library()
         self.handle = register_spectrum(spectrum)
@@ -99,6 +99,28 @@ class DeviceCase:
         self.n, self.L = n, L
         self.input_bytes = sum(t.numel() * t.element_size() for k, t in self.tensors.items() if not k.startswith("out_"))
         self.output_bytes = sum(t.numel() * t.element_size() for k, t in self.tensors.items() if k.startswith("out_"))
+        if not keep_host:
+            # the host copies are on the device now; keep only the small
+            # option arrays the cloud struct points at
+            m.keep = [a for a in m.keep if getattr(a, "nbytes", 0) <= 4096]
+            m.flux_up = m.flux_down = m.flux_direct = m.flux_div = m.heating_rate = None
+
+    def clone(self, precision: int) -> "DeviceCase":
+        """The same problem at another precision: inputs shared, outputs new."""
+        import copy
+        import torch
+        c = copy.copy(self)
+        c.tensors = {k: v for k, v in self.tensors.items() if not k.startswith("out_")}
+        c.control = type(self.control).from_buffer_copy(self.control)
+        c.control.precision = precision
+        c.radout = abi.Radout()
+        dp = C.POINTER(C.c_double)
+        for k, t in self.tensors.items():
+            if k.startswith("out_"):
+                nt = torch.zeros_like(t)
+                c.tensors[k] = nt
+                setattr(c.radout, k[4:], C.cast(C.c_void_p(nt.data_ptr()), dp))
+        return c
 
     def tensor_bytes(self, name: str) -> int:
         t = self.tensors.get(name)

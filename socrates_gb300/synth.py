@@ -167,7 +167,7 @@ def lw_spectrum(seed: int = 1, nk: int = 9, clouds: bool = False) -> Spectrum:
         flux = _planck_band(edges[b], edges[b + 1], temps)
         coeff[:, b] = np.polynomial.polynomial.polyfit(temps / t_ref, flux, 5)
     sp = Spectrum(**d, n_deg_fit=5, t_ref_planck=t_ref, thermal_coeff=np.asfortranarray(coeff),
-                  name=f"synthetic_lw_{nk}k_seed{seed}")
+                  name=f"synthetic_lw_{nk}k_seed{seed}" + ("_cld" if clouds else ""))
     if clouds:
         sp.drop_parm_list, sp.ice_parm_list = _pade_sets(9, False, st)
         sp.i_drop_parm = np.array([5], np.int32)
@@ -189,7 +189,8 @@ def sw_spectrum(seed: int = 2, nk: int = 8, clouds: bool = False) -> Spectrum:
     frac /= frac.sum()
     lam = np.sqrt(edges[:-1] * edges[1:]) / 1.0e-6
     ray = 8.6e-7 * lam ** -4.0
-    sp = Spectrum(**d, solar_flux_band=frac, rayleigh_coeff=ray, name=f"synthetic_sw_{nk}k_seed{seed}")
+    sp = Spectrum(**d, solar_flux_band=frac, rayleigh_coeff=ray,
+                  name=f"synthetic_sw_{nk}k_seed{seed}" + ("_cld" if clouds else ""))
     if clouds:
         sp.drop_parm_list, sp.ice_parm_list = _pade_sets(6, True, st)
         sp.i_drop_parm = np.array([5], np.int32)
@@ -326,6 +327,29 @@ def add_clouds(col: Column, seed: int, n_subcol: int = 16, decorrelation_m: floa
                    condensed_mix_ratio=cond, condensed_dim_char=dim,
                    dp_corr_cloud=f(dp_corr), dp_corr_cond=f(0.5 * dp_corr), rand_seed=seeds, n_subcol_gen=n_subcol)
     return col
+
+
+def window(col: Column, start: int, n: int) -> Column:
+    """Columns start .. start+n-1 of col as a new Column (copies, Fortran
+    order).  Per-column arrays are those whose first extent is n_profile."""
+    import copy
+    c = copy.copy(col)
+    c.n_profile = n
+    sl = slice(start, start + n)
+
+    def cut(v):
+        if isinstance(v, np.ndarray) and v.ndim >= 1 and v.shape[0] == col.n_profile:
+            return np.asfortranarray(v[sl])
+        return v
+
+    for name in ("p", "t", "p_level", "t_level", "mass", "gas_mix_ratio", "z", "t_ground", "zen_0", "solar_irrad",
+                 "rho_alb"):
+        setattr(c, name, cut(getattr(col, name)))
+    if col.aer:
+        c.aer = {k: cut(v) for k, v in col.aer.items()}
+    if col.cld:
+        c.cld = {k: cut(v) for k, v in col.cld.items()}
+    return c
 
 
 # ---------------------------------------------------------------------------

@@ -58,3 +58,16 @@ def test_spectral_file_round_trip(tmp_path):
         if sp.solar_flux_band is not None:
             assert abs(back.solar_flux_band - sp.solar_flux_band).max() < 1e-9
         assert abs(back.drop_parm_list - sp.drop_parm_list).max() <= 1e-9 * abs(sp.drop_parm_list).max()
+
+
+def test_tile_table_validation(lib):
+    # host-only bookkeeping: no device call
+    assert lib.socgpu_tune_set(1, 1, 100, 32, 4, 8) == abi.I_NORMAL
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    assert lib.socgpu_tune_get(1, 1, 100, C.byref(a), C.byref(b), C.byref(c)) == abi.I_NORMAL
+    assert (a.value, b.value, c.value) == (32, 4, 8)
+    assert lib.socgpu_tune_set(1, 1, 100, 32, 3, 8) == abi.I_ERR_RANGE     # 96 layers do not cover 100
+    assert lib.socgpu_tune_set(1, 1, 100, 32, 6, 8) == abi.I_ERR_RANGE     # no 6-layer chunk is built
+    assert lib.socgpu_tune_set(0, 1, 100, 8, 13, 8) == abi.I_ERR_RANGE     # FP64 has no 8-lane kernels
+    assert lib.socgpu_tune_set(1, 1, 100, 0, 0, 0) == abi.I_NORMAL          # remove
+    assert lib.socgpu_tune_get(1, 1, 100, C.byref(a), C.byref(b), C.byref(c)) == abi.I_ERR_EXIST
