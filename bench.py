@@ -48,7 +48,9 @@ def parse():
     ap.add_argument("--impl", default="socgpu", choices=["socgpu", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=N_COL, help="columns of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU work of the baseline sample")
-    ap.add_argument("--workload", default="sw", choices=["sw", "batched"])
+    ap.add_argument("--workload", default="sw", choices=["sw", "batched", "serve"])
+    ap.add_argument("--rates", default="200,1000,5000", help="arrival rates (requests/s) of the serving workload")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
     ap.add_argument("--batches", type=int, default=4096, help="column batches of the batched workload")
     return ap.parse_args()
 
@@ -313,6 +315,144 @@ def run_batched(args):
         dist.destroy_process_group()
 
 
+def run_serve(args):
+    """The serving workload: Poisson arrivals of requests drawn like the
+    multi-batch workload, served by the continuous-batching server; p50/p99
+    latency and throughput per arrival rate, beside the plain FP64
+    per-request GPU path on the same arrival trace and the CPU port."""
+    import ctypes
+    import numpy as np
+    import torch
+    rank, world = dist_setup(args.gpus)
+    from dataclasses import replace
+    from socrates_gb300 import abi
+    from socrates_gb300 import build as B
+    from socrates_gb300 import radiance as R
+    from socrates_gb300.server import Server
+    from socrates_gb300.workload import PinnedArena, Pools, pin_outputs, request_specs
+    B.build()
+    rates = [float(r) for r in args.rates.split(",")]
+    seed = 5 + rank
+    # 128 request slots: page-locked inputs and outputs drawn like the
+    # multi-batch workload; request i of a trace uses slot i mod 128, once
+    # the slot's previous request has finished
+    n_slot = 128
+    specs = request_specs(n_slot, seed)
+    pools = Pools(specs, seed)
+
+    def need(s):
+        return s.n_profile * (s.n_layer + 1) * 8 * 48 + (1 << 16)
+    arena = PinnedArena(sum(need(s) for s in specs) + (64 << 20))
+    slots = []
+    for s in specs:
+        ctl, sp, col, mc = pools.request(s, abi.PRECISION_MIXED, arena.take)
+        m = pin_outputs(R.Marshal(ctl, sp, col, mc), arena.take)
+        slots.append((m, sp, (ctl, sp, col, mc)))
+        R.register_spectrum(sp)
+    srv = Server(device_bytes=0, streams=4, max_wave_requests=256)
+    for i in range(n_slot):                      # warm-up: every kernel class once
+        srv.wait(srv.submit(slots[i][0], slots[i][1]))
+    results = []
+    for rate in rates:
+        n = int(rate * args.serve_seconds)
+        rng = np.random.default_rng(int(rate))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+        tickets = [None] * n
+        lat = [0.0] * n
+        queue = [0.0] * n
+        done = [0]
+        cv = threading.Condition()
+
+        def waiter():
+            for i in range(n):
+                with cv:
+                    cv.wait_for(lambda: tickets[i] is not None)
+                queue[i], lat[i] = srv.wait(tickets[i])
+                with cv:
+                    done[0] = i + 1
+                    cv.notify_all()
+        th = threading.Thread(target=waiter)
+        th.start()
+        s0 = srv.stats()
+        t0 = time.perf_counter()
+        late = 0
+        for i in range(n):
+            if i >= n_slot:
+                with cv:
+                    cv.wait_for(lambda: done[0] > i - n_slot)
+            while time.perf_counter() - t0 < arrivals[i]:
+                pass
+            late += (time.perf_counter() - t0 - arrivals[i]) > 1e-3
+            m, sp, _ = slots[i % n_slot]
+            t = srv.submit(m, sp)
+            with cv:
+                tickets[i] = t
+                cv.notify_all()
+        th.join()
+        t_end = time.perf_counter()
+        s1 = srv.stats()
+        colg = s1["column_gpoints"] - s0["column_gpoints"]
+        results.append({"rate_rps": rate, "requests": n, "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99)), "queue_p99_ms": float(np.percentile(queue, 99)),
+                        "column_gpoints_per_s": colg / max(t_end - t0, 1e-9),
+                        "offered_column_gpoints_per_s": colg / max(float(arrivals[-1]), 1e-9),
+                        "submits_late_over_1ms": int(late), "waves": s1["waves"] - s0["waves"],
+                        "max_wave_requests": s1["max_wave_requests"], "peak_device_bytes": s1["peak_bytes"]})
+    srv.close()
+    # the plain FP64 per-request GPU path on the same arrival trace (first
+    # 200 requests of each rate): one synchronous socgpu_radiance_calc per
+    # request, in arrival order, latency from arrival to return
+    lib = R.load_library()
+    fp64 = []
+    m64 = []
+    for m, sp, (ctl, sp_, col, mc) in slots:
+        m64.append((R.Marshal(replace(ctl, precision=abi.PRECISION_FP64), sp, col, mc), sp))
+    msg = ctypes.create_string_buffer(256)
+    for rate in rates:
+        n = min(200, int(rate * args.serve_seconds))
+        rng = np.random.default_rng(int(rate))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+        lat = []
+        colg = 0
+        t0 = time.perf_counter()
+        for i in range(n):
+            m, sp = m64[i % n_slot]
+            while time.perf_counter() - t0 < arrivals[i]:
+                pass
+            st = lib.socgpu_radiance_calc(*m.args(R.register_spectrum(sp)), msg, 256)
+            if st != 0:
+                raise SystemExit(f"FP64 request failed: {msg.value.decode()}")
+            lat.append((time.perf_counter() - t0 - arrivals[i]) * 1e3)
+            colg += m.n * sp.n_gpoint
+        fp64.append({"rate_rps": rate, "requests": n, "p50_ms": float(np.percentile(lat, 50)),
+                     "p99_ms": float(np.percentile(lat, 99)),
+                     "column_gpoints_per_s": colg / (time.perf_counter() - t0)})
+    # the CPU port on a sample of the same requests (about --cpu-seconds)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    colg, k = 0, 0
+    while time.perf_counter() - t0 < args.cpu_seconds and k < n_slot:
+        ctl, sp, col, mc = slots[k][2]
+        O.radiance_calc(replace(ctl, precision=abi.PRECISION_FP64), sp, col, mc, threads=threads)
+        colg += col.n_profile * sp.n_gpoint
+        k += 1
+    cpu = {"value": colg / (time.perf_counter() - t0), "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{k} requests of the trace, one FP64 oracle call each, OpenMP over column segments"}
+    if rank == 0:
+        best = max(results, key=lambda r: r["column_gpoints_per_s"])
+        line = {"metric": METRIC, "value": best["column_gpoints_per_s"], "unit": UNIT, "n_gpus": world,
+                "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded windows of per-kind pools)",
+                "config": {"workload": "serving: Poisson arrivals, requests drawn like the multi-batch workload "
+                                       "(log-normal columns, median 256; layers {38,60,85,137}; LW/SW; clear or "
+                                       "McICA), page-locked host arrays, continuous batching over 4 streams",
+                           "rates_rps": rates, "window_s": args.serve_seconds, "request_slots": n_slot},
+                "serve": results, "fp64_per_request": fp64, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.steps is None:
@@ -322,6 +462,9 @@ def main():
         return
     if args.workload == "batched":
         run_batched(args)
+        return
+    if args.workload == "serve":
+        run_serve(args)
         return
     import numpy as np
     import torch

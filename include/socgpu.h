@@ -424,6 +424,57 @@ SOCGPU_API int socgpu_tune_get(int precision, int mode, int n_layer, int *lanes_
 SOCGPU_API int socgpu_tune_set(int precision, int mode, int n_layer, int lanes_per_solve,
                                int layers_per_lane, int warps_per_cta);
 
+/* ---- request server (extension) -----------------------------------------
+ * Continuous batching of radiance_calc requests with host arrays.  The
+ * reference has no counterpart: its callers call radiance_calc
+ * (src/radiance_core/radiance_calc.F90:16) synchronously, once per batch of
+ * columns, as socgpu_radiance_calc does.
+ *
+ * Every request's inputs and outputs take one block of a device arena of
+ * device_bytes while the request is in flight.  A scheduler thread admits
+ * queued requests in arrival order while their blocks fit (admission by free
+ * device memory) and launches them as one wave on a free stream slot: copy
+ * in, one persistent batched launch per kernel class, copy out.  Up to
+ * `streams` waves run at once, so new arrivals are admitted as soon as a slot
+ * and memory free up, and their work overlaps on the device.  Host arrays
+ * (and the option arrays the structs point at) must stay valid until
+ * socgpu_server_wait returns for the request.  Page-locked host memory lets
+ * the copies run asynchronously. */
+typedef struct socgpu_server_config {
+    size_t device_bytes;        /* arena for request data; 0: half of the free device memory */
+    int streams;                /* waves in flight; 0: 4 */
+    int max_wave_requests;      /* requests per wave; 0: 256 */
+} socgpu_server_config;
+
+typedef struct socgpu_server_stats {
+    long long submitted, completed, waves, max_wave_requests, queued;
+    long long column_gpoints;   /* of the requests completed without error */
+    size_t device_bytes, peak_bytes;
+} socgpu_server_stats;
+
+/* A request: the arguments of socgpu_radiance_calc, host pointers. */
+typedef socgpu_batch_item socgpu_request;
+typedef struct socgpu_server_s *socgpu_server;
+
+/* socgpu_server_wait: the request did not finish within the timeout. */
+#define SOCGPU_SERVER_PENDING 100
+
+SOCGPU_API int socgpu_server_create(const socgpu_server_config *config, socgpu_server *server,
+                                    char *msg, size_t msg_len);
+/* Validate (the checks of socgpu_radiance_calc) and queue; returns at once.
+ * A request larger than the arena is rejected with SOCGPU_I_ERR_RANGE. */
+SOCGPU_API int socgpu_server_submit(socgpu_server server, const socgpu_request *request, long long *ticket,
+                                    char *msg, size_t msg_len);
+/* Block until the request is done (timeout_s < 0: no limit); *status is the
+ * request's own status (msg its message), *queue_ms the time from submit to
+ * launch and *latency_ms from submit to completion.  The ticket is then
+ * released. */
+SOCGPU_API int socgpu_server_wait(socgpu_server server, long long ticket, double timeout_s, int *status,
+                                  double *queue_ms, double *latency_ms, char *msg, size_t msg_len);
+SOCGPU_API int socgpu_server_stats_get(socgpu_server server, socgpu_server_stats *stats);
+/* Finish every queued request, then release the server. */
+SOCGPU_API int socgpu_server_destroy(socgpu_server server);
+
 /* Kernel launches made by this thread since the library loaded (profiling
  * aid, extension). */
 SOCGPU_API long long socgpu_kernel_launch_count(void);

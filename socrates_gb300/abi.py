@@ -121,12 +121,26 @@ class BatchItem(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("device_bytes", C.c_size_t), ("streams", C.c_int), ("max_wave_requests", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("waves", C.c_longlong),
+                ("max_wave_requests", C.c_longlong), ("queued", C.c_longlong), ("column_gpoints", C.c_longlong),
+                ("device_bytes", C.c_size_t), ("peak_bytes", C.c_size_t)]
+
+
+SERVER_PENDING = 100
+
 ABI_FUNCTIONS = (
     "socgpu_abi_version", "socgpu_spectrum_register", "socgpu_spectrum_lookup", "socgpu_spectrum_n_gpoint",
     "socgpu_spectrum_release", "socgpu_radiance_calc", "socgpu_radiance_calc_device", "socgpu_cloud_gen",
     "socgpu_cloud_gen_device", "socgpu_kernel_launch_count", "socgpu_set_device", "socgpu_set_tile_config",
     "socgpu_cloud_gen_device_noalloc", "socgpu_batch_create", "socgpu_batch_run", "socgpu_batch_tune",
     "socgpu_batch_info", "socgpu_batch_destroy", "socgpu_tune_get", "socgpu_tune_set",
+    "socgpu_server_create", "socgpu_server_submit", "socgpu_server_wait", "socgpu_server_stats_get",
+    "socgpu_server_destroy",
 )
 
 _CALC_ARGS = [C.POINTER(Control), C.POINTER(Dimen), C.c_int, C.POINTER(Atm), C.POINTER(Cld), C.POINTER(Aer),
@@ -157,6 +171,13 @@ def declare(lib: C.CDLL) -> C.CDLL:
     lib.socgpu_tune_get.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                     C.POINTER(C.c_int)]
     lib.socgpu_tune_set.argtypes = [C.c_int] * 6
+    lib.socgpu_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]
+    lib.socgpu_server_submit.argtypes = [C.c_void_p, C.POINTER(BatchItem), C.POINTER(C.c_longlong), C.c_char_p,
+                                         C.c_size_t]
+    lib.socgpu_server_wait.argtypes = [C.c_void_p, C.c_longlong, C.c_double, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_char_p, C.c_size_t]
+    lib.socgpu_server_stats_get.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    lib.socgpu_server_destroy.argtypes = [C.c_void_p]
     lib.socgpu_kernel_launch_count.restype = C.c_longlong
     lib.socgpu_set_device.argtypes = [C.c_int]
     lib.socgpu_set_tile_config.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]

@@ -20,7 +20,7 @@
 #include <tuple>
 #include <vector>
 
-#include "socgpu_internal.h"
+#include "host_internal.h"
 
 namespace socgpu {
 
@@ -40,8 +40,6 @@ int launch_cloud_gen_noalloc(int nd_layer, int cloud_top, int n_layer, int nd_pr
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
-namespace {
-
 void set_msg(char *msg, size_t len, const char *fmt, ...) {
   if (!msg || len == 0) return;
   va_list ap;
@@ -50,25 +48,10 @@ void set_msg(char *msg, size_t len, const char *fmt, ...) {
   va_end(ap);
 }
 
-#define CUDA_TRY(expr)                                                                  \
-  do {                                                                                  \
-    cudaError_t e_ = (expr);                                                            \
-    if (e_ != cudaSuccess) {                                                            \
-      set_msg(msg, msg_len, "%s failed: %s", #expr, cudaGetErrorString(e_));            \
-      return SOCGPU_I_ABORT_CALCULATION;                                                \
-    }                                                                                   \
-  } while (0)
+namespace {
 
 // ---------------------------------------------------------------------------
 // Spectrum registry.
-struct SpectrumEntry {
-  std::string name;
-  SpectrumDev dev{};
-  std::vector<BandInfo> bands_host;
-  std::vector<GPoint> gpoints_host;
-  int device = 0;
-};
-
 std::mutex g_reg_mutex;
 std::map<int, std::unique_ptr<SpectrumEntry>> g_spectra;
 std::map<std::string, int> g_names;
@@ -258,6 +241,8 @@ void free_spectrum(SpectrumEntry &e) {
   cudaFree(e.dev.ice_parm_f);
 }
 
+}  // namespace
+
 SpectrumEntry *find_spectrum(int h) {
   std::lock_guard<std::mutex> lk(g_reg_mutex);
   auto it = g_spectra.find(h);
@@ -266,13 +251,7 @@ SpectrumEntry *find_spectrum(int h) {
 
 // ---------------------------------------------------------------------------
 // Kernel variants and tile choice.
-using LaunchFn = int (*)(const FluxParams &, const TileConfig &, cudaStream_t, char *, size_t);
-using PrepareFn = int (*)(BatchGroup &, char *, size_t);
-struct FluxVariant {
-  int precision, mode, lanes;
-  LaunchFn launch;
-  PrepareFn prepare;
-};
+namespace {
 #define SOCGPU_VARIANT(p, m, l) {p, m, l, launch_flux_##p##_##m##_##l, prepare_flux_##p##_##m##_##l}
 const FluxVariant kVariants[] = {
     SOCGPU_VARIANT(0, 0, 16), SOCGPU_VARIANT(0, 0, 32), SOCGPU_VARIANT(0, 1, 16), SOCGPU_VARIANT(0, 1, 32),
@@ -281,6 +260,7 @@ const FluxVariant kVariants[] = {
     SOCGPU_VARIANT(1, 2, 8),  SOCGPU_VARIANT(1, 2, 16), SOCGPU_VARIANT(1, 2, 32),
 };
 #undef SOCGPU_VARIANT
+}  // namespace
 
 const FluxVariant *find_variant(int precision, int mode, int lanes) {
   for (const FluxVariant &v : kVariants)
@@ -497,6 +477,121 @@ int launch(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *
 }
 
 // ---------------------------------------------------------------------------
+// Staging of a host-pointer call.
+void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntry *s, const socgpu_atm *a,
+                       const socgpu_cld *cl, const socgpu_aer *ae, const socgpu_bound *b, socgpu_radout *r) {
+  control = c; dimen = dm; sp = s; atm = a; cld = cl; aer = ae; bound = b; radout = r;
+  plan = Plan{};
+  const size_t ndp = dm->nd_profile, ndl = dm->nd_layer, np = a->n_profile, nl = a->n_layer;
+  const size_t nb = s->dev.n_band, ns = std::max(1, s->dev.n_species);
+  sw = c->isolir == SOCGPU_IP_SOLAR;
+  mc = c->i_cloud == SOCGPU_IP_CLOUD_MCICA;
+  aero = c->l_aerosol_mode && ae && ae->n_mode > 0;
+  const size_t D = sizeof(double), none = (size_t)-1;
+  // inputs: (nd_profile, rows) arrays copied with their valid profiles only;
+  // t_level feeds only the infra-red Planck terms, t_ground only the IR surface
+  o_p = plan.add(a->p, D, ndp, np, nl);
+  o_t = plan.add(a->t, D, ndp, np, nl);
+  o_tl = !sw ? plan.add(a->t_level, D, ndp, np, nl + 1) : none;
+  o_m = plan.add(a->mass, D, ndp, np, nl);
+  o_g = c->l_gas ? plan.add(a->gas_mix_ratio, D, ndp, np, ndl * ns) : none;
+  o_z = sw ? plan.add(b->zen_0, D, ndp, np, 1) : none;
+  o_si = sw ? plan.add(b->solar_irrad, D, ndp, np, 1) : none;
+  o_alb = plan.add(b->rho_alb, D, ndp, np, 2 * nb);
+  o_tg = !sw ? plan.add(b->t_ground, D, ndp, np, 1) : none;
+  o_amr = o_aab = o_asc = o_aas = none;
+  const size_t ndm = dm->nd_aerosol_mode;
+  if (aero) {
+    o_amr = plan.add(ae->mode_mix_ratio, D, ndp, np, ndl * ndm);
+    o_aab = plan.add(ae->mode_absorption, D, ndp, np, ndl * ndm * nb);
+    o_asc = plan.add(ae->mode_scattering, D, ndp, np, ndl * ndm * nb);
+    o_aas = plan.add(ae->mode_asymmetry, D, ndp, np, ndl * ndm * nb);
+  }
+  o_wb = c->weight_band ? plan.add(c->weight_band, D, nb, nb, 1) : none;
+  o_cmr = o_cdc = o_wc = o_fc = o_cs = o_fcl = o_nsc = o_sk = o_fsk = o_sro = none;
+  if (mc) {
+    const size_t ndc = ndl - (dm->id_cloud_top - 1);
+    const size_t ncc = std::max(1, dm->nd_cloud_component), nct = std::max(1, dm->nd_cloud_type);
+    o_cmr = plan.add(cl->condensed_mix_ratio, D, ndp, np, ndc * ncc);
+    o_cdc = plan.add(cl->condensed_dim_char, D, ndp, np, ndc * ncc);
+    o_wc = plan.add(cl->w_cloud, D, ndp, np, ndc);
+    o_fc = plan.add(cl->frac_cloud, D, ndp, np, ndc * nct);
+    o_cs = plan.add(cl->c_sub, D, ndp, np, ndc * cl->n_subcol_gen);
+    o_fcl = plan.add(cl->frac_cloudy, D, ndp, np, 1);
+    if (cl->n_subcol_cld) o_nsc = plan.add(cl->n_subcol_cld, sizeof(int), ndp, np, 1);
+    const size_t ndb = s->dev.nd_band, ndk = s->dev.nd_k_term;
+    o_sk = plan.add(cl->subcol_k, sizeof(int), ndb * ndk, ndb * ndk, 1);
+    o_fsk = plan.add(cl->first_subcol_k, sizeof(int), ndb * (ndk + 1), ndb * (ndk + 1), 1);
+    o_sro = plan.add(cl->subcol_reorder, sizeof(int), cl->n_subcol_req, cl->n_subcol_req, 1);
+  }
+  n_inputs = plan.slots.size();
+  o_fu = plan.add(nullptr, D, ndp, np, nl + 1, true, r->flux_up);
+  o_fd = plan.add(nullptr, D, ndp, np, nl + 1, true, r->flux_down);
+  o_fdir = (sw && r->flux_direct) ? plan.add(nullptr, D, ndp, np, nl + 1, true, r->flux_direct) : none;
+  o_div = r->flux_div ? plan.add(nullptr, D, ndp, np, nl, true, r->flux_div) : none;
+  o_hr = r->heating_rate ? plan.add(nullptr, D, ndp, np, nl, true, r->heating_rate) : none;
+}
+
+int StagedCall::copy_in(char *base, cudaStream_t s, char *msg, size_t msg_len) const {
+  for (size_t k = 0; k < n_inputs; ++k) {
+    const Slot &sl = plan.slots[k];
+    if (sl.row_bytes == 0) continue;
+    CUDA_TRY(cudaMemcpy2DAsync(base + sl.off, sl.dev_pitch, sl.host, sl.host_pitch, sl.row_bytes, sl.rows,
+                               cudaMemcpyHostToDevice, s));
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+int StagedCall::copy_out(char *base, cudaStream_t s, char *msg, size_t msg_len) const {
+  for (size_t k = n_inputs; k < plan.slots.size(); ++k) {
+    const Slot &sl = plan.slots[k];
+    if (sl.row_bytes == 0) continue;
+    CUDA_TRY(cudaMemcpy2DAsync(sl.out_host, sl.host_pitch, base + sl.off, sl.dev_pitch, sl.row_bytes, sl.rows,
+                               cudaMemcpyDeviceToHost, s));
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+void StagedCall::params(char *base, FluxParams &p) const {
+  auto dptr = [&](size_t off) -> void * { return off == (size_t)-1 ? nullptr : (void *)(base + off); };
+  socgpu_atm a2 = *atm;
+  a2.p = (const double *)dptr(o_p); a2.t = (const double *)dptr(o_t); a2.t_level = (const double *)dptr(o_tl);
+  a2.mass = (const double *)dptr(o_m); a2.gas_mix_ratio = (const double *)dptr(o_g); a2.p_level = nullptr;
+  socgpu_bound b2 = *bound;
+  b2.zen_0 = (const double *)dptr(o_z); b2.solar_irrad = (const double *)dptr(o_si);
+  b2.rho_alb = (const double *)dptr(o_alb); b2.t_ground = (const double *)dptr(o_tg);
+  socgpu_aer e2{};
+  if (aero) {
+    e2 = *aer;
+    e2.mode_mix_ratio = (const double *)dptr(o_amr); e2.mode_absorption = (const double *)dptr(o_aab);
+    e2.mode_scattering = (const double *)dptr(o_asc); e2.mode_asymmetry = (const double *)dptr(o_aas);
+  }
+  socgpu_cld c2{};
+  if (mc) {
+    c2 = *cld;
+    c2.condensed_mix_ratio = (const double *)dptr(o_cmr); c2.condensed_dim_char = (const double *)dptr(o_cdc);
+    c2.w_cloud = (const double *)dptr(o_wc); c2.frac_cloud = (const double *)dptr(o_fc);
+    c2.c_sub = (const double *)dptr(o_cs); c2.frac_cloudy = (const double *)dptr(o_fcl);
+    c2.n_subcol_cld = (const int *)dptr(o_nsc);
+    c2.subcol_k = (const int *)dptr(o_sk); c2.first_subcol_k = (const int *)dptr(o_fsk);
+    c2.subcol_reorder = (const int *)dptr(o_sro);
+  }
+  socgpu_radout r2{};
+  r2.flux_up = (double *)dptr(o_fu); r2.flux_down = (double *)dptr(o_fd);
+  r2.flux_direct = (double *)dptr(o_fdir); r2.flux_div = (double *)dptr(o_div);
+  r2.heating_rate = (double *)dptr(o_hr);
+  fill_params(p, control, dimen, sp, &a2, mc ? &c2 : nullptr, aero ? &e2 : nullptr, &b2, &r2,
+              (const double *)dptr(o_wb));
+}
+
+long long StagedCall::column_gpoints() const {
+  const int g0 = sp->dev.host_first_g[control->first_band - 1], g1 = sp->dev.host_first_g[control->last_band];
+  return (long long)atm->n_profile * (g1 - g0);
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
 // Per-thread device workspace for the host-pointer entry points.
 struct Workspace {
   int device = -1;
@@ -534,30 +629,6 @@ int ensure_workspace(size_t bytes, char *msg, size_t msg_len) {
   }
   return SOCGPU_I_NORMAL;
 }
-
-// A plan of device copies: each host array gets a 256-byte aligned slot.
-struct Slot {
-  const void *host;
-  void *out_host;
-  size_t off, rows, row_bytes, host_pitch, dev_pitch;
-  bool output;
-};
-
-struct Plan {
-  std::vector<Slot> slots;
-  size_t bytes = 0;
-  // Add an array of `rows` rows of `n_valid` elements each, with leading
-  // (Fortran) extent nd in host memory; on the device the same extent is kept.
-  size_t add(const void *host, size_t esize, size_t nd, size_t n_valid, size_t rows, bool output = false,
-             void *out_host = nullptr) {
-    if (!host && !out_host) return (size_t)-1;
-    size_t off = (bytes + 255) & ~(size_t)255;
-    Slot s{host, out_host, off, rows, n_valid * esize, nd * esize, nd * esize, output};
-    slots.push_back(s);
-    bytes = off + nd * esize * rows;
-    return off;
-  }
-};
 
 }  // namespace
 }  // namespace socgpu
@@ -781,105 +852,20 @@ int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dime
   SpectrumEntry *sp = find_spectrum(spectrum);
   int st = validate(control, dimen, sp, atm, cld, aer, bound, radout, msg, msg_len);
   if (st != SOCGPU_I_NORMAL) return st;
-  const size_t ndp = dimen->nd_profile, ndl = dimen->nd_layer, np = atm->n_profile, nl = atm->n_layer;
-  const size_t nb = sp->dev.n_band, ns = std::max(1, sp->dev.n_species);
-  const bool sw = control->isolir == SOCGPU_IP_SOLAR;
-  const bool mc = control->i_cloud == SOCGPU_IP_CLOUD_MCICA;
-  const bool aero = control->l_aerosol_mode && aer && aer->n_mode > 0;
-  Plan plan;
-  const size_t D = sizeof(double);
-  // inputs: (nd_profile, rows) arrays copied with their valid profiles only
-  size_t o_p = plan.add(atm->p, D, ndp, np, nl);
-  size_t o_t = plan.add(atm->t, D, ndp, np, nl);
-  size_t o_tl = !sw ? plan.add(atm->t_level, D, ndp, np, nl + 1) : (size_t)-1;
-  size_t o_m = plan.add(atm->mass, D, ndp, np, nl);
-  size_t o_g = control->l_gas ? plan.add(atm->gas_mix_ratio, D, ndp, np, ndl * ns) : (size_t)-1;
-  size_t o_z = sw ? plan.add(bound->zen_0, D, ndp, np, 1) : (size_t)-1;
-  size_t o_si = sw ? plan.add(bound->solar_irrad, D, ndp, np, 1) : (size_t)-1;
-  size_t o_alb = plan.add(bound->rho_alb, D, ndp, np, 2 * nb);
-  size_t o_tg = !sw ? plan.add(bound->t_ground, D, ndp, np, 1) : (size_t)-1;
-  size_t o_amr = (size_t)-1, o_aab = (size_t)-1, o_asc = (size_t)-1, o_aas = (size_t)-1;
-  const size_t ndm = dimen->nd_aerosol_mode;
-  if (aero) {
-    o_amr = plan.add(aer->mode_mix_ratio, D, ndp, np, ndl * ndm);
-    o_aab = plan.add(aer->mode_absorption, D, ndp, np, ndl * ndm * nb);
-    o_asc = plan.add(aer->mode_scattering, D, ndp, np, ndl * ndm * nb);
-    o_aas = plan.add(aer->mode_asymmetry, D, ndp, np, ndl * ndm * nb);
-  }
-  size_t o_wb = control->weight_band ? plan.add(control->weight_band, D, nb, nb, 1) : (size_t)-1;
-  size_t o_cmr = (size_t)-1, o_cdc = (size_t)-1, o_wc = (size_t)-1, o_fc = (size_t)-1, o_cs = (size_t)-1;
-  size_t o_fcl = (size_t)-1, o_nsc = (size_t)-1, o_sk = (size_t)-1, o_fsk = (size_t)-1, o_sro = (size_t)-1;
-  if (mc) {
-    const size_t ndc = ndl - (dimen->id_cloud_top - 1);
-    const size_t ncc = std::max(1, dimen->nd_cloud_component), nct = std::max(1, dimen->nd_cloud_type);
-    o_cmr = plan.add(cld->condensed_mix_ratio, D, ndp, np, ndc * ncc);
-    o_cdc = plan.add(cld->condensed_dim_char, D, ndp, np, ndc * ncc);
-    o_wc = plan.add(cld->w_cloud, D, ndp, np, ndc);
-    o_fc = plan.add(cld->frac_cloud, D, ndp, np, ndc * nct);
-    o_cs = plan.add(cld->c_sub, D, ndp, np, ndc * cld->n_subcol_gen);
-    o_fcl = plan.add(cld->frac_cloudy, D, ndp, np, 1);
-    if (cld->n_subcol_cld) o_nsc = plan.add(cld->n_subcol_cld, sizeof(int), ndp, np, 1);
-    const size_t ndb = sp->dev.nd_band, ndk = sp->dev.nd_k_term;
-    o_sk = plan.add(cld->subcol_k, sizeof(int), ndb * ndk, ndb * ndk, 1);
-    o_fsk = plan.add(cld->first_subcol_k, sizeof(int), ndb * (ndk + 1), ndb * (ndk + 1), 1);
-    o_sro = plan.add(cld->subcol_reorder, sizeof(int), cld->n_subcol_req, cld->n_subcol_req, 1);
-  }
-  const size_t n_inputs = plan.slots.size();
-  // outputs
-  size_t o_fu = plan.add(nullptr, D, ndp, np, nl + 1, true, radout->flux_up);
-  size_t o_fd = plan.add(nullptr, D, ndp, np, nl + 1, true, radout->flux_down);
-  size_t o_fdir = (sw && radout->flux_direct) ? plan.add(nullptr, D, ndp, np, nl + 1, true, radout->flux_direct) : (size_t)-1;
-  size_t o_div = radout->flux_div ? plan.add(nullptr, D, ndp, np, nl, true, radout->flux_div) : (size_t)-1;
-  size_t o_hr = radout->heating_rate ? plan.add(nullptr, D, ndp, np, nl, true, radout->heating_rate) : (size_t)-1;
-
-  st = ensure_workspace(plan.bytes, msg, msg_len);
+  StagedCall call;
+  call.stage(control, dimen, sp, atm, cld, aer, bound, radout);
+  st = ensure_workspace(call.plan.bytes, msg, msg_len);
   if (st != SOCGPU_I_NORMAL) return st;
   char *base = (char *)tl_ws.buf;
   cudaStream_t s = tl_ws.stream;
-  for (size_t k = 0; k < n_inputs; ++k) {
-    const Slot &sl = plan.slots[k];
-    if (sl.row_bytes == 0) continue;
-    CUDA_TRY(cudaMemcpy2DAsync(base + sl.off, sl.dev_pitch, sl.host, sl.host_pitch, sl.row_bytes, sl.rows,
-                               cudaMemcpyHostToDevice, s));
-  }
-  auto dptr = [&](size_t off) -> void * { return off == (size_t)-1 ? nullptr : (void *)(base + off); };
-  socgpu_atm a2 = *atm;
-  a2.p = (const double *)dptr(o_p); a2.t = (const double *)dptr(o_t); a2.t_level = (const double *)dptr(o_tl);
-  a2.mass = (const double *)dptr(o_m); a2.gas_mix_ratio = (const double *)dptr(o_g); a2.p_level = nullptr;
-  socgpu_bound b2 = *bound;
-  b2.zen_0 = (const double *)dptr(o_z); b2.solar_irrad = (const double *)dptr(o_si);
-  b2.rho_alb = (const double *)dptr(o_alb); b2.t_ground = (const double *)dptr(o_tg);
-  socgpu_aer e2{};
-  if (aero) {
-    e2 = *aer;
-    e2.mode_mix_ratio = (const double *)dptr(o_amr); e2.mode_absorption = (const double *)dptr(o_aab);
-    e2.mode_scattering = (const double *)dptr(o_asc); e2.mode_asymmetry = (const double *)dptr(o_aas);
-  }
-  socgpu_cld c2{};
-  if (mc) {
-    c2 = *cld;
-    c2.condensed_mix_ratio = (const double *)dptr(o_cmr); c2.condensed_dim_char = (const double *)dptr(o_cdc);
-    c2.w_cloud = (const double *)dptr(o_wc); c2.frac_cloud = (const double *)dptr(o_fc);
-    c2.c_sub = (const double *)dptr(o_cs); c2.frac_cloudy = (const double *)dptr(o_fcl);
-    c2.n_subcol_cld = (const int *)dptr(o_nsc);
-    c2.subcol_k = (const int *)dptr(o_sk); c2.first_subcol_k = (const int *)dptr(o_fsk);
-    c2.subcol_reorder = (const int *)dptr(o_sro);
-  }
-  socgpu_radout r2{};
-  r2.flux_up = (double *)dptr(o_fu); r2.flux_down = (double *)dptr(o_fd);
-  r2.flux_direct = (double *)dptr(o_fdir); r2.flux_div = (double *)dptr(o_div);
-  r2.heating_rate = (double *)dptr(o_hr);
+  st = call.copy_in(base, s, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) { cudaStreamSynchronize(s); return st; }
   FluxParams p;
-  fill_params(p, control, dimen, sp, &a2, mc ? &c2 : nullptr, aero ? &e2 : nullptr, &b2, &r2,
-              (const double *)dptr(o_wb));
+  call.params(base, p);
   st = launch(p, control, s, msg, msg_len);
   if (st != SOCGPU_I_NORMAL) { cudaStreamSynchronize(s); return st; }
-  for (size_t k = n_inputs; k < plan.slots.size(); ++k) {
-    const Slot &sl = plan.slots[k];
-    if (sl.row_bytes == 0) continue;
-    CUDA_TRY(cudaMemcpy2DAsync(sl.out_host, sl.host_pitch, base + sl.off, sl.dev_pitch, sl.row_bytes, sl.rows,
-                               cudaMemcpyDeviceToHost, s));
-  }
+  st = call.copy_out(base, s, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) { cudaStreamSynchronize(s); return st; }
   CUDA_TRY(cudaStreamSynchronize(s));
   return SOCGPU_I_NORMAL;
 }

@@ -1,0 +1,454 @@
+// server.cu -- continuous-batching request server (socgpu_server_*).
+//
+// Requests are radiance_calc calls with host arrays.  Every request's inputs
+// and outputs live in one device arena, sized at creation, while the request
+// is in flight.  One scheduler thread runs this loop:
+//   * it retires finished waves: their requests are marked done and their
+//     arena blocks freed;
+//   * when a stream slot is free, it admits queued requests in arrival order
+//     for as long as their blocks fit the arena (admission by free device
+//     memory), up to max_wave_requests, and launches them as one wave.
+// A wave copies its inputs in, runs one persistent batched launch per
+// kernel class (precision, mode, tile), copies the results out and records
+// an event, all on its stream slot's stream.  Up to `streams` waves are in
+// flight at once, so requests that arrive while others run are admitted as
+// soon as a slot and memory free up, and their work overlaps on the device.
+// The spectra stay device resident in the library's registry.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "host_internal.h"
+
+using namespace socgpu;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+// First-fit allocator over one device allocation; blocks are 256-byte
+// aligned and merged with their neighbours when freed.  Used by the
+// scheduler thread only.
+class Arena {
+ public:
+  void init(size_t bytes) {
+    size_ = bytes;
+    free_.clear();
+    free_[0] = bytes;
+    used_ = peak_ = 0;
+  }
+  bool alloc(size_t bytes, size_t *off) {
+    bytes = align256(bytes);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second < bytes) continue;
+      *off = it->first;
+      const size_t rest = it->second - bytes, start = it->first + bytes;
+      free_.erase(it);
+      if (rest) free_[start] = rest;
+      used_ += bytes;
+      peak_ = std::max(peak_, used_);
+      return true;
+    }
+    return false;
+  }
+  void release(size_t off, size_t bytes) {
+    bytes = align256(bytes);
+    used_ -= bytes;
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  size_t size() const { return size_; }
+  size_t peak() const { return peak_; }
+
+ private:
+  size_t size_ = 0, used_ = 0, peak_ = 0;
+  std::map<size_t, size_t> free_;
+};
+
+struct Request {
+  long long ticket = 0;
+  socgpu_control control{};
+  socgpu_dimen dimen{};
+  socgpu_atm atm{};
+  socgpu_cld cld{};
+  socgpu_aer aer{};
+  socgpu_bound bound{};
+  socgpu_radout radout{};
+  bool has_cld = false, has_aer = false;
+  StagedCall call;
+  size_t bytes = 0, off = 0;
+  long long colg = 0;
+  Clock::time_point t_submit, t_start, t_done;
+  int status = SOCGPU_I_NORMAL;
+  bool done = false;
+  std::string msg;
+};
+
+struct StreamSlot {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  FluxParams *d_items = nullptr, *h_items = nullptr;     // per-wave kernel tables
+  long long *d_start = nullptr, *h_start = nullptr;
+  bool busy = false;
+  std::vector<Request *> reqs;
+};
+
+}  // namespace
+
+struct socgpu_server_s {
+  socgpu_server_config cfg{};
+  int device = 0;
+  char *dmem = nullptr;
+  Arena arena;
+  std::vector<StreamSlot> slots;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request *> pending;
+  std::unordered_map<long long, std::unique_ptr<Request>> requests;
+  long long next_ticket = 1;
+  bool stop = false;
+  std::thread worker;
+  socgpu_server_stats stats{};
+};
+
+namespace {
+
+// Retire a finished wave (called with the server mutex held).
+void finish(socgpu_server_s &S, StreamSlot &sl, cudaError_t e) {
+  const Clock::time_point now = Clock::now();
+  for (Request *r : sl.reqs) {
+    r->t_done = now;
+    if (e != cudaSuccess && r->status == SOCGPU_I_NORMAL) {
+      r->status = SOCGPU_I_ABORT_CALCULATION;
+      r->msg = std::string("wave failed on the device: ") + cudaGetErrorString(e);
+    }
+    r->done = true;
+    S.arena.release(r->off, r->bytes);
+    S.stats.completed += 1;
+    if (r->status == SOCGPU_I_NORMAL) S.stats.column_gpoints += r->colg;
+  }
+  sl.reqs.clear();
+  sl.busy = false;
+}
+
+void fail_all(std::vector<Request *> &wave, int status, const char *msg) {
+  for (Request *r : wave) {
+    if (r->status == SOCGPU_I_NORMAL) {
+      r->status = status;
+      r->msg = msg;
+    }
+  }
+}
+
+// Enqueue one wave on its slot's stream (called without the mutex; the
+// slot is already marked busy and owns the requests).
+void launch_wave(socgpu_server_s &S, StreamSlot &sl) {
+  std::vector<Request *> &wave = sl.reqs;
+  cudaStream_t st = sl.stream;
+  char msg[512] = "";
+  const size_t msg_len = sizeof(msg);
+  const Clock::time_point now = Clock::now();
+  for (Request *r : wave) r->t_start = now;
+  // inputs
+  for (Request *r : wave)
+    if (r->call.copy_in(S.dmem + r->off, st, msg, msg_len) != SOCGPU_I_NORMAL) {
+      fail_all(wave, SOCGPU_I_ABORT_CALCULATION, msg);
+      cudaEventRecord(sl.done, st);
+      return;
+    }
+  // kernel classes of the wave
+  std::map<std::tuple<int, int, int, int, int>, std::vector<int>> classes;
+  std::vector<FluxParams> params(wave.size());
+  for (size_t i = 0; i < wave.size(); ++i) {
+    Request *r = wave[i];
+    r->call.params(S.dmem + r->off, params[i]);
+    const int mode = mode_index(&r->control);
+    TileConfig t = choose_tile(r->control.precision, mode, r->atm.n_layer);
+    classes[std::make_tuple(r->control.precision, mode, t.lanes_per_solve, t.chunk, t.warps_per_cta)].push_back(
+        (int)i);
+  }
+  size_t n_item = 0, n_start = 0;
+  std::vector<BatchGroup> groups;
+  std::vector<std::pair<size_t, size_t>> table_off;
+  for (auto &kv : classes) {
+    BatchGroup g{};
+    g.precision = std::get<0>(kv.first);
+    g.mode = std::get<1>(kv.first);
+    g.tile = TileConfig{std::get<2>(kv.first), std::get<4>(kv.first), std::get<3>(kv.first)};
+    FluxParams *items = sl.h_items + n_item;
+    long long *start = sl.h_start + n_start;
+    start[0] = 0;
+    int k = 0;
+    for (int i : kv.second) {
+      items[k] = params[i];
+      start[k + 1] = start[k] + params[i].n_profile;
+      ++k;
+    }
+    g.items = items;
+    g.col_start = start;
+    g.n_items = k;
+    g.total = start[k];
+    const FluxVariant *v = find_variant(g.precision, g.mode, g.tile.lanes_per_solve);
+    if (!v || v->prepare(g, msg, msg_len) != SOCGPU_I_NORMAL) {
+      if (!v) snprintf(msg, msg_len, "no kernel built for %d lanes per solve", g.tile.lanes_per_solve);
+      fail_all(wave, SOCGPU_I_ERR_RANGE, msg);
+      cudaEventRecord(sl.done, st);
+      return;
+    }
+    groups.push_back(g);
+    table_off.emplace_back(n_item, n_start);
+    n_item += k;
+    n_start += k + 1;
+  }
+  cudaError_t e = cudaMemcpyAsync(sl.d_items, sl.h_items, sizeof(FluxParams) * n_item, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(sl.d_start, sl.h_start, sizeof(long long) * n_start, cudaMemcpyHostToDevice, st);
+  for (size_t gi = 0; gi < groups.size() && e == cudaSuccess; ++gi) {
+    const BatchGroup &g = groups[gi];
+    if (g.total <= 0) continue;
+    FluxParams *di = sl.d_items + table_off[gi].first;
+    long long *ds = sl.d_start + table_off[gi].second;
+    int n = g.n_items;
+    long long total = g.total;
+    void *args[] = {&di, &ds, &n, &total};
+    e = cudaLaunchKernel(g.kernel, dim3(g.grid), dim3(g.threads), args, g.smem, st);
+    count_launch();
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail_all(wave, SOCGPU_I_ABORT_CALCULATION, cudaGetErrorString(e));
+    cudaEventRecord(sl.done, st);
+    return;
+  }
+  for (Request *r : wave)
+    if (r->call.copy_out(S.dmem + r->off, st, msg, msg_len) != SOCGPU_I_NORMAL) fail_all(wave, SOCGPU_I_ABORT_CALCULATION, msg);
+  cudaEventRecord(sl.done, st);
+}
+
+void worker_main(socgpu_server_s *Sp) {
+  socgpu_server_s &S = *Sp;
+  cudaSetDevice(S.device);
+  std::unique_lock<std::mutex> lk(S.mu);
+  for (;;) {
+    bool progressed = false;
+    for (StreamSlot &sl : S.slots) {
+      if (!sl.busy) continue;
+      cudaError_t e = cudaEventQuery(sl.done);
+      if (e == cudaErrorNotReady) continue;
+      finish(S, sl, e);
+      progressed = true;
+    }
+    if (progressed) S.cv_done.notify_all();
+    StreamSlot *free_slot = nullptr;
+    for (StreamSlot &sl : S.slots)
+      if (!sl.busy) { free_slot = &sl; break; }
+    if (free_slot && !S.pending.empty()) {
+      std::vector<Request *> wave;
+      while (!S.pending.empty() && (int)wave.size() < S.cfg.max_wave_requests) {
+        Request *r = S.pending.front();
+        size_t off = 0;
+        if (!S.arena.alloc(r->bytes, &off)) break;
+        r->off = off;
+        wave.push_back(r);
+        S.pending.pop_front();
+      }
+      if (!wave.empty()) {
+        free_slot->busy = true;
+        free_slot->reqs = std::move(wave);
+        S.stats.waves += 1;
+        S.stats.max_wave_requests = std::max<long long>(S.stats.max_wave_requests, (long long)free_slot->reqs.size());
+        S.stats.peak_bytes = S.arena.peak();
+        lk.unlock();
+        launch_wave(S, *free_slot);
+        lk.lock();
+        progressed = true;
+      }
+    }
+    bool any_busy = false;
+    for (StreamSlot &sl : S.slots) any_busy |= sl.busy;
+    if (S.stop && S.pending.empty() && !any_busy) break;
+    if (!progressed) {
+      if (any_busy) {
+        lk.unlock();
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+        lk.lock();
+      } else {
+        S.cv_work.wait(lk, [&] { return S.stop || !S.pending.empty(); });
+      }
+    }
+  }
+}
+
+void destroy_server(socgpu_server_s *S) {
+  for (StreamSlot &sl : S->slots) {
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+    if (sl.d_items) cudaFree(sl.d_items);
+    if (sl.d_start) cudaFree(sl.d_start);
+    if (sl.h_items) cudaFreeHost(sl.h_items);
+    if (sl.h_start) cudaFreeHost(sl.h_start);
+  }
+  if (S->dmem) cudaFree(S->dmem);
+  delete S;
+}
+
+}  // namespace
+
+extern "C" {
+
+int socgpu_server_create(const socgpu_server_config *config, socgpu_server *server, char *msg, size_t msg_len) {
+  if (!server) { set_msg(msg, msg_len, "null argument"); return SOCGPU_I_ERR_FATAL; }
+  socgpu_server_config cfg{};
+  if (config) cfg = *config;
+  if (cfg.streams <= 0) cfg.streams = 4;
+  if (cfg.max_wave_requests <= 0) cfg.max_wave_requests = 256;
+  if (cfg.streams > 64 || cfg.max_wave_requests > 65536) {
+    set_msg(msg, msg_len, "streams (1..64) or max_wave_requests (1..65536) out of range");
+    return SOCGPU_I_ERR_RANGE;
+  }
+  std::unique_ptr<socgpu_server_s> S(new socgpu_server_s);
+  CUDA_TRY(cudaGetDevice(&S->device));
+  if (cfg.device_bytes == 0) {
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    cfg.device_bytes = free_b / 2;
+  }
+  cfg.device_bytes = align256(cfg.device_bytes);
+  S->cfg = cfg;
+  S->arena.init(cfg.device_bytes);
+  cudaError_t e = cudaMalloc(&S->dmem, cfg.device_bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_msg(msg, msg_len, "device arena of %zu bytes not available: %s", cfg.device_bytes, cudaGetErrorString(e));
+    return SOCGPU_I_ERR_RANGE;
+  }
+  S->slots.resize(cfg.streams);
+  const size_t n_items = cfg.max_wave_requests;
+  // a wave has at most one kernel class per request, so n_items + 1 starts per class fit in 2 n_items + 1
+  const size_t n_start = 2 * n_items + 1;
+  for (StreamSlot &sl : S->slots) {
+    if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc(&sl.d_items, sizeof(FluxParams) * n_items) != cudaSuccess ||
+        cudaMalloc(&sl.d_start, sizeof(long long) * n_start) != cudaSuccess ||
+        cudaMallocHost(&sl.h_items, sizeof(FluxParams) * n_items) != cudaSuccess ||
+        cudaMallocHost(&sl.h_start, sizeof(long long) * n_start) != cudaSuccess) {
+      cudaGetLastError();
+      set_msg(msg, msg_len, "stream slot resources not available");
+      destroy_server(S.release());
+      return SOCGPU_I_ABORT_CALCULATION;
+    }
+  }
+  S->stats.device_bytes = cfg.device_bytes;
+  socgpu_server_s *raw = S.release();
+  raw->worker = std::thread(worker_main, raw);
+  *server = raw;
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_server_submit(socgpu_server server, const socgpu_request *q, long long *ticket, char *msg,
+                         size_t msg_len) {
+  if (!server || !q || !ticket) { set_msg(msg, msg_len, "null argument"); return SOCGPU_I_ERR_FATAL; }
+  SpectrumEntry *sp = find_spectrum(q->spectrum);
+  int st = validate(q->control, q->dimen, sp, q->atm, q->cld, q->aer, q->bound, q->radout, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  std::unique_ptr<Request> r(new Request);
+  r->control = *q->control;
+  r->dimen = *q->dimen;
+  r->atm = *q->atm;
+  r->bound = *q->bound;
+  r->radout = *q->radout;
+  if (q->cld) { r->cld = *q->cld; r->has_cld = true; }
+  if (q->aer) { r->aer = *q->aer; r->has_aer = true; }
+  r->call.stage(&r->control, &r->dimen, sp, &r->atm, r->has_cld ? &r->cld : nullptr,
+                r->has_aer ? &r->aer : nullptr, &r->bound, &r->radout);
+  r->bytes = align256(r->call.plan.bytes);
+  r->colg = r->call.column_gpoints();
+  if (r->bytes > server->arena.size()) {
+    set_msg(msg, msg_len, "request needs %zu bytes of device memory, more than the server's %zu", r->bytes,
+            server->arena.size());
+    return SOCGPU_I_ERR_RANGE;
+  }
+  {
+    std::lock_guard<std::mutex> lk(server->mu);
+    if (server->stop) { set_msg(msg, msg_len, "server is shutting down"); return SOCGPU_I_ERR_FATAL; }
+    r->ticket = server->next_ticket++;
+    r->t_submit = Clock::now();
+    *ticket = r->ticket;
+    server->pending.push_back(r.get());
+    server->stats.submitted += 1;
+    server->requests[r->ticket] = std::move(r);
+  }
+  server->cv_work.notify_one();
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_server_wait(socgpu_server server, long long ticket, double timeout_s, int *status, double *queue_ms,
+                       double *latency_ms, char *msg, size_t msg_len) {
+  if (!server) { set_msg(msg, msg_len, "null argument"); return SOCGPU_I_ERR_FATAL; }
+  std::unique_lock<std::mutex> lk(server->mu);
+  auto it = server->requests.find(ticket);
+  if (it == server->requests.end()) { set_msg(msg, msg_len, "unknown ticket %lld", ticket); return SOCGPU_I_ERR_EXIST; }
+  Request *r = it->second.get();
+  auto ready = [&] { return r->done; };
+  if (timeout_s < 0) {
+    server->cv_done.wait(lk, ready);
+  } else if (!server->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) {
+    set_msg(msg, msg_len, "request %lld not finished", ticket);
+    return SOCGPU_SERVER_PENDING;
+  }
+  if (status) *status = r->status;
+  if (queue_ms) *queue_ms = std::chrono::duration<double, std::milli>(r->t_start - r->t_submit).count();
+  if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  if (r->status != SOCGPU_I_NORMAL) set_msg(msg, msg_len, "%s", r->msg.c_str());
+  server->requests.erase(it);
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_server_stats_get(socgpu_server server, socgpu_server_stats *stats) {
+  if (!server || !stats) return SOCGPU_I_ERR_FATAL;
+  std::lock_guard<std::mutex> lk(server->mu);
+  *stats = server->stats;
+  stats->peak_bytes = server->arena.peak();
+  stats->queued = (long long)server->pending.size();
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_server_destroy(socgpu_server server) {
+  if (!server) return SOCGPU_I_NORMAL;
+  {
+    std::lock_guard<std::mutex> lk(server->mu);
+    server->stop = true;
+  }
+  server->cv_work.notify_all();
+  if (server->worker.joinable()) server->worker.join();
+  destroy_server(server);
+  return SOCGPU_I_NORMAL;
+}
+
+}  // extern "C"

@@ -329,9 +329,11 @@ def add_clouds(col: Column, seed: int, n_subcol: int = 16, decorrelation_m: floa
     return col
 
 
-def window(col: Column, start: int, n: int) -> Column:
+def window(col: Column, start: int, n: int, alloc=None) -> Column:
     """Columns start .. start+n-1 of col as a new Column (copies, Fortran
-    order).  Per-column arrays are those whose first extent is n_profile."""
+    order).  Per-column arrays are those whose first extent is n_profile.
+    `alloc(shape, dtype)`, when given, provides the destination arrays
+    (e.g. in page-locked memory)."""
     import copy
     c = copy.copy(col)
     c.n_profile = n
@@ -339,7 +341,11 @@ def window(col: Column, start: int, n: int) -> Column:
 
     def cut(v):
         if isinstance(v, np.ndarray) and v.ndim >= 1 and v.shape[0] == col.n_profile:
-            return np.asfortranarray(v[sl])
+            if alloc is None:
+                return np.asfortranarray(v[sl])
+            out = alloc(v[sl].shape, v.dtype)
+            out[...] = v[sl]
+            return out
         return v
 
     for name in ("p", "t", "p_level", "t_level", "mass", "gas_mix_ratio", "z", "t_ground", "zen_0", "solar_irrad",

@@ -90,16 +90,61 @@ class Pools:
             return R.lw_control(i_cloud=abi.IP_CLOUD_MCICA, precision=precision)
         return R.sw_control(i_cloud=abi.IP_CLOUD_MCICA, precision=precision)
 
-    def request(self, s: RequestSpec, precision: int):
-        """(control, spectrum, column, mcica) of one request."""
+    def request(self, s: RequestSpec, precision: int, alloc=None):
+        """(control, spectrum, column, mcica) of one request; `alloc(shape,
+        dtype)` places the request's arrays (e.g. PinnedArena.take)."""
         sp, col, mc = self.pool[(s.kind, s.n_layer)]
-        c = synth.window(col, s.offset, s.n_profile)
+        c = synth.window(col, s.offset, s.n_profile, alloc)
         m = None
         if mc is not None:
             sl = slice(s.offset, s.offset + s.n_profile)
-            m = replace(mc, c_sub=np.asfortranarray(mc.c_sub[sl]), n_subcol_cld=np.ascontiguousarray(mc.n_subcol_cld[sl]),
-                        frac_cloudy=np.ascontiguousarray(mc.frac_cloudy[sl]))
+
+            def cut(v):
+                if alloc is None:
+                    return np.asfortranarray(v[sl]) if v.ndim > 1 else np.ascontiguousarray(v[sl])
+                out = alloc(v[sl].shape, v.dtype)
+                out[...] = v[sl]
+                return out
+            m = replace(mc, c_sub=cut(mc.c_sub), n_subcol_cld=cut(mc.n_subcol_cld), frac_cloudy=cut(mc.frac_cloudy))
         return self.control(s.kind, precision), sp, c, m
+
+
+class PinnedArena:
+    """Page-locked host memory handed out as Fortran-ordered numpy arrays
+    (bump allocation; freed as a whole)."""
+
+    def __init__(self, nbytes: int):
+        import torch
+        self._buf = torch.empty(int(nbytes), dtype=torch.uint8, pin_memory=True)
+        self._mem = self._buf.numpy()
+        self._off = 0
+
+    def take(self, shape, dtype) -> np.ndarray:
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        off = (self._off + 255) & ~255
+        if off + n > self._mem.size:
+            raise MemoryError("pinned arena exhausted")
+        self._off = off + n
+        return np.ndarray(shape, dtype=dtype, buffer=self._mem, offset=off, order="F")
+
+    def reset(self) -> None:
+        self._off = 0
+
+
+def pin_outputs(m: R.Marshal, alloc) -> R.Marshal:
+    """Point a Marshal's outputs at arrays from `alloc` (page-locked)."""
+    import ctypes as C
+    dp = C.POINTER(C.c_double)
+    for name in ("flux_up", "flux_down", "flux_direct", "flux_div", "heating_rate"):
+        a = getattr(m, name)
+        if a is None:
+            continue
+        b = alloc(a.shape, a.dtype)
+        b[...] = 0.0
+        setattr(m, name, b)
+        setattr(m.radout, name, b.ctypes.data_as(dp))
+    return m
 
 
 def n_gpoint(kind: str) -> int:
