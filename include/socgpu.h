@@ -36,7 +36,7 @@ extern "C" {
 #define SOCGPU_API
 #endif
 
-#define SOCGPU_ABI_VERSION 1
+#define SOCGPU_ABI_VERSION 2
 
 /* ---- status codes: rad_pcf.F90:391-405 ------------------------------- */
 #define SOCGPU_I_NORMAL             0
@@ -101,6 +101,10 @@ extern "C" {
 #define SOCGPU_IP_SCALE_DOPPLER_QUAD    3
 /* Rayleigh schemes, rad_pcf.F90:729-731 */
 #define SOCGPU_IP_RAYLEIGH_TOTAL        1
+/* Continuum types (rad_pcf.F90 ip_self_continuum, ip_frn_continuum) */
+#define SOCGPU_IP_SELF_CONTINUUM 1
+#define SOCGPU_IP_FRN_CONTINUUM  2
+
 /* McICA overlap (socrates_cloud_gen.F90 ioverlap), rad_pcf.F90:294-300 */
 #define SOCGPU_IP_MAX_RAND              0
 #define SOCGPU_IP_RAND                  1
@@ -170,6 +174,16 @@ typedef struct socgpu_spectrum_desc {
     const int    *l_ice_type;           /* (nd_ice_type) or NULL */
     const int    *i_ice_parm;           /* (nd_ice_type) */
     const double *ice_parm_list;        /* (nd_cloud_parameter, nd_band, nd_ice_type) */
+    /* StrSpecCont, blocks 8 and 9 (NULL n_band_continuum: no continua) */
+    int nd_continuum;
+    const int    *n_band_continuum;     /* (nd_band) */
+    const int    *index_continuum;      /* (nd_band, nd_continuum): SOCGPU_IP_SELF_CONTINUUM / FRN */
+    int index_water;                    /* 1-based absorber index of water vapour */
+    const int    *i_scale_fnc_cont;     /* (nd_band, nd_continuum) */
+    const double *k_cont;               /* (nd_band, nd_continuum) [m5/(kg mol)] */
+    const double *scale_cont;           /* (nd_scale_variable, nd_band, nd_continuum) */
+    const double *p_ref_cont;           /* (nd_continuum, nd_band) [Pa] */
+    const double *t_ref_cont;           /* (nd_continuum, nd_band) [K] */
 } socgpu_spectrum_desc;
 
 typedef int32_t socgpu_spectrum_handle;   /* > 0 when valid */
@@ -196,6 +210,8 @@ typedef struct socgpu_control {
     const double *weight_band;  /* (n_band) or NULL (all 1); device memory for
                                    socgpu_radiance_calc_device */
     int precision;              /* SOCGPU_PRECISION_* (extension) */
+    int l_continuum;            /* water-vapour continuum absorption (blocks 8 and 9) */
+    int l_mixing_ratio;         /* gas amounts per unit mass of dry air (foreign continuum) */
 } socgpu_control;
 
 /* ---- StrDim subset (src/radiance_core/def_dimen.F90) ----------------- */
@@ -216,6 +232,7 @@ typedef struct socgpu_atm {
     const double *t_level;       /* (nd_profile, 0:nd_layer) [K] */
     const double *mass;          /* (nd_profile, nd_layer) [kg/m2] */
     const double *gas_mix_ratio; /* (nd_profile, nd_layer, nd_species) [kg/kg] */
+    const double *density;       /* (nd_profile, nd_layer) [kg/m3]; needed with l_continuum */
 } socgpu_atm;
 
 /* ---- StrBound (src/radiance_core/def_bound.F90) ----------------------- */

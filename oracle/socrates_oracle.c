@@ -268,7 +268,7 @@ static void single_scatter_cell(const socgpu_control *c, double k_grey_tot, doub
  * leading dimension `wp`; caller arrays keep dimen->nd_profile.          */
 typedef struct {
     int wp, ndl, n_profile, n_layer;
-    double *k_grey_tot, *k_ext_scat, *phase_fnc, *forward_scatter;
+    double *k_grey_tot, *k_ext_scat, *phase_fnc, *forward_scatter, *cont_amount;
     double *phase_fnc_nc, *forward_scatter_nc;
     double *k_ext_tot_cc, *k_ext_scat_cc, *phf_cc, *fwd_cc;   /* per cloud component */
     double *gfr;                                              /* per absorber of the band */
@@ -304,7 +304,7 @@ static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(doub
     X(s_up, pl) X(s_down, pl) X(source_ground, wp) \
     X(flux_direct, pl1) X(flux_direct_dir, pl1) X(flux_total, pl2) \
     X(flux_direct_acc, pl1) X(flux_total_acc, pl2) X(flux_direct_clear, pl1) X(flux_total_clear, pl2) \
-    X(alpha, wp) X(s_up_prime, wp) X(beta, pl) X(gam, pl) X(h, pl)
+    X(alpha, wp) X(s_up_prime, wp) X(beta, pl) X(gam, pl) X(h, pl) X(cont_amount, pl)
 
 static void work_init(work *w, int wp, int ndl, int n_profile, int n_layer, int nc, int na)
 {
@@ -471,8 +471,45 @@ static void clear_coefficients(work *w, const socgpu_control *c, const double *m
  * Cloud-component optics through opt_prop_pade_2
  * (opt_prop_pade_2_mod.F90:99-140, the rescaled n_order_forward=2 path of
  * opt_prop_water_cloud.F90:212-219 and opt_prop_ice_cloud.F90:228-236). */
+/* Physical constants (rad_ccf.F90:42-58, gas_list_pcf.F90:303-306). */
+#define MOL_WEIGHT_AIR 28.966e-03
+#define REPSILON (18.0153 / 28.966)
+
+/* rescale_continuum (rescale_continuum.F90): amount of continuum j of band
+ * b in every layer, from the p/T scaling and the water vapour. */
+static void rescale_continuum(const socgpu_control *c, const socgpu_spectrum_desc *d, const socgpu_atm *atm,
+                              int ndp, int ndl, int n_profile, int n_layer, int b, int j, double *amount, int wp)
+{
+    const int ndb = d->nd_band, ndc = d->nd_continuum;
+    const int i_cont = d->index_continuum[b + ndb * j];
+    const int fnc = d->i_scale_fnc_cont[b + ndb * j];
+    const double p_ref = d->p_ref_cont[j + ndc * b], t_ref = d->t_ref_cont[j + ndc * b];
+    const double *sc = d->scale_cont + (size_t)d->nd_scale_variable * ((size_t)b + (size_t)ndb * j);
+    const int iw = d->index_water - 1;
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < n_profile; ++l) {
+            double p = IX2(atm->p, l, i, ndp), t = IX2(atm->t, l, i, ndp);
+            double a = pow(p / p_ref, sc[0]);
+            if (fnc == SOCGPU_IP_SCALE_POWER_LAW) a = a * pow(t / t_ref, sc[1]);
+            else if (fnc == SOCGPU_IP_SCALE_POWER_QUAD) {
+                double x = t / t_ref - 1.0e+00;
+                a = a * (1.0e+00 + sc[1] * x + sc[2] * (x * x));
+            }
+            double water = IX3(atm->gas_mix_ratio, l, i, iw, ndp, ndl);
+            double rho = IX2(atm->density, l, i, ndp);
+            if (i_cont == SOCGPU_IP_SELF_CONTINUUM) {
+                double molar_density_water = rho * water / (REPSILON * MOL_WEIGHT_AIR);
+                a = a * molar_density_water * water;
+            } else if (i_cont == SOCGPU_IP_FRN_CONTINUUM) {
+                if (c->l_mixing_ratio) a = a * rho * water / MOL_WEIGHT_AIR;
+                else a = a * rho * water * (1.0 - water) / MOL_WEIGHT_AIR;
+            }
+            IX2(amount, l, i, wp) = a;
+        }
+}
+
 static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *dm,
-                         const socgpu_spectrum_desc *d, const socgpu_aer *aer,
+                         const socgpu_spectrum_desc *d, const socgpu_atm *atm, const socgpu_aer *aer,
                          const socgpu_cld *cld, int b, int l_cloud)
 {
     int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp, ndl = w->ndl;
@@ -511,6 +548,16 @@ static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *d
                                 + k_scatter * pow(g, (double)c->n_order_forward);
                     }
                 }
+    }
+    /* continuum absorption (grey_opt_prop.F90:801-817) */
+    if (c->l_continuum && d->n_band_continuum) {
+        for (int j = 0; j < d->n_band_continuum[b]; ++j) {
+            const double kc = d->k_cont[b + d->nd_band * j];
+            rescale_continuum(c, d, atm, ndp, ndl, n_profile, n_layer, b, j, w->cont_amount, wp);
+            for (int i = 0; i < n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l)
+                    IX2(w->k_grey_tot, l, i, wp) = IX2(w->k_grey_tot, l, i, wp) + kc * IX2(w->cont_amount, l, i, wp);
+        }
     }
     for (int i = 0; i < n_layer; ++i)
         for (int l = 0; l < n_profile; ++l)
@@ -773,6 +820,9 @@ static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
         set_msg(msg, msg_len, "band range outside the spectrum"); return SOCGPU_I_ERR_RANGE; }
     if (atm->n_profile < 0 || atm->n_profile > dm->nd_profile || atm->n_layer < 1 || atm->n_layer > dm->nd_layer) {
         set_msg(msg, msg_len, "profile/layer counts exceed their dimensions"); return SOCGPU_I_ERR_RANGE; }
+    if (c->l_continuum && d->n_band_continuum &&
+        (!atm->density || d->index_water < 1 || !d->k_cont || !d->scale_cont)) {
+        set_msg(msg, msg_len, "continuum absorption needs the layer density and water vapour"); return SOCGPU_I_ERR_FATAL; }
     if (c->isolir == SOCGPU_IP_INFRA_RED && !d->thermal_coeff) {
         set_msg(msg, msg_len, "infra-red calculation without Planck data"); return SOCGPU_I_ERR_FATAL; }
     if (c->isolir == SOCGPU_IP_SOLAR && !d->solar_flux_band) {
@@ -800,6 +850,7 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
     socgpu_atm atm = *atm0;
     atm.p += p0; atm.t += p0; atm.t_level += p0; atm.mass += p0; atm.gas_mix_ratio += p0;
     if (atm.p_level) atm.p_level += p0;
+    if (atm.density) atm.density += p0;
     socgpu_aer aerv, *aer = NULL;
     if (aer0) {
         aerv = *aer0; aer = &aerv;
@@ -849,7 +900,7 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
 
     for (int b = c->first_band - 1; b < c->last_band && status == SOCGPU_I_NORMAL; ++b) {
         double weight_band = c->weight_band ? c->weight_band[b] : 1.0;
-        status = grey_opt_prop(&w, c, dm, d, aer, cld, b, l_cloud);
+        status = grey_opt_prop(&w, c, dm, d, &atm, aer, cld, b, l_cloud);
         if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "unsupported optical property option"); break; }
 
         /* gas scaling of each absorber (radiance_calc.F90:1330-1470) */

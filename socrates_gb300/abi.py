@@ -35,7 +35,8 @@ IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0,
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RNG_LCG, RNG_PHILOX = 0, 1
 NOALLOC_MAX_CLOUD_LAYERS = 1024   # SOCGPU_NOALLOC_MAX_CLOUD_LAYERS
-ABI_VERSION = 1
+ABI_VERSION = 2
+IP_SELF_CONTINUUM, IP_FRN_CONTINUUM = 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -56,6 +57,8 @@ class SpectrumDesc(C.Structure):
         ("n_deg_fit", C.c_int), ("t_ref_planck", C.c_double), ("thermal_coeff", _dp),
         ("l_drop_type", _ip), ("i_drop_parm", _ip), ("drop_parm_list", _dp),
         ("l_ice_type", _ip), ("i_ice_parm", _ip), ("ice_parm_list", _dp),
+        ("nd_continuum", C.c_int), ("n_band_continuum", _ip), ("index_continuum", _ip), ("index_water", C.c_int),
+        ("i_scale_fnc_cont", _ip), ("k_cont", _dp), ("scale_cont", _dp), ("p_ref_cont", _dp), ("t_ref_cont", _dp),
     ]
 
 
@@ -67,6 +70,7 @@ class Control(C.Structure):
         ("l_rescale", C.c_int), ("n_order_forward", C.c_int), ("l_ir_source_quad", C.c_int),
         ("l_rayleigh", C.c_int), ("l_gas", C.c_int), ("l_aerosol_mode", C.c_int), ("l_flux_div", C.c_int),
         ("first_band", C.c_int), ("last_band", C.c_int), ("weight_band", _dp), ("precision", C.c_int),
+        ("l_continuum", C.c_int), ("l_mixing_ratio", C.c_int),
     ]
 
 
@@ -82,6 +86,7 @@ class Atm(C.Structure):
     _fields_ = [
         ("n_profile", C.c_int), ("n_layer", C.c_int),
         ("p", _dp), ("t", _dp), ("p_level", _dp), ("t_level", _dp), ("mass", _dp), ("gas_mix_ratio", _dp),
+        ("density", _dp),
     ]
 
 

@@ -52,6 +52,7 @@ class DeviceCase:
         self.atm.t_level = dev("t_level", col.t_level)
         self.atm.mass = dev("mass", col.mass)
         self.atm.gas_mix_ratio = dev("gas", col.gas_mix_ratio)
+        self.atm.density = dev("density", getattr(col, "density", None))
         self.bound = abi.Bound()
         self.bound.zen_0 = dev("zen_0", col.zen_0)
         self.bound.solar_irrad = dev("solar_irrad", col.solar_irrad)

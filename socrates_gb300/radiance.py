@@ -73,6 +73,8 @@ class Control:
     last_band: int = 0           # 0: all bands
     weight_band: np.ndarray | None = None
     precision: int = abi.PRECISION_FP64
+    l_continuum: bool = False
+    l_mixing_ratio: bool = False
 
     def as_struct(self, n_band: int, keep: list) -> abi.Control:
         c = abi.Control()
@@ -87,6 +89,7 @@ class Control:
         c.last_band = self.last_band if self.last_band > 0 else n_band
         c.weight_band = _dp(self.weight_band, keep)
         c.precision = self.precision
+        c.l_continuum, c.l_mixing_ratio = int(self.l_continuum), int(self.l_mixing_ratio)
         return c
 
 
@@ -195,6 +198,7 @@ class Marshal:
         a.p, a.t = _dp(col.p, k), _dp(col.t, k)
         a.p_level, a.t_level = _dp(col.p_level, k), _dp(col.t_level, k)
         a.mass, a.gas_mix_ratio = _dp(col.mass, k), _dp(col.gas_mix_ratio, k)
+        a.density = _dp(getattr(col, "density", None), k)
         self.atm = a
         b = abi.Bound()
         b.zen_0, b.solar_irrad = _dp(col.zen_0, k), _dp(col.solar_irrad, k)

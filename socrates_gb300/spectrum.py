@@ -21,6 +21,10 @@ GAS_NAMES = {1: "Water Vapour", 2: "Carbon Dioxide", 3: "Ozone", 4: "Dinitrogen 
              6: "Methane", 7: "Oxygen"}
 
 
+# Parameters of each scaling function (rad_pcf.F90 n_scale_variable).
+N_SCALE_VARIABLE = {0: 0, 1: 2, 2: 3, 3: 4, 4: 0, 5: 0, 6: 6, 7: 8, 8: 10, 9: 0, 10: 0}
+
+
 def _f(a, dtype):
     return np.asfortranarray(np.asarray(a, dtype=dtype))
 
@@ -51,6 +55,18 @@ class Spectrum:
     i_drop_parm: np.ndarray | None = None    # (n_drop_type)
     ice_parm_list: np.ndarray | None = None  # (16, n_band, n_ice_type)
     i_ice_parm: np.ndarray | None = None
+    # block 13: Doppler broadening (per absorber)
+    l_doppler: np.ndarray | None = None      # (n_absorb) 0/1
+    doppler_cor: np.ndarray | None = None    # (n_absorb)
+    # blocks 8 and 9: continua (StrSpecCont)
+    n_band_continuum: np.ndarray | None = None   # (n_band)
+    index_continuum: np.ndarray | None = None    # (n_band, nd_continuum) 1 self, 2 foreign
+    index_water: int = 0                         # 1-based absorber index of water vapour
+    i_scale_fnc_cont: np.ndarray | None = None   # (n_band, nd_continuum)
+    k_cont: np.ndarray | None = None             # (n_band, nd_continuum) m5/(kg mol)
+    scale_cont: np.ndarray | None = None         # (nd_scale_variable, n_band, nd_continuum)
+    p_ref_cont: np.ndarray | None = None         # (nd_continuum, n_band)
+    t_ref_cont: np.ndarray | None = None         # (nd_continuum, n_band)
     name: str = "spectrum"
     _keep: list = field(default_factory=list, repr=False)
 
@@ -133,8 +149,26 @@ class Spectrum:
         tr[: self.n_absorb] = self.t_ref
         d.p_ref = dp(pr)
         d.t_ref = dp(tr)
-        d.l_doppler = None
-        d.doppler_cor = None
+        d.l_doppler = ip(self.l_doppler) if self.l_doppler is not None else None
+        d.doppler_cor = dp(self.doppler_cor) if self.doppler_cor is not None else None
+        if self.n_band_continuum is not None:
+            ndc = self.index_continuum.shape[1]
+            d.nd_continuum = ndc
+            d.n_band_continuum = ip(self.n_band_continuum)
+            d.index_continuum = ip(self.index_continuum)
+            d.index_water = int(self.index_water)
+            d.i_scale_fnc_cont = ip(self.i_scale_fnc_cont)
+            d.k_cont = dp(self.k_cont)
+            nsv = self.scale_cont.shape[0]
+            if nsv != d.nd_scale_variable:
+                sc = np.zeros((d.nd_scale_variable, self.n_band, ndc))
+                m = min(nsv, d.nd_scale_variable)
+                sc[:m] = self.scale_cont[:m]
+                d.scale_cont = dp(sc)
+            else:
+                d.scale_cont = dp(self.scale_cont)
+            d.p_ref_cont = dp(self.p_ref_cont)
+            d.t_ref_cont = dp(self.t_ref_cont)
         if self.thermal_coeff is not None:
             d.n_deg_fit = self.n_deg_fit
             d.t_ref_planck = self.t_ref_planck
@@ -154,6 +188,37 @@ class Spectrum:
             d.l_ice_type = ip(np.ones(d.nd_ice_type, np.int32))
         self._keep = keep
         return d
+
+    # ------------------------------------------------------------------
+    def save_npz(self, path) -> None:
+        """Store the arrays (for fixtures of parsed spectral files)."""
+        from dataclasses import fields
+        out = {}
+        for f in fields(self):
+            if f.name.startswith("_"):
+                continue
+            v = getattr(self, f.name)
+            if v is None:
+                continue
+            out[f.name] = np.asarray(v)
+        np.savez_compressed(path, **out)
+
+    @classmethod
+    def load_npz(cls, path, prefix: str = "") -> "Spectrum":
+        from dataclasses import fields
+        data = np.load(path)
+        kw = {}
+        for f in fields(cls):
+            key = prefix + f.name
+            if key not in data.files:
+                continue
+            v = data[key]
+            if v.ndim == 0:
+                v = v.item()
+            elif v.dtype.kind in "fi":
+                v = np.asfortranarray(v)
+            kw[f.name] = v
+        return cls(**kw)
 
     # ------------------------------------------------------------------
     def write_text(self, path) -> None:
@@ -210,7 +275,6 @@ class Spectrum:
         L.append("Band        Gas, Number of k-terms, Scaling type and scaling function,")
         L.append("             followed by reference pressure and temperature,")
         L.append("                   k-terms, weights and scaling parameters.")
-        nsv = {0: 0, 1: 2, 2: 3, 3: 4}
         for b in range(self.n_band):
             for j in range(int(self.n_band_absorb[b])):
                 g = int(self.index_absorb[j, b]) - 1
@@ -219,8 +283,14 @@ class Spectrum:
                 L.append(f"{b + 1:5d}       {g + 1:5d}       {nk:5d}       {int(self.i_scale_k[b, g]):5d}       {fnc:5d}")
                 L.append(f"      {e(self.p_ref[g, b])}      {e(self.t_ref[g, b])}")
                 for kk in range(nk):
-                    sc = "".join(f"   {e(self.scale[v, kk, b, g])}" for v in range(nsv.get(fnc, 0)))
-                    L.append(f"   {e(self.k[kk, b, g])}   {e(self.w[kk, b, g])}  1{sc}")
+                    # read_spectrum.F90 block 5: (2(3x, 1pe16.9), i3, :, (t42, 1pe16.9, 3x, 1pe16.9))
+                    vals = [self.scale[v, kk, b, g] for v in range(N_SCALE_VARIABLE.get(fnc, 0))]
+                    line = f"   {e(self.k[kk, b, g])}   {e(self.w[kk, b, g])}  0"
+                    if not vals:
+                        L.append(line)
+                    for q in range(0, len(vals), 2):
+                        pair = "   ".join(e(v) for v in vals[q:q + 2])
+                        L.append((line if q == 0 else " " * 41) + pair)
         L.append("*END")
         if self.thermal_coeff is not None:
             L.append("*BLOCK: TYPE =    6: SUBTYPE =    0: VERSION =    0")
@@ -230,6 +300,45 @@ class Spectrum:
             L.append("Band          w/m2")
             for b in range(self.n_band):
                 L.append(f"{b + 1:5d}   " + " ".join(e(c) for c in self.thermal_coeff[:, b]))
+            L.append("*END")
+        if self.n_band_continuum is not None:
+            L.append("*BLOCK: TYPE =    8: SUBTYPE =    0: VERSION =    0")
+            L.append("Continuum absorbers in each interval")
+            L.append("(The number is the indexing number of each type as set out")
+            L.append(" in the file continuum.pcf.)")
+            L.append("A zero indicates that there in no continuum absorption in the interval.")
+            L.append("Band         Number of active continua followed by indexing numbers")
+            for b in range(self.n_band):
+                n = int(self.n_band_continuum[b])
+                L.append(f"{b + 1:5d}       {n:5d}")
+                if n:
+                    L.append("     " + "".join(f"  {int(self.index_continuum[b, j]):3d}" for j in range(n)))
+            L.append("Indexing numbers of gases for continua:")
+            L.append(f"     Index of water = {int(self.index_water):5d}")
+            L.append("*END")
+            L.append("*BLOCK: TYPE =    9: SUBTYPE =    0: VERSION =    0")
+            L.append("Continuum absorption coefficients: (units: m5/(kg.mol))")
+            L.append("Band        Continuum   Scaling function followed by reference pressure and")
+            L.append("             temperature, extinction, and scaling parameters.")
+            for b in range(self.n_band):
+                for j in range(int(self.n_band_continuum[b])):
+                    fnc = int(self.i_scale_fnc_cont[b, j])
+                    L.append(f"{b + 1:5d}       {int(self.index_continuum[b, j]):5d}       {fnc:5d}")
+                    L.append(f"      {e(self.p_ref_cont[j, b])}      {e(self.t_ref_cont[j, b])}")
+                    vals = [self.scale_cont[v, b, j] for v in range(N_SCALE_VARIABLE.get(fnc, 0))]
+                    # (6x, 1pe16.9, (t23, 2(6x, 1pe16.9)))
+                    line = f"      {e(self.k_cont[b, j])}"
+                    for q in range(0, max(len(vals), 1), 2):
+                        pair = "".join(f"      {e(v)}" for v in vals[q:q + 2])
+                        L.append((line if q == 0 else " " * 22) + pair)
+            L.append("*END")
+        if self.l_doppler is not None:
+            L.append("*BLOCK: TYPE =   13: SUBTYPE =    0: VERSION =    0")
+            L.append("Doppler broadening coefficients for the gases")
+            L.append("Species    Doppler flag   Doppler coefficient")
+            for i in range(self.n_absorb):
+                flag = "T" if self.l_doppler[i] else "F"
+                L.append(f"{i + 1:5d}       {flag:>6s}         {self.doppler_cor[i]:12.5E}")
             L.append("*END")
         for blk, parm, ids, label in ((10, self.drop_parm_list, self.i_drop_parm, "droplets"),
                                       (12, self.ice_parm_list, self.i_ice_parm, "ice crystals")):
@@ -249,17 +358,21 @@ class Spectrum:
 
     @classmethod
     def read_text(cls, path, name: str | None = None) -> "Spectrum":
-        """Read blocks 0-6, 10 and 12 of a spectral file in the text format.
-
-        Only what write_text produces is guaranteed; lookup-table k scaling
-        (ip_scale_lookup, '_k' files) and continua are not read."""
+        """Read a spectral file in the reference's text format: blocks 0
+        (summary, versions 1 and 2), 1 (band limits), 2 (solar spectrum), 3
+        (Rayleigh), 4 (absorbers per band), 5 (k-terms), 6 (Planck
+        polynomial), 8 and 9 (continua), 13 (Doppler broadening) and the
+        Pade droplet/ice blocks 10 and 12 (parametrisations 5 and 20); record
+        layouts of read_spectrum.F90 (blocks 0-13).  Other blocks (surface
+        properties, aerosols, other cloud parametrisations) are skipped.
+        Lookup-table k scaling (the '_k' companion files) is not read."""
         text = open(path).read().splitlines()
         blocks = []
         cur = None
         for ln in text:
             if ln.startswith("*BLOCK"):
                 parts = ln.replace(":", " ").replace("=", " ").split()
-                cur = {"type": int(parts[2]), "lines": []}
+                cur = {"type": int(parts[2]), "subtype": int(parts[4]), "version": int(parts[6]), "lines": []}
                 blocks.append(cur)
             elif ln.startswith("*END"):
                 cur = None
@@ -267,94 +380,212 @@ class Spectrum:
                 cur["lines"].append(ln)
         by = {}
         for bl in blocks:
-            by.setdefault(bl["type"], []).append(bl["lines"])
-        b0 = by[0][0]
-        n_band = int(b0[1].split("=")[1])
-        n_abs = int(b0[2].split("=")[1])
-        nd_k = int(b0[3].split("=")[1])
-        types = [int(l.split()[1]) for l in b0[7:7 + n_abs]]
-        wl = np.array([[float(x) for x in l.split()[1:3]] for l in by[1][0][3:3 + n_band]])
-        sol = None
-        if 2 in by:
-            sol = np.array([float(l.split()[1]) for l in by[2][0][2:2 + n_band]])
-        ray = None
-        if 3 in by:
-            ray = np.array([float(l.split()[1]) for l in by[3][0][2:2 + n_band]])
-        # block 4
-        toks = " ".join(by[4][0][5:]).split()
+            by.setdefault(bl["type"], []).append(bl)
+
+        def after_eq(line):
+            return line.split("=")[1].split()[0]
+
+        # block 0: summary
+        b0 = by[0][0]["lines"]
+        n_band = n_abs = None
+        types = []
+        for q, ln in enumerate(b0):
+            u = ln.upper()
+            if "SPECTRAL BANDS" in u:
+                n_band = int(after_eq(ln))
+            elif "GASEOUS ABSORBERS" in u:
+                n_abs = int(after_eq(ln))
+            elif "INDEXING NUMBERS AND ABSORBERS" in u or ("INDEXING NUMBERS" in u and "ABSORBER" in u
+                                                            and "AEROSOL" not in u):
+                for r in b0[q + 2:q + 2 + n_abs]:
+                    types.append(int(r.split()[1]))
+        # block 1: band limits
+        wl = np.zeros((n_band, 2))
+        for r in by[1][0]["lines"][3:3 + n_band]:
+            v = r.split()
+            wl[int(v[0]) - 1] = float(v[1]), float(v[2])
+
+        def band_values(blk, skip):
+            if blk not in by:
+                return None
+            out = np.zeros(n_band)
+            for r in by[blk][0]["lines"][skip:]:
+                v = r.split()
+                if len(v) >= 2 and v[0].isdigit():
+                    out[int(v[0]) - 1] = float(v[1])
+            return out
+        sol = band_values(2, 2)
+        ray = band_values(3, 3)
+        # block 4: absorbers in each band (token stream after 5 header lines)
+        toks = " ".join(by[4][0]["lines"][5:]).split()
         nba = np.zeros(n_band, np.int32)
         ia = np.zeros((max(1, n_abs), n_band), np.int32)
         q = 0
-        for b in range(n_band):
-            q += 1  # band index
-            nba[b] = int(toks[q]); q += 1
+        for _ in range(n_band):
+            b = int(toks[q]) - 1
+            nba[b] = int(toks[q + 1])
+            q += 2
             for j in range(nba[b]):
-                ia[j, b] = int(toks[q]); q += 1
-        # block 5
+                ia[j, b] = int(toks[q])
+                q += 1
+        # block 5: k-terms, fixed columns (2(3x, 1pe16.9), i3, :, (t42, 1pe16.9, 3x, 1pe16.9))
+        recs = []
+        lines = by[5][0]["lines"][4:]
+        q = 0
+        nd_k, nsv_max = 1, 4
+        while q < len(lines):
+            parts = lines[q].split()
+            if len(parts) < 5:
+                q += 1
+                continue
+            b, g, nk, sk, fnc = (int(x) for x in parts[:5])
+            if fnc in (9, 10):
+                raise ValueError("lookup-table k scaling is not supported")
+            p_ref, t_ref = (float(x) for x in lines[q + 1].split()[:2])
+            q += 2
+            nsv = N_SCALE_VARIABLE.get(fnc, 0)
+            terms = []
+            for _ in range(nk):
+                ln = lines[q]
+                k_ = float(ln[3:19])
+                w_ = float(ln[22:38])
+                vals = []
+                col = ln
+                while len(vals) < nsv:
+                    for a, z in ((41, 57), (60, 76)):
+                        if len(vals) < nsv and len(col) > a and col[a:z].strip():
+                            vals.append(float(col[a:z]))
+                    if len(vals) < nsv:
+                        q += 1
+                        col = lines[q]
+                q += 1
+                terms.append((k_, w_, vals))
+            recs.append((b - 1, g - 1, nk, sk, fnc, p_ref, t_ref, terms))
+            nd_k = max(nd_k, nk)
+            nsv_max = max(nsv_max, nsv)
         ibk = np.zeros((n_band, n_abs), np.int32)
         isk = np.zeros((n_band, n_abs), np.int32)
         isf = np.zeros((n_band, n_abs), np.int32)
         kk = np.zeros((nd_k, n_band, n_abs))
         ww = np.zeros((nd_k, n_band, n_abs))
-        sc = np.zeros((4, nd_k, n_band, n_abs))
+        sc = np.zeros((nsv_max, nd_k, n_band, n_abs))
         pr = np.zeros((n_abs, n_band))
         tr = np.zeros((n_abs, n_band))
-        lines = by[5][0][4:]
-        q = 0
-        nsv = {0: 0, 1: 2, 2: 3, 3: 4}
-        while q < len(lines):
-            parts = lines[q].split()
-            if not parts:
-                q += 1
-                continue
-            b, g, nk, sk, fnc = (int(x) for x in parts[:5])
-            b -= 1
-            g -= 1
+        for b, g, nk, sk, fnc, p_ref, t_ref, terms in recs:
             ibk[b, g], isk[b, g], isf[b, g] = nk, sk, fnc
-            pr[g, b], tr[g, b] = (float(x) for x in lines[q + 1].split()[:2])
-            for t in range(nk):
-                v = lines[q + 2 + t].split()
-                kk[t, b, g], ww[t, b, g] = float(v[0]), float(v[1])
-                for s in range(nsv.get(fnc, 0)):
-                    sc[s, t, b, g] = float(v[3 + s])
-            q += 2 + nk
-        tc = None
-        ndeg = 0
-        tref = 0.0
+            pr[g, b], tr[g, b] = p_ref, t_ref
+            for t, (k_, w_, vals) in enumerate(terms):
+                kk[t, b, g], ww[t, b, g] = k_, w_
+                sc[:len(vals), t, b, g] = vals
+        # block 6: Planck polynomial
+        tc, ndeg, tref = None, 0, 0.0
         if 6 in by:
-            hdr = by[6][0][1]
-            ndeg = int(hdr.split(":")[0].split("=")[1])
-            tref = float(hdr.split(":")[1].split("=")[1])
+            b6 = by[6][0]["lines"]
+            hdr = next(ln for ln in b6 if "=" in ln)
+            ndeg = int(hdr.split("=")[1].split(":")[0])
+            tref = float(hdr.split("=")[2])
+            vals = " ".join(b6[b6.index(hdr) + 3:]).split()
             tc = np.zeros((ndeg + 1, n_band))
-            vals = " ".join(by[6][0][4:]).split()
             q = 0
-            for b in range(n_band):
-                q += 1
-                tc[:, b] = [float(x) for x in vals[q:q + ndeg + 1]]
-                q += ndeg + 1
-
-        def cloud(blk):
-            if blk not in by:
-                return None, None
-            sets, ids = [], []
-            for lines in by[blk]:
-                ids.append(int(lines[2].split("=")[1].split(":")[0]))
-                npar = int(lines[2].split("=")[2])
-                arr = np.zeros((npar, n_band))
-                vals = " ".join(lines[4:]).split()
+            for _ in range(n_band):
+                b = int(vals[q]) - 1
+                tc[:, b] = [float(x) for x in vals[q + 1:q + 2 + ndeg]]
+                q += ndeg + 2
+        # blocks 8 and 9: continua
+        cont = {}
+        if 8 in by:
+            b8 = by[8][0]["lines"]
+            toks = []
+            iw = 0
+            for ln in b8[5:]:
+                if "=" in ln:
+                    iw = int(after_eq(ln))
+                elif ln.strip() and ln.strip()[0].isdigit():
+                    toks += ln.split()
+            nbc = np.zeros(n_band, np.int32)
+            idx = {}
+            q = 0
+            while q < len(toks):
+                b = int(toks[q]) - 1
+                n = int(toks[q + 1])
+                nbc[b] = n
+                idx[b] = [int(x) for x in toks[q + 2:q + 2 + n]]
+                q += 2 + n
+            ndc = max(1, int(nbc.max()))
+            ic = np.zeros((n_band, ndc), np.int32)
+            for b, v in idx.items():
+                ic[b, :len(v)] = v
+            fc = np.zeros((n_band, ndc), np.int32)
+            kc = np.zeros((n_band, ndc))
+            scc = np.zeros((max(nsv_max, 3), n_band, ndc))
+            prc = np.zeros((ndc, n_band))
+            trc = np.zeros((ndc, n_band))
+            if 9 in by:
+                toks = " ".join(by[9][0]["lines"][3:]).split()
                 q = 0
-                for b in range(n_band):
-                    q += 1
-                    arr[:, b] = [float(x) for x in vals[q:q + npar]]
-                    q += npar
+                while q < len(toks):
+                    b, ci, fnc = int(toks[q]) - 1, int(toks[q + 1]), int(toks[q + 2])
+                    j = list(ic[b]).index(ci)
+                    fc[b, j] = fnc
+                    prc[j, b], trc[j, b] = float(toks[q + 3]), float(toks[q + 4])
+                    kc[b, j] = float(toks[q + 5])
+                    nsv = N_SCALE_VARIABLE.get(fnc, 0)
+                    scc[:nsv, b, j] = [float(x) for x in toks[q + 6:q + 6 + nsv]]
+                    q += 6 + nsv
+            cont = dict(n_band_continuum=nbc, index_continuum=_f(ic, np.int32), index_water=iw,
+                        i_scale_fnc_cont=_f(fc, np.int32), k_cont=_f(kc, np.float64),
+                        scale_cont=_f(scc, np.float64), p_ref_cont=_f(prc, np.float64),
+                        t_ref_cont=_f(trc, np.float64))
+        # block 13: Doppler broadening
+        ldop = dcor = None
+        if 13 in by:
+            ldop = np.zeros(n_abs, np.int32)
+            dcor = np.zeros(n_abs)
+            for ln in by[13][0]["lines"][2:]:
+                v = ln.split()
+                if len(v) >= 3 and v[0].isdigit():
+                    i = int(v[0]) - 1
+                    ldop[i] = 1 if v[1].upper().startswith("T") else 0
+                    dcor[i] = float(v[2])
+
+        def pade(blk, want):
+            sets, ids = [], []
+            for bl in by.get(blk, []):
+                lines = bl["lines"]
+                head = next((ln for ln in lines if "=" in ln and "PARAMETERS" in ln.upper()), None)
+                if head is None:
+                    continue
+                scheme = int(head.split("=")[1].split(":")[0])
+                npar = int(head.split("=")[2])
+                if scheme != want or npar != 16:
+                    continue
+                vals = []
+                for ln in lines[lines.index(head) + 1:]:
+                    u = ln.upper()
+                    if "RANGE" in u or not any(ch.isdigit() for ch in ln):
+                        continue
+                    if "BAND" in u and "=" in ln:
+                        vals.append(ln.split("=")[1].split()[0])
+                    else:
+                        vals += ln.split()
+                arr = np.zeros((npar, n_band))
+                q = 0
+                for _ in range(n_band):
+                    b = int(vals[q]) - 1
+                    arr[:, b] = [float(x) for x in vals[q + 1:q + 1 + npar]]
+                    q += npar + 1
                 sets.append(arr)
+                ids.append(scheme)
+            if not sets:
+                return None, None
             return np.asfortranarray(np.stack(sets, axis=2)), np.array(ids, np.int32)
 
-        dpl, dids = cloud(10)
-        ipl, iids = cloud(12)
+        dpl, dids = pade(10, abi.IP_DROP_PADE_2)
+        ipl, iids = pade(12, abi.IP_ICE_PADE_2_PHF)
         return cls(n_band=n_band, wavelength_short=wl[:, 0], wavelength_long=wl[:, 1],
                    type_absorb=np.array(types, np.int32), n_band_absorb=nba, index_absorb=ia,
                    i_band_k=ibk, i_scale_k=isk, i_scale_fnc=isf, k=_f(kk, np.float64), w=_f(ww, np.float64),
                    scale=_f(sc, np.float64), p_ref=pr, t_ref=tr, solar_flux_band=sol, rayleigh_coeff=ray,
                    n_deg_fit=ndeg, t_ref_planck=tref, thermal_coeff=tc, drop_parm_list=dpl, i_drop_parm=dids,
-                   ice_parm_list=ipl, i_ice_parm=iids, name=name or str(path))
+                   ice_parm_list=ipl, i_ice_parm=iids, l_doppler=ldop, doppler_cor=dcor, name=name or str(path),
+                   **cont)

@@ -218,6 +218,7 @@ class Column:
     rho_alb: np.ndarray | None = None  # (n_profile, 2, n_band)
     aer: dict | None = None
     cld: dict | None = None
+    density: np.ndarray | None = None  # (n_profile, n_layer) kg/m3, for continua
     extra: dict = field(default_factory=dict)
 
 
@@ -349,7 +350,7 @@ def window(col: Column, start: int, n: int, alloc=None) -> Column:
         return v
 
     for name in ("p", "t", "p_level", "t_level", "mass", "gas_mix_ratio", "z", "t_ground", "zen_0", "solar_irrad",
-                 "rho_alb"):
+                 "rho_alb", "density"):
         setattr(c, name, cut(getattr(col, name)))
     if col.aer:
         c.aer = {k: cut(v) for k, v in col.aer.items()}

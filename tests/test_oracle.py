@@ -204,10 +204,43 @@ def test_cloud_gen_compaction_and_fraction():
 
 
 # ---------------------------------------------------------------------------
-@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz")))
+@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("icrccm")))
 def test_oracle_reproduces_golden_fixture(name):
     from golden_cases import CASES
     data = np.load(GOLDEN / f"{name}.npz")
     out = CASES[name](lambda ctl, sp, col, mc=None: O.radiance_calc(ctl, sp, col, mc))
     for key in out:
         np.testing.assert_allclose(out[key], data[key], rtol=1e-12, atol=1e-12, err_msg=f"{name}:{key}")
+
+
+def test_oracle_reproduces_icrccm27_known_good_output():
+    """Pin against the reference's own known-good output: ICRCCM case 27
+    (examples/aer_cmp, HadCM3 LW spectral file with continuum, random
+    overlap of up to 9 gases, Elsasser, solver 13).  The reference prints
+    heating rates to 6 significant digits (laer27_ref.hrts); every layer
+    must agree to half a unit of the 6th digit."""
+    import icrccm27 as K
+    ctl, sp, col, kgo = K.load()
+    hr = K.heating_rate(O.radiance_calc(ctl, sp, col), col.mass)[0]
+    half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
+    err = np.abs(hr - kgo) / half_unit
+    assert err.max() <= 1.0, f"layer {err.argmax()}: {hr[err.argmax()]} vs {kgo[err.argmax()]}"
+
+
+def test_reference_spectral_file_round_trip(tmp_path):
+    """The parsed HadCM3 file (blocks 0-9, 13) written in the reference's
+    record layouts and read back gives the same arrays."""
+    from socrates_gb300.spectrum import Spectrum
+    import icrccm27 as K
+    sp = Spectrum.load_npz(K.FIXTURE, prefix="sp_")
+    path = tmp_path / "sp_lw"
+    sp.write_text(path)
+    back = Spectrum.read_text(path)
+    for name in ("n_band_absorb", "index_absorb", "i_band_k", "i_scale_k", "i_scale_fnc", "n_band_continuum",
+                 "index_continuum", "i_scale_fnc_cont", "l_doppler"):
+        np.testing.assert_array_equal(getattr(back, name), getattr(sp, name), err_msg=name)
+    for name in ("k", "w", "scale", "p_ref", "t_ref", "thermal_coeff", "k_cont", "scale_cont", "p_ref_cont",
+                 "t_ref_cont", "doppler_cor"):
+        a, b = getattr(back, name), getattr(sp, name)
+        m = min(a.shape[0], b.shape[0])
+        np.testing.assert_allclose(a[:m], b[:m], rtol=1e-9, atol=0, err_msg=name)
