@@ -86,6 +86,33 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
       }
     bi.rayleigh_f = (float)bi.rayleigh_coeff;
     bi.solar_flux_band_f = (float)bi.solar_flux_band;
+    // continua of the band (blocks 8 and 9)
+    if (d->n_band_continuum) {
+      const int nc = d->n_band_continuum[b];
+      if (nc < 0 || nc > kMaxContPerBand || nc > d->nd_continuum) {
+        set_msg(msg, msg_len, "band %d has %d continua; at most %d supported", b + 1, nc, kMaxContPerBand);
+        return SOCGPU_I_ERR_RANGE;
+      }
+      bi.n_cont = nc;
+      for (int j = 0; j < nc; ++j) {
+        BandCont &c = bi.cont[j];
+        const size_t bj = (size_t)b + (size_t)d->nd_band * j;
+        c.type = d->index_continuum[bj];
+        c.fnc = d->i_scale_fnc_cont[bj];
+        if ((c.type != SOCGPU_IP_SELF_CONTINUUM && c.type != SOCGPU_IP_FRN_CONTINUUM) ||
+            (c.fnc != SOCGPU_IP_SCALE_POWER_LAW && c.fnc != SOCGPU_IP_SCALE_POWER_QUAD)) {
+          set_msg(msg, msg_len, "band %d: continuum type %d with scaling %d unsupported", b + 1, c.type, c.fnc);
+          return SOCGPU_I_ERR_FATAL;
+        }
+        c.p_ref = d->p_ref_cont[(size_t)j + (size_t)d->nd_continuum * b];
+        c.t_ref = d->t_ref_cont[(size_t)j + (size_t)d->nd_continuum * b];
+        c.k = d->k_cont[bj];
+        for (int v = 0; v < 3; ++v)
+          c.scale[v] = v < d->nd_scale_variable ? d->scale_cont[(size_t)v + (size_t)d->nd_scale_variable * bj] : 0.0;
+        c.p_ref_f = (float)c.p_ref; c.t_ref_f = (float)c.t_ref; c.k_f = (float)c.k;
+        for (int v = 0; v < 3; ++v) c.scale_f[v] = (float)c.scale[v];
+      }
+    }
     int n_abs = d->n_band_absorb ? d->n_band_absorb[b] : 0;
     if (n_abs > kMaxAbsPerBand) {
       set_msg(msg, msg_len, "band %d has %d absorbers; at most %d supported", b + 1, n_abs, kMaxAbsPerBand);
@@ -183,6 +210,8 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   s.has_solar = d->solar_flux_band != nullptr;
   s.has_planck = d->thermal_coeff != nullptr;
   s.has_rayleigh = d->rayleigh_coeff != nullptr;
+  s.has_continuum = d->n_band_continuum != nullptr;
+  s.index_water = d->index_water;
   for (int b = 0; b < d->n_band; ++b) s.host_first_g[b] = e.bands_host[b].g_first;
   s.host_first_g[d->n_band] = s.n_gpoint;
   // cloud parameter sets
@@ -369,6 +398,11 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     set_msg(msg, msg_len, "solar calculation without zen_0/solar_irrad"); return SOCGPU_I_ERR_FATAL; }
   if (c->isolir == SOCGPU_IP_INFRA_RED && !bd->t_ground) {
     set_msg(msg, msg_len, "infra-red calculation without t_ground"); return SOCGPU_I_ERR_FATAL; }
+  if (c->l_continuum && sp->dev.has_continuum &&
+      (!atm->density || !atm->gas_mix_ratio || sp->dev.index_water < 1 || sp->dev.index_water > sp->dev.n_species)) {
+    set_msg(msg, msg_len, "continuum absorption needs the layer density, the gas mixing ratios and water vapour");
+    return SOCGPU_I_ERR_FATAL;
+  }
   // t_level feeds only the Planck terms of the infra-red
   if (!bd->rho_alb || !atm->p || !atm->t || !atm->mass || (c->l_gas && !atm->gas_mix_ratio) ||
       (c->isolir == SOCGPU_IP_INFRA_RED && !atm->t_level)) {
@@ -420,6 +454,9 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
   p.l_aerosol_mode = c->l_aerosol_mode && aer && aer->n_mode > 0; p.l_flux_div = c->l_flux_div;
   p.first_band = c->first_band; p.last_band = c->last_band;
   p.mcica = c->i_cloud == SOCGPU_IP_CLOUD_MCICA;
+  p.l_continuum = c->l_continuum && sp->dev.has_continuum;
+  p.l_mixing_ratio = c->l_mixing_ratio;
+  p.i_water = sp->dev.index_water - 1;
   p.n_profile = atm->n_profile; p.n_layer = atm->n_layer;
   p.nd_profile = dm->nd_profile; p.nd_layer = dm->nd_layer;
   p.id_ct = (p.mcica ? dm->id_cloud_top : 1) - 1;
@@ -435,6 +472,7 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
   p.t_ref_planck_f = (float)sp->dev.t_ref_planck;
   p.weight_band = weight_band_dev;
   p.p = atm->p; p.t = atm->t; p.t_level = atm->t_level; p.mass = atm->mass; p.gas_mix_ratio = atm->gas_mix_ratio;
+  p.density = atm->density;
   p.nd_species = sp->dev.n_species;
   p.zen_0 = bd->zen_0; p.solar_irrad = bd->solar_irrad; p.rho_alb = bd->rho_alb; p.t_ground = bd->t_ground;
   if (p.l_aerosol_mode) {
@@ -494,7 +532,9 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
   o_t = plan.add(a->t, D, ndp, np, nl);
   o_tl = !sw ? plan.add(a->t_level, D, ndp, np, nl + 1) : none;
   o_m = plan.add(a->mass, D, ndp, np, nl);
-  o_g = c->l_gas ? plan.add(a->gas_mix_ratio, D, ndp, np, ndl * ns) : none;
+  const bool cont = c->l_continuum && s->dev.has_continuum;
+  o_g = (c->l_gas || cont) ? plan.add(a->gas_mix_ratio, D, ndp, np, ndl * ns) : none;
+  o_rho = cont ? plan.add(a->density, D, ndp, np, nl) : none;
   o_z = sw ? plan.add(b->zen_0, D, ndp, np, 1) : none;
   o_si = sw ? plan.add(b->solar_irrad, D, ndp, np, 1) : none;
   o_alb = plan.add(b->rho_alb, D, ndp, np, 2 * nb);
@@ -557,6 +597,7 @@ void StagedCall::params(char *base, FluxParams &p) const {
   socgpu_atm a2 = *atm;
   a2.p = (const double *)dptr(o_p); a2.t = (const double *)dptr(o_t); a2.t_level = (const double *)dptr(o_tl);
   a2.mass = (const double *)dptr(o_m); a2.gas_mix_ratio = (const double *)dptr(o_g); a2.p_level = nullptr;
+  a2.density = (const double *)dptr(o_rho);
   socgpu_bound b2 = *bound;
   b2.zen_0 = (const double *)dptr(o_z); b2.solar_irrad = (const double *)dptr(o_si);
   b2.rho_alb = (const double *)dptr(o_alb); b2.t_ground = (const double *)dptr(o_tg);

@@ -487,6 +487,47 @@ struct FluxKernel {
           }
         }
       }
+      if (p.l_continuum) {
+        // continuum absorption (grey_opt_prop.F90:801-817), amounts as
+        // rescale_continuum.F90 (self: molar density of water x water;
+        // foreign: air density x water / molar weight of air)
+        const R water = load_in<R>(p.gas_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * p.i_water));
+        const R rho = load_in<R>(p.density + (size_t)col + (size_t)ndp * i);
+        for (int j = 0; j < bd.n_cont; ++j) {
+          const BandCont &c = bd.cont[j];
+          R a;
+          if constexpr (kFP64) {
+            a = pow(S.p[s] / c.p_ref, c.scale[0]);
+            if (c.fnc == SOCGPU_IP_SCALE_POWER_LAW) {
+              a = a * pow(S.t[s] / c.t_ref, c.scale[1]);
+            } else if (c.fnc == SOCGPU_IP_SCALE_POWER_QUAD) {
+              const double x = S.t[s] / c.t_ref - 1.0;
+              a = a * (1.0 + c.scale[1] * x + c.scale[2] * (x * x));
+            }
+            if (c.type == SOCGPU_IP_SELF_CONTINUUM) {
+              a = a * (rho * water / ((18.0153 / 28.966) * 28.966e-03)) * water;
+            } else if (c.type == SOCGPU_IP_FRN_CONTINUUM) {
+              a = p.l_mixing_ratio ? a * rho * water / 28.966e-03 : a * rho * water * (1.0 - water) / 28.966e-03;
+            }
+            kabs = kabs + c.k * a;
+          } else {
+            a = __powf(S.p[s] / c.p_ref_f, c.scale_f[0]);
+            if (c.fnc == SOCGPU_IP_SCALE_POWER_LAW) {
+              a = a * __powf(S.t[s] / c.t_ref_f, c.scale_f[1]);
+            } else if (c.fnc == SOCGPU_IP_SCALE_POWER_QUAD) {
+              const float x = S.t[s] / c.t_ref_f - 1.0f;
+              a = a * (1.0f + c.scale_f[1] * x + c.scale_f[2] * (x * x));
+            }
+            if (c.type == SOCGPU_IP_SELF_CONTINUUM) {
+              a = a * (rho * water * (1.0f / 0.0180153f)) * water;
+            } else if (c.type == SOCGPU_IP_FRN_CONTINUUM) {
+              a = p.l_mixing_ratio ? a * rho * water * (1.0f / 0.028966f)
+                                   : a * rho * water * (1.0f - water) * (1.0f / 0.028966f);
+            }
+            kabs = kabs + c.k_f * a;
+          }
+        }
+      }
       R kgt = kabs + kes;     // grey_opt_prop.F90:773-790
       if (MCICA) { S.phf_nc[q] = phf; S.fwd_nc[q] = fwd; }
       R asym = phf, f = fwd;
@@ -687,9 +728,12 @@ struct FluxKernel {
         }
       return kg;
     }
+    // per-term scaling: a rolled loop; k comes from the g-point table (a
+    // broadcast load) so that the register copy is never indexed dynamically
     for (int j = 0; j < gt.n_abs; ++j) {
       R a = amt[(size_t)j * LP + s];
       R kal;
+      const R kj = kFP64 ? (R)gp.k[j] : (R)gp.kf[j];
       if (bd.gas[j].i_scale_k == SOCGPU_IP_SCALE_TERM) {
         R gf;
         if constexpr (kFP64)
@@ -699,9 +743,9 @@ struct FluxKernel {
           gf = scale_factor_mix(bd.gas[j].i_scale_fnc, pl, tl, bd.gas[j].p_ref_f, bd.gas[j].t_ref_f,
                                 gp.term_scale_f[j], bd.gas[j].l_doppler, bd.gas[j].doppler_cor_f);
         R v = gf * a;
-        kal = gt.k[j] * (v > R(0) ? v : R(0));
+        kal = kj * (v > R(0) ? v : R(0));
       } else {
-        kal = gt.k[j] * a;
+        kal = kj * a;
       }
       kg = (j == 0) ? kal : kg + kal;
     }
@@ -1033,8 +1077,14 @@ struct FluxKernel {
   }
 };
 
+// Resident CTAs asked of the register allocator for the single-batch kernel:
+// short chunks of the clear-sky kernels keep 4 CTAs of 256 threads (64
+// registers) per SM, which the shared memory of a 100-layer solar column
+// also allows; the McICA kernels would spill at 64 registers.
+constexpr int single_min_ctas(int ch, bool mcica) { return (ch <= 4 && !mcica) ? 4 : 1; }
+
 template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA>
-__global__ void __launch_bounds__(256) flux_kernel(const __grid_constant__ FluxParams p) {
+__global__ void __launch_bounds__(256, single_min_ctas(CH, MCICA)) flux_kernel(const __grid_constant__ FluxParams p) {
   FluxKernel<R, MIX, P, CH, NOSCAT, MCICA>::run(p, blockIdx.x);
 }
 

@@ -97,7 +97,7 @@ struct StagedCall {
   const socgpu_bound *bound = nullptr;
   socgpu_radout *radout = nullptr;
   bool sw = false, mc = false, aero = false;
-  size_t o_p, o_t, o_tl, o_m, o_g, o_z, o_si, o_alb, o_tg, o_amr, o_aab, o_asc, o_aas, o_wb;
+  size_t o_p, o_t, o_tl, o_m, o_g, o_rho, o_z, o_si, o_alb, o_tg, o_amr, o_aab, o_asc, o_aas, o_wb;
   size_t o_cmr, o_cdc, o_wc, o_fc, o_cs, o_fcl, o_nsc, o_sk, o_fsk, o_sro;
   size_t o_fu, o_fd, o_fdir, o_div, o_hr;
 

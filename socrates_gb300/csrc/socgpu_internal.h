@@ -11,7 +11,7 @@
 namespace socgpu {
 
 // Most absorbers one k-term product may combine (random overlap).
-constexpr int kMaxAbsPerBand = 8;
+constexpr int kMaxAbsPerBand = 12;
 // Planck polynomial degree limit (block 6).
 constexpr int kMaxPlanckCoeff = 12;
 // Cloud parameters per Pade set (opt_prop_pade_2_mod.F90: 16 coefficients).
@@ -29,8 +29,19 @@ struct BandGas {
   float p_ref_f, t_ref_f, doppler_cor_f, scale_f[4];   // FP32 copies for the mixed kernels
 };
 
+// One continuum of a band (blocks 8 and 9; rescale_continuum.F90).
+constexpr int kMaxContPerBand = 4;
+struct BandCont {
+  int type;                   // SOCGPU_IP_SELF_CONTINUUM / SOCGPU_IP_FRN_CONTINUUM
+  int fnc;                    // ip_scale_power_law / ip_scale_power_quad
+  double p_ref, t_ref, k, scale[3];
+  float p_ref_f, t_ref_f, k_f, scale_f[3];
+};
+
 struct BandInfo {
   int n_abs;                  // absorbers of the band (0 if l_gas false)
+  int n_cont;                 // continua of the band
+  BandCont cont[kMaxContPerBand];
   int g_first, g_count;       // range of g-points (k-term products) of the band
   double solar_flux_band;     // fraction of the solar constant
   double rayleigh_coeff;      // m2/kg
@@ -60,7 +71,7 @@ struct SpectrumDev {
   int n_band, n_gpoint, n_species, n_deg_fit;
   int nd_band, nd_k_term;           // leading extents of McICA subcol_k tables
   double t_ref_planck;
-  int has_solar, has_planck, has_rayleigh;
+  int has_solar, has_planck, has_rayleigh, has_continuum, index_water;
   int n_drop_type, n_ice_type;
   BandInfo *bands;                  // [n_band]
   GPoint *gpoints;                  // [n_gpoint]
@@ -79,6 +90,7 @@ struct FluxParams {
   int l_rescale, n_order_forward, l_ir_source_quad, l_rayleigh, l_gas, l_aerosol_mode;
   int l_flux_div, first_band, last_band;
   int mcica;
+  int l_continuum, l_mixing_ratio, i_water;   // i_water: 0-based species of water vapour
   // sizes
   int n_profile, n_layer, nd_profile, nd_layer, id_ct;  // id_ct 0-based first cloudy layer
   int g_begin, g_end;               // g-point range of the band range
@@ -94,7 +106,7 @@ struct FluxParams {
   float t_ref_planck_f;
   const double *weight_band;        // device copy, [n_band]
   // atm
-  const double *p, *t, *t_level, *mass, *gas_mix_ratio;
+  const double *p, *t, *t_level, *mass, *gas_mix_ratio, *density;
   int nd_species;
   // bound
   const double *zen_0, *solar_irrad, *rho_alb, *t_ground;

@@ -182,3 +182,22 @@ def test_kernels_launch_on_device(gpu_lib):
     before = R.launch_count()
     CASES["lw_noscat"](_gpu)
     assert R.launch_count() > before
+
+
+def test_icrccm27_known_good_output_on_gpu(gpu_lib):
+    """The reference's ICRCCM case 27 (HadCM3 LW with continuum, up to 9
+    gases per band) through the CUDA path: FP64 against the oracle at
+    1e-10, and against the reference's printed heating rates to half a
+    unit of their 6th digit; mixed precision within 0.1 W/m2 and
+    0.05 K/day."""
+    import icrccm27 as K
+    ctl, sp, col, kgo = K.load()
+    ref = {**O.radiance_calc(ctl, sp, col), "mass": col.mass}
+    g64 = {**R.radiance_calc(ctl, sp, col), "mass": col.mass}
+    assert_fp64_parity(g64, ref, "icrccm27 fp64: ")
+    hr = K.heating_rate(g64, col.mass)[0]
+    half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
+    assert (np.abs(hr - kgo) / half_unit).max() <= 1.0
+    gmx = R.radiance_calc(_with(ctl, abi.PRECISION_MIXED), sp, col)
+    assert_mixed_tolerance({**gmx, "heating_rate": K.heating_rate(gmx, col.mass)},
+                           {**ref, "heating_rate": K.heating_rate(ref, col.mass)}, "icrccm27 mixed: ")
