@@ -547,7 +547,7 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
     o_asc = plan.add(ae->mode_scattering, D, ndp, np, ndl * ndm * nb);
     o_aas = plan.add(ae->mode_asymmetry, D, ndp, np, ndl * ndm * nb);
   }
-  o_wb = c->weight_band ? plan.add(c->weight_band, D, nb, nb, 1) : none;
+  o_wb = c->weight_band ? plan.add(c->weight_band, D, nb, nb, 1, false, nullptr, false) : none;
   o_cmr = o_cdc = o_wc = o_fc = o_cs = o_fcl = o_nsc = o_sk = o_fsk = o_sro = none;
   if (mc) {
     const size_t ndc = ndl - (dm->id_cloud_top - 1);
@@ -560,9 +560,9 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
     o_fcl = plan.add(cl->frac_cloudy, D, ndp, np, 1);
     if (cl->n_subcol_cld) o_nsc = plan.add(cl->n_subcol_cld, sizeof(int), ndp, np, 1);
     const size_t ndb = s->dev.nd_band, ndk = s->dev.nd_k_term;
-    o_sk = plan.add(cl->subcol_k, sizeof(int), ndb * ndk, ndb * ndk, 1);
-    o_fsk = plan.add(cl->first_subcol_k, sizeof(int), ndb * (ndk + 1), ndb * (ndk + 1), 1);
-    o_sro = plan.add(cl->subcol_reorder, sizeof(int), cl->n_subcol_req, cl->n_subcol_req, 1);
+    o_sk = plan.add(cl->subcol_k, sizeof(int), ndb * ndk, ndb * ndk, 1, false, nullptr, false);
+    o_fsk = plan.add(cl->first_subcol_k, sizeof(int), ndb * (ndk + 1), ndb * (ndk + 1), 1, false, nullptr, false);
+    o_sro = plan.add(cl->subcol_reorder, sizeof(int), cl->n_subcol_req, cl->n_subcol_req, 1, false, nullptr, false);
   }
   n_inputs = plan.slots.size();
   o_fu = plan.add(nullptr, D, ndp, np, nl + 1, true, r->flux_up);
@@ -590,6 +590,47 @@ int StagedCall::copy_out(char *base, cudaStream_t s, char *msg, size_t msg_len) 
                                cudaMemcpyDeviceToHost, s));
   }
   return SOCGPU_I_NORMAL;
+}
+
+int StagedCall::copy_in_window(char *base, cudaStream_t s, size_t c0, size_t n, bool shared, char *msg,
+                               size_t msg_len) const {
+  for (size_t k = 0; k < n_inputs; ++k) {
+    const Slot &sl = plan.slots[k];
+    if (sl.row_bytes == 0) continue;
+    if (!sl.per_profile) {
+      if (shared)
+        CUDA_TRY(cudaMemcpy2DAsync(base + sl.off, sl.dev_pitch, sl.host, sl.host_pitch, sl.row_bytes, sl.rows,
+                                   cudaMemcpyHostToDevice, s));
+      continue;
+    }
+    const size_t es = sl.row_bytes / (size_t)atm->n_profile;   // element size
+    if (n == 0) continue;
+    CUDA_TRY(cudaMemcpy2DAsync(base + sl.off + c0 * es, sl.dev_pitch, (const char *)sl.host + c0 * es, sl.host_pitch,
+                               n * es, sl.rows, cudaMemcpyHostToDevice, s));
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+int StagedCall::copy_out_window(char *base, cudaStream_t s, size_t c0, size_t n, char *msg, size_t msg_len) const {
+  for (size_t k = n_inputs; k < plan.slots.size(); ++k) {
+    const Slot &sl = plan.slots[k];
+    if (sl.row_bytes == 0 || n == 0) continue;
+    const size_t es = sl.row_bytes / (size_t)atm->n_profile;
+    CUDA_TRY(cudaMemcpy2DAsync((char *)sl.out_host + c0 * es, sl.host_pitch, base + sl.off + c0 * es, sl.dev_pitch,
+                               n * es, sl.rows, cudaMemcpyDeviceToHost, s));
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+void window_params(FluxParams &p, int c0, int n) {
+  auto mv = [&](auto &ptr) { if (ptr) ptr += c0; };
+  mv(p.p); mv(p.t); mv(p.t_level); mv(p.mass); mv(p.gas_mix_ratio); mv(p.density);
+  mv(p.zen_0); mv(p.solar_irrad); mv(p.rho_alb); mv(p.t_ground);
+  mv(p.mode_mix_ratio); mv(p.mode_absorption); mv(p.mode_scattering); mv(p.mode_asymmetry);
+  mv(p.condensed_mix_ratio); mv(p.condensed_dim_char); mv(p.w_cloud); mv(p.frac_cloud);
+  mv(p.c_sub); mv(p.frac_cloudy); mv(p.n_subcol_cld);
+  mv(p.flux_up); mv(p.flux_down); mv(p.flux_direct); mv(p.flux_div); mv(p.heating_rate);
+  p.n_profile = n;
 }
 
 void StagedCall::params(char *base, FluxParams &p) const {
@@ -634,9 +675,14 @@ namespace {
 
 // ---------------------------------------------------------------------------
 // Per-thread device workspace for the host-pointer entry points.
+// The host-pointer call pipelines column chunks over kPipe streams: the
+// inputs of one chunk copy in while another computes and a third copies out.
+constexpr int kPipe = 3;
 struct Workspace {
   int device = -1;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux[kPipe - 1] = {};
+  cudaEvent_t shared_done = nullptr;
   void *buf = nullptr;
   size_t cap = 0;
   int *range = nullptr;
@@ -644,6 +690,9 @@ struct Workspace {
     if (buf) cudaFree(buf);
     if (range) cudaFree(range);
     if (stream) cudaStreamDestroy(stream);
+    for (cudaStream_t a : aux)
+      if (a) cudaStreamDestroy(a);
+    if (shared_done) cudaEventDestroy(shared_done);
   }
 };
 thread_local Workspace tl_ws;
@@ -657,7 +706,15 @@ int ensure_workspace(size_t bytes, char *msg, size_t msg_len) {
     tl_ws.buf = nullptr; tl_ws.cap = 0; tl_ws.range = nullptr;
     if (tl_ws.stream) cudaStreamDestroy(tl_ws.stream);
     tl_ws.stream = nullptr;
+    for (cudaStream_t &a : tl_ws.aux) {
+      if (a) cudaStreamDestroy(a);
+      a = nullptr;
+    }
+    if (tl_ws.shared_done) cudaEventDestroy(tl_ws.shared_done);
+    tl_ws.shared_done = nullptr;
     CUDA_TRY(cudaStreamCreateWithFlags(&tl_ws.stream, cudaStreamNonBlocking));
+    for (cudaStream_t &a : tl_ws.aux) CUDA_TRY(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&tl_ws.shared_done, cudaEventDisableTiming));
     CUDA_TRY(cudaMalloc(&tl_ws.range, 2 * sizeof(int)));
     tl_ws.device = dev;
   }
@@ -893,21 +950,41 @@ int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dime
   SpectrumEntry *sp = find_spectrum(spectrum);
   int st = validate(control, dimen, sp, atm, cld, aer, bound, radout, msg, msg_len);
   if (st != SOCGPU_I_NORMAL) return st;
+  if (atm->n_profile == 0) return SOCGPU_I_NORMAL;
   StagedCall call;
   call.stage(control, dimen, sp, atm, cld, aer, bound, radout);
   st = ensure_workspace(call.plan.bytes, msg, msg_len);
   if (st != SOCGPU_I_NORMAL) return st;
   char *base = (char *)tl_ws.buf;
-  cudaStream_t s = tl_ws.stream;
-  st = call.copy_in(base, s, msg, msg_len);
-  if (st != SOCGPU_I_NORMAL) { cudaStreamSynchronize(s); return st; }
+  cudaStream_t streams[kPipe] = {tl_ws.stream, tl_ws.aux[0], tl_ws.aux[1]};
+  auto sync_all = [&] {
+    for (cudaStream_t x : streams) cudaStreamSynchronize(x);
+  };
+  // column chunks: copy in, compute and copy out of different chunks overlap
+  const int np = atm->n_profile;
+  const int n_chunk = np >= 4096 ? 4 : (np >= 1024 ? 2 : 1);
+  const int chunk = (np + n_chunk - 1) / n_chunk;
+  // the arrays shared by all columns go first, on the first stream
+  st = call.copy_in_window(base, streams[0], 0, 0, true, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
+  CUDA_TRY(cudaEventRecord(tl_ws.shared_done, streams[0]));
+  for (int k = 1; k < kPipe; ++k) CUDA_TRY(cudaStreamWaitEvent(streams[k], tl_ws.shared_done, 0));
   FluxParams p;
   call.params(base, p);
-  st = launch(p, control, s, msg, msg_len);
-  if (st != SOCGPU_I_NORMAL) { cudaStreamSynchronize(s); return st; }
-  st = call.copy_out(base, s, msg, msg_len);
-  if (st != SOCGPU_I_NORMAL) { cudaStreamSynchronize(s); return st; }
-  CUDA_TRY(cudaStreamSynchronize(s));
+  for (int k = 0; k < n_chunk; ++k) {
+    const int c0 = k * chunk, n = std::min(chunk, np - c0);
+    if (n <= 0) break;
+    cudaStream_t sk = streams[k % kPipe];
+    st = call.copy_in_window(base, sk, c0, n, false, msg, msg_len);
+    if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
+    FluxParams pk = p;
+    window_params(pk, c0, n);
+    st = launch(pk, control, sk, msg, msg_len);
+    if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
+    st = call.copy_out_window(base, sk, c0, n, msg, msg_len);
+    if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
+  }
+  for (cudaStream_t x : streams) CUDA_TRY(cudaStreamSynchronize(x));
   return SOCGPU_I_NORMAL;
 }
 

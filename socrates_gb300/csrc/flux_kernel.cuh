@@ -720,6 +720,8 @@ struct FluxKernel {
                                             const R *amt, int s, R pl, R tl) {
     R kg = R(0);
     if (!gt.any_term) {
+      // one absorber (the common case) without the guarded loop
+      if (gt.n_abs == 1) return gt.k[0] * amt[s];
 #pragma unroll
       for (int j = 0; j < kMaxAbsPerBand; ++j)
         if (j < gt.n_abs) {

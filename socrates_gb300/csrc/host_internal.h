@@ -54,6 +54,10 @@ struct FluxVariant {
 };
 const FluxVariant *find_variant(int precision, int mode, int lanes);
 
+// The kernel parameters of columns c0 .. c0+n-1 of a launch (every
+// per-column pointer moved by c0; the leading extents stay).
+void window_params(FluxParams &p, int c0, int n);
+
 // One launch of a single batch (tile from choose_tile).
 int launch(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *msg, size_t msg_len);
 
@@ -63,6 +67,7 @@ struct Slot {
   void *out_host;
   size_t off, rows, row_bytes, host_pitch, dev_pitch;
   bool output;
+  bool per_profile;   // rows of (profile) columns, split by column windows
 };
 
 struct Plan {
@@ -71,10 +76,10 @@ struct Plan {
   // Add an array of `rows` rows of `n_valid` elements each, with leading
   // (Fortran) extent nd in host memory; on the device the same extent is kept.
   size_t add(const void *host, size_t esize, size_t nd, size_t n_valid, size_t rows, bool output = false,
-             void *out_host = nullptr) {
+             void *out_host = nullptr, bool per_profile = true) {
     if (!host && !out_host) return (size_t)-1;
     size_t off = (bytes + 255) & ~(size_t)255;
-    Slot s{host, out_host, off, rows, n_valid * esize, nd * esize, nd * esize, output};
+    Slot s{host, out_host, off, rows, n_valid * esize, nd * esize, nd * esize, output, per_profile};
     slots.push_back(s);
     bytes = off + nd * esize * rows;
     return off;
@@ -106,6 +111,11 @@ struct StagedCall {
   int copy_in(char *base, cudaStream_t s, char *msg, size_t msg_len) const;
   void params(char *base, FluxParams &p) const;
   int copy_out(char *base, cudaStream_t s, char *msg, size_t msg_len) const;
+  // Copies of the column window c0 .. c0+n-1 only; `shared`: the arrays
+  // that are not per column (copied once).
+  int copy_in_window(char *base, cudaStream_t s, size_t c0, size_t n, bool shared, char *msg,
+                     size_t msg_len) const;
+  int copy_out_window(char *base, cudaStream_t s, size_t c0, size_t n, char *msg, size_t msg_len) const;
   long long column_gpoints() const;
 };
 

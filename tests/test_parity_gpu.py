@@ -201,3 +201,20 @@ def test_icrccm27_known_good_output_on_gpu(gpu_lib):
     gmx = R.radiance_calc(_with(ctl, abi.PRECISION_MIXED), sp, col)
     assert_mixed_tolerance({**gmx, "heating_rate": K.heating_rate(gmx, col.mass)},
                            {**ref, "heating_rate": K.heating_rate(ref, col.mass)}, "icrccm27 mixed: ")
+
+
+@pytest.mark.parametrize("prec", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_pipelined_host_path_equals_device_path(gpu_lib, prec):
+    """socgpu_radiance_calc splits a large batch into column chunks whose
+    copies and kernels overlap on several streams; every column must come
+    out exactly as from one device-pointer launch."""
+    import torch
+    from socrates_gb300.device import DeviceCase
+    sp, col = synth.config2(5003, 60, seed=31)
+    ctl = R.sw_control(l_aerosol_mode=True, precision=prec)
+    host = R.radiance_calc(ctl, sp, col)
+    dc = DeviceCase(ctl, sp, col)
+    dc.run(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    for k in ("flux_up", "flux_down", "flux_direct", "heating_rate"):
+        np.testing.assert_array_equal(host[k], dc.output(k), err_msg=k)
