@@ -99,6 +99,8 @@ extern "C" {
 #define SOCGPU_IP_SCALE_POWER_LAW       1
 #define SOCGPU_IP_SCALE_POWER_QUAD      2
 #define SOCGPU_IP_SCALE_DOPPLER_QUAD    3
+#define SOCGPU_IP_SCALE_LOOKUP          9   /* not supported: rejected when read */
+#define SOCGPU_IP_SCALE_T_LOOKUP       10   /* not supported: rejected when read */
 /* Rayleigh schemes, rad_pcf.F90:729-731 */
 #define SOCGPU_IP_RAYLEIGH_TOTAL        1
 /* Continuum types (rad_pcf.F90 ip_self_continuum, ip_frn_continuum) */
@@ -294,6 +296,15 @@ typedef struct socgpu_radout {
 } socgpu_radout;
 
 /* ---- entry points ------------------------------------------------------ */
+
+/* Read a spectral file in the reference's text format and register it
+ * under `name` (the file-reading half of set_spectrum,
+ * src/interface_core/socrates_set_spectrum.F90:90-121; record layouts of
+ * src/radiance_core/read_spectrum.F90).  Blocks 0-6, 8, 9, 13 and the
+ * Pade cloud blocks 10/12 are read; lookup-table k scaling returns
+ * SOCGPU_I_ERR_IO with a message. */
+SOCGPU_API int socgpu_spectrum_load(const char *name, const char *path, socgpu_spectrum_handle *handle,
+                                    char *msg, size_t msg_len);
 
 /* ABI version of the loaded library (compare with SOCGPU_ABI_VERSION). */
 SOCGPU_API int socgpu_abi_version(void);

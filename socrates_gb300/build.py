@@ -34,10 +34,14 @@ PER_FILE = {"cloud_gen.cu": ["-fmad=false"]}
 FLUX_LANES = {0: (16, 32), 1: (8, 16, 32)}
 
 
+TOOL = PKG / "socgpu_run"
+TOOL_MAIN = "run_main.cpp"
+
+
 def units() -> list[tuple[Path, str, list[str]]]:
     """(source, object stem, extra flags) of every object of the library."""
     out = []
-    for src in sorted(CSRC.glob("*.cu")):
+    for src in sorted(list(CSRC.glob("*.cu")) + [p for p in CSRC.glob("*.cpp") if p.name != TOOL_MAIN]):
         if src.name == "flux_inst.cu":
             for prec, lanes_list in FLUX_LANES.items():
                 for mode in (0, 1, 2):
@@ -62,6 +66,8 @@ def _stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
+    if not TOOL.exists():
+        return True
     deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps)
 
@@ -94,8 +100,17 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the column-file driver (socgpu_run), linked against the library
+    tool_tmp = TOOL.with_suffix(".tmp")
+    cmd = [nvcc(), *ARCH, "-std=c++17", "-O2", f"-I{INCLUDE}", f"-I{CSRC}", str(CSRC / TOOL_MAIN),
+           str(BUILD / "cdf_io.o"), "-o", str(tool_tmp), f"-L{PKG}", "-lsocgpu", "-cudart", "shared",
+           "-Xlinker", "-rpath=$ORIGIN", "-Xlinker", "-rpath=/usr/local/cuda/lib64"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link of socgpu_run failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tool_tmp, TOOL)
     if verbose:
-        print(f"built {LIB}", file=sys.stderr)
+        print(f"built {LIB} and {TOOL}", file=sys.stderr)
     return LIB
 
 

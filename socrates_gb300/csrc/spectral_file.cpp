@@ -1,0 +1,464 @@
+// spectral_file.cpp -- reading the reference's text spectral files into a
+// socgpu_spectrum_desc, and socgpu_spectrum_load (the file-reading part of
+// set_spectrum, src/interface_core/socrates_set_spectrum.F90:90-121).
+//
+// Record layouts of read_spectrum.F90 (blocks 0-13): block 0 summary
+// (versions 1 and 2), 1 band limits, 2 solar spectrum, 3 Rayleigh, 4
+// absorbers per band, 5 k-terms (fixed columns: (2(3x,1pe16.9), i3, :,
+// (t42, 1pe16.9, 3x, 1pe16.9))), 6 Planck polynomial, 8 and 9 continua, 13
+// Doppler broadening, 10 and 12 Pade droplet and ice parameters (schemes 5
+// and 20).  Other blocks are skipped; lookup-table k scaling is rejected.
+#include <cctype>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "host_internal.h"
+
+namespace socgpu {
+namespace {
+
+// Parameters of each scaling function (rad_pcf.F90 n_scale_variable).
+int n_scale_variable(int fnc) {
+  static const int n[] = {0, 2, 3, 4, 0, 0, 6, 8, 10, 0, 0};
+  return (fnc >= 0 && fnc <= 10) ? n[fnc] : 0;
+}
+
+std::string upper(std::string s) {
+  for (char &c : s) c = (char)std::toupper((unsigned char)c);
+  return s;
+}
+
+std::vector<std::string> split(const std::string &s) {
+  std::istringstream in(s);
+  std::vector<std::string> out;
+  std::string w;
+  while (in >> w) out.push_back(w);
+  return out;
+}
+
+bool is_int(const std::string &w) {
+  if (w.empty()) return false;
+  for (char c : w)
+    if (!std::isdigit((unsigned char)c) && c != '-' && c != '+') return false;
+  return true;
+}
+
+double num(const std::string &w) {
+  std::string t = w;
+  for (char &c : t)
+    if (c == 'D' || c == 'd') c = 'E';
+  return std::strtod(t.c_str(), nullptr);
+}
+
+// the first integer after '=' in a line
+int int_after_eq(const std::string &line, int which = 0) {
+  size_t p = 0;
+  for (int k = 0; k <= which; ++k) {
+    p = line.find('=', p);
+    if (p == std::string::npos) return 0;
+    ++p;
+  }
+  return std::atoi(line.c_str() + p);
+}
+
+double fixed(const std::string &line, size_t a, size_t b, bool &present) {
+  present = line.size() > a && line.find_first_not_of(' ', a) < std::min(b, line.size());
+  if (!present) return 0.0;
+  return num(line.substr(a, b - a));
+}
+
+struct Block {
+  int type = 0;
+  std::vector<std::string> lines;
+};
+
+}  // namespace
+
+// Owned arrays of one spectral file, in the layouts of socgpu_spectrum_desc.
+struct SpectralFile {
+  int n_band = 0, n_abs = 0, nd_k = 1, nsv = 4, ndc = 1;
+  std::vector<double> wl_s, wl_l, solar, rayleigh;
+  std::vector<int> type_absorb, n_band_absorb, index_absorb, i_band_k, i_scale_k, i_scale_fnc;
+  std::vector<double> k, w, scale, p_ref, t_ref;
+  std::vector<int> l_doppler;
+  std::vector<double> doppler_cor;
+  int n_deg_fit = 0;
+  double t_ref_planck = 0.0;
+  std::vector<double> thermal;
+  std::vector<int> n_band_cont, index_cont, fnc_cont;
+  std::vector<double> k_cont, scale_cont, p_ref_cont, t_ref_cont;
+  int index_water = 0;
+  std::vector<double> drop_parm, ice_parm;
+  std::vector<int> drop_ids, ice_ids, drop_on, ice_on;
+
+  socgpu_spectrum_desc desc() const {
+    socgpu_spectrum_desc d{};
+    d.nd_band = n_band;
+    d.nd_species = std::max(1, n_abs);
+    d.nd_k_term = nd_k;
+    d.nd_scale_variable = nsv;
+    d.n_band = n_band;
+    d.wavelength_short = wl_s.data();
+    d.wavelength_long = wl_l.data();
+    d.solar_flux_band = solar.empty() ? nullptr : solar.data();
+    d.i_rayleigh_scheme = SOCGPU_IP_RAYLEIGH_TOTAL;
+    d.rayleigh_coeff = rayleigh.empty() ? nullptr : rayleigh.data();
+    d.n_absorb = n_abs;
+    d.type_absorb = type_absorb.data();
+    d.n_band_absorb = n_band_absorb.data();
+    d.index_absorb = index_absorb.data();
+    d.i_band_k = i_band_k.data();
+    d.i_scale_k = i_scale_k.data();
+    d.i_scale_fnc = i_scale_fnc.data();
+    d.k = k.data();
+    d.w = w.data();
+    d.scale = scale.data();
+    d.p_ref = p_ref.data();
+    d.t_ref = t_ref.data();
+    d.l_doppler = l_doppler.empty() ? nullptr : l_doppler.data();
+    d.doppler_cor = doppler_cor.empty() ? nullptr : doppler_cor.data();
+    if (!thermal.empty()) {
+      d.n_deg_fit = n_deg_fit;
+      d.t_ref_planck = t_ref_planck;
+      d.nd_thermal_coeff = n_deg_fit + 1;
+      d.thermal_coeff = thermal.data();
+    }
+    if (!drop_ids.empty()) {
+      d.nd_cloud_parameter = 16;
+      d.nd_drop_type = (int)drop_ids.size();
+      d.drop_parm_list = drop_parm.data();
+      d.i_drop_parm = drop_ids.data();
+      d.l_drop_type = drop_on.data();
+    }
+    if (!ice_ids.empty()) {
+      d.nd_cloud_parameter = 16;
+      d.nd_ice_type = (int)ice_ids.size();
+      d.ice_parm_list = ice_parm.data();
+      d.i_ice_parm = ice_ids.data();
+      d.l_ice_type = ice_on.data();
+    }
+    if (!n_band_cont.empty()) {
+      d.nd_continuum = ndc;
+      d.n_band_continuum = n_band_cont.data();
+      d.index_continuum = index_cont.data();
+      d.index_water = index_water;
+      d.i_scale_fnc_cont = fnc_cont.data();
+      d.k_cont = k_cont.data();
+      d.scale_cont = scale_cont.data();
+      d.p_ref_cont = p_ref_cont.data();
+      d.t_ref_cont = t_ref_cont.data();
+    }
+    return d;
+  }
+};
+
+bool read_spectral_file(const std::string &path, SpectralFile &sf, std::string &err) {
+  std::ifstream in(path);
+  if (!in) { err = "cannot open spectral file " + path; return false; }
+  std::vector<Block> blocks;
+  Block *cur = nullptr;
+  std::string line;
+  while (std::getline(in, line)) {
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    if (line.rfind("*BLOCK", 0) == 0) {
+      std::string t = line;
+      for (char &c : t)
+        if (c == ':' || c == '=') c = ' ';
+      auto w = split(t);
+      blocks.emplace_back();
+      cur = &blocks.back();
+      cur->type = w.size() > 2 ? std::atoi(w[2].c_str()) : -1;
+    } else if (line.rfind("*END", 0) == 0) {
+      cur = nullptr;
+    } else if (cur) {
+      cur->lines.push_back(line);
+    }
+  }
+  auto first = [&](int t) -> const Block * {
+    for (const Block &b : blocks)
+      if (b.type == t) return &b;
+    return nullptr;
+  };
+  const Block *b0 = first(0), *b1 = first(1), *b4 = first(4), *b5 = first(5);
+  if (!b0 || !b1) { err = path + ": summary or band limits missing"; return false; }
+  SpectralFile s;
+  for (size_t q = 0; q < b0->lines.size(); ++q) {
+    std::string u = upper(b0->lines[q]);
+    if (u.find("SPECTRAL BANDS") != std::string::npos) s.n_band = int_after_eq(u);
+    else if (u.find("GASEOUS ABSORBERS") != std::string::npos) s.n_abs = int_after_eq(u);
+    else if (u.find("INDEXING NUMBERS") != std::string::npos && u.find("ABSORBER") != std::string::npos &&
+             u.find("AEROSOL") == std::string::npos) {
+      for (int i = 0; i < s.n_abs && q + 2 + i < b0->lines.size(); ++i) {
+        auto w = split(b0->lines[q + 2 + i]);
+        if (w.size() < 2) { err = path + ": bad absorber list"; return false; }
+        s.type_absorb.push_back(std::atoi(w[1].c_str()));
+      }
+    }
+  }
+  if (s.n_band < 1 || (int)s.type_absorb.size() != s.n_abs) { err = path + ": bad summary block"; return false; }
+  const int nb = s.n_band, na = std::max(1, s.n_abs);
+  s.wl_s.assign(nb, 0.0);
+  s.wl_l.assign(nb, 0.0);
+  for (size_t q = 3; q < b1->lines.size(); ++q) {
+    auto w = split(b1->lines[q]);
+    if (w.size() >= 3 && is_int(w[0])) {
+      int b = std::atoi(w[0].c_str()) - 1;
+      if (b >= 0 && b < nb) { s.wl_s[b] = num(w[1]); s.wl_l[b] = num(w[2]); }
+    }
+  }
+  auto band_values = [&](int t, std::vector<double> &out) {
+    const Block *bl = first(t);
+    if (!bl) return;
+    out.assign(nb, 0.0);
+    for (const std::string &l : bl->lines) {
+      auto w = split(l);
+      if (w.size() >= 2 && is_int(w[0])) {
+        int b = std::atoi(w[0].c_str()) - 1;
+        if (b >= 0 && b < nb) out[b] = num(w[1]);
+      }
+    }
+  };
+  band_values(2, s.solar);
+  band_values(3, s.rayleigh);
+  // block 4
+  s.n_band_absorb.assign(nb, 0);
+  s.index_absorb.assign((size_t)na * nb, 0);
+  if (b4) {
+    std::vector<std::string> tok;
+    for (size_t q = 5; q < b4->lines.size(); ++q)
+      for (auto &w : split(b4->lines[q])) tok.push_back(w);
+    size_t q = 0;
+    for (int i = 0; i < nb && q + 1 < tok.size(); ++i) {
+      int b = std::atoi(tok[q].c_str()) - 1, n = std::atoi(tok[q + 1].c_str());
+      q += 2;
+      if (b < 0 || b >= nb || n < 0 || n > na) { err = path + ": bad block 4"; return false; }
+      s.n_band_absorb[b] = n;
+      for (int j = 0; j < n && q < tok.size(); ++j) s.index_absorb[(size_t)j + (size_t)na * b] = std::atoi(tok[q++].c_str());
+    }
+  }
+  // block 5: first pass for sizes
+  struct Term { double k, w; std::vector<double> sc; };
+  struct Rec { int b, g, nk, sk, fnc; double p, t; std::vector<Term> terms; };
+  std::vector<Rec> recs;
+  if (b5) {
+    const auto &L = b5->lines;
+    size_t q = 4;
+    while (q < L.size()) {
+      auto w = split(L[q]);
+      if (w.size() < 5 || !is_int(w[0])) { ++q; continue; }
+      Rec r{std::atoi(w[0].c_str()) - 1, std::atoi(w[1].c_str()) - 1, std::atoi(w[2].c_str()),
+            std::atoi(w[3].c_str()), std::atoi(w[4].c_str()), 0.0, 0.0, {}};
+      if (r.fnc == SOCGPU_IP_SCALE_LOOKUP || r.fnc == SOCGPU_IP_SCALE_T_LOOKUP) {
+        err = path + ": lookup-table k scaling is not supported";
+        return false;
+      }
+      if (q + 1 >= L.size()) break;
+      auto pt = split(L[q + 1]);
+      if (pt.size() < 2) { err = path + ": bad block 5"; return false; }
+      r.p = num(pt[0]);
+      r.t = num(pt[1]);
+      q += 2;
+      const int nsv = n_scale_variable(r.fnc);
+      for (int t = 0; t < r.nk && q < L.size(); ++t) {
+        Term tm;
+        bool pr = false;
+        tm.k = fixed(L[q], 3, 19, pr);
+        tm.w = fixed(L[q], 22, 38, pr);
+        std::string col = L[q];
+        while ((int)tm.sc.size() < nsv) {
+          const size_t starts[2] = {41, 60};
+          for (size_t a : starts)
+            if ((int)tm.sc.size() < nsv) {
+              double v = fixed(col, a, a + 16, pr);
+              if (pr) tm.sc.push_back(v);
+            }
+          if ((int)tm.sc.size() < nsv) {
+            if (++q >= L.size()) break;
+            col = L[q];
+          }
+        }
+        ++q;
+        r.terms.push_back(tm);
+      }
+      s.nd_k = std::max(s.nd_k, r.nk);
+      s.nsv = std::max(s.nsv, nsv);
+      recs.push_back(std::move(r));
+    }
+  }
+  const size_t ndk = s.nd_k, nsv = s.nsv;
+  s.i_band_k.assign((size_t)nb * na, 0);
+  s.i_scale_k.assign((size_t)nb * na, 0);
+  s.i_scale_fnc.assign((size_t)nb * na, 0);
+  s.k.assign(ndk * nb * na, 0.0);
+  s.w.assign(ndk * nb * na, 0.0);
+  s.scale.assign(nsv * ndk * nb * na, 0.0);
+  s.p_ref.assign((size_t)na * nb, 0.0);
+  s.t_ref.assign((size_t)na * nb, 0.0);
+  for (const Rec &r : recs) {
+    if (r.b < 0 || r.b >= nb || r.g < 0 || r.g >= na) { err = path + ": bad band/gas in block 5"; return false; }
+    const size_t bg = (size_t)r.b + (size_t)nb * r.g;
+    s.i_band_k[bg] = r.nk;
+    s.i_scale_k[bg] = r.sk;
+    s.i_scale_fnc[bg] = r.fnc;
+    s.p_ref[(size_t)r.g + (size_t)na * r.b] = r.p;
+    s.t_ref[(size_t)r.g + (size_t)na * r.b] = r.t;
+    for (size_t t = 0; t < r.terms.size(); ++t) {
+      const size_t tbg = t + ndk * ((size_t)r.b + (size_t)nb * r.g);
+      s.k[tbg] = r.terms[t].k;
+      s.w[tbg] = r.terms[t].w;
+      for (size_t v = 0; v < r.terms[t].sc.size(); ++v) s.scale[v + nsv * tbg] = r.terms[t].sc[v];
+    }
+  }
+  // block 6
+  if (const Block *b6 = first(6)) {
+    size_t h = 0;
+    while (h < b6->lines.size() && b6->lines[h].find('=') == std::string::npos) ++h;
+    if (h >= b6->lines.size()) { err = path + ": bad block 6"; return false; }
+    s.n_deg_fit = int_after_eq(b6->lines[h]);
+    const size_t eq2 = b6->lines[h].find('=', b6->lines[h].find('=') + 1);
+    s.t_ref_planck = num(b6->lines[h].substr(eq2 + 1));
+    std::vector<std::string> tok;
+    for (size_t q = h + 3; q < b6->lines.size(); ++q)
+      for (auto &w : split(b6->lines[q])) tok.push_back(w);
+    s.thermal.assign((size_t)(s.n_deg_fit + 1) * nb, 0.0);
+    size_t q = 0;
+    for (int i = 0; i < nb && q < tok.size(); ++i) {
+      int b = std::atoi(tok[q++].c_str()) - 1;
+      for (int j = 0; j <= s.n_deg_fit && q < tok.size(); ++j)
+        if (b >= 0 && b < nb) s.thermal[(size_t)j + (size_t)(s.n_deg_fit + 1) * b] = num(tok[q++]);
+    }
+  }
+  // blocks 8 and 9
+  if (const Block *b8 = first(8)) {
+    std::vector<std::string> tok;
+    for (size_t q = 5; q < b8->lines.size(); ++q) {
+      const std::string &l = b8->lines[q];
+      if (l.find('=') != std::string::npos) s.index_water = int_after_eq(l);
+      else {
+        auto w = split(l);
+        if (!w.empty() && is_int(w[0]))
+          for (auto &x : w) tok.push_back(x);
+      }
+    }
+    std::vector<std::vector<int>> idx(nb);
+    size_t q = 0;
+    int maxc = 1;
+    while (q + 1 < tok.size()) {
+      int b = std::atoi(tok[q].c_str()) - 1, n = std::atoi(tok[q + 1].c_str());
+      q += 2;
+      if (b < 0 || b >= nb || n < 0) { err = path + ": bad block 8"; return false; }
+      for (int j = 0; j < n && q < tok.size(); ++j) idx[b].push_back(std::atoi(tok[q++].c_str()));
+      maxc = std::max(maxc, n);
+    }
+    s.ndc = maxc;
+    const size_t ndc = s.ndc;
+    s.n_band_cont.assign(nb, 0);
+    s.index_cont.assign((size_t)nb * ndc, 0);
+    s.fnc_cont.assign((size_t)nb * ndc, 0);
+    s.k_cont.assign((size_t)nb * ndc, 0.0);
+    s.scale_cont.assign(nsv * nb * ndc, 0.0);
+    s.p_ref_cont.assign(ndc * nb, 0.0);
+    s.t_ref_cont.assign(ndc * nb, 0.0);
+    for (int b = 0; b < nb; ++b) {
+      s.n_band_cont[b] = (int)idx[b].size();
+      for (size_t j = 0; j < idx[b].size(); ++j) s.index_cont[(size_t)b + (size_t)nb * j] = idx[b][j];
+    }
+    if (const Block *b9 = first(9)) {
+      std::vector<std::string> t9;
+      for (size_t q9 = 3; q9 < b9->lines.size(); ++q9)
+        for (auto &x : split(b9->lines[q9])) t9.push_back(x);
+      size_t r = 0;
+      while (r + 5 < t9.size()) {
+        int b = std::atoi(t9[r].c_str()) - 1, ci = std::atoi(t9[r + 1].c_str()), fnc = std::atoi(t9[r + 2].c_str());
+        if (b < 0 || b >= nb) { err = path + ": bad block 9"; return false; }
+        size_t j = 0;
+        while (j < idx[b].size() && idx[b][j] != ci) ++j;
+        if (j == idx[b].size()) { err = path + ": continuum of block 9 not listed in block 8"; return false; }
+        const size_t bj = (size_t)b + (size_t)nb * j;
+        s.fnc_cont[bj] = fnc;
+        s.p_ref_cont[j + ndc * b] = num(t9[r + 3]);
+        s.t_ref_cont[j + ndc * b] = num(t9[r + 4]);
+        s.k_cont[bj] = num(t9[r + 5]);
+        const int nv = n_scale_variable(fnc);
+        for (int v = 0; v < nv && r + 6 + v < t9.size(); ++v) s.scale_cont[(size_t)v + nsv * bj] = num(t9[r + 6 + v]);
+        r += 6 + nv;
+      }
+    }
+  }
+  // block 13
+  if (const Block *b13 = first(13)) {
+    s.l_doppler.assign(na, 0);
+    s.doppler_cor.assign(na, 0.0);
+    for (size_t q = 2; q < b13->lines.size(); ++q) {
+      auto w = split(b13->lines[q]);
+      if (w.size() >= 3 && is_int(w[0])) {
+        int i = std::atoi(w[0].c_str()) - 1;
+        if (i >= 0 && i < na) {
+          s.l_doppler[i] = (std::toupper((unsigned char)w[1][0]) == 'T') ? 1 : 0;
+          s.doppler_cor[i] = num(w[2]);
+        }
+      }
+    }
+  }
+  // blocks 10 and 12: Pade parameter sets
+  auto pade = [&](int t, int want, std::vector<double> &parm, std::vector<int> &ids, std::vector<int> &on) {
+    for (const Block &bl : blocks) {
+      if (bl.type != t) continue;
+      size_t h = 0;
+      while (h < bl.lines.size() &&
+             !(bl.lines[h].find('=') != std::string::npos && upper(bl.lines[h]).find("PARAMETERS") != std::string::npos))
+        ++h;
+      if (h >= bl.lines.size()) continue;
+      const int scheme = int_after_eq(bl.lines[h]), npar = int_after_eq(bl.lines[h], 1);
+      if (scheme != want || npar != 16) continue;
+      std::vector<std::string> tok;
+      for (size_t q = h + 1; q < bl.lines.size(); ++q) {
+        const std::string &l = bl.lines[q];
+        const std::string u = upper(l);
+        bool digit = false;
+        for (char c : l) digit |= (bool)std::isdigit((unsigned char)c);
+        if (u.find("RANGE") != std::string::npos || !digit) continue;
+        if (u.find("BAND") != std::string::npos && l.find('=') != std::string::npos) tok.push_back(std::to_string(int_after_eq(l)));
+        else
+          for (auto &x : split(l)) tok.push_back(x);
+      }
+      const size_t base = parm.size();
+      parm.resize(base + 16 * (size_t)nb, 0.0);
+      size_t q = 0;
+      for (int i = 0; i < nb && q < tok.size(); ++i) {
+        int b = std::atoi(tok[q++].c_str()) - 1;
+        for (int v = 0; v < 16 && q < tok.size(); ++v)
+          if (b >= 0 && b < nb) parm[base + (size_t)v + 16 * (size_t)b] = num(tok[q++]);
+      }
+      ids.push_back(scheme);
+      on.push_back(1);
+    }
+  };
+  pade(10, SOCGPU_IP_DROP_PADE_2, s.drop_parm, s.drop_ids, s.drop_on);
+  pade(12, SOCGPU_IP_ICE_PADE_2_PHF, s.ice_parm, s.ice_ids, s.ice_on);
+  sf = std::move(s);
+  return true;
+}
+
+}  // namespace socgpu
+
+using namespace socgpu;
+
+extern "C" int socgpu_spectrum_load(const char *name, const char *path, socgpu_spectrum_handle *handle, char *msg,
+                                    size_t msg_len) {
+  if (!name || !path || !handle) { set_msg(msg, msg_len, "null argument"); return SOCGPU_I_ERR_FATAL; }
+  SpectralFile sf;
+  std::string err;
+  if (!read_spectral_file(path, sf, err)) {
+    set_msg(msg, msg_len, "%s", err.c_str());
+    return SOCGPU_I_ERR_IO;
+  }
+  socgpu_spectrum_desc d = sf.desc();
+  return socgpu_spectrum_register(name, &d, handle, msg, msg_len);
+}

@@ -25,3 +25,25 @@ def field(path, coord="plev"):
     names = [k for k in v if k not in ("lat", "lon", "plev", "basis")]
     assert len(names) == 1, (path, names)
     return v.get(coord), v[names[0]]
+
+
+def write_cdl(path, name, dims, variables):
+    """Write a CDL file like the reference's column files: `dims` is a list
+    of (name, length); `variables` a list of (name, dim names, values,
+    {attribute: text}) with values in C order."""
+    lines = [f"netcdf {name}{{", "", "dimensions:"]
+    for d, n in dims:
+        lines.append(f"    {d:<15s}= {n:3d};")
+    lines += ["", "", "variables:"]
+    for v, vd, _, atts in variables:
+        lines.append(f"    float {v}({','.join(vd)});")
+        for k, t in atts.items():
+            lines.append(f'             {v}:{k} = "{t}";')
+    lines += ["", "data:"]
+    for v, _, vals, _ in variables:
+        flat = [f"{x: .6E}" for x in np.ravel(vals)]
+        body = ",\n                    ".join(", ".join(flat[i:i + 4]) for i in range(0, len(flat), 4))
+        lines.append(f"{v:>17s} = {body};")
+    lines += ["", "}"]
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")

@@ -1,0 +1,123 @@
+"""socgpu_run, the drop-in for the reference's Cl_run_cdl / Cl_run_cdf
+column drivers: netCDF classic and CDL files in, the same files out.
+
+CPU tests check the file formats (CDL -> CDF -> CDL through the driver's
+converter, cross-checked with scipy's netCDF reader); GPU tests run the
+reference's ICRCCM case 27 (examples/aer_cmp/run27) end to end from CDL and
+from netCDF files and compare the written heating rates with the reference's
+known-good output."""
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import icrccm27 as K
+from cdl import field, read_cdl, write_cdl
+from socrates_gb300 import build
+
+ROOT = Path(__file__).resolve().parent.parent
+SUFFIX = {1: "q", 2: "co2", 3: "o3", 4: "n2o", 6: "ch4", 14: "cfc11", 15: "cfc12", 16: "cfc113", 17: "hcfc22",
+          18: "hfc125", 19: "hfc134a"}
+
+
+def _tool():
+    build.build()
+    return str(build.TOOL)
+
+
+def _case27_files(tmp, to_cdf=False):
+    """The case's inputs written as column files like the reference's."""
+    d = np.load(K.FIXTURE)
+    from socrates_gb300.spectrum import Spectrum
+    sp = Spectrum.load_npz(K.FIXTURE, prefix="sp_")
+    sp_path = tmp / "sp_lw_hadcm3"
+    sp.write_text(sp_path)
+    base = tmp / "laer27"
+    dims3 = [("lat", 1), ("lon", 1), ("plev", None)]
+    coord = {"units": "degree", "title": "latitude"}
+
+    def put(suffix, plev, values, name, units="None"):
+        dims = [("lat", 1), ("lon", 1), ("plev", len(plev))]
+        variables = [("lat", ["lat"], [0.0], coord), ("lon", ["lon"], [0.0], {"units": "degree", "title": "longitude"}),
+                     ("plev", ["plev"], plev, {"units": "Pa", "title": "PRESSURE"}),
+                     (name, ["plev", "lon", "lat"], np.reshape(values, (len(plev), 1, 1)), {"units": units})]
+        path = tmp / f"laer27.{suffix}"
+        write_cdl(path, f"laer27.{suffix}", dims, variables)
+        return path
+
+    files = [put("t", d["p"], d["t"], "t", "K"), put("tl", d["p_level"], d["t_level"], "tl", "K")]
+    for j, ty in enumerate(sp.type_absorb):
+        files.append(put(SUFFIX[int(ty)], d["p"], d["gas"][:, j], SUFFIX[int(ty)]))
+    files.append(put("tstar", [1.013e5], d["t_ground"], "tstar", "K"))
+    surf = tmp / "laer27.surf"
+    write_cdl(surf, "laer27.surf", [("lat", 1), ("lon", 1), ("basis", 1)],
+              [("lat", ["lat"], [1.0], {}), ("lon", ["lon"], [0.0], {}), ("basis", ["basis"], [1.0], {}),
+               ("alb", ["basis", "lat", "lon"], np.reshape(d["alb"], (1, 1, 1)), {"title": "ALBEDO WEIGHTS"})])
+    files.append(surf)
+    if to_cdf:
+        tool = _tool()
+        for f in files:
+            tmp_out = f.with_name(f.name + ".cdf")
+            subprocess.run([tool, "--convert", str(f), str(tmp_out)], check=True)
+            tmp_out.replace(f)
+    return sp_path, base
+
+
+def test_cdl_cdf_round_trip(tmp_path):
+    scipy_io = pytest.importorskip("scipy.io")
+    tool = _tool()
+    src = tmp_path / "x.t"
+    plev = np.array([10.0, 200.0, 3000.5, 90000.0])
+    write_cdl(src, "x.t", [("lat", 2), ("lon", 3), ("plev", 4)],
+              [("lat", ["lat"], [0.0, 1.0], {"units": "degree"}), ("lon", ["lon"], [0.0, 1.0, 2.0], {}),
+               ("plev", ["plev"], plev, {"units": "Pa"}),
+               ("t", ["plev", "lon", "lat"], np.arange(24.0).reshape(4, 3, 2) + 200.25, {"units": "K"})])
+    cdf = tmp_path / "x.cdf"
+    subprocess.run([tool, "--convert", str(src), str(cdf)], check=True)
+    with scipy_io.netcdf_file(str(cdf), "r", mmap=False) as nc:
+        np.testing.assert_allclose(nc.variables["plev"][:], plev, rtol=1e-6)
+        np.testing.assert_allclose(nc.variables["t"][:], np.arange(24.0).reshape(4, 3, 2) + 200.25, rtol=1e-6)
+        assert nc.variables["t"].units in (b"K", "K")
+    back = tmp_path / "y.cdl"
+    subprocess.run([tool, "--convert", str(cdf), str(back)], check=True)
+    dims, v = read_cdl(back)
+    assert dims == {"lat": 2, "lon": 3, "plev": 4}
+    np.testing.assert_allclose(v["t"], (np.arange(24.0) + 200.25), rtol=1e-6)
+
+
+def test_driver_rejects_bad_options(tmp_path):
+    tool = _tool()
+    r = subprocess.run([tool, "-B", str(tmp_path / "none")], capture_output=True, text=True)
+    assert r.returncode != 0 and "Spectral file not set" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("to_cdf", [False, True])
+def test_driver_reproduces_icrccm27(gpu_lib, tmp_path, to_cdf):
+    tool = _tool()
+    sp, base = _case27_files(tmp_path, to_cdf)
+    cmd = [tool, "-s", str(sp), "-R", "1", "8", "-I", "-g", "2", "-c", "-t", "12", "-v", "13", "-C", "5",
+           "-B", str(base)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = str(base) + ".hrts"
+    if to_cdf:
+        scipy_io = pytest.importorskip("scipy.io")
+        with scipy_io.netcdf_file(out, "r", mmap=False) as nc:
+            hr = np.array(nc.variables["hrts"][:]).ravel()
+    else:
+        _, hr = field(out)
+    kgo = K.load()[3]
+    if to_cdf:
+        # netCDF "float" variables hold single precision: inputs and outputs
+        # rounded to float32 move the heating rates by up to about 1e-6 relative
+        assert np.abs(hr - kgo).max() <= 2e-5 * np.abs(kgo).max()
+    else:
+        # CDL text carries 7 significant digits: the reference's 6 must match
+        half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
+        assert (np.abs(hr - kgo) / half_unit).max() <= 1.05
+    r = subprocess.run(cmd + ["-P", "mixed"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _, hr_mixed = field(out) if not to_cdf else (None, hr)
+    assert np.abs(hr_mixed - kgo).max() <= 0.05
