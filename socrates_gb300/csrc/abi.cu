@@ -685,8 +685,11 @@ struct Workspace {
   cudaEvent_t shared_done = nullptr;
   void *buf = nullptr;
   size_t cap = 0;
+  char *pinned = nullptr;          // page-locked staging for pageable caller arrays
+  size_t pinned_cap = 0;
   int *range = nullptr;
   ~Workspace() {
+    if (pinned) cudaFreeHost(pinned);
     if (buf) cudaFree(buf);
     if (range) cudaFree(range);
     if (stream) cudaStreamDestroy(stream);
@@ -724,6 +727,95 @@ int ensure_workspace(size_t bytes, char *msg, size_t msg_len) {
     size_t want = bytes + bytes / 4;
     CUDA_TRY(cudaMalloc(&tl_ws.buf, want));
     tl_ws.cap = want;
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+// Host-pointer call from pageable caller arrays: column chunks are packed
+// into page-locked staging (one region per stream, reused once the stream's
+// previous chunk is done), copied in, computed and copied out; the results
+// are unpacked into the caller's arrays after the chunk's stream is synchronised.
+int staged_radiance_calc(const StagedCall &call, const socgpu_control *control, char *base,
+                         cudaStream_t *streams, char *msg, size_t msg_len) {
+  const size_t np = (size_t)call.atm->n_profile;
+  const auto &slots = call.plan.slots;
+  // the arrays shared by all columns (small): synchronous copies
+  for (size_t k = 0; k < call.n_inputs; ++k) {
+    const Slot &sl = slots[k];
+    if (sl.per_profile || sl.row_bytes == 0) continue;
+    CUDA_TRY(cudaMemcpy2D(base + sl.off, sl.dev_pitch, sl.host, sl.host_pitch, sl.row_bytes, sl.rows,
+                          cudaMemcpyHostToDevice));
+  }
+  size_t per_col = 0;
+  for (const Slot &sl : slots)
+    if (sl.per_profile && sl.row_bytes) per_col += sl.rows * (sl.row_bytes / np);
+  const size_t target = (size_t)64 << 20;
+  size_t cols = std::max<size_t>(256, target / std::max<size_t>(per_col, 1));
+  cols = std::min(cols, np);
+  const size_t region = (cols * per_col + 255) & ~(size_t)255;
+  if (tl_ws.pinned_cap < region * kPipe) {
+    if (tl_ws.pinned) cudaFreeHost(tl_ws.pinned);
+    tl_ws.pinned = nullptr;
+    tl_ws.pinned_cap = 0;
+    CUDA_TRY(cudaMallocHost((void **)&tl_ws.pinned, region * kPipe));
+    tl_ws.pinned_cap = region * kPipe;
+  }
+  FluxParams p;
+  call.params(base, p);
+  const size_t n_chunk = (np + cols - 1) / cols;
+  std::vector<size_t> chunk_c0(n_chunk), chunk_n(n_chunk);
+  auto unpack = [&](size_t k) {
+    char *r = tl_ws.pinned + region * (k % kPipe);
+    const size_t c0 = chunk_c0[k], n = chunk_n[k];
+    size_t pos = 0;
+    for (const Slot &sl : slots) {
+      if (!sl.per_profile || sl.row_bytes == 0) continue;
+      const size_t es = sl.row_bytes / np, w = n * es;
+      if (sl.output)
+        for (size_t row = 0; row < sl.rows; ++row)
+          std::memcpy((char *)sl.out_host + c0 * es + row * sl.host_pitch, r + pos + row * w, w);
+      pos += sl.rows * w;
+    }
+  };
+  for (size_t k = 0; k < n_chunk; ++k) {
+    const size_t c0 = k * cols, n = std::min(cols, np - c0);
+    chunk_c0[k] = c0;
+    chunk_n[k] = n;
+    cudaStream_t sk = streams[k % kPipe];
+    if (k >= (size_t)kPipe) {        // the region's previous chunk must be done and unpacked
+      CUDA_TRY(cudaStreamSynchronize(sk));
+      unpack(k - kPipe);
+    }
+    char *r = tl_ws.pinned + region * (k % kPipe);
+    size_t pos = 0;
+    for (const Slot &sl : slots) {
+      if (!sl.per_profile || sl.row_bytes == 0) continue;
+      const size_t es = sl.row_bytes / np, w = n * es;
+      if (!sl.output) {
+        for (size_t row = 0; row < sl.rows; ++row)
+          std::memcpy(r + pos + row * w, (const char *)sl.host + c0 * es + row * sl.host_pitch, w);
+        CUDA_TRY(cudaMemcpy2DAsync(base + sl.off + c0 * es, sl.dev_pitch, r + pos, w, w, sl.rows,
+                                   cudaMemcpyHostToDevice, sk));
+      }
+      pos += sl.rows * w;
+    }
+    FluxParams pk = p;
+    window_params(pk, (int)c0, (int)n);
+    int st = launch(pk, control, sk, msg, msg_len);
+    if (st != SOCGPU_I_NORMAL) return st;
+    pos = 0;
+    for (const Slot &sl : slots) {
+      if (!sl.per_profile || sl.row_bytes == 0) continue;
+      const size_t es = sl.row_bytes / np, w = n * es;
+      if (sl.output)
+        CUDA_TRY(cudaMemcpy2DAsync(r + pos, w, base + sl.off + c0 * es, sl.dev_pitch, w, sl.rows,
+                                   cudaMemcpyDeviceToHost, sk));
+      pos += sl.rows * w;
+    }
+  }
+  for (size_t k = (n_chunk > (size_t)kPipe ? n_chunk - kPipe : 0); k < n_chunk; ++k) {
+    CUDA_TRY(cudaStreamSynchronize(streams[k % kPipe]));
+    unpack(k);
   }
   return SOCGPU_I_NORMAL;
 }
@@ -960,6 +1052,20 @@ int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dime
   auto sync_all = [&] {
     for (cudaStream_t x : streams) cudaStreamSynchronize(x);
   };
+  // Caller arrays that are not page-locked never go to the copy engines
+  // directly: they are packed chunk by chunk into page-locked staging.
+  bool all_pinned = true;
+  for (const Slot &sl : call.plan.slots) {
+    const void *hp = sl.output ? sl.out_host : sl.host;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, hp) != cudaSuccess) { cudaGetLastError(); all_pinned = false; break; }
+    if (at.type != cudaMemoryTypeHost) { all_pinned = false; break; }
+  }
+  if (!all_pinned) {
+    st = staged_radiance_calc(call, control, base, streams, msg, msg_len);
+    if (st != SOCGPU_I_NORMAL) sync_all();
+    return st;
+  }
   // column chunks: copy in, compute and copy out of different chunks overlap
   const int np = atm->n_profile;
   const int n_chunk = np >= 4096 ? 4 : (np >= 1024 ? 2 : 1);
