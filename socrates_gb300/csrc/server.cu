@@ -13,7 +13,10 @@
 // an event, all on its stream slot's stream.  Up to `streams` waves are in
 // flight at once, so requests that arrive while others run are admitted as
 // soon as a slot and memory free up, and their work overlaps on the device.
-// The spectra stay device resident in the library's registry.
+// The spectra stay device resident in the library's registry.  Requests
+// whose host arrays are page-locked are copied asynchronously on the wave's
+// stream; pageable ones synchronously, in before the wave's kernels and out
+// when the wave is retired.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -100,6 +103,7 @@ struct Request {
   socgpu_radout radout{};
   bool has_cld = false, has_aer = false;
   StagedCall call;
+  bool pinned = false;   // every host array page-locked: asynchronous copies on the wave's stream
   size_t bytes = 0, off = 0;
   long long colg = 0;
   Clock::time_point t_submit, t_start, t_done;
@@ -137,8 +141,34 @@ struct socgpu_server_s {
 
 namespace {
 
+// Synchronous copies of a request whose host arrays are pageable: the
+// copy engines never read or write pageable memory asynchronously.
+int copy_sync(const Request &r, char *base, bool out, char *msg, size_t msg_len) {
+  const auto &slots = r.call.plan.slots;
+  for (size_t k = out ? r.call.n_inputs : 0; k < (out ? slots.size() : r.call.n_inputs); ++k) {
+    const Slot &sl = slots[k];
+    if (sl.row_bytes == 0) continue;
+    if (out)
+      CUDA_TRY(cudaMemcpy2D(sl.out_host, sl.host_pitch, base + sl.off, sl.dev_pitch, sl.row_bytes, sl.rows,
+                            cudaMemcpyDeviceToHost));
+    else
+      CUDA_TRY(cudaMemcpy2D(base + sl.off, sl.dev_pitch, sl.host, sl.host_pitch, sl.row_bytes, sl.rows,
+                            cudaMemcpyHostToDevice));
+  }
+  return SOCGPU_I_NORMAL;
+}
+
 // Retire a finished wave (called with the server mutex held).
 void finish(socgpu_server_s &S, StreamSlot &sl, cudaError_t e) {
+  for (Request *r : sl.reqs) {
+    if (e == cudaSuccess && r->status == SOCGPU_I_NORMAL && !r->pinned) {
+      char m[256] = "";
+      if (copy_sync(*r, S.dmem + r->off, true, m, sizeof(m)) != SOCGPU_I_NORMAL) {
+        r->status = SOCGPU_I_ABORT_CALCULATION;
+        r->msg = m;
+      }
+    }
+  }
   const Clock::time_point now = Clock::now();
   for (Request *r : sl.reqs) {
     r->t_done = now;
@@ -175,7 +205,8 @@ void launch_wave(socgpu_server_s &S, StreamSlot &sl) {
   for (Request *r : wave) r->t_start = now;
   // inputs
   for (Request *r : wave)
-    if (r->call.copy_in(S.dmem + r->off, st, msg, msg_len) != SOCGPU_I_NORMAL) {
+    if ((r->pinned ? r->call.copy_in(S.dmem + r->off, st, msg, msg_len)
+                   : copy_sync(*r, S.dmem + r->off, false, msg, msg_len)) != SOCGPU_I_NORMAL) {
       fail_all(wave, SOCGPU_I_ABORT_CALCULATION, msg);
       cudaEventRecord(sl.done, st);
       return;
@@ -245,7 +276,8 @@ void launch_wave(socgpu_server_s &S, StreamSlot &sl) {
     return;
   }
   for (Request *r : wave)
-    if (r->call.copy_out(S.dmem + r->off, st, msg, msg_len) != SOCGPU_I_NORMAL) fail_all(wave, SOCGPU_I_ABORT_CALCULATION, msg);
+    if (r->pinned && r->call.copy_out(S.dmem + r->off, st, msg, msg_len) != SOCGPU_I_NORMAL)
+      fail_all(wave, SOCGPU_I_ABORT_CALCULATION, msg);
   cudaEventRecord(sl.done, st);
 }
 
@@ -388,6 +420,13 @@ int socgpu_server_submit(socgpu_server server, const socgpu_request *q, long lon
   r->call.stage(&r->control, &r->dimen, sp, &r->atm, r->has_cld ? &r->cld : nullptr,
                 r->has_aer ? &r->aer : nullptr, &r->bound, &r->radout);
   r->bytes = align256(r->call.plan.bytes);
+  r->pinned = true;
+  for (const Slot &sl : r->call.plan.slots) {
+    cudaPointerAttributes at{};
+    const void *hp = sl.output ? sl.out_host : sl.host;
+    if (cudaPointerGetAttributes(&at, hp) != cudaSuccess) { cudaGetLastError(); r->pinned = false; break; }
+    if (at.type != cudaMemoryTypeHost) { r->pinned = false; break; }
+  }
   r->colg = r->call.column_gpoints();
   if (r->bytes > server->arena.size()) {
     set_msg(msg, msg_len, "request needs %zu bytes of device memory, more than the server's %zu", r->bytes,
