@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -731,6 +732,18 @@ int ensure_workspace(size_t bytes, char *msg, size_t msg_len) {
   return SOCGPU_I_NORMAL;
 }
 
+// Bytes of one column chunk of the host-pointer pipeline: 24 MB unless the
+// environment variable SOCGPU_CHUNK_MB sets another size (a tuning knob,
+// read once).
+size_t pipeline_chunk_bytes() {
+  static const size_t bytes = [] {
+    const char *e = std::getenv("SOCGPU_CHUNK_MB");
+    const long mb = e ? std::atol(e) : 0;
+    return (size_t)(mb > 0 ? mb : 24) << 20;
+  }();
+  return bytes;
+}
+
 // Host-pointer call from pageable caller arrays: column chunks are packed
 // into page-locked staging (one region per stream, reused once the stream's
 // previous chunk is done), copied in, computed and copied out; the results
@@ -749,7 +762,7 @@ int staged_radiance_calc(const StagedCall &call, const socgpu_control *control, 
   size_t per_col = 0;
   for (const Slot &sl : slots)
     if (sl.per_profile && sl.row_bytes) per_col += sl.rows * (sl.row_bytes / np);
-  const size_t target = (size_t)64 << 20;
+  const size_t target = std::max<size_t>(pipeline_chunk_bytes(), (size_t)64 << 20);
   size_t cols = std::max<size_t>(256, target / std::max<size_t>(per_col, 1));
   cols = std::min(cols, np);
   const size_t region = (cols * per_col + 255) & ~(size_t)255;
@@ -1066,10 +1079,15 @@ int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dime
     if (st != SOCGPU_I_NORMAL) sync_all();
     return st;
   }
-  // column chunks: copy in, compute and copy out of different chunks overlap
+  // column chunks: copy in, compute and copy out of different chunks overlap;
+  // chunks of about pipeline_chunk_bytes(), at least 512 columns
   const int np = atm->n_profile;
-  const int n_chunk = np >= 4096 ? 4 : (np >= 1024 ? 2 : 1);
-  const int chunk = (np + n_chunk - 1) / n_chunk;
+  size_t per_col = 0;
+  for (const Slot &sl : call.plan.slots)
+    if (sl.per_profile && sl.row_bytes) per_col += sl.rows * (sl.row_bytes / (size_t)np);
+  const size_t want = std::max<size_t>(512, pipeline_chunk_bytes() / std::max<size_t>(per_col, 1));
+  const int chunk = (int)std::min<size_t>((size_t)np, want);
+  const int n_chunk = (np + chunk - 1) / chunk;
   // the arrays shared by all columns go first, on the first stream
   st = call.copy_in_window(base, streams[0], 0, 0, true, msg, msg_len);
   if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
