@@ -923,11 +923,11 @@ int launch_group(const BatchGroup &g, FluxParams *di, long long *ds, cudaStream_
 // Group the batches by the tile each one is given (tuner table, overrides or
 // heuristic), prepare, upload and capture the graph.
 int build_plan(socgpu_batch_s &b, char *msg, size_t msg_len) {
-  std::map<std::tuple<int, int, int, int, int>, std::vector<int>> classes;
+  std::map<std::tuple<int, int, int, int, int, int>, std::vector<int>> classes;
   for (size_t i = 0; i < b.params.size(); ++i) {
     TileConfig t = choose_tile(b.precision[i], b.mode[i], b.params[i].n_layer);
-    classes[std::make_tuple(b.precision[i], b.mode[i], t.lanes_per_solve, t.chunk, t.warps_per_cta)].push_back(
-        (int)i);
+    classes[std::make_tuple(b.precision[i], b.mode[i], t.lanes_per_solve, t.chunk, t.warps_per_cta,
+                            b.params[i].isolir)].push_back((int)i);
   }
   b.groups.assign(classes.size(), BatchGroup{});
   b.group_items.assign(classes.size(), {});
@@ -1252,6 +1252,8 @@ int socgpu_batch_tune(socgpu_batch batch, void *stream, int reps, char *msg, siz
   socgpu_batch_s &b = *batch;
   if (reps < 1) reps = 3;
   cudaStream_t st = (cudaStream_t)stream;
+  // tuning sets: (precision, mode, layers); each set is timed per source
+  // (solar and infra-red run different kernels) and the times summed
   std::map<std::tuple<int, int, int>, std::vector<int>> keys;
   for (size_t i = 0; i < b.params.size(); ++i)
     keys[std::make_tuple(b.precision[i], b.mode[i], b.params[i].n_layer)].push_back((int)i);
@@ -1269,26 +1271,39 @@ int socgpu_batch_tune(socgpu_batch batch, void *stream, int reps, char *msg, siz
       if (!find_variant(prec, mode, lanes) || chunk == 0) continue;
       for (int warps : {4, 8}) {
         TileConfig t{lanes, warps, chunk};
-        std::vector<BatchGroup> one(1);
-        std::vector<FluxParams> items;
-        std::vector<long long> start;
-        char sub[256] = "";
-        if (make_group(b, kv.second, prec, mode, t, one[0], items, start, sub, sizeof(sub)) != SOCGPU_I_NORMAL)
-          continue;   // this tile does not fit (shared memory): not a candidate
+        // one group per source
+        std::vector<std::vector<int>> by_src(2);
+        for (int i : kv.second) by_src[b.params[i].isolir == SOCGPU_IP_SOLAR ? 0 : 1].push_back(i);
+        std::vector<BatchGroup> groups;
+        std::vector<std::vector<FluxParams>> items;
+        std::vector<std::vector<long long>> starts;
+        groups.reserve(2); items.reserve(2); starts.reserve(2);
+        bool fits = true;
+        for (auto &idx : by_src) {
+          if (idx.empty()) continue;
+          groups.emplace_back(); items.emplace_back(); starts.emplace_back();
+          char sub[256] = "";
+          if (make_group(b, idx, prec, mode, t, groups.back(), items.back(), starts.back(), sub, sizeof(sub)) !=
+              SOCGPU_I_NORMAL)
+            fits = false;
+        }
+        if (!fits) continue;   // this tile does not fit (shared memory): not a candidate
         char *tbuf = nullptr;
         std::vector<FluxParams *> di;
         std::vector<long long *> ds;
-        if (upload_groups(one, tbuf, di, ds, sub, sizeof(sub)) != SOCGPU_I_NORMAL) {
+        char sub[256] = "";
+        if (upload_groups(groups, tbuf, di, ds, sub, sizeof(sub)) != SOCGPU_I_NORMAL) {
           if (tbuf) cudaFree(tbuf);
           status = SOCGPU_I_ABORT_CALCULATION;
           set_msg(msg, msg_len, "tuning upload failed: %s", sub);
           break;
         }
         float ms = 1e30f;
-        int bad = launch_group(one[0], di[0], ds[0], st);    // warm-up
+        int bad = 0;
+        for (size_t q = 0; q < groups.size(); ++q) bad |= launch_group(groups[q], di[q], ds[q], st);   // warm-up
         for (int r = 0; r < reps && !bad; ++r) {
           cudaEventRecord(e0, st);
-          bad |= launch_group(one[0], di[0], ds[0], st);
+          for (size_t q = 0; q < groups.size(); ++q) bad |= launch_group(groups[q], di[q], ds[q], st);
           cudaEventRecord(e1, st);
           if (cudaEventSynchronize(e1) != cudaSuccess) { bad = 1; break; }
           float m = 0.f;

@@ -260,7 +260,11 @@ __device__ __forceinline__ float planck_diff_mix(const float *c, int n_deg, floa
 }
 
 // ---------------------------------------------------------------------------
-template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA>
+// SRC: the source of the radiation, SOCGPU_IP_SOLAR or SOCGPU_IP_INFRA_RED,
+// fixed at compile time so that each kernel carries only its own paths (the
+// solar kernel without the Planck terms and the IR coefficients, and the
+// reverse): a smaller body keeps the hot loop in the instruction cache.
+template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA, int SRC>
 struct FluxKernel {
   using Acc = R;
   static constexpr bool kFP64 = (sizeof(R) == 8);
@@ -294,7 +298,7 @@ struct FluxKernel {
         om = om * (1.0 - fwd) / (1.0 - om * fwd);
       }
       Coef c = NOSCAT ? fast_lw_ref(p.l_ir_source_quad, tau)
-                      : two_coeff_ref(p.isolir, p.i_2stream, p.l_ir_source_quad, asym, om, tau, sec0);
+                      : two_coeff_ref(SRC, p.i_2stream, p.l_ir_source_quad, asym, om, tau, sec0);
       T = c.T; Rf = c.R; T0 = c.T0; c1 = c.c1; c2 = c.c2; omtr = R(0);
     } else {
       float tau, om, omc;
@@ -320,7 +324,7 @@ struct FluxKernel {
         omc = omc * inv;                            // 1 - omega' = (1-omega)/(1-omega f)
       }
       CoefF c = NOSCAT ? fast_lw_mix(p.l_ir_source_quad, tau)
-                       : two_coeff_mix(p.isolir, p.i_2stream, p.l_ir_source_quad, asym, om, omc, tau, sec0);
+                       : two_coeff_mix(SRC, p.i_2stream, p.l_ir_source_quad, asym, om, omc, tau, sec0);
       T = c.T; Rf = c.R; T0 = c.T0; c1 = c.c1; c2 = c.c2; omtr = c.omtr;
     }
   }
@@ -353,7 +357,7 @@ struct FluxKernel {
     const int nbat = p.band_batch;             // bands staged at a time
     const int nthreads = blockDim.x;
     const int n_groups = nthreads / P;
-    const bool lw = (p.isolir == SOCGPU_IP_INFRA_RED);
+    constexpr bool lw = (SRC == SOCGPU_IP_INFRA_RED);
     const int max_abs = p.max_abs;
     const SmemLayout lay = make_layout<R>(LP, P, nbat, max_abs, MCICA ? p.n_condensed : 0,
                                          MCICA ? p.n_subcol_gen : 0, n_groups, lw, MCICA);
@@ -1085,9 +1089,9 @@ struct FluxKernel {
 // also allows; the McICA kernels would spill at 64 registers.
 constexpr int single_min_ctas(int ch, bool mcica) { return (ch <= 4 && !mcica) ? 4 : 1; }
 
-template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA>
+template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA, int SRC>
 __global__ void __launch_bounds__(256, single_min_ctas(CH, MCICA)) flux_kernel(const __grid_constant__ FluxParams p) {
-  FluxKernel<R, MIX, P, CH, NOSCAT, MCICA>::run(p, blockIdx.x);
+  FluxKernel<R, MIX, P, CH, NOSCAT, MCICA, SRC>::run(p, blockIdx.x);
 }
 
 // Persistent form over many column batches: items[i] describes one batch
@@ -1102,7 +1106,7 @@ __global__ void __launch_bounds__(256, single_min_ctas(CH, MCICA)) flux_kernel(c
 // lane).
 constexpr int batched_min_ctas(int ch) { return ch <= 4 ? 3 : (ch <= 9 ? 2 : 1); }
 
-template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA>
+template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA, int SRC>
 __global__ void __launch_bounds__(256, batched_min_ctas(CH))
 flux_kernel_batched(const FluxParams *__restrict__ items, const long long *__restrict__ col_start, int n_items,
                     long long total) {
@@ -1128,7 +1132,7 @@ flux_kernel_batched(const FluxParams *__restrict__ items, const long long *__res
       cur = it;
     }
     __syncthreads();
-    FluxKernel<R, MIX, P, CH, NOSCAT, MCICA>::run(sp, (int)(w - col_start[it]));
+    FluxKernel<R, MIX, P, CH, NOSCAT, MCICA, SRC>::run(sp, (int)(w - col_start[it]));
     __syncthreads();
   }
 }

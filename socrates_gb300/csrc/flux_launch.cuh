@@ -11,7 +11,7 @@ namespace socgpu {
 template <int P_, int CH_>
 struct Shape { static constexpr int P = P_, CH = CH_; };
 
-template <class R, bool MIX, bool NOSCAT, bool MCICA, class S>
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int SRC, class S>
 int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len,
                bool &done) {
   if (done || cfg.lanes_per_solve != S::P || S::P * S::CH < p.n_layer) return 0;
@@ -39,7 +39,7 @@ int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char
   const int threads = warps * 32;
   FluxParams q = p;
   q.band_batch = batch;
-  auto kern = flux_kernel<R, MIX, S::P, S::CH, NOSCAT, MCICA>;
+  auto kern = flux_kernel<R, MIX, S::P, S::CH, NOSCAT, MCICA, SRC>;
   if (lay.bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.bytes);
     if (e != cudaSuccess) {
@@ -62,7 +62,7 @@ int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char
 // Prepare one kernel class of a multi-batch launch for shape S: the band
 // batch of every item so that all fit one shared-memory size, the kernel
 // attribute, and a persistent grid of the resident CTAs of every SM.
-template <class R, bool MIX, bool NOSCAT, bool MCICA, class S>
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int SRC, class S>
 int try_prepare(BatchGroup &g, char *msg, size_t len, bool &done) {
   if (done || g.tile.lanes_per_solve != S::P || g.tile.chunk != S::CH) return 0;
   done = true;
@@ -76,7 +76,7 @@ int try_prepare(BatchGroup &g, char *msg, size_t len, bool &done) {
     return make_layout<R>(S::P * S::CH, S::P, batch, p.max_abs, MCICA ? p.n_condensed : 0,
                           MCICA ? p.n_subcol_gen : 0, n_groups, p.isolir == SOCGPU_IP_INFRA_RED, MCICA).bytes;
   };
-  auto kern = flux_kernel_batched<R, MIX, S::P, S::CH, NOSCAT, MCICA>;
+  auto kern = flux_kernel_batched<R, MIX, S::P, S::CH, NOSCAT, MCICA, SRC>;
   // the kernel's static shared memory (its parameter copy) counts against
   // the same per-CTA limit
   cudaFuncAttributes fa{};
@@ -132,11 +132,11 @@ int try_prepare(BatchGroup &g, char *msg, size_t len, bool &done) {
   return 0;
 }
 
-template <class R, bool MIX, bool NOSCAT, bool MCICA, class... Shapes>
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int SRC, class... Shapes>
 int prepare_shapes(BatchGroup &g, char *msg, size_t len) {
   bool done = false;
   int status = 0;
-  ((status = status ? status : try_prepare<R, MIX, NOSCAT, MCICA, Shapes>(g, msg, len, done)), ...);
+  ((status = status ? status : try_prepare<R, MIX, NOSCAT, MCICA, SRC, Shapes>(g, msg, len, done)), ...);
   if (!done && status == 0) {
     snprintf(msg, len, "no kernel instantiated for %d lanes per solve and %d layers per lane",
              g.tile.lanes_per_solve, g.tile.chunk);
@@ -145,11 +145,11 @@ int prepare_shapes(BatchGroup &g, char *msg, size_t len) {
   return status;
 }
 
-template <class R, bool MIX, bool NOSCAT, bool MCICA, class... Shapes>
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int SRC, class... Shapes>
 int launch_shapes(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len) {
   bool done = false;
   int status = 0;
-  ((status = status ? status : try_launch<R, MIX, NOSCAT, MCICA, Shapes>(p, cfg, st, msg, len, done)), ...);
+  ((status = status ? status : try_launch<R, MIX, NOSCAT, MCICA, SRC, Shapes>(p, cfg, st, msg, len, done)), ...);
   if (!done && status == 0) {
     snprintf(msg, len, "no kernel instantiated for %d lanes per solve and %d layers", cfg.lanes_per_solve,
              p.n_layer);
@@ -159,14 +159,34 @@ int launch_shapes(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, c
 }
 
 
+// The source (solar or infra-red) picks the kernel at run time; the
+// no-scatter family is infra-red only.
 template <class R, bool MIX, bool NOSCAT, bool MCICA, int P, int... CH>
 int launch_chunks(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len) {
-  return launch_shapes<R, MIX, NOSCAT, MCICA, Shape<P, CH>...>(p, cfg, st, msg, len);
+  if constexpr (NOSCAT) {
+    return launch_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_INFRA_RED, Shape<P, CH>...>(p, cfg, st, msg, len);
+  } else {
+    if (p.isolir == SOCGPU_IP_INFRA_RED)
+      return launch_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_INFRA_RED, Shape<P, CH>...>(p, cfg, st, msg, len);
+    return launch_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_SOLAR, Shape<P, CH>...>(p, cfg, st, msg, len);
+  }
 }
 
 template <class R, bool MIX, bool NOSCAT, bool MCICA, int P, int... CH>
 int prepare_chunks(BatchGroup &g, char *msg, size_t len) {
-  return prepare_shapes<R, MIX, NOSCAT, MCICA, Shape<P, CH>...>(g, msg, len);
+  const int src = g.n_items > 0 ? g.items[0].isolir : SOCGPU_IP_INFRA_RED;
+  for (int i = 0; i < g.n_items; ++i)
+    if (g.items[i].isolir != src) {
+      snprintf(msg, len, "a kernel class mixes solar and infra-red batches");
+      return SOCGPU_I_ERR_FATAL;
+    }
+  if constexpr (NOSCAT) {
+    return prepare_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_INFRA_RED, Shape<P, CH>...>(g, msg, len);
+  } else {
+    if (src == SOCGPU_IP_INFRA_RED)
+      return prepare_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_INFRA_RED, Shape<P, CH>...>(g, msg, len);
+    return prepare_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_SOLAR, Shape<P, CH>...>(g, msg, len);
+  }
 }
 
 }  // namespace socgpu

@@ -212,15 +212,15 @@ void launch_wave(socgpu_server_s &S, StreamSlot &sl) {
       return;
     }
   // kernel classes of the wave
-  std::map<std::tuple<int, int, int, int, int>, std::vector<int>> classes;
+  std::map<std::tuple<int, int, int, int, int, int>, std::vector<int>> classes;
   std::vector<FluxParams> params(wave.size());
   for (size_t i = 0; i < wave.size(); ++i) {
     Request *r = wave[i];
     r->call.params(S.dmem + r->off, params[i]);
     const int mode = mode_index(&r->control);
     TileConfig t = choose_tile(r->control.precision, mode, r->atm.n_layer);
-    classes[std::make_tuple(r->control.precision, mode, t.lanes_per_solve, t.chunk, t.warps_per_cta)].push_back(
-        (int)i);
+    classes[std::make_tuple(r->control.precision, mode, t.lanes_per_solve, t.chunk, t.warps_per_cta,
+                            r->control.isolir)].push_back((int)i);
   }
   size_t n_item = 0, n_start = 0;
   std::vector<BatchGroup> groups;
