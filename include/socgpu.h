@@ -36,7 +36,7 @@ extern "C" {
 #define SOCGPU_API
 #endif
 
-#define SOCGPU_ABI_VERSION 2
+#define SOCGPU_ABI_VERSION 3
 
 /* ---- status codes: rad_pcf.F90:391-405 ------------------------------- */
 #define SOCGPU_I_NORMAL             0
@@ -91,6 +91,9 @@ extern "C" {
 #define SOCGPU_IP_ICE_PADE_2_PHF       20
 /* gas overlap, rad_pcf.F90:427 */
 #define SOCGPU_IP_OVERLAP_RANDOM        2
+#define SOCGPU_IP_OVERLAP_K_EQV_SCL     4   /* rad_pcf.F90:432: equivalent extinction of minor gases */
+#define SOCGPU_IP_OVERLAP_K_EQV         5   /* rad_pcf.F90:434: solved as K_EQV_SCL */
+#define SOCGPU_IP_OVERLAP_K_EQV_MOD     6   /* rad_pcf.F90:436: solved as K_EQV_SCL */
 /* k scaling, rad_pcf.F90:412-416 and 509-515 */
 #define SOCGPU_IP_SCALE_NULL            0
 #define SOCGPU_IP_SCALE_BAND            1
@@ -99,8 +102,9 @@ extern "C" {
 #define SOCGPU_IP_SCALE_POWER_LAW       1
 #define SOCGPU_IP_SCALE_POWER_QUAD      2
 #define SOCGPU_IP_SCALE_DOPPLER_QUAD    3
-#define SOCGPU_IP_SCALE_LOOKUP          9   /* not supported: rejected when read */
-#define SOCGPU_IP_SCALE_T_LOOKUP       10   /* not supported: rejected when read */
+#define SOCGPU_IP_SCALE_WENYI           4   /* CO2 tables of bands 4 and 6 (scale_absorb.F90:238-281) */
+#define SOCGPU_IP_SCALE_LOOKUP          9   /* P/T (and gas-fraction) tables of the '_k' file */
+#define SOCGPU_IP_SCALE_T_LOOKUP       10   /* temperature tables of the '_k' file */
 /* Rayleigh schemes, rad_pcf.F90:729-731 */
 #define SOCGPU_IP_RAYLEIGH_TOTAL        1
 /* Continuum types (rad_pcf.F90 ip_self_continuum, ip_frn_continuum) */
@@ -186,6 +190,32 @@ typedef struct socgpu_spectrum_desc {
     const double *scale_cont;           /* (nd_scale_variable, nd_band, nd_continuum) */
     const double *p_ref_cont;           /* (nd_continuum, nd_band) [Pa] */
     const double *t_ref_cont;           /* (nd_continuum, nd_band) [K] */
+    /* Lookup-table k scaling, read from the '_k' companion file of block 5
+       (read_spectrum.F90:1340-1560; inter_pt_lookup.F90, inter_t_lookup.F90).
+       Absorbers with i_scale_fnc SOCGPU_IP_SCALE_LOOKUP take their k from
+       k_lookup (or k_lookup_sb when self-broadened), not from k. */
+    int n_pre, n_tmp;                   /* P/T table extents (0: no P/T tables) */
+    const double *p_lookup;             /* (n_pre) ln(p / Pa), increasing */
+    const double *t_lookup;             /* (n_tmp, n_pre) [K], increasing along n_tmp */
+    const double *k_lookup;             /* (n_tmp, n_pre, nd_k_term, nd_species, nd_band) [m2/kg] */
+    const int    *index_sb;             /* (nd_species) 1-based self-broadened index, 0: none; or NULL */
+    int nd_species_sb, n_gas_frac;      /* self-broadened absorbers, gas-fraction table extent */
+    const double *gf_lookup;            /* (n_gas_frac) gas fractions, increasing */
+    const double *k_lookup_sb;          /* (n_tmp, n_pre, n_gas_frac, nd_k_term, nd_species_sb, nd_band) */
+    const double *molar_weight;         /* (nd_species) [g/mol] of each absorber, for self-broadening */
+    int nd_t_lookup_gas;                /* temperature-only tables (SOCGPU_IP_SCALE_T_LOOKUP) */
+    const int    *n_t_lookup_gas;       /* (nd_species) */
+    const double *t_lookup_gas;         /* (nd_t_lookup_gas, nd_species) [K], increasing */
+    const double *k_t_lookup_gas;       /* (nd_t_lookup_gas, nd_k_term, nd_species, nd_band) [m2/kg] */
+    /* Wen-Yi Zhong's CO2 tables for SOCGPU_IP_SCALE_WENYI (module scale_wenyi);
+       the reference compiles them in, here the caller supplies them. */
+    int wenyi_n_term4, wenyi_n_term6;   /* third extents of wenyi_gk4 / wenyi_gk6 (0: absent) */
+    const double *wenyi_plg;            /* (26) ln(p / 100 Pa) grid */
+    const double *wenyi_ttb;            /* (10) temperatures of the band-4 table [K] */
+    const double *wenyi_tto;            /* (9) temperatures of the band-6 table [K] */
+    const double *wenyi_gk250b;         /* (wenyi_n_term4) band-4 normalisation at 250 K */
+    const double *wenyi_gk4;            /* (10, 26, wenyi_n_term4) */
+    const double *wenyi_gk6;            /* (9, 26, wenyi_n_term6) */
 } socgpu_spectrum_desc;
 
 typedef int32_t socgpu_spectrum_handle;   /* > 0 when valid */
@@ -199,7 +229,7 @@ typedef struct socgpu_control {
     int i_solver;               /* SOCGPU_IP_SOLVER_NO_SCAT | SOLVER_HOMOGEN_DIRECT */
     int i_cloud;                /* SOCGPU_IP_CLOUD_CLEAR | SOCGPU_IP_CLOUD_MCICA */
     int i_cloud_representation; /* SOCGPU_IP_CLOUD_ICE_WATER with McICA */
-    int i_gas_overlap;          /* SOCGPU_IP_OVERLAP_RANDOM */
+    int i_gas_overlap;          /* SOCGPU_IP_OVERLAP_RANDOM | K_EQV_SCL (K_EQV, K_EQV_MOD alike) */
     int i_direct_tau;           /* SOCGPU_IP_DIRECT_DELTA_SCALING (default) | NOSCALING */
     int l_rescale;              /* delta-rescaling of tau, omega and the phase function */
     int n_order_forward;        /* order of the forward-scattering term (2: f = g^2) */
@@ -214,6 +244,7 @@ typedef struct socgpu_control {
     int precision;              /* SOCGPU_PRECISION_* (extension) */
     int l_continuum;            /* water-vapour continuum absorption (blocks 8 and 9) */
     int l_mixing_ratio;         /* gas amounts per unit mass of dry air (foreign continuum) */
+    int l_grey_single;          /* k_eqv_scl, infra-red: single-term minor gases as grey absorbers */
 } socgpu_control;
 
 /* ---- StrDim subset (src/radiance_core/def_dimen.F90) ----------------- */

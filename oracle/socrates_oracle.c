@@ -86,14 +86,47 @@ static const double *sp_scale(const socgpu_spectrum_desc *d, int k, int b, int g
 }
 
 /* --------------------------------------------------------------------- */
-/* scale_absorb (scale_absorb.F90:110-224): pressure/temperature scaling
+/* scale_absorb (scale_absorb.F90:110-281): pressure/temperature scaling
  * factor of one absorber for all cells of the segment.                  */
 static int scale_absorb(int n_profile, int n_layer, int ndp_in, int ndp_w,
                         const double *p, const double *t, double *gfr,
                         int i_fnc, double p_reference, double t_reference,
-                        const double *sp, int l_doppler, double doppler_correction)
+                        const double *sp, int l_doppler, double doppler_correction,
+                        const socgpu_spectrum_desc *d, int iex, int i_band)
 {
     double pressure_offset = l_doppler ? doppler_correction : 0.0;
+    if (i_fnc == SOCGPU_IP_SCALE_WENYI) {
+        /* scale_absorb.F90:238-281: bilinear interpolation in ln(p/100 Pa)
+         * and T of the CO2 (band 4) or O3 (band 6) tables; iex is the
+         * 0-based k-term, i_band the 1-based band */
+        if (!d->wenyi_plg) return SOCGPU_I_ERR_FATAL;
+        int n_t, t_shift, nterm;
+        const double *gk, *tt;
+        if (i_band == 4) { n_t = 10; t_shift = 7; gk = d->wenyi_gk4; tt = d->wenyi_ttb; nterm = d->wenyi_n_term4; }
+        else if (i_band == 6) { n_t = 9; t_shift = 5; gk = d->wenyi_gk6; tt = d->wenyi_tto; nterm = d->wenyi_n_term6; }
+        else return SOCGPU_I_ERR_FATAL;
+        if (!gk || !tt || iex >= nterm || (i_band == 4 && !d->wenyi_gk250b)) return SOCGPU_I_ERR_FATAL;
+#define GK(a, b) gk[(size_t)((a) - 1) + (size_t)n_t * ((size_t)((b) - 1) + 26u * (size_t)iex)]
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                double pl = IX2(p, l, i, ndp_in), tl = IX2(t, l, i, ndp_in);
+                double cgp = log(pl / 100.0);
+                if (cgp < -5.5) cgp = -5.5;
+                int jp = (int)((5.5 + cgp) * 2.0) + 1;
+                jp = jp < 1 ? 1 : (jp > 26 ? 26 : jp);
+                int jp1 = jp + 1 < 26 ? jp + 1 : 26;
+                int jt = (int)((tl - 240.0) / 20.0 + (double)t_shift);
+                jt = jt < 1 ? 1 : (jt > n_t ? n_t : jt);
+                int jt1 = jt + 1 < n_t ? jt + 1 : n_t;
+                double dp = (cgp - d->wenyi_plg[jp - 1]) * 2.0;
+                double gkpb = GK(jt, jp) + (GK(jt, jp1) - GK(jt, jp)) * dp;
+                double gkpc = GK(jt1, jp) + (GK(jt1, jp1) - GK(jt1, jp)) * dp;
+                double v = gkpb + (gkpc - gkpb) * (tl - tt[jt - 1]) / 20.0;
+                IX2(gfr, l, i, ndp_w) = (i_band == 4) ? v / d->wenyi_gk250b[iex] : v;
+            }
+#undef GK
+        return SOCGPU_I_NORMAL;
+    }
     if (i_fnc == SOCGPU_IP_SCALE_POWER_LAW) {
         /* scale_absorb.F90:122-137: ((p+off)/(pref+off))**sp1 * (t/tref)**sp2 */
         double t_inv = 1.0 / t_reference;
@@ -286,6 +319,7 @@ typedef struct {
     double *ty_tau[3], *ty_tau_dir[3], *ty_omega[3], *ty_asym[3];      /* cloud types 1..2 */
     double *ty_valid[3];
     int *slot;
+    const double *adj;          /* adjust_solar_ke of k_eqv_scl (solar), or NULL */
 } work;
 
 static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
@@ -370,17 +404,30 @@ static void column_solve(work *w, const socgpu_control *c, int no_scat)
             IX2(fd, l, 0, wp) = w->flux_inc_direct[l];
             if (l_dir) IX2(w->flux_direct_dir, l, 0, wp) = w->flux_inc_direct[l];
         }
-        for (int i = 1; i <= n_layer; ++i)
-            for (int l = 0; l < n_profile; ++l) {
-                IX2(fd, l, i, wp) = IX2(fd, l, i - 1, wp) * IX2(w->trans_0, l, i - 1, wp);
-                IX2(w->s_up, l, i - 1, wp) = IX2(w->sc1, l, i - 1, wp) * IX2(fd, l, i - 1, wp);
-                IX2(w->s_down, l, i - 1, wp) = IX2(w->sc2, l, i - 1, wp) * IX2(fd, l, i - 1, wp);
-            }
+        if (w->adj) {
+            /* l_scale_solar (solar_source.F90:115-130) */
+            for (int i = 1; i <= n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l) {
+                    IX2(fd, l, i, wp) = IX2(fd, l, i - 1, wp) * IX2(w->trans_0, l, i - 1, wp) * IX2(w->adj, l, i - 1, wp);
+                    IX2(w->s_up, l, i - 1, wp) = IX2(w->sc1, l, i - 1, wp) * IX2(fd, l, i - 1, wp);
+                    IX2(w->s_down, l, i - 1, wp) = (IX2(w->sc2, l, i - 1, wp) - IX2(w->trans_0, l, i - 1, wp))
+                        * IX2(fd, l, i - 1, wp) + IX2(fd, l, i, wp);
+                }
+        } else {
+            for (int i = 1; i <= n_layer; ++i)
+                for (int l = 0; l < n_profile; ++l) {
+                    IX2(fd, l, i, wp) = IX2(fd, l, i - 1, wp) * IX2(w->trans_0, l, i - 1, wp);
+                    IX2(w->s_up, l, i - 1, wp) = IX2(w->sc1, l, i - 1, wp) * IX2(fd, l, i - 1, wp);
+                    IX2(w->s_down, l, i - 1, wp) = IX2(w->sc2, l, i - 1, wp) * IX2(fd, l, i - 1, wp);
+                }
+        }
         if (l_dir) {
             for (int i = 1; i <= n_layer; ++i)
-                for (int l = 0; l < n_profile; ++l)
+                for (int l = 0; l < n_profile; ++l) {
                     IX2(w->flux_direct_dir, l, i, wp) =
                         IX2(w->flux_direct_dir, l, i - 1, wp) * IX2(w->trans_0_dir, l, i - 1, wp);
+                    if (w->adj) IX2(w->flux_direct_dir, l, i, wp) = IX2(w->flux_direct_dir, l, i, wp) * IX2(w->adj, l, i - 1, wp);
+                }
             for (int i = 0; i <= n_layer; ++i)
                 for (int l = 0; l < n_profile; ++l)
                     IX2(fd, l, i, wp) = IX2(w->flux_direct_dir, l, i, wp);
@@ -791,6 +838,364 @@ static void solve_mcica_term(work *w, const socgpu_control *c, const socgpu_dime
 }
 
 /* --------------------------------------------------------------------- */
+/* Lookup-table k scaling.  Interpolation factors of every cell of the
+ * segment: inter_pt_lookup.F90:146-268 (pressure, temperature and gas
+ * fraction) and inter_t_lookup.F90:70-86 (temperature only).  Indices are
+ * stored 0-based. */
+typedef struct {
+    double *fac00, *fac01, *fac10, *fac11;   /* (wp, ndl) */
+    int *jp, *jt, *jtt;                       /* (wp, ndl) */
+    double *fgf; int *jgf, *jgfp1;            /* (wp, ndl, nd_species_sb) */
+    double *wt_gas; int *jt_gas;              /* (wp, ndl, nd_species) */
+} lookup_fac;
+
+/* MINLOC(x - tab(1:n), MASK = x - tab >= 0): the first index of the smallest
+ * non-negative difference, 0-based (0 when none qualifies; the clamps before
+ * every call keep x inside the table). */
+static int minloc_below(double x, const double *tab, int n)
+{
+    int best = -1;
+    double dmin = 0.0;
+    for (int k = 0; k < n; ++k) {
+        double dd = x - tab[k];
+        if (dd >= 0.0 && (best < 0 || dd < dmin)) { best = k; dmin = dd; }
+    }
+    return best < 0 ? 0 : best;
+}
+
+static void lookup_fac_free(lookup_fac *f)
+{
+    free(f->fac00); free(f->fac01); free(f->fac10); free(f->fac11);
+    free(f->jp); free(f->jt); free(f->jtt);
+    free(f->fgf); free(f->jgf); free(f->jgfp1); free(f->wt_gas); free(f->jt_gas);
+    memset(f, 0, sizeof(*f));
+}
+
+static void lookup_fac_init(lookup_fac *f, const socgpu_control *c, const socgpu_spectrum_desc *d,
+                            const socgpu_atm *atm, int np, int n_layer, int ndp, int wp, int ndl)
+{
+    memset(f, 0, sizeof(*f));
+    int any_pt = 0, any_t = 0;
+    for (int b = c->first_band - 1; b < c->last_band; ++b)
+        for (int j = 0; j < d->n_band_absorb[b]; ++j) {
+            int fnc = sp_bg(d->i_scale_fnc, d, b, sp_index_absorb(d, j, b));
+            any_pt |= (fnc == SOCGPU_IP_SCALE_LOOKUP);
+            any_t |= (fnc == SOCGPU_IP_SCALE_T_LOOKUP);
+        }
+    size_t pl = (size_t)wp * ndl;
+    const double eps = EPS_R;
+    if (any_pt && d->n_pre > 1 && d->n_tmp > 1 && d->p_lookup && d->t_lookup) {
+        int npre = d->n_pre, ntmp = d->n_tmp;
+        f->fac00 = zalloc(pl); f->fac01 = zalloc(pl); f->fac10 = zalloc(pl); f->fac11 = zalloc(pl);
+        f->jp = (int *)calloc(pl, sizeof(int)); f->jt = (int *)calloc(pl, sizeof(int));
+        f->jtt = (int *)calloc(pl, sizeof(int));
+        double p_min = d->p_lookup[0] + fmax(fabs(d->p_lookup[0]) * eps, eps);
+        double p_max = d->p_lookup[npre - 1] - fmax(fabs(d->p_lookup[npre - 1]) * eps, eps);
+#define TL(it, ip) d->t_lookup[(size_t)(it) + (size_t)ntmp * (size_t)(ip)]
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < np; ++l) {
+                double p_layer = fmin(fmax(log(IX2(atm->p, l, i, ndp)), p_min), p_max);
+                int jp = minloc_below(p_layer, d->p_lookup, npre);
+                double fp = (p_layer - d->p_lookup[jp]) / (d->p_lookup[jp + 1] - d->p_lookup[jp]);
+                double t = IX2(atm->t, l, i, ndp);
+                double t_layer = fmin(fmax(t, TL(0, jp) * (1.0 + eps)), TL(ntmp - 1, jp) * (1.0 - eps));
+                int jt = minloc_below(t_layer, &TL(0, jp), ntmp);
+                double ft = (t_layer - TL(jt, jp)) / (TL(jt + 1, jp) - TL(jt, jp));
+                t_layer = fmin(fmax(t, TL(0, jp + 1) * (1.0 + eps)), TL(ntmp - 1, jp + 1) * (1.0 - eps));
+                int jtt = minloc_below(t_layer, &TL(0, jp + 1), ntmp);
+                double ftt = (t_layer - TL(jtt, jp + 1)) / (TL(jtt + 1, jp + 1) - TL(jtt, jp + 1));
+                double compfp = 1.0 - fp;
+                IX2(f->fac00, l, i, wp) = compfp * (1.0 - ft);
+                IX2(f->fac10, l, i, wp) = fp * (1.0 - ftt);
+                IX2(f->fac01, l, i, wp) = compfp * ft;
+                IX2(f->fac11, l, i, wp) = fp * ftt;
+                IX2(f->jp, l, i, wp) = jp; IX2(f->jt, l, i, wp) = jt; IX2(f->jtt, l, i, wp) = jtt;
+            }
+#undef TL
+        /* gas fractions of the self-broadened absorbers (inter_pt_lookup.F90:198-266) */
+        int nsb = d->nd_species_sb;
+        if (d->index_sb && nsb > 0 && d->n_gas_frac >= 1 && d->gf_lookup) {
+            int ngf = d->n_gas_frac;
+            f->fgf = zalloc(pl * nsb);
+            f->jgf = (int *)calloc(pl * nsb, sizeof(int));
+            f->jgfp1 = (int *)calloc(pl * nsb, sizeof(int));
+            double gf_min = d->gf_lookup[0] + fmax(d->gf_lookup[0] * eps, eps);
+            double gf_max = d->gf_lookup[ngf - 1] - fmax(d->gf_lookup[ngf - 1] * eps, eps);
+            int iw = d->index_water - 1;
+            if (iw < 0) iw = 0;   /* i_pointer_water = MAX(index_water, 1) */
+            int l_water = 0;
+            double mw_w = 18.0153;
+            for (int g = 0; g < d->n_absorb; ++g)
+                if (d->type_absorb[g] == 1) {
+                    l_water = 1;
+                    if (d->molar_weight) mw_w = d->molar_weight[g];
+                }
+            for (int g = 0; g < d->n_absorb; ++g) {
+                int jsb = d->index_sb[g] - 1;
+                if (jsb < 0 || jsb >= nsb) continue;
+                double mw_g = d->molar_weight ? d->molar_weight[g] : 0.0;
+                double ratio_gas = MOL_WEIGHT_AIR / (mw_g * 1.0e-03);
+                double ratio_water = MOL_WEIGHT_AIR / (mw_w * 1.0e-03);
+                for (int i = 0; i < n_layer; ++i)
+                    for (int l = 0; l < np; ++l) {
+                        double mr = IX3(atm->gas_mix_ratio, l, i, g, ndp, ndl);
+                        double gf;
+                        if (l_water) {
+                            double q = IX3(atm->gas_mix_ratio, l, i, iw, ndp, ndl);
+                            gf = c->l_mixing_ratio ? mr * ratio_gas / (1.0 + q * ratio_water)
+                                                   : mr * ratio_gas / (1.0 + q * (ratio_water - 1.0));
+                        } else {
+                            gf = mr * ratio_gas;
+                        }
+                        size_t q3 = (size_t)l + (size_t)wp * ((size_t)i + (size_t)ndl * jsb);
+                        if (ngf == 1) {
+                            f->jgf[q3] = 0; f->jgfp1[q3] = 0; f->fgf[q3] = 1.0;
+                        } else {
+                            double gl = fmin(fmax(gf, gf_min), gf_max);
+                            int jg = minloc_below(gl, d->gf_lookup, ngf);
+                            f->jgf[q3] = jg; f->jgfp1[q3] = jg + 1;
+                            f->fgf[q3] = 1.0 - (gl - d->gf_lookup[jg]) / (d->gf_lookup[jg + 1] - d->gf_lookup[jg]);
+                        }
+                    }
+            }
+        }
+    }
+    if (any_t && d->n_t_lookup_gas && d->t_lookup_gas && d->nd_t_lookup_gas > 1) {
+        int nsp = d->nd_species;
+        f->wt_gas = zalloc(pl * nsp);
+        f->jt_gas = (int *)calloc(pl * nsp, sizeof(int));
+        for (int g = 0; g < d->n_absorb; ++g) {
+            int n = d->n_t_lookup_gas[g];
+            if (n < 2) continue;
+            const double *tc = d->t_lookup_gas + (size_t)d->nd_t_lookup_gas * g;
+            for (int i = 0; i < n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    double t_layer = fmin(fmax(IX2(atm->t, l, i, ndp), tc[0] * (1.0 + eps)), tc[n - 1] * (1.0 - eps));
+                    int jt = minloc_below(t_layer, tc, n);
+                    size_t q3 = (size_t)l + (size_t)wp * ((size_t)i + (size_t)ndl * g);
+                    f->jt_gas[q3] = jt;
+                    f->wt_gas[q3] = 1.0 - (t_layer - tc[jt]) / (tc[jt + 1] - tc[jt]);
+                }
+        }
+    }
+}
+
+/* k_abs_layer(:, :, iex, j) of radiance_calc.F90:1330-1470 for absorber j
+ * (species g) of band b: band-scaled amounts from gfr (ip_scale_band: the
+ * scaled amount; ip_scale_null: the mixing ratio), per-term scaling through
+ * scale_absorb, or the lookup tables (k_esft_layer of
+ * radiance_calc.F90:1097-1170; k of block 5 is then unused).  tmp is a (wp,
+ * ndl) scratch array. */
+static int absorber_term_k(const lookup_fac *lf, const socgpu_spectrum_desc *d, const socgpu_atm *atm,
+                           int np, int n_layer, int ndp, int wp, int ndl,
+                           int b, int g, int iex, const double *gfr, double *tmp, double *kout)
+{
+    int isk = sp_bg(d->i_scale_k, d, b, g), fnc = sp_bg(d->i_scale_fnc, d, b, g);
+    double kval = sp_kw(d->k, d, iex, b, g);
+    if (isk != SOCGPU_IP_SCALE_TERM) {
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < np; ++l) IX2(kout, l, i, wp) = kval * IX2(gfr, l, i, wp);
+        return SOCGPU_I_NORMAL;
+    }
+    if (fnc == SOCGPU_IP_SCALE_LOOKUP) {
+        if (!lf->fac00) return SOCGPU_I_ERR_FATAL;
+        int ntmp = d->n_tmp, npre = d->n_pre;
+        int jsb = (d->index_sb && lf->fgf) ? d->index_sb[g] - 1 : -1;
+        if (jsb < 0) {
+            if (!d->k_lookup) return SOCGPU_I_ERR_FATAL;
+            const double *K = d->k_lookup + (size_t)ntmp * npre *
+                ((size_t)iex + (size_t)d->nd_k_term * ((size_t)g + (size_t)d->nd_species * b));
+#define KL(it, ip) K[(size_t)(it) + (size_t)ntmp * (size_t)(ip)]
+            for (int i = 0; i < n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    int jp = IX2(lf->jp, l, i, wp), jt = IX2(lf->jt, l, i, wp), jtt = IX2(lf->jtt, l, i, wp);
+                    double ke = IX2(lf->fac00, l, i, wp) * KL(jt, jp) + IX2(lf->fac10, l, i, wp) * KL(jtt, jp + 1)
+                        + IX2(lf->fac01, l, i, wp) * KL(jt + 1, jp) + IX2(lf->fac11, l, i, wp) * KL(jtt + 1, jp + 1);
+                    ke = ke > 0.0 ? ke : 0.0;
+                    double v = ke * IX3(atm->gas_mix_ratio, l, i, g, ndp, ndl);
+                    IX2(kout, l, i, wp) = v > 0.0 ? v : 0.0;
+                }
+#undef KL
+        } else {
+            if (!d->k_lookup_sb) return SOCGPU_I_ERR_FATAL;
+            int ngf = d->n_gas_frac;
+            const double *K = d->k_lookup_sb + (size_t)ntmp * npre * ngf *
+                ((size_t)iex + (size_t)d->nd_k_term * ((size_t)jsb + (size_t)d->nd_species_sb * b));
+#define KS(it, ip, ig) K[(size_t)(it) + (size_t)ntmp * ((size_t)(ip) + (size_t)npre * (size_t)(ig))]
+            for (int i = 0; i < n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    int jp = IX2(lf->jp, l, i, wp), jt = IX2(lf->jt, l, i, wp), jtt = IX2(lf->jtt, l, i, wp);
+                    size_t q3 = (size_t)l + (size_t)wp * ((size_t)i + (size_t)ndl * jsb);
+                    int g0 = lf->jgf[q3], g1 = lf->jgfp1[q3];
+                    double f00 = IX2(lf->fac00, l, i, wp), f10 = IX2(lf->fac10, l, i, wp);
+                    double f01 = IX2(lf->fac01, l, i, wp), f11 = IX2(lf->fac11, l, i, wp);
+                    double fg = lf->fgf[q3];
+                    double ke = fg * (f00 * KS(jt, jp, g0) + f10 * KS(jtt, jp + 1, g0)
+                                      + f01 * KS(jt + 1, jp, g0) + f11 * KS(jtt + 1, jp + 1, g0))
+                        + (1.0 - fg) * (f00 * KS(jt, jp, g1) + f10 * KS(jtt, jp + 1, g1)
+                                        + f01 * KS(jt + 1, jp, g1) + f11 * KS(jtt + 1, jp + 1, g1));
+                    ke = ke > 0.0 ? ke : 0.0;
+                    double v = ke * IX3(atm->gas_mix_ratio, l, i, g, ndp, ndl);
+                    IX2(kout, l, i, wp) = v > 0.0 ? v : 0.0;
+                }
+#undef KS
+        }
+        return SOCGPU_I_NORMAL;
+    }
+    if (fnc == SOCGPU_IP_SCALE_T_LOOKUP) {
+        if (!lf->wt_gas || !d->k_t_lookup_gas) return SOCGPU_I_ERR_FATAL;
+        const double *K = d->k_t_lookup_gas + (size_t)d->nd_t_lookup_gas *
+            ((size_t)iex + (size_t)d->nd_k_term * ((size_t)g + (size_t)d->nd_species * b));
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < np; ++l) {
+                size_t q3 = (size_t)l + (size_t)wp * ((size_t)i + (size_t)ndl * g);
+                int jt = lf->jt_gas[q3];
+                double wt = lf->wt_gas[q3];
+                double ke = wt * K[jt] + (1.0 - wt) * K[jt + 1];
+                ke = ke > 0.0 ? ke : 0.0;
+                double v = ke * IX3(atm->gas_mix_ratio, l, i, g, ndp, ndl);
+                IX2(kout, l, i, wp) = v > 0.0 ? v : 0.0;
+            }
+        return SOCGPU_I_NORMAL;
+    }
+    int st = scale_absorb(np, n_layer, ndp, wp, atm->p, atm->t, tmp, fnc,
+                          IX2(d->p_ref, g, b, d->nd_species), IX2(d->t_ref, g, b, d->nd_species),
+                          sp_scale(d, iex, b, g), d->l_doppler ? d->l_doppler[g] : 0,
+                          d->doppler_cor ? d->doppler_cor[g] : 0.0, d, iex, b + 1);
+    if (st != SOCGPU_I_NORMAL) return st;
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < np; ++l) {
+            double v = IX2(tmp, l, i, wp) * IX3(atm->gas_mix_ratio, l, i, g, ndp, ndl);
+            IX2(kout, l, i, wp) = kval * (v > 0.0 ? v : 0.0);
+        }
+    return SOCGPU_I_NORMAL;
+}
+
+/* Equivalent extinction of the minor gases (index_abs 2..n_abs) of band b
+ * (solve_band_k_eqv_scl.F90:560-1040, the two-stream, non-spherical
+ * branches).  Solar: each gas's k-terms are weighted by the direct flux
+ * they transmit to the surface, and adjust_solar_ke corrects the direct
+ * beam of the major gas's solve.  Infra-red: the weights are the fluxes
+ * incident on each layer from monochromatic_gas_flux.F90:100-197 (no
+ * scattering, diffusivity 1.66).  k_eqv + k_grey is added to the grey
+ * extinction. */
+static int k_eqv_minor(work *w, const socgpu_control *c, const lookup_fac *lf, const socgpu_spectrum_desc *d,
+                       const socgpu_atm *atm, int np, int n_layer, int ndp, int b, int n_abs, const int *gas_of,
+                       const int *nk, double *k_eqv, double *adj)
+{
+    int wp = w->wp, ndl = w->ndl;
+    size_t pl = (size_t)wp * ndl, pl2 = (size_t)wp * (2 * ndl + 2);
+    double *kab = zalloc(pl), *tmp = zalloc(pl), *k_min = zalloc(pl), *k_grey = zalloc(pl);
+    double *skf = zalloc(pl2), *sfl = zalloc(pl2), *ft = zalloc(pl2), *trans = zalloc(pl), *su = zalloc(pl);
+    double *fgas = zalloc((size_t)wp * (ndl + 1)), *fdt = zalloc((size_t)wp * (ndl + 1));
+    int status = SOCGPU_I_NORMAL;
+    const double *mass = atm->mass;
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < np; ++l) {
+            IX2(k_eqv, l, i, wp) = 0.0; IX2(k_grey, l, i, wp) = 0.0;
+            if (adj) IX2(adj, l, i, wp) = 1.0;
+        }
+    for (int j = 1; j < n_abs && status == SOCGPU_I_NORMAL; ++j) {
+        int g = gas_of[j];
+        const double *gfr = w->gfr + pl * j;
+        if (c->isolir == SOCGPU_IP_SOLAR) {
+            for (int l = 0; l < np; ++l) { IX2(fgas, l, 0, wp) = 1.0; IX2(sfl, l, 0, wp) = 0.0; }
+            for (int i = 0; i < n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    IX2(fgas, l, i + 1, wp) = 0.0; IX2(skf, l, i, wp) = 0.0; IX2(k_min, l, i, wp) = HUGE_VAL;
+                }
+            for (int iex = 0; iex < nk[j]; ++iex) {
+                double we = sp_kw(d->w, d, iex, b, g);
+                status = absorber_term_k(lf, d, atm, np, n_layer, ndp, wp, ndl, b, g, iex, gfr, tmp, kab);
+                if (status != SOCGPU_I_NORMAL) break;
+                for (int l = 0; l < np; ++l) IX2(fdt, l, 0, wp) = we;
+                for (int i = 1; i <= n_layer; ++i)
+                    for (int l = 0; l < np; ++l) {
+                        double e = exp(-IX2(kab, l, i - 1, wp) * IX2(mass, l, i - 1, ndp) * w->sec_0[l]);
+                        IX2(fdt, l, i, wp) = IX2(fdt, l, i - 1, wp) * e;
+                        IX2(fgas, l, i, wp) = IX2(fgas, l, i, wp) + IX2(fdt, l, i, wp);
+                    }
+                for (int i = 0; i < n_layer; ++i)
+                    for (int l = 0; l < np; ++l) {
+                        IX2(skf, l, i, wp) = IX2(skf, l, i, wp) + IX2(kab, l, i, wp) * IX2(fdt, l, n_layer, wp);
+                        IX2(k_min, l, i, wp) = fmin(IX2(k_min, l, i, wp), IX2(kab, l, i, wp));
+                    }
+                for (int l = 0; l < np; ++l) IX2(sfl, l, 0, wp) = IX2(sfl, l, 0, wp) + IX2(fdt, l, n_layer, wp);
+            }
+            for (int i = 1; i <= n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    double sf = IX2(sfl, l, 0, wp);
+                    if (sf > 0.0) IX2(k_eqv, l, i - 1, wp) = IX2(k_eqv, l, i - 1, wp) + IX2(skf, l, i - 1, wp) / sf;
+                    else IX2(k_eqv, l, i - 1, wp) = IX2(k_eqv, l, i - 1, wp) + IX2(k_min, l, i - 1, wp);
+                    if (IX2(fgas, l, i - 1, wp) > 0.0)
+                        IX2(adj, l, i - 1, wp) = IX2(adj, l, i - 1, wp) * IX2(fgas, l, i, wp) / IX2(fgas, l, i - 1, wp);
+                }
+        } else {
+            if (nk[j] == 1 && c->l_grey_single) {
+                status = absorber_term_k(lf, d, atm, np, n_layer, ndp, wp, ndl, b, g, 0, gfr, tmp, kab);
+                for (int i = 0; i < n_layer; ++i)
+                    for (int l = 0; l < np; ++l) IX2(k_grey, l, i, wp) = IX2(k_grey, l, i, wp) + IX2(kab, l, i, wp);
+                continue;
+            }
+            for (size_t q = 0; q < pl2; ++q) { skf[q] = 0.0; sfl[q] = 0.0; }
+            for (size_t q = 0; q < pl; ++q) k_min[q] = HUGE_VAL;
+            const double sq_eps = sqrt(EPS_R), dfac = 1.66;   /* diffusivity_factor_minor */
+            for (int iex = 0; iex < nk[j]; ++iex) {
+                double we = sp_kw(d->w, d, iex, b, g);
+                status = absorber_term_k(lf, d, atm, np, n_layer, ndp, wp, ndl, b, g, iex, gfr, tmp, kab);
+                if (status != SOCGPU_I_NORMAL) break;
+                /* monochromatic_gas_flux.F90:100-197; ft as flux_total: 2i up, 2i+1 down at level i */
+                for (int i = 0; i < n_layer; ++i)
+                    for (int l = 0; l < np; ++l) {
+                        double tau = IX2(kab, l, i, wp) * IX2(mass, l, i, ndp);
+                        IX2(k_min, l, i, wp) = fmin(IX2(k_min, l, i, wp), IX2(kab, l, i, wp));
+                        double t = exp(-dfac * tau);
+                        IX2(trans, l, i, wp) = t;
+                        IX2(su, l, i, wp) = (1.0 - t + sq_eps) * IX2(w->planck_diff, l, i, wp) / (dfac * tau + sq_eps);
+                    }
+                for (int l = 0; l < np; ++l) IX2(ft, l, 1, wp) = w->flux_inc_down[l];
+                for (int i = 1; i <= n_layer; ++i)
+                    for (int l = 0; l < np; ++l)
+                        IX2(ft, l, 2 * i + 1, wp) = IX2(trans, l, i - 1, wp) * IX2(ft, l, 2 * i - 1, wp) - IX2(su, l, i - 1, wp);
+                for (int l = 0; l < np; ++l)
+                    IX2(ft, l, 2 * n_layer, wp) = w->d_planck_flux_surface[l] + w->alb_diff[l] * IX2(ft, l, 2 * n_layer + 1, wp);
+                for (int i = n_layer; i >= 1; --i)
+                    for (int l = 0; l < np; ++l)
+                        IX2(ft, l, 2 * i - 2, wp) = IX2(trans, l, i - 1, wp) * IX2(ft, l, 2 * i, wp) + IX2(su, l, i - 1, wp);
+                /* solve_band_k_eqv_scl.F90:993-1004 over flux_term(2 .. 2L+1), layer m/2 */
+                for (int m = 2; m <= 2 * n_layer + 1; ++m)
+                    for (int l = 0; l < np; ++l) {
+                        double a = fabs(IX2(ft, l, m - 1, wp));
+                        IX2(skf, l, m - 1, wp) = IX2(skf, l, m - 1, wp) + IX2(kab, l, m / 2 - 1, wp) * we * a;
+                        IX2(sfl, l, m - 1, wp) = IX2(sfl, l, m - 1, wp) + we * a;
+                    }
+            }
+            for (int i = 1; i <= n_layer; ++i)
+                for (int l = 0; l < np; ++l) {
+                    double kf = IX2(skf, l, 2 * i - 1, wp) + IX2(skf, l, 2 * i, wp);
+                    double fl = IX2(sfl, l, 2 * i - 1, wp) + IX2(sfl, l, 2 * i, wp);
+                    if (fl > 0.0) IX2(k_eqv, l, i - 1, wp) = IX2(k_eqv, l, i - 1, wp) + kf / fl;
+                    else IX2(k_eqv, l, i - 1, wp) = IX2(k_eqv, l, i - 1, wp) + IX2(k_min, l, i - 1, wp);
+                }
+        }
+    }
+    if (status == SOCGPU_I_NORMAL && c->isolir == SOCGPU_IP_SOLAR) {
+        const double temp_max = log(1.0 / EPS_R);
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < np; ++l)
+                IX2(adj, l, i, wp) = IX2(adj, l, i, wp)
+                    * exp(fmin(IX2(k_eqv, l, i, wp) * IX2(mass, l, i, ndp) * w->sec_0[l], temp_max));
+    }
+    /* solve_band_k_eqv_scl.F90:1024-1040 */
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < np; ++l)
+            IX2(w->k_grey_tot, l, i, wp) = IX2(w->k_grey_tot, l, i, wp) + IX2(k_eqv, l, i, wp) + IX2(k_grey, l, i, wp);
+    free(kab); free(tmp); free(k_min); free(k_grey); free(skf); free(sfl); free(ft); free(trans); free(su);
+    free(fgas); free(fdt);
+    return status;
+}
+
+/* --------------------------------------------------------------------- */
 static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
                          const socgpu_atm *atm, const socgpu_dimen *dm, const socgpu_cld *cld,
                          char *msg, size_t msg_len)
@@ -799,8 +1204,10 @@ static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
         set_msg(msg, msg_len, "only two-stream angular integration is supported"); return SOCGPU_I_ERR_FATAL; }
     if (c->isolir != SOCGPU_IP_SOLAR && c->isolir != SOCGPU_IP_INFRA_RED) {
         set_msg(msg, msg_len, "isolir must be solar or infra-red"); return SOCGPU_I_ERR_FATAL; }
-    if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_RANDOM) {
-        set_msg(msg, msg_len, "only random gas overlap is supported"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_RANDOM && c->i_gas_overlap != SOCGPU_IP_OVERLAP_K_EQV_SCL &&
+        c->i_gas_overlap != SOCGPU_IP_OVERLAP_K_EQV && c->i_gas_overlap != SOCGPU_IP_OVERLAP_K_EQV_MOD) {
+        set_msg(msg, msg_len, "only random and equivalent-extinction gas overlaps are supported");
+        return SOCGPU_I_ERR_FATAL; }
     double s, t;
     if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
         if (two_coeff_basic(c->i_2stream, 0.5, 0.5, &s, &t) != SOCGPU_I_NORMAL) {
@@ -880,6 +1287,9 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
     work w;
     work_init(&w, np, ndl, np, n_layer, cld ? cld->n_condensed : 0, max_abs);
     int wp = np;
+    lookup_fac lf;
+    lookup_fac_init(&lf, c, d, &atm, np, n_layer, ndp, wp, ndl);
+    double *kterm = zalloc((size_t)wp * ndl), *k_eqv = zalloc((size_t)wp * ndl), *adj = zalloc((size_t)wp * ndl);
 
     /* zero the outputs (augment_radiance's l_initial branch is equivalent) */
     for (int i = 0; i <= n_layer; ++i)
@@ -916,7 +1326,7 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
                 status = scale_absorb(np, n_layer, ndp, wp, atm.p, atm.t, gfr, sp_bg(d->i_scale_fnc, d, b, g),
                                       IX2(d->p_ref, g, b, d->nd_species), IX2(d->t_ref, g, b, d->nd_species),
                                       sp_scale(d, 0, b, g), d->l_doppler ? d->l_doppler[g] : 0,
-                                      d->doppler_cor ? d->doppler_cor[g] : 0.0);
+                                      d->doppler_cor ? d->doppler_cor[g] : 0.0, d, 0, b + 1);
                 for (int i = 0; i < n_layer; ++i)
                     for (int l = 0; l < np; ++l) {
                         double v = IX2(gfr, l, i, wp) * IX3(atm.gas_mix_ratio, l, i, g, ndp, ndl);
@@ -931,7 +1341,6 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
             if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "illegal type of scaling"); break; }
         }
         if (status != SOCGPU_I_NORMAL) break;
-
         /* Planck terms (diff_planck_source_mod.F90:102-136) and boundary
          * fluxes (solve_band_random_overlap.F90:565-600) */
         for (int l = 0; l < np; ++l) {
@@ -969,58 +1378,49 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
             }
         }
 
-        /* k-term products of random overlap (solve_band_random_overlap.F90:533-560) */
+        int keqv = (c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV_SCL || c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV
+                    || c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV_MOD) && n_abs > 0;
+        w.adj = NULL;
+        if (keqv) {
+            status = k_eqv_minor(&w, c, &lf, d, &atm, np, n_layer, ndp, b, n_abs, gas_of, nk, k_eqv,
+                                 c->isolir == SOCGPU_IP_SOLAR ? adj : NULL);
+            if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "illegal type of scaling"); break; }
+            if (c->isolir == SOCGPU_IP_SOLAR) w.adj = adj;
+        }
+
+        /* k-terms: products over the absorbers under random overlap
+         * (solve_band_random_overlap.F90:533-560), the major absorber's
+         * terms under k_eqv_scl (solve_band_k_eqv_scl.F90:1043-1100) */
         int n_term = 1;
-        for (int j = 0; j < n_abs; ++j) n_term *= nk[j];
+        if (keqv) n_term = nk[0];
+        else for (int j = 0; j < n_abs; ++j) n_term *= nk[j];
+        int n_sum = keqv ? 1 : n_abs;
         for (int kt = 0; kt < n_term; ++kt) {
             int iex_of[SOCGPU_MAX_SPECIES];
             double product_weight = 1.0;
             int step_prod = 1;
-            for (int j = 0; j < n_abs; ++j) {
+            for (int j = 0; j < n_sum; ++j) {
                 step_prod *= nk[j];
                 int step = n_term / step_prod;
                 iex_of[j] = (kt / step) % nk[j];
                 double wj = sp_kw(d->w, d, iex_of[j], b, gas_of[j]);
                 product_weight = (j == 0) ? wj : product_weight * wj;
             }
-            if (n_abs > 0 && !(product_weight > 0.0)) continue;
+            if (!keqv && n_abs > 0 && !(product_weight > 0.0)) continue;
             if (n_abs == 0) product_weight = 1.0;
-            /* gas_optical_properties (gas_optical_properties.F90:80-95) with
-             * k_abs_layer = k * gas_frac_rescaled (radiance_calc.F90:1386-1470) */
+            /* gas_optical_properties (gas_optical_properties.F90:80-95) */
             for (int i = 0; i < n_layer; ++i)
                 for (int l = 0; l < np; ++l) IX2(w.k_gas_abs, l, i, wp) = 0.0;
-            for (int j = 0; j < n_abs; ++j) {
-                int g = gas_of[j], iex = iex_of[j];
-                double kval = sp_kw(d->k, d, iex, b, g);
-                int isk = sp_bg(d->i_scale_k, d, b, g);
-                const double *gfr = w.gfr + (size_t)wp * ndl * j;
+            for (int j = 0; j < n_sum; ++j) {
+                status = absorber_term_k(&lf, d, &atm, np, n_layer, ndp, wp, ndl, b, gas_of[j], iex_of[j],
+                                         w.gfr + (size_t)wp * ndl * j, w.beta, kterm);
+                if (status != SOCGPU_I_NORMAL) break;
                 for (int i = 0; i < n_layer; ++i)
-                    for (int l = 0; l < np; ++l) {
-                        double kal;
-                        if (isk == SOCGPU_IP_SCALE_TERM) {
-                            /* per-term scaling: computed below */
-                            kal = 0.0;
-                        } else {
-                            kal = kval * IX2(gfr, l, i, wp);
-                        }
-                        if (j == 0) IX2(w.k_gas_abs, l, i, wp) = kal;
-                        else IX2(w.k_gas_abs, l, i, wp) = IX2(w.k_gas_abs, l, i, wp) + kal;
-                    }
-                if (isk == SOCGPU_IP_SCALE_TERM) {
-                    double *tmp = w.beta;   /* scratch */
-                    status = scale_absorb(np, n_layer, ndp, wp, atm.p, atm.t, tmp, sp_bg(d->i_scale_fnc, d, b, g),
-                                          IX2(d->p_ref, g, b, d->nd_species), IX2(d->t_ref, g, b, d->nd_species),
-                                          sp_scale(d, iex, b, g), d->l_doppler ? d->l_doppler[g] : 0,
-                                          d->doppler_cor ? d->doppler_cor[g] : 0.0);
-                    for (int i = 0; i < n_layer; ++i)
-                        for (int l = 0; l < np; ++l) {
-                            double v = IX2(tmp, l, i, wp) * IX3(atm.gas_mix_ratio, l, i, g, ndp, ndl);
-                            double kal = kval * (v > 0.0 ? v : 0.0);
-                            if (j == 0) IX2(w.k_gas_abs, l, i, wp) = kal;
-                            else IX2(w.k_gas_abs, l, i, wp) = IX2(w.k_gas_abs, l, i, wp) + kal;
-                        }
-                }
+                    for (int l = 0; l < np; ++l)
+                        IX2(w.k_gas_abs, l, i, wp) = (j == 0) ? IX2(kterm, l, i, wp)
+                                                              : IX2(w.k_gas_abs, l, i, wp) + IX2(kterm, l, i, wp);
             }
+            if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "illegal type of scaling"); break; }
             if (l_cloud) {
                 solve_mcica_term(&w, c, dm, d, atm.mass, cld, b, n_abs > 0 ? iex_of[0] : 0);
             } else {
@@ -1075,6 +1475,8 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
                 IX2(out.heating_rate, l, i - 1, ndp) = hr;
             }
     (void)ict;
+    lookup_fac_free(&lf);
+    free(kterm); free(k_eqv); free(adj);
     work_free(&w);
     return status;
 }

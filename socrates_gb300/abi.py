@@ -26,8 +26,10 @@ IP_PHASE_WATER, IP_PHASE_ICE = 1, 2
 IP_CLCMP_ST_WATER, IP_CLCMP_ST_ICE = 1, 2
 IP_DROP_PADE_2, IP_ICE_PADE_2_PHF = 5, 20
 IP_OVERLAP_RANDOM = 2
+IP_OVERLAP_K_EQV_SCL, IP_OVERLAP_K_EQV, IP_OVERLAP_K_EQV_MOD = 4, 5, 6
 IP_SCALE_NULL, IP_SCALE_BAND, IP_SCALE_TERM = 0, 1, 2
 IP_SCALE_FNC_NULL, IP_SCALE_POWER_LAW, IP_SCALE_POWER_QUAD, IP_SCALE_DOPPLER_QUAD = 0, 1, 2, 3
+IP_SCALE_WENYI, IP_SCALE_LOOKUP, IP_SCALE_T_LOOKUP = 4, 9, 10
 IP_RAYLEIGH_TOTAL = 1
 IP_MAX_RAND, IP_RAND, IP_EXPONENTIAL, IP_EXPONENTIAL_RAND = 0, 1, 2, 3
 IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0, 1, 2
@@ -35,7 +37,7 @@ IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0,
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RNG_LCG, RNG_PHILOX = 0, 1
 NOALLOC_MAX_CLOUD_LAYERS = 1024   # SOCGPU_NOALLOC_MAX_CLOUD_LAYERS
-ABI_VERSION = 2
+ABI_VERSION = 3
 IP_SELF_CONTINUUM, IP_FRN_CONTINUUM = 1, 2
 
 _dp = C.POINTER(C.c_double)
@@ -59,6 +61,14 @@ class SpectrumDesc(C.Structure):
         ("l_ice_type", _ip), ("i_ice_parm", _ip), ("ice_parm_list", _dp),
         ("nd_continuum", C.c_int), ("n_band_continuum", _ip), ("index_continuum", _ip), ("index_water", C.c_int),
         ("i_scale_fnc_cont", _ip), ("k_cont", _dp), ("scale_cont", _dp), ("p_ref_cont", _dp), ("t_ref_cont", _dp),
+        # lookup-table k scaling (the '_k' companion file)
+        ("n_pre", C.c_int), ("n_tmp", C.c_int), ("p_lookup", _dp), ("t_lookup", _dp), ("k_lookup", _dp),
+        ("index_sb", _ip), ("nd_species_sb", C.c_int), ("n_gas_frac", C.c_int), ("gf_lookup", _dp),
+        ("k_lookup_sb", _dp), ("molar_weight", _dp),
+        ("nd_t_lookup_gas", C.c_int), ("n_t_lookup_gas", _ip), ("t_lookup_gas", _dp), ("k_t_lookup_gas", _dp),
+        # CO2/O3 tables of ip_scale_wenyi
+        ("wenyi_n_term4", C.c_int), ("wenyi_n_term6", C.c_int), ("wenyi_plg", _dp), ("wenyi_ttb", _dp),
+        ("wenyi_tto", _dp), ("wenyi_gk250b", _dp), ("wenyi_gk4", _dp), ("wenyi_gk6", _dp),
     ]
 
 
@@ -70,7 +80,7 @@ class Control(C.Structure):
         ("l_rescale", C.c_int), ("n_order_forward", C.c_int), ("l_ir_source_quad", C.c_int),
         ("l_rayleigh", C.c_int), ("l_gas", C.c_int), ("l_aerosol_mode", C.c_int), ("l_flux_div", C.c_int),
         ("first_band", C.c_int), ("last_band", C.c_int), ("weight_band", _dp), ("precision", C.c_int),
-        ("l_continuum", C.c_int), ("l_mixing_ratio", C.c_int),
+        ("l_continuum", C.c_int), ("l_mixing_ratio", C.c_int), ("l_grey_single", C.c_int),
     ]
 
 

@@ -75,6 +75,7 @@ class Control:
     precision: int = abi.PRECISION_FP64
     l_continuum: bool = False
     l_mixing_ratio: bool = False
+    l_grey_single: bool = False
 
     def as_struct(self, n_band: int, keep: list) -> abi.Control:
         c = abi.Control()
@@ -90,6 +91,7 @@ class Control:
         c.weight_band = _dp(self.weight_band, keep)
         c.precision = self.precision
         c.l_continuum, c.l_mixing_ratio = int(self.l_continuum), int(self.l_mixing_ratio)
+        c.l_grey_single = int(self.l_grey_single)
         return c
 
 

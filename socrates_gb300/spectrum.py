@@ -13,6 +13,8 @@ from __future__ import annotations
 import ctypes as C
 from dataclasses import dataclass, field
 
+from pathlib import Path
+
 import numpy as np
 
 from . import abi
@@ -25,8 +27,134 @@ GAS_NAMES = {1: "Water Vapour", 2: "Carbon Dioxide", 3: "Ozone", 4: "Dinitrogen 
 N_SCALE_VARIABLE = {0: 0, 1: 2, 2: 3, 3: 4, 4: 0, 5: 0, 6: 6, 7: 8, 8: 10, 9: 0, 10: 0}
 
 
+# Molar weights [g/mol] of the absorbers by gas identifier (the published
+# values of J. A. Duffy, General Inorganic Chemistry (1970), and NIST, as
+# gas_list_pcf.F90:303-330 lists them); used for self-broadened gas fractions.
+MOLAR_WEIGHT = {1: 18.0153, 2: 44.0100, 3: 47.9982, 4: 44.0128, 5: 28.0106, 6: 16.0430, 7: 31.9988, 8: 30.0061,
+                9: 64.0628, 10: 46.0055, 11: 17.0306, 12: 63.0129, 13: 28.0134, 14: 137.3686, 15: 120.9140,
+                16: 187.3765, 17: 86.46892, 18: 120.02227, 19: 102.03184, 20: 170.921, 21: 63.866, 22: 66.9409,
+                23: 2.01588, 24: 4.002602, 25: 60.075}
+
+
 def _f(a, dtype):
     return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+def _fields13(line):
+    """The 1PE13.6 fields of one record."""
+    line = line.rstrip()
+    return [float(line[i:i + 13]) for i in range(0, len(line), 13) if line[i:i + 13].strip()]
+
+
+def read_wenyi_tables(path) -> dict:
+    """The CO2 (band 4) and O3 (band 6) tables of ip_scale_wenyi from a
+    SOCRATES source file that defines them (the module scale_wenyi): the
+    reference compiles them in, so a caller reads them from its own SOCRATES
+    installation and passes them with the spectral data.  The band-4 and
+    band-6 tables are assembled as their RESHAPE(..., ORDER=(3, 2, 1)) builds
+    them: one source array per temperature, the k-term index fastest."""
+    import re
+    text = Path(path).read_text()
+    arrays = {}
+    for m in re.finditer(r"PARAMETER\s*::\s*(\w+)\(\s*(\d+)\s*\)\s*=\s*\(/(.*?)/\)", text, re.S):
+        body = re.sub(r"!.*", "", m.group(3))
+        vals = [float(v.split("_")[0].replace("D", "E").replace("d", "e"))
+                for v in re.findall(r"[-+]?\d+\.?\d*(?:[EeDd][-+]?\d+)?_RealK", body)]
+        if len(vals) != int(m.group(2)):
+            raise ValueError(f"{path}: {m.group(1)} has {len(vals)} values, declared {m.group(2)}")
+        arrays[m.group(1).lower()] = np.array(vals)
+
+    def table(prefix, n_t):
+        parts = [arrays[f"{prefix}_{i}"] for i in range(1, n_t + 1)]
+        n_term = parts[0].size // 26
+        return np.asfortranarray(np.stack([p.reshape(26, n_term) for p in parts], axis=0))
+
+    return dict(wenyi_plg=arrays["plg"], wenyi_ttb=arrays["ttb"], wenyi_tto=arrays["tto"],
+                wenyi_gk250b=arrays["gk250b"], wenyi_gk4=table("gk4", arrays["ttb"].size),
+                wenyi_gk6=table("gk6", arrays["tto"].size))
+
+
+def _read_k_file(path, n_band, n_abs, nd_k, recs, ia, nba, isb, n_pre, n_tmp):
+    """Lookup tables of the '_k' file in the order read_spectrum.F90:1420-1560
+    reads them: the P/T grid, the gas fractions of self-broadened absorbers,
+    one table per (band, absorber) record of block 5, then the
+    temperature-only tables."""
+    text = Path(path).read_text().splitlines()
+
+    def values(q, n):
+        out = []
+        while len(out) < n:
+            out += _fields13(text[q])
+            q += 1
+        return out[:n], q
+
+    def block(title):
+        for q, ln in enumerate(text):
+            if ln.startswith("*BLOCK") and ln[8:8 + len(title)] == title:
+                return q
+        raise ValueError(f"{path}: no '{title}' block")
+
+    out = {}
+    if any(r[4] == abi.IP_SCALE_LOOKUP for r in recs):
+        q = block("k-table") + 3
+        p_lk = np.zeros(n_pre)
+        t_lk = np.zeros((n_tmp, n_pre))
+        for ip in range(n_pre):
+            v, q = values(q, 1 + n_tmp)
+            p_lk[ip] = np.log(v[0])
+            t_lk[:, ip] = v[1:]
+        sb = isb is not None and bool(np.any(isb > 0))
+        gf = None
+        if sb:
+            n_gf = int(text[q + 1][14:18])
+            gf, q = values(q + 2, n_gf)
+            gf = np.array(gf)
+            nsb = int(isb.max())
+            k_sb = np.zeros((n_tmp, n_pre, n_gf, nd_k, nsb, n_band))
+        k_lk = np.zeros((n_tmp, n_pre, nd_k, n_abs, n_band))
+        for b, g, nk, sk, fnc, *_ in recs:
+            if fnc != abi.IP_SCALE_LOOKUP:
+                continue
+            q += 2
+            if sb and isb[g] > 0:
+                for t in range(nk):
+                    for ig in range(n_gf):
+                        for ip in range(n_pre):
+                            v, q = values(q, n_tmp)
+                            k_sb[:, ip, ig, t, isb[g] - 1, b] = v
+            else:
+                for t in range(nk):
+                    for ip in range(n_pre):
+                        v, q = values(q, n_tmp)
+                        k_lk[:, ip, t, g, b] = v
+        out.update(p_lookup=p_lk, t_lookup=_f(t_lk, np.float64), k_lookup=_f(k_lk, np.float64))
+        if sb:
+            out.update(index_sb=isb, gf_lookup=gf, k_lookup_sb=_f(k_sb, np.float64))
+    t_gases = sorted({r[1] for r in recs if r[4] == abi.IP_SCALE_T_LOOKUP})
+    if t_gases:
+        q = block("temperature k-tables")
+        ndt = int(text[q + 2][9:13])
+        q += 3
+        n_t = np.zeros(n_abs, np.int32)
+        t_g = np.zeros((ndt, n_abs))
+        for g in t_gases:
+            n_t[g] = int(text[q + 1][27:31])
+            v, q = values(q + 2, n_t[g])
+            t_g[: n_t[g], g] = v
+        fnc_of = {(r[0], r[1]): r[4] for r in recs}
+        nk_of = {(r[0], r[1]): r[2] for r in recs}
+        k_t = np.zeros((ndt, nd_k, n_abs, n_band))
+        for b in range(n_band):
+            for j in range(int(nba[b])):
+                g = int(ia[j, b]) - 1
+                if fnc_of.get((b, g)) != abi.IP_SCALE_T_LOOKUP:
+                    continue
+                q += 2
+                for t in range(nk_of[(b, g)]):
+                    v, q = values(q, n_t[g])
+                    k_t[: n_t[g], t, g, b] = v
+        out.update(n_t_lookup_gas=n_t, t_lookup_gas=_f(t_g, np.float64), k_t_lookup_gas=_f(k_t, np.float64))
+    return out
 
 
 @dataclass
@@ -67,6 +195,24 @@ class Spectrum:
     scale_cont: np.ndarray | None = None         # (nd_scale_variable, n_band, nd_continuum)
     p_ref_cont: np.ndarray | None = None         # (nd_continuum, n_band)
     t_ref_cont: np.ndarray | None = None         # (nd_continuum, n_band)
+    i_overlap: np.ndarray | None = None          # (n_band) overlap method of each band (block 4 version 1)
+    # lookup-table k scaling: block 5 with the '_k' companion file
+    p_lookup: np.ndarray | None = None           # (n_pre) ln(p / Pa)
+    t_lookup: np.ndarray | None = None           # (n_tmp, n_pre) K
+    k_lookup: np.ndarray | None = None           # (n_tmp, n_pre, nd_k_term, n_absorb, n_band)
+    index_sb: np.ndarray | None = None           # (n_absorb) 1-based self-broadened index, 0 none
+    gf_lookup: np.ndarray | None = None          # (n_gas_frac)
+    k_lookup_sb: np.ndarray | None = None        # (n_tmp, n_pre, n_gas_frac, nd_k_term, nd_species_sb, n_band)
+    n_t_lookup_gas: np.ndarray | None = None     # (n_absorb)
+    t_lookup_gas: np.ndarray | None = None       # (nd_t_lookup_gas, n_absorb) K
+    k_t_lookup_gas: np.ndarray | None = None     # (nd_t_lookup_gas, nd_k_term, n_absorb, n_band)
+    # CO2 and O3 tables of ip_scale_wenyi (the reference compiles them in)
+    wenyi_plg: np.ndarray | None = None          # (26)
+    wenyi_ttb: np.ndarray | None = None          # (10)
+    wenyi_tto: np.ndarray | None = None          # (9)
+    wenyi_gk250b: np.ndarray | None = None       # (n_term4)
+    wenyi_gk4: np.ndarray | None = None          # (10, 26, n_term4)
+    wenyi_gk6: np.ndarray | None = None          # (9, 26, n_term6)
     name: str = "spectrum"
     _keep: list = field(default_factory=list, repr=False)
 
@@ -169,6 +315,47 @@ class Spectrum:
                 d.scale_cont = dp(self.scale_cont)
             d.p_ref_cont = dp(self.p_ref_cont)
             d.t_ref_cont = dp(self.t_ref_cont)
+        nk = self.nd_k_term
+        if self.k_lookup is not None:
+            n_tmp, n_pre = self.t_lookup.shape
+            d.n_tmp, d.n_pre = n_tmp, n_pre
+            d.p_lookup = dp(self.p_lookup)
+            d.t_lookup = dp(self.t_lookup)
+            kl = np.zeros((n_tmp, n_pre, nk, nds, self.n_band))
+            kl[:, :, :, : self.n_absorb] = self.k_lookup
+            d.k_lookup = dp(kl)
+        if self.index_sb is not None and self.k_lookup_sb is not None:
+            isb = np.zeros(nds, np.int32)
+            isb[: self.n_absorb] = self.index_sb
+            d.index_sb = ip(isb)
+            d.nd_species_sb = int(self.k_lookup_sb.shape[4])
+            d.n_gas_frac = int(self.gf_lookup.size)
+            d.gf_lookup = dp(self.gf_lookup)
+            d.k_lookup_sb = dp(self.k_lookup_sb)
+        mw = np.zeros(nds)
+        mw[: self.n_absorb] = [MOLAR_WEIGHT.get(int(t), 0.0) for t in self.type_absorb]
+        d.molar_weight = dp(mw)
+        if self.k_t_lookup_gas is not None:
+            ndt = int(self.t_lookup_gas.shape[0])
+            d.nd_t_lookup_gas = ndt
+            nt = np.zeros(nds, np.int32)
+            nt[: self.n_absorb] = self.n_t_lookup_gas
+            d.n_t_lookup_gas = ip(nt)
+            tg = np.zeros((ndt, nds))
+            tg[:, : self.n_absorb] = self.t_lookup_gas
+            d.t_lookup_gas = dp(tg)
+            kt = np.zeros((ndt, nk, nds, self.n_band))
+            kt[:, :, : self.n_absorb] = self.k_t_lookup_gas
+            d.k_t_lookup_gas = dp(kt)
+        if self.wenyi_plg is not None:
+            d.wenyi_plg = dp(self.wenyi_plg)
+            d.wenyi_ttb = dp(self.wenyi_ttb)
+            d.wenyi_tto = dp(self.wenyi_tto)
+            d.wenyi_gk250b = dp(self.wenyi_gk250b)
+            d.wenyi_gk4 = dp(self.wenyi_gk4)
+            d.wenyi_gk6 = dp(self.wenyi_gk6)
+            d.wenyi_n_term4 = int(self.wenyi_gk4.shape[2])
+            d.wenyi_n_term6 = int(self.wenyi_gk6.shape[2])
         if self.thermal_coeff is not None:
             d.n_deg_fit = self.n_deg_fit
             d.t_ref_planck = self.t_ref_planck
@@ -357,7 +544,7 @@ class Spectrum:
             fh.write("\n".join(L) + "\n")
 
     @classmethod
-    def read_text(cls, path, name: str | None = None) -> "Spectrum":
+    def read_text(cls, path, name: str | None = None, k_path=None) -> "Spectrum":
         """Read a spectral file in the reference's text format: blocks 0
         (summary, versions 1 and 2), 1 (band limits), 2 (solar spectrum), 3
         (Rayleigh), 4 (absorbers per band), 5 (k-terms), 6 (Planck
@@ -365,7 +552,8 @@ class Spectrum:
         Pade droplet/ice blocks 10 and 12 (parametrisations 5 and 20); record
         layouts of read_spectrum.F90 (blocks 0-13).  Other blocks (surface
         properties, aerosols, other cloud parametrisations) are skipped.
-        Lookup-table k scaling (the '_k' companion files) is not read."""
+        The lookup tables of block 5 come from the '_k' companion file (path +
+        '_k' unless k_path is given)."""
         text = open(path).read().splitlines()
         blocks = []
         cur = None
@@ -416,32 +604,57 @@ class Spectrum:
             return out
         sol = band_values(2, 2)
         ray = band_values(3, 3)
-        # block 4: absorbers in each band (token stream after 5 header lines)
+        # block 4: absorbers in each band (token stream after 5 header lines);
+        # version 1 adds each band's overlap method (read_spectrum.F90 block 4_0_1)
         toks = " ".join(by[4][0]["lines"][5:]).split()
+        with_overlap = by[4][0]["version"] >= 1
         nba = np.zeros(n_band, np.int32)
+        i_ovl = np.zeros(n_band, np.int32) if with_overlap else None
         ia = np.zeros((max(1, n_abs), n_band), np.int32)
         q = 0
         for _ in range(n_band):
             b = int(toks[q]) - 1
             nba[b] = int(toks[q + 1])
             q += 2
+            if with_overlap:
+                i_ovl[b] = int(toks[q])
+                q += 1
             for j in range(nba[b]):
                 ia[j, b] = int(toks[q])
                 q += 1
-        # block 5: k-terms, fixed columns (2(3x, 1pe16.9), i3, :, (t42, 1pe16.9, 3x, 1pe16.9))
+        # block 5: k-terms, fixed columns (2(3x, 1pe16.9), i3, :, (t42, 1pe16.9, 3x, 1pe16.9)).
+        # Version 1 may first list the self-broadened absorbers
+        # (read_spectrum.F90:1268-1300); lookup-table records give the table
+        # extents in place of the reference pressure and temperature.
+        b5 = by[5][0]["lines"]
+        isb = None
+        q0 = 4
+        for q, ln in enumerate(b5):
+            if ln.strip().startswith("Self-broadened indexing numbers"):
+                vals, r = [], q + 2
+                while len(vals) < n_abs:
+                    vals += [int(x) for x in b5[r].split()]
+                    r += 1
+                isb = np.array(vals[:n_abs], np.int32)
+            if ln.startswith("Band        Gas, Number of k-terms"):
+                q0 = q + 3
+                break
         recs = []
-        lines = by[5][0]["lines"][4:]
+        lines = b5[q0:]
         q = 0
         nd_k, nsv_max = 1, 4
+        n_pre = n_tmp = 0
         while q < len(lines):
             parts = lines[q].split()
             if len(parts) < 5:
                 q += 1
                 continue
             b, g, nk, sk, fnc = (int(x) for x in parts[:5])
-            if fnc in (9, 10):
-                raise ValueError("lookup-table k scaling is not supported")
-            p_ref, t_ref = (float(x) for x in lines[q + 1].split()[:2])
+            p_ref = t_ref = 0.0
+            if fnc == abi.IP_SCALE_LOOKUP:
+                n_pre, n_tmp = (int(x) for x in lines[q + 1].split()[:2])
+            elif fnc != abi.IP_SCALE_T_LOOKUP:
+                p_ref, t_ref = (float(x) for x in lines[q + 1].split()[:2])
             q += 2
             nsv = N_SCALE_VARIABLE.get(fnc, 0)
             terms = []
@@ -463,6 +676,12 @@ class Spectrum:
             recs.append((b - 1, g - 1, nk, sk, fnc, p_ref, t_ref, terms))
             nd_k = max(nd_k, nk)
             nsv_max = max(nsv_max, nsv)
+        tables = {}
+        if any(r[4] in (abi.IP_SCALE_LOOKUP, abi.IP_SCALE_T_LOOKUP) for r in recs):
+            kp = Path(k_path) if k_path is not None else Path(str(path) + "_k")
+            if not kp.exists():
+                raise ValueError(f"the k-term lookup tables of block 5 are in {kp}, which cannot be read")
+            tables = _read_k_file(kp, n_band, n_abs, nd_k, recs, ia, nba, isb, n_pre, n_tmp)
         ibk = np.zeros((n_band, n_abs), np.int32)
         isk = np.zeros((n_band, n_abs), np.int32)
         isf = np.zeros((n_band, n_abs), np.int32)
@@ -562,7 +781,7 @@ class Spectrum:
                 vals = []
                 for ln in lines[lines.index(head) + 1:]:
                     u = ln.upper()
-                    if "RANGE" in u or not any(ch.isdigit() for ch in ln):
+                    if "RANGE" in u or "MOMENTS" in u or not any(ch.isdigit() for ch in ln):
                         continue
                     if "BAND" in u and "=" in ln:
                         vals.append(ln.split("=")[1].split()[0])
@@ -588,4 +807,4 @@ class Spectrum:
                    scale=_f(sc, np.float64), p_ref=pr, t_ref=tr, solar_flux_band=sol, rayleigh_coeff=ray,
                    n_deg_fit=ndeg, t_ref_planck=tref, thermal_coeff=tc, drop_parm_list=dpl, i_drop_parm=dids,
                    ice_parm_list=ipl, i_ice_parm=iids, l_doppler=ldop, doppler_cor=dcor, name=name or str(path),
-                   **cont)
+                   i_overlap=i_ovl, **cont, **tables)

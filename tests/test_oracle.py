@@ -204,7 +204,10 @@ def test_cloud_gen_compaction_and_fraction():
 
 
 # ---------------------------------------------------------------------------
-@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("icrccm")))
+KGO_FIXTURES = ("icrccm", "circ6")
+
+
+@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(KGO_FIXTURES)))
 def test_oracle_reproduces_golden_fixture(name):
     from golden_cases import CASES
     data = np.load(GOLDEN / f"{name}.npz")
@@ -220,6 +223,22 @@ def test_oracle_reproduces_icrccm27_known_good_output():
     heating rates to 6 significant digits (laer27_ref.hrts); every layer
     must agree to half a unit of the 6th digit."""
     import icrccm27 as K
+    ctl, sp, col, kgo = K.load()
+    hr = K.heating_rate(O.radiance_calc(ctl, sp, col), col.mass)[0]
+    half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
+    err = np.abs(hr - kgo) / half_unit
+    assert err.max() <= 1.0, f"layer {err.argmax()}: {hr[err.argmax()]} vs {kgo[err.argmax()]}"
+
+
+def test_oracle_reproduces_circ6_ga7_known_good_output():
+    """Pin against the reference's known-good output for the GA7 long-wave
+    spectral file: CIRC case 6, clear sky (examples/netcdf/CIRC_case6,
+    ref_case6_lw_ga7_clr.hrts).  GA7 takes its k-terms from lookup tables
+    (ip_scale_lookup), the band-4 CO2 terms from Wen-Yi Zhong's tables
+    (ip_scale_wenyi) and overlaps its gases by equivalent extinction
+    (k_eqv_scl), with the water-vapour continuum.  Every layer must agree to
+    half a unit of the 6th significant digit the reference prints."""
+    import circ6 as K
     ctl, sp, col, kgo = K.load()
     hr = K.heating_rate(O.radiance_calc(ctl, sp, col), col.mass)[0]
     half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
