@@ -19,11 +19,19 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "host_internal.h"
 
 namespace socgpu {
+
+// The equivalent-extinction overlaps (rad_pcf.F90:432-436), all solved by
+// solve_band_k_eqv_scl.
+bool is_keqv(const socgpu_control *c) {
+  return c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV_SCL || c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV ||
+         c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV_MOD;
+}
 
 int launch_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2,
                      int n_subcol, int n1, int n2, int ipph, int ioverlap, const int *rand_seed,
@@ -76,6 +84,39 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   }
   e.bands_host.assign(d->n_band, BandInfo{});
   e.gpoints_host.clear();
+  std::vector<BandInfo> bands_keqv;
+  std::vector<GPoint> gpoints_keqv;
+  std::vector<TermK> minor;
+  bool random_ok = true;
+  // lookup tables, gathered into one compact array: one block per (band,
+  // absorber, k-term) that uses them (P/T: n_tmp x n_pre, or with gas
+  // fractions n_tmp x n_pre x n_gf; temperature only: n_t)
+  const int n_pre = d->n_pre, n_tmp = d->n_tmp;
+  const bool sb_tables = d->index_sb && d->nd_species_sb > 0 && d->n_gas_frac >= 1 && d->gf_lookup && d->k_lookup_sb;
+  std::vector<double> k_lk;
+  std::map<std::tuple<int, int, int>, int> lk_of;
+  auto lookup_block = [&](int b, int g, int iex, int fnc) -> int {
+    if (fnc != SOCGPU_IP_SCALE_LOOKUP && fnc != SOCGPU_IP_SCALE_T_LOOKUP) return -1;
+    auto key = std::make_tuple(b, g, iex);
+    auto it = lk_of.find(key);
+    if (it != lk_of.end()) return it->second;
+    const int off = (int)k_lk.size();
+    if (fnc == SOCGPU_IP_SCALE_T_LOOKUP) {
+      const size_t src = (size_t)d->nd_t_lookup_gas * ((size_t)iex + (size_t)d->nd_k_term * ((size_t)g + (size_t)d->nd_species * b));
+      for (int q = 0; q < d->n_t_lookup_gas[g]; ++q) k_lk.push_back(d->k_t_lookup_gas[src + q]);
+    } else if (sb_tables && d->index_sb[g] > 0) {
+      const size_t n = (size_t)n_tmp * n_pre * d->n_gas_frac;
+      const size_t src = n * ((size_t)iex + (size_t)d->nd_k_term * ((size_t)(d->index_sb[g] - 1) + (size_t)d->nd_species_sb * b));
+      k_lk.insert(k_lk.end(), d->k_lookup_sb + src, d->k_lookup_sb + src + n);
+    } else {
+      const size_t n = (size_t)n_tmp * n_pre;
+      const size_t src = n * ((size_t)iex + (size_t)d->nd_k_term * ((size_t)g + (size_t)d->nd_species * b));
+      k_lk.insert(k_lk.end(), d->k_lookup + src, d->k_lookup + src + n);
+    }
+    lk_of[key] = off;
+    return off;
+  };
+  bool any_lookup = false;
   for (int b = 0; b < d->n_band; ++b) {
     BandInfo &bi = e.bands_host[b];
     bi.solar_flux_band = d->solar_flux_band ? d->solar_flux_band[b] : 0.0;
@@ -136,17 +177,55 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
       gs.doppler_cor = d->doppler_cor ? d->doppler_cor[g] : 0.0;
       gs.p_ref = fget2(d->p_ref, g, b, d->nd_species);
       gs.t_ref = fget2(d->t_ref, g, b, d->nd_species);
+      gs.sb = -1;
+      gs.n_t = 0;
       if (gs.i_scale_k != SOCGPU_IP_SCALE_NULL && gs.i_scale_k != SOCGPU_IP_SCALE_BAND &&
           gs.i_scale_k != SOCGPU_IP_SCALE_TERM) {
         set_msg(msg, msg_len, "band %d absorber %d: illegal type of scaling %d", b + 1, g + 1, gs.i_scale_k);
         return SOCGPU_I_ERR_FATAL;
       }
-      if (gs.i_scale_k != SOCGPU_IP_SCALE_NULL && gs.i_scale_fnc != SOCGPU_IP_SCALE_FNC_NULL &&
-          gs.i_scale_fnc != SOCGPU_IP_SCALE_POWER_LAW && gs.i_scale_fnc != SOCGPU_IP_SCALE_POWER_QUAD &&
-          gs.i_scale_fnc != SOCGPU_IP_SCALE_DOPPLER_QUAD) {
-        set_msg(msg, msg_len, "band %d absorber %d: scaling function %d is not supported on the device path "
-                "(lookup tables and double power laws are not implemented)", b + 1, g + 1, gs.i_scale_fnc);
-        return SOCGPU_I_ERR_FATAL;
+      const int fnc = gs.i_scale_fnc;
+      if (gs.i_scale_k != SOCGPU_IP_SCALE_NULL) {
+        const bool table = fnc == SOCGPU_IP_SCALE_LOOKUP || fnc == SOCGPU_IP_SCALE_T_LOOKUP;
+        if (fnc != SOCGPU_IP_SCALE_FNC_NULL && fnc != SOCGPU_IP_SCALE_POWER_LAW && fnc != SOCGPU_IP_SCALE_POWER_QUAD &&
+            fnc != SOCGPU_IP_SCALE_DOPPLER_QUAD && fnc != SOCGPU_IP_SCALE_WENYI && !table) {
+          set_msg(msg, msg_len, "band %d absorber %d: scaling function %d is not supported on the device path "
+                  "(double power laws are not implemented)", b + 1, g + 1, fnc);
+          return SOCGPU_I_ERR_FATAL;
+        }
+        if (table && gs.i_scale_k != SOCGPU_IP_SCALE_TERM) {
+          set_msg(msg, msg_len, "band %d absorber %d: lookup tables need per-term scaling", b + 1, g + 1);
+          return SOCGPU_I_ERR_FATAL;
+        }
+        if (fnc == SOCGPU_IP_SCALE_LOOKUP) {
+          if (n_pre < 2 || n_tmp < 2 || n_tmp > 255 || n_pre > 255 || !d->p_lookup || !d->t_lookup || !d->k_lookup) {
+            set_msg(msg, msg_len, "band %d absorber %d: P/T lookup tables missing or outside 2..255 entries",
+                    b + 1, g + 1);
+            return SOCGPU_I_ERR_FATAL;
+          }
+          if (sb_tables && d->index_sb[g] > 0) {
+            gs.sb = d->index_sb[g] - 1;
+            if (gs.sb >= kMaxSb || gs.sb >= d->nd_species_sb || d->n_gas_frac > 255) {
+              set_msg(msg, msg_len, "absorber %d: self-broadened index %d outside 1..%d", g + 1, gs.sb + 1, kMaxSb);
+              return SOCGPU_I_ERR_RANGE;
+            }
+          }
+          any_lookup = true;
+        }
+        if (fnc == SOCGPU_IP_SCALE_T_LOOKUP) {
+          if (!d->n_t_lookup_gas || !d->t_lookup_gas || !d->k_t_lookup_gas || d->n_t_lookup_gas[g] < 2 ||
+              d->n_t_lookup_gas[g] > d->nd_t_lookup_gas) {
+            set_msg(msg, msg_len, "band %d absorber %d: temperature lookup tables missing", b + 1, g + 1);
+            return SOCGPU_I_ERR_FATAL;
+          }
+          gs.n_t = d->n_t_lookup_gas[g];
+        }
+        if (fnc == SOCGPU_IP_SCALE_WENYI &&
+            (!d->wenyi_plg || !((b == 3 && d->wenyi_gk4 && d->wenyi_gk250b && d->wenyi_ttb) ||
+                                (b == 5 && d->wenyi_gk6 && d->wenyi_tto)))) {
+          set_msg(msg, msg_len, "band %d absorber %d: Wen-Yi scaling needs band 4 or 6 and its tables", b + 1, g + 1);
+          return SOCGPU_I_ERR_FATAL;
+        }
       }
       int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
       for (int v = 0; v < nv; ++v) {
@@ -158,20 +237,33 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
       gs.t_ref_f = (float)gs.t_ref;
       gs.doppler_cor_f = (float)gs.doppler_cor;
       nk[j] = fget2(d->i_band_k, b, g, d->nd_band);
-      if (nk[j] < 1 || nk[j] > d->nd_k_term) {
+      if (nk[j] < 1 || nk[j] > d->nd_k_term ||
+          (fnc == SOCGPU_IP_SCALE_WENYI && nk[j] > (b == 3 ? d->wenyi_n_term4 : d->wenyi_n_term6))) {
         set_msg(msg, msg_len, "band %d absorber %d: %d k-terms", b + 1, g + 1, nk[j]);
         return SOCGPU_I_ERR_RANGE;
       }
-      n_term *= nk[j];
+      if (n_term <= SOCGPU_MAX_GPOINT) n_term *= nk[j];
     }
+    // one k-term of absorber j as a g-point entry; returns its weight
+    auto set_term = [&](GPoint &gp, int j, int iex) {
+      const int g = bi.gas[j].species;
+      const size_t q = (size_t)iex + (size_t)d->nd_k_term * ((size_t)b + (size_t)d->nd_band * g);
+      gp.k[j] = d->k[q];
+      gp.kf[j] = (float)d->k[q];
+      gp.iex[j] = (short)iex;
+      gp.lk_off[j] = lookup_block(b, g, iex, bi.gas[j].i_scale_fnc);
+      const int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
+      for (int v = 0; v < nv; ++v) {
+        gp.term_scale[j][v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable * q];
+        gp.term_scale_f[j][v] = (float)gp.term_scale[j][v];
+      }
+      return d->w[q];
+    };
+    // k-term products of random overlap (solve_band_random_overlap.F90:533-560)
     bi.g_first = (int)e.gpoints_host.size();
     if (n_abs == 0) n_term = 1;
-    if ((long long)e.gpoints_host.size() + n_term > SOCGPU_MAX_GPOINT) {
-      set_msg(msg, msg_len, "more than %d k-term products", SOCGPU_MAX_GPOINT);
-      return SOCGPU_I_ERR_RANGE;
-    }
-    // k-term products of random overlap (solve_band_random_overlap.F90:533-560)
-    for (long long kt = 0; kt < n_term; ++kt) {
+    if ((long long)e.gpoints_host.size() + n_term > SOCGPU_MAX_GPOINT) random_ok = false;
+    for (long long kt = 0; random_ok && kt < n_term; ++kt) {
       GPoint gp{};
       gp.band = b;
       gp.n_abs = n_abs;
@@ -181,24 +273,58 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
         step_prod *= nk[j];
         long long step = n_term / step_prod;
         int iex = (int)((kt / step) % nk[j]);
-        int g = bi.gas[j].species;
-        size_t q = (size_t)iex + (size_t)d->nd_k_term * ((size_t)b + (size_t)d->nd_band * g);
-        double wj = d->w[q];
+        double wj = set_term(gp, j, iex);
         gp.weight = (j == 0) ? wj : gp.weight * wj;
-        gp.k[j] = d->k[q];
-        gp.kf[j] = (float)d->k[q];
         if (j == 0) gp.iex_major = iex;
-        int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
-        for (int v = 0; v < nv; ++v) {
-          gp.term_scale[j][v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable * q];
-          gp.term_scale_f[j][v] = (float)gp.term_scale[j][v];
-        }
       }
       gp.weight_f = (float)gp.weight;
       if (n_abs > 0 && !(gp.weight > 0.0)) continue;   // n_term_reduced
       e.gpoints_host.push_back(gp);
     }
-    bi.g_count = (int)e.gpoints_host.size() - bi.g_first;
+    bi.g_count = random_ok ? (int)e.gpoints_host.size() - bi.g_first : 0;
+    // equivalent extinction (solve_band_k_eqv_scl.F90:1043-1100): the major
+    // absorber's terms are solved, the minor absorbers' terms weighted
+    BandInfo bk = bi;
+    bk.g_first = (int)gpoints_keqv.size();
+    const int n_major = n_abs > 0 ? nk[0] : 1;
+    for (int iex = 0; iex < n_major; ++iex) {
+      GPoint gp{};
+      gp.band = b;
+      gp.n_abs = n_abs > 0 ? 1 : 0;
+      gp.weight = n_abs > 0 ? set_term(gp, 0, iex) : 1.0;
+      gp.iex_major = iex;
+      gp.weight_f = (float)gp.weight;
+      gpoints_keqv.push_back(gp);
+    }
+    bk.g_count = n_major;
+    for (int j = 1; j < n_abs; ++j) {
+      bk.minor_first[j] = (int)minor.size();
+      bk.minor_count[j] = nk[j];
+      const int g = bi.gas[j].species;
+      for (int iex = 0; iex < nk[j]; ++iex) {
+        TermK t{};
+        const size_t q = (size_t)iex + (size_t)d->nd_k_term * ((size_t)b + (size_t)d->nd_band * g);
+        t.iex = iex;
+        t.k = d->k[q]; t.w = d->w[q];
+        t.kf = (float)t.k; t.wf = (float)t.w;
+        t.lk_off = lookup_block(b, g, iex, bi.gas[j].i_scale_fnc);
+        const int nv = d->nd_scale_variable < 4 ? d->nd_scale_variable : 4;
+        for (int v = 0; v < nv; ++v) {
+          t.scale[v] = d->scale[(size_t)v + (size_t)d->nd_scale_variable * q];
+          t.scale_f[v] = (float)t.scale[v];
+        }
+        minor.push_back(t);
+      }
+    }
+    bands_keqv.push_back(bk);
+  }
+  if ((long long)gpoints_keqv.size() > SOCGPU_MAX_GPOINT) {
+    set_msg(msg, msg_len, "more than %d k-terms of major absorbers", SOCGPU_MAX_GPOINT);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  if (!random_ok) {
+    e.gpoints_host.clear();
+    for (auto &bb : e.bands_host) { bb.g_first = 0; bb.g_count = 0; }
   }
   SpectrumDev &s = e.dev;
   s.n_band = d->n_band;
@@ -215,6 +341,62 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   s.index_water = d->index_water;
   for (int b = 0; b < d->n_band; ++b) s.host_first_g[b] = e.bands_host[b].g_first;
   s.host_first_g[d->n_band] = s.n_gpoint;
+  s.random_ok = random_ok;
+  s.n_gpoint_keqv = (int)gpoints_keqv.size();
+  for (int b = 0; b < d->n_band; ++b) s.host_first_g_keqv[b] = bands_keqv[b].g_first;
+  s.host_first_g_keqv[d->n_band] = s.n_gpoint_keqv;
+  // lookup grids: ln p [n_pre], T [n_pre][n_tmp], gas fractions [n_gf]
+  std::vector<double> grid;
+  s.has_lookup = any_lookup;
+  if (any_lookup) {
+    s.lk_n_pre = n_pre; s.lk_n_tmp = n_tmp;
+    grid.assign(d->p_lookup, d->p_lookup + n_pre);
+    grid.insert(grid.end(), d->t_lookup, d->t_lookup + (size_t)n_tmp * n_pre);
+    if (sb_tables) {
+      s.lk_n_gf = d->n_gas_frac;
+      grid.insert(grid.end(), d->gf_lookup, d->gf_lookup + d->n_gas_frac);
+      // gas fractions (inter_pt_lookup.F90:198-230): molar weights of the
+      // self-broadened absorbers and of water vapour
+      s.n_sb = 0;
+      s.l_water = 0;
+      int iw = -1;
+      for (int g = 0; g < d->n_absorb; ++g)
+        if (d->type_absorb[g] == 1) { s.l_water = 1; if (iw < 0) iw = g; }
+      const double mw_air = 28.966e-03;
+      const double mw_w = (iw >= 0 && d->molar_weight && d->molar_weight[iw] > 0.0) ? d->molar_weight[iw] : 18.0153;
+      s.ratio_water = mw_air / (mw_w * 1.0e-03);
+      for (int g = 0; g < d->n_absorb; ++g) {
+        const int jsb = d->index_sb[g] - 1;
+        if (jsb < 0) continue;
+        if (jsb >= kMaxSb || !d->molar_weight || !(d->molar_weight[g] > 0.0)) {
+          set_msg(msg, msg_len, "self-broadened absorber %d: index above %d or no molar weight", g + 1, kMaxSb);
+          return SOCGPU_I_ERR_RANGE;
+        }
+        s.sb_species[jsb] = g;
+        s.sb_ratio_gas[jsb] = mw_air / (d->molar_weight[g] * 1.0e-03);
+        s.n_sb = std::max(s.n_sb, jsb + 1);
+      }
+    }
+  }
+  std::vector<double> tgas;
+  bool any_t = false;
+  for (int g = 0; g < d->n_absorb && d->n_t_lookup_gas; ++g) any_t |= d->n_t_lookup_gas[g] > 1;
+  if (any_t) {
+    s.nd_t_lookup_gas = d->nd_t_lookup_gas;
+    tgas.assign(d->t_lookup_gas, d->t_lookup_gas + (size_t)d->nd_t_lookup_gas * d->n_absorb);
+  }
+  // Wen-Yi tables: plg[26], ttb[10], tto[9], gk250b[n4], gk4[10][26][n4] (Fortran order), gk6[9][26][n6]
+  std::vector<double> wy;
+  if (d->wenyi_plg) {
+    s.wenyi_n4 = (d->wenyi_gk4 && d->wenyi_gk250b && d->wenyi_ttb) ? d->wenyi_n_term4 : 0;
+    s.wenyi_n6 = (d->wenyi_gk6 && d->wenyi_tto) ? d->wenyi_n_term6 : 0;
+    wy.assign(d->wenyi_plg, d->wenyi_plg + 26);
+    for (int q = 0; q < 10; ++q) wy.push_back(s.wenyi_n4 ? d->wenyi_ttb[q] : 0.0);
+    for (int q = 0; q < 9; ++q) wy.push_back(s.wenyi_n6 ? d->wenyi_tto[q] : 0.0);
+    for (int q = 0; q < s.wenyi_n4; ++q) wy.push_back(d->wenyi_gk250b[q]);
+    if (s.wenyi_n4) wy.insert(wy.end(), d->wenyi_gk4, d->wenyi_gk4 + (size_t)260 * s.wenyi_n4);
+    if (s.wenyi_n6) wy.insert(wy.end(), d->wenyi_gk6, d->wenyi_gk6 + (size_t)234 * s.wenyi_n6);
+  }
   // cloud parameter sets
   std::vector<double> drop, ice;
   s.n_drop_type = (d->drop_parm_list && d->nd_drop_type > 0) ? d->nd_drop_type : 0;
@@ -237,6 +419,22 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
             d->ice_parm_list[(size_t)c + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * t)];
   std::vector<float> drop_f(drop.begin(), drop.end()), ice_f(ice.begin(), ice.end());
   cudaGetDevice(&e.device);
+  // the tables of lookup scaling, equivalent extinction and Wen-Yi scaling
+  auto up = [&](auto *&dst, const auto &v) -> bool {
+    using T = typename std::decay_t<decltype(v)>::value_type;
+    if (v.empty()) { dst = nullptr; return true; }
+    if (cudaMalloc((void **)&dst, sizeof(T) * v.size()) != cudaSuccess) return false;
+    return cudaMemcpy(dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  std::vector<float> grid_f(grid.begin(), grid.end()), k_lk_f(k_lk.begin(), k_lk.end());
+  std::vector<float> tgas_f(tgas.begin(), tgas.end()), wy_f(wy.begin(), wy.end());
+  if (!up(s.bands_keqv, bands_keqv) || !up(s.gpoints_keqv, gpoints_keqv) || !up(s.minor_terms, minor) ||
+      !up(s.lk_grid, grid) || !up(s.lk_grid_f, grid_f) || !up(s.k_lookup, k_lk) || !up(s.k_lookup_f, k_lk_f) ||
+      !up(s.t_lookup_gas, tgas) || !up(s.t_lookup_gas_f, tgas_f) || !up(s.wenyi, wy) || !up(s.wenyi_f, wy_f)) {
+    cudaGetLastError();
+    set_msg(msg, msg_len, "device allocation or upload of lookup and overlap tables failed");
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
   if (cudaMalloc(&s.bands, sizeof(BandInfo) * s.n_band) != cudaSuccess ||
       cudaMalloc(&s.gpoints, sizeof(GPoint) * std::max(1, s.n_gpoint)) != cudaSuccess ||
       cudaMalloc(&s.drop_parm, sizeof(double) * drop.size()) != cudaSuccess ||
@@ -263,6 +461,17 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
 }
 
 void free_spectrum(SpectrumEntry &e) {
+  cudaFree(e.dev.bands_keqv);
+  cudaFree(e.dev.gpoints_keqv);
+  cudaFree(e.dev.minor_terms);
+  cudaFree(e.dev.lk_grid);
+  cudaFree(e.dev.lk_grid_f);
+  cudaFree(e.dev.k_lookup);
+  cudaFree(e.dev.k_lookup_f);
+  cudaFree(e.dev.t_lookup_gas);
+  cudaFree(e.dev.t_lookup_gas_f);
+  cudaFree(e.dev.wenyi);
+  cudaFree(e.dev.wenyi_f);
   cudaFree(e.dev.bands);
   cudaFree(e.dev.gpoints);
   cudaFree(e.dev.drop_parm);
@@ -346,8 +555,15 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     set_msg(msg, msg_len, "only two-stream angular integration is supported"); return SOCGPU_I_ERR_FATAL; }
   if (c->isolir != SOCGPU_IP_SOLAR && c->isolir != SOCGPU_IP_INFRA_RED) {
     set_msg(msg, msg_len, "isolir must be solar or infra-red"); return SOCGPU_I_ERR_FATAL; }
-  if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_RANDOM) {
-    set_msg(msg, msg_len, "only random gas overlap is supported"); return SOCGPU_I_ERR_FATAL; }
+  if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_RANDOM && !is_keqv(c)) {
+    set_msg(msg, msg_len, "only random and equivalent-extinction gas overlaps are supported");
+    return SOCGPU_I_ERR_FATAL;
+  }
+  if (c->i_gas_overlap == SOCGPU_IP_OVERLAP_RANDOM && !sp->dev.random_ok) {
+    set_msg(msg, msg_len, "random overlap of this spectrum needs more than %d k-term products; "
+            "use equivalent extinction (i_gas_overlap 4)", SOCGPU_MAX_GPOINT);
+    return SOCGPU_I_ERR_RANGE;
+  }
   switch (c->i_2stream) {
     case SOCGPU_IP_EDDINGTON: case SOCGPU_IP_ELSASSER: case SOCGPU_IP_DISCRETE_ORD: case SOCGPU_IP_PIFM85:
     case SOCGPU_IP_2S_TEST: case SOCGPU_IP_HEMI_MEAN: case SOCGPU_IP_PIFM80: break;
@@ -461,12 +677,37 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
   p.n_profile = atm->n_profile; p.n_layer = atm->n_layer;
   p.nd_profile = dm->nd_profile; p.nd_layer = dm->nd_layer;
   p.id_ct = (p.mcica ? dm->id_cloud_top : 1) - 1;
-  p.g_begin = sp->dev.host_first_g[c->first_band - 1];
-  p.g_end = sp->dev.host_first_g[c->last_band];
+  p.keqv = is_keqv(c);
+  p.l_grey_single = c->l_grey_single;
+  const int *first_g = p.keqv ? sp->dev.host_first_g_keqv : sp->dev.host_first_g;
+  p.g_begin = first_g[c->first_band - 1];
+  p.g_end = first_g[c->last_band];
   p.max_abs = 1;
   for (int b = c->first_band - 1; b < c->last_band; ++b)
     p.max_abs = std::max(p.max_abs, c->l_gas ? sp->bands_host[b].n_abs : 0);
-  p.bands = sp->dev.bands; p.gpoints = sp->dev.gpoints;
+  p.bands = p.keqv ? sp->dev.bands_keqv : sp->dev.bands;
+  p.gpoints = p.keqv ? sp->dev.gpoints_keqv : sp->dev.gpoints;
+  p.minor_terms = sp->dev.minor_terms;
+  // lookup tables (staged per column only when a band of the range uses them)
+  const SpectrumDev &sd = sp->dev;
+  bool lk = false;
+  if (c->l_gas && sd.has_lookup)
+    for (int b = c->first_band - 1; b < c->last_band; ++b)
+      for (int j = 0; j < sp->bands_host[b].n_abs; ++j)
+        lk |= sp->bands_host[b].gas[j].i_scale_fnc == SOCGPU_IP_SCALE_LOOKUP;
+  p.lk_on = lk;
+  bool term = p.keqv;
+  if (c->l_gas)
+    for (int b = c->first_band - 1; b < c->last_band; ++b)
+      for (int j = 0; j < sp->bands_host[b].n_abs; ++j)
+        term |= sp->bands_host[b].gas[j].i_scale_k == SOCGPU_IP_SCALE_TERM;
+  p.term_scr = term;
+  p.lk_n_pre = sd.lk_n_pre; p.lk_n_tmp = sd.lk_n_tmp; p.lk_n_gf = sd.lk_n_gf; p.n_sb = lk ? sd.n_sb : 0;
+  p.lk_grid = sd.lk_grid; p.lk_grid_f = sd.lk_grid_f; p.k_lookup = sd.k_lookup; p.k_lookup_f = sd.k_lookup_f;
+  for (int q = 0; q < kMaxSb; ++q) { p.sb_species[q] = sd.sb_species[q]; p.sb_ratio_gas[q] = sd.sb_ratio_gas[q]; }
+  p.ratio_water = sd.ratio_water; p.l_water = sd.l_water;
+  p.nd_t_lookup_gas = sd.nd_t_lookup_gas; p.t_lookup_gas = sd.t_lookup_gas; p.t_lookup_gas_f = sd.t_lookup_gas_f;
+  p.wenyi_n4 = sd.wenyi_n4; p.wenyi_n6 = sd.wenyi_n6; p.wenyi = sd.wenyi; p.wenyi_f = sd.wenyi_f;
   p.drop_parm = sp->dev.drop_parm; p.ice_parm = sp->dev.ice_parm;
   p.drop_parm_f = sp->dev.drop_parm_f; p.ice_parm_f = sp->dev.ice_parm_f;
   p.n_band = sp->dev.n_band; p.n_deg_fit = sp->dev.n_deg_fit; p.t_ref_planck = sp->dev.t_ref_planck;
@@ -668,7 +909,8 @@ void StagedCall::params(char *base, FluxParams &p) const {
 }
 
 long long StagedCall::column_gpoints() const {
-  const int g0 = sp->dev.host_first_g[control->first_band - 1], g1 = sp->dev.host_first_g[control->last_band];
+  const int *first_g = is_keqv(control) ? sp->dev.host_first_g_keqv : sp->dev.host_first_g;
+  const int g0 = first_g[control->first_band - 1], g1 = first_g[control->last_band];
   return (long long)atm->n_profile * (g1 - g0);
 }
 

@@ -151,17 +151,23 @@ struct SmemLayout {
   size_t off_planck, off_dB, off_dB2;
   size_t off_phf_nc, off_fwd_nc, off_c_ke, off_c_ks, off_c_ka, off_c_phf, off_c_fwd;
   size_t off_wcld, off_frac, off_csub;
+  size_t off_aux, off_lkf, off_lki, off_sbf, off_sbj, off_kscr;
   size_t off_acc;
   size_t bytes;
 };
 
+// The layout of a column of batch p: nb bands staged at a time, n_groups
+// solve groups of P lanes, LP = P*CH layer slots.
 template <class R>
-__host__ __device__ inline SmemLayout make_layout(int LP, int P, int nb, int max_abs, int n_comp, int n_sub,
-                                                  int n_groups, bool lw, bool mcica) {
+__host__ __device__ inline SmemLayout make_layout(const FluxParams &p, int LP, int P, int nb, int n_groups,
+                                                  bool mcica) {
+  const int max_abs = p.max_abs, n_comp = mcica ? p.n_condensed : 0, n_sub = mcica ? p.n_subcol_gen : 0;
+  const bool lw = p.isolir == SOCGPU_IP_INFRA_RED;
   SmemLayout s{};
   s.LP = LP; s.nb = nb; s.max_abs = max_abs; s.n_comp = n_comp; s.n_sub = n_sub; s.n_groups = n_groups;
   size_t o = 0;
   auto take = [&](size_t elems) { size_t r = (o + 15) & ~(size_t)15; o = r + elems * sizeof(R); return r; };
+  auto take_int = [&](size_t elems) { size_t r = (o + 15) & ~(size_t)15; o = r + elems * sizeof(int); return r; };
   s.off_p = take(LP);
   s.off_t = take(LP);
   s.off_mass = take(LP);
@@ -187,6 +193,15 @@ __host__ __device__ inline SmemLayout make_layout(int LP, int P, int nb, int max
     s.off_frac = take((size_t)2 * LP);
     s.off_csub = take((size_t)n_sub * LP);
   }
+  // equivalent extinction, solar: each minor absorber's direct-beam factor
+  s.off_aux = (p.keqv && !lw) ? take((size_t)nb * max_abs * LP) : o;
+  // lookup tables: interpolation factors and packed indices of each slot
+  s.off_lkf = p.lk_on ? take((size_t)4 * LP) : o;
+  s.off_lki = p.lk_on ? take_int(LP) : o;
+  s.off_sbf = p.n_sb > 0 ? take((size_t)p.n_sb * LP) : o;
+  s.off_sbj = p.n_sb > 0 ? take_int((size_t)p.n_sb * LP) : o;
+  // per-group scratch row for k of per-term scaled absorbers
+  s.off_kscr = p.term_scr ? take((size_t)n_groups * LP) : o;
   // per-group accumulator slices, offset by P words mod 32 so that the
   // groups of one warp land on different banks
   const int words = (int)(sizeof(R) / 4);
@@ -332,6 +347,8 @@ struct FluxKernel {
   struct Smem {
     R *p, *t, *mass, *kgt, *kes, *kabs, *asym, *fwd, *amt, *bscal, *planck, *dB, *dB2;
     R *phf_nc, *fwd_nc, *c_ke, *c_ks, *c_ka, *c_phf, *c_fwd, *wcld, *frac, *csub;
+    R *aux, *lkf, *sbf, *kscr;
+    int *lki, *sbj;
     Acc *acc;
   };
 
@@ -346,9 +363,179 @@ struct FluxKernel {
     s.c_ke = (R *)(smem + l.off_c_ke); s.c_ks = (R *)(smem + l.off_c_ks); s.c_ka = (R *)(smem + l.off_c_ka);
     s.c_phf = (R *)(smem + l.off_c_phf); s.c_fwd = (R *)(smem + l.off_c_fwd);
     s.wcld = (R *)(smem + l.off_wcld); s.frac = (R *)(smem + l.off_frac); s.csub = (R *)(smem + l.off_csub);
+    s.aux = (R *)(smem + l.off_aux);
+    s.lkf = (R *)(smem + l.off_lkf); s.lki = (int *)(smem + l.off_lki);
+    s.sbf = (R *)(smem + l.off_sbf); s.sbj = (int *)(smem + l.off_sbj);
+    s.kscr = (R *)(smem + l.off_kscr);
     s.acc = (Acc *)(smem + l.off_acc);
     return s;
   }
+
+  // ---------------- lookup-table k scaling ----------------------------------
+  // The staged interpolation factors of the column (passed on their own so
+  // that calls need not spill the whole shared-memory map).
+  struct Lk {
+    const R *f;                 // fac00, fac10, fac01, fac11 of each slot
+    const int *idx;             // jp | jt << 8 | jtt << 16
+    const R *sbf;               // gas-fraction weight of each self-broadened index and slot
+    const int *sbj;             // its indices jgf | jgfp1 << 8
+  };
+  __device__ static __forceinline__ Lk lk_of(const Smem &S) { return Lk{S.lkf, S.lki, S.sbf, S.sbj}; }
+  __device__ static __forceinline__ const R *lk_grid(const FluxParams &p) {
+    if constexpr (kFP64) return p.lk_grid; else return p.lk_grid_f;
+  }
+  __device__ static __forceinline__ const R *lk_table(const FluxParams &p) {
+    if constexpr (kFP64) return p.k_lookup; else return p.k_lookup_f;
+  }
+  // Largest index k in 0..n-2 with tab[k] <= x (MINLOC of the non-negative
+  // differences in inter_pt_lookup.F90, for increasing tables).
+  __device__ static __forceinline__ int below(const R *tab, int n, R x) {
+    int lo = 0, hi = n - 2;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab[mid] <= x) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+  }
+  // Interpolation factors of slot s (inter_pt_lookup.F90:146-268): pressure
+  // and temperature weights and indices, and the gas fractions of the
+  // self-broadened absorbers.
+  __device__ static __forceinline__ void lookup_slot(const FluxParams &p, R *lkf, int *lki, R *sbf, int *sbj, R pv,
+                                                  R tv, int col, int s, int i) {
+    const R eps = kFP64 ? (R)kEps64 : R(0);
+    const int npre = p.lk_n_pre, ntmp = p.lk_n_tmp;
+    const R *g = lk_grid(p), *tt = g + npre;
+    const R lo_p = g[0] + fmax(fabs(g[0]) * eps, eps), hi_p = g[npre - 1] - fmax(fabs(g[npre - 1]) * eps, eps);
+    R x = log(pv);
+    x = fmin(fmax(x, lo_p), hi_p);
+    const int jp = below(g, npre, x);
+    const R fp = (x - g[jp]) / (g[jp + 1] - g[jp]);
+    const R *t0 = tt + (size_t)ntmp * jp, *t1 = t0 + ntmp;
+    R tl = fmin(fmax(tv, t0[0] * (R(1) + eps)), t0[ntmp - 1] * (R(1) - eps));
+    const int jt = below(t0, ntmp, tl);
+    const R ft = (tl - t0[jt]) / (t0[jt + 1] - t0[jt]);
+    tl = fmin(fmax(tv, t1[0] * (R(1) + eps)), t1[ntmp - 1] * (R(1) - eps));
+    const int jtt = below(t1, ntmp, tl);
+    const R ftt = (tl - t1[jtt]) / (t1[jtt + 1] - t1[jtt]);
+    const R compfp = R(1) - fp;
+    lkf[s] = compfp * (R(1) - ft);
+    lkf[LP + s] = fp * (R(1) - ftt);
+    lkf[2 * LP + s] = compfp * ft;
+    lkf[3 * LP + s] = fp * ftt;
+    lki[s] = jp | (jt << 8) | (jtt << 16);
+    if (p.n_sb > 0) {
+      const int ngf = p.lk_n_gf;
+      const R *gf = tt + (size_t)ntmp * npre;
+      const R lo_g = gf[0] + fmax(gf[0] * eps, eps), hi_g = gf[ngf - 1] - fmax(gf[ngf - 1] * eps, eps);
+      const size_t base = (size_t)col + (size_t)p.nd_profile * i;
+      const size_t stride = (size_t)p.nd_profile * p.nd_layer;
+      const R q = p.l_water ? load_in<R>(p.gas_mix_ratio + base + stride * (p.i_water >= 0 ? p.i_water : 0)) : R(0);
+      for (int k = 0; k < p.n_sb; ++k) {
+        const R mr = load_in<R>(p.gas_mix_ratio + base + stride * p.sb_species[k]);
+        const R rg = (R)p.sb_ratio_gas[k], rw = (R)p.ratio_water;
+        R v;
+        if (!p.l_water) v = mr * rg;
+        else if (p.l_mixing_ratio) v = mr * rg / (R(1) + q * rw);
+        else v = mr * rg / (R(1) + q * (rw - R(1)));
+        if (ngf == 1) {
+          sbf[(size_t)k * LP + s] = R(1);
+          sbj[(size_t)k * LP + s] = 0;
+        } else {
+          v = fmin(fmax(v, lo_g), hi_g);
+          const int jg = below(gf, ngf, v);
+          sbf[(size_t)k * LP + s] = R(1) - (v - gf[jg]) / (gf[jg + 1] - gf[jg]);
+          sbj[(size_t)k * LP + s] = jg | ((jg + 1) << 8);
+        }
+      }
+    }
+  }
+  // k of one term from the P/T tables (radiance_calc.F90:1097-1145), times
+  // the absorber amount a.
+  __device__ static __forceinline__ R lookup_k(const FluxParams &p, Lk lk, int off, int sb, int s, R a) {
+    const R *K = lk_table(p) + off;
+    const int nt = p.lk_n_tmp, idx = lk.idx[s];
+    const int jp = idx & 255, jt = (idx >> 8) & 255, jtt = idx >> 16;
+    const R f00 = lk.f[s], f10 = lk.f[LP + s], f01 = lk.f[2 * LP + s], f11 = lk.f[3 * LP + s];
+    const int i00 = jt + nt * jp, i10 = jtt + nt * (jp + 1), i01 = jt + 1 + nt * jp, i11 = jtt + 1 + nt * (jp + 1);
+    R ke;
+    if (sb < 0) {
+      ke = f00 * K[i00] + f10 * K[i10] + f01 * K[i01] + f11 * K[i11];
+    } else {
+      const int jj = lk.sbj[(size_t)sb * LP + s];
+      const R fg = lk.sbf[(size_t)sb * LP + s];
+      const R *K0 = K + (size_t)nt * p.lk_n_pre * (jj & 255), *K1 = K + (size_t)nt * p.lk_n_pre * (jj >> 8);
+      ke = fg * (f00 * K0[i00] + f10 * K0[i10] + f01 * K0[i01] + f11 * K0[i11])
+         + (R(1) - fg) * (f00 * K1[i00] + f10 * K1[i10] + f01 * K1[i01] + f11 * K1[i11]);
+    }
+    ke = ke > R(0) ? ke : R(0);
+    R v = ke * a;
+    v = v > R(0) ? v : R(0);
+    // unfilled table entries (about 1e37) would overflow FP32 optical depths;
+    // any k this large already makes the layer opaque
+    if constexpr (!kFP64) v = fminf(v, 1.0e30f);
+    return v;
+  }
+  // k of one term from a temperature-only table (inter_t_lookup.F90:70-86,
+  // radiance_calc.F90:1154-1166), times the absorber amount a.
+  __device__ static __forceinline__ R t_lookup_k(const FluxParams &p, const BandGas &gs, int off, R tl, R a) {
+    const R eps = kFP64 ? (R)kEps64 : R(0);
+    const R *tg;
+    const R *K;
+    if constexpr (kFP64) { tg = p.t_lookup_gas; K = p.k_lookup; } else { tg = p.t_lookup_gas_f; K = p.k_lookup_f; }
+    tg += (size_t)p.nd_t_lookup_gas * gs.species;
+    K += off;
+    const int n = gs.n_t;
+    const R t = fmin(fmax(tl, tg[0] * (R(1) + eps)), tg[n - 1] * (R(1) - eps));
+    const int jt = below(tg, n, t);
+    const R wt = R(1) - (t - tg[jt]) / (tg[jt + 1] - tg[jt]);
+    R ke = wt * K[jt] + (R(1) - wt) * K[jt + 1];
+    ke = ke > R(0) ? ke : R(0);
+    const R v = ke * a;
+    return v > R(0) ? v : R(0);
+  }
+  // Wen-Yi Zhong's scaling of the CO2 (band 4) and O3 (band 6) terms
+  // (scale_absorb.F90:238-281); b is the 0-based band.
+  __device__ static __forceinline__ R wenyi_factor(const FluxParams &p, int b, int iex, R pl, R tl) {
+    const R *W;
+    if constexpr (kFP64) W = p.wenyi; else W = p.wenyi_f;
+    const R *plg = W, *ttb = W + 26, *tto = W + 36, *gk250b = W + 45;
+    const R *gk4 = gk250b + p.wenyi_n4, *gk6 = gk4 + (size_t)260 * p.wenyi_n4;
+    R cgp = log(pl / R(100));
+    if (cgp < R(-5.5)) cgp = R(-5.5);
+    int jp = (int)((R(5.5) + cgp) * R(2)) + 1;
+    jp = jp < 1 ? 1 : (jp > 26 ? 26 : jp);
+    const int jp1 = jp + 1 < 26 ? jp + 1 : 26;
+    const bool b4 = (b == 3);
+    const int n_t = b4 ? 10 : 9;
+    const R *gk = b4 ? gk4 : gk6, *tref = b4 ? ttb : tto;
+    int jt = (int)((tl - R(240)) / R(20) + (b4 ? R(7) : R(5)));
+    jt = jt < 1 ? 1 : (jt > n_t ? n_t : jt);
+    const int jt1 = jt + 1 < n_t ? jt + 1 : n_t;
+    auto G = [&](int a, int c) { return gk[(size_t)(a - 1) + (size_t)n_t * ((size_t)(c - 1) + (size_t)26 * iex)]; };
+    const R dp = (cgp - plg[jp - 1]) * R(2);
+    const R gkpb = G(jt, jp) + (G(jt, jp1) - G(jt, jp)) * dp;
+    const R gkpc = G(jt1, jp) + (G(jt1, jp1) - G(jt1, jp)) * dp;
+    const R v = gkpb + (gkpc - gkpb) * (tl - tref[jt - 1]) / R(20);
+    return b4 ? v / gk250b[iex] : v;
+  }
+  // k of one term of absorber gs at slot s (k_abs_layer of
+  // radiance_calc.F90:1330-1470): a is the staged amount (the scaled amount
+  // under ip_scale_band, the mixing ratio otherwise), kj the term's k, sc its
+  // scaling parameters, lk_off its lookup table, iex the term.
+  __device__ static __forceinline__ R term_k(const FluxParams &p, Lk lk, const BandGas &gs, int b, R kj, const R *sc,
+                             int lk_off, int iex, R a, int s, R pl, R tl) {
+    if (gs.i_scale_k != SOCGPU_IP_SCALE_TERM) return kj * a;
+    const int fnc = gs.i_scale_fnc;
+    if (fnc == SOCGPU_IP_SCALE_LOOKUP) return lookup_k(p, lk, lk_off, gs.sb, s, a);
+    if (fnc == SOCGPU_IP_SCALE_T_LOOKUP) return t_lookup_k(p, gs, lk_off, tl, a);
+    R gf;
+    if (fnc == SOCGPU_IP_SCALE_WENYI) gf = wenyi_factor(p, b, iex, pl, tl);
+    else if constexpr (kFP64) gf = scale_factor_ref(fnc, pl, tl, gs.p_ref, gs.t_ref, sc, gs.l_doppler, gs.doppler_cor);
+    else gf = scale_factor_mix(fnc, pl, tl, gs.p_ref_f, gs.t_ref_f, sc, gs.l_doppler, gs.doppler_cor_f);
+    const R v = gf * a;
+    return kj * (v > R(0) ? v : R(0));
+  }
+
 
   __device__ static void run(const FluxParams &p, const int col) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -359,8 +546,7 @@ struct FluxKernel {
     const int n_groups = nthreads / P;
     constexpr bool lw = (SRC == SOCGPU_IP_INFRA_RED);
     const int max_abs = p.max_abs;
-    const SmemLayout lay = make_layout<R>(LP, P, nbat, max_abs, MCICA ? p.n_condensed : 0,
-                                         MCICA ? p.n_subcol_gen : 0, n_groups, lw, MCICA);
+    const SmemLayout lay = make_layout<R>(p, LP, P, nbat, n_groups, MCICA);
     const Smem S = bind(smem, lay);
     const int ndp = p.nd_profile;
 
@@ -371,6 +557,7 @@ struct FluxKernel {
         S.p[s] = load_in<R>(p.p + (size_t)col + (size_t)ndp * i);
         S.t[s] = load_in<R>(p.t + (size_t)col + (size_t)ndp * i);
         S.mass[s] = load_in<R>(p.mass + (size_t)col + (size_t)ndp * i);
+        if (p.lk_on) lookup_slot(p, S.lkf, S.lki, S.sbf, S.sbj, S.p[s], S.t[s], col, s, i);
       }
     }
     for (int q = threadIdx.x; q < n_groups * lay.acc_stride; q += nthreads) S.acc[q] = Acc(0);
@@ -389,6 +576,12 @@ struct FluxKernel {
       __syncthreads();
       stage_boundary(p, S, col, bstart, nb, lw);
       __syncthreads();
+      if (p.keqv) {
+        stage_keqv(p, S, bstart, nb, sec0);
+        __syncthreads();
+        fold_keqv(p, S, bstart, nb, sec0);
+        __syncthreads();
+      }
       // g-point solves.  Every group of every warp runs the same number of
       // rounds so that the full-warp shuffles of the scans always see all
       // 32 lanes; a group with no g-point left in the last round solves the
@@ -719,43 +912,309 @@ struct FluxKernel {
     return t;
   }
 
-  // Gas absorption of a g-point at slot s (gas_optical_properties.F90:80-95).
-  __device__ static __forceinline__ R gas_k(const GasTerm &gt, const GPoint &gp, const BandInfo &bd,
-                                            const R *amt, int s, R pl, R tl) {
+  // Gas absorption of a g-point at slot s (gas_optical_properties.F90:80-95)
+  // when no absorber of the band is scaled per term.
+  __device__ static __forceinline__ R gas_k(const GasTerm &gt, const R *amt, int s) {
+    // one absorber (the common case) without the guarded loop
+    if (gt.n_abs == 1) return gt.k[0] * amt[s];
     R kg = R(0);
-    if (!gt.any_term) {
-      // one absorber (the common case) without the guarded loop
-      if (gt.n_abs == 1) return gt.k[0] * amt[s];
 #pragma unroll
-      for (int j = 0; j < kMaxAbsPerBand; ++j)
-        if (j < gt.n_abs) {
-          R kal = gt.k[j] * amt[(size_t)j * LP + s];
+    for (int j = 0; j < kMaxAbsPerBand; ++j)
+      if (j < gt.n_abs) {
+        R kal = gt.k[j] * amt[(size_t)j * LP + s];
+        kg = (j == 0) ? kal : kg + kal;
+      }
+    return kg;
+  }
+
+  // Gas absorption of a g-point in the lane's layers when an absorber is
+  // scaled per term (power laws per term, Wen-Yi or lookup tables), written
+  // to the group's scratch row.  The layer loop stays rolled so that the
+  // table code appears once, without calls.
+  __device__ static __forceinline__ void gas_k_terms(const FluxParams &p, const Smem &S, const GPoint &gp,
+                                                     const BandInfo &bd, int n_abs, const R *amt, int r, int L,
+                                                     R *scr) {
+    const Lk lk = lk_of(S);
+#pragma unroll 1
+    for (int jj = 0; jj < CH; ++jj) {
+      const int i = r * CH + jj, s = jj * P + r;
+      R kg = R(0);
+      if (i < L) {
+        for (int j = 0; j < n_abs; ++j) {
+          const R kj = kFP64 ? (R)gp.k[j] : (R)gp.kf[j];
+          const R *sc;
+          if constexpr (kFP64) sc = gp.term_scale[j]; else sc = gp.term_scale_f[j];
+          const R kal = term_k(p, lk, bd.gas[j], gp.band, kj, sc, gp.lk_off[j], gp.iex[j], amt[(size_t)j * LP + s],
+                               s, S.p[s], S.t[s]);
           kg = (j == 0) ? kal : kg + kal;
         }
-      return kg;
-    }
-    // per-term scaling: a rolled loop; k comes from the g-point table (a
-    // broadcast load) so that the register copy is never indexed dynamically
-    for (int j = 0; j < gt.n_abs; ++j) {
-      R a = amt[(size_t)j * LP + s];
-      R kal;
-      const R kj = kFP64 ? (R)gp.k[j] : (R)gp.kf[j];
-      if (bd.gas[j].i_scale_k == SOCGPU_IP_SCALE_TERM) {
-        R gf;
-        if constexpr (kFP64)
-          gf = scale_factor_ref(bd.gas[j].i_scale_fnc, pl, tl, bd.gas[j].p_ref, bd.gas[j].t_ref, gp.term_scale[j],
-                                bd.gas[j].l_doppler, bd.gas[j].doppler_cor);
-        else
-          gf = scale_factor_mix(bd.gas[j].i_scale_fnc, pl, tl, bd.gas[j].p_ref_f, bd.gas[j].t_ref_f,
-                                gp.term_scale_f[j], bd.gas[j].l_doppler, bd.gas[j].doppler_cor_f);
-        R v = gf * a;
-        kal = kj * (v > R(0) ? v : R(0));
-      } else {
-        kal = kj * a;
       }
-      kg = (j == 0) ? kal : kg + kal;
+      scr[s] = kg;
     }
-    return kg;
+  }
+
+  // The gas absorption of a g-point in the lane's layers.
+  __device__ static __forceinline__ void gas_k_lane(const FluxParams &p, const Smem &S, const GasTerm &gt,
+                                                    const GPoint &gp, const BandInfo &bd, const R *amt, int r, int L,
+                                                    R (&kgv)[CH]) {
+    if (p.l_gas && gt.any_term) {
+      R *scr = S.kscr + (size_t)(threadIdx.x / P) * LP;
+      gas_k_terms(p, S, gp, bd, gt.n_abs, amt, r, L, scr);
+#pragma unroll
+      for (int jj = 0; jj < CH; ++jj) kgv[jj] = scr[jj * P + r];
+    } else {
+#pragma unroll
+      for (int jj = 0; jj < CH; ++jj) {
+        const int i = r * CH + jj, s = jj * P + r;
+        kgv[jj] = (i < L && p.l_gas) ? gas_k(gt, amt, s) : R(0);
+      }
+    }
+  }
+
+  // k of one k-term of one absorber in the lane's layers, into registers
+  // through the group's scratch row (as gas_k_terms).
+  __device__ static __forceinline__ void term_k_lane(const FluxParams &p, const Smem &S, const BandGas &gs, int b,
+                                                     R kj, const R *sc, int lk_off, int iex, const R *amt, int r,
+                                                     int L, R (&kk)[CH]) {
+    R *scr = S.kscr + (size_t)(threadIdx.x / P) * LP;
+    const Lk lk = lk_of(S);
+#pragma unroll 1
+    for (int jj = 0; jj < CH; ++jj) {
+      const int i = r * CH + jj, s = jj * P + r;
+      scr[s] = (i < L) ? term_k(p, lk, gs, b, kj, sc, lk_off, iex, amt[s], s, S.p[s], S.t[s]) : R(0);
+    }
+#pragma unroll
+    for (int jj = 0; jj < CH; ++jj) kk[jj] = scr[jj * P + r];
+  }
+
+  // ---------------- equivalent extinction (k_eqv_scl) ------------------------
+  // Minor absorber j of staged band bi, solved by one group of P lanes
+  // (solve_band_k_eqv_scl.F90:560-1040, two-stream, plane parallel).  Its
+  // k-terms are weighted by the fluxes they leave: the direct flux reaching
+  // the surface (solar), or the fluxes incident on each layer from a
+  // scattering-free solve with diffusivity 1.66 (monochromatic_gas_flux.F90,
+  // infra-red).  The absorber's share of k_eqv replaces its staged amount;
+  // under the solar source its direct-beam factor goes to aux.  gm is the
+  // group's lane mask: groups of one warp may run different absorbers.
+  __device__ static __forceinline__ void minor_gas(const FluxParams &p, const Smem &S, int bi, int b, int j, R sec0,
+                                                int r, unsigned gm) {
+    constexpr bool lw = (SRC == SOCGPU_IP_INFRA_RED);
+    const int L = p.n_layer, max_abs = p.max_abs;
+    const BandInfo &bd = p.bands[b];
+    const BandGas &gs = bd.gas[j];
+    R *amt = S.amt + ((size_t)bi * max_abs + j) * LP;
+    const int t0 = bd.minor_first[j], nt = bd.minor_count[j];
+    // infra-red: sfl, the flux weights; solar: fg, the direct flux of the
+    // absorber alone at each layer's bottom, and (FP32, in the absorber's
+    // aux row) the flux it loses in each layer, summed without cancellation
+    R skf[CH], sfl[CH], kmin[CH], fg[CH];
+    R sfs = R(0);
+    R *loss = S.aux + ((size_t)bi * max_abs + j) * LP;
+#pragma unroll
+    for (int jj = 0; jj < CH; ++jj) {
+      skf[jj] = R(0); sfl[jj] = R(0); fg[jj] = R(0); kmin[jj] = R(3.0e38);
+      if constexpr (!lw && !kFP64) loss[jj * P + r] = R(0);
+    }
+    if (lw && nt == 1 && p.l_grey_single) {
+      // a single-term minor absorber as a grey absorber (l_grey_single)
+      const TermK &tk = p.minor_terms[t0];
+      const R *sc;
+      if constexpr (kFP64) sc = tk.scale; else sc = tk.scale_f;
+      R kk[CH];
+      term_k_lane(p, S, gs, b, kFP64 ? (R)tk.k : (R)tk.kf, sc, tk.lk_off, tk.iex, amt, r, L, kk);
+#pragma unroll
+      for (int jj = 0; jj < CH; ++jj) {
+        const int i = r * CH + jj, s = jj * P + r;
+        if (i < L) amt[s] = kk[jj];
+      }
+      return;
+    }
+    const R *bs = S.bscal + bi * kBandScal;
+    const R *dB_b = S.dB + (size_t)bi * LP;
+    for (int t = 0; t < nt; ++t) {
+      const TermK &tk = p.minor_terms[t0 + t];
+      const R kj = kFP64 ? (R)tk.k : (R)tk.kf, we = kFP64 ? (R)tk.w : (R)tk.wf;
+      const R *sc;
+      if constexpr (kFP64) sc = tk.scale; else sc = tk.scale_f;
+      R kk[CH];
+      term_k_lane(p, S, gs, b, kj, sc, tk.lk_off, tk.iex, amt, r, L, kk);
+#pragma unroll
+      for (int jj = 0; jj < CH; ++jj)
+        if (r * CH + jj < L) kmin[jj] = kk[jj] < kmin[jj] ? kk[jj] : kmin[jj];
+      if constexpr (!lw) {
+        // direct beam of this term alone: an exclusive product scan
+        R e[CH], prod = R(1);
+#pragma unroll
+        for (int jj = 0; jj < CH; ++jj) {
+          const int i = r * CH + jj, s = jj * P + r;
+          if (i < L) {
+            if constexpr (kFP64) e[jj] = exp(-kk[jj] * S.mass[s] * sec0);
+            else e[jj] = expf(-kk[jj] * S.mass[s] * sec0);
+          } else {
+            e[jj] = R(1);
+          }
+          prod *= e[jj];
+        }
+        R incl = prod;
+#pragma unroll
+        for (int d = 1; d < P; d <<= 1) {
+          const R y = __shfl_up_sync(gm, incl, d, P);
+          if (r >= d) incl = y * incl;
+        }
+        R f = __shfl_up_sync(gm, incl, 1, P);
+        if (r == 0) f = R(1);
+        f = we * f;
+        const R f_surf = we * __shfl_sync(gm, incl, P - 1, P);
+#pragma unroll
+        for (int jj = 0; jj < CH; ++jj) {
+          if constexpr (!kFP64) {
+            const int s = jj * P + r;
+            if (r * CH + jj < L) loss[s] += f * -expm1f(-kk[jj] * S.mass[s] * sec0);
+          }
+          f = f * e[jj];
+          fg[jj] += f;
+          skf[jj] += kk[jj] * f_surf;
+        }
+        sfs += f_surf;
+      } else {
+        // monochromatic_gas_flux.F90:100-197: downward then upward affine scans
+        R T[CH], su[CH];
+#pragma unroll
+        for (int jj = 0; jj < CH; ++jj) {
+          const int i = r * CH + jj, s = jj * P + r;
+          if (i < L) {
+            R c1;
+            if constexpr (kFP64) { Coef c = fast_lw_ref(0, kk[jj] * S.mass[s]); T[jj] = c.T; c1 = c.c1; }
+            else { CoefF c = fast_lw_mix(0, kk[jj] * S.mass[s]); T[jj] = c.T; c1 = c.c1; }
+            su[jj] = c1 * dB_b[s];
+          } else {
+            T[jj] = R(1); su[jj] = R(0);
+          }
+        }
+        R A = R(1), B = R(0);
+#pragma unroll
+        for (int jj = 0; jj < CH; ++jj) { A = T[jj] * A; B = T[jj] * B - su[jj]; }
+        R iA = A, iB = B;
+#pragma unroll
+        for (int d = 1; d < P; d <<= 1) {
+          const R yA = __shfl_up_sync(gm, iA, d, P), yB = __shfl_up_sync(gm, iB, d, P);
+          if (r >= d) { iB = iA * yB + iB; iA = iA * yA; }
+        }
+        R eA = __shfl_up_sync(gm, iA, 1, P), eB = __shfl_up_sync(gm, iB, 1, P);
+        if (r == 0) { eA = R(1); eB = R(0); }
+        const R f_top = bs[0];
+        const R fdn_top = eA * f_top + eB;
+        const R fdn_surf = __shfl_sync(gm, iA, P - 1, P) * f_top + __shfl_sync(gm, iB, P - 1, P);
+        const R fup_surf = bs[4] + bs[2] * fdn_surf;
+        R C = R(1), E = R(0);
+#pragma unroll
+        for (int jj = CH - 1; jj >= 0; --jj) { C = T[jj] * C; E = su[jj] + T[jj] * E; }
+        R sC = C, sE = E;
+#pragma unroll
+        for (int d = 1; d < P; d <<= 1) {
+          const R yC = __shfl_down_sync(gm, sC, d, P), yE = __shfl_down_sync(gm, sE, d, P);
+          if (r + d < P) { sE = sC * yE + sE; sC = sC * yC; }
+        }
+        R xC = __shfl_down_sync(gm, sC, 1, P), xE = __shfl_down_sync(gm, sE, 1, P);
+        if (r == P - 1) { xC = R(1); xE = R(0); }
+        R fu = xC * fup_surf + xE;         // F_up at the bottom of this lane's chunk
+        R fub[CH];
+#pragma unroll
+        for (int jj = CH - 1; jj >= 0; --jj) { fub[jj] = fu; fu = su[jj] + T[jj] * fu; }
+        R fd = fdn_top;
+#pragma unroll
+        for (int jj = 0; jj < CH; ++jj) {
+          const R a = fabs(fd) + fabs(fub[jj]);
+          skf[jj] += kk[jj] * we * a;
+          sfl[jj] += we * a;
+          fd = T[jj] * fd - su[jj];
+        }
+      }
+    }
+    // this absorber's share of k_eqv (and its direct-beam factor)
+    R fg_above = __shfl_up_sync(gm, fg[CH - 1], 1, P);
+    if (r == 0) fg_above = R(1);
+#pragma unroll
+    for (int jj = 0; jj < CH; ++jj) {
+      const int i = r * CH + jj, s = jj * P + r;
+      if (i < L) {
+        if constexpr (!lw) {
+          amt[s] = sfs > R(0) ? skf[jj] / sfs : kmin[jj];
+          // FP64: the ratio of the absorber's direct flux across the layer;
+          // FP32: its logarithm log1p(-loss / flux above), so that the factor
+          // can be formed as f - 1 without cancellation
+          R v;
+          if constexpr (kFP64) v = fg_above > R(0) ? fg[jj] / fg_above : R(1);
+          else v = fg_above > R(0) ? log1pf(-fminf(loss[s] / fg_above, 1.0f)) : R(0);
+          loss[s] = v;
+        } else {
+          amt[s] = sfl[jj] > R(0) ? skf[jj] / sfl[jj] : kmin[jj];
+        }
+      }
+      fg_above = fg[jj];
+    }
+  }
+
+  // The minor absorbers of the staged bands, one (band, absorber) per group.
+  __device__ static void stage_keqv(const FluxParams &p, const Smem &S, int bstart, int nb, R sec0) {
+    const int n_groups = blockDim.x / P, gid = threadIdx.x / P, r = threadIdx.x % P;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned gm = (P == 32) ? 0xffffffffu : (((1u << P) - 1u) << (lane & ~(unsigned)(P - 1)));
+    int item = 0;
+    for (int bi = 0; bi < nb; ++bi) {
+      const int na = p.l_gas ? min(p.bands[bstart + bi].n_abs, p.max_abs) : 0;
+      for (int j = 1; j < na; ++j, ++item)
+        if (item % n_groups == gid) minor_gas(p, S, bi, bstart + bi, j, sec0, r, gm);
+    }
+  }
+
+  // k_eqv of every slot into the grey absorption, and the solar direct-beam
+  // factor adjust_solar_ke (solve_band_k_eqv_scl.F90:975-1040), summed over
+  // the minor absorbers in their order.
+  __device__ static void fold_keqv(const FluxParams &p, const Smem &S, int bstart, int nb, R sec0) {
+    constexpr bool lw = (SRC == SOCGPU_IP_INFRA_RED);
+    const int L = p.n_layer, max_abs = p.max_abs;
+    for (int q = threadIdx.x; q < nb * LP; q += blockDim.x) {
+      const int bi = q / LP, s = q - bi * LP;
+      if (layer_of_slot(s) >= L) continue;
+      const int na = p.l_gas ? min(p.bands[bstart + bi].n_abs, max_abs) : 0;
+      // FP64: adj is the product of the absorbers' ratios; FP32: the sum of
+      // their logarithms
+      R keq = R(0), adj = kFP64 ? R(1) : R(0);
+      for (int j = 1; j < na; ++j) {
+        keq += S.amt[((size_t)bi * max_abs + j) * LP + s];
+        if (!lw) {
+          if constexpr (kFP64) adj *= S.aux[((size_t)bi * max_abs + j) * LP + s];
+          else adj += S.aux[((size_t)bi * max_abs + j) * LP + s];
+        }
+      }
+      S.kgt[q] += keq;
+      S.kabs[q] += keq;
+      if constexpr (!lw) {
+        const R tmax = R(36.04365338911715);   // ln(1 / epsilon) of FP64
+        const R x = keq * S.mass[s] * sec0;
+        // FP64: the factor f itself; FP32: f - 1
+        if constexpr (kFP64) S.aux[(size_t)bi * max_abs * LP + s] = adj * exp(x < tmax ? x : tmax);
+        else S.aux[(size_t)bi * max_abs * LP + s] = expm1f(adj + (x < tmax ? x : tmax));
+      }
+    }
+  }
+
+  // The direct-beam factor folded into the layer coefficients
+  // (solar_source.F90:115-130 with l_scale_solar): T0' = T0 f and
+  // c2' = c2 + T0 (f - 1).  The staged value is f in FP64 and f - 1 in FP32.
+  __device__ static __forceinline__ void fold_direct(const Smem &S, int bi, int max_abs, int r, int L,
+                                                     R (&T0)[CH], R (&c2)[CH]) {
+    const R *a = S.aux + (size_t)bi * max_abs * LP;
+#pragma unroll
+    for (int jj = 0; jj < CH; ++jj) {
+      const int i = r * CH + jj, s = jj * P + r;
+      if (i < L) {
+        const R fm1 = kFP64 ? a[s] - R(1) : a[s];
+        c2[jj] = c2[jj] + T0[jj] * fm1;
+        T0[jj] = kFP64 ? T0[jj] * a[s] : T0[jj] + T0[jj] * fm1;
+      }
+    }
   }
 
   // One g-point of one column (all its subcolumns under McICA).
@@ -775,18 +1234,23 @@ struct FluxKernel {
     const R f_inc_down = bs[0], f_inc_dir = bs[1], alb_diff = bs[2], alb_dir = bs[3], dB_surf = bs[4];
 
     if (!MCICA) {
+      // the gas absorption of the lane's layers first, while few registers
+      // are live, then the coefficients
+      R kgv[CH];
+      gas_k_lane(p, S, gt, gp, bd, amt_b, r, L, kgv);
       R T[CH], Rf[CH], T0[CH], c1[CH], c2[CH], om[CH];
 #pragma unroll
       for (int j = 0; j < CH; ++j) {
         const int i = r * CH + j, s = j * P + r;
         if (i < L) {
-          R kg = p.l_gas ? gas_k(gt, gp, bd, amt_b, s, S.p[s], S.t[s]) : R(0);
-          cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kg, S.mass[s], asym_b[s], fwd_b[s], sec0,
+          cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kgv[j], S.mass[s], asym_b[s], fwd_b[s], sec0,
                     T[j], Rf[j], T0[j], c1[j], c2[j], om[j]);
         } else {
           T[j] = R(1); Rf[j] = R(0); T0[j] = R(1); c1[j] = R(0); c2[j] = R(0); om[j] = R(0);
         }
       }
+      if constexpr (SRC == SOCGPU_IP_SOLAR)
+        if (p.keqv) fold_direct(S, bi, max_abs, r, L, T0, c2);
       solve_column(p, T, Rf, T0, c1, c2, om, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
                    alb_diff, alb_dir, dB_surf, w_g, acc, active);
     } else {
@@ -824,6 +1288,9 @@ struct FluxKernel {
     // Solve index it = 0 is the clear solve, it = 1.. the subcolumns
     // first..last.  The count is made uniform over the warp (all groups
     // take part in every shuffle); surplus iterations are discarded.
+    // the gas absorption of the lane's layers is the same for every subcolumn
+    R kgv[CH];
+    gas_k_lane(p, S, gt, gp, bd, amt_b, r, L, kgv);
     const int n_iter = last - first + 2;
     const int n_iter_warp = __reduce_max_sync(0xffffffffu, n_iter);
     for (int it = 0; it < n_iter_warp; ++it) {
@@ -848,7 +1315,7 @@ struct FluxKernel {
       for (int jj = 0; jj < CH; ++jj) {
         const int i = r * CH + jj, s = jj * P + r;
         if (i < L) {
-          R kg = p.l_gas ? gas_k(gt, gp, bd, amt_b, s, S.p[s], S.t[s]) : R(0);
+          const R kg = kgv[jj];
           R cs_i = (slot_sub >= 0) ? S.csub[(size_t)slot_sub * LP + s] : R(0);
           bool cloudy = false;
           if (slot_sub >= 0 && S.wcld[s] > R(0)) {
@@ -890,6 +1357,8 @@ struct FluxKernel {
           T[jj] = R(1); Rf[jj] = R(0); T0[jj] = R(1); c1[jj] = R(0); c2[jj] = R(0); om[jj] = R(0);
         }
       }
+      if constexpr (SRC == SOCGPU_IP_SOLAR)
+        if (p.keqv) fold_direct(S, bi, max_abs, r, L, T0, c2);
       solve_column(p, T, Rf, T0, c1, c2, om, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
                    alb_diff, alb_dir, dB_surf, clear ? w_clr : w_sub, acc, use);
     }

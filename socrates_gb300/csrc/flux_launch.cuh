@@ -27,8 +27,7 @@ int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char
   int warps = cfg.warps_per_cta, batch = nb;
   SmemLayout lay{};
   for (;;) {
-    lay = make_layout<R>(S::P * S::CH, S::P, batch, p.max_abs, MCICA ? p.n_condensed : 0,
-                         MCICA ? p.n_subcol_gen : 0, warps * 32 / S::P, p.isolir == SOCGPU_IP_INFRA_RED, MCICA);
+    lay = make_layout<R>(p, S::P * S::CH, S::P, batch, warps * 32 / S::P, MCICA);
     if ((long long)lay.bytes <= max_smem) break;
     if (batch > 1) { --batch; continue; }
     if (warps > 1) { warps /= 2; batch = nb; continue; }
@@ -73,8 +72,7 @@ int try_prepare(BatchGroup &g, char *msg, size_t len, bool &done) {
   const int warps = g.tile.warps_per_cta;
   const int n_groups = warps * 32 / S::P;
   auto bytes_of = [&](const FluxParams &p, int batch) {
-    return make_layout<R>(S::P * S::CH, S::P, batch, p.max_abs, MCICA ? p.n_condensed : 0,
-                          MCICA ? p.n_subcol_gen : 0, n_groups, p.isolir == SOCGPU_IP_INFRA_RED, MCICA).bytes;
+    return make_layout<R>(p, S::P * S::CH, S::P, batch, n_groups, MCICA).bytes;
   };
   auto kern = flux_kernel_batched<R, MIX, S::P, S::CH, NOSCAT, MCICA, SRC>;
   // the kernel's static shared memory (its parameter copy) counts against

@@ -35,6 +35,7 @@ struct SpectrumEntry {
 };
 
 SpectrumEntry *find_spectrum(int handle);
+bool is_keqv(const socgpu_control *c);
 
 int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntry *sp, const socgpu_atm *atm,
              const socgpu_cld *cld, const socgpu_aer *aer, const socgpu_bound *bd, const socgpu_radout *out,

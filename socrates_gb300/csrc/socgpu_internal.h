@@ -18,12 +18,17 @@ constexpr int kMaxPlanckCoeff = 12;
 constexpr int kPadeParm = 16;
 constexpr int kMaxCloudComp = 4;
 
+// Self-broadened absorbers whose gas fractions a column stages (lookup tables).
+constexpr int kMaxSb = 4;
+
 // One absorber of a band (block 4/5 entries for (band, species)).
 struct BandGas {
   int species;     // 0-based species index into gas_mix_ratio
   int i_scale_k;   // ip_scale_band / term / null
-  int i_scale_fnc; // ip_scale_power_law / quad / doppler_quad / fnc_null
+  int i_scale_fnc; // ip_scale_power_law / quad / doppler_quad / wenyi / lookup / t_lookup / fnc_null
   int l_doppler;
+  int sb;          // lookup tables: 0-based self-broadened index (staged gas fraction), -1 none
+  int n_t;         // temperature-only tables: entries of the species' temperature grid
   double p_ref, t_ref, doppler_cor;
   double scale[4]; // band scaling parameters (ip_scale_band)
   float p_ref_f, t_ref_f, doppler_cor_f, scale_f[4];   // FP32 copies for the mixed kernels
@@ -49,6 +54,18 @@ struct BandInfo {
   float rayleigh_f, solar_flux_band_f;
   float planck_f[kMaxPlanckCoeff];
   BandGas gas[kMaxAbsPerBand];
+  // equivalent extinction (k_eqv_scl): the k-terms of absorber j >= 1 are
+  // TermK entries minor_first[j] .. minor_first[j] + minor_count[j] - 1
+  int minor_first[kMaxAbsPerBand], minor_count[kMaxAbsPerBand];
+};
+
+// One k-term of one absorber of a band: the minor gases of k_eqv_scl.
+struct TermK {
+  int iex;                          // 0-based k-term
+  int lk_off;                       // offset of its lookup table in k_lookup, -1 without
+  double k, w;
+  double scale[4];                  // per-term scaling parameters (ip_scale_term)
+  float kf, wf, scale_f[4];
 };
 
 // One g-point: a k-term product of random overlap
@@ -64,6 +81,8 @@ struct GPoint {
   float weight_f;                   // FP32 copies for the mixed kernels
   float kf[kMaxAbsPerBand];
   float term_scale_f[kMaxAbsPerBand][4];
+  int lk_off[kMaxAbsPerBand];       // offset of each absorber's lookup table in k_lookup, -1 without
+  short iex[kMaxAbsPerBand];        // each absorber's 0-based k-term (Wen-Yi tables)
 };
 
 // Device-resident spectrum.
@@ -75,6 +94,30 @@ struct SpectrumDev {
   int n_drop_type, n_ice_type;
   BandInfo *bands;                  // [n_band]
   GPoint *gpoints;                  // [n_gpoint]
+  int random_ok;                    // the random-overlap products fit SOCGPU_MAX_GPOINT
+  // equivalent extinction: the major absorber's terms as g-points, the minor
+  // absorbers' terms as TermK entries
+  BandInfo *bands_keqv;
+  GPoint *gpoints_keqv;
+  TermK *minor_terms;
+  int n_gpoint_keqv;
+  int host_first_g_keqv[SOCGPU_MAX_BAND + 1];
+  // lookup tables: P/T grid, gas fractions, compact k tables, temperature-only grids
+  int has_lookup, lk_n_pre, lk_n_tmp, lk_n_gf, n_sb;
+  double *lk_grid;                  // ln p [n_pre], T [n_pre][n_tmp], gas fractions [n_gf]
+  float *lk_grid_f;
+  double *k_lookup;
+  float *k_lookup_f;
+  int sb_species[kMaxSb];           // 0-based species of each self-broadened index
+  double sb_ratio_gas[kMaxSb], ratio_water;
+  int l_water;
+  int nd_t_lookup_gas;
+  double *t_lookup_gas;             // [n_species][nd_t_lookup_gas]
+  float *t_lookup_gas_f;
+  // Wen-Yi tables packed as plg[26], ttb[10], tto[9], gk250b[n4], gk4[10][26][n4], gk6[9][26][n6]
+  int wenyi_n4, wenyi_n6;
+  double *wenyi;
+  float *wenyi_f;
   double *drop_parm;                // [n_drop_type][n_band][16]
   double *ice_parm;                 // [n_ice_type][n_band][16]
   float *drop_parm_f, *ice_parm_f;  // FP32 copies
@@ -126,6 +169,23 @@ struct FluxParams {
   // outputs
   double *flux_up, *flux_down, *flux_direct, *flux_div, *heating_rate;
   int *error_flag;                  // device flag: set when a bound is violated
+  // equivalent extinction (k_eqv_scl): minor absorbers folded into grey absorption
+  int keqv, l_grey_single;
+  int term_scr;                     // a scratch row per group: per-term scaled absorbers or k_eqv
+  const TermK *minor_terms;
+  // lookup-table k scaling: the column stages interpolation factors
+  int lk_on, lk_n_pre, lk_n_tmp, lk_n_gf, n_sb;
+  const double *lk_grid, *k_lookup;
+  const float *lk_grid_f, *k_lookup_f;
+  int sb_species[kMaxSb];
+  double sb_ratio_gas[kMaxSb], ratio_water;
+  int l_water;
+  int nd_t_lookup_gas;
+  const double *t_lookup_gas;
+  const float *t_lookup_gas_f;
+  int wenyi_n4, wenyi_n6;
+  const double *wenyi;
+  const float *wenyi_f;
 };
 
 // Launch configuration chosen by the tuner.

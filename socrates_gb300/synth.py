@@ -33,6 +33,10 @@ from .spectrum import Spectrum
 GRAV = 9.80665          # rad_ccf.F90:50
 R_DRY = 287.026         # rad_ccf.F90:54
 SOLAR_CONSTANT = 1361.0
+# Background mass mixing ratios of trace gases by identifier (N2O, CH4, O2,
+# SO2, CFC11, CFC12, CFC113, HCFC22, HFC134a, OCS).
+TRACE_MMR = {4: 4.8e-7, 6: 1.0e-6, 7: 0.231, 9: 1.0e-9, 14: 1.1e-9, 15: 2.3e-9, 16: 4.5e-10, 17: 7.5e-10,
+             19: 2.8e-10, 25: 1.0e-9}
 
 # ---------------------------------------------------------------------------
 # Philox4x32-10, vectorised (Salmon et al., SC'11)
@@ -251,8 +255,31 @@ def atmosphere(n_profile: int, n_layer: int, species: np.ndarray, seed: int) -> 
             gas[:, :, j] = 6.0e-4
         elif s == 3:
             gas[:, :, j] = 1.0e-5 * np.exp(-0.5 * np.log(p / 1000.0) ** 2)
+        elif int(s) in TRACE_MMR:
+            gas[:, :, j] = TRACE_MMR[int(s)]
     return Column(n_profile, n_layer, p, t, p_level, t_level, mass, gas, z,
                   t_ground=np.ascontiguousarray(t_level[:, -1]))
+
+
+def add_density(col: Column, index_water: int) -> Column:
+    """Moist air density of each layer (l_run_cdf.F90:1220-1235), which the
+    water-vapour continuum needs; index_water is 1-based."""
+    q = col.gas_mix_ratio[:, :, index_water - 1] if index_water > 0 else 0.0
+    col.density = np.asfortranarray(col.p / (R_DRY * col.t * (1.0 + (28.966e-03 / 18.0153e-03 - 1.0) * q)))
+    return col
+
+
+def operational_case(sp: Spectrum, n_profile: int, n_layer: int, seed: int, solar: bool) -> Column:
+    """Columns for an operational spectral file (many absorbers, continuum):
+    the synthetic atmosphere with background amounts of the trace gases,
+    its moist density and a surface for the source."""
+    col = atmosphere(n_profile, n_layer, sp.type_absorb, seed)
+    add_density(col, int(sp.index_water))
+    if solar:
+        add_sw_surface(col, sp.n_band, seed)
+    else:
+        add_lw_surface(col, sp.n_band)
+    return col
 
 
 def add_lw_surface(col: Column, n_band: int, emissivity: float = 0.98) -> Column:

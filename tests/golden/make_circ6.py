@@ -9,8 +9,9 @@ GA7 takes most of its k-terms from the lookup tables of sp_lw_ga7_k and the
 CO2 terms of band 4 from Wen-Yi Zhong's tables (module scale_wenyi).  This
 script reads the netCDF inputs, the parsed spectral file with its tables and
 the reference heating rates from a SOCRATES source tree and stores them in
-circ6_lw_ga7.npz beside it (the tree is not available where the tests run on
-the GPU).  Absorbers without an input file (SO2, CFC113, HCFC22, HFC134a,
+circ6_lw_ga7.npz beside it, and the parsed GA7 short-wave spectral file in
+ga7_sw_spectrum.npz (the tree is not available where the tests run on the
+GPU).  Absorbers without an input file (SO2, CFC113, HCFC22, HFC134a,
 OCS) have zero mixing ratios, as l_run_cdf.F90:797-833 sets them.
 
     python tests/golden/make_circ6.py /path/to/socrates
@@ -77,6 +78,12 @@ def main(root):
     sp_file.unlink()
     np.savez_compressed(out, **arrays)
     print(f"wrote {out} ({out.stat().st_size} bytes); gases with input files: {present}")
+    # the GA7 short-wave spectral file (lookup tables, no Wen-Yi terms), for
+    # synthetic solar cases
+    sw = Spectrum.read_text(root / "data" / "spectra" / "ga7" / "sp_sw_ga7", name="sp_sw_ga7")
+    sw_out = HERE / "ga7_sw_spectrum.npz"
+    sw.save_npz(sw_out)
+    print(f"wrote {sw_out} ({sw_out.stat().st_size} bytes)")
 
 
 if __name__ == "__main__":

@@ -163,7 +163,7 @@ def test_invalid_item_names_its_index(gpu_lib):
     from socrates_gb300.batch import Batch
     from socrates_gb300.device import DeviceCase
     good = _capture("lw_noscat", abi.PRECISION_MIXED)
-    bad = (replace(good[0], i_gas_overlap=4),) + good[1:]      # k_eqv_scl overlap is not on this path
+    bad = (replace(good[0], i_gas_overlap=8),) + good[1:]      # resort-rebin overlap is not on this path
     with pytest.raises(R.RadianceError) as e:
         Batch([DeviceCase(*good), DeviceCase(*bad)])
     assert e.value.status == abi.I_ERR_FATAL

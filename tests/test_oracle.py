@@ -204,7 +204,7 @@ def test_cloud_gen_compaction_and_fraction():
 
 
 # ---------------------------------------------------------------------------
-KGO_FIXTURES = ("icrccm", "circ6")
+KGO_FIXTURES = ("icrccm", "circ6", "ga7")
 
 
 @pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(KGO_FIXTURES)))

@@ -161,7 +161,7 @@ def test_unsupported_options_return_status(gpu_lib):
         (R.lw_control(i_2stream=abi.IP_IFM), abi.I_ERR_FATAL),
         (R.lw_control(i_solver=abi.IP_SOLVER_NO_SCAT), abi.I_ERR_FATAL),
         (R.lw_control(first_band=3, last_band=12), abi.I_ERR_RANGE),
-        (R.lw_control(i_gas_overlap=4), abi.I_ERR_FATAL),
+        (R.lw_control(i_gas_overlap=8), abi.I_ERR_FATAL),
     ]
     for ctl, status in bad:
         with pytest.raises(R.RadianceError) as e:

@@ -117,7 +117,7 @@ def test_invalid_request_rejected_at_submit(gpu_lib):
     from socrates_gb300.server import Server
     _, reqs = _requests(1, seed=25)
     c, sp, col, mc = reqs[0]
-    bad = replace(c, i_gas_overlap=4)
+    bad = replace(c, i_gas_overlap=8)
     srv = Server(device_bytes=64 << 20, streams=1)
     with pytest.raises(R.RadianceError) as e:
         srv.submit(R.Marshal(bad, sp, col, mc), sp)
