@@ -332,10 +332,18 @@ typedef struct socgpu_radout {
  * under `name` (the file-reading half of set_spectrum,
  * src/interface_core/socrates_set_spectrum.F90:90-121; record layouts of
  * src/radiance_core/read_spectrum.F90).  Blocks 0-6, 8, 9, 13 and the
- * Pade cloud blocks 10/12 are read; lookup-table k scaling returns
- * SOCGPU_I_ERR_IO with a message. */
+ * Pade cloud blocks 10/12 are read, with the lookup tables of block 5 from
+ * the '_k' file beside it (path + "_k"). */
 SOCGPU_API int socgpu_spectrum_load(const char *name, const char *path, socgpu_spectrum_handle *handle,
                                     char *msg, size_t msg_len);
+/* As socgpu_spectrum_load, with the lookup tables of block 5 read from k_path
+   (NULL: path + "_k", read_spectrum.F90:1420-1560) and Wen-Yi Zhong's CO2
+   and O3 tables read from wenyi_path, a SOCRATES source file that defines
+   them (the module scale_wenyi, which the reference compiles in; NULL: none,
+   and spectra that scale with them are rejected when registered). */
+SOCGPU_API int socgpu_spectrum_load_ext(const char *name, const char *path, const char *k_path,
+                                        const char *wenyi_path, socgpu_spectrum_handle *handle, char *msg,
+                                        size_t msg_len);
 
 /* ABI version of the loaded library (compare with SOCGPU_ABI_VERSION). */
 SOCGPU_API int socgpu_abi_version(void);

@@ -155,7 +155,7 @@ ABI_FUNCTIONS = (
     "socgpu_cloud_gen_device_noalloc", "socgpu_batch_create", "socgpu_batch_run", "socgpu_batch_tune",
     "socgpu_batch_info", "socgpu_batch_destroy", "socgpu_tune_get", "socgpu_tune_set",
     "socgpu_server_create", "socgpu_server_submit", "socgpu_server_wait", "socgpu_server_stats_get",
-    "socgpu_server_destroy", "socgpu_spectrum_load",
+    "socgpu_server_destroy", "socgpu_spectrum_load", "socgpu_spectrum_load_ext",
 )
 
 _CALC_ARGS = [C.POINTER(Control), C.POINTER(Dimen), C.c_int, C.POINTER(Atm), C.POINTER(Cld), C.POINTER(Aer),
@@ -170,6 +170,8 @@ def declare(lib: C.CDLL) -> C.CDLL:
                                              C.c_size_t]
     lib.socgpu_spectrum_lookup.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
     lib.socgpu_spectrum_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_int), C.c_char_p, C.c_size_t]
+    lib.socgpu_spectrum_load_ext.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_int),
+                                             C.c_char_p, C.c_size_t]
     lib.socgpu_spectrum_n_gpoint.argtypes = [C.c_int]
     lib.socgpu_spectrum_release.argtypes = [C.c_int]
     lib.socgpu_radiance_calc.argtypes = _CALC_ARGS + [C.c_char_p, C.c_size_t]

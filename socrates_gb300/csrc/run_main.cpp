@@ -6,7 +6,7 @@
 //   socgpu_run -s <spectral file> -R <first band> <last band> (-I | -S) -B <base>
 //              [-g <gas overlap>] [-c] [-r] [+R] [-q] [-t <two-stream scheme>]
 //              [-v <solver>] [-C <cloud scheme>] [-z <scatter method>]
-//              [-ds <direct tau>] [-P fp64|mixed]
+//              [-ds <direct tau>] [-P fp64|mixed] [-W <scale_wenyi source>]
 //   socgpu_run --convert <in> <out.cdf|out.cdl>
 //
 // Inputs: .t (layer temperatures on the layer pressures `plev`), .tl (level
@@ -16,6 +16,9 @@
 // gas), .tstar (infra-red), .szen and .stoa (solar), .surf (albedo weights).
 // Outputs: .uflx, .dflx, .nflx, .hrts, and in the solar .vflx (direct) and
 // .sflx (diffuse down).  Only the clear-sky two-stream path is driven.
+// Lookup tables are read from the spectral file's '_k' companion; spectral
+// files with Wen-Yi CO2 terms (GA7 and GA9 long wave) need -W, the SOCRATES
+// source file that defines those tables (the reference compiles them in).
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -40,8 +43,10 @@ const double kMolarWeightH2O = 18.0153;
 const char *gas_suffix(int type) {
   static const char *s[] = {"",       "q",      "co2",    "o3",      "n2o",    "co",   "ch4",  "o2",
                             "no",     "so2",    "no2",    "nh3",     "hno3",   "n2",   "cfc11", "cfc12",
-                            "cfc113", "hcfc22", "hfc125", "hfc134a", "cfc114"};
-  return (type >= 1 && type <= 20) ? s[type] : nullptr;
+                            "cfc113", "hcfc22", "hfc125", "hfc134a", "cfc114", "tio",  "vo",   "h2",
+                            "he",     "ocs",    "na",     "k",       "feh",    "crh",  "li",   "rb",
+                            "cs",     "ph3",    "c2h2",   "hcn",     "h2s",    "ar"};
+  return (type >= 1 && type < (int)(sizeof(s) / sizeof(s[0]))) ? s[type] : nullptr;
 }
 
 int die(const std::string &m) {
@@ -135,7 +140,7 @@ int main(int argc, char **argv) {
     if (!(to_cdf ? socgpu::write_cdf(a[2], f, err) : socgpu::write_cdl(a[2], f, err))) return die(err);
     return 0;
   }
-  std::string sp_file, base;
+  std::string sp_file, base, wenyi_file;   // -W: the Wen-Yi tables (SOCRATES's scale_wenyi source)
   int first = 0, last = 0, isolir = 0, overlap = 0, two_stream = 0, solver = 0, cloud = SOCGPU_IP_CLOUD_CLEAR;
   int scatter = SOCGPU_IP_SCATTER_FULL, direct_tau = SOCGPU_IP_DIRECT_DELTA_SCALING;
   bool cont = false, rayleigh = false, rescale = false, quad = false, gas = false;
@@ -144,6 +149,7 @@ int main(int argc, char **argv) {
     const std::string &o = a[i];
     auto need = [&](size_t n) { return i + n < a.size(); };
     if (o == "-s" && need(1)) sp_file = a[++i];
+    else if (o == "-W" && need(1)) wenyi_file = a[++i];
     else if (o == "-B" && need(1)) base = a[++i];
     else if (o == "-R" && need(2)) { first = std::atoi(a[i + 1].c_str()); last = std::atoi(a[i + 2].c_str()); i += 2; }
     else if (o == "-I") isolir = SOCGPU_IP_INFRA_RED;
@@ -173,7 +179,8 @@ int main(int argc, char **argv) {
 
   char msg[512] = "";
   socgpu_spectrum_handle h = 0;
-  int st = socgpu_spectrum_load(sp_file.c_str(), sp_file.c_str(), &h, msg, sizeof(msg));
+  int st = socgpu_spectrum_load_ext(sp_file.c_str(), sp_file.c_str(), nullptr,
+                                    wenyi_file.empty() ? nullptr : wenyi_file.c_str(), &h, msg, sizeof(msg));
   if (st != SOCGPU_I_NORMAL) return die(msg);
 
   // the spectral file's absorbers (for the gas files)

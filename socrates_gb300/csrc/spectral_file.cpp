@@ -7,7 +7,11 @@
 // absorbers per band, 5 k-terms (fixed columns: (2(3x,1pe16.9), i3, :,
 // (t42, 1pe16.9, 3x, 1pe16.9))), 6 Planck polynomial, 8 and 9 continua, 13
 // Doppler broadening, 10 and 12 Pade droplet and ice parameters (schemes 5
-// and 20).  Other blocks are skipped; lookup-table k scaling is rejected.
+// and 20).  Other blocks are skipped.  Lookup tables come from the '_k' file.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <map>
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
@@ -74,9 +78,21 @@ double fixed(const std::string &line, size_t a, size_t b, bool &present) {
 }
 
 struct Block {
-  int type = 0;
+  int type = 0, version = 0;
   std::vector<std::string> lines;
 };
+
+// The 1PE13.6 fields of one record of a '_k' file.
+std::vector<double> fields13(const std::string &line) {
+  std::vector<double> v;
+  size_t end = line.find_last_not_of(" \r");
+  if (end == std::string::npos) return v;
+  for (size_t i = 0; i <= end; i += 13) {
+    const std::string f = line.substr(i, 13);
+    if (f.find_first_not_of(' ') != std::string::npos) v.push_back(std::strtod(f.c_str(), nullptr));
+  }
+  return v;
+}
 
 }  // namespace
 
@@ -96,6 +112,13 @@ struct SpectralFile {
   int index_water = 0;
   std::vector<double> drop_parm, ice_parm;
   std::vector<int> drop_ids, ice_ids, drop_on, ice_on;
+  // lookup tables of the '_k' file
+  int n_pre = 0, n_tmp = 0, n_gf = 0, nsb = 0, nd_t = 0;
+  std::vector<double> p_lookup, t_lookup, k_lookup, gf_lookup, k_lookup_sb, molar_weight;
+  std::vector<int> index_sb, n_t_gas;
+  std::vector<double> t_gas, k_t_gas;
+  // Wen-Yi tables
+  std::vector<double> wy_plg, wy_ttb, wy_tto, wy_gk250b, wy_gk4, wy_gk6;
 
   socgpu_spectrum_desc desc() const {
     socgpu_spectrum_desc d{};
@@ -143,6 +166,24 @@ struct SpectralFile {
       d.i_ice_parm = ice_ids.data();
       d.l_ice_type = ice_on.data();
     }
+    if (!k_lookup.empty()) {
+      d.n_pre = n_pre; d.n_tmp = n_tmp;
+      d.p_lookup = p_lookup.data(); d.t_lookup = t_lookup.data(); d.k_lookup = k_lookup.data();
+    }
+    if (!k_lookup_sb.empty()) {
+      d.index_sb = index_sb.data(); d.nd_species_sb = nsb; d.n_gas_frac = n_gf;
+      d.gf_lookup = gf_lookup.data(); d.k_lookup_sb = k_lookup_sb.data();
+    }
+    d.molar_weight = molar_weight.empty() ? nullptr : molar_weight.data();
+    if (!k_t_gas.empty()) {
+      d.nd_t_lookup_gas = nd_t; d.n_t_lookup_gas = n_t_gas.data();
+      d.t_lookup_gas = t_gas.data(); d.k_t_lookup_gas = k_t_gas.data();
+    }
+    if (!wy_plg.empty()) {
+      d.wenyi_plg = wy_plg.data(); d.wenyi_ttb = wy_ttb.data(); d.wenyi_tto = wy_tto.data();
+      d.wenyi_gk250b = wy_gk250b.data(); d.wenyi_gk4 = wy_gk4.data(); d.wenyi_gk6 = wy_gk6.data();
+      d.wenyi_n_term4 = (int)wy_gk250b.size(); d.wenyi_n_term6 = (int)(wy_gk6.size() / 234);
+    }
     if (!n_band_cont.empty()) {
       d.nd_continuum = ndc;
       d.n_band_continuum = n_band_cont.data();
@@ -158,7 +199,216 @@ struct SpectralFile {
   }
 };
 
-bool read_spectral_file(const std::string &path, SpectralFile &sf, std::string &err) {
+// Molar weights [g/mol] of the absorbers by gas identifier (the published
+// values of J. A. Duffy, General Inorganic Chemistry (1970), and NIST, as
+// gas_list_pcf.F90:303-330 lists them); used for self-broadened gas fractions.
+double molar_weight_of(int type) {
+  static const double mw[] = {0.0, 18.0153, 44.0100, 47.9982, 44.0128, 28.0106, 16.0430, 31.9988, 30.0061,
+                              64.0628, 46.0055, 17.0306, 63.0129, 28.0134, 137.3686, 120.9140, 187.3765,
+                              86.46892, 120.02227, 102.03184, 170.921, 63.866, 66.9409, 2.01588, 4.002602,
+                              60.075};
+  return (type >= 1 && type < (int)(sizeof(mw) / sizeof(mw[0]))) ? mw[type] : 0.0;
+}
+
+// The lookup tables of a '_k' file in the order read_spectrum.F90:1420-1560
+// reads them: the P/T grid, the gas fractions of self-broadened absorbers,
+// one table per (band, absorber) record of block 5 (recs: band, absorber,
+// scaling function, 0-based), then the temperature-only tables.
+bool read_k_file(const std::string &path, SpectralFile &s, const std::vector<std::array<int, 3>> &recs,
+                 std::string &err) {
+  std::ifstream in(path);
+  if (!in) { err = "the k-term lookup tables of block 5 are in " + path + ", which cannot be read"; return false; }
+  std::vector<std::string> text;
+  std::string line;
+  while (std::getline(in, line)) {
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    text.push_back(line);
+  }
+  auto values = [&](size_t &q, size_t n, std::vector<double> &out) -> bool {
+    out.clear();
+    while (out.size() < n) {
+      if (q >= text.size()) return false;
+      for (double v : fields13(text[q++])) out.push_back(v);
+    }
+    out.resize(n);
+    return true;
+  };
+  auto block = [&](const std::string &title, size_t &q) -> bool {
+    for (q = 0; q < text.size(); ++q)
+      if (text[q].rfind("*BLOCK", 0) == 0 && text[q].compare(8, title.size(), title) == 0) return true;
+    return false;
+  };
+  const int nb = s.n_band, na = std::max(1, s.n_abs), ndk = s.nd_k;
+  auto nk_of = [&](int b, int g) { return s.i_band_k[(size_t)b + (size_t)nb * g]; };
+  std::vector<double> v;
+  bool any_pt = false, any_t = false;
+  for (auto &r : recs) { any_pt |= r[2] == SOCGPU_IP_SCALE_LOOKUP; any_t |= r[2] == SOCGPU_IP_SCALE_T_LOOKUP; }
+  if (any_pt) {
+    size_t q = 0;
+    if (!block("k-table", q)) { err = path + ": no k-table block"; return false; }
+    q += 3;
+    const int npre = s.n_pre, ntmp = s.n_tmp;
+    if (npre < 2 || ntmp < 2) { err = path + ": bad P/T table extents"; return false; }
+    s.p_lookup.assign(npre, 0.0);
+    s.t_lookup.assign((size_t)ntmp * npre, 0.0);
+    for (int ip = 0; ip < npre; ++ip) {
+      if (!values(q, 1 + ntmp, v)) { err = path + ": P/T grid truncated"; return false; }
+      s.p_lookup[ip] = std::log(v[0]);
+      for (int it = 0; it < ntmp; ++it) s.t_lookup[(size_t)it + (size_t)ntmp * ip] = v[1 + it];
+    }
+    bool sb = false;
+    for (int x : s.index_sb) { sb |= x > 0; s.nsb = std::max(s.nsb, x); }
+    if (sb) {
+      if (q + 1 >= text.size()) { err = path + ": gas-fraction table missing"; return false; }
+      s.n_gf = std::atoi(text[q + 1].substr(std::min<size_t>(14, text[q + 1].size())).c_str());
+      q += 2;
+      if (s.n_gf < 1 || !values(q, s.n_gf, s.gf_lookup)) { err = path + ": bad gas-fraction table"; return false; }
+      s.k_lookup_sb.assign((size_t)ntmp * npre * s.n_gf * ndk * s.nsb * nb, 0.0);
+    } else {
+      s.index_sb.clear();
+    }
+    s.k_lookup.assign((size_t)ntmp * npre * ndk * na * nb, 0.0);
+    for (auto &r : recs) {
+      if (r[2] != SOCGPU_IP_SCALE_LOOKUP) continue;
+      const int b = r[0], g = r[1], nk = nk_of(b, g);
+      q += 2;
+      const int jsb = sb ? s.index_sb[g] - 1 : -1;
+      for (int t = 0; t < nk; ++t) {
+        const int ngf = jsb >= 0 ? s.n_gf : 1;
+        for (int ig = 0; ig < ngf; ++ig)
+          for (int ip = 0; ip < npre; ++ip) {
+            if (!values(q, ntmp, v)) { err = path + ": k table truncated"; return false; }
+            for (int it = 0; it < ntmp; ++it) {
+              if (jsb >= 0)
+                s.k_lookup_sb[(size_t)it + (size_t)ntmp * ((size_t)ip + (size_t)npre * ((size_t)ig + (size_t)s.n_gf *
+                    ((size_t)t + (size_t)ndk * ((size_t)jsb + (size_t)s.nsb * b))))] = v[it];
+              else
+                s.k_lookup[(size_t)it + (size_t)ntmp * ((size_t)ip + (size_t)npre * ((size_t)t + (size_t)ndk *
+                    ((size_t)g + (size_t)na * b)))] = v[it];
+            }
+          }
+      }
+    }
+  }
+  if (any_t) {
+    size_t q = 0;
+    if (!block("temperature k-tables", q)) { err = path + ": no temperature k-tables block"; return false; }
+    if (q + 2 >= text.size()) { err = path + ": bad temperature tables"; return false; }
+    s.nd_t = std::atoi(text[q + 2].substr(std::min<size_t>(9, text[q + 2].size())).c_str());
+    q += 3;
+    s.n_t_gas.assign(na, 0);
+    s.t_gas.assign((size_t)s.nd_t * na, 0.0);
+    std::vector<int> t_gases;
+    for (auto &r : recs)
+      if (r[2] == SOCGPU_IP_SCALE_T_LOOKUP && std::find(t_gases.begin(), t_gases.end(), r[1]) == t_gases.end())
+        t_gases.push_back(r[1]);
+    std::sort(t_gases.begin(), t_gases.end());
+    for (int g : t_gases) {
+      if (q + 1 >= text.size()) { err = path + ": temperature grid missing"; return false; }
+      s.n_t_gas[g] = std::atoi(text[q + 1].substr(std::min<size_t>(27, text[q + 1].size())).c_str());
+      q += 2;
+      if (s.n_t_gas[g] < 2 || s.n_t_gas[g] > s.nd_t || !values(q, s.n_t_gas[g], v)) {
+        err = path + ": bad temperature grid";
+        return false;
+      }
+      for (int k = 0; k < s.n_t_gas[g]; ++k) s.t_gas[(size_t)k + (size_t)s.nd_t * g] = v[k];
+    }
+    s.k_t_gas.assign((size_t)s.nd_t * ndk * na * nb, 0.0);
+    for (int b = 0; b < nb; ++b)
+      for (int j = 0; j < s.n_band_absorb[b]; ++j) {
+        const int g = s.index_absorb[(size_t)j + (size_t)na * b] - 1;
+        bool is_t = false;
+        for (auto &r : recs) is_t |= r[0] == b && r[1] == g && r[2] == SOCGPU_IP_SCALE_T_LOOKUP;
+        if (!is_t) continue;
+        q += 2;
+        for (int t = 0; t < nk_of(b, g); ++t) {
+          if (!values(q, s.n_t_gas[g], v)) { err = path + ": temperature k table truncated"; return false; }
+          for (int k = 0; k < s.n_t_gas[g]; ++k)
+            s.k_t_gas[(size_t)k + (size_t)s.nd_t * ((size_t)t + (size_t)ndk * ((size_t)g + (size_t)na * b))] = v[k];
+        }
+      }
+  }
+  return true;
+}
+
+// Wen-Yi Zhong's CO2 (band 4) and O3 (band 6) tables from a SOCRATES source
+// file that defines them (the module scale_wenyi), which the reference
+// compiles in.  The band tables are assembled as RESHAPE(..., ORDER=(3, 2,
+// 1)) builds them: one source array per temperature, the k-term index fastest.
+bool read_wenyi(const std::string &path, SpectralFile &s, std::string &err) {
+  std::ifstream in(path);
+  if (!in) { err = "cannot open the Wen-Yi tables " + path; return false; }
+  std::stringstream ss;
+  ss << in.rdbuf();
+  std::string text = ss.str();
+  std::map<std::string, std::vector<double>> arrays;
+  size_t pos = 0;
+  while ((pos = text.find("PARAMETER", pos)) != std::string::npos) {
+    size_t colon = text.find("::", pos), open = text.find("(/", pos), close = text.find("/)", pos);
+    pos += 9;
+    if (colon == std::string::npos || open == std::string::npos || close == std::string::npos || open > close)
+      continue;
+    std::string decl = text.substr(colon + 2, open - colon - 2);
+    size_t paren = decl.find('(');
+    if (paren == std::string::npos || decl.find("RESHAPE") != std::string::npos) continue;
+    std::string name = decl.substr(0, paren);
+    name.erase(0, name.find_first_not_of(" \t"));
+    name.erase(name.find_last_not_of(" \t") + 1);
+    for (char &c : name) c = (char)std::tolower((unsigned char)c);
+    const size_t declared = (size_t)std::atol(decl.c_str() + paren + 1);
+    std::string body = text.substr(open + 2, close - open - 2);
+    std::vector<double> vals;
+    size_t b = 0;
+    while ((b = body.find("_RealK", b)) != std::string::npos) {
+      size_t a = b;
+      while (a > 0 && (std::isdigit((unsigned char)body[a - 1]) || body[a - 1] == '.' || body[a - 1] == 'E' ||
+                       body[a - 1] == 'e' || body[a - 1] == 'D' || body[a - 1] == 'd' ||
+                       ((body[a - 1] == '-' || body[a - 1] == '+') && a > 1 &&
+                        (body[a - 2] == 'E' || body[a - 2] == 'e' || body[a - 2] == 'D' || body[a - 2] == 'd' ||
+                         !std::isalnum((unsigned char)body[a - 2])))))
+        --a;
+      std::string num_s = body.substr(a, b - a);
+      for (char &c : num_s)
+        if (c == 'D' || c == 'd') c = 'E';
+      vals.push_back(std::strtod(num_s.c_str(), nullptr));
+      b += 6;
+    }
+    if (vals.size() != declared) { err = path + ": " + name + " has the wrong number of values"; return false; }
+    arrays[name] = vals;
+    pos = close;
+  }
+  auto need = [&](const std::string &n) -> const std::vector<double> * {
+    auto it = arrays.find(n);
+    return it == arrays.end() ? nullptr : &it->second;
+  };
+  const auto *plg = need("plg"), *ttb = need("ttb"), *tto = need("tto"), *g250 = need("gk250b");
+  if (!plg || !ttb || !tto || !g250 || plg->size() != 26 || ttb->size() != 10 || tto->size() != 9) {
+    err = path + ": the Wen-Yi grids are missing";
+    return false;
+  }
+  auto table = [&](const std::string &prefix, int n_t, std::vector<double> &out) -> bool {
+    const auto *first_t = need(prefix + "_1");
+    if (!first_t || first_t->size() % 26) return false;
+    const size_t n_term = first_t->size() / 26;
+    out.assign((size_t)n_t * 26 * n_term, 0.0);
+    for (int t = 0; t < n_t; ++t) {
+      const auto *a = need(prefix + "_" + std::to_string(t + 1));
+      if (!a || a->size() != 26 * n_term) return false;
+      for (size_t p = 0; p < 26; ++p)
+        for (size_t k = 0; k < n_term; ++k) out[(size_t)t + (size_t)n_t * (p + 26 * k)] = (*a)[p * n_term + k];
+    }
+    return true;
+  };
+  if (!table("gk4", 10, s.wy_gk4) || !table("gk6", 9, s.wy_gk6)) {
+    err = path + ": the Wen-Yi k tables are incomplete";
+    return false;
+  }
+  s.wy_plg = *plg; s.wy_ttb = *ttb; s.wy_tto = *tto; s.wy_gk250b = *g250;
+  return true;
+}
+
+bool read_spectral_file(const std::string &path, const std::string &k_path, const std::string &wenyi_path,
+                        SpectralFile &sf, std::string &err) {
   std::ifstream in(path);
   if (!in) { err = "cannot open spectral file " + path; return false; }
   std::vector<Block> blocks;
@@ -174,6 +424,7 @@ bool read_spectral_file(const std::string &path, SpectralFile &sf, std::string &
       blocks.emplace_back();
       cur = &blocks.back();
       cur->type = w.size() > 2 ? std::atoi(w[2].c_str()) : -1;
+      cur->version = w.size() > 6 ? std::atoi(w[6].c_str()) : 0;
     } else if (line.rfind("*END", 0) == 0) {
       cur = nullptr;
     } else if (cur) {
@@ -234,9 +485,10 @@ bool read_spectral_file(const std::string &path, SpectralFile &sf, std::string &
     for (size_t q = 5; q < b4->lines.size(); ++q)
       for (auto &w : split(b4->lines[q])) tok.push_back(w);
     size_t q = 0;
+    const bool with_overlap = b4->version >= 1;   // each band's overlap method follows its count
     for (int i = 0; i < nb && q + 1 < tok.size(); ++i) {
       int b = std::atoi(tok[q].c_str()) - 1, n = std::atoi(tok[q + 1].c_str());
-      q += 2;
+      q += with_overlap ? 3 : 2;
       if (b < 0 || b >= nb || n < 0 || n > na) { err = path + ": bad block 4"; return false; }
       s.n_band_absorb[b] = n;
       for (int j = 0; j < n && q < tok.size(); ++j) s.index_absorb[(size_t)j + (size_t)na * b] = std::atoi(tok[q++].c_str());
@@ -249,20 +501,32 @@ bool read_spectral_file(const std::string &path, SpectralFile &sf, std::string &
   if (b5) {
     const auto &L = b5->lines;
     size_t q = 4;
+    // version 1: the self-broadened indices of all absorbers may come first
+    // (read_spectrum.F90:1268-1300)
+    for (size_t h = 0; h < L.size(); ++h) {
+      if (L[h].find("Self-broadened indexing numbers") != std::string::npos) {
+        size_t r = h + 2;
+        while ((int)s.index_sb.size() < s.n_abs && r < L.size())
+          for (auto &x : split(L[r++])) s.index_sb.push_back(std::atoi(x.c_str()));
+      }
+      if (L[h].rfind("Band        Gas, Number of k-terms", 0) == 0) { q = h + 3; break; }
+    }
     while (q < L.size()) {
       auto w = split(L[q]);
       if (w.size() < 5 || !is_int(w[0])) { ++q; continue; }
       Rec r{std::atoi(w[0].c_str()) - 1, std::atoi(w[1].c_str()) - 1, std::atoi(w[2].c_str()),
             std::atoi(w[3].c_str()), std::atoi(w[4].c_str()), 0.0, 0.0, {}};
-      if (r.fnc == SOCGPU_IP_SCALE_LOOKUP || r.fnc == SOCGPU_IP_SCALE_T_LOOKUP) {
-        err = path + ": lookup-table k scaling is not supported";
-        return false;
-      }
       if (q + 1 >= L.size()) break;
       auto pt = split(L[q + 1]);
-      if (pt.size() < 2) { err = path + ": bad block 5"; return false; }
-      r.p = num(pt[0]);
-      r.t = num(pt[1]);
+      if (r.fnc == SOCGPU_IP_SCALE_LOOKUP) {
+        if (pt.size() < 2) { err = path + ": bad block 5 table extents"; return false; }
+        s.n_pre = std::atoi(pt[0].c_str());
+        s.n_tmp = std::atoi(pt[1].c_str());
+      } else if (r.fnc != SOCGPU_IP_SCALE_T_LOOKUP) {
+        if (pt.size() < 2) { err = path + ": bad block 5"; return false; }
+        r.p = num(pt[0]);
+        r.t = num(pt[1]);
+      }
       q += 2;
       const int nsv = n_scale_variable(r.fnc);
       for (int t = 0; t < r.nk && q < L.size(); ++t) {
@@ -315,6 +579,19 @@ bool read_spectral_file(const std::string &path, SpectralFile &sf, std::string &
       for (size_t v = 0; v < r.terms[t].sc.size(); ++v) s.scale[v + nsv * tbg] = r.terms[t].sc[v];
     }
   }
+  // the lookup tables (read_spectrum.F90:1420-1560)
+  {
+    std::vector<std::array<int, 3>> lrecs;
+    bool any = false;
+    for (const Rec &r : recs) {
+      lrecs.push_back({r.b, r.g, r.fnc});
+      any |= r.fnc == SOCGPU_IP_SCALE_LOOKUP || r.fnc == SOCGPU_IP_SCALE_T_LOOKUP;
+    }
+    if (any && !read_k_file(k_path.empty() ? path + "_k" : k_path, s, lrecs, err)) return false;
+  }
+  if (!wenyi_path.empty() && !read_wenyi(wenyi_path, s, err)) return false;
+  s.molar_weight.assign(na, 0.0);
+  for (int g = 0; g < s.n_abs; ++g) s.molar_weight[g] = molar_weight_of(s.type_absorb[g]);
   // block 6
   if (const Block *b6 = first(6)) {
     size_t h = 0;
@@ -452,10 +729,16 @@ using namespace socgpu;
 
 extern "C" int socgpu_spectrum_load(const char *name, const char *path, socgpu_spectrum_handle *handle, char *msg,
                                     size_t msg_len) {
+  return socgpu_spectrum_load_ext(name, path, nullptr, nullptr, handle, msg, msg_len);
+}
+
+extern "C" int socgpu_spectrum_load_ext(const char *name, const char *path, const char *k_path,
+                                        const char *wenyi_path, socgpu_spectrum_handle *handle, char *msg,
+                                        size_t msg_len) {
   if (!name || !path || !handle) { set_msg(msg, msg_len, "null argument"); return SOCGPU_I_ERR_FATAL; }
   SpectralFile sf;
   std::string err;
-  if (!read_spectral_file(path, sf, err)) {
+  if (!read_spectral_file(path, k_path ? k_path : "", wenyi_path ? wenyi_path : "", sf, err)) {
     set_msg(msg, msg_len, "%s", err.c_str());
     return SOCGPU_I_ERR_IO;
   }

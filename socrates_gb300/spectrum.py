@@ -446,19 +446,30 @@ class Spectrum:
             for b in range(self.n_band):
                 L.append(f"{b + 1:5d}       {e(self.rayleigh_coeff[b])}")
             L.append("*END")
-        L.append("*BLOCK: TYPE =    4: SUBTYPE =    0: VERSION =    0")
+        v4 = self.i_overlap is not None
+        L.append(f"*BLOCK: TYPE =    4: SUBTYPE =    0: VERSION =    {1 if v4 else 0}")
         L.append("Gaseous absorbers in each interval")
         L.append("(The number is the indexing number of the species as set out")
         L.append(" in the summary block 0.)")
         L.append("A zero indicates that there in no gaseous absorption in the interval.")
-        L.append("Band        Number of active absorbers followed by indexing numbers")
+        L.append("Band, number of absorbers and overlap method, followed by indexing numbers" if v4 else
+                 "Band        Number of active absorbers followed by indexing numbers")
         for b in range(self.n_band):
-            L.append(f"{b + 1:5d}       {int(self.n_band_absorb[b]):5d}")
+            L.append(f"{b + 1:5d}       {int(self.n_band_absorb[b]):5d}"
+                     + (f"       {int(self.i_overlap[b]):5d}" if v4 else ""))
             if self.n_band_absorb[b] > 0:
                 L.append("   " + "".join(f"{int(self.index_absorb[j, b]):5d}" for j in range(int(self.n_band_absorb[b]))))
         L.append("*END")
-        L.append("*BLOCK: TYPE =    5: SUBTYPE =    0: VERSION =    0")
+        tables = self.k_lookup is not None or self.k_t_lookup_gas is not None
+        L.append(f"*BLOCK: TYPE =    5: SUBTYPE =    0: VERSION =    {1 if tables else 0}")
         L.append("Exponential sum fiting coefficients: (exponents: m2/kg)")
+        if self.index_sb is not None and self.k_lookup_sb is not None:
+            # read_spectrum.F90 block 5_0_1: (/,6(2x, i3))
+            L.append("Self-broadened indexing numbers of all absorbers.")
+            L.append("(Zero means no self-broadening.)")
+            isb = [int(x) for x in self.index_sb]
+            for q in range(0, len(isb), 6):
+                L.append("".join(f"  {x:3d}" for x in isb[q:q + 6]))
         L.append("Band        Gas, Number of k-terms, Scaling type and scaling function,")
         L.append("             followed by reference pressure and temperature,")
         L.append("                   k-terms, weights and scaling parameters.")
@@ -468,7 +479,13 @@ class Spectrum:
                 nk = int(self.i_band_k[b, g])
                 fnc = int(self.i_scale_fnc[b, g])
                 L.append(f"{b + 1:5d}       {g + 1:5d}       {nk:5d}       {int(self.i_scale_k[b, g]):5d}       {fnc:5d}")
-                L.append(f"      {e(self.p_ref[g, b])}      {e(self.t_ref[g, b])}")
+                if fnc == abi.IP_SCALE_LOOKUP:            # (2(7x, i5)): table extents
+                    n_tmp, n_pre = self.t_lookup.shape
+                    L.append(f"       {n_pre:5d}       {n_tmp:5d}")
+                elif fnc == abi.IP_SCALE_T_LOOKUP:        # (14x, i5)
+                    L.append(" " * 14 + f"{int(self.n_t_lookup_gas[g]):5d}")
+                else:
+                    L.append(f"      {e(self.p_ref[g, b])}      {e(self.t_ref[g, b])}")
                 for kk in range(nk):
                     # read_spectrum.F90 block 5: (2(3x, 1pe16.9), i3, :, (t42, 1pe16.9, 3x, 1pe16.9))
                     vals = [self.scale[v, kk, b, g] for v in range(N_SCALE_VARIABLE.get(fnc, 0))]
@@ -542,6 +559,81 @@ class Spectrum:
                 L.append("*END")
         with open(path, "w") as fh:
             fh.write("\n".join(L) + "\n")
+
+    def write_k_file(self, path) -> None:
+        """Write the lookup tables in the '_k' companion file's record layouts,
+        in the order read_spectrum.F90:1420-1560 reads them."""
+        def rows(vals):
+            out = []
+            vals = list(vals)
+            for q in range(0, len(vals), 6):
+                out.append("".join(f"{v:13.6E}" for v in vals[q:q + 6]))
+            return out
+        L = []
+        recs = [(b, int(self.index_absorb[j, b]) - 1) for b in range(self.n_band)
+                for j in range(int(self.n_band_absorb[b]))]
+        if self.k_lookup is not None:
+            n_tmp, n_pre = self.t_lookup.shape
+            L += ["*BLOCK: k-table", "", f"Lookup table: {n_pre:4d} pressures, {n_tmp:4d} temperatures."]
+            for ip in range(n_pre):
+                L += rows([np.exp(self.p_lookup[ip])] + list(self.t_lookup[:, ip]))
+            sb = self.index_sb is not None and self.k_lookup_sb is not None
+            if sb:
+                L += ["", f"Gas fractions:{self.gf_lookup.size:4d}"] + rows(self.gf_lookup)
+            for b, g in recs:
+                if int(self.i_scale_fnc[b, g]) != abi.IP_SCALE_LOOKUP:
+                    continue
+                nk = int(self.i_band_k[b, g])
+                L += ["", f"Band: {b + 1:4d}, gas: {g + 1:4d}, k-terms: {nk:4d}"]
+                for t in range(nk):
+                    if sb and self.index_sb[g] > 0:
+                        for ig in range(self.gf_lookup.size):
+                            for ip in range(n_pre):
+                                L += rows(self.k_lookup_sb[:, ip, ig, t, self.index_sb[g] - 1, b])
+                    else:
+                        for ip in range(n_pre):
+                            L += rows(self.k_lookup[:, ip, t, g, b])
+            L.append("*END")
+        if self.k_t_lookup_gas is not None:
+            ndt = self.t_lookup_gas.shape[0]
+            L += ["*BLOCK: temperature k-tables", "", f"nd_t =   {ndt:4d}"]
+            for g in range(self.n_absorb):
+                if int(self.n_t_lookup_gas[g]) > 1:
+                    n = int(self.n_t_lookup_gas[g])
+                    L += ["", "Temperatures of absorber   " + f"{n:4d}"] + rows(self.t_lookup_gas[:n, g])
+            for b, g in recs:
+                if int(self.i_scale_fnc[b, g]) != abi.IP_SCALE_T_LOOKUP:
+                    continue
+                n = int(self.n_t_lookup_gas[g])
+                L += ["", f"Band: {b + 1:4d}, gas: {g + 1:4d}"]
+                for t in range(int(self.i_band_k[b, g])):
+                    L += rows(self.k_t_lookup_gas[:n, t, g, b])
+            L.append("*END")
+        Path(path).write_text("\n".join(L) + "\n")
+
+    def write_wenyi_source(self, path) -> None:
+        """Write the Wen-Yi tables as Fortran array constants in the form of
+        the module that defines them, one array per temperature of each
+        band table (the form read_wenyi_tables and socgpu_spectrum_load_ext
+        read)."""
+        L = ["MODULE scale_wenyi_tables"]
+
+        def arr(name, vals):
+            vals = [f"{v:.9E}_RealK" for v in vals]
+            L.append(f"  REAL (RealK), PARAMETER :: {name}({len(vals)}) = (/ &")
+            for q in range(0, len(vals), 3):
+                tail = ", &" if q + 3 < len(vals) else " /)"
+                L.append("     " + ",".join(vals[q:q + 3]) + tail)
+        arr("plg", self.wenyi_plg)
+        arr("ttb", self.wenyi_ttb)
+        arr("tto", self.wenyi_tto)
+        arr("gk250b", self.wenyi_gk250b)
+        for t in range(self.wenyi_gk4.shape[0]):
+            arr(f"gk4_{t + 1}", self.wenyi_gk4[t].reshape(-1))
+        for t in range(self.wenyi_gk6.shape[0]):
+            arr(f"gk6_{t + 1}", self.wenyi_gk6[t].reshape(-1))
+        L.append("END MODULE scale_wenyi_tables")
+        Path(path).write_text("\n".join(L) + "\n")
 
     @classmethod
     def read_text(cls, path, name: str | None = None, k_path=None) -> "Spectrum":

@@ -27,10 +27,11 @@ def field(path, coord="plev"):
     return v.get(coord), v[names[0]]
 
 
-def write_cdl(path, name, dims, variables):
+def write_cdl(path, name, dims, variables, digits=7):
     """Write a CDL file like the reference's column files: `dims` is a list
     of (name, length); `variables` a list of (name, dim names, values,
-    {attribute: text}) with values in C order."""
+    {attribute: text}) with values in C order, printed with `digits`
+    significant digits (the reference's files carry 7)."""
     lines = [f"netcdf {name}{{", "", "dimensions:"]
     for d, n in dims:
         lines.append(f"    {d:<15s}= {n:3d};")
@@ -41,7 +42,7 @@ def write_cdl(path, name, dims, variables):
             lines.append(f'             {v}:{k} = "{t}";')
     lines += ["", "data:"]
     for v, _, vals, _ in variables:
-        flat = [f"{x: .6E}" for x in np.ravel(vals)]
+        flat = [f"{x: .{digits - 1}E}" for x in np.ravel(vals)]
         body = ",\n                    ".join(", ".join(flat[i:i + 4]) for i in range(0, len(flat), 4))
         lines.append(f"{v:>17s} = {body};")
     lines += ["", "}"]

@@ -126,6 +126,8 @@ def _self_broadened(sp):
     ksb = np.zeros((n_tmp, n_pre, 3, nk, 1, nb))
     for ig in range(3):
         ksb[:, :, ig, :, 0, :] = sp.k_lookup[:, :, :, iw, :] * (1.0 + 2.0 * ig)
+    # 7 significant digits, as the '_k' file records them (1PE13.6)
+    ksb = np.array([float(f"{v:.6E}") for v in ksb.ravel(order="F")]).reshape(ksb.shape, order="F")
     sp.k_lookup_sb = np.asfortranarray(ksb)
     return sp
 

@@ -263,3 +263,43 @@ def test_reference_spectral_file_round_trip(tmp_path):
         a, b = getattr(back, name), getattr(sp, name)
         m = min(a.shape[0], b.shape[0])
         np.testing.assert_allclose(a[:m], b[:m], rtol=1e-9, atol=0, err_msg=name)
+
+
+@pytest.mark.parametrize("kind", ["plain", "self_broadened", "temperature_tables"])
+def test_k_file_round_trip(tmp_path, kind):
+    """The GA7 long-wave file and its lookup tables (P/T, self-broadened,
+    temperature-only) written in the reference's record layouts (block 5
+    version 1 and the '_k' file) and read back give the same arrays; the
+    Wen-Yi tables round-trip through their Fortran-constant form."""
+    import test_lookup_gpu as T
+    from socrates_gb300.spectrum import Spectrum, read_wenyi_tables
+    sp = T._ga7_lw()
+    if kind == "self_broadened":
+        sp = T._self_broadened(sp)
+    elif kind == "temperature_tables":
+        sp = T._temperature_tables(sp)
+    path = tmp_path / "sp_lw"
+    sp.write_text(path)
+    sp.write_k_file(str(path) + "_k")
+    back = Spectrum.read_text(path)
+    for name in ("i_scale_fnc", "i_band_k", "index_absorb", "index_sb", "n_t_lookup_gas"):
+        if getattr(sp, name) is not None:
+            np.testing.assert_array_equal(getattr(back, name), getattr(sp, name), err_msg=name)
+    for name in ("k", "w", "p_lookup", "t_lookup", "k_lookup", "gf_lookup", "k_lookup_sb", "t_lookup_gas",
+                 "k_t_lookup_gas"):
+        a = getattr(sp, name)
+        if a is None:
+            continue
+        if name == "k_lookup":
+            # only (band, absorber) pairs with P/T tables have them, and a
+            # self-broadened absorber's tables are read into k_lookup_sb only
+            a = a.copy()
+            for b in range(sp.n_band):
+                for g in range(sp.n_absorb):
+                    if sp.i_scale_fnc[b, g] != abi.IP_SCALE_LOOKUP or (sp.index_sb is not None and sp.index_sb[g]):
+                        a[:, :, :, g, b] = 0.0
+        np.testing.assert_allclose(getattr(back, name), a, rtol=1e-12, atol=0, err_msg=name)
+    wy = tmp_path / "wy.f90"
+    sp.write_wenyi_source(wy)
+    for k, v in read_wenyi_tables(wy).items():
+        np.testing.assert_array_equal(v, getattr(sp, k), err_msg=k)

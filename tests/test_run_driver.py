@@ -17,8 +17,8 @@ from cdl import field, read_cdl, write_cdl
 from socrates_gb300 import build
 
 ROOT = Path(__file__).resolve().parent.parent
-SUFFIX = {1: "q", 2: "co2", 3: "o3", 4: "n2o", 6: "ch4", 14: "cfc11", 15: "cfc12", 16: "cfc113", 17: "hcfc22",
-          18: "hfc125", 19: "hfc134a"}
+SUFFIX = {1: "q", 2: "co2", 3: "o3", 4: "n2o", 6: "ch4", 7: "o2", 9: "so2", 14: "cfc11", 15: "cfc12",
+          16: "cfc113", 17: "hcfc22", 18: "hfc125", 19: "hfc134a", 25: "ocs"}
 
 
 def _tool():
@@ -26,32 +26,38 @@ def _tool():
     return str(build.TOOL)
 
 
-def _case27_files(tmp, to_cdf=False):
-    """The case's inputs written as column files like the reference's."""
-    d = np.load(K.FIXTURE)
-    from socrates_gb300.spectrum import Spectrum
-    sp = Spectrum.load_npz(K.FIXTURE, prefix="sp_")
-    sp_path = tmp / "sp_lw_hadcm3"
+def _column_files(tmp, name, d, sp, sp_name, to_cdf=False, gases=None, wenyi=False, digits=7):
+    """A case's inputs written as column files like the reference's, with the
+    spectral file (and its '_k' tables) written beside them.  gases: the
+    absorber types that have input files (default all); digits: significant
+    digits of the CDL values."""
+    sp_path = tmp / sp_name
     sp.write_text(sp_path)
-    base = tmp / "laer27"
-    dims3 = [("lat", 1), ("lon", 1), ("plev", None)]
+    if sp.k_lookup is not None or sp.k_t_lookup_gas is not None:
+        sp.write_k_file(str(sp_path) + "_k")
+    wy = None
+    if wenyi:
+        wy = tmp / "wenyi_tables.f90"
+        sp.write_wenyi_source(wy)
+    base = tmp / name
     coord = {"units": "degree", "title": "latitude"}
 
-    def put(suffix, plev, values, name, units="None"):
+    def put(suffix, plev, values, vname, units="None"):
         dims = [("lat", 1), ("lon", 1), ("plev", len(plev))]
         variables = [("lat", ["lat"], [0.0], coord), ("lon", ["lon"], [0.0], {"units": "degree", "title": "longitude"}),
                      ("plev", ["plev"], plev, {"units": "Pa", "title": "PRESSURE"}),
-                     (name, ["plev", "lon", "lat"], np.reshape(values, (len(plev), 1, 1)), {"units": units})]
-        path = tmp / f"laer27.{suffix}"
-        write_cdl(path, f"laer27.{suffix}", dims, variables)
+                     (vname, ["plev", "lon", "lat"], np.reshape(values, (len(plev), 1, 1)), {"units": units})]
+        path = tmp / f"{name}.{suffix}"
+        write_cdl(path, f"{name}.{suffix}", dims, variables, digits)
         return path
 
     files = [put("t", d["p"], d["t"], "t", "K"), put("tl", d["p_level"], d["t_level"], "tl", "K")]
     for j, ty in enumerate(sp.type_absorb):
-        files.append(put(SUFFIX[int(ty)], d["p"], d["gas"][:, j], SUFFIX[int(ty)]))
+        if gases is None or int(ty) in gases:
+            files.append(put(SUFFIX[int(ty)], d["p"], d["gas"][:, j], SUFFIX[int(ty)]))
     files.append(put("tstar", [1.013e5], d["t_ground"], "tstar", "K"))
-    surf = tmp / "laer27.surf"
-    write_cdl(surf, "laer27.surf", [("lat", 1), ("lon", 1), ("basis", 1)],
+    surf = tmp / f"{name}.surf"
+    write_cdl(surf, f"{name}.surf", [("lat", 1), ("lon", 1), ("basis", 1)],
               [("lat", ["lat"], [1.0], {}), ("lon", ["lon"], [0.0], {}), ("basis", ["basis"], [1.0], {}),
                ("alb", ["basis", "lat", "lon"], np.reshape(d["alb"], (1, 1, 1)), {"title": "ALBEDO WEIGHTS"})])
     files.append(surf)
@@ -61,6 +67,13 @@ def _case27_files(tmp, to_cdf=False):
             tmp_out = f.with_name(f.name + ".cdf")
             subprocess.run([tool, "--convert", str(f), str(tmp_out)], check=True)
             tmp_out.replace(f)
+    return sp_path, base, wy
+
+
+def _case27_files(tmp, to_cdf=False):
+    from socrates_gb300.spectrum import Spectrum
+    sp = Spectrum.load_npz(K.FIXTURE, prefix="sp_")
+    sp_path, base, _ = _column_files(tmp, "laer27", np.load(K.FIXTURE), sp, "sp_lw_hadcm3", to_cdf)
     return sp_path, base
 
 
@@ -121,3 +134,76 @@ def test_driver_reproduces_icrccm27(gpu_lib, tmp_path, to_cdf):
     assert r.returncode == 0, r.stderr
     _, hr_mixed = field(out) if not to_cdf else (None, hr)
     assert np.abs(hr_mixed - kgo).max() <= 0.05
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("to_cdf", [False, True])
+def test_driver_reproduces_circ6_ga7(gpu_lib, tmp_path, to_cdf):
+    """CIRC case 6 with the GA7 long-wave file through the column driver
+    (examples/netcdf/CIRC_case6/run_me: -R 1 9 -I -g 4 -c -C 5): the spectral
+    file with its '_k' lookup tables and the Wen-Yi tables (-W) read by the
+    C++ loader, absorbers without input files taken as absent."""
+    import circ6 as K6
+    from socrates_gb300.spectrum import Spectrum
+    tool = _tool()
+    d = np.load(K6.FIXTURE)
+    sp = Spectrum.load_npz(K6.FIXTURE, prefix="sp_")
+    # the case's inputs are single-precision netCDF values: CDL with 17 digits
+    # carries them exactly
+    sp_path, base, wy = _column_files(tmp_path, "case6", d, sp, "sp_lw_ga7", to_cdf,
+                                      gases=set(int(x) for x in d["gases_present"]), wenyi=True, digits=17)
+    cmd = [tool, "-s", str(sp_path), "-R", "1", "9", "-I", "-g", "4", "-c", "-C", "5", "-B", str(base),
+           "-W", str(wy)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = str(base) + ".hrts"
+    if to_cdf:
+        scipy_io = pytest.importorskip("scipy.io")
+        with scipy_io.netcdf_file(out, "r", mmap=False) as nc:
+            hr = np.array(nc.variables["hrts"][:]).ravel()
+    else:
+        _, hr = field(out)
+    kgo = d["kgo_hrts"]
+    if to_cdf:
+        assert np.abs(hr - kgo).max() <= 2e-5 * np.abs(kgo).max()
+    else:
+        half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
+        assert (np.abs(hr - kgo) / half_unit).max() <= 1.05
+    # without the Wen-Yi tables the band-4 CO2 terms cannot be scaled
+    r = subprocess.run(cmd[:-2], capture_output=True, text=True)
+    assert r.returncode != 0 and "Wen-Yi" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["self_broadened", "temperature_tables"])
+def test_loader_reads_self_broadened_and_temperature_tables(gpu_lib, tmp_path, kind):
+    """Self-broadened and temperature-only tables written in the '_k'
+    layouts, read back by the C++ loader (socgpu_spectrum_load_ext) and
+    solved on the GPU, match the oracle on the arrays they were written from."""
+    import ctypes as C
+    import oracle as O
+    import test_lookup_gpu as T
+    from socrates_gb300 import abi, synth
+    from socrates_gb300 import radiance as R
+    sp = (T._self_broadened if kind == "self_broadened" else T._temperature_tables)(T._ga7_lw())
+    sp_path = tmp_path / "sp"
+    sp.write_text(sp_path)
+    sp.write_k_file(str(sp_path) + "_k")
+    wy = tmp_path / "wy.f90"
+    sp.write_wenyi_source(wy)
+    lib = R.load_library()
+    h = C.c_int(0)
+    msg = C.create_string_buffer(512)
+    name = f"loaded_{kind}".encode()
+    st = lib.socgpu_spectrum_load_ext(name, str(sp_path).encode(), None, str(wy).encode(), C.byref(h), msg, 512)
+    assert st == 0, msg.value.decode()
+    col = synth.operational_case(sp, 33, 40, seed=51, solar=False)
+    ctl = R.lw_control(l_continuum=True, i_gas_overlap=abi.IP_OVERLAP_K_EQV_SCL)
+    m = R.Marshal(ctl, sp, col)
+    st = lib.socgpu_radiance_calc(*m.args(h.value), msg, 512)
+    assert st == 0, msg.value.decode()
+    got = m.result()
+    ref = O.radiance_calc(ctl, sp, col)
+    fscale = np.abs(ref["flux_up"]).max()
+    for k in ("flux_up", "flux_down"):
+        assert np.abs(got[k] - ref[k]).max() <= 1e-10 * fscale, k
