@@ -36,7 +36,7 @@ extern "C" {
 #define SOCGPU_API
 #endif
 
-#define SOCGPU_ABI_VERSION 3
+#define SOCGPU_ABI_VERSION 4
 
 /* ---- status codes: rad_pcf.F90:391-405 ------------------------------- */
 #define SOCGPU_I_NORMAL             0
@@ -274,6 +274,10 @@ typedef struct socgpu_bound {
     const double *solar_irrad;   /* (nd_profile) [W/m2] */
     const double *rho_alb;       /* (nd_profile, 2, nd_band): diffuse (1) and direct (2) albedo */
     const double *t_ground;      /* (nd_profile) [K] */
+    /* (nd_profile, nd_band) [W/m2] or NULL: the surface's Planck flux in each
+       band in place of that of t_ground (planck%flux_ground of
+       diff_planck_source_mod.F90:123-135, l_flux_ground and surface tiles) */
+    const double *flux_ground;
 } socgpu_bound;
 
 /* ---- StrAer modal part (src/radiance_core/def_aer.F90:36-44) ---------- */
@@ -438,6 +442,71 @@ SOCGPU_API int socgpu_cloud_gen_device_noalloc(int nd_layer, int cloud_top, int 
                             const double *zf, const double *xcw,
                             int *n_subcol_cld, double *c_sub, int rng,
                             void *stream, char *msg, size_t msg_len);
+
+/* ---- runes: the model-facing interface ---------------------------------
+ * socgpu_runes replaces runes (src/interface_core/socrates_runes.F90:47-1079)
+ * for clear-sky calls: set_control's defaults (socrates_set_control.F90:
+ * 232-300), the absorbers of the spectrum filled from profiles or
+ * well-mixed values (socrates_set_atm.F90:535-622), the surface from a grey
+ * or per-band albedo, per-band emission and tiles (socrates_set_bound.F90,
+ * diff_planck_source_mod.F90:123-190), and the diagnostics of
+ * socrates_set_diag.F90:140-220.  Arrays have the profile index fastest. */
+#define SOCGPU_IP_SOURCE_ILLUMINATE 1   /* socrates_runes.F90: the solar source */
+#define SOCGPU_IP_SOURCE_THERMAL    2   /* the thermal source */
+#define SOCGPU_RUNES_N_GAS         80   /* gas identifiers 1..79 of gas_list_pcf.F90 */
+
+typedef struct socgpu_runes_args {
+    int n_profile, n_layer;
+    const char *spectrum_name;          /* registered or loaded under this name (set_spectrum) */
+    int i_source;                       /* SOCGPU_IP_SOURCE_ILLUMINATE | SOCGPU_IP_SOURCE_THERMAL */
+    /* atmosphere: (n_profile, n_layer) and (n_profile, 0:n_layer) */
+    const double *p_layer, *t_layer, *mass, *density, *p_level, *t_level;
+    /* absorbers by gas identifier (the <gas>, <gas>_mix_ratio and
+       l_<gas>_well_mixed arguments): a profile (n_profile, n_layer), or the
+       well-mixed value where there is no profile or gas_well_mixed is set
+       with has_mix_ratio; anything else is absent */
+    const double *gas[SOCGPU_RUNES_N_GAS];
+    double gas_mix_ratio[SOCGPU_RUNES_N_GAS];
+    int has_mix_ratio[SOCGPU_RUNES_N_GAS];
+    int gas_well_mixed[SOCGPU_RUNES_N_GAS];
+    int l_invert;                       /* vertical arrays given surface first */
+    /* surface */
+    const double *t_ground;             /* (n_profile) [K] */
+    int l_flux_ground;
+    const double *flux_ground;          /* (n_profile, n_band) surface emission per band [W/m2] */
+    const double *cos_zenith_angle, *solar_irrad;   /* (n_profile) */
+    int l_grey_albedo;
+    double grey_albedo;
+    const double *albedo_diff, *albedo_dir;         /* (n_profile, n_band), when not grey */
+    int l_tile, n_tile;
+    const int *l_flux_tile;             /* (n_tile): the tile's emission is given */
+    const double *frac_tile, *t_tile;   /* (n_profile, n_tile) */
+    const double *flux_tile;            /* (n_profile, n_tile, n_band) [W/m2] */
+    const double *albedo_diff_tile, *albedo_dir_tile;   /* (n_profile, n_tile, n_band) or NULL */
+    /* options; 0 selects set_control's default */
+    int i_scatter_method, i_gas_overlap;
+    int l_rayleigh, l_mixing_ratio;
+    /* modal aerosol optical properties */
+    int l_aerosol_mode, n_aer_mode;
+    const double *aer_mix_ratio;        /* (n_profile, n_layer, n_aer_mode) */
+    const double *aer_absorption, *aer_scattering, *aer_asymmetry;  /* (n_profile, n_layer, n_aer_mode, n_band) */
+    const double *layer_heat_capacity;  /* (n_profile, n_layer) [J/(m2 K)] or NULL */
+    int precision;                      /* SOCGPU_PRECISION_* */
+} socgpu_runes_args;
+
+/* StrDiag (socrates_def_diag.F90): NULL members are not filled. */
+typedef struct socgpu_runes_diag {
+    double *heating_rate;   /* (n_profile, n_layer): [K/s] with layer_heat_capacity, else the
+                               layer's flux divergence [W/m2] */
+    double *flux_up, *flux_down, *flux_direct;                   /* (n_profile, 0:n_layer) */
+    double *flux_up_surf, *flux_down_surf, *flux_direct_surf;    /* (n_profile) */
+    double *flux_up_toa, *flux_down_toa, *flux_direct_toa;       /* (n_profile) */
+} socgpu_runes_diag;
+
+/* runes (socrates_runes.F90:47) on the GPU: maps the arguments, calls
+ * socgpu_radiance_calc with host arrays and fills the diagnostics.  Clouds
+ * are not taken through this interface (socgpu_radiance_calc runs McICA). */
+SOCGPU_API int socgpu_runes(const socgpu_runes_args *args, socgpu_runes_diag *diag, char *msg, size_t msg_len);
 
 /* ---- multi-batch launches (extension) -----------------------------------
  * Many column batches of different layer counts, spectra, options and

@@ -1364,7 +1364,10 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
                             + IX2(w.planck_flux, l, i - 1, wp) - 2.0 * bt);
                     }
             for (int l = 0; l < np; ++l) {
-                w.flux_ground[l] = planck_flux_band(d, b, bd->t_ground[p0 + l]);
+                /* the surface's Planck flux given per band (l_flux_ground and tiles,
+                 * diff_planck_source_mod.F90:123-135), else that of t_ground */
+                w.flux_ground[l] = bd->flux_ground ? IX2(bd->flux_ground, p0 + l, b, ndp)
+                                                   : planck_flux_band(d, b, bd->t_ground[p0 + l]);
                 w.flux_inc_direct[l] = 0.0;
                 w.flux_inc_down[l] = -IX2(w.planck_flux, l, 0, wp);
                 w.d_planck_flux_surface[l] = w.flux_ground[l] - IX2(w.planck_flux, l, n_layer, wp);

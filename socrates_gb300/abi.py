@@ -37,7 +37,7 @@ IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0,
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RNG_LCG, RNG_PHILOX = 0, 1
 NOALLOC_MAX_CLOUD_LAYERS = 1024   # SOCGPU_NOALLOC_MAX_CLOUD_LAYERS
-ABI_VERSION = 3
+ABI_VERSION = 4
 IP_SELF_CONTINUUM, IP_FRN_CONTINUUM = 1, 2
 
 _dp = C.POINTER(C.c_double)
@@ -100,8 +100,40 @@ class Atm(C.Structure):
     ]
 
 
+RUNES_N_GAS = 80
+IP_SOURCE_ILLUMINATE, IP_SOURCE_THERMAL = 1, 2
+
+
+class RunesArgs(C.Structure):
+    """socgpu_runes_args."""
+    _fields_ = [
+        ("n_profile", C.c_int), ("n_layer", C.c_int), ("spectrum_name", C.c_char_p), ("i_source", C.c_int),
+        ("p_layer", _dp), ("t_layer", _dp), ("mass", _dp), ("density", _dp), ("p_level", _dp), ("t_level", _dp),
+        ("gas", _dp * RUNES_N_GAS), ("gas_mix_ratio", C.c_double * RUNES_N_GAS),
+        ("has_mix_ratio", C.c_int * RUNES_N_GAS), ("gas_well_mixed", C.c_int * RUNES_N_GAS),
+        ("l_invert", C.c_int),
+        ("t_ground", _dp), ("l_flux_ground", C.c_int), ("flux_ground", _dp),
+        ("cos_zenith_angle", _dp), ("solar_irrad", _dp),
+        ("l_grey_albedo", C.c_int), ("grey_albedo", C.c_double), ("albedo_diff", _dp), ("albedo_dir", _dp),
+        ("l_tile", C.c_int), ("n_tile", C.c_int), ("l_flux_tile", _ip), ("frac_tile", _dp), ("t_tile", _dp),
+        ("flux_tile", _dp), ("albedo_diff_tile", _dp), ("albedo_dir_tile", _dp),
+        ("i_scatter_method", C.c_int), ("i_gas_overlap", C.c_int), ("l_rayleigh", C.c_int),
+        ("l_mixing_ratio", C.c_int),
+        ("l_aerosol_mode", C.c_int), ("n_aer_mode", C.c_int), ("aer_mix_ratio", _dp), ("aer_absorption", _dp),
+        ("aer_scattering", _dp), ("aer_asymmetry", _dp),
+        ("layer_heat_capacity", _dp), ("precision", C.c_int),
+    ]
+
+
+class RunesDiag(C.Structure):
+    """socgpu_runes_diag."""
+    _fields_ = [(n, _dp) for n in ("heating_rate", "flux_up", "flux_down", "flux_direct", "flux_up_surf",
+                                   "flux_down_surf", "flux_direct_surf", "flux_up_toa", "flux_down_toa",
+                                   "flux_direct_toa")]
+
+
 class Bound(C.Structure):
-    _fields_ = [("zen_0", _dp), ("solar_irrad", _dp), ("rho_alb", _dp), ("t_ground", _dp)]
+    _fields_ = [("zen_0", _dp), ("solar_irrad", _dp), ("rho_alb", _dp), ("t_ground", _dp), ("flux_ground", _dp)]
 
 
 class Aer(C.Structure):
@@ -155,7 +187,7 @@ ABI_FUNCTIONS = (
     "socgpu_cloud_gen_device_noalloc", "socgpu_batch_create", "socgpu_batch_run", "socgpu_batch_tune",
     "socgpu_batch_info", "socgpu_batch_destroy", "socgpu_tune_get", "socgpu_tune_set",
     "socgpu_server_create", "socgpu_server_submit", "socgpu_server_wait", "socgpu_server_stats_get",
-    "socgpu_server_destroy", "socgpu_spectrum_load", "socgpu_spectrum_load_ext",
+    "socgpu_server_destroy", "socgpu_spectrum_load", "socgpu_spectrum_load_ext", "socgpu_runes",
 )
 
 _CALC_ARGS = [C.POINTER(Control), C.POINTER(Dimen), C.c_int, C.POINTER(Atm), C.POINTER(Cld), C.POINTER(Aer),
@@ -172,6 +204,7 @@ def declare(lib: C.CDLL) -> C.CDLL:
     lib.socgpu_spectrum_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_int), C.c_char_p, C.c_size_t]
     lib.socgpu_spectrum_load_ext.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_int),
                                              C.c_char_p, C.c_size_t]
+    lib.socgpu_runes.argtypes = [C.POINTER(RunesArgs), C.POINTER(RunesDiag), C.c_char_p, C.c_size_t]
     lib.socgpu_spectrum_n_gpoint.argtypes = [C.c_int]
     lib.socgpu_spectrum_release.argtypes = [C.c_int]
     lib.socgpu_radiance_calc.argtypes = _CALC_ARGS + [C.c_char_p, C.c_size_t]

@@ -84,6 +84,7 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   }
   e.bands_host.assign(d->n_band, BandInfo{});
   e.gpoints_host.clear();
+  e.type_absorb.assign(d->type_absorb, d->type_absorb + d->n_absorb);
   std::vector<BandInfo> bands_keqv;
   std::vector<GPoint> gpoints_keqv;
   std::vector<TermK> minor;
@@ -613,8 +614,8 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     set_msg(msg, msg_len, "Rayleigh scattering requested without Rayleigh coefficients"); return SOCGPU_I_ERR_FATAL; }
   if (c->isolir == SOCGPU_IP_SOLAR && (!bd->zen_0 || !bd->solar_irrad)) {
     set_msg(msg, msg_len, "solar calculation without zen_0/solar_irrad"); return SOCGPU_I_ERR_FATAL; }
-  if (c->isolir == SOCGPU_IP_INFRA_RED && !bd->t_ground) {
-    set_msg(msg, msg_len, "infra-red calculation without t_ground"); return SOCGPU_I_ERR_FATAL; }
+  if (c->isolir == SOCGPU_IP_INFRA_RED && !bd->t_ground && !bd->flux_ground) {
+    set_msg(msg, msg_len, "infra-red calculation without t_ground or flux_ground"); return SOCGPU_I_ERR_FATAL; }
   if (c->l_continuum && sp->dev.has_continuum &&
       (!atm->density || !atm->gas_mix_ratio || sp->dev.index_water < 1 || sp->dev.index_water > sp->dev.n_species)) {
     set_msg(msg, msg_len, "continuum absorption needs the layer density, the gas mixing ratios and water vapour");
@@ -717,6 +718,7 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
   p.density = atm->density;
   p.nd_species = sp->dev.n_species;
   p.zen_0 = bd->zen_0; p.solar_irrad = bd->solar_irrad; p.rho_alb = bd->rho_alb; p.t_ground = bd->t_ground;
+  p.flux_ground = bd->flux_ground;
   if (p.l_aerosol_mode) {
     p.n_mode = aer->n_mode; p.nd_mode = dm->nd_aerosol_mode;
     p.mode_mix_ratio = aer->mode_mix_ratio; p.mode_absorption = aer->mode_absorption;
@@ -781,6 +783,7 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
   o_si = sw ? plan.add(b->solar_irrad, D, ndp, np, 1) : none;
   o_alb = plan.add(b->rho_alb, D, ndp, np, 2 * nb);
   o_tg = !sw ? plan.add(b->t_ground, D, ndp, np, 1) : none;
+  o_fg = !sw ? plan.add(b->flux_ground, D, ndp, np, nb) : none;
   o_amr = o_aab = o_asc = o_aas = none;
   const size_t ndm = dm->nd_aerosol_mode;
   if (aero) {
@@ -867,7 +870,7 @@ int StagedCall::copy_out_window(char *base, cudaStream_t s, size_t c0, size_t n,
 void window_params(FluxParams &p, int c0, int n) {
   auto mv = [&](auto &ptr) { if (ptr) ptr += c0; };
   mv(p.p); mv(p.t); mv(p.t_level); mv(p.mass); mv(p.gas_mix_ratio); mv(p.density);
-  mv(p.zen_0); mv(p.solar_irrad); mv(p.rho_alb); mv(p.t_ground);
+  mv(p.zen_0); mv(p.solar_irrad); mv(p.rho_alb); mv(p.t_ground); mv(p.flux_ground);
   mv(p.mode_mix_ratio); mv(p.mode_absorption); mv(p.mode_scattering); mv(p.mode_asymmetry);
   mv(p.condensed_mix_ratio); mv(p.condensed_dim_char); mv(p.w_cloud); mv(p.frac_cloud);
   mv(p.c_sub); mv(p.frac_cloudy); mv(p.n_subcol_cld);
@@ -884,6 +887,7 @@ void StagedCall::params(char *base, FluxParams &p) const {
   socgpu_bound b2 = *bound;
   b2.zen_0 = (const double *)dptr(o_z); b2.solar_irrad = (const double *)dptr(o_si);
   b2.rho_alb = (const double *)dptr(o_alb); b2.t_ground = (const double *)dptr(o_tg);
+  b2.flux_ground = (const double *)dptr(o_fg);
   socgpu_aer e2{};
   if (aero) {
     e2 = *aer;

@@ -810,7 +810,10 @@ struct FluxKernel {
       if (lw) {
         v[0] = -S.planck[bi * (LP + 1) + LP];
         v[1] = R(0);
-        if constexpr (kFP64) {
+        if (p.flux_ground) {
+          // the surface's Planck flux given per band (l_flux_ground, tiles)
+          v[4] = load_in<R>(p.flux_ground + (size_t)col + (size_t)ndp * b) - S.planck[bi * (LP + 1) + level_slot(L)];
+        } else if constexpr (kFP64) {
           double bg = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_ground, col, 0, ndp) / p.t_ref_planck);
           v[4] = bg - S.planck[bi * (LP + 1) + level_slot(L)];
         } else {

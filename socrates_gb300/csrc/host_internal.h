@@ -31,6 +31,7 @@ struct SpectrumEntry {
   SpectrumDev dev{};
   std::vector<BandInfo> bands_host;
   std::vector<GPoint> gpoints_host;
+  std::vector<int> type_absorb;       // gas identifier of each absorber (runes maps gases by name)
   int device = 0;
 };
 
@@ -103,7 +104,7 @@ struct StagedCall {
   const socgpu_bound *bound = nullptr;
   socgpu_radout *radout = nullptr;
   bool sw = false, mc = false, aero = false;
-  size_t o_p, o_t, o_tl, o_m, o_g, o_rho, o_z, o_si, o_alb, o_tg, o_amr, o_aab, o_asc, o_aas, o_wb;
+  size_t o_p, o_t, o_tl, o_m, o_g, o_rho, o_z, o_si, o_alb, o_tg, o_amr, o_aab, o_asc, o_aas, o_wb, o_fg = (size_t)-1;
   size_t o_cmr, o_cdc, o_wc, o_fc, o_cs, o_fcl, o_nsc, o_sk, o_fsk, o_sro;
   size_t o_fu, o_fd, o_fdir, o_div, o_hr;
 

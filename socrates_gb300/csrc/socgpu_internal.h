@@ -153,6 +153,7 @@ struct FluxParams {
   int nd_species;
   // bound
   const double *zen_0, *solar_irrad, *rho_alb, *t_ground;
+  const double *flux_ground;        // (nd_profile, nd_band) surface Planck flux per band, or null
   // aerosol
   int n_mode, nd_mode;
   const double *mode_mix_ratio, *mode_absorption, *mode_scattering, *mode_asymmetry;

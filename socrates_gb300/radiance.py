@@ -205,6 +205,7 @@ class Marshal:
         b = abi.Bound()
         b.zen_0, b.solar_irrad = _dp(col.zen_0, k), _dp(col.solar_irrad, k)
         b.rho_alb, b.t_ground = _dp(col.rho_alb, k), _dp(col.t_ground, k)
+        b.flux_ground = _dp(getattr(col, "flux_ground", None), k)
         self.bound = b
         self.aer = abi.Aer()
         if control.l_aerosol_mode and col.aer:

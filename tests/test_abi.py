@@ -71,3 +71,36 @@ def test_tile_table_validation(lib):
     assert lib.socgpu_tune_set(0, 1, 100, 8, 13, 8) == abi.I_ERR_RANGE     # FP64 has no 8-lane kernels
     assert lib.socgpu_tune_set(1, 1, 100, 0, 0, 0) == abi.I_NORMAL          # remove
     assert lib.socgpu_tune_get(1, 1, 100, C.byref(a), C.byref(b), C.byref(c)) == abi.I_ERR_EXIST
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ctypes mirror in abi.py has the size and field offsets of its
+    struct in include/socgpu.h, as gcc lays them out."""
+    import ctypes as C
+    import subprocess
+    from pathlib import Path
+    from socrates_gb300 import abi
+    root = Path(__file__).resolve().parent.parent
+    mirrors = {"socgpu_spectrum_desc": abi.SpectrumDesc, "socgpu_control": abi.Control, "socgpu_dimen": abi.Dimen,
+               "socgpu_atm": abi.Atm, "socgpu_bound": abi.Bound, "socgpu_aer": abi.Aer, "socgpu_cld": abi.Cld,
+               "socgpu_radout": abi.Radout, "socgpu_runes_args": abi.RunesArgs, "socgpu_runes_diag": abi.RunesDiag,
+               "socgpu_batch_item": abi.BatchItem, "socgpu_server_config": abi.ServerConfig,
+               "socgpu_server_stats": abi.ServerStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "socgpu.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{root / 'include'}", str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        cname, field, value = ln.split()
+        got[(cname, field)] = int(value)
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, f"{cname}.{fname}"

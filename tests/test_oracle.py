@@ -204,7 +204,7 @@ def test_cloud_gen_compaction_and_fraction():
 
 
 # ---------------------------------------------------------------------------
-KGO_FIXTURES = ("icrccm", "circ6", "ga7")
+KGO_FIXTURES = ("icrccm", "circ6", "ga7", "runes")
 
 
 @pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(KGO_FIXTURES)))
@@ -244,6 +244,25 @@ def test_oracle_reproduces_circ6_ga7_known_good_output():
     half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
     err = np.abs(hr - kgo) / half_unit
     assert err.max() <= 1.0, f"layer {err.argmax()}: {hr[err.argmax()]} vs {kgo[err.argmax()]}"
+
+
+@pytest.mark.parametrize("section", ["sw", "lw_tground", "lw_flux_ground", "lw_tiles"])
+def test_oracle_reproduces_runes_ga9_known_good_output(section):
+    """Pin against the reference's runes test (src/aux/runes_driver.f90,
+    examples/runes/gfortran_8_1_0.txt) with the GA9 spectral files: a solar
+    call with Rayleigh scattering and three thermal calls whose surface is a
+    skin temperature, an emission per band, or two tiles.  The oracle is run
+    with the control runes sets up (socrates_set_control.F90:232-300) and the
+    surface emission socrates_set_bound.F90 forms.  The printed fluxes and
+    K/day heating rates (8 decimals) must agree to 1e-8; the reference's own
+    outputs from different compilers differ by up to 3.4e-7."""
+    import runes_case as RC
+    d = RC.data()
+    sw, lw = RC.spectra()
+    ctl, sp, col = RC.direct_case(d, sw, lw, section)
+    got = RC.printed(O.radiance_calc(ctl, sp, col), RC.derived(d)[2])
+    err = np.abs(got - d["kgo_" + section])
+    assert err.max() <= 1e-8, f"level {err.max(axis=1).argmax() + 1}: max error {err.max():.2e}"
 
 
 def test_reference_spectral_file_round_trip(tmp_path):
