@@ -87,7 +87,11 @@ extern "C" {
 #define SOCGPU_IP_PHASE_WATER           1
 #define SOCGPU_IP_PHASE_ICE             2
 /* condensed-phase parametrizations, rad_pcf.F90:206,486 */
+/* cloud parametrization schemes (rad_pcf.F90:200-209, 447-486) */
+#define SOCGPU_IP_SLINGO_SCHRECKER      1   /* droplets: k = q (a1 + a2/re), 1 - w = a3 + a4 re, g = a5 + a6 re */
 #define SOCGPU_IP_DROP_PADE_2           5
+#define SOCGPU_IP_SLINGO_SCHRECKER_ICE  1   /* ice: the same form in the ice dimension */
+#define SOCGPU_IP_ICE_FU_PHF           12   /* Fu's ice fits, one phase-function moment (opt_prop_fu_phf_mod.F90) */
 #define SOCGPU_IP_ICE_PADE_2_PHF       20
 /* gas overlap, rad_pcf.F90:427 */
 #define SOCGPU_IP_OVERLAP_RANDOM        2
@@ -173,12 +177,13 @@ typedef struct socgpu_spectrum_desc {
     double t_ref_planck;
     const double *thermal_coeff;        /* (0:nd_thermal_coeff-1, nd_band) or NULL */
     /* StrSpecDrop, block 10 */
-    const int    *l_drop_type;          /* (nd_drop_type) or NULL */
-    const int    *i_drop_parm;          /* (nd_drop_type) */
+    const int    *l_drop_type;          /* (nd_drop_type) or NULL: the type is defined */
+    const int    *i_drop_parm;          /* (nd_drop_type) scheme of each type, indexed by the
+                                           file's type number (read_spectrum.F90 block 10) */
     const double *drop_parm_list;       /* (nd_cloud_parameter, nd_band, nd_drop_type) */
     /* StrSpecIce, block 12 */
     const int    *l_ice_type;           /* (nd_ice_type) or NULL */
-    const int    *i_ice_parm;           /* (nd_ice_type) */
+    const int    *i_ice_parm;           /* (nd_ice_type) scheme of each type (block 12) */
     const double *ice_parm_list;        /* (nd_cloud_parameter, nd_band, nd_ice_type) */
     /* StrSpecCont, blocks 8 and 9 (NULL n_band_continuum: no continua) */
     int nd_continuum;
@@ -296,7 +301,10 @@ typedef struct socgpu_cld {
     int n_condensed;
     const int *type_condensed;        /* (nd_cloud_component) ip_clcmp_* */
     const int *i_cloud_type;          /* (nd_cloud_component) cloud type of each component */
-    const int *i_condensed_param;     /* (nd_cloud_component) parametrization (ip_drop_pade_2, ip_ice_pade_2_phf) */
+    const int *i_condensed_param;     /* (nd_cloud_component) parametrization: droplets
+                                         SOCGPU_IP_SLINGO_SCHRECKER or _DROP_PADE_2; ice
+                                         SOCGPU_IP_SLINGO_SCHRECKER_ICE, _ICE_FU_PHF or
+                                         _ICE_PADE_2_PHF; the scheme of the chosen type */
     const int *i_condensed_type;      /* (nd_cloud_component) 1-based drop type (water) or ice type (ice)
                                          in the spectrum: the parameter set parm_list(:, band, type) */
     const double *condensed_mix_ratio;/* (nd_profile, id_ct:nd_layer, nd_cloud_component), in-cloud */
@@ -364,6 +372,13 @@ SOCGPU_API int socgpu_spectrum_lookup(const char *name, socgpu_spectrum_handle *
 SOCGPU_API int socgpu_spectrum_n_gpoint(socgpu_spectrum_handle handle);
 /* Release a spectrum and its device tables. */
 SOCGPU_API int socgpu_spectrum_release(socgpu_spectrum_handle handle);
+/* The k-term counts set_cld_mcica reads from the spectrum to lay out the
+ * McICA sampling (socrates_set_cld_mcica.F90:106-139): the band count,
+ * nd_k_term (the leading extent of subcol_k and first_subcol_k) and, for
+ * each band, the k-terms of its first absorber (0 without absorbers);
+ * n_k_major has room for n_band_max entries.  Any pointer may be NULL. */
+SOCGPU_API int socgpu_spectrum_k_terms(socgpu_spectrum_handle handle, int n_band_max, int *n_band, int *nd_k_term,
+                                       int *n_k_major);
 
 /* Replaces radiance_calc (src/radiance_core/radiance_calc.F90:16) for the
  * two-stream clear-sky and McICA paths.  All pointers are host memory; the

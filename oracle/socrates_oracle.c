@@ -517,10 +517,55 @@ static void clear_coefficients(work *w, const socgpu_control *c, const double *m
  * rescale_phase_fnc.F90:120-128 as called at radiance_calc.F90:996-1017).
  * Cloud-component optics through opt_prop_pade_2
  * (opt_prop_pade_2_mod.F90:99-140, the rescaled n_order_forward=2 path of
- * opt_prop_water_cloud.F90:212-219 and opt_prop_ice_cloud.F90:228-236). */
+ * opt_prop_water_cloud.F90:212-219 and opt_prop_ice_cloud.F90:228-236),
+ * Slingo and Schrecker's fits (opt_prop_water_cloud.F90:231-247,
+ * opt_prop_ice_cloud.F90:278-294) and Fu's ice fits
+ * (opt_prop_fu_phf_mod.F90:92-130). */
 /* Physical constants (rad_ccf.F90:42-58, gas_list_pcf.F90:303-306). */
 #define MOL_WEIGHT_AIR 28.966e-03
 #define REPSILON (18.0153 / 28.966)
+
+static int cloud_scheme_known(int phase, int scheme)
+{
+    if (phase == SOCGPU_IP_PHASE_WATER) return scheme == SOCGPU_IP_SLINGO_SCHRECKER || scheme == SOCGPU_IP_DROP_PADE_2;
+    if (phase == SOCGPU_IP_PHASE_ICE)
+        return scheme == SOCGPU_IP_SLINGO_SCHRECKER_ICE || scheme == SOCGPU_IP_ICE_FU_PHF ||
+               scheme == SOCGPU_IP_ICE_PADE_2_PHF;
+    return 0;
+}
+
+/* Extinction, scattering and asymmetry of one cloud component of mass
+ * fraction q and characteristic dimension re under scheme `scheme` with the
+ * coefficients cp of its type in this band; 0 when the scheme is not one of
+ * these. */
+static int cloud_component_optics(int phase, int scheme, const double *cp, double q, double re,
+                                  double *ke, double *ks, double *g)
+{
+    if ((phase == SOCGPU_IP_PHASE_WATER && scheme == SOCGPU_IP_SLINGO_SCHRECKER) ||
+        (phase == SOCGPU_IP_PHASE_ICE && scheme == SOCGPU_IP_SLINGO_SCHRECKER_ICE)) {
+        *ke = q * (cp[0] + cp[1] / re);
+        *ks = *ke * (1.0e+00 - cp[2] - cp[3] * re);
+        *g = cp[4] + cp[5] * re;
+        return 1;
+    }
+    if ((phase == SOCGPU_IP_PHASE_WATER && scheme == SOCGPU_IP_DROP_PADE_2) ||
+        (phase == SOCGPU_IP_PHASE_ICE && scheme == SOCGPU_IP_ICE_PADE_2_PHF)) {
+        *ke = q * (cp[0] + re * (cp[1] + re * cp[2])) / (1.0e+00 + re * (cp[3] + re * (cp[4] + re * cp[5])));
+        *ks = *ke * (1.0e+00 - (cp[6] + re * (cp[7] + re * cp[8])) / (1.0e+00 + re * (cp[9] + re * cp[10])));
+        *g = (cp[11] + re * (cp[12] + re * cp[13])) / (1.0e+00 + re * (cp[14] + re * cp[15]));
+        return 1;
+    }
+    if (phase == SOCGPU_IP_PHASE_ICE && scheme == SOCGPU_IP_ICE_FU_PHF) {
+        double x = cp[3] / re;
+        *ke = q * ((cp[2] * x + cp[1]) * x + cp[0]);
+        x = re / cp[8];
+        *ks = *ke * (1.0e+00 - (cp[4] + x * (cp[5] + x * (cp[6] + x * cp[7]))));
+        x = re / cp[13];
+        *g = cp[9] + x * (cp[10] + x * (cp[11] + x * cp[12]));
+        return 1;
+    }
+    return 0;
+}
 
 /* rescale_continuum (rescale_continuum.F90): amount of continuum j of band
  * b in every layer, from the p/T scaling and the water vapour. */
@@ -639,13 +684,15 @@ static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *d
         for (int k = 0; k < cld->n_condensed; ++k) {
             const double *cp0;
             int ity = cld->i_condensed_type[k] - 1;
-            if (cld->type_condensed[k] == SOCGPU_IP_PHASE_WATER) {
-                if (cld->i_condensed_param[k] != SOCGPU_IP_DROP_PADE_2 || !d->drop_parm_list) return SOCGPU_I_ERR_FATAL;
+            const int phase = cld->type_condensed[k], scheme = cld->i_condensed_param[k];
+            if (phase == SOCGPU_IP_PHASE_WATER) {
+                if (!d->drop_parm_list || ity < 0 || ity >= d->nd_drop_type) return SOCGPU_I_ERR_FATAL;
                 cp0 = d->drop_parm_list + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * (size_t)ity);
             } else {
-                if (cld->i_condensed_param[k] != SOCGPU_IP_ICE_PADE_2_PHF || !d->ice_parm_list) return SOCGPU_I_ERR_FATAL;
+                if (!d->ice_parm_list || ity < 0 || ity >= d->nd_ice_type) return SOCGPU_I_ERR_FATAL;
                 cp0 = d->ice_parm_list + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * (size_t)ity);
             }
+            if (!cloud_scheme_known(phase, scheme)) return SOCGPU_I_ERR_FATAL;
             double *kext = w->k_ext_tot_cc + pl * k, *kscat = w->k_ext_scat_cc + pl * k;
             double *phf = w->phf_cc + pl * k, *fwd = w->fwd_cc + pl * k;
             for (int i = ict; i < n_layer; ++i)
@@ -653,13 +700,8 @@ static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *d
                     size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
                     double q = cld->condensed_mix_ratio[qc + (size_t)ndp * ndc * k];
                     double re = cld->condensed_dim_char[qc + (size_t)ndp * ndc * k];
-                    const double *cp = cp0;
-                    double ke = q * (cp[0] + re * (cp[1] + re * cp[2]))
-                        / (1.0e+00 + re * (cp[3] + re * (cp[4] + re * cp[5])));
-                    double ks = ke * (1.0e+00 - (cp[6] + re * (cp[7] + re * cp[8]))
-                                      / (1.0e+00 + re * (cp[9] + re * cp[10])));
-                    double g = (cp[11] + re * (cp[12] + re * cp[13]))
-                        / (1.0e+00 + re * (cp[14] + re * cp[15]));
+                    double ke = 0.0, ks = 0.0, g = 0.0;
+                    if (re > 0.0) cloud_component_optics(phase, scheme, cp0, q, re, &ke, &ks, &g);
                     IX2(kext, l, i, wp) = ke;
                     IX2(kscat, l, i, wp) = ks;
                     IX2(phf, l, i, wp) = ks * g;
@@ -721,32 +763,36 @@ static void solve_mcica_term(work *w, const socgpu_control *c, const socgpu_dime
             memcpy(w->flux_direct_clear, w->flux_direct, pl1 * sizeof(double));
             memcpy(w->flux_total_clear, w->flux_total, pl2 * sizeof(double));
         }
-        /* cloudy-type optics (mcica_sample.F90:472-560) and their optical
-         * depths (single_scattering_all, rescale_tau_omega) */
+        /* cloudy-type optics (mcica_sample.F90:472-700): each type starts
+         * from the clear-sky values and adds its components in order, scaled
+         * by c_sub (one component per type under ip_cloud_ice_water, all of
+         * them in type 1 under ip_cloud_homogen); then their optical depths
+         * (single_scattering_all, rescale_tau_omega) */
         for (int t = 1; t <= 2; ++t)
             for (size_t q = 0; q < pl; ++q) w->ty_valid[t][q] = 0.0;
-        for (int k = 0; k < cld->n_condensed; ++k) {
-            int t = cld->i_cloud_type[k];
-            const double *kext = w->k_ext_tot_cc + pl * k, *kscat = w->k_ext_scat_cc + pl * k;
-            const double *phf = w->phf_cc + pl * k, *fwdc = w->fwd_cc + pl * k;
+        for (int t = 1; t <= cld->n_cloud_type; ++t)
             for (int i = ict; i < n_layer; ++i)
                 for (int l = 0; l < n_profile; ++l) {
                     size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
                     if (!(cld->w_cloud[qc] > 0.0)) continue;
                     double cs = CSUB_AT(qc, l);
-                    double kgt = IX2(w->k_grey_tot, l, i, wp) + IX2(kext, l, i, wp) * cs;
-                    double kes = IX2(w->k_ext_scat, l, i, wp) + IX2(kscat, l, i, wp) * cs;
-                    double fwd, asym;
+                    double kgt = IX2(w->k_grey_tot, l, i, wp), kes = IX2(w->k_ext_scat, l, i, wp);
+                    double fwd = IX2(w->forward_scatter_nc, l, i, wp), phf = IX2(w->phase_fnc_nc, l, i, wp);
+                    for (int k = 0; k < cld->n_condensed; ++k) {
+                        if (cld->i_cloud_type[k] != t) continue;
+                        kgt = kgt + IX2(w->k_ext_tot_cc + pl * k, l, i, wp) * cs;
+                        kes = kes + IX2(w->k_ext_scat_cc + pl * k, l, i, wp) * cs;
+                        fwd = fwd + IX2(w->fwd_cc + pl * k, l, i, wp) * cs;
+                        phf = phf + IX2(w->phf_cc + pl * k, l, i, wp) * cs;
+                    }
+                    double asym;
                     if (c->l_rescale) {
-                        fwd = IX2(w->forward_scatter_nc, l, i, wp) + IX2(fwdc, l, i, wp) * cs;
                         double den = kes - fwd;
-                        asym = (IX2(w->phase_fnc_nc, l, i, wp) + IX2(phf, l, i, wp) * cs - fwd)
-                            / (den > eps ? den : eps);
+                        asym = (phf - fwd) / (den > eps ? den : eps);
                         fwd = fwd / (kes > eps ? kes : eps);
                     } else {
                         fwd = 0.0;
-                        asym = (IX2(w->phase_fnc_nc, l, i, wp) + IX2(phf, l, i, wp) * cs)
-                            / (kes > eps ? kes : eps);
+                        asym = phf / (kes > eps ? kes : eps);
                     }
                     double tau, tau_dir, om;
                     single_scatter_cell(c, kgt, kes, IX2(w->k_gas_abs, l, i, wp),
@@ -755,7 +801,6 @@ static void solve_mcica_term(work *w, const socgpu_control *c, const socgpu_dime
                     IX2(w->ty_omega[t], l, i, wp) = om; IX2(w->ty_asym[t], l, i, wp) = asym;
                     IX2(w->ty_valid[t], l, i, wp) = 1.0;
                 }
-        }
         /* mcica_column.F90:336-470: clear coefficients, then the cloudy
          * cells of this subcolumn get the frac_cloud-weighted cloudy ones */
         memcpy(w->trans, w->trans_clr, pl * sizeof(double));

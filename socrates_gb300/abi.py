@@ -25,6 +25,7 @@ IP_CLOUD_TYPE_WATER, IP_CLOUD_TYPE_ICE = 1, 2
 IP_PHASE_WATER, IP_PHASE_ICE = 1, 2
 IP_CLCMP_ST_WATER, IP_CLCMP_ST_ICE = 1, 2
 IP_DROP_PADE_2, IP_ICE_PADE_2_PHF = 5, 20
+IP_SLINGO_SCHRECKER, IP_SLINGO_SCHRECKER_ICE, IP_ICE_FU_PHF = 1, 1, 12
 IP_OVERLAP_RANDOM = 2
 IP_OVERLAP_K_EQV_SCL, IP_OVERLAP_K_EQV, IP_OVERLAP_K_EQV_MOD = 4, 5, 6
 IP_SCALE_NULL, IP_SCALE_BAND, IP_SCALE_TERM = 0, 1, 2
@@ -188,6 +189,7 @@ ABI_FUNCTIONS = (
     "socgpu_batch_info", "socgpu_batch_destroy", "socgpu_tune_get", "socgpu_tune_set",
     "socgpu_server_create", "socgpu_server_submit", "socgpu_server_wait", "socgpu_server_stats_get",
     "socgpu_server_destroy", "socgpu_spectrum_load", "socgpu_spectrum_load_ext", "socgpu_runes",
+    "socgpu_spectrum_k_terms",
 )
 
 _CALC_ARGS = [C.POINTER(Control), C.POINTER(Dimen), C.c_int, C.POINTER(Atm), C.POINTER(Cld), C.POINTER(Aer),
@@ -206,6 +208,8 @@ def declare(lib: C.CDLL) -> C.CDLL:
                                              C.c_char_p, C.c_size_t]
     lib.socgpu_runes.argtypes = [C.POINTER(RunesArgs), C.POINTER(RunesDiag), C.c_char_p, C.c_size_t]
     lib.socgpu_spectrum_n_gpoint.argtypes = [C.c_int]
+    lib.socgpu_spectrum_k_terms.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_int)]
     lib.socgpu_spectrum_release.argtypes = [C.c_int]
     lib.socgpu_radiance_calc.argtypes = _CALC_ARGS + [C.c_char_p, C.c_size_t]
     lib.socgpu_radiance_calc_device.argtypes = _CALC_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]

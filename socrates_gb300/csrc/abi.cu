@@ -85,6 +85,7 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   e.bands_host.assign(d->n_band, BandInfo{});
   e.gpoints_host.clear();
   e.type_absorb.assign(d->type_absorb, d->type_absorb + d->n_absorb);
+  e.n_k_major.assign(d->n_band, 0);
   std::vector<BandInfo> bands_keqv;
   std::vector<GPoint> gpoints_keqv;
   std::vector<TermK> minor;
@@ -243,6 +244,7 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
         set_msg(msg, msg_len, "band %d absorber %d: %d k-terms", b + 1, g + 1, nk[j]);
         return SOCGPU_I_ERR_RANGE;
       }
+      if (j == 0) e.n_k_major[b] = nk[0];
       if (n_term <= SOCGPU_MAX_GPOINT) n_term *= nk[j];
     }
     // one k-term of absorber j as a g-point entry; returns its weight
@@ -402,21 +404,27 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   std::vector<double> drop, ice;
   s.n_drop_type = (d->drop_parm_list && d->nd_drop_type > 0) ? d->nd_drop_type : 0;
   s.n_ice_type = (d->ice_parm_list && d->nd_ice_type > 0) ? d->nd_ice_type : 0;
-  if (s.n_drop_type > 0 && d->nd_cloud_parameter < kPadeParm) {
-    set_msg(msg, msg_len, "droplet parameter sets need %d coefficients", kPadeParm);
-    return SOCGPU_I_ERR_RANGE;
-  }
-  drop.assign((size_t)std::max(1, s.n_drop_type) * d->n_band * kPadeParm, 0.0);
-  ice.assign((size_t)std::max(1, s.n_ice_type) * d->n_band * kPadeParm, 0.0);
+  // each set at its type number (read_spectrum.F90 blocks 10 and 12), the
+  // first kCloudParm coefficients; the scheme of each type stays on the host
+  const int ncp = std::min(d->nd_cloud_parameter, kCloudParm);
+  e.n_cloud_parameter = d->nd_cloud_parameter;
+  e.drop_scheme.assign(s.n_drop_type, 0);
+  e.ice_scheme.assign(s.n_ice_type, 0);
+  for (int t = 0; t < s.n_drop_type; ++t)
+    if ((!d->l_drop_type || d->l_drop_type[t]) && d->i_drop_parm) e.drop_scheme[t] = d->i_drop_parm[t];
+  for (int t = 0; t < s.n_ice_type; ++t)
+    if ((!d->l_ice_type || d->l_ice_type[t]) && d->i_ice_parm) e.ice_scheme[t] = d->i_ice_parm[t];
+  drop.assign((size_t)std::max(1, s.n_drop_type) * d->n_band * kCloudParm, 0.0);
+  ice.assign((size_t)std::max(1, s.n_ice_type) * d->n_band * kCloudParm, 0.0);
   for (int t = 0; t < s.n_drop_type; ++t)
     for (int b = 0; b < d->n_band; ++b)
-      for (int c = 0; c < kPadeParm; ++c)
-        drop[((size_t)t * d->n_band + b) * kPadeParm + c] =
+      for (int c = 0; c < ncp; ++c)
+        drop[((size_t)t * d->n_band + b) * kCloudParm + c] =
             d->drop_parm_list[(size_t)c + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * t)];
   for (int t = 0; t < s.n_ice_type; ++t)
     for (int b = 0; b < d->n_band; ++b)
-      for (int c = 0; c < kPadeParm; ++c)
-        ice[((size_t)t * d->n_band + b) * kPadeParm + c] =
+      for (int c = 0; c < ncp; ++c)
+        ice[((size_t)t * d->n_band + b) * kCloudParm + c] =
             d->ice_parm_list[(size_t)c + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * t)];
   std::vector<float> drop_f(drop.begin(), drop.end()), ice_f(ice.begin(), ice.end());
   cudaGetDevice(&e.device);
@@ -645,18 +653,37 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     for (int k = 0; k < cld->n_condensed; ++k) {
       int ph = cld->type_condensed[k], parm = cld->i_condensed_param[k], ty = cld->i_condensed_type[k];
       if (ph == SOCGPU_IP_PHASE_WATER) {
-        if (parm != SOCGPU_IP_DROP_PADE_2 || ty < 1 || ty > sp->dev.n_drop_type) {
+        if ((parm != SOCGPU_IP_SLINGO_SCHRECKER && parm != SOCGPU_IP_DROP_PADE_2) || ty < 1 ||
+            ty > sp->dev.n_drop_type) {
           set_msg(msg, msg_len, "droplet parametrization %d (type %d) unsupported", parm, ty); return SOCGPU_I_ERR_FATAL; }
+        if (sp->drop_scheme[ty - 1] != parm) {
+          set_msg(msg, msg_len, "droplet type %d of the spectrum has scheme %d, not %d", ty, sp->drop_scheme[ty - 1],
+                  parm);
+          return SOCGPU_I_ERR_FATAL;
+        }
       } else if (ph == SOCGPU_IP_PHASE_ICE) {
-        if (parm != SOCGPU_IP_ICE_PADE_2_PHF || ty < 1 || ty > sp->dev.n_ice_type) {
+        if ((parm != SOCGPU_IP_SLINGO_SCHRECKER_ICE && parm != SOCGPU_IP_ICE_FU_PHF &&
+             parm != SOCGPU_IP_ICE_PADE_2_PHF) || ty < 1 || ty > sp->dev.n_ice_type) {
           set_msg(msg, msg_len, "ice parametrization %d (type %d) unsupported", parm, ty); return SOCGPU_I_ERR_FATAL; }
+        if (sp->ice_scheme[ty - 1] != parm) {
+          set_msg(msg, msg_len, "ice type %d of the spectrum has scheme %d, not %d", ty, sp->ice_scheme[ty - 1], parm);
+          return SOCGPU_I_ERR_FATAL;
+        }
       } else {
         set_msg(msg, msg_len, "unknown condensed phase %d", ph); return SOCGPU_I_ERR_FATAL; }
+      const int need = (parm == SOCGPU_IP_DROP_PADE_2 || parm == SOCGPU_IP_ICE_PADE_2_PHF) ? 16
+                       : parm == SOCGPU_IP_ICE_FU_PHF ? 14 : 6;
+      if (sp->n_cloud_parameter < need) {
+        set_msg(msg, msg_len, "cloud scheme %d needs %d coefficients, the spectrum holds %d", parm, need,
+                sp->n_cloud_parameter);
+        return SOCGPU_I_ERR_RANGE;
+      }
       if (cld->i_cloud_type[k] < 1 || cld->i_cloud_type[k] > cld->n_cloud_type) {
         set_msg(msg, msg_len, "component cloud type out of range"); return SOCGPU_I_ERR_RANGE; }
     }
     if (c->l_rescale && c->n_order_forward != 2) {
-      set_msg(msg, msg_len, "McICA cloud optics need n_order_forward=2 (the Pade path)"); return SOCGPU_I_ERR_FATAL; }
+      set_msg(msg, msg_len, "McICA cloud optics need n_order_forward=2 (forward scattering k_scat g^2)");
+      return SOCGPU_I_ERR_FATAL; }
   }
   return SOCGPU_I_NORMAL;
 }
@@ -730,6 +757,7 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
       p.comp_type[k] = cld->i_cloud_type[k];
       p.comp_phase[k] = cld->type_condensed[k];
       p.comp_parm_index[k] = cld->i_condensed_type[k] - 1;
+      p.comp_scheme[k] = cld->i_condensed_param[k];
     }
     p.condensed_mix_ratio = cld->condensed_mix_ratio; p.condensed_dim_char = cld->condensed_dim_char;
     p.w_cloud = cld->w_cloud; p.frac_cloud = cld->frac_cloud; p.c_sub = cld->c_sub;
@@ -1266,6 +1294,17 @@ int socgpu_spectrum_lookup(const char *name, socgpu_spectrum_handle *handle) {
 int socgpu_spectrum_n_gpoint(socgpu_spectrum_handle handle) {
   SpectrumEntry *e = find_spectrum(handle);
   return e ? e->dev.n_gpoint : -1;
+}
+
+int socgpu_spectrum_k_terms(socgpu_spectrum_handle handle, int n_band_max, int *n_band, int *nd_k_term,
+                            int *n_k_major) {
+  SpectrumEntry *e = find_spectrum(handle);
+  if (!e) return SOCGPU_I_ERR_EXIST;
+  if (n_band) *n_band = e->dev.n_band;
+  if (nd_k_term) *nd_k_term = e->dev.nd_k_term;
+  if (n_k_major)
+    for (int b = 0; b < e->dev.n_band && b < n_band_max; ++b) n_k_major[b] = e->n_k_major[b];
+  return SOCGPU_I_NORMAL;
 }
 
 int socgpu_spectrum_release(socgpu_spectrum_handle handle) {

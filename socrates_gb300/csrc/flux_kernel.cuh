@@ -833,8 +833,11 @@ struct FluxKernel {
     }
   }
 
-  // Cloud-component optics of bands bstart..bstart+nb-1 through
-  // opt_prop_pade_2 (opt_prop_pade_2_mod.F90:99-140).
+  // Cloud-component optics of bands bstart..bstart+nb-1: opt_prop_pade_2
+  // (opt_prop_pade_2_mod.F90:99-140), Slingo and Schrecker's fits
+  // (opt_prop_water_cloud.F90:231-247, opt_prop_ice_cloud.F90:278-294) and
+  // Fu's ice fits (opt_prop_fu_phf_mod.F90:92-130).  Forward scattering is
+  // k_scat g^2 (n_order_forward 2) for all of them.
   __device__ static void stage_cloud_bands(const FluxParams &p, const Smem &S, int col, int bstart, int nb) {
     const int L = p.n_layer, ndp = p.nd_profile, ndl = p.nd_layer, ict = p.id_ct;
     const int ndc = ndl - ict, nc = p.n_condensed;
@@ -844,22 +847,38 @@ struct FluxKernel {
       R vke = R(0), vks = R(0), vka = R(0), vph = R(0), vfw = R(0);
       if (i < L && i >= ict) {
         const size_t qc = (size_t)col + (size_t)ndp * (size_t)(i - ict);
-        if (load_in<R>(p.w_cloud + qc) > R(0)) {
-          const size_t po = ((size_t)p.comp_parm_index[k] * p.n_band + (bstart + bi)) * kPadeParm;
+        R re = load_in<R>(p.condensed_dim_char + qc + (size_t)ndp * ndc * k);
+        if (load_in<R>(p.w_cloud + qc) > R(0) && re > R(0)) {
+          const size_t po = ((size_t)p.comp_parm_index[k] * p.n_band + (bstart + bi)) * kCloudParm;
           R qm = load_in<R>(p.condensed_mix_ratio + qc + (size_t)ndp * ndc * k);
-          R re = load_in<R>(p.condensed_dim_char + qc + (size_t)ndp * ndc * k);
-          R cp[kPadeParm];
+          R cp[kCloudParm];
           if constexpr (kFP64) {
             const double *c = (p.comp_phase[k] == SOCGPU_IP_PHASE_WATER ? p.drop_parm : p.ice_parm) + po;
-            for (int m = 0; m < kPadeParm; ++m) cp[m] = c[m];
+            for (int m = 0; m < kCloudParm; ++m) cp[m] = c[m];
           } else {
             const float *c = (p.comp_phase[k] == SOCGPU_IP_PHASE_WATER ? p.drop_parm_f : p.ice_parm_f) + po;
-            for (int m = 0; m < kPadeParm; ++m) cp[m] = c[m];
+            for (int m = 0; m < kCloudParm; ++m) cp[m] = c[m];
           }
-          R kext = qm * (cp[0] + re * (cp[1] + re * cp[2])) / (R(1) + re * (cp[3] + re * (cp[4] + re * cp[5])));
-          R coalb = (cp[6] + re * (cp[7] + re * cp[8])) / (R(1) + re * (cp[9] + re * cp[10]));
-          R kscat = kext * (R(1) - coalb);
-          R g = (cp[11] + re * (cp[12] + re * cp[13])) / (R(1) + re * (cp[14] + re * cp[15]));
+          const int scheme = p.comp_scheme[k];
+          R kext, coalb, g;
+          if (scheme == SOCGPU_IP_SLINGO_SCHRECKER) {
+            // the droplet and ice forms are the same (both schemes are 1)
+            kext = qm * (cp[0] + cp[1] / re);
+            coalb = cp[2] + cp[3] * re;
+            g = cp[4] + cp[5] * re;
+          } else if (scheme == SOCGPU_IP_ICE_FU_PHF && p.comp_phase[k] == SOCGPU_IP_PHASE_ICE) {
+            R x = cp[3] / re;
+            kext = qm * ((cp[2] * x + cp[1]) * x + cp[0]);
+            x = re / cp[8];
+            coalb = cp[4] + x * (cp[5] + x * (cp[6] + x * cp[7]));
+            x = re / cp[13];
+            g = cp[9] + x * (cp[10] + x * (cp[11] + x * cp[12]));
+          } else {
+            kext = qm * (cp[0] + re * (cp[1] + re * cp[2])) / (R(1) + re * (cp[3] + re * (cp[4] + re * cp[5])));
+            coalb = (cp[6] + re * (cp[7] + re * cp[8])) / (R(1) + re * (cp[9] + re * cp[10]));
+            g = (cp[11] + re * (cp[12] + re * cp[13])) / (R(1) + re * (cp[14] + re * cp[15]));
+          }
+          const R kscat = kext * (R(1) - coalb);
           vke = kext; vks = kscat; vka = kext * coalb; vph = kscat * g; vfw = kscat * g * g;
         }
       }
@@ -1328,25 +1347,32 @@ struct FluxKernel {
             cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kg, S.mass[s], asym_b[s], fwd_b[s], sec0,
                       T[jj], Rf[jj], T0[jj], c1[jj], c2[jj], om[jj]);
           } else {
-            // mcica_sample.F90:472-560 then mcica_column.F90:336-470
+            // mcica_sample.F90:472-700 then mcica_column.F90:336-470: each
+            // cloud type is the clear cell plus its components in order,
+            // scaled by c_sub (one component per type for ice/water clouds,
+            // both in type 1 for homogeneous clouds)
             R sT = R(0), sR = R(0), sT0 = R(0), s1 = R(0), s2 = R(0), sO = R(0);
-            for (int k = 0; k < nc; ++k) {
-              const int t = p.comp_type[k] - 1;
+            for (int t = 0; t < p.n_cloud_type; ++t) {
               const R fc = S.frac[(size_t)t * LP + s];
               if (!(cs_i * fc > R(0))) continue;
-              const size_t qk = (size_t)k * LP + s;
-              R kgt = kgt_b[s] + c_ke[qk] * cs_i;
-              R kes = kes_b[s] + c_ks[qk] * cs_i;
-              R kab = kabs_b[s] + c_ka[qk] * cs_i;
+              R kgt = kgt_b[s], kes = kes_b[s], kab = kabs_b[s], fw = fwd_nc[s], ph = phf_nc[s];
+              for (int k = 0; k < nc; ++k) {
+                if (p.comp_type[k] - 1 != t) continue;
+                const size_t qk = (size_t)k * LP + s;
+                kgt = kgt + c_ke[qk] * cs_i;
+                kes = kes + c_ks[qk] * cs_i;
+                kab = kab + c_ka[qk] * cs_i;
+                fw = fw + c_fw[qk] * cs_i;
+                ph = ph + c_ph[qk] * cs_i;
+              }
               R asym, fwd;
               const R eps = (R)kEps64;
               if (p.l_rescale) {
-                R fw = fwd_nc[s] + c_fw[qk] * cs_i;
                 R den = kes - fw;
-                asym = (phf_nc[s] + c_ph[qk] * cs_i - fw) / (den > eps ? den : eps);
+                asym = (ph - fw) / (den > eps ? den : eps);
                 fwd = fw / (kes > eps ? kes : eps);
               } else {
-                asym = (phf_nc[s] + c_ph[qk] * cs_i) / (kes > eps ? kes : eps);
+                asym = ph / (kes > eps ? kes : eps);
                 fwd = R(0);
               }
               R tT, tR, tT0, t1, t2, tO;

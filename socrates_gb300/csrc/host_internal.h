@@ -32,6 +32,9 @@ struct SpectrumEntry {
   std::vector<BandInfo> bands_host;
   std::vector<GPoint> gpoints_host;
   std::vector<int> type_absorb;       // gas identifier of each absorber (runes maps gases by name)
+  std::vector<int> drop_scheme, ice_scheme;   // scheme of each droplet / ice type, 0 where undefined
+  int n_cloud_parameter = 0;          // coefficients per parameter set in the spectrum
+  std::vector<int> n_k_major;         // k-terms of each band's first absorber (McICA tables)
   int device = 0;
 };
 

@@ -7,6 +7,8 @@
 //              [-g <gas overlap>] [-c] [-r] [+R] [-q] [-t <two-stream scheme>]
 //              [-v <solver>] [-C <cloud scheme>] [-z <scatter method>]
 //              [-ds <direct tau>] [-P fp64|mixed] [-W <scale_wenyi source>]
+//              [-C 10 -K <cloud representation> -d <droplet type> -i <ice type>
+//               -m <condensate relative std. deviation> +m <sampling> -dp <decorrelation scale>]
 //   socgpu_run --convert <in> <out.cdf|out.cdl>
 //
 // Inputs: .t (layer temperatures on the layer pressures `plev`), .tl (level
@@ -15,7 +17,13 @@
 // gas_list_pcf.F90: q, co2, o3, ...; an absent file means none of that
 // gas), .tstar (infra-red), .szen and .stoa (solar), .surf (albedo weights).
 // Outputs: .uflx, .dflx, .nflx, .hrts, and in the solar .vflx (direct) and
-// .sflx (diffuse down).  Only the clear-sky two-stream path is driven.
+// .sflx (diffuse down).  The two-stream path is driven clear (-C 5) or with
+// McICA (-C 10): clouds of one homogeneous type (-K 1: .clfr) or of water and
+// ice types (-K 2: .wclfr, .iclfr), droplets from .lwm and .re with the
+// spectral file's droplet type -d, ice from .iwm and .ire with ice type -i
+// (input_cloud_cdf.f:340-790), and the subcolumns of set_cld_mcica from the
+// McICA data file beside the spectral file (l_run_cdf.F90:998-1010,
+// 1281-1296).
 // Lookup tables are read from the spectral file's '_k' companion; spectral
 // files with Wen-Yi CO2 terms (GA7 and GA9 long wave) need -W, the SOCRATES
 // source file that defines those tables (the reference compiles them in).
@@ -24,6 +32,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <string>
 #include <vector>
@@ -128,6 +137,122 @@ bool write_field(const std::string &path, bool cdf, const std::string &name, con
   return cdf ? socgpu::write_cdf(path, f, err) : socgpu::write_cdl(path, f, err);
 }
 
+// Blocks 10 and 12 of a spectral file: the scheme and range of validity of
+// each droplet or ice type (read_spectrum.F90 read_block_10_0_2 and 12_0_2).
+struct CloudTypeInfo {
+  int scheme = 0;
+  double lo = 0.0, hi = 0.0;
+};
+
+bool read_cloud_types(const std::string &path, std::map<int, CloudTypeInfo> &drop,
+                      std::map<int, CloudTypeInfo> &ice) {
+  FILE *f = std::fopen(path.c_str(), "r");
+  if (!f) return false;
+  char line[512];
+  int blk = -1, type = 0;
+  CloudTypeInfo cur;
+  auto flush = [&]() {
+    if ((blk == 10 || blk == 12) && type > 0) (blk == 10 ? drop : ice)[type] = cur;
+    type = 0;
+    cur = CloudTypeInfo{};
+  };
+  while (std::fgets(line, sizeof(line), f)) {
+    std::string s(line), u = s;
+    for (char &c : u) c = (char)std::toupper((unsigned char)c);
+    if (s.rfind("*BLOCK", 0) == 0) {
+      flush();
+      const size_t e = s.find('=');
+      blk = e == std::string::npos ? -1 : std::atoi(s.c_str() + e + 1);
+      continue;
+    }
+    if (s.rfind("*END", 0) == 0) { flush(); blk = -1; continue; }
+    if (blk != 10 && blk != 12) continue;
+    const size_t e = s.find('=');
+    if (e == std::string::npos) continue;
+    if (u.find("TYPE NUMBER") != std::string::npos) type = std::atoi(s.c_str() + e + 1);
+    else if (u.find("PARAMETRIZATION SCHEME") != std::string::npos) cur.scheme = std::atoi(s.c_str() + e + 1);
+    else if (u.find("RANGE OF VALIDITY") != std::string::npos) {
+      const size_t dd = s.find("--", e);
+      if (dd != std::string::npos) {
+        cur.lo = std::strtod(s.c_str() + e + 1, nullptr);
+        cur.hi = std::strtod(s.c_str() + dd + 2, nullptr);
+      }
+    }
+  }
+  flush();
+  std::fclose(f);
+  return true;
+}
+
+// The McICA data file (read_mcica_data, def_mcica.F90): keyword records of
+// the *DATA block, each followed by its values.
+struct McicaData {
+  int gen = 0, req_single = 0, req_optimal = 0, ipph = 0, n1 = 0, n2 = 0;
+  std::vector<int> reorder_single, reorder_optimal;
+  std::map<std::pair<int, int>, int> sw_subcol_k, lw_subcol_k;
+  std::vector<double> xcw;   // (n1, n2)
+};
+
+bool read_mcica_data(const std::string &path, McicaData &m, std::string &err) {
+  FILE *f = std::fopen(path.c_str(), "r");
+  if (!f) { err = "McICA data file " + path + " could not be opened"; return false; }
+  std::vector<std::string> lines;
+  char buf[4096];
+  while (std::fgets(buf, sizeof(buf), f)) {
+    std::string s(buf);
+    while (!s.empty() && (s.back() == '\n' || s.back() == '\r' || s.back() == ' ')) s.pop_back();
+    lines.push_back(s);
+  }
+  std::fclose(f);
+  size_t i = 0;
+  while (i < lines.size() && lines[i].rfind("*DATA", 0) != 0) ++i;
+  if (i == lines.size()) { err = "No *DATA block present in McICA data file"; return false; }
+  ++i;
+  // the next n values (integers or reals) from line i on
+  auto values = [&](size_t n, std::vector<double> &out) {
+    out.clear();
+    while (out.size() < n && i < lines.size()) {
+      const char *c = lines[i++].c_str();
+      char *end = nullptr;
+      for (double v = std::strtod(c, &end); end != c; v = std::strtod(c, &end)) {
+        out.push_back(v);
+        c = end;
+      }
+    }
+    return out.size() == n;
+  };
+  std::vector<double> v;
+  while (i < lines.size() && lines[i].rfind("*END", 0) != 0) {
+    std::string key = lines[i++];
+    key.erase(0, key.find_first_not_of(' '));
+    bool ok = true;
+    if (key == "tot_subcol_gen" || key == "n_subcol_gen") { ok = values(1, v); m.gen = (int)v[0]; }
+    else if (key == "subcol_need_single" || key == "n_subcol_req_single") { ok = values(1, v); m.req_single = (int)v[0]; }
+    else if (key == "subcol_need_optimal" || key == "n_subcol_req_optimal") { ok = values(1, v); m.req_optimal = (int)v[0]; }
+    else if (key == "ipph") { ok = values(1, v); m.ipph = (int)v[0]; }
+    else if (key == "n1") { ok = values(1, v); m.n1 = (int)v[0]; }
+    else if (key == "n2") { ok = values(1, v); m.n2 = (int)v[0]; }
+    else if (key == "lw_subcol_reorder_single" || key == "lw_subcol_reorder_optimal") {
+      const bool single = key == "lw_subcol_reorder_single";
+      ok = values((size_t)(single ? m.req_single : m.req_optimal), v);
+      (single ? m.reorder_single : m.reorder_optimal).assign(v.begin(), v.end());
+    } else if (key == "sw_subcol_k" || key == "lw_subcol_k") {
+      auto &tab = key == "sw_subcol_k" ? m.sw_subcol_k : m.lw_subcol_k;
+      for (;;) {
+        if (!values(3, v)) { ok = false; break; }
+        if ((int)v[0] == -99) break;
+        tab[{(int)v[0], (int)v[1]}] = (int)v[2];
+      }
+    } else if (key == "xcw") {
+      ok = values((size_t)m.n1 * (size_t)m.n2, v);
+      m.xcw = v;
+    }
+    if (!ok) { err = "Error reading data from McICA data file (" + key + ")"; return false; }
+  }
+  if (m.gen < 1 || m.xcw.empty()) { err = "McICA data file without subcolumn count or xcw"; return false; }
+  return true;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -145,6 +270,9 @@ int main(int argc, char **argv) {
   int scatter = SOCGPU_IP_SCATTER_FULL, direct_tau = SOCGPU_IP_DIRECT_DELTA_SCALING;
   bool cont = false, rayleigh = false, rescale = false, quad = false, gas = false;
   int precision = SOCGPU_PRECISION_FP64;
+  // clouds (-K, -d, -i) and McICA (-m, +m, -dp)
+  int representation = 0, drop_type = 0, ice_type = 0, sampling = 2;
+  double mcica_sigma = 0.0, dp_corr_strat = 0.0;
   for (size_t i = 0; i < a.size(); ++i) {
     const std::string &o = a[i];
     auto need = [&](size_t n) { return i + n < a.size(); };
@@ -164,6 +292,12 @@ int main(int argc, char **argv) {
     else if (o == "-C" && need(1)) cloud = std::atoi(a[++i].c_str());
     else if (o == "-z" && need(1)) scatter = std::atoi(a[++i].c_str());
     else if (o == "-ds" && need(1)) direct_tau = std::atoi(a[++i].c_str());
+    else if (o == "-K" && need(1)) representation = std::atoi(a[++i].c_str());
+    else if (o == "-d" && need(1)) drop_type = std::atoi(a[++i].c_str());
+    else if (o == "-i" && need(1)) ice_type = std::atoi(a[++i].c_str());
+    else if (o == "-m" && need(1)) mcica_sigma = std::atof(a[++i].c_str());
+    else if (o == "+m" && need(1)) sampling = std::atoi(a[++i].c_str());
+    else if (o == "-dp" && need(1)) dp_corr_strat = std::atof(a[++i].c_str());
     else if (o == "-P" && need(1)) {
       std::string p = a[++i];
       precision = (p == "mixed") ? SOCGPU_PRECISION_MIXED : SOCGPU_PRECISION_FP64;
@@ -173,7 +307,13 @@ int main(int argc, char **argv) {
   if (base.empty()) return die("Base name not set.");
   if (!isolir) return die("Spectral region not set.");
   if (first < 1 || last < first) return die("Range of bands not set");
-  if (cloud != SOCGPU_IP_CLOUD_CLEAR) return die("only clear-sky runs (-C 5) are driven");
+  if (cloud != SOCGPU_IP_CLOUD_CLEAR && cloud != SOCGPU_IP_CLOUD_MCICA)
+    return die("cloud scheme " + std::to_string(cloud) + " is not driven (clear sky -C 5 or McICA -C 10)");
+  const bool mcica = cloud == SOCGPU_IP_CLOUD_MCICA;
+  if (mcica && representation != 1 && representation != SOCGPU_IP_CLOUD_ICE_WATER)
+    return die("McICA needs the cloud representation -K 1 (homogeneous) or -K 2 (ice and water)");
+  if (mcica && !drop_type && !ice_type) return die("Clouds are specified, but no cloudy processes are included.");
+  if (mcica && (sampling < 0 || sampling > 2)) return die("The value of i_mcica_sampling is not valid.");
   if (!two_stream) two_stream = isolir == SOCGPU_IP_INFRA_RED ? 12 : 16;
   if (!solver) solver = scatter == SOCGPU_IP_SCATTER_FULL ? SOCGPU_IP_SOLVER_HOMOGEN_DIRECT : SOCGPU_IP_SOLVER_NO_SCAT;
 
@@ -294,14 +434,140 @@ int main(int argc, char **argv) {
     }
   }
 
+  // clouds and McICA (input_cloud_cdf.f:340-790; l_run_cdf.F90:1281-1296 with
+  // socrates_set_cld_mcica.F90:82-228)
+  int nc = 0, n_cloud_type = 1, n_subcol_req = 1, gen = 1, nd_k = 1;
+  std::vector<int> type_condensed, i_cloud_type, i_condensed_param, i_condensed_type;
+  std::vector<double> cmr, dim, w_cloud, frac_cloud, c_sub, frac_cloudy;
+  std::vector<int> n_subcol_cld, subcol_k, first_subcol_k, subcol_reorder;
+  if (mcica) {
+    std::map<int, CloudTypeInfo> drops, ices;
+    if (!read_cloud_types(sp_file, drops, ices)) return die("cannot open " + sp_file);
+    struct Comp { int phase, type; const char *mr, *dim; };
+    std::vector<Comp> comps;
+    if (drop_type) comps.push_back({SOCGPU_IP_PHASE_WATER, drop_type, "lwm", "re"});
+    if (ice_type) comps.push_back({SOCGPU_IP_PHASE_ICE, ice_type, "iwm", "ire"});
+    nc = (int)comps.size();
+    n_cloud_type = representation == 1 ? 1 : 2;
+    cmr.assign(np * nl * nc, 0.0);
+    dim.assign(np * nl * nc, 0.0);
+    for (int k = 0; k < nc; ++k) {
+      const Comp &cp = comps[k];
+      auto &tab = cp.phase == SOCGPU_IP_PHASE_WATER ? drops : ices;
+      auto it = tab.find(cp.type);
+      if (it == tab.end() || it->second.scheme == 0)
+        return die(std::string(cp.phase == SOCGPU_IP_PHASE_WATER ? "droplet" : "ice") + " type " +
+                   std::to_string(cp.type) + " is not in the spectral file");
+      type_condensed.push_back(cp.phase);
+      i_cloud_type.push_back(representation == 1 ? 1 : (cp.phase == SOCGPU_IP_PHASE_WATER ? 1 : 2));
+      i_condensed_param.push_back(it->second.scheme);
+      i_condensed_type.push_back(cp.type);
+      Field fm, fd;
+      if (!read_field(base + "." + cp.mr, fm, err) || !read_field(base + "." + cp.dim, fd, err)) return die(err);
+      if (fm.n_prof() != np || fm.n_lev != nl || fd.n_prof() != np || fd.n_lev != nl)
+        return die(std::string(cp.mr) + "/" + cp.dim + ": not on the layers of .t");
+      for (size_t q = 0; q < np * nl; ++q) {
+        cmr[q + np * nl * k] = fm.v[q];
+        dim[q + np * nl * k] = std::min(std::max(fd.v[q], it->second.lo), it->second.hi);
+      }
+    }
+    // cloud fractions of each type, normalised by their sum (input_cloud_cdf.f:760-790)
+    const char *frac_suffix[2] = {representation == 1 ? "clfr" : "wclfr", "iclfr"};
+    frac_cloud.assign(np * nl * n_cloud_type, 0.0);
+    w_cloud.assign(np * nl, 0.0);
+    for (int t2 = 0; t2 < n_cloud_type; ++t2) {
+      Field ff;
+      if (!read_field(base + "." + frac_suffix[t2], ff, err)) return die(err);
+      if (ff.n_prof() != np || ff.n_lev != nl) return die(std::string(frac_suffix[t2]) + ": not on the layers of .t");
+      for (size_t q = 0; q < np * nl; ++q) frac_cloud[q + np * nl * t2] = ff.v[q];
+    }
+    for (size_t q = 0; q < np * nl; ++q) {
+      for (int t2 = 0; t2 < n_cloud_type; ++t2) w_cloud[q] += frac_cloud[q + np * nl * t2];
+      if (w_cloud[q] > 0.0)
+        for (int t2 = 0; t2 < n_cloud_type; ++t2) frac_cloud[q + np * nl * t2] /= w_cloud[q];
+    }
+    // McICA data beside the spectral file
+    const size_t slash = sp_file.find_last_of('/');
+    const std::string mcica_path = (slash == std::string::npos ? std::string() : sp_file.substr(0, slash + 1)) +
+                                   "mcica_data";
+    McicaData md;
+    if (!read_mcica_data(mcica_path, md, err)) return die(err);
+    gen = md.gen;
+    if (gen > SOCGPU_MAX_SUBCOL) return die("more subcolumns than the solver takes");
+    int nbands = 0;
+    std::vector<int> n_k_major(n_band > 0 ? n_band : 1, 0);
+    if (socgpu_spectrum_k_terms(h, n_band, &nbands, &nd_k, n_k_major.data()) != SOCGPU_I_NORMAL)
+      return die("spectrum lookup failed");
+    // sampling tables (socrates_set_cld_mcica.F90:106-160)
+    subcol_k.assign((size_t)n_band * nd_k, 1);
+    if (sampling == 0) {
+      n_subcol_req = gen;
+      std::fill(subcol_k.begin(), subcol_k.end(), gen);
+    } else if (sampling == 1) {
+      n_subcol_req = md.req_single;
+    } else {
+      n_subcol_req = md.req_optimal;
+      for (const auto &kv : isolir == SOCGPU_IP_SOLAR ? md.sw_subcol_k : md.lw_subcol_k) {
+        const int b = kv.first.first, k = kv.first.second;
+        if (b >= 1 && b <= n_band && k >= 1 && k <= nd_k) subcol_k[(size_t)(b - 1) + (size_t)n_band * (k - 1)] = kv.second;
+      }
+    }
+    if (n_subcol_req < 1) return die("the McICA data file gives no subcolumns for this sampling");
+    first_subcol_k.assign((size_t)n_band * (nd_k + 1), 0);
+    auto fs = [&](int b, int k) -> int & { return first_subcol_k[(size_t)b + (size_t)n_band * k]; };
+    fs(first - 1, 0) = 1;
+    for (int b = first - 1; b < last; ++b) {
+      const int n_k = n_k_major[b];
+      for (int k = 0; k < n_k; ++k) fs(b, k + 1) = fs(b, k) + subcol_k[(size_t)b + (size_t)n_band * k];
+      if (b < last - 1) fs(b + 1, 0) = fs(b, n_k);
+    }
+    subcol_reorder.assign(n_subcol_req, 0);
+    for (int l = 1; l <= n_subcol_req; ++l) {
+      int v2;
+      if (isolir == SOCGPU_IP_SOLAR) v2 = l % gen;
+      else if (sampling == 0) v2 = l;
+      else {
+        const std::vector<int> &src = sampling == 1 ? md.reorder_single : md.reorder_optimal;
+        if ((int)src.size() < n_subcol_req) return die("McICA data file: short subcolumn reorder list");
+        v2 = src[l - 1] % gen;
+      }
+      subcol_reorder[l - 1] = v2 == 0 ? gen : v2;
+    }
+    // the generator's inputs: condensate variability weighted by the
+    // grid-box condensate, decorrelation scales, seeds 10 + profile
+    std::vector<double> cond_rsd(np * nl), dp_cloud(np * nl, dp_corr_strat), dp_cond(np * nl, 0.5 * dp_corr_strat);
+    std::vector<double> zero(np * nl, 0.0);
+    const double eps = std::numeric_limits<double>::epsilon();
+    for (size_t q = 0; q < np * nl; ++q) {
+      double num = 0.0, den = 0.0;
+      for (int k = 0; k < nc; ++k) {
+        const double wgt = std::max(eps, cmr[q + np * nl * k] * frac_cloud[q + np * nl * (i_cloud_type[k] - 1)]);
+        num += mcica_sigma * wgt;
+        den += wgt;
+      }
+      cond_rsd[q] = num / den;
+    }
+    std::vector<int> seeds(np);
+    for (size_t l = 0; l < np; ++l) seeds[l] = 10 + (int)l + 1;
+    c_sub.assign(np * nl * (size_t)gen, 0.0);
+    n_subcol_cld.assign(np, 0);
+    st = socgpu_cloud_gen((int)nl, 1, (int)nl, (int)np, 1, (int)np, gen, md.n1, md.n2, md.ipph, 2, seeds.data(),
+                          dp_cloud.data(), dp_cond.data(), cond_rsd.data(), w_cloud.data(), zero.data(), zero.data(),
+                          p.data(), md.xcw.data(), n_subcol_cld.data(), c_sub.data(), SOCGPU_RNG_LCG, msg, sizeof(msg));
+    if (st != SOCGPU_I_NORMAL) return die(msg);
+    frac_cloudy.assign(np, 1.0);
+    if (sampling != 0)
+      for (size_t l = 0; l < np; ++l) frac_cloudy[l] = (double)n_subcol_cld[l] / (double)gen;
+  }
+
   socgpu_control c{};
   c.isolir = isolir;
   c.i_angular_integration = SOCGPU_IP_TWO_STREAM;
   c.i_2stream = two_stream;
   c.i_scatter_method = scatter;
   c.i_solver = solver;
-  c.i_cloud = SOCGPU_IP_CLOUD_CLEAR;
-  c.i_cloud_representation = SOCGPU_IP_CLOUD_ICE_WATER;
+  c.i_cloud = mcica ? SOCGPU_IP_CLOUD_MCICA : SOCGPU_IP_CLOUD_CLEAR;
+  c.i_cloud_representation = representation ? representation : SOCGPU_IP_CLOUD_ICE_WATER;
   c.i_gas_overlap = gas ? overlap : SOCGPU_IP_OVERLAP_RANDOM;
   c.i_direct_tau = direct_tau;
   c.l_rescale = rescale;
@@ -319,10 +585,10 @@ int main(int argc, char **argv) {
   d.nd_layer = (int)nl;
   d.id_cloud_top = 1;
   d.nd_aerosol_mode = 1;
-  d.nd_cloud_component = 1;
-  d.nd_cloud_type = 1;
-  d.nd_subcol_gen = 1;
-  d.nd_subcol_req = 1;
+  d.nd_cloud_component = std::max(1, nc);
+  d.nd_cloud_type = n_cloud_type;
+  d.nd_subcol_gen = gen;
+  d.nd_subcol_req = n_subcol_req;
   socgpu_atm atm{};
   atm.n_profile = (int)np;
   atm.n_layer = (int)nl;
@@ -344,6 +610,26 @@ int main(int argc, char **argv) {
   out.flux_direct = isolir == SOCGPU_IP_SOLAR ? direct.data() : nullptr;
   socgpu_aer aer{};
   socgpu_cld cld{};
+  if (mcica) {
+    cld.n_condensed = nc;
+    cld.type_condensed = type_condensed.data();
+    cld.i_cloud_type = i_cloud_type.data();
+    cld.i_condensed_param = i_condensed_param.data();
+    cld.i_condensed_type = i_condensed_type.data();
+    cld.condensed_mix_ratio = cmr.data();
+    cld.condensed_dim_char = dim.data();
+    cld.n_cloud_type = n_cloud_type;
+    cld.w_cloud = w_cloud.data();
+    cld.frac_cloud = frac_cloud.data();
+    cld.n_subcol_gen = gen;
+    cld.n_subcol_req = n_subcol_req;
+    cld.c_sub = c_sub.data();
+    cld.frac_cloudy = frac_cloudy.data();
+    cld.n_subcol_cld = n_subcol_cld.data();
+    cld.subcol_k = subcol_k.data();
+    cld.first_subcol_k = first_subcol_k.data();
+    cld.subcol_reorder = subcol_reorder.data();
+  }
   const auto t0 = std::chrono::steady_clock::now();
   st = socgpu_radiance_calc(&c, &d, h, &atm, &cld, &aer, &bd, &out, msg, sizeof(msg));
   const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -14,8 +14,9 @@ namespace socgpu {
 constexpr int kMaxAbsPerBand = 12;
 // Planck polynomial degree limit (block 6).
 constexpr int kMaxPlanckCoeff = 12;
-// Cloud parameters per Pade set (opt_prop_pade_2_mod.F90: 16 coefficients).
-constexpr int kPadeParm = 16;
+// Coefficients kept per cloud parameter set: the most any supported scheme
+// reads (Pade: 16, opt_prop_pade_2_mod.F90; Fu: 14; Slingo-Schrecker: 6).
+constexpr int kCloudParm = 16;
 constexpr int kMaxCloudComp = 4;
 
 // Self-broadened absorbers whose gas fractions a column stages (lookup tables).
@@ -162,6 +163,7 @@ struct FluxParams {
   int comp_type[kMaxCloudComp];      // cloud type of each component (1-based)
   int comp_phase[kMaxCloudComp];     // ip_phase_water / ice
   int comp_parm_index[kMaxCloudComp];// 0-based drop or ice type
+  int comp_scheme[kMaxCloudComp];    // parametrization (ip_slingo_schrecker, ip_drop_pade_2, ...)
   const double *condensed_mix_ratio, *condensed_dim_char, *w_cloud, *frac_cloud;
   const double *c_sub, *frac_cloudy;
   const int *n_subcol_cld;

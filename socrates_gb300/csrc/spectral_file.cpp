@@ -110,7 +110,9 @@ struct SpectralFile {
   std::vector<int> n_band_cont, index_cont, fnc_cont;
   std::vector<double> k_cont, scale_cont, p_ref_cont, t_ref_cont;
   int index_water = 0;
-  std::vector<double> drop_parm, ice_parm;
+  // blocks 10 and 12: (ncp, n_band, n_type) at the file's type numbers
+  int ncp = 0;
+  std::vector<double> drop_parm, ice_parm, drop_lo, drop_hi, ice_lo, ice_hi;
   std::vector<int> drop_ids, ice_ids, drop_on, ice_on;
   // lookup tables of the '_k' file
   int n_pre = 0, n_tmp = 0, n_gf = 0, nsb = 0, nd_t = 0;
@@ -153,14 +155,14 @@ struct SpectralFile {
       d.thermal_coeff = thermal.data();
     }
     if (!drop_ids.empty()) {
-      d.nd_cloud_parameter = 16;
+      d.nd_cloud_parameter = ncp;
       d.nd_drop_type = (int)drop_ids.size();
       d.drop_parm_list = drop_parm.data();
       d.i_drop_parm = drop_ids.data();
       d.l_drop_type = drop_on.data();
     }
     if (!ice_ids.empty()) {
-      d.nd_cloud_parameter = 16;
+      d.nd_cloud_parameter = ncp;
       d.nd_ice_type = (int)ice_ids.size();
       d.ice_parm_list = ice_parm.data();
       d.i_ice_parm = ice_ids.data();
@@ -683,42 +685,75 @@ bool read_spectral_file(const std::string &path, const std::string &k_path, cons
       }
     }
   }
-  // blocks 10 and 12: Pade parameter sets
-  auto pade = [&](int t, int want, std::vector<double> &parm, std::vector<int> &ids, std::vector<int> &on) {
+  // blocks 10 and 12 (read_block_10_0_2 / read_block_12_0_2 of
+  // read_spectrum.F90): every parameter set at its type number, with its
+  // scheme and range of validity
+  struct CloudSet { int type, scheme, npar; double lo, hi; std::vector<double> v; };
+  auto cloud_sets = [&](int t) {
+    std::vector<CloudSet> out;
     for (const Block &bl : blocks) {
       if (bl.type != t) continue;
-      size_t h = 0;
+      size_t h = 0, ht = bl.lines.size();
+      for (size_t q = 0; q < bl.lines.size(); ++q) {
+        const std::string u = upper(bl.lines[q]);
+        if (u.find("TYPE NUMBER") != std::string::npos) ht = q;
+      }
       while (h < bl.lines.size() &&
              !(bl.lines[h].find('=') != std::string::npos && upper(bl.lines[h]).find("PARAMETERS") != std::string::npos))
         ++h;
-      if (h >= bl.lines.size()) continue;
-      const int scheme = int_after_eq(bl.lines[h]), npar = int_after_eq(bl.lines[h], 1);
-      if (scheme != want || npar != 16) continue;
+      if (h >= bl.lines.size() || ht >= bl.lines.size()) continue;
+      CloudSet cs{int_after_eq(bl.lines[ht]), int_after_eq(bl.lines[h]), int_after_eq(bl.lines[h], 1), 0.0, 0.0, {}};
+      if (cs.type < 1 || cs.npar < 1) continue;
       std::vector<std::string> tok;
       for (size_t q = h + 1; q < bl.lines.size(); ++q) {
         const std::string &l = bl.lines[q];
         const std::string u = upper(l);
         bool digit = false;
         for (char c : l) digit |= (bool)std::isdigit((unsigned char)c);
-        if (u.find("RANGE") != std::string::npos || !digit) continue;
+        if (u.find("MOMENTS") != std::string::npos || !digit) continue;
+        if (u.find("RANGE") != std::string::npos) {
+          const size_t e = l.find('='), dd = l.find("--");
+          if (e != std::string::npos && dd != std::string::npos && dd > e) {
+            cs.lo = num(l.substr(e + 1, dd - e - 1));
+            cs.hi = num(l.substr(dd + 2));
+          }
+          continue;
+        }
         if (u.find("BAND") != std::string::npos && l.find('=') != std::string::npos) tok.push_back(std::to_string(int_after_eq(l)));
         else
           for (auto &x : split(l)) tok.push_back(x);
       }
-      const size_t base = parm.size();
-      parm.resize(base + 16 * (size_t)nb, 0.0);
+      cs.v.assign((size_t)cs.npar * nb, 0.0);
       size_t q = 0;
       for (int i = 0; i < nb && q < tok.size(); ++i) {
         int b = std::atoi(tok[q++].c_str()) - 1;
-        for (int v = 0; v < 16 && q < tok.size(); ++v)
-          if (b >= 0 && b < nb) parm[base + (size_t)v + 16 * (size_t)b] = num(tok[q++]);
+        for (int v = 0; v < cs.npar && q < tok.size(); ++v)
+          if (b >= 0 && b < nb) cs.v[(size_t)v + (size_t)cs.npar * b] = num(tok[q++]);
       }
-      ids.push_back(scheme);
-      on.push_back(1);
+      out.push_back(std::move(cs));
+    }
+    return out;
+  };
+  const std::vector<CloudSet> drops = cloud_sets(10), ices = cloud_sets(12);
+  for (const auto &c : drops) s.ncp = std::max(s.ncp, c.npar);
+  for (const auto &c : ices) s.ncp = std::max(s.ncp, c.npar);
+  auto place = [&](const std::vector<CloudSet> &sets, std::vector<double> &parm, std::vector<int> &ids,
+                   std::vector<int> &on, std::vector<double> &lo, std::vector<double> &hi) {
+    int nt = 0;
+    for (const auto &c : sets) nt = std::max(nt, c.type);
+    if (nt == 0) return;
+    parm.assign((size_t)s.ncp * nb * nt, 0.0);
+    ids.assign(nt, 0); on.assign(nt, 0); lo.assign(nt, 0.0); hi.assign(nt, 0.0);
+    for (const auto &c : sets) {
+      const int t = c.type - 1;
+      ids[t] = c.scheme; on[t] = 1; lo[t] = c.lo; hi[t] = c.hi;
+      for (int b = 0; b < nb; ++b)
+        for (int v = 0; v < c.npar; ++v)
+          parm[(size_t)v + (size_t)s.ncp * ((size_t)b + (size_t)nb * t)] = c.v[(size_t)v + (size_t)c.npar * b];
     }
   };
-  pade(10, SOCGPU_IP_DROP_PADE_2, s.drop_parm, s.drop_ids, s.drop_on);
-  pade(12, SOCGPU_IP_ICE_PADE_2_PHF, s.ice_parm, s.ice_ids, s.ice_on);
+  place(drops, s.drop_parm, s.drop_ids, s.drop_on, s.drop_lo, s.drop_hi);
+  place(ices, s.ice_parm, s.ice_ids, s.ice_on, s.ice_lo, s.ice_hi);
   sf = std::move(s);
   return true;
 }

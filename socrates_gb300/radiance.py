@@ -140,14 +140,119 @@ class McicaState:
     subcol_reorder: np.ndarray   # (n_subcol_req)
 
 
+@dataclass
+class McicaData:
+    """The McICA data file of a pair of spectral files (StrMcica,
+    def_mcica.F90): subcolumn counts, the sampling tables and the table of
+    the water-content distribution for cloud_gen."""
+    n_subcol_gen: int = 0
+    n_subcol_req_single: int = 0
+    n_subcol_req_optimal: int = 0
+    ipph: int = 0
+    lw_subcol_reorder_single: np.ndarray | None = None
+    lw_subcol_reorder_optimal: np.ndarray | None = None
+    sw_subcol_k: dict | None = None      # {(band, k): subcolumns}, 1-based; others take 1
+    lw_subcol_k: dict | None = None
+    xcw: np.ndarray | None = None        # (n1, n2)
+
+
+def read_mcica_data(path) -> McicaData:
+    """read_mcica_data (def_mcica.F90): the keyword records of the *DATA
+    block, each followed by its values."""
+    lines = open(path).read().splitlines()
+    i = next(q for q, ln in enumerate(lines) if ln.startswith("*DATA")) + 1
+    d = McicaData()
+    n1 = n2 = 0
+
+    def numbers(start, count, conv=int):
+        out, q = [], start
+        while len(out) < count:
+            out += [conv(x) for x in lines[q].split()]
+            q += 1
+        return out[:count], q
+
+    while i < len(lines) and not lines[i].startswith("*END"):
+        key = lines[i].strip()
+        i += 1
+        if key in ("tot_subcol_gen", "n_subcol_gen"):
+            (d.n_subcol_gen,), i = numbers(i, 1)
+        elif key in ("subcol_need_single", "n_subcol_req_single"):
+            (d.n_subcol_req_single,), i = numbers(i, 1)
+        elif key in ("subcol_need_optimal", "n_subcol_req_optimal"):
+            (d.n_subcol_req_optimal,), i = numbers(i, 1)
+        elif key == "ipph":
+            (d.ipph,), i = numbers(i, 1)
+        elif key == "lw_subcol_reorder_single":
+            v, i = numbers(i, d.n_subcol_req_single)
+            d.lw_subcol_reorder_single = np.array(v, np.int32)
+        elif key == "lw_subcol_reorder_optimal":
+            v, i = numbers(i, d.n_subcol_req_optimal)
+            d.lw_subcol_reorder_optimal = np.array(v, np.int32)
+        elif key in ("sw_subcol_k", "lw_subcol_k"):
+            table = {}
+            while True:
+                b, k, n = (int(x) for x in lines[i].split()[:3])
+                i += 1
+                if b == -99:
+                    break
+                table[(b, k)] = n
+            setattr(d, key, table)
+        elif key == "n1":
+            (n1,), i = numbers(i, 1)
+        elif key == "n2":
+            (n2,), i = numbers(i, 1)
+        elif key == "xcw":
+            v, i = numbers(i, n1 * n2, float)
+            d.xcw = np.asfortranarray(np.array(v).reshape((n1, n2), order="F"))
+    return d
+
+
+def write_mcica_data(path, d: McicaData) -> None:
+    """The McICA data file in the record layout read_mcica_data reads."""
+    L = ["*DATA", "", "tot_subcol_gen", f"{d.n_subcol_gen:5d}", "subcol_need_single", f"{d.n_subcol_req_single:5d}",
+         "subcol_need_optimal", f"{d.n_subcol_req_optimal:5d}", "ipph", f"{d.ipph:5d}", ""]
+    rows = lambda v, fmt, n: ["".join(fmt.format(x) for x in v[q:q + n]) for q in range(0, len(v), n)]
+    for key in ("lw_subcol_reorder_single", "lw_subcol_reorder_optimal"):
+        v = getattr(d, key)
+        if v is not None:
+            L += [key] + rows(list(v), "{:5d}", 10) + [""]
+    for key in ("sw_subcol_k", "lw_subcol_k"):
+        L.append(key)
+        L += [f"{b:4d}{k:4d}{n:4d}" for (b, k), n in sorted((getattr(d, key) or {}).items())]
+        L += [f"{-99:4d}{0:4d}{0:4d}", ""]
+    n1, n2 = d.xcw.shape
+    L += ["n1", f"{n1:6d}", "n2", f"{n2:6d}", "xcw"]
+    L += rows(list(d.xcw.ravel(order="F")), " {:15.8E}", 5)
+    L.append("*END")
+    with open(path, "w") as fh:
+        fh.write("\n".join(L) + "\n")
+
+
 def mcica_sampling(spectrum: Spectrum, isolir: int, n_subcol_gen: int, sampling: int, first_band: int = 1,
-                   last_band: int = 0):
+                   last_band: int = 0, data: McicaData | None = None):
     """subcol_k, first_subcol_k, subcol_reorder and n_subcol_req of
-    set_cld_mcica (socrates_set_cld_mcica.F90:106-160).  Optimal sampling
-    needs the reference's mcica_data tables; single sampling here takes one
-    subcolumn per k-term with n_subcol_req = number of k-terms."""
+    set_cld_mcica (socrates_set_cld_mcica.F90:106-160) with the counts of
+    l_run_cdf.F90:1281-1290.  With the McICA data file, the tables are the
+    reference's; without it single sampling takes one subcolumn per k-term
+    with n_subcol_req = number of k-terms, and optimal sampling is refused."""
     nb, ndk = spectrum.n_band, spectrum.nd_k_term
     last_band = last_band or nb
+    if data is not None and sampling != abi.IP_MCICA_FULL_SAMPLING:
+        single = sampling == abi.IP_MCICA_SINGLE_SAMPLING
+        req = data.n_subcol_req_single if single else data.n_subcol_req_optimal
+        subcol_k = np.ones((nb, ndk), np.int32)
+        if not single:
+            table = data.sw_subcol_k if isolir == abi.IP_SOLAR else data.lw_subcol_k
+            for (b, k), n in (table or {}).items():
+                if 1 <= b <= nb and 1 <= k <= ndk:
+                    subcol_k[b - 1, k - 1] = n
+        if isolir == abi.IP_SOLAR:
+            reorder = np.array([l % n_subcol_gen for l in range(1, req + 1)], np.int32)
+        else:
+            src = data.lw_subcol_reorder_single if single else data.lw_subcol_reorder_optimal
+            reorder = np.asarray(src[:req], np.int32) % n_subcol_gen
+        reorder[reorder == 0] = n_subcol_gen
+        return np.asfortranarray(subcol_k), _first_subcol(spectrum, subcol_k, first_band, last_band), reorder, req
     if sampling == abi.IP_MCICA_FULL_SAMPLING:
         subcol_k = np.full((nb, ndk), n_subcol_gen, np.int32)
         req = n_subcol_gen
@@ -160,6 +265,18 @@ def mcica_sampling(spectrum: Spectrum, isolir: int, n_subcol_gen: int, sampling:
         req = max(req, 1)
     else:
         raise RadianceError(abi.I_ERR_FATAL, "optimal sampling needs the reference's mcica_data tables")
+    first = _first_subcol(spectrum, subcol_k, first_band, last_band)
+    if isolir == abi.IP_SOLAR or sampling != abi.IP_MCICA_FULL_SAMPLING:
+        reorder = np.array([l % n_subcol_gen for l in range(1, req + 1)], np.int32)
+    else:
+        reorder = np.arange(1, req + 1, dtype=np.int32)
+    reorder[reorder == 0] = n_subcol_gen
+    return np.asfortranarray(subcol_k), np.asfortranarray(first), reorder, req
+
+
+def _first_subcol(spectrum: Spectrum, subcol_k, first_band: int, last_band: int):
+    """first_subcol_k (socrates_set_cld_mcica.F90:129-139)."""
+    nb, ndk = spectrum.n_band, spectrum.nd_k_term
     first = np.zeros((nb, ndk + 1), np.int32)
     first[first_band - 1, 0] = 1
     for b in range(first_band - 1, last_band):
@@ -169,12 +286,7 @@ def mcica_sampling(spectrum: Spectrum, isolir: int, n_subcol_gen: int, sampling:
             first[b, k + 1] = first[b, k] + subcol_k[b, k]
         if b < last_band - 1:
             first[b + 1, 0] = first[b, n_k]
-    if isolir == abi.IP_SOLAR or sampling != abi.IP_MCICA_FULL_SAMPLING:
-        reorder = np.array([l % n_subcol_gen for l in range(1, req + 1)], np.int32)
-    else:
-        reorder = np.arange(1, req + 1, dtype=np.int32)
-    reorder[reorder == 0] = n_subcol_gen
-    return np.asfortranarray(subcol_k), np.asfortranarray(first), reorder, req
+    return np.asfortranarray(first)
 
 
 # ---------------------------------------------------------------------------
@@ -220,14 +332,16 @@ class Marshal:
             cd = col.cld
             ict = id_cloud_top - 1
             cl = self.cld
-            cl.n_condensed = 2
-            cl.type_condensed = _ip([abi.IP_PHASE_WATER, abi.IP_PHASE_ICE], k)
-            cl.i_cloud_type = _ip([abi.IP_CLOUD_TYPE_WATER, abi.IP_CLOUD_TYPE_ICE], k)
-            cl.i_condensed_param = _ip([abi.IP_DROP_PADE_2, abi.IP_ICE_PADE_2_PHF], k)
-            cl.i_condensed_type = _ip([1, 1], k)
+            # components: water and ice as two cloud types with the Pade
+            # schemes of type 1 unless the cloud fields say otherwise
+            cl.n_condensed = int(cd.get("n_condensed", 2))
+            cl.type_condensed = _ip(cd.get("type_condensed", [abi.IP_PHASE_WATER, abi.IP_PHASE_ICE]), k)
+            cl.i_cloud_type = _ip(cd.get("i_cloud_type", [abi.IP_CLOUD_TYPE_WATER, abi.IP_CLOUD_TYPE_ICE]), k)
+            cl.i_condensed_param = _ip(cd.get("i_condensed_param", [abi.IP_DROP_PADE_2, abi.IP_ICE_PADE_2_PHF]), k)
+            cl.i_condensed_type = _ip(cd.get("i_condensed_type", [1, 1]), k)
             cl.condensed_mix_ratio = _dp(cd["condensed_mix_ratio"][:, ict:, :], k)
             cl.condensed_dim_char = _dp(cd["condensed_dim_char"][:, ict:, :], k)
-            cl.n_cloud_type = 2
+            cl.n_cloud_type = int(cd.get("n_cloud_type", 2))
             cl.w_cloud = _dp(cd["w_cloud"][:, ict:], k)
             cl.frac_cloud = _dp(cd["frac_cloud"][:, ict:, :], k)
             cl.n_subcol_gen, cl.n_subcol_req = mcica.n_subcol_gen, mcica.n_subcol_req
@@ -333,14 +447,38 @@ def cloud_gen(col, n_subcol: int, ioverlap: int = abi.IP_EXPONENTIAL_RAND, rng: 
 
 def set_cld_mcica(spectrum: Spectrum, col, isolir: int, sampling: int = abi.IP_MCICA_SINGLE_SAMPLING,
                   ioverlap: int = abi.IP_EXPONENTIAL_RAND, rng: int = abi.RNG_LCG, id_cloud_top: int = 1,
-                  c_sub=None, n_subcol_cld=None) -> McicaState:
+                  c_sub=None, n_subcol_cld=None, data: McicaData | None = None, impl=None) -> McicaState:
     """set_cld_mcica (socrates_set_cld_mcica.F90:82-228): sampling tables,
     the generator and frac_cloudy; the fill of cloudy subcolumns is applied
-    by the solver from n_subcol_cld."""
-    gen = int(col.cld["n_subcol_gen"])
-    subcol_k, first, reorder, req = mcica_sampling(spectrum, isolir, gen, sampling)
-    if c_sub is None:
-        c_sub, n_subcol_cld = cloud_gen(col, gen, ioverlap, rng, id_cloud_top)
+    by the solver from n_subcol_cld.
+
+    With the McICA data file (`data`) the call is the reference's: its
+    subcolumn counts and tables, the generator's ipph and xcw, the relative
+    standard deviation of each component (col.cld["rel_var_dens"]) combined
+    with the grid-box condensate as weights, and the condensate decorrelation
+    at half the cloud's (lines 165-193)."""
+    cd = col.cld
+    gen = int(data.n_subcol_gen if data is not None else cd["n_subcol_gen"])
+    subcol_k, first, reorder, req = mcica_sampling(spectrum, isolir, gen, sampling, data=data)
+    if c_sub is None and data is not None:
+        ict = id_cloud_top - 1
+        nc = int(cd.get("n_condensed", 2))
+        types = cd.get("i_cloud_type", [abi.IP_CLOUD_TYPE_WATER, abi.IP_CLOUD_TYPE_ICE])
+        rvd = np.broadcast_to(np.asarray(cd.get("rel_var_dens", 0.0), dtype=np.float64), (nc,))
+        eps = np.finfo(np.float64).eps
+        num = np.zeros((col.n_profile, col.n_layer - ict))
+        den = np.zeros_like(num)
+        for i in range(nc):
+            wgt = np.maximum(eps, cd["condensed_mix_ratio"][:, ict:, i] * cd["frac_cloud"][:, ict:, types[i] - 1])
+            num = num + rvd[i] * wgt
+            den = den + wgt
+        cols = dict(cd)
+        cols["dp_corr_cond"] = cd["dp_corr_cloud"] * 0.5
+        col2 = type(col)(**{**col.__dict__, "cld": cols})
+        c_sub, n_subcol_cld = cloud_gen(col2, gen, ioverlap, rng, id_cloud_top, ipph=data.ipph, xcw=data.xcw,
+                                        sigma_qcw=np.asfortranarray(num / den), impl=impl)
+    elif c_sub is None:
+        c_sub, n_subcol_cld = cloud_gen(col, gen, ioverlap, rng, id_cloud_top, impl=impl)
     if sampling == abi.IP_MCICA_FULL_SAMPLING:
         frac_cloudy = np.ones(col.n_profile)
     else:

@@ -179,10 +179,19 @@ class Spectrum:
     n_deg_fit: int = 0
     t_ref_planck: float = 0.0
     thermal_coeff: np.ndarray | None = None  # (n_deg_fit+1, n_band)
-    drop_parm_list: np.ndarray | None = None # (16, n_band, n_drop_type)
-    i_drop_parm: np.ndarray | None = None    # (n_drop_type)
-    ice_parm_list: np.ndarray | None = None  # (16, n_band, n_ice_type)
+    # blocks 10 and 12: cloud parameter sets, indexed by the file's type number
+    drop_parm_list: np.ndarray | None = None # (n_parameter, n_band, n_drop_type)
+    i_drop_parm: np.ndarray | None = None    # (n_drop_type) scheme, 0 where the type is undefined
+    ice_parm_list: np.ndarray | None = None  # (n_parameter, n_band, n_ice_type)
     i_ice_parm: np.ndarray | None = None
+    drop_n_parm: np.ndarray | None = None    # (n_drop_type) coefficients the file gives per band
+    drop_n_phf: np.ndarray | None = None     # (n_drop_type) phase-function moments
+    drop_parm_min_dim: np.ndarray | None = None  # (n_drop_type) range of validity [m]
+    drop_parm_max_dim: np.ndarray | None = None
+    ice_n_parm: np.ndarray | None = None
+    ice_n_phf: np.ndarray | None = None
+    ice_parm_min_dim: np.ndarray | None = None
+    ice_parm_max_dim: np.ndarray | None = None
     # block 13: Doppler broadening (per absorber)
     l_doppler: np.ndarray | None = None      # (n_absorb) 0/1
     doppler_cor: np.ndarray | None = None    # (n_absorb)
@@ -361,18 +370,22 @@ class Spectrum:
             d.t_ref_planck = self.t_ref_planck
             d.nd_thermal_coeff = self.thermal_coeff.shape[0]
             d.thermal_coeff = dp(self.thermal_coeff)
+        # both lists share nd_cloud_parameter (StrSpecDim), so pad the shorter
+        ncp = max([a.shape[0] for a in (self.drop_parm_list, self.ice_parm_list) if a is not None], default=0)
+        pad = lambda a: np.asfortranarray(np.concatenate(
+            [a, np.zeros((ncp - a.shape[0],) + a.shape[1:])], axis=0)) if a.shape[0] < ncp else a
         if self.drop_parm_list is not None:
-            d.nd_cloud_parameter = self.drop_parm_list.shape[0]
+            d.nd_cloud_parameter = ncp
             d.nd_drop_type = self.drop_parm_list.shape[2]
-            d.drop_parm_list = dp(self.drop_parm_list)
+            d.drop_parm_list = dp(pad(self.drop_parm_list))
             d.i_drop_parm = ip(self.i_drop_parm)
-            d.l_drop_type = ip(np.ones(d.nd_drop_type, np.int32))
+            d.l_drop_type = ip((np.asarray(self.i_drop_parm) > 0).astype(np.int32))
         if self.ice_parm_list is not None:
-            d.nd_cloud_parameter = max(d.nd_cloud_parameter, self.ice_parm_list.shape[0])
+            d.nd_cloud_parameter = ncp
             d.nd_ice_type = self.ice_parm_list.shape[2]
-            d.ice_parm_list = dp(self.ice_parm_list)
+            d.ice_parm_list = dp(pad(self.ice_parm_list))
             d.i_ice_parm = ip(self.i_ice_parm)
-            d.l_ice_type = ip(np.ones(d.nd_ice_type, np.int32))
+            d.l_ice_type = ip((np.asarray(self.i_ice_parm) > 0).astype(np.int32))
         self._keep = keep
         return d
 
@@ -544,18 +557,33 @@ class Spectrum:
                 flag = "T" if self.l_doppler[i] else "F"
                 L.append(f"{i + 1:5d}       {flag:>6s}         {self.doppler_cor[i]:12.5E}")
             L.append("*END")
-        for blk, parm, ids, label in ((10, self.drop_parm_list, self.i_drop_parm, "droplets"),
-                                      (12, self.ice_parm_list, self.i_ice_parm, "ice crystals")):
+        # blocks 10 and 12 in the fixed layout read_spectrum.F90 reads
+        # (read_block_10_0_2: 4(4x, 1pe12.5) per line, six significant digits)
+        for blk, pre, parm, ids, label in ((10, "drop", self.drop_parm_list, self.i_drop_parm, "droplets"),
+                                           (12, "ice", self.ice_parm_list, self.i_ice_parm, "ice crystals")):
             if parm is None:
                 continue
+            npar = getattr(self, pre + "_n_parm")
+            nphf = getattr(self, pre + "_n_phf")
+            lo, hi = getattr(self, pre + "_parm_min_dim"), getattr(self, pre + "_parm_max_dim")
+            word = "Number" if blk == 10 else "number"
             for t in range(parm.shape[2]):
+                if int(ids[t]) <= 0:
+                    continue
+                n = int(npar[t]) if npar is not None else parm.shape[0]
                 L.append(f"*BLOCK: TYPE = {blk:4d}: SUBTYPE =    0: VERSION =    2")
                 L.append(f"Parametrized scattering data for {label}.")
-                L.append(f" Type number = {t + 1:5d}")
-                L.append(f"Index of parametrization scheme = {int(ids[t]):5d}:   Number of parameters = {parm.shape[0]:5d}")
-                L.append("Band        Parameters")
+                L.append(f" Type number of {label} = {t + 1:5d}")
+                L.append(f"Index of parametrization scheme = {int(ids[t]):5d}:   {word} of parameters = {n:5d}")
+                L.append(f"Number of moments of the phase function = {int(nphf[t]) if nphf is not None else 1:5d}")
+                rlo = float(lo[t]) if lo is not None else 1.0e-07
+                rhi = float(hi[t]) if hi is not None else 1.0e-03
+                L.append(f"Range of validity of parametrization = {rlo:12.5E} -- {rhi:12.5E}")
                 for b in range(self.n_band):
-                    L.append(f"{b + 1:5d}   " + " ".join(e(c) for c in parm[:, b, t]))
+                    L.append(f"Band = {b + 1:5d}     Fitting parameters:")
+                    vals = parm[:n, b, t]
+                    for q in range(0, n, 4):
+                        L.append("".join(f"    {v:12.5E}" for v in vals[q:q + 4]))
                 L.append("*END")
         with open(path, "w") as fh:
             fh.write("\n".join(L) + "\n")
@@ -859,21 +887,32 @@ class Spectrum:
                     ldop[i] = 1 if v[1].upper().startswith("T") else 0
                     dcor[i] = float(v[2])
 
-        def pade(blk, want):
-            sets, ids = [], []
+        def cloud_sets(blk):
+            """Blocks 10 or 12 (read_block_10_0_2 / read_block_12_0_2 of
+            read_spectrum.F90): every set at its type number, with its scheme,
+            phase-function moments and range of validity."""
+            found = {}
             for bl in by.get(blk, []):
                 lines = bl["lines"]
                 head = next((ln for ln in lines if "=" in ln and "PARAMETERS" in ln.upper()), None)
-                if head is None:
+                tline = next((ln for ln in lines if "TYPE NUMBER" in ln.upper()), None)
+                if head is None or tline is None:
                     continue
+                ty = int(tline.split("=")[1].split()[0])
                 scheme = int(head.split("=")[1].split(":")[0])
                 npar = int(head.split("=")[2])
-                if scheme != want or npar != 16:
-                    continue
+                nphf, lo, hi = 1, 0.0, 0.0
                 vals = []
                 for ln in lines[lines.index(head) + 1:]:
                     u = ln.upper()
-                    if "RANGE" in u or "MOMENTS" in u or not any(ch.isdigit() for ch in ln):
+                    if "MOMENTS" in u:
+                        nphf = int(ln.split("=")[1].split()[0])
+                        continue
+                    if "RANGE" in u:
+                        r = ln.split("=")[1].split("--")
+                        lo, hi = float(r[0]), float(r[1])
+                        continue
+                    if not any(ch.isdigit() for ch in ln):
                         continue
                     if "BAND" in u and "=" in ln:
                         vals.append(ln.split("=")[1].split()[0])
@@ -885,18 +924,31 @@ class Spectrum:
                     b = int(vals[q]) - 1
                     arr[:, b] = [float(x) for x in vals[q + 1:q + 1 + npar]]
                     q += npar + 1
-                sets.append(arr)
-                ids.append(scheme)
-            if not sets:
-                return None, None
-            return np.asfortranarray(np.stack(sets, axis=2)), np.array(ids, np.int32)
+                found[ty] = (scheme, npar, nphf, lo, hi, arr)
+            if not found:
+                return None
+            nt = max(found)
+            ncp = max(v[1] for v in found.values())
+            parm = np.zeros((ncp, n_band, nt))
+            ids, npars, nphfs = (np.zeros(nt, np.int32) for _ in range(3))
+            lo, hi = np.zeros(nt), np.zeros(nt)
+            for ty, (scheme, npar, nphf, a, b, arr) in found.items():
+                parm[:npar, :, ty - 1] = arr
+                ids[ty - 1], npars[ty - 1], nphfs[ty - 1] = scheme, npar, nphf
+                lo[ty - 1], hi[ty - 1] = a, b
+            return np.asfortranarray(parm), ids, npars, nphfs, lo, hi
 
-        dpl, dids = pade(10, abi.IP_DROP_PADE_2)
-        ipl, iids = pade(12, abi.IP_ICE_PADE_2_PHF)
+        cloud = {}
+        for blk, pre in ((10, "drop"), (12, "ice")):
+            r = cloud_sets(blk)
+            if r is not None:
+                parm, ids, npars, nphfs, lo, hi = r
+                cloud.update({f"{pre}_parm_list": parm, f"i_{pre}_parm": ids, f"{pre}_n_parm": npars,
+                              f"{pre}_n_phf": nphfs, f"{pre}_parm_min_dim": lo, f"{pre}_parm_max_dim": hi})
         return cls(n_band=n_band, wavelength_short=wl[:, 0], wavelength_long=wl[:, 1],
                    type_absorb=np.array(types, np.int32), n_band_absorb=nba, index_absorb=ia,
                    i_band_k=ibk, i_scale_k=isk, i_scale_fnc=isf, k=_f(kk, np.float64), w=_f(ww, np.float64),
                    scale=_f(sc, np.float64), p_ref=pr, t_ref=tr, solar_flux_band=sol, rayleigh_coeff=ray,
-                   n_deg_fit=ndeg, t_ref_planck=tref, thermal_coeff=tc, drop_parm_list=dpl, i_drop_parm=dids,
-                   ice_parm_list=ipl, i_ice_parm=iids, l_doppler=ldop, doppler_cor=dcor, name=name or str(path),
-                   i_overlap=i_ovl, **cont, **tables)
+                   n_deg_fit=ndeg, t_ref_planck=tref, thermal_coeff=tc,
+                   l_doppler=ldop, doppler_cor=dcor, name=name or str(path),
+                   i_overlap=i_ovl, **cont, **tables, **cloud)

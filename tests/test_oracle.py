@@ -204,7 +204,7 @@ def test_cloud_gen_compaction_and_fraction():
 
 
 # ---------------------------------------------------------------------------
-KGO_FIXTURES = ("icrccm", "circ6", "ga7", "runes")
+KGO_FIXTURES = ("icrccm", "circ6", "ga7", "runes", "mcica5118")
 
 
 @pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(KGO_FIXTURES)))
@@ -244,6 +244,28 @@ def test_oracle_reproduces_circ6_ga7_known_good_output():
     half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
     err = np.abs(hr - kgo) / half_unit
     assert err.max() <= 1.0, f"layer {err.argmax()}: {hr[err.argmax()]} vs {kgo[err.argmax()]}"
+
+
+@pytest.mark.parametrize("run", ["lw_avg", "sw_avg", "sw_ds0_avg", "lw_ga7", "sw_ga7"])
+def test_oracle_reproduces_mcica5118_known_good_output(run):
+    """Pin McICA against the reference's known-good outputs
+    (examples/netcdf/mcica/run_me, ref_<run>.hrts): one cloud-resolving
+    column with water and ice as one homogeneous cloud type, 64 subcolumns
+    from cloud_gen's generator with the seeds, decorrelation scale and
+    water-content variability set_cld_mcica gives it, optimal sampling from
+    the McICA data files; GA3.0 files with Slingo-Schrecker droplets and
+    k_eqv overlap, GA7 files with Pade droplets and k_eqv_scl.  Every layer
+    must agree to half a unit of the 6th significant digit the reference
+    prints, up to 5 % of that half unit for values that sit on a rounding
+    boundary (the worst is 0.5608694890 against a printed 0.56087)."""
+    import circ6
+    import mcica5118 as M
+    out, m, col, kgo = M.run_case(run, M.spectra(), O.radiance_calc, impl=O.cloud_gen_impl)
+    assert 0 < int(m.n_subcol_cld[0]) < m.n_subcol_gen
+    hr = circ6.heating_rate(out, col.mass)[0]
+    half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
+    err = np.abs(hr - kgo) / half_unit
+    assert err.max() <= 1.05, f"layer {err.argmax()}: {hr[err.argmax()]} vs {kgo[err.argmax()]}"
 
 
 @pytest.mark.parametrize("section", ["sw", "lw_tground", "lw_flux_ground", "lw_tiles"])

@@ -26,11 +26,12 @@ def _tool():
     return str(build.TOOL)
 
 
-def _column_files(tmp, name, d, sp, sp_name, to_cdf=False, gases=None, wenyi=False, digits=7):
+def _column_files(tmp, name, d, sp, sp_name, to_cdf=False, gases=None, wenyi=False, digits=7, extra=None):
     """A case's inputs written as column files like the reference's, with the
     spectral file (and its '_k' tables) written beside them.  gases: the
     absorber types that have input files (default all); digits: significant
-    digits of the CDL values."""
+    digits of the CDL values; extra: {suffix: (coordinate, values)} of more
+    fields (clouds, the solar zenith angle and irradiance)."""
     sp_path = tmp / sp_name
     sp.write_text(sp_path)
     if sp.k_lookup is not None or sp.k_t_lookup_gas is not None:
@@ -56,6 +57,8 @@ def _column_files(tmp, name, d, sp, sp_name, to_cdf=False, gases=None, wenyi=Fal
         if gases is None or int(ty) in gases:
             files.append(put(SUFFIX[int(ty)], d["p"], d["gas"][:, j], SUFFIX[int(ty)]))
     files.append(put("tstar", [1.013e5], d["t_ground"], "tstar", "K"))
+    for suffix, (plev, values) in (extra or {}).items():
+        files.append(put(suffix, plev, values, suffix))
     surf = tmp / f"{name}.surf"
     write_cdl(surf, f"{name}.surf", [("lat", 1), ("lon", 1), ("basis", 1)],
               [("lat", ["lat"], [1.0], {}), ("lon", ["lon"], [0.0], {}), ("basis", ["basis"], [1.0], {}),
@@ -207,3 +210,69 @@ def test_loader_reads_self_broadened_and_temperature_tables(gpu_lib, tmp_path, k
     fscale = np.abs(ref["flux_up"]).max()
     for k in ("flux_up", "flux_down"):
         assert np.abs(got[k] - ref[k]).max() <= 1e-10 * fscale, k
+
+
+def _mcica5118_files(tmp, run, to_cdf):
+    """The inputs of one run of examples/netcdf/mcica as column files, with
+    its spectral file, the McICA data file beside it and the Wen-Yi tables;
+    returns (spectral file, base name, Wen-Yi source, options)."""
+    import mcica5118 as M
+    from socrates_gb300.radiance import write_mcica_data
+    d = np.load(M.FIXTURE)
+    sps = M.spectra()
+    solar, ga7 = run.startswith("sw"), run.endswith("ga7")
+    sp = sps[("sw_" if solar else "lw_") + ("ga7" if ga7 else "ga3")]
+    gases = {1: "q", 2: "co2", 3: "o3", 4: "n2o", 6: "ch4", 7: "o2"}
+    gas = np.zeros((d["p"].size, sp.n_absorb))
+    for j, ty in enumerate(sp.type_absorb):
+        if int(ty) in gases:
+            gas[:, j] = d[gases[int(ty)]]
+    case = dict(p=d["p"], t=d["t"], p_level=d["p_level"], t_level=d["t_level"], gas=gas, t_ground=d["tstar"],
+                alb=d["surfsw" if solar else "surflw"])
+    extra = {k: (d["p"], d[k]) for k in ("clfr", "lwm", "iwm", "re", "ire")}
+    if solar:
+        extra.update(szen=([1.013e5], d["szen"]), stoa=([1.013e5], d["stoa"]))
+    name = "sp_" + ("sw" if solar else "lw") + ("_ga7" if ga7 else "_ga3_0")
+    sp_path, base, wy = _column_files(tmp, "5118_142", case, sp, name, to_cdf, gases=set(gases),
+                                      wenyi=not solar, digits=17, extra=extra)
+    write_mcica_data(tmp / "mcica_data", M.mcica_data(d, "ga7_" if ga7 else "ga3_"))
+    opts = {"lw_avg": "-R 1 9 -I -t 12 +R -v 13 -g 5 -c -C 10 -K 1 -d 1 -i 1",
+            "sw_avg": "-R 1 6 -S -t 2 +R -v 13 -g 5 -r -C 10 -K 1 -d 3 -i 3",
+            "lw_ga7": "-R 1 9 -I +R -g 4 -c -C 10 -K 1 -d 5 -i 8",
+            "sw_ga7": "-R 1 6 -S +R -g 4 -r -C 10 -K 1 -d 5 -i 8"}[run].split()
+    opts += ["-m", "0.75", "+m", "2", "-dp", "10000"]
+    return sp_path, base, wy, opts, np.asarray(d["kgo_" + run])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("run,to_cdf", [("lw_avg", False), ("sw_avg", True), ("lw_ga7", True), ("sw_ga7", False)])
+def test_driver_reproduces_mcica5118(gpu_lib, tmp_path, run, to_cdf):
+    """The reference's McICA example (examples/netcdf/mcica/run_me) through
+    the column driver: cloud fields, droplet and ice types of the spectral
+    file, the McICA data file beside it, cloud_gen's subcolumns and optimal
+    sampling, from CDL or netCDF files; the written heating rates against
+    the known-good output to half a unit of the 6th digit (CDL, which
+    carries the single-precision inputs exactly) or 2e-5 of the largest
+    (netCDF output, single precision)."""
+    tool = _tool()
+    sp_path, base, wy, opts, kgo = _mcica5118_files(tmp_path, run, to_cdf)
+    cmd = [tool, "-s", str(sp_path)] + opts + ["-B", str(base)] + (["-W", str(wy)] if wy else [])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = str(base) + ".hrts"
+    if to_cdf:
+        scipy_io = pytest.importorskip("scipy.io")
+        with scipy_io.netcdf_file(out, "r", mmap=False) as nc:
+            hr = np.array(nc.variables["hrts"][:]).ravel()
+        assert np.abs(hr - kgo).max() <= 2e-5 * np.abs(kgo).max()
+    else:
+        _, hr = field(out)
+        half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
+        assert (np.abs(hr - kgo) / half_unit).max() <= 1.05
+
+
+def test_driver_refuses_clouds_without_processes(tmp_path):
+    """-C 10 without a droplet or ice type: the reference's message, no run."""
+    r = subprocess.run([_tool(), "-s", "x", "-R", "1", "1", "-I", "-C", "10", "-K", "1", "-B", "y"],
+                       capture_output=True, text=True)
+    assert r.returncode != 0 and "no cloudy processes" in r.stderr
