@@ -74,11 +74,16 @@ extern "C" {
 #define SOCGPU_IP_DIRECT_CSR_SCALING    2
 /* solvers, rad_pcf.F90:566-572 */
 #define SOCGPU_IP_SOLVER_NO_SCAT        2
+#define SOCGPU_IP_SOLVER_MIX_DIRECT     11   /* two cloud regions (solver_mix_direct.F90) */
 #define SOCGPU_IP_SOLVER_HOMOGEN_DIRECT 13
+#define SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN 16 /* two regions, Hogan's form (solver_mix_direct_hogan.F90) */
 /* cloud schemes, rad_pcf.F90:313,322 */
+#define SOCGPU_IP_CLOUD_MIX_MAX         2   /* clear and cloudy regions, maximum-random overlap */
+#define SOCGPU_IP_CLOUD_MIX_RANDOM      4   /* clear and cloudy regions, random overlap */
 #define SOCGPU_IP_CLOUD_CLEAR           5
 #define SOCGPU_IP_CLOUD_MCICA          10
 /* cloud representation, rad_pcf.F90:238-254 */
+#define SOCGPU_IP_CLOUD_HOMOGEN         1   /* one cloud type of all components */
 #define SOCGPU_IP_CLOUD_ICE_WATER       2
 /* cloud types, rad_pcf.F90:332-334 */
 #define SOCGPU_IP_CLOUD_TYPE_WATER      1

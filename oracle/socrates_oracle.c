@@ -318,6 +318,11 @@ typedef struct {
     double *alpha, *s_up_prime, *beta, *gam, *h;
     double *ty_tau[3], *ty_tau_dir[3], *ty_omega[3], *ty_asym[3];      /* cloud types 1..2 */
     double *ty_valid[3];
+    /* cloud regions (mix_column): cloudy-region coefficients and sources,
+     * the solver's elimination coefficients, the interface coefficients */
+    double *tc, *rc, *t0c, *t0dc, *sc1c, *sc2c, *s_up_c, *s_down_c;
+    double *b11, *b21, *b22, *g11, *g12, *g21, *g22, *h1, *h2, *ovl;
+    int nct;                    /* n_cloud_top, 1-based */
     int *slot;
     const double *adj;          /* adjust_solar_ke of k_eqv_scl (solar), or NULL */
 } work;
@@ -338,7 +343,10 @@ static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(doub
     X(s_up, pl) X(s_down, pl) X(source_ground, wp) \
     X(flux_direct, pl1) X(flux_direct_dir, pl1) X(flux_total, pl2) \
     X(flux_direct_acc, pl1) X(flux_total_acc, pl2) X(flux_direct_clear, pl1) X(flux_total_clear, pl2) \
-    X(alpha, wp) X(s_up_prime, wp) X(beta, pl) X(gam, pl) X(h, pl) X(cont_amount, pl)
+    X(alpha, wp) X(s_up_prime, wp) X(beta, pl) X(gam, pl) X(h, pl) X(cont_amount, pl) \
+    X(tc, pl) X(rc, pl) X(t0c, pl) X(t0dc, pl) X(sc1c, pl) X(sc2c, pl) X(s_up_c, pl) X(s_down_c, pl) \
+    X(b11, pl) X(b21, pl) X(b22, pl) X(g11, pl) X(g12, pl) X(g21, pl) X(g22, pl) X(h1, pl) X(h2, pl) \
+    X(ovl, pl1 * 8)
 
 static void work_init(work *w, int wp, int ndl, int n_profile, int n_layer, int nc, int na)
 {
@@ -1241,6 +1249,383 @@ static int k_eqv_minor(work *w, const socgpu_control *c, const lookup_fac *lf, c
 }
 
 /* --------------------------------------------------------------------- */
+/* Clouds in two regions, clear and cloudy (mix_column.F90), for
+ * ip_cloud_mix_max and ip_cloud_mix_random with ip_solver_mix_direct and
+ * ip_solver_mix_direct_hogan.  Layers are 1-based in the comments and
+ * 0-based in the arrays; interface i lies below layer i (0: the top). */
+
+/* The cloud fraction of 1-based layer i of profile l. */
+static double cloud_w(const socgpu_cld *cld, int ndp, int ict, int l, int i)
+{
+    return (i - 1 >= ict) ? cld->w_cloud[(size_t)l + (size_t)ndp * (size_t)(i - 1 - ict)] : 0.0;
+}
+
+/* set_cloud_geometry (set_cloud_geometry.F90:76-96): the first layer from
+ * id_ct with a cloudy profile, at most n_layer. */
+static int cloud_top(const socgpu_cld *cld, int ndp, int ict, int n_profile, int n_layer)
+{
+    int top = ict + 1;
+    for (;;) {
+        int any = 0;
+        for (int l = 0; l < n_profile && !any; ++l) any = cloud_w(cld, ndp, ict, l, top) > 0.0;
+        if (any || top >= n_layer) return top;
+        ++top;
+    }
+}
+
+/* overlap_coupled (overlap_coupled.F90:120-440) for the clear (region 1) and
+ * the cloudy (region 2) region: at each interface i = nct-1 .. n_layer the
+ * fractions of each upper region that lie over each lower one (ovl[0..3],
+ * cloud_overlap(:, i, 1..4)) and of each lower region under each upper one
+ * (ovl[4..7]).  0-based ovl index 2 j + k for region k above and j below,
+ * 4 + 2 j + k for region k below and j above. */
+static void overlap_coupled2(work *w, const socgpu_cld *cld, int ndp, int ict, int i_cloud)
+{
+    const int n_layer = w->n_layer, wp = w->wp, nct = w->nct;
+    const double tol = 1.0e+02 * EPS_R;
+    for (int l = 0; l < w->n_profile; ++l) {
+        double au[2] = {1.0, 0.0};
+        for (int i = nct - 1; i <= n_layer; ++i) {
+            const double corr = (i_cloud == SOCGPU_IP_CLOUD_MIX_MAX) ? 1.0 : 0.0;
+            double al[2], ao[2][2];
+            if (i < n_layer) {
+                const double wc = cloud_w(cld, ndp, ict, l, i + 1);
+                al[0] = 1.0 - wc;
+                al[1] = wc * 1.0;
+            } else {
+                al[0] = 1.0;
+                al[1] = 0.0;
+            }
+            for (int k = 0; k < 2; ++k) ao[k][k] = corr * (al[k] < au[k] ? al[k] : au[k]);
+            ao[0][1] = 0.0;
+            ao[1][0] = 0.0;
+            double art = 1.0 - ao[0][0];
+            art = art - ao[1][1];
+            double aru[2], arl[2];
+            for (int k = 0; k < 2; ++k) {
+                aru[k] = au[k] - ao[k][k];
+                arl[k] = al[k] - ao[k][k];
+            }
+            for (int k = 0; k < 2; ++k)
+                for (int j = 0; j < 2; ++j)
+                    if (art > tol) ao[k][j] = ao[k][j] + aru[k] * arl[j] / art;
+            double *cv = w->ovl + 8 * ((size_t)l + (size_t)wp * (size_t)i);
+            for (int k = 0; k < 2; ++k) {
+                cv[2 * k + k] = 1.0;
+                for (int j = 0; j < k; ++j) { cv[2 * j + k] = 0.0; cv[2 * k + j] = 0.0; }
+            }
+            for (int k = 0; k < 2; ++k)
+                if (au[k] > tol)
+                    for (int j = 0; j < 2; ++j) cv[2 * j + k] = ao[k][j] / au[k];
+            for (int k = 0; k < 2; ++k) {
+                cv[4 + 2 * k + k] = 1.0;
+                for (int j = 0; j < k; ++j) { cv[4 + 2 * j + k] = 0.0; cv[4 + 2 * k + j] = 0.0; }
+            }
+            for (int k = 0; k < 2; ++k)
+                if (al[k] > tol)
+                    for (int j = 0; j < 2; ++j) cv[4 + 2 * j + k] = ao[j][k] / al[k];
+            if (i < n_layer) { au[0] = al[0]; au[1] = al[1]; }
+        }
+    }
+}
+
+/* One k-term in two regions (mix_column.F90:150-460): the clear
+ * coefficients of every layer, the frac_cloud-weighted coefficients of the
+ * cloud types (two_coeff_cloud.F90), the sources (ir_source with w_free and
+ * w_cloud, or mixed_solar_source.F90) and solver_mix_direct.F90 or
+ * solver_mix_direct_hogan.F90.  Leaves flux_total and flux_direct as
+ * column_solve does. */
+static void solve_region_term(work *w, const socgpu_control *c, const socgpu_dimen *dm, const double *mass,
+                              const socgpu_cld *cld)
+{
+    const int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp, ndp = dm->nd_profile;
+    const int ict = dm->id_cloud_top - 1, ndc = w->ndl - ict, nct = w->nct;
+    const int solar = (c->isolir == SOCGPU_IP_SOLAR);
+    const int l_dir = (c->i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING || c->i_direct_tau == SOCGPU_IP_DIRECT_CSR_SCALING);
+    const double tiny_k = TINY_R;
+#define OV(l, i, m) (w->ovl[8 * ((size_t)(l) + (size_t)wp * (size_t)(i)) + (m)])
+    clear_coefficients(w, c, mass, ndp);
+    /* two_coeff_cloud */
+    for (int i = nct - 1; i < n_layer; ++i)
+        for (int l = 0; l < n_profile; ++l) {
+            IX2(w->tc, l, i, wp) = 0.0; IX2(w->rc, l, i, wp) = 0.0; IX2(w->t0c, l, i, wp) = 0.0;
+            IX2(w->t0dc, l, i, wp) = 0.0; IX2(w->sc1c, l, i, wp) = 0.0; IX2(w->sc2c, l, i, wp) = 0.0;
+        }
+    const size_t pl = (size_t)wp * w->ndl;
+    for (int t = 1; t <= cld->n_cloud_type; ++t)
+        for (int i = nct - 1; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                if (i < ict) continue;
+                const size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
+                const double fc = cld->frac_cloud[qc + (size_t)ndp * ndc * (size_t)(t - 1)];
+                if (!(fc > 0.0) || !(cld->w_cloud[qc] > 0.0)) continue;
+                /* the type's optical properties (grey_opt_prop.F90:980-1000,
+                 * 1195-1240), normalised and rescaled (1475-1500,
+                 * rescale_phase_fnc.F90) */
+                double kgt = IX2(w->k_grey_tot, l, i, wp), kes = IX2(w->k_ext_scat, l, i, wp);
+                double fwd = IX2(w->forward_scatter_nc, l, i, wp), phf = IX2(w->phase_fnc_nc, l, i, wp);
+                for (int k = 0; k < cld->n_condensed; ++k) {
+                    if (cld->i_cloud_type[k] != t) continue;
+                    kgt = kgt + IX2(w->k_ext_tot_cc + pl * k, l, i, wp);
+                    kes = kes + IX2(w->k_ext_scat_cc + pl * k, l, i, wp);
+                    fwd = fwd + IX2(w->fwd_cc + pl * k, l, i, wp);
+                    phf = phf + IX2(w->phf_cc + pl * k, l, i, wp);
+                }
+                double asym = phf;
+                if (kes > tiny_k) {
+                    const double inv = 1.0 / kes;
+                    if (c->l_rescale) {
+                        fwd = fwd * inv;
+                        asym = phf * inv;
+                        asym = (asym - fwd) / (1.0 - fwd);
+                    } else {
+                        asym = phf / kes;
+                    }
+                }
+                if (!c->l_rescale) fwd = 0.0;
+                double tau, tau_dir, om;
+                single_scatter_cell(c, kgt, kes, IX2(w->k_gas_abs, l, i, wp), IX2(mass, l, i, ndp), fwd,
+                                    &tau, &tau_dir, &om);
+                coeffs o;
+                two_coeff_cell(c->isolir, c->i_2stream, c->i_direct_tau, c->l_ir_source_quad, asym, om, tau_dir, tau,
+                               w->sec_0[l], &o);
+                IX2(w->tc, l, i, wp) = IX2(w->tc, l, i, wp) + fc * o.trans;
+                IX2(w->rc, l, i, wp) = IX2(w->rc, l, i, wp) + fc * o.reflect;
+                IX2(w->sc1c, l, i, wp) = IX2(w->sc1c, l, i, wp) + fc * o.sc1;
+                if (solar || c->l_ir_source_quad) IX2(w->sc2c, l, i, wp) = IX2(w->sc2c, l, i, wp) + fc * o.sc2;
+                if (solar) {
+                    IX2(w->t0c, l, i, wp) = IX2(w->t0c, l, i, wp) + fc * o.trans_0;
+                    if (l_dir) IX2(w->t0dc, l, i, wp) = IX2(w->t0dc, l, i, wp) + fc * o.trans_0_dir;
+                }
+            }
+    /* sources */
+    double *fd = w->flux_direct;
+    if (!solar) {
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                const double d1 = IX2(w->planck_diff, l, i, wp), d2 = IX2(w->planck_diff_2, l, i, wp);
+                double su, sd, suc = 0.0, sdc = 0.0;
+                if (c->l_ir_source_quad) {
+                    su = IX2(w->sc1, l, i, wp) * d1 + IX2(w->sc2, l, i, wp) * d2;
+                    sd = -IX2(w->sc1, l, i, wp) * d1 + IX2(w->sc2, l, i, wp) * d2;
+                    suc = IX2(w->sc1c, l, i, wp) * d1 + IX2(w->sc2c, l, i, wp) * d2;
+                    sdc = -IX2(w->sc1c, l, i, wp) * d1 + IX2(w->sc2c, l, i, wp) * d2;
+                } else {
+                    su = IX2(w->sc1, l, i, wp) * d1;
+                    sd = -su;
+                    suc = IX2(w->sc1c, l, i, wp) * d1;
+                    sdc = -suc;
+                }
+                if (i >= nct - 1) {
+                    const double wc = cloud_w(cld, ndp, ict, l, i + 1), wf = 1.0 - wc;
+                    su = wf * su; sd = wf * sd;
+                    suc = wc * suc; sdc = wc * sdc;
+                }
+                IX2(w->s_up, l, i, wp) = su; IX2(w->s_down, l, i, wp) = sd;
+                IX2(w->s_up_c, l, i, wp) = suc; IX2(w->s_down_c, l, i, wp) = sdc;
+            }
+    } else {
+        /* mixed_solar_source (mixed_solar_source.F90:95-250) */
+        const double *adj = w->adj;
+        for (int l = 0; l < n_profile; ++l) {
+            IX2(fd, l, 0, wp) = w->flux_inc_direct[l];
+            if (l_dir) IX2(w->flux_direct_dir, l, 0, wp) = w->flux_inc_direct[l];
+        }
+        for (int i = 1; i <= nct - 1; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                const int ii = i - 1;
+                const double f0 = IX2(fd, l, i - 1, wp), t0 = IX2(w->trans_0, l, ii, wp);
+                if (adj) {
+                    IX2(fd, l, i, wp) = f0 * t0 * IX2(adj, l, ii, wp);
+                    IX2(w->s_up, l, ii, wp) = IX2(w->sc1, l, ii, wp) * f0;
+                    IX2(w->s_down, l, ii, wp) = (IX2(w->sc2, l, ii, wp) - t0) * f0 + IX2(fd, l, i, wp);
+                } else {
+                    IX2(fd, l, i, wp) = f0 * t0;
+                    IX2(w->s_up, l, ii, wp) = IX2(w->sc1, l, ii, wp) * f0;
+                    IX2(w->s_down, l, ii, wp) = IX2(w->sc2, l, ii, wp) * f0;
+                }
+                if (l_dir) {
+                    double v = IX2(w->flux_direct_dir, l, i - 1, wp) * IX2(w->trans_0_dir, l, ii, wp);
+                    if (adj) v = v * IX2(adj, l, ii, wp);
+                    IX2(w->flux_direct_dir, l, i, wp) = v;
+                }
+            }
+        for (int l = 0; l < n_profile; ++l) {
+            double bf = IX2(fd, l, nct - 1, wp), bc = 0.0;
+            for (int i = nct; i <= n_layer; ++i) {
+                const int ii = i - 1;
+                const double tc_ = OV(l, i - 1, 3) * bc + OV(l, i - 1, 2) * bf;
+                const double tf_ = OV(l, i - 1, 0) * bf + OV(l, i - 1, 1) * bc;
+                const double t0f = IX2(w->trans_0, l, ii, wp), t0c = IX2(w->t0c, l, ii, wp);
+                if (adj) {
+                    const double a = IX2(adj, l, ii, wp);
+                    bf = tf_ * t0f * a;
+                    bc = tc_ * t0c * a;
+                    IX2(w->s_up, l, ii, wp) = IX2(w->sc1, l, ii, wp) * tf_;
+                    IX2(w->s_down, l, ii, wp) = (IX2(w->sc2, l, ii, wp) - t0f) * tf_ + bf;
+                    IX2(w->s_up_c, l, ii, wp) = IX2(w->sc1c, l, ii, wp) * tc_;
+                    IX2(w->s_down_c, l, ii, wp) = (IX2(w->sc2c, l, ii, wp) - t0c) * tc_ + bc;
+                } else {
+                    bf = tf_ * t0f;
+                    bc = tc_ * t0c;
+                    IX2(w->s_up, l, ii, wp) = IX2(w->sc1, l, ii, wp) * tf_;
+                    IX2(w->s_down, l, ii, wp) = IX2(w->sc2, l, ii, wp) * tf_;
+                    IX2(w->s_up_c, l, ii, wp) = IX2(w->sc1c, l, ii, wp) * tc_;
+                    IX2(w->s_down_c, l, ii, wp) = IX2(w->sc2c, l, ii, wp) * tc_;
+                }
+                IX2(fd, l, i, wp) = bf + bc;
+            }
+            w->alpha[l] = bc;          /* the direct flux reaching the ground under cloud */
+            if (l_dir) {
+                double df = IX2(w->flux_direct_dir, l, nct - 1, wp), dc = 0.0;
+                for (int i = nct; i <= n_layer; ++i) {
+                    const int ii = i - 1;
+                    const double tc_ = OV(l, i - 1, 3) * dc + OV(l, i - 1, 2) * df;
+                    const double tf_ = OV(l, i - 1, 0) * df + OV(l, i - 1, 1) * dc;
+                    const double a = adj ? IX2(adj, l, ii, wp) : 1.0;
+                    df = adj ? tf_ * IX2(w->trans_0_dir, l, ii, wp) * a : tf_ * IX2(w->trans_0_dir, l, ii, wp);
+                    dc = adj ? tc_ * IX2(w->t0dc, l, ii, wp) * a : tc_ * IX2(w->t0dc, l, ii, wp);
+                    IX2(w->flux_direct_dir, l, i, wp) = df + dc;
+                }
+                for (int i = 0; i <= n_layer; ++i) IX2(fd, l, i, wp) = IX2(w->flux_direct_dir, l, i, wp);
+                w->alpha[l] = dc;
+            }
+        }
+    }
+    /* ground sources (mix_column.F90:365-385) */
+    for (int l = 0; l < n_profile; ++l) {
+        if (solar) {
+            const double fdc = w->alpha[l];
+            w->source_ground[l] = (w->alb_dir[l] - w->alb_diff[l]) * (IX2(fd, l, n_layer, wp) - fdc);
+            w->s_up_prime[l] = (w->alb_dir[l] - w->alb_diff[l]) * fdc;
+        } else {
+            w->source_ground[l] = OV(l, n_layer, 4) * (1.0 - w->alb_diff[l]) * w->d_planck_flux_surface[l];
+            w->s_up_prime[l] = OV(l, n_layer, 6) * (1.0 - w->alb_diff[l]) * w->d_planck_flux_surface[l];
+        }
+    }
+    /* solver_mix_direct.F90:88-300 or solver_mix_direct_hogan.F90:78-260,
+     * with v11 = ovl 0, v21 = ovl 2, v12 = ovl 1, v22 = ovl 3, u11 = ovl 4,
+     * u12 = ovl 5, u21 = ovl 6, u22 = ovl 7 */
+    const int hogan = (c->i_solver == SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN);
+    double *ft = w->flux_total;
+    for (int l = 0; l < n_profile; ++l) {
+        double a11 = 0.0, a12 = 0.0, a21 = 0.0, a22 = 0.0, g1 = 0.0, g2 = 0.0;
+        for (int i = n_layer + 1; i >= 1; --i) {
+            const int ii = i - 1;
+            if (i < n_layer + 1 && i >= nct) {
+                const double r = IX2(w->reflect, l, ii, wp), t = IX2(w->trans, l, ii, wp);
+                const double rcl = IX2(w->rc, l, ii, wp), tcl = IX2(w->tc, l, ii, wp);
+                const double sd = IX2(w->s_down, l, ii, wp), su = IX2(w->s_up, l, ii, wp);
+                const double sdc = IX2(w->s_down_c, l, ii, wp), suc = IX2(w->s_up_c, l, ii, wp);
+                const double v11 = OV(l, i, 0), v21 = OV(l, i, 2), v12 = OV(l, i, 1), v22 = OV(l, i, 3);
+                const double u11 = OV(l, i - 1, 4), u12 = OV(l, i - 1, 5), u21 = OV(l, i - 1, 6), u22 = OV(l, i - 1, 7);
+                if (!hogan) {
+                    const double th11 = a11 * v11 + a12 * v21, th12 = a11 * v12 + a12 * v22;
+                    const double th21 = a21 * v11 + a22 * v21, th22 = a21 * v12 + a22 * v22;
+                    const double b21 = -th21 * r;
+                    const double b22 = 1.0 / (1.0 - th22 * rcl);
+                    const double gm21 = th21 * t, gm22 = th22 * tcl;
+                    const double hh2 = g2 + th21 * sd + th22 * sdc;
+                    double lam = th12 * rcl * b22;
+                    const double b11 = 1.0 / (1.0 - th11 * r + lam * b21);
+                    const double gm11 = th11 * t + lam * gm21, gm12 = th12 * tcl + lam * gm22;
+                    const double hh1 = g1 + th11 * sd + th12 * sdc + lam * hh2;
+                    IX2(w->b21, l, ii, wp) = b21; IX2(w->b22, l, ii, wp) = b22; IX2(w->b11, l, ii, wp) = b11;
+                    IX2(w->g11, l, ii, wp) = gm11; IX2(w->g12, l, ii, wp) = gm12;
+                    IX2(w->g21, l, ii, wp) = gm21; IX2(w->g22, l, ii, wp) = gm22;
+                    IX2(w->h1, l, ii, wp) = hh1; IX2(w->h2, l, ii, wp) = hh2;
+                    lam = u22 * tcl * b22;
+                    double lamb = (u21 * t + lam * b21) * b11;
+                    a21 = u21 * r + lam * gm21 + lamb * gm11;
+                    a22 = u22 * rcl + lam * gm22 + lamb * gm12;
+                    const double ng2 = u21 * su + u22 * suc + lam * hh2 + lamb * hh1;
+                    lam = u12 * tcl * b22;
+                    lamb = (u11 * t + lam * b21) * b11;
+                    a11 = u11 * r + lam * gm21 + lamb * gm11;
+                    a12 = u12 * rcl + lam * gm22 + lamb * gm12;
+                    g1 = u11 * su + u12 * suc + lam * hh2 + lamb * hh1;
+                    g2 = ng2;
+                } else {
+                    const double th11 = a11 * v11 + a22 * v21, th22 = a11 * v12 + a22 * v22;
+                    const double b11 = 1.0 / (1.0 - th11 * r), gm11 = th11 * t, hh1 = g1 + th11 * sd;
+                    const double b22 = 1.0 / (1.0 - th22 * rcl), gm22 = th22 * tcl, hh2 = g2 + th22 * sdc;
+                    const double l1 = su + hh1 * t * b11, l2 = suc + hh2 * tcl * b22;
+                    IX2(w->b11, l, ii, wp) = b11; IX2(w->g11, l, ii, wp) = gm11; IX2(w->h1, l, ii, wp) = hh1;
+                    IX2(w->b22, l, ii, wp) = b22; IX2(w->g22, l, ii, wp) = gm22; IX2(w->h2, l, ii, wp) = hh2;
+                    a11 = r + th11 * t * t * b11;
+                    g1 = u11 * l1 + u12 * l2;
+                    a22 = rcl + th22 * tcl * tcl * b22;
+                    g2 = u21 * l1 + u22 * l2;
+                }
+            } else if (i < nct - 1) {
+                const double r = IX2(w->reflect, l, ii, wp), t = IX2(w->trans, l, ii, wp);
+                const double b11 = 1.0 / (1.0 - a11 * r), gm11 = a11 * t;
+                const double hh1 = g1 + a11 * IX2(w->s_down, l, ii, wp);
+                IX2(w->b11, l, ii, wp) = b11; IX2(w->g11, l, ii, wp) = gm11; IX2(w->h1, l, ii, wp) = hh1;
+                const double lam = t * b11;
+                a11 = r + lam * gm11;
+                g1 = IX2(w->s_up, l, ii, wp) + lam * hh1;
+            } else if (i == nct - 1) {
+                const double r = IX2(w->reflect, l, ii, wp), t = IX2(w->trans, l, ii, wp);
+                const double th11 = (nct < n_layer) ? (hogan ? a11 * OV(l, i, 0) + a22 * OV(l, i, 2)
+                                                             : a11 * OV(l, i, 0) + a12 * OV(l, i, 2))
+                                                    : a11;
+                const double b11 = 1.0 / (1.0 - th11 * r), gm11 = th11 * t;
+                const double hh1 = g1 + th11 * IX2(w->s_down, l, ii, wp);
+                IX2(w->b11, l, ii, wp) = b11; IX2(w->g11, l, ii, wp) = gm11; IX2(w->h1, l, ii, wp) = hh1;
+                const double lam = t * b11;
+                a11 = r + lam * gm11;
+                g1 = IX2(w->s_up, l, ii, wp) + lam * hh1;
+            } else if (i == n_layer + 1) {
+                a11 = w->alb_diff[l];
+                a22 = w->alb_diff[l];
+                a21 = 0.0;
+                a12 = 0.0;
+                g1 = w->source_ground[l];
+                g2 = w->s_up_prime[l];
+            }
+        }
+        IX2(ft, l, 1, wp) = w->flux_inc_down[l];
+        if (nct > 1) IX2(ft, l, 0, wp) = a11 * IX2(ft, l, 1, wp) + g1;
+        else IX2(ft, l, 0, wp) = g1 + w->flux_inc_down[l] * (OV(l, 0, 0) * a11 + OV(l, 0, 2) * (hogan ? a22 : a12));
+        for (int i = 1; i <= nct - 1; ++i) {
+            const int ii = i - 1;
+            IX2(ft, l, 2 * i, wp) = (IX2(w->g11, l, ii, wp) * IX2(ft, l, 2 * i - 1, wp) + IX2(w->h1, l, ii, wp))
+                * IX2(w->b11, l, ii, wp);
+            IX2(ft, l, 2 * i + 1, wp) = IX2(w->trans, l, ii, wp) * IX2(ft, l, 2 * i - 1, wp)
+                + IX2(w->reflect, l, ii, wp) * IX2(ft, l, 2 * i, wp) + IX2(w->s_down, l, ii, wp);
+        }
+        double fd1 = 0.0, fd2 = 0.0;
+        for (int i = nct; i <= n_layer; ++i) {
+            const int ii = i - 1;
+            if (i > nct) {
+                const double d1 = fd1, d2 = fd2;
+                fd1 = OV(l, i - 1, 0) * d1 + OV(l, i - 1, 1) * d2;
+                fd2 = OV(l, i - 1, 2) * d1 + OV(l, i - 1, 3) * d2;
+            } else {
+                fd1 = OV(l, i - 1, 0) * IX2(ft, l, 2 * i - 1, wp);
+                fd2 = OV(l, i - 1, 2) * IX2(ft, l, 2 * i - 1, wp);
+            }
+            double fu1, fu2;
+            if (!hogan) {
+                fu1 = (IX2(w->g11, l, ii, wp) * fd1 + IX2(w->g12, l, ii, wp) * fd2 + IX2(w->h1, l, ii, wp))
+                    * IX2(w->b11, l, ii, wp);
+                fu2 = (IX2(w->g21, l, ii, wp) * fd1 + IX2(w->g22, l, ii, wp) * fd2 - IX2(w->b21, l, ii, wp) * fu1
+                       + IX2(w->h2, l, ii, wp)) * IX2(w->b22, l, ii, wp);
+            } else {
+                fu1 = (IX2(w->g11, l, ii, wp) * fd1 + IX2(w->h1, l, ii, wp)) * IX2(w->b11, l, ii, wp);
+                fu2 = (IX2(w->g22, l, ii, wp) * fd2 + IX2(w->h2, l, ii, wp)) * IX2(w->b22, l, ii, wp);
+            }
+            fd1 = IX2(w->trans, l, ii, wp) * fd1 + IX2(w->reflect, l, ii, wp) * fu1 + IX2(w->s_down, l, ii, wp);
+            fd2 = IX2(w->tc, l, ii, wp) * fd2 + IX2(w->rc, l, ii, wp) * fu2 + IX2(w->s_down_c, l, ii, wp);
+            IX2(ft, l, 2 * i, wp) = fu1 + fu2;
+            IX2(ft, l, 2 * i + 1, wp) = fd1 + fd2;
+        }
+    }
+#undef OV
+}
+
+/* --------------------------------------------------------------------- */
 static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
                          const socgpu_atm *atm, const socgpu_dimen *dm, const socgpu_cld *cld,
                          char *msg, size_t msg_len)
@@ -1257,17 +1642,31 @@ static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
     if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
         if (two_coeff_basic(c->i_2stream, 0.5, 0.5, &s, &t) != SOCGPU_I_NORMAL) {
             set_msg(msg, msg_len, "unrecognised or unimplemented two-stream scheme"); return SOCGPU_I_ERR_FATAL; }
-        if (c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
+        const int region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM);
+        if (!region && c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
             set_msg(msg, msg_len, "scattering requires solver_homogen_direct"); return SOCGPU_I_ERR_FATAL; }
+        if (region && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN) {
+            set_msg(msg, msg_len, "cloud regions require solver_mix_direct or solver_mix_direct_hogan");
+            return SOCGPU_I_ERR_FATAL; }
     } else if (c->i_scatter_method == SOCGPU_IP_NO_SCATTER_ABS || c->i_scatter_method == SOCGPU_IP_NO_SCATTER_EXT) {
         if (c->i_solver != SOCGPU_IP_SOLVER_NO_SCAT) {
             set_msg(msg, msg_len, "no-scattering methods require solver_no_scat"); return SOCGPU_I_ERR_FATAL; }
     } else {
         set_msg(msg, msg_len, "unsupported scattering method"); return SOCGPU_I_ERR_FATAL; }
-    if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA) {
-        set_msg(msg, msg_len, "only clear-sky and McICA cloud schemes are supported"); return SOCGPU_I_ERR_FATAL; }
-    if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA && !cld) {
-        set_msg(msg, msg_len, "McICA requires cloud fields"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA &&
+        c->i_cloud != SOCGPU_IP_CLOUD_MIX_MAX && c->i_cloud != SOCGPU_IP_CLOUD_MIX_RANDOM) {
+        set_msg(msg, msg_len, "only clear-sky, McICA and two-region cloud schemes are supported"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR &&
+        (!cld || cld->n_condensed < 1 || !cld->type_condensed || !cld->i_cloud_type || !cld->i_condensed_param ||
+         !cld->i_condensed_type || !cld->condensed_mix_ratio || !cld->condensed_dim_char || !cld->w_cloud ||
+         !cld->frac_cloud || cld->n_cloud_type < 1 || cld->n_cloud_type > 2)) {
+        set_msg(msg, msg_len, "clouds require cloud fields"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA &&
+        (!cld->c_sub || !cld->frac_cloudy || !cld->subcol_k || !cld->first_subcol_k || !cld->subcol_reorder)) {
+        set_msg(msg, msg_len, "McICA requires the subcolumn fields"); return SOCGPU_I_ERR_FATAL; }
+    if ((c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM) &&
+        c->i_scatter_method != SOCGPU_IP_SCATTER_FULL) {
+        set_msg(msg, msg_len, "cloud regions require full scattering"); return SOCGPU_I_ERR_FATAL; }
     if (c->first_band < 1 || c->last_band > d->n_band || c->first_band > c->last_band) {
         set_msg(msg, msg_len, "band range outside the spectrum"); return SOCGPU_I_ERR_RANGE; }
     if (atm->n_profile < 0 || atm->n_profile > dm->nd_profile || atm->n_layer < 1 || atm->n_layer > dm->nd_layer) {
@@ -1296,6 +1695,7 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
     if (np <= 0) return SOCGPU_I_NORMAL;
     int ndp = dm->nd_profile, ndl = dm->nd_layer, n_layer = atm0->n_layer;
     int l_cloud = (c->i_cloud == SOCGPU_IP_CLOUD_MCICA);
+    int l_region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM);
     int ict = dm->id_cloud_top - 1;
 
     /* views shifted to the first profile of the segment */
@@ -1312,10 +1712,12 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
         }
     }
     socgpu_cld cldv, *cld = NULL;
-    if (cld0 && l_cloud) {
+    if (cld0 && (l_cloud || l_region)) {
         cldv = *cld0; cld = &cldv;
         cldv.condensed_mix_ratio += p0; cldv.condensed_dim_char += p0;
-        cldv.w_cloud += p0; cldv.frac_cloud += p0; cldv.c_sub += p0; cldv.frac_cloudy += p0;
+        cldv.w_cloud += p0; cldv.frac_cloud += p0;
+        if (cldv.c_sub) cldv.c_sub += p0;
+        if (cldv.frac_cloudy) cldv.frac_cloudy += p0;
         if (cldv.n_subcol_cld) cldv.n_subcol_cld += p0;
     }
     socgpu_radout out = *out0;
@@ -1335,6 +1737,11 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
     lookup_fac lf;
     lookup_fac_init(&lf, c, d, &atm, np, n_layer, ndp, wp, ndl);
     double *kterm = zalloc((size_t)wp * ndl), *k_eqv = zalloc((size_t)wp * ndl), *adj = zalloc((size_t)wp * ndl);
+    if (l_region) {
+        /* set_cloud_geometry and overlap_coupled (radiance_calc.F90:640-700) */
+        w.nct = cloud_top(cld, ndp, ict, np, n_layer);
+        overlap_coupled2(&w, cld, ndp, ict, c->i_cloud);
+    }
 
     /* zero the outputs (augment_radiance's l_initial branch is equivalent) */
     for (int i = 0; i <= n_layer; ++i)
@@ -1355,7 +1762,7 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
 
     for (int b = c->first_band - 1; b < c->last_band && status == SOCGPU_I_NORMAL; ++b) {
         double weight_band = c->weight_band ? c->weight_band[b] : 1.0;
-        status = grey_opt_prop(&w, c, dm, d, &atm, aer, cld, b, l_cloud);
+        status = grey_opt_prop(&w, c, dm, d, &atm, aer, cld, b, l_cloud || l_region);
         if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "unsupported optical property option"); break; }
 
         /* gas scaling of each absorber (radiance_calc.F90:1330-1470) */
@@ -1471,6 +1878,8 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
             if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "illegal type of scaling"); break; }
             if (l_cloud) {
                 solve_mcica_term(&w, c, dm, d, atm.mass, cld, b, n_abs > 0 ? iex_of[0] : 0);
+            } else if (l_region) {
+                solve_region_term(&w, c, dm, atm.mass, cld);
             } else {
                 clear_coefficients(&w, c, atm.mass, ndp);
                 column_solve(&w, c, c->i_scatter_method != SOCGPU_IP_SCATTER_FULL);

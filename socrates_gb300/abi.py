@@ -20,6 +20,9 @@ IP_SCATTER_FULL, IP_NO_SCATTER_ABS, IP_NO_SCATTER_EXT = 1, 2, 3
 IP_DIRECT_NOSCALING, IP_DIRECT_DELTA_SCALING, IP_DIRECT_CSR_SCALING = 0, 1, 2
 IP_SOLVER_NO_SCAT, IP_SOLVER_HOMOGEN_DIRECT = 2, 13
 IP_CLOUD_CLEAR, IP_CLOUD_MCICA = 5, 10
+IP_CLOUD_MIX_MAX, IP_CLOUD_MIX_RANDOM = 2, 4
+IP_SOLVER_MIX_DIRECT, IP_SOLVER_MIX_DIRECT_HOGAN = 11, 16
+IP_CLOUD_HOMOGEN = 1
 IP_CLOUD_ICE_WATER = 2
 IP_CLOUD_TYPE_WATER, IP_CLOUD_TYPE_ICE = 1, 2
 IP_PHASE_WATER, IP_PHASE_ICE = 1, 2

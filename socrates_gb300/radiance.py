@@ -328,7 +328,8 @@ class Marshal:
             self.aer.mode_scattering = _dp(ae["mode_scattering"], k)
             self.aer.mode_asymmetry = _dp(ae["mode_asymmetry"], k)
         self.cld = abi.Cld()
-        if mcica is not None:
+        region = control.i_cloud in (abi.IP_CLOUD_MIX_MAX, abi.IP_CLOUD_MIX_RANDOM)
+        if mcica is not None or (region and col.cld):
             cd = col.cld
             ict = id_cloud_top - 1
             cl = self.cld
@@ -344,13 +345,14 @@ class Marshal:
             cl.n_cloud_type = int(cd.get("n_cloud_type", 2))
             cl.w_cloud = _dp(cd["w_cloud"][:, ict:], k)
             cl.frac_cloud = _dp(cd["frac_cloud"][:, ict:, :], k)
-            cl.n_subcol_gen, cl.n_subcol_req = mcica.n_subcol_gen, mcica.n_subcol_req
-            cl.c_sub = _dp(mcica.c_sub, k)
-            cl.frac_cloudy = _dp(mcica.frac_cloudy, k)
-            cl.n_subcol_cld = _ip(mcica.n_subcol_cld, k)
-            cl.subcol_k = _ip(mcica.subcol_k, k)
-            cl.first_subcol_k = _ip(mcica.first_subcol_k, k)
-            cl.subcol_reorder = _ip(mcica.subcol_reorder, k)
+            if mcica is not None:
+                cl.n_subcol_gen, cl.n_subcol_req = mcica.n_subcol_gen, mcica.n_subcol_req
+                cl.c_sub = _dp(mcica.c_sub, k)
+                cl.frac_cloudy = _dp(mcica.frac_cloudy, k)
+                cl.n_subcol_cld = _ip(mcica.n_subcol_cld, k)
+                cl.subcol_k = _ip(mcica.subcol_k, k)
+                cl.first_subcol_k = _ip(mcica.first_subcol_k, k)
+                cl.subcol_reorder = _ip(mcica.subcol_reorder, k)
         f = lambda *s: np.zeros(s, order="F")
         self.flux_up, self.flux_down = f(n, L + 1), f(n, L + 1)
         self.flux_direct = f(n, L + 1) if control.isolir == abi.IP_SOLAR else None

@@ -204,7 +204,7 @@ def test_cloud_gen_compaction_and_fraction():
 
 
 # ---------------------------------------------------------------------------
-KGO_FIXTURES = ("icrccm", "circ6", "ga7", "runes", "mcica5118")
+KGO_FIXTURES = ("icrccm", "circ6", "ga7", "runes", "mcica5118", "cld7460")
 
 
 @pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(KGO_FIXTURES)))
@@ -266,6 +266,28 @@ def test_oracle_reproduces_mcica5118_known_good_output(run):
     half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
     err = np.abs(hr - kgo) / half_unit
     assert err.max() <= 1.05, f"layer {err.argmax()}: {hr[err.argmax()]} vs {kgo[err.argmax()]}"
+
+
+@pytest.mark.parametrize("run", ["lw_avg", "sw_avg", "sw_ds0_avg", "sw2", "sw2_ds0", "sw_ga9_avg", "lw_ga9_avg",
+                                 "ipa_lw", "ipa_sw"])
+def test_oracle_reproduces_cloud_region_known_good_output(run):
+    """Pin the two-region cloud solvers against the reference's known-good
+    outputs (examples/netcdf/7460_28/run_me, ref_*.hrts and ref_*.nflx):
+    167 layers of cloud-resolving-model data with water and ice as one
+    homogeneous type in a clear and a cloudy region of maximum-random overlap
+    (-C 2), solved by solver_mix_direct (-v 11, HadGEM1 files, random gas
+    overlap, one or two surface albedos, direct beam with and without
+    delta-scaling) or by Hogan's form (the default -v 16, GA9 files, k_eqv_scl),
+    as one averaged column and as 20 columns (ipa0/).  Every printed value
+    must agree to half a unit of its 6th significant digit, up to 5 % of that
+    half unit for values on a rounding boundary."""
+    import cld7460 as K
+    ctl, sp, col, kgo, kind = K.setup(run, K.spectra())
+    got = K.printed(O.radiance_calc(ctl, sp, col), col, kind)
+    got = got[0] if kgo.ndim == 1 else got.T
+    err = K.half_units(got, kgo)
+    i = np.unravel_index(err.argmax(), err.shape)
+    assert err.max() <= 1.05, f"{run} at {i}: {got[i]} vs {kgo[i]}"
 
 
 @pytest.mark.parametrize("section", ["sw", "lw_tground", "lw_flux_ground", "lw_tiles"])
