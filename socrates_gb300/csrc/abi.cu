@@ -582,16 +582,20 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
         return SOCGPU_I_ERR_FATAL;
       }
   }
+  const bool region = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
   if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
-    if (c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
+    if (!region && c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
       set_msg(msg, msg_len, "scattering requires solver_homogen_direct"); return SOCGPU_I_ERR_FATAL; }
+    if (region && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN) {
+      set_msg(msg, msg_len, "cloud regions require solver_mix_direct or solver_mix_direct_hogan");
+      return SOCGPU_I_ERR_FATAL; }
   } else if (c->i_scatter_method == SOCGPU_IP_NO_SCATTER_ABS || c->i_scatter_method == SOCGPU_IP_NO_SCATTER_EXT) {
     if (c->i_solver != SOCGPU_IP_SOLVER_NO_SCAT) {
       set_msg(msg, msg_len, "no-scattering methods require solver_no_scat"); return SOCGPU_I_ERR_FATAL; }
     if (c->isolir == SOCGPU_IP_SOLAR) {
       set_msg(msg, msg_len, "the solar path requires scattering"); return SOCGPU_I_ERR_FATAL; }
-    if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA) {
-      set_msg(msg, msg_len, "McICA requires full scattering on the device path"); return SOCGPU_I_ERR_FATAL; }
+    if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA || region) {
+      set_msg(msg, msg_len, "clouds require full scattering on the device path"); return SOCGPU_I_ERR_FATAL; }
   } else {
     set_msg(msg, msg_len, "unsupported scattering method %d", c->i_scatter_method); return SOCGPU_I_ERR_FATAL; }
   if (c->isolir == SOCGPU_IP_SOLAR && c->i_direct_tau != SOCGPU_IP_DIRECT_DELTA_SCALING) {
@@ -600,8 +604,9 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
   }
   if (c->l_rescale && c->n_order_forward < 1) {
     set_msg(msg, msg_len, "n_order_forward must be positive"); return SOCGPU_I_ERR_FATAL; }
-  if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA) {
-    set_msg(msg, msg_len, "only clear-sky and McICA cloud schemes are supported"); return SOCGPU_I_ERR_FATAL; }
+  if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA && !region) {
+    set_msg(msg, msg_len, "only clear-sky, McICA and two-region cloud schemes are supported");
+    return SOCGPU_I_ERR_FATAL; }
   if (c->precision != SOCGPU_PRECISION_FP64 && c->precision != SOCGPU_PRECISION_MIXED) {
     set_msg(msg, msg_len, "unknown precision %d", c->precision); return SOCGPU_I_ERR_FATAL; }
   if (c->first_band < 1 || c->last_band > sp->dev.n_band || c->first_band > c->last_band) {
@@ -642,14 +647,18 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     if (!aer->mode_mix_ratio || !aer->mode_absorption || !aer->mode_scattering || !aer->mode_asymmetry) {
       set_msg(msg, msg_len, "missing aerosol mode fields"); return SOCGPU_I_ERR_FATAL; }
   }
-  if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA) {
-    if (!cld) { set_msg(msg, msg_len, "McICA requires cloud fields"); return SOCGPU_I_ERR_FATAL; }
+  if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA || region) {
+    if (!cld || !cld->type_condensed || !cld->i_cloud_type || !cld->i_condensed_param || !cld->i_condensed_type ||
+        !cld->condensed_mix_ratio || !cld->condensed_dim_char || !cld->w_cloud || !cld->frac_cloud) {
+      set_msg(msg, msg_len, "clouds require cloud fields"); return SOCGPU_I_ERR_FATAL; }
     if (cld->n_condensed < 1 || cld->n_condensed > kMaxCloudComp || cld->n_cloud_type < 1 || cld->n_cloud_type > 2) {
       set_msg(msg, msg_len, "cloud components/types outside the supported range"); return SOCGPU_I_ERR_RANGE; }
     if (dm->id_cloud_top < 1 || dm->id_cloud_top > atm->n_layer) {
       set_msg(msg, msg_len, "id_cloud_top outside the column"); return SOCGPU_I_ERR_RANGE; }
-    if (cld->n_subcol_gen < 1 || cld->n_subcol_gen > SOCGPU_MAX_SUBCOL || cld->n_subcol_req < 1) {
+    if (!region && (cld->n_subcol_gen < 1 || cld->n_subcol_gen > SOCGPU_MAX_SUBCOL || cld->n_subcol_req < 1)) {
       set_msg(msg, msg_len, "subcolumn counts outside 1..%d", SOCGPU_MAX_SUBCOL); return SOCGPU_I_ERR_RANGE; }
+    if (!region && (!cld->c_sub || !cld->frac_cloudy || !cld->subcol_k || !cld->first_subcol_k || !cld->subcol_reorder)) {
+      set_msg(msg, msg_len, "McICA requires the subcolumn fields"); return SOCGPU_I_ERR_FATAL; }
     for (int k = 0; k < cld->n_condensed; ++k) {
       int ph = cld->type_condensed[k], parm = cld->i_condensed_param[k], ty = cld->i_condensed_type[k];
       if (ph == SOCGPU_IP_PHASE_WATER) {
@@ -698,7 +707,10 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
   p.l_ir_source_quad = c->l_ir_source_quad; p.l_rayleigh = c->l_rayleigh; p.l_gas = c->l_gas;
   p.l_aerosol_mode = c->l_aerosol_mode && aer && aer->n_mode > 0; p.l_flux_div = c->l_flux_div;
   p.first_band = c->first_band; p.last_band = c->last_band;
-  p.mcica = c->i_cloud == SOCGPU_IP_CLOUD_MCICA;
+  p.region = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
+  p.mcica = c->i_cloud == SOCGPU_IP_CLOUD_MCICA || p.region;
+  p.solver_hogan = c->i_solver == SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN;
+  p.mix_max = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX;
   p.l_continuum = c->l_continuum && sp->dev.has_continuum;
   p.l_mixing_ratio = c->l_mixing_ratio;
   p.i_water = sp->dev.index_water - 1;
@@ -763,7 +775,9 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
     p.w_cloud = cld->w_cloud; p.frac_cloud = cld->frac_cloud; p.c_sub = cld->c_sub;
     p.frac_cloudy = cld->frac_cloudy; p.n_subcol_cld = cld->n_subcol_cld;
     p.subcol_k = cld->subcol_k; p.first_subcol_k = cld->first_subcol_k; p.subcol_reorder = cld->subcol_reorder;
-    p.n_subcol_gen = cld->n_subcol_gen; p.n_subcol_req = cld->n_subcol_req; p.nd_band_sp = sp->dev.nd_band;
+    p.n_subcol_gen = p.region ? 0 : cld->n_subcol_gen;
+    p.n_subcol_req = p.region ? 0 : cld->n_subcol_req;
+    p.nd_band_sp = sp->dev.nd_band;
   }
   p.flux_up = out->flux_up; p.flux_down = out->flux_down;
   p.flux_direct = c->isolir == SOCGPU_IP_SOLAR ? out->flux_direct : nullptr;
@@ -771,7 +785,10 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
 }
 
 int mode_index(const socgpu_control *c) {
-  if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA) return 2;
+  // McICA and cloud regions share the kernels that stage cloud optics
+  if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA || c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX ||
+      c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM)
+    return 2;
   return c->i_scatter_method == SOCGPU_IP_SCATTER_FULL ? 1 : 0;
 }
 
@@ -795,7 +812,8 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
   const size_t ndp = dm->nd_profile, ndl = dm->nd_layer, np = a->n_profile, nl = a->n_layer;
   const size_t nb = s->dev.n_band, ns = std::max(1, s->dev.n_species);
   sw = c->isolir == SOCGPU_IP_SOLAR;
-  mc = c->i_cloud == SOCGPU_IP_CLOUD_MCICA;
+  mc = c->i_cloud == SOCGPU_IP_CLOUD_MCICA || c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX ||
+       c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
   aero = c->l_aerosol_mode && ae && ae->n_mode > 0;
   const size_t D = sizeof(double), none = (size_t)-1;
   // inputs: (nd_profile, rows) arrays copied with their valid profiles only;

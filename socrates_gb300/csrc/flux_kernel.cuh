@@ -152,9 +152,22 @@ struct SmemLayout {
   size_t off_phf_nc, off_fwd_nc, off_c_ke, off_c_ks, off_c_ka, off_c_phf, off_c_fwd;
   size_t off_wcld, off_frac, off_csub;
   size_t off_aux, off_lkf, off_lki, off_sbf, off_sbj, off_kscr;
+  size_t off_ovl, off_reg, off_regd, off_nct;
   size_t off_acc;
   size_t bytes;
 };
+
+// Rows of a group's scratch for the two-region solve (cloud regions): the
+// clear (free) and cloudy coefficients of each layer, the elimination
+// coefficients of the solver, the level fluxes and the layer divergence.
+enum RegRow {
+  kRgFT, kRgFR, kRgFT0, kRgFC1, kRgFC2, kRgFOM,
+  kRgCT, kRgCR, kRgCT0, kRgCC1, kRgCC2, kRgCOM,
+  kRgFU, kRgFD, kRgFDIR, kRgDIV, kRegRows
+};
+// The solver's elimination coefficients, kept in FP64 in every build: the
+// serial solve runs on one lane in FP64 from the coefficients of the layers.
+enum RegDRow { kRgB11, kRgB21, kRgB22, kRgG11, kRgG12, kRgG21, kRgG22, kRgH1, kRgH2, kRegDRows };
 
 // The layout of a column of batch p: nb bands staged at a time, n_groups
 // solve groups of P lanes, LP = P*CH layer slots.
@@ -168,6 +181,7 @@ __host__ __device__ inline SmemLayout make_layout(const FluxParams &p, int LP, i
   size_t o = 0;
   auto take = [&](size_t elems) { size_t r = (o + 15) & ~(size_t)15; o = r + elems * sizeof(R); return r; };
   auto take_int = [&](size_t elems) { size_t r = (o + 15) & ~(size_t)15; o = r + elems * sizeof(int); return r; };
+  auto take_dbl = [&](size_t elems) { size_t r = (o + 15) & ~(size_t)15; o = r + elems * sizeof(double); return r; };
   s.off_p = take(LP);
   s.off_t = take(LP);
   s.off_mass = take(LP);
@@ -202,6 +216,13 @@ __host__ __device__ inline SmemLayout make_layout(const FluxParams &p, int LP, i
   s.off_sbj = p.n_sb > 0 ? take_int((size_t)p.n_sb * LP) : o;
   // per-group scratch row for k of per-term scaled absorbers
   s.off_kscr = p.term_scr ? take((size_t)n_groups * LP) : o;
+  // cloud regions: the column's interface coefficients and cloud top, and
+  // each group's rows for the serial two-region solve
+  const bool region = mcica && p.region;
+  s.off_ovl = region ? take((size_t)8 * (LP + 1)) : o;
+  s.off_reg = region ? take((size_t)n_groups * kRegRows * (LP + 1)) : o;
+  s.off_regd = region ? take_dbl((size_t)n_groups * kRegDRows * (LP + 1)) : o;
+  s.off_nct = region ? take_int(4) : o;
   // per-group accumulator slices, offset by P words mod 32 so that the
   // groups of one warp land on different banks
   const int words = (int)(sizeof(R) / 4);
@@ -349,6 +370,9 @@ struct FluxKernel {
     R *phf_nc, *fwd_nc, *c_ke, *c_ks, *c_ka, *c_phf, *c_fwd, *wcld, *frac, *csub;
     R *aux, *lkf, *sbf, *kscr;
     int *lki, *sbj;
+    R *ovl, *reg;
+    double *regd;
+    int *nct;
     Acc *acc;
   };
 
@@ -367,6 +391,8 @@ struct FluxKernel {
     s.lkf = (R *)(smem + l.off_lkf); s.lki = (int *)(smem + l.off_lki);
     s.sbf = (R *)(smem + l.off_sbf); s.sbj = (int *)(smem + l.off_sbj);
     s.kscr = (R *)(smem + l.off_kscr);
+    s.ovl = (R *)(smem + l.off_ovl); s.reg = (R *)(smem + l.off_reg); s.nct = (int *)(smem + l.off_nct);
+    s.regd = (double *)(smem + l.off_regd);
     s.acc = (Acc *)(smem + l.off_acc);
     return s;
   }
@@ -562,6 +588,7 @@ struct FluxKernel {
     }
     for (int q = threadIdx.x; q < n_groups * lay.acc_stride; q += nthreads) S.acc[q] = Acc(0);
     if (MCICA) stage_cloud_column(p, S, col);
+    if (MCICA && p.region) stage_regions(p, S, col, LP);
     const int gid = threadIdx.x / P;
     const int r = threadIdx.x % P;
     const R sec0 = p.zen_0 ? load_in<R>(p.zen_0 + col) : R(1);
@@ -1275,9 +1302,362 @@ struct FluxKernel {
         if (p.keqv) fold_direct(S, bi, max_abs, r, L, T0, c2);
       solve_column(p, T, Rf, T0, c1, c2, om, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
                    alb_diff, alb_dir, dB_surf, w_g, acc, active);
+    } else if (p.region) {
+      solve_region(p, g, bstart, sec0, r, lw, active);
     } else {
       solve_mcica(p, S, col, gp, gt, bd, bi, b, r, L, lw, sec0, dB_b, dB2_b, f_inc_down, f_inc_dir,
                   alb_diff, alb_dir, dB_surf, w_g, acc, max_abs, active);
+    }
+  }
+
+  // set_cloud_geometry and overlap_coupled (set_cloud_geometry.F90:76-96,
+  // overlap_coupled.F90:120-440) for the column, by one thread: the first
+  // cloudy layer (1-based, at most n_layer) and, at each interface i (0: the
+  // top), the fractions of each upper region (clear, cloudy) over each lower
+  // one (ovl rows 2 j + k) and of each lower region under each upper one
+  // (rows 4 + 2 j + k).  The interfaces above the cloud top keep the identity.
+  __device__ static void stage_regions(const FluxParams &p, const Smem &S, int col, int LP_) {
+    if (threadIdx.x != 0) return;
+    const int L = p.n_layer, ndp = p.nd_profile, ict = p.id_ct;
+    auto wc = [&](int i1) -> R {
+      return (i1 - 1 >= ict) ? load_in<R>(p.w_cloud + (size_t)col + (size_t)ndp * (size_t)(i1 - 1 - ict)) : R(0);
+    };
+    int nct = ict + 1;
+    while (nct < L && !(wc(nct) > R(0))) ++nct;
+    S.nct[0] = nct;
+    const R tol = (R)(1.0e+02 * kEps64);
+    for (int i = 0; i < nct - 1; ++i)
+      for (int m = 0; m < 8; ++m) S.ovl[(size_t)m * (LP_ + 1) + i] = (m == 0 || m == 3 || m == 4 || m == 7) ? R(1) : R(0);
+    R au0 = R(1), au1 = R(0);
+    for (int i = nct - 1; i <= L; ++i) {
+      const R corr = p.mix_max ? R(1) : R(0);
+      R al0, al1;
+      if (i < L) { const R w = wc(i + 1); al0 = R(1) - w; al1 = w; }
+      else { al0 = R(1); al1 = R(0); }
+      R a00 = corr * (al0 < au0 ? al0 : au0), a11 = corr * (al1 < au1 ? al1 : au1), a01 = R(0), a10 = R(0);
+      R art = R(1) - a00;
+      art = art - a11;
+      const R ru0 = au0 - a00, ru1 = au1 - a11, rl0 = al0 - a00, rl1 = al1 - a11;
+      if (art > tol) {
+        a00 = a00 + ru0 * rl0 / art; a01 = a01 + ru0 * rl1 / art;
+        a10 = a10 + ru1 * rl0 / art; a11 = a11 + ru1 * rl1 / art;
+      }
+      R v[8] = {R(1), R(0), R(0), R(1), R(1), R(0), R(0), R(1)};
+      if (au0 > tol) { v[0] = a00 / au0; v[2] = a01 / au0; }
+      if (au1 > tol) { v[1] = a10 / au1; v[3] = a11 / au1; }
+      if (al0 > tol) { v[4] = a00 / al0; v[6] = a10 / al0; }
+      if (al1 > tol) { v[5] = a01 / al1; v[7] = a11 / al1; }
+      for (int m = 0; m < 8; ++m) S.ovl[(size_t)m * (LP_ + 1) + i] = v[m];
+      if (i < L) { au0 = al0; au1 = al1; }
+    }
+  }
+
+  // One g-point of a column in a clear and a cloudy region (mix_column.F90:
+  // 150-460).  The lanes of the group compute the clear coefficients and the
+  // frac_cloud-weighted coefficients of the cloud types (two_coeff_cloud.F90)
+  // of their layers, and the infra-red sources; lane 0 then runs the serial
+  // parts from the group's scratch rows: the direct beam through both regions
+  // (mixed_solar_source.F90), solver_mix_direct.F90 or
+  // solver_mix_direct_hogan.F90 and the back-substitution; the lanes add the
+  // level fluxes to the group's accumulators.
+  // Called out of line with scalars only, so that the McICA kernels it
+  // shares keep their registers: the shared-memory view, the g-point and
+  // the group's accumulators are rebuilt here as the column loop builds them.
+  __device__ static __noinline__ void solve_region(const FluxParams &p, int g, int bstart, R sec0, int r, bool lw,
+                                                   bool active) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int n_groups = blockDim.x / P, L = p.n_layer, max_abs = p.max_abs;
+    const SmemLayout lay = make_layout<R>(p, LP, P, p.band_batch, n_groups, MCICA);
+    const Smem S = bind(smem, lay);
+    const GPoint &gp = p.gpoints[g];
+    const int b = gp.band, bi = b - bstart;
+    const BandInfo &bd = p.bands[b];
+    const GasTerm gt = load_gas(gp, bd, max_abs);
+    const R *bs = S.bscal + bi * kBandScal;
+    const R w_g = kFP64 ? (R)(bs[5] * gp.weight) : (R)(bs[5] * gp.weight_f);
+    const R f_inc_down = bs[0], f_inc_dir = bs[1], alb_diff = bs[2], alb_dir = bs[3], dB_surf = bs[4];
+    const R *dB_b = S.dB + (size_t)bi * LP, *dB2_b = S.dB2 + (size_t)bi * LP;
+    const int nc = p.n_condensed;
+    const int gid = threadIdx.x / P;
+    Acc *acc = S.acc + (size_t)gid * lay.acc_stride;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned gm = (P == 32) ? 0xffffffffu : (((1u << P) - 1u) << (lane & ~(unsigned)(P - 1)));
+    const R *kgt_b = S.kgt + (size_t)bi * LP, *kes_b = S.kes + (size_t)bi * LP;
+    const R *kabs_b = S.kabs + (size_t)bi * LP, *asym_b = S.asym + (size_t)bi * LP;
+    const R *fwd_b = S.fwd + (size_t)bi * LP, *amt_b = S.amt + (size_t)bi * max_abs * LP;
+    const R *phf_nc = S.phf_nc + (size_t)bi * LP, *fwd_nc = S.fwd_nc + (size_t)bi * LP;
+    const R *c_ke = S.c_ke + (size_t)bi * nc * LP, *c_ks = S.c_ks + (size_t)bi * nc * LP;
+    const R *c_ka = S.c_ka + (size_t)bi * nc * LP, *c_ph = S.c_phf + (size_t)bi * nc * LP;
+    const R *c_fw = S.c_fwd + (size_t)bi * nc * LP;
+    R *X = S.reg + (size_t)gid * kRegRows * (LP + 1);
+    auto row = [&](int k) { return X + (size_t)k * (LP + 1); };
+    const int nct = S.nct[0];
+
+    R kgv[CH];
+    gas_k_lane(p, S, gt, gp, bd, amt_b, r, L, kgv);
+    R Tf[CH], Rff[CH], T0f[CH], c1f[CH], c2f[CH], omf[CH];
+    R Tc[CH], Rc[CH], T0c[CH], c1c[CH], c2c[CH], omc[CH];
+#pragma unroll
+    for (int j = 0; j < CH; ++j) {
+      const int i = r * CH + j, s = j * P + r;
+      Tc[j] = R(0); Rc[j] = R(0); T0c[j] = R(0); c1c[j] = R(0); c2c[j] = R(0); omc[j] = R(0);
+      if (i < L) {
+        cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kgv[j], S.mass[s], asym_b[s], fwd_b[s], sec0,
+                  Tf[j], Rff[j], T0f[j], c1f[j], c2f[j], omf[j]);
+        if (S.wcld[s] > R(0)) {
+          for (int t = 0; t < p.n_cloud_type; ++t) {
+            const R fc = S.frac[(size_t)t * LP + s];
+            if (!(fc > R(0))) continue;
+            // the type's optical properties (grey_opt_prop.F90:980-1000,
+            // 1195-1240, 1475-1500; rescale_phase_fnc.F90)
+            R kgt = kgt_b[s], kes = kes_b[s], kab = kabs_b[s], fw = fwd_nc[s], ph = phf_nc[s];
+            for (int k = 0; k < nc; ++k) {
+              if (p.comp_type[k] - 1 != t) continue;
+              const size_t qk = (size_t)k * LP + s;
+              kgt = kgt + c_ke[qk]; kes = kes + c_ks[qk]; kab = kab + c_ka[qk];
+              fw = fw + c_fw[qk]; ph = ph + c_ph[qk];
+            }
+            R asym = ph, fwd = R(0);
+            if (kes > (R)kTiny64) {
+              const R inv = R(1) / kes;
+              if (p.l_rescale) {
+                fwd = fw * inv;
+                asym = (ph * inv - fwd) / (R(1) - fwd);
+              } else {
+                asym = ph * inv;
+              }
+            }
+            R tT, tR, tT0, t1, t2, tO;
+            cell_coef(p, kgt, kes, kab, kgv[j], S.mass[s], asym, fwd, sec0, tT, tR, tT0, t1, t2, tO);
+            Tc[j] = Tc[j] + fc * tT; Rc[j] = Rc[j] + fc * tR; T0c[j] = T0c[j] + fc * tT0;
+            c1c[j] = c1c[j] + fc * t1; c2c[j] = c2c[j] + fc * t2; omc[j] = omc[j] + fc * tO;
+          }
+        }
+      } else {
+        Tf[j] = R(1); Rff[j] = R(0); T0f[j] = R(1); c1f[j] = R(0); c2f[j] = R(0); omf[j] = R(0);
+      }
+    }
+    if constexpr (SRC == SOCGPU_IP_SOLAR)
+      if (p.keqv) { fold_direct(S, bi, max_abs, r, L, T0f, c2f); fold_direct(S, bi, max_abs, r, L, T0c, c2c); }
+#pragma unroll
+    for (int j = 0; j < CH; ++j) {
+      const int i = r * CH + j, s = j * P + r;
+      if (i >= L) continue;
+      if (lw) {
+        // ir_source.F90:93-119 in each region, weighted by its area in the
+        // cloudy layers (mix_column.F90:185-230)
+        const R dB = dB_b[s];
+        R su, sd, suc, sdc;
+        if (p.l_ir_source_quad) {
+          su = c1f[j] * dB + c2f[j] * dB2_b[s]; sd = -c1f[j] * dB + c2f[j] * dB2_b[s];
+          suc = c1c[j] * dB + c2c[j] * dB2_b[s]; sdc = -c1c[j] * dB + c2c[j] * dB2_b[s];
+        } else {
+          su = c1f[j] * dB; sd = -su; suc = c1c[j] * dB; sdc = -suc;
+        }
+        if (i + 1 >= nct) {
+          const R wc = S.wcld[s], wf = R(1) - wc;
+          su = wf * su; sd = wf * sd; suc = wc * suc; sdc = wc * sdc;
+        }
+        c1f[j] = su; c2f[j] = sd; c1c[j] = suc; c2c[j] = sdc;
+      }
+      row(kRgFT)[i] = Tf[j]; row(kRgFR)[i] = Rff[j]; row(kRgFT0)[i] = T0f[j];
+      row(kRgFC1)[i] = c1f[j]; row(kRgFC2)[i] = c2f[j]; row(kRgFOM)[i] = omf[j];
+      row(kRgCT)[i] = Tc[j]; row(kRgCR)[i] = Rc[j]; row(kRgCT0)[i] = T0c[j];
+      row(kRgCC1)[i] = c1c[j]; row(kRgCC2)[i] = c2c[j]; row(kRgCOM)[i] = omc[j];
+    }
+    __syncwarp(gm);
+    if (r == 0)
+      region_serial(p, S, X, S.regd + (size_t)gid * kRegDRows * (LP + 1), nct, L, lw, f_inc_down, f_inc_dir,
+                    alb_diff, alb_dir, dB_surf);
+    __syncwarp(gm);
+    // accumulate the level fluxes and the layer divergence
+    const int L_acc = active ? L : -1;
+    Acc *acc_up = acc, *acc_dn = acc + (LP + 1), *acc_dir = acc + 2 * (LP + 1), *acc_div = acc + 3 * (LP + 1);
+    const R *fu = row(kRgFU), *fd = row(kRgFD), *fdir = row(kRgFDIR), *dv = row(kRgDIV);
+    if (r == 0 && active) {
+      acc_up[LP] += w_g * fu[0]; acc_dn[LP] += w_g * fd[0];
+      if (!lw) acc_dir[LP] += w_g * fdir[0];
+    }
+#pragma unroll
+    for (int j = 0; j < CH; ++j) {
+      const int i = r * CH + j, s = j * P + r;
+      if (i < L_acc) {
+        acc_up[s] += w_g * fu[i + 1];
+        acc_dn[s] += w_g * fd[i + 1];
+        if (!lw) acc_dir[s] += w_g * fdir[i + 1];
+        acc_div[s] += w_g * dv[i];
+      }
+    }
+    __syncwarp(gm);
+  }
+
+  // The serial part of the two-region solve, on one lane, in FP64 in every
+  // build (the FP32 coefficients of the layers are its inputs): rows as
+  // solve_region leaves them; writes the level fluxes (diffuse in the
+  // solar), the direct flux and the layer divergence.  Layers i are 0-based
+  // here; interface i lies below layer i-1 (0: the top).
+  __device__ static __noinline__ void region_serial(const FluxParams &p, const Smem &S, R *X, double *Y, int nct,
+                                                    int L, bool lw, R f_inc_down_r, R f_inc_dir_r, R alb_diff_r,
+                                                    R alb_dir_r, R dB_surf_r) {
+    using D = double;
+    auto row = [&](int k) { return X + (size_t)k * (LP + 1); };
+    auto drow = [&](int k) { return Y + (size_t)k * (LP + 1); };
+    auto ov = [&](int m, int i) -> D { return (D)S.ovl[(size_t)m * (LP + 1) + i]; };
+    const D f_inc_down = f_inc_down_r, f_inc_dir = f_inc_dir_r, alb_diff = alb_diff_r, alb_dir = alb_dir_r;
+    const D dB_surf = dB_surf_r;
+    R *FT = row(kRgFT), *FR = row(kRgFR), *FT0 = row(kRgFT0), *FC1 = row(kRgFC1), *FC2 = row(kRgFC2);
+    R *CT = row(kRgCT), *CR = row(kRgCR), *CT0 = row(kRgCT0), *CC1 = row(kRgCC1), *CC2 = row(kRgCC2);
+    R *FOM = row(kRgFOM), *COM = row(kRgCOM);
+    D *B11 = drow(kRgB11), *B21 = drow(kRgB21), *B22 = drow(kRgB22), *G11 = drow(kRgG11), *G12 = drow(kRgG12);
+    D *G21 = drow(kRgG21), *G22 = drow(kRgG22), *H1 = drow(kRgH1), *H2 = drow(kRgH2);
+    R *FU = row(kRgFU), *FD = row(kRgFD), *FDIR = row(kRgFDIR), *DV = row(kRgDIV);
+    const bool hogan = p.solver_hogan;
+    // the solar sources of each region in FP64 (mixed_solar_source.F90:
+    // 95-250), held in four of the elimination rows until the elimination
+    // (which reads a layer's sources before it writes that layer's row)
+    // takes them over
+    D *SU = G21, *SD = G22, *SUC = G12, *SDC = B21;
+    D bc = 0.0;
+    if (!lw) {
+      D f = f_inc_dir;
+      FDIR[0] = (R)f;
+      for (int i1 = 1; i1 <= nct - 1; ++i1) {
+        const int ii = i1 - 1;
+        SU[ii] = (D)FC1[ii] * f;
+        SD[ii] = (D)FC2[ii] * f;
+        f = f * (D)FT0[ii];
+        FDIR[i1] = (R)f;
+      }
+      D bf = f;
+      for (int i1 = nct; i1 <= L; ++i1) {
+        const int ii = i1 - 1;
+        const D tc = ov(3, i1 - 1) * bc + ov(2, i1 - 1) * bf;
+        const D tf = ov(0, i1 - 1) * bf + ov(1, i1 - 1) * bc;
+        SU[ii] = (D)FC1[ii] * tf; SD[ii] = (D)FC2[ii] * tf;
+        SUC[ii] = (D)CC1[ii] * tc; SDC[ii] = (D)CC2[ii] * tc;
+        bf = tf * (D)FT0[ii];
+        bc = tc * (D)CT0[ii];
+        FDIR[i1] = (R)(bf + bc);
+      }
+      // the layers' source rows now hold the sources themselves
+      for (int ii = 0; ii < L; ++ii) {
+        FC1[ii] = (R)SU[ii]; FC2[ii] = (R)SD[ii];
+        if (ii + 1 >= nct) { CC1[ii] = (R)SUC[ii]; CC2[ii] = (R)SDC[ii]; }
+      }
+    }
+    auto su_of = [&](int ii) -> D { return lw ? (D)FC1[ii] : SU[ii]; };
+    auto sd_of = [&](int ii) -> D { return lw ? (D)FC2[ii] : SD[ii]; };
+    auto suc_of = [&](int ii) -> D { return lw ? (D)CC1[ii] : SUC[ii]; };
+    auto sdc_of = [&](int ii) -> D { return lw ? (D)CC2[ii] : SDC[ii]; };
+    // ground sources (mix_column.F90:365-385)
+    D sgf, sgc;
+    if (!lw) { sgf = (alb_dir - alb_diff) * ((D)FDIR[L] - bc); sgc = (alb_dir - alb_diff) * bc; }
+    else { sgf = ov(4, L) * (1.0 - alb_diff) * dB_surf; sgc = ov(6, L) * (1.0 - alb_diff) * dB_surf; }
+    // elimination, from the ground up (solver_mix_direct.F90:88-180,
+    // solver_mix_direct_hogan.F90:78-140); the solar sources of layer ii are
+    // read before row ii of the coefficients is written
+    D a11 = alb_diff, a22 = alb_diff, a12 = 0.0, a21 = 0.0, g1 = sgf, g2 = sgc;
+    for (int i1 = L; i1 >= 1; --i1) {
+      const int ii = i1 - 1;
+      const D r = FR[ii], t = FT[ii], sd = sd_of(ii), su = su_of(ii);
+      if (i1 >= nct) {
+        const D rcl = CR[ii], tcl = CT[ii], sdc = sdc_of(ii), suc = suc_of(ii);
+        const D v11 = ov(0, i1), v21 = ov(2, i1), v12 = ov(1, i1), v22 = ov(3, i1);
+        const D u11 = ov(4, i1 - 1), u12 = ov(5, i1 - 1), u21 = ov(6, i1 - 1), u22 = ov(7, i1 - 1);
+        if (!hogan) {
+          const D th11 = a11 * v11 + a12 * v21, th12 = a11 * v12 + a12 * v22;
+          const D th21 = a21 * v11 + a22 * v21, th22 = a21 * v12 + a22 * v22;
+          const D b21 = -th21 * r, b22 = 1.0 / (1.0 - th22 * rcl);
+          const D gm21 = th21 * t, gm22 = th22 * tcl;
+          const D hh2 = g2 + th21 * sd + th22 * sdc;
+          D lam = th12 * rcl * b22;
+          const D b11 = 1.0 / (1.0 - th11 * r + lam * b21);
+          const D gm11 = th11 * t + lam * gm21, gm12 = th12 * tcl + lam * gm22;
+          const D hh1 = g1 + th11 * sd + th12 * sdc + lam * hh2;
+          B11[ii] = b11; B21[ii] = b21; B22[ii] = b22; G11[ii] = gm11; G12[ii] = gm12; G21[ii] = gm21;
+          G22[ii] = gm22; H1[ii] = hh1; H2[ii] = hh2;
+          lam = u22 * tcl * b22;
+          D lamb = (u21 * t + lam * b21) * b11;
+          const D n21 = u21 * r + lam * gm21 + lamb * gm11;
+          const D n22 = u22 * rcl + lam * gm22 + lamb * gm12;
+          const D ng2 = u21 * su + u22 * suc + lam * hh2 + lamb * hh1;
+          lam = u12 * tcl * b22;
+          lamb = (u11 * t + lam * b21) * b11;
+          a11 = u11 * r + lam * gm21 + lamb * gm11;
+          a12 = u12 * rcl + lam * gm22 + lamb * gm12;
+          g1 = u11 * su + u12 * suc + lam * hh2 + lamb * hh1;
+          a21 = n21; a22 = n22; g2 = ng2;
+        } else {
+          const D th11 = a11 * v11 + a22 * v21, th22 = a11 * v12 + a22 * v22;
+          const D b11 = 1.0 / (1.0 - th11 * r), gm11 = th11 * t, hh1 = g1 + th11 * sd;
+          const D b22 = 1.0 / (1.0 - th22 * rcl), gm22 = th22 * tcl, hh2 = g2 + th22 * sdc;
+          const D l1 = su + hh1 * t * b11, l2 = suc + hh2 * tcl * b22;
+          B11[ii] = b11; G11[ii] = gm11; H1[ii] = hh1; B22[ii] = b22; G22[ii] = gm22; H2[ii] = hh2;
+          a11 = r + th11 * t * t * b11;
+          a22 = rcl + th22 * tcl * tcl * b22;
+          g1 = u11 * l1 + u12 * l2;
+          g2 = u21 * l1 + u22 * l2;
+        }
+      } else {
+        D th11 = a11;
+        if (i1 == nct - 1 && nct < L) th11 = hogan ? a11 * ov(0, i1) + a22 * ov(2, i1) : a11 * ov(0, i1) + a12 * ov(2, i1);
+        const D b11 = 1.0 / (1.0 - th11 * r), gm11 = th11 * t, hh1 = g1 + th11 * sd;
+        B11[ii] = b11; G11[ii] = gm11; H1[ii] = hh1;
+        const D lam = t * b11;
+        a11 = r + lam * gm11;
+        g1 = su + lam * hh1;
+      }
+    }
+    // back-substitution (solver_mix_direct.F90:182-300); the sources are
+    // read back from the rows, which hold them rounded to the build's type
+    D fd_prev = f_inc_down, fu_prev;
+    FD[0] = (R)f_inc_down;
+    if (nct > 1) fu_prev = a11 * f_inc_down + g1;
+    else fu_prev = g1 + f_inc_down * (ov(0, 0) * a11 + ov(2, 0) * (hogan ? a22 : a12));
+    FU[0] = (R)fu_prev;
+    for (int i1 = 1; i1 <= nct - 1; ++i1) {
+      const int ii = i1 - 1;
+      const D fdt = fd_prev;
+      const D fub = (G11[ii] * fdt + H1[ii]) * B11[ii];
+      const D fdb = (D)FT[ii] * fdt + (D)FR[ii] * fub + (D)FC2[ii];
+      FU[i1] = (R)fub; FD[i1] = (R)fdb;
+      if constexpr (kFP64) DV[ii] = fub - fu_prev + fdt - fdb;
+      else DV[ii] = (R)((D)FOM[ii] * (fdt + fub) - ((D)FC1[ii] + (D)FC2[ii]));
+      fu_prev = fub; fd_prev = fdb;
+    }
+    D fd1 = 0.0, fd2 = 0.0;
+    for (int i1 = nct; i1 <= L; ++i1) {
+      const int ii = i1 - 1;
+      if (i1 > nct) {
+        const D d1 = fd1, d2 = fd2;
+        fd1 = ov(0, i1 - 1) * d1 + ov(1, i1 - 1) * d2;
+        fd2 = ov(2, i1 - 1) * d1 + ov(3, i1 - 1) * d2;
+      } else {
+        fd1 = ov(0, i1 - 1) * fd_prev;
+        fd2 = ov(2, i1 - 1) * fd_prev;
+      }
+      D fu1, fu2;
+      if (!hogan) {
+        fu1 = (G11[ii] * fd1 + G12[ii] * fd2 + H1[ii]) * B11[ii];
+        fu2 = (G21[ii] * fd1 + G22[ii] * fd2 - B21[ii] * fu1 + H2[ii]) * B22[ii];
+      } else {
+        fu1 = (G11[ii] * fd1 + H1[ii]) * B11[ii];
+        fu2 = (G22[ii] * fd2 + H2[ii]) * B22[ii];
+      }
+      const D nd1 = (D)FT[ii] * fd1 + (D)FR[ii] * fu1 + (D)FC2[ii];
+      const D nd2 = (D)CT[ii] * fd2 + (D)CR[ii] * fu2 + (D)CC2[ii];
+      const D fdt = fd_prev, fut = fu_prev;
+      fu_prev = fu1 + fu2; fd_prev = nd1 + nd2;
+      FU[i1] = (R)fu_prev; FD[i1] = (R)fd_prev;
+      // the layer's divergence: from the level fluxes of the FP64 solve, or
+      // in the mixed build under Hogan's form from each region's absorption,
+      // whose region fluxes close each region's layer equations (those of
+      // solver_mix_direct close only in their sum over the regions)
+      if (kFP64 || !hogan) DV[ii] = (R)(fu_prev - fut + fdt - fd_prev);
+      else
+        DV[ii] = (R)((D)FOM[ii] * (fd1 + fu1) - ((D)FC1[ii] + (D)FC2[ii]) + (D)COM[ii] * (fd2 + fu2) -
+                     ((D)CC1[ii] + (D)CC2[ii]));
+      fd1 = nd1; fd2 = nd2;
     }
   }
 

@@ -17,8 +17,10 @@
 // gas_list_pcf.F90: q, co2, o3, ...; an absent file means none of that
 // gas), .tstar (infra-red), .szen and .stoa (solar), .surf (albedo weights).
 // Outputs: .uflx, .dflx, .nflx, .hrts, and in the solar .vflx (direct) and
-// .sflx (diffuse down).  The two-stream path is driven clear (-C 5) or with
-// McICA (-C 10): clouds of one homogeneous type (-K 1: .clfr) or of water and
+// .sflx (diffuse down).  The two-stream path is driven clear (-C 5), with
+// clouds in a clear and a cloudy region (-C 2 maximum-random, -C 4 random
+// overlap; solver 16 unless -v 11) or with McICA (-C 10): clouds of one
+// homogeneous type (-K 1: .clfr) or of water and
 // ice types (-K 2: .wclfr, .iclfr), droplets from .lwm and .re with the
 // spectral file's droplet type -d, ice from .iwm and .ire with ice type -i
 // (input_cloud_cdf.f:340-790), and the subcolumns of set_cld_mcica from the
@@ -307,15 +309,21 @@ int main(int argc, char **argv) {
   if (base.empty()) return die("Base name not set.");
   if (!isolir) return die("Spectral region not set.");
   if (first < 1 || last < first) return die("Range of bands not set");
-  if (cloud != SOCGPU_IP_CLOUD_CLEAR && cloud != SOCGPU_IP_CLOUD_MCICA)
-    return die("cloud scheme " + std::to_string(cloud) + " is not driven (clear sky -C 5 or McICA -C 10)");
+  const bool region = cloud == SOCGPU_IP_CLOUD_MIX_MAX || cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
+  if (cloud != SOCGPU_IP_CLOUD_CLEAR && cloud != SOCGPU_IP_CLOUD_MCICA && !region)
+    return die("cloud scheme " + std::to_string(cloud) +
+               " is not driven (clear sky -C 5, cloud regions -C 2 or 4, McICA -C 10)");
   const bool mcica = cloud == SOCGPU_IP_CLOUD_MCICA;
-  if (mcica && representation != 1 && representation != SOCGPU_IP_CLOUD_ICE_WATER)
-    return die("McICA needs the cloud representation -K 1 (homogeneous) or -K 2 (ice and water)");
-  if (mcica && !drop_type && !ice_type) return die("Clouds are specified, but no cloudy processes are included.");
+  const bool clouds = mcica || region;
+  if (clouds && representation != 1 && representation != SOCGPU_IP_CLOUD_ICE_WATER)
+    return die("clouds need the cloud representation -K 1 (homogeneous) or -K 2 (ice and water)");
+  if (clouds && !drop_type && !ice_type) return die("Clouds are specified, but no cloudy processes are included.");
   if (mcica && (sampling < 0 || sampling > 2)) return die("The value of i_mcica_sampling is not valid.");
   if (!two_stream) two_stream = isolir == SOCGPU_IP_INFRA_RED ? 12 : 16;
-  if (!solver) solver = scatter == SOCGPU_IP_SCATTER_FULL ? SOCGPU_IP_SOLVER_HOMOGEN_DIRECT : SOCGPU_IP_SOLVER_NO_SCAT;
+  // the solver Cl_run_cdf picks for the cloud scheme (sbin/Cl_run_cdf:293-310)
+  if (!solver)
+    solver = region ? SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN
+                    : scatter == SOCGPU_IP_SCATTER_FULL ? SOCGPU_IP_SOLVER_HOMOGEN_DIRECT : SOCGPU_IP_SOLVER_NO_SCAT;
 
   char msg[512] = "";
   socgpu_spectrum_handle h = 0;
@@ -412,13 +420,40 @@ int main(int argc, char **argv) {
   const int nb_total = n_band;
   std::vector<double> rho_alb(np * 2 * (size_t)nb_total, 0.0), t_ground(np, 0.0), zen_0(np, 1.0), irrad(np, 0.0);
   if (exists(base + ".surf")) {
-    Field sf;
-    if (!read_field(base + ".surf", sf, err)) return die(err);
-    for (size_t l = 0; l < np; ++l)
-      for (int b = 0; b < nb_total; ++b) {
-        const double alb = sf.v[l + np * std::min<size_t>((size_t)b, sf.n_lev - 1) * (sf.n_lev > 1 ? 1 : 0)];
-        rho_alb[l + np * (0 + 2 * (size_t)b)] = alb;
-        rho_alb[l + np * (1 + 2 * (size_t)b)] = alb;
+    // albedo weights per basis function, and per band where the file has a
+    // band dimension (assign_surface_char_cdf.f:150-350): in the two-stream
+    // the first is the diffuse albedo and the second the direct one, which
+    // is the diffuse one when only one is given
+    NcFile sfile;
+    if (!socgpu::read_nc(base + ".surf", sfile, err)) return die(err);
+    const NcVar *alb = sfile.var("alb");
+    if (!alb) return die(base + ".surf: no variable alb");
+    size_t len[4] = {1, 1, 1, 1}, stride[4] = {0, 0, 0, 0};
+    int id[4] = {-1, -1, -1, -1};    // lat, lon, basis, band
+    for (size_t q = 0; q < alb->dims.size(); ++q) {
+      const std::string &dn = sfile.dims[alb->dims[q]].first;
+      const int k = dn == "lat" ? 0 : dn == "lon" ? 1 : dn == "basis" ? 2 : dn == "band" ? 3 : -1;
+      if (k < 0) return die(base + ".surf: unexpected dimension " + dn);
+      id[k] = (int)q;
+      len[k] = sfile.dims[alb->dims[q]].second;
+    }
+    if (id[2] < 0 || len[2] < 1 || len[2] > 2) return die(base + ".surf: one or two basis functions expected");
+    if (id[3] >= 0 && (int)len[3] != nb_total) return die(base + ".surf: band dimension differs from the spectral file");
+    if (len[0] * len[1] != np) return die(base + ".surf: not on the columns of .t");
+    std::vector<size_t> dstride(alb->dims.size(), 1);
+    for (int q = (int)alb->dims.size() - 2; q >= 0; --q)
+      dstride[q] = dstride[q + 1] * sfile.dims[alb->dims[q + 1]].second;
+    for (int k = 0; k < 4; ++k) stride[k] = id[k] >= 0 ? dstride[id[k]] : 0;
+    for (size_t a = 0; a < len[0]; ++a)
+      for (size_t o = 0; o < len[1]; ++o) {
+        const size_t l = a * len[1] + o;
+        for (int b = 0; b < nb_total; ++b)
+          for (int k = 0; k < 2; ++k) {
+            const size_t basis = std::min<size_t>((size_t)k, len[2] - 1);
+            const size_t at = a * stride[0] + o * stride[1] + basis * stride[2] + (size_t)b * stride[3];
+            if (at >= alb->data.size()) return die(base + ".surf: short data");
+            rho_alb[l + np * ((size_t)k + 2 * (size_t)b)] = alb->data[at];
+          }
       }
   }
   if (isolir == SOCGPU_IP_INFRA_RED) {
@@ -440,7 +475,7 @@ int main(int argc, char **argv) {
   std::vector<int> type_condensed, i_cloud_type, i_condensed_param, i_condensed_type;
   std::vector<double> cmr, dim, w_cloud, frac_cloud, c_sub, frac_cloudy;
   std::vector<int> n_subcol_cld, subcol_k, first_subcol_k, subcol_reorder;
-  if (mcica) {
+  if (clouds) {
     std::map<int, CloudTypeInfo> drops, ices;
     if (!read_cloud_types(sp_file, drops, ices)) return die("cannot open " + sp_file);
     struct Comp { int phase, type; const char *mr, *dim; };
@@ -486,6 +521,8 @@ int main(int argc, char **argv) {
       if (w_cloud[q] > 0.0)
         for (int t2 = 0; t2 < n_cloud_type; ++t2) frac_cloud[q + np * nl * t2] /= w_cloud[q];
     }
+  }
+  if (mcica) {
     // McICA data beside the spectral file
     const size_t slash = sp_file.find_last_of('/');
     const std::string mcica_path = (slash == std::string::npos ? std::string() : sp_file.substr(0, slash + 1)) +
@@ -566,7 +603,7 @@ int main(int argc, char **argv) {
   c.i_2stream = two_stream;
   c.i_scatter_method = scatter;
   c.i_solver = solver;
-  c.i_cloud = mcica ? SOCGPU_IP_CLOUD_MCICA : SOCGPU_IP_CLOUD_CLEAR;
+  c.i_cloud = cloud;
   c.i_cloud_representation = representation ? representation : SOCGPU_IP_CLOUD_ICE_WATER;
   c.i_gas_overlap = gas ? overlap : SOCGPU_IP_OVERLAP_RANDOM;
   c.i_direct_tau = direct_tau;
@@ -587,8 +624,8 @@ int main(int argc, char **argv) {
   d.nd_aerosol_mode = 1;
   d.nd_cloud_component = std::max(1, nc);
   d.nd_cloud_type = n_cloud_type;
-  d.nd_subcol_gen = gen;
-  d.nd_subcol_req = n_subcol_req;
+  d.nd_subcol_gen = mcica ? gen : 1;
+  d.nd_subcol_req = mcica ? n_subcol_req : 1;
   socgpu_atm atm{};
   atm.n_profile = (int)np;
   atm.n_layer = (int)nl;
@@ -610,7 +647,7 @@ int main(int argc, char **argv) {
   out.flux_direct = isolir == SOCGPU_IP_SOLAR ? direct.data() : nullptr;
   socgpu_aer aer{};
   socgpu_cld cld{};
-  if (mcica) {
+  if (clouds) {
     cld.n_condensed = nc;
     cld.type_condensed = type_condensed.data();
     cld.i_cloud_type = i_cloud_type.data();
@@ -621,6 +658,8 @@ int main(int argc, char **argv) {
     cld.n_cloud_type = n_cloud_type;
     cld.w_cloud = w_cloud.data();
     cld.frac_cloud = frac_cloud.data();
+  }
+  if (mcica) {
     cld.n_subcol_gen = gen;
     cld.n_subcol_req = n_subcol_req;
     cld.c_sub = c_sub.data();

@@ -133,7 +133,10 @@ struct FluxParams {
   int isolir, i_2stream, i_scatter_method, i_direct_tau;
   int l_rescale, n_order_forward, l_ir_source_quad, l_rayleigh, l_gas, l_aerosol_mode;
   int l_flux_div, first_band, last_band;
-  int mcica;
+  int mcica;                         // cloud fields staged (McICA or cloud regions)
+  int region;                        // clear and cloudy regions (ip_cloud_mix_max / mix_random)
+  int solver_hogan;                  // regions solved by solver_mix_direct_hogan, else solver_mix_direct
+  int mix_max;                       // regions overlap maximally where adjacent (else randomly)
   int l_continuum, l_mixing_ratio, i_water;   // i_water: 0-based species of water vapour
   // sizes
   int n_profile, n_layer, nd_profile, nd_layer, id_ct;  // id_ct 0-based first cloudy layer

@@ -343,6 +343,8 @@ class Marshal:
             cl.condensed_mix_ratio = _dp(cd["condensed_mix_ratio"][:, ict:, :], k)
             cl.condensed_dim_char = _dp(cd["condensed_dim_char"][:, ict:, :], k)
             cl.n_cloud_type = int(cd.get("n_cloud_type", 2))
+            # the extents of the arrays as given (the host path copies them whole)
+            self.dimen.nd_cloud_component, self.dimen.nd_cloud_type = cl.n_condensed, cl.n_cloud_type
             cl.w_cloud = _dp(cd["w_cloud"][:, ict:], k)
             cl.frac_cloud = _dp(cd["frac_cloud"][:, ict:, :], k)
             if mcica is not None:

@@ -1,0 +1,106 @@
+"""Clouds in a clear and a cloudy region (ip_cloud_mix_max / mix_random with
+solver_mix_direct and Hogan's form) on the GPU: the reference's 7460_28
+known-good outputs, FP64 against the oracle within 1e-10 of the largest flux,
+mixed precision within 0.1 W/m2 and 0.05 K/day; synthetic columns over both
+overlaps, both solvers, both cloud representations and both sources."""
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+import cld7460 as K
+from socrates_gb300 import abi, synth
+from socrates_gb300 import radiance as R
+from test_parity_gpu import assert_fp64_parity, assert_mixed_tolerance
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def O():
+    import oracle
+    return oracle
+
+
+@pytest.fixture(scope="module")
+def sps():
+    return K.spectra()
+
+
+def _check(ctl, sp, col, O, tag):
+    ref = O.radiance_calc(ctl, sp, col)
+    g64 = R.radiance_calc(replace(ctl, precision=abi.PRECISION_FP64), sp, col)
+    assert_fp64_parity({**g64, "mass": col.mass}, {**ref, "mass": col.mass}, f"{tag} fp64: ")
+    gmx = R.radiance_calc(replace(ctl, precision=abi.PRECISION_MIXED), sp, col)
+    net = ref["flux_down"] - ref["flux_up"]
+    hr = 8.64e+04 * (net[:, :-1] - net[:, 1:]) / (col.mass * 1.005e+03)
+    assert_mixed_tolerance(gmx, {**ref, "heating_rate": hr}, f"{tag} mixed: ")
+    return ref, g64
+
+
+@pytest.mark.parametrize("run", [r for r in K.RUNS if "ds0" not in r])
+def test_cloud_regions_known_good_output_on_gpu(gpu_lib, O, sps, run):
+    ctl, sp, col, kgo, kind = K.setup(run, sps)
+    _, g64 = _check(ctl, sp, col, O, run)
+    got = K.printed(g64, col, kind)
+    got = got[0] if kgo.ndim == 1 else got.T
+    err = K.half_units(got, kgo)
+    i = np.unravel_index(err.argmax(), err.shape)
+    assert err.max() <= 1.05, f"{run} at {i}: {got[i]} vs {kgo[i]}"
+
+
+def _clouded(sp, n, L, seed, solar, representation):
+    """operational_case columns with cloud layers of water and ice."""
+    col = synth.operational_case(sp, n, L, seed=seed, solar=solar)
+    rng = np.random.default_rng(seed)
+    w = np.where(rng.uniform(size=(n, L)) < 0.35, rng.uniform(0.05, 1.0, size=(n, L)), 0.0)
+    w[:, : L // 4] = 0.0                                   # clear stratosphere
+    lwm = np.where(w > 0, rng.uniform(1e-5, 5e-4, size=(n, L)), 0.0)
+    iwm = np.where(w > 0, rng.uniform(0.0, 2e-4, size=(n, L)), 0.0)
+    f = lambda a: np.asfortranarray(a)
+    dtype, itype = 5, 8
+    re = np.clip(rng.uniform(4e-6, 2e-5, size=(n, L)), sp.drop_parm_min_dim[dtype - 1], sp.drop_parm_max_dim[dtype - 1])
+    ire = np.clip(rng.uniform(2e-5, 1e-4, size=(n, L)), sp.ice_parm_min_dim[itype - 1], sp.ice_parm_max_dim[itype - 1])
+    cld = dict(n_condensed=2, type_condensed=[abi.IP_PHASE_WATER, abi.IP_PHASE_ICE],
+               i_condensed_param=[int(sp.i_drop_parm[dtype - 1]), int(sp.i_ice_parm[itype - 1])],
+               i_condensed_type=[dtype, itype], condensed_mix_ratio=f(np.stack([lwm, iwm], axis=2)),
+               condensed_dim_char=f(np.stack([re, ire], axis=2)), w_cloud=f(w))
+    if representation == abi.IP_CLOUD_HOMOGEN:
+        cld.update(i_cloud_type=[1, 1], n_cloud_type=1, frac_cloud=f(np.where(w > 0, 1.0, 0.0)[:, :, None]))
+    else:
+        fw = np.where(w > 0, rng.uniform(0.2, 0.8, size=(n, L)), 0.0)
+        cld.update(i_cloud_type=[1, 2], n_cloud_type=2, frac_cloud=f(np.stack([fw, np.where(w > 0, 1.0 - fw, 0.0)],
+                                                                               axis=2)))
+    col.cld = cld
+    return col
+
+
+@pytest.mark.parametrize("solar", [False, True])
+@pytest.mark.parametrize("scheme,solver,representation", [
+    (abi.IP_CLOUD_MIX_MAX, abi.IP_SOLVER_MIX_DIRECT, abi.IP_CLOUD_HOMOGEN),
+    (abi.IP_CLOUD_MIX_MAX, abi.IP_SOLVER_MIX_DIRECT_HOGAN, abi.IP_CLOUD_ICE_WATER),
+    (abi.IP_CLOUD_MIX_RANDOM, abi.IP_SOLVER_MIX_DIRECT, abi.IP_CLOUD_ICE_WATER),
+    (abi.IP_CLOUD_MIX_RANDOM, abi.IP_SOLVER_MIX_DIRECT_HOGAN, abi.IP_CLOUD_HOMOGEN)])
+def test_cloud_regions_synthetic(gpu_lib, O, sps, solar, scheme, solver, representation):
+    """97 columns of 60 layers with the GA9 files, k_eqv_scl and continuum:
+    random cloud layers of water (Pade) and ice (Fu) as one type or as two."""
+    sp = sps["ga9sw" if solar else "ga9lw"]
+    col = _clouded(sp, 97, 60, seed=61 + solar, solar=solar, representation=representation)
+    common = dict(i_cloud=scheme, i_solver=solver, l_continuum=True, i_gas_overlap=abi.IP_OVERLAP_K_EQV_SCL,
+                  l_flux_div=False)
+    ctl = R.sw_control(l_rayleigh=True, **common) if solar else R.lw_control(l_ir_source_quad=True, **common)
+    ref, _ = _check(ctl, sp, col, O, f"{scheme}/{solver}/{representation} solar={solar}")
+    clear = O.radiance_calc(replace(ctl, i_cloud=abi.IP_CLOUD_CLEAR, i_solver=abi.IP_SOLVER_HOMOGEN_DIRECT), sp, col)
+    assert np.abs(ref["flux_up"] - clear["flux_up"]).max() > 1.0          # the clouds matter
+
+
+def test_cloud_regions_refusals(gpu_lib, sps):
+    """The unscaled direct beam and a solver of another scheme are refused."""
+    ctl, sp, col, _, _ = K.setup("sw_ds0_avg", sps)
+    with pytest.raises(R.RadianceError) as e:
+        R.radiance_calc(ctl, sp, col)
+    assert e.value.status == abi.I_ERR_FATAL
+    ctl, sp, col, _, _ = K.setup("sw_avg", sps)
+    with pytest.raises(R.RadianceError) as e:
+        R.radiance_calc(replace(ctl, i_solver=abi.IP_SOLVER_HOMOGEN_DIRECT), sp, col)
+    assert e.value.status == abi.I_ERR_FATAL and "solver_mix" in str(e.value)

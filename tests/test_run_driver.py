@@ -276,3 +276,68 @@ def test_driver_refuses_clouds_without_processes(tmp_path):
     r = subprocess.run([_tool(), "-s", "x", "-R", "1", "1", "-I", "-C", "10", "-K", "1", "-B", "y"],
                        capture_output=True, text=True)
     assert r.returncode != 0 and "no cloudy processes" in r.stderr
+
+
+def _cld7460_files(tmp, run, to_cdf):
+    """The inputs of one averaged-column run of examples/netcdf/7460_28 as
+    column files, with its spectral file beside them and, for .surfsw2, a
+    surface of two albedo weights (diffuse, direct)."""
+    import cld7460 as K
+    d = np.load(K.FIXTURE)
+    sps = K.spectra()
+    solar, ga9 = "sw" in run, "ga9" in run
+    sp = sps[("ga9" if ga9 else "h") + ("sw" if solar else "lw")]
+    gases = {1: "q", 2: "co2", 3: "o3", 4: "n2o", 6: "ch4", 7: "o2"}
+    gas = np.zeros((d["avg_p"].size, sp.n_absorb))
+    for j, ty in enumerate(sp.type_absorb):
+        if int(ty) in gases:
+            gas[:, j] = d["avg_" + gases[int(ty)]][:, 0]
+    case = dict(p=d["avg_p"], t=d["avg_t"][:, 0], p_level=d["avg_p_level"], t_level=d["avg_t_level"][:, 0], gas=gas,
+                t_ground=d["avg_tstar"], alb=d["avg_surfsw" if solar else "avg_surflw"])
+    extra = {k: (d["avg_p"], d["avg_" + k][:, 0]) for k in ("clfr", "lwm", "iwm", "re", "ire")}
+    if solar:
+        extra.update(szen=([1.013e5], d["avg_szen"]), stoa=([1.013e5], d["avg_stoa"]))
+    sp_path, base, wy = _column_files(tmp, "7460_28", case, sp, f"sp_{run}", False, gases=set(gases),
+                                      wenyi=ga9 and not solar, digits=17, extra=extra)
+    if run.startswith("sw2") or (ga9 and solar):
+        surf = tmp / "7460_28.surf"
+        write_cdl(surf, "7460_28.surf", [("lat", 1), ("lon", 1), ("basis", 2)],
+                  [("lat", ["lat"], [1.0], {}), ("lon", ["lon"], [0.0], {}), ("basis", ["basis"], [1.0, 2.0], {}),
+                   ("alb", ["basis", "lat", "lon"], np.reshape(d["avg_surfsw2"], (2, 1, 1)),
+                    {"title": "ALBEDO WEIGHTS"})])
+    if to_cdf:
+        tool = _tool()
+        for f in tmp.glob("7460_28.*"):
+            tmp_out = f.with_name(f.name + ".cdf")
+            subprocess.run([tool, "--convert", str(f), str(tmp_out)], check=True)
+            tmp_out.replace(f)
+    opts = {"lw_avg": "-R 1 9 -I -t 12 +R -v 11 -g 2 -c -C 2 -K 1 -d 1 -i 1",
+            "sw2": "-R 1 6 -S -t 2 +R -v 11 -g 2 -r -C 2 -K 1 -d 3 -i 3",
+            "sw_ga9_avg": "-R 1 6 -S +R -g 4 -c -r -C 2 -K 1 -d 5 -i 8"}[run].split()
+    return sp_path, base, wy, opts, np.asarray(d["kgo_" + run]), ("nflx" if ga9 else "hrts")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("run,to_cdf", [("lw_avg", False), ("sw2", True), ("sw_ga9_avg", False)])
+def test_driver_reproduces_cld7460(gpu_lib, tmp_path, run, to_cdf):
+    """The reference's cloud-region example (examples/netcdf/7460_28/run_me)
+    through the column driver: -C 2 with solver 11, or the default solver 16
+    with the GA9 file; a surface of one albedo weight or of two (diffuse and
+    direct); the written heating rates or net fluxes against the
+    known-good output (half a unit of the 6th digit from CDL, 2e-5 of the
+    largest from single-precision netCDF)."""
+    import cld7460 as K
+    tool = _tool()
+    sp_path, base, wy, opts, kgo, kind = _cld7460_files(tmp_path, run, to_cdf)
+    cmd = [tool, "-s", str(sp_path)] + opts + ["-B", str(base)] + (["-W", str(wy)] if wy else [])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = str(base) + "." + kind
+    if to_cdf:
+        scipy_io = pytest.importorskip("scipy.io")
+        with scipy_io.netcdf_file(out, "r", mmap=False) as nc:
+            got = np.array(nc.variables[kind][:]).ravel()
+        assert np.abs(got - kgo).max() <= 2e-5 * np.abs(kgo).max()
+    else:
+        _, got = field(out)
+        assert K.half_units(got, kgo).max() <= 1.05
