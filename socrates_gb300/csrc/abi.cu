@@ -1352,6 +1352,68 @@ int socgpu_radiance_calc_device(const socgpu_control *control, const socgpu_dime
   return launch(p, control, (cudaStream_t)stream, msg, msg_len);
 }
 
+// Page-locked caller arrays read and written in place by the kernel through
+// their mapped device addresses (on Grace the GPU reaches host memory over
+// NVLink-C2C), in place of the copy pipeline.  SOCGPU_HOST_ACCESS=direct
+// selects it, =copy the pipeline.
+constexpr int kDirectUnavailable = -1;
+
+bool host_access_direct() {
+  const char *e = std::getenv("SOCGPU_HOST_ACCESS");
+  return e && std::strcmp(e, "direct") == 0;
+}
+
+int direct_radiance_calc(const socgpu_control *control, const socgpu_dimen *dimen, socgpu_spectrum_handle spectrum,
+                         const socgpu_atm *atm, const socgpu_cld *cld, const socgpu_aer *aer,
+                         const socgpu_bound *bound, socgpu_radout *radout, cudaStream_t stream, char *msg,
+                         size_t msg_len) {
+  bool ok = true;
+  auto map = [&](auto *h) {
+    using T = std::remove_cv_t<std::remove_pointer_t<decltype(h)>>;
+    if (!h || !ok) return (T *)nullptr;
+    void *d = nullptr;
+    if (cudaHostGetDevicePointer(&d, (void *)h, 0) != cudaSuccess) { cudaGetLastError(); ok = false; }
+    return (T *)d;
+  };
+  socgpu_control c2 = *control;
+  c2.weight_band = map(control->weight_band);
+  socgpu_atm a2 = *atm;
+  a2.p = map(atm->p); a2.t = map(atm->t); a2.p_level = map(atm->p_level); a2.t_level = map(atm->t_level);
+  a2.mass = map(atm->mass); a2.gas_mix_ratio = map(atm->gas_mix_ratio); a2.density = map(atm->density);
+  socgpu_bound b2 = *bound;
+  b2.zen_0 = map(bound->zen_0); b2.solar_irrad = map(bound->solar_irrad); b2.rho_alb = map(bound->rho_alb);
+  b2.t_ground = map(bound->t_ground); b2.flux_ground = map(bound->flux_ground);
+  socgpu_aer e2{};
+  if (aer) {
+    e2 = *aer;
+    e2.mode_mix_ratio = map(aer->mode_mix_ratio); e2.mode_absorption = map(aer->mode_absorption);
+    e2.mode_scattering = map(aer->mode_scattering); e2.mode_asymmetry = map(aer->mode_asymmetry);
+  }
+  socgpu_cld k2{};
+  if (cld) {
+    k2 = *cld;   // the descriptors of the components stay host arrays
+    k2.condensed_mix_ratio = map(cld->condensed_mix_ratio); k2.condensed_dim_char = map(cld->condensed_dim_char);
+    k2.w_cloud = map(cld->w_cloud); k2.frac_cloud = map(cld->frac_cloud); k2.c_sub = map(cld->c_sub);
+    k2.frac_cloudy = map(cld->frac_cloudy); k2.n_subcol_cld = map(cld->n_subcol_cld);
+    k2.subcol_k = map(cld->subcol_k); k2.first_subcol_k = map(cld->first_subcol_k);
+    k2.subcol_reorder = map(cld->subcol_reorder);
+  }
+  socgpu_radout r2 = *radout;
+  r2.flux_up = map(radout->flux_up); r2.flux_down = map(radout->flux_down);
+  r2.flux_direct = map(radout->flux_direct); r2.flux_div = map(radout->flux_div);
+  r2.heating_rate = map(radout->heating_rate); r2.flux_up_band = map(radout->flux_up_band);
+  r2.flux_down_band = map(radout->flux_down_band);
+  if (!ok) return kDirectUnavailable;
+  int st = socgpu_radiance_calc_device(&c2, dimen, spectrum, &a2, cld ? &k2 : nullptr, aer ? &e2 : nullptr, &b2, &r2,
+                                       stream, msg, msg_len);
+  if (st != SOCGPU_I_NORMAL) return st;
+  if (cudaStreamSynchronize(stream) != cudaSuccess) {
+    set_msg(msg, msg_len, "radiance calculation failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  return SOCGPU_I_NORMAL;
+}
+
 int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dimen, socgpu_spectrum_handle spectrum,
                          const socgpu_atm *atm, const socgpu_cld *cld, const socgpu_aer *aer,
                          const socgpu_bound *bound, socgpu_radout *radout, char *msg, size_t msg_len) {
@@ -1381,6 +1443,10 @@ int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dime
     st = staged_radiance_calc(call, control, base, streams, msg, msg_len);
     if (st != SOCGPU_I_NORMAL) sync_all();
     return st;
+  }
+  if (host_access_direct()) {
+    st = direct_radiance_calc(control, dimen, spectrum, atm, cld, aer, bound, radout, tl_ws.stream, msg, msg_len);
+    if (st != kDirectUnavailable) return st;
   }
   // column chunks: copy in, compute and copy out of different chunks overlap;
   // chunks of about pipeline_chunk_bytes(), at least 512 columns

@@ -294,7 +294,7 @@ class Marshal:
     """Builds the C structures of one radiance_calc call from numpy arrays."""
 
     def __init__(self, control: Control, spectrum: Spectrum, col, mcica: McicaState | None = None,
-                 id_cloud_top: int = 1):
+                 id_cloud_top: int = 1, alloc=None):
         self.keep: list = []
         k = self.keep
         n, L = col.n_profile, col.n_layer
@@ -355,7 +355,8 @@ class Marshal:
                 cl.subcol_k = _ip(mcica.subcol_k, k)
                 cl.first_subcol_k = _ip(mcica.first_subcol_k, k)
                 cl.subcol_reorder = _ip(mcica.subcol_reorder, k)
-        f = lambda *s: np.zeros(s, order="F")
+        # outputs from `alloc(*shape)` (F-ordered zeros), e.g. page-locked
+        f = alloc or (lambda *s: np.zeros(s, order="F"))
         self.flux_up, self.flux_down = f(n, L + 1), f(n, L + 1)
         self.flux_direct = f(n, L + 1) if control.isolir == abi.IP_SOLAR else None
         self.flux_div = f(n, L) if control.l_flux_div else None
