@@ -163,6 +163,7 @@ struct SmemLayout {
 enum RegRow {
   kRgFT, kRgFR, kRgFT0, kRgFC1, kRgFC2, kRgFOM,
   kRgCT, kRgCR, kRgCT0, kRgCC1, kRgCC2, kRgCOM,
+  kRgFT0D, kRgCT0D,          // unscaled direct transmissions (i_direct_tau = ip_direct_noscaling)
   kRgFU, kRgFD, kRgFDIR, kRgDIV, kRegRows
 };
 // The solver's elimination coefficients, kept in FP64 in every build: the
@@ -1397,10 +1398,18 @@ struct FluxKernel {
     gas_k_lane(p, S, gt, gp, bd, amt_b, r, L, kgv);
     R Tf[CH], Rff[CH], T0f[CH], c1f[CH], c2f[CH], omf[CH];
     R Tc[CH], Rc[CH], T0c[CH], c1c[CH], c2c[CH], omc[CH];
+    // the direct beam without delta-scaling (two_coeff.F90 trans_0_dir):
+    // exp(-tau sec0) of the optical depth before rescaling, per region
+    const bool dir_unscaled = !lw && p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING;
+    auto t0_unscaled = [&](R kgt, R kg, R dm) -> R {
+      if constexpr (kFP64) return exp(-(kgt + kg) * dm * sec0);
+      else return expf(-(kgt + kg) * dm * sec0);
+    };
 #pragma unroll
     for (int j = 0; j < CH; ++j) {
       const int i = r * CH + j, s = j * P + r;
       Tc[j] = R(0); Rc[j] = R(0); T0c[j] = R(0); c1c[j] = R(0); c2c[j] = R(0); omc[j] = R(0);
+      if (i < L && dir_unscaled) { row(kRgFT0D)[i] = t0_unscaled(kgt_b[s], kgv[j], S.mass[s]); row(kRgCT0D)[i] = R(0); }
       if (i < L) {
         cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kgv[j], S.mass[s], asym_b[s], fwd_b[s], sec0,
                   Tf[j], Rff[j], T0f[j], c1f[j], c2f[j], omf[j]);
@@ -1430,6 +1439,7 @@ struct FluxKernel {
             R tT, tR, tT0, t1, t2, tO;
             cell_coef(p, kgt, kes, kab, kgv[j], S.mass[s], asym, fwd, sec0, tT, tR, tT0, t1, t2, tO);
             Tc[j] = Tc[j] + fc * tT; Rc[j] = Rc[j] + fc * tR; T0c[j] = T0c[j] + fc * tT0;
+            if (dir_unscaled) row(kRgCT0D)[i] = row(kRgCT0D)[i] + fc * t0_unscaled(kgt, kgv[j], S.mass[s]);
             c1c[j] = c1c[j] + fc * t1; c2c[j] = c2c[j] + fc * t2; omc[j] = omc[j] + fc * tO;
           }
         }
@@ -1438,7 +1448,23 @@ struct FluxKernel {
       }
     }
     if constexpr (SRC == SOCGPU_IP_SOLAR)
-      if (p.keqv) { fold_direct(S, bi, max_abs, r, L, T0f, c2f); fold_direct(S, bi, max_abs, r, L, T0c, c2c); }
+      if (p.keqv) {
+        fold_direct(S, bi, max_abs, r, L, T0f, c2f);
+        fold_direct(S, bi, max_abs, r, L, T0c, c2c);
+        if (dir_unscaled) {
+          // adjust_solar_ke on the unscaled beam too (mixed_solar_source.F90:130-140)
+          const R *a = S.aux + (size_t)bi * max_abs * LP;
+#pragma unroll
+          for (int j = 0; j < CH; ++j) {
+            const int i = r * CH + j, s = j * P + r;
+            if (i < L) {
+              const R f = kFP64 ? a[s] : R(1) + a[s];
+              row(kRgFT0D)[i] = row(kRgFT0D)[i] * f;
+              row(kRgCT0D)[i] = row(kRgCT0D)[i] * f;
+            }
+          }
+        }
+      }
 #pragma unroll
     for (int j = 0; j < CH; ++j) {
       const int i = r * CH + j, s = j * P + r;
@@ -1538,6 +1564,23 @@ struct FluxKernel {
         bf = tf * (D)FT0[ii];
         bc = tc * (D)CT0[ii];
         FDIR[i1] = (R)(bf + bc);
+      }
+      if (p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING) {
+        // the direct flux without delta-scaling, which the outputs and the
+        // ground's direct reflection take (mixed_solar_source.F90:200-240)
+        const R *FT0D = row(kRgFT0D), *CT0D = row(kRgCT0D);
+        D fdd = f_inc_dir;
+        for (int i1 = 1; i1 <= nct - 1; ++i1) { fdd = fdd * (D)FT0D[i1 - 1]; FDIR[i1] = (R)fdd; }
+        D df = fdd, dc = 0.0;
+        for (int i1 = nct; i1 <= L; ++i1) {
+          const int ii = i1 - 1;
+          const D tc = ov(3, i1 - 1) * dc + ov(2, i1 - 1) * df;
+          const D tf = ov(0, i1 - 1) * df + ov(1, i1 - 1) * dc;
+          df = tf * (D)FT0D[ii];
+          dc = tc * (D)CT0D[ii];
+          FDIR[i1] = (R)(df + dc);
+        }
+        bc = dc;
       }
       // the layers' source rows now hold the sources themselves
       for (int ii = 0; ii < L; ++ii) {

@@ -38,7 +38,7 @@ def _check(ctl, sp, col, O, tag):
     return ref, g64
 
 
-@pytest.mark.parametrize("run", [r for r in K.RUNS if "ds0" not in r])
+@pytest.mark.parametrize("run", K.RUNS)
 def test_cloud_regions_known_good_output_on_gpu(gpu_lib, O, sps, run):
     ctl, sp, col, kgo, kind = K.setup(run, sps)
     _, g64 = _check(ctl, sp, col, O, run)
@@ -95,11 +95,12 @@ def test_cloud_regions_synthetic(gpu_lib, O, sps, solar, scheme, solver, represe
 
 
 def test_cloud_regions_refusals(gpu_lib, sps):
-    """The unscaled direct beam and a solver of another scheme are refused."""
+    """The unscaled direct beam outside the cloud regions, and a solver of
+    another scheme, are refused."""
     ctl, sp, col, _, _ = K.setup("sw_ds0_avg", sps)
     with pytest.raises(R.RadianceError) as e:
-        R.radiance_calc(ctl, sp, col)
-    assert e.value.status == abi.I_ERR_FATAL
+        R.radiance_calc(replace(ctl, i_cloud=abi.IP_CLOUD_CLEAR, i_solver=abi.IP_SOLVER_HOMOGEN_DIRECT), sp, col)
+    assert e.value.status == abi.I_ERR_FATAL and "i_direct_tau" in str(e.value)
     ctl, sp, col, _, _ = K.setup("sw_avg", sps)
     with pytest.raises(R.RadianceError) as e:
         R.radiance_calc(replace(ctl, i_solver=abi.IP_SOLVER_HOMOGEN_DIRECT), sp, col)
