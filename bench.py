@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--impl", default="socgpu", choices=["socgpu", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=N_COL, help="columns of the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU work of the baseline sample")
-    ap.add_argument("--workload", default="sw", choices=["sw", "batched", "serve"])
+    ap.add_argument("--workload", default="sw", choices=["sw", "batched", "serve", "ga9"])
     ap.add_argument("--rates", default="200,1000,5000", help="arrival rates (requests/s) of the serving workload")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
     ap.add_argument("--batches", type=int, default=4096, help="column batches of the batched workload")
@@ -453,6 +453,71 @@ def run_serve(args):
         print(json.dumps(line), flush=True)
 
 
+def run_ga9(args):
+    """The operational spectral files: the GA9 long-wave and short-wave files
+    (lookup-table k, Wen-Yi CO2 terms, equivalent-extinction overlap,
+    continuum) on 10000 columns of 100 layers, mixed and FP64 device paths;
+    the inputs are resident and a 256 MiB L2 flush runs between steps."""
+    import numpy as np
+    import torch
+    rank, world = dist_setup(args.gpus)
+    from pathlib import Path
+    from dataclasses import replace
+    from socrates_gb300 import abi
+    from socrates_gb300 import build as B
+    from socrates_gb300 import radiance as R
+    from socrates_gb300.device import DeviceCase
+    from socrates_gb300.spectrum import Spectrum
+    from socrates_gb300.synth import operational_case
+    if rank == 0:
+        B.build()
+    barrier(world)
+    fixture = Path(__file__).resolve().parent / "tests" / "golden" / "runes_ga9.npz"
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    lines = {}
+    for solar in (False, True):
+        sp = Spectrum.load_npz(fixture, prefix="sw_" if solar else "lw_")
+        col = operational_case(sp, N_COL, N_LAYER, seed=SEED + rank, solar=solar)
+        common = dict(l_continuum=True, i_gas_overlap=abi.IP_OVERLAP_K_EQV_SCL, l_flux_div=False)
+        ctl = R.sw_control(l_rayleigh=True, **common) if solar else R.lw_control(**common)
+        res = {}
+        for prec, steps in ((abi.PRECISION_MIXED, args.steps), (abi.PRECISION_FP64, max(3, args.steps // 20))):
+            case = DeviceCase(replace(ctl, precision=prec), sp, col)
+            for _ in range(args.warmup):
+                case.run(stream.cuda_stream)
+            torch.cuda.synchronize()
+            ms = []
+            for _ in range(steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                case.run(stream.cuda_stream)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            t = max_over_ranks(float(np.mean(ms)) / 1e3, world)
+            res[prec] = (t, {k: case.output(k).copy() for k in ("flux_up", "flux_down", "heating_rate")})
+        (t_mx, o_mx), (t_64, o_64) = res[abi.PRECISION_MIXED], res[abi.PRECISION_FP64]
+        # the solves under k_eqv_scl: the k-terms of each band's first
+        # absorber (one grey solve in a band without absorbers)
+        g = sum(int(sp.i_band_k[b, int(sp.index_absorb[0, b]) - 1]) if int(sp.n_band_absorb[b]) > 0 else 1
+                for b in range(sp.n_band))
+        lines["sw" if solar else "lw"] = {
+            "value": world * N_COL * g / t_mx, "ms_per_step": t_mx * 1e3, "g_points": g,
+            "fp64_value": world * N_COL * g / t_64, "fp64_ms_per_step": t_64 * 1e3,
+            "max_flux_err_wm2": float(max(np.abs(o_mx[k] - o_64[k]).max() for k in ("flux_up", "flux_down"))),
+            "max_heating_rate_err_kday": float(np.abs(o_mx["heating_rate"] - o_64["heating_rate"]).max())}
+    if rank == 0:
+        print(json.dumps({"metric": "column·g-points/s on the GA9 operational spectral files", "unit": UNIT,
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                          "scaling": "weak", "dtype": "f32+f64", "data": "synthetic columns, GA9 spectral files",
+                          "config": {"workload": f"GA9 LW and SW, lookup-table k, Wen-Yi, k_eqv_scl, continuum, "
+                                                 f"{N_COL} columns x {N_LAYER} layers, clear sky",
+                                     "l2": "256 MiB L2 flush between timed steps"},
+                          "lw": lines["lw"], "sw": lines["sw"]}))
+
+
 def main():
     args = parse()
     if args.steps is None:
@@ -465,6 +530,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "ga9":
+        run_ga9(args)
         return
     import numpy as np
     import torch
