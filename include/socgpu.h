@@ -240,7 +240,7 @@ typedef struct socgpu_control {
     int i_cloud;                /* SOCGPU_IP_CLOUD_CLEAR | SOCGPU_IP_CLOUD_MCICA */
     int i_cloud_representation; /* SOCGPU_IP_CLOUD_ICE_WATER with McICA */
     int i_gas_overlap;          /* SOCGPU_IP_OVERLAP_RANDOM | K_EQV_SCL (K_EQV, K_EQV_MOD alike) */
-    int i_direct_tau;           /* SOCGPU_IP_DIRECT_DELTA_SCALING (default) | NOSCALING */
+    int i_direct_tau;           /* SOCGPU_IP_DIRECT_DELTA_SCALING (default) | NOSCALING; CSR_SCALING refused */
     int l_rescale;              /* delta-rescaling of tau, omega and the phase function */
     int n_order_forward;        /* order of the forward-scattering term (2: f = g^2) */
     int l_ir_source_quad;       /* quadratic IR source */

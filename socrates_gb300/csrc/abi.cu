@@ -599,9 +599,8 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
   } else {
     set_msg(msg, msg_len, "unsupported scattering method %d", c->i_scatter_method); return SOCGPU_I_ERR_FATAL; }
   if (c->isolir == SOCGPU_IP_SOLAR && c->i_direct_tau != SOCGPU_IP_DIRECT_DELTA_SCALING &&
-      !(region && c->i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING)) {
-    set_msg(msg, msg_len, "only delta-scaled direct optical depths (i_direct_tau=1) are supported, and "
-            "unscaled ones (0) with cloud regions");
+      c->i_direct_tau != SOCGPU_IP_DIRECT_NOSCALING) {
+    set_msg(msg, msg_len, "only delta-scaled (i_direct_tau=1) and unscaled (0) direct optical depths are supported");
     return SOCGPU_I_ERR_FATAL;
   }
   if (c->l_rescale && c->n_order_forward < 1) {

@@ -152,7 +152,7 @@ struct SmemLayout {
   size_t off_phf_nc, off_fwd_nc, off_c_ke, off_c_ks, off_c_ka, off_c_phf, off_c_fwd;
   size_t off_wcld, off_frac, off_csub;
   size_t off_aux, off_lkf, off_lki, off_sbf, off_sbj, off_kscr;
-  size_t off_ovl, off_reg, off_regd, off_nct;
+  size_t off_ovl, off_reg, off_regd, off_nct, off_t0d;
   size_t off_acc;
   size_t bytes;
 };
@@ -224,6 +224,9 @@ __host__ __device__ inline SmemLayout make_layout(const FluxParams &p, int LP, i
   s.off_reg = region ? take((size_t)n_groups * kRegRows * (LP + 1)) : o;
   s.off_regd = region ? take_dbl((size_t)n_groups * kRegDRows * (LP + 1)) : o;
   s.off_nct = region ? take_int(4) : o;
+  // the direct beam without delta-scaling: each group's row of the layers'
+  // unscaled direct transmissions
+  s.off_t0d = (!lw && p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING && !region) ? take((size_t)n_groups * LP) : o;
   // per-group accumulator slices, offset by P words mod 32 so that the
   // groups of one warp land on different banks
   const int words = (int)(sizeof(R) / 4);
@@ -371,7 +374,7 @@ struct FluxKernel {
     R *phf_nc, *fwd_nc, *c_ke, *c_ks, *c_ka, *c_phf, *c_fwd, *wcld, *frac, *csub;
     R *aux, *lkf, *sbf, *kscr;
     int *lki, *sbj;
-    R *ovl, *reg;
+    R *ovl, *reg, *t0d;
     double *regd;
     int *nct;
     Acc *acc;
@@ -394,6 +397,7 @@ struct FluxKernel {
     s.kscr = (R *)(smem + l.off_kscr);
     s.ovl = (R *)(smem + l.off_ovl); s.reg = (R *)(smem + l.off_reg); s.nct = (int *)(smem + l.off_nct);
     s.regd = (double *)(smem + l.off_regd);
+    s.t0d = (R *)(smem + l.off_t0d);
     s.acc = (Acc *)(smem + l.off_acc);
     return s;
   }
@@ -1267,6 +1271,22 @@ struct FluxKernel {
     }
   }
 
+  // The direct transmission of a cell before delta-rescaling, exp(-tau sec0)
+  // (two_coeff.F90 trans_0_dir for ip_direct_noscaling).
+  __device__ static __forceinline__ R t0_unscaled(R kgt, R kg, R dm, R sec0) {
+    if constexpr (kFP64) return exp(-(kgt + kg) * dm * sec0);
+    else return expf(-(kgt + kg) * dm * sec0);
+  }
+  // adjust_solar_ke on a row of unscaled transmissions (k_eqv_scl, solar)
+  __device__ static __forceinline__ void fold_direct_row(const Smem &S, int bi, int max_abs, int r, int L, R *row) {
+    const R *a = S.aux + (size_t)bi * max_abs * LP;
+#pragma unroll
+    for (int jj = 0; jj < CH; ++jj) {
+      const int i = r * CH + jj, s = jj * P + r;
+      if (i < L) row[s] = row[s] * (kFP64 ? a[s] : R(1) + a[s]);
+    }
+  }
+
   // One g-point of one column (all its subcolumns under McICA).
   __device__ static void solve_gpoint(const FluxParams &p, const Smem &S, int col, int g, int bstart, int max_abs,
                                       R sec0, int r, Acc *acc, bool lw, bool active) {
@@ -1283,6 +1303,9 @@ struct FluxKernel {
     const R *dB_b = S.dB + (size_t)bi * LP, *dB2_b = S.dB2 + (size_t)bi * LP;
     const R f_inc_down = bs[0], f_inc_dir = bs[1], alb_diff = bs[2], alb_dir = bs[3], dB_surf = bs[4];
 
+    // the unscaled direct transmissions (i_direct_tau = ip_direct_noscaling)
+    R *t0d = (!lw && p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING && !p.region)
+                 ? S.t0d + (size_t)(threadIdx.x / P) * LP : nullptr;
     if (!MCICA) {
       // the gas absorption of the lane's layers first, while few registers
       // are live, then the coefficients
@@ -1295,14 +1318,19 @@ struct FluxKernel {
         if (i < L) {
           cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kgv[j], S.mass[s], asym_b[s], fwd_b[s], sec0,
                     T[j], Rf[j], T0[j], c1[j], c2[j], om[j]);
+          if (t0d) t0d[s] = t0_unscaled(kgt_b[s], kgv[j], S.mass[s], sec0);
         } else {
           T[j] = R(1); Rf[j] = R(0); T0[j] = R(1); c1[j] = R(0); c2[j] = R(0); om[j] = R(0);
+          if (t0d) t0d[s] = R(1);
         }
       }
       if constexpr (SRC == SOCGPU_IP_SOLAR)
-        if (p.keqv) fold_direct(S, bi, max_abs, r, L, T0, c2);
+        if (p.keqv) {
+          fold_direct(S, bi, max_abs, r, L, T0, c2);
+          if (t0d) fold_direct_row(S, bi, max_abs, r, L, t0d);
+        }
       solve_column(p, T, Rf, T0, c1, c2, om, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
-                   alb_diff, alb_dir, dB_surf, w_g, acc, active);
+                   alb_diff, alb_dir, dB_surf, w_g, acc, active, t0d);
     } else if (p.region) {
       solve_region(p, g, bstart, sec0, r, lw, active);
     } else {
@@ -1710,6 +1738,7 @@ struct FluxKernel {
                                      R alb_diff, R alb_dir, R dB_surf, R w_g, Acc *acc, int max_abs,
                                      bool active) {
     const int ndp = p.nd_profile, nc = p.n_condensed;
+    R *t0d = (!lw && p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING) ? S.t0d + (size_t)(threadIdx.x / P) * LP : nullptr;
     const R *kgt_b = S.kgt + (size_t)bi * LP, *kes_b = S.kes + (size_t)bi * LP;
     const R *kabs_b = S.kabs + (size_t)bi * LP, *asym_b = S.asym + (size_t)bi * LP;
     const R *fwd_b = S.fwd + (size_t)bi * LP, *amt_b = S.amt + (size_t)bi * max_abs * LP;
@@ -1769,12 +1798,13 @@ struct FluxKernel {
           if (!cloudy) {
             cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kg, S.mass[s], asym_b[s], fwd_b[s], sec0,
                       T[jj], Rf[jj], T0[jj], c1[jj], c2[jj], om[jj]);
+            if (t0d) t0d[s] = t0_unscaled(kgt_b[s], kg, S.mass[s], sec0);
           } else {
             // mcica_sample.F90:472-700 then mcica_column.F90:336-470: each
             // cloud type is the clear cell plus its components in order,
             // scaled by c_sub (one component per type for ice/water clouds,
             // both in type 1 for homogeneous clouds)
-            R sT = R(0), sR = R(0), sT0 = R(0), s1 = R(0), s2 = R(0), sO = R(0);
+            R sT = R(0), sR = R(0), sT0 = R(0), s1 = R(0), s2 = R(0), sO = R(0), sT0d = R(0);
             for (int t = 0; t < p.n_cloud_type; ++t) {
               const R fc = S.frac[(size_t)t * LP + s];
               if (!(cs_i * fc > R(0))) continue;
@@ -1802,17 +1832,23 @@ struct FluxKernel {
               cell_coef(p, kgt, kes, kab, kg, S.mass[s], asym, fwd, sec0, tT, tR, tT0, t1, t2, tO);
               sT = sT + fc * tT; sR = sR + fc * tR; sT0 = sT0 + fc * tT0;
               s1 = s1 + fc * t1; s2 = s2 + fc * t2; sO = sO + fc * tO;
+              if (t0d) sT0d = sT0d + fc * t0_unscaled(kgt, kg, S.mass[s], sec0);
             }
             T[jj] = sT; Rf[jj] = sR; T0[jj] = lw ? R(1) : sT0; c1[jj] = s1; c2[jj] = s2; om[jj] = sO;
+            if (t0d) t0d[s] = sT0d;
           }
         } else {
           T[jj] = R(1); Rf[jj] = R(0); T0[jj] = R(1); c1[jj] = R(0); c2[jj] = R(0); om[jj] = R(0);
+          if (t0d) t0d[s] = R(1);
         }
       }
       if constexpr (SRC == SOCGPU_IP_SOLAR)
-        if (p.keqv) fold_direct(S, bi, max_abs, r, L, T0, c2);
+        if (p.keqv) {
+          fold_direct(S, bi, max_abs, r, L, T0, c2);
+          if (t0d) fold_direct_row(S, bi, max_abs, r, L, t0d);
+        }
       solve_column(p, T, Rf, T0, c1, c2, om, r, L, lw, dB_b, dB2_b, f_inc_down, f_inc_dir,
-                   alb_diff, alb_dir, dB_surf, clear ? w_clr : w_sub, acc, use);
+                   alb_diff, alb_dir, dB_surf, clear ? w_clr : w_sub, acc, use, t0d);
     }
   }
 
@@ -1821,7 +1857,8 @@ struct FluxKernel {
   __device__ static void solve_column(const FluxParams &p, R (&T)[CH], R (&Rf)[CH], R (&T0)[CH],
                                       R (&c1)[CH], R (&c2)[CH], R (&om)[CH], int r, int L, bool lw,
                                       const R *dB_b, const R *dB2_b, R f_inc_down, R f_inc_dir,
-                                      R alb_diff, R alb_dir, R dB_surf, R w, Acc *acc, bool active) {
+                                      R alb_diff, R alb_dir, R dB_surf, R w, Acc *acc, bool active,
+                                      const R *t0d = nullptr) {
     // the last layer a lane accumulates into: none when the solve is discarded
     const int L_acc = active ? L : -1;
     Acc *acc_up = acc, *acc_dn = acc + (LP + 1), *acc_dir = acc + 2 * (LP + 1), *acc_div = acc + 3 * (LP + 1);
@@ -1854,7 +1891,31 @@ struct FluxKernel {
         c1[j] = su; c2[j] = sd;
         ssum[j] = su + sd;
         fd = fd * T0[j];
-        if (i < L_acc) acc_dir[j * P + r] += w * fd;
+        if (!t0d && i < L_acc) acc_dir[j * P + r] += w * fd;
+      }
+      if (t0d) {
+        // ip_direct_noscaling (solar_source.F90:157-176): the reported direct
+        // flux and the ground's direct reflection take the unscaled beam,
+        // the sources the scaled one
+        R pd = R(1);
+#pragma unroll
+        for (int j = 0; j < CH; ++j) pd *= t0d[j * P + r];
+        R incd = pd;
+#pragma unroll
+        for (int d = 1; d < P; d <<= 1) {
+          R y = __shfl_up_sync(0xffffffffu, incd, d, P);
+          if (r >= d) incd = y * incd;
+        }
+        R exd = __shfl_up_sync(0xffffffffu, incd, 1, P);
+        if (r == 0) exd = R(1);
+        R fdd = f_inc_dir * exd;
+        fdir_bottom = f_inc_dir * __shfl_sync(0xffffffffu, incd, P - 1, P);
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          const int i = r * CH + j;
+          fdd = fdd * t0d[j * P + r];
+          if (i < L_acc) acc_dir[j * P + r] += w * fdd;
+        }
       }
     } else {
 #pragma unroll

@@ -95,12 +95,7 @@ def test_cloud_regions_synthetic(gpu_lib, O, sps, solar, scheme, solver, represe
 
 
 def test_cloud_regions_refusals(gpu_lib, sps):
-    """The unscaled direct beam outside the cloud regions, and a solver of
-    another scheme, are refused."""
-    ctl, sp, col, _, _ = K.setup("sw_ds0_avg", sps)
-    with pytest.raises(R.RadianceError) as e:
-        R.radiance_calc(replace(ctl, i_cloud=abi.IP_CLOUD_CLEAR, i_solver=abi.IP_SOLVER_HOMOGEN_DIRECT), sp, col)
-    assert e.value.status == abi.I_ERR_FATAL and "i_direct_tau" in str(e.value)
+    """A solver of another scheme is refused."""
     ctl, sp, col, _, _ = K.setup("sw_avg", sps)
     with pytest.raises(R.RadianceError) as e:
         R.radiance_calc(replace(ctl, i_solver=abi.IP_SOLVER_HOMOGEN_DIRECT), sp, col)

@@ -43,7 +43,7 @@ def _state(run, sps, O, ice=False, n_col=1):
     return ctl, sp, col, m_gpu, kgo
 
 
-@pytest.mark.parametrize("run", [r for r in M.RUNS if r != "sw_ds0_avg"])
+@pytest.mark.parametrize("run", M.RUNS)
 def test_mcica5118_known_good_output_on_gpu(gpu_lib, O, sps, run):
     ctl, sp, col, m, kgo = _state(run, sps, O)
     ref = O.radiance_calc(ctl, sp, col, m)
@@ -72,11 +72,35 @@ def test_mcica5118_with_ice_on_gpu(gpu_lib, O, sps, run):
     assert_mixed_tolerance(gmx, {**ref, "heating_rate": circ6.heating_rate(ref, col.mass)}, f"{run} ice mixed: ")
 
 
-def test_unscaled_direct_beam_is_refused(gpu_lib, O, sps):
-    """The direct beam without delta-scaling (-ds 0, i_direct_tau = 0) is
-    not built in the kernels: the call fails with i_err_fatal and a message
-    (the oracle reproduces that run's known-good output)."""
-    ctl, sp, col, m, _ = _state("sw_ds0_avg", sps, O)
+def test_csr_scaled_direct_beam_is_refused(gpu_lib, O, sps):
+    """The direct beam scaled by the circumsolar correction (i_direct_tau = 2)
+    is not built in the kernels: the call fails with i_err_fatal and a
+    message."""
+    ctl, sp, col, m, _ = _state("sw_avg", sps, O)
     with pytest.raises(R.RadianceError) as e:
-        R.radiance_calc(ctl, sp, col, m)
+        R.radiance_calc(replace(ctl, i_direct_tau=abi.IP_DIRECT_CSR_SCALING), sp, col, m)
     assert e.value.status == abi.I_ERR_FATAL and "i_direct_tau" in str(e.value)
+
+
+@pytest.mark.parametrize("name,gas_overlap", [("hsw", abi.IP_OVERLAP_RANDOM), ("ga9sw", abi.IP_OVERLAP_K_EQV_SCL)])
+def test_unscaled_direct_beam_clear_sky(gpu_lib, O, name, gas_overlap):
+    """Clear sky with the direct beam not delta-scaled (i_direct_tau = 0):
+    HadGEM1 shortwave with random overlap and GA9 with k_eqv_scl and the
+    continuum, Rayleigh and a delta-rescaled aerosol mode, 97 columns of 60
+    layers, FP64 and mixed against the oracle, and the direct flux and the
+    ground's direct reflection differing from the scaled run."""
+    import cld7460 as K
+    from socrates_gb300 import synth
+    sp = K.spectra()[name]
+    col = synth.add_aerosol(synth.operational_case(sp, 97, 60, seed=67, solar=True), sp, seed=67)
+    col.rho_alb[:, 1, :] = 0.55 * col.rho_alb[:, 0, :] + 0.05       # direct albedos apart from the diffuse ones
+    ctl = R.sw_control(l_rayleigh=True, l_continuum=name == "ga9sw", l_aerosol_mode=True, l_rescale=True,
+                       i_gas_overlap=gas_overlap, i_direct_tau=abi.IP_DIRECT_NOSCALING, l_flux_div=False)
+    ref = O.radiance_calc(ctl, sp, col)
+    scaled = O.radiance_calc(replace(ctl, i_direct_tau=abi.IP_DIRECT_DELTA_SCALING), sp, col)
+    assert np.abs(ref["flux_direct"] - scaled["flux_direct"]).max() > 1.0
+    assert np.abs(ref["flux_up"] - scaled["flux_up"]).max() > 1e-2          # the ground's direct reflection
+    g64 = R.radiance_calc(replace(ctl, precision=abi.PRECISION_FP64), sp, col)
+    assert_fp64_parity({**g64, "mass": col.mass}, {**ref, "mass": col.mass}, "ds0 fp64: ")
+    gmx = R.radiance_calc(replace(ctl, precision=abi.PRECISION_MIXED), sp, col)
+    assert_mixed_tolerance(gmx, {**ref, "heating_rate": circ6.heating_rate(ref, col.mass)}, "ds0 mixed: ")
