@@ -1318,10 +1318,15 @@ struct FluxKernel {
         if (i < L) {
           cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kgv[j], S.mass[s], asym_b[s], fwd_b[s], sec0,
                     T[j], Rf[j], T0[j], c1[j], c2[j], om[j]);
-          if (t0d) t0d[s] = t0_unscaled(kgt_b[s], kgv[j], S.mass[s], sec0);
         } else {
           T[j] = R(1); Rf[j] = R(0); T0[j] = R(1); c1[j] = R(0); c2[j] = R(0); om[j] = R(0);
-          if (t0d) t0d[s] = R(1);
+        }
+      }
+      if (t0d) {
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          const int i = r * CH + j, s = j * P + r;
+          t0d[s] = i < L ? t0_unscaled(kgt_b[s], kgv[j], S.mass[s], sec0) : R(1);
         }
       }
       if constexpr (SRC == SOCGPU_IP_SOLAR)
@@ -1891,7 +1896,7 @@ struct FluxKernel {
         c1[j] = su; c2[j] = sd;
         ssum[j] = su + sd;
         fd = fd * T0[j];
-        if (!t0d && i < L_acc) acc_dir[j * P + r] += w * fd;
+        if (i < L_acc) acc_dir[j * P + r] += w * fd;
       }
       if (t0d) {
         // ip_direct_noscaling (solar_source.F90:157-176): the reported direct
@@ -1908,13 +1913,15 @@ struct FluxKernel {
         }
         R exd = __shfl_up_sync(0xffffffffu, incd, 1, P);
         if (r == 0) exd = R(1);
-        R fdd = f_inc_dir * exd;
+        R fdd = f_inc_dir * exd, fds = f_inc_dir * excl;
         fdir_bottom = f_inc_dir * __shfl_sync(0xffffffffu, incd, P - 1, P);
+        // the scaled beam is already in acc_dir: add the difference
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
           const int i = r * CH + j;
           fdd = fdd * t0d[j * P + r];
-          if (i < L_acc) acc_dir[j * P + r] += w * fdd;
+          fds = fds * T0[j];
+          if (i < L_acc) acc_dir[j * P + r] += w * (fdd - fds);
         }
       }
     } else {
