@@ -355,9 +355,10 @@ SOCGPU_API int socgpu_spectrum_load(const char *name, const char *path, socgpu_s
                                     char *msg, size_t msg_len);
 /* As socgpu_spectrum_load, with the lookup tables of block 5 read from k_path
    (NULL: path + "_k", read_spectrum.F90:1420-1560) and Wen-Yi Zhong's CO2
-   and O3 tables read from wenyi_path, a SOCRATES source file that defines
-   them (the module scale_wenyi, which the reference compiles in; NULL: none,
-   and spectra that scale with them are rejected when registered). */
+   and O3 tables read from wenyi_path, their data file (the reference
+   compiles the tables in, module scale_wenyi; socrates_gb300/wenyi.py
+   writes the data file from a SOCRATES source tree once; NULL: none, and
+   spectra that scale with them are rejected when registered). */
 SOCGPU_API int socgpu_spectrum_load_ext(const char *name, const char *path, const char *k_path,
                                         const char *wenyi_path, socgpu_spectrum_handle *handle, char *msg,
                                         size_t msg_len);
@@ -574,7 +575,10 @@ SOCGPU_API int socgpu_batch_destroy(socgpu_batch batch);
 
 /* The tile table (extension): read or set the entry for (precision, mode
  * 0 lwns / 1 full / 2 mcica, n_layer); lanes_per_solve 0 removes it.  Lets
- * a caller save the tuner's choices and restore them in a later process. */
+ * a caller save the tuner's choices and restore them in a later process.
+ * lanes_per_solve 1 is the phased kernel (modes 0 and 1, up to 256 layers);
+ * its layers_per_lane is the number of k-terms solved per batch (1..32) and
+ * its warps_per_cta at least 2. */
 SOCGPU_API int socgpu_tune_get(int precision, int mode, int n_layer, int *lanes_per_solve,
                                int *layers_per_lane, int *warps_per_cta);
 SOCGPU_API int socgpu_tune_set(int precision, int mode, int n_layer, int lanes_per_solve,
@@ -600,12 +604,19 @@ typedef struct socgpu_server_config {
     size_t device_bytes;        /* arena for request data; 0: half of the free device memory */
     int streams;                /* waves in flight; 0: 4 */
     int max_wave_requests;      /* requests per wave; 0: 256 */
+    /* Requests of at most this many column x g-points are "small": they are
+       waved apart from larger ones, on high-priority streams (half of the
+       streams, at least one when there are two or more), so that a large
+       request in flight does not hold them back.  0: 131072. */
+    long long small_column_gpoints;
 } socgpu_server_config;
 
 typedef struct socgpu_server_stats {
     long long submitted, completed, waves, max_wave_requests, queued;
     long long column_gpoints;   /* of the requests completed without error */
     size_t device_bytes, peak_bytes;
+    long long max_waves_in_flight;   /* most waves on the device at one time */
+    long long small_waves;           /* waves of small requests (high-priority streams) */
 } socgpu_server_stats;
 
 /* A request: the arguments of socgpu_radiance_calc, host pointers. */
@@ -641,7 +652,10 @@ SOCGPU_API int socgpu_set_device(int device);
 /* Fix the tile shape of one kernel family (extension, used by the tuner):
  * precision SOCGPU_PRECISION_*, mode 0 = infra-red without scattering,
  * 1 = full scattering, 2 = McICA; lanes_per_solve in {8 (mixed only), 16,
- * 32} lanes sharing one (column, g-point) solve; warps_per_cta in 1..8.
+ * 32} lanes sharing one (column, g-point) solve, or 1 for the phased kernel
+ * (one thread per k-term for the column's recurrences; modes 0 and 1: calls
+ * it does not cover -- equivalent extinction, the unscaled direct beam,
+ * more than 256 layers -- run on the scan kernels); warps_per_cta in 1..8.
  * Zeros restore the built-in choice. */
 SOCGPU_API int socgpu_set_tile_config(int precision, int mode, int lanes_per_solve, int warps_per_cta);
 

@@ -3,8 +3,9 @@
 Used by tests/, the smoke check and bench.py's CPU-baseline leg as the
 checker.  It feeds the oracle the same C structures the product library
 receives (socrates_gb300.radiance.Marshal), so both see identical inputs.
-Parity of this restatement is unpinned against reference-produced numbers:
-see socrates_oracle.h.
+The restatement is pinned to the reference's printed known-good outputs
+(ICRCCM case 27, CIRC case 6, the runes test, the McICA and cloud-region
+examples): see socrates_oracle.h.
 """
 from __future__ import annotations
 

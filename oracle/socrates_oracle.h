@@ -4,12 +4,17 @@
  * CPU-baseline leg of bench.py as the checker.  The product path never links
  * or calls it.
  *
- * Parity status: unpinned against reference-produced numbers.  The
- * reference (Fortran) has no compiler in this environment and its own
- * fixtures (CIRC, 7460_28, runes KGOs) need lookup-table k scaling, the
- * water-vapour continuum and k_eqv_scl overlap, which this restatement does
- * not implement.  The restatement is checked against analytic known-answer
- * cases instead (tests/test_oracle.py).
+ * Parity status: pinned to the reference's own known-good outputs.  The
+ * reference (Fortran) cannot be compiled here, but its example runs ship
+ * printed results, and this restatement reproduces them to half a unit of
+ * the printed last digit (tests/test_oracle.py): ICRCCM case 27 (HadCM3
+ * long wave, random overlap, continuum), CIRC case 6 with the GA7 long-wave
+ * file (lookup-table k, Wen-Yi terms, k_eqv_scl), the runes test with the
+ * GA9 files (solar and three thermal surfaces), the McICA example 5118_142
+ * (GA3.0 and GA7, long and short wave) and the cloud-region example 7460_28
+ * (HadGEM1 and GA9).  Parts no example exercises (the modal aerosol, the
+ * synthetic power-law spectra) are checked against analytic known answers
+ * and by reading against the reference source.
  */
 #ifndef SOCRATES_ORACLE_H
 #define SOCRATES_ORACLE_H

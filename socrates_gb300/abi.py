@@ -173,13 +173,15 @@ class BatchItem(C.Structure):
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("device_bytes", C.c_size_t), ("streams", C.c_int), ("max_wave_requests", C.c_int)]
+    _fields_ = [("device_bytes", C.c_size_t), ("streams", C.c_int), ("max_wave_requests", C.c_int),
+                ("small_column_gpoints", C.c_longlong)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("waves", C.c_longlong),
                 ("max_wave_requests", C.c_longlong), ("queued", C.c_longlong), ("column_gpoints", C.c_longlong),
-                ("device_bytes", C.c_size_t), ("peak_bytes", C.c_size_t)]
+                ("device_bytes", C.c_size_t), ("peak_bytes", C.c_size_t), ("max_waves_in_flight", C.c_longlong),
+                ("small_waves", C.c_longlong)]
 
 
 SERVER_PENDING = 100

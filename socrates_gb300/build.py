@@ -50,6 +50,13 @@ def units() -> list[tuple[Path, str, list[str]]]:
                         if prec == 1:
                             flags.append("-use_fast_math")
                         out.append((src, f"flux_{prec}_{mode}_{lanes}", flags))
+        elif src.name == "flux_phased.cu":
+            for prec in (0, 1):
+                for mode in (0, 1):
+                    flags = [f"-DSOCGPU_PREC={prec}", f"-DSOCGPU_MODE={mode}"]
+                    if prec == 1:
+                        flags.append("-use_fast_math")
+                    out.append((src, f"phased_{prec}_{mode}", flags))
         else:
             out.append((src, src.stem, PER_FILE.get(src.name, [])))
     return out
@@ -89,7 +96,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     BUILD.mkdir(exist_ok=True)
     todo = units()
     # the largest objects first, so the slowest compiles start early
-    todo.sort(key=lambda u: 0 if u[1].startswith("flux_") else 1)
+    todo.sort(key=lambda u: 0 if u[1].startswith(("flux_", "phased_")) else 1)
     jobs = min(len(todo), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda u: _compile(u, extra or []), todo))

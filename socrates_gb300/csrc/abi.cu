@@ -506,6 +506,9 @@ const FluxVariant kVariants[] = {
     SOCGPU_VARIANT(0, 2, 16), SOCGPU_VARIANT(0, 2, 32), SOCGPU_VARIANT(1, 0, 8),  SOCGPU_VARIANT(1, 0, 16),
     SOCGPU_VARIANT(1, 0, 32), SOCGPU_VARIANT(1, 1, 8),  SOCGPU_VARIANT(1, 1, 16), SOCGPU_VARIANT(1, 1, 32),
     SOCGPU_VARIANT(1, 2, 8),  SOCGPU_VARIANT(1, 2, 16), SOCGPU_VARIANT(1, 2, 32),
+    // the phased kernel: single-batch launches only
+    {0, 0, 1, launch_phased_0_0, nullptr}, {0, 1, 1, launch_phased_0_1, nullptr},
+    {1, 0, 1, launch_phased_1_0, nullptr}, {1, 1, 1, launch_phased_1_1, nullptr},
 };
 #undef SOCGPU_VARIANT
 }  // namespace
@@ -521,6 +524,17 @@ const FluxVariant *find_variant(int precision, int mode, int lanes) {
 std::mutex g_tile_mutex;
 int g_tile[2][3][2] = {};   // [precision][mode][lanes, warps]
 std::map<std::tuple<int, int, int>, TileConfig> g_tuned;
+
+// The built-in scan tile: 32 lanes above 64 layers (mixed) or above 128
+// layers (FP64), else 16; 8 warps; the smallest chunk covering the column.
+TileConfig scan_tile(int precision, int n_layer) {
+  TileConfig t{};
+  t.lanes_per_solve = precision == SOCGPU_PRECISION_MIXED ? (n_layer <= 64 ? 16 : 32) : (n_layer <= 128 ? 16 : 32);
+  t.warps_per_cta = 8;
+  while (t.lanes_per_solve < 32 && smallest_chunk(precision, t.lanes_per_solve, n_layer) == 0) t.lanes_per_solve *= 2;
+  t.chunk = smallest_chunk(precision, t.lanes_per_solve, n_layer);
+  return t;
+}
 
 TileConfig choose_tile(int precision, int mode, int n_layer) {
   TileConfig t{};
@@ -544,6 +558,8 @@ TileConfig choose_tile(int precision, int mode, int n_layer) {
     if (t.warps_per_cta <= 0) t.warps_per_cta = 8;
     t.chunk = 0;
   }
+  // the phased kernel's chunk is its k-term batch (0: the launcher's default)
+  if (t.lanes_per_solve == 1) return t;
   // the chunk must cover the column
   while (t.lanes_per_solve < 32 && smallest_chunk(precision, t.lanes_per_solve, n_layer) == 0)
     t.lanes_per_solve *= 2;
@@ -796,7 +812,10 @@ int mode_index(const socgpu_control *c) {
 int launch(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *msg, size_t msg_len) {
   const int mode = mode_index(c);
   TileConfig t = choose_tile(c->precision, mode, p.n_layer);
+  // options the phased kernel does not cover run on the scan kernels
+  if (t.lanes_per_solve == 1 && !phased_supported(p)) t = scan_tile(c->precision, p.n_layer);
   const FluxVariant *v = find_variant(c->precision, mode, t.lanes_per_solve);
+  if (v && t.lanes_per_solve == 1) return v->launch(p, t, st, msg, msg_len);
   if (!v || t.chunk == 0) {
     set_msg(msg, msg_len, "no kernel built for %d lanes per solve and %d layers", t.lanes_per_solve, p.n_layer);
     return SOCGPU_I_ERR_RANGE;
@@ -982,7 +1001,9 @@ struct Workspace {
   char *pinned = nullptr;          // page-locked staging for pageable caller arrays
   size_t pinned_cap = 0;
   int *range = nullptr;
+  std::vector<cudaEvent_t> events;  // per-chunk hand-offs of the pinned pipeline
   ~Workspace() {
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
     if (pinned) cudaFreeHost(pinned);
     if (buf) cudaFree(buf);
     if (range) cudaFree(range);
@@ -1009,6 +1030,8 @@ int ensure_workspace(size_t bytes, char *msg, size_t msg_len) {
     }
     if (tl_ws.shared_done) cudaEventDestroy(tl_ws.shared_done);
     tl_ws.shared_done = nullptr;
+    for (cudaEvent_t e : tl_ws.events) cudaEventDestroy(e);
+    tl_ws.events.clear();
     CUDA_TRY(cudaStreamCreateWithFlags(&tl_ws.stream, cudaStreamNonBlocking));
     for (cudaStream_t &a : tl_ws.aux) CUDA_TRY(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&tl_ws.shared_done, cudaEventDisableTiming));
@@ -1219,6 +1242,8 @@ int build_plan(socgpu_batch_s &b, char *msg, size_t msg_len) {
   std::map<std::tuple<int, int, int, int, int, int>, std::vector<int>> classes;
   for (size_t i = 0; i < b.params.size(); ++i) {
     TileConfig t = choose_tile(b.precision[i], b.mode[i], b.params[i].n_layer);
+    // the phased kernel has no persistent multi-batch form
+    if (t.lanes_per_solve == 1) t = scan_tile(b.precision[i], b.params[i].n_layer);
     classes[std::make_tuple(b.precision[i], b.mode[i], t.lanes_per_solve, t.chunk, t.warps_per_cta,
                             b.params[i].isolir)].push_back((int)i);
   }
@@ -1269,9 +1294,11 @@ int socgpu_set_device(int device) { return cudaSetDevice(device) == cudaSuccess 
 
 int socgpu_set_tile_config(int precision, int mode, int lanes_per_solve, int warps_per_cta) {
   if (precision < 0 || precision > 1 || mode < 0 || mode > 2) return SOCGPU_I_ERR_RANGE;
-  if (lanes_per_solve != 0 && lanes_per_solve != 8 && lanes_per_solve != 16 && lanes_per_solve != 32)
+  if (lanes_per_solve != 0 && lanes_per_solve != 1 && lanes_per_solve != 8 && lanes_per_solve != 16 &&
+      lanes_per_solve != 32)
     return SOCGPU_I_ERR_RANGE;
   if (precision == SOCGPU_PRECISION_FP64 && lanes_per_solve == 8) return SOCGPU_I_ERR_RANGE;
+  if (lanes_per_solve == 1 && mode == 2) return SOCGPU_I_ERR_RANGE;   // the phased kernel is clear-sky only
   if (warps_per_cta < 0 || warps_per_cta > 8) return SOCGPU_I_ERR_RANGE;
   std::lock_guard<std::mutex> lk(g_tile_mutex);
   g_tile[precision][mode][0] = lanes_per_solve;
@@ -1353,68 +1380,6 @@ int socgpu_radiance_calc_device(const socgpu_control *control, const socgpu_dime
   return launch(p, control, (cudaStream_t)stream, msg, msg_len);
 }
 
-// Page-locked caller arrays read and written in place by the kernel through
-// their mapped device addresses (on Grace the GPU reaches host memory over
-// NVLink-C2C), in place of the copy pipeline.  SOCGPU_HOST_ACCESS=direct
-// selects it, =copy the pipeline.
-constexpr int kDirectUnavailable = -1;
-
-bool host_access_direct() {
-  const char *e = std::getenv("SOCGPU_HOST_ACCESS");
-  return e && std::strcmp(e, "direct") == 0;
-}
-
-int direct_radiance_calc(const socgpu_control *control, const socgpu_dimen *dimen, socgpu_spectrum_handle spectrum,
-                         const socgpu_atm *atm, const socgpu_cld *cld, const socgpu_aer *aer,
-                         const socgpu_bound *bound, socgpu_radout *radout, cudaStream_t stream, char *msg,
-                         size_t msg_len) {
-  bool ok = true;
-  auto map = [&](auto *h) {
-    using T = std::remove_cv_t<std::remove_pointer_t<decltype(h)>>;
-    if (!h || !ok) return (T *)nullptr;
-    void *d = nullptr;
-    if (cudaHostGetDevicePointer(&d, (void *)h, 0) != cudaSuccess) { cudaGetLastError(); ok = false; }
-    return (T *)d;
-  };
-  socgpu_control c2 = *control;
-  c2.weight_band = map(control->weight_band);
-  socgpu_atm a2 = *atm;
-  a2.p = map(atm->p); a2.t = map(atm->t); a2.p_level = map(atm->p_level); a2.t_level = map(atm->t_level);
-  a2.mass = map(atm->mass); a2.gas_mix_ratio = map(atm->gas_mix_ratio); a2.density = map(atm->density);
-  socgpu_bound b2 = *bound;
-  b2.zen_0 = map(bound->zen_0); b2.solar_irrad = map(bound->solar_irrad); b2.rho_alb = map(bound->rho_alb);
-  b2.t_ground = map(bound->t_ground); b2.flux_ground = map(bound->flux_ground);
-  socgpu_aer e2{};
-  if (aer) {
-    e2 = *aer;
-    e2.mode_mix_ratio = map(aer->mode_mix_ratio); e2.mode_absorption = map(aer->mode_absorption);
-    e2.mode_scattering = map(aer->mode_scattering); e2.mode_asymmetry = map(aer->mode_asymmetry);
-  }
-  socgpu_cld k2{};
-  if (cld) {
-    k2 = *cld;   // the descriptors of the components stay host arrays
-    k2.condensed_mix_ratio = map(cld->condensed_mix_ratio); k2.condensed_dim_char = map(cld->condensed_dim_char);
-    k2.w_cloud = map(cld->w_cloud); k2.frac_cloud = map(cld->frac_cloud); k2.c_sub = map(cld->c_sub);
-    k2.frac_cloudy = map(cld->frac_cloudy); k2.n_subcol_cld = map(cld->n_subcol_cld);
-    k2.subcol_k = map(cld->subcol_k); k2.first_subcol_k = map(cld->first_subcol_k);
-    k2.subcol_reorder = map(cld->subcol_reorder);
-  }
-  socgpu_radout r2 = *radout;
-  r2.flux_up = map(radout->flux_up); r2.flux_down = map(radout->flux_down);
-  r2.flux_direct = map(radout->flux_direct); r2.flux_div = map(radout->flux_div);
-  r2.heating_rate = map(radout->heating_rate); r2.flux_up_band = map(radout->flux_up_band);
-  r2.flux_down_band = map(radout->flux_down_band);
-  if (!ok) return kDirectUnavailable;
-  int st = socgpu_radiance_calc_device(&c2, dimen, spectrum, &a2, cld ? &k2 : nullptr, aer ? &e2 : nullptr, &b2, &r2,
-                                       stream, msg, msg_len);
-  if (st != SOCGPU_I_NORMAL) return st;
-  if (cudaStreamSynchronize(stream) != cudaSuccess) {
-    set_msg(msg, msg_len, "radiance calculation failed: %s", cudaGetErrorString(cudaGetLastError()));
-    return SOCGPU_I_ABORT_CALCULATION;
-  }
-  return SOCGPU_I_NORMAL;
-}
-
 int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dimen, socgpu_spectrum_handle spectrum,
                          const socgpu_atm *atm, const socgpu_cld *cld, const socgpu_aer *aer,
                          const socgpu_bound *bound, socgpu_radout *radout, char *msg, size_t msg_len) {
@@ -1445,37 +1410,45 @@ int socgpu_radiance_calc(const socgpu_control *control, const socgpu_dimen *dime
     if (st != SOCGPU_I_NORMAL) sync_all();
     return st;
   }
-  if (host_access_direct()) {
-    st = direct_radiance_calc(control, dimen, spectrum, atm, cld, aer, bound, radout, tl_ws.stream, msg, msg_len);
-    if (st != kDirectUnavailable) return st;
-  }
-  // column chunks: copy in, compute and copy out of different chunks overlap;
-  // chunks of about pipeline_chunk_bytes(), at least 512 columns
+  // Column chunks of about pipeline_chunk_bytes() (at least 256 columns).
+  // Each stream has one role: the first copies every chunk in, back to back;
+  // the second runs a chunk's kernel once its copy has landed; the third
+  // copies a chunk's outputs back once its kernel is done.  Every column
+  // has its own place in the workspace, so no chunk waits for a buffer and
+  // the host link stays busy from the first copy to the last.
   const int np = atm->n_profile;
   size_t per_col = 0;
   for (const Slot &sl : call.plan.slots)
     if (sl.per_profile && sl.row_bytes) per_col += sl.rows * (sl.row_bytes / (size_t)np);
-  const size_t want = std::max<size_t>(512, pipeline_chunk_bytes() / std::max<size_t>(per_col, 1));
+  const size_t want = std::max<size_t>(256, pipeline_chunk_bytes() / std::max<size_t>(per_col, 1));
   const int chunk = (int)std::min<size_t>((size_t)np, want);
   const int n_chunk = (np + chunk - 1) / chunk;
-  // the arrays shared by all columns go first, on the first stream
-  st = call.copy_in_window(base, streams[0], 0, 0, true, msg, msg_len);
+  while (tl_ws.events.size() < 2 * (size_t)n_chunk) {
+    cudaEvent_t e = nullptr;
+    CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    tl_ws.events.push_back(e);
+  }
+  cudaStream_t s_in = streams[0], s_run = streams[1], s_out = streams[2];
+  // the arrays shared by all columns go first, ahead of chunk 0's columns
+  st = call.copy_in_window(base, s_in, 0, 0, true, msg, msg_len);
   if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
-  CUDA_TRY(cudaEventRecord(tl_ws.shared_done, streams[0]));
-  for (int k = 1; k < kPipe; ++k) CUDA_TRY(cudaStreamWaitEvent(streams[k], tl_ws.shared_done, 0));
   FluxParams p;
   call.params(base, p);
   for (int k = 0; k < n_chunk; ++k) {
     const int c0 = k * chunk, n = std::min(chunk, np - c0);
     if (n <= 0) break;
-    cudaStream_t sk = streams[k % kPipe];
-    st = call.copy_in_window(base, sk, c0, n, false, msg, msg_len);
+    cudaEvent_t landed = tl_ws.events[2 * k], done = tl_ws.events[2 * k + 1];
+    st = call.copy_in_window(base, s_in, c0, n, false, msg, msg_len);
     if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
+    CUDA_TRY(cudaEventRecord(landed, s_in));
+    CUDA_TRY(cudaStreamWaitEvent(s_run, landed, 0));
     FluxParams pk = p;
     window_params(pk, c0, n);
-    st = launch(pk, control, sk, msg, msg_len);
+    st = launch(pk, control, s_run, msg, msg_len);
     if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
-    st = call.copy_out_window(base, sk, c0, n, msg, msg_len);
+    CUDA_TRY(cudaEventRecord(done, s_run));
+    CUDA_TRY(cudaStreamWaitEvent(s_out, done, 0));
+    st = call.copy_out_window(base, s_out, c0, n, msg, msg_len);
     if (st != SOCGPU_I_NORMAL) { sync_all(); return st; }
   }
   for (cudaStream_t x : streams) CUDA_TRY(cudaStreamSynchronize(x));
@@ -1737,6 +1710,14 @@ int socgpu_tune_set(int precision, int mode, int n_layer, int lanes_per_solve, i
     return SOCGPU_I_ERR_RANGE;
   std::lock_guard<std::mutex> lk(g_tile_mutex);
   if (lanes_per_solve == 0) { g_tuned.erase(std::make_tuple(precision, mode, n_layer)); return SOCGPU_I_NORMAL; }
+  if (lanes_per_solve == 1) {
+    // the phased kernel: layers_per_lane is its k-term batch
+    if (mode == 2 || n_layer > kPhasedMaxLayers || layers_per_lane < 1 || layers_per_lane > 32 || warps_per_cta < 2 ||
+        warps_per_cta > 8)
+      return SOCGPU_I_ERR_RANGE;
+    g_tuned[std::make_tuple(precision, mode, n_layer)] = TileConfig{1, warps_per_cta, layers_per_lane};
+    return SOCGPU_I_NORMAL;
+  }
   const int *c = nullptr;
   const int n = chunk_list(precision, lanes_per_solve, &c);
   bool ok = false;

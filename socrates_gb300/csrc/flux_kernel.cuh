@@ -1889,6 +1889,9 @@ struct FluxKernel {
       R fd = f_inc_dir * excl;
       fdir_bottom = f_inc_dir * __shfl_sync(0xffffffffu, incl, P - 1, P);
       if (r == 0 && active) acc_dir[LP] += w * fd;
+      // the reported direct flux: the scaled beam here, or the unscaled one
+      // below (ip_direct_noscaling)
+      const int L_dir = t0d ? -1 : L_acc;
 #pragma unroll
       for (int j = 0; j < CH; ++j) {
         const int i = r * CH + j;
@@ -1896,7 +1899,7 @@ struct FluxKernel {
         c1[j] = su; c2[j] = sd;
         ssum[j] = su + sd;
         fd = fd * T0[j];
-        if (i < L_acc) acc_dir[j * P + r] += w * fd;
+        if (i < L_dir) acc_dir[j * P + r] += w * fd;
       }
       if (t0d) {
         // ip_direct_noscaling (solar_source.F90:157-176): the reported direct
@@ -1913,15 +1916,13 @@ struct FluxKernel {
         }
         R exd = __shfl_up_sync(0xffffffffu, incd, 1, P);
         if (r == 0) exd = R(1);
-        R fdd = f_inc_dir * exd, fds = f_inc_dir * excl;
+        R fdd = f_inc_dir * exd;
         fdir_bottom = f_inc_dir * __shfl_sync(0xffffffffu, incd, P - 1, P);
-        // the scaled beam is already in acc_dir: add the difference
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
           const int i = r * CH + j;
           fdd = fdd * t0d[j * P + r];
-          fds = fds * T0[j];
-          if (i < L_acc) acc_dir[j * P + r] += w * (fdd - fds);
+          if (i < L_acc) acc_dir[j * P + r] += w * fdd;
         }
       }
     } else {

@@ -49,6 +49,9 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
                  socgpu_radout *out, const double *weight_band_dev);
 int mode_index(const socgpu_control *c);
 TileConfig choose_tile(int precision, int mode, int n_layer);
+// The built-in tile of the scan kernels (flux_kernel), for launches the
+// phased kernel does not take (persistent multi-batch classes).
+TileConfig scan_tile(int precision, int n_layer);
 
 using LaunchFn = int (*)(const FluxParams &, const TileConfig &, cudaStream_t, char *, size_t);
 using PrepareFn = int (*)(BatchGroup &, char *, size_t);

@@ -6,7 +6,7 @@
 //   socgpu_run -s <spectral file> -R <first band> <last band> (-I | -S) -B <base>
 //              [-g <gas overlap>] [-c] [-r] [+R] [-q] [-t <two-stream scheme>]
 //              [-v <solver>] [-C <cloud scheme>] [-z <scatter method>]
-//              [-ds <direct tau>] [-P fp64|mixed] [-W <scale_wenyi source>]
+//              [-ds <direct tau>] [-P fp64|mixed] [-W <Wen-Yi tables file>]
 //              [-C 10 -K <cloud representation> -d <droplet type> -i <ice type>
 //               -m <condensate relative std. deviation> +m <sampling> -dp <decorrelation scale>]
 //   socgpu_run --convert <in> <out.cdf|out.cdl>
@@ -27,8 +27,9 @@
 // McICA data file beside the spectral file (l_run_cdf.F90:998-1010,
 // 1281-1296).
 // Lookup tables are read from the spectral file's '_k' companion; spectral
-// files with Wen-Yi CO2 terms (GA7 and GA9 long wave) need -W, the SOCRATES
-// source file that defines those tables (the reference compiles them in).
+// files with Wen-Yi CO2 terms (GA7 and GA9 long wave) need -W, the data file
+// of those tables (the reference compiles them in; socrates_gb300/wenyi.py
+// converts them from a SOCRATES source tree once).
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -267,7 +268,7 @@ int main(int argc, char **argv) {
     if (!(to_cdf ? socgpu::write_cdf(a[2], f, err) : socgpu::write_cdl(a[2], f, err))) return die(err);
     return 0;
   }
-  std::string sp_file, base, wenyi_file;   // -W: the Wen-Yi tables (SOCRATES's scale_wenyi source)
+  std::string sp_file, base, wenyi_file;   // -W: the Wen-Yi tables' data file
   int first = 0, last = 0, isolir = 0, overlap = 0, two_stream = 0, solver = 0, cloud = SOCGPU_IP_CLOUD_CLEAR;
   int scatter = SOCGPU_IP_SCATTER_FULL, direct_tau = SOCGPU_IP_DIRECT_DELTA_SCALING;
   bool cont = false, rayleigh = false, rescale = false, quad = false, gas = false;

@@ -3,20 +3,29 @@
 // Requests are radiance_calc calls with host arrays.  Every request's inputs
 // and outputs live in one device arena, sized at creation, while the request
 // is in flight.  One scheduler thread runs this loop:
-//   * it retires finished waves: their requests are marked done and their
-//     arena blocks freed;
+//   * it retires finished requests one by one (each has its own event,
+//     recorded after its outputs are copied back): they are marked done and
+//     their arena blocks freed; a stream slot is free again when all of its
+//     wave's requests are;
 //   * when a stream slot is free, it admits queued requests in arrival order
 //     for as long as their blocks fit the arena (admission by free device
 //     memory), up to max_wave_requests, and launches them as one wave.
-// A wave copies its inputs in, runs one persistent batched launch per
-// kernel class (precision, mode, tile), copies the results out and records
-// an event, all on its stream slot's stream.  Up to `streams` waves are in
-// flight at once, so requests that arrive while others run are admitted as
-// soon as a slot and memory free up, and their work overlaps on the device.
-// The spectra stay device resident in the library's registry.  Requests
-// whose host arrays are page-locked are copied asynchronously on the wave's
-// stream; pageable ones synchronously, in before the wave's kernels and out
-// when the wave is retired.
+// Requests are of two size classes.  Small ones (at most
+// small_column_gpoints column x g-points) are waved on high-priority streams
+// and large ones on low-priority streams (a low-priority slot takes small
+// requests only when no large one waits), so that a small request never
+// shares a wave with a large one.  Each kernel class of a wave (precision,
+// mode, tile) is one launch of the batched kernel with one CTA per column: as
+// the CTAs of a large wave retire, the block scheduler gives the SMs to the
+// pending CTAs of high-priority streams first, so a small request that
+// arrives during a large one waits for a few columns' worth of work, not for
+// the whole wave.  Up to `streams` waves are in flight at once, so requests
+// that arrive while others run are admitted as soon as a slot and memory
+// free up, and their work overlaps on the device.  The spectra stay device
+// resident in the library's registry.  Requests whose host arrays are
+// page-locked are copied asynchronously on the wave's stream; pageable ones
+// synchronously, in before the wave's kernels and out when the request is
+// retired.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -114,10 +123,12 @@ struct Request {
 
 struct StreamSlot {
   cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
+  bool high = false;                  // high priority: waves of small requests
+  std::vector<cudaEvent_t> done;      // one per request of the wave, in wave order
   FluxParams *d_items = nullptr, *h_items = nullptr;     // per-wave kernel tables
   long long *d_start = nullptr, *h_start = nullptr;
   bool busy = false;
+  size_t n_retired = 0;               // requests of the wave already retired (in order)
   std::vector<Request *> reqs;
 };
 
@@ -132,6 +143,7 @@ struct socgpu_server_s {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Request *> pending;
+  long long small_colg = 0;
   std::unordered_map<long long, std::unique_ptr<Request>> requests;
   long long next_ticket = 1;
   bool stop = false;
@@ -158,31 +170,49 @@ int copy_sync(const Request &r, char *base, bool out, char *msg, size_t msg_len)
   return SOCGPU_I_NORMAL;
 }
 
-// Retire a finished wave (called with the server mutex held).
-void finish(socgpu_server_s &S, StreamSlot &sl, cudaError_t e) {
-  for (Request *r : sl.reqs) {
-    if (e == cudaSuccess && r->status == SOCGPU_I_NORMAL && !r->pinned) {
-      char m[256] = "";
-      if (copy_sync(*r, S.dmem + r->off, true, m, sizeof(m)) != SOCGPU_I_NORMAL) {
-        r->status = SOCGPU_I_ABORT_CALCULATION;
-        r->msg = m;
-      }
-    }
-  }
-  const Clock::time_point now = Clock::now();
-  for (Request *r : sl.reqs) {
-    r->t_done = now;
-    if (e != cudaSuccess && r->status == SOCGPU_I_NORMAL) {
+// Retire one finished request of a wave (called with the server mutex held).
+void finish(socgpu_server_s &S, Request *r, cudaError_t e) {
+  if (e == cudaSuccess && r->status == SOCGPU_I_NORMAL && !r->pinned) {
+    char m[256] = "";
+    if (copy_sync(*r, S.dmem + r->off, true, m, sizeof(m)) != SOCGPU_I_NORMAL) {
       r->status = SOCGPU_I_ABORT_CALCULATION;
-      r->msg = std::string("wave failed on the device: ") + cudaGetErrorString(e);
+      r->msg = m;
     }
-    r->done = true;
-    S.arena.release(r->off, r->bytes);
-    S.stats.completed += 1;
-    if (r->status == SOCGPU_I_NORMAL) S.stats.column_gpoints += r->colg;
   }
-  sl.reqs.clear();
-  sl.busy = false;
+  r->t_done = Clock::now();
+  if (e != cudaSuccess && r->status == SOCGPU_I_NORMAL) {
+    r->status = SOCGPU_I_ABORT_CALCULATION;
+    r->msg = std::string("wave failed on the device: ") + cudaGetErrorString(e);
+  }
+  r->done = true;
+  S.arena.release(r->off, r->bytes);
+  S.stats.completed += 1;
+  if (r->status == SOCGPU_I_NORMAL) S.stats.column_gpoints += r->colg;
+}
+
+// Retire the requests of a wave whose events have fired, in wave order;
+// the slot is free once all are retired.  Returns whether any was retired.
+bool retire(socgpu_server_s &S, StreamSlot &sl) {
+  bool any = false;
+  while (sl.n_retired < sl.reqs.size()) {
+    cudaError_t e = cudaEventQuery(sl.done[sl.n_retired]);
+    if (e == cudaErrorNotReady) break;
+    finish(S, sl.reqs[sl.n_retired], e);
+    ++sl.n_retired;
+    any = true;
+  }
+  if (sl.n_retired == sl.reqs.size()) {
+    sl.reqs.clear();
+    sl.n_retired = 0;
+    sl.busy = false;
+  }
+  return any;
+}
+
+// Every request's event of a wave that stops early (on the slot's stream,
+// after whatever was enqueued).
+void record_all(StreamSlot &sl) {
+  for (size_t i = 0; i < sl.reqs.size(); ++i) cudaEventRecord(sl.done[i], sl.stream);
 }
 
 void fail_all(std::vector<Request *> &wave, int status, const char *msg) {
@@ -208,7 +238,7 @@ void launch_wave(socgpu_server_s &S, StreamSlot &sl) {
     if ((r->pinned ? r->call.copy_in(S.dmem + r->off, st, msg, msg_len)
                    : copy_sync(*r, S.dmem + r->off, false, msg, msg_len)) != SOCGPU_I_NORMAL) {
       fail_all(wave, SOCGPU_I_ABORT_CALCULATION, msg);
-      cudaEventRecord(sl.done, st);
+      record_all(sl);
       return;
     }
   // kernel classes of the wave
@@ -219,6 +249,7 @@ void launch_wave(socgpu_server_s &S, StreamSlot &sl) {
     r->call.params(S.dmem + r->off, params[i]);
     const int mode = mode_index(&r->control);
     TileConfig t = choose_tile(r->control.precision, mode, r->atm.n_layer);
+    if (t.lanes_per_solve == 1) t = scan_tile(r->control.precision, r->atm.n_layer);
     classes[std::make_tuple(r->control.precision, mode, t.lanes_per_solve, t.chunk, t.warps_per_cta,
                             r->control.isolir)].push_back((int)i);
   }
@@ -247,9 +278,12 @@ void launch_wave(socgpu_server_s &S, StreamSlot &sl) {
     if (!v || v->prepare(g, msg, msg_len) != SOCGPU_I_NORMAL) {
       if (!v) snprintf(msg, msg_len, "no kernel built for %d lanes per solve", g.tile.lanes_per_solve);
       fail_all(wave, SOCGPU_I_ERR_RANGE, msg);
-      cudaEventRecord(sl.done, st);
+      record_all(sl);
       return;
     }
+    // one CTA per column (not the persistent grid): CTAs retire column by
+    // column, so higher-priority streams get SMs as they do
+    g.grid = (int)std::min<long long>(g.total, 0x7fffffffLL);
     groups.push_back(g);
     table_off.emplace_back(n_item, n_start);
     n_item += k;
@@ -272,53 +306,66 @@ void launch_wave(socgpu_server_s &S, StreamSlot &sl) {
   if (e != cudaSuccess) {
     cudaGetLastError();
     fail_all(wave, SOCGPU_I_ABORT_CALCULATION, cudaGetErrorString(e));
-    cudaEventRecord(sl.done, st);
+    record_all(sl);
     return;
   }
-  for (Request *r : wave)
-    if (r->pinned && r->call.copy_out(S.dmem + r->off, st, msg, msg_len) != SOCGPU_I_NORMAL)
-      fail_all(wave, SOCGPU_I_ABORT_CALCULATION, msg);
-  cudaEventRecord(sl.done, st);
+  // each request's outputs, then its own event
+  for (size_t i = 0; i < wave.size(); ++i) {
+    Request *r = wave[i];
+    if (r->pinned && r->status == SOCGPU_I_NORMAL &&
+        r->call.copy_out(S.dmem + r->off, st, msg, msg_len) != SOCGPU_I_NORMAL) {
+      r->status = SOCGPU_I_ABORT_CALCULATION;
+      r->msg = msg;
+    }
+    cudaEventRecord(sl.done[i], st);
+  }
 }
 
 void worker_main(socgpu_server_s *Sp) {
   socgpu_server_s &S = *Sp;
   cudaSetDevice(S.device);
   std::unique_lock<std::mutex> lk(S.mu);
+  // Take queued requests of one size class for a wave, in arrival order,
+  // while their blocks fit the arena.
+  auto take = [&](bool small, std::vector<Request *> &wave) {
+    for (auto it = S.pending.begin(); it != S.pending.end() && (int)wave.size() < S.cfg.max_wave_requests;) {
+      Request *r = *it;
+      if ((r->colg <= S.small_colg) != small) { ++it; continue; }
+      size_t off = 0;
+      if (!S.arena.alloc(r->bytes, &off)) break;
+      r->off = off;
+      wave.push_back(r);
+      it = S.pending.erase(it);
+    }
+  };
   for (;;) {
     bool progressed = false;
-    for (StreamSlot &sl : S.slots) {
-      if (!sl.busy) continue;
-      cudaError_t e = cudaEventQuery(sl.done);
-      if (e == cudaErrorNotReady) continue;
-      finish(S, sl, e);
-      progressed = true;
-    }
-    if (progressed) S.cv_done.notify_all();
-    StreamSlot *free_slot = nullptr;
     for (StreamSlot &sl : S.slots)
-      if (!sl.busy) { free_slot = &sl; break; }
-    if (free_slot && !S.pending.empty()) {
+      if (sl.busy) progressed |= retire(S, sl);
+    if (progressed) S.cv_done.notify_all();
+    for (StreamSlot &sl : S.slots) {
+      if (sl.busy || S.pending.empty()) continue;
       std::vector<Request *> wave;
-      while (!S.pending.empty() && (int)wave.size() < S.cfg.max_wave_requests) {
-        Request *r = S.pending.front();
-        size_t off = 0;
-        if (!S.arena.alloc(r->bytes, &off)) break;
-        r->off = off;
-        wave.push_back(r);
-        S.pending.pop_front();
-      }
-      if (!wave.empty()) {
-        free_slot->busy = true;
-        free_slot->reqs = std::move(wave);
-        S.stats.waves += 1;
-        S.stats.max_wave_requests = std::max<long long>(S.stats.max_wave_requests, (long long)free_slot->reqs.size());
-        S.stats.peak_bytes = S.arena.peak();
-        lk.unlock();
-        launch_wave(S, *free_slot);
-        lk.lock();
-        progressed = true;
-      }
+      // high-priority slots take small requests; the others large ones
+      // first, and small ones when no large request waits
+      bool small = sl.high;
+      take(small, wave);
+      if (wave.empty() && !sl.high) { small = true; take(true, wave); }
+      if (wave.empty()) continue;
+      sl.busy = true;
+      sl.n_retired = 0;
+      sl.reqs = std::move(wave);
+      S.stats.waves += 1;
+      if (small) S.stats.small_waves += 1;
+      S.stats.max_wave_requests = std::max<long long>(S.stats.max_wave_requests, (long long)sl.reqs.size());
+      S.stats.peak_bytes = S.arena.peak();
+      long long in_flight = 0;
+      for (const StreamSlot &x : S.slots) in_flight += x.busy;
+      S.stats.max_waves_in_flight = std::max(S.stats.max_waves_in_flight, in_flight);
+      lk.unlock();
+      launch_wave(S, sl);
+      lk.lock();
+      progressed = true;
     }
     bool any_busy = false;
     for (StreamSlot &sl : S.slots) any_busy |= sl.busy;
@@ -338,7 +385,8 @@ void worker_main(socgpu_server_s *Sp) {
 void destroy_server(socgpu_server_s *S) {
   for (StreamSlot &sl : S->slots) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
-    if (sl.done) cudaEventDestroy(sl.done);
+    for (cudaEvent_t e : sl.done)
+      if (e) cudaEventDestroy(e);
     if (sl.stream) cudaStreamDestroy(sl.stream);
     if (sl.d_items) cudaFree(sl.d_items);
     if (sl.d_start) cudaFree(sl.d_start);
@@ -365,6 +413,8 @@ int socgpu_server_create(const socgpu_server_config *config, socgpu_server *serv
   }
   std::unique_ptr<socgpu_server_s> S(new socgpu_server_s);
   CUDA_TRY(cudaGetDevice(&S->device));
+  int prio_low = 0, prio_high = 0;
+  CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
   if (cfg.device_bytes == 0) {
     size_t free_b = 0, total_b = 0;
     CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
@@ -379,13 +429,21 @@ int socgpu_server_create(const socgpu_server_config *config, socgpu_server *serv
     set_msg(msg, msg_len, "device arena of %zu bytes not available: %s", cfg.device_bytes, cudaGetErrorString(e));
     return SOCGPU_I_ERR_RANGE;
   }
+  S->small_colg = cfg.small_column_gpoints > 0 ? cfg.small_column_gpoints : (1LL << 17);
   S->slots.resize(cfg.streams);
   const size_t n_items = cfg.max_wave_requests;
   // a wave has at most one kernel class per request, so n_items + 1 starts per class fit in 2 n_items + 1
   const size_t n_start = 2 * n_items + 1;
-  for (StreamSlot &sl : S->slots) {
-    if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess ||
+  const int n_high = cfg.streams >= 2 ? cfg.streams / 2 : 0;
+  for (size_t q = 0; q < S->slots.size(); ++q) {
+    StreamSlot &sl = S->slots[q];
+    sl.high = (int)q < n_high;
+    sl.done.assign(n_items, nullptr);
+    bool ok = true;
+    for (cudaEvent_t &e : sl.done) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok ||
+        cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, sl.high ? prio_high : prio_low) !=
+            cudaSuccess ||
         cudaMalloc(&sl.d_items, sizeof(FluxParams) * n_items) != cudaSuccess ||
         cudaMalloc(&sl.d_start, sizeof(long long) * n_start) != cudaSuccess ||
         cudaMallocHost(&sl.h_items, sizeof(FluxParams) * n_items) != cudaSuccess ||

@@ -270,6 +270,25 @@ SOCGPU_DECL_FLUX_MODES(1, 32)
 #undef SOCGPU_DECL_FLUX_MODES
 #undef SOCGPU_DECL_FLUX
 
+// The phased kernel (flux_phased.cu), one launcher per (precision, mode
+// 0 lwns / 1 full); its tile is lanes_per_solve = 1, chunk = k-terms per batch.
+#define SOCGPU_DECL_PHASED(prec, mode)                                                                  \
+  int launch_phased_##prec##_##mode(const FluxParams &p, const TileConfig &cfg, cudaStream_t s, char *msg, \
+                                    size_t len);
+SOCGPU_DECL_PHASED(0, 0)
+SOCGPU_DECL_PHASED(0, 1)
+SOCGPU_DECL_PHASED(1, 0)
+SOCGPU_DECL_PHASED(1, 1)
+#undef SOCGPU_DECL_PHASED
+
+// Whether the phased kernel covers a launch: clear sky, no equivalent
+// extinction, the direct beam delta-scaled, at most 256 layers.
+constexpr int kPhasedMaxLayers = 256;
+inline bool phased_supported(const FluxParams &p) {
+  return !p.mcica && !p.keqv && p.n_layer <= kPhasedMaxLayers &&
+         !(p.isolir == SOCGPU_IP_SOLAR && p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING);
+}
+
 void count_launch();
 
 }  // namespace socgpu

@@ -333,79 +333,43 @@ bool read_k_file(const std::string &path, SpectralFile &s, const std::vector<std
   return true;
 }
 
-// Wen-Yi Zhong's CO2 (band 4) and O3 (band 6) tables from a SOCRATES source
-// file that defines them (the module scale_wenyi), which the reference
-// compiles in.  The band tables are assembled as RESHAPE(..., ORDER=(3, 2,
-// 1)) builds them: one source array per temperature, the k-term index fastest.
+// Wen-Yi Zhong's CO2 (band 4) and O3 (band 6) tables from their data file
+// (socrates_gb300/wenyi.py writes it from the reference's scale_wenyi
+// module): a header line "socgpu-wenyi-tables 1", then the arrays plg (26),
+// ttb (10), tto (9), gk250b (n4), gk4 (10 x 26 x n4) and gk6 (9 x 26 x n6),
+// each as "<name> <dims...>" followed by its values, first index fastest.
 bool read_wenyi(const std::string &path, SpectralFile &s, std::string &err) {
   std::ifstream in(path);
   if (!in) { err = "cannot open the Wen-Yi tables " + path; return false; }
-  std::stringstream ss;
-  ss << in.rdbuf();
-  std::string text = ss.str();
-  std::map<std::string, std::vector<double>> arrays;
-  size_t pos = 0;
-  while ((pos = text.find("PARAMETER", pos)) != std::string::npos) {
-    size_t colon = text.find("::", pos), open = text.find("(/", pos), close = text.find("/)", pos);
-    pos += 9;
-    if (colon == std::string::npos || open == std::string::npos || close == std::string::npos || open > close)
-      continue;
-    std::string decl = text.substr(colon + 2, open - colon - 2);
-    size_t paren = decl.find('(');
-    if (paren == std::string::npos || decl.find("RESHAPE") != std::string::npos) continue;
-    std::string name = decl.substr(0, paren);
-    name.erase(0, name.find_first_not_of(" \t"));
-    name.erase(name.find_last_not_of(" \t") + 1);
-    for (char &c : name) c = (char)std::tolower((unsigned char)c);
-    const size_t declared = (size_t)std::atol(decl.c_str() + paren + 1);
-    std::string body = text.substr(open + 2, close - open - 2);
-    std::vector<double> vals;
-    size_t b = 0;
-    while ((b = body.find("_RealK", b)) != std::string::npos) {
-      size_t a = b;
-      while (a > 0 && (std::isdigit((unsigned char)body[a - 1]) || body[a - 1] == '.' || body[a - 1] == 'E' ||
-                       body[a - 1] == 'e' || body[a - 1] == 'D' || body[a - 1] == 'd' ||
-                       ((body[a - 1] == '-' || body[a - 1] == '+') && a > 1 &&
-                        (body[a - 2] == 'E' || body[a - 2] == 'e' || body[a - 2] == 'D' || body[a - 2] == 'd' ||
-                         !std::isalnum((unsigned char)body[a - 2])))))
-        --a;
-      std::string num_s = body.substr(a, b - a);
-      for (char &c : num_s)
-        if (c == 'D' || c == 'd') c = 'E';
-      vals.push_back(std::strtod(num_s.c_str(), nullptr));
-      b += 6;
-    }
-    if (vals.size() != declared) { err = path + ": " + name + " has the wrong number of values"; return false; }
-    arrays[name] = vals;
-    pos = close;
-  }
-  auto need = [&](const std::string &n) -> const std::vector<double> * {
-    auto it = arrays.find(n);
-    return it == arrays.end() ? nullptr : &it->second;
-  };
-  const auto *plg = need("plg"), *ttb = need("ttb"), *tto = need("tto"), *g250 = need("gk250b");
-  if (!plg || !ttb || !tto || !g250 || plg->size() != 26 || ttb->size() != 10 || tto->size() != 9) {
-    err = path + ": the Wen-Yi grids are missing";
+  std::string magic, version;
+  in >> magic >> version;
+  if (magic != "socgpu-wenyi-tables" || version != "1") {
+    err = path + ": not a Wen-Yi tables file (no 'socgpu-wenyi-tables 1' header)";
     return false;
   }
-  auto table = [&](const std::string &prefix, int n_t, std::vector<double> &out) -> bool {
-    const auto *first_t = need(prefix + "_1");
-    if (!first_t || first_t->size() % 26) return false;
-    const size_t n_term = first_t->size() / 26;
-    out.assign((size_t)n_t * 26 * n_term, 0.0);
-    for (int t = 0; t < n_t; ++t) {
-      const auto *a = need(prefix + "_" + std::to_string(t + 1));
-      if (!a || a->size() != 26 * n_term) return false;
-      for (size_t p = 0; p < 26; ++p)
-        for (size_t k = 0; k < n_term; ++k) out[(size_t)t + (size_t)n_t * (p + 26 * k)] = (*a)[p * n_term + k];
+  struct Want { const char *name; int ndim; std::vector<double> *dst; std::vector<long> dims; };
+  Want want[] = {{"plg", 1, &s.wy_plg, {}}, {"ttb", 1, &s.wy_ttb, {}}, {"tto", 1, &s.wy_tto, {}},
+                 {"gk250b", 1, &s.wy_gk250b, {}}, {"gk4", 3, &s.wy_gk4, {}}, {"gk6", 3, &s.wy_gk6, {}}};
+  for (Want &w : want) {
+    std::string name;
+    in >> name;
+    if (name != w.name) { err = path + ": expected the array '" + w.name + "'"; return false; }
+    size_t n = 1;
+    for (int d = 0; d < w.ndim; ++d) {
+      long v = 0;
+      in >> v;
+      if (!in || v < 1 || v > 4096) { err = path + ": bad dimensions of '" + name + "'"; return false; }
+      w.dims.push_back(v);
+      n *= (size_t)v;
     }
-    return true;
-  };
-  if (!table("gk4", 10, s.wy_gk4) || !table("gk6", 9, s.wy_gk6)) {
-    err = path + ": the Wen-Yi k tables are incomplete";
-    return false;
+    w.dst->assign(n, 0.0);
+    for (size_t q = 0; q < n; ++q) in >> (*w.dst)[q];
+    if (!in) { err = path + ": '" + name + "' is short of values"; return false; }
   }
-  s.wy_plg = *plg; s.wy_ttb = *ttb; s.wy_tto = *tto; s.wy_gk250b = *g250;
+  const bool ok = want[0].dims[0] == 26 && want[1].dims[0] == 10 && want[2].dims[0] == 9 &&
+                  want[4].dims[0] == 10 && want[4].dims[1] == 26 && want[4].dims[2] == want[3].dims[0] &&
+                  want[5].dims[0] == 9 && want[5].dims[1] == 26;
+  if (!ok) { err = path + ": the Wen-Yi tables have the wrong shapes"; return false; }
   return true;
 }
 

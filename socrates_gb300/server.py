@@ -15,9 +15,10 @@ from .radiance import Marshal, RadianceError, load_library, register_spectrum
 
 
 class Server:
-    def __init__(self, device_bytes: int = 0, streams: int = 4, max_wave_requests: int = 256):
+    def __init__(self, device_bytes: int = 0, streams: int = 4, max_wave_requests: int = 256,
+                 small_column_gpoints: int = 0):
         self.lib = load_library()
-        cfg = abi.ServerConfig(device_bytes, streams, max_wave_requests)
+        cfg = abi.ServerConfig(device_bytes, streams, max_wave_requests, small_column_gpoints)
         self.handle = C.c_void_p()
         msg = C.create_string_buffer(512)
         st = self.lib.socgpu_server_create(C.byref(cfg), C.byref(self.handle), msg, 512)

@@ -47,31 +47,11 @@ def _fields13(line):
 
 
 def read_wenyi_tables(path) -> dict:
-    """The CO2 (band 4) and O3 (band 6) tables of ip_scale_wenyi from a
-    SOCRATES source file that defines them (the module scale_wenyi): the
-    reference compiles them in, so a caller reads them from its own SOCRATES
-    installation and passes them with the spectral data.  The band-4 and
-    band-6 tables are assembled as their RESHAPE(..., ORDER=(3, 2, 1)) builds
-    them: one source array per temperature, the k-term index fastest."""
-    import re
-    text = Path(path).read_text()
-    arrays = {}
-    for m in re.finditer(r"PARAMETER\s*::\s*(\w+)\(\s*(\d+)\s*\)\s*=\s*\(/(.*?)/\)", text, re.S):
-        body = re.sub(r"!.*", "", m.group(3))
-        vals = [float(v.split("_")[0].replace("D", "E").replace("d", "e"))
-                for v in re.findall(r"[-+]?\d+\.?\d*(?:[EeDd][-+]?\d+)?_RealK", body)]
-        if len(vals) != int(m.group(2)):
-            raise ValueError(f"{path}: {m.group(1)} has {len(vals)} values, declared {m.group(2)}")
-        arrays[m.group(1).lower()] = np.array(vals)
-
-    def table(prefix, n_t):
-        parts = [arrays[f"{prefix}_{i}"] for i in range(1, n_t + 1)]
-        n_term = parts[0].size // 26
-        return np.asfortranarray(np.stack([p.reshape(26, n_term) for p in parts], axis=0))
-
-    return dict(wenyi_plg=arrays["plg"], wenyi_ttb=arrays["ttb"], wenyi_tto=arrays["tto"],
-                wenyi_gk250b=arrays["gk250b"], wenyi_gk4=table("gk4", arrays["ttb"].size),
-                wenyi_gk6=table("gk6", arrays["tto"].size))
+    """The CO2 (band 4) and O3 (band 6) tables of ip_scale_wenyi from their
+    data file (socrates_gb300.wenyi: the reference compiles the tables into
+    its source; the converter there writes them out once as data)."""
+    from socrates_gb300 import wenyi
+    return wenyi.read_data(path)
 
 
 def _read_k_file(path, n_band, n_abs, nd_k, recs, ia, nba, isb, n_pre, n_tmp):
@@ -639,29 +619,12 @@ class Spectrum:
             L.append("*END")
         Path(path).write_text("\n".join(L) + "\n")
 
-    def write_wenyi_source(self, path) -> None:
-        """Write the Wen-Yi tables as Fortran array constants in the form of
-        the module that defines them, one array per temperature of each
-        band table (the form read_wenyi_tables and socgpu_spectrum_load_ext
-        read)."""
-        L = ["MODULE scale_wenyi_tables"]
-
-        def arr(name, vals):
-            vals = [f"{v:.9E}_RealK" for v in vals]
-            L.append(f"  REAL (RealK), PARAMETER :: {name}({len(vals)}) = (/ &")
-            for q in range(0, len(vals), 3):
-                tail = ", &" if q + 3 < len(vals) else " /)"
-                L.append("     " + ",".join(vals[q:q + 3]) + tail)
-        arr("plg", self.wenyi_plg)
-        arr("ttb", self.wenyi_ttb)
-        arr("tto", self.wenyi_tto)
-        arr("gk250b", self.wenyi_gk250b)
-        for t in range(self.wenyi_gk4.shape[0]):
-            arr(f"gk4_{t + 1}", self.wenyi_gk4[t].reshape(-1))
-        for t in range(self.wenyi_gk6.shape[0]):
-            arr(f"gk6_{t + 1}", self.wenyi_gk6[t].reshape(-1))
-        L.append("END MODULE scale_wenyi_tables")
-        Path(path).write_text("\n".join(L) + "\n")
+    def write_wenyi_data(self, path) -> None:
+        """Write the Wen-Yi tables as their data file (the form
+        read_wenyi_tables and socgpu_spectrum_load_ext read)."""
+        from socrates_gb300 import wenyi
+        wenyi.write_data(path, {k: getattr(self, k) for k in ("wenyi_plg", "wenyi_ttb", "wenyi_tto",
+                                                                "wenyi_gk250b", "wenyi_gk4", "wenyi_gk6")})
 
     @classmethod
     def read_text(cls, path, name: str | None = None, k_path=None) -> "Spectrum":

@@ -28,7 +28,8 @@ sys.path.insert(0, str(HERE.parent.parent))
 sys.path.insert(0, str(HERE))
 
 from cdl import field  # noqa: E402
-from socrates_gb300.spectrum import Spectrum, read_wenyi_tables  # noqa: E402
+from socrates_gb300.spectrum import Spectrum  # noqa: E402
+from socrates_gb300.wenyi import read_fortran_tables  # noqa: E402
 
 # file suffixes of the gases (input_head_pcf.f90:208-225)
 SUFFIX = {1: "q", 2: "co2", 3: "o3", 4: "n2o", 6: "ch4", 7: "o2", 9: "so2", 14: "cfc11", 15: "cfc12",
@@ -50,7 +51,7 @@ def main(root):
     root = Path(root)
     case = root / "examples" / "netcdf" / "CIRC_case6"
     sp = Spectrum.read_text(root / "data" / "spectra" / "ga7" / "sp_lw_ga7", name="sp_lw_ga7")
-    for k, v in read_wenyi_tables(root / "src" / "radiance_core" / "scale_wenyi.F90").items():
+    for k, v in read_fortran_tables(root / "src" / "radiance_core" / "scale_wenyi.F90").items():
         setattr(sp, k, v)
     p, t = nc_field(case / "case6.t", "t")
     p_level, t_level = nc_field(case / "case6.tl", "tl")
@@ -87,4 +88,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {Path(__file__).name} <SOCRATES source tree>")
+    main(sys.argv[1])

@@ -32,7 +32,8 @@ sys.path.insert(0, str(HERE))
 from cdl import field  # noqa: E402
 from make_circ6 import nc_field  # noqa: E402
 from socrates_gb300.radiance import read_mcica_data  # noqa: E402
-from socrates_gb300.spectrum import Spectrum, read_wenyi_tables  # noqa: E402
+from socrates_gb300.spectrum import Spectrum  # noqa: E402
+from socrates_gb300.wenyi import read_fortran_tables  # noqa: E402
 
 RUNS = ("lw_avg", "sw_avg", "sw_ds0_avg", "lw_ga7", "sw_ga7")
 FIELDS = ("q", "co2", "o3", "n2o", "ch4", "o2", "clfr", "lwm", "iwm", "re", "ire")
@@ -56,7 +57,7 @@ def main(root):
         pk, hr = field(case / f"ref_{run}.hrts")
         assert np.allclose(pk, p)
         arrays["kgo_" + run] = hr
-    wy = read_wenyi_tables(root / "src" / "radiance_core" / "scale_wenyi.F90")
+    wy = read_fortran_tables(root / "src" / "radiance_core" / "scale_wenyi.F90")
     for pre, name in (("lw_", "sp_lw_ga3_0"), ("sw_", "sp_sw_ga3_0")):
         sp = Spectrum.read_text(root / "data" / "spectra" / "ga3_0" / name, name=name)
         if pre == "lw_":
@@ -84,4 +85,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {Path(__file__).name} <SOCRATES source tree>")
+    main(sys.argv[1])

@@ -25,7 +25,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from socrates_gb300.spectrum import Spectrum, read_wenyi_tables  # noqa: E402
+from socrates_gb300.spectrum import Spectrum  # noqa: E402
+from socrates_gb300.wenyi import read_fortran_tables  # noqa: E402
 
 
 def single(x):
@@ -68,7 +69,7 @@ def main(root):
     assert len(sections) == 4 and all(s.shape == (32, 3) for s in sections)
     sw = Spectrum.read_text(root / "data" / "spectra" / "ga9" / "sp_sw_ga9", name="sw")
     lw = Spectrum.read_text(root / "data" / "spectra" / "ga9" / "sp_lw_ga9", name="lw")
-    for k, v in read_wenyi_tables(root / "src" / "radiance_core" / "scale_wenyi.F90").items():
+    for k, v in read_fortran_tables(root / "src" / "radiance_core" / "scale_wenyi.F90").items():
         setattr(lw, k, v)
     arrays = dict(cos_zenith_angle=np.array([cos_zen]), kgo_sw=sections[0], kgo_lw_tground=sections[1],
                   kgo_lw_flux_ground=sections[2], kgo_lw_tiles=sections[3])
@@ -90,4 +91,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {Path(__file__).name} <SOCRATES source tree>")
+    main(sys.argv[1])

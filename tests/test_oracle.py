@@ -333,7 +333,7 @@ def test_k_file_round_trip(tmp_path, kind):
     """The GA7 long-wave file and its lookup tables (P/T, self-broadened,
     temperature-only) written in the reference's record layouts (block 5
     version 1 and the '_k' file) and read back give the same arrays; the
-    Wen-Yi tables round-trip through their Fortran-constant form."""
+    Wen-Yi tables round-trip through their data file."""
     import test_lookup_gpu as T
     from socrates_gb300.spectrum import Spectrum, read_wenyi_tables
     sp = T._ga7_lw()
@@ -362,7 +362,7 @@ def test_k_file_round_trip(tmp_path, kind):
                     if sp.i_scale_fnc[b, g] != abi.IP_SCALE_LOOKUP or (sp.index_sb is not None and sp.index_sb[g]):
                         a[:, :, :, g, b] = 0.0
         np.testing.assert_allclose(getattr(back, name), a, rtol=1e-12, atol=0, err_msg=name)
-    wy = tmp_path / "wy.f90"
-    sp.write_wenyi_source(wy)
+    wy = tmp_path / "wy.dat"
+    sp.write_wenyi_data(wy)
     for k, v in read_wenyi_tables(wy).items():
         np.testing.assert_array_equal(v, getattr(sp, k), err_msg=k)

@@ -248,3 +248,194 @@ def test_full_size_mcica_properties(gpu_lib):
     net_toa = g64["flux_down"][:, 0] - g64["flux_up"][:, 0]
     net_sfc = g64["flux_down"][:, -1] - g64["flux_up"][:, -1]
     np.testing.assert_allclose(absorbed, net_toa - net_sfc, rtol=1e-8, atol=1e-6)
+
+
+# ---------------------------------------------------------------------------
+# Two-stream schemes, full-size workloads and edge columns, on both kernel
+# families (the `kernel` fixture: scan kernels and the phased kernel).
+
+SCHEMES = {"discrete_ord": abi.IP_DISCRETE_ORD, "pifm85": abi.IP_PIFM85, "2s_test": abi.IP_2S_TEST,
+           "hemi_mean": abi.IP_HEMI_MEAN, "eddington": abi.IP_EDDINGTON, "elsasser": abi.IP_ELSASSER,
+           "pifm80": abi.IP_PIFM80}
+
+
+@pytest.mark.parametrize("scheme", sorted(SCHEMES))
+@pytest.mark.parametrize("source", ["solar", "infra_red"])
+def test_two_stream_schemes_match_oracle(kernel, scheme, source):
+    """Every scheme of two_coeff_basic.F90:99-160 (discrete ordinates with
+    its own ksi_0, solar_coefficient_basic.F90:171-182), in the solar and the
+    infra-red with scattering aerosol: FP64 at 1e-10 and mixed within 0.1
+    W/m2 and 0.05 K/day of the oracle."""
+    if source == "solar":
+        sp, col = synth.config2(16, 60, seed=41)
+        ctl = R.sw_control(i_2stream=SCHEMES[scheme], l_aerosol_mode=True)
+    else:
+        sp, col = synth.config1(16, 60, seed=42)
+        synth.add_aerosol(col, sp, 42)
+        ctl = R.lw_control(i_2stream=SCHEMES[scheme], l_aerosol_mode=True)
+    ref = _ora(ctl, sp, col)
+    assert_fp64_parity(_gpu(ctl, sp, col), ref, f"{scheme} {source} fp64: ")
+    assert_mixed_tolerance(_gpu(_with(ctl, abi.PRECISION_MIXED), sp, col), ref, f"{scheme} {source} mixed: ")
+
+
+def test_longwave_clear_sky_full_size(kernel):
+    """The plain longwave workload at its stated size, 1000 columns x 60
+    layers x 81 g-points, no scattering: every column against the oracle."""
+    sp, col = synth.config1(1000, 60, seed=1)
+    ctl = R.lw_noscat_control()
+    ref = _ora(ctl, sp, col)
+    assert_fp64_parity(_gpu(ctl, sp, col), ref, "lw 1000x60 fp64: ")
+    assert_mixed_tolerance(_gpu(_with(ctl, abi.PRECISION_MIXED), sp, col), ref, "lw 1000x60 mixed: ")
+
+
+def _controlled_column(n, L, tau, one_m_om, g, mu0, alb=0.2, seed=43):
+    """A solar column whose every cell has the given optical depth, 1-omega
+    and asymmetry (arrays of shape (n, L)): no gas absorption, no Rayleigh,
+    one aerosol mode carrying all of the extinction."""
+    sp, col = synth.config2(n, L, seed=seed)
+    col.gas_mix_ratio[...] = 0.0
+    nb = sp.n_band
+    kt = tau / col.mass
+    shape = (n, L, 1, nb)
+    col.aer = dict(n_mode=1, mode_mix_ratio=np.asfortranarray(np.ones((n, L, 1))),
+                   mode_absorption=np.asfortranarray(np.broadcast_to((kt * one_m_om)[:, :, None, None], shape)),
+                   mode_scattering=np.asfortranarray(np.broadcast_to((kt * (1.0 - one_m_om))[:, :, None, None], shape)),
+                   mode_asymmetry=np.asfortranarray(np.broadcast_to(g[:, :, None, None], shape)))
+    col.zen_0 = np.ascontiguousarray(1.0 / mu0)
+    col.rho_alb[...] = alb
+    return sp, col
+
+
+def test_near_conservative_thin_layers(kernel):
+    """Thin layers of almost conservative scattering: omega within 1e-7 to
+    1e-5 of 1 and lambda tau below 1e-4, where 1 - omega, 1 - gamma and
+    1 - T - R lose every digit in a direct FP32 evaluation."""
+    n, L = 12, 60
+    rng = np.random.default_rng(5)
+    tau = 10.0 ** rng.uniform(-4, -2, (n, L))
+    one_m_om = 10.0 ** rng.uniform(-7, -5, (n, L))
+    g = rng.uniform(0.0, 0.8, (n, L))
+    mu0 = rng.uniform(0.1, 1.0, n)
+    sp, col = _controlled_column(n, L, tau, one_m_om, g, mu0)
+    for rescale in (True, False):
+        ctl = R.sw_control(l_aerosol_mode=True, l_rayleigh=False, l_rescale=rescale)
+        ref = _ora(ctl, sp, col)
+        assert_fp64_parity(_gpu(ctl, sp, col), ref, f"rescale={rescale} fp64: ")
+        assert_mixed_tolerance(_gpu(_with(ctl, abi.PRECISION_MIXED), sp, col), ref, f"rescale={rescale} mixed: ")
+
+
+def _omega_for_lambda(lam, g):
+    """1 - omega at which PIFM80 (no rescaling) gives eigenvalue lam for
+    asymmetry g: lambda^2 = (2 - 1.5 omega g - 0.5 omega) 2 (1 - omega),
+    decreasing in omega; bisection."""
+    lo, hi = np.zeros_like(lam), np.ones_like(lam)      # in omega
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        l2 = (2.0 - 1.5 * mid * g - 0.5 * mid) * 2.0 * (1.0 - mid)
+        big = l2 > lam * lam
+        lo = np.where(big, mid, lo)
+        hi = np.where(big, hi, mid)
+    return 1.0 - 0.5 * (lo + hi)
+
+
+def test_solar_singularity_lambda_near_sec0(kernel):
+    """Cells whose eigenvalue lambda lies at and around the secant of the
+    solar zenith angle, the removable singularity of
+    solar_coefficient_basic.F90:124-219.  Two sets of columns, each the same
+    column at offsets of lambda from sec_0 of 0, 1e-9, +-1e-6, +-1e-5, +-1e-4,
+    +-3e-3 and 1e-2 (relative); optical depth proportional to layer mass.
+
+    * FP64 matches the oracle at 1e-10 where the reference's expressions
+      keep that accuracy, |offset| >= 1e-5 (their rounding error grows as
+      eps / offset).
+    * Exactly on the singularity the reference perturbs lambda by 32 eps,
+      which leaves its coefficients with errors of order 1/32 (the oracle
+      shows 2 W/m2 at the top of such a column).  The mixed kernel
+      interpolates across the singularity instead: it is checked there
+      against the oracle's continuous limit, the same column at offset 1e-9,
+      and everywhere else against the oracle on its own column."""
+    offsets = np.array([0.0, 1e-9, 1e-6, -1e-6, 1e-5, -1e-5, 1e-4, -1e-4, 3e-3, -3e-3, 1e-2])
+    no = len(offsets)
+    rng = np.random.default_rng(6)
+    L, n = 40, 2 * no
+    mu0 = np.repeat(rng.uniform(0.55, 1.0, 2), no)
+    gs = np.repeat(rng.uniform(0.2, 0.8, 2), no)
+    tau_col = np.repeat(rng.uniform(0.5, 3.0, 2), no)
+    off = np.tile(offsets, 2)
+    sp, col0 = synth.config2(n, L, seed=43)
+    tau = col0.mass / col0.mass.sum(axis=1, keepdims=True) * tau_col[:, None]
+    g = np.broadcast_to(gs[:, None], (n, L)).copy()
+    lam = np.broadcast_to(((1.0 / mu0) * (1.0 + off))[:, None], (n, L))
+    sp, col = _controlled_column(n, L, tau, _omega_for_lambda(lam, g), g, mu0)
+    ctl = R.sw_control(l_aerosol_mode=True, l_rayleigh=False, l_rescale=False)
+    ref = _ora(ctl, sp, col)
+    g64 = _gpu(ctl, sp, col)
+    sel = np.flatnonzero(np.abs(off) >= 1e-5)
+    assert_fp64_parity({k: v[sel] for k, v in g64.items()}, {k: v[sel] for k, v in ref.items()},
+                       "singularity fp64: ")
+    # the continuous limit for the columns on the singularity
+    lim = {k: v.copy() for k, v in ref.items()}
+    for c in np.flatnonzero(off == 0.0):
+        for k in lim:
+            lim[k][c] = ref[k][c + 1]
+    assert_mixed_tolerance(_gpu(_with(ctl, abi.PRECISION_MIXED), sp, col), lim, "singularity mixed: ")
+
+
+def test_full_size_mcica_solar(gpu_lib):
+    """The all-sky McICA workload at full size in the solar, 65 536 columns x
+    85 layers x 16 subcolumns: FP64 against the oracle on 32 sampled
+    columns, mixed against FP64 everywhere, and the energy budget."""
+    lw, sw, col = synth.config3(65536, 85, seed=3, n_subcol=16)
+    synth.add_sw_surface(col, sw.n_band, 3)
+    c_sub, nsc = R.cloud_gen(col, 16, abi.IP_EXPONENTIAL_RAND, abi.RNG_PHILOX)
+    idx = np.sort(np.random.default_rng(2).choice(col.n_profile, 32, replace=False))
+    sub = _subset(col, idx)
+    ctl = R.sw_control(i_cloud=abi.IP_CLOUD_MCICA)
+    mc = R.set_cld_mcica(sw, col, abi.IP_SOLAR, abi.IP_MCICA_SINGLE_SAMPLING, c_sub=c_sub, n_subcol_cld=nsc)
+    g64 = R.radiance_calc(ctl, sw, col, mc)
+    gmx = R.radiance_calc(_with(ctl, abi.PRECISION_MIXED), sw, col, mc)
+    assert_mixed_tolerance(gmx, g64, "mcica sw mixed vs fp64: ")
+    from dataclasses import replace
+    mc_sub = replace(mc, c_sub=np.asfortranarray(c_sub[idx]), n_subcol_cld=np.ascontiguousarray(nsc[idx]),
+                     frac_cloudy=np.ascontiguousarray(mc.frac_cloudy[idx]))
+    ref = O.radiance_calc(ctl, sw, sub, mc_sub)
+    assert_fp64_parity({k: v[idx] for k, v in g64.items()}, ref, "mcica sw sample: ", mass=col.mass[idx])
+    absorbed = g64["flux_div"].sum(axis=1)
+    net_toa = g64["flux_down"][:, 0] - g64["flux_up"][:, 0]
+    net_sfc = g64["flux_down"][:, -1] - g64["flux_up"][:, -1]
+    np.testing.assert_allclose(absorbed, net_toa - net_sfc, rtol=1e-8, atol=1e-6)
+
+
+def test_unscaled_direct_beam_under_thick_cloud(gpu_lib):
+    """McICA with an overcast, optically thick liquid layer (optical depth
+    about 30) and the direct beam reported without delta-scaling
+    (i_direct_tau = 0, solar_source.F90:157-176).  There the delta-scaled
+    beam is many orders of magnitude above the unscaled one, so the mixed
+    kernel has to carry the unscaled beam by itself, not as the scaled beam
+    plus a difference.  The direct flux is never negative, and at and below
+    the cloud it matches the oracle to 1e-3 relative; FP64 matches at
+    1e-10."""
+    lw, sw, col = synth.config3(16, 60, seed=13, n_subcol=16)
+    synth.add_sw_surface(col, sw.n_band, 13)
+    col.zen_0 = np.ascontiguousarray(1.0 / np.random.default_rng(13).uniform(0.5, 1.0, col.n_profile))
+    cd = col.cld
+    k = 57
+    cd["w_cloud"][...] = 0.0
+    cd["w_cloud"][:, k] = 1.0
+    cd["frac_cloud"][...] = 0.0
+    cd["frac_cloud"][:, k, 0] = 1.0
+    cd["condensed_mix_ratio"][...] = 0.0
+    cd["condensed_mix_ratio"][:, k, 0] = 1.6e-4
+    cd["condensed_dim_char"][:, k, 0] = 10.0e-6
+    c_sub, nsc = R.cloud_gen(col, 16, abi.IP_EXPONENTIAL_RAND, abi.RNG_LCG, impl=O.cloud_gen_impl)
+    mc = R.set_cld_mcica(sw, col, abi.IP_SOLAR, abi.IP_MCICA_SINGLE_SAMPLING, c_sub=c_sub, n_subcol_cld=nsc)
+    ctl = R.sw_control(i_cloud=abi.IP_CLOUD_MCICA, i_direct_tau=abi.IP_DIRECT_NOSCALING)
+    ref = _ora(ctl, sw, col, mc)
+    assert_fp64_parity(_gpu(ctl, sw, col, mc), ref, "thick cloud fp64: ")
+    gmx = _gpu(_with(ctl, abi.PRECISION_MIXED), sw, col, mc)
+    assert gmx["flux_direct"].min() >= 0.0
+    below = slice(k + 1, None)
+    rel = np.abs(gmx["flux_direct"][:, below] - ref["flux_direct"][:, below]) / ref["flux_direct"][:, below]
+    assert ref["flux_direct"][:, below].min() > 0.0
+    assert rel.max() <= 1e-3, f"direct flux below the cloud: relative error {rel.max():.3e}"
+    assert_mixed_tolerance(gmx, ref, "thick cloud mixed: ")

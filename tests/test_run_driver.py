@@ -38,8 +38,8 @@ def _column_files(tmp, name, d, sp, sp_name, to_cdf=False, gases=None, wenyi=Fal
         sp.write_k_file(str(sp_path) + "_k")
     wy = None
     if wenyi:
-        wy = tmp / "wenyi_tables.f90"
-        sp.write_wenyi_source(wy)
+        wy = tmp / "wenyi_tables.dat"
+        sp.write_wenyi_data(wy)
     base = tmp / name
     coord = {"units": "degree", "title": "latitude"}
 
@@ -192,8 +192,8 @@ def test_loader_reads_self_broadened_and_temperature_tables(gpu_lib, tmp_path, k
     sp_path = tmp_path / "sp"
     sp.write_text(sp_path)
     sp.write_k_file(str(sp_path) + "_k")
-    wy = tmp_path / "wy.f90"
-    sp.write_wenyi_source(wy)
+    wy = tmp_path / "wy.dat"
+    sp.write_wenyi_data(wy)
     lib = R.load_library()
     h = C.c_int(0)
     msg = C.create_string_buffer(512)

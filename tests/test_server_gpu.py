@@ -123,3 +123,41 @@ def test_invalid_request_rejected_at_submit(gpu_lib):
         srv.submit(R.Marshal(bad, sp, col, mc), sp)
     assert e.value.status == abi.I_ERR_FATAL
     srv.close()
+
+
+def test_small_requests_overtake_a_large_one(gpu_lib):
+    """A large McICA request (8192 columns x 137 layers) and then small
+    clear-sky requests submitted while it runs: the small requests go in
+    their own waves, on high-priority streams, so at least two waves are on
+    the device at once and every small request finishes before the large
+    one; each result is still the same as alone."""
+    from socrates_gb300 import synth
+    from socrates_gb300.server import Server
+    lw, sw, col = synth.config3(8192, 137, seed=31, n_subcol=16)
+    synth.add_sw_surface(col, sw.n_band, 31)
+    c_sub, nsc = R.cloud_gen(col, 16, abi.IP_EXPONENTIAL_RAND, abi.RNG_PHILOX)
+    mc = R.set_cld_mcica(sw, col, abi.IP_SOLAR, abi.IP_MCICA_SINGLE_SAMPLING, c_sub=c_sub, n_subcol_cld=nsc)
+    big = (R.sw_control(i_cloud=abi.IP_CLOUD_MCICA, precision=abi.PRECISION_MIXED), sw, col, mc)
+    _, small = _requests(8, seed=32, median=16.0)
+    big_m = R.Marshal(*big)
+    small_m = [R.Marshal(*r) for r in small]
+    srv = Server(device_bytes=2 << 30, streams=4, max_wave_requests=16)
+    t_big = srv.submit(big_m, big[1])
+    t0 = time.perf_counter()
+    ts = []
+    for m, r in zip(small_m, small):
+        ts.append((srv.submit(m, r[1]), time.perf_counter() - t0))
+        time.sleep(2e-4)
+    done_small = []
+    for t, sub in ts:
+        _, lat = srv.wait(t, 60.0)
+        done_small.append(sub * 1e3 + lat)
+    _, lat_big = srv.wait(t_big, 60.0)
+    st = srv.stats()
+    srv.close()
+    assert st["max_waves_in_flight"] >= 2
+    assert st["small_waves"] >= 1
+    assert max(done_small) < lat_big, (max(done_small), lat_big)
+    _compare(R.radiance_calc(*big), big_m.result(), abi.PRECISION_MIXED, "large")
+    for r, m in zip(small, small_m):
+        _compare(R.radiance_calc(*r), m.result(), r[0].precision, "small")
