@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--rates", default="200,1000,5000", help="arrival rates (requests/s) of the serving workload")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
     ap.add_argument("--batches", type=int, default=4096, help="column batches of the batched workload")
+    ap.add_argument("--batched-steps", type=int, default=10, help="timed graph replays of the batched workload")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="the default run without the multi-batch and serving figures")
     return ap.parse_args()
 
 
@@ -222,19 +225,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_batched(args):
-    """The multi-batch workload: one graph replay per step."""
-    import numpy as np
+def batched_figures(args, rank: int = 0, world: int = 1) -> dict:
+    """The multi-batch workload: 4096 uneven column batches replayed as one
+    CUDA graph of autotuned launches, the same batches one call each (mixed
+    and FP64), and the mixed-vs-FP64 error over all of them."""
     import torch
-    rank, world = dist_setup(args.gpus)
-    dev = torch.cuda.current_device()
     from socrates_gb300 import abi
     from socrates_gb300 import build as B
     from socrates_gb300 import radiance as R
     from socrates_gb300.batch import Batch
     from socrates_gb300.device import DeviceCase
-    from socrates_gb300.workload import Pools, n_gpoint, request_specs
+    from socrates_gb300.workload import Pools, request_specs
     B.build()
+    dev = torch.cuda.current_device()
     seed = 4 + rank
     t_setup = time.perf_counter()
     specs = request_specs(args.batches, seed)
@@ -254,7 +257,7 @@ def run_batched(args):
         batch.run(stream.cuda_stream)
     torch.cuda.synchronize()
     barrier(world)
-    steps = max(1, args.steps)
+    steps = max(1, args.batched_steps)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     l0 = R.launch_count()
     with ClockSampler(dev) as clk:
@@ -266,6 +269,7 @@ def run_batched(args):
     launches = R.launch_count() - l0
     ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / steps, world)
     value = world * colg / (ms * 1e-3)
+
     # the same requests one call each, without batching, mixed and FP64
     def per_request(cs, reps):
         for c in cs:
@@ -293,29 +297,43 @@ def run_batched(args):
     kinds = {}
     for s in specs:
         kinds[s.kind] = kinds.get(s.kind, 0) + 1
+    out = {"value": value, "unit": UNIT, "ms_per_step": ms, "steps": steps,
+           "config": {"workload": f"{args.batches} uneven column batches in one CUDA-graph replay: columns "
+                                  "log-normal (median 256, sigma 1, clip 1-8192), layers from {38,60,85,137}, "
+                                  "LW 81 / SW 48 g-points, clear or McICA all-sky (16 subcolumns), mixed precision",
+                      "batches": args.batches, "columns": info["columns"], "column_gpoints": colg,
+                      "kinds": kinds, "kernel_classes": info["kernel_classes"],
+                      "l2": f"inputs {in_bytes / 1e9:.1f} GB, far above the 129 MB L2; no flush needed"},
+           "per_request_mixed": {"value": world * colg / (ms_single * 1e-3), "ms_per_step": ms_single,
+                                 "note": "the same requests, one socgpu_radiance_calc_device call each"},
+           "fp64_per_request": {"value": world * colg / (ms_64 * 1e-3), "ms_per_step": ms_64,
+                                "note": "the same requests in FP64, one call each (the plain FP64 GPU path)"},
+           "speedup_batched_mixed_over_fp64": ms_64 / ms,
+           "accuracy_vs_fp64": {"max_flux_err_wm2": err_flux, "max_heating_rate_err_kday": err_hr},
+           "setup_s": t_setup, "tune_s": t_tune, "gpu_launches": int(launches), "clocks": clk.summary()}
+    del batch, cases, cases64
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_batched(args):
+    """The multi-batch workload as its own bench line."""
+    rank, world = dist_setup(args.gpus)
+    f = batched_figures(args, rank, world)
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
-                "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded windows of per-kind pools)",
-                "config": {"workload": f"{args.batches} uneven column batches in one CUDA-graph replay: columns "
-                                       "log-normal (median 256, sigma 1, clip 1-8192), layers from {38,60,85,137}, "
-                                       "LW 81 / SW 48 g-points, clear or McICA all-sky (16 subcolumns)",
-                           "batches": args.batches, "columns": info["columns"], "column_gpoints": colg,
-                           "kinds": kinds, "kernel_classes": info["kernel_classes"],
-                           "l2": f"inputs {in_bytes / 1e9:.1f} GB, far above the 129 MB L2; no flush needed"},
-                "per_request_mixed": {"value": world * colg / (ms_single * 1e-3), "ms_per_step": ms_single,
-                                      "note": "the same requests, one socgpu_radiance_calc_device call each"},
-                "fp64_per_request": {"value": world * colg / (ms_64 * 1e-3), "ms_per_step": ms_64,
-                                     "speedup_batched_mixed_over_fp64": ms_64 / ms},
-                "accuracy_vs_fp64": {"max_flux_err_wm2": err_flux, "max_heating_rate_err_kday": err_hr},
-                "setup_s": t_setup, "tune_s": t_tune, "gpu_launches": int(launches), "clocks": clk.summary()}
+        line = {"metric": METRIC, "value": f["value"], "unit": UNIT, "n_gpus": world, "steps": f["steps"],
+                "warmup": max(3, args.warmup), "ms_per_step": f["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded windows of per-kind pools)", "config": f["config"],
+                **{k: f[k] for k in ("per_request_mixed", "fp64_per_request", "speedup_batched_mixed_over_fp64",
+                                     "accuracy_vs_fp64", "setup_s", "tune_s", "gpu_launches", "clocks")}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
 
 
-def run_serve(args):
+def serve_figures(args, rank: int = 0) -> dict:
     """The serving workload: Poisson arrivals of requests drawn like the
     multi-batch workload, served by the continuous-batching server; p50/p99
     latency and throughput per arrival rate, beside the plain FP64
@@ -323,7 +341,6 @@ def run_serve(args):
     import ctypes
     import numpy as np
     import torch
-    rank, world = dist_setup(args.gpus)
     from dataclasses import replace
     from socrates_gb300 import abi
     from socrates_gb300 import build as B
@@ -440,16 +457,26 @@ def run_serve(args):
         k += 1
     cpu = {"value": colg / (time.perf_counter() - t0), "unit": UNIT, "cores": threads, "kind": "port",
            "sample": f"{k} requests of the trace, one FP64 oracle call each, OpenMP over column segments"}
+    return {"results": results, "fp64_per_request": fp64, "cpu_baseline": cpu, "rates_rps": rates,
+            "window_s": args.serve_seconds, "request_slots": n_slot,
+            "config": {"workload": "serving: Poisson arrivals, requests drawn like the multi-batch workload "
+                                   "(log-normal columns, median 256; layers {38,60,85,137}; LW/SW; clear or "
+                                   "McICA), page-locked host arrays, continuous batching over 4 streams "
+                                   "(2 high-priority for small requests)",
+                       "rates_rps": rates, "window_s": args.serve_seconds, "request_slots": n_slot}}
+
+
+def run_serve(args):
+    """The serving workload as its own bench line."""
+    rank, world = dist_setup(args.gpus)
+    f = serve_figures(args, rank)
     if rank == 0:
-        best = max(results, key=lambda r: r["column_gpoints_per_s"])
+        best = max(f["results"], key=lambda r: r["column_gpoints_per_s"])
         line = {"metric": METRIC, "value": best["column_gpoints_per_s"], "unit": UNIT, "n_gpus": world,
-                "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded windows of per-kind pools)",
-                "config": {"workload": "serving: Poisson arrivals, requests drawn like the multi-batch workload "
-                                       "(log-normal columns, median 256; layers {38,60,85,137}; LW/SW; clear or "
-                                       "McICA), page-locked host arrays, continuous batching over 4 streams",
-                           "rates_rps": rates, "window_s": args.serve_seconds, "request_slots": n_slot},
-                "serve": results, "fp64_per_request": fp64, "cpu_baseline": cpu}
+                "steps": len(f["rates_rps"]), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded windows of per-kind pools)", "config": f["config"],
+                "serve": f["results"], "fp64_per_request": f["fp64_per_request"], "cpu_baseline": f["cpu_baseline"]}
         print(json.dumps(line), flush=True)
 
 
@@ -521,7 +548,9 @@ def run_ga9(args):
 def main():
     args = parse()
     if args.steps is None:
-        args.steps = 20 if args.workload == "batched" else 200
+        args.steps = 200
+    if args.workload == "batched" and "--steps" in sys.argv and "--batched-steps" not in sys.argv:
+        args.batched_steps = args.steps
     if args.impl == "reference":
         run_reference(args)
         return
@@ -579,6 +608,11 @@ def main():
 
     with ClockSampler(dev) as clk:
         ms_mx, launches, wall = timed(case, args.steps, max(3, args.warmup))
+    # the same step repeated for about a second, with clocks sampled over it:
+    # the K timed steps above can be a few milliseconds only
+    n_sus = max(args.steps, int(1000.0 / max(ms_mx, 1e-3)))
+    with ClockSampler(dev) as clk_sus:
+        ms_sus, _, wall_sus = timed(case, n_sus, 0)
     ms_64, _, _ = timed(case64, max(3, args.steps // 4), 3)
     ms_mx = max_over_ranks(ms_mx, world)
     ms_64 = max_over_ranks(ms_64, world)
@@ -661,7 +695,20 @@ def main():
                 "config": CONFIG, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "fp64_device": {"value": value_64, "ms_per_step": ms_64, "speedup_mixed_over_fp64": ms_64 / ms_mx},
                 "accuracy_vs_fp64": {"max_flux_err_wm2": err_flux, "max_heating_rate_err_kday": err_hr},
-                "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s_timed_region": wall}
+                "gpu_launches": int(launches), "clocks": clk.summary(), "wall_s_timed_region": wall,
+                "sustained": {"steps": n_sus, "ms_per_step": ms_sus, "wall_s": wall_sus, "clocks": clk_sus.summary(),
+                              "note": "the timed step repeated for about 1 s (L2 flushed between steps)"}}
+        if world == 1 and not args.no_extras:
+            # the multi-batch graph (4096 uneven batches) and the serving
+            # loop, measured in the same run and reported beside the headline
+            del case, case64
+            torch.cuda.empty_cache()
+            line["batched"] = batched_figures(args)
+            sv = serve_figures(args)
+            line["serve"] = sv["results"]
+            line["serve_fp64_per_request"] = sv["fp64_per_request"]
+            line["serve_cpu_baseline"] = sv["cpu_baseline"]
+            line["serve_config"] = sv["config"]
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
