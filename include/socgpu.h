@@ -36,7 +36,7 @@ extern "C" {
 #define SOCGPU_API
 #endif
 
-#define SOCGPU_ABI_VERSION 4
+#define SOCGPU_ABI_VERSION 5
 
 /* ---- status codes: rad_pcf.F90:391-405 ------------------------------- */
 #define SOCGPU_I_NORMAL             0
@@ -116,6 +116,17 @@ extern "C" {
 #define SOCGPU_IP_SCALE_T_LOOKUP       10   /* temperature tables of the '_k' file */
 /* Rayleigh schemes, rad_pcf.F90:729-731 */
 #define SOCGPU_IP_RAYLEIGH_TOTAL        1
+/* parametrizations of aerosol species (rad_pcf.F90:22-30) */
+#define SOCGPU_IP_AEROSOL_PARAM_DRY       1   /* mass coefficients and an asymmetry */
+#define SOCGPU_IP_AEROSOL_PARAM_MOIST     2   /* the same, tabulated in relative humidity */
+#define SOCGPU_IP_AEROSOL_UNPARAMETRIZED  3   /* observed optical properties: not supported */
+#define SOCGPU_IP_AEROSOL_PARAM_PHF_DRY   4   /* moments of the phase function */
+#define SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST 5
+/* sources of aerosol mixing ratios (rad_pcf.F90:163-170); the radiatively
+   active ones are 0-2, each inactive one is its active one plus 10 */
+#define SOCGPU_IP_AERSRC_CUSACK_RON       0
+#define SOCGPU_IP_AERSRC_CLASSIC_RON      1
+#define SOCGPU_IP_AERSRC_ARCL_RON         2
 /* Continuum types (rad_pcf.F90 ip_self_continuum, ip_frn_continuum) */
 #define SOCGPU_IP_SELF_CONTINUUM 1
 #define SOCGPU_IP_FRN_CONTINUUM  2
@@ -226,6 +237,17 @@ typedef struct socgpu_spectrum_desc {
     const double *wenyi_gk250b;         /* (wenyi_n_term4) band-4 normalisation at 250 K */
     const double *wenyi_gk4;            /* (10, 26, wenyi_n_term4) */
     const double *wenyi_gk6;            /* (9, 26, wenyi_n_term6) */
+    /* StrSpecAerosol, block 11 (read_spectrum.F90:2335-2640): the classic
+       aerosol species; n_aerosol 0 (or NULL arrays): none */
+    int n_aerosol, nd_aerosol_species, nd_humidity, nd_phase_term;
+    const int    *type_aerosol;         /* (nd_aerosol_species) type numbers */
+    const int    *i_aerosol_parm;       /* (nd_aerosol_species) SOCGPU_IP_AEROSOL_PARAM_* */
+    const int    *nhumidity;            /* (nd_aerosol_species) humidities tabulated (moist), 0 (dry) */
+    const int    *n_aerosol_phf_term;   /* (nd_aerosol_species) phase-function moments */
+    const double *aerosol_humidities;   /* (nd_humidity, nd_aerosol_species) */
+    const double *aerosol_abs;          /* (nd_humidity, nd_aerosol_species, nd_band) [m2/kg] */
+    const double *aerosol_scat;         /* (nd_humidity, nd_aerosol_species, nd_band) [m2/kg] */
+    const double *aerosol_phf;          /* (nd_humidity, nd_phase_term, nd_aerosol_species, nd_band) */
 } socgpu_spectrum_desc;
 
 typedef int32_t socgpu_spectrum_handle;   /* > 0 when valid */
@@ -255,6 +277,8 @@ typedef struct socgpu_control {
     int l_continuum;            /* water-vapour continuum absorption (blocks 8 and 9) */
     int l_mixing_ratio;         /* gas amounts per unit mass of dry air (foreign continuum) */
     int l_grey_single;          /* k_eqv_scl, infra-red: single-term minor gases as grey absorbers */
+    int l_aerosol;              /* classic aerosol species of the spectral file (block 11) */
+    int l_henyey_greenstein_pf; /* classic aerosol: phase-function moments from the asymmetry */
 } socgpu_control;
 
 /* ---- StrDim subset (src/radiance_core/def_dimen.F90) ----------------- */
@@ -264,6 +288,7 @@ typedef struct socgpu_dimen {
     int nd_aerosol_mode;
     int nd_cloud_component, nd_cloud_type;
     int nd_subcol_gen, nd_subcol_req;
+    int nd_aerosol_mr;          /* third extent of socgpu_aer.mix_ratio */
 } socgpu_dimen;
 
 /* ---- StrAtm (src/radiance_core/def_atm.F90) --------------------------- */
@@ -297,6 +322,14 @@ typedef struct socgpu_aer {
     const double *mode_absorption;  /* (nd_profile, nd_layer, nd_aerosol_mode, nd_band) [m2/kg] */
     const double *mode_scattering;  /* same */
     const double *mode_asymmetry;   /* same */
+    /* classic aerosol (def_aer.F90:26-34), with control.l_aerosol: mixing
+       ratios of the spectral file's species, and the layers' mean relative
+       humidity for moist species */
+    int n_aerosol_mr;
+    const double *mix_ratio;         /* (nd_profile, nd_layer, nd_aerosol_mr) [kg/kg] */
+    const int    *mr_type_index;     /* (nd_aerosol_mr) 1-based species of the spectral file */
+    const int    *mr_source;         /* (nd_aerosol_mr) SOCGPU_IP_AERSRC_*: only the active ones count */
+    const double *mean_rel_humidity; /* (nd_profile, nd_layer) in [0, 1], or NULL without moist species */
 } socgpu_aer;
 
 /* ---- StrCld with the McICA state (def_cld.F90, def_mcica.F90) --------
@@ -446,7 +479,10 @@ SOCGPU_API int socgpu_cloud_gen_device(int nd_layer, int cloud_top, int n_layer,
  * free: its scratch (per-layer cloud flags and the batch's cloud layer range)
  * is a fixed array in the library's device memory.
  * - The first call on each device looks up that array's address; make it
- *   once at set-up, outside any time-critical region.
+ *   once at set-up, outside any time-critical region.  The address is kept
+ *   for the life of the device's primary context: a caller that destroys
+ *   that context (cudaDeviceReset) must not call this entry point again in
+ *   the same process.
  * - n_layer - cloud_top + 1 above SOCGPU_NOALLOC_MAX_CLOUD_LAYERS is
  *   rejected with SOCGPU_I_ERR_RANGE and a message; nothing is enqueued.
  * - Every call clears the flags it uses on `stream` before use; nothing has to
@@ -607,7 +643,9 @@ typedef struct socgpu_server_config {
     /* Requests of at most this many column x g-points are "small": they are
        waved apart from larger ones, on high-priority streams (half of the
        streams, at least one when there are two or more), so that a large
-       request in flight does not hold them back.  0: 131072. */
+       request in flight does not hold them back; the low-priority streams
+       take small requests only while no large request waits or runs.
+       0: 131072. */
     long long small_column_gpoints;
 } socgpu_server_config;
 
@@ -616,7 +654,7 @@ typedef struct socgpu_server_stats {
     long long column_gpoints;   /* of the requests completed without error */
     size_t device_bytes, peak_bytes;
     long long max_waves_in_flight;   /* most waves on the device at one time */
-    long long small_waves;           /* waves of small requests (high-priority streams) */
+    long long small_waves;           /* waves of small requests */
 } socgpu_server_stats;
 
 /* A request: the arguments of socgpu_radiance_calc, host pointers. */

@@ -19,11 +19,13 @@ TYPE, BIND(C) :: socgpu_control
                     first_band, last_band
   TYPE(c_ptr)    :: weight_band
   INTEGER(c_int) :: precision, l_continuum, l_mixing_ratio, l_grey_single
+  INTEGER(c_int) :: l_aerosol, l_henyey_greenstein_pf
 END TYPE
 
 TYPE, BIND(C) :: socgpu_dimen
   INTEGER(c_int) :: nd_profile, nd_layer, id_cloud_top, nd_aerosol_mode, &
-                    nd_cloud_component, nd_cloud_type, nd_subcol_gen, nd_subcol_req
+                    nd_cloud_component, nd_cloud_type, nd_subcol_gen, nd_subcol_req, &
+                    nd_aerosol_mr
 END TYPE
 
 TYPE, BIND(C) :: socgpu_atm
@@ -38,6 +40,8 @@ END TYPE
 TYPE, BIND(C) :: socgpu_aer
   INTEGER(c_int) :: n_mode
   TYPE(c_ptr)    :: mode_mix_ratio, mode_absorption, mode_scattering, mode_asymmetry
+  INTEGER(c_int) :: n_aerosol_mr
+  TYPE(c_ptr)    :: mix_ratio, mr_type_index, mr_source, mean_rel_humidity
 END TYPE
 
 TYPE, BIND(C) :: socgpu_cld

@@ -608,6 +608,89 @@ static void rescale_continuum(const socgpu_control *c, const socgpu_spectrum_des
         }
 }
 
+/* opt_prop_aerosol (opt_prop_aerosol.F90:273-640), two-stream phase
+ * functions (n_order_phase 1), for band b: every radiatively active entry of
+ * the mixing ratios adds its species' absorption and scattering, interpolated
+ * in the mean relative humidity for moist species, the asymmetry to the first
+ * phase-function moment and, with rescaling, the forward-scattering moment.
+ * The humidity pointer follows radiance_calc.F90:603-623 (one table, that of
+ * the last moist species of the spectrum); it is clamped to the table, where
+ * the reference would read past it for a humidity of 1. */
+static int opt_prop_aerosol(work *w, const socgpu_control *c, const socgpu_dimen *dm,
+                            const socgpu_spectrum_desc *d, const socgpu_aer *aer, int b)
+{
+    const int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp, ndl = w->ndl, ndp = dm->nd_profile;
+    const int ndh = d->nd_humidity, nda = d->nd_aerosol_species, ndf = d->nd_phase_term;
+    if (d->n_aerosol <= 0 || !d->i_aerosol_parm || !d->aerosol_abs || !d->aerosol_scat || !d->aerosol_phf)
+        return SOCGPU_I_ERR_FATAL;
+    int nhc = 0;
+    for (int j = 0; j < d->n_aerosol; ++j)
+        if (d->i_aerosol_parm[j] == SOCGPU_IP_AEROSOL_PARAM_MOIST ||
+            d->i_aerosol_parm[j] == SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST)
+            nhc = d->nhumidity[j];
+    const double delta_humidity = nhc > 1 ? 1.0e+00 / ((double)nhc - 1.0e+00) : 0.0;
+    for (int jm = 0; jm < aer->n_aerosol_mr; ++jm) {
+        const int src = aer->mr_source ? aer->mr_source[jm] : SOCGPU_IP_AERSRC_CLASSIC_RON;
+        if (src != SOCGPU_IP_AERSRC_CUSACK_RON && src != SOCGPU_IP_AERSRC_CLASSIC_RON && src != SOCGPU_IP_AERSRC_ARCL_RON)
+            continue;
+        const int j = aer->mr_type_index[jm] - 1;
+        if (j < 0 || j >= d->n_aerosol) return SOCGPU_I_ERR_RANGE;
+        const int parm = d->i_aerosol_parm[j];
+        const int moist = parm == SOCGPU_IP_AEROSOL_PARAM_MOIST || parm == SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST;
+        const int hg = c->l_henyey_greenstein_pf || parm == SOCGPU_IP_AEROSOL_PARAM_DRY ||
+                       parm == SOCGPU_IP_AEROSOL_PARAM_MOIST;
+        if (!hg && parm != SOCGPU_IP_AEROSOL_PARAM_PHF_DRY && parm != SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST)
+            return SOCGPU_I_ERR_FATAL;
+        if (moist && (nhc < 2 || !aer->mean_rel_humidity || !d->aerosol_humidities)) return SOCGPU_I_ERR_FATAL;
+#define AEROSOL_PHF(h, m) d->aerosol_phf[(size_t)(h) + (size_t)ndh * ((size_t)(m) + (size_t)ndf * ((size_t)j + (size_t)nda * b))]
+#define AEROSOL_TAB(a, h) (a)[(size_t)(h) + (size_t)ndh * ((size_t)j + (size_t)nda * b)]
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                const double mmr = aer->mix_ratio[(size_t)l + (size_t)ndp * ((size_t)i + (size_t)ndl * jm)];
+                int ip = 0;            /* 0-based i_pointer - 1 */
+                double weight_upper = 0.0;
+                if (moist) {
+                    const double mrh = IX2(aer->mean_rel_humidity, l, i, ndp);
+                    int i_pointer = 1 + (int)(mrh * (nhc - 1));
+                    if (i_pointer < 1) i_pointer = 1;
+                    if (i_pointer > nhc - 1) i_pointer = nhc - 1;
+                    ip = i_pointer - 1;
+                    weight_upper = (mrh - d->aerosol_humidities[(size_t)ip + (size_t)ndh * j]) / delta_humidity;
+                }
+                double ab = AEROSOL_TAB(d->aerosol_abs, ip), sc = AEROSOL_TAB(d->aerosol_scat, ip);
+                double g = AEROSOL_PHF(ip, 0);
+                if (moist) {
+                    ab = ab + weight_upper * (AEROSOL_TAB(d->aerosol_abs, ip + 1) - AEROSOL_TAB(d->aerosol_abs, ip));
+                    sc = sc + weight_upper * (AEROSOL_TAB(d->aerosol_scat, ip + 1) - AEROSOL_TAB(d->aerosol_scat, ip));
+                    g = g + weight_upper * (AEROSOL_PHF(ip + 1, 0) - AEROSOL_PHF(ip, 0));
+                }
+                IX2(w->k_grey_tot, l, i, wp) = IX2(w->k_grey_tot, l, i, wp) + mmr * ab;
+                const double k_scatter = mmr * sc;
+                IX2(w->k_ext_scat, l, i, wp) = IX2(w->k_ext_scat, l, i, wp) + k_scatter;
+                IX2(w->phase_fnc, l, i, wp) = IX2(w->phase_fnc, l, i, wp) + k_scatter * g;
+                if (c->l_rescale) {
+                    double f;
+                    if (!hg) {
+                        const int m = c->n_order_forward - 1;
+                        f = AEROSOL_PHF(ip, m);
+                        if (moist) f = f + weight_upper * (AEROSOL_PHF(ip + 1, m) - AEROSOL_PHF(ip, m));
+                        f = k_scatter * f;
+                    } else if (c->n_order_forward == 1) {
+                        f = k_scatter * g;
+                    } else if (c->n_order_forward == 2) {
+                        f = k_scatter * g * g;
+                    } else {
+                        f = k_scatter * pow(g, (double)c->n_order_forward);
+                    }
+                    IX2(w->forward_scatter, l, i, wp) = IX2(w->forward_scatter, l, i, wp) + f;
+                }
+            }
+#undef AEROSOL_PHF
+#undef AEROSOL_TAB
+    }
+    return SOCGPU_I_NORMAL;
+}
+
 static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *dm,
                          const socgpu_spectrum_desc *d, const socgpu_atm *atm, const socgpu_aer *aer,
                          const socgpu_cld *cld, int b, int l_cloud)
@@ -623,6 +706,10 @@ static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *d
         if (d->i_rayleigh_scheme != SOCGPU_IP_RAYLEIGH_TOTAL || !d->rayleigh_coeff) return SOCGPU_I_ERR_FATAL;
         for (int i = 0; i < n_layer; ++i)
             for (int l = 0; l < n_profile; ++l) IX2(w->k_ext_scat, l, i, wp) = d->rayleigh_coeff[b];
+    }
+    if (c->l_aerosol && aer && aer->n_aerosol_mr > 0) {
+        int st = opt_prop_aerosol(w, c, dm, d, aer, b);
+        if (st != SOCGPU_I_NORMAL) return st;
     }
     if (c->l_aerosol_mode && aer && aer->n_mode > 0) {
         int ndm = dm->nd_aerosol_mode;
@@ -1710,6 +1797,8 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
             aerv.mode_mix_ratio += p0; aerv.mode_absorption += p0;
             aerv.mode_scattering += p0; aerv.mode_asymmetry += p0;
         }
+        if (aerv.n_aerosol_mr > 0 && aerv.mix_ratio) aerv.mix_ratio += p0;
+        if (aerv.mean_rel_humidity) aerv.mean_rel_humidity += p0;
     }
     socgpu_cld cldv, *cld = NULL;
     if (cld0 && (l_cloud || l_region)) {

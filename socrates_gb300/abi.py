@@ -35,13 +35,16 @@ IP_SCALE_NULL, IP_SCALE_BAND, IP_SCALE_TERM = 0, 1, 2
 IP_SCALE_FNC_NULL, IP_SCALE_POWER_LAW, IP_SCALE_POWER_QUAD, IP_SCALE_DOPPLER_QUAD = 0, 1, 2, 3
 IP_SCALE_WENYI, IP_SCALE_LOOKUP, IP_SCALE_T_LOOKUP = 4, 9, 10
 IP_RAYLEIGH_TOTAL = 1
+IP_AEROSOL_PARAM_DRY, IP_AEROSOL_PARAM_MOIST, IP_AEROSOL_UNPARAMETRIZED = 1, 2, 3
+IP_AEROSOL_PARAM_PHF_DRY, IP_AEROSOL_PARAM_PHF_MOIST = 4, 5
+IP_AERSRC_CUSACK_RON, IP_AERSRC_CLASSIC_RON, IP_AERSRC_ARCL_RON = 0, 1, 2
 IP_MAX_RAND, IP_RAND, IP_EXPONENTIAL, IP_EXPONENTIAL_RAND = 0, 1, 2, 3
 IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0, 1, 2
 
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RNG_LCG, RNG_PHILOX = 0, 1
 NOALLOC_MAX_CLOUD_LAYERS = 1024   # SOCGPU_NOALLOC_MAX_CLOUD_LAYERS
-ABI_VERSION = 4
+ABI_VERSION = 5
 IP_SELF_CONTINUUM, IP_FRN_CONTINUUM = 1, 2
 
 _dp = C.POINTER(C.c_double)
@@ -73,6 +76,11 @@ class SpectrumDesc(C.Structure):
         # CO2/O3 tables of ip_scale_wenyi
         ("wenyi_n_term4", C.c_int), ("wenyi_n_term6", C.c_int), ("wenyi_plg", _dp), ("wenyi_ttb", _dp),
         ("wenyi_tto", _dp), ("wenyi_gk250b", _dp), ("wenyi_gk4", _dp), ("wenyi_gk6", _dp),
+        # classic aerosol species (block 11)
+        ("n_aerosol", C.c_int), ("nd_aerosol_species", C.c_int), ("nd_humidity", C.c_int),
+        ("nd_phase_term", C.c_int), ("type_aerosol", _ip), ("i_aerosol_parm", _ip), ("nhumidity", _ip),
+        ("n_aerosol_phf_term", _ip), ("aerosol_humidities", _dp), ("aerosol_abs", _dp), ("aerosol_scat", _dp),
+        ("aerosol_phf", _dp),
     ]
 
 
@@ -85,6 +93,7 @@ class Control(C.Structure):
         ("l_rayleigh", C.c_int), ("l_gas", C.c_int), ("l_aerosol_mode", C.c_int), ("l_flux_div", C.c_int),
         ("first_band", C.c_int), ("last_band", C.c_int), ("weight_band", _dp), ("precision", C.c_int),
         ("l_continuum", C.c_int), ("l_mixing_ratio", C.c_int), ("l_grey_single", C.c_int),
+        ("l_aerosol", C.c_int), ("l_henyey_greenstein_pf", C.c_int),
     ]
 
 
@@ -92,7 +101,7 @@ class Dimen(C.Structure):
     _fields_ = [
         ("nd_profile", C.c_int), ("nd_layer", C.c_int), ("id_cloud_top", C.c_int), ("nd_aerosol_mode", C.c_int),
         ("nd_cloud_component", C.c_int), ("nd_cloud_type", C.c_int), ("nd_subcol_gen", C.c_int),
-        ("nd_subcol_req", C.c_int),
+        ("nd_subcol_req", C.c_int), ("nd_aerosol_mr", C.c_int),
     ]
 
 
@@ -144,6 +153,8 @@ class Aer(C.Structure):
     _fields_ = [
         ("n_mode", C.c_int), ("mode_mix_ratio", _dp), ("mode_absorption", _dp),
         ("mode_scattering", _dp), ("mode_asymmetry", _dp),
+        ("n_aerosol_mr", C.c_int), ("mix_ratio", _dp), ("mr_type_index", _ip), ("mr_source", _ip),
+        ("mean_rel_humidity", _dp),
     ]
 
 

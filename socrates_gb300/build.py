@@ -46,10 +46,13 @@ def units() -> list[tuple[Path, str, list[str]]]:
             for prec, lanes_list in FLUX_LANES.items():
                 for mode in (0, 1, 2):
                     for lanes in lanes_list:
-                        flags = [f"-DSOCGPU_PREC={prec}", f"-DSOCGPU_MODE={mode}", f"-DSOCGPU_LANES={lanes}"]
-                        if prec == 1:
-                            flags.append("-use_fast_math")
-                        out.append((src, f"flux_{prec}_{mode}_{lanes}", flags))
+                        # one object per source (1 solar, 2 infra-red)
+                        for src_id, tag in ((2, "ir"), (1, "sw")) if mode else ((2, "ir"),):
+                            flags = [f"-DSOCGPU_PREC={prec}", f"-DSOCGPU_MODE={mode}", f"-DSOCGPU_LANES={lanes}",
+                                     f"-DSOCGPU_SRC={src_id}"]
+                            if prec == 1:
+                                flags.append("-use_fast_math")
+                            out.append((src, f"flux_{prec}_{mode}_{lanes}_{tag}", flags))
         elif src.name == "flux_phased.cu":
             for prec in (0, 1):
                 for mode in (0, 1):

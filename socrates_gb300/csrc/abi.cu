@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <set>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -427,6 +428,49 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
         ice[((size_t)t * d->n_band + b) * kCloudParm + c] =
             d->ice_parm_list[(size_t)c + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * t)];
   std::vector<float> drop_f(drop.begin(), drop.end()), ice_f(ice.begin(), ice.end());
+  // classic aerosol species (block 11): one row per (band, species,
+  // humidity) of absorption, scattering and the phase-function moments
+  std::vector<double> aer_tab, aer_hum;
+  e.aer_parm.clear(); e.aer_nhum.clear(); e.aer_nphf.clear();
+  if (d->n_aerosol > 0 && d->i_aerosol_parm && d->aerosol_abs && d->aerosol_scat && d->aerosol_phf) {
+    if (d->n_aerosol > d->nd_aerosol_species || d->nd_humidity < 1 || d->nd_phase_term < 1) {
+      set_msg(msg, msg_len, "aerosol extents inconsistent (%d species, %d allocated)", d->n_aerosol,
+              d->nd_aerosol_species);
+      return SOCGPU_I_ERR_RANGE;
+    }
+    const int nsp = d->n_aerosol;
+    int nh = 1, nphf = 1;
+    for (int j = 0; j < nsp; ++j) {
+      const int hj = d->nhumidity ? d->nhumidity[j] : 0, fj = d->n_aerosol_phf_term ? d->n_aerosol_phf_term[j] : 1;
+      if (hj > d->nd_humidity || fj > d->nd_phase_term) {
+        set_msg(msg, msg_len, "aerosol species %d: %d humidities or %d moments exceed the allocation", j + 1, hj, fj);
+        return SOCGPU_I_ERR_RANGE;
+      }
+      e.aer_parm.push_back(d->i_aerosol_parm[j]);
+      e.aer_nhum.push_back(hj);
+      e.aer_nphf.push_back(std::max(1, fj));
+      nh = std::max(nh, hj);
+      nphf = std::max(nphf, fj);
+    }
+    s.aer_n_species = nsp; s.aer_nh = nh; s.aer_nphf = nphf;
+    const int row = 2 + nphf, ndh = d->nd_humidity, ndf = d->nd_phase_term, nda = d->nd_aerosol_species;
+    aer_tab.assign((size_t)d->n_band * nsp * nh * row, 0.0);
+    aer_hum.assign((size_t)nsp * nh, 0.0);
+    for (int j = 0; j < nsp; ++j)
+      for (int h = 0; h < std::max(1, e.aer_nhum[j]); ++h)
+        if (d->aerosol_humidities && e.aer_nhum[j] > 0) aer_hum[(size_t)j * nh + h] = d->aerosol_humidities[h + (size_t)ndh * j];
+    for (int b = 0; b < d->n_band; ++b)
+      for (int j = 0; j < nsp; ++j)
+        for (int h = 0; h < std::max(1, e.aer_nhum[j]); ++h) {
+          double *r = &aer_tab[(((size_t)b * nsp + j) * nh + h) * row];
+          const size_t q = (size_t)h + (size_t)ndh * ((size_t)j + (size_t)nda * b);
+          r[0] = d->aerosol_abs[q];
+          r[1] = d->aerosol_scat[q];
+          for (int m = 0; m < e.aer_nphf[j]; ++m)
+            r[2 + m] = d->aerosol_phf[(size_t)h + (size_t)ndh * ((size_t)m + (size_t)ndf * ((size_t)j + (size_t)nda * b))];
+        }
+  }
+  std::vector<float> aer_tab_f(aer_tab.begin(), aer_tab.end()), aer_hum_f(aer_hum.begin(), aer_hum.end());
   cudaGetDevice(&e.device);
   // the tables of lookup scaling, equivalent extinction and Wen-Yi scaling
   auto up = [&](auto *&dst, const auto &v) -> bool {
@@ -439,7 +483,9 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   std::vector<float> tgas_f(tgas.begin(), tgas.end()), wy_f(wy.begin(), wy.end());
   if (!up(s.bands_keqv, bands_keqv) || !up(s.gpoints_keqv, gpoints_keqv) || !up(s.minor_terms, minor) ||
       !up(s.lk_grid, grid) || !up(s.lk_grid_f, grid_f) || !up(s.k_lookup, k_lk) || !up(s.k_lookup_f, k_lk_f) ||
-      !up(s.t_lookup_gas, tgas) || !up(s.t_lookup_gas_f, tgas_f) || !up(s.wenyi, wy) || !up(s.wenyi_f, wy_f)) {
+      !up(s.t_lookup_gas, tgas) || !up(s.t_lookup_gas_f, tgas_f) || !up(s.wenyi, wy) || !up(s.wenyi_f, wy_f) ||
+      !up(s.aer_tab, aer_tab) || !up(s.aer_tab_f, aer_tab_f) || !up(s.aer_hum, aer_hum) ||
+      !up(s.aer_hum_f, aer_hum_f)) {
     cudaGetLastError();
     set_msg(msg, msg_len, "device allocation or upload of lookup and overlap tables failed");
     return SOCGPU_I_ABORT_CALCULATION;
@@ -481,6 +527,10 @@ void free_spectrum(SpectrumEntry &e) {
   cudaFree(e.dev.t_lookup_gas_f);
   cudaFree(e.dev.wenyi);
   cudaFree(e.dev.wenyi_f);
+  cudaFree(e.dev.aer_tab);
+  cudaFree(e.dev.aer_tab_f);
+  cudaFree(e.dev.aer_hum);
+  cudaFree(e.dev.aer_hum_f);
   cudaFree(e.dev.bands);
   cudaFree(e.dev.gpoints);
   cudaFree(e.dev.drop_parm);
@@ -500,15 +550,16 @@ SpectrumEntry *find_spectrum(int h) {
 // ---------------------------------------------------------------------------
 // Kernel variants and tile choice.
 namespace {
-#define SOCGPU_VARIANT(p, m, l) {p, m, l, launch_flux_##p##_##m##_##l, prepare_flux_##p##_##m##_##l}
+#define SOCGPU_VARIANT(p, m, l) \
+  {p, m, l, launch_flux_##p##_##m##_##l, prepare_flux_##p##_##m##_##l, preload_flux_##p##_##m##_##l}
 const FluxVariant kVariants[] = {
     SOCGPU_VARIANT(0, 0, 16), SOCGPU_VARIANT(0, 0, 32), SOCGPU_VARIANT(0, 1, 16), SOCGPU_VARIANT(0, 1, 32),
     SOCGPU_VARIANT(0, 2, 16), SOCGPU_VARIANT(0, 2, 32), SOCGPU_VARIANT(1, 0, 8),  SOCGPU_VARIANT(1, 0, 16),
     SOCGPU_VARIANT(1, 0, 32), SOCGPU_VARIANT(1, 1, 8),  SOCGPU_VARIANT(1, 1, 16), SOCGPU_VARIANT(1, 1, 32),
     SOCGPU_VARIANT(1, 2, 8),  SOCGPU_VARIANT(1, 2, 16), SOCGPU_VARIANT(1, 2, 32),
     // the phased kernel: single-batch launches only
-    {0, 0, 1, launch_phased_0_0, nullptr}, {0, 1, 1, launch_phased_0_1, nullptr},
-    {1, 0, 1, launch_phased_1_0, nullptr}, {1, 1, 1, launch_phased_1_1, nullptr},
+    {0, 0, 1, launch_phased_0_0, nullptr, nullptr}, {0, 1, 1, launch_phased_0_1, nullptr, nullptr},
+    {1, 0, 1, launch_phased_1_0, nullptr, nullptr}, {1, 1, 1, launch_phased_1_1, nullptr, nullptr},
 };
 #undef SOCGPU_VARIANT
 }  // namespace
@@ -517,6 +568,22 @@ const FluxVariant *find_variant(int precision, int mode, int lanes) {
   for (const FluxVariant &v : kVariants)
     if (v.precision == precision && v.mode == mode && v.lanes == lanes) return &v;
   return nullptr;
+}
+
+int preload_kernels() {
+  static std::mutex m;
+  static std::set<int> loaded;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SOCGPU_I_ABORT_CALCULATION; }
+  std::lock_guard<std::mutex> lk(m);
+  if (loaded.count(dev)) return SOCGPU_I_NORMAL;
+  for (const FluxVariant &v : kVariants)
+    if (v.preload) {
+      const int st = v.preload();
+      if (st != 0) return st;
+    }
+  loaded.insert(dev);
+  return SOCGPU_I_NORMAL;
 }
 
 // Tile overrides (socgpu_set_tile_config) and the tuner's table, keyed by
@@ -664,6 +731,52 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     if (!aer->mode_mix_ratio || !aer->mode_absorption || !aer->mode_scattering || !aer->mode_asymmetry) {
       set_msg(msg, msg_len, "missing aerosol mode fields"); return SOCGPU_I_ERR_FATAL; }
   }
+  if (c->l_aerosol) {
+    // classic aerosol species (radiance_calc.F90:603-626, opt_prop_aerosol.F90)
+    const int nsp = (int)sp->aer_parm.size();
+    if (nsp == 0) {
+      set_msg(msg, msg_len, "aerosols requested but the spectral file has no aerosol species (block 11)");
+      return SOCGPU_I_ERR_FATAL;
+    }
+    if (!aer || aer->n_aerosol_mr < 0 || aer->n_aerosol_mr > dm->nd_aerosol_mr) {
+      set_msg(msg, msg_len, "aerosol mixing-ratio entries %d outside 0..nd_aerosol_mr", aer ? aer->n_aerosol_mr : -1);
+      return SOCGPU_I_ERR_RANGE;
+    }
+    if (aer->n_aerosol_mr > 0 && (!aer->mix_ratio || !aer->mr_type_index)) {
+      set_msg(msg, msg_len, "missing aerosol mixing ratios or their species"); return SOCGPU_I_ERR_FATAL; }
+    int active = 0;
+    bool moist = false;
+    for (int k = 0; k < aer->n_aerosol_mr; ++k) {
+      const int src = aer->mr_source ? aer->mr_source[k] : SOCGPU_IP_AERSRC_CLASSIC_RON;
+      if (src < SOCGPU_IP_AERSRC_CUSACK_RON || src > SOCGPU_IP_AERSRC_ARCL_RON) continue;   // radiatively inactive
+      const int j = aer->mr_type_index[k];
+      if (j < 1 || j > nsp) {
+        set_msg(msg, msg_len, "aerosol entry %d: species %d is not in the spectral file", k + 1, j);
+        return SOCGPU_I_ERR_RANGE;
+      }
+      const int parm = sp->aer_parm[j - 1];
+      if (parm != SOCGPU_IP_AEROSOL_PARAM_DRY && parm != SOCGPU_IP_AEROSOL_PARAM_MOIST &&
+          parm != SOCGPU_IP_AEROSOL_PARAM_PHF_DRY && parm != SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST) {
+        set_msg(msg, msg_len, "aerosol species %d: parametrization %d is not supported", j, parm);
+        return SOCGPU_I_ERR_FATAL;
+      }
+      if (parm == SOCGPU_IP_AEROSOL_PARAM_MOIST || parm == SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST) {
+        moist = true;
+        if (sp->aer_nhum[j - 1] < 2) {
+          set_msg(msg, msg_len, "moist aerosol species %d has fewer than two humidities", j); return SOCGPU_I_ERR_FATAL; }
+      }
+      if ((parm == SOCGPU_IP_AEROSOL_PARAM_PHF_DRY || parm == SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST) && c->l_rescale &&
+          !c->l_henyey_greenstein_pf && c->n_order_forward > sp->aer_nphf[j - 1]) {
+        set_msg(msg, msg_len, "aerosol species %d has %d phase-function moments; forward scattering needs %d", j,
+                sp->aer_nphf[j - 1], c->n_order_forward);
+        return SOCGPU_I_ERR_FATAL;
+      }
+      if (++active > kMaxAerMr) {
+        set_msg(msg, msg_len, "more than %d active aerosol entries", kMaxAerMr); return SOCGPU_I_ERR_RANGE; }
+    }
+    if (moist && !aer->mean_rel_humidity) {
+      set_msg(msg, msg_len, "moist aerosols need the mean relative humidity"); return SOCGPU_I_ERR_FATAL; }
+  }
   if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA || region) {
     if (!cld || !cld->type_condensed || !cld->i_cloud_type || !cld->i_condensed_param || !cld->i_condensed_type ||
         !cld->condensed_mix_ratio || !cld->condensed_dim_char || !cld->w_cloud || !cld->frac_cloud) {
@@ -780,6 +893,33 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
     p.mode_mix_ratio = aer->mode_mix_ratio; p.mode_absorption = aer->mode_absorption;
     p.mode_scattering = aer->mode_scattering; p.mode_asymmetry = aer->mode_asymmetry;
   }
+  if (c->l_aerosol && aer && aer->n_aerosol_mr > 0 && !sp->aer_parm.empty()) {
+    // the active entries, in order (opt_prop_aerosol.F90:273-283)
+    for (int k = 0; k < aer->n_aerosol_mr && p.n_aer_mr < kMaxAerMr; ++k) {
+      const int src = aer->mr_source ? aer->mr_source[k] : SOCGPU_IP_AERSRC_CLASSIC_RON;
+      if (src < SOCGPU_IP_AERSRC_CUSACK_RON || src > SOCGPU_IP_AERSRC_ARCL_RON) continue;
+      const int j = aer->mr_type_index[k] - 1;
+      p.aer_entry[p.n_aer_mr] = k;
+      p.aer_species[p.n_aer_mr] = j;
+      p.aer_parm[p.n_aer_mr] = sp->aer_parm[j];
+      ++p.n_aer_mr;
+    }
+    p.l_aerosol = p.n_aer_mr > 0;
+    p.l_hg = c->l_henyey_greenstein_pf;
+    p.aer_n_species = sp->dev.aer_n_species; p.aer_nh = sp->dev.aer_nh; p.aer_nphf = sp->dev.aer_nphf;
+    // one humidity table for all moist species: that of the last one
+    // (radiance_calc.F90:606-623)
+    p.aer_nh_common = 0;
+    for (size_t j = 0; j < sp->aer_parm.size(); ++j)
+      if (sp->aer_parm[j] == SOCGPU_IP_AEROSOL_PARAM_MOIST || sp->aer_parm[j] == SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST)
+        p.aer_nh_common = sp->aer_nhum[j];
+    p.aer_dhum = p.aer_nh_common > 1 ? 1.0 / ((double)p.aer_nh_common - 1.0) : 0.0;
+    p.aer_dhum_f = (float)p.aer_dhum;
+    p.aer_mix_ratio = aer->mix_ratio;
+    p.mean_rel_humidity = aer->mean_rel_humidity;
+    p.aer_tab = sp->dev.aer_tab; p.aer_tab_f = sp->dev.aer_tab_f;
+    p.aer_hum = sp->dev.aer_hum; p.aer_hum_f = sp->dev.aer_hum_f;
+  }
   if (p.mcica) {
     p.n_condensed = cld->n_condensed; p.n_cloud_type = cld->n_cloud_type;
     for (int k = 0; k < cld->n_condensed; ++k) {
@@ -857,6 +997,13 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
     o_aab = plan.add(ae->mode_absorption, D, ndp, np, ndl * ndm * nb);
     o_asc = plan.add(ae->mode_scattering, D, ndp, np, ndl * ndm * nb);
     o_aas = plan.add(ae->mode_asymmetry, D, ndp, np, ndl * ndm * nb);
+  }
+  // classic aerosol: the mixing ratios of every entry, and the humidity
+  o_xmr = o_mrh = none;
+  classic = c->l_aerosol && ae && ae->n_aerosol_mr > 0 && ae->mix_ratio;
+  if (classic) {
+    o_xmr = plan.add(ae->mix_ratio, D, ndp, np, ndl * (size_t)ae->n_aerosol_mr);
+    if (ae->mean_rel_humidity) o_mrh = plan.add(ae->mean_rel_humidity, D, ndp, np, nl);
   }
   o_wb = c->weight_band ? plan.add(c->weight_band, D, nb, nb, 1, false, nullptr, false) : none;
   o_cmr = o_cdc = o_wc = o_fc = o_cs = o_fcl = o_nsc = o_sk = o_fsk = o_sro = none;
@@ -938,6 +1085,7 @@ void window_params(FluxParams &p, int c0, int n) {
   mv(p.p); mv(p.t); mv(p.t_level); mv(p.mass); mv(p.gas_mix_ratio); mv(p.density);
   mv(p.zen_0); mv(p.solar_irrad); mv(p.rho_alb); mv(p.t_ground); mv(p.flux_ground);
   mv(p.mode_mix_ratio); mv(p.mode_absorption); mv(p.mode_scattering); mv(p.mode_asymmetry);
+  mv(p.aer_mix_ratio); mv(p.mean_rel_humidity);
   mv(p.condensed_mix_ratio); mv(p.condensed_dim_char); mv(p.w_cloud); mv(p.frac_cloud);
   mv(p.c_sub); mv(p.frac_cloudy); mv(p.n_subcol_cld);
   mv(p.flux_up); mv(p.flux_down); mv(p.flux_direct); mv(p.flux_div); mv(p.heating_rate);
@@ -955,10 +1103,13 @@ void StagedCall::params(char *base, FluxParams &p) const {
   b2.rho_alb = (const double *)dptr(o_alb); b2.t_ground = (const double *)dptr(o_tg);
   b2.flux_ground = (const double *)dptr(o_fg);
   socgpu_aer e2{};
-  if (aero) {
-    e2 = *aer;
+  if (aero || classic) {
+    e2 = *aer;    // the entries' species and sources stay host arrays
     e2.mode_mix_ratio = (const double *)dptr(o_amr); e2.mode_absorption = (const double *)dptr(o_aab);
     e2.mode_scattering = (const double *)dptr(o_asc); e2.mode_asymmetry = (const double *)dptr(o_aas);
+    if (!aero) e2.n_mode = 0;
+    e2.mix_ratio = (const double *)dptr(o_xmr);
+    e2.mean_rel_humidity = (const double *)dptr(o_mrh);
   }
   socgpu_cld c2{};
   if (mc) {
@@ -974,7 +1125,7 @@ void StagedCall::params(char *base, FluxParams &p) const {
   r2.flux_up = (double *)dptr(o_fu); r2.flux_down = (double *)dptr(o_fd);
   r2.flux_direct = (double *)dptr(o_fdir); r2.flux_div = (double *)dptr(o_div);
   r2.heating_rate = (double *)dptr(o_hr);
-  fill_params(p, control, dimen, sp, &a2, mc ? &c2 : nullptr, aero ? &e2 : nullptr, &b2, &r2,
+  fill_params(p, control, dimen, sp, &a2, mc ? &c2 : nullptr, (aero || classic) ? &e2 : nullptr, &b2, &r2,
               (const double *)dptr(o_wb));
 }
 

@@ -290,7 +290,9 @@ constexpr int kMaxDevices = 64;
 int *g_noalloc_addr[kMaxDevices] = {};
 
 // Device address of the scratch on the current device, looked up once per
-// device (the first call on a device does this setup).
+// device (the first call on a device does this setup).  The address holds for
+// the life of the device's primary context; the header tells callers not to
+// use this entry point after destroying that context (cudaDeviceReset).
 int noalloc_scratch(int **out, char *msg, size_t len) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

@@ -695,6 +695,7 @@ struct FluxKernel {
       // grey optics: grey_opt_prop.F90:470-790 (Rayleigh, modal aerosol)
       R kes = p.l_rayleigh ? (kFP64 ? (R)bd.rayleigh_coeff : (R)bd.rayleigh_f) : R(0);
       R kabs = R(0), phf = R(0), fwd = R(0);
+      if (p.l_aerosol) classic_aerosol(p, col, i, b, kabs, kes, phf, fwd);
       if (p.l_aerosol_mode) {
         for (int j = 0; j < p.n_mode; ++j) {
           R mmr = load_in<R>(p.mode_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * j));
@@ -823,6 +824,60 @@ struct FluxKernel {
             S.dB2[q] = 2.0f * (planck_diff_mix(bd.planck_f, p.n_deg_fit, x1, xl) +
                                planck_diff_mix(bd.planck_f, p.n_deg_fit, x0, xl));
           }
+        }
+      }
+    }
+  }
+
+  // Classic aerosol species in cell (col, i) of band b (opt_prop_aerosol.F90:
+  // 273-640 for two-stream phase functions): each active mixing-ratio entry
+  // adds its absorption and scattering, interpolated in the layer's mean
+  // relative humidity for moist species (radiance_calc.F90:617-623 for the
+  // pointer into the common humidity table, clamped to the table here), the
+  // first phase-function moment (the asymmetry) and, with rescaling, the
+  // forward-scattering moment: a power of the asymmetry for Henyey-Greenstein
+  // species, the tabulated moment n_order_forward otherwise.
+  __device__ static __forceinline__ void classic_aerosol(const FluxParams &p, int col, int i, int b, R &kabs,
+                                                         R &kes, R &phf, R &fwd) {
+    const int ndp = p.nd_profile, ndl = p.nd_layer;
+    const int row = 2 + p.aer_nphf;
+    const R *tab, *hum;
+    if constexpr (kFP64) { tab = p.aer_tab; hum = p.aer_hum; } else { tab = p.aer_tab_f; hum = p.aer_hum_f; }
+    const R dhum = kFP64 ? (R)p.aer_dhum : (R)p.aer_dhum_f;
+    for (int e = 0; e < p.n_aer_mr; ++e) {
+      const int j = p.aer_species[e], parm = p.aer_parm[e];
+      const R mmr = load_in<R>(p.aer_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * p.aer_entry[e]));
+      const R *t0 = tab + ((size_t)b * p.aer_n_species + j) * p.aer_nh * row;
+      const bool moist = parm == SOCGPU_IP_AEROSOL_PARAM_MOIST || parm == SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST;
+      R wu = R(0);
+      const R *t1 = t0;
+      if (moist) {
+        const R mrh = load_in<R>(p.mean_rel_humidity + (size_t)col + (size_t)ndp * i);
+        int ip = 1 + (int)(mrh * (R)(p.aer_nh_common - 1));
+        ip = ip < 1 ? 1 : (ip > p.aer_nh_common - 1 ? p.aer_nh_common - 1 : ip);
+        wu = (mrh - hum[(size_t)j * p.aer_nh + ip - 1]) / dhum;
+        t0 = t0 + (size_t)(ip - 1) * row;
+        t1 = t0 + row;
+      }
+      auto at = [&](int c) { return moist ? t0[c] + wu * (t1[c] - t0[c]) : t0[c]; };
+      kabs = kabs + mmr * at(0);
+      const R ks = mmr * at(1);
+      kes = kes + ks;
+      const R g = at(2);
+      phf = phf + ks * g;
+      if (p.l_rescale) {
+        const bool hg = p.l_hg || parm == SOCGPU_IP_AEROSOL_PARAM_DRY || parm == SOCGPU_IP_AEROSOL_PARAM_MOIST;
+        const int nof = p.n_order_forward;
+        if (!hg) {
+          fwd = fwd + ks * at(1 + nof);
+        } else if (nof == 1) {
+          fwd = fwd + ks * g;
+        } else if (nof == 2) {
+          fwd = fwd + ks * g * g;
+        } else {
+          R gp = R(1);
+          for (int o = 0; o < nof; ++o) gp *= g;
+          fwd = fwd + ks * gp;
         }
       }
     }

@@ -157,34 +157,36 @@ int launch_shapes(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, c
 }
 
 
-// The source (solar or infra-red) picks the kernel at run time; the
-// no-scatter family is infra-red only.
-template <class R, bool MIX, bool NOSCAT, bool MCICA, int P, int... CH>
+// The kernels of one source (SOCGPU_IP_SOLAR or SOCGPU_IP_INFRA_RED) over the
+// chunk list; the build compiles the two sources as separate objects and the
+// infra-red object's entry points hand solar work to the solar one.
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int SRC, int P, int... CH>
 int launch_chunks(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char *msg, size_t len) {
-  if constexpr (NOSCAT) {
-    return launch_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_INFRA_RED, Shape<P, CH>...>(p, cfg, st, msg, len);
-  } else {
-    if (p.isolir == SOCGPU_IP_INFRA_RED)
-      return launch_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_INFRA_RED, Shape<P, CH>...>(p, cfg, st, msg, len);
-    return launch_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_SOLAR, Shape<P, CH>...>(p, cfg, st, msg, len);
-  }
+  return launch_shapes<R, MIX, NOSCAT, MCICA, SRC, Shape<P, CH>...>(p, cfg, st, msg, len);
 }
 
-template <class R, bool MIX, bool NOSCAT, bool MCICA, int P, int... CH>
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int SRC, int P, int... CH>
 int prepare_chunks(BatchGroup &g, char *msg, size_t len) {
-  const int src = g.n_items > 0 ? g.items[0].isolir : SOCGPU_IP_INFRA_RED;
   for (int i = 0; i < g.n_items; ++i)
-    if (g.items[i].isolir != src) {
+    if (g.items[i].isolir != SRC) {
       snprintf(msg, len, "a kernel class mixes solar and infra-red batches");
       return SOCGPU_I_ERR_FATAL;
     }
-  if constexpr (NOSCAT) {
-    return prepare_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_INFRA_RED, Shape<P, CH>...>(g, msg, len);
-  } else {
-    if (src == SOCGPU_IP_INFRA_RED)
-      return prepare_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_INFRA_RED, Shape<P, CH>...>(g, msg, len);
-    return prepare_shapes<R, MIX, NOSCAT, MCICA, SOCGPU_IP_SOLAR, Shape<P, CH>...>(g, msg, len);
-  }
+  return prepare_shapes<R, MIX, NOSCAT, MCICA, SRC, Shape<P, CH>...>(g, msg, len);
+}
+
+// Load every kernel of the chunk list onto the device now (cudaFuncGetAttributes
+// loads a lazily-loaded function): a first launch that loads its module can
+// wait for kernels already running, which a request server must not do.
+template <class R, bool MIX, bool NOSCAT, bool MCICA, int SRC, int P, int... CH>
+int preload_chunks() {
+  cudaFuncAttributes a{};
+  bool ok = true;
+  ((ok = ok && cudaFuncGetAttributes(&a, flux_kernel<R, MIX, P, CH, NOSCAT, MCICA, SRC>) == cudaSuccess), ...);
+  ((ok = ok && cudaFuncGetAttributes(&a, flux_kernel_batched<R, MIX, P, CH, NOSCAT, MCICA, SRC>) == cudaSuccess),
+   ...);
+  if (!ok) cudaGetLastError();
+  return ok ? 0 : SOCGPU_I_ABORT_CALCULATION;
 }
 
 }  // namespace socgpu

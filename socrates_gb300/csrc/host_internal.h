@@ -35,6 +35,9 @@ struct SpectrumEntry {
   std::vector<int> drop_scheme, ice_scheme;   // scheme of each droplet / ice type, 0 where undefined
   int n_cloud_parameter = 0;          // coefficients per parameter set in the spectrum
   std::vector<int> n_k_major;         // k-terms of each band's first absorber (McICA tables)
+  // classic aerosol species (block 11): parametrization, humidities and
+  // phase-function moments of each, for validation
+  std::vector<int> aer_parm, aer_nhum, aer_nphf;
   int device = 0;
 };
 
@@ -59,8 +62,12 @@ struct FluxVariant {
   int precision, mode, lanes;
   LaunchFn launch;
   PrepareFn prepare;
+  int (*preload)();
 };
 const FluxVariant *find_variant(int precision, int mode, int lanes);
+// Loads every scan-kernel variant onto the current device (once per process
+// and device); returns 0 or a SOCGPU_I_* status.
+int preload_kernels();
 
 // The kernel parameters of columns c0 .. c0+n-1 of a launch (every
 // per-column pointer moved by c0; the leading extents stay).
@@ -109,8 +116,9 @@ struct StagedCall {
   const socgpu_aer *aer = nullptr;
   const socgpu_bound *bound = nullptr;
   socgpu_radout *radout = nullptr;
-  bool sw = false, mc = false, aero = false;
+  bool sw = false, mc = false, aero = false, classic = false;
   size_t o_p, o_t, o_tl, o_m, o_g, o_rho, o_z, o_si, o_alb, o_tg, o_amr, o_aab, o_asc, o_aas, o_wb, o_fg = (size_t)-1;
+  size_t o_xmr = (size_t)-1, o_mrh = (size_t)-1;   // classic aerosol mixing ratios, mean relative humidity
   size_t o_cmr, o_cdc, o_wc, o_fc, o_cs, o_fcl, o_nsc, o_sk, o_fsk, o_sro;
   size_t o_fu, o_fd, o_fdir, o_div, o_hr;
 

@@ -13,8 +13,10 @@
 // Requests are of two size classes.  Small ones (at most
 // small_column_gpoints column x g-points) are waved on high-priority streams
 // and large ones on low-priority streams (a low-priority slot takes small
-// requests only when no large one waits), so that a small request never
-// shares a wave with a large one.  Each kernel class of a wave (precision,
+// requests only when no large one waits or runs), so that a small request
+// never shares a wave, or a stream priority, with a large one.  Every kernel
+// is loaded onto the device when the server is created: a first launch that
+// loaded its module could wait for the kernels already running.  Each kernel class of a wave (precision,
 // mode, tile) is one launch of the batched kernel with one CTA per column: as
 // the CTAs of a large wave retire, the block scheduler gives the SMs to the
 // pending CTAs of high-priority streams first, so a small request that
@@ -124,6 +126,7 @@ struct Request {
 struct StreamSlot {
   cudaStream_t stream = nullptr;
   bool high = false;                  // high priority: waves of small requests
+  bool small_wave = false;            // the wave in flight is of small requests
   std::vector<cudaEvent_t> done;      // one per request of the wave, in wave order
   FluxParams *d_items = nullptr, *h_items = nullptr;     // per-wave kernel tables
   long long *d_start = nullptr, *h_start = nullptr;
@@ -347,12 +350,18 @@ void worker_main(socgpu_server_s *Sp) {
       if (sl.busy || S.pending.empty()) continue;
       std::vector<Request *> wave;
       // high-priority slots take small requests; the others large ones
-      // first, and small ones when no large request waits
+      // first, and small ones when no large request waits or runs (a small
+      // wave on a low-priority stream would queue behind a large wave's CTAs)
       bool small = sl.high;
       take(small, wave);
-      if (wave.empty() && !sl.high) { small = true; take(true, wave); }
+      if (wave.empty() && !sl.high) {
+        bool large_running = false;
+        for (const StreamSlot &x : S.slots) large_running |= x.busy && !x.small_wave;
+        if (!large_running) { small = true; take(true, wave); }
+      }
       if (wave.empty()) continue;
       sl.busy = true;
+      sl.small_wave = small;
       sl.n_retired = 0;
       sl.reqs = std::move(wave);
       S.stats.waves += 1;
@@ -413,6 +422,12 @@ int socgpu_server_create(const socgpu_server_config *config, socgpu_server *serv
   }
   std::unique_ptr<socgpu_server_s> S(new socgpu_server_s);
   CUDA_TRY(cudaGetDevice(&S->device));
+  // every kernel loaded before the first wave, so that no launch waits on a
+  // module load behind a long-running kernel of another wave
+  if (preload_kernels() != SOCGPU_I_NORMAL) {
+    set_msg(msg, msg_len, "the flux kernels could not be loaded onto the device");
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
   int prio_low = 0, prio_high = 0;
   CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
   if (cfg.device_bytes == 0) {

@@ -22,6 +22,10 @@ constexpr int kMaxCloudComp = 4;
 // Self-broadened absorbers whose gas fractions a column stages (lookup tables).
 constexpr int kMaxSb = 4;
 
+// Classic aerosol: mixing-ratio entries a launch takes (radiatively active
+// ones), and the widest humidity table and phase-function moments per entry.
+constexpr int kMaxAerMr = 32;
+
 // One absorber of a band (block 4/5 entries for (band, species)).
 struct BandGas {
   int species;     // 0-based species index into gas_mix_ratio
@@ -119,6 +123,13 @@ struct SpectrumDev {
   int wenyi_n4, wenyi_n6;
   double *wenyi;
   float *wenyi_f;
+  // classic aerosol species (block 11): per band, species and humidity the
+  // row (absorption, scattering, phase-function moments 1..aer_nphf)
+  int aer_n_species, aer_nh, aer_nphf;
+  double *aer_tab;                  // [n_band][aer_n_species][aer_nh][2 + aer_nphf]
+  float *aer_tab_f;
+  double *aer_hum;                  // [aer_n_species][aer_nh] humidities of each species' rows
+  float *aer_hum_f;
   double *drop_parm;                // [n_drop_type][n_band][16]
   double *ice_parm;                 // [n_ice_type][n_band][16]
   float *drop_parm_f, *ice_parm_f;  // FP32 copies
@@ -172,6 +183,18 @@ struct FluxParams {
   const int *n_subcol_cld;
   const int *subcol_k, *first_subcol_k, *subcol_reorder;
   int n_subcol_gen, n_subcol_req, nd_band_sp;
+  // classic aerosol (opt_prop_aerosol.F90): the active mixing-ratio entries
+  int l_aerosol, n_aer_mr, l_hg;    // l_hg: Henyey-Greenstein moments for every species
+  int aer_n_species, aer_nh, aer_nphf, aer_nh_common;
+  int aer_entry[kMaxAerMr];         // third index of aer_mix_ratio of each active entry
+  int aer_species[kMaxAerMr];       // its 0-based species
+  int aer_parm[kMaxAerMr];          // the species' SOCGPU_IP_AEROSOL_PARAM_*
+  double aer_dhum;                  // humidity step of the common table, 1 / (aer_nh_common - 1)
+  float aer_dhum_f;
+  const double *aer_mix_ratio;      // (nd_profile, nd_layer, nd_aerosol_mr)
+  const double *mean_rel_humidity;  // (nd_profile, nd_layer), moist species only
+  const double *aer_tab, *aer_hum;
+  const float *aer_tab_f, *aer_hum_f;
   // outputs
   double *flux_up, *flux_down, *flux_direct, *flux_div, *heating_rate;
   int *error_flag;                  // device flag: set when a bound is violated
@@ -259,7 +282,8 @@ inline int smallest_chunk(int precision, int lanes, int n_layer) {
 #define SOCGPU_DECL_FLUX(prec, mode, lanes)                                                             \
   int launch_flux_##prec##_##mode##_##lanes(const FluxParams &p, const TileConfig &cfg, cudaStream_t s, \
                                             char *msg, size_t len);                                    \
-  int prepare_flux_##prec##_##mode##_##lanes(BatchGroup &g, char *msg, size_t len);
+  int prepare_flux_##prec##_##mode##_##lanes(BatchGroup &g, char *msg, size_t len);                     \
+  int preload_flux_##prec##_##mode##_##lanes();
 #define SOCGPU_DECL_FLUX_MODES(prec, lanes) \
   SOCGPU_DECL_FLUX(prec, 0, lanes) SOCGPU_DECL_FLUX(prec, 1, lanes) SOCGPU_DECL_FLUX(prec, 2, lanes)
 SOCGPU_DECL_FLUX_MODES(0, 16)

@@ -53,6 +53,17 @@ bool is_int(const std::string &w) {
   return true;
 }
 
+// a Fortran real or integer literal (1.0E+00, 1.0D-03, -5, .5)
+bool is_number(const std::string &w) {
+  if (w.empty()) return false;
+  bool digit = false;
+  for (char c : w) {
+    if (std::isdigit((unsigned char)c)) digit = true;
+    else if (c != '-' && c != '+' && c != '.' && c != 'E' && c != 'e' && c != 'D' && c != 'd') return false;
+  }
+  return digit;
+}
+
 double num(const std::string &w) {
   std::string t = w;
   for (char &c : t)
@@ -78,7 +89,7 @@ double fixed(const std::string &line, size_t a, size_t b, bool &present) {
 }
 
 struct Block {
-  int type = 0, version = 0;
+  int type = 0, subtype = 0, version = 0;
   std::vector<std::string> lines;
 };
 
@@ -121,6 +132,10 @@ struct SpectralFile {
   std::vector<double> t_gas, k_t_gas;
   // Wen-Yi tables
   std::vector<double> wy_plg, wy_ttb, wy_tto, wy_gk250b, wy_gk4, wy_gk6;
+  // block 11: classic aerosol species
+  int n_aer = 0, nd_hum = 1, nd_phf = 1;
+  std::vector<int> aer_type, aer_parm, aer_nhum, aer_nphf;
+  std::vector<double> aer_hum, aer_abs, aer_scat, aer_phf;
 
   socgpu_spectrum_desc desc() const {
     socgpu_spectrum_desc d{};
@@ -185,6 +200,14 @@ struct SpectralFile {
       d.wenyi_plg = wy_plg.data(); d.wenyi_ttb = wy_ttb.data(); d.wenyi_tto = wy_tto.data();
       d.wenyi_gk250b = wy_gk250b.data(); d.wenyi_gk4 = wy_gk4.data(); d.wenyi_gk6 = wy_gk6.data();
       d.wenyi_n_term4 = (int)wy_gk250b.size(); d.wenyi_n_term6 = (int)(wy_gk6.size() / 234);
+    }
+    if (n_aer > 0) {
+      d.n_aerosol = d.nd_aerosol_species = n_aer;
+      d.nd_humidity = nd_hum; d.nd_phase_term = nd_phf;
+      d.type_aerosol = aer_type.data(); d.i_aerosol_parm = aer_parm.data();
+      d.nhumidity = aer_nhum.data(); d.n_aerosol_phf_term = aer_nphf.data();
+      d.aerosol_humidities = aer_hum.data(); d.aerosol_abs = aer_abs.data();
+      d.aerosol_scat = aer_scat.data(); d.aerosol_phf = aer_phf.data();
     }
     if (!n_band_cont.empty()) {
       d.nd_continuum = ndc;
@@ -390,6 +413,7 @@ bool read_spectral_file(const std::string &path, const std::string &k_path, cons
       blocks.emplace_back();
       cur = &blocks.back();
       cur->type = w.size() > 2 ? std::atoi(w[2].c_str()) : -1;
+      cur->subtype = w.size() > 4 ? std::atoi(w[4].c_str()) : 0;
       cur->version = w.size() > 6 ? std::atoi(w[6].c_str()) : 0;
     } else if (line.rfind("*END", 0) == 0) {
       cur = nullptr;
@@ -718,6 +742,77 @@ bool read_spectral_file(const std::string &path, const std::string &k_path, cons
   };
   place(drops, s.drop_parm, s.drop_ids, s.drop_on, s.drop_lo, s.drop_hi);
   place(ices, s.ice_parm, s.ice_ids, s.ice_on, s.ice_lo, s.ice_hi);
+  // block 11 (read_spectrum.F90:2335-2640): the species' number and type
+  // numbers come from block 0; each block gives one species, dry (subtype 0:
+  // per band the band index, absorption, scattering and the phase-function
+  // moments) or moist (subtype 1: per band one row per humidity of humidity,
+  // absorption, scattering and moments), the values as numeric records after
+  // the header lines
+  for (size_t q = 0; q < b0->lines.size(); ++q) {
+    const std::string u = upper(b0->lines[q]);
+    if (u.find("NUMBER OF AEROSOLS") != std::string::npos) s.n_aer = int_after_eq(u);
+    else if (u.find("INDEXING NUMBERS OF AEROSOLS") != std::string::npos)
+      for (int i = 0; i < s.n_aer && q + 2 + i < b0->lines.size(); ++i) {
+        auto w = split(b0->lines[q + 2 + i]);
+        s.aer_type.push_back(w.size() >= 2 ? std::atoi(w[1].c_str()) : 0);
+      }
+  }
+  if (s.n_aer > 0) {
+    struct Species { bool moist; int rows, nphf; std::vector<double> v; };
+    std::map<int, Species> found;
+    for (const Block &bl : blocks) {
+      if (bl.type != 11) continue;
+      int idx = -1, nh = 1, nphf = 1;
+      std::vector<double> v;
+      for (const std::string &l : bl.lines) {
+        const std::string u = upper(l);
+        if (u.find("INDEX OF SPECIES") != std::string::npos) idx = int_after_eq(u);
+        else if (u.find("NUMBER OF HUMIDITY") != std::string::npos) nh = int_after_eq(u);
+        else if (u.find("NUMBER OF TERMS IN PHASE FUNCTION") != std::string::npos) nphf = int_after_eq(u);
+        auto w = split(l);
+        bool all = !w.empty();
+        for (auto &x : w) all = all && is_number(x);
+        if (all)
+          for (auto &x : w) v.push_back(num(x));
+      }
+      const bool moist = bl.subtype == 1;
+      const int rows = moist ? nh : 1;
+      if (idx < 1 || idx > s.n_aer || rows < 1 || nphf < 1 || v.size() < (size_t)nb * rows * (3 + nphf)) {
+        err = path + ": bad aerosol block (species " + std::to_string(idx) + ")";
+        return false;
+      }
+      found[idx] = Species{moist, rows, nphf, v};
+      s.nd_hum = std::max(s.nd_hum, rows);
+      s.nd_phf = std::max(s.nd_phf, nphf);
+    }
+    const int na_ = s.n_aer, ndh = s.nd_hum, ndf = s.nd_phf;
+    s.aer_parm.assign(na_, SOCGPU_IP_AEROSOL_UNPARAMETRIZED);
+    s.aer_nhum.assign(na_, 0);
+    s.aer_nphf.assign(na_, 1);
+    s.aer_hum.assign((size_t)ndh * na_, 0.0);
+    s.aer_abs.assign((size_t)ndh * na_ * nb, 0.0);
+    s.aer_scat.assign((size_t)ndh * na_ * nb, 0.0);
+    s.aer_phf.assign((size_t)ndh * ndf * na_ * nb, 0.0);
+    for (const auto &kv : found) {
+      const int j = kv.first - 1;
+      const Species &sp = kv.second;
+      s.aer_nphf[j] = sp.nphf;
+      s.aer_nhum[j] = sp.moist ? sp.rows : 0;
+      s.aer_parm[j] = sp.moist ? (sp.nphf == 1 ? SOCGPU_IP_AEROSOL_PARAM_MOIST : SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST)
+                               : (sp.nphf == 1 ? SOCGPU_IP_AEROSOL_PARAM_DRY : SOCGPU_IP_AEROSOL_PARAM_PHF_DRY);
+      const int per = 3 + sp.nphf;
+      for (int b = 0; b < nb; ++b)
+        for (int h = 0; h < sp.rows; ++h) {
+          const double *r = &sp.v[((size_t)b * sp.rows + h) * per];
+          const size_t q = (size_t)h + (size_t)ndh * ((size_t)j + (size_t)na_ * b);
+          if (sp.moist) s.aer_hum[(size_t)h + (size_t)ndh * j] = r[0];
+          s.aer_abs[q] = r[1];
+          s.aer_scat[q] = r[2];
+          for (int m = 0; m < sp.nphf; ++m)
+            s.aer_phf[(size_t)h + (size_t)ndh * ((size_t)m + (size_t)ndf * ((size_t)j + (size_t)na_ * b))] = r[3 + m];
+        }
+    }
+  }
   sf = std::move(s);
   return true;
 }

@@ -76,6 +76,8 @@ class Control:
     l_continuum: bool = False
     l_mixing_ratio: bool = False
     l_grey_single: bool = False
+    l_aerosol: bool = False
+    l_henyey_greenstein_pf: bool = False
 
     def as_struct(self, n_band: int, keep: list) -> abi.Control:
         c = abi.Control()
@@ -92,6 +94,7 @@ class Control:
         c.precision = self.precision
         c.l_continuum, c.l_mixing_ratio = int(self.l_continuum), int(self.l_mixing_ratio)
         c.l_grey_single = int(self.l_grey_single)
+        c.l_aerosol, c.l_henyey_greenstein_pf = int(self.l_aerosol), int(self.l_henyey_greenstein_pf)
         return c
 
 
@@ -327,6 +330,19 @@ class Marshal:
             self.aer.mode_absorption = _dp(ae["mode_absorption"], k)
             self.aer.mode_scattering = _dp(ae["mode_scattering"], k)
             self.aer.mode_asymmetry = _dp(ae["mode_asymmetry"], k)
+        # classic aerosol: col.aer["mix_ratio"] (n, L, n_entries) of the
+        # spectral file's species "mr_type_index" (1-based), with optional
+        # "mr_source" and, for moist species, "mean_rel_humidity" (n, L)
+        d.nd_aerosol_mr = 1
+        if control.l_aerosol and col.aer and "mix_ratio" in col.aer:
+            ae = col.aer
+            mr = ae["mix_ratio"]
+            self.aer.n_aerosol_mr = int(mr.shape[2])
+            d.nd_aerosol_mr = max(1, int(mr.shape[2]))
+            self.aer.mix_ratio = _dp(mr, k)
+            self.aer.mr_type_index = _ip(ae["mr_type_index"], k)
+            self.aer.mr_source = _ip(ae.get("mr_source"), k)
+            self.aer.mean_rel_humidity = _dp(ae.get("mean_rel_humidity"), k)
         self.cld = abi.Cld()
         region = control.i_cloud in (abi.IP_CLOUD_MIX_MAX, abi.IP_CLOUD_MIX_RANDOM)
         if mcica is not None or (region and col.cld):

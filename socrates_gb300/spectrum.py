@@ -202,6 +202,15 @@ class Spectrum:
     wenyi_gk250b: np.ndarray | None = None       # (n_term4)
     wenyi_gk4: np.ndarray | None = None          # (10, 26, n_term4)
     wenyi_gk6: np.ndarray | None = None          # (9, 26, n_term6)
+    # block 11: classic aerosol species (StrSpecAerosol, read_spectrum.F90:2335-2640)
+    type_aerosol: np.ndarray | None = None       # (n_aerosol) type numbers
+    i_aerosol_parm: np.ndarray | None = None     # (n_aerosol) IP_AEROSOL_PARAM_*
+    nhumidity: np.ndarray | None = None          # (n_aerosol) 0 for dry species
+    n_aerosol_phf_term: np.ndarray | None = None # (n_aerosol)
+    aerosol_humidities: np.ndarray | None = None # (nd_humidity, n_aerosol)
+    aerosol_abs: np.ndarray | None = None        # (nd_humidity, n_aerosol, n_band) m2/kg
+    aerosol_scat: np.ndarray | None = None       # (nd_humidity, n_aerosol, n_band) m2/kg
+    aerosol_phf: np.ndarray | None = None        # (nd_humidity, nd_phase_term, n_aerosol, n_band)
     name: str = "spectrum"
     _keep: list = field(default_factory=list, repr=False)
 
@@ -366,6 +375,18 @@ class Spectrum:
             d.ice_parm_list = dp(pad(self.ice_parm_list))
             d.i_ice_parm = ip(self.i_ice_parm)
             d.l_ice_type = ip((np.asarray(self.i_ice_parm) > 0).astype(np.int32))
+        if self.aerosol_abs is not None:
+            d.n_aerosol = d.nd_aerosol_species = int(self.aerosol_abs.shape[1])
+            d.nd_humidity = int(self.aerosol_abs.shape[0])
+            d.nd_phase_term = int(self.aerosol_phf.shape[1])
+            d.type_aerosol = ip(self.type_aerosol)
+            d.i_aerosol_parm = ip(self.i_aerosol_parm)
+            d.nhumidity = ip(self.nhumidity)
+            d.n_aerosol_phf_term = ip(self.n_aerosol_phf_term)
+            d.aerosol_humidities = dp(self.aerosol_humidities)
+            d.aerosol_abs = dp(self.aerosol_abs)
+            d.aerosol_scat = dp(self.aerosol_scat)
+            d.aerosol_phf = dp(self.aerosol_phf)
         self._keep = keep
         return d
 
@@ -410,13 +431,16 @@ class Spectrum:
         L.append(f"Number of spectral bands = {self.n_band:5d}")
         L.append(f"Total number of gaseous absorbers = {self.n_absorb:5d}")
         L.append(f"Maximum number of k-terms in a band = {self.nd_k_term:5d}")
-        L.append(f"Total number of aerosols = {0:5d}")
+        n_aer = 0 if self.aerosol_abs is None else int(self.aerosol_abs.shape[1])
+        L.append(f"Total number of aerosols = {n_aer:5d}")
         L.append("List of indexing numbers and absorbers.")
         L.append("Index       Absorber(identifier and name)")
         for i, t in enumerate(self.type_absorb):
             L.append(f"{i + 1:5d}       {int(t):5d}       {GAS_NAMES.get(int(t), 'Gas'):20s}")
         L.append("List of indexing numbers of aerosols.")
         L.append("Index       Aerosol(type number and name)")
+        for i in range(n_aer):
+            L.append(f"{i + 1:5d}       {int(self.type_aerosol[i]):5d}       {'Aerosol':20s}")
         L.append("*END")
         L.append("*BLOCK: TYPE =    1: SUBTYPE =    0: VERSION =    0")
         L.append("Specification of spectral intervals")
@@ -434,8 +458,10 @@ class Spectrum:
             L.append("*END")
         if self.rayleigh_coeff is not None:
             L.append("*BLOCK: TYPE =    3: SUBTYPE =    0: VERSION =    0")
-            L.append("Rayleigh mass scattering coefficients.")
-            L.append("Band        Rayleigh coefficient (m2/kg)")
+            # three header records: read_spectrum.F90:882 skips them with '(//)'
+            L.append("Rayleigh mass scattering coefficients at STP: unit m**2/kg")
+            L.append("Band        Rayleigh coefficient")
+            L.append("                 m2/kg")
             for b in range(self.n_band):
                 L.append(f"{b + 1:5d}       {e(self.rayleigh_coeff[b])}")
             L.append("*END")
@@ -564,6 +590,36 @@ class Spectrum:
                     vals = parm[:n, b, t]
                     for q in range(0, n, 4):
                         L.append("".join(f"    {v:12.5E}" for v in vals[q:q + 4]))
+                L.append("*END")
+        # block 11: dry species as subtype 0, moist ones as subtype 1, both
+        # version 2 (read_block_11_0_2 / read_block_11_1_2 layouts)
+        if self.aerosol_abs is not None:
+            for j in range(self.aerosol_abs.shape[1]):
+                nphf = int(self.n_aerosol_phf_term[j])
+                nh = int(self.nhumidity[j])
+                moist = int(self.i_aerosol_parm[j]) in (2, 5)
+                L.append(f"*BLOCK: TYPE =   11: SUBTYPE =    {1 if moist else 0}: VERSION =    2")
+                L.append(f"Scattering parameters for {'moist' if moist else 'dry'} aerosols.")
+                L.append(f"Index of species = {j + 1:5d}  Aerosol")
+                if moist:
+                    L.append(f"Number of humidity values = {nh:3d}")
+                L.append(f"Number of terms in phase function = {nphf:5d}")
+                if not moist:
+                    L.append("Band        Absorption          Scattering          Phase fnc")
+                    L.append("            (m2.kg-1)           (m2.kg-1)")
+                for b in range(self.n_band):
+                    if moist:
+                        L.append(f"Band = {b + 1:4d}")
+                        L.append("        Humidity            Absorption         Scattering          Phase fnc.")
+                        L.append("                            (m2.kg-1)          (m2.kg-1)")
+                        for h in range(nh):
+                            vals = [self.aerosol_humidities[h, j], self.aerosol_abs[h, j, b],
+                                    self.aerosol_scat[h, j, b]] + list(self.aerosol_phf[h, :nphf, j, b])
+                            L.append("".join(f"    {v:16.9E}" for v in vals))
+                    else:
+                        vals = [self.aerosol_abs[0, j, b], self.aerosol_scat[0, j, b]] + \
+                            list(self.aerosol_phf[0, :nphf, j, b])
+                        L.append(f"{b + 1:5d}" + "".join(f"    {v:16.9E}" for v in vals))
                 L.append("*END")
         with open(path, "w") as fh:
             fh.write("\n".join(L) + "\n")
@@ -901,6 +957,69 @@ class Spectrum:
                 lo[ty - 1], hi[ty - 1] = a, b
             return np.asfortranarray(parm), ids, npars, nphfs, lo, hi
 
+        # block 11: classic aerosol species; block 0 gives their number and
+        # type numbers (read_spectrum.F90:2335-2640)
+        aerosol = {}
+        n_aer, aer_types = 0, []
+        for q, ln in enumerate(b0):
+            u = ln.upper()
+            if "NUMBER OF AEROSOLS" in u:
+                n_aer = int(after_eq(ln))
+            elif "INDEXING NUMBERS OF AEROSOLS" in u:
+                for r in b0[q + 2:q + 2 + n_aer]:
+                    aer_types.append(int(r.split()[1]))
+        if n_aer > 0 and 11 in by:
+            def numeric(line):
+                try:
+                    return [float(x.replace("D", "E").replace("d", "e")) for x in line.split()]
+                except ValueError:
+                    return None
+            parsed = {}
+            for bl in by[11]:
+                lines = bl["lines"]
+                sp_i = nh = None
+                nphf = 1
+                for ln in lines:
+                    u = ln.upper()
+                    if "INDEX OF SPECIES" in u:
+                        sp_i = int(after_eq(ln))
+                    elif "NUMBER OF HUMIDITY" in u:
+                        nh = int(after_eq(ln))
+                    elif "NUMBER OF TERMS IN PHASE FUNCTION" in u:
+                        nphf = int(after_eq(ln))
+                toks = []
+                for ln in lines:
+                    v = numeric(ln)
+                    if v:
+                        toks += v
+                moist = bl["subtype"] == 1
+                rows = nh if moist else 1
+                per = (3 + nphf) * rows
+                if len(toks) < per * n_band:
+                    raise ValueError(f"{path}: aerosol species {sp_i}: short of values")
+                parsed[sp_i] = (moist, rows, nphf, np.array(toks[:per * n_band]).reshape(n_band, rows, 3 + nphf))
+            ndh = max(v[1] for v in parsed.values())
+            ndp = max(v[2] for v in parsed.values())
+            hum = np.zeros((ndh, n_aer))
+            ab, sc = np.zeros((ndh, n_aer, n_band)), np.zeros((ndh, n_aer, n_band))
+            phf = np.zeros((ndh, ndp, n_aer, n_band))
+            parm, nhum, nterm = (np.zeros(n_aer, np.int32) for _ in range(3))
+            for sp_i, (moist, rows, nphf, arr) in parsed.items():
+                j = sp_i - 1
+                nterm[j] = nphf
+                nhum[j] = rows if moist else 0
+                parm[j] = (2 if nphf == 1 else 5) if moist else (1 if nphf == 1 else 4)
+                for b in range(n_band):
+                    if moist:
+                        hum[:rows, j] = arr[b, :, 0]
+                    ab[:rows, j, b] = arr[b, :, 1]
+                    sc[:rows, j, b] = arr[b, :, 2]
+                    phf[:rows, :nphf, j, b] = arr[b, :, 3:3 + nphf]
+            aerosol = dict(type_aerosol=np.array(aer_types, np.int32), i_aerosol_parm=parm, nhumidity=nhum,
+                           n_aerosol_phf_term=nterm, aerosol_humidities=_f(hum, np.float64),
+                           aerosol_abs=_f(ab, np.float64), aerosol_scat=_f(sc, np.float64),
+                           aerosol_phf=_f(phf, np.float64))
+
         cloud = {}
         for blk, pre in ((10, "drop"), (12, "ice")):
             r = cloud_sets(blk)
@@ -914,4 +1033,4 @@ class Spectrum:
                    scale=_f(sc, np.float64), p_ref=pr, t_ref=tr, solar_flux_band=sol, rayleigh_coeff=ray,
                    n_deg_fit=ndeg, t_ref_planck=tref, thermal_coeff=tc,
                    l_doppler=ldop, doppler_cor=dcor, name=name or str(path),
-                   i_overlap=i_ovl, **cont, **tables, **cloud)
+                   i_overlap=i_ovl, **cont, **tables, **cloud, **aerosol)

@@ -28,6 +28,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import abi
 from .spectrum import Spectrum
 
 GRAV = 9.80665          # rad_ccf.F90:50
@@ -320,6 +321,84 @@ def add_aerosol(col: Column, sp: Spectrum, seed: int) -> Column:
     col.aer = dict(n_mode=1, mode_mix_ratio=np.asfortranarray(mmr[:, :, None]),
                    mode_absorption=np.asfortranarray(ab), mode_scattering=np.asfortranarray(sc),
                    mode_asymmetry=np.asfortranarray(asy))
+    return col
+
+
+def add_aerosol_species(sp: Spectrum, seed: int, n_humidity: int = 11, n_phf: int = 2) -> Spectrum:
+    """Classic aerosol species in the layout of spectral-file block 11
+    (read_spectrum.F90:2335-2640): four species,
+      1 water soluble (type 1), moist, humidities 0, 1/(n_humidity-1) .. 1
+        (the equal spacing radiance_calc.F90:617-623 assumes), extinction
+        growing with humidity;
+      2 soot (type 4), dry;
+      3 dust-like (type 2), dry with n_phf tabulated phase-function moments,
+        the second not the square of the first;
+      4 oceanic (type 3), moist with n_phf tabulated moments.
+    Mass coefficients follow an Angstrom law in the band centre wavelength."""
+    st = Stream(seed, 5)
+    nb, nh, na = sp.n_band, n_humidity, 4
+    lam = np.sqrt(sp.wavelength_short * sp.wavelength_long) / 0.55e-6     # (nb)
+    hum = np.linspace(0.0, 1.0, nh)
+    growth = 1.0 + 4.0 * hum ** 4                                         # (nh)
+    k550 = np.array([4.0e3, 8.0e3, 1.0e3, 2.0e3])
+    ang = np.array([1.4, 1.0, 0.3, 0.6])
+    omega = np.array([0.95, 0.25, 0.9, 0.99]) - 0.04 * st.uniform((na,))
+    g0 = np.array([0.65, 0.35, 0.72, 0.78]) + 0.05 * st.uniform((na,))
+    abs_ = np.zeros((nh, na, nb), order="F")
+    scat = np.zeros((nh, na, nb), order="F")
+    phf = np.zeros((nh, n_phf, na, nb), order="F")
+    moist = (True, False, False, True)
+    n_terms = (1, 1, n_phf, n_phf)
+    for j in range(na):
+        ext = k550[j] * lam ** -ang[j]                                    # (nb)
+        rows = growth if moist[j] else np.ones(nh)
+        for h in range(nh):
+            if not moist[j] and h > 0:
+                continue
+            w = min(omega[j] + (0.03 * hum[h] if moist[j] else 0.0), 0.999)
+            abs_[h, j, :] = ext * rows[h] * (1.0 - w)
+            scat[h, j, :] = ext * rows[h] * w
+            g = np.minimum(g0[j] * (1.0 + 0.1 * hum[h] if moist[j] else 1.0) * lam ** -0.05, 0.9)
+            for m in range(n_terms[j]):
+                # tabulated moments of a phase function sharper than
+                # Henyey-Greenstein beyond the first
+                phf[h, m, j, :] = g ** (m + 1) * (1.0 if m == 0 else 1.08)
+    sp.type_aerosol = np.array([1, 4, 2, 3], np.int32)
+    sp.i_aerosol_parm = np.array([abi.IP_AEROSOL_PARAM_MOIST, abi.IP_AEROSOL_PARAM_DRY,
+                                  abi.IP_AEROSOL_PARAM_PHF_DRY, abi.IP_AEROSOL_PARAM_PHF_MOIST], np.int32)
+    sp.nhumidity = np.array([nh, 0, 0, nh], np.int32)
+    sp.n_aerosol_phf_term = np.array(n_terms, np.int32)
+    h2 = np.zeros((nh, na), order="F")
+    h2[:, 0] = hum
+    h2[:, 3] = hum
+    sp.aerosol_humidities = h2
+    sp.aerosol_abs, sp.aerosol_scat, sp.aerosol_phf = abs_, scat, phf
+    sp.name = f"{sp.name}_aer{seed}_{nh}h_{n_phf}m"
+    return sp
+
+
+def add_aerosol_mix(col: Column, seed: int, entries=(1, 2, 3, 4), sources=None, tau550: float = 0.3) -> Column:
+    """Mixing ratios of classic aerosol entries (def_aer.F90:26-34) for the
+    species of add_aerosol_species: entry e refers to species entries[e]
+    (1-based, repeats allowed) with source sources[e] (IP_AERSRC_*;
+    classic_ron by default), each in the lowest 3 km with a column loading
+    near tau550/len(entries)/k550, and the mean relative humidity of each
+    layer in [0, 1], exactly 0 and exactly 1 included."""
+    st = Stream(seed, 6)
+    n, L, ne = col.n_profile, col.n_layer, len(entries)
+    low = col.z < 3000.0
+    colmass = np.maximum(np.where(low, col.mass, 0.0).sum(axis=1), 1e-12)
+    mr = np.zeros((n, L, ne), order="F")
+    for e in range(ne):
+        scale = (0.2 + 1.6 * st.uniform((n,))) * tau550 / ne / 4.0e3
+        prof = np.exp(-col.z / 1500.0) * (0.5 + st.uniform((n, L)))
+        mr[:, :, e] = np.where(low, (scale / colmass)[:, None] * prof, 0.0)
+    rh = np.asfortranarray(np.clip(st.uniform((n, L)) * 1.1 - 0.05, 0.0, 1.0))
+    col.aer = dict(col.aer or {})
+    col.aer.update(mix_ratio=mr, mr_type_index=np.asarray(entries, np.int32),
+                   mr_source=np.asarray(sources if sources is not None else [abi.IP_AERSRC_CLASSIC_RON] * ne,
+                                        np.int32),
+                   mean_rel_humidity=rh)
     return col
 
 

@@ -57,6 +57,9 @@ def test_spectral_file_round_trip(tmp_path):
             assert abs(back.thermal_coeff - sp.thermal_coeff).max() <= 1e-8 * abs(sp.thermal_coeff).max()
         if sp.solar_flux_band is not None:
             assert abs(back.solar_flux_band - sp.solar_flux_band).max() < 1e-9
+        if sp.rayleigh_coeff is not None:
+            # every band, the first included (block 3 has three header records)
+            assert (abs(back.rayleigh_coeff - sp.rayleigh_coeff) <= 1e-9 * sp.rayleigh_coeff).all()
         # cloud parameter sets are written as read_block_10_0_2 reads them,
         # 4(4x, 1pe12.5): six significant digits
         for a, b in ((sp.drop_parm_list, back.drop_parm_list), (sp.ice_parm_list, back.ice_parm_list)):

@@ -366,3 +366,113 @@ def test_k_file_round_trip(tmp_path, kind):
     sp.write_wenyi_data(wy)
     for k, v in read_wenyi_tables(wy).items():
         np.testing.assert_array_equal(v, getattr(sp, k), err_msg=k)
+
+
+def _classic_case(solar, n=6, L=48, seed=41, sources=None, entries=(1, 2, 3, 4)):
+    if solar:
+        sp, col = synth.config2(n, L, seed=seed)
+    else:
+        sp, col = synth.config1(n, L, seed=seed)
+    col.aer = None
+    synth.add_aerosol_species(sp, seed)
+    synth.add_aerosol_mix(col, seed, entries=entries, sources=sources)
+    return sp, col
+
+
+def _modal_equivalent(sp, col, solar):
+    """The classic entries of col as UKCA-style modes: the species' tables
+    interpolated in humidity as opt_prop_aerosol.F90:322-420 does (pointer
+    of radiance_calc.F90:617-623), one mode per active entry."""
+    ae = col.aer
+    n, L, nb = col.n_profile, col.n_layer, sp.n_band
+    nhc = [int(sp.nhumidity[j]) for j in range(len(sp.i_aerosol_parm))
+           if sp.i_aerosol_parm[j] in (abi.IP_AEROSOL_PARAM_MOIST, abi.IP_AEROSOL_PARAM_PHF_MOIST)][-1]
+    rh = ae["mean_rel_humidity"]
+    ip = np.clip(1 + (rh * (nhc - 1)).astype(int), 1, nhc - 1) - 1
+    modes = [e for e in range(len(ae["mr_type_index"])) if ae["mr_source"][e] in
+             (abi.IP_AERSRC_CUSACK_RON, abi.IP_AERSRC_CLASSIC_RON, abi.IP_AERSRC_ARCL_RON)]
+    shape = (n, L, len(modes), nb)
+    ab, sc, g = (np.zeros(shape, order="F") for _ in range(3))
+    for m, e in enumerate(modes):
+        j = int(ae["mr_type_index"][e]) - 1
+        moist = sp.i_aerosol_parm[j] in (abi.IP_AEROSOL_PARAM_MOIST, abi.IP_AEROSOL_PARAM_PHF_MOIST)
+        for b in range(nb):
+            ta, ts, tg = sp.aerosol_abs[:, j, b], sp.aerosol_scat[:, j, b], sp.aerosol_phf[:, 0, j, b]
+            if moist:
+                w = (rh - sp.aerosol_humidities[ip, j]) / (1.0 / (nhc - 1.0))
+                ab[:, :, m, b] = ta[ip] + w * (ta[ip + 1] - ta[ip])
+                sc[:, :, m, b] = ts[ip] + w * (ts[ip + 1] - ts[ip])
+                g[:, :, m, b] = tg[ip] + w * (tg[ip + 1] - tg[ip])
+            else:
+                ab[:, :, m, b], sc[:, :, m, b], g[:, :, m, b] = ta[0], ts[0], tg[0]
+    mc = synth.Column(**{k: getattr(col, k) for k in col.__dataclass_fields__})
+    mc.aer = dict(n_mode=len(modes), mode_mix_ratio=np.asfortranarray(ae["mix_ratio"][:, :, modes]),
+                  mode_absorption=ab, mode_scattering=sc, mode_asymmetry=g)
+    return mc
+
+
+@pytest.mark.parametrize("solar", [False, True])
+def test_classic_aerosol_matches_modal_form(solar):
+    """With Henyey-Greenstein moments the parametrized species of
+    opt_prop_aerosol.F90:273-420 add exactly the terms of the modal form
+    (opt_prop_ukca_aerosol.F90:128-208) fed the humidity-interpolated
+    tables: mass absorption and scattering times mixing ratio, asymmetry and
+    (with rescaling) its square.  An inactive entry (classic_roff) and a
+    repeated species are included."""
+    sources = [abi.IP_AERSRC_CLASSIC_RON, abi.IP_AERSRC_CLASSIC_RON + 10, abi.IP_AERSRC_CLASSIC_RON,
+               abi.IP_AERSRC_CLASSIC_RON, abi.IP_AERSRC_ARCL_RON]
+    sp, col = _classic_case(solar, sources=sources, entries=(1, 2, 3, 4, 1))
+    mk = R.sw_control if solar else R.lw_control
+    classic = O.radiance_calc(mk(l_aerosol=True, l_henyey_greenstein_pf=True), sp, col)
+    modal = O.radiance_calc(mk(l_aerosol_mode=True), sp, _modal_equivalent(sp, col, solar))
+    clear = O.radiance_calc(mk(), sp, col)
+    for k in ("flux_up", "flux_down"):
+        scale = np.abs(modal[k]).max()
+        assert np.abs(classic[k] - modal[k]).max() <= 1e-13 * scale, k
+        assert np.abs(classic[k] - clear[k]).max() > 1e-3 * scale, f"{k}: the aerosol changed nothing"
+
+
+def test_classic_aerosol_tabulated_moments_and_humidity_edges():
+    """Tabulated phase-function moments (ip_aerosol_param_phf_*) give the
+    forward scattering from moment n_order_forward, not the square of the
+    asymmetry; a humidity of exactly 1 reads the last table interval (the
+    pointer is clamped where opt_prop_aerosol.F90:322-331 would read past
+    the table)."""
+    sp, col = _classic_case(True, entries=(3, 4))
+    tab = O.radiance_calc(R.sw_control(l_aerosol=True), sp, col)
+    hg = O.radiance_calc(R.sw_control(l_aerosol=True, l_henyey_greenstein_pf=True), sp, col)
+    assert np.abs(tab["flux_down"] - hg["flux_down"]).max() > 1e-3
+    col.aer["mean_rel_humidity"][:] = 1.0
+    top = O.radiance_calc(R.sw_control(l_aerosol=True, l_henyey_greenstein_pf=True), sp, col)
+    modal = O.radiance_calc(R.sw_control(l_aerosol_mode=True), sp, _modal_equivalent(sp, col, True))
+    assert np.abs(top["flux_down"] - modal["flux_down"]).max() <= 1e-13 * np.abs(modal["flux_down"]).max()
+
+
+def test_classic_aerosol_inputs_are_checked():
+    """A species index outside the spectral file, or a moist species without
+    mean relative humidities, is an error, not a silent skip."""
+    sp, col = _classic_case(False, entries=(1, 2))
+    col.aer["mr_type_index"] = np.array([1, 5], np.int32)
+    with pytest.raises(R.RadianceError):
+        O.radiance_calc(R.lw_control(l_aerosol=True), sp, col)
+    sp, col = _classic_case(False, entries=(1, 2))
+    col.aer["mean_rel_humidity"] = None
+    with pytest.raises(R.RadianceError):
+        O.radiance_calc(R.lw_control(l_aerosol=True), sp, col)
+
+
+def test_aerosol_block_round_trip(tmp_path):
+    """Classic species written as spectral-file block 11 (dry: subtype 0,
+    moist: subtype 1, version 2 with phase-function moments) and read back
+    give the same tables."""
+    from socrates_gb300.spectrum import Spectrum
+    sp = synth.add_aerosol_species(synth.sw_spectrum(2, 8), 5, n_humidity=21, n_phf=3)
+    path = tmp_path / "sp_sw"
+    sp.write_text(path)
+    back = Spectrum.read_text(path)
+    for name in ("type_aerosol", "i_aerosol_parm", "nhumidity", "n_aerosol_phf_term"):
+        np.testing.assert_array_equal(getattr(back, name), getattr(sp, name), err_msg=name)
+    for name in ("aerosol_humidities", "aerosol_abs", "aerosol_scat", "aerosol_phf"):
+        a, b = getattr(sp, name), getattr(back, name)
+        assert a.shape == b.shape, name
+        np.testing.assert_allclose(b, a, rtol=1e-6, atol=0, err_msg=name)

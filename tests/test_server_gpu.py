@@ -127,25 +127,26 @@ def test_invalid_request_rejected_at_submit(gpu_lib):
 
 def test_small_requests_overtake_a_large_one(gpu_lib):
     """A large McICA request (8192 columns x 137 layers) and then small
-    clear-sky requests submitted while it runs: the small requests go in
-    their own waves, on high-priority streams, so at least two waves are on
-    the device at once and every small request finishes before the large
-    one; each result is still the same as alone."""
-    from socrates_gb300 import synth
+    requests submitted while it runs, all with page-locked host arrays (the
+    server's asynchronous path): the small requests go in their own waves,
+    on high-priority streams, so at least two waves are on the device at
+    once and every small request finishes before the large one; each result
+    is still the same as alone."""
     from socrates_gb300.server import Server
-    lw, sw, col = synth.config3(8192, 137, seed=31, n_subcol=16)
-    synth.add_sw_surface(col, sw.n_band, 31)
-    c_sub, nsc = R.cloud_gen(col, 16, abi.IP_EXPONENTIAL_RAND, abi.RNG_PHILOX)
-    mc = R.set_cld_mcica(sw, col, abi.IP_SOLAR, abi.IP_MCICA_SINGLE_SAMPLING, c_sub=c_sub, n_subcol_cld=nsc)
-    big = (R.sw_control(i_cloud=abi.IP_CLOUD_MCICA, precision=abi.PRECISION_MIXED), sw, col, mc)
-    _, small = _requests(8, seed=32, median=16.0)
-    big_m = R.Marshal(*big)
-    small_m = [R.Marshal(*r) for r in small]
+    from socrates_gb300.workload import PinnedArena, RequestSpec, pin_outputs
+    big_spec = RequestSpec("sw_cloudy", 137, 8192, 0.0)
+    small_specs = request_specs(8, 32, median=16.0, sigma=0.8, clip=(1, 64))
+    pools = Pools([big_spec] + small_specs, 31)
+    arena = PinnedArena(1 << 30)
+    reqs = [pools.request(q, abi.PRECISION_MIXED, arena.take) for q in [big_spec] + small_specs]
+    marshals = [pin_outputs(R.Marshal(*r), arena.take) for r in reqs]
     srv = Server(device_bytes=2 << 30, streams=4, max_wave_requests=16)
-    t_big = srv.submit(big_m, big[1])
+    for m, r in zip(marshals[1:], reqs[1:]):          # every kernel class once, before timing
+        srv.wait(srv.submit(m, r[1]), 60.0)
     t0 = time.perf_counter()
+    t_big = srv.submit(marshals[0], reqs[0][1])
     ts = []
-    for m, r in zip(small_m, small):
+    for m, r in zip(marshals[1:], reqs[1:]):
         ts.append((srv.submit(m, r[1]), time.perf_counter() - t0))
         time.sleep(2e-4)
     done_small = []
@@ -155,9 +156,11 @@ def test_small_requests_overtake_a_large_one(gpu_lib):
     _, lat_big = srv.wait(t_big, 60.0)
     st = srv.stats()
     srv.close()
-    assert st["max_waves_in_flight"] >= 2
-    assert st["small_waves"] >= 1
-    assert max(done_small) < lat_big, (max(done_small), lat_big)
-    _compare(R.radiance_calc(*big), big_m.result(), abi.PRECISION_MIXED, "large")
-    for r, m in zip(small, small_m):
-        _compare(R.radiance_calc(*r), m.result(), r[0].precision, "small")
+    colg = [r[2].n_profile * r[1].n_gpoint for r in reqs]
+    diag = f"small done at {[round(x, 3) for x in done_small]} ms, large at {lat_big:.3f} ms, stats {st}, colg {colg}"
+    assert colg[0] > max(colg[1:]), diag
+    assert st["max_waves_in_flight"] >= 2, diag
+    assert st["small_waves"] >= 1, diag
+    assert max(done_small) < lat_big, diag
+    for r, m in zip(reqs, marshals):
+        _compare(R.radiance_calc(*r), m.result(), r[0].precision, "overtake")
