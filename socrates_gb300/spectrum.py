@@ -1001,7 +1001,7 @@ class Spectrum:
             ndh = max(v[1] for v in parsed.values())
             ndp = max(v[2] for v in parsed.values())
             hum = np.zeros((ndh, n_aer))
-            ab, sc = np.zeros((ndh, n_aer, n_band)), np.zeros((ndh, n_aer, n_band))
+            ab, scat = np.zeros((ndh, n_aer, n_band)), np.zeros((ndh, n_aer, n_band))
             phf = np.zeros((ndh, ndp, n_aer, n_band))
             parm, nhum, nterm = (np.zeros(n_aer, np.int32) for _ in range(3))
             for sp_i, (moist, rows, nphf, arr) in parsed.items():
@@ -1013,11 +1013,11 @@ class Spectrum:
                     if moist:
                         hum[:rows, j] = arr[b, :, 0]
                     ab[:rows, j, b] = arr[b, :, 1]
-                    sc[:rows, j, b] = arr[b, :, 2]
+                    scat[:rows, j, b] = arr[b, :, 2]
                     phf[:rows, :nphf, j, b] = arr[b, :, 3:3 + nphf]
             aerosol = dict(type_aerosol=np.array(aer_types, np.int32), i_aerosol_parm=parm, nhumidity=nhum,
                            n_aerosol_phf_term=nterm, aerosol_humidities=_f(hum, np.float64),
-                           aerosol_abs=_f(ab, np.float64), aerosol_scat=_f(sc, np.float64),
+                           aerosol_abs=_f(ab, np.float64), aerosol_scat=_f(scat, np.float64),
                            aerosol_phf=_f(phf, np.float64))
 
         cloud = {}
