@@ -36,7 +36,7 @@ extern "C" {
 #define SOCGPU_API
 #endif
 
-#define SOCGPU_ABI_VERSION 5
+#define SOCGPU_ABI_VERSION 6
 
 /* ---- status codes: rad_pcf.F90:391-405 ------------------------------- */
 #define SOCGPU_I_NORMAL             0
@@ -289,6 +289,10 @@ typedef struct socgpu_dimen {
     int nd_cloud_component, nd_cloud_type;
     int nd_subcol_gen, nd_subcol_req;
     int nd_aerosol_mr;          /* third extent of socgpu_aer.mix_ratio */
+    /* extents of the prescribed aerosol optical properties (def_dimen.F90
+       nd_profile_aerosol_prsc, nd_opt_level_aerosol_prsc,
+       nd_phf_term_aerosol_prsc) */
+    int nd_profile_aerosol_prsc, nd_opt_level_aerosol_prsc, nd_phf_term_aerosol_prsc;
 } socgpu_dimen;
 
 /* ---- StrAtm (src/radiance_core/def_atm.F90) --------------------------- */
@@ -330,6 +334,20 @@ typedef struct socgpu_aer {
     const int    *mr_type_index;     /* (nd_aerosol_mr) 1-based species of the spectral file */
     const int    *mr_source;         /* (nd_aerosol_mr) SOCGPU_IP_AERSRC_*: only the active ones count */
     const double *mean_rel_humidity; /* (nd_profile, nd_layer) in [0, 1], or NULL without moist species */
+    /* prescribed optical properties (def_aer.F90:46-60) of the species whose
+       parametrization in the spectrum is SOCGPU_IP_AEROSOL_UNPARAMETRIZED
+       (l_run_cdf's overlay of observed properties): per species, values on
+       its own pressure levels (ascending), fitted by cubic splines in
+       pressure and evaluated at the layer pressures (prsc_opt_prop.F90,
+       prsc_gather_spline.F90); absorption and scattering are volume
+       coefficients [1/m], divided by atm.density.  Zero outside the levels. */
+    const int    *n_opt_level_prsc;  /* (nd_aerosol_species) levels of each species (host array) */
+    const int    *n_phase_term_prsc; /* (nd_aerosol_species) phase-function moments given (host array) */
+    const double *pressure_prsc;     /* (nd_profile_aerosol_prsc, nd_opt_level_aerosol_prsc, nd_aerosol_species) [Pa] */
+    const double *absorption_prsc;   /* (nd_profile_aerosol_prsc, nd_opt_level_aerosol_prsc, nd_aerosol_species, nd_band) */
+    const double *scattering_prsc;   /* same */
+    const double *phase_fnc_prsc;    /* (nd_profile_aerosol_prsc, nd_opt_level_aerosol_prsc, nd_phf_term_aerosol_prsc,
+                                         nd_aerosol_species, nd_band) */
 } socgpu_aer;
 
 /* ---- StrCld with the McICA state (def_cld.F90, def_mcica.F90) --------

@@ -25,7 +25,8 @@ END TYPE
 TYPE, BIND(C) :: socgpu_dimen
   INTEGER(c_int) :: nd_profile, nd_layer, id_cloud_top, nd_aerosol_mode, &
                     nd_cloud_component, nd_cloud_type, nd_subcol_gen, nd_subcol_req, &
-                    nd_aerosol_mr
+                    nd_aerosol_mr, nd_profile_aerosol_prsc, nd_opt_level_aerosol_prsc, &
+                    nd_phf_term_aerosol_prsc
 END TYPE
 
 TYPE, BIND(C) :: socgpu_atm
@@ -42,6 +43,8 @@ TYPE, BIND(C) :: socgpu_aer
   TYPE(c_ptr)    :: mode_mix_ratio, mode_absorption, mode_scattering, mode_asymmetry
   INTEGER(c_int) :: n_aerosol_mr
   TYPE(c_ptr)    :: mix_ratio, mr_type_index, mr_source, mean_rel_humidity
+  TYPE(c_ptr)    :: n_opt_level_prsc, n_phase_term_prsc, pressure_prsc, absorption_prsc, &
+                    scattering_prsc, phase_fnc_prsc
 END TYPE
 
 TYPE, BIND(C) :: socgpu_cld

@@ -608,6 +608,106 @@ static void rescale_continuum(const socgpu_control *c, const socgpu_spectrum_des
         }
 }
 
+/* spline_fit.F90: second derivatives of the natural cubic spline through
+ * (x[k], y[k]) by tridiagonal elimination (the reference leaves y2 unset for
+ * one point; spline_at never reads it then). */
+static void spline_fit(int n, const double *x, const double *y, double *y2)
+{
+    if (n == 1) { y2[0] = 0.0; return; }
+    double *u = (double *)malloc(sizeof(double) * (size_t)n);
+    y2[0] = 0.0;
+    u[0] = 0.0;
+    for (int i = 1; i < n - 1; ++i) {
+        const double sigma = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+        const double rho = sigma * y2[i - 1] + 2.0;
+        y2[i] = (sigma - 1.0) / rho;
+        u[i] = (6.0 * ((y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]))
+                / (x[i + 1] - x[i - 1]) - sigma * u[i - 1]) / rho;
+    }
+    y2[n - 1] = 0.0;
+    for (int i = n - 2; i >= 0; --i) y2[i] = y2[i] * y2[i + 1] + u[i];
+    free(u);
+}
+
+/* spline_evaluate.F90: the spline at xp (bisection for the interval); 1 when
+ * xp lies outside [x[0], x[n-1]] (the reference's i_err_range). */
+static int spline_at(int n, const double *x, const double *y, const double *y2, double xp, double *yp)
+{
+    if (n == 1) { *yp = y[0]; return 0; }
+    if (xp > x[n - 1] || xp < x[0]) return 1;
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        const int m = (lo + hi) / 2;
+        if (xp > x[m]) lo = m; else hi = m;
+    }
+    const double delta = x[hi] - x[lo];
+    const double a = (x[hi] - xp) / delta, bb = (xp - x[lo]) / delta, cc = delta * delta / 6.0;
+    *yp = a * (y[lo] + (a * a - 1.0) * y2[lo] * cc) + bb * (y[hi] + (bb * bb - 1.0) * y2[hi] * cc);
+    return 0;
+}
+
+/* prsc_gather_spline.F90: one prescribed quantity of species j (values v of
+ * stride `st` between levels, from the profile's first level) at the layer
+ * pressures of profile l; zero outside the levels. */
+static void prsc_gather(int nl, const double *x, const double *v, size_t st, const double *p, int ndp, int l,
+                        int n_layer, double *out)
+{
+    double *y = (double *)malloc(sizeof(double) * (size_t)nl), *y2 = (double *)malloc(sizeof(double) * (size_t)nl);
+    for (int k = 0; k < nl; ++k) y[k] = v[(size_t)k * st];
+    spline_fit(nl, x, y, y2);
+    for (int i = 0; i < n_layer; ++i)
+        if (spline_at(nl, x, y, y2, IX2(p, l, i, ndp), &out[i])) out[i] = 0.0;
+    free(y); free(y2);
+}
+
+/* prsc_opt_prop.F90:165-300 for two-stream phase functions: species j's
+ * prescribed absorption and scattering (volume coefficients over the air
+ * density, floored at zero) and its asymmetry or tabulated moments, added to
+ * the grey optics of band b. */
+static void prsc_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *dm, const socgpu_spectrum_desc *d,
+                          const socgpu_atm *atm, const socgpu_aer *aer, int j, int b)
+{
+    const int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp, ndp = dm->nd_profile;
+    const size_t ndpp = (size_t)dm->nd_profile_aerosol_prsc, ndlv = (size_t)dm->nd_opt_level_aerosol_prsc;
+    const size_t ndf = (size_t)dm->nd_phf_term_aerosol_prsc, nsp = (size_t)d->nd_aerosol_species;
+    const int nl = aer->n_opt_level_prsc[j], nof = c->n_order_forward;
+    double *x = (double *)malloc(sizeof(double) * (size_t)nl);
+    double *ka = (double *)malloc(sizeof(double) * (size_t)n_layer), *ks = (double *)malloc(sizeof(double) * (size_t)n_layer);
+    double *g = (double *)malloc(sizeof(double) * (size_t)n_layer), *f = (double *)malloc(sizeof(double) * (size_t)n_layer);
+#define PRSC_AT(a, l, k) (a)[(size_t)(l) + ndpp * ((size_t)(k) + ndlv * ((size_t)j + nsp * (size_t)b))]
+#define PRSC_PHF(l, m) &aer->phase_fnc_prsc[(size_t)(l) + ndpp * (ndlv * ((size_t)(m) + ndf * ((size_t)j + nsp * (size_t)b)))]
+    for (int l = 0; l < n_profile; ++l) {
+        for (int k = 0; k < nl; ++k) x[k] = aer->pressure_prsc[(size_t)l + ndpp * ((size_t)k + ndlv * (size_t)j)];
+        prsc_gather(nl, x, &PRSC_AT(aer->absorption_prsc, l, 0), ndpp, atm->p, ndp, l, n_layer, ka);
+        prsc_gather(nl, x, &PRSC_AT(aer->scattering_prsc, l, 0), ndpp, atm->p, ndp, l, n_layer, ks);
+        for (int i = 0; i < n_layer; ++i) {
+            const double rho = IX2(atm->density, l, i, ndp);
+            ks[i] = fmax(0.0, ks[i] / rho);
+            ka[i] = fmax(0.0, ka[i] / rho);
+        }
+        prsc_gather(nl, x, PRSC_PHF(l, 0), ndpp, atm->p, ndp, l, n_layer, g);
+        if (c->l_rescale && !c->l_henyey_greenstein_pf)
+            prsc_gather(nl, x, PRSC_PHF(l, nof - 1), ndpp, atm->p, ndp, l, n_layer, f);
+        for (int i = 0; i < n_layer; ++i) {
+            IX2(w->k_grey_tot, l, i, wp) = IX2(w->k_grey_tot, l, i, wp) + ka[i];
+            IX2(w->k_ext_scat, l, i, wp) = IX2(w->k_ext_scat, l, i, wp) + ks[i];
+            const double phf1 = ks[i] * g[i];
+            IX2(w->phase_fnc, l, i, wp) = IX2(w->phase_fnc, l, i, wp) + phf1;
+            if (c->l_rescale) {
+                double fw;
+                if (!c->l_henyey_greenstein_pf) fw = ks[i] * f[i];
+                else if (nof == 1) fw = phf1;
+                else if (nof == 2) fw = phf1 * g[i];
+                else fw = ks[i] * pow(g[i], (double)nof);
+                IX2(w->forward_scatter, l, i, wp) = IX2(w->forward_scatter, l, i, wp) + fw;
+            }
+        }
+    }
+#undef PRSC_AT
+#undef PRSC_PHF
+    free(x); free(ka); free(ks); free(g); free(f);
+}
+
 /* opt_prop_aerosol (opt_prop_aerosol.F90:273-640), two-stream phase
  * functions (n_order_phase 1), for band b: every radiatively active entry of
  * the mixing ratios adds its species' absorption and scattering, interpolated
@@ -617,7 +717,7 @@ static void rescale_continuum(const socgpu_control *c, const socgpu_spectrum_des
  * the last moist species of the spectrum); it is clamped to the table, where
  * the reference would read past it for a humidity of 1. */
 static int opt_prop_aerosol(work *w, const socgpu_control *c, const socgpu_dimen *dm,
-                            const socgpu_spectrum_desc *d, const socgpu_aer *aer, int b)
+                            const socgpu_spectrum_desc *d, const socgpu_atm *atm, const socgpu_aer *aer, int b)
 {
     const int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp, ndl = w->ndl, ndp = dm->nd_profile;
     const int ndh = d->nd_humidity, nda = d->nd_aerosol_species, ndf = d->nd_phase_term;
@@ -636,6 +736,20 @@ static int opt_prop_aerosol(work *w, const socgpu_control *c, const socgpu_dimen
         const int j = aer->mr_type_index[jm] - 1;
         if (j < 0 || j >= d->n_aerosol) return SOCGPU_I_ERR_RANGE;
         const int parm = d->i_aerosol_parm[j];
+        if (parm == SOCGPU_IP_AEROSOL_UNPARAMETRIZED) {
+            /* opt_prop_aerosol.F90:714-790 */
+            if (!aer->n_opt_level_prsc || !aer->n_phase_term_prsc || !aer->pressure_prsc || !aer->absorption_prsc ||
+                !aer->scattering_prsc || !aer->phase_fnc_prsc || !atm->density)
+                return SOCGPU_I_ERR_FATAL;
+            const int need = (c->l_henyey_greenstein_pf || !c->l_rescale) ? 1 :
+                             (c->n_order_forward > 1 ? c->n_order_forward : 1);
+            if (aer->n_opt_level_prsc[j] < 1 || aer->n_opt_level_prsc[j] > dm->nd_opt_level_aerosol_prsc ||
+                aer->n_phase_term_prsc[j] < need || aer->n_phase_term_prsc[j] > dm->nd_phf_term_aerosol_prsc ||
+                dm->nd_profile_aerosol_prsc < n_profile)
+                return SOCGPU_I_ERR_RANGE;
+            prsc_opt_prop(w, c, dm, d, atm, aer, j, b);
+            continue;
+        }
         const int moist = parm == SOCGPU_IP_AEROSOL_PARAM_MOIST || parm == SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST;
         const int hg = c->l_henyey_greenstein_pf || parm == SOCGPU_IP_AEROSOL_PARAM_DRY ||
                        parm == SOCGPU_IP_AEROSOL_PARAM_MOIST;
@@ -708,7 +822,7 @@ static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *d
             for (int l = 0; l < n_profile; ++l) IX2(w->k_ext_scat, l, i, wp) = d->rayleigh_coeff[b];
     }
     if (c->l_aerosol && aer && aer->n_aerosol_mr > 0) {
-        int st = opt_prop_aerosol(w, c, dm, d, aer, b);
+        int st = opt_prop_aerosol(w, c, dm, d, atm, aer, b);
         if (st != SOCGPU_I_NORMAL) return st;
     }
     if (c->l_aerosol_mode && aer && aer->n_mode > 0) {
@@ -1799,6 +1913,10 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
         }
         if (aerv.n_aerosol_mr > 0 && aerv.mix_ratio) aerv.mix_ratio += p0;
         if (aerv.mean_rel_humidity) aerv.mean_rel_humidity += p0;
+        if (aerv.pressure_prsc) aerv.pressure_prsc += p0;
+        if (aerv.absorption_prsc) aerv.absorption_prsc += p0;
+        if (aerv.scattering_prsc) aerv.scattering_prsc += p0;
+        if (aerv.phase_fnc_prsc) aerv.phase_fnc_prsc += p0;
     }
     socgpu_cld cldv, *cld = NULL;
     if (cld0 && (l_cloud || l_region)) {

@@ -44,7 +44,7 @@ IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0,
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RNG_LCG, RNG_PHILOX = 0, 1
 NOALLOC_MAX_CLOUD_LAYERS = 1024   # SOCGPU_NOALLOC_MAX_CLOUD_LAYERS
-ABI_VERSION = 5
+ABI_VERSION = 6
 IP_SELF_CONTINUUM, IP_FRN_CONTINUUM = 1, 2
 
 _dp = C.POINTER(C.c_double)
@@ -102,6 +102,8 @@ class Dimen(C.Structure):
         ("nd_profile", C.c_int), ("nd_layer", C.c_int), ("id_cloud_top", C.c_int), ("nd_aerosol_mode", C.c_int),
         ("nd_cloud_component", C.c_int), ("nd_cloud_type", C.c_int), ("nd_subcol_gen", C.c_int),
         ("nd_subcol_req", C.c_int), ("nd_aerosol_mr", C.c_int),
+        ("nd_profile_aerosol_prsc", C.c_int), ("nd_opt_level_aerosol_prsc", C.c_int),
+        ("nd_phf_term_aerosol_prsc", C.c_int),
     ]
 
 
@@ -155,6 +157,8 @@ class Aer(C.Structure):
         ("mode_scattering", _dp), ("mode_asymmetry", _dp),
         ("n_aerosol_mr", C.c_int), ("mix_ratio", _dp), ("mr_type_index", _ip), ("mr_source", _ip),
         ("mean_rel_humidity", _dp),
+        ("n_opt_level_prsc", _ip), ("n_phase_term_prsc", _ip), ("pressure_prsc", _dp), ("absorption_prsc", _dp),
+        ("scattering_prsc", _dp), ("phase_fnc_prsc", _dp),
     ]
 
 

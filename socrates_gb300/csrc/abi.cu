@@ -453,6 +453,7 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
       nphf = std::max(nphf, fj);
     }
     s.aer_n_species = nsp; s.aer_nh = nh; s.aer_nphf = nphf;
+    e.aer_nd_species = d->nd_aerosol_species;
     const int row = 2 + nphf, ndh = d->nd_humidity, ndf = d->nd_phase_term, nda = d->nd_aerosol_species;
     aer_tab.assign((size_t)d->n_band * nsp * nh * row, 0.0);
     aer_hum.assign((size_t)nsp * nh, 0.0);
@@ -755,6 +756,29 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
         return SOCGPU_I_ERR_RANGE;
       }
       const int parm = sp->aer_parm[j - 1];
+      if (parm == SOCGPU_IP_AEROSOL_UNPARAMETRIZED) {
+        // prescribed optical properties (prsc_opt_prop.F90)
+        if (!aer->n_opt_level_prsc || !aer->n_phase_term_prsc || !aer->pressure_prsc || !aer->absorption_prsc ||
+            !aer->scattering_prsc || !aer->phase_fnc_prsc) {
+          set_msg(msg, msg_len, "aerosol species %d is unparametrized but its prescribed properties are missing", j);
+          return SOCGPU_I_ERR_FATAL;
+        }
+        const int nl = aer->n_opt_level_prsc[j - 1], nm = aer->n_phase_term_prsc[j - 1];
+        const int need = (c->l_henyey_greenstein_pf || !c->l_rescale) ? 1 : std::max(1, c->n_order_forward);
+        if (nl < 1 || nl > dm->nd_opt_level_aerosol_prsc || dm->nd_profile_aerosol_prsc < atm->n_profile ||
+            nm < need || nm > dm->nd_phf_term_aerosol_prsc) {
+          set_msg(msg, msg_len,
+                  "aerosol species %d: %d prescribed levels and %d moments (%d needed) do not fit the extents "
+                  "(%d profiles, %d levels, %d moments)", j, nl, nm, need, dm->nd_profile_aerosol_prsc,
+                  dm->nd_opt_level_aerosol_prsc, dm->nd_phf_term_aerosol_prsc);
+          return SOCGPU_I_ERR_RANGE;
+        }
+        if (!atm->density) {
+          set_msg(msg, msg_len, "prescribed aerosol properties need the air density"); return SOCGPU_I_ERR_FATAL; }
+        if (++active > kMaxAerMr) {
+          set_msg(msg, msg_len, "more than %d active aerosol entries", kMaxAerMr); return SOCGPU_I_ERR_RANGE; }
+        continue;
+      }
       if (parm != SOCGPU_IP_AEROSOL_PARAM_DRY && parm != SOCGPU_IP_AEROSOL_PARAM_MOIST &&
           parm != SOCGPU_IP_AEROSOL_PARAM_PHF_DRY && parm != SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST) {
         set_msg(msg, msg_len, "aerosol species %d: parametrization %d is not supported", j, parm);
@@ -899,12 +923,35 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
       const int src = aer->mr_source ? aer->mr_source[k] : SOCGPU_IP_AERSRC_CLASSIC_RON;
       if (src < SOCGPU_IP_AERSRC_CUSACK_RON || src > SOCGPU_IP_AERSRC_ARCL_RON) continue;
       const int j = aer->mr_type_index[k] - 1;
+      if (sp->aer_parm[j] == SOCGPU_IP_AEROSOL_UNPARAMETRIZED) {
+        // prescribed: once per species, counted per entry
+        int s = 0;
+        while (s < p.n_prsc && p.prsc_species[s] != j) ++s;
+        if (s == p.n_prsc) {
+          p.prsc_species[s] = j;
+          p.prsc_count[s] = 0;
+          p.prsc_nlev[s] = aer->n_opt_level_prsc[j];
+          ++p.n_prsc;
+        }
+        ++p.prsc_count[s];
+        continue;
+      }
       p.aer_entry[p.n_aer_mr] = k;
       p.aer_species[p.n_aer_mr] = j;
       p.aer_parm[p.n_aer_mr] = sp->aer_parm[j];
       ++p.n_aer_mr;
     }
     p.l_aerosol = p.n_aer_mr > 0;
+    p.l_aer_prsc = p.n_prsc > 0;
+    if (p.l_aer_prsc) {
+      p.prsc_nq = (c->l_henyey_greenstein_pf || !c->l_rescale) ? 1 : std::max(1, c->n_order_forward);
+      p.nd_prof_prsc = dm->nd_profile_aerosol_prsc;
+      p.nd_lev_prsc = dm->nd_opt_level_aerosol_prsc;
+      p.nd_phf_prsc = dm->nd_phf_term_aerosol_prsc;
+      p.nd_sp_prsc = sp->aer_nd_species;
+      p.prsc_p = aer->pressure_prsc; p.prsc_abs = aer->absorption_prsc;
+      p.prsc_scat = aer->scattering_prsc; p.prsc_phf = aer->phase_fnc_prsc;
+    }
     p.l_hg = c->l_henyey_greenstein_pf;
     p.aer_n_species = sp->dev.aer_n_species; p.aer_nh = sp->dev.aer_nh; p.aer_nphf = sp->dev.aer_nphf;
     // one humidity table for all moist species: that of the last one
@@ -949,7 +996,30 @@ int mode_index(const socgpu_control *c) {
   return c->i_scatter_method == SOCGPU_IP_SCATTER_FULL ? 1 : 0;
 }
 
+namespace {
+int launch_flux(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *msg, size_t msg_len);
+}
+
 int launch(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *msg, size_t msg_len) {
+  if (!p.l_aer_prsc) return launch_flux(p, c, st, msg, msg_len);
+  // prescribed aerosol properties: their per-layer sums in stream-ordered
+  // scratch memory, then the flux kernel
+  void *scratch = nullptr;
+  if (cudaMallocAsync(&scratch, std::max<size_t>(prsc_bytes(p), 256), st) != cudaSuccess) {
+    cudaGetLastError();
+    set_msg(msg, msg_len, "no device memory for the prescribed aerosol properties");
+    return SOCGPU_I_ABORT_CALCULATION;
+  }
+  FluxParams q = p;
+  q.aer_prsc = (const double *)scratch;
+  int st_ = launch_prsc(q, (double *)scratch, st, msg, msg_len);
+  if (st_ == SOCGPU_I_NORMAL) st_ = launch_flux(q, c, st, msg, msg_len);
+  cudaFreeAsync(scratch, st);
+  return st_;
+}
+
+namespace {
+int launch_flux(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *msg, size_t msg_len) {
   const int mode = mode_index(c);
   TileConfig t = choose_tile(c->precision, mode, p.n_layer);
   // options the phased kernel does not cover run on the scan kernels
@@ -962,6 +1032,7 @@ int launch(const FluxParams &p, const socgpu_control *c, cudaStream_t st, char *
   }
   return v->launch(p, t, st, msg, msg_len);
 }
+}  // namespace
 
 // ---------------------------------------------------------------------------
 // Staging of a host-pointer call.
@@ -984,7 +1055,18 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
   o_m = plan.add(a->mass, D, ndp, np, nl);
   const bool cont = c->l_continuum && s->dev.has_continuum;
   o_g = (c->l_gas || cont) ? plan.add(a->gas_mix_ratio, D, ndp, np, ndl * ns) : none;
-  o_rho = cont ? plan.add(a->density, D, ndp, np, nl) : none;
+  // prescribed aerosol properties: species whose spectral parametrization is
+  // unparametrized, named by an active entry
+  prsc = false;
+  if (c->l_aerosol && ae && ae->n_aerosol_mr > 0 && ae->mr_type_index)
+    for (int k = 0; k < ae->n_aerosol_mr; ++k) {
+      const int src = ae->mr_source ? ae->mr_source[k] : SOCGPU_IP_AERSRC_CLASSIC_RON;
+      const int j = ae->mr_type_index[k] - 1;
+      if (src >= SOCGPU_IP_AERSRC_CUSACK_RON && src <= SOCGPU_IP_AERSRC_ARCL_RON && j >= 0 &&
+          j < (int)s->aer_parm.size() && s->aer_parm[j] == SOCGPU_IP_AEROSOL_UNPARAMETRIZED)
+        prsc = true;
+    }
+  o_rho = (cont || prsc) ? plan.add(a->density, D, ndp, np, nl) : none;
   o_z = sw ? plan.add(b->zen_0, D, ndp, np, 1) : none;
   o_si = sw ? plan.add(b->solar_irrad, D, ndp, np, 1) : none;
   o_alb = plan.add(b->rho_alb, D, ndp, np, 2 * nb);
@@ -1004,6 +1086,15 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
   if (classic) {
     o_xmr = plan.add(ae->mix_ratio, D, ndp, np, ndl * (size_t)ae->n_aerosol_mr);
     if (ae->mean_rel_humidity) o_mrh = plan.add(ae->mean_rel_humidity, D, ndp, np, nl);
+  }
+  o_pp = o_pab = o_psc = o_pph = none;
+  if (prsc) {
+    const size_t ndpp = dm->nd_profile_aerosol_prsc, nlv = dm->nd_opt_level_aerosol_prsc;
+    const size_t nsp = s->aer_nd_species, nph = dm->nd_phf_term_aerosol_prsc, ndb = s->dev.nd_band;
+    o_pp = plan.add(ae->pressure_prsc, D, ndpp, np, nlv * nsp);
+    o_pab = plan.add(ae->absorption_prsc, D, ndpp, np, nlv * nsp * ndb);
+    o_psc = plan.add(ae->scattering_prsc, D, ndpp, np, nlv * nsp * ndb);
+    o_pph = plan.add(ae->phase_fnc_prsc, D, ndpp, np, nlv * nph * nsp * ndb);
   }
   o_wb = c->weight_band ? plan.add(c->weight_band, D, nb, nb, 1, false, nullptr, false) : none;
   o_cmr = o_cdc = o_wc = o_fc = o_cs = o_fcl = o_nsc = o_sk = o_fsk = o_sro = none;
@@ -1086,6 +1177,7 @@ void window_params(FluxParams &p, int c0, int n) {
   mv(p.zen_0); mv(p.solar_irrad); mv(p.rho_alb); mv(p.t_ground); mv(p.flux_ground);
   mv(p.mode_mix_ratio); mv(p.mode_absorption); mv(p.mode_scattering); mv(p.mode_asymmetry);
   mv(p.aer_mix_ratio); mv(p.mean_rel_humidity);
+  mv(p.prsc_p); mv(p.prsc_abs); mv(p.prsc_scat); mv(p.prsc_phf);
   mv(p.condensed_mix_ratio); mv(p.condensed_dim_char); mv(p.w_cloud); mv(p.frac_cloud);
   mv(p.c_sub); mv(p.frac_cloudy); mv(p.n_subcol_cld);
   mv(p.flux_up); mv(p.flux_down); mv(p.flux_direct); mv(p.flux_div); mv(p.heating_rate);
@@ -1110,6 +1202,8 @@ void StagedCall::params(char *base, FluxParams &p) const {
     if (!aero) e2.n_mode = 0;
     e2.mix_ratio = (const double *)dptr(o_xmr);
     e2.mean_rel_humidity = (const double *)dptr(o_mrh);
+    e2.pressure_prsc = (const double *)dptr(o_pp); e2.absorption_prsc = (const double *)dptr(o_pab);
+    e2.scattering_prsc = (const double *)dptr(o_psc); e2.phase_fnc_prsc = (const double *)dptr(o_pph);
   }
   socgpu_cld c2{};
   if (mc) {
@@ -1343,6 +1437,11 @@ int make_group(socgpu_batch_s &b, const std::vector<int> &idx, int precision, in
   items.clear();
   start.assign(1, 0);
   for (int i : idx) {
+    if (b.params[i].l_aer_prsc) {
+      set_msg(msg, msg_len, "batch %d: prescribed aerosol properties run through socgpu_radiance_calc and "
+                            "socgpu_radiance_calc_device, not multi-batch launches", i);
+      return SOCGPU_I_ERR_FATAL;
+    }
     items.push_back(b.params[i]);
     start.push_back(start.back() + b.params[i].n_profile);
   }

@@ -696,6 +696,15 @@ struct FluxKernel {
       R kes = p.l_rayleigh ? (kFP64 ? (R)bd.rayleigh_coeff : (R)bd.rayleigh_f) : R(0);
       R kabs = R(0), phf = R(0), fwd = R(0);
       if (p.l_aerosol) classic_aerosol(p, col, i, b, kabs, kes, phf, fwd);
+      if (p.l_aer_prsc) {
+        // prescribed species: the sums of the prescribed-property kernel
+        const size_t plane = (size_t)(p.last_band - p.first_band + 1) * L * p.n_profile;
+        const size_t q0 = ((size_t)(b - (p.first_band - 1)) * L + i) * p.n_profile + col;
+        kabs = kabs + load_in<R>(p.aer_prsc + q0);
+        kes = kes + load_in<R>(p.aer_prsc + plane + q0);
+        phf = phf + load_in<R>(p.aer_prsc + 2 * plane + q0);
+        if (p.l_rescale) fwd = fwd + load_in<R>(p.aer_prsc + 3 * plane + q0);
+      }
       if (p.l_aerosol_mode) {
         for (int j = 0; j < p.n_mode; ++j) {
           R mmr = load_in<R>(p.mode_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * j));

@@ -38,6 +38,7 @@ struct SpectrumEntry {
   // classic aerosol species (block 11): parametrization, humidities and
   // phase-function moments of each, for validation
   std::vector<int> aer_parm, aer_nhum, aer_nphf;
+  int aer_nd_species = 0;             // the species extent of the aerosol arrays
   int device = 0;
 };
 
@@ -119,6 +120,8 @@ struct StagedCall {
   bool sw = false, mc = false, aero = false, classic = false;
   size_t o_p, o_t, o_tl, o_m, o_g, o_rho, o_z, o_si, o_alb, o_tg, o_amr, o_aab, o_asc, o_aas, o_wb, o_fg = (size_t)-1;
   size_t o_xmr = (size_t)-1, o_mrh = (size_t)-1;   // classic aerosol mixing ratios, mean relative humidity
+  bool prsc = false;                                // prescribed aerosol properties
+  size_t o_pp = (size_t)-1, o_pab = (size_t)-1, o_psc = (size_t)-1, o_pph = (size_t)-1;
   size_t o_cmr, o_cdc, o_wc, o_fc, o_cs, o_fcl, o_nsc, o_sk, o_fsk, o_sro;
   size_t o_fu, o_fd, o_fdir, o_div, o_hr;
 

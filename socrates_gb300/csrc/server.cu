@@ -492,6 +492,11 @@ int socgpu_server_submit(socgpu_server server, const socgpu_request *q, long lon
   if (q->aer) { r->aer = *q->aer; r->has_aer = true; }
   r->call.stage(&r->control, &r->dimen, sp, &r->atm, r->has_cld ? &r->cld : nullptr,
                 r->has_aer ? &r->aer : nullptr, &r->bound, &r->radout);
+  if (r->call.prsc) {
+    set_msg(msg, msg_len, "prescribed aerosol properties run through socgpu_radiance_calc and "
+                          "socgpu_radiance_calc_device, not the server");
+    return SOCGPU_I_ERR_FATAL;
+  }
   r->bytes = align256(r->call.plan.bytes);
   r->pinned = true;
   for (const Slot &sl : r->call.plan.slots) {

@@ -195,6 +195,19 @@ struct FluxParams {
   const double *mean_rel_humidity;  // (nd_profile, nd_layer), moist species only
   const double *aer_tab, *aer_hum;
   const float *aer_tab_f, *aer_hum_f;
+  // prescribed aerosol optical properties (prsc_opt_prop.F90) of the
+  // unparametrized species of the active entries: the data on their levels,
+  // and the per-layer sums the prescribed-property kernel writes before the
+  // flux kernel runs
+  int l_aer_prsc, n_prsc, prsc_nq;  // prsc_nq: phase-function moments interpolated
+  int nd_prof_prsc, nd_lev_prsc, nd_phf_prsc, nd_sp_prsc;
+  int prsc_species[kMaxAerMr];      // 0-based species
+  int prsc_count[kMaxAerMr];        // active entries that name it
+  int prsc_nlev[kMaxAerMr];         // its levels
+  const double *prsc_p, *prsc_abs, *prsc_scat, *prsc_phf;
+  // [4][last_band - first_band + 1][n_layer][n_profile]: absorption,
+  // scattering, scattering x asymmetry, scattering x forward moment
+  const double *aer_prsc;
   // outputs
   double *flux_up, *flux_down, *flux_direct, *flux_div, *heating_rate;
   int *error_flag;                  // device flag: set when a bound is violated
@@ -304,6 +317,11 @@ SOCGPU_DECL_PHASED(0, 1)
 SOCGPU_DECL_PHASED(1, 0)
 SOCGPU_DECL_PHASED(1, 1)
 #undef SOCGPU_DECL_PHASED
+
+// The prescribed-aerosol kernel (aerosol_prsc.cu): bytes of its output for
+// a launch, and its launch into `out` on stream st.
+size_t prsc_bytes(const FluxParams &p);
+int launch_prsc(const FluxParams &p, double *out, cudaStream_t st, char *msg, size_t len);
 
 // Whether the phased kernel covers a launch: clear sky, no equivalent
 // extinction, the direct beam delta-scaled, at most 256 layers.

@@ -343,6 +343,21 @@ class Marshal:
             self.aer.mr_type_index = _ip(ae["mr_type_index"], k)
             self.aer.mr_source = _ip(ae.get("mr_source"), k)
             self.aer.mean_rel_humidity = _dp(ae.get("mean_rel_humidity"), k)
+            # prescribed properties of unparametrized species: "pressure_prsc"
+            # (n, levels, species), "absorption_prsc"/"scattering_prsc" (n,
+            # levels, species, bands), "phase_fnc_prsc" (n, levels, moments,
+            # species, bands), "n_opt_level_prsc" and "n_phase_term_prsc"
+            # (species)
+            if "pressure_prsc" in ae:
+                ph = ae["phase_fnc_prsc"]
+                d.nd_profile_aerosol_prsc, d.nd_opt_level_aerosol_prsc = ph.shape[0], ph.shape[1]
+                d.nd_phf_term_aerosol_prsc = ph.shape[2]
+                self.aer.n_opt_level_prsc = _ip(ae["n_opt_level_prsc"], k)
+                self.aer.n_phase_term_prsc = _ip(ae["n_phase_term_prsc"], k)
+                self.aer.pressure_prsc = _dp(ae["pressure_prsc"], k)
+                self.aer.absorption_prsc = _dp(ae["absorption_prsc"], k)
+                self.aer.scattering_prsc = _dp(ae["scattering_prsc"], k)
+                self.aer.phase_fnc_prsc = _dp(ph, k)
         self.cld = abi.Cld()
         region = control.i_cloud in (abi.IP_CLOUD_MIX_MAX, abi.IP_CLOUD_MIX_RANDOM)
         if mcica is not None or (region and col.cld):

@@ -402,6 +402,52 @@ def add_aerosol_mix(col: Column, seed: int, entries=(1, 2, 3, 4), sources=None, 
     return col
 
 
+def add_prescribed_aerosol(sp: Spectrum, col: Column, seed: int, species=(2,), n_level: int = 30,
+                           n_phf: int = 2, p_top: float = 5.0e3) -> tuple[Spectrum, Column]:
+    """Prescribed optical properties (l_run_cdf's overlay of observations,
+    def_aer.F90:46-60) for the given 1-based species of add_aerosol_species,
+    which become unparametrized in a copy of the spectrum: per column,
+    n_level pressures log-spaced from p_top to just above the surface (layers
+    above p_top lie outside the levels), volume absorption and scattering
+    [1/m] decaying with height, and n_phf phase-function moments.  Returns
+    (spectrum, column); col.aer gains the *_prsc arrays."""
+    import copy
+    st = Stream(seed, 7)
+    sp2 = copy.copy(sp)
+    parm = np.array(sp.i_aerosol_parm, np.int32)
+    nsp, nb, n = len(parm), sp.n_band, col.n_profile
+    lam = np.sqrt(sp.wavelength_short * sp.wavelength_long) / 0.55e-6
+    pl = np.zeros((n, n_level, nsp), order="F")
+    ab = np.zeros((n, n_level, nsp, nb), order="F")
+    sc = np.zeros((n, n_level, nsp, nb), order="F")
+    ph = np.zeros((n, n_level, n_phf, nsp, nb), order="F")
+    nlev = np.ones(nsp, np.int32)
+    nmom = np.ones(nsp, np.int32)
+    for s in species:
+        j = s - 1
+        parm[j] = abi.IP_AEROSOL_UNPARAMETRIZED
+        nlev[j], nmom[j] = n_level, n_phf
+        p_bot = col.p_level[:, -1] * (0.995 - 0.01 * st.uniform((n,)))
+        lev = np.exp(np.linspace(0.0, 1.0, n_level)[None, :] * np.log(p_bot / p_top)[:, None]) * p_top
+        pl[:, :, j] = lev
+        ext0 = 2.0e-5 * (0.5 + st.uniform((n,)))                          # 1/m at the surface
+        shape = (lev / p_bot[:, None]) ** 6                                 # ~ 1.3 km scale height
+        w = 0.8 + 0.15 * st.uniform((n,))
+        for b in range(nb):
+            e = ext0[:, None] * shape * lam[b] ** -0.5
+            ab[:, :, j, b] = e * (1.0 - w[:, None])
+            sc[:, :, j, b] = e * w[:, None]
+            g = 0.6 + 0.1 * (lev / p_bot[:, None])
+            for m in range(n_phf):
+                ph[:, :, m, j, b] = g ** (m + 1) * (1.0 if m == 0 else 1.05)
+    sp2.i_aerosol_parm = parm
+    sp2.name = f"{sp.name}_prsc{''.join(map(str, species))}"
+    col.aer = dict(col.aer or {})
+    col.aer.update(n_opt_level_prsc=nlev, n_phase_term_prsc=nmom, pressure_prsc=pl, absorption_prsc=ab,
+                   scattering_prsc=sc, phase_fnc_prsc=ph)
+    return sp2, col
+
+
 def add_clouds(col: Column, seed: int, n_subcol: int = 16, decorrelation_m: float = 2000.0,
                cloud_prob: float = 0.3, p_top: float = 1.0e4) -> Column:
     """Cloud fields as set_cld leaves them for ip_cloud_ice_water

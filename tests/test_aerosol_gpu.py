@@ -121,3 +121,64 @@ def test_classic_aerosol_with_mcica_clouds(gpu_lib):
     gpu = {**R.radiance_calc(ctl, sw, col, mc), "mass": col.mass}
     ref = {**O.radiance_calc(ctl, sw, col, mc), "mass": col.mass}
     assert_fp64_parity(gpu, ref, "mcica: ")
+
+
+def _prsc_case(solar, n=40, L=70, seed=66, n_phf=2):
+    if solar:
+        sp, col = synth.config2(n, L, seed=seed)
+    else:
+        sp, col = synth.config1(n, L, seed=seed)
+    col.aer = None
+    synth.add_density(col, 1)
+    synth.add_aerosol_species(sp, seed, n_humidity=21, n_phf=3)
+    # species 2 prescribed, named by an inactive entry and an active one;
+    # the others parametrized
+    synth.add_aerosol_mix(col, seed, entries=(1, 2, 3, 2, 4), sources=SOURCES)
+    return synth.add_prescribed_aerosol(sp, col, seed, species=(2,), n_phf=n_phf)
+
+
+@pytest.mark.parametrize("hg", [False, True], ids=["tabulated", "hg"])
+@pytest.mark.parametrize("solar", [False, True], ids=["lw", "sw"])
+def test_prescribed_aerosol_fp64(kernel, solar, hg):
+    """Prescribed optical properties (prsc_opt_prop.F90) of one species next
+    to parametrized ones: the spline kernel and the flux kernels against the
+    oracle."""
+    sp, col = _prsc_case(solar)
+    mk = R.sw_control if solar else R.lw_control
+    gpu, ref = _both(mk(l_aerosol=True, l_henyey_greenstein_pf=hg), sp, col)
+    assert_fp64_parity(gpu, ref, f"{kernel} prescribed: ")
+
+
+@pytest.mark.parametrize("solar", [False, True], ids=["lw", "sw"])
+def test_prescribed_aerosol_mixed(kernel, solar):
+    sp, col = _prsc_case(solar, seed=67)
+    mk = R.sw_control if solar else R.lw_control
+    gpu, ref = _both(mk(l_aerosol=True, l_henyey_greenstein_pf=True, precision=abi.PRECISION_MIXED), sp, col)
+    assert_mixed_tolerance(gpu, ref, f"{kernel} prescribed: ")
+
+
+def test_prescribed_aerosol_in_column_windows(gpu_lib):
+    """Enough columns that the host path copies and solves them in several
+    windows: the prescribed arrays move with each window."""
+    sp, col = _prsc_case(True, n=1500, L=40, seed=68)
+    gpu, ref = _both(R.sw_control(l_aerosol=True, l_henyey_greenstein_pf=True), sp, col)
+    assert_fp64_parity(gpu, ref, "windows: ")
+
+
+def test_prescribed_aerosol_checks(gpu_lib):
+    from socrates_gb300.server import Server
+    sp, col = _prsc_case(False, n=6, L=30, seed=69)
+    # moments: the tabulated forward moment needs n_order_forward (2) of them
+    col.aer["n_phase_term_prsc"] = np.ones_like(col.aer["n_phase_term_prsc"])
+    with pytest.raises(R.RadianceError, match="moments"):
+        R.radiance_calc(R.lw_control(l_aerosol=True), sp, col)
+    sp, col = _prsc_case(False, n=6, L=30, seed=69)
+    col.density = None
+    with pytest.raises(R.RadianceError, match="density"):
+        R.radiance_calc(R.lw_control(l_aerosol=True), sp, col)
+    sp, col = _prsc_case(False, n=6, L=30, seed=69)
+    R.register_spectrum(sp)
+    srv = Server(device_bytes=64 << 20, streams=1)
+    with pytest.raises(R.RadianceError, match="server"):
+        srv.submit(R.Marshal(R.lw_control(l_aerosol=True), sp, col), sp)
+    srv.close()

@@ -481,3 +481,61 @@ def test_aerosol_block_round_trip(tmp_path):
             b = b[:m]
         assert a.shape == b.shape, name
         np.testing.assert_allclose(b, a, rtol=1e-6, atol=0, err_msg=name)
+
+
+def _prescribed_as_modes(col, species, hg=True):
+    """The prescribed properties of the given 0-based species at the layer
+    pressures, by scipy's natural cubic spline (an independent fit), in the
+    modal form: unit mixing ratio, absorption and scattering divided by the
+    air density and floored at zero, asymmetry; zero outside the levels."""
+    from scipy.interpolate import CubicSpline
+    ae = col.aer
+    n, L = col.n_profile, col.n_layer
+    nb = ae["absorption_prsc"].shape[3]
+    shape = (n, L, len(species), nb)
+    ab, sc, g = (np.zeros(shape, order="F") for _ in range(3))
+    for m, j in enumerate(species):
+        nl = int(ae["n_opt_level_prsc"][j])
+        for l in range(n):
+            x = ae["pressure_prsc"][l, :nl, j]
+            inside = (col.p[l] >= x[0]) & (col.p[l] <= x[-1])
+            for b in range(nb):
+                for arr, y in ((ab, ae["absorption_prsc"][l, :nl, j, b]), (sc, ae["scattering_prsc"][l, :nl, j, b]),
+                               (g, ae["phase_fnc_prsc"][l, :nl, 0, j, b])):
+                    v = np.where(inside, CubicSpline(x, y, bc_type="natural")(col.p[l]), 0.0)
+                    if arr is not g:
+                        v = np.maximum(0.0, v / col.density[l])
+                    arr[l, :, m, b] = v
+    mc = synth.Column(**{k: getattr(col, k) for k in col.__dataclass_fields__})
+    mc.aer = dict(n_mode=len(species), mode_mix_ratio=np.ones((n, L, len(species)), order="F"),
+                  mode_absorption=ab, mode_scattering=sc, mode_asymmetry=g)
+    return mc
+
+
+@pytest.mark.parametrize("solar", [False, True])
+def test_prescribed_aerosol_matches_independent_spline(solar):
+    """Prescribed optical properties (prsc_opt_prop.F90 with the natural
+    cubic spline of spline_fit.F90 / spline_evaluate.F90) equal the modal
+    form fed scipy's natural cubic spline of the same data; a species named
+    by two active entries counts twice; layers above the top level get
+    nothing."""
+    if solar:
+        sp, col = synth.config2(5, 60, seed=71)
+    else:
+        sp, col = synth.config1(5, 60, seed=71)
+    col.aer = None
+    synth.add_density(col, 1)
+    synth.add_aerosol_species(sp, 71)
+    synth.add_aerosol_mix(col, 71, entries=(2, 2))
+    sp, col = synth.add_prescribed_aerosol(sp, col, 71, species=(2,))
+    assert (col.p[:, 0] < col.aer["pressure_prsc"][:, 0, 1]).all()      # some layers outside the levels
+    mk = R.sw_control if solar else R.lw_control
+    got = O.radiance_calc(mk(l_aerosol=True, l_henyey_greenstein_pf=True), sp, col)
+    mc = _prescribed_as_modes(col, [1, 1])
+    ref = O.radiance_calc(mk(l_aerosol_mode=True), sp, mc)
+    clear = O.radiance_calc(mk(), sp, col)
+    # the two spline solvers round differently (values spanning several decades)
+    for k in ("flux_up", "flux_down"):
+        scale = np.abs(ref[k]).max()
+        assert np.abs(got[k] - ref[k]).max() <= 1e-10 * scale, k
+        assert np.abs(got[k] - clear[k]).max() > 1e-3, f"{k}: the aerosol changed nothing"
