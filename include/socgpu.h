@@ -436,6 +436,21 @@ SOCGPU_API int socgpu_spectrum_release(socgpu_spectrum_handle handle);
  * n_k_major has room for n_band_max entries.  Any pointer may be NULL. */
 SOCGPU_API int socgpu_spectrum_k_terms(socgpu_spectrum_handle handle, int n_band_max, int *n_band, int *nd_k_term,
                                        int *n_k_major);
+/* The classic aerosol species of a spectrum (block 11 with the list of
+ * block 0): their count and, for up to n_max species, type numbers,
+ * parametrizations (SOCGPU_IP_AEROSOL_PARAM_* or _UNPARAMETRIZED) and
+ * tabulated humidities.  Any array pointer may be NULL. */
+SOCGPU_API int socgpu_spectrum_aerosols(socgpu_spectrum_handle handle, int n_max, int *n_aerosol,
+                                        int *type_aerosol, int *i_aerosol_parm, int *nhumidity);
+/* Sets the parametrization of species `species` (1-based) of a registered
+ * spectrum, as l_run_cdf does when it overlays observed optical properties
+ * (input_aerosol_cdf.f:102-143): SOCGPU_IP_AEROSOL_UNPARAMETRIZED (the
+ * species then takes socgpu_aer's prescribed properties) or the species'
+ * parametrization in its spectral file.  Calls already running keep the
+ * value they read; do not change it while another thread submits work that
+ * uses the spectrum. */
+SOCGPU_API int socgpu_spectrum_set_aerosol_parm(socgpu_spectrum_handle handle, int species, int parm, char *msg,
+                                                size_t msg_len);
 
 /* Replaces radiance_calc (src/radiance_core/radiance_calc.F90:16) for the
  * two-stream clear-sky and McICA paths.  All pointers are host memory; the

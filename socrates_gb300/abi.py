@@ -209,7 +209,7 @@ ABI_FUNCTIONS = (
     "socgpu_batch_info", "socgpu_batch_destroy", "socgpu_tune_get", "socgpu_tune_set",
     "socgpu_server_create", "socgpu_server_submit", "socgpu_server_wait", "socgpu_server_stats_get",
     "socgpu_server_destroy", "socgpu_spectrum_load", "socgpu_spectrum_load_ext", "socgpu_runes",
-    "socgpu_spectrum_k_terms",
+    "socgpu_spectrum_k_terms", "socgpu_spectrum_aerosols", "socgpu_spectrum_set_aerosol_parm",
 )
 
 _CALC_ARGS = [C.POINTER(Control), C.POINTER(Dimen), C.c_int, C.POINTER(Atm), C.POINTER(Cld), C.POINTER(Aer),
@@ -230,6 +230,9 @@ def declare(lib: C.CDLL) -> C.CDLL:
     lib.socgpu_spectrum_n_gpoint.argtypes = [C.c_int]
     lib.socgpu_spectrum_k_terms.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_int)]
+    lib.socgpu_spectrum_aerosols.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                             C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.socgpu_spectrum_set_aerosol_parm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_size_t]
     lib.socgpu_spectrum_release.argtypes = [C.c_int]
     lib.socgpu_radiance_calc.argtypes = _CALC_ARGS + [C.c_char_p, C.c_size_t]
     lib.socgpu_radiance_calc_device.argtypes = _CALC_ARGS + [C.c_void_p, C.c_char_p, C.c_size_t]

@@ -431,7 +431,7 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   // classic aerosol species (block 11): one row per (band, species,
   // humidity) of absorption, scattering and the phase-function moments
   std::vector<double> aer_tab, aer_hum;
-  e.aer_parm.clear(); e.aer_nhum.clear(); e.aer_nphf.clear();
+  e.aer_parm.clear(); e.aer_nhum.clear(); e.aer_nphf.clear(); e.aer_type.clear();
   if (d->n_aerosol > 0 && d->i_aerosol_parm && d->aerosol_abs && d->aerosol_scat && d->aerosol_phf) {
     if (d->n_aerosol > d->nd_aerosol_species || d->nd_humidity < 1 || d->nd_phase_term < 1) {
       set_msg(msg, msg_len, "aerosol extents inconsistent (%d species, %d allocated)", d->n_aerosol,
@@ -447,6 +447,7 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
         return SOCGPU_I_ERR_RANGE;
       }
       e.aer_parm.push_back(d->i_aerosol_parm[j]);
+      e.aer_type.push_back(d->type_aerosol ? d->type_aerosol[j] : 0);
       e.aer_nhum.push_back(hj);
       e.aer_nphf.push_back(std::max(1, fj));
       nh = std::max(nh, hj);
@@ -454,6 +455,7 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
     }
     s.aer_n_species = nsp; s.aer_nh = nh; s.aer_nphf = nphf;
     e.aer_nd_species = d->nd_aerosol_species;
+    e.aer_parm_file = e.aer_parm;
     const int row = 2 + nphf, ndh = d->nd_humidity, ndf = d->nd_phase_term, nda = d->nd_aerosol_species;
     aer_tab.assign((size_t)d->n_band * nsp * nh * row, 0.0);
     aer_hum.assign((size_t)nsp * nh, 0.0);
@@ -1600,6 +1602,36 @@ int socgpu_spectrum_k_terms(socgpu_spectrum_handle handle, int n_band_max, int *
   if (nd_k_term) *nd_k_term = e->dev.nd_k_term;
   if (n_k_major)
     for (int b = 0; b < e->dev.n_band && b < n_band_max; ++b) n_k_major[b] = e->n_k_major[b];
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_spectrum_aerosols(socgpu_spectrum_handle handle, int n_max, int *n_aerosol, int *type_aerosol,
+                             int *i_aerosol_parm, int *nhumidity) {
+  SpectrumEntry *e = find_spectrum(handle);
+  if (!e) return SOCGPU_I_ERR_EXIST;
+  const int n = (int)e->aer_parm.size();
+  if (n_aerosol) *n_aerosol = n;
+  for (int j = 0; j < n && j < n_max; ++j) {
+    if (type_aerosol) type_aerosol[j] = e->aer_type[j];
+    if (i_aerosol_parm) i_aerosol_parm[j] = e->aer_parm[j];
+    if (nhumidity) nhumidity[j] = e->aer_nhum[j];
+  }
+  return SOCGPU_I_NORMAL;
+}
+
+int socgpu_spectrum_set_aerosol_parm(socgpu_spectrum_handle handle, int species, int parm, char *msg,
+                                     size_t msg_len) {
+  SpectrumEntry *e = find_spectrum(handle);
+  if (!e) { set_msg(msg, msg_len, "no spectrum with handle %d", handle); return SOCGPU_I_ERR_EXIST; }
+  if (species < 1 || species > (int)e->aer_parm.size()) {
+    set_msg(msg, msg_len, "aerosol species %d is not in the spectrum", species); return SOCGPU_I_ERR_RANGE; }
+  if (parm != SOCGPU_IP_AEROSOL_UNPARAMETRIZED && parm != e->aer_parm_file[species - 1]) {
+    set_msg(msg, msg_len, "aerosol species %d: parametrization %d is neither prescribed nor the file's %d", species,
+            parm, e->aer_parm_file[species - 1]);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  std::lock_guard<std::mutex> lk(g_reg_mutex);
+  e->aer_parm[species - 1] = parm;
   return SOCGPU_I_NORMAL;
 }
 

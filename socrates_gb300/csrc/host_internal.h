@@ -38,6 +38,8 @@ struct SpectrumEntry {
   // classic aerosol species (block 11): parametrization, humidities and
   // phase-function moments of each, for validation
   std::vector<int> aer_parm, aer_nhum, aer_nphf;
+  std::vector<int> aer_type;          // type numbers of the species
+  std::vector<int> aer_parm_file;     // parametrizations as the spectral file gives them
   int aer_nd_species = 0;             // the species extent of the aerosol arrays
   int device = 0;
 };

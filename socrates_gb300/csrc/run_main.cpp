@@ -9,6 +9,7 @@
 //              [-ds <direct tau>] [-P fp64|mixed] [-W <Wen-Yi tables file>]
 //              [-C 10 -K <cloud representation> -d <droplet type> -i <ice type>
 //               -m <condensate relative std. deviation> +m <sampling> -dp <decorrelation scale>]
+//              [-a [+A]]
 //   socgpu_run --convert <in> <out.cdf|out.cdl>
 //
 // Inputs: .t (layer temperatures on the layer pressures `plev`), .tl (level
@@ -25,11 +26,16 @@
 // spectral file's droplet type -d, ice from .iwm and .ire with ice type -i
 // (input_cloud_cdf.f:340-790), and the subcolumns of set_cld_mcica from the
 // McICA data file beside the spectral file (l_run_cdf.F90:998-1010,
-// 1281-1296).
+// 1281-1296).  With -a the spectral file's aerosol species are included:
+// mixing ratios from <base>.<species suffix> (wtsol, dust, ocn, soot, ...;
+// none without a file) and, with +A, prescribed optical properties from
+// <base>.op_<species suffix> in place of the species' parametrization.
+// Moist species take the clear-sky mean relative humidity of the layers.
 // Lookup tables are read from the spectral file's '_k' companion; spectral
 // files with Wen-Yi CO2 terms (GA7 and GA9 long wave) need -W, the data file
 // of those tables (the reference compiles them in; socrates_gb300/wenyi.py
 // converts them from a SOCRATES source tree once).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -59,6 +65,37 @@ const char *gas_suffix(int type) {
                             "he",     "ocs",    "na",     "k",       "feh",    "crh",  "li",   "rb",
                             "cs",     "ph3",    "c2h2",   "hcn",     "h2s",    "ar"};
   return (type >= 1 && type < (int)(sizeof(s) / sizeof(s[0]))) ? s[type] : nullptr;
+}
+
+// File suffixes of the aerosol species by type number (the names
+// l_run_cdf's input_aerosol_cdf.f looks for: <base>.<suffix> holds mixing
+// ratios, <base>.op_<suffix> prescribed optical properties)
+const char *aerosol_suffix(int type) {
+  static const char *s[] = {"",         "wtsol",    "dust",     "ocn",      "soot",     "ash",     "sulph",
+                            "nh4so4",   "aunch",    "sahara",   "accum",    "aitken",   "frsoot",  "agsoot",
+                            "nacl",     "naclflm",  "nacljet",  "dustdiv1", "dustdiv2", "dustdiv3", "dustdiv4",
+                            "dustdiv5", "dustdiv6", "bioms1",   "bioms2",   "biogenic", "frocff",  "agocff",
+                            "delta",    "",         "nitrate",  "dust2bin1", "dust2bin2"};
+  return (type >= 1 && type < (int)(sizeof(s) / sizeof(s[0])) && s[type][0]) ? s[type] : nullptr;
+}
+
+// Saturation mixing ratio over water [kg/kg] at temperature t [K] and
+// pressure p [Pa]: the Goff-Gratch saturation vapour pressure over a plane
+// water surface (WMO), t held to 183.15-338.15 K, times Gill's (1982,
+// A4.7) factor for vapour in air, then the mixing ratio with the pressure
+// floored at the vapour pressure (the role of qsat_wat.F90 in
+// set_moist_aerosol_properties.F90; that routine interpolates a 0.1 K table
+// of the same formula instead).
+double qsat_water(double t, double p) {
+  const double ts = 373.16, tt = std::min(std::max(t, 183.15), 338.15);
+  const double r = ts / tt;
+  const double log10_hpa = -7.90298 * (r - 1.0) + 5.02808 * std::log10(r) -
+                           1.3816e-7 * (std::pow(10.0, 11.344 * (1.0 - 1.0 / r)) - 1.0) +
+                           8.1328e-3 * (std::pow(10.0, -3.49149 * (r - 1.0)) - 1.0) + std::log10(1013.246);
+  const double fsubw = 1.0 + 1.0e-8 * p * (4.5 + 6.0e-4 * (t - 273.15) * (t - 273.15));
+  const double e = 100.0 * std::pow(10.0, log10_hpa) * fsubw;
+  const double eps = kMolarWeightH2O * 1.0e-03 / kMolWeightAir;
+  return eps * e / (std::max(p, e) - (1.0 - eps) * e);
 }
 
 int die(const std::string &m) {
@@ -275,6 +312,7 @@ int main(int argc, char **argv) {
   int precision = SOCGPU_PRECISION_FP64;
   // clouds (-K, -d, -i) and McICA (-m, +m, -dp)
   int representation = 0, drop_type = 0, ice_type = 0, sampling = 2;
+  bool aerosol = false, overlay = false;   // -a: classic aerosols; +A: overlay of optical properties
   double mcica_sigma = 0.0, dp_corr_strat = 0.0;
   for (size_t i = 0; i < a.size(); ++i) {
     const std::string &o = a[i];
@@ -288,6 +326,8 @@ int main(int argc, char **argv) {
     else if (o == "-g" && need(1)) { gas = true; overlap = std::atoi(a[++i].c_str()); }
     else if (o == "-c") cont = true;
     else if (o == "-r") rayleigh = true;
+    else if (o == "-a") aerosol = true;
+    else if (o == "+A") overlay = true;
     else if (o == "+R") rescale = true;
     else if (o == "-q") quad = true;
     else if (o == "-t" && need(1)) two_stream = std::atoi(a[++i].c_str());
@@ -310,6 +350,7 @@ int main(int argc, char **argv) {
   if (base.empty()) return die("Base name not set.");
   if (!isolir) return die("Spectral region not set.");
   if (first < 1 || last < first) return die("Range of bands not set");
+  if (overlay && !aerosol) return die("+A overlays aerosol optical properties: it needs -a");
   const bool region = cloud == SOCGPU_IP_CLOUD_MIX_MAX || cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
   if (cloud != SOCGPU_IP_CLOUD_CLEAR && cloud != SOCGPU_IP_CLOUD_MCICA && !region)
     return die("cloud scheme " + std::to_string(cloud) +
@@ -433,7 +474,8 @@ int main(int argc, char **argv) {
     int id[4] = {-1, -1, -1, -1};    // lat, lon, basis, band
     for (size_t q = 0; q < alb->dims.size(); ++q) {
       const std::string &dn = sfile.dims[alb->dims[q]].first;
-      const int k = dn == "lat" ? 0 : dn == "lon" ? 1 : dn == "basis" ? 2 : dn == "band" ? 3 : -1;
+      // a dimension whose name starts with "band" (assign_surface_char_cdf.f:213-218)
+      const int k = dn == "lat" ? 0 : dn == "lon" ? 1 : dn == "basis" ? 2 : dn.compare(0, 4, "band") == 0 ? 3 : -1;
       if (k < 0) return die(base + ".surf: unexpected dimension " + dn);
       id[k] = (int)q;
       len[k] = sfile.dims[alb->dims[q]].second;
@@ -598,6 +640,115 @@ int main(int argc, char **argv) {
       for (size_t l = 0; l < np; ++l) frac_cloudy[l] = (double)n_subcol_cld[l] / (double)gen;
   }
 
+  // classic aerosols (-a; l_run_cdf.F90:847-920 with input_aerosol_cdf.f):
+  // for each species of the spectral file, with +A a file of optical
+  // properties <base>.op_<suffix> overlays it (the species becomes
+  // unparametrized), otherwise its mixing ratios come from <base>.<suffix>
+  // (none without a file); moist species need the clear-sky mean relative
+  // humidity (set_moist_aerosol_properties.F90)
+  int n_aer = 0, nd_lev_prsc = 1, nd_mom_prsc = 1;
+  std::vector<int> aer_type, aer_parm, aer_nhum, mr_index, mr_source, nlev_prsc, nmom_prsc;
+  std::vector<double> aer_mr, mrh, p_prsc, abs_prsc, scat_prsc, phf_prsc;
+  if (aerosol) {
+    if (socgpu_spectrum_aerosols(h, 0, &n_aer, nullptr, nullptr, nullptr) != SOCGPU_I_NORMAL || n_aer < 1)
+      return die("The spectral file contains no aerosol data.");
+    aer_type.resize(n_aer); aer_parm.resize(n_aer); aer_nhum.resize(n_aer);
+    socgpu_spectrum_aerosols(h, n_aer, &n_aer, aer_type.data(), aer_parm.data(), aer_nhum.data());
+    aer_mr.assign(np * nl * (size_t)n_aer, 0.0);
+    nlev_prsc.assign(n_aer, 1);
+    nmom_prsc.assign(n_aer, 1);
+    struct Opt { size_t nlev, nmom; std::vector<double> lev, ab, sc, ph; };   // ab, sc: (band, lev, profile)
+    std::map<int, Opt> opt;
+    for (int i = 0; i < n_aer; ++i) {
+      const char *suf = aerosol_suffix(aer_type[i]);
+      if (!suf) continue;
+      const std::string op_path = base + ".op_" + suf;
+      if (overlay && exists(op_path)) {
+        // assign_input_opt_cdf.f: abs and scat (band, plev, lat, lon), phf
+        // (band, mom, plev, lat, lon) on the pressures of plev
+        NcFile f;
+        if (!socgpu::read_nc(op_path, f, err)) return die(err);
+        const NcVar *va = f.var("abs"), *vs = f.var("scat"), *vp = f.var("phf"), *lev = f.var("plev");
+        const size_t nlev = f.dim_len("plev"), nmom = std::max<size_t>(1, f.dim_len("mom"));
+        if (!va || !vs || !vp || !lev || nlev < 1) return die(op_path + ": abs, scat, phf and plev expected");
+        auto dims_are = [&](const NcVar *v, std::vector<std::string> want) {
+          if (v->dims.size() != want.size()) return false;
+          for (size_t q = 0; q < want.size(); ++q)
+            if (f.dims[v->dims[q]].first != want[q]) return false;
+          return true;
+        };
+        if (!dims_are(va, {"band", "plev", "lat", "lon"}) || !dims_are(vs, {"band", "plev", "lat", "lon"}) ||
+            !dims_are(vp, {"band", "mom", "plev", "lat", "lon"}))
+          return die(op_path + ": dimensions (band, [mom,] plev, lat, lon) expected");
+        if ((int)f.dim_len("band") != nb_total) return die(op_path + ": band dimension differs from the spectral file");
+        if (f.dim_len("lat") * std::max<size_t>(1, f.dim_len("lon")) != np) return die(op_path + ": not on the columns of .t");
+        for (size_t k = 1; k < nlev; ++k)
+          if (!(lev->data[k] > lev->data[k - 1])) return die(op_path + ": pressures must increase");
+        if (va->data.size() != (size_t)nb_total * nlev * np || vs->data.size() != va->data.size() ||
+            vp->data.size() != (size_t)nb_total * nmom * nlev * np)
+          return die(op_path + ": short data");
+        Opt o{nlev, nmom, lev->data, va->data, vs->data, vp->data};
+        opt[i] = std::move(o);
+        if (socgpu_spectrum_set_aerosol_parm(h, i + 1, SOCGPU_IP_AEROSOL_UNPARAMETRIZED, msg, sizeof(msg)) !=
+            SOCGPU_I_NORMAL)
+          return die(msg);
+        aer_parm[i] = SOCGPU_IP_AEROSOL_UNPARAMETRIZED;
+        nlev_prsc[i] = (int)nlev;
+        nmom_prsc[i] = (int)nmom;
+        nd_lev_prsc = std::max(nd_lev_prsc, (int)nlev);
+        nd_mom_prsc = std::max(nd_mom_prsc, (int)nmom);
+        continue;
+      }
+      const std::string mr_path = base + "." + suf;
+      if (!exists(mr_path)) continue;
+      Field fm;
+      if (!read_field(mr_path, fm, err)) return die(err);
+      if (fm.n_prof() != np || fm.n_lev != nl) return die(mr_path + ": not on the layers of .t");
+      for (size_t q = 0; q < np * nl; ++q) aer_mr[q + np * nl * (size_t)i] = fm.v[q];
+    }
+    for (int i = 0; i < n_aer; ++i) {
+      mr_index.push_back(i + 1);
+      mr_source.push_back(SOCGPU_IP_AERSRC_CLASSIC_RON);
+    }
+    if (!opt.empty()) {
+      const size_t ndl = (size_t)nd_lev_prsc, ndm = (size_t)nd_mom_prsc, na = (size_t)n_aer, nbt = (size_t)nb_total;
+      p_prsc.assign(np * ndl * na, 0.0);
+      abs_prsc.assign(np * ndl * na * nbt, 0.0);
+      scat_prsc.assign(np * ndl * na * nbt, 0.0);
+      phf_prsc.assign(np * ndl * ndm * na * nbt, 0.0);
+      for (const auto &kv : opt) {
+        const size_t j = (size_t)kv.first;
+        const Opt &o = kv.second;
+        for (size_t k = 0; k < o.nlev; ++k)
+          for (size_t l = 0; l < np; ++l) {
+            p_prsc[l + np * (k + ndl * j)] = o.lev[k];
+            for (size_t b = 0; b < nbt; ++b) {
+              abs_prsc[l + np * (k + ndl * (j + na * b))] = o.ab[(b * o.nlev + k) * np + l];
+              scat_prsc[l + np * (k + ndl * (j + na * b))] = o.sc[(b * o.nlev + k) * np + l];
+              for (size_t m = 0; m < o.nmom; ++m)
+                phf_prsc[l + np * (k + ndl * (m + ndm * (j + na * b)))] = o.ph[((b * o.nmom + m) * o.nlev + k) * np + l];
+            }
+          }
+      }
+    }
+    bool moist = false;
+    for (int i = 0; i < n_aer; ++i)
+      moist = moist || aer_parm[i] == SOCGPU_IP_AEROSOL_PARAM_MOIST || aer_parm[i] == SOCGPU_IP_AEROSOL_PARAM_PHF_MOIST;
+    if (moist) {
+      if (i_water < 0) return die("Water vapour must be included in the spectral file to treat moist aerosols.");
+      mrh.assign(np * nl, 0.0);
+      for (size_t q = 0; q < np * nl; ++q) {
+        const double qw = gas_mr[q + np * nl * (size_t)i_water];
+        const double qs = qsat_water(t.v[q], p[q]);
+        const double wc = clouds ? w_cloud[q] : 0.0;
+        double clr = (qw - wc * qs) / std::max(1.0 - wc, 0.001);
+        clr = std::max(std::min(clr, qw), 0.0);
+        const double rh = clr * (1.0 - qs) / ((1.0 - clr) * qs);
+        mrh[q] = std::max(std::min(rh, 0.99999), 0.0);
+      }
+    }
+  }
+
   socgpu_control c{};
   c.isolir = isolir;
   c.i_angular_integration = SOCGPU_IP_TWO_STREAM;
@@ -618,6 +769,10 @@ int main(int argc, char **argv) {
   c.last_band = last;
   c.precision = precision;
   c.l_continuum = cont;
+  // two-stream with rescaling: Henyey-Greenstein phase functions
+  // (angular_control_cdf.f:236-246)
+  c.l_aerosol = aerosol;
+  c.l_henyey_greenstein_pf = rescale;
   socgpu_dimen d{};
   d.nd_profile = (int)np;
   d.nd_layer = (int)nl;
@@ -627,6 +782,10 @@ int main(int argc, char **argv) {
   d.nd_cloud_type = n_cloud_type;
   d.nd_subcol_gen = mcica ? gen : 1;
   d.nd_subcol_req = mcica ? n_subcol_req : 1;
+  d.nd_aerosol_mr = std::max(1, n_aer);
+  d.nd_profile_aerosol_prsc = p_prsc.empty() ? 1 : (int)np;
+  d.nd_opt_level_aerosol_prsc = nd_lev_prsc;
+  d.nd_phf_term_aerosol_prsc = nd_mom_prsc;
   socgpu_atm atm{};
   atm.n_profile = (int)np;
   atm.n_layer = (int)nl;
@@ -647,6 +806,21 @@ int main(int argc, char **argv) {
   out.flux_down = down.data();
   out.flux_direct = isolir == SOCGPU_IP_SOLAR ? direct.data() : nullptr;
   socgpu_aer aer{};
+  if (aerosol) {
+    aer.n_aerosol_mr = n_aer;
+    aer.mix_ratio = aer_mr.data();
+    aer.mr_type_index = mr_index.data();
+    aer.mr_source = mr_source.data();
+    aer.mean_rel_humidity = mrh.empty() ? nullptr : mrh.data();
+    if (!p_prsc.empty()) {
+      aer.n_opt_level_prsc = nlev_prsc.data();
+      aer.n_phase_term_prsc = nmom_prsc.data();
+      aer.pressure_prsc = p_prsc.data();
+      aer.absorption_prsc = abs_prsc.data();
+      aer.scattering_prsc = scat_prsc.data();
+      aer.phase_fnc_prsc = phf_prsc.data();
+    }
+  }
   socgpu_cld cld{};
   if (clouds) {
     cld.n_condensed = nc;

@@ -182,3 +182,23 @@ def test_prescribed_aerosol_checks(gpu_lib):
     with pytest.raises(R.RadianceError, match="server"):
         srv.submit(R.Marshal(R.lw_control(l_aerosol=True), sp, col), sp)
     srv.close()
+
+
+def test_circ6_sw_aerosol_known_good_output(gpu_lib, kernel):
+    """The reference's CIRC case 6 short-wave run with prescribed soot and
+    two-region clouds (ref_case6_sw_ga7.hrts) on the GPU: FP64 within 1e-10
+    of the oracle and within half a unit of the 6th significant digit of the
+    known-good heating rates (5 % slack on rounding boundaries); mixed
+    precision within its tolerance of the oracle."""
+    import circ6_sw as K
+    from cld7460 import half_units
+    ctl, sp, col, kgo = K.load()
+    gpu, ref = _both(ctl, sp, col)
+    assert_fp64_parity(gpu, ref, f"{kernel} circ6 sw: ")
+    hr = K.heating_rate(gpu, col)[0]
+    err = half_units(hr, kgo)
+    assert err.max() <= 1.05, f"layer {err.argmax()}: {hr[err.argmax()]} vs {kgo[err.argmax()]}"
+    from dataclasses import replace
+    ctl_m = replace(ctl, precision=abi.PRECISION_MIXED)
+    gpu_m, ref_m = _both(ctl_m, sp, col)
+    assert_mixed_tolerance(gpu_m, ref, f"{kernel} circ6 sw mixed: ")

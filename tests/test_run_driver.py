@@ -341,3 +341,63 @@ def test_driver_reproduces_cld7460(gpu_lib, tmp_path, run, to_cdf):
     else:
         _, got = field(out)
         assert K.half_units(got, kgo).max() <= 1.05
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("to_cdf", [False, True])
+def test_driver_reproduces_circ6_sw_aerosol(gpu_lib, tmp_path, to_cdf):
+    """CIRC case 6 in the short wave with the GA7 file, two-region clouds and
+    the overlay of prescribed soot optical properties through the column
+    driver (examples/netcdf/CIRC_case6/run_me: -R 1 6 -S +R -g 4 -c -r -a +A
+    -C 2 -K 1 -d 5 -i 8): the driver reads the aerosol species of the
+    spectral file (block 11), finds case6.op_soot, makes soot unparametrized
+    and runs the others with zero mixing ratios (no files); the surface file
+    has a 'bands' dimension (one albedo per band)."""
+    import circ6_sw as K
+    from socrates_gb300.spectrum import Spectrum
+    tool = _tool()
+    d = dict(np.load(K.FIXTURE))
+    sp = Spectrum.load_npz(K.FIXTURE, prefix="sp_")
+    d["t_ground"] = np.zeros(1)
+    d["alb"] = np.zeros(1)
+    extra = {k: (d["p"], d[k]) for k in ("clfr", "lwm", "iwm", "re", "ire")}
+    extra.update(szen=([1.013e5], d["szen"]), stoa=([1.013e5], d["stoa"]))
+    sp_path, base, _ = _column_files(tmp_path, "case6", d, sp, "sp_sw_ga7", False,
+                                     gases=set(int(x) for x in d["gases_present"]), digits=17, extra=extra)
+    nb = sp.n_band
+    surf = tmp_path / "case6.surf"
+    write_cdl(surf, "case6.surf", [("lon", 1), ("lat", 1), ("basis", 1), ("bands", nb)],
+              [("lon", ["lon"], [0.0], {}), ("lat", ["lat"], [0.0], {}), ("basis", ["basis"], [1.0], {}),
+               ("bands", ["bands"], np.arange(1, nb + 1), {}),
+               ("alb", ["bands", "basis", "lat", "lon"], np.reshape(np.load(K.FIXTURE)["alb"], (nb, 1, 1, 1)), {})],
+              digits=17)
+    lev = d["soot_plev"]
+    nl, nm = lev.size, d["soot_phf"].shape[1]
+    op = tmp_path / "case6.op_soot"
+    write_cdl(op, "case6.op_soot", [("lon", 1), ("lat", 1), ("plev", nl), ("mom", nm), ("band", nb)],
+              [("lon", ["lon"], [0.0], {}), ("lat", ["lat"], [0.0], {}), ("plev", ["plev"], lev, {"units": "Pa"}),
+               ("mom", ["mom"], np.arange(1, nm + 1), {}), ("band", ["band"], np.arange(1, nb + 1), {}),
+               ("abs", ["band", "plev", "lat", "lon"], np.reshape(d["soot_abs"], (nb, nl, 1, 1)), {}),
+               ("scat", ["band", "plev", "lat", "lon"], np.reshape(d["soot_scat"], (nb, nl, 1, 1)), {}),
+               ("phf", ["band", "mom", "plev", "lat", "lon"], np.reshape(d["soot_phf"], (nb, nm, nl, 1, 1)), {})],
+              digits=17)
+    if to_cdf:
+        for f in (surf, op):
+            out = f.with_name(f.name + ".cdf")
+            subprocess.run([tool, "--convert", str(f), str(out)], check=True)
+            out.replace(f)
+    cmd = [tool, "-s", str(sp_path), "-R", "1", str(nb), "-S", "+R", "-g", "4", "-c", "-r", "-a", "+A", "-C", "2",
+           "-K", "1", "-d", "5", "-i", "8", "-B", str(base)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _, hr = field(str(base) + ".hrts")
+    kgo = d["kgo_hrts"]
+    half_unit = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(kgo))) - 5)
+    err = np.abs(hr - kgo) / half_unit
+    assert err.max() <= 1.05, f"layer {err.argmax()}: {hr[err.argmax()]} vs {kgo[err.argmax()]}"
+    # without the overlay soot falls back to its parametrization with no
+    # mixing ratio: the heating rates lose the aerosol
+    r = subprocess.run([x for x in cmd if x != "+A"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _, hr2 = field(str(base) + ".hrts")
+    assert (np.abs(hr2 - kgo) / half_unit).max() > 1000.0
