@@ -36,7 +36,7 @@ extern "C" {
 #define SOCGPU_API
 #endif
 
-#define SOCGPU_ABI_VERSION 6
+#define SOCGPU_ABI_VERSION 7
 
 /* ---- status codes: rad_pcf.F90:391-405 ------------------------------- */
 #define SOCGPU_I_NORMAL             0
@@ -85,6 +85,23 @@ extern "C" {
 /* cloud representation, rad_pcf.F90:238-254 */
 #define SOCGPU_IP_CLOUD_HOMOGEN         1   /* one cloud type of all components */
 #define SOCGPU_IP_CLOUD_ICE_WATER       2
+#define SOCGPU_IP_CLOUD_CONV_STRAT      3   /* representations, rad_pcf.F90:238-260 */
+#define SOCGPU_IP_CLOUD_CSIW            4
+#define SOCGPU_IP_CLOUD_OFF             5
+#define SOCGPU_IP_CLOUD_COMBINE_HOMOGEN   6
+#define SOCGPU_IP_CLOUD_COMBINE_ICE_WATER 7
+#define SOCGPU_IP_CLOUD_SPLIT_HOMOGEN     8
+#define SOCGPU_IP_CLOUD_SPLIT_ICE_WATER   9
+/* condensate inhomogeneity and cloud entrapment, rad_pcf.F90:267-286 */
+#define SOCGPU_IP_MAX_ENTRAPMENT        1
+#define SOCGPU_IP_ZERO_ENTRAPMENT       2
+#define SOCGPU_IP_HOMOGENEOUS           0
+#define SOCGPU_IP_SCALING               1
+#define SOCGPU_IP_MCICA                 2
+/* droplet effective radius, rad_pcf.F90:356-360 */
+#define SOCGPU_IP_RE_EXTERNAL           2
+#define SOCGPU_IP_RE_LIU                3
+#define SOCGPU_IP_RE_CONSTANT           4
 /* cloud types, rad_pcf.F90:332-334 */
 #define SOCGPU_IP_CLOUD_TYPE_WATER      1
 #define SOCGPU_IP_CLOUD_TYPE_ICE        2
@@ -248,6 +265,11 @@ typedef struct socgpu_spectrum_desc {
     const double *aerosol_abs;          /* (nd_humidity, nd_aerosol_species, nd_band) [m2/kg] */
     const double *aerosol_scat;         /* (nd_humidity, nd_aerosol_species, nd_band) [m2/kg] */
     const double *aerosol_phf;          /* (nd_humidity, nd_phase_term, nd_aerosol_species, nd_band) */
+    /* ranges of validity [m] of the droplet and ice parameter sets (blocks 10
+       and 12: parm_min_dim, parm_max_dim), indexed like i_drop_parm and
+       i_ice_parm; NULL: no limits (set_cld_dim clamps sizes to them) */
+    const double *drop_parm_min_dim, *drop_parm_max_dim;
+    const double *ice_parm_min_dim, *ice_parm_max_dim;
 } socgpu_spectrum_desc;
 
 typedef int32_t socgpu_spectrum_handle;   /* > 0 when valid */
@@ -544,6 +566,7 @@ SOCGPU_API int socgpu_cloud_gen_device_noalloc(int nd_layer, int cloud_top, int 
 #define SOCGPU_IP_SOURCE_ILLUMINATE 1   /* socrates_runes.F90: the solar source */
 #define SOCGPU_IP_SOURCE_THERMAL    2   /* the thermal source */
 #define SOCGPU_RUNES_N_GAS         80   /* gas identifiers 1..79 of gas_list_pcf.F90 */
+#define SOCGPU_RUNES_N_AER         33   /* aerosol types 1..32 of rad_pcf.F90 */
 
 typedef struct socgpu_runes_args {
     int n_profile, n_layer;
@@ -582,6 +605,39 @@ typedef struct socgpu_runes_args {
     const double *aer_absorption, *aer_scattering, *aer_asymmetry;  /* (n_profile, n_layer, n_aer_mode, n_band) */
     const double *layer_heat_capacity;  /* (n_profile, n_layer) [J/(m2 K)] or NULL */
     int precision;                      /* SOCGPU_PRECISION_* */
+    /* classic aerosol species of the spectral file (set_aer,
+       socrates_set_aer.F90:190-290): the mixing ratios (n_profile, n_layer)
+       of each aerosol type, indexed by the type number of rad_pcf.F90
+       (1 water soluble, 2 dust-like, 3 oceanic, 4 soot, ... 32 two-bin dust
+       2); NULL where the runes flag l_<species> is off, and the species is
+       then radiatively inactive.  Moist species need mean_rel_humidity. */
+    const double *aerosol[SOCGPU_RUNES_N_AER];
+    const double *mean_rel_humidity;    /* (n_profile, n_layer) in [0, 1) */
+    /* clouds (set_control's cloud options, set_cld, set_cld_dim,
+       set_cld_mcica); 0 selects set_control's default */
+    int i_cloud_representation;         /* 0 (off), SOCGPU_IP_CLOUD_HOMOGEN, _ICE_WATER, _COMBINE_HOMOGEN,
+                                           _COMBINE_ICE_WATER */
+    int i_overlap;                      /* SOCGPU_IP_MAX_RAND (0, the default), SOCGPU_IP_RAND,
+                                           SOCGPU_IP_EXPONENTIAL_RAND (McICA only) */
+    int i_inhom;                        /* SOCGPU_IP_HOMOGENEOUS, SOCGPU_IP_SCALING, SOCGPU_IP_MCICA */
+    int i_cloud_entrapment;             /* SOCGPU_IP_ZERO_ENTRAPMENT (default: Hogan's solver) or
+                                           SOCGPU_IP_MAX_ENTRAPMENT (solver_mix_direct) */
+    int i_mcica_sampling;               /* SOCGPU_IP_MCICA_*_SAMPLING; -1 selects the default, optimal */
+    int i_st_water, i_st_ice;           /* droplet and ice types of the spectral file */
+    int i_drop_re;                      /* SOCGPU_IP_RE_EXTERNAL (default) or SOCGPU_IP_RE_CONSTANT */
+    int n_cloud_layer;                  /* 0: any layer may be cloudy; else only the lowest n_cloud_layer */
+    /* (n_profile, n_layer) grid-box fields; conv_* and *_conv_* combine with
+       the stratiform ones under the combine representations */
+    const double *cloud_frac, *conv_frac, *liq_frac, *ice_frac, *liq_conv_frac, *ice_conv_frac;
+    const double *liq_mmr, *ice_mmr, *liq_conv_mmr, *ice_conv_mmr;
+    const double *liq_dim, *ice_dim;    /* effective dimensions [m]; NULL: set_cld_dim's parametrizations */
+    const double *liq_rsd, *ice_rsd;    /* relative standard deviations of the condensate */
+    int has_liq_dim_constant, has_cloud_vertical_decorr, has_cloud_horizontal_rsd;
+    double liq_dim_constant;            /* [m], with SOCGPU_IP_RE_CONSTANT */
+    double cloud_vertical_decorr;       /* decorrelation pressure scale [Pa] of the McICA generator */
+    double cloud_horizontal_rsd;        /* condensate RSD where liq_rsd / ice_rsd are NULL */
+    const int *rand_seed;               /* (n_profile) McICA seeds; NULL: 10 + profile */
+    const char *mcica_data;             /* path of the McICA data file (with SOCGPU_IP_MCICA) */
 } socgpu_runes_args;
 
 /* StrDiag (socrates_def_diag.F90): NULL members are not filled. */
@@ -595,7 +651,10 @@ typedef struct socgpu_runes_diag {
 
 /* runes (socrates_runes.F90:47) on the GPU: maps the arguments, calls
  * socgpu_radiance_calc with host arrays and fills the diagnostics.  Clouds
- * are not taken through this interface (socgpu_radiance_calc runs McICA). */
+ * of one homogeneous type or of separate water and ice types (and their
+ * combinations with convective cloud) run in two regions with maximum-random
+ * or random overlap, or with McICA subcolumns; the representations with
+ * separate convective cloud (three regions) are refused. */
 SOCGPU_API int socgpu_runes(const socgpu_runes_args *args, socgpu_runes_diag *diag, char *msg, size_t msg_len);
 
 /* ---- multi-batch launches (extension) -----------------------------------

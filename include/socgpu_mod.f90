@@ -63,6 +63,7 @@ TYPE, BIND(C) :: socgpu_radout
 END TYPE
 
 INTEGER, PARAMETER :: socgpu_runes_n_gas = 80
+INTEGER, PARAMETER :: socgpu_runes_n_aer = 33
 
 TYPE, BIND(C) :: socgpu_runes_args
   INTEGER(c_int) :: n_profile, n_layer
@@ -86,6 +87,15 @@ TYPE, BIND(C) :: socgpu_runes_args
   TYPE(c_ptr)    :: aer_mix_ratio, aer_absorption, aer_scattering, aer_asymmetry
   TYPE(c_ptr)    :: layer_heat_capacity
   INTEGER(c_int) :: precision
+  TYPE(c_ptr)    :: aerosol(socgpu_runes_n_aer)
+  TYPE(c_ptr)    :: mean_rel_humidity
+  INTEGER(c_int) :: i_cloud_representation, i_overlap, i_inhom, i_cloud_entrapment, &
+                    i_mcica_sampling, i_st_water, i_st_ice, i_drop_re, n_cloud_layer
+  TYPE(c_ptr)    :: cloud_frac, conv_frac, liq_frac, ice_frac, liq_conv_frac, ice_conv_frac, &
+                    liq_mmr, ice_mmr, liq_conv_mmr, ice_conv_mmr, liq_dim, ice_dim, liq_rsd, ice_rsd
+  INTEGER(c_int) :: has_liq_dim_constant, has_cloud_vertical_decorr, has_cloud_horizontal_rsd
+  REAL(c_double) :: liq_dim_constant, cloud_vertical_decorr, cloud_horizontal_rsd
+  TYPE(c_ptr)    :: rand_seed, mcica_data
 END TYPE
 
 TYPE, BIND(C) :: socgpu_runes_diag

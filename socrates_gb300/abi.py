@@ -44,7 +44,7 @@ IP_MCICA_FULL_SAMPLING, IP_MCICA_SINGLE_SAMPLING, IP_MCICA_OPTIMAL_SAMPLING = 0,
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RNG_LCG, RNG_PHILOX = 0, 1
 NOALLOC_MAX_CLOUD_LAYERS = 1024   # SOCGPU_NOALLOC_MAX_CLOUD_LAYERS
-ABI_VERSION = 6
+ABI_VERSION = 7
 IP_SELF_CONTINUUM, IP_FRN_CONTINUUM = 1, 2
 
 _dp = C.POINTER(C.c_double)
@@ -81,6 +81,7 @@ class SpectrumDesc(C.Structure):
         ("nd_phase_term", C.c_int), ("type_aerosol", _ip), ("i_aerosol_parm", _ip), ("nhumidity", _ip),
         ("n_aerosol_phf_term", _ip), ("aerosol_humidities", _dp), ("aerosol_abs", _dp), ("aerosol_scat", _dp),
         ("aerosol_phf", _dp),
+        ("drop_parm_min_dim", _dp), ("drop_parm_max_dim", _dp), ("ice_parm_min_dim", _dp), ("ice_parm_max_dim", _dp),
     ]
 
 
@@ -116,6 +117,12 @@ class Atm(C.Structure):
 
 
 RUNES_N_GAS = 80
+RUNES_N_AER = 33
+IP_CLOUD_CONV_STRAT, IP_CLOUD_CSIW, IP_CLOUD_OFF = 3, 4, 5
+IP_CLOUD_COMBINE_HOMOGEN, IP_CLOUD_COMBINE_ICE_WATER, IP_CLOUD_SPLIT_HOMOGEN, IP_CLOUD_SPLIT_ICE_WATER = 6, 7, 8, 9
+IP_MAX_ENTRAPMENT, IP_ZERO_ENTRAPMENT = 1, 2
+IP_HOMOGENEOUS, IP_SCALING, IP_MCICA = 0, 1, 2
+IP_RE_EXTERNAL, IP_RE_LIU, IP_RE_CONSTANT = 2, 3, 4
 IP_SOURCE_ILLUMINATE, IP_SOURCE_THERMAL = 1, 2
 
 
@@ -137,6 +144,17 @@ class RunesArgs(C.Structure):
         ("l_aerosol_mode", C.c_int), ("n_aer_mode", C.c_int), ("aer_mix_ratio", _dp), ("aer_absorption", _dp),
         ("aer_scattering", _dp), ("aer_asymmetry", _dp),
         ("layer_heat_capacity", _dp), ("precision", C.c_int),
+        ("aerosol", _dp * RUNES_N_AER), ("mean_rel_humidity", _dp),
+        ("i_cloud_representation", C.c_int), ("i_overlap", C.c_int), ("i_inhom", C.c_int),
+        ("i_cloud_entrapment", C.c_int), ("i_mcica_sampling", C.c_int), ("i_st_water", C.c_int),
+        ("i_st_ice", C.c_int), ("i_drop_re", C.c_int), ("n_cloud_layer", C.c_int),
+        ("cloud_frac", _dp), ("conv_frac", _dp), ("liq_frac", _dp), ("ice_frac", _dp), ("liq_conv_frac", _dp),
+        ("ice_conv_frac", _dp), ("liq_mmr", _dp), ("ice_mmr", _dp), ("liq_conv_mmr", _dp), ("ice_conv_mmr", _dp),
+        ("liq_dim", _dp), ("ice_dim", _dp), ("liq_rsd", _dp), ("ice_rsd", _dp),
+        ("has_liq_dim_constant", C.c_int), ("has_cloud_vertical_decorr", C.c_int),
+        ("has_cloud_horizontal_rsd", C.c_int), ("liq_dim_constant", C.c_double),
+        ("cloud_vertical_decorr", C.c_double), ("cloud_horizontal_rsd", C.c_double),
+        ("rand_seed", _ip), ("mcica_data", C.c_char_p),
     ]
 
 

@@ -113,7 +113,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     # the column-file driver (socgpu_run), linked against the library
     tool_tmp = TOOL.with_suffix(".tmp")
     cmd = [nvcc(), *ARCH, "-std=c++17", "-O2", f"-I{INCLUDE}", f"-I{CSRC}", str(CSRC / TOOL_MAIN),
-           str(BUILD / "cdf_io.o"), "-o", str(tool_tmp), f"-L{PKG}", "-lsocgpu", "-cudart", "shared",
+           str(BUILD / "cdf_io.o"), str(BUILD / "mcica_setup.o"), "-o", str(tool_tmp), f"-L{PKG}", "-lsocgpu", "-cudart", "shared",
            "-Xlinker", "-rpath=$ORIGIN", "-Xlinker", "-rpath=/usr/local/cuda/lib64"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -411,6 +411,15 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   e.n_cloud_parameter = d->nd_cloud_parameter;
   e.drop_scheme.assign(s.n_drop_type, 0);
   e.ice_scheme.assign(s.n_ice_type, 0);
+  e.drop_min_dim.clear(); e.drop_max_dim.clear(); e.ice_min_dim.clear(); e.ice_max_dim.clear();
+  if (d->drop_parm_min_dim && d->drop_parm_max_dim) {
+    e.drop_min_dim.assign(d->drop_parm_min_dim, d->drop_parm_min_dim + s.n_drop_type);
+    e.drop_max_dim.assign(d->drop_parm_max_dim, d->drop_parm_max_dim + s.n_drop_type);
+  }
+  if (d->ice_parm_min_dim && d->ice_parm_max_dim) {
+    e.ice_min_dim.assign(d->ice_parm_min_dim, d->ice_parm_min_dim + s.n_ice_type);
+    e.ice_max_dim.assign(d->ice_parm_max_dim, d->ice_parm_max_dim + s.n_ice_type);
+  }
   for (int t = 0; t < s.n_drop_type; ++t)
     if ((!d->l_drop_type || d->l_drop_type[t]) && d->i_drop_parm) e.drop_scheme[t] = d->i_drop_parm[t];
   for (int t = 0; t < s.n_ice_type; ++t)

@@ -12,6 +12,7 @@
 // (column seed, subcolumn, layer): four deviates per cell, so a column's
 // masks depend only on its own seed and inputs.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
@@ -201,6 +202,20 @@ __global__ void cloud_gen_kernel(GenArgs a) {
 
 }  // namespace
 
+// Threads per CTA of the generator (one thread per column): as few as a
+// warp, so that the columns spread over every SM -- each thread's work is a
+// serial chain of FP64 arithmetic and random draws, and the FP64 units of an
+// SM are shared by its warps -- up to 128 once there are two CTAs per SM.
+static int gen_block(int ncol) {
+  int n_sm = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    n_sm = 1;
+  }
+  const int per = (ncol + 2 * n_sm - 1) / (2 * n_sm);
+  return std::min(128, std::max(32, (per + 31) / 32 * 32));
+}
+
 int launch_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2,
                      int n_subcol, int n1, int n2, int ipph, int ioverlap, const int *rand_seed,
                      const double *rlc_cf, const double *rlc_cw, const double *sigma_qcw,
@@ -220,7 +235,8 @@ int launch_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, i
   if (blocks < 1) blocks = 1;
   cloud_range_kernel<<<blocks, 256, 0, st>>>(a);
   count_launch();
-  cloud_gen_kernel<<<(ncol + 127) / 128, 128, 0, st>>>(a);
+  const int bs = gen_block(ncol);
+  cloud_gen_kernel<<<(ncol + bs - 1) / bs, bs, 0, st>>>(a);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -353,7 +369,8 @@ int launch_cloud_gen_noalloc(int nd_layer, int cloud_top, int n_layer, int nd_pr
   }
   cloud_layer_range_kernel<<<1, 256, 0, st>>>(scratch, ncl > 0 ? ncl : 0, cloud_top, n_layer, range);
   count_launch();
-  cloud_gen_kernel<<<(ncol + 127) / 128, 128, 0, st>>>(a);
+  const int bs = gen_block(ncol);
+  cloud_gen_kernel<<<(ncol + bs - 1) / bs, bs, 0, st>>>(a);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

@@ -698,8 +698,8 @@ struct FluxKernel {
       if (p.l_aerosol) classic_aerosol(p, col, i, b, kabs, kes, phf, fwd);
       if (p.l_aer_prsc) {
         // prescribed species: the sums of the prescribed-property kernel
-        const size_t plane = (size_t)(p.last_band - p.first_band + 1) * L * p.n_profile;
-        const size_t q0 = ((size_t)(b - (p.first_band - 1)) * L + i) * p.n_profile + col;
+        const size_t plane = (size_t)(p.last_band - p.first_band + 1) * L;
+        const size_t q0 = ((size_t)col * 4 * (p.last_band - p.first_band + 1) + (b - (p.first_band - 1))) * L + i;
         kabs = kabs + load_in<R>(p.aer_prsc + q0);
         kes = kes + load_in<R>(p.aer_prsc + plane + q0);
         phf = phf + load_in<R>(p.aer_prsc + 2 * plane + q0);

@@ -33,6 +33,7 @@ struct SpectrumEntry {
   std::vector<GPoint> gpoints_host;
   std::vector<int> type_absorb;       // gas identifier of each absorber (runes maps gases by name)
   std::vector<int> drop_scheme, ice_scheme;   // scheme of each droplet / ice type, 0 where undefined
+  std::vector<double> drop_min_dim, drop_max_dim, ice_min_dim, ice_max_dim;   // their ranges of validity [m]
   int n_cloud_parameter = 0;          // coefficients per parameter set in the spectrum
   std::vector<int> n_k_major;         // k-terms of each band's first absorber (McICA tables)
   // classic aerosol species (block 11): parametrization, humidities and

@@ -48,9 +48,14 @@
 
 #include "../../include/socgpu.h"
 #include "cdf_io.h"
+#include "mcica_setup.h"
 
+using socgpu::McicaData;
+using socgpu::McicaState;
 using socgpu::NcFile;
 using socgpu::NcVar;
+using socgpu::read_mcica_data;
+using socgpu::set_cld_mcica;
 
 namespace {
 
@@ -226,73 +231,6 @@ bool read_cloud_types(const std::string &path, std::map<int, CloudTypeInfo> &dro
 
 // The McICA data file (read_mcica_data, def_mcica.F90): keyword records of
 // the *DATA block, each followed by its values.
-struct McicaData {
-  int gen = 0, req_single = 0, req_optimal = 0, ipph = 0, n1 = 0, n2 = 0;
-  std::vector<int> reorder_single, reorder_optimal;
-  std::map<std::pair<int, int>, int> sw_subcol_k, lw_subcol_k;
-  std::vector<double> xcw;   // (n1, n2)
-};
-
-bool read_mcica_data(const std::string &path, McicaData &m, std::string &err) {
-  FILE *f = std::fopen(path.c_str(), "r");
-  if (!f) { err = "McICA data file " + path + " could not be opened"; return false; }
-  std::vector<std::string> lines;
-  char buf[4096];
-  while (std::fgets(buf, sizeof(buf), f)) {
-    std::string s(buf);
-    while (!s.empty() && (s.back() == '\n' || s.back() == '\r' || s.back() == ' ')) s.pop_back();
-    lines.push_back(s);
-  }
-  std::fclose(f);
-  size_t i = 0;
-  while (i < lines.size() && lines[i].rfind("*DATA", 0) != 0) ++i;
-  if (i == lines.size()) { err = "No *DATA block present in McICA data file"; return false; }
-  ++i;
-  // the next n values (integers or reals) from line i on
-  auto values = [&](size_t n, std::vector<double> &out) {
-    out.clear();
-    while (out.size() < n && i < lines.size()) {
-      const char *c = lines[i++].c_str();
-      char *end = nullptr;
-      for (double v = std::strtod(c, &end); end != c; v = std::strtod(c, &end)) {
-        out.push_back(v);
-        c = end;
-      }
-    }
-    return out.size() == n;
-  };
-  std::vector<double> v;
-  while (i < lines.size() && lines[i].rfind("*END", 0) != 0) {
-    std::string key = lines[i++];
-    key.erase(0, key.find_first_not_of(' '));
-    bool ok = true;
-    if (key == "tot_subcol_gen" || key == "n_subcol_gen") { ok = values(1, v); m.gen = (int)v[0]; }
-    else if (key == "subcol_need_single" || key == "n_subcol_req_single") { ok = values(1, v); m.req_single = (int)v[0]; }
-    else if (key == "subcol_need_optimal" || key == "n_subcol_req_optimal") { ok = values(1, v); m.req_optimal = (int)v[0]; }
-    else if (key == "ipph") { ok = values(1, v); m.ipph = (int)v[0]; }
-    else if (key == "n1") { ok = values(1, v); m.n1 = (int)v[0]; }
-    else if (key == "n2") { ok = values(1, v); m.n2 = (int)v[0]; }
-    else if (key == "lw_subcol_reorder_single" || key == "lw_subcol_reorder_optimal") {
-      const bool single = key == "lw_subcol_reorder_single";
-      ok = values((size_t)(single ? m.req_single : m.req_optimal), v);
-      (single ? m.reorder_single : m.reorder_optimal).assign(v.begin(), v.end());
-    } else if (key == "sw_subcol_k" || key == "lw_subcol_k") {
-      auto &tab = key == "sw_subcol_k" ? m.sw_subcol_k : m.lw_subcol_k;
-      for (;;) {
-        if (!values(3, v)) { ok = false; break; }
-        if ((int)v[0] == -99) break;
-        tab[{(int)v[0], (int)v[1]}] = (int)v[2];
-      }
-    } else if (key == "xcw") {
-      ok = values((size_t)m.n1 * (size_t)m.n2, v);
-      m.xcw = v;
-    }
-    if (!ok) { err = "Error reading data from McICA data file (" + key + ")"; return false; }
-  }
-  if (m.gen < 1 || m.xcw.empty()) { err = "McICA data file without subcolumn count or xcw"; return false; }
-  return true;
-}
-
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -514,10 +452,10 @@ int main(int argc, char **argv) {
 
   // clouds and McICA (input_cloud_cdf.f:340-790; l_run_cdf.F90:1281-1296 with
   // socrates_set_cld_mcica.F90:82-228)
-  int nc = 0, n_cloud_type = 1, n_subcol_req = 1, gen = 1, nd_k = 1;
+  int nc = 0, n_cloud_type = 1;
   std::vector<int> type_condensed, i_cloud_type, i_condensed_param, i_condensed_type;
-  std::vector<double> cmr, dim, w_cloud, frac_cloud, c_sub, frac_cloudy;
-  std::vector<int> n_subcol_cld, subcol_k, first_subcol_k, subcol_reorder;
+  std::vector<double> cmr, dim, w_cloud, frac_cloud;
+  McicaState mst;
   if (clouds) {
     std::map<int, CloudTypeInfo> drops, ices;
     if (!read_cloud_types(sp_file, drops, ices)) return die("cannot open " + sp_file);
@@ -566,57 +504,15 @@ int main(int argc, char **argv) {
     }
   }
   if (mcica) {
-    // McICA data beside the spectral file
+    // McICA data beside the spectral file, then set_cld_mcica
     const size_t slash = sp_file.find_last_of('/');
     const std::string mcica_path = (slash == std::string::npos ? std::string() : sp_file.substr(0, slash + 1)) +
                                    "mcica_data";
     McicaData md;
     if (!read_mcica_data(mcica_path, md, err)) return die(err);
-    gen = md.gen;
-    if (gen > SOCGPU_MAX_SUBCOL) return die("more subcolumns than the solver takes");
-    int nbands = 0;
-    std::vector<int> n_k_major(n_band > 0 ? n_band : 1, 0);
-    if (socgpu_spectrum_k_terms(h, n_band, &nbands, &nd_k, n_k_major.data()) != SOCGPU_I_NORMAL)
-      return die("spectrum lookup failed");
-    // sampling tables (socrates_set_cld_mcica.F90:106-160)
-    subcol_k.assign((size_t)n_band * nd_k, 1);
-    if (sampling == 0) {
-      n_subcol_req = gen;
-      std::fill(subcol_k.begin(), subcol_k.end(), gen);
-    } else if (sampling == 1) {
-      n_subcol_req = md.req_single;
-    } else {
-      n_subcol_req = md.req_optimal;
-      for (const auto &kv : isolir == SOCGPU_IP_SOLAR ? md.sw_subcol_k : md.lw_subcol_k) {
-        const int b = kv.first.first, k = kv.first.second;
-        if (b >= 1 && b <= n_band && k >= 1 && k <= nd_k) subcol_k[(size_t)(b - 1) + (size_t)n_band * (k - 1)] = kv.second;
-      }
-    }
-    if (n_subcol_req < 1) return die("the McICA data file gives no subcolumns for this sampling");
-    first_subcol_k.assign((size_t)n_band * (nd_k + 1), 0);
-    auto fs = [&](int b, int k) -> int & { return first_subcol_k[(size_t)b + (size_t)n_band * k]; };
-    fs(first - 1, 0) = 1;
-    for (int b = first - 1; b < last; ++b) {
-      const int n_k = n_k_major[b];
-      for (int k = 0; k < n_k; ++k) fs(b, k + 1) = fs(b, k) + subcol_k[(size_t)b + (size_t)n_band * k];
-      if (b < last - 1) fs(b + 1, 0) = fs(b, n_k);
-    }
-    subcol_reorder.assign(n_subcol_req, 0);
-    for (int l = 1; l <= n_subcol_req; ++l) {
-      int v2;
-      if (isolir == SOCGPU_IP_SOLAR) v2 = l % gen;
-      else if (sampling == 0) v2 = l;
-      else {
-        const std::vector<int> &src = sampling == 1 ? md.reorder_single : md.reorder_optimal;
-        if ((int)src.size() < n_subcol_req) return die("McICA data file: short subcolumn reorder list");
-        v2 = src[l - 1] % gen;
-      }
-      subcol_reorder[l - 1] = v2 == 0 ? gen : v2;
-    }
     // the generator's inputs: condensate variability weighted by the
     // grid-box condensate, decorrelation scales, seeds 10 + profile
-    std::vector<double> cond_rsd(np * nl), dp_cloud(np * nl, dp_corr_strat), dp_cond(np * nl, 0.5 * dp_corr_strat);
-    std::vector<double> zero(np * nl, 0.0);
+    std::vector<double> cond_rsd(np * nl);
     const double eps = std::numeric_limits<double>::epsilon();
     for (size_t q = 0; q < np * nl; ++q) {
       double num = 0.0, den = 0.0;
@@ -629,17 +525,11 @@ int main(int argc, char **argv) {
     }
     std::vector<int> seeds(np);
     for (size_t l = 0; l < np; ++l) seeds[l] = 10 + (int)l + 1;
-    c_sub.assign(np * nl * (size_t)gen, 0.0);
-    n_subcol_cld.assign(np, 0);
-    st = socgpu_cloud_gen((int)nl, 1, (int)nl, (int)np, 1, (int)np, gen, md.n1, md.n2, md.ipph, 2, seeds.data(),
-                          dp_cloud.data(), dp_cond.data(), cond_rsd.data(), w_cloud.data(), zero.data(), zero.data(),
-                          p.data(), md.xcw.data(), n_subcol_cld.data(), c_sub.data(), SOCGPU_RNG_LCG, msg, sizeof(msg));
+    st = set_cld_mcica(h, md, isolir, sampling, SOCGPU_IP_EXPONENTIAL, first, last, (int)np, (int)nl, 1,
+                       seeds.data(), dp_corr_strat, cond_rsd.data(), w_cloud.data(), p.data(), mst, msg,
+                       sizeof(msg));
     if (st != SOCGPU_I_NORMAL) return die(msg);
-    frac_cloudy.assign(np, 1.0);
-    if (sampling != 0)
-      for (size_t l = 0; l < np; ++l) frac_cloudy[l] = (double)n_subcol_cld[l] / (double)gen;
   }
-
   // classic aerosols (-a; l_run_cdf.F90:847-920 with input_aerosol_cdf.f):
   // for each species of the spectral file, with +A a file of optical
   // properties <base>.op_<suffix> overlays it (the species becomes
@@ -780,8 +670,8 @@ int main(int argc, char **argv) {
   d.nd_aerosol_mode = 1;
   d.nd_cloud_component = std::max(1, nc);
   d.nd_cloud_type = n_cloud_type;
-  d.nd_subcol_gen = mcica ? gen : 1;
-  d.nd_subcol_req = mcica ? n_subcol_req : 1;
+  d.nd_subcol_gen = mcica ? mst.gen : 1;
+  d.nd_subcol_req = mcica ? mst.n_subcol_req : 1;
   d.nd_aerosol_mr = std::max(1, n_aer);
   d.nd_profile_aerosol_prsc = p_prsc.empty() ? 1 : (int)np;
   d.nd_opt_level_aerosol_prsc = nd_lev_prsc;
@@ -834,16 +724,7 @@ int main(int argc, char **argv) {
     cld.w_cloud = w_cloud.data();
     cld.frac_cloud = frac_cloud.data();
   }
-  if (mcica) {
-    cld.n_subcol_gen = gen;
-    cld.n_subcol_req = n_subcol_req;
-    cld.c_sub = c_sub.data();
-    cld.frac_cloudy = frac_cloudy.data();
-    cld.n_subcol_cld = n_subcol_cld.data();
-    cld.subcol_k = subcol_k.data();
-    cld.first_subcol_k = first_subcol_k.data();
-    cld.subcol_reorder = subcol_reorder.data();
-  }
+  if (mcica) mst.attach(cld);
   const auto t0 = std::chrono::steady_clock::now();
   st = socgpu_radiance_calc(&c, &d, h, &atm, &cld, &aer, &bd, &out, msg, sizeof(msg));
   const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -9,12 +9,15 @@
 // (socrates_set_bound.F90:138-640) with the surface Planck flux of
 // diff_planck_source_mod.F90:123-190, and set_diag's diagnostics
 // (socrates_set_diag.F90:140-220).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <vector>
 
 #include "host_internal.h"
+#include "mcica_setup.h"
 
 namespace socgpu {
 namespace {
@@ -175,15 +178,327 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
         flux_ground[l + NP * b] = fg;
       }
   }
+  // clouds (socrates_set_control.F90:291-370, socrates_set_cld.F90,
+  // socrates_set_cld_dim.F90, socrates_set_cld_mcica.F90)
+  int rep = a->i_cloud_representation ? a->i_cloud_representation : SOCGPU_IP_CLOUD_OFF;
+  if (rep == SOCGPU_IP_CLOUD_CONV_STRAT || rep == SOCGPU_IP_CLOUD_CSIW || rep == SOCGPU_IP_CLOUD_SPLIT_HOMOGEN ||
+      rep == SOCGPU_IP_CLOUD_SPLIT_ICE_WATER) {
+    set_msg(msg, msg_len, "cloud representation %d (separate convective cloud: three regions) is not built", rep);
+    return SOCGPU_I_ERR_RANGE;
+  }
+  if (rep != SOCGPU_IP_CLOUD_OFF && rep != SOCGPU_IP_CLOUD_HOMOGEN && rep != SOCGPU_IP_CLOUD_ICE_WATER &&
+      rep != SOCGPU_IP_CLOUD_COMBINE_HOMOGEN && rep != SOCGPU_IP_CLOUD_COMBINE_ICE_WATER) {
+    set_msg(msg, msg_len, "cloud representation %d unrecognised", rep);
+    return SOCGPU_I_ERR_FATAL;
+  }
+  const bool clouds = rep != SOCGPU_IP_CLOUD_OFF;
+  const bool mcica = clouds && a->i_inhom == SOCGPU_IP_MCICA;
+  const bool homogen = rep == SOCGPU_IP_CLOUD_HOMOGEN || rep == SOCGPU_IP_CLOUD_COMBINE_HOMOGEN;
+  const bool combine = rep == SOCGPU_IP_CLOUD_COMBINE_HOMOGEN || rep == SOCGPU_IP_CLOUD_COMBINE_ICE_WATER;
+  const int scatter = a->i_scatter_method ? a->i_scatter_method : SOCGPU_IP_SCATTER_FULL;
+  int i_cloud = SOCGPU_IP_CLOUD_CLEAR, solver = scatter == SOCGPU_IP_SCATTER_FULL ? SOCGPU_IP_SOLVER_HOMOGEN_DIRECT
+                                                                               : SOCGPU_IP_SOLVER_NO_SCAT;
+  if (clouds && !mcica) {
+    if (a->i_inhom != SOCGPU_IP_HOMOGENEOUS && a->i_inhom != SOCGPU_IP_SCALING) {
+      set_msg(msg, msg_len, "condensate inhomogeneity %d is not built for cloud regions", a->i_inhom);
+      return SOCGPU_I_ERR_RANGE;
+    }
+    if (a->i_overlap == SOCGPU_IP_EXPONENTIAL_RAND) {
+      set_msg(msg, msg_len, "exponential-random overlap of cloud regions (ip_cloud_part_corr) is not built");
+      return SOCGPU_I_ERR_RANGE;
+    }
+    if (scatter != SOCGPU_IP_SCATTER_FULL) {
+      set_msg(msg, msg_len, "cloud regions need the full scattering treatment");
+      return SOCGPU_I_ERR_RANGE;
+    }
+    i_cloud = a->i_overlap == SOCGPU_IP_MAX_RAND ? SOCGPU_IP_CLOUD_MIX_MAX : SOCGPU_IP_CLOUD_MIX_RANDOM;
+    solver = a->i_cloud_entrapment == SOCGPU_IP_MAX_ENTRAPMENT ? SOCGPU_IP_SOLVER_MIX_DIRECT
+                                                                : SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN;
+  } else if (mcica) {
+    i_cloud = SOCGPU_IP_CLOUD_MCICA;
+  }
+  const int ict = (clouds && a->n_cloud_layer > 0) ? nl + 1 - std::min(a->n_cloud_layer, nl) : 1;
+  const size_t ncl = (size_t)(nl - ict + 1), NC = NP * ncl;
+  const int nct = homogen ? 1 : 2;
+  std::vector<double> cmr, cdim, w_cloud, frac_cloud, c_cloud, c_ratio, rsd_w;
+  std::vector<int> type_condensed, i_cloud_type, i_condensed_param, i_condensed_type;
+  McicaState mst;
+  if (clouds) {
+    const double eps = std::numeric_limits<double>::epsilon(), min_cloud_fraction = 0.001;
+    // a (n_profile, n_layer) argument on the cloudy layers, floored at zero
+    auto cfield = [&](const double *src, std::vector<double> &dst, bool floor0) {
+      dst.assign(NC, 0.0);
+      for (size_t k = 0; k < ncl; ++k)
+        for (int l = 0; l < np; ++l) {
+          const double v = src[l + (size_t)np * lay(ict - 1 + (int)k)];
+          dst[l + NP * k] = floor0 ? std::max(v, 0.0) : v;
+        }
+    };
+    // components: stratiform water (droplet type i_st_water) and ice
+    struct Comp { int phase, type; };
+    const Comp comps[2] = {{SOCGPU_IP_PHASE_WATER, a->i_st_water}, {SOCGPU_IP_PHASE_ICE, a->i_st_ice}};
+    const int nc = 2;
+    cmr.assign(NC * nc, 0.0);
+    cdim.assign(NC * nc, 0.0);
+    rsd_w.assign(NC * nc, 0.0);
+    c_cloud.assign(NC, 0.0);
+    c_ratio.assign(NC, 0.0);
+    std::vector<double> tmp, rsd;
+    for (int k = 0; k < nc; ++k) {
+      const bool water = comps[k].phase == SOCGPU_IP_PHASE_WATER;
+      const int ty = comps[k].type;
+      const std::vector<int> &schemes = water ? e->drop_scheme : e->ice_scheme;
+      if (ty <= 0) {
+        set_msg(msg, msg_len, water ? "Prescribed liquid cloud not yet implemented." : "Prescribed ice cloud not yet implemented.");
+        return SOCGPU_I_ERR_FATAL;
+      }
+      if (ty > (int)schemes.size() || schemes[ty - 1] == 0) {
+        set_msg(msg, msg_len, water ? "Liquid cloud type not in spectral file." : "Ice cloud type not in spectral file.");
+        return SOCGPU_I_ERR_FATAL;
+      }
+      type_condensed.push_back(comps[k].phase);
+      i_condensed_param.push_back(schemes[ty - 1]);
+      i_condensed_type.push_back(ty);
+      i_cloud_type.push_back(homogen ? 1 : (water ? 1 : 2));
+      const double *mmr = water ? a->liq_mmr : a->ice_mmr, *conv = water ? a->liq_conv_mmr : a->ice_conv_mmr;
+      if (!mmr) { set_msg(msg, msg_len, water ? "Liquid MMR not provided." : "Ice MMR not provided."); return SOCGPU_I_ERR_FATAL; }
+      cfield(mmr, tmp, true);
+      std::copy(tmp.begin(), tmp.end(), cmr.begin() + NC * k);
+      if (combine && conv) {
+        cfield(conv, tmp, true);
+        for (size_t q = 0; q < NC; ++q) { cmr[q + NC * k] += tmp[q]; c_ratio[q] += tmp[q]; }
+      }
+      const double *rsd_src = water ? a->liq_rsd : a->ice_rsd;
+      if (rsd_src) cfield(rsd_src, rsd, true);
+      else rsd.assign(NC, a->has_cloud_horizontal_rsd ? a->cloud_horizontal_rsd : 0.0);
+      for (size_t q = 0; q < NC; ++q) {
+        if (a->i_inhom == SOCGPU_IP_SCALING) cmr[q + NC * k] /= (1.0 + rsd[q] * rsd[q]);
+        rsd_w[q + NC * k] = rsd[q];
+      }
+    }
+    // fractions (socrates_set_cld.F90:475-565)
+    frac_cloud.assign(NC * nct, 0.0);
+    if (homogen) {
+      if (!a->cloud_frac) { set_msg(msg, msg_len, "Cloud fraction not provided."); return SOCGPU_I_ERR_FATAL; }
+      cfield(a->cloud_frac, tmp, true);
+      std::copy(tmp.begin(), tmp.end(), frac_cloud.begin());
+      if (combine && a->conv_frac) {
+        cfield(a->conv_frac, c_cloud, true);
+        for (size_t q = 0; q < NC; ++q) frac_cloud[q] += c_cloud[q];
+      }
+    } else {
+      // split a mixed-phase fraction between ice and liquid by the ratio of
+      // their in-cloud mixing ratios
+      auto split = [&](std::vector<double> &fl, std::vector<double> &fi, const std::vector<double> &f, int tw,
+                       int ti) {
+        for (size_t q = 0; q < NC; ++q) {
+          if (fl[q] + fi[q] > eps) {
+            const double mix = fl[q] + fi[q] - f[q];
+            if (mix > eps && fl[q] > eps && fi[q] > eps) {
+              double lm = 0.0, im = 0.0;
+              for (int k = 0; k < nc; ++k) {
+                if (i_cloud_type[k] == tw) lm += cmr[q + NC * k] / fl[q];
+                else if (i_cloud_type[k] == ti) im += cmr[q + NC * k] / fi[q];
+              }
+              if (lm + im > eps) {
+                fl[q] = std::max(fl[q] - mix * im / (lm + im), 0.0);
+                fi[q] = std::max(fi[q] - mix * lm / (lm + im), 0.0);
+              }
+            }
+            const double s2 = fl[q] + fi[q];
+            const double nl_ = f[q] * fl[q] / s2, ni_ = f[q] * fi[q] / s2;
+            fl[q] = nl_;
+            fi[q] = ni_;
+          } else {
+            fl[q] = 0.0;
+            fi[q] = 0.0;
+          }
+        }
+      };
+      std::vector<double> fl, fi, f;
+      if (a->liq_frac && a->ice_frac && a->cloud_frac) {
+        cfield(a->liq_frac, fl, true); cfield(a->ice_frac, fi, true); cfield(a->cloud_frac, f, true);
+        split(fl, fi, f, 1, 2);
+      } else if (a->liq_frac && a->ice_frac) {
+        cfield(a->liq_frac, fl, true); cfield(a->ice_frac, fi, true);
+      } else {
+        set_msg(msg, msg_len, "Liquid and ice cloud fractions not provided.");
+        return SOCGPU_I_ERR_FATAL;
+      }
+      std::copy(fl.begin(), fl.end(), frac_cloud.begin());
+      std::copy(fi.begin(), fi.end(), frac_cloud.begin() + NC);
+      if (combine && a->liq_conv_frac && a->ice_conv_frac) {
+        std::vector<double> cl, ci, cf;
+        cfield(a->liq_conv_frac, cl, true); cfield(a->ice_conv_frac, ci, true);
+        if (a->conv_frac) {
+          cfield(a->conv_frac, cf, true);
+          // the convective split keeps its fractions where both are zero
+          for (size_t q = 0; q < NC; ++q) {
+            if (cl[q] + ci[q] > eps) {
+              const double mix = cl[q] + ci[q] - cf[q];
+              if (mix > eps && cl[q] > eps && ci[q] > eps) {
+                double lm = 0.0, im = 0.0;
+                for (int k = 0; k < nc; ++k) {
+                  if (i_cloud_type[k] == 1) lm += cmr[q + NC * k] / cl[q];
+                  else if (i_cloud_type[k] == 2) im += cmr[q + NC * k] / ci[q];
+                }
+                if (lm + im > eps) {
+                  cl[q] = std::max(cl[q] - mix * im / (lm + im), 0.0);
+                  ci[q] = std::max(ci[q] - mix * lm / (lm + im), 0.0);
+                }
+              }
+              // in sequence, as socrates_set_cld.F90:548-551 updates them
+              cl[q] = cf[q] * cl[q] / (cl[q] + ci[q]);
+              ci[q] = cf[q] * ci[q] / (cl[q] + ci[q]);
+            }
+          }
+        }
+        for (size_t q = 0; q < NC; ++q) {
+          frac_cloud[q] += cl[q];
+          frac_cloud[q + NC] += ci[q];
+          c_cloud[q] = cl[q] + ci[q];
+        }
+      }
+    }
+    std::vector<double> cond_total;
+    if (combine) {
+      cond_total.assign(NC, 0.0);
+      for (size_t q = 0; q < NC; ++q) {
+        c_ratio[q] = c_ratio[q] / std::max(c_cloud[q], eps);
+        for (int k = 0; k < nc; ++k) cond_total[q] += cmr[q + NC * k];
+      }
+    }
+    // in-cloud mixing ratios, then normalised fractions
+    for (int k = 0; k < nc; ++k)
+      for (size_t q = 0; q < NC; ++q) {
+        const double f = frac_cloud[q + NC * (i_cloud_type[k] - 1)];
+        cmr[q + NC * k] = f > eps ? cmr[q + NC * k] / f : 0.0;
+      }
+    w_cloud.assign(NC, 0.0);
+    for (size_t q = 0; q < NC; ++q) {
+      double w = 0.0;
+      for (int t2 = 0; t2 < nct; ++t2) w += frac_cloud[q + NC * t2];
+      if (w > min_cloud_fraction) {
+        for (int t2 = 0; t2 < nct; ++t2) frac_cloud[q + NC * t2] /= w;
+        if (combine) c_ratio[q] = c_ratio[q] * w / std::max(cond_total[q], eps);
+      } else {
+        w = 0.0;
+        for (int t2 = 0; t2 < nct; ++t2) frac_cloud[q + NC * t2] = 0.0;
+        if (combine) { c_cloud[q] = 0.0; c_ratio[q] = 0.0; }
+      }
+      if (w > 1.0 + min_cloud_fraction) { set_msg(msg, msg_len, "Cloud fraction greater than 1."); return SOCGPU_I_ERR_FATAL; }
+      w_cloud[q] = std::min(w, 1.0);
+    }
+    // effective dimensions (socrates_set_cld_dim.F90:155-230)
+    for (int k = 0; k < nc; ++k) {
+      const bool water = type_condensed[k] == SOCGPU_IP_PHASE_WATER;
+      double *dst = cdim.data() + NC * k;
+      if (water) {
+        const int re = a->i_drop_re ? a->i_drop_re : SOCGPU_IP_RE_EXTERNAL;
+        if (re == SOCGPU_IP_RE_EXTERNAL && a->liq_dim) {
+          cfield(a->liq_dim, tmp, false);
+          std::copy(tmp.begin(), tmp.end(), dst);
+        } else if (re == SOCGPU_IP_RE_CONSTANT && a->has_liq_dim_constant) {
+          std::fill(dst, dst + NC, a->liq_dim_constant);
+        } else if (re == SOCGPU_IP_RE_LIU) {
+          set_msg(msg, msg_len, "droplet radii from droplet numbers (ip_re_liu) are not mapped; give liq_dim");
+          return SOCGPU_I_ERR_RANGE;
+        } else {
+          std::fill(dst, dst + NC, 7.0e-6);
+        }
+      } else if (a->ice_dim) {
+        cfield(a->ice_dim, tmp, false);
+        std::copy(tmp.begin(), tmp.end(), dst);
+      } else {
+        // set_ice_dim: sizes from the layer temperature
+        const int scheme = i_condensed_param[k];
+        for (size_t kk = 0; kk < ncl; ++kk)
+          for (int l = 0; l < np; ++l) {
+            const double tk = t[l + NP * (ict - 1 + kk)];
+            double dge;
+            switch (scheme) {
+              case 6:    // ip_ice_adt
+                dst[l + NP * kk] = std::min(7.198755e-04, std::exp(5.522e-02 * (tk - 2.7965e+02)) / 9.702e+02);
+                break;
+              case 12: case 16:   // ip_ice_agg_de, ip_ice_agg_de_sun
+                dge = tk < 216.208 ? 7.5094588e-04 * std::exp(0.05 * (tk - 279.5)) + 5.0830326e-07
+                                   : 1.3505403e-04 * std::exp(0.05 * (tk - 279.5)) + 2.6517429e-05;
+                dst[l + NP * kk] = (3.0 / 2.0) * (3.0 / (2.0 * std::sqrt(3.0))) * std::min(1.24e-04, std::max(8.0e-06, dge));
+                break;
+              case 19:   // ip_ice_baran
+                dst[l + NP * kk] = 1.868e-6 * tk - 353.613e-6;
+                break;
+              case 20:   // ip_ice_pade_2_phf: from ice crystal numbers
+                set_msg(msg, msg_len, "ice sizes from crystal numbers (ip_ice_pade_2_phf) are not mapped; give ice_dim");
+                return SOCGPU_I_ERR_RANGE;
+              default:
+                dst[l + NP * kk] = 30.0e-6;
+            }
+          }
+      }
+      const std::vector<double> &lo = water ? e->drop_min_dim : e->ice_min_dim, &hi = water ? e->drop_max_dim : e->ice_max_dim;
+      const int ty = i_condensed_type[k];
+      if (ty <= (int)lo.size() && ty <= (int)hi.size())
+        for (size_t q = 0; q < NC; ++q) dst[q] = std::min(std::max(dst[q], lo[ty - 1]), hi[ty - 1]);
+    }
+    if (mcica) {
+      if (!a->mcica_data) { set_msg(msg, msg_len, "McICA needs the McICA data file (mcica_data)"); return SOCGPU_I_ERR_FATAL; }
+      McicaData md;
+      std::string err;
+      if (!read_mcica_data(a->mcica_data, md, err)) { set_msg(msg, msg_len, "%s", err.c_str()); return SOCGPU_I_ERR_IO; }
+      // the condensate RSD weighted by each component's grid-box condensate
+      std::vector<double> cond_rsd(NC, 0.0);
+      for (size_t q = 0; q < NC; ++q) {
+        double num = 0.0, den = 0.0;
+        for (int k = 0; k < nc; ++k) {
+          const double wgt = std::max(eps, cmr[q + NC * k] * frac_cloud[q + NC * (i_cloud_type[k] - 1)]);
+          num += rsd_w[q + NC * k] * wgt;
+          den += wgt;
+        }
+        cond_rsd[q] = num / den;
+      }
+      std::vector<int> seeds(NP);
+      for (int l = 0; l < np; ++l) seeds[l] = a->rand_seed ? a->rand_seed[l] : 10 + l + 1;
+      const int sampling = a->i_mcica_sampling >= 0 ? a->i_mcica_sampling : SOCGPU_IP_MCICA_OPTIMAL_SAMPLING;
+      const int st_m = set_cld_mcica(h, md, solar ? SOCGPU_IP_SOLAR : SOCGPU_IP_INFRA_RED, sampling, a->i_overlap, 1, nb,
+                                     np, nl, ict, seeds.data(), a->has_cloud_vertical_decorr ? a->cloud_vertical_decorr : 0.0,
+                                     cond_rsd.data(), w_cloud.data(), p.data(), mst, msg, msg_len,
+                                     combine ? c_cloud.data() : nullptr, combine ? c_ratio.data() : nullptr);
+      if (st_m != SOCGPU_I_NORMAL) return st_m;
+    }
+  }
+  // classic aerosol species (set_aer): every species an entry, active where
+  // its mixing ratios are given
+  const int n_aer_sp = (int)e->aer_parm.size();
+  std::vector<double> aer_mr, mrh;
+  std::vector<int> mr_index, mr_source;
+  bool classic = false;
+  for (int j = 0; j < n_aer_sp; ++j) {
+    const int ty = e->aer_type[j];
+    classic = classic || (ty > 0 && ty < SOCGPU_RUNES_N_AER && a->aerosol[ty]);
+  }
+  if (classic) {
+    aer_mr.assign(NP * nl * n_aer_sp, 0.0);
+    for (int j = 0; j < n_aer_sp; ++j) {
+      const int ty = e->aer_type[j];
+      const double *src = (ty > 0 && ty < SOCGPU_RUNES_N_AER) ? a->aerosol[ty] : nullptr;
+      mr_index.push_back(j + 1);
+      mr_source.push_back(src ? SOCGPU_IP_AERSRC_CLASSIC_RON : SOCGPU_IP_AERSRC_CLASSIC_RON + 10);
+      if (src)
+        for (int i = 0; i < nl; ++i)
+          for (int l = 0; l < np; ++l) aer_mr[l + NP * (i + (size_t)nl * j)] = src[l + (size_t)np * lay(i)];
+    }
+    if (a->mean_rel_humidity) layer_field(a->mean_rel_humidity, mrh);
+  }
   // control (set_control's defaults for the two-stream path)
   socgpu_control c{};
   c.isolir = solar ? SOCGPU_IP_SOLAR : SOCGPU_IP_INFRA_RED;
   c.i_angular_integration = SOCGPU_IP_TWO_STREAM;
   c.i_2stream = solar ? SOCGPU_IP_PIFM80 : SOCGPU_IP_ELSASSER;
-  c.i_scatter_method = a->i_scatter_method ? a->i_scatter_method : SOCGPU_IP_SCATTER_FULL;
-  c.i_solver = c.i_scatter_method == SOCGPU_IP_SCATTER_FULL ? SOCGPU_IP_SOLVER_HOMOGEN_DIRECT : SOCGPU_IP_SOLVER_NO_SCAT;
-  c.i_cloud = SOCGPU_IP_CLOUD_CLEAR;
-  c.i_cloud_representation = 0;
+  c.i_scatter_method = scatter;
+  c.i_solver = solver;
+  c.i_cloud = i_cloud;
+  c.i_cloud_representation = clouds ? (homogen ? SOCGPU_IP_CLOUD_HOMOGEN : SOCGPU_IP_CLOUD_ICE_WATER) : 0;
   c.i_gas_overlap = a->i_gas_overlap ? a->i_gas_overlap : SOCGPU_IP_OVERLAP_K_EQV_SCL;
   c.i_direct_tau = SOCGPU_IP_DIRECT_DELTA_SCALING;
   c.l_rescale = 1;
@@ -195,6 +510,7 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
   c.l_mixing_ratio = a->l_mixing_ratio;
   c.l_grey_single = c.i_scatter_method != SOCGPU_IP_SCATTER_FULL;
   c.l_aerosol_mode = a->l_aerosol_mode && a->n_aer_mode > 0;
+  c.l_aerosol = classic;
   c.l_flux_div = 0;
   c.first_band = 1;
   c.last_band = nb;
@@ -202,8 +518,14 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
   socgpu_dimen dm{};
   dm.nd_profile = (int)NP;
   dm.nd_layer = nl;
-  dm.id_cloud_top = 1;
+  dm.id_cloud_top = ict;
   dm.nd_aerosol_mode = std::max(1, a->n_aer_mode);
+  dm.nd_cloud_component = 2;
+  dm.nd_cloud_type = nct;
+  dm.nd_subcol_gen = mcica ? mst.gen : 1;
+  dm.nd_subcol_req = mcica ? mst.n_subcol_req : 1;
+  dm.nd_aerosol_mr = std::max(1, n_aer_sp);
+  dm.nd_profile_aerosol_prsc = dm.nd_opt_level_aerosol_prsc = dm.nd_phf_term_aerosol_prsc = 1;
   socgpu_atm atm{};
   atm.n_profile = np;
   atm.n_layer = nl;
@@ -246,14 +568,35 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
     aer.mode_mix_ratio = amr.data(); aer.mode_absorption = aab.data();
     aer.mode_scattering = asc.data(); aer.mode_asymmetry = aas.data();
   }
+  if (classic) {
+    aer.n_aerosol_mr = n_aer_sp;
+    aer.mix_ratio = aer_mr.data();
+    aer.mr_type_index = mr_index.data();
+    aer.mr_source = mr_source.data();
+    aer.mean_rel_humidity = mrh.empty() ? nullptr : mrh.data();
+  }
+  socgpu_cld cld{};
+  if (clouds) {
+    cld.n_condensed = (int)type_condensed.size();
+    cld.type_condensed = type_condensed.data();
+    cld.i_cloud_type = i_cloud_type.data();
+    cld.i_condensed_param = i_condensed_param.data();
+    cld.i_condensed_type = i_condensed_type.data();
+    cld.condensed_mix_ratio = cmr.data();
+    cld.condensed_dim_char = cdim.data();
+    cld.n_cloud_type = nct;
+    cld.w_cloud = w_cloud.data();
+    cld.frac_cloud = frac_cloud.data();
+    if (mcica) mst.attach(cld);
+  }
   std::vector<double> fu(NP * (nl + 1)), fd(NP * (nl + 1)), fdir(NP * (nl + 1)), hr(NP * nl);
   socgpu_radout out{};
   out.flux_up = fu.data(); out.flux_down = fd.data();
   out.flux_direct = solar ? fdir.data() : nullptr;
   out.heating_rate = hr.data();
   if (np == 0) return SOCGPU_I_NORMAL;
-  int st = socgpu_radiance_calc(&c, &dm, h, &atm, nullptr, c.l_aerosol_mode ? &aer : nullptr, &bd, &out, msg,
-                                msg_len);
+  int st = socgpu_radiance_calc(&c, &dm, h, &atm, clouds ? &cld : nullptr,
+                                (c.l_aerosol_mode || c.l_aerosol) ? &aer : nullptr, &bd, &out, msg, msg_len);
   if (st != SOCGPU_I_NORMAL) return st;
   // diagnostics (set_diag): levels and layers back in the caller's order
   for (int i = 0; i <= nl; ++i)

@@ -205,7 +205,7 @@ struct FluxParams {
   int prsc_count[kMaxAerMr];        // active entries that name it
   int prsc_nlev[kMaxAerMr];         // its levels
   const double *prsc_p, *prsc_abs, *prsc_scat, *prsc_phf;
-  // [4][last_band - first_band + 1][n_layer][n_profile]: absorption,
+  // [n_profile][4][last_band - first_band + 1][n_layer]: absorption,
   // scattering, scattering x asymmetry, scattering x forward moment
   const double *aer_prsc;
   // outputs

@@ -175,6 +175,8 @@ struct SpectralFile {
       d.drop_parm_list = drop_parm.data();
       d.i_drop_parm = drop_ids.data();
       d.l_drop_type = drop_on.data();
+      d.drop_parm_min_dim = drop_lo.data();
+      d.drop_parm_max_dim = drop_hi.data();
     }
     if (!ice_ids.empty()) {
       d.nd_cloud_parameter = ncp;
@@ -182,6 +184,8 @@ struct SpectralFile {
       d.ice_parm_list = ice_parm.data();
       d.i_ice_parm = ice_ids.data();
       d.l_ice_type = ice_on.data();
+      d.ice_parm_min_dim = ice_lo.data();
+      d.ice_parm_max_dim = ice_hi.data();
     }
     if (!k_lookup.empty()) {
       d.n_pre = n_pre; d.n_tmp = n_tmp;

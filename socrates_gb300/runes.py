@@ -10,7 +10,8 @@ src/interface_core/socrates_runes.F90:47-200), over socgpu_runes.
 Arrays have the profile index first, as the reference's (n_profile, n_layer)
 arguments.  The diagnostics come back as a dict of the StrDiag members
 (heating_rate, flux_up, flux_down, flux_direct, flux_*_surf, flux_*_toa).
-Clear sky: clouds are run through radiance.radiance_calc (McICA)."""
+Clouds (set_cld, set_cld_dim, set_cld_mcica) and classic aerosol species
+(set_aer) take the reference's argument names too."""
 from __future__ import annotations
 
 import ctypes as C
@@ -31,6 +32,17 @@ GAS_NAMES = ["h2o", "co2", "o3", "n2o", "co", "ch4", "o2", "no", "so2", "no2", "
              "yosos", "ch3cho", "ch3ooh", "ch3coch3", "ch3cocho", "chocho", "c2h5cho", "hoch2cho", "c2h5coch3",
              "mvk", "macr", "pan", "ch3ono2"]
 GAS_ID = {name: i + 1 for i, name in enumerate(GAS_NAMES) if name}
+
+# runes' classic aerosol arguments by aerosol type (rad_pcf.F90:
+# ip_water_soluble = 1 ... ip_twobindust_2 = 32; 29 is murk)
+AEROSOL_NAMES = ["water_soluble", "dust_like", "oceanic", "soot", "ash", "sulphuric", "ammonium_sulphate", None,
+                 "saharan_dust", "accum_sulphate", "aitken_sulphate", "fresh_soot", "aged_soot", "sodium_chloride",
+                 "seasalt_film", "seasalt_jet", "dust_div1", "dust_div2", "dust_div3", "dust_div4", "dust_div5",
+                 "dust_div6", "biomass_1", "biomass_2", "biogenic", "ocff_fresh", "ocff_aged", "delta", "murk",
+                 "nitrate", "twobindust_1", "twobindust_2"]
+AEROSOL_ID = {name: i + 1 for i, name in enumerate(AEROSOL_NAMES) if name}
+CLOUD_ARRAYS = ("cloud_frac", "conv_frac", "liq_frac", "ice_frac", "liq_conv_frac", "ice_conv_frac", "liq_mmr",
+                "ice_mmr", "liq_conv_mmr", "ice_conv_mmr", "liq_dim", "ice_dim", "liq_rsd", "ice_rsd")
 
 
 def set_spectrum(spectrum_name: str, spectral_file=None, spectrum: Spectrum | None = None, wenyi_file=None,
@@ -60,10 +72,17 @@ def runes(n_profile: int, n_layer: int, spectrum_name: str, i_source: int, *, p_
           albedo_diff_tile=None, albedo_dir_tile=None, i_scatter_method=0, i_gas_overlap=0, l_rayleigh=False,
           l_mixing_ratio=False, l_aerosol_mode=False, n_aer_mode=0, aer_mix_ratio=None, aer_absorption=None,
           aer_scattering=None, aer_asymmetry=None, layer_heat_capacity=None, l_invert=False,
-          precision=abi.PRECISION_FP64, **gases) -> dict:
+          precision=abi.PRECISION_FP64, mean_rel_humidity=None, i_cloud_representation=0, i_overlap=0,
+          i_inhom=0, i_cloud_entrapment=0, i_mcica_sampling=-1, i_st_water=0, i_st_ice=0, i_drop_re=0,
+          n_cloud_layer=0, liq_dim_constant=None, cloud_vertical_decorr=None, cloud_horizontal_rsd=None,
+          rand_seed=None, mcica_data=None, **kw) -> dict:
     """runes (socrates_runes.F90:47) through socgpu_runes.  Gases are passed
     by the reference's names: <gas> a profile (n_profile, n_layer),
-    <gas>_mix_ratio a well-mixed value, l_<gas>_well_mixed to prefer it."""
+    <gas>_mix_ratio a well-mixed value, l_<gas>_well_mixed to prefer it.
+    Classic aerosols by the names of set_aer (water_soluble, dust_like, ...
+    each a (n_profile, n_layer) mixing ratio; l_<name>=False drops one).
+    Clouds by the names of set_cld and set_cld_dim (cloud_frac, liq_mmr,
+    liq_dim, ...); mcica_data is the path of the McICA data file."""
     lib = load_library()
     keep = []
 
@@ -80,6 +99,32 @@ def runes(n_profile: int, n_layer: int, spectrum_name: str, i_source: int, *, p_
     a.spectrum_name = name
     a.p_layer, a.t_layer, a.mass, a.density = dp(p_layer), dp(t_layer), dp(mass), dp(density)
     a.p_level, a.t_level = dp(p_level), dp(t_level)
+    aer_flags = {k[2:]: bool(v) for k, v in kw.items() if k.startswith("l_") and k[2:] in AEROSOL_ID}
+    gases = {}
+    for key, val in kw.items():
+        if key.startswith("l_") and key[2:] in AEROSOL_ID:
+            continue
+        if key in AEROSOL_ID:
+            if aer_flags.get(key, True) and val is not None:
+                a.aerosol[AEROSOL_ID[key]] = dp(val)
+        elif key in CLOUD_ARRAYS:
+            setattr(a, key, dp(val))
+        else:
+            gases[key] = val
+    a.mean_rel_humidity = dp(mean_rel_humidity)
+    a.i_cloud_representation, a.i_overlap, a.i_inhom = int(i_cloud_representation), int(i_overlap), int(i_inhom)
+    a.i_cloud_entrapment, a.i_mcica_sampling = int(i_cloud_entrapment), int(i_mcica_sampling)
+    a.i_st_water, a.i_st_ice, a.i_drop_re, a.n_cloud_layer = int(i_st_water), int(i_st_ice), int(i_drop_re), \
+        int(n_cloud_layer)
+    for name, val in (("liq_dim_constant", liq_dim_constant), ("cloud_vertical_decorr", cloud_vertical_decorr),
+                      ("cloud_horizontal_rsd", cloud_horizontal_rsd)):
+        if val is not None:
+            setattr(a, name, float(val))
+            setattr(a, "has_" + name, 1)
+    if rand_seed is not None:
+        a.rand_seed = dp(np.asarray(rand_seed, dtype=np.int32), np.int32)
+    mcica_path = None if mcica_data is None else str(mcica_data).encode()
+    a.mcica_data = mcica_path
     for key, val in gases.items():
         if key.startswith("l_") and key.endswith("_well_mixed"):
             gid = GAS_ID.get(key[2:-len("_well_mixed")])

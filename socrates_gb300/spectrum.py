@@ -369,12 +369,16 @@ class Spectrum:
             d.drop_parm_list = dp(pad(self.drop_parm_list))
             d.i_drop_parm = ip(self.i_drop_parm)
             d.l_drop_type = ip((np.asarray(self.i_drop_parm) > 0).astype(np.int32))
+            if self.drop_parm_min_dim is not None and self.drop_parm_max_dim is not None:
+                d.drop_parm_min_dim, d.drop_parm_max_dim = dp(self.drop_parm_min_dim), dp(self.drop_parm_max_dim)
         if self.ice_parm_list is not None:
             d.nd_cloud_parameter = ncp
             d.nd_ice_type = self.ice_parm_list.shape[2]
             d.ice_parm_list = dp(pad(self.ice_parm_list))
             d.i_ice_parm = ip(self.i_ice_parm)
             d.l_ice_type = ip((np.asarray(self.i_ice_parm) > 0).astype(np.int32))
+            if self.ice_parm_min_dim is not None and self.ice_parm_max_dim is not None:
+                d.ice_parm_min_dim, d.ice_parm_max_dim = dp(self.ice_parm_min_dim), dp(self.ice_parm_max_dim)
         if self.aerosol_abs is not None:
             d.n_aerosol = d.nd_aerosol_species = int(self.aerosol_abs.shape[1])
             d.nd_humidity = int(self.aerosol_abs.shape[0])
