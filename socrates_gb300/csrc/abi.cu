@@ -868,6 +868,22 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
                  socgpu_radout *out, const double *weight_band_dev) {
   std::memset(&p, 0, sizeof(p));
   p.isolir = c->isolir; p.i_2stream = c->i_2stream; p.i_scatter_method = c->i_scatter_method;
+  {
+    // sum = A - omega (B g + C), diff = D (1 - omega), ksi_0 = K g / sec_0
+    // (two_coeff_basic.F90:99-160, solar_coefficient_basic.F90:171-182)
+    const float r3 = 1.7320508f;
+    float a = 2.0f, b = 1.5f, cc = 0.5f, d = 2.0f, k = 1.5f;          // ip_pifm80
+    switch (c->i_2stream) {
+      case SOCGPU_IP_EDDINGTON: a = 1.5f; b = 1.5f; cc = 0.0f; d = 2.0f; break;
+      case SOCGPU_IP_ELSASSER: a = 1.66f; b = 1.5f; cc = 0.0f; d = 1.66f; break;
+      case SOCGPU_IP_DISCRETE_ORD: a = r3; b = r3; cc = 0.0f; d = r3; k = r3; break;
+      case SOCGPU_IP_PIFM85: a = 2.0f; b = 1.5f; cc = 0.0f; d = 2.0f; break;
+      case SOCGPU_IP_2S_TEST: a = 1.5f; b = 1.5f; cc = 0.0f; d = 1.5f; break;
+      case SOCGPU_IP_HEMI_MEAN: a = 2.0f; b = 2.0f; cc = 0.0f; d = 2.0f; break;
+      default: break;
+    }
+    p.scheme_f[0] = a; p.scheme_f[1] = b; p.scheme_f[2] = cc; p.scheme_f[3] = d; p.scheme_f[4] = k;
+  }
   p.i_direct_tau = c->i_direct_tau; p.l_rescale = c->l_rescale; p.n_order_forward = c->n_order_forward;
   p.l_ir_source_quad = c->l_ir_source_quad; p.l_rayleigh = c->l_rayleigh; p.l_gas = c->l_gas;
   p.l_aerosol_mode = c->l_aerosol_mode && aer && aer->n_mode > 0; p.l_flux_div = c->l_flux_div;

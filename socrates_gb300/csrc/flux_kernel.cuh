@@ -356,15 +356,15 @@ struct FluxKernel {
         tau = (kgt + kgas) * dm; om = 0.0f; omc = 1.0f;
       }
       if (p.l_rescale) {
-        float of = om * fwd;
-        float den = 1.0f - of;
+        float den = fmaf(-om, fwd, 1.0f);
         tau = tau * den;
         float inv = 1.0f / den;
         om = om * (1.0f - fwd) * inv;
         omc = omc * inv;                            // 1 - omega' = (1-omega)/(1-omega f)
       }
+      const SchemeF sc{p.scheme_f[0], p.scheme_f[1], p.scheme_f[2], p.scheme_f[3], p.scheme_f[4]};
       CoefF c = NOSCAT ? fast_lw_mix(p.l_ir_source_quad, tau)
-                       : two_coeff_mix(SRC, p.i_2stream, p.l_ir_source_quad, asym, om, omc, tau, sec0);
+                       : two_coeff_mix(SRC, sc, p.l_ir_source_quad, asym, om, omc, tau, sec0);
       T = c.T; Rf = c.R; T0 = c.T0; c1 = c.c1; c2 = c.c2; omtr = c.omtr;
     }
   }
@@ -2068,14 +2068,27 @@ struct FluxKernel {
       return;
     }
 
-    // --- adding-method solve as a scan of composites ---------------------------
-    Comp<R> cc = comp_identity<R>();
+    // --- adding method (solver_homogen_direct.F90:94-131), eliminated from
+    // the top down: at each level F_dn = rho F_up + sig, and across layer j
+    // F_up(top) = a_j F_up(bottom) + b_j.  The chunks' states from above come
+    // from a prefix scan of their layer composites; the upward fluxes at the
+    // chunk bottoms from a suffix scan of the chunks' affine maps (a, b).
+    // the chunk's composite, stacked pairwise (a tree of depth log2 CH, so
+    // that the divisions of independent pairs overlap)
+    Comp<R> cc;
+    {
+      Comp<R> lv[CH];
 #pragma unroll
-    for (int j = 0; j < CH; ++j) {
-      Comp<R> lj; lj.R1 = Rf[j]; lj.R2 = Rf[j]; lj.Td = T[j]; lj.Tu = T[j]; lj.Su = c1[j]; lj.Sd = c2[j];
-      cc = (j == 0) ? lj : stack(cc, lj);
+      for (int j = 0; j < CH; ++j) {
+        lv[j].R1 = Rf[j]; lv[j].R2 = Rf[j]; lv[j].Td = T[j]; lv[j].Tu = T[j]; lv[j].Su = c1[j]; lv[j].Sd = c2[j];
+      }
+#pragma unroll
+      for (int w = 1; w < CH; w <<= 1)
+#pragma unroll
+        for (int j = 0; j + w < CH; j += 2 * w) lv[j] = stack(lv[j], lv[j + w]);
+      cc = lv[0];
     }
-    // above: inclusive prefix C_0 .. C_r
+    // above: inclusive prefix C_0 .. C_r, then the exclusive one
     Comp<R> pre = cc;
 #pragma unroll
     for (int d = 1; d < P; d <<= 1) {
@@ -2083,57 +2096,57 @@ struct FluxKernel {
       if (r >= d) pre = stack(y, pre);
     }
     Comp<R> ex = shfl_up_comp(pre, 1, P);
-    // state above this chunk: rho (reflection back down), sigma (downward flux source)
-    R rho, sigma;
-    if (r == 0) { rho = R(0); sigma = f_inc_down; }
-    else { rho = ex.R2; sigma = ex.Sd + ex.Td * f_inc_down; }
-    // below: inclusive suffix C_r .. C_{P-1}
-    Comp<R> suf = cc;
-#pragma unroll
-    for (int d = 1; d < P; d <<= 1) {
-      Comp<R> y = shfl_down_comp(suf, d, P);
-      if (r + d < P) suf = stack(suf, y);
-    }
-    Comp<R> bx = shfl_down_comp(suf, 1, P);
-    R alpha, S;     // albedo and upward source at the bottom of this chunk
-    if (r == P - 1) { alpha = alb_diff; S = src_ground; }
-    else {
-      R D = R(1) / (R(1) - bx.R2 * alb_diff);
-      alpha = bx.R1 + bx.Tu * alb_diff * D * bx.Td;
-      S = bx.Su + bx.Tu * D * (src_ground + alb_diff * bx.Sd);
-    }
-    // elimination inside the chunk (solver_homogen_direct.F90:94-110)
-    R (&beta)[CH] = T0;   // the direct transmission is no longer needed
-    R gam[CH];
-#pragma unroll
-    for (int j = CH - 1; j >= 0; --j) {
-      R bt = R(1) / (R(1) - alpha * Rf[j]);
-      R gm = alpha * T[j];
-      R h = S + alpha * c2[j];
-      alpha = Rf[j] + bt * gm * T[j];
-      S = c1[j] + bt * T[j] * h;
-      beta[j] = bt; gam[j] = gm; c1[j] = h;
-    }
-    // fluxes at the chunk top, then back-substitution (solver_homogen_direct.F90:112-128)
-    R fdn = (sigma + rho * S) / (R(1) - rho * alpha);
-    R fup = alpha * fdn + S;
-    if (r == 0) {
-      fdn = f_inc_down; fup = alpha * fdn + S;
-      if (active) { acc_up[LP] += w * fup; acc_dn[LP] += w * fdn; }
-    }
+    R rho, sig;            // the state at the top of this chunk
+    if (r == 0) { rho = R(0); sig = f_inc_down; }
+    else { rho = ex.R2; sig = ex.Sd + ex.Td * f_inc_down; }
+    // elimination through the chunk.  The arrays now hold, per layer,
+    // a (T), b (Rf) and the state at its top, rho (c1) and sig (c2);
+    // F_up(chunk top) = A F_up(chunk bottom) + B.  Padding layers (T = 1,
+    // R = 0, no sources) are the identity.
+    R A = R(1), B = R(0);
 #pragma unroll
     for (int j = 0; j < CH; ++j) {
+      const R q = R(1) / (R(1) - Rf[j] * rho);
+      const R a = T[j] * q;
+      const R b = (Rf[j] * sig + c1[j]) * q;
+      const R rho_n = Rf[j] + (T[j] * T[j] * rho) * q;     // T^2 rho formed beside the division
+      const R sig_n = c2[j] + a * (sig + rho * c1[j]);
+      T[j] = a; Rf[j] = b; c1[j] = rho; c2[j] = sig;
+      B = B + A * b; A = A * a;
+      rho = rho_n; sig = sig_n;
+    }
+    // the surface closes the last chunk: F_up = alb F_dn + src_ground with
+    // F_dn = rho F_up + sig; that chunk's map becomes the constant F_up(top)
+    R fu_surf = R(0);
+    if (r == P - 1) {
+      fu_surf = (alb_diff * sig + src_ground) / (R(1) - alb_diff * rho);
+      B = A * fu_surf + B; A = R(0);
+    }
+    // suffix scan of the affine maps: F_up at the top of every chunk
+#pragma unroll
+    for (int d = 1; d < P; d <<= 1) {
+      R yA = __shfl_down_sync(0xffffffffu, A, d, P), yB = __shfl_down_sync(0xffffffffu, B, d, P);
+      if (r + d < P) { B = A * yB + B; A = A * yA; }
+    }
+    R fu = __shfl_down_sync(0xffffffffu, B, 1, P);     // F_up at the bottom of this chunk
+    if (r == P - 1) fu = fu_surf;
+    R fd = rho * fu + sig;
+    // back-substitution from the chunk bottom up, accumulating the level
+    // below each layer and the layer's divergence
+#pragma unroll
+    for (int j = CH - 1; j >= 0; --j) {
       const int i = r * CH + j, s = j * P + r;
-      R fu = beta[j] * (c1[j] + gam[j] * fdn);
-      R fd = c2[j] + T[j] * fdn + Rf[j] * fu;
+      const R fu_top = T[j] * fu + Rf[j];
+      const R fd_top = c1[j] * fu_top + c2[j];
       if (i < L_acc) {
         acc_up[s] += w * fu;
         acc_dn[s] += w * fd;
-        if constexpr (kFP64) acc_div[s] += w * (fu - fup + fdn - fd);
-        else acc_div[s] += w * (om[j] * (fdn + fu) - ssum[j]);
+        if constexpr (kFP64) acc_div[s] += w * (fu - fu_top + fd_top - fd);
+        else acc_div[s] += w * (om[j] * (fd_top + fu) - ssum[j]);
       }
-      fup = fu; fdn = fd;
+      fu = fu_top; fd = fd_top;
     }
+    if (r == 0 && active) { acc_up[LP] += w * fu; acc_dn[LP] += w * fd; }
   }
 };
 
@@ -2141,7 +2154,7 @@ struct FluxKernel {
 // short chunks of the clear-sky kernels keep 4 CTAs of 256 threads (64
 // registers) per SM, which the shared memory of a 100-layer solar column
 // also allows; the McICA kernels would spill at 64 registers.
-constexpr int single_min_ctas(int ch, bool mcica) { return (ch <= 4 && !mcica) ? 4 : 1; }
+constexpr int single_min_ctas(int ch, bool mcica) { return (ch <= 4 && !mcica) ? 4 : (ch <= 13 && !mcica ? 2 : 1); }
 
 template <class R, bool MIX, int P, int CH, bool NOSCAT, bool MCICA, int SRC>
 __global__ void __launch_bounds__(256, single_min_ctas(CH, MCICA)) flux_kernel(const __grid_constant__ FluxParams p) {

@@ -142,6 +142,7 @@ struct SpectrumDev {
 struct FluxParams {
   // control
   int isolir, i_2stream, i_scatter_method, i_direct_tau;
+  float scheme_f[5];                 // the mixed kernels' constants of i_2stream (SchemeF: A, B, C, D, K)
   int l_rescale, n_order_forward, l_ir_source_quad, l_rayleigh, l_gas, l_aerosol_mode;
   int l_flux_div, first_band, last_band;
   int mcica;                         // cloud fields staged (McICA or cloud regions)

@@ -53,20 +53,6 @@ __device__ __forceinline__ void sum_diff_ref(int scheme, double om, double g, do
   }
 }
 
-// Same in FP32, taking 1-omega directly (no cancellation in diff).
-__device__ __forceinline__ void sum_diff_mix(int scheme, float om, float one_m_om, float g,
-                                             float &sum, float &diff) {
-  switch (scheme) {
-    case SOCGPU_IP_EDDINGTON: sum = 1.5f * (1.0f - om * g); diff = 2.0f * one_m_om; break;
-    case SOCGPU_IP_ELSASSER: sum = 1.66f - 1.5f * om * g; diff = 1.66f * one_m_om; break;
-    case SOCGPU_IP_DISCRETE_ORD: sum = 1.7320508f * (1.0f - om * g); diff = 1.7320508f * one_m_om; break;
-    case SOCGPU_IP_PIFM85: sum = 2.0f - 1.5f * om * g; diff = 2.0f * one_m_om; break;
-    case SOCGPU_IP_2S_TEST: sum = 1.5f - 1.5f * om * g; diff = 1.5f * one_m_om; break;
-    case SOCGPU_IP_HEMI_MEAN: sum = 2.0f * (1.0f - om * g); diff = 2.0f * one_m_om; break;
-    default: sum = 2.0f - 1.5f * om * g - 0.5f * om; diff = 2.0f * one_m_om; break;
-  }
-}
-
 // ---- full two-stream coefficients, reference form -------------------------
 __device__ __forceinline__ Coef two_coeff_ref(int isolir, int scheme, int l_quad,
                                               double g, double om, double tau, double sec0) {
@@ -126,14 +112,19 @@ __device__ __forceinline__ Coef fast_lw_ref(int l_quad, double tau) {
 }
 
 // ---- mixed-precision forms -------------------------------------------------
-// Small-argument helpers, from the Taylor series of exp (nested Horner form;
-// below x = 0.25 the truncation error is under 1e-10 relative).
-// 1 - exp(-x) given e = exp(-x).
+// Scheme constants of the mixed kernels (two_coeff_basic.F90:99-160,
+// solar_coefficient_basic.F90:171-182): sum = A - omega (B g + C),
+// diff = D (1 - omega), ksi_0 = K g / sec_0.  The host fills them once per
+// call (FluxParams::scheme_f), so the per-cell code has no switch.
+struct SchemeF { float A, B, C, D, K; };
+
+// 1 - exp(-x) given e = exp(-x): below x = 0.25 the Taylor series to x^6
+// (relative truncation error under 5e-8), above it 1 - e (which then loses
+// at most a factor 1/0.22 of FP32 rounding).  Branch-free.
 __device__ __forceinline__ float one_minus_exp(float x, float e) {
-  if (x < 0.25f)
-    return x * (1.0f - x * 0.5f * (1.0f - x * (1.0f / 3.0f) * (1.0f - x * 0.25f * (1.0f - x * 0.2f *
-           (1.0f - x * (1.0f / 6.0f) * (1.0f - x * (1.0f / 7.0f) * (1.0f - x * 0.125f)))))));
-  return 1.0f - e;
+  const float p = x * fmaf(x, fmaf(x, fmaf(x, fmaf(x, fmaf(x, -1.0f / 720.0f, 1.0f / 120.0f), -1.0f / 24.0f),
+                                             1.0f / 6.0f), -0.5f), 1.0f);
+  return x < 0.25f ? p : 1.0f - e;
 }
 // phi(x) = x - (1 - exp(-x)) = x^2/2 - x^3/6 + ...
 __device__ __forceinline__ float phi_exp(float x, float em1) {
@@ -154,92 +145,98 @@ __device__ __forceinline__ float psi_exp(float x, float e) {
 // coefficients are interpolated across the removable singularity.
 constexpr float kSolarSingularTol = 3.0e-3f;
 
-struct SwEval { float T, R, c1, c2, omt, omtr; };
-
-// Reflection, transmission and solar source coefficients for given
-// (sum, diff, lambda); the expressions of trans_source_coeff.F90:144-263
-// and solar_coefficient_basic.F90:124-219 regrouped around 1-e, 1-gamma,
-// 1-T and 1-T0 so that none cancels.
-__device__ __forceinline__ SwEval sw_eval(int scheme, float sum, float diff, float lambda, float om, float g,
-                                          float tau, float sec0, float T0, float one_m_t0) {
-  SwEval c;
-  const float x = lambda * tau;
-  const float e = __expf(-x);
-  const float em1 = one_minus_exp(x, e);
+// Reflection and transmission of a homogeneous layer (trans_source_coeff.F90:
+// 144-200) regrouped around 1 - e, 1 - gamma = 2 lambda/(sum + lambda) and
+// 1 - e gamma = (1 - e) + e (1 - gamma), so that none cancels; with 1 - T and
+// 1 - T - R in factored form.
+struct LayerF { float x, e, em1, gamma, omg, eg, T, R, omt, omtr; };
+__device__ __forceinline__ LayerF layer_mix(float sum, float lambda, float tau) {
+  LayerF l;
+  l.x = lambda * tau;
+  l.e = __expf(-l.x);
+  l.em1 = one_minus_exp(l.x, l.e);
   const float inv_sl = 1.0f / (sum + lambda);
-  const float gamma = (sum - lambda) * inv_sl;
-  const float one_m_gamma = 2.0f * lambda * inv_sl;
-  const float eg = e * gamma;
-  const float inv_den = 1.0f / ((em1 + e * one_m_gamma) * (1.0f + eg));   // 1/(1 - e^2 gamma^2)
-  c.T = e * one_m_gamma * (1.0f + gamma) * inv_den;
-  c.R = gamma * em1 * (1.0f + e) * inv_den;
-  c.omt = em1 * (1.0f + eg * gamma) * inv_den;                 // 1 - T
-  c.omtr = em1 * one_m_gamma / (1.0f + eg);                    // 1 - T - R
-  const float ksi0 = ((scheme == SOCGPU_IP_DISCRETE_ORD) ? 1.7320508f : 1.5f) * g / sec0;
+  l.gamma = (sum - lambda) * inv_sl;
+  l.omg = 2.0f * lambda * inv_sl;
+  l.eg = l.e * l.gamma;
+  const float u = fmaf(l.e, l.omg, l.em1);                  // 1 - e gamma
+  const float inv_den = 1.0f / (u * (1.0f + l.eg));          // 1 / (1 - e^2 gamma^2)
+  l.T = l.e * l.omg * (1.0f + l.gamma) * inv_den;
+  l.R = l.gamma * l.em1 * (1.0f + l.e) * inv_den;
+  l.omt = l.em1 * fmaf(l.eg, l.gamma, 1.0f) * inv_den;       // 1 - T
+  l.omtr = l.em1 * l.omg * u * inv_den;                      // 1 - T - R = em1 (1 - gamma) / (1 + e gamma)
+  return l;
+}
+
+// Solar source coefficients (solar_coefficient_basic.F90:124-219,
+// trans_source_coeff.F90:144-263): c1 = gam_up - R(1+gam_dn) - gam_up T T0
+// and c2 = T0(1+gam_dn-gam_up R) - (1+gam_dn) T, regrouped with
+// 1 - T T0 = (1-T0) + T0 (1-T) and T0 - T = (1-T) - (1-T0).
+__device__ __forceinline__ void solar_c12(float K, float sum, float diff, float lambda, float om, float g,
+                                          float sec0, float T0, float omt0, float R, float omt,
+                                          float &c1, float &c2) {
+  const float ksi0 = K * g / sec0;
   const float factor = 0.5f * om * sec0 / ((lambda - sec0) * (lambda + sec0));
   const float gam_up = factor * (sum - sec0 - ksi0 * (diff - sec0));
   const float gam_dn = factor * (sum + sec0 + ksi0 * (diff + sec0));
-  // c1 = gam_up - R(1+gam_dn) - gam_up T T0, c2 = T0(1+gam_dn-gam_up R) - (1+gam_dn) T,
-  // with 1 - T T0 = (1-T0) + T0 (1-T) and T0 - T = (1-T) - (1-T0)
-  c.c1 = gam_up * (one_m_t0 + T0 * c.omt) - c.R * (1.0f + gam_dn);
-  c.c2 = (1.0f + gam_dn) * (c.omt - one_m_t0) - gam_up * c.R * T0;
-  return c;
+  const float opd = 1.0f + gam_dn;
+  c1 = gam_up * fmaf(T0, omt, omt0) - R * opd;
+  c2 = opd * (omt - omt0) - gam_up * R * T0;
 }
 
-__device__ __forceinline__ CoefF two_coeff_mix(int isolir, int scheme, int l_quad,
+// The solar source coefficients where lambda lies within kSolarSingularTol of
+// sec_0.  They are smooth through lambda = sec_0, where the particular
+// solution's 1/(lambda^2 - sec_0^2) cancels: evaluate at (sum, diff, lambda)
+// scaled by rho_a, rho_b placed a safe distance either side of the
+// singularity and interpolate linearly to rho = 1 (error ~ tol^2 + FP32
+// eps / tol).  Out of line: few cells take it, and the hot loop stays small.
+static __device__ __noinline__ float2 solar_c12_singular(float K, float sum, float diff, float lambda, float om,
+                                                  float g, float tau, float sec0, float T0, float omt0) {
+  const float ra = sec0 * (1.0f - kSolarSingularTol) / lambda;
+  const float rb = sec0 * (1.0f + kSolarSingularTol) / lambda;
+  float a1, a2, b1, b2;
+  const LayerF la = layer_mix(ra * sum, ra * lambda, tau);
+  solar_c12(K, ra * sum, ra * diff, ra * lambda, om, g, sec0, T0, omt0, la.R, la.omt, a1, a2);
+  const LayerF lb = layer_mix(rb * sum, rb * lambda, tau);
+  solar_c12(K, rb * sum, rb * diff, rb * lambda, om, g, sec0, T0, omt0, lb.R, lb.omt, b1, b2);
+  const float w = (1.0f - ra) / (rb - ra);
+  return make_float2(a1 + w * (b1 - a1), a2 + w * (b2 - a2));
+}
+
+__device__ __forceinline__ CoefF two_coeff_mix(int isolir, const SchemeF &sc, int l_quad,
                                                float g, float om, float one_m_om,
                                                float tau, float sec0) {
   CoefF c;
-  float sum, diff;
-  sum_diff_mix(scheme, om, one_m_om, g, sum, diff);
+  const float sum = fmaf(-om, fmaf(sc.B, g, sc.C), sc.A);
+  const float diff = sc.D * one_m_om;
   const float lambda = sqrtf(sum * diff);
+  const LayerF l = layer_mix(sum, lambda, tau);
+  c.T = l.T; c.R = l.R; c.omtr = l.omtr;
   if (isolir == SOCGPU_IP_SOLAR) {
     const float x0 = tau * sec0;
     const float T0 = __expf(-x0);
-    const float one_m_t0 = one_minus_exp(x0, T0);
-    SwEval v = sw_eval(scheme, sum, diff, lambda, om, g, tau, sec0, T0, one_m_t0);
+    const float omt0 = one_minus_exp(x0, T0);
+    solar_c12(sc.K, sum, diff, lambda, om, g, sec0, T0, omt0, l.R, l.omt, c.c1, c.c2);
     if (fabsf(lambda - sec0) < kSolarSingularTol * sec0) {
-      // The coefficients are smooth through lambda = sec_0, where the
-      // particular solution's 1/(lambda^2 - sec_0^2) cancels.  Evaluate at
-      // (sum, diff, lambda) scaled by rho_a, rho_b placed a safe distance
-      // either side of the singularity and interpolate linearly to rho = 1
-      // (error ~ tol^2 + FP32 eps / tol).
-      const float ra = sec0 * (1.0f - kSolarSingularTol) / lambda;
-      const float rb = sec0 * (1.0f + kSolarSingularTol) / lambda;
-      SwEval a = sw_eval(scheme, ra * sum, ra * diff, ra * lambda, om, g, tau, sec0, T0, one_m_t0);
-      SwEval b = sw_eval(scheme, rb * sum, rb * diff, rb * lambda, om, g, tau, sec0, T0, one_m_t0);
-      const float w = (1.0f - ra) / (rb - ra);
-      v.c1 = a.c1 + w * (b.c1 - a.c1);
-      v.c2 = a.c2 + w * (b.c2 - a.c2);
+      const float2 v = solar_c12_singular(sc.K, sum, diff, lambda, om, g, tau, sec0, T0, omt0);
+      c.c1 = v.x; c.c2 = v.y;
     }
-    c.T = v.T; c.R = v.R; c.T0 = T0; c.c1 = v.c1; c.c2 = v.c2; c.omtr = v.omtr;
+    c.T0 = T0;
     return c;
   }
-  // infra-red
-  const float x = lambda * tau;
-  const float e = __expf(-x);
-  const float em1 = one_minus_exp(x, e);
-  const float inv_sl = 1.0f / (sum + lambda);
-  const float gamma = (sum - lambda) * inv_sl;
-  const float one_m_gamma = 2.0f * lambda * inv_sl;
-  const float opg = 1.0f + gamma;
-  const float eg = e * gamma;
-  const float inv_den = 1.0f / ((em1 + e * one_m_gamma) * (1.0f + eg));
-  c.T = e * one_m_gamma * opg * inv_den;
-  c.R = gamma * em1 * (1.0f + e) * inv_den;
-  c.T0 = 1.0f;
-  c.omtr = em1 * one_m_gamma / (1.0f + eg);
-  const float one_m_t = em1 * (1.0f + eg * gamma) * inv_den;
+  // infra-red (trans_source_coeff.F90:200-257)
   const float sq = (float)kSqEps64;
-  c.c1 = (one_m_t + c.R + sq) / (sq + tau * sum);
+  c.T0 = 1.0f;
+  c.c1 = (l.omt + l.R + sq) / fmaf(tau, sum, sq);
   c.c2 = 0.0f;
   if (l_quad) {
-    // trans_source_coeff.F90:233-257: the numerator 1 + R + T + s2 equals
-    // d tau - (1-T-R) (thin layers) or 2 (d tau - (1-T-R))/(d tau + sq) - (1-T-R);
+    // the numerator 1 + R + T + s2 equals d tau - (1-T-R) (thin layers) or
+    // 2 (d tau - (1-T-R))/(d tau + sq) - (1-T-R);
     // d tau - (1-T-R) = (1-gamma)(phi(x) + gamma psi(x)) / ((1+gamma)(1+e gamma))
-    const float dmo = one_m_gamma * (phi_exp(x, em1) + gamma * psi_exp(x, e)) / (opg * (1.0f + eg));
-    const float num = (tau > (float)kTolQuad64) ? 2.0f * dmo / (diff * tau + sq) - c.omtr : dmo;
-    c.c2 = -num / (sum * tau + sq);
+    const float dmo = l.omg * (phi_exp(l.x, l.em1) + l.gamma * psi_exp(l.x, l.e)) /
+                      ((1.0f + l.gamma) * (1.0f + l.eg));
+    const float num = (tau > (float)kTolQuad64) ? 2.0f * dmo / fmaf(diff, tau, sq) - l.omtr : dmo;
+    c.c2 = -num / fmaf(sum, tau, sq);
   }
   return c;
 }
