@@ -85,6 +85,17 @@ __device__ __forceinline__ R load_in(const double *a) {
   if constexpr (sizeof(R) == 8) return __ldg(a);
   else return narrow(__ldg(a));
 }
+// A raw FP64 input already in shared memory, in R.
+template <class R>
+__device__ __forceinline__ R raw_in(double v) {
+  if constexpr (sizeof(R) == 8) return v;
+  else return narrow(v);
+}
+// One asynchronous 8-byte copy from global to shared memory (cp.async).
+__device__ __forceinline__ void cp_async8(double *dst, const double *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
 template <class R>
 __device__ __forceinline__ double store_out(R v) {
   if constexpr (sizeof(R) == 8) return v;
@@ -154,6 +165,11 @@ struct SmemLayout {
   size_t off_aux, off_lkf, off_lki, off_sbf, off_sbj, off_kscr;
   size_t off_ovl, off_reg, off_regd, off_nct, off_t0d;
   size_t off_acc;
+  // the column's FP64 inputs, fetched into shared memory ahead of staging
+  // (offsets in doubles from off_acc, whose space they share); raw_on false
+  // leaves staging on direct global loads
+  int raw_on, raw_n;
+  int r_p, r_t, r_mass, r_gas, r_mmr, r_mabs, r_msca, r_masy, r_sol, r_zen, r_alb, r_tg, r_fg, r_tl;
   size_t bytes;
 };
 
@@ -174,7 +190,7 @@ enum RegDRow { kRgB11, kRgB21, kRgB22, kRgG11, kRgG12, kRgG21, kRgG22, kRgH1, kR
 // solve groups of P lanes, LP = P*CH layer slots.
 template <class R>
 __host__ __device__ inline SmemLayout make_layout(const FluxParams &p, int LP, int P, int nb, int n_groups,
-                                                  bool mcica) {
+                                                  bool mcica, bool raw_ok = false) {
   const int max_abs = p.max_abs, n_comp = mcica ? p.n_condensed : 0, n_sub = mcica ? p.n_subcol_gen : 0;
   const bool lw = p.isolir == SOCGPU_IP_INFRA_RED;
   SmemLayout s{};
@@ -236,6 +252,32 @@ __host__ __device__ inline SmemLayout make_layout(const FluxParams &p, int LP, i
   while (rem != want) { ++stride; rem = (stride * words) % 32; }
   s.acc_stride = stride;
   s.off_acc = take((size_t)n_groups * stride);
+  // The raw inputs of the column: layer fields, gas mixing ratios (up to
+  // kMaxRawGas species), modal aerosol and the surface values, when the
+  // whole band range is staged at once.  They are read only by the staging,
+  // before the accumulators are cleared, so they share their space.
+  s.raw_on = 0; s.raw_n = 0;
+  if (raw_ok && nb == p.last_band - p.first_band + 1) {
+    const int L = p.n_layer;
+    int n = 0;
+    auto seg = [&](int len) { int r = n; n += len; return r; };
+    s.r_p = seg(L); s.r_t = seg(L); s.r_mass = seg(L);
+    s.r_gas = seg((p.l_gas && p.nd_species <= kMaxRawGas) ? p.nd_species * L : 0);
+    const bool aer = p.l_aerosol_mode && p.n_mode > 0;
+    s.r_mmr = seg(aer ? p.n_mode * L : 0);
+    s.r_mabs = seg(aer ? p.n_mode * nb * L : 0);
+    s.r_msca = seg(aer ? p.n_mode * nb * L : 0);
+    s.r_masy = seg(aer ? p.n_mode * nb * L : 0);
+    s.r_sol = seg(!lw && p.solar_irrad ? 1 : 0);
+    s.r_zen = seg(!lw && p.zen_0 ? 1 : 0);
+    s.r_alb = seg(2 * nb);
+    s.r_tg = seg(lw && p.t_ground ? 1 : 0);
+    s.r_fg = seg(lw && p.flux_ground ? nb : 0);
+    s.r_tl = seg(lw && p.t_level ? L + 1 : 0);
+    s.raw_on = 1; s.raw_n = n;
+    const size_t need = s.off_acc + (size_t)n * sizeof(double);
+    if (need > o) o = need;
+  }
   s.bytes = (o + 15) & ~(size_t)15;
   return s;
 }
@@ -310,6 +352,12 @@ struct FluxKernel {
   static constexpr bool kFP64 = (sizeof(R) == 8);
   static constexpr int LP = P * CH;
 
+  // Fetch the column's raw inputs ahead of staging (fetch_raw) for tiles of
+  // at most 16 lanes per solve.  Measured on GB300: their CTAs have few warps
+  // (long chunks hold many registers), so each CTA's staging round trips
+  // stalled most of its warps; the 32-lane tiles' 8-warp CTAs hide them, and
+  // the prefetch cost them 8 %.
+  static constexpr bool kRawFetch = P <= 16;
   __device__ static __forceinline__ int slot(int i) { return (i % CH) * P + i / CH; }
   __device__ static __forceinline__ int layer_of_slot(int s) { return (s % P) * CH + s / P; }
   __device__ static __forceinline__ int level_slot(int lev) { return lev == 0 ? LP : slot(lev - 1); }
@@ -378,6 +426,9 @@ struct FluxKernel {
     double *regd;
     int *nct;
     Acc *acc;
+    // the column's raw inputs (null: read them from global memory)
+    const double *raw;
+    int r_p, r_t, r_mass, r_gas, r_mmr, r_mabs, r_msca, r_masy, r_sol, r_zen, r_alb, r_tg, r_fg, r_tl;
   };
 
   __device__ static Smem bind(unsigned char *smem, const SmemLayout &l) {
@@ -399,6 +450,10 @@ struct FluxKernel {
     s.regd = (double *)(smem + l.off_regd);
     s.t0d = (R *)(smem + l.off_t0d);
     s.acc = (Acc *)(smem + l.off_acc);
+    s.raw = l.raw_on ? (const double *)(smem + l.off_acc) : nullptr;
+    s.r_p = l.r_p; s.r_t = l.r_t; s.r_mass = l.r_mass; s.r_gas = l.r_gas; s.r_mmr = l.r_mmr;
+    s.r_mabs = l.r_mabs; s.r_msca = l.r_msca; s.r_masy = l.r_masy; s.r_sol = l.r_sol; s.r_zen = l.r_zen;
+    s.r_alb = l.r_alb; s.r_tg = l.r_tg; s.r_fg = l.r_fg; s.r_tl = l.r_tl;
     return s;
   }
 
@@ -568,6 +623,54 @@ struct FluxKernel {
   }
 
 
+  // The temperature at level lev, in T.
+  template <class T>
+  __device__ static __forceinline__ T t_lev(const FluxParams &p, const Smem &S, int col, int lev) {
+    if (S.raw) return raw_in<T>(S.raw[S.r_tl + lev]);
+    return load_in<T>(p.t_level + (size_t)col + (size_t)p.nd_profile * lev);
+  }
+
+  // The column's raw FP64 inputs into shared memory (layout of make_layout):
+  // one asynchronous 8-byte copy per element, all in flight together, so
+  // that staging waits for one round trip to memory instead of one per
+  // dependent load.  Every source is an element the staging would read.
+  __device__ static void fetch_raw(const FluxParams &p, const SmemLayout &l, double *raw, int col, int bstart) {
+    const int L = p.n_layer, ndp = p.nd_profile, ndl = p.nd_layer, nt = blockDim.x, nb = l.nb;
+    const size_t c = (size_t)col;
+    for (int k = threadIdx.x; k < L; k += nt) {
+      cp_async8(raw + l.r_p + k, p.p + c + (size_t)ndp * k);
+      cp_async8(raw + l.r_t + k, p.t + c + (size_t)ndp * k);
+      cp_async8(raw + l.r_mass + k, p.mass + c + (size_t)ndp * k);
+    }
+    for (int k = threadIdx.x; k < l.r_mmr - l.r_gas; k += nt) {
+      const int sp = k / L, i = k - sp * L;
+      cp_async8(raw + l.r_gas + k, p.gas_mix_ratio + c + (size_t)ndp * ((size_t)i + (size_t)ndl * sp));
+    }
+    for (int k = threadIdx.x; k < l.r_mabs - l.r_mmr; k += nt) {
+      const int m = k / L, i = k - m * L;
+      cp_async8(raw + l.r_mmr + k, p.mode_mix_ratio + c + (size_t)ndp * ((size_t)i + (size_t)ndl * m));
+    }
+    for (int k = threadIdx.x; k < l.r_msca - l.r_mabs; k += nt) {
+      const int mb = k / L, i = k - mb * L, m = mb / nb, b = bstart + (mb - m * nb);
+      const size_t q4 = c + (size_t)ndp * ((size_t)i + (size_t)ndl * ((size_t)m + (size_t)p.nd_mode * b));
+      cp_async8(raw + l.r_mabs + k, p.mode_absorption + q4);
+      cp_async8(raw + l.r_msca + k, p.mode_scattering + q4);
+      cp_async8(raw + l.r_masy + k, p.mode_asymmetry + q4);
+    }
+    if (threadIdx.x == 0) {
+      if (l.r_zen > l.r_sol) cp_async8(raw + l.r_sol, p.solar_irrad + c);
+      if (l.r_alb > l.r_zen) cp_async8(raw + l.r_zen, p.zen_0 + c);
+      if (l.r_fg > l.r_tg) cp_async8(raw + l.r_tg, p.t_ground + c);
+    }
+    for (int k = threadIdx.x; k < 2 * nb; k += nt)
+      cp_async8(raw + l.r_alb + k, p.rho_alb + c + (size_t)ndp * ((size_t)(k & 1) + 2 * (size_t)(bstart + (k >> 1))));
+    for (int k = threadIdx.x; k < l.r_tl - l.r_fg; k += nt)
+      cp_async8(raw + l.r_fg + k, p.flux_ground + c + (size_t)ndp * (size_t)(bstart + k));
+    for (int k = threadIdx.x; k < l.raw_n - l.r_tl; k += nt)
+      cp_async8(raw + l.r_tl + k, p.t_level + c + (size_t)ndp * k);
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+  }
+
   __device__ static void run(const FluxParams &p, const int col) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int L = p.n_layer;
@@ -577,26 +680,37 @@ struct FluxKernel {
     const int n_groups = nthreads / P;
     constexpr bool lw = (SRC == SOCGPU_IP_INFRA_RED);
     const int max_abs = p.max_abs;
-    const SmemLayout lay = make_layout<R>(p, LP, P, nbat, n_groups, MCICA);
+    const SmemLayout lay = make_layout<R>(p, LP, P, nbat, n_groups, MCICA, kRawFetch);
     const Smem S = bind(smem, lay);
     const int ndp = p.nd_profile;
+    if (lay.raw_on) {
+      fetch_raw(p, lay, (double *)(smem + lay.off_acc), col, p.first_band - 1);
+      __syncthreads();
+    }
 
     // ---------------- column fields and accumulators ------------------------
     for (int s = threadIdx.x; s < LP; s += nthreads) {
       const int i = layer_of_slot(s);
       if (i < L) {
-        S.p[s] = load_in<R>(p.p + (size_t)col + (size_t)ndp * i);
-        S.t[s] = load_in<R>(p.t + (size_t)col + (size_t)ndp * i);
-        S.mass[s] = load_in<R>(p.mass + (size_t)col + (size_t)ndp * i);
+        if (S.raw) {
+          S.p[s] = raw_in<R>(S.raw[S.r_p + i]);
+          S.t[s] = raw_in<R>(S.raw[S.r_t + i]);
+          S.mass[s] = raw_in<R>(S.raw[S.r_mass + i]);
+        } else {
+          S.p[s] = load_in<R>(p.p + (size_t)col + (size_t)ndp * i);
+          S.t[s] = load_in<R>(p.t + (size_t)col + (size_t)ndp * i);
+          S.mass[s] = load_in<R>(p.mass + (size_t)col + (size_t)ndp * i);
+        }
         if (p.lk_on) lookup_slot(p, S.lkf, S.lki, S.sbf, S.sbj, S.p[s], S.t[s], col, s, i);
       }
     }
-    for (int q = threadIdx.x; q < n_groups * lay.acc_stride; q += nthreads) S.acc[q] = Acc(0);
+    if (!S.raw)
+      for (int q = threadIdx.x; q < n_groups * lay.acc_stride; q += nthreads) S.acc[q] = Acc(0);
     if (MCICA) stage_cloud_column(p, S, col);
     if (MCICA && p.region) stage_regions(p, S, col, LP);
     const int gid = threadIdx.x / P;
     const int r = threadIdx.x % P;
-    const R sec0 = p.zen_0 ? load_in<R>(p.zen_0 + col) : R(1);
+    const R sec0 = !p.zen_0 ? R(1) : (S.raw && S.r_alb > S.r_zen) ? raw_in<R>(S.raw[S.r_zen]) : load_in<R>(p.zen_0 + col);
     Acc *acc = S.acc + (size_t)gid * lay.acc_stride;
     __syncthreads();
 
@@ -608,6 +722,12 @@ struct FluxKernel {
       __syncthreads();
       stage_boundary(p, S, col, bstart, nb, lw);
       __syncthreads();
+      if (S.raw) {
+        // the raw inputs are consumed: their space becomes the accumulators
+        // (the whole band range is staged at once, so this runs once)
+        for (int q = threadIdx.x; q < n_groups * lay.acc_stride; q += nthreads) S.acc[q] = Acc(0);
+        __syncthreads();
+      }
       if (p.keqv) {
         stage_keqv(p, S, bstart, nb, sec0);
         __syncthreads();
@@ -707,11 +827,22 @@ struct FluxKernel {
       }
       if (p.l_aerosol_mode) {
         for (int j = 0; j < p.n_mode; ++j) {
-          R mmr = load_in<R>(p.mode_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * j));
-          size_t q4 = (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * ((size_t)j + (size_t)p.nd_mode * b));
-          R g = load_in<R>(p.mode_asymmetry + q4);
-          kabs = kabs + mmr * load_in<R>(p.mode_absorption + q4);
-          R ks = mmr * load_in<R>(p.mode_scattering + q4);
+          R mmr, g, ka, ksc;
+          if (S.raw && S.r_mabs > S.r_mmr) {
+            const int qr = (j * nb + bi) * L + i;
+            mmr = raw_in<R>(S.raw[S.r_mmr + j * L + i]);
+            g = raw_in<R>(S.raw[S.r_masy + qr]);
+            ka = raw_in<R>(S.raw[S.r_mabs + qr]);
+            ksc = raw_in<R>(S.raw[S.r_msca + qr]);
+          } else {
+            mmr = load_in<R>(p.mode_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * j));
+            size_t q4 = (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * ((size_t)j + (size_t)p.nd_mode * b));
+            g = load_in<R>(p.mode_asymmetry + q4);
+            ka = load_in<R>(p.mode_absorption + q4);
+            ksc = load_in<R>(p.mode_scattering + q4);
+          }
+          kabs = kabs + mmr * ka;
+          R ks = mmr * ksc;
           kes = kes + ks;
           phf = phf + ks * g;
           if (p.l_rescale) {
@@ -780,7 +911,9 @@ struct FluxKernel {
       const int n_abs_b = p.l_gas ? min(bd.n_abs, max_abs) : 0;
       for (int j = 0; j < n_abs_b; ++j) {
         const BandGas &gs = bd.gas[j];
-        R mmr = load_in<R>(p.gas_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * gs.species));
+        R mmr = (S.raw && S.r_mmr > S.r_gas)
+                    ? raw_in<R>(S.raw[S.r_gas + gs.species * L + i])
+                    : load_in<R>(p.gas_mix_ratio + (size_t)col + (size_t)ndp * ((size_t)i + (size_t)ndl * gs.species));
         R amt;
         if (gs.i_scale_k == SOCGPU_IP_SCALE_BAND) {
           R gf;
@@ -806,10 +939,10 @@ struct FluxKernel {
         if (lev > L) continue;
         const BandInfo &bd = p.bands[bstart + bi];
         if constexpr (kFP64)
-          S.planck[q] = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_level, col, lev, ndp) / p.t_ref_planck);
+          S.planck[q] = planck_ref(bd.planck, p.n_deg_fit, t_lev<double>(p, S, col, lev) / p.t_ref_planck);
         else
           S.planck[q] = planck_mix(bd.planck_f, p.n_deg_fit,
-                                   load_in<float>(p.t_level + (size_t)col + (size_t)ndp * lev) / p.t_ref_planck_f);
+                                   t_lev<float>(p, S, col, lev) / p.t_ref_planck_f);
       }
       for (int q = threadIdx.x; q < nb * LP; q += nthreads) {
         const int bi = q / LP, s = q - bi * LP;
@@ -817,16 +950,17 @@ struct FluxKernel {
         if (i >= L) continue;
         const BandInfo &bd = p.bands[bstart + bi];
         if constexpr (kFP64) {
-          double b1 = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_level, col, i + 1, ndp) / p.t_ref_planck);
-          double bm = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_level, col, i, ndp) / p.t_ref_planck);
+          double b1 = planck_ref(bd.planck, p.n_deg_fit, t_lev<double>(p, S, col, i + 1) / p.t_ref_planck);
+          double bm = planck_ref(bd.planck, p.n_deg_fit, t_lev<double>(p, S, col, i) / p.t_ref_planck);
           S.dB[q] = b1 - bm;
           if (p.l_ir_source_quad) {
-            double bl = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t, col, i, ndp) / p.t_ref_planck);
+            double bl = planck_ref(bd.planck, p.n_deg_fit,
+                                   (S.raw ? S.raw[S.r_t + i] : ld2(p.t, col, i, ndp)) / p.t_ref_planck);
             S.dB2[q] = 2.0 * (b1 + bm - 2.0 * bl);
           }
         } else {
-          const float x1 = load_in<float>(p.t_level + (size_t)col + (size_t)ndp * (i + 1)) / p.t_ref_planck_f;
-          const float x0 = load_in<float>(p.t_level + (size_t)col + (size_t)ndp * i) / p.t_ref_planck_f;
+          const float x1 = t_lev<float>(p, S, col, i + 1) / p.t_ref_planck_f;
+          const float x0 = t_lev<float>(p, S, col, i) / p.t_ref_planck_f;
           S.dB[q] = planck_diff_mix(bd.planck_f, p.n_deg_fit, x1, x0);
           if (p.l_ir_source_quad) {
             const float xl = S.t[s] / p.t_ref_planck_f;
@@ -900,28 +1034,38 @@ struct FluxKernel {
       const int b = bstart + bi;
       const BandInfo &bd = p.bands[b];
       R *v = S.bscal + bi * kBandScal;
-      v[2] = load_in<R>(p.rho_alb + (size_t)col + (size_t)ndp * (0 + 2 * (size_t)b));
-      v[3] = load_in<R>(p.rho_alb + (size_t)col + (size_t)ndp * (1 + 2 * (size_t)b));
+      if (S.raw) {
+        v[2] = raw_in<R>(S.raw[S.r_alb + 2 * bi]);
+        v[3] = raw_in<R>(S.raw[S.r_alb + 2 * bi + 1]);
+      } else {
+        v[2] = load_in<R>(p.rho_alb + (size_t)col + (size_t)ndp * (0 + 2 * (size_t)b));
+        v[3] = load_in<R>(p.rho_alb + (size_t)col + (size_t)ndp * (1 + 2 * (size_t)b));
+      }
       v[5] = p.weight_band ? load_in<R>(p.weight_band + b) : R(1);
       if (lw) {
         v[0] = -S.planck[bi * (LP + 1) + LP];
         v[1] = R(0);
         if (p.flux_ground) {
           // the surface's Planck flux given per band (l_flux_ground, tiles)
-          v[4] = load_in<R>(p.flux_ground + (size_t)col + (size_t)ndp * b) - S.planck[bi * (LP + 1) + level_slot(L)];
+          v[4] = (S.raw ? raw_in<R>(S.raw[S.r_fg + bi]) : load_in<R>(p.flux_ground + (size_t)col + (size_t)ndp * b)) -
+                 S.planck[bi * (LP + 1) + level_slot(L)];
         } else if constexpr (kFP64) {
-          double bg = planck_ref(bd.planck, p.n_deg_fit, ld2(p.t_ground, col, 0, ndp) / p.t_ref_planck);
+          double bg = planck_ref(bd.planck, p.n_deg_fit,
+                                 (S.raw ? S.raw[S.r_tg] : ld2(p.t_ground, col, 0, ndp)) / p.t_ref_planck);
           v[4] = bg - S.planck[bi * (LP + 1) + level_slot(L)];
         } else {
-          v[4] = planck_diff_mix(bd.planck_f, p.n_deg_fit, load_in<float>(p.t_ground + col) / p.t_ref_planck_f,
-                                 load_in<float>(p.t_level + (size_t)col + (size_t)ndp * L) / p.t_ref_planck_f);
+          const float tg = S.raw ? raw_in<float>(S.raw[S.r_tg]) : load_in<float>(p.t_ground + col);
+          v[4] = planck_diff_mix(bd.planck_f, p.n_deg_fit, tg / p.t_ref_planck_f,
+                                 t_lev<float>(p, S, col, L) / p.t_ref_planck_f);
         }
       } else {
         if constexpr (kFP64) {
-          double sib = ld2(p.solar_irrad, col, 0, ndp) * bd.solar_flux_band;
-          v[0] = sib / ld2(p.zen_0, col, 0, ndp);
+          double sib = (S.raw ? S.raw[S.r_sol] : ld2(p.solar_irrad, col, 0, ndp)) * bd.solar_flux_band;
+          v[0] = sib / (S.raw ? S.raw[S.r_zen] : ld2(p.zen_0, col, 0, ndp));
         } else {
-          v[0] = load_in<float>(p.solar_irrad + col) * bd.solar_flux_band_f / load_in<float>(p.zen_0 + col);
+          const float sol = S.raw ? raw_in<float>(S.raw[S.r_sol]) : load_in<float>(p.solar_irrad + col);
+          const float zen = S.raw ? raw_in<float>(S.raw[S.r_zen]) : load_in<float>(p.zen_0 + col);
+          v[0] = sol * bd.solar_flux_band_f / zen;
         }
         v[1] = v[0];
         v[4] = R(0);

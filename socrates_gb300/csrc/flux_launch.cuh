@@ -27,7 +27,8 @@ int try_launch(const FluxParams &p, const TileConfig &cfg, cudaStream_t st, char
   int warps = cfg.warps_per_cta, batch = nb;
   SmemLayout lay{};
   for (;;) {
-    lay = make_layout<R>(p, S::P * S::CH, S::P, batch, warps * 32 / S::P, MCICA);
+    lay = make_layout<R>(p, S::P * S::CH, S::P, batch, warps * 32 / S::P, MCICA,
+                         FluxKernel<R, MIX, S::P, S::CH, NOSCAT, MCICA, SRC>::kRawFetch);
     if ((long long)lay.bytes <= max_smem) break;
     if (batch > 1) { --batch; continue; }
     if (warps > 1) { warps /= 2; batch = nb; continue; }
@@ -72,7 +73,8 @@ int try_prepare(BatchGroup &g, char *msg, size_t len, bool &done) {
   const int warps = g.tile.warps_per_cta;
   const int n_groups = warps * 32 / S::P;
   auto bytes_of = [&](const FluxParams &p, int batch) {
-    return make_layout<R>(p, S::P * S::CH, S::P, batch, n_groups, MCICA).bytes;
+    return make_layout<R>(p, S::P * S::CH, S::P, batch, n_groups, MCICA,
+                          FluxKernel<R, MIX, S::P, S::CH, NOSCAT, MCICA, SRC>::kRawFetch).bytes;
   };
   auto kern = flux_kernel_batched<R, MIX, S::P, S::CH, NOSCAT, MCICA, SRC>;
   // the kernel's static shared memory (its parameter copy) counts against

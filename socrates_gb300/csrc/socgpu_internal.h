@@ -25,6 +25,8 @@ constexpr int kMaxSb = 4;
 // Classic aerosol: mixing-ratio entries a launch takes (radiatively active
 // ones), and the widest humidity table and phase-function moments per entry.
 constexpr int kMaxAerMr = 32;
+// Most gas species a flux kernel fetches ahead of staging (more: direct loads).
+constexpr int kMaxRawGas = 8;
 
 // One absorber of a band (block 4/5 entries for (band, species)).
 struct BandGas {
