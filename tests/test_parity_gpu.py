@@ -220,6 +220,70 @@ def test_pipelined_host_path_equals_device_path(gpu_lib, prec):
         np.testing.assert_array_equal(host[k], dc.output(k), err_msg=k)
 
 
+def _page_locked(a, keep):
+    """A page-locked copy of array a (same shape, Fortran order)."""
+    import torch
+    a = np.asfortranarray(a, dtype=np.int32 if np.issubdtype(np.asarray(a).dtype, np.integer) else np.float64)
+    t = torch.empty(a.size, dtype=torch.from_numpy(np.zeros(1, a.dtype)).dtype, pin_memory=True)
+    v = t.numpy().reshape(a.shape, order="F")
+    v[...] = a
+    keep.append(t)
+    return v
+
+
+def _page_locked_call(ctl, sp, col, mc=None):
+    """radiance_calc through the C-ABI with every caller array page-locked:
+    the pipelined path whose column windows the copy engines move straight
+    from the caller's arrays."""
+    import ctypes as C
+    from dataclasses import replace
+    keep = []
+    c = copy.copy(col)
+    for name in ("p", "t", "p_level", "t_level", "mass", "gas_mix_ratio", "t_ground", "zen_0", "solar_irrad",
+                 "rho_alb"):
+        if getattr(c, name) is not None:
+            setattr(c, name, _page_locked(getattr(c, name), keep))
+    if c.aer:
+        c.aer = {k: (_page_locked(v, keep) if isinstance(v, np.ndarray) else v) for k, v in c.aer.items()}
+    if c.cld:
+        c.cld = {k: (_page_locked(v, keep) if isinstance(v, np.ndarray) else v) for k, v in c.cld.items()}
+    if mc is not None:
+        mc = replace(mc, **{f: _page_locked(getattr(mc, f), keep)
+                            for f in ("c_sub", "frac_cloudy", "n_subcol_cld", "subcol_k", "first_subcol_k",
+                                      "subcol_reorder") if getattr(mc, f) is not None})
+    m = R.Marshal(ctl, sp, c, mc, alloc=lambda *s: _page_locked(np.zeros(s, order="F"), keep))
+    lib = R.load_library()
+    msg = C.create_string_buffer(512)
+    st = lib.socgpu_radiance_calc(*m.args(R.register_spectrum(sp)), msg, 512)
+    assert st == abi.I_NORMAL, msg.value.decode()
+    return {k: np.array(v) for k, v in m.result().items()}
+
+
+@pytest.mark.parametrize("prec", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_page_locked_host_path_equals_pageable_path(gpu_lib, prec):
+    """Page-locked caller arrays take the pipelined path (each chunk's column
+    windows copied straight from them on one stream, the kernel on a second,
+    the outputs back on a third); pageable ones are packed into page-locked
+    staging first.  Both must give every column bit for bit: the solar
+    workload over many chunks, and a McICA batch whose inputs include 4-byte
+    integer arrays (n_subcol_cld) and subcolumn fields."""
+    sp, col = synth.config2(5003, 60, seed=31)
+    ctl = R.sw_control(l_aerosol_mode=True, precision=prec)
+    ref = R.radiance_calc(ctl, sp, col)
+    got = _page_locked_call(ctl, sp, col)
+    for k in ref:
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    lw, sw, col3 = synth.config3(3001, 85, seed=5, n_subcol=16)
+    synth.add_lw_surface(col3, lw.n_band)
+    c_sub, nsc = R.cloud_gen(col3, 16, abi.IP_EXPONENTIAL_RAND, abi.RNG_PHILOX)
+    mc = R.set_cld_mcica(lw, col3, abi.IP_INFRA_RED, abi.IP_MCICA_SINGLE_SAMPLING, c_sub=c_sub, n_subcol_cld=nsc)
+    ctl3 = R.lw_control(i_cloud=abi.IP_CLOUD_MCICA, precision=prec)
+    ref3 = R.radiance_calc(ctl3, lw, col3, mc)
+    got3 = _page_locked_call(ctl3, lw, col3, mc)
+    for k in ref3:
+        np.testing.assert_array_equal(got3[k], ref3[k], err_msg="mcica " + k)
+
+
 def test_full_size_mcica_properties(gpu_lib):
     """The all-sky McICA workload at full size, 65 536 columns x 85 layers x
     16 subcolumns, infra-red.  The GPU generator (Philox) matches the oracle
