@@ -77,9 +77,11 @@ extern "C" {
 #define SOCGPU_IP_SOLVER_MIX_DIRECT     11   /* two cloud regions (solver_mix_direct.F90) */
 #define SOCGPU_IP_SOLVER_HOMOGEN_DIRECT 13
 #define SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN 16 /* two regions, Hogan's form (solver_mix_direct_hogan.F90) */
+#define SOCGPU_IP_SOLVER_TRIPLE_HOGAN  17  /* three regions, Hogan's form (solver_triple_hogan.F90) */
 /* cloud schemes, rad_pcf.F90:313,322 */
 #define SOCGPU_IP_CLOUD_MIX_MAX         2   /* clear and cloudy regions, maximum-random overlap */
 #define SOCGPU_IP_CLOUD_MIX_RANDOM      4   /* clear and cloudy regions, random overlap */
+#define SOCGPU_IP_CLOUD_TRIPLE          6   /* clear, stratiform and convective regions, maximum-random */
 #define SOCGPU_IP_CLOUD_CLEAR           5
 #define SOCGPU_IP_CLOUD_MCICA          10
 /* cloud representation, rad_pcf.F90:238-254 */
@@ -102,9 +104,16 @@ extern "C" {
 #define SOCGPU_IP_RE_EXTERNAL           2
 #define SOCGPU_IP_RE_LIU                3
 #define SOCGPU_IP_RE_CONSTANT           4
-/* cloud types, rad_pcf.F90:332-334 */
+/* cloud types, rad_pcf.F90:332-348: water and ice; stratiform and
+   convective; stratiform water and ice, convective water and ice */
 #define SOCGPU_IP_CLOUD_TYPE_WATER      1
 #define SOCGPU_IP_CLOUD_TYPE_ICE        2
+#define SOCGPU_IP_CLOUD_TYPE_STRAT      1
+#define SOCGPU_IP_CLOUD_TYPE_CONV       2
+#define SOCGPU_IP_CLOUD_TYPE_SW         1
+#define SOCGPU_IP_CLOUD_TYPE_SI         2
+#define SOCGPU_IP_CLOUD_TYPE_CW         3
+#define SOCGPU_IP_CLOUD_TYPE_CI         4
 /* condensed phases, rad_pcf.F90:494-496 */
 #define SOCGPU_IP_PHASE_WATER           1
 #define SOCGPU_IP_PHASE_ICE             2

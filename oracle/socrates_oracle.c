@@ -322,12 +322,23 @@ typedef struct {
      * the solver's elimination coefficients, the interface coefficients */
     double *tc, *rc, *t0c, *t0dc, *sc1c, *sc2c, *s_up_c, *s_down_c;
     double *b11, *b21, *b22, *g11, *g12, *g21, *g22, *h1, *h2, *ovl;
+    /* three regions (triple_column): the convective region's coefficients
+     * and sources (the stratiform region uses the cloudy-region arrays
+     * above), its elimination coefficients, the regions' fractions of the
+     * cloud, and the direct flux and sources at the ground of the two
+     * cloudy regions */
+    double *tv, *rv, *t0v, *t0dv, *sc1v, *sc2v, *s_up_v, *s_down_v;
+    double *b33, *g33, *h3, *fr2, *fr3, *fdg2, *fdg3, *sg2, *sg3;
     int nct;                    /* n_cloud_top, 1-based */
     int *slot;
     const double *adj;          /* adjust_solar_ke of k_eqv_scl (solar), or NULL */
 } work;
 
 static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
+
+/* Interface coefficients kept per (profile, interface): two regions use
+ * 8 (overlap_coupled2), three use 18 (overlap_coupled3). */
+#define OVS 18
 
 #define WORK_FIELDS(X) \
     X(k_grey_tot, pl) X(k_ext_scat, pl) X(phase_fnc, pl) X(forward_scatter, pl) \
@@ -346,7 +357,9 @@ static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(doub
     X(alpha, wp) X(s_up_prime, wp) X(beta, pl) X(gam, pl) X(h, pl) X(cont_amount, pl) \
     X(tc, pl) X(rc, pl) X(t0c, pl) X(t0dc, pl) X(sc1c, pl) X(sc2c, pl) X(s_up_c, pl) X(s_down_c, pl) \
     X(b11, pl) X(b21, pl) X(b22, pl) X(g11, pl) X(g12, pl) X(g21, pl) X(g22, pl) X(h1, pl) X(h2, pl) \
-    X(ovl, pl1 * 8)
+    X(ovl, pl1 * OVS) \
+    X(tv, pl) X(rv, pl) X(t0v, pl) X(t0dv, pl) X(sc1v, pl) X(sc2v, pl) X(s_up_v, pl) X(s_down_v, pl) \
+    X(b33, pl) X(g33, pl) X(h3, pl) X(fr2, pl) X(fr3, pl) X(fdg2, wp) X(fdg3, wp) X(sg2, wp) X(sg3, wp)
 
 static void work_init(work *w, int wp, int ndl, int n_profile, int n_layer, int nc, int na)
 {
@@ -1510,7 +1523,7 @@ static void overlap_coupled2(work *w, const socgpu_cld *cld, int ndp, int ict, i
             for (int k = 0; k < 2; ++k)
                 for (int j = 0; j < 2; ++j)
                     if (art > tol) ao[k][j] = ao[k][j] + aru[k] * arl[j] / art;
-            double *cv = w->ovl + 8 * ((size_t)l + (size_t)wp * (size_t)i);
+            double *cv = w->ovl + OVS * ((size_t)l + (size_t)wp * (size_t)i);
             for (int k = 0; k < 2; ++k) {
                 cv[2 * k + k] = 1.0;
                 for (int j = 0; j < k; ++j) { cv[2 * j + k] = 0.0; cv[2 * k + j] = 0.0; }
@@ -1530,6 +1543,43 @@ static void overlap_coupled2(work *w, const socgpu_cld *cld, int ndp, int ict, i
     }
 }
 
+/* The two-stream coefficients of cloud type t (1-based) in cell (l, i):
+ * the clear grey optics plus the type's components, normalised and
+ * rescaled (grey_opt_prop.F90:980-1000, 1195-1240, 1475-1500,
+ * rescale_phase_fnc.F90), then single_scattering and two_coeff
+ * (two_coeff_cloud.F90, two_coeff_region.F90:275-380). */
+static void type_coeffs(const work *w, const socgpu_control *c, const double *mass, int ndp, const socgpu_cld *cld,
+                        int l, int i, int t, coeffs *o)
+{
+    const int wp = w->wp;
+    const size_t pl = (size_t)wp * w->ndl;
+    double kgt = IX2(w->k_grey_tot, l, i, wp), kes = IX2(w->k_ext_scat, l, i, wp);
+    double fwd = IX2(w->forward_scatter_nc, l, i, wp), phf = IX2(w->phase_fnc_nc, l, i, wp);
+    for (int k = 0; k < cld->n_condensed; ++k) {
+        if (cld->i_cloud_type[k] != t) continue;
+        kgt = kgt + IX2(w->k_ext_tot_cc + pl * k, l, i, wp);
+        kes = kes + IX2(w->k_ext_scat_cc + pl * k, l, i, wp);
+        fwd = fwd + IX2(w->fwd_cc + pl * k, l, i, wp);
+        phf = phf + IX2(w->phf_cc + pl * k, l, i, wp);
+    }
+    double asym = phf;
+    if (kes > TINY_R) {
+        const double inv = 1.0 / kes;
+        if (c->l_rescale) {
+            fwd = fwd * inv;
+            asym = phf * inv;
+            asym = (asym - fwd) / (1.0 - fwd);
+        } else {
+            asym = phf / kes;
+        }
+    }
+    if (!c->l_rescale) fwd = 0.0;
+    double tau, tau_dir, om;
+    single_scatter_cell(c, kgt, kes, IX2(w->k_gas_abs, l, i, wp), IX2(mass, l, i, ndp), fwd, &tau, &tau_dir, &om);
+    two_coeff_cell(c->isolir, c->i_2stream, c->i_direct_tau, c->l_ir_source_quad, asym, om, tau_dir, tau,
+                   w->sec_0[l], o);
+}
+
 /* One k-term in two regions (mix_column.F90:150-460): the clear
  * coefficients of every layer, the frac_cloud-weighted coefficients of the
  * cloud types (two_coeff_cloud.F90), the sources (ir_source with w_free and
@@ -1543,8 +1593,7 @@ static void solve_region_term(work *w, const socgpu_control *c, const socgpu_dim
     const int ict = dm->id_cloud_top - 1, ndc = w->ndl - ict, nct = w->nct;
     const int solar = (c->isolir == SOCGPU_IP_SOLAR);
     const int l_dir = (c->i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING || c->i_direct_tau == SOCGPU_IP_DIRECT_CSR_SCALING);
-    const double tiny_k = TINY_R;
-#define OV(l, i, m) (w->ovl[8 * ((size_t)(l) + (size_t)wp * (size_t)(i)) + (m)])
+#define OV(l, i, m) (w->ovl[OVS * ((size_t)(l) + (size_t)wp * (size_t)(i)) + (m)])
     clear_coefficients(w, c, mass, ndp);
     /* two_coeff_cloud */
     for (int i = nct - 1; i < n_layer; ++i)
@@ -1552,7 +1601,6 @@ static void solve_region_term(work *w, const socgpu_control *c, const socgpu_dim
             IX2(w->tc, l, i, wp) = 0.0; IX2(w->rc, l, i, wp) = 0.0; IX2(w->t0c, l, i, wp) = 0.0;
             IX2(w->t0dc, l, i, wp) = 0.0; IX2(w->sc1c, l, i, wp) = 0.0; IX2(w->sc2c, l, i, wp) = 0.0;
         }
-    const size_t pl = (size_t)wp * w->ndl;
     for (int t = 1; t <= cld->n_cloud_type; ++t)
         for (int i = nct - 1; i < n_layer; ++i)
             for (int l = 0; l < n_profile; ++l) {
@@ -1560,36 +1608,8 @@ static void solve_region_term(work *w, const socgpu_control *c, const socgpu_dim
                 const size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
                 const double fc = cld->frac_cloud[qc + (size_t)ndp * ndc * (size_t)(t - 1)];
                 if (!(fc > 0.0) || !(cld->w_cloud[qc] > 0.0)) continue;
-                /* the type's optical properties (grey_opt_prop.F90:980-1000,
-                 * 1195-1240), normalised and rescaled (1475-1500,
-                 * rescale_phase_fnc.F90) */
-                double kgt = IX2(w->k_grey_tot, l, i, wp), kes = IX2(w->k_ext_scat, l, i, wp);
-                double fwd = IX2(w->forward_scatter_nc, l, i, wp), phf = IX2(w->phase_fnc_nc, l, i, wp);
-                for (int k = 0; k < cld->n_condensed; ++k) {
-                    if (cld->i_cloud_type[k] != t) continue;
-                    kgt = kgt + IX2(w->k_ext_tot_cc + pl * k, l, i, wp);
-                    kes = kes + IX2(w->k_ext_scat_cc + pl * k, l, i, wp);
-                    fwd = fwd + IX2(w->fwd_cc + pl * k, l, i, wp);
-                    phf = phf + IX2(w->phf_cc + pl * k, l, i, wp);
-                }
-                double asym = phf;
-                if (kes > tiny_k) {
-                    const double inv = 1.0 / kes;
-                    if (c->l_rescale) {
-                        fwd = fwd * inv;
-                        asym = phf * inv;
-                        asym = (asym - fwd) / (1.0 - fwd);
-                    } else {
-                        asym = phf / kes;
-                    }
-                }
-                if (!c->l_rescale) fwd = 0.0;
-                double tau, tau_dir, om;
-                single_scatter_cell(c, kgt, kes, IX2(w->k_gas_abs, l, i, wp), IX2(mass, l, i, ndp), fwd,
-                                    &tau, &tau_dir, &om);
                 coeffs o;
-                two_coeff_cell(c->isolir, c->i_2stream, c->i_direct_tau, c->l_ir_source_quad, asym, om, tau_dir, tau,
-                               w->sec_0[l], &o);
+                type_coeffs(w, c, mass, ndp, cld, l, i, t, &o);
                 IX2(w->tc, l, i, wp) = IX2(w->tc, l, i, wp) + fc * o.trans;
                 IX2(w->rc, l, i, wp) = IX2(w->rc, l, i, wp) + fc * o.reflect;
                 IX2(w->sc1c, l, i, wp) = IX2(w->sc1c, l, i, wp) + fc * o.sc1;
@@ -1826,6 +1846,345 @@ static void solve_region_term(work *w, const socgpu_control *c, const socgpu_dim
 #undef OV
 }
 
+/* Clouds in three regions, clear (1), stratiform (2) and convective (3)
+ * (triple_column.F90), for ip_cloud_triple with ip_solver_triple_hogan.
+ * Layers are 1-based in the comments and 0-based in the arrays; interface
+ * i lies below layer i (0: the top). */
+
+/* aggregate_cloud (aggregate_cloud.F90:107-160): the region of cloud type t
+ * (1-based).  Stratiform water and ice, then convective water and ice
+ * (csiw, split_ice_water); or stratiform, then convective (conv_strat,
+ * split_homogen). */
+static int region_of_type(int rep, int t)
+{
+    if (rep == SOCGPU_IP_CLOUD_CSIW || rep == SOCGPU_IP_CLOUD_SPLIT_ICE_WATER)
+        return (t == SOCGPU_IP_CLOUD_TYPE_SW || t == SOCGPU_IP_CLOUD_TYPE_SI) ? 2 : 3;
+    return t == SOCGPU_IP_CLOUD_TYPE_STRAT ? 2 : 3;
+}
+
+/* The regions' shares of the cloud (frac_region, aggregate_cloud.F90) and
+ * overlap_coupled (overlap_coupled.F90:150-450) for three regions with
+ * like regions maximally overlapped (ip_cloud_triple): at each interface
+ * i = nct-1 .. n_layer the fraction v_jk of upper region k going into lower
+ * region j (ovl[3 j + k], cloud_overlap(:, i, 3 j + k + 1)) and the fraction
+ * u_jk of lower region k going into upper region j (ovl[9 + 3 j + k]). */
+static void overlap_coupled3(work *w, const socgpu_control *c, const socgpu_cld *cld, int ndp, int ict)
+{
+    const int n_layer = w->n_layer, wp = w->wp, nct = w->nct, ndc = w->ndl - ict;
+    const double tol = 1.0e+02 * EPS_R;
+    for (int i = 0; i < n_layer; ++i)
+        for (int l = 0; l < w->n_profile; ++l) {
+            double f2 = 0.0, f3 = 0.0;
+            if (i >= ict)
+                for (int t = 1; t <= cld->n_cloud_type; ++t) {
+                    const double fc = cld->frac_cloud[(size_t)l + (size_t)ndp * ((size_t)(i - ict) + (size_t)ndc * (t - 1))];
+                    if (region_of_type(c->i_cloud_representation, t) == 2) f2 = f2 + fc; else f3 = f3 + fc;
+                }
+            IX2(w->fr2, l, i, wp) = f2;
+            IX2(w->fr3, l, i, wp) = f3;
+        }
+    for (int l = 0; l < w->n_profile; ++l) {
+        double au[3] = {1.0, 0.0, 0.0};
+        for (int i = nct - 1; i <= n_layer; ++i) {
+            double al[3], ao[3][3];
+            if (i < n_layer) {
+                const double wc = cloud_w(cld, ndp, ict, l, i + 1);
+                al[0] = 1.0 - wc;
+                al[1] = wc * IX2(w->fr2, l, i, wp);
+                al[2] = wc * IX2(w->fr3, l, i, wp);
+            } else {
+                al[0] = 1.0; al[1] = 0.0; al[2] = 0.0;
+            }
+            for (int k = 0; k < 3; ++k) ao[k][k] = 1.0 * (al[k] < au[k] ? al[k] : au[k]);
+            for (int k = 0; k < 3; ++k)
+                for (int j = 0; j < k; ++j) { ao[k][j] = 0.0; ao[j][k] = 0.0; }
+            double art = 1.0 - ao[0][0];
+            for (int k = 1; k < 3; ++k) art = art - ao[k][k];
+            double aru[3], arl[3];
+            for (int k = 0; k < 3; ++k) {
+                aru[k] = au[k] - ao[k][k];
+                arl[k] = al[k] - ao[k][k];
+            }
+            for (int k = 0; k < 3; ++k)
+                for (int j = 0; j < 3; ++j)
+                    if (art > tol) ao[k][j] = ao[k][j] + aru[k] * arl[j] / art;
+            double *cv = w->ovl + OVS * ((size_t)l + (size_t)wp * (size_t)i);
+            for (int k = 0; k < 3; ++k) {
+                cv[3 * k + k] = 1.0;
+                for (int j = 0; j < k; ++j) { cv[3 * j + k] = 0.0; cv[3 * k + j] = 0.0; }
+            }
+            for (int k = 0; k < 3; ++k)
+                if (au[k] > tol)
+                    for (int j = 0; j < 3; ++j) cv[3 * j + k] = ao[k][j] / au[k];
+            for (int k = 0; k < 3; ++k) {
+                cv[9 + 3 * k + k] = 1.0;
+                for (int j = 0; j < k; ++j) { cv[9 + 3 * j + k] = 0.0; cv[9 + 3 * k + j] = 0.0; }
+            }
+            for (int k = 0; k < 3; ++k)
+                if (al[k] > tol)
+                    for (int j = 0; j < 3; ++j) cv[9 + 3 * j + k] = ao[j][k] / al[k];
+            if (i < n_layer) { au[0] = al[0]; au[1] = al[1]; au[2] = al[2]; }
+        }
+    }
+}
+
+/* One k-term in three regions (triple_column.F90:260-560): the clear
+ * coefficients of every layer, each cloudy region's coefficients as the
+ * frac_cloud-weighted sum over its cloud types divided by its share
+ * (two_coeff_region.F90:230-440), the infra-red sources weighted by the
+ * regions' areas or triple_solar_source.F90, the ground sources and
+ * solver_triple_hogan.F90.  Leaves flux_total and flux_direct as
+ * column_solve does. */
+static void solve_triple_term(work *w, const socgpu_control *c, const socgpu_dimen *dm, const double *mass,
+                              const socgpu_cld *cld)
+{
+    const int n_profile = w->n_profile, n_layer = w->n_layer, wp = w->wp, ndp = dm->nd_profile;
+    const int ict = dm->id_cloud_top - 1, ndc = w->ndl - ict, nct = w->nct;
+    const int solar = (c->isolir == SOCGPU_IP_SOLAR);
+    const int l_dir = (c->i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING || c->i_direct_tau == SOCGPU_IP_DIRECT_CSR_SCALING);
+#define OV3(l, i, m) (w->ovl[OVS * ((size_t)(l) + (size_t)wp * (size_t)(i)) + (m)])
+    /* region k's arrays: 1 the clear, 2 the stratiform, 3 the convective */
+    double *T[4] = {NULL, w->trans, w->tc, w->tv}, *Rr[4] = {NULL, w->reflect, w->rc, w->rv};
+    double *T0[4] = {NULL, w->trans_0, w->t0c, w->t0v}, *T0D[4] = {NULL, w->trans_0_dir, w->t0dc, w->t0dv};
+    double *S1[4] = {NULL, w->sc1, w->sc1c, w->sc1v}, *S2[4] = {NULL, w->sc2, w->sc2c, w->sc2v};
+    double *SU[4] = {NULL, w->s_up, w->s_up_c, w->s_up_v}, *SD[4] = {NULL, w->s_down, w->s_down_c, w->s_down_v};
+    double *FR[4] = {NULL, NULL, w->fr2, w->fr3};
+    clear_coefficients(w, c, mass, ndp);
+    for (int k = 2; k <= 3; ++k)
+        for (int i = nct - 1; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                IX2(T[k], l, i, wp) = 0.0; IX2(Rr[k], l, i, wp) = 0.0; IX2(T0[k], l, i, wp) = 0.0;
+                IX2(T0D[k], l, i, wp) = 0.0; IX2(S1[k], l, i, wp) = 0.0; IX2(S2[k], l, i, wp) = 0.0;
+            }
+    for (int t = 1; t <= cld->n_cloud_type; ++t) {
+        const int k = region_of_type(c->i_cloud_representation, t);
+        for (int i = nct - 1; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                if (i < ict) continue;
+                const size_t qc = (size_t)l + (size_t)ndp * (size_t)(i - ict);
+                const double fc = cld->frac_cloud[qc + (size_t)ndp * ndc * (size_t)(t - 1)];
+                if (!(fc > TINY_R) || !(cld->w_cloud[qc] > 0.0)) continue;
+                coeffs o;
+                type_coeffs(w, c, mass, ndp, cld, l, i, t, &o);
+                IX2(T[k], l, i, wp) = IX2(T[k], l, i, wp) + fc * o.trans;
+                IX2(Rr[k], l, i, wp) = IX2(Rr[k], l, i, wp) + fc * o.reflect;
+                IX2(S1[k], l, i, wp) = IX2(S1[k], l, i, wp) + fc * o.sc1;
+                if (solar || c->l_ir_source_quad) IX2(S2[k], l, i, wp) = IX2(S2[k], l, i, wp) + fc * o.sc2;
+                if (solar) {
+                    IX2(T0[k], l, i, wp) = IX2(T0[k], l, i, wp) + fc * o.trans_0;
+                    if (l_dir) IX2(T0D[k], l, i, wp) = IX2(T0D[k], l, i, wp) + fc * o.trans_0_dir;
+                }
+            }
+    }
+    for (int k = 2; k <= 3; ++k)
+        for (int i = nct - 1; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                const double fr = IX2(FR[k], l, i, wp);
+                if (!(fr > TINY_R)) continue;
+                const double inv = 1.0 / fr;
+                IX2(T[k], l, i, wp) = IX2(T[k], l, i, wp) * inv;
+                IX2(Rr[k], l, i, wp) = IX2(Rr[k], l, i, wp) * inv;
+                if (solar) {
+                    IX2(T0[k], l, i, wp) = IX2(T0[k], l, i, wp) * inv;
+                    if (l_dir) IX2(T0D[k], l, i, wp) = IX2(T0D[k], l, i, wp) * inv;
+                }
+                IX2(S1[k], l, i, wp) = IX2(S1[k], l, i, wp) * inv;
+                if (solar || c->l_ir_source_quad) IX2(S2[k], l, i, wp) = IX2(S2[k], l, i, wp) * inv;
+            }
+    /* sources */
+    double *fd = w->flux_direct;
+    if (!solar) {
+        /* ir_source per region, then weighted by the areas (triple_column.F90:296-350) */
+        for (int i = 0; i < n_layer; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                const double d1 = IX2(w->planck_diff, l, i, wp), d2 = IX2(w->planck_diff_2, l, i, wp);
+                for (int k = 1; k <= 3; ++k) {
+                    if (k > 1 && i < nct - 1) continue;
+                    double su, sd;
+                    if (c->l_ir_source_quad) {
+                        su = IX2(S1[k], l, i, wp) * d1 + IX2(S2[k], l, i, wp) * d2;
+                        sd = -IX2(S1[k], l, i, wp) * d1 + IX2(S2[k], l, i, wp) * d2;
+                    } else {
+                        su = IX2(S1[k], l, i, wp) * d1;
+                        sd = -su;
+                    }
+                    if (i >= nct - 1) {
+                        const double wc = cloud_w(cld, ndp, ict, l, i + 1);
+                        const double a = (k == 1) ? 1.0 - wc : wc * IX2(FR[k], l, i, wp);
+                        su = a * su; sd = a * sd;
+                    }
+                    IX2(SU[k], l, i, wp) = su; IX2(SD[k], l, i, wp) = sd;
+                }
+            }
+    } else {
+        /* triple_solar_source (triple_solar_source.F90:160-400) */
+        const double *adj = w->adj;
+        for (int l = 0; l < n_profile; ++l) {
+            IX2(fd, l, 0, wp) = w->flux_inc_direct[l];
+            if (l_dir) IX2(w->flux_direct_dir, l, 0, wp) = w->flux_inc_direct[l];
+        }
+        for (int i = 1; i <= nct - 1; ++i)
+            for (int l = 0; l < n_profile; ++l) {
+                const int ii = i - 1;
+                const double f0 = IX2(fd, l, i - 1, wp), t0 = IX2(w->trans_0, l, ii, wp);
+                if (adj) {
+                    IX2(fd, l, i, wp) = f0 * t0 * IX2(adj, l, ii, wp);
+                    IX2(w->s_up, l, ii, wp) = IX2(w->sc1, l, ii, wp) * f0;
+                    IX2(w->s_down, l, ii, wp) = (IX2(w->sc2, l, ii, wp) - t0) * f0 + IX2(fd, l, i, wp);
+                } else {
+                    IX2(fd, l, i, wp) = f0 * t0;
+                    IX2(w->s_up, l, ii, wp) = IX2(w->sc1, l, ii, wp) * f0;
+                    IX2(w->s_down, l, ii, wp) = IX2(w->sc2, l, ii, wp) * f0;
+                }
+                if (l_dir) {
+                    double v = IX2(w->flux_direct_dir, l, i - 1, wp) * IX2(w->trans_0_dir, l, ii, wp);
+                    if (adj) v = v * IX2(adj, l, ii, wp);
+                    IX2(w->flux_direct_dir, l, i, wp) = v;
+                }
+            }
+        for (int l = 0; l < n_profile; ++l) {
+            double base[3] = {IX2(fd, l, nct - 1, wp), 0.0, 0.0};
+            for (int i = nct; i <= n_layer; ++i) {
+                const int ii = i - 1;
+                double top[3];
+                for (int j = 0; j < 3; ++j)
+                    top[j] = OV3(l, i - 1, 3 * j) * base[0] + OV3(l, i - 1, 3 * j + 1) * base[1]
+                           + OV3(l, i - 1, 3 * j + 2) * base[2];
+                for (int k = 1; k <= 3; ++k) {
+                    const double t0 = IX2(T0[k], l, ii, wp);
+                    if (adj) {
+                        base[k - 1] = top[k - 1] * t0 * IX2(adj, l, ii, wp);
+                        IX2(SU[k], l, ii, wp) = IX2(S1[k], l, ii, wp) * top[k - 1];
+                        IX2(SD[k], l, ii, wp) = (IX2(S2[k], l, ii, wp) - t0) * top[k - 1] + base[k - 1];
+                    } else {
+                        base[k - 1] = top[k - 1] * t0;
+                        IX2(SU[k], l, ii, wp) = IX2(S1[k], l, ii, wp) * top[k - 1];
+                        IX2(SD[k], l, ii, wp) = IX2(S2[k], l, ii, wp) * top[k - 1];
+                    }
+                }
+                IX2(fd, l, i, wp) = base[0] + base[1] + base[2];
+            }
+            w->alpha[l] = base[0]; w->fdg2[l] = base[1]; w->fdg3[l] = base[2];
+            if (l_dir) {
+                double db[3] = {IX2(w->flux_direct_dir, l, nct - 1, wp), 0.0, 0.0};
+                for (int i = nct; i <= n_layer; ++i) {
+                    const int ii = i - 1;
+                    double top[3];
+                    for (int j = 0; j < 3; ++j)
+                        top[j] = OV3(l, i - 1, 3 * j) * db[0] + OV3(l, i - 1, 3 * j + 1) * db[1]
+                               + OV3(l, i - 1, 3 * j + 2) * db[2];
+                    for (int k = 1; k <= 3; ++k) {
+                        double v = top[k - 1] * IX2(T0D[k], l, ii, wp);
+                        if (adj) v = v * IX2(adj, l, ii, wp);
+                        db[k - 1] = v;
+                    }
+                    IX2(w->flux_direct_dir, l, i, wp) = db[0] + db[1] + db[2];
+                }
+                for (int i = 0; i <= n_layer; ++i) IX2(fd, l, i, wp) = IX2(w->flux_direct_dir, l, i, wp);
+                w->alpha[l] = db[0]; w->fdg2[l] = db[1]; w->fdg3[l] = db[2];
+            }
+        }
+    }
+    /* ground sources (triple_column.F90:380-410) */
+    for (int l = 0; l < n_profile; ++l) {
+        if (solar) {
+            const double a = w->alb_dir[l] - w->alb_diff[l];
+            w->source_ground[l] = a * w->alpha[l];
+            w->sg2[l] = a * w->fdg2[l];
+            w->sg3[l] = a * w->fdg3[l];
+        } else {
+            const double e = (1.0 - w->alb_diff[l]) * w->d_planck_flux_surface[l];
+            w->source_ground[l] = OV3(l, n_layer, 9) * e;
+            w->sg2[l] = OV3(l, n_layer, 12) * e;
+            w->sg3[l] = OV3(l, n_layer, 15) * e;
+        }
+    }
+    /* solver_triple_hogan (solver_triple_hogan.F90:200-410), v_jk = ovl 3 j + k,
+     * u_jk = ovl 9 + 3 j + k (0-based regions) */
+    double *B[4] = {NULL, w->b11, w->b22, w->b33}, *G[4] = {NULL, w->g11, w->g22, w->g33};
+    double *H[4] = {NULL, w->h1, w->h2, w->h3};
+    double *ft = w->flux_total;
+    for (int l = 0; l < n_profile; ++l) {
+        double a[4] = {0.0, 0.0, 0.0, 0.0}, g[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int i = n_layer + 1; i >= 1; --i) {
+            const int ii = i - 1;
+            if (i < n_layer + 1 && i >= nct) {
+                double th[4], lam[4];
+                for (int k = 1; k <= 3; ++k)
+                    th[k] = a[1] * OV3(l, i, k - 1) + a[2] * OV3(l, i, 3 + k - 1) + a[3] * OV3(l, i, 6 + k - 1);
+                for (int k = 1; k <= 3; ++k) {
+                    const double r = IX2(Rr[k], l, ii, wp), t = IX2(T[k], l, ii, wp);
+                    const double b = 1.0 / (1.0 - th[k] * r);
+                    IX2(B[k], l, ii, wp) = b;
+                    IX2(G[k], l, ii, wp) = th[k] * t;
+                    IX2(H[k], l, ii, wp) = g[k] + th[k] * IX2(SD[k], l, ii, wp);
+                    lam[k] = IX2(SU[k], l, ii, wp) + IX2(H[k], l, ii, wp) * t * b;
+                    a[k] = r + th[k] * t * t * b;
+                }
+                for (int j = 1; j <= 3; ++j)
+                    g[j] = OV3(l, i - 1, 9 + 3 * (j - 1)) * lam[1] + OV3(l, i - 1, 9 + 3 * (j - 1) + 1) * lam[2]
+                         + OV3(l, i - 1, 9 + 3 * (j - 1) + 2) * lam[3];
+            } else if (i < nct - 1) {
+                const double r = IX2(w->reflect, l, ii, wp), t = IX2(w->trans, l, ii, wp);
+                const double b11 = 1.0 / (1.0 - a[1] * r), gm11 = a[1] * t;
+                const double hh1 = g[1] + a[1] * IX2(w->s_down, l, ii, wp);
+                IX2(w->b11, l, ii, wp) = b11; IX2(w->g11, l, ii, wp) = gm11; IX2(w->h1, l, ii, wp) = hh1;
+                const double lam = t * b11;
+                a[1] = r + lam * gm11;
+                g[1] = IX2(w->s_up, l, ii, wp) + lam * hh1;
+            } else if (i == nct - 1) {
+                const double r = IX2(w->reflect, l, ii, wp), t = IX2(w->trans, l, ii, wp);
+                const double th11 = (nct < n_layer) ? a[1] * OV3(l, i, 0) + a[2] * OV3(l, i, 3) + a[3] * OV3(l, i, 6)
+                                                    : a[1];
+                const double b11 = 1.0 / (1.0 - th11 * r), gm11 = th11 * t;
+                const double hh1 = g[1] + th11 * IX2(w->s_down, l, ii, wp);
+                IX2(w->b11, l, ii, wp) = b11; IX2(w->g11, l, ii, wp) = gm11; IX2(w->h1, l, ii, wp) = hh1;
+                const double lam = t * b11;
+                a[1] = r + lam * gm11;
+                g[1] = IX2(w->s_up, l, ii, wp) + lam * hh1;
+            } else if (i == n_layer + 1) {
+                a[1] = a[2] = a[3] = w->alb_diff[l];
+                g[1] = w->source_ground[l];
+                g[2] = w->sg2[l];
+                g[3] = w->sg3[l];
+            }
+        }
+        IX2(ft, l, 1, wp) = w->flux_inc_down[l];
+        if (nct > 1) IX2(ft, l, 0, wp) = a[1] * IX2(ft, l, 1, wp) + g[1];
+        else IX2(ft, l, 0, wp) = g[1] + w->flux_inc_down[l] * (OV3(l, 0, 0) * a[1] + OV3(l, 0, 3) * a[2]
+                                                              + OV3(l, 0, 6) * a[3]);
+        for (int i = 1; i <= nct - 1; ++i) {
+            const int ii = i - 1;
+            IX2(ft, l, 2 * i, wp) = (IX2(w->g11, l, ii, wp) * IX2(ft, l, 2 * i - 1, wp) + IX2(w->h1, l, ii, wp))
+                * IX2(w->b11, l, ii, wp);
+            IX2(ft, l, 2 * i + 1, wp) = IX2(w->trans, l, ii, wp) * IX2(ft, l, 2 * i - 1, wp)
+                + IX2(w->reflect, l, ii, wp) * IX2(ft, l, 2 * i, wp) + IX2(w->s_down, l, ii, wp);
+        }
+        double fdn[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int i = nct; i <= n_layer; ++i) {
+            const int ii = i - 1;
+            double d[4];
+            if (i > nct) {
+                for (int j = 1; j <= 3; ++j)
+                    d[j] = OV3(l, i - 1, 3 * (j - 1)) * fdn[1] + OV3(l, i - 1, 3 * (j - 1) + 1) * fdn[2]
+                         + OV3(l, i - 1, 3 * (j - 1) + 2) * fdn[3];
+            } else {
+                for (int j = 1; j <= 3; ++j) d[j] = OV3(l, i - 1, 3 * (j - 1)) * IX2(ft, l, 2 * i - 1, wp);
+            }
+            double fu_sum = 0.0, fd_sum = 0.0;
+            for (int k = 1; k <= 3; ++k) {
+                const double fu = (IX2(G[k], l, ii, wp) * d[k] + IX2(H[k], l, ii, wp)) * IX2(B[k], l, ii, wp);
+                fdn[k] = IX2(T[k], l, ii, wp) * d[k] + IX2(Rr[k], l, ii, wp) * fu + IX2(SD[k], l, ii, wp);
+                fu_sum = fu_sum + fu;
+                fd_sum = fd_sum + fdn[k];
+            }
+            IX2(ft, l, 2 * i, wp) = fu_sum;
+            IX2(ft, l, 2 * i + 1, wp) = fd_sum;
+        }
+    }
+#undef OV3
+}
+
 /* --------------------------------------------------------------------- */
 static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
                          const socgpu_atm *atm, const socgpu_dimen *dm, const socgpu_cld *cld,
@@ -1844,7 +2203,16 @@ static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
         if (two_coeff_basic(c->i_2stream, 0.5, 0.5, &s, &t) != SOCGPU_I_NORMAL) {
             set_msg(msg, msg_len, "unrecognised or unimplemented two-stream scheme"); return SOCGPU_I_ERR_FATAL; }
         const int region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM);
-        if (!region && c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
+        const int triple = (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE);
+        if (triple && c->i_solver != SOCGPU_IP_SOLVER_TRIPLE_HOGAN) {
+            set_msg(msg, msg_len, "three cloud regions require solver_triple_hogan"); return SOCGPU_I_ERR_FATAL; }
+        if (triple && c->i_cloud_representation != SOCGPU_IP_CLOUD_CONV_STRAT &&
+            c->i_cloud_representation != SOCGPU_IP_CLOUD_CSIW && c->i_cloud_representation != SOCGPU_IP_CLOUD_SPLIT_HOMOGEN &&
+            c->i_cloud_representation != SOCGPU_IP_CLOUD_SPLIT_ICE_WATER) {
+            set_msg(msg, msg_len, "This representation of clouds is not compatible with separate convective and "
+                                  "stratiform overlap.");
+            return SOCGPU_I_ERR_FATAL; }
+        if (!region && !triple && c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
             set_msg(msg, msg_len, "scattering requires solver_homogen_direct"); return SOCGPU_I_ERR_FATAL; }
         if (region && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN) {
             set_msg(msg, msg_len, "cloud regions require solver_mix_direct or solver_mix_direct_hogan");
@@ -1855,18 +2223,21 @@ static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
     } else {
         set_msg(msg, msg_len, "unsupported scattering method"); return SOCGPU_I_ERR_FATAL; }
     if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA &&
-        c->i_cloud != SOCGPU_IP_CLOUD_MIX_MAX && c->i_cloud != SOCGPU_IP_CLOUD_MIX_RANDOM) {
-        set_msg(msg, msg_len, "only clear-sky, McICA and two-region cloud schemes are supported"); return SOCGPU_I_ERR_FATAL; }
+        c->i_cloud != SOCGPU_IP_CLOUD_MIX_MAX && c->i_cloud != SOCGPU_IP_CLOUD_MIX_RANDOM &&
+        c->i_cloud != SOCGPU_IP_CLOUD_TRIPLE) {
+        set_msg(msg, msg_len, "only clear-sky, McICA and two- and three-region cloud schemes are supported");
+        return SOCGPU_I_ERR_FATAL; }
     if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR &&
         (!cld || cld->n_condensed < 1 || !cld->type_condensed || !cld->i_cloud_type || !cld->i_condensed_param ||
          !cld->i_condensed_type || !cld->condensed_mix_ratio || !cld->condensed_dim_char || !cld->w_cloud ||
-         !cld->frac_cloud || cld->n_cloud_type < 1 || cld->n_cloud_type > 2)) {
+         !cld->frac_cloud || cld->n_cloud_type < 1 ||
+         cld->n_cloud_type > (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE ? 4 : 2))) {
         set_msg(msg, msg_len, "clouds require cloud fields"); return SOCGPU_I_ERR_FATAL; }
     if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA &&
         (!cld->c_sub || !cld->frac_cloudy || !cld->subcol_k || !cld->first_subcol_k || !cld->subcol_reorder)) {
         set_msg(msg, msg_len, "McICA requires the subcolumn fields"); return SOCGPU_I_ERR_FATAL; }
-    if ((c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM) &&
-        c->i_scatter_method != SOCGPU_IP_SCATTER_FULL) {
+    if ((c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM ||
+         c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE) && c->i_scatter_method != SOCGPU_IP_SCATTER_FULL) {
         set_msg(msg, msg_len, "cloud regions require full scattering"); return SOCGPU_I_ERR_FATAL; }
     if (c->first_band < 1 || c->last_band > d->n_band || c->first_band > c->last_band) {
         set_msg(msg, msg_len, "band range outside the spectrum"); return SOCGPU_I_ERR_RANGE; }
@@ -1896,7 +2267,8 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
     if (np <= 0) return SOCGPU_I_NORMAL;
     int ndp = dm->nd_profile, ndl = dm->nd_layer, n_layer = atm0->n_layer;
     int l_cloud = (c->i_cloud == SOCGPU_IP_CLOUD_MCICA);
-    int l_region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM);
+    int l_triple = (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE);
+    int l_region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM) || l_triple;
     int ict = dm->id_cloud_top - 1;
 
     /* views shifted to the first profile of the segment */
@@ -1945,9 +2317,11 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
     lookup_fac_init(&lf, c, d, &atm, np, n_layer, ndp, wp, ndl);
     double *kterm = zalloc((size_t)wp * ndl), *k_eqv = zalloc((size_t)wp * ndl), *adj = zalloc((size_t)wp * ndl);
     if (l_region) {
-        /* set_cloud_geometry and overlap_coupled (radiance_calc.F90:640-700) */
+        /* set_cloud_geometry, aggregate_cloud and overlap_coupled
+         * (radiance_calc.F90:640-700) */
         w.nct = cloud_top(cld, ndp, ict, np, n_layer);
-        overlap_coupled2(&w, cld, ndp, ict, c->i_cloud);
+        if (l_triple) overlap_coupled3(&w, c, cld, ndp, ict);
+        else overlap_coupled2(&w, cld, ndp, ict, c->i_cloud);
     }
 
     /* zero the outputs (augment_radiance's l_initial branch is equivalent) */
@@ -2085,6 +2459,8 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
             if (status != SOCGPU_I_NORMAL) { set_msg(msg, msg_len, "illegal type of scaling"); break; }
             if (l_cloud) {
                 solve_mcica_term(&w, c, dm, d, atm.mass, cld, b, n_abs > 0 ? iex_of[0] : 0);
+            } else if (l_triple) {
+                solve_triple_term(&w, c, dm, atm.mass, cld);
             } else if (l_region) {
                 solve_region_term(&w, c, dm, atm.mass, cld);
             } else {

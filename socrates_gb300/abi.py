@@ -22,6 +22,9 @@ IP_SOLVER_NO_SCAT, IP_SOLVER_HOMOGEN_DIRECT = 2, 13
 IP_CLOUD_CLEAR, IP_CLOUD_MCICA = 5, 10
 IP_CLOUD_MIX_MAX, IP_CLOUD_MIX_RANDOM = 2, 4
 IP_SOLVER_MIX_DIRECT, IP_SOLVER_MIX_DIRECT_HOGAN = 11, 16
+IP_CLOUD_TRIPLE, IP_SOLVER_TRIPLE_HOGAN = 6, 17      # three regions: clear, stratiform, convective
+IP_CLOUD_TYPE_STRAT, IP_CLOUD_TYPE_CONV = 1, 2
+IP_CLOUD_TYPE_SW, IP_CLOUD_TYPE_SI, IP_CLOUD_TYPE_CW, IP_CLOUD_TYPE_CI = 1, 2, 3, 4
 IP_CLOUD_HOMOGEN = 1
 IP_CLOUD_ICE_WATER = 2
 IP_CLOUD_TYPE_WATER, IP_CLOUD_TYPE_ICE = 1, 2

@@ -677,11 +677,22 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
         return SOCGPU_I_ERR_FATAL;
       }
   }
-  const bool region = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
+  const bool triple = c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE;
+  const bool region = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || triple;
   if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
     if (!region && c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
       set_msg(msg, msg_len, "scattering requires solver_homogen_direct"); return SOCGPU_I_ERR_FATAL; }
-    if (region && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN) {
+    if (triple && c->i_solver != SOCGPU_IP_SOLVER_TRIPLE_HOGAN) {
+      set_msg(msg, msg_len, "three cloud regions require solver_triple_hogan"); return SOCGPU_I_ERR_FATAL; }
+    if (triple && c->i_cloud_representation != SOCGPU_IP_CLOUD_CONV_STRAT &&
+        c->i_cloud_representation != SOCGPU_IP_CLOUD_CSIW && c->i_cloud_representation != SOCGPU_IP_CLOUD_SPLIT_HOMOGEN &&
+        c->i_cloud_representation != SOCGPU_IP_CLOUD_SPLIT_ICE_WATER) {
+      // aggregate_cloud.F90:155-160
+      set_msg(msg, msg_len, "This representation of clouds is not compatible with separate convective and "
+                            "stratiform overlap.");
+      return SOCGPU_I_ERR_FATAL; }
+    if (region && !triple && c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT &&
+        c->i_solver != SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN) {
       set_msg(msg, msg_len, "cloud regions require solver_mix_direct or solver_mix_direct_hogan");
       return SOCGPU_I_ERR_FATAL; }
   } else if (c->i_scatter_method == SOCGPU_IP_NO_SCATTER_ABS || c->i_scatter_method == SOCGPU_IP_NO_SCATTER_EXT) {
@@ -701,7 +712,7 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
   if (c->l_rescale && c->n_order_forward < 1) {
     set_msg(msg, msg_len, "n_order_forward must be positive"); return SOCGPU_I_ERR_FATAL; }
   if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA && !region) {
-    set_msg(msg, msg_len, "only clear-sky, McICA and two-region cloud schemes are supported");
+    set_msg(msg, msg_len, "only clear-sky, McICA and two- and three-region cloud schemes are supported");
     return SOCGPU_I_ERR_FATAL; }
   if (c->precision != SOCGPU_PRECISION_FP64 && c->precision != SOCGPU_PRECISION_MIXED) {
     set_msg(msg, msg_len, "unknown precision %d", c->precision); return SOCGPU_I_ERR_FATAL; }
@@ -816,7 +827,8 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     if (!cld || !cld->type_condensed || !cld->i_cloud_type || !cld->i_condensed_param || !cld->i_condensed_type ||
         !cld->condensed_mix_ratio || !cld->condensed_dim_char || !cld->w_cloud || !cld->frac_cloud) {
       set_msg(msg, msg_len, "clouds require cloud fields"); return SOCGPU_I_ERR_FATAL; }
-    if (cld->n_condensed < 1 || cld->n_condensed > kMaxCloudComp || cld->n_cloud_type < 1 || cld->n_cloud_type > 2) {
+    if (cld->n_condensed < 1 || cld->n_condensed > kMaxCloudComp || cld->n_cloud_type < 1 ||
+        cld->n_cloud_type > (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE ? 4 : 2)) {
       set_msg(msg, msg_len, "cloud components/types outside the supported range"); return SOCGPU_I_ERR_RANGE; }
     if (dm->id_cloud_top < 1 || dm->id_cloud_top > atm->n_layer) {
       set_msg(msg, msg_len, "id_cloud_top outside the column"); return SOCGPU_I_ERR_RANGE; }
@@ -888,10 +900,19 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
   p.l_ir_source_quad = c->l_ir_source_quad; p.l_rayleigh = c->l_rayleigh; p.l_gas = c->l_gas;
   p.l_aerosol_mode = c->l_aerosol_mode && aer && aer->n_mode > 0; p.l_flux_div = c->l_flux_div;
   p.first_band = c->first_band; p.last_band = c->last_band;
-  p.region = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
+  p.triple = c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE;
+  p.region = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || p.triple;
   p.mcica = c->i_cloud == SOCGPU_IP_CLOUD_MCICA || p.region;
-  p.solver_hogan = c->i_solver == SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN;
-  p.mix_max = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX;
+  p.solver_hogan = c->i_solver == SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN || c->i_solver == SOCGPU_IP_SOLVER_TRIPLE_HOGAN;
+  // like regions overlap maximally under ip_cloud_triple (overlap_coupled.F90:192-198)
+  p.mix_max = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || p.triple;
+  // aggregate_cloud (aggregate_cloud.F90:107-155): stratiform water and
+  // ice then convective water and ice, or stratiform then convective
+  for (int t = 0; t < 4; ++t) {
+    const bool four = c->i_cloud_representation == SOCGPU_IP_CLOUD_CSIW ||
+                      c->i_cloud_representation == SOCGPU_IP_CLOUD_SPLIT_ICE_WATER;
+    p.type_region[t] = four ? (t < 2 ? 2 : 3) : (t == 0 ? 2 : 3);
+  }
   p.l_continuum = c->l_continuum && sp->dev.has_continuum;
   p.l_mixing_ratio = c->l_mixing_ratio;
   p.i_water = sp->dev.index_water - 1;
@@ -1018,7 +1039,7 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
 int mode_index(const socgpu_control *c) {
   // McICA and cloud regions share the kernels that stage cloud optics
   if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA || c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX ||
-      c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM)
+      c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE)
     return 2;
   return c->i_scatter_method == SOCGPU_IP_SCATTER_FULL ? 1 : 0;
 }
@@ -1071,7 +1092,7 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
   const size_t nb = s->dev.n_band, ns = std::max(1, s->dev.n_species);
   sw = c->isolir == SOCGPU_IP_SOLAR;
   mc = c->i_cloud == SOCGPU_IP_CLOUD_MCICA || c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX ||
-       c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
+       c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE;
   aero = c->l_aerosol_mode && ae && ae->n_mode > 0;
   const size_t D = sizeof(double), none = (size_t)-1;
   // inputs: (nd_profile, rows) arrays copied with their valid profiles only;

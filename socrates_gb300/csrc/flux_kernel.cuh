@@ -163,7 +163,8 @@ struct SmemLayout {
   size_t off_phf_nc, off_fwd_nc, off_c_ke, off_c_ks, off_c_ka, off_c_phf, off_c_fwd;
   size_t off_wcld, off_frac, off_csub;
   size_t off_aux, off_lkf, off_lki, off_sbf, off_sbj, off_kscr;
-  size_t off_ovl, off_reg, off_regd, off_nct, off_t0d;
+  size_t off_ovl, off_reg, off_regd, off_nct, off_t0d, off_frr;
+  int reg_rows, regd_rows;            // rows per group of the region solves (two or three regions)
   size_t off_acc;
   // the column's FP64 inputs, fetched into shared memory ahead of staging
   // (offsets in doubles from off_acc, whose space they share); raw_on false
@@ -180,11 +181,17 @@ enum RegRow {
   kRgFT, kRgFR, kRgFT0, kRgFC1, kRgFC2, kRgFOM,
   kRgCT, kRgCR, kRgCT0, kRgCC1, kRgCC2, kRgCOM,
   kRgFT0D, kRgCT0D,          // unscaled direct transmissions (i_direct_tau = ip_direct_noscaling)
-  kRgFU, kRgFD, kRgFDIR, kRgDIV, kRegRows
+  kRgFU, kRgFD, kRgFDIR, kRgDIV, kRegRows,
+  // three regions: the convective region's coefficients after the rows
+  // above (the stratiform region uses the cloudy rows)
+  kRgVT = kRegRows, kRgVR, kRgVT0, kRgVC1, kRgVC2, kRgVOM, kRgVT0D, kRegRows3
 };
 // The solver's elimination coefficients, kept in FP64 in every build: the
 // serial solve runs on one lane in FP64 from the coefficients of the layers.
-enum RegDRow { kRgB11, kRgB21, kRgB22, kRgG11, kRgG12, kRgG21, kRgG22, kRgH1, kRgH2, kRegDRows };
+enum RegDRow { kRgB11, kRgB21, kRgB22, kRgG11, kRgG12, kRgG21, kRgG22, kRgH1, kRgH2, kRegDRows,
+               // three regions (Hogan's form): the convective region's
+               // elimination coefficients and its solar sources in FP64
+               kRgB33 = kRegDRows, kRgG33, kRgH3, kRgSUV, kRgSDV, kRegDRows3 };
 
 // The layout of a column of batch p: nb bands staged at a time, n_groups
 // solve groups of P lanes, LP = P*CH layer slots.
@@ -221,7 +228,7 @@ __host__ __device__ inline SmemLayout make_layout(const FluxParams &p, int LP, i
     s.off_c_phf = take((size_t)nb * n_comp * LP);
     s.off_c_fwd = take((size_t)nb * n_comp * LP);
     s.off_wcld = take(LP);
-    s.off_frac = take((size_t)2 * LP);
+    s.off_frac = take((size_t)(p.n_cloud_type > 2 ? p.n_cloud_type : 2) * LP);
     s.off_csub = take((size_t)n_sub * LP);
   }
   // equivalent extinction, solar: each minor absorber's direct-beam factor
@@ -236,10 +243,16 @@ __host__ __device__ inline SmemLayout make_layout(const FluxParams &p, int LP, i
   // cloud regions: the column's interface coefficients and cloud top, and
   // each group's rows for the serial two-region solve
   const bool region = mcica && p.region;
-  s.off_ovl = region ? take((size_t)8 * (LP + 1)) : o;
-  s.off_reg = region ? take((size_t)n_groups * kRegRows * (LP + 1)) : o;
-  s.off_regd = region ? take_dbl((size_t)n_groups * kRegDRows * (LP + 1)) : o;
+  const bool triple = region && p.triple;
+  s.reg_rows = triple ? kRegRows3 : kRegRows;
+  s.regd_rows = triple ? kRegDRows3 : kRegDRows;
+  s.off_ovl = region ? take((size_t)(triple ? 18 : 8) * (LP + 1)) : o;
+  s.off_reg = region ? take((size_t)n_groups * s.reg_rows * (LP + 1)) : o;
+  s.off_regd = region ? take_dbl((size_t)n_groups * s.regd_rows * (LP + 1)) : o;
   s.off_nct = region ? take_int(4) : o;
+  // three regions: the stratiform and convective shares of each layer's
+  // cloud (frac_region), by layer
+  s.off_frr = triple ? take((size_t)2 * LP) : o;
   // the direct beam without delta-scaling: each group's row of the layers'
   // unscaled direct transmissions
   s.off_t0d = (!lw && p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING && !region) ? take((size_t)n_groups * LP) : o;
@@ -422,7 +435,7 @@ struct FluxKernel {
     R *phf_nc, *fwd_nc, *c_ke, *c_ks, *c_ka, *c_phf, *c_fwd, *wcld, *frac, *csub;
     R *aux, *lkf, *sbf, *kscr;
     int *lki, *sbj;
-    R *ovl, *reg, *t0d;
+    R *ovl, *reg, *t0d, *frr;
     double *regd;
     int *nct;
     Acc *acc;
@@ -449,6 +462,7 @@ struct FluxKernel {
     s.ovl = (R *)(smem + l.off_ovl); s.reg = (R *)(smem + l.off_reg); s.nct = (int *)(smem + l.off_nct);
     s.regd = (double *)(smem + l.off_regd);
     s.t0d = (R *)(smem + l.off_t0d);
+    s.frr = (R *)(smem + l.off_frr);
     s.acc = (Acc *)(smem + l.off_acc);
     s.raw = l.raw_on ? (const double *)(smem + l.off_acc) : nullptr;
     s.r_p = l.r_p; s.r_t = l.r_t; s.r_mass = l.r_mass; s.r_gas = l.r_gas; s.r_mmr = l.r_mmr;
@@ -707,7 +721,10 @@ struct FluxKernel {
     if (!S.raw)
       for (int q = threadIdx.x; q < n_groups * lay.acc_stride; q += nthreads) S.acc[q] = Acc(0);
     if (MCICA) stage_cloud_column(p, S, col);
-    if (MCICA && p.region) stage_regions(p, S, col, LP);
+    if (MCICA && p.region) {
+      if (p.triple) stage_regions3(p, S, col, LP);
+      else stage_regions(p, S, col, LP);
+    }
     const int gid = threadIdx.x / P;
     const int r = threadIdx.x % P;
     const R sec0 = !p.zen_0 ? R(1) : (S.raw && S.r_alb > S.r_zen) ? raw_in<R>(S.raw[S.r_zen]) : load_in<R>(p.zen_0 + col);
@@ -1132,14 +1149,15 @@ struct FluxKernel {
     const int ndc = ndl - ict;
     for (int s = threadIdx.x; s < LP; s += blockDim.x) {
       const int i = layer_of_slot(s);
-      R w = R(0), f1 = R(0), f2 = R(0);
+      R w = R(0), f[4] = {R(0), R(0), R(0), R(0)};
       if (i < L && i >= ict) {
         size_t qc = (size_t)col + (size_t)ndp * (size_t)(i - ict);
         w = load_in<R>(p.w_cloud + qc);
-        f1 = load_in<R>(p.frac_cloud + qc);
-        if (p.n_cloud_type > 1) f2 = load_in<R>(p.frac_cloud + qc + (size_t)ndp * ndc);
+        for (int t = 0; t < p.n_cloud_type && t < 4; ++t) f[t] = load_in<R>(p.frac_cloud + qc + (size_t)ndp * ndc * t);
       }
-      S.wcld[s] = w; S.frac[s] = f1; S.frac[LP + s] = f2;
+      S.wcld[s] = w;
+      const int nt = p.n_cloud_type > 2 ? p.n_cloud_type : 2;
+      for (int t = 0; t < nt && t < 4; ++t) S.frac[(size_t)t * LP + s] = f[t];
     }
     for (int q = threadIdx.x; q < p.n_subcol_gen * LP; q += blockDim.x) {
       const int s = q % LP, sub = q / LP;
@@ -1594,6 +1612,65 @@ struct FluxKernel {
     }
   }
 
+  // set_cloud_geometry, aggregate_cloud and overlap_coupled for three
+  // regions, clear (0), stratiform (1) and convective (2), with like regions
+  // maximally overlapped (aggregate_cloud.F90:107-155, overlap_coupled.F90:
+  // 150-450), by one thread: the cloud top, each layer's stratiform and
+  // convective shares of its cloud (frr rows), and at each interface i the
+  // fraction v_jk of upper region k going into lower region j (ovl row
+  // 3 j + k) and the fraction u_jk of lower region k going into upper region
+  // j (row 9 + 3 j + k).  The interfaces above the cloud top keep the
+  // identity.
+  __device__ static void stage_regions3(const FluxParams &p, const Smem &S, int col, int LP_) {
+    if (threadIdx.x != 0) return;
+    const int L = p.n_layer, ndp = p.nd_profile, ict = p.id_ct, ndc = p.nd_layer - ict;
+    auto wc = [&](int i1) -> R {
+      return (i1 - 1 >= ict) ? load_in<R>(p.w_cloud + (size_t)col + (size_t)ndp * (size_t)(i1 - 1 - ict)) : R(0);
+    };
+    int nct = ict + 1;
+    while (nct < L && !(wc(nct) > R(0))) ++nct;
+    S.nct[0] = nct;
+    for (int i = 0; i < L; ++i) {
+      R f2 = R(0), f3 = R(0);
+      if (i >= ict)
+        for (int t = 0; t < p.n_cloud_type; ++t) {
+          const R fc = load_in<R>(p.frac_cloud + (size_t)col + (size_t)ndp * ((size_t)(i - ict) + (size_t)ndc * t));
+          if (p.type_region[t] == 2) f2 = f2 + fc; else f3 = f3 + fc;
+        }
+      S.frr[i] = f2; S.frr[LP_ + i] = f3;
+    }
+    const R tol = (R)(1.0e+02 * kEps64);
+    for (int i = 0; i < nct - 1; ++i)
+      for (int m = 0; m < 18; ++m) S.ovl[(size_t)m * (LP_ + 1) + i] = (m == 0 || m == 4 || m == 8 || m == 9 || m == 13 || m == 17) ? R(1) : R(0);
+    R au[3] = {R(1), R(0), R(0)};
+    for (int i = nct - 1; i <= L; ++i) {
+      R al[3], ao[3][3];
+      if (i < L) { const R w = wc(i + 1); al[0] = R(1) - w; al[1] = w * S.frr[i]; al[2] = w * S.frr[LP_ + i]; }
+      else { al[0] = R(1); al[1] = R(0); al[2] = R(0); }
+      for (int k = 0; k < 3; ++k) ao[k][k] = R(1) * (al[k] < au[k] ? al[k] : au[k]);
+      for (int k = 0; k < 3; ++k)
+        for (int j = 0; j < k; ++j) { ao[k][j] = R(0); ao[j][k] = R(0); }
+      R art = R(1) - ao[0][0];
+      for (int k = 1; k < 3; ++k) art = art - ao[k][k];
+      R aru[3], arl[3];
+      for (int k = 0; k < 3; ++k) { aru[k] = au[k] - ao[k][k]; arl[k] = al[k] - ao[k][k]; }
+      if (art > tol)
+        for (int k = 0; k < 3; ++k)
+          for (int j = 0; j < 3; ++j) ao[k][j] = ao[k][j] + aru[k] * arl[j] / art;
+      R v[18];
+      for (int m = 0; m < 18; ++m) v[m] = R(0);
+      for (int k = 0; k < 3; ++k) { v[3 * k + k] = R(1); v[9 + 3 * k + k] = R(1); }
+      for (int k = 0; k < 3; ++k)
+        if (au[k] > tol)
+          for (int j = 0; j < 3; ++j) v[3 * j + k] = ao[k][j] / au[k];
+      for (int k = 0; k < 3; ++k)
+        if (al[k] > tol)
+          for (int j = 0; j < 3; ++j) v[9 + 3 * j + k] = ao[j][k] / al[k];
+      for (int m = 0; m < 18; ++m) S.ovl[(size_t)m * (LP_ + 1) + i] = v[m];
+      if (i < L) { au[0] = al[0]; au[1] = al[1]; au[2] = al[2]; }
+    }
+  }
+
   // One g-point of a column in a clear and a cloudy region (mix_column.F90:
   // 150-460).  The lanes of the group compute the clear coefficients and the
   // frac_cloud-weighted coefficients of the cloud types (two_coeff_cloud.F90)
@@ -1631,14 +1708,20 @@ struct FluxKernel {
     const R *c_ke = S.c_ke + (size_t)bi * nc * LP, *c_ks = S.c_ks + (size_t)bi * nc * LP;
     const R *c_ka = S.c_ka + (size_t)bi * nc * LP, *c_ph = S.c_phf + (size_t)bi * nc * LP;
     const R *c_fw = S.c_fwd + (size_t)bi * nc * LP;
-    R *X = S.reg + (size_t)gid * kRegRows * (LP + 1);
+    R *X = S.reg + (size_t)gid * lay.reg_rows * (LP + 1);
     auto row = [&](int k) { return X + (size_t)k * (LP + 1); };
     const int nct = S.nct[0];
+    const bool triple = p.triple;
 
     R kgv[CH];
     gas_k_lane(p, S, gt, gp, bd, amt_b, r, L, kgv);
     R Tf[CH], Rff[CH], T0f[CH], c1f[CH], c2f[CH], omf[CH];
     R Tc[CH], Rc[CH], T0c[CH], c1c[CH], c2c[CH], omc[CH];
+    // three regions: the convective region's coefficients are summed in its
+    // rows of the group's scratch (the stratiform region uses Tc..), so the
+    // McICA kernels this function shares keep their registers
+    R *VT = row(kRgVT), *VR = row(kRgVR), *VT0 = row(kRgVT0), *VC1 = row(kRgVC1), *VC2 = row(kRgVC2);
+    R *VOM = row(kRgVOM);
     // the direct beam without delta-scaling (two_coeff.F90 trans_0_dir):
     // exp(-tau sec0) of the optical depth before rescaling, per region
     const bool dir_unscaled = !lw && p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING;
@@ -1650,7 +1733,11 @@ struct FluxKernel {
     for (int j = 0; j < CH; ++j) {
       const int i = r * CH + j, s = j * P + r;
       Tc[j] = R(0); Rc[j] = R(0); T0c[j] = R(0); c1c[j] = R(0); c2c[j] = R(0); omc[j] = R(0);
-      if (i < L && dir_unscaled) { row(kRgFT0D)[i] = t0_unscaled(kgt_b[s], kgv[j], S.mass[s]); row(kRgCT0D)[i] = R(0); }
+      if (triple && i < L) { VT[i] = R(0); VR[i] = R(0); VT0[i] = R(0); VC1[i] = R(0); VC2[i] = R(0); VOM[i] = R(0); }
+      if (i < L && dir_unscaled) {
+        row(kRgFT0D)[i] = t0_unscaled(kgt_b[s], kgv[j], S.mass[s]); row(kRgCT0D)[i] = R(0);
+        if (triple) row(kRgVT0D)[i] = R(0);
+      }
       if (i < L) {
         cell_coef(p, kgt_b[s], kes_b[s], kabs_b[s], kgv[j], S.mass[s], asym_b[s], fwd_b[s], sec0,
                   Tf[j], Rff[j], T0f[j], c1f[j], c2f[j], omf[j]);
@@ -1679,9 +1766,33 @@ struct FluxKernel {
             }
             R tT, tR, tT0, t1, t2, tO;
             cell_coef(p, kgt, kes, kab, kgv[j], S.mass[s], asym, fwd, sec0, tT, tR, tT0, t1, t2, tO);
-            Tc[j] = Tc[j] + fc * tT; Rc[j] = Rc[j] + fc * tR; T0c[j] = T0c[j] + fc * tT0;
-            if (dir_unscaled) row(kRgCT0D)[i] = row(kRgCT0D)[i] + fc * t0_unscaled(kgt, kgv[j], S.mass[s]);
-            c1c[j] = c1c[j] + fc * t1; c2c[j] = c2c[j] + fc * t2; omc[j] = omc[j] + fc * tO;
+            if (triple && p.type_region[t] == 3) {
+              // a convective type (aggregate_cloud.F90:107-155)
+              VT[i] = VT[i] + fc * tT; VR[i] = VR[i] + fc * tR; VT0[i] = VT0[i] + fc * tT0;
+              if (dir_unscaled) row(kRgVT0D)[i] = row(kRgVT0D)[i] + fc * t0_unscaled(kgt, kgv[j], S.mass[s]);
+              VC1[i] = VC1[i] + fc * t1; VC2[i] = VC2[i] + fc * t2; VOM[i] = VOM[i] + fc * tO;
+            } else {
+              Tc[j] = Tc[j] + fc * tT; Rc[j] = Rc[j] + fc * tR; T0c[j] = T0c[j] + fc * tT0;
+              if (dir_unscaled) row(kRgCT0D)[i] = row(kRgCT0D)[i] + fc * t0_unscaled(kgt, kgv[j], S.mass[s]);
+              c1c[j] = c1c[j] + fc * t1; c2c[j] = c2c[j] + fc * t2; omc[j] = omc[j] + fc * tO;
+            }
+          }
+          if (triple) {
+            // each cloudy region's weighted sums over its share of the cloud
+            // (two_coeff_region.F90:383-440)
+            const R f2 = S.frr[i], f3 = S.frr[LP + i];
+            if (f2 > (R)kTiny64) {
+              const R inv = R(1) / f2;
+              Tc[j] = Tc[j] * inv; Rc[j] = Rc[j] * inv; T0c[j] = T0c[j] * inv;
+              c1c[j] = c1c[j] * inv; c2c[j] = c2c[j] * inv; omc[j] = omc[j] * inv;
+              if (dir_unscaled) row(kRgCT0D)[i] = row(kRgCT0D)[i] * inv;
+            }
+            if (f3 > (R)kTiny64) {
+              const R inv = R(1) / f3;
+              VT[i] = VT[i] * inv; VR[i] = VR[i] * inv; VT0[i] = VT0[i] * inv;
+              VC1[i] = VC1[i] * inv; VC2[i] = VC2[i] * inv; VOM[i] = VOM[i] * inv;
+              if (dir_unscaled) row(kRgVT0D)[i] = row(kRgVT0D)[i] * inv;
+            }
           }
         }
       } else {
@@ -1692,6 +1803,19 @@ struct FluxKernel {
       if (p.keqv) {
         fold_direct(S, bi, max_abs, r, L, T0f, c2f);
         fold_direct(S, bi, max_abs, r, L, T0c, c2c);
+        if (triple) {
+          // the same correction on the convective rows (fold_direct)
+          const R *a = S.aux + (size_t)bi * max_abs * LP;
+#pragma unroll
+          for (int j = 0; j < CH; ++j) {
+            const int i = r * CH + j, s = j * P + r;
+            if (i < L) {
+              const R fm1 = kFP64 ? a[s] - R(1) : a[s];
+              VC2[i] = VC2[i] + VT0[i] * fm1;
+              VT0[i] = kFP64 ? VT0[i] * a[s] : VT0[i] + VT0[i] * fm1;
+            }
+          }
+        }
         if (dir_unscaled) {
           // adjust_solar_ke on the unscaled beam too (mixed_solar_source.F90:130-140)
           const R *a = S.aux + (size_t)bi * max_abs * LP;
@@ -1702,6 +1826,7 @@ struct FluxKernel {
               const R f = kFP64 ? a[s] : R(1) + a[s];
               row(kRgFT0D)[i] = row(kRgFT0D)[i] * f;
               row(kRgCT0D)[i] = row(kRgCT0D)[i] * f;
+              if (triple) row(kRgVT0D)[i] = row(kRgVT0D)[i] * f;
             }
           }
         }
@@ -1714,18 +1839,28 @@ struct FluxKernel {
         // ir_source.F90:93-119 in each region, weighted by its area in the
         // cloudy layers (mix_column.F90:185-230)
         const R dB = dB_b[s];
-        R su, sd, suc, sdc;
+        R su, sd, suc, sdc, suv = R(0), sdv = R(0);
         if (p.l_ir_source_quad) {
           su = c1f[j] * dB + c2f[j] * dB2_b[s]; sd = -c1f[j] * dB + c2f[j] * dB2_b[s];
           suc = c1c[j] * dB + c2c[j] * dB2_b[s]; sdc = -c1c[j] * dB + c2c[j] * dB2_b[s];
+          if (triple) { suv = VC1[i] * dB + VC2[i] * dB2_b[s]; sdv = -VC1[i] * dB + VC2[i] * dB2_b[s]; }
         } else {
           su = c1f[j] * dB; sd = -su; suc = c1c[j] * dB; sdc = -suc;
+          if (triple) { suv = VC1[i] * dB; sdv = -suv; }
         }
         if (i + 1 >= nct) {
           const R wc = S.wcld[s], wf = R(1) - wc;
-          su = wf * su; sd = wf * sd; suc = wc * suc; sdc = wc * sdc;
+          su = wf * su; sd = wf * sd;
+          if (triple) {
+            // the areas of the three regions (triple_column.F90:320-350)
+            const R a2 = wc * S.frr[i], a3 = wc * S.frr[LP + i];
+            suc = a2 * suc; sdc = a2 * sdc; suv = a3 * suv; sdv = a3 * sdv;
+          } else {
+            suc = wc * suc; sdc = wc * sdc;
+          }
         }
         c1f[j] = su; c2f[j] = sd; c1c[j] = suc; c2c[j] = sdc;
+        if (triple) { VC1[i] = suv; VC2[i] = sdv; }
       }
       row(kRgFT)[i] = Tf[j]; row(kRgFR)[i] = Rff[j]; row(kRgFT0)[i] = T0f[j];
       row(kRgFC1)[i] = c1f[j]; row(kRgFC2)[i] = c2f[j]; row(kRgFOM)[i] = omf[j];
@@ -1733,9 +1868,11 @@ struct FluxKernel {
       row(kRgCC1)[i] = c1c[j]; row(kRgCC2)[i] = c2c[j]; row(kRgCOM)[i] = omc[j];
     }
     __syncwarp(gm);
-    if (r == 0)
-      region_serial(p, S, X, S.regd + (size_t)gid * kRegDRows * (LP + 1), nct, L, lw, f_inc_down, f_inc_dir,
-                    alb_diff, alb_dir, dB_surf);
+    if (r == 0) {
+      double *Y = S.regd + (size_t)gid * lay.regd_rows * (LP + 1);
+      if (triple) region_serial3(p, S, X, Y, nct, L, lw, f_inc_down, f_inc_dir, alb_diff, alb_dir, dB_surf);
+      else region_serial(p, S, X, Y, nct, L, lw, f_inc_down, f_inc_dir, alb_diff, alb_dir, dB_surf);
+    }
     __syncwarp(gm);
     // accumulate the level fluxes and the layer divergence
     const int L_acc = active ? L : -1;
@@ -1942,6 +2079,160 @@ struct FluxKernel {
         DV[ii] = (R)((D)FOM[ii] * (fd1 + fu1) - ((D)FC1[ii] + (D)FC2[ii]) + (D)COM[ii] * (fd2 + fu2) -
                      ((D)CC1[ii] + (D)CC2[ii]));
       fd1 = nd1; fd2 = nd2;
+    }
+  }
+
+  // The serial part of the three-region solve (clear, stratiform and
+  // convective) on one lane, in FP64 in every build: triple_solar_source.F90:
+  // 160-400, the ground sources of triple_column.F90:380-410 and
+  // solver_triple_hogan.F90:200-410.  Rows as solve_region leaves them, the
+  // interface coefficients of stage_regions3 (v_jk row 3 j + k, u_jk row
+  // 9 + 3 j + k); writes the level fluxes (diffuse in the solar), the direct
+  // flux and the layer divergence.  Layers i are 0-based here; interface i
+  // lies below layer i-1 (0: the top).
+  __device__ static __noinline__ void region_serial3(const FluxParams &p, const Smem &S, R *X, double *Y, int nct,
+                                                     int L, bool lw, R f_inc_down_r, R f_inc_dir_r, R alb_diff_r,
+                                                     R alb_dir_r, R dB_surf_r) {
+    using D = double;
+    auto row = [&](int k) { return X + (size_t)k * (LP + 1); };
+    auto drow = [&](int k) { return Y + (size_t)k * (LP + 1); };
+    auto ov = [&](int m, int i) -> D { return (D)S.ovl[(size_t)m * (LP + 1) + i]; };
+    const D f_inc_down = f_inc_down_r, f_inc_dir = f_inc_dir_r, alb_diff = alb_diff_r, alb_dir = alb_dir_r;
+    const D dB_surf = dB_surf_r;
+    // region k's rows: 0 the clear, 1 the stratiform, 2 the convective
+    R *T[3] = {row(kRgFT), row(kRgCT), row(kRgVT)}, *RR[3] = {row(kRgFR), row(kRgCR), row(kRgVR)};
+    R *T0[3] = {row(kRgFT0), row(kRgCT0), row(kRgVT0)}, *C1[3] = {row(kRgFC1), row(kRgCC1), row(kRgVC1)};
+    R *C2[3] = {row(kRgFC2), row(kRgCC2), row(kRgVC2)}, *OM[3] = {row(kRgFOM), row(kRgCOM), row(kRgVOM)};
+    D *B[3] = {drow(kRgB11), drow(kRgB22), drow(kRgB33)}, *G[3] = {drow(kRgG11), drow(kRgG22), drow(kRgG33)};
+    D *H[3] = {drow(kRgH1), drow(kRgH2), drow(kRgH3)};
+    // the solar sources of each region in FP64 (Hogan's form leaves the
+    // coupling rows free)
+    D *SU[3] = {drow(kRgG21), drow(kRgG12), drow(kRgSUV)}, *SD[3] = {drow(kRgB21), drow(kRgH2), drow(kRgSDV)};
+    R *FU = row(kRgFU), *FD = row(kRgFD), *FDIR = row(kRgFDIR), *DV = row(kRgDIV);
+    D base[3] = {0.0, 0.0, 0.0};
+    if (!lw) {
+      D f = f_inc_dir;
+      FDIR[0] = (R)f;
+      for (int i1 = 1; i1 <= nct - 1; ++i1) {
+        const int ii = i1 - 1;
+        SU[0][ii] = (D)C1[0][ii] * f;
+        SD[0][ii] = (D)C2[0][ii] * f;
+        f = f * (D)T0[0][ii];
+        FDIR[i1] = (R)f;
+      }
+      base[0] = f;
+      for (int i1 = nct; i1 <= L; ++i1) {
+        const int ii = i1 - 1;
+        D top[3];
+        for (int j = 0; j < 3; ++j)
+          top[j] = ov(3 * j, i1 - 1) * base[0] + ov(3 * j + 1, i1 - 1) * base[1] + ov(3 * j + 2, i1 - 1) * base[2];
+        for (int k = 0; k < 3; ++k) {
+          base[k] = top[k] * (D)T0[k][ii];
+          SU[k][ii] = (D)C1[k][ii] * top[k];
+          SD[k][ii] = (D)C2[k][ii] * top[k];
+        }
+        FDIR[i1] = (R)(base[0] + base[1] + base[2]);
+      }
+      if (p.i_direct_tau == SOCGPU_IP_DIRECT_NOSCALING) {
+        // the direct flux without delta-scaling, which the outputs and the
+        // ground's direct reflection take (triple_solar_source.F90:300-350)
+        const R *T0D[3] = {row(kRgFT0D), row(kRgCT0D), row(kRgVT0D)};
+        D fdd = f_inc_dir;
+        for (int i1 = 1; i1 <= nct - 1; ++i1) { fdd = fdd * (D)T0D[0][i1 - 1]; FDIR[i1] = (R)fdd; }
+        D db[3] = {fdd, 0.0, 0.0};
+        for (int i1 = nct; i1 <= L; ++i1) {
+          const int ii = i1 - 1;
+          D top[3];
+          for (int j = 0; j < 3; ++j)
+            top[j] = ov(3 * j, i1 - 1) * db[0] + ov(3 * j + 1, i1 - 1) * db[1] + ov(3 * j + 2, i1 - 1) * db[2];
+          for (int k = 0; k < 3; ++k) db[k] = top[k] * (D)T0D[k][ii];
+          FDIR[i1] = (R)(db[0] + db[1] + db[2]);
+        }
+        for (int k = 0; k < 3; ++k) base[k] = db[k];
+      }
+      // the layers' source rows now hold the sources themselves
+      for (int ii = 0; ii < L; ++ii)
+        for (int k = 0; k < 3; ++k)
+          if (k == 0 || ii + 1 >= nct) { C1[k][ii] = (R)SU[k][ii]; C2[k][ii] = (R)SD[k][ii]; }
+    }
+    auto su_of = [&](int k, int ii) -> D { return lw ? (D)C1[k][ii] : SU[k][ii]; };
+    auto sd_of = [&](int k, int ii) -> D { return lw ? (D)C2[k][ii] : SD[k][ii]; };
+    // ground sources (triple_column.F90:380-410)
+    D sg[3];
+    for (int k = 0; k < 3; ++k)
+      sg[k] = lw ? ov(9 + 3 * k, L) * (1.0 - alb_diff) * dB_surf : (alb_dir - alb_diff) * base[k];
+    // elimination from the ground up (solver_triple_hogan.F90:200-320); the
+    // solar sources of layer ii are read before its coefficient rows are
+    // written
+    D a[3] = {alb_diff, alb_diff, alb_diff}, g[3] = {sg[0], sg[1], sg[2]};
+    for (int i1 = L; i1 >= 1; --i1) {
+      const int ii = i1 - 1;
+      if (i1 >= nct) {
+        D th[3], lam[3];
+        for (int k = 0; k < 3; ++k) th[k] = a[0] * ov(k, i1) + a[1] * ov(3 + k, i1) + a[2] * ov(6 + k, i1);
+        for (int k = 0; k < 3; ++k) {
+          const D r = RR[k][ii], t = T[k][ii], sd = sd_of(k, ii), su = su_of(k, ii);
+          const D b = 1.0 / (1.0 - th[k] * r);
+          const D hh = g[k] + th[k] * sd;
+          B[k][ii] = b; G[k][ii] = th[k] * t; H[k][ii] = hh;
+          lam[k] = su + hh * t * b;
+          a[k] = r + th[k] * t * t * b;
+        }
+        for (int j = 0; j < 3; ++j)
+          g[j] = ov(9 + 3 * j, i1 - 1) * lam[0] + ov(9 + 3 * j + 1, i1 - 1) * lam[1] + ov(9 + 3 * j + 2, i1 - 1) * lam[2];
+      } else {
+        const D r = RR[0][ii], t = T[0][ii], sd = sd_of(0, ii), su = su_of(0, ii);
+        D th11 = a[0];
+        if (i1 == nct - 1 && nct < L) th11 = a[0] * ov(0, i1) + a[1] * ov(3, i1) + a[2] * ov(6, i1);
+        const D b11 = 1.0 / (1.0 - th11 * r), gm11 = th11 * t, hh1 = g[0] + th11 * sd;
+        B[0][ii] = b11; G[0][ii] = gm11; H[0][ii] = hh1;
+        const D lam = t * b11;
+        a[0] = r + lam * gm11;
+        g[0] = su + lam * hh1;
+      }
+    }
+    // back-substitution (solver_triple_hogan.F90:320-410); the sources are
+    // read back from the rows, which hold them rounded to the build's type
+    D fd_prev = f_inc_down, fu_prev;
+    FD[0] = (R)f_inc_down;
+    if (nct > 1) fu_prev = a[0] * f_inc_down + g[0];
+    else fu_prev = g[0] + f_inc_down * (ov(0, 0) * a[0] + ov(3, 0) * a[1] + ov(6, 0) * a[2]);
+    FU[0] = (R)fu_prev;
+    for (int i1 = 1; i1 <= nct - 1; ++i1) {
+      const int ii = i1 - 1;
+      const D fdt = fd_prev;
+      const D fub = (G[0][ii] * fdt + H[0][ii]) * B[0][ii];
+      const D fdb = (D)T[0][ii] * fdt + (D)RR[0][ii] * fub + (D)C2[0][ii];
+      FU[i1] = (R)fub; FD[i1] = (R)fdb;
+      if constexpr (kFP64) DV[ii] = fub - fu_prev + fdt - fdb;
+      else DV[ii] = (R)((D)OM[0][ii] * (fdt + fub) - ((D)C1[0][ii] + (D)C2[0][ii]));
+      fu_prev = fub; fd_prev = fdb;
+    }
+    D fdk[3] = {0.0, 0.0, 0.0};
+    for (int i1 = nct; i1 <= L; ++i1) {
+      const int ii = i1 - 1;
+      D d[3];
+      if (i1 > nct) {
+        for (int j = 0; j < 3; ++j)
+          d[j] = ov(3 * j, i1 - 1) * fdk[0] + ov(3 * j + 1, i1 - 1) * fdk[1] + ov(3 * j + 2, i1 - 1) * fdk[2];
+      } else {
+        for (int j = 0; j < 3; ++j) d[j] = ov(3 * j, i1 - 1) * fd_prev;
+      }
+      const D fdt = fd_prev, fut = fu_prev;
+      D fu_sum = 0.0, fd_sum = 0.0, div = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        const D fu = (G[k][ii] * d[k] + H[k][ii]) * B[k][ii];
+        fdk[k] = (D)T[k][ii] * d[k] + (D)RR[k][ii] * fu + (D)C2[k][ii];
+        fu_sum = fu_sum + fu;
+        fd_sum = fd_sum + fdk[k];
+        // each region's absorption closes its own layer equations under
+        // Hogan's form: the mixed build forms the divergence from it
+        div = div + ((D)OM[k][ii] * (d[k] + fu) - ((D)C1[k][ii] + (D)C2[k][ii]));
+      }
+      fu_prev = fu_sum; fd_prev = fd_sum;
+      FU[i1] = (R)fu_prev; FD[i1] = (R)fd_prev;
+      if constexpr (kFP64) DV[ii] = (R)(fu_prev - fut + fdt - fd_prev);
+      else DV[ii] = (R)div;
     }
   }
 

@@ -151,6 +151,8 @@ struct FluxParams {
   int region;                        // clear and cloudy regions (ip_cloud_mix_max / mix_random)
   int solver_hogan;                  // regions solved by solver_mix_direct_hogan, else solver_mix_direct
   int mix_max;                       // regions overlap maximally where adjacent (else randomly)
+  int triple;                        // three regions: clear, stratiform and convective (ip_cloud_triple)
+  int type_region[4];                // the region (2 stratiform, 3 convective) of each 0-based cloud type
   int l_continuum, l_mixing_ratio, i_water;   // i_water: 0-based species of water vapour
   // sizes
   int n_profile, n_layer, nd_profile, nd_layer, id_ct;  // id_ct 0-based first cloudy layer

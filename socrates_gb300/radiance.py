@@ -78,12 +78,15 @@ class Control:
     l_grey_single: bool = False
     l_aerosol: bool = False
     l_henyey_greenstein_pf: bool = False
+    # how the cloud types group into regions (the three-region scheme needs
+    # conv_strat, csiw or a split representation)
+    i_cloud_representation: int = abi.IP_CLOUD_ICE_WATER
 
     def as_struct(self, n_band: int, keep: list) -> abi.Control:
         c = abi.Control()
         c.isolir, c.i_angular_integration, c.i_2stream = self.isolir, abi.IP_TWO_STREAM, self.i_2stream
         c.i_scatter_method, c.i_solver, c.i_cloud = self.i_scatter_method, self.i_solver, self.i_cloud
-        c.i_cloud_representation = abi.IP_CLOUD_ICE_WATER
+        c.i_cloud_representation = self.i_cloud_representation
         c.i_gas_overlap, c.i_direct_tau = self.i_gas_overlap, self.i_direct_tau
         c.l_rescale, c.n_order_forward = int(self.l_rescale), self.n_order_forward
         c.l_ir_source_quad, c.l_rayleigh, c.l_gas = int(self.l_ir_source_quad), int(self.l_rayleigh), int(self.l_gas)
@@ -359,7 +362,7 @@ class Marshal:
                 self.aer.scattering_prsc = _dp(ae["scattering_prsc"], k)
                 self.aer.phase_fnc_prsc = _dp(ph, k)
         self.cld = abi.Cld()
-        region = control.i_cloud in (abi.IP_CLOUD_MIX_MAX, abi.IP_CLOUD_MIX_RANDOM)
+        region = control.i_cloud in (abi.IP_CLOUD_MIX_MAX, abi.IP_CLOUD_MIX_RANDOM, abi.IP_CLOUD_TRIPLE)
         if mcica is not None or (region and col.cld):
             cd = col.cld
             ict = id_cloud_top - 1

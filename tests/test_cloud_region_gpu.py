@@ -100,3 +100,81 @@ def test_cloud_regions_refusals(gpu_lib, sps):
     with pytest.raises(R.RadianceError) as e:
         R.radiance_calc(replace(ctl, i_solver=abi.IP_SOLVER_HOMOGEN_DIRECT), sp, col)
     assert e.value.status == abi.I_ERR_FATAL and "solver_mix" in str(e.value)
+
+
+def _three_region(sp, n, L, seed, solar, representation):
+    """_clouded columns whose water and ice are split between a stratiform and
+    a convective part (the convective one denser): four cloud types under
+    csiw (stratiform water and ice, convective water and ice), or two under
+    conv_strat (each type holding a water and an ice component)."""
+    col = _clouded(sp, n, L, seed, solar, abi.IP_CLOUD_ICE_WATER)
+    c = col.cld
+    rng = np.random.default_rng(seed + 100)
+    w = c["w_cloud"]
+    x = np.where(w > 0, rng.uniform(0.2, 0.8, size=w.shape), 0.0)          # the stratiform share
+    fw = c["frac_cloud"][:, :, 0]                                           # the water share
+    mr, dc = c["condensed_mix_ratio"], c["condensed_dim_char"]
+    f = lambda a: np.asfortranarray(a)
+    cld = dict(c)
+    cld.update(n_condensed=4, type_condensed=[abi.IP_PHASE_WATER, abi.IP_PHASE_ICE] * 2,
+               i_condensed_param=list(c["i_condensed_param"]) * 2, i_condensed_type=list(c["i_condensed_type"]) * 2,
+               condensed_mix_ratio=f(np.concatenate([mr, mr * np.array([2.0, 1.5])], axis=2)),
+               condensed_dim_char=f(np.concatenate([dc, dc], axis=2)))
+    if representation == abi.IP_CLOUD_CSIW:
+        cld.update(i_cloud_type=[abi.IP_CLOUD_TYPE_SW, abi.IP_CLOUD_TYPE_SI, abi.IP_CLOUD_TYPE_CW, abi.IP_CLOUD_TYPE_CI],
+                   n_cloud_type=4,
+                   frac_cloud=f(np.stack([fw * x, (1 - fw) * x * (w > 0), fw * (1 - x), (1 - fw) * (1 - x) * (w > 0)],
+                                         axis=2)))
+    else:
+        cld.update(i_cloud_type=[abi.IP_CLOUD_TYPE_STRAT, abi.IP_CLOUD_TYPE_STRAT, abi.IP_CLOUD_TYPE_CONV,
+                                 abi.IP_CLOUD_TYPE_CONV],
+                   n_cloud_type=2, frac_cloud=f(np.stack([x, np.where(w > 0, 1.0 - x, 0.0)], axis=2)))
+    col.cld = cld
+    return col
+
+
+def _three_region_control(solar, representation, **kw):
+    common = dict(i_cloud=abi.IP_CLOUD_TRIPLE, i_solver=abi.IP_SOLVER_TRIPLE_HOGAN, l_continuum=True,
+                  i_gas_overlap=abi.IP_OVERLAP_K_EQV_SCL, l_flux_div=False, i_cloud_representation=representation)
+    common.update(kw)
+    return R.sw_control(l_rayleigh=True, **common) if solar else R.lw_control(l_ir_source_quad=True, **common)
+
+
+@pytest.mark.parametrize("solar", [False, True])
+@pytest.mark.parametrize("representation", [abi.IP_CLOUD_CSIW, abi.IP_CLOUD_CONV_STRAT])
+def test_three_regions_synthetic(gpu_lib, O, sps, solar, representation):
+    """Clouds in three regions, clear, stratiform and convective (ip_cloud_triple,
+    triple_column.F90, solver_triple_hogan.F90): 97 columns of 60 layers with the
+    GA9 files, k_eqv_scl and continuum, the cloud split at random between a
+    stratiform and a denser convective part.  FP64 within 1e-10 of the oracle,
+    mixed within 0.1 W/m2 and 0.05 K/day; the split changes the answer of one
+    cloudy region."""
+    sp = sps["ga9sw" if solar else "ga9lw"]
+    col = _three_region(sp, 97, 60, seed=71 + solar, solar=solar, representation=representation)
+    ctl = _three_region_control(solar, representation)
+    ref, _ = _check(ctl, sp, col, O, f"triple {representation} solar={solar}")
+    one = _clouded(sp, 97, 60, seed=71 + solar, solar=solar, representation=abi.IP_CLOUD_ICE_WATER)
+    two = O.radiance_calc(replace(ctl, i_cloud=abi.IP_CLOUD_MIX_MAX, i_solver=abi.IP_SOLVER_MIX_DIRECT_HOGAN,
+                                  i_cloud_representation=abi.IP_CLOUD_ICE_WATER), sp, one)
+    assert np.abs(ref["flux_up"] - two["flux_up"]).max() > 0.5
+
+
+def test_three_regions_unscaled_direct_beam(gpu_lib, O, sps):
+    """The solar direct beam without delta-scaling (i_direct_tau = 0) through
+    the three regions (triple_solar_source.F90:300-350)."""
+    sp = sps["ga9sw"]
+    col = _three_region(sp, 61, 60, seed=83, solar=True, representation=abi.IP_CLOUD_CSIW)
+    _check(_three_region_control(True, abi.IP_CLOUD_CSIW, i_direct_tau=abi.IP_DIRECT_NOSCALING), sp, col, O,
+           "triple unscaled beam")
+
+
+def test_three_regions_refusals(gpu_lib, sps):
+    """ip_cloud_triple needs solver_triple_hogan and a representation that
+    separates convective from stratiform cloud (aggregate_cloud.F90:155-160)."""
+    sp = sps["ga9lw"]
+    col = _three_region(sp, 4, 60, seed=5, solar=False, representation=abi.IP_CLOUD_CSIW)
+    for kw, text in ((dict(i_solver=abi.IP_SOLVER_MIX_DIRECT_HOGAN), "solver_triple_hogan"),
+                     (dict(i_cloud_representation=abi.IP_CLOUD_ICE_WATER), "not compatible")):
+        with pytest.raises(R.RadianceError) as e:
+            R.radiance_calc(_three_region_control(False, abi.IP_CLOUD_CSIW, **kw), sp, col)
+        assert e.value.status == abi.I_ERR_FATAL and text in str(e.value)

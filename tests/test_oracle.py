@@ -560,3 +560,35 @@ def test_oracle_reproduces_circ6_sw_aerosol_known_good_output():
     from dataclasses import replace
     bare = K.heating_rate(O.radiance_calc(replace(ctl, l_aerosol=False), sp, col), col)[0]
     assert half_units(bare, kgo).max() > 1000.0
+
+
+@pytest.mark.parametrize("solar", [False, True])
+def test_oracle_three_regions_reduce_to_two(solar):
+    """Clouds in three regions (ip_cloud_triple: triple_column.F90,
+    overlap_coupled.F90 for three regions, triple_solar_source.F90,
+    solver_triple_hogan.F90) with all the cloud stratiform, or all of it
+    convective, give the answer of the same cloud in two regions
+    (ip_cloud_mix_max with solver_mix_direct_hogan); a cloud split between the
+    regions differs from it."""
+    import cld7460 as K
+    from test_cloud_region_gpu import _clouded, _three_region_control
+    sp = K.spectra()["ga9sw" if solar else "ga9lw"]
+    col = _clouded(sp, 23, 60, seed=61 + solar, solar=solar, representation=abi.IP_CLOUD_ICE_WATER)
+    ctl = _three_region_control(solar, abi.IP_CLOUD_CSIW)
+    from dataclasses import replace
+    two = O.radiance_calc(replace(ctl, i_cloud=abi.IP_CLOUD_MIX_MAX, i_solver=abi.IP_SOLVER_MIX_DIRECT_HOGAN,
+                                  i_cloud_representation=abi.IP_CLOUD_ICE_WATER), sp, col)
+    fw = col.cld["frac_cloud"]
+    z = np.zeros(fw.shape[:2])
+    base = dict(col.cld)
+    for types, frac in (([1, 2], [fw[:, :, 0], fw[:, :, 1], z, z]), ([3, 4], [z, z, fw[:, :, 0], fw[:, :, 1]])):
+        col.cld = dict(base, i_cloud_type=types, n_cloud_type=4, frac_cloud=np.asfortranarray(np.stack(frac, axis=2)))
+        three = O.radiance_calc(ctl, sp, col)
+        for k in two:
+            scale = np.abs(two[k]).max()
+            assert np.abs(three[k] - two[k]).max() <= 1e-12 * scale, (types, k)
+    col.cld = dict(base, i_cloud_type=[1, 4], n_cloud_type=4,
+                   frac_cloud=np.asfortranarray(np.stack([fw[:, :, 0], z, z, fw[:, :, 1]], axis=2)))
+    mixed = O.radiance_calc(ctl, sp, col)
+    assert np.abs(mixed["flux_up"] - two["flux_up"]).max() > 0.5
+    assert all(np.isfinite(v).all() for v in mixed.values())
