@@ -114,6 +114,11 @@ extern "C" {
 #define SOCGPU_IP_CLOUD_TYPE_SI         2
 #define SOCGPU_IP_CLOUD_TYPE_CW         3
 #define SOCGPU_IP_CLOUD_TYPE_CI         4
+/* condensed components, rad_pcf.F90:187-193: stratiform and convective water and ice */
+#define SOCGPU_IP_CLCMP_ST_WATER        1
+#define SOCGPU_IP_CLCMP_ST_ICE          2
+#define SOCGPU_IP_CLCMP_CNV_WATER       3
+#define SOCGPU_IP_CLCMP_CNV_ICE         4
 /* condensed phases, rad_pcf.F90:494-496 */
 #define SOCGPU_IP_PHASE_WATER           1
 #define SOCGPU_IP_PHASE_ICE             2

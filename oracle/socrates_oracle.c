@@ -906,7 +906,10 @@ static int grey_opt_prop(work *w, const socgpu_control *c, const socgpu_dimen *d
         for (int k = 0; k < cld->n_condensed; ++k) {
             const double *cp0;
             int ity = cld->i_condensed_type[k] - 1;
-            const int phase = cld->type_condensed[k], scheme = cld->i_condensed_param[k];
+            /* stratiform or convective water (ip_clcmp 1, 3) or ice (2, 4), rad_pcf.F90:187-193 */
+            const int tc = cld->type_condensed[k];
+            const int phase = (tc == 1 || tc == 3) ? SOCGPU_IP_PHASE_WATER : (tc == 2 || tc == 4) ? SOCGPU_IP_PHASE_ICE : tc;
+            const int scheme = cld->i_condensed_param[k];
             if (phase == SOCGPU_IP_PHASE_WATER) {
                 if (!d->drop_parm_list || ity < 0 || ity >= d->nd_drop_type) return SOCGPU_I_ERR_FATAL;
                 cp0 = d->drop_parm_list + (size_t)d->nd_cloud_parameter * ((size_t)b + (size_t)d->nd_band * (size_t)ity);

@@ -29,7 +29,7 @@ IP_CLOUD_HOMOGEN = 1
 IP_CLOUD_ICE_WATER = 2
 IP_CLOUD_TYPE_WATER, IP_CLOUD_TYPE_ICE = 1, 2
 IP_PHASE_WATER, IP_PHASE_ICE = 1, 2
-IP_CLCMP_ST_WATER, IP_CLCMP_ST_ICE = 1, 2
+IP_CLCMP_ST_WATER, IP_CLCMP_ST_ICE, IP_CLCMP_CNV_WATER, IP_CLCMP_CNV_ICE = 1, 2, 3, 4
 IP_DROP_PADE_2, IP_ICE_PADE_2_PHF = 5, 20
 IP_SLINGO_SCHRECKER, IP_SLINGO_SCHRECKER_ICE, IP_ICE_FU_PHF = 1, 1, 12
 IP_OVERLAP_RANDOM = 2

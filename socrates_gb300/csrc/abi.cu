@@ -647,6 +647,15 @@ TileConfig choose_tile(int precision, int mode, int n_layer) {
   return t;
 }
 
+// The phase of a condensed component (rad_pcf.F90:187-193): stratiform or
+// convective water (ip_clcmp_st_water 1, ip_clcmp_cnv_water 3) or ice (2, 4).
+int condensed_phase(int type_condensed) {
+  if (type_condensed == SOCGPU_IP_CLCMP_ST_WATER || type_condensed == SOCGPU_IP_CLCMP_CNV_WATER)
+    return SOCGPU_IP_PHASE_WATER;
+  if (type_condensed == SOCGPU_IP_CLCMP_ST_ICE || type_condensed == SOCGPU_IP_CLCMP_CNV_ICE) return SOCGPU_IP_PHASE_ICE;
+  return type_condensed;
+}
+
 // ---------------------------------------------------------------------------
 // Validation (mirrors the checks the reference makes before and during
 // radiance_calc; unsupported options are fatal, never a CPU fallback).
@@ -837,7 +846,7 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     if (!region && (!cld->c_sub || !cld->frac_cloudy || !cld->subcol_k || !cld->first_subcol_k || !cld->subcol_reorder)) {
       set_msg(msg, msg_len, "McICA requires the subcolumn fields"); return SOCGPU_I_ERR_FATAL; }
     for (int k = 0; k < cld->n_condensed; ++k) {
-      int ph = cld->type_condensed[k], parm = cld->i_condensed_param[k], ty = cld->i_condensed_type[k];
+      int ph = condensed_phase(cld->type_condensed[k]), parm = cld->i_condensed_param[k], ty = cld->i_condensed_type[k];
       if (ph == SOCGPU_IP_PHASE_WATER) {
         if ((parm != SOCGPU_IP_SLINGO_SCHRECKER && parm != SOCGPU_IP_DROP_PADE_2) || ty < 1 ||
             ty > sp->dev.n_drop_type) {
@@ -1019,7 +1028,7 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
     p.n_condensed = cld->n_condensed; p.n_cloud_type = cld->n_cloud_type;
     for (int k = 0; k < cld->n_condensed; ++k) {
       p.comp_type[k] = cld->i_cloud_type[k];
-      p.comp_phase[k] = cld->type_condensed[k];
+      p.comp_phase[k] = condensed_phase(cld->type_condensed[k]);
       p.comp_parm_index[k] = cld->i_condensed_type[k] - 1;
       p.comp_scheme[k] = cld->i_condensed_param[k];
     }

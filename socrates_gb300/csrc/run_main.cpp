@@ -9,6 +9,8 @@
 //              [-ds <direct tau>] [-P fp64|mixed] [-W <Wen-Yi tables file>]
 //              [-C 10 -K <cloud representation> -d <droplet type> -i <ice type>
 //               -m <condensate relative std. deviation> +m <sampling> -dp <decorrelation scale>]
+//              [-C 6 -K 3|4 -d <droplet type> -i <ice type> +d <convective droplet type>
+//               +i <convective ice type>]
 //              [-a [+A]]
 //   socgpu_run --convert <in> <out.cdf|out.cdl>
 //
@@ -26,6 +28,10 @@
 // spectral file's droplet type -d, ice from .iwm and .ire with ice type -i
 // (input_cloud_cdf.f:340-790), and the subcolumns of set_cld_mcica from the
 // McICA data file beside the spectral file (l_run_cdf.F90:998-1010,
+// 1281-1296).  Three regions (-C 6, solver 17 unless -v is given) take
+// stratiform and convective cloud: -K 3 with .clfr and .ccfr, or -K 4 with
+// .wclfr, .iclfr, .wccfr and .iccfr; convective droplets from .lwmcv and
+// .recv (type +d), convective ice from .iwmcv and .irecv (type +i).
 // 1281-1296).  With -a the spectral file's aerosol species are included:
 // mixing ratios from <base>.<species suffix> (wtsol, dust, ocn, soot, ...;
 // none without a file) and, with +A, prescribed optical properties from
@@ -250,6 +256,7 @@ int main(int argc, char **argv) {
   int precision = SOCGPU_PRECISION_FP64;
   // clouds (-K, -d, -i) and McICA (-m, +m, -dp)
   int representation = 0, drop_type = 0, ice_type = 0, sampling = 2;
+  int conv_drop_type = 0, conv_ice_type = 0;   // +d, +i: convective particles (three regions)
   bool aerosol = false, overlay = false;   // -a: classic aerosols; +A: overlay of optical properties
   double mcica_sigma = 0.0, dp_corr_strat = 0.0;
   for (size_t i = 0; i < a.size(); ++i) {
@@ -276,6 +283,8 @@ int main(int argc, char **argv) {
     else if (o == "-K" && need(1)) representation = std::atoi(a[++i].c_str());
     else if (o == "-d" && need(1)) drop_type = std::atoi(a[++i].c_str());
     else if (o == "-i" && need(1)) ice_type = std::atoi(a[++i].c_str());
+    else if (o == "+d" && need(1)) conv_drop_type = std::atoi(a[++i].c_str());
+    else if (o == "+i" && need(1)) conv_ice_type = std::atoi(a[++i].c_str());
     else if (o == "-m" && need(1)) mcica_sigma = std::atof(a[++i].c_str());
     else if (o == "+m" && need(1)) sampling = std::atoi(a[++i].c_str());
     else if (o == "-dp" && need(1)) dp_corr_strat = std::atof(a[++i].c_str());
@@ -289,20 +298,28 @@ int main(int argc, char **argv) {
   if (!isolir) return die("Spectral region not set.");
   if (first < 1 || last < first) return die("Range of bands not set");
   if (overlay && !aerosol) return die("+A overlays aerosol optical properties: it needs -a");
-  const bool region = cloud == SOCGPU_IP_CLOUD_MIX_MAX || cloud == SOCGPU_IP_CLOUD_MIX_RANDOM;
+  const bool triple = cloud == SOCGPU_IP_CLOUD_TRIPLE;
+  const bool region = cloud == SOCGPU_IP_CLOUD_MIX_MAX || cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || triple;
   if (cloud != SOCGPU_IP_CLOUD_CLEAR && cloud != SOCGPU_IP_CLOUD_MCICA && !region)
     return die("cloud scheme " + std::to_string(cloud) +
-               " is not driven (clear sky -C 5, cloud regions -C 2 or 4, McICA -C 10)");
+               " is not driven (clear sky -C 5, cloud regions -C 2 or 4, three regions -C 6, McICA -C 10)");
   const bool mcica = cloud == SOCGPU_IP_CLOUD_MCICA;
   const bool clouds = mcica || region;
-  if (clouds && representation != 1 && representation != SOCGPU_IP_CLOUD_ICE_WATER)
+  const bool conv = representation == SOCGPU_IP_CLOUD_CONV_STRAT || representation == SOCGPU_IP_CLOUD_CSIW;
+  if (clouds && !triple && representation != 1 && representation != SOCGPU_IP_CLOUD_ICE_WATER)
     return die("clouds need the cloud representation -K 1 (homogeneous) or -K 2 (ice and water)");
+  if (triple && !conv)
+    return die("three regions need the cloud representation -K 3 (convective and stratiform) or -K 4 "
+               "(convective and stratiform ice and water)");
   if (clouds && !drop_type && !ice_type) return die("Clouds are specified, but no cloudy processes are included.");
+  // sbin/Cl_run_cdf:218-260: a convective type for each stratiform process
+  if (conv && ((drop_type && !conv_drop_type) || (ice_type && !conv_ice_type)))
+    return die("Types of convective particles have not been set.");
   if (mcica && (sampling < 0 || sampling > 2)) return die("The value of i_mcica_sampling is not valid.");
   if (!two_stream) two_stream = isolir == SOCGPU_IP_INFRA_RED ? 12 : 16;
   // the solver Cl_run_cdf picks for the cloud scheme (sbin/Cl_run_cdf:293-310)
   if (!solver)
-    solver = region ? SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN
+    solver = triple ? SOCGPU_IP_SOLVER_TRIPLE_HOGAN : region ? SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN
                     : scatter == SOCGPU_IP_SCATTER_FULL ? SOCGPU_IP_SOLVER_HOMOGEN_DIRECT : SOCGPU_IP_SOLVER_NO_SCAT;
 
   char msg[512] = "";
@@ -459,12 +476,23 @@ int main(int argc, char **argv) {
   if (clouds) {
     std::map<int, CloudTypeInfo> drops, ices;
     if (!read_cloud_types(sp_file, drops, ices)) return die("cannot open " + sp_file);
-    struct Comp { int phase, type; const char *mr, *dim; };
+    // components in the order of input_cloud_cdf.f (stratiform water and
+    // ice, then convective water and ice) with their ip_clcmp codes and the
+    // cloud type of each under the representation (input_cloud_cdf.f:640-760)
+    struct Comp { int clcmp, phase, type, cloud_type; const char *mr, *dim; };
     std::vector<Comp> comps;
-    if (drop_type) comps.push_back({SOCGPU_IP_PHASE_WATER, drop_type, "lwm", "re"});
-    if (ice_type) comps.push_back({SOCGPU_IP_PHASE_ICE, ice_type, "iwm", "ire"});
+    const bool csiw = representation == SOCGPU_IP_CLOUD_CSIW;
+    if (drop_type)
+      comps.push_back({SOCGPU_IP_CLCMP_ST_WATER, SOCGPU_IP_PHASE_WATER, drop_type, 1, "lwm", "re"});
+    if (ice_type)
+      comps.push_back({SOCGPU_IP_CLCMP_ST_ICE, SOCGPU_IP_PHASE_ICE, ice_type,
+                       representation == 1 || representation == SOCGPU_IP_CLOUD_CONV_STRAT ? 1 : 2, "iwm", "ire"});
+    if (conv && drop_type)
+      comps.push_back({SOCGPU_IP_CLCMP_CNV_WATER, SOCGPU_IP_PHASE_WATER, conv_drop_type, csiw ? 3 : 2, "lwmcv", "recv"});
+    if (conv && ice_type)
+      comps.push_back({SOCGPU_IP_CLCMP_CNV_ICE, SOCGPU_IP_PHASE_ICE, conv_ice_type, csiw ? 4 : 2, "iwmcv", "irecv"});
     nc = (int)comps.size();
-    n_cloud_type = representation == 1 ? 1 : 2;
+    n_cloud_type = representation == 1 ? 1 : csiw ? 4 : 2;
     cmr.assign(np * nl * nc, 0.0);
     dim.assign(np * nl * nc, 0.0);
     for (int k = 0; k < nc; ++k) {
@@ -474,8 +502,8 @@ int main(int argc, char **argv) {
       if (it == tab.end() || it->second.scheme == 0)
         return die(std::string(cp.phase == SOCGPU_IP_PHASE_WATER ? "droplet" : "ice") + " type " +
                    std::to_string(cp.type) + " is not in the spectral file");
-      type_condensed.push_back(cp.phase);
-      i_cloud_type.push_back(representation == 1 ? 1 : (cp.phase == SOCGPU_IP_PHASE_WATER ? 1 : 2));
+      type_condensed.push_back(cp.clcmp);
+      i_cloud_type.push_back(cp.cloud_type);
       i_condensed_param.push_back(it->second.scheme);
       i_condensed_type.push_back(cp.type);
       Field fm, fd;
@@ -488,7 +516,8 @@ int main(int argc, char **argv) {
       }
     }
     // cloud fractions of each type, normalised by their sum (input_cloud_cdf.f:760-790)
-    const char *frac_suffix[2] = {representation == 1 ? "clfr" : "wclfr", "iclfr"};
+    const char *frac_suffix[4] = {representation == 1 ? "clfr" : "wclfr", "iclfr", "wccfr", "iccfr"};
+    if (representation == SOCGPU_IP_CLOUD_CONV_STRAT) { frac_suffix[0] = "clfr"; frac_suffix[1] = "ccfr"; }
     frac_cloud.assign(np * nl * n_cloud_type, 0.0);
     w_cloud.assign(np * nl, 0.0);
     for (int t2 = 0; t2 < n_cloud_type; ++t2) {

@@ -116,7 +116,8 @@ def _three_region(sp, n, L, seed, solar, representation):
     mr, dc = c["condensed_mix_ratio"], c["condensed_dim_char"]
     f = lambda a: np.asfortranarray(a)
     cld = dict(c)
-    cld.update(n_condensed=4, type_condensed=[abi.IP_PHASE_WATER, abi.IP_PHASE_ICE] * 2,
+    cld.update(n_condensed=4, type_condensed=[abi.IP_CLCMP_ST_WATER, abi.IP_CLCMP_ST_ICE, abi.IP_CLCMP_CNV_WATER,
+                                              abi.IP_CLCMP_CNV_ICE],
                i_condensed_param=list(c["i_condensed_param"]) * 2, i_condensed_type=list(c["i_condensed_type"]) * 2,
                condensed_mix_ratio=f(np.concatenate([mr, mr * np.array([2.0, 1.5])], axis=2)),
                condensed_dim_char=f(np.concatenate([dc, dc], axis=2)))

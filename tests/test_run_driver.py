@@ -401,3 +401,49 @@ def test_driver_reproduces_circ6_sw_aerosol(gpu_lib, tmp_path, to_cdf):
     assert r.returncode == 0, r.stderr
     _, hr2 = field(str(base) + ".hrts")
     assert (np.abs(hr2 - kgo) / half_unit).max() > 1000.0
+
+
+@pytest.mark.gpu
+def test_driver_three_regions(gpu_lib, tmp_path):
+    """Three regions through the column driver (-C 6 -K 3, solver 17 by
+    default): the 7460_28 long-wave column with 40 % of its cloud made
+    convective (.ccfr) and denser convective water (.lwmcv), .clfr holding
+    the stratiform rest.  The written heating rates match the oracle on the
+    same clouds (set up as input_cloud_cdf.f does: stratiform water and ice
+    of type 1, convective water and ice of type 2) to half a unit of their
+    6th digit."""
+    import cld7460 as K
+    import oracle as O
+    from dataclasses import replace
+    from socrates_gb300 import abi
+    tool = _tool()
+    sp_path, base, wy, opts, _, _ = _cld7460_files(tmp_path, "lw_avg", False)
+    lev, clfr = field(str(base) + ".clfr")
+    _, lwm = field(str(base) + ".lwm")
+    lev, clfr, lwm = (np.asarray(a, dtype=np.float64).ravel() for a in (lev, clfr, lwm))
+    for suffix, vals in (("clfr", 0.6 * clfr), ("ccfr", 0.4 * clfr), ("lwmcv", 1.5 * lwm)):
+        write_cdl(tmp_path / f"7460_28.{suffix}", f"7460_28.{suffix}", [("lat", 1), ("lon", 1), ("plev", lev.size)],
+                  [("lat", ["lat"], [1.0], {}), ("lon", ["lon"], [0.0], {}),
+                   ("plev", ["plev"], lev, {"units": "Pa", "title": "PRESSURE"}),
+                   (suffix, ["plev", "lon", "lat"], np.reshape(vals, (lev.size, 1, 1)), {"units": "None"})], 17)
+    for src, dst in (("re", "recv"), ("iwm", "iwmcv"), ("ire", "irecv")):
+        text = (tmp_path / f"7460_28.{src}").read_text().replace(f"7460_28.{src}", f"7460_28.{dst}")
+        (tmp_path / f"7460_28.{dst}").write_text(text)
+    opts = "-R 1 9 -I -t 12 +R -g 2 -c -C 6 -K 3 -d 1 -i 1 +d 1 +i 1".split()
+    r = subprocess.run([tool, "-s", str(sp_path)] + opts + ["-B", str(base)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _, got = field(str(base) + ".hrts")
+    ctl, sp, col, _, _ = K.setup("lw_avg", K.spectra())
+    c = col.cld
+    w = c["w_cloud"]
+    mr, dc = c["condensed_mix_ratio"], c["condensed_dim_char"]
+    col.cld = dict(c, n_condensed=4, type_condensed=[1, 2, 3, 4], i_cloud_type=[1, 1, 2, 2], n_cloud_type=2,
+                   i_condensed_param=list(c["i_condensed_param"]) * 2, i_condensed_type=list(c["i_condensed_type"]) * 2,
+                   condensed_mix_ratio=np.asfortranarray(np.concatenate([mr, mr * np.array([1.5, 1.0])], axis=2)),
+                   condensed_dim_char=np.asfortranarray(np.concatenate([dc, dc], axis=2)),
+                   frac_cloud=np.asfortranarray(np.stack([np.where(w > 0, 0.6, 0.0), np.where(w > 0, 0.4, 0.0)],
+                                                         axis=2)))
+    ctl = replace(ctl, i_cloud=abi.IP_CLOUD_TRIPLE, i_solver=abi.IP_SOLVER_TRIPLE_HOGAN,
+                  i_cloud_representation=abi.IP_CLOUD_CONV_STRAT)
+    ref = K.printed(O.radiance_calc(ctl, sp, col), col, "hrts")[0]
+    assert K.half_units(got, ref).max() <= 1.05
