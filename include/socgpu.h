@@ -100,6 +100,7 @@ extern "C" {
 #define SOCGPU_IP_HOMOGENEOUS           0
 #define SOCGPU_IP_SCALING               1
 #define SOCGPU_IP_MCICA                 2
+#define SOCGPU_IP_TRIPLECLOUDS_2019     4   /* rad_pcf.F90:286 */
 /* droplet effective radius, rad_pcf.F90:356-360 */
 #define SOCGPU_IP_RE_EXTERNAL           2
 #define SOCGPU_IP_RE_LIU                3
@@ -630,10 +631,13 @@ typedef struct socgpu_runes_args {
     /* clouds (set_control's cloud options, set_cld, set_cld_dim,
        set_cld_mcica); 0 selects set_control's default */
     int i_cloud_representation;         /* 0 (off), SOCGPU_IP_CLOUD_HOMOGEN, _ICE_WATER, _COMBINE_HOMOGEN,
-                                           _COMBINE_ICE_WATER */
+                                           _COMBINE_ICE_WATER; three regions: _CONV_STRAT, _CSIW,
+                                           _SPLIT_HOMOGEN, _SPLIT_ICE_WATER */
     int i_overlap;                      /* SOCGPU_IP_MAX_RAND (0, the default), SOCGPU_IP_RAND,
                                            SOCGPU_IP_EXPONENTIAL_RAND (McICA only) */
-    int i_inhom;                        /* SOCGPU_IP_HOMOGENEOUS, SOCGPU_IP_SCALING, SOCGPU_IP_MCICA */
+    int i_inhom;                        /* SOCGPU_IP_HOMOGENEOUS, SOCGPU_IP_SCALING, SOCGPU_IP_MCICA,
+                                           SOCGPU_IP_TRIPLECLOUDS_2019 (the split representations'
+                                           thin and thick parts from the condensate RSD) */
     int i_cloud_entrapment;             /* SOCGPU_IP_ZERO_ENTRAPMENT (default: Hogan's solver) or
                                            SOCGPU_IP_MAX_ENTRAPMENT (solver_mix_direct) */
     int i_mcica_sampling;               /* SOCGPU_IP_MCICA_*_SAMPLING; -1 selects the default, optimal */
@@ -652,6 +656,17 @@ typedef struct socgpu_runes_args {
     double cloud_horizontal_rsd;        /* condensate RSD where liq_rsd / ice_rsd are NULL */
     const int *rand_seed;               /* (n_profile) McICA seeds; NULL: 10 + profile */
     const char *mcica_data;             /* path of the McICA data file (with SOCGPU_IP_MCICA) */
+    /* separate convective cloud (SOCGPU_IP_CLOUD_CONV_STRAT, _CSIW,
+       _SPLIT_HOMOGEN, _SPLIT_ICE_WATER): the convective droplet and ice
+       types, and the convective sizes and RSDs (set_cld_dim's liq_conv_dim,
+       ice_conv_dim, liq_conv_dim_constant; set_cld's liq_conv_rsd,
+       ice_conv_rsd).  The split representations size and bound their
+       convective (optically thick) part by the stratiform arguments. */
+    int i_cnv_water, i_cnv_ice;
+    const double *liq_conv_dim, *ice_conv_dim;  /* (n_profile, n_layer) [m] or NULL */
+    const double *liq_conv_rsd, *ice_conv_rsd;  /* (n_profile, n_layer) or NULL */
+    int has_liq_conv_dim_constant;
+    double liq_conv_dim_constant;       /* [m], with SOCGPU_IP_RE_CONSTANT */
 } socgpu_runes_args;
 
 /* StrDiag (socrates_def_diag.F90): NULL members are not filled. */
@@ -668,7 +683,8 @@ typedef struct socgpu_runes_diag {
  * of one homogeneous type or of separate water and ice types (and their
  * combinations with convective cloud) run in two regions with maximum-random
  * or random overlap, or with McICA subcolumns; the representations with
- * separate convective cloud (three regions) are refused. */
+ * separate convective cloud run in three regions (clear, stratiform and
+ * convective) with maximum-random overlap and Hogan's solver. */
 SOCGPU_API int socgpu_runes(const socgpu_runes_args *args, socgpu_runes_diag *diag, char *msg, size_t msg_len);
 
 /* ---- multi-batch launches (extension) -----------------------------------

@@ -96,6 +96,10 @@ TYPE, BIND(C) :: socgpu_runes_args
   INTEGER(c_int) :: has_liq_dim_constant, has_cloud_vertical_decorr, has_cloud_horizontal_rsd
   REAL(c_double) :: liq_dim_constant, cloud_vertical_decorr, cloud_horizontal_rsd
   TYPE(c_ptr)    :: rand_seed, mcica_data
+  INTEGER(c_int) :: i_cnv_water, i_cnv_ice
+  TYPE(c_ptr)    :: liq_conv_dim, ice_conv_dim, liq_conv_rsd, ice_conv_rsd
+  INTEGER(c_int) :: has_liq_conv_dim_constant
+  REAL(c_double) :: liq_conv_dim_constant
 END TYPE
 
 TYPE, BIND(C) :: socgpu_runes_diag

@@ -124,7 +124,7 @@ RUNES_N_AER = 33
 IP_CLOUD_CONV_STRAT, IP_CLOUD_CSIW, IP_CLOUD_OFF = 3, 4, 5
 IP_CLOUD_COMBINE_HOMOGEN, IP_CLOUD_COMBINE_ICE_WATER, IP_CLOUD_SPLIT_HOMOGEN, IP_CLOUD_SPLIT_ICE_WATER = 6, 7, 8, 9
 IP_MAX_ENTRAPMENT, IP_ZERO_ENTRAPMENT = 1, 2
-IP_HOMOGENEOUS, IP_SCALING, IP_MCICA = 0, 1, 2
+IP_HOMOGENEOUS, IP_SCALING, IP_MCICA, IP_TRIPLECLOUDS_2019 = 0, 1, 2, 4
 IP_RE_EXTERNAL, IP_RE_LIU, IP_RE_CONSTANT = 2, 3, 4
 IP_SOURCE_ILLUMINATE, IP_SOURCE_THERMAL = 1, 2
 
@@ -158,6 +158,9 @@ class RunesArgs(C.Structure):
         ("has_cloud_horizontal_rsd", C.c_int), ("liq_dim_constant", C.c_double),
         ("cloud_vertical_decorr", C.c_double), ("cloud_horizontal_rsd", C.c_double),
         ("rand_seed", _ip), ("mcica_data", C.c_char_p),
+        ("i_cnv_water", C.c_int), ("i_cnv_ice", C.c_int), ("liq_conv_dim", _dp), ("ice_conv_dim", _dp),
+        ("liq_conv_rsd", _dp), ("ice_conv_rsd", _dp), ("has_liq_conv_dim_constant", C.c_int),
+        ("liq_conv_dim_constant", C.c_double),
     ]
 
 

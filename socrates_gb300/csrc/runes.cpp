@@ -181,45 +181,66 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
   // clouds (socrates_set_control.F90:291-370, socrates_set_cld.F90,
   // socrates_set_cld_dim.F90, socrates_set_cld_mcica.F90)
   int rep = a->i_cloud_representation ? a->i_cloud_representation : SOCGPU_IP_CLOUD_OFF;
-  if (rep == SOCGPU_IP_CLOUD_CONV_STRAT || rep == SOCGPU_IP_CLOUD_CSIW || rep == SOCGPU_IP_CLOUD_SPLIT_HOMOGEN ||
-      rep == SOCGPU_IP_CLOUD_SPLIT_ICE_WATER) {
-    set_msg(msg, msg_len, "cloud representation %d (separate convective cloud: three regions) is not built", rep);
-    return SOCGPU_I_ERR_RANGE;
-  }
-  if (rep != SOCGPU_IP_CLOUD_OFF && rep != SOCGPU_IP_CLOUD_HOMOGEN && rep != SOCGPU_IP_CLOUD_ICE_WATER &&
-      rep != SOCGPU_IP_CLOUD_COMBINE_HOMOGEN && rep != SOCGPU_IP_CLOUD_COMBINE_ICE_WATER) {
+  if (rep < SOCGPU_IP_CLOUD_HOMOGEN || rep > SOCGPU_IP_CLOUD_SPLIT_ICE_WATER) {
     set_msg(msg, msg_len, "cloud representation %d unrecognised", rep);
     return SOCGPU_I_ERR_FATAL;
   }
   const bool clouds = rep != SOCGPU_IP_CLOUD_OFF;
-  const bool mcica = clouds && a->i_inhom == SOCGPU_IP_MCICA;
+  // separate convective cloud runs in clear, stratiform and convective
+  // regions; the split representations combine the two clouds and split the
+  // total into an optically thin and a thick part (socrates_set_cld.F90:215-229)
+  const bool split = rep == SOCGPU_IP_CLOUD_SPLIT_HOMOGEN || rep == SOCGPU_IP_CLOUD_SPLIT_ICE_WATER;
+  const bool conv_sep = split || rep == SOCGPU_IP_CLOUD_CONV_STRAT || rep == SOCGPU_IP_CLOUD_CSIW;
+  const bool four_types = rep == SOCGPU_IP_CLOUD_CSIW || rep == SOCGPU_IP_CLOUD_SPLIT_ICE_WATER;
+  // McICA does not take separate convective cloud (socrates_set_control.F90:336)
+  const int inhom = (conv_sep && a->i_inhom == SOCGPU_IP_MCICA) ? SOCGPU_IP_HOMOGENEOUS : a->i_inhom;
+  const bool mcica = clouds && inhom == SOCGPU_IP_MCICA;
   const bool homogen = rep == SOCGPU_IP_CLOUD_HOMOGEN || rep == SOCGPU_IP_CLOUD_COMBINE_HOMOGEN;
-  const bool combine = rep == SOCGPU_IP_CLOUD_COMBINE_HOMOGEN || rep == SOCGPU_IP_CLOUD_COMBINE_ICE_WATER;
+  const bool combine = split || rep == SOCGPU_IP_CLOUD_COMBINE_HOMOGEN || rep == SOCGPU_IP_CLOUD_COMBINE_ICE_WATER;
   const int scatter = a->i_scatter_method ? a->i_scatter_method : SOCGPU_IP_SCATTER_FULL;
   int i_cloud = SOCGPU_IP_CLOUD_CLEAR, solver = scatter == SOCGPU_IP_SCATTER_FULL ? SOCGPU_IP_SOLVER_HOMOGEN_DIRECT
                                                                                : SOCGPU_IP_SOLVER_NO_SCAT;
   if (clouds && !mcica) {
-    if (a->i_inhom != SOCGPU_IP_HOMOGENEOUS && a->i_inhom != SOCGPU_IP_SCALING) {
-      set_msg(msg, msg_len, "condensate inhomogeneity %d is not built for cloud regions", a->i_inhom);
-      return SOCGPU_I_ERR_RANGE;
-    }
-    if (a->i_overlap == SOCGPU_IP_EXPONENTIAL_RAND) {
-      set_msg(msg, msg_len, "exponential-random overlap of cloud regions (ip_cloud_part_corr) is not built");
+    if (inhom != SOCGPU_IP_HOMOGENEOUS && inhom != SOCGPU_IP_SCALING && inhom != SOCGPU_IP_TRIPLECLOUDS_2019) {
+      set_msg(msg, msg_len, "condensate inhomogeneity %d is not built for cloud regions", inhom);
       return SOCGPU_I_ERR_RANGE;
     }
     if (scatter != SOCGPU_IP_SCATTER_FULL) {
       set_msg(msg, msg_len, "cloud regions need the full scattering treatment");
       return SOCGPU_I_ERR_RANGE;
     }
-    i_cloud = a->i_overlap == SOCGPU_IP_MAX_RAND ? SOCGPU_IP_CLOUD_MIX_MAX : SOCGPU_IP_CLOUD_MIX_RANDOM;
-    solver = a->i_cloud_entrapment == SOCGPU_IP_MAX_ENTRAPMENT ? SOCGPU_IP_SOLVER_MIX_DIRECT
-                                                                : SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN;
+    if (conv_sep) {
+      if (a->i_overlap == SOCGPU_IP_EXPONENTIAL_RAND) {
+        set_msg(msg, msg_len, "exponential-random overlap of three regions (ip_cloud_part_corr_cnv) is not built");
+        return SOCGPU_I_ERR_RANGE;
+      }
+      if (a->i_overlap == SOCGPU_IP_RAND) {
+        // random overlap keeps two regions, whose solver (mix_column.F90:438-530)
+        // does not take solver_triple_hogan
+        set_msg(msg, msg_len, "***Error: The solver specified is not valid here.");
+        return SOCGPU_I_ERR_FATAL;
+      }
+      if (a->i_cloud_entrapment == SOCGPU_IP_MAX_ENTRAPMENT) {
+        set_msg(msg, msg_len, "maximal entrapment in three regions (solver_triple) is not built");
+        return SOCGPU_I_ERR_RANGE;
+      }
+      i_cloud = SOCGPU_IP_CLOUD_TRIPLE;
+      solver = SOCGPU_IP_SOLVER_TRIPLE_HOGAN;
+    } else {
+      if (a->i_overlap == SOCGPU_IP_EXPONENTIAL_RAND) {
+        set_msg(msg, msg_len, "exponential-random overlap of cloud regions (ip_cloud_part_corr) is not built");
+        return SOCGPU_I_ERR_RANGE;
+      }
+      i_cloud = a->i_overlap == SOCGPU_IP_MAX_RAND ? SOCGPU_IP_CLOUD_MIX_MAX : SOCGPU_IP_CLOUD_MIX_RANDOM;
+      solver = a->i_cloud_entrapment == SOCGPU_IP_MAX_ENTRAPMENT ? SOCGPU_IP_SOLVER_MIX_DIRECT
+                                                                  : SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN;
+    }
   } else if (mcica) {
     i_cloud = SOCGPU_IP_CLOUD_MCICA;
   }
   const int ict = (clouds && a->n_cloud_layer > 0) ? nl + 1 - std::min(a->n_cloud_layer, nl) : 1;
   const size_t ncl = (size_t)(nl - ict + 1), NC = NP * ncl;
-  const int nct = homogen ? 1 : 2;
+  const int nct = homogen ? 1 : (four_types ? 4 : 2);
   std::vector<double> cmr, cdim, w_cloud, frac_cloud, c_cloud, c_ratio, rsd_w;
   std::vector<int> type_condensed, i_cloud_type, i_condensed_param, i_condensed_type;
   McicaState mst;
@@ -234,10 +255,16 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
           dst[l + NP * k] = floor0 ? std::max(v, 0.0) : v;
         }
     };
-    // components: stratiform water (droplet type i_st_water) and ice
-    struct Comp { int phase, type; };
-    const Comp comps[2] = {{SOCGPU_IP_PHASE_WATER, a->i_st_water}, {SOCGPU_IP_PHASE_ICE, a->i_st_ice}};
-    const int nc = 2;
+    // condensed components (socrates_set_cld.F90:175-212): stratiform water
+    // and ice, then convective water and ice where convective cloud is separate
+    struct Comp { int clcmp, phase, type; bool conv; };
+    std::vector<Comp> comps = {{SOCGPU_IP_CLCMP_ST_WATER, SOCGPU_IP_PHASE_WATER, a->i_st_water, false},
+                               {SOCGPU_IP_CLCMP_ST_ICE, SOCGPU_IP_PHASE_ICE, a->i_st_ice, false}};
+    if (conv_sep) {
+      comps.push_back({SOCGPU_IP_CLCMP_CNV_WATER, SOCGPU_IP_PHASE_WATER, a->i_cnv_water, true});
+      comps.push_back({SOCGPU_IP_CLCMP_CNV_ICE, SOCGPU_IP_PHASE_ICE, a->i_cnv_ice, true});
+    }
+    const int nc = (int)comps.size();
     cmr.assign(NC * nc, 0.0);
     cdim.assign(NC * nc, 0.0);
     rsd_w.assign(NC * nc, 0.0);
@@ -245,7 +272,7 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
     c_ratio.assign(NC, 0.0);
     std::vector<double> tmp, rsd;
     for (int k = 0; k < nc; ++k) {
-      const bool water = comps[k].phase == SOCGPU_IP_PHASE_WATER;
+      const bool water = comps[k].phase == SOCGPU_IP_PHASE_WATER, conv = comps[k].conv;
       const int ty = comps[k].type;
       const std::vector<int> &schemes = water ? e->drop_scheme : e->ice_scheme;
       if (ty <= 0) {
@@ -256,77 +283,103 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
         set_msg(msg, msg_len, water ? "Liquid cloud type not in spectral file." : "Ice cloud type not in spectral file.");
         return SOCGPU_I_ERR_FATAL;
       }
-      type_condensed.push_back(comps[k].phase);
+      type_condensed.push_back(comps[k].clcmp);
       i_condensed_param.push_back(schemes[ty - 1]);
       i_condensed_type.push_back(ty);
-      i_cloud_type.push_back(homogen ? 1 : (water ? 1 : 2));
-      const double *mmr = water ? a->liq_mmr : a->ice_mmr, *conv = water ? a->liq_conv_mmr : a->ice_conv_mmr;
-      if (!mmr) { set_msg(msg, msg_len, water ? "Liquid MMR not provided." : "Ice MMR not provided."); return SOCGPU_I_ERR_FATAL; }
-      cfield(mmr, tmp, true);
-      std::copy(tmp.begin(), tmp.end(), cmr.begin() + NC * k);
-      if (combine && conv) {
-        cfield(conv, tmp, true);
-        for (size_t q = 0; q < NC; ++q) { cmr[q + NC * k] += tmp[q]; c_ratio[q] += tmp[q]; }
+      // the component's cloud type (socrates_set_cld.F90:475-660)
+      int ct;
+      if (homogen) ct = 1;
+      else if (four_types) ct = water ? (conv ? SOCGPU_IP_CLOUD_TYPE_CW : SOCGPU_IP_CLOUD_TYPE_SW)
+                                      : (conv ? SOCGPU_IP_CLOUD_TYPE_CI : SOCGPU_IP_CLOUD_TYPE_SI);
+      else if (conv_sep) ct = conv ? SOCGPU_IP_CLOUD_TYPE_CONV : SOCGPU_IP_CLOUD_TYPE_STRAT;
+      else ct = water ? SOCGPU_IP_CLOUD_TYPE_WATER : SOCGPU_IP_CLOUD_TYPE_ICE;
+      i_cloud_type.push_back(ct);
+      // grid-box mixing ratios; combined cloud adds the other part's condensate
+      const double *st = water ? a->liq_mmr : a->ice_mmr, *cv = water ? a->liq_conv_mmr : a->ice_conv_mmr;
+      double *dst = cmr.data() + NC * k;
+      if (!conv) {
+        if (!st) { set_msg(msg, msg_len, water ? "Liquid MMR not provided." : "Ice MMR not provided."); return SOCGPU_I_ERR_FATAL; }
+        cfield(st, tmp, true);
+        std::copy(tmp.begin(), tmp.end(), dst);
+        if (combine && cv) {
+          cfield(cv, tmp, true);
+          for (size_t q = 0; q < NC; ++q) { dst[q] += tmp[q]; c_ratio[q] += tmp[q]; }
+        }
+      } else {
+        if (cv) {
+          cfield(cv, tmp, true);
+          std::copy(tmp.begin(), tmp.end(), dst);
+        } else if (!split) {
+          set_msg(msg, msg_len, water ? "Convective liquid MMR not provided." : "Convective ice MMR not provided.");
+          return SOCGPU_I_ERR_FATAL;
+        }
+        if (combine && st) {
+          cfield(st, tmp, true);
+          for (size_t q = 0; q < NC; ++q) dst[q] += tmp[q];
+        }
       }
-      const double *rsd_src = water ? a->liq_rsd : a->ice_rsd;
+      const double *rsd_src = conv ? (water ? a->liq_conv_rsd : a->ice_conv_rsd) : (water ? a->liq_rsd : a->ice_rsd);
       if (rsd_src) cfield(rsd_src, rsd, true);
       else rsd.assign(NC, a->has_cloud_horizontal_rsd ? a->cloud_horizontal_rsd : 0.0);
       for (size_t q = 0; q < NC; ++q) {
-        if (a->i_inhom == SOCGPU_IP_SCALING) cmr[q + NC * k] /= (1.0 + rsd[q] * rsd[q]);
+        if (inhom == SOCGPU_IP_SCALING) dst[q] /= (1.0 + rsd[q] * rsd[q]);
         rsd_w[q + NC * k] = rsd[q];
       }
     }
-    // fractions (socrates_set_cld.F90:475-565)
+    // fractions (socrates_set_cld.F90:475-790)
     frac_cloud.assign(NC * nct, 0.0);
+    auto fr = [&](int type) { return frac_cloud.data() + NC * (size_t)(type - 1); };
+    auto put = [&](int type, const std::vector<double> &v) { std::copy(v.begin(), v.end(), fr(type)); };
+    // split a mixed-phase fraction between ice and liquid by the ratio of
+    // their in-cloud mixing ratios (split_mix_phase, socrates_set_cld.F90:905-935),
+    // then share the total out in proportion
+    auto split_phase = [&](std::vector<double> &fl, std::vector<double> &fi, const std::vector<double> &f, int tw,
+                           int ti) {
+      for (size_t q = 0; q < NC; ++q) {
+        if (fl[q] + fi[q] > eps) {
+          const double mix = fl[q] + fi[q] - f[q];
+          if (mix > eps && fl[q] > eps && fi[q] > eps) {
+            double lm = 0.0, im = 0.0;
+            for (int k = 0; k < nc; ++k) {
+              if (i_cloud_type[k] == tw) lm += cmr[q + NC * k] / fl[q];
+              else if (i_cloud_type[k] == ti) im += cmr[q + NC * k] / fi[q];
+            }
+            if (lm + im > eps) {
+              fl[q] = std::max(fl[q] - mix * im / (lm + im), 0.0);
+              fi[q] = std::max(fi[q] - mix * lm / (lm + im), 0.0);
+            }
+          }
+          const double s2 = fl[q] + fi[q];
+          const double nl_ = f[q] * fl[q] / s2, ni_ = f[q] * fi[q] / s2;
+          fl[q] = nl_;
+          fi[q] = ni_;
+        } else {
+          fl[q] = 0.0;
+          fi[q] = 0.0;
+        }
+      }
+    };
     if (homogen) {
       if (!a->cloud_frac) { set_msg(msg, msg_len, "Cloud fraction not provided."); return SOCGPU_I_ERR_FATAL; }
       cfield(a->cloud_frac, tmp, true);
-      std::copy(tmp.begin(), tmp.end(), frac_cloud.begin());
+      put(1, tmp);
       if (combine && a->conv_frac) {
         cfield(a->conv_frac, c_cloud, true);
         for (size_t q = 0; q < NC; ++q) frac_cloud[q] += c_cloud[q];
       }
-    } else {
-      // split a mixed-phase fraction between ice and liquid by the ratio of
-      // their in-cloud mixing ratios
-      auto split = [&](std::vector<double> &fl, std::vector<double> &fi, const std::vector<double> &f, int tw,
-                       int ti) {
-        for (size_t q = 0; q < NC; ++q) {
-          if (fl[q] + fi[q] > eps) {
-            const double mix = fl[q] + fi[q] - f[q];
-            if (mix > eps && fl[q] > eps && fi[q] > eps) {
-              double lm = 0.0, im = 0.0;
-              for (int k = 0; k < nc; ++k) {
-                if (i_cloud_type[k] == tw) lm += cmr[q + NC * k] / fl[q];
-                else if (i_cloud_type[k] == ti) im += cmr[q + NC * k] / fi[q];
-              }
-              if (lm + im > eps) {
-                fl[q] = std::max(fl[q] - mix * im / (lm + im), 0.0);
-                fi[q] = std::max(fi[q] - mix * lm / (lm + im), 0.0);
-              }
-            }
-            const double s2 = fl[q] + fi[q];
-            const double nl_ = f[q] * fl[q] / s2, ni_ = f[q] * fi[q] / s2;
-            fl[q] = nl_;
-            fi[q] = ni_;
-          } else {
-            fl[q] = 0.0;
-            fi[q] = 0.0;
-          }
-        }
-      };
+    } else if (!conv_sep) {
       std::vector<double> fl, fi, f;
       if (a->liq_frac && a->ice_frac && a->cloud_frac) {
         cfield(a->liq_frac, fl, true); cfield(a->ice_frac, fi, true); cfield(a->cloud_frac, f, true);
-        split(fl, fi, f, 1, 2);
+        split_phase(fl, fi, f, 1, 2);
       } else if (a->liq_frac && a->ice_frac) {
         cfield(a->liq_frac, fl, true); cfield(a->ice_frac, fi, true);
       } else {
         set_msg(msg, msg_len, "Liquid and ice cloud fractions not provided.");
         return SOCGPU_I_ERR_FATAL;
       }
-      std::copy(fl.begin(), fl.end(), frac_cloud.begin());
-      std::copy(fi.begin(), fi.end(), frac_cloud.begin() + NC);
+      put(1, fl);
+      put(2, fi);
       if (combine && a->liq_conv_frac && a->ice_conv_frac) {
         std::vector<double> cl, ci, cf;
         cfield(a->liq_conv_frac, cl, true); cfield(a->ice_conv_frac, ci, true);
@@ -359,6 +412,90 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
           c_cloud[q] = cl[q] + ci[q];
         }
       }
+    } else if (!four_types) {
+      // stratiform and convective types (socrates_set_cld.F90:567-600)
+      if (a->cloud_frac && a->conv_frac) {
+        cfield(a->cloud_frac, tmp, true);
+        put(SOCGPU_IP_CLOUD_TYPE_STRAT, tmp);
+        cfield(a->conv_frac, tmp, true);
+        put(SOCGPU_IP_CLOUD_TYPE_CONV, tmp);
+      } else if (split && a->cloud_frac) {
+        cfield(a->cloud_frac, tmp, true);
+        put(SOCGPU_IP_CLOUD_TYPE_STRAT, tmp);
+      } else {
+        set_msg(msg, msg_len, "Cloud fractions not provided.");
+        return SOCGPU_I_ERR_FATAL;
+      }
+    } else {
+      // stratiform and convective water and ice (socrates_set_cld.F90:642-747)
+      std::vector<double> fl, fi, f;
+      if (a->liq_frac && a->ice_frac && a->cloud_frac) {
+        cfield(a->liq_frac, fl, true); cfield(a->ice_frac, fi, true); cfield(a->cloud_frac, f, true);
+        split_phase(fl, fi, f, SOCGPU_IP_CLOUD_TYPE_SW, SOCGPU_IP_CLOUD_TYPE_SI);
+      } else if (a->liq_frac && a->ice_frac) {
+        cfield(a->liq_frac, fl, true); cfield(a->ice_frac, fi, true);
+      } else {
+        set_msg(msg, msg_len, "Liquid and ice cloud fractions not provided.");
+        return SOCGPU_I_ERR_FATAL;
+      }
+      put(SOCGPU_IP_CLOUD_TYPE_SW, fl);
+      put(SOCGPU_IP_CLOUD_TYPE_SI, fi);
+      if (a->liq_conv_frac && a->ice_conv_frac && a->conv_frac) {
+        cfield(a->liq_conv_frac, fl, true); cfield(a->ice_conv_frac, fi, true); cfield(a->conv_frac, f, true);
+        split_phase(fl, fi, f, SOCGPU_IP_CLOUD_TYPE_CW, SOCGPU_IP_CLOUD_TYPE_CI);
+      } else if (a->liq_conv_frac && a->ice_conv_frac) {
+        cfield(a->liq_conv_frac, fl, true); cfield(a->ice_conv_frac, fi, true);
+      } else if (split) {
+        fl.assign(NC, 0.0);
+        fi.assign(NC, 0.0);
+      } else {
+        set_msg(msg, msg_len, "Liquid and ice convective cloud fractions not provided.");
+        return SOCGPU_I_ERR_FATAL;
+      }
+      put(SOCGPU_IP_CLOUD_TYPE_CW, fl);
+      put(SOCGPU_IP_CLOUD_TYPE_CI, fi);
+    }
+    if (split) {
+      // the combined cloud split into an optically thin and a thick part
+      // (socrates_set_cld.F90:602-640, 749-790): by the condensate RSD with
+      // equations A1 and A2 of Hogan et al. (2019), else in equal halves
+      for (int ph = 0; ph < (four_types ? 2 : 1); ++ph) {
+        const int thin = four_types ? (ph == 0 ? SOCGPU_IP_CLOUD_TYPE_SW : SOCGPU_IP_CLOUD_TYPE_SI)
+                                    : SOCGPU_IP_CLOUD_TYPE_STRAT;
+        const int thick = four_types ? (ph == 0 ? SOCGPU_IP_CLOUD_TYPE_CW : SOCGPU_IP_CLOUD_TYPE_CI)
+                                     : SOCGPU_IP_CLOUD_TYPE_CONV;
+        double *ft = fr(thin), *fk = fr(thick);
+        for (size_t q = 0; q < NC; ++q) {
+          const double frac = ft[q] + fk[q];
+          if (inhom != SOCGPU_IP_TRIPLECLOUDS_2019) {
+            ft[q] = 0.5 * frac;
+            fk[q] = 0.5 * frac;
+            continue;
+          }
+          // one RSD per part: the thin type's own (water and ice apart), or
+          // the condensate-weighted mean over the stratiform components
+          double r = 0.0;
+          if (four_types) {
+            for (int k = 0; k < nc; ++k)
+              if (i_cloud_type[k] == thin) r = rsd_w[q + NC * k];
+          } else {
+            double num = 0.0, den = 0.0;
+            for (int k = 0; k < nc; ++k)
+              if (i_cloud_type[k] == thin) { num += rsd_w[q + NC * k] * cmr[q + NC * k]; den += cmr[q + NC * k]; }
+            r = num / std::max(den, eps);
+          }
+          const double f_thin = std::max(0.5, std::min(0.9, r * (0.4 / 2.25) + 0.525 / 2.25));
+          ft[q] = frac * f_thin;
+          fk[q] = frac * (1.0 - f_thin);
+          const double ratio = 0.025 + 0.975 * std::exp(-r - r * r / 2.0 - r * r * r / 4.0);
+          for (int k = 0; k < nc; ++k) {
+            if (i_cloud_type[k] == thin) cmr[q + NC * k] *= ratio * f_thin;
+            else if (i_cloud_type[k] == thick) cmr[q + NC * k] *= 1.0 - ratio * f_thin;
+          }
+        }
+      }
+      if (inhom != SOCGPU_IP_TRIPLECLOUDS_2019)
+        for (double &v : cmr) v *= 0.5;
     }
     std::vector<double> cond_total;
     if (combine) {
@@ -389,25 +526,29 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
       if (w > 1.0 + min_cloud_fraction) { set_msg(msg, msg_len, "Cloud fraction greater than 1."); return SOCGPU_I_ERR_FATAL; }
       w_cloud[q] = std::min(w, 1.0);
     }
-    // effective dimensions (socrates_set_cld_dim.F90:155-230)
+    // effective dimensions (socrates_set_cld_dim.F90:155-230); the split
+    // representations size and bound their convective part as the stratiform one
     for (int k = 0; k < nc; ++k) {
-      const bool water = type_condensed[k] == SOCGPU_IP_PHASE_WATER;
+      const bool water = comps[k].phase == SOCGPU_IP_PHASE_WATER, own = comps[k].conv && !split;
       double *dst = cdim.data() + NC * k;
+      const double *ice_src = own ? a->ice_conv_dim : a->ice_dim;
       if (water) {
         const int re = a->i_drop_re ? a->i_drop_re : SOCGPU_IP_RE_EXTERNAL;
-        if (re == SOCGPU_IP_RE_EXTERNAL && a->liq_dim) {
-          cfield(a->liq_dim, tmp, false);
+        const double *src = own ? a->liq_conv_dim : a->liq_dim;
+        const bool has_c = own ? a->has_liq_conv_dim_constant : a->has_liq_dim_constant;
+        if (re == SOCGPU_IP_RE_EXTERNAL && src) {
+          cfield(src, tmp, false);
           std::copy(tmp.begin(), tmp.end(), dst);
-        } else if (re == SOCGPU_IP_RE_CONSTANT && a->has_liq_dim_constant) {
-          std::fill(dst, dst + NC, a->liq_dim_constant);
+        } else if (re == SOCGPU_IP_RE_CONSTANT && has_c) {
+          std::fill(dst, dst + NC, own ? a->liq_conv_dim_constant : a->liq_dim_constant);
         } else if (re == SOCGPU_IP_RE_LIU) {
           set_msg(msg, msg_len, "droplet radii from droplet numbers (ip_re_liu) are not mapped; give liq_dim");
           return SOCGPU_I_ERR_RANGE;
         } else {
           std::fill(dst, dst + NC, 7.0e-6);
         }
-      } else if (a->ice_dim) {
-        cfield(a->ice_dim, tmp, false);
+      } else if (ice_src) {
+        cfield(ice_src, tmp, false);
         std::copy(tmp.begin(), tmp.end(), dst);
       } else {
         // set_ice_dim: sizes from the layer temperature
@@ -437,7 +578,7 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
           }
       }
       const std::vector<double> &lo = water ? e->drop_min_dim : e->ice_min_dim, &hi = water ? e->drop_max_dim : e->ice_max_dim;
-      const int ty = i_condensed_type[k];
+      const int ty = own ? comps[k].type : (water ? a->i_st_water : a->i_st_ice);
       if (ty <= (int)lo.size() && ty <= (int)hi.size())
         for (size_t q = 0; q < NC; ++q) dst[q] = std::min(std::max(dst[q], lo[ty - 1]), hi[ty - 1]);
     }
@@ -498,7 +639,7 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
   c.i_scatter_method = scatter;
   c.i_solver = solver;
   c.i_cloud = i_cloud;
-  c.i_cloud_representation = clouds ? (homogen ? SOCGPU_IP_CLOUD_HOMOGEN : SOCGPU_IP_CLOUD_ICE_WATER) : 0;
+  c.i_cloud_representation = !clouds ? 0 : conv_sep ? rep : (homogen ? SOCGPU_IP_CLOUD_HOMOGEN : SOCGPU_IP_CLOUD_ICE_WATER);
   c.i_gas_overlap = a->i_gas_overlap ? a->i_gas_overlap : SOCGPU_IP_OVERLAP_K_EQV_SCL;
   c.i_direct_tau = SOCGPU_IP_DIRECT_DELTA_SCALING;
   c.l_rescale = 1;
@@ -520,7 +661,7 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
   dm.nd_layer = nl;
   dm.id_cloud_top = ict;
   dm.nd_aerosol_mode = std::max(1, a->n_aer_mode);
-  dm.nd_cloud_component = 2;
+  dm.nd_cloud_component = std::max(2, (int)type_condensed.size());
   dm.nd_cloud_type = nct;
   dm.nd_subcol_gen = mcica ? mst.gen : 1;
   dm.nd_subcol_req = mcica ? mst.n_subcol_req : 1;

@@ -42,7 +42,8 @@ AEROSOL_NAMES = ["water_soluble", "dust_like", "oceanic", "soot", "ash", "sulphu
                  "nitrate", "twobindust_1", "twobindust_2"]
 AEROSOL_ID = {name: i + 1 for i, name in enumerate(AEROSOL_NAMES) if name}
 CLOUD_ARRAYS = ("cloud_frac", "conv_frac", "liq_frac", "ice_frac", "liq_conv_frac", "ice_conv_frac", "liq_mmr",
-                "ice_mmr", "liq_conv_mmr", "ice_conv_mmr", "liq_dim", "ice_dim", "liq_rsd", "ice_rsd")
+                "ice_mmr", "liq_conv_mmr", "ice_conv_mmr", "liq_dim", "ice_dim", "liq_rsd", "ice_rsd",
+                "liq_conv_dim", "ice_conv_dim", "liq_conv_rsd", "ice_conv_rsd")
 
 
 def set_spectrum(spectrum_name: str, spectral_file=None, spectrum: Spectrum | None = None, wenyi_file=None,
@@ -75,7 +76,8 @@ def runes(n_profile: int, n_layer: int, spectrum_name: str, i_source: int, *, p_
           precision=abi.PRECISION_FP64, mean_rel_humidity=None, i_cloud_representation=0, i_overlap=0,
           i_inhom=0, i_cloud_entrapment=0, i_mcica_sampling=-1, i_st_water=0, i_st_ice=0, i_drop_re=0,
           n_cloud_layer=0, liq_dim_constant=None, cloud_vertical_decorr=None, cloud_horizontal_rsd=None,
-          rand_seed=None, mcica_data=None, **kw) -> dict:
+          rand_seed=None, mcica_data=None, i_cnv_water=0, i_cnv_ice=0, liq_conv_dim_constant=None,
+          **kw) -> dict:
     """runes (socrates_runes.F90:47) through socgpu_runes.  Gases are passed
     by the reference's names: <gas> a profile (n_profile, n_layer),
     <gas>_mix_ratio a well-mixed value, l_<gas>_well_mixed to prefer it.
@@ -116,8 +118,9 @@ def runes(n_profile: int, n_layer: int, spectrum_name: str, i_source: int, *, p_
     a.i_cloud_entrapment, a.i_mcica_sampling = int(i_cloud_entrapment), int(i_mcica_sampling)
     a.i_st_water, a.i_st_ice, a.i_drop_re, a.n_cloud_layer = int(i_st_water), int(i_st_ice), int(i_drop_re), \
         int(n_cloud_layer)
+    a.i_cnv_water, a.i_cnv_ice = int(i_cnv_water), int(i_cnv_ice)
     for name, val in (("liq_dim_constant", liq_dim_constant), ("cloud_vertical_decorr", cloud_vertical_decorr),
-                      ("cloud_horizontal_rsd", cloud_horizontal_rsd)):
+                      ("cloud_horizontal_rsd", cloud_horizontal_rsd), ("liq_conv_dim_constant", liq_conv_dim_constant)):
         if val is not None:
             setattr(a, name, float(val))
             setattr(a, "has_" + name, 1)

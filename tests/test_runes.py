@@ -119,6 +119,124 @@ def test_runes_surface_and_gas_options(ga9, O):
         assert e <= 1e-10, f"{k}: scaled error {e:.2e}"
 
 
+def _repeated(col, n):
+    """The driver's single column repeated n times."""
+    from socrates_gb300.synth import Column
+    rep = lambda a: np.asfortranarray(np.repeat(a, n, axis=0))
+    c = Column(n, col.n_layer, rep(col.p), rep(col.t), rep(col.p_level), rep(col.t_level), rep(col.mass),
+               rep(col.gas_mix_ratio), z=np.zeros((n, col.n_layer)), t_ground=np.repeat(col.t_ground, n),
+               density=rep(col.density))
+    c.rho_alb = rep(col.rho_alb)
+    for k in ("zen_0", "solar_irrad"):
+        if getattr(col, k, None) is not None:
+            setattr(c, k, np.repeat(getattr(col, k), n))
+    return c
+
+
+def _cloud_fields(n, L, seed):
+    """Stratiform and convective cloud in the lower two thirds: fractions whose
+    liquid and ice parts overlap (a mixed-phase share to split), grid-box
+    mixing ratios, sizes and relative standard deviations, by the names of
+    set_cld and set_cld_dim."""
+    rng = np.random.default_rng(seed)
+    cloudy = rng.uniform(size=(n, L)) < 0.6
+    cloudy[:, : L // 3] = False
+    u = lambda lo, hi: np.asfortranarray(np.where(cloudy, rng.uniform(lo, hi, size=(n, L)), 0.0))
+    cf, cv = u(0.1, 0.6), u(0.0, 0.35)
+    return dict(cloud_frac=cf, conv_frac=cv, liq_frac=cf * u(0.4, 1.0), ice_frac=cf * u(0.4, 1.0),
+                liq_conv_frac=cv * u(0.4, 1.0), ice_conv_frac=cv * u(0.4, 1.0),
+                liq_mmr=u(1e-5, 3e-4), ice_mmr=u(0.0, 1e-4), liq_conv_mmr=u(2e-5, 6e-4), ice_conv_mmr=u(0.0, 2e-4),
+                liq_dim=u(5e-6, 1.5e-5), ice_dim=u(2e-5, 8e-5), liq_conv_dim=u(6e-6, 2e-5),
+                ice_conv_dim=u(3e-5, 1e-4), liq_rsd=u(0.3, 1.5), ice_rsd=u(0.3, 1.5), liq_conv_rsd=u(0.3, 1.5),
+                ice_conv_rsd=u(0.3, 1.5))
+
+
+CLOUD_CASES = [
+    (abi.IP_CLOUD_HOMOGEN, {}),
+    (abi.IP_CLOUD_ICE_WATER, dict(i_inhom=abi.IP_SCALING)),
+    (abi.IP_CLOUD_COMBINE_HOMOGEN, dict(i_overlap=abi.IP_RAND)),
+    (abi.IP_CLOUD_COMBINE_ICE_WATER, dict(i_cloud_entrapment=abi.IP_MAX_ENTRAPMENT)),
+    (abi.IP_CLOUD_CONV_STRAT, dict(ice_dim=None)),              # stratiform ice sizes from temperature
+    (abi.IP_CLOUD_CSIW, dict(i_inhom=abi.IP_SCALING, n_cloud_layer=20)),
+    (abi.IP_CLOUD_SPLIT_HOMOGEN, dict(i_inhom=abi.IP_TRIPLECLOUDS_2019)),
+    (abi.IP_CLOUD_SPLIT_ICE_WATER, dict(liq_conv_mmr=None, ice_conv_mmr=None, liq_conv_frac=None,
+                                        ice_conv_frac=None)),
+    (abi.IP_CLOUD_SPLIT_ICE_WATER, dict(i_inhom=abi.IP_TRIPLECLOUDS_2019)),
+]
+THREE = (abi.IP_CLOUD_CONV_STRAT, abi.IP_CLOUD_CSIW, abi.IP_CLOUD_SPLIT_HOMOGEN, abi.IP_CLOUD_SPLIT_ICE_WATER)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("section", ["sw", "lw_tground"])
+@pytest.mark.parametrize("case", range(len(CLOUD_CASES)))
+def test_runes_clouds(ga9, O, section, case):
+    """Every cloud representation through socgpu_runes (set_control's scheme
+    and solver, set_cld's components, types, fractions, mixed-phase split
+    and thin/thick split, set_cld_dim's sizes) on 4 columns against the
+    oracle's radiance_calc on the fields a numpy restatement of set_cld
+    makes: FP64 within 1e-10 of the largest flux.  The three-region
+    representations use convective ice of another type (Pade, type 12)."""
+    import set_cld as SC
+    from dataclasses import replace
+    d, sw, lw = ga9
+    rep, opts = CLOUD_CASES[case]
+    n = 4
+    kw = RC.runes_kwargs(d, section)
+    for k in ("p_layer", "t_layer", "mass", "density", "layer_heat_capacity", "h2o", "o3", "t_level"):
+        if k in kw:
+            kw[k] = np.asfortranarray(np.repeat(kw[k], n, axis=0))
+    for k in ("cos_zenith_angle", "solar_irrad", "t_ground"):
+        if k in kw:
+            kw[k] = np.repeat(kw[k], n)
+    fields = {**_cloud_fields(n, 32, seed=70 + case), **opts}
+    types = dict(i_st_water=5, i_st_ice=8, i_cnv_water=5, i_cnv_ice=12)
+    diag = RN.runes(n_profile=n, **{k: v for k, v in kw.items() if k != "n_profile"}, i_cloud_representation=rep,
+                    **types, **{k: v for k, v in fields.items() if v is not None})
+    ctl, sp, col = RC.direct_case(d, sw, lw, section)
+    col = _repeated(col, n)
+    arrays = {k: v for k, v in fields.items() if k not in ("i_inhom", "i_overlap", "i_cloud_entrapment")}
+    cld, ict = SC.set_cld(sp, kw["t_layer"], rep, i_inhom=opts.get("i_inhom", abi.IP_HOMOGENEOUS), **types, **arrays)
+    col.cld = cld
+    if rep in THREE:
+        ctl = replace(ctl, i_cloud=abi.IP_CLOUD_TRIPLE, i_solver=abi.IP_SOLVER_TRIPLE_HOGAN, i_cloud_representation=rep)
+    else:
+        homogen = rep in (abi.IP_CLOUD_HOMOGEN, abi.IP_CLOUD_COMBINE_HOMOGEN)
+        ctl = replace(ctl, i_cloud=abi.IP_CLOUD_MIX_RANDOM if opts.get("i_overlap") == abi.IP_RAND
+                      else abi.IP_CLOUD_MIX_MAX,
+                      i_solver=abi.IP_SOLVER_MIX_DIRECT if opts.get("i_cloud_entrapment") == abi.IP_MAX_ENTRAPMENT
+                      else abi.IP_SOLVER_MIX_DIRECT_HOGAN,
+                      i_cloud_representation=abi.IP_CLOUD_HOMOGEN if homogen else abi.IP_CLOUD_ICE_WATER)
+    ref = O.radiance_calc(ctl, sp, col, id_cloud_top=ict)
+    clear = O.radiance_calc(replace(ctl, i_cloud=abi.IP_CLOUD_CLEAR, i_solver=abi.IP_SOLVER_HOMOGEN_DIRECT), sp, col)
+    assert np.abs(ref["flux_up"] - clear["flux_up"]).max() > 1.0          # the clouds matter
+    scale = max(np.abs(ref["flux_down"]).max(), np.abs(ref["flux_up"]).max())
+    for k in ("flux_down", "flux_up") + (("flux_direct",) if section == "sw" else ()):
+        e = np.abs(diag[k] - ref[k]).max() / scale
+        assert e <= 1e-10, f"{k}: scaled error {e:.2e}"
+
+
+@pytest.mark.gpu
+def test_runes_three_region_refusals(ga9):
+    """Separate convective cloud: random overlap leaves two regions whose
+    solver does not take solver_triple_hogan (mix_column.F90:526-530);
+    exponential-random overlap and maximal entrapment are not built; the
+    convective mixing ratios are required unless the cloud is split."""
+    d, _, _ = ga9
+    kw = RC.runes_kwargs(d, "lw_tground")
+    fields = _cloud_fields(1, 32, seed=5)
+    base = dict(kw, i_cloud_representation=abi.IP_CLOUD_CSIW, i_st_water=5, i_st_ice=8, i_cnv_water=5, i_cnv_ice=8,
+                **fields)
+    for extra, status, words in ((dict(i_overlap=abi.IP_RAND), abi.I_ERR_FATAL, "solver specified is not valid"),
+                                 (dict(i_overlap=abi.IP_EXPONENTIAL_RAND), abi.I_ERR_RANGE, "part_corr_cnv"),
+                                 (dict(i_cloud_entrapment=abi.IP_MAX_ENTRAPMENT), abi.I_ERR_RANGE, "solver_triple"),
+                                 (dict(liq_conv_mmr=None), abi.I_ERR_FATAL, "Convective liquid MMR not provided"),
+                                 (dict(i_cnv_ice=0), abi.I_ERR_FATAL, "Prescribed ice cloud")):
+        args = {k: v for k, v in {**base, **extra}.items() if v is not None}
+        with pytest.raises(RadianceError) as e:
+            RN.runes(**args)
+        assert e.value.status == status and words in str(e.value), (extra, str(e.value))
+
+
 # ---------------------------------------------------------------------------
 # host side (no GPU)
 
