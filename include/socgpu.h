@@ -131,6 +131,7 @@ extern "C" {
 #define SOCGPU_IP_ICE_FU_PHF           12   /* Fu's ice fits, one phase-function moment (opt_prop_fu_phf_mod.F90) */
 #define SOCGPU_IP_ICE_PADE_2_PHF       20
 /* gas overlap, rad_pcf.F90:427 */
+#define SOCGPU_IP_OVERLAP_HYBRID        0   /* rad_pcf.F90:423: each band's method from the spectral file */
 #define SOCGPU_IP_OVERLAP_RANDOM        2
 #define SOCGPU_IP_OVERLAP_K_EQV_SCL     4   /* rad_pcf.F90:432: equivalent extinction of minor gases */
 #define SOCGPU_IP_OVERLAP_K_EQV         5   /* rad_pcf.F90:434: solved as K_EQV_SCL */
@@ -285,6 +286,11 @@ typedef struct socgpu_spectrum_desc {
        i_ice_parm; NULL: no limits (set_cld_dim clamps sizes to them) */
     const double *drop_parm_min_dim, *drop_parm_max_dim;
     const double *ice_parm_min_dim, *ice_parm_max_dim;
+    /* the gas overlap method each band names (block 4 version 1,
+       Sp%Gas%i_overlap, read_spectrum.F90:1012-1016), which a control of
+       SOCGPU_IP_OVERLAP_HYBRID takes (radiance_calc.F90:888-893); NULL or 0:
+       none named */
+    const int *i_overlap;               /* (nd_band) */
 } socgpu_spectrum_desc;
 
 typedef int32_t socgpu_spectrum_handle;   /* > 0 when valid */
@@ -298,7 +304,8 @@ typedef struct socgpu_control {
     int i_solver;               /* SOCGPU_IP_SOLVER_NO_SCAT | SOLVER_HOMOGEN_DIRECT */
     int i_cloud;                /* SOCGPU_IP_CLOUD_CLEAR | SOCGPU_IP_CLOUD_MCICA */
     int i_cloud_representation; /* SOCGPU_IP_CLOUD_ICE_WATER with McICA */
-    int i_gas_overlap;          /* SOCGPU_IP_OVERLAP_RANDOM | K_EQV_SCL (K_EQV, K_EQV_MOD alike) */
+    int i_gas_overlap;          /* SOCGPU_IP_OVERLAP_RANDOM | K_EQV_SCL (K_EQV, K_EQV_MOD alike) | HYBRID
+                                   (the method the spectrum's bands name; the bands of the call must agree) */
     int i_direct_tau;           /* SOCGPU_IP_DIRECT_DELTA_SCALING (default) | NOSCALING; CSR_SCALING refused */
     int l_rescale;              /* delta-rescaling of tau, omega and the phase function */
     int n_order_forward;        /* order of the forward-scattering term (2: f = g^2) */

@@ -32,7 +32,7 @@ IP_PHASE_WATER, IP_PHASE_ICE = 1, 2
 IP_CLCMP_ST_WATER, IP_CLCMP_ST_ICE, IP_CLCMP_CNV_WATER, IP_CLCMP_CNV_ICE = 1, 2, 3, 4
 IP_DROP_PADE_2, IP_ICE_PADE_2_PHF = 5, 20
 IP_SLINGO_SCHRECKER, IP_SLINGO_SCHRECKER_ICE, IP_ICE_FU_PHF = 1, 1, 12
-IP_OVERLAP_RANDOM = 2
+IP_OVERLAP_HYBRID, IP_OVERLAP_RANDOM = 0, 2
 IP_OVERLAP_K_EQV_SCL, IP_OVERLAP_K_EQV, IP_OVERLAP_K_EQV_MOD = 4, 5, 6
 IP_SCALE_NULL, IP_SCALE_BAND, IP_SCALE_TERM = 0, 1, 2
 IP_SCALE_FNC_NULL, IP_SCALE_POWER_LAW, IP_SCALE_POWER_QUAD, IP_SCALE_DOPPLER_QUAD = 0, 1, 2, 3
@@ -85,6 +85,7 @@ class SpectrumDesc(C.Structure):
         ("n_aerosol_phf_term", _ip), ("aerosol_humidities", _dp), ("aerosol_abs", _dp), ("aerosol_scat", _dp),
         ("aerosol_phf", _dp),
         ("drop_parm_min_dim", _dp), ("drop_parm_max_dim", _dp), ("ice_parm_min_dim", _dp), ("ice_parm_max_dim", _dp),
+        ("i_overlap", _ip),
     ]
 
 

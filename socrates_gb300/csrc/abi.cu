@@ -29,9 +29,19 @@ namespace socgpu {
 
 // The equivalent-extinction overlaps (rad_pcf.F90:432-436), all solved by
 // solve_band_k_eqv_scl.
-bool is_keqv(const socgpu_control *c) {
-  return c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV_SCL || c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV ||
-         c->i_gas_overlap == SOCGPU_IP_OVERLAP_K_EQV_MOD;
+int gas_overlap(const socgpu_control *c, const SpectrumEntry *sp) {
+  if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_HYBRID) return c->i_gas_overlap;
+  const int nb = (int)sp->band_overlap.size();
+  const int b0 = std::max(c->first_band, 1), b1 = std::min(c->last_band, nb);
+  int ov = b0 <= b1 ? sp->band_overlap[b0 - 1] : 0;
+  for (int b = b0; b <= b1; ++b)
+    if (sp->band_overlap[b - 1] != ov) return 0;
+  return ov == SOCGPU_IP_OVERLAP_HYBRID ? 0 : ov;
+}
+
+bool is_keqv(const socgpu_control *c, const SpectrumEntry *sp) {
+  const int ov = gas_overlap(c, sp);
+  return ov == SOCGPU_IP_OVERLAP_K_EQV_SCL || ov == SOCGPU_IP_OVERLAP_K_EQV || ov == SOCGPU_IP_OVERLAP_K_EQV_MOD;
 }
 
 int launch_cloud_gen(int nd_layer, int cloud_top, int n_layer, int nd_profile, int il1, int il2,
@@ -412,6 +422,8 @@ int build_spectrum(const socgpu_spectrum_desc *d, SpectrumEntry &e, char *msg, s
   e.drop_scheme.assign(s.n_drop_type, 0);
   e.ice_scheme.assign(s.n_ice_type, 0);
   e.drop_min_dim.clear(); e.drop_max_dim.clear(); e.ice_min_dim.clear(); e.ice_max_dim.clear();
+  e.band_overlap.assign(d->n_band, 0);
+  if (d->i_overlap) e.band_overlap.assign(d->i_overlap, d->i_overlap + d->n_band);
   if (d->drop_parm_min_dim && d->drop_parm_max_dim) {
     e.drop_min_dim.assign(d->drop_parm_min_dim, d->drop_parm_min_dim + s.n_drop_type);
     e.drop_max_dim.assign(d->drop_parm_max_dim, d->drop_parm_max_dim + s.n_drop_type);
@@ -668,11 +680,17 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
     set_msg(msg, msg_len, "only two-stream angular integration is supported"); return SOCGPU_I_ERR_FATAL; }
   if (c->isolir != SOCGPU_IP_SOLAR && c->isolir != SOCGPU_IP_INFRA_RED) {
     set_msg(msg, msg_len, "isolir must be solar or infra-red"); return SOCGPU_I_ERR_FATAL; }
-  if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_RANDOM && !is_keqv(c)) {
+  const int ovl = gas_overlap(c, sp);
+  if (c->i_gas_overlap == SOCGPU_IP_OVERLAP_HYBRID && ovl == 0) {
+    set_msg(msg, msg_len, "ip_overlap_hybrid: bands %d..%d of the spectral file do not name one overlap method "
+            "(bands of several methods in one call are not built)", c->first_band, c->last_band);
+    return SOCGPU_I_ERR_FATAL;
+  }
+  if (ovl != SOCGPU_IP_OVERLAP_RANDOM && !is_keqv(c, sp)) {
     set_msg(msg, msg_len, "only random and equivalent-extinction gas overlaps are supported");
     return SOCGPU_I_ERR_FATAL;
   }
-  if (c->i_gas_overlap == SOCGPU_IP_OVERLAP_RANDOM && !sp->dev.random_ok) {
+  if (ovl == SOCGPU_IP_OVERLAP_RANDOM && !sp->dev.random_ok) {
     set_msg(msg, msg_len, "random overlap of this spectrum needs more than %d k-term products; "
             "use equivalent extinction (i_gas_overlap 4)", SOCGPU_MAX_GPOINT);
     return SOCGPU_I_ERR_RANGE;
@@ -928,7 +946,7 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
   p.n_profile = atm->n_profile; p.n_layer = atm->n_layer;
   p.nd_profile = dm->nd_profile; p.nd_layer = dm->nd_layer;
   p.id_ct = (p.mcica ? dm->id_cloud_top : 1) - 1;
-  p.keqv = is_keqv(c);
+  p.keqv = is_keqv(c, sp);
   p.l_grey_single = c->l_grey_single;
   const int *first_g = p.keqv ? sp->dev.host_first_g_keqv : sp->dev.host_first_g;
   p.g_begin = first_g[c->first_band - 1];
@@ -1281,7 +1299,7 @@ void StagedCall::params(char *base, FluxParams &p) const {
 }
 
 long long StagedCall::column_gpoints() const {
-  const int *first_g = is_keqv(control) ? sp->dev.host_first_g_keqv : sp->dev.host_first_g;
+  const int *first_g = is_keqv(control, sp) ? sp->dev.host_first_g_keqv : sp->dev.host_first_g;
   const int g0 = first_g[control->first_band - 1], g1 = first_g[control->last_band];
   return (long long)atm->n_profile * (g1 - g0);
 }

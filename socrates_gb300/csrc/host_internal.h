@@ -36,6 +36,7 @@ struct SpectrumEntry {
   std::vector<double> drop_min_dim, drop_max_dim, ice_min_dim, ice_max_dim;   // their ranges of validity [m]
   int n_cloud_parameter = 0;          // coefficients per parameter set in the spectrum
   std::vector<int> n_k_major;         // k-terms of each band's first absorber (McICA tables)
+  std::vector<int> band_overlap;      // the gas overlap method each band names, 0 where none
   // classic aerosol species (block 11): parametrization, humidities and
   // phase-function moments of each, for validation
   std::vector<int> aer_parm, aer_nhum, aer_nphf;
@@ -46,7 +47,11 @@ struct SpectrumEntry {
 };
 
 SpectrumEntry *find_spectrum(int handle);
-bool is_keqv(const socgpu_control *c);
+// the gas overlap of a call: the control's, or under ip_overlap_hybrid the
+// method every band of the call names in the spectral file (0 when they
+// differ or name none; radiance_calc.F90:888-893)
+int gas_overlap(const socgpu_control *c, const SpectrumEntry *sp);
+bool is_keqv(const socgpu_control *c, const SpectrumEntry *sp);
 
 int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntry *sp, const socgpu_atm *atm,
              const socgpu_cld *cld, const socgpu_aer *aer, const socgpu_bound *bd, const socgpu_radout *out,

@@ -111,7 +111,7 @@ std::vector<double> fields13(const std::string &line) {
 struct SpectralFile {
   int n_band = 0, n_abs = 0, nd_k = 1, nsv = 4, ndc = 1;
   std::vector<double> wl_s, wl_l, solar, rayleigh;
-  std::vector<int> type_absorb, n_band_absorb, index_absorb, i_band_k, i_scale_k, i_scale_fnc;
+  std::vector<int> type_absorb, n_band_absorb, band_overlap, index_absorb, i_band_k, i_scale_k, i_scale_fnc;
   std::vector<double> k, w, scale, p_ref, t_ref;
   std::vector<int> l_doppler;
   std::vector<double> doppler_cor;
@@ -152,6 +152,7 @@ struct SpectralFile {
     d.n_absorb = n_abs;
     d.type_absorb = type_absorb.data();
     d.n_band_absorb = n_band_absorb.data();
+    d.i_overlap = band_overlap.data();
     d.index_absorb = index_absorb.data();
     d.i_band_k = i_band_k.data();
     d.i_scale_k = i_scale_k.data();
@@ -473,6 +474,7 @@ bool read_spectral_file(const std::string &path, const std::string &k_path, cons
   band_values(3, s.rayleigh);
   // block 4
   s.n_band_absorb.assign(nb, 0);
+  s.band_overlap.assign(nb, 0);
   s.index_absorb.assign((size_t)na * nb, 0);
   if (b4) {
     std::vector<std::string> tok;
@@ -482,9 +484,11 @@ bool read_spectral_file(const std::string &path, const std::string &k_path, cons
     const bool with_overlap = b4->version >= 1;   // each band's overlap method follows its count
     for (int i = 0; i < nb && q + 1 < tok.size(); ++i) {
       int b = std::atoi(tok[q].c_str()) - 1, n = std::atoi(tok[q + 1].c_str());
+      const int ov = with_overlap && q + 2 < tok.size() ? std::atoi(tok[q + 2].c_str()) : 0;
       q += with_overlap ? 3 : 2;
       if (b < 0 || b >= nb || n < 0 || n > na) { err = path + ": bad block 4"; return false; }
       s.n_band_absorb[b] = n;
+      s.band_overlap[b] = ov;
       for (int j = 0; j < n && q < tok.size(); ++j) s.index_absorb[(size_t)j + (size_t)na * b] = std::atoi(tok[q++].c_str());
     }
   }

@@ -276,6 +276,8 @@ class Spectrum:
         d.n_absorb = self.n_absorb
         d.type_absorb = ip(self.type_absorb)
         d.n_band_absorb = ip(self.n_band_absorb)
+        if self.i_overlap is not None:
+            d.i_overlap = ip(self.i_overlap)
         # index_absorb is (nd_species, n_band); nd_species also indexes p_ref/t_ref
         nds = d.nd_species
         ia = np.zeros((nds, self.n_band), np.int32)

@@ -115,6 +115,33 @@ def test_ga7_sw_random_overlap_too_many_products(gpu_lib):
     R.radiance_calc(replace(ctl, i_gas_overlap=abi.IP_OVERLAP_K_EQV_SCL), sp, col)
 
 
+@pytest.mark.parametrize("named", [abi.IP_OVERLAP_K_EQV_SCL, abi.IP_OVERLAP_RANDOM])
+def test_hybrid_overlap_takes_the_bands_method(gpu_lib, named):
+    """ip_overlap_hybrid (radiance_calc.F90:888-893): when every band of the
+    call names one method in the spectral file, the fluxes are that method's
+    bit for bit; bands naming different methods are refused with a message,
+    and a band range over which they agree runs."""
+    base = _ga7_lw()
+    col = synth.operational_case(base, 16, 40, seed=49, solar=False)
+    ctl = R.lw_control(l_continuum=True, i_gas_overlap=named)
+    hybrid = replace(ctl, i_gas_overlap=abi.IP_OVERLAP_HYBRID)
+    sp = replace(base, i_overlap=np.full(base.n_band, named, np.int32), name=f"{base.name}_hybrid{named}")
+    want, got = R.radiance_calc(ctl, base, col), R.radiance_calc(hybrid, sp, col)
+    for k in ("flux_up", "flux_down", "heating_rate"):
+        assert np.array_equal(got[k], want[k]), k
+    other = abi.IP_OVERLAP_RANDOM + abi.IP_OVERLAP_K_EQV_SCL - named
+    mixed = np.full(base.n_band, named, np.int32)
+    mixed[-1] = other
+    sp2 = replace(base, i_overlap=mixed, name=f"{base.name}_hybrid{named}_mixed")
+    with pytest.raises(R.RadianceError) as e:
+        R.radiance_calc(hybrid, sp2, col)
+    assert e.value.status == abi.I_ERR_FATAL and "ip_overlap_hybrid" in str(e.value)
+    nb = base.n_band - 1
+    got = R.radiance_calc(replace(hybrid, last_band=nb), sp2, col)
+    want = R.radiance_calc(replace(ctl, last_band=nb), base, col)
+    assert np.array_equal(got["flux_up"], want["flux_up"]) and np.array_equal(got["flux_down"], want["flux_down"])
+
+
 def _self_broadened(sp):
     """GA7 long wave with water vapour made self-broadened: three gas
     fractions, k growing with the fraction."""
