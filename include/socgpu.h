@@ -82,6 +82,10 @@ extern "C" {
 #define SOCGPU_IP_CLOUD_MIX_MAX         2   /* clear and cloudy regions, maximum-random overlap */
 #define SOCGPU_IP_CLOUD_MIX_RANDOM      4   /* clear and cloudy regions, random overlap */
 #define SOCGPU_IP_CLOUD_TRIPLE          6   /* clear, stratiform and convective regions, maximum-random */
+#define SOCGPU_IP_CLOUD_PART_CORR       7   /* clear and cloudy regions, like regions correlated over
+                                               dp_corr_strat (rad_pcf.F90:317) */
+#define SOCGPU_IP_CLOUD_PART_CORR_CNV   8   /* three regions, stratiform over dp_corr_strat and
+                                               convective over dp_corr_conv (rad_pcf.F90:319) */
 #define SOCGPU_IP_CLOUD_CLEAR           5
 #define SOCGPU_IP_CLOUD_MCICA          10
 /* cloud representation, rad_pcf.F90:238-254 */
@@ -425,6 +429,10 @@ typedef struct socgpu_cld {
     const int *subcol_k;              /* (nd_band, nd_k_term) of the spectrum */
     const int *first_subcol_k;        /* (nd_band, nd_k_term+1) of the spectrum */
     const int *subcol_reorder;        /* (nd_subcol_req) */
+    /* pressure scales [Pa] over which like stratiform and like convective
+       regions decorrelate under SOCGPU_IP_CLOUD_PART_CORR(_CNV)
+       (overlap_coupled.F90:209-236) */
+    double dp_corr_strat, dp_corr_conv;
 } socgpu_cld;
 
 /* ---- StrOut subset (src/radiance_core/def_out.F90), one channel ------ */
@@ -641,7 +649,8 @@ typedef struct socgpu_runes_args {
                                            _COMBINE_ICE_WATER; three regions: _CONV_STRAT, _CSIW,
                                            _SPLIT_HOMOGEN, _SPLIT_ICE_WATER */
     int i_overlap;                      /* SOCGPU_IP_MAX_RAND (0, the default), SOCGPU_IP_RAND,
-                                           SOCGPU_IP_EXPONENTIAL_RAND (McICA only) */
+                                           SOCGPU_IP_EXPONENTIAL_RAND (McICA, or like regions correlated
+                                           over cloud_vertical_decorr / conv_vertical_decorr) */
     int i_inhom;                        /* SOCGPU_IP_HOMOGENEOUS, SOCGPU_IP_SCALING, SOCGPU_IP_MCICA,
                                            SOCGPU_IP_TRIPLECLOUDS_2019 (the split representations'
                                            thin and thick parts from the condensate RSD) */
@@ -659,7 +668,8 @@ typedef struct socgpu_runes_args {
     const double *liq_rsd, *ice_rsd;    /* relative standard deviations of the condensate */
     int has_liq_dim_constant, has_cloud_vertical_decorr, has_cloud_horizontal_rsd;
     double liq_dim_constant;            /* [m], with SOCGPU_IP_RE_CONSTANT */
-    double cloud_vertical_decorr;       /* decorrelation pressure scale [Pa] of the McICA generator */
+    double cloud_vertical_decorr;       /* decorrelation pressure scale [Pa] of the McICA generator and of
+                                           like stratiform regions */
     double cloud_horizontal_rsd;        /* condensate RSD where liq_rsd / ice_rsd are NULL */
     const int *rand_seed;               /* (n_profile) McICA seeds; NULL: 10 + profile */
     const char *mcica_data;             /* path of the McICA data file (with SOCGPU_IP_MCICA) */
@@ -674,6 +684,11 @@ typedef struct socgpu_runes_args {
     const double *liq_conv_rsd, *ice_conv_rsd;  /* (n_profile, n_layer) or NULL */
     int has_liq_conv_dim_constant;
     double liq_conv_dim_constant;       /* [m], with SOCGPU_IP_RE_CONSTANT */
+    /* the pressure scale [Pa] over which like convective regions decorrelate
+       under exponential-random overlap (set_cld's conv_vertical_decorr; the
+       stratiform scale is cloud_vertical_decorr) */
+    int has_conv_vertical_decorr;
+    double conv_vertical_decorr;
 } socgpu_runes_args;
 
 /* StrDiag (socrates_def_diag.F90): NULL members are not filled. */
@@ -688,10 +703,11 @@ typedef struct socgpu_runes_diag {
 /* runes (socrates_runes.F90:47) on the GPU: maps the arguments, calls
  * socgpu_radiance_calc with host arrays and fills the diagnostics.  Clouds
  * of one homogeneous type or of separate water and ice types (and their
- * combinations with convective cloud) run in two regions with maximum-random
- * or random overlap, or with McICA subcolumns; the representations with
- * separate convective cloud run in three regions (clear, stratiform and
- * convective) with maximum-random overlap and Hogan's solver. */
+ * combinations with convective cloud) run in two regions with maximum-random,
+ * random or exponential-random overlap, or with McICA subcolumns; the
+ * representations with separate convective cloud run in three regions
+ * (clear, stratiform and convective) with maximum-random or
+ * exponential-random overlap and Hogan's solver. */
 SOCGPU_API int socgpu_runes(const socgpu_runes_args *args, socgpu_runes_diag *diag, char *msg, size_t msg_len);
 
 /* ---- multi-batch launches (extension) -----------------------------------

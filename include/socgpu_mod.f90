@@ -55,6 +55,7 @@ TYPE, BIND(C) :: socgpu_cld
   TYPE(c_ptr)    :: w_cloud, frac_cloud
   INTEGER(c_int) :: n_subcol_gen, n_subcol_req
   TYPE(c_ptr)    :: c_sub, frac_cloudy, n_subcol_cld, subcol_k, first_subcol_k, subcol_reorder
+  REAL(c_double) :: dp_corr_strat, dp_corr_conv
 END TYPE
 
 TYPE, BIND(C) :: socgpu_radout
@@ -100,6 +101,8 @@ TYPE, BIND(C) :: socgpu_runes_args
   TYPE(c_ptr)    :: liq_conv_dim, ice_conv_dim, liq_conv_rsd, ice_conv_rsd
   INTEGER(c_int) :: has_liq_conv_dim_constant
   REAL(c_double) :: liq_conv_dim_constant
+  INTEGER(c_int) :: has_conv_vertical_decorr
+  REAL(c_double) :: conv_vertical_decorr
 END TYPE
 
 TYPE, BIND(C) :: socgpu_runes_diag

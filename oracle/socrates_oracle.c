@@ -1496,14 +1496,29 @@ static int cloud_top(const socgpu_cld *cld, int ndp, int ict, int n_profile, int
  * cloud_overlap(:, i, 1..4)) and of each lower region under each upper one
  * (ovl[4..7]).  0-based ovl index 2 j + k for region k above and j below,
  * 4 + 2 j + k for region k below and j above. */
-static void overlap_coupled2(work *w, const socgpu_cld *cld, int ndp, int ict, int i_cloud)
+/* The correlation of like region k (0 clear, 1 stratiform, 2 convective) at
+ * interface i (overlap_coupled.F90:190-236): maximal (1) under mix_max and
+ * triple, random (0) under mix_random; under part_corr and part_corr_cnv
+ * exp((p(i) - p(i+1)) / dp_corr) between layers 1 < i < n_layer, with
+ * dp_corr 1 Pa for the clear region and dp_corr_strat / dp_corr_conv for the
+ * others, and 1 at the two ends. */
+static double like_corr(int i_cloud, const socgpu_cld *cld, const double *p, int ndp, int l, int i, int n_layer,
+                        int k)
+{
+    if (i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || i_cloud == SOCGPU_IP_CLOUD_TRIPLE) return 1.0;
+    if (i_cloud != SOCGPU_IP_CLOUD_PART_CORR && i_cloud != SOCGPU_IP_CLOUD_PART_CORR_CNV) return 0.0;
+    if (!(i < n_layer && i > 1)) return 1.0;
+    const double dp_corr = k == 0 ? 1.0 : (k == 1 ? cld->dp_corr_strat : cld->dp_corr_conv);
+    return exp((p[(size_t)l + (size_t)ndp * (size_t)(i - 1)] - p[(size_t)l + (size_t)ndp * (size_t)i]) / dp_corr);
+}
+
+static void overlap_coupled2(work *w, const socgpu_cld *cld, const double *p, int ndp, int ict, int i_cloud)
 {
     const int n_layer = w->n_layer, wp = w->wp, nct = w->nct;
     const double tol = 1.0e+02 * EPS_R;
     for (int l = 0; l < w->n_profile; ++l) {
         double au[2] = {1.0, 0.0};
         for (int i = nct - 1; i <= n_layer; ++i) {
-            const double corr = (i_cloud == SOCGPU_IP_CLOUD_MIX_MAX) ? 1.0 : 0.0;
             double al[2], ao[2][2];
             if (i < n_layer) {
                 const double wc = cloud_w(cld, ndp, ict, l, i + 1);
@@ -1513,7 +1528,8 @@ static void overlap_coupled2(work *w, const socgpu_cld *cld, int ndp, int ict, i
                 al[0] = 1.0;
                 al[1] = 0.0;
             }
-            for (int k = 0; k < 2; ++k) ao[k][k] = corr * (al[k] < au[k] ? al[k] : au[k]);
+            for (int k = 0; k < 2; ++k)
+                ao[k][k] = like_corr(i_cloud, cld, p, ndp, l, i, n_layer, k) * (al[k] < au[k] ? al[k] : au[k]);
             ao[0][1] = 0.0;
             ao[1][0] = 0.0;
             double art = 1.0 - ao[0][0];
@@ -1871,7 +1887,8 @@ static int region_of_type(int rep, int t)
  * i = nct-1 .. n_layer the fraction v_jk of upper region k going into lower
  * region j (ovl[3 j + k], cloud_overlap(:, i, 3 j + k + 1)) and the fraction
  * u_jk of lower region k going into upper region j (ovl[9 + 3 j + k]). */
-static void overlap_coupled3(work *w, const socgpu_control *c, const socgpu_cld *cld, int ndp, int ict)
+static void overlap_coupled3(work *w, const socgpu_control *c, const socgpu_cld *cld, const double *p, int ndp,
+                             int ict)
 {
     const int n_layer = w->n_layer, wp = w->wp, nct = w->nct, ndc = w->ndl - ict;
     const double tol = 1.0e+02 * EPS_R;
@@ -1898,7 +1915,8 @@ static void overlap_coupled3(work *w, const socgpu_control *c, const socgpu_cld 
             } else {
                 al[0] = 1.0; al[1] = 0.0; al[2] = 0.0;
             }
-            for (int k = 0; k < 3; ++k) ao[k][k] = 1.0 * (al[k] < au[k] ? al[k] : au[k]);
+            for (int k = 0; k < 3; ++k)
+                ao[k][k] = like_corr(c->i_cloud, cld, p, ndp, l, i, n_layer, k) * (al[k] < au[k] ? al[k] : au[k]);
             for (int k = 0; k < 3; ++k)
                 for (int j = 0; j < k; ++j) { ao[k][j] = 0.0; ao[j][k] = 0.0; }
             double art = 1.0 - ao[0][0];
@@ -2205,8 +2223,9 @@ static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
     if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
         if (two_coeff_basic(c->i_2stream, 0.5, 0.5, &s, &t) != SOCGPU_I_NORMAL) {
             set_msg(msg, msg_len, "unrecognised or unimplemented two-stream scheme"); return SOCGPU_I_ERR_FATAL; }
-        const int region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM);
-        const int triple = (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE);
+        const int region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM ||
+                            c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR);
+        const int triple = (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE || c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR_CNV);
         if (triple && c->i_solver != SOCGPU_IP_SOLVER_TRIPLE_HOGAN) {
             set_msg(msg, msg_len, "three cloud regions require solver_triple_hogan"); return SOCGPU_I_ERR_FATAL; }
         if (triple && c->i_cloud_representation != SOCGPU_IP_CLOUD_CONV_STRAT &&
@@ -2227,20 +2246,22 @@ static int check_options(const socgpu_control *c, const socgpu_spectrum_desc *d,
         set_msg(msg, msg_len, "unsupported scattering method"); return SOCGPU_I_ERR_FATAL; }
     if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR && c->i_cloud != SOCGPU_IP_CLOUD_MCICA &&
         c->i_cloud != SOCGPU_IP_CLOUD_MIX_MAX && c->i_cloud != SOCGPU_IP_CLOUD_MIX_RANDOM &&
-        c->i_cloud != SOCGPU_IP_CLOUD_TRIPLE) {
+        c->i_cloud != SOCGPU_IP_CLOUD_TRIPLE && c->i_cloud != SOCGPU_IP_CLOUD_PART_CORR &&
+        c->i_cloud != SOCGPU_IP_CLOUD_PART_CORR_CNV) {
         set_msg(msg, msg_len, "only clear-sky, McICA and two- and three-region cloud schemes are supported");
         return SOCGPU_I_ERR_FATAL; }
     if (c->i_cloud != SOCGPU_IP_CLOUD_CLEAR &&
         (!cld || cld->n_condensed < 1 || !cld->type_condensed || !cld->i_cloud_type || !cld->i_condensed_param ||
          !cld->i_condensed_type || !cld->condensed_mix_ratio || !cld->condensed_dim_char || !cld->w_cloud ||
          !cld->frac_cloud || cld->n_cloud_type < 1 ||
-         cld->n_cloud_type > (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE ? 4 : 2))) {
+         cld->n_cloud_type > ((c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE || c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR_CNV) ? 4 : 2))) {
         set_msg(msg, msg_len, "clouds require cloud fields"); return SOCGPU_I_ERR_FATAL; }
     if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA &&
         (!cld->c_sub || !cld->frac_cloudy || !cld->subcol_k || !cld->first_subcol_k || !cld->subcol_reorder)) {
         set_msg(msg, msg_len, "McICA requires the subcolumn fields"); return SOCGPU_I_ERR_FATAL; }
     if ((c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM ||
-         c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE) && c->i_scatter_method != SOCGPU_IP_SCATTER_FULL) {
+         c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE || c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR ||
+         c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR_CNV) && c->i_scatter_method != SOCGPU_IP_SCATTER_FULL) {
         set_msg(msg, msg_len, "cloud regions require full scattering"); return SOCGPU_I_ERR_FATAL; }
     if (c->first_band < 1 || c->last_band > d->n_band || c->first_band > c->last_band) {
         set_msg(msg, msg_len, "band range outside the spectrum"); return SOCGPU_I_ERR_RANGE; }
@@ -2270,8 +2291,9 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
     if (np <= 0) return SOCGPU_I_NORMAL;
     int ndp = dm->nd_profile, ndl = dm->nd_layer, n_layer = atm0->n_layer;
     int l_cloud = (c->i_cloud == SOCGPU_IP_CLOUD_MCICA);
-    int l_triple = (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE);
-    int l_region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM) || l_triple;
+    int l_triple = (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE || c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR_CNV);
+    int l_region = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM ||
+                    c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR) || l_triple;
     int ict = dm->id_cloud_top - 1;
 
     /* views shifted to the first profile of the segment */
@@ -2323,8 +2345,8 @@ static int segment_radiance_calc(const socgpu_control *c, const socgpu_dimen *dm
         /* set_cloud_geometry, aggregate_cloud and overlap_coupled
          * (radiance_calc.F90:640-700) */
         w.nct = cloud_top(cld, ndp, ict, np, n_layer);
-        if (l_triple) overlap_coupled3(&w, c, cld, ndp, ict);
-        else overlap_coupled2(&w, cld, ndp, ict, c->i_cloud);
+        if (l_triple) overlap_coupled3(&w, c, cld, atm.p, ndp, ict);
+        else overlap_coupled2(&w, cld, atm.p, ndp, ict, c->i_cloud);
     }
 
     /* zero the outputs (augment_radiance's l_initial branch is equivalent) */

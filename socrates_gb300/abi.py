@@ -23,6 +23,7 @@ IP_CLOUD_CLEAR, IP_CLOUD_MCICA = 5, 10
 IP_CLOUD_MIX_MAX, IP_CLOUD_MIX_RANDOM = 2, 4
 IP_SOLVER_MIX_DIRECT, IP_SOLVER_MIX_DIRECT_HOGAN = 11, 16
 IP_CLOUD_TRIPLE, IP_SOLVER_TRIPLE_HOGAN = 6, 17      # three regions: clear, stratiform, convective
+IP_CLOUD_PART_CORR, IP_CLOUD_PART_CORR_CNV = 7, 8    # like regions correlated over a pressure scale
 IP_CLOUD_TYPE_STRAT, IP_CLOUD_TYPE_CONV = 1, 2
 IP_CLOUD_TYPE_SW, IP_CLOUD_TYPE_SI, IP_CLOUD_TYPE_CW, IP_CLOUD_TYPE_CI = 1, 2, 3, 4
 IP_CLOUD_HOMOGEN = 1
@@ -161,7 +162,8 @@ class RunesArgs(C.Structure):
         ("rand_seed", _ip), ("mcica_data", C.c_char_p),
         ("i_cnv_water", C.c_int), ("i_cnv_ice", C.c_int), ("liq_conv_dim", _dp), ("ice_conv_dim", _dp),
         ("liq_conv_rsd", _dp), ("ice_conv_rsd", _dp), ("has_liq_conv_dim_constant", C.c_int),
-        ("liq_conv_dim_constant", C.c_double),
+        ("liq_conv_dim_constant", C.c_double), ("has_conv_vertical_decorr", C.c_int),
+        ("conv_vertical_decorr", C.c_double),
     ]
 
 
@@ -194,6 +196,7 @@ class Cld(C.Structure):
         ("n_cloud_type", C.c_int), ("w_cloud", _dp), ("frac_cloud", _dp),
         ("n_subcol_gen", C.c_int), ("n_subcol_req", C.c_int), ("c_sub", _dp), ("frac_cloudy", _dp),
         ("n_subcol_cld", _ip), ("subcol_k", _ip), ("first_subcol_k", _ip), ("subcol_reorder", _ip),
+        ("dp_corr_strat", C.c_double), ("dp_corr_conv", C.c_double),
     ]
 
 

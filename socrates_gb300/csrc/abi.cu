@@ -29,6 +29,13 @@ namespace socgpu {
 
 // The equivalent-extinction overlaps (rad_pcf.F90:432-436), all solved by
 // solve_band_k_eqv_scl.
+// three regions (clear, stratiform, convective), and any region scheme
+bool triple_cloud(int i_cloud) { return i_cloud == SOCGPU_IP_CLOUD_TRIPLE || i_cloud == SOCGPU_IP_CLOUD_PART_CORR_CNV; }
+bool region_cloud(int i_cloud) {
+  return i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM ||
+         i_cloud == SOCGPU_IP_CLOUD_PART_CORR || triple_cloud(i_cloud);
+}
+
 int gas_overlap(const socgpu_control *c, const SpectrumEntry *sp) {
   if (c->i_gas_overlap != SOCGPU_IP_OVERLAP_HYBRID) return c->i_gas_overlap;
   const int nb = (int)sp->band_overlap.size();
@@ -704,8 +711,8 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
         return SOCGPU_I_ERR_FATAL;
       }
   }
-  const bool triple = c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE;
-  const bool region = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || triple;
+  const bool triple = triple_cloud(c->i_cloud);
+  const bool region = region_cloud(c->i_cloud);
   if (c->i_scatter_method == SOCGPU_IP_SCATTER_FULL) {
     if (!region && c->i_solver != SOCGPU_IP_SOLVER_HOMOGEN_DIRECT) {
       set_msg(msg, msg_len, "scattering requires solver_homogen_direct"); return SOCGPU_I_ERR_FATAL; }
@@ -855,7 +862,7 @@ int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntr
         !cld->condensed_mix_ratio || !cld->condensed_dim_char || !cld->w_cloud || !cld->frac_cloud) {
       set_msg(msg, msg_len, "clouds require cloud fields"); return SOCGPU_I_ERR_FATAL; }
     if (cld->n_condensed < 1 || cld->n_condensed > kMaxCloudComp || cld->n_cloud_type < 1 ||
-        cld->n_cloud_type > (c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE ? 4 : 2)) {
+        cld->n_cloud_type > (triple_cloud(c->i_cloud) ? 4 : 2)) {
       set_msg(msg, msg_len, "cloud components/types outside the supported range"); return SOCGPU_I_ERR_RANGE; }
     if (dm->id_cloud_top < 1 || dm->id_cloud_top > atm->n_layer) {
       set_msg(msg, msg_len, "id_cloud_top outside the column"); return SOCGPU_I_ERR_RANGE; }
@@ -927,12 +934,20 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
   p.l_ir_source_quad = c->l_ir_source_quad; p.l_rayleigh = c->l_rayleigh; p.l_gas = c->l_gas;
   p.l_aerosol_mode = c->l_aerosol_mode && aer && aer->n_mode > 0; p.l_flux_div = c->l_flux_div;
   p.first_band = c->first_band; p.last_band = c->last_band;
-  p.triple = c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE;
-  p.region = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || p.triple;
+  p.triple = triple_cloud(c->i_cloud);
+  p.region = region_cloud(c->i_cloud);
   p.mcica = c->i_cloud == SOCGPU_IP_CLOUD_MCICA || p.region;
   p.solver_hogan = c->i_solver == SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN || c->i_solver == SOCGPU_IP_SOLVER_TRIPLE_HOGAN;
-  // like regions overlap maximally under ip_cloud_triple (overlap_coupled.F90:192-198)
-  p.mix_max = c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || p.triple;
+  // the correlation of like regions at an interface (overlap_coupled.F90:
+  // 190-236): 1 under mix_max and triple, 0 under mix_random, and under the
+  // partially correlated schemes exp(dp / dp_corr) with the clear region's
+  // scale 1 Pa, the stratiform region's dp_corr_strat and the convective
+  // region's dp_corr_conv
+  p.corr_mode = (c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX || c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE) ? 1
+              : (c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR || c->i_cloud == SOCGPU_IP_CLOUD_PART_CORR_CNV) ? 2 : 0;
+  p.dp_corr[0] = 1.0;
+  p.dp_corr[1] = cld ? cld->dp_corr_strat : 0.0;
+  p.dp_corr[2] = cld ? cld->dp_corr_conv : 0.0;
   // aggregate_cloud (aggregate_cloud.F90:107-155): stratiform water and
   // ice then convective water and ice, or stratiform then convective
   for (int t = 0; t < 4; ++t) {
@@ -1065,8 +1080,7 @@ void fill_params(FluxParams &p, const socgpu_control *c, const socgpu_dimen *dm,
 
 int mode_index(const socgpu_control *c) {
   // McICA and cloud regions share the kernels that stage cloud optics
-  if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA || c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX ||
-      c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE)
+  if (c->i_cloud == SOCGPU_IP_CLOUD_MCICA || region_cloud(c->i_cloud))
     return 2;
   return c->i_scatter_method == SOCGPU_IP_SCATTER_FULL ? 1 : 0;
 }
@@ -1118,8 +1132,7 @@ void StagedCall::stage(const socgpu_control *c, const socgpu_dimen *dm, const Sp
   const size_t ndp = dm->nd_profile, ndl = dm->nd_layer, np = a->n_profile, nl = a->n_layer;
   const size_t nb = s->dev.n_band, ns = std::max(1, s->dev.n_species);
   sw = c->isolir == SOCGPU_IP_SOLAR;
-  mc = c->i_cloud == SOCGPU_IP_CLOUD_MCICA || c->i_cloud == SOCGPU_IP_CLOUD_MIX_MAX ||
-       c->i_cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || c->i_cloud == SOCGPU_IP_CLOUD_TRIPLE;
+  mc = c->i_cloud == SOCGPU_IP_CLOUD_MCICA || region_cloud(c->i_cloud);
   aero = c->l_aerosol_mode && ae && ae->n_mode > 0;
   const size_t D = sizeof(double), none = (size_t)-1;
   // inputs: (nd_profile, rows) arrays copied with their valid profiles only;

@@ -1570,6 +1570,18 @@ struct FluxKernel {
     }
   }
 
+  // the correlation of like region k (0 clear, 1 stratiform, 2 convective)
+  // at interface i (overlap_coupled.F90:190-236): 1 under mix_max and triple,
+  // 0 under mix_random, and under part_corr and part_corr_cnv
+  // exp((p(i) - p(i+1)) / dp_corr) between layers 1 < i < n_layer (1 at the
+  // ends), in FP64
+  __device__ static R like_corr(const FluxParams &p, int col, int i, int k) {
+    if (p.corr_mode != 2) return p.corr_mode == 1 ? R(1) : R(0);
+    if (!(i < p.n_layer && i > 1)) return R(1);
+    const size_t q = (size_t)col + (size_t)p.nd_profile * (size_t)(i - 1);
+    return (R)exp((p.p[q] - p.p[q + (size_t)p.nd_profile]) / p.dp_corr[k]);
+  }
+
   // set_cloud_geometry and overlap_coupled (set_cloud_geometry.F90:76-96,
   // overlap_coupled.F90:120-440) for the column, by one thread: the first
   // cloudy layer (1-based, at most n_layer) and, at each interface i (0: the
@@ -1590,11 +1602,11 @@ struct FluxKernel {
       for (int m = 0; m < 8; ++m) S.ovl[(size_t)m * (LP_ + 1) + i] = (m == 0 || m == 3 || m == 4 || m == 7) ? R(1) : R(0);
     R au0 = R(1), au1 = R(0);
     for (int i = nct - 1; i <= L; ++i) {
-      const R corr = p.mix_max ? R(1) : R(0);
       R al0, al1;
       if (i < L) { const R w = wc(i + 1); al0 = R(1) - w; al1 = w; }
       else { al0 = R(1); al1 = R(0); }
-      R a00 = corr * (al0 < au0 ? al0 : au0), a11 = corr * (al1 < au1 ? al1 : au1), a01 = R(0), a10 = R(0);
+      R a00 = like_corr(p, col, i, 0) * (al0 < au0 ? al0 : au0), a11 = like_corr(p, col, i, 1) * (al1 < au1 ? al1 : au1);
+      R a01 = R(0), a10 = R(0);
       R art = R(1) - a00;
       art = art - a11;
       const R ru0 = au0 - a00, ru1 = au1 - a11, rl0 = al0 - a00, rl1 = al1 - a11;
@@ -1647,7 +1659,7 @@ struct FluxKernel {
       R al[3], ao[3][3];
       if (i < L) { const R w = wc(i + 1); al[0] = R(1) - w; al[1] = w * S.frr[i]; al[2] = w * S.frr[LP_ + i]; }
       else { al[0] = R(1); al[1] = R(0); al[2] = R(0); }
-      for (int k = 0; k < 3; ++k) ao[k][k] = R(1) * (al[k] < au[k] ? al[k] : au[k]);
+      for (int k = 0; k < 3; ++k) ao[k][k] = like_corr(p, col, i, k) * (al[k] < au[k] ? al[k] : au[k]);
       for (int k = 0; k < 3; ++k)
         for (int j = 0; j < k; ++j) { ao[k][j] = R(0); ao[j][k] = R(0); }
       R art = R(1) - ao[0][0];

@@ -51,6 +51,8 @@ SpectrumEntry *find_spectrum(int handle);
 // method every band of the call names in the spectral file (0 when they
 // differ or name none; radiance_calc.F90:888-893)
 int gas_overlap(const socgpu_control *c, const SpectrumEntry *sp);
+bool triple_cloud(int i_cloud);
+bool region_cloud(int i_cloud);
 bool is_keqv(const socgpu_control *c, const SpectrumEntry *sp);
 
 int validate(const socgpu_control *c, const socgpu_dimen *dm, const SpectrumEntry *sp, const socgpu_atm *atm,

@@ -210,11 +210,7 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
       return SOCGPU_I_ERR_RANGE;
     }
     if (conv_sep) {
-      if (a->i_overlap == SOCGPU_IP_EXPONENTIAL_RAND) {
-        set_msg(msg, msg_len, "exponential-random overlap of three regions (ip_cloud_part_corr_cnv) is not built");
-        return SOCGPU_I_ERR_RANGE;
-      }
-      if (a->i_overlap == SOCGPU_IP_RAND) {
+      if (a->i_overlap != SOCGPU_IP_MAX_RAND && a->i_overlap != SOCGPU_IP_EXPONENTIAL_RAND) {
         // random overlap keeps two regions, whose solver (mix_column.F90:438-530)
         // does not take solver_triple_hogan
         set_msg(msg, msg_len, "***Error: The solver specified is not valid here.");
@@ -224,14 +220,11 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
         set_msg(msg, msg_len, "maximal entrapment in three regions (solver_triple) is not built");
         return SOCGPU_I_ERR_RANGE;
       }
-      i_cloud = SOCGPU_IP_CLOUD_TRIPLE;
+      i_cloud = a->i_overlap == SOCGPU_IP_EXPONENTIAL_RAND ? SOCGPU_IP_CLOUD_PART_CORR_CNV : SOCGPU_IP_CLOUD_TRIPLE;
       solver = SOCGPU_IP_SOLVER_TRIPLE_HOGAN;
     } else {
-      if (a->i_overlap == SOCGPU_IP_EXPONENTIAL_RAND) {
-        set_msg(msg, msg_len, "exponential-random overlap of cloud regions (ip_cloud_part_corr) is not built");
-        return SOCGPU_I_ERR_RANGE;
-      }
-      i_cloud = a->i_overlap == SOCGPU_IP_MAX_RAND ? SOCGPU_IP_CLOUD_MIX_MAX : SOCGPU_IP_CLOUD_MIX_RANDOM;
+      i_cloud = a->i_overlap == SOCGPU_IP_MAX_RAND ? SOCGPU_IP_CLOUD_MIX_MAX
+              : a->i_overlap == SOCGPU_IP_EXPONENTIAL_RAND ? SOCGPU_IP_CLOUD_PART_CORR : SOCGPU_IP_CLOUD_MIX_RANDOM;
       solver = a->i_cloud_entrapment == SOCGPU_IP_MAX_ENTRAPMENT ? SOCGPU_IP_SOLVER_MIX_DIRECT
                                                                   : SOCGPU_IP_SOLVER_MIX_DIRECT_HOGAN;
     }
@@ -728,6 +721,9 @@ extern "C" int socgpu_runes(const socgpu_runes_args *a, socgpu_runes_diag *diag,
     cld.n_cloud_type = nct;
     cld.w_cloud = w_cloud.data();
     cld.frac_cloud = frac_cloud.data();
+    // decorrelation scales of like regions (socrates_set_cld.F90:454-465)
+    cld.dp_corr_strat = a->has_cloud_vertical_decorr ? a->cloud_vertical_decorr : 0.0;
+    cld.dp_corr_conv = a->has_conv_vertical_decorr ? a->conv_vertical_decorr : 0.0;
     if (mcica) mst.attach(cld);
   }
   std::vector<double> fu(NP * (nl + 1)), fd(NP * (nl + 1)), fdir(NP * (nl + 1)), hr(NP * nl);

@@ -150,7 +150,8 @@ struct FluxParams {
   int mcica;                         // cloud fields staged (McICA or cloud regions)
   int region;                        // clear and cloudy regions (ip_cloud_mix_max / mix_random)
   int solver_hogan;                  // regions solved by solver_mix_direct_hogan, else solver_mix_direct
-  int mix_max;                       // regions overlap maximally where adjacent (else randomly)
+  int corr_mode;                     // like regions at an interface: 0 random, 1 maximal, 2 exp(dp / dp_corr)
+  double dp_corr[3];                 // decorrelation scales [Pa] of the clear, stratiform, convective regions
   int triple;                        // three regions: clear, stratiform and convective (ip_cloud_triple)
   int type_region[4];                // the region (2 stratiform, 3 convective) of each 0-based cloud type
   int l_continuum, l_mixing_ratio, i_water;   // i_water: 0-based species of water vapour

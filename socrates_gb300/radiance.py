@@ -362,7 +362,8 @@ class Marshal:
                 self.aer.scattering_prsc = _dp(ae["scattering_prsc"], k)
                 self.aer.phase_fnc_prsc = _dp(ph, k)
         self.cld = abi.Cld()
-        region = control.i_cloud in (abi.IP_CLOUD_MIX_MAX, abi.IP_CLOUD_MIX_RANDOM, abi.IP_CLOUD_TRIPLE)
+        region = control.i_cloud in (abi.IP_CLOUD_MIX_MAX, abi.IP_CLOUD_MIX_RANDOM, abi.IP_CLOUD_TRIPLE,
+                                     abi.IP_CLOUD_PART_CORR, abi.IP_CLOUD_PART_CORR_CNV)
         if mcica is not None or (region and col.cld):
             cd = col.cld
             ict = id_cloud_top - 1
@@ -381,6 +382,8 @@ class Marshal:
             self.dimen.nd_cloud_component, self.dimen.nd_cloud_type = cl.n_condensed, cl.n_cloud_type
             cl.w_cloud = _dp(cd["w_cloud"][:, ict:], k)
             cl.frac_cloud = _dp(cd["frac_cloud"][:, ict:, :], k)
+            cl.dp_corr_strat = float(cd.get("dp_corr_strat", 0.0))
+            cl.dp_corr_conv = float(cd.get("dp_corr_conv", 0.0))
             if mcica is not None:
                 cl.n_subcol_gen, cl.n_subcol_req = mcica.n_subcol_gen, mcica.n_subcol_req
                 cl.c_sub = _dp(mcica.c_sub, k)

@@ -77,7 +77,7 @@ def runes(n_profile: int, n_layer: int, spectrum_name: str, i_source: int, *, p_
           i_inhom=0, i_cloud_entrapment=0, i_mcica_sampling=-1, i_st_water=0, i_st_ice=0, i_drop_re=0,
           n_cloud_layer=0, liq_dim_constant=None, cloud_vertical_decorr=None, cloud_horizontal_rsd=None,
           rand_seed=None, mcica_data=None, i_cnv_water=0, i_cnv_ice=0, liq_conv_dim_constant=None,
-          **kw) -> dict:
+          conv_vertical_decorr=None, **kw) -> dict:
     """runes (socrates_runes.F90:47) through socgpu_runes.  Gases are passed
     by the reference's names: <gas> a profile (n_profile, n_layer),
     <gas>_mix_ratio a well-mixed value, l_<gas>_well_mixed to prefer it.
@@ -120,7 +120,8 @@ def runes(n_profile: int, n_layer: int, spectrum_name: str, i_source: int, *, p_
         int(n_cloud_layer)
     a.i_cnv_water, a.i_cnv_ice = int(i_cnv_water), int(i_cnv_ice)
     for name, val in (("liq_dim_constant", liq_dim_constant), ("cloud_vertical_decorr", cloud_vertical_decorr),
-                      ("cloud_horizontal_rsd", cloud_horizontal_rsd), ("liq_conv_dim_constant", liq_conv_dim_constant)):
+                      ("cloud_horizontal_rsd", cloud_horizontal_rsd), ("liq_conv_dim_constant", liq_conv_dim_constant),
+                      ("conv_vertical_decorr", conv_vertical_decorr)):
         if val is not None:
             setattr(a, name, float(val))
             setattr(a, "has_" + name, 1)

@@ -53,7 +53,7 @@ def set_cld(sp, t, rep, i_st_water, i_st_ice, n_cloud_layer=0, i_inhom=abi.IP_HO
             ice_mmr=None, liq_conv_mmr=None, ice_conv_mmr=None, liq_dim=None, ice_dim=None, liq_rsd=None,
             ice_rsd=None, cloud_horizontal_rsd=None, i_drop_re=abi.IP_RE_EXTERNAL, liq_dim_constant=None,
             i_cnv_water=0, i_cnv_ice=0, liq_conv_dim=None, ice_conv_dim=None, liq_conv_rsd=None, ice_conv_rsd=None,
-            liq_conv_dim_constant=None):
+            liq_conv_dim_constant=None, cloud_vertical_decorr=None, conv_vertical_decorr=None):
     """col.cld for radiance.Marshal and the id_cloud_top runes uses."""
     n, L = t.shape
     ict = L + 1 - min(n_cloud_layer, L) if n_cloud_layer > 0 else 1
@@ -217,7 +217,9 @@ def set_cld(sp, t, rep, i_st_water, i_st_ice, n_cloud_layer=0, i_inhom=abi.IP_HO
                # one relative standard deviation per component where uniform
                # (radiance.set_cld_mcica weights it by the condensate)
                rel_var_dens=[float(r.flat[0]) if np.all(r == r.flat[0]) else r for r in rsd],
-               c_cloud=np.asfortranarray(full(c_cloud)), c_ratio=np.asfortranarray(full(c_ratio)))
+               c_cloud=np.asfortranarray(full(c_cloud)), c_ratio=np.asfortranarray(full(c_ratio)),
+               # decorrelation scales of like regions (set_cld.F90:454-465)
+               dp_corr_strat=float(cloud_vertical_decorr or 0.0), dp_corr_conv=float(conv_vertical_decorr or 0.0))
     return cld, ict
 
 

@@ -160,6 +160,31 @@ def test_three_regions_synthetic(gpu_lib, O, sps, solar, representation):
     assert np.abs(ref["flux_up"] - two["flux_up"]).max() > 0.5
 
 
+@pytest.mark.parametrize("solar", [False, True])
+@pytest.mark.parametrize("three", [False, True])
+def test_partially_correlated_regions(gpu_lib, O, sps, solar, three):
+    """Like regions correlated over a pressure scale (ip_cloud_part_corr with
+    two regions, ip_cloud_part_corr_cnv with three; overlap_coupled.F90:
+    209-236): exp(dp / dp_corr) at each interior interface, 1 Pa for the clear
+    region, 3000 Pa stratiform and 1000 Pa convective.  FP64 within 1e-10 of
+    the oracle and mixed within tolerance; the answer lies apart from both
+    maximal and random overlap."""
+    sp = sps["ga9sw" if solar else "ga9lw"]
+    if three:
+        col = _three_region(sp, 97, 60, seed=91 + solar, solar=solar, representation=abi.IP_CLOUD_CSIW)
+        ctl = _three_region_control(solar, abi.IP_CLOUD_CSIW, i_cloud=abi.IP_CLOUD_PART_CORR_CNV)
+    else:
+        col = _clouded(sp, 97, 60, seed=91 + solar, solar=solar, representation=abi.IP_CLOUD_ICE_WATER)
+        common = dict(i_cloud=abi.IP_CLOUD_PART_CORR, i_solver=abi.IP_SOLVER_MIX_DIRECT_HOGAN, l_continuum=True,
+                      i_gas_overlap=abi.IP_OVERLAP_K_EQV_SCL, l_flux_div=False)
+        ctl = R.sw_control(l_rayleigh=True, **common) if solar else R.lw_control(l_ir_source_quad=True, **common)
+    col.cld = dict(col.cld, dp_corr_strat=3000.0, dp_corr_conv=1000.0)
+    ref, _ = _check(ctl, sp, col, O, f"part_corr three={three} solar={solar}")
+    for other in ((abi.IP_CLOUD_TRIPLE,) if three else (abi.IP_CLOUD_MIX_MAX, abi.IP_CLOUD_MIX_RANDOM)):
+        alt = O.radiance_calc(replace(ctl, i_cloud=other), sp, col)
+        assert np.abs(ref["flux_up"] - alt["flux_up"]).max() > 0.05, other
+
+
 def test_three_regions_unscaled_direct_beam(gpu_lib, O, sps):
     """The solar direct beam without delta-scaling (i_direct_tau = 0) through
     the three regions (triple_solar_source.F90:300-350)."""

@@ -162,6 +162,9 @@ CLOUD_CASES = [
     (abi.IP_CLOUD_SPLIT_ICE_WATER, dict(liq_conv_mmr=None, ice_conv_mmr=None, liq_conv_frac=None,
                                         ice_conv_frac=None)),
     (abi.IP_CLOUD_SPLIT_ICE_WATER, dict(i_inhom=abi.IP_TRIPLECLOUDS_2019)),
+    (abi.IP_CLOUD_ICE_WATER, dict(i_overlap=abi.IP_EXPONENTIAL_RAND, cloud_vertical_decorr=5000.0)),
+    (abi.IP_CLOUD_CSIW, dict(i_overlap=abi.IP_EXPONENTIAL_RAND, cloud_vertical_decorr=4000.0,
+                             conv_vertical_decorr=1500.0)),
 ]
 THREE = (abi.IP_CLOUD_CONV_STRAT, abi.IP_CLOUD_CSIW, abi.IP_CLOUD_SPLIT_HOMOGEN, abi.IP_CLOUD_SPLIT_ICE_WATER)
 
@@ -197,12 +200,14 @@ def test_runes_clouds(ga9, O, section, case):
     arrays = {k: v for k, v in fields.items() if k not in ("i_inhom", "i_overlap", "i_cloud_entrapment")}
     cld, ict = SC.set_cld(sp, kw["t_layer"], rep, i_inhom=opts.get("i_inhom", abi.IP_HOMOGENEOUS), **types, **arrays)
     col.cld = cld
+    expo = opts.get("i_overlap") == abi.IP_EXPONENTIAL_RAND
     if rep in THREE:
-        ctl = replace(ctl, i_cloud=abi.IP_CLOUD_TRIPLE, i_solver=abi.IP_SOLVER_TRIPLE_HOGAN, i_cloud_representation=rep)
+        ctl = replace(ctl, i_cloud=abi.IP_CLOUD_PART_CORR_CNV if expo else abi.IP_CLOUD_TRIPLE,
+                      i_solver=abi.IP_SOLVER_TRIPLE_HOGAN, i_cloud_representation=rep)
     else:
         homogen = rep in (abi.IP_CLOUD_HOMOGEN, abi.IP_CLOUD_COMBINE_HOMOGEN)
         ctl = replace(ctl, i_cloud=abi.IP_CLOUD_MIX_RANDOM if opts.get("i_overlap") == abi.IP_RAND
-                      else abi.IP_CLOUD_MIX_MAX,
+                      else abi.IP_CLOUD_PART_CORR if expo else abi.IP_CLOUD_MIX_MAX,
                       i_solver=abi.IP_SOLVER_MIX_DIRECT if opts.get("i_cloud_entrapment") == abi.IP_MAX_ENTRAPMENT
                       else abi.IP_SOLVER_MIX_DIRECT_HOGAN,
                       i_cloud_representation=abi.IP_CLOUD_HOMOGEN if homogen else abi.IP_CLOUD_ICE_WATER)
@@ -219,15 +224,14 @@ def test_runes_clouds(ga9, O, section, case):
 def test_runes_three_region_refusals(ga9):
     """Separate convective cloud: random overlap leaves two regions whose
     solver does not take solver_triple_hogan (mix_column.F90:526-530);
-    exponential-random overlap and maximal entrapment are not built; the
-    convective mixing ratios are required unless the cloud is split."""
+    maximal entrapment is not built; the convective mixing ratios are
+    required unless the cloud is split."""
     d, _, _ = ga9
     kw = RC.runes_kwargs(d, "lw_tground")
     fields = _cloud_fields(1, 32, seed=5)
     base = dict(kw, i_cloud_representation=abi.IP_CLOUD_CSIW, i_st_water=5, i_st_ice=8, i_cnv_water=5, i_cnv_ice=8,
                 **fields)
     for extra, status, words in ((dict(i_overlap=abi.IP_RAND), abi.I_ERR_FATAL, "solver specified is not valid"),
-                                 (dict(i_overlap=abi.IP_EXPONENTIAL_RAND), abi.I_ERR_RANGE, "part_corr_cnv"),
                                  (dict(i_cloud_entrapment=abi.IP_MAX_ENTRAPMENT), abi.I_ERR_RANGE, "solver_triple"),
                                  (dict(liq_conv_mmr=None), abi.I_ERR_FATAL, "Convective liquid MMR not provided"),
                                  (dict(i_cnv_ice=0), abi.I_ERR_FATAL, "Prescribed ice cloud")):
