@@ -150,10 +150,6 @@ struct FluxParams {
   int mcica;                         // cloud fields staged (McICA or cloud regions)
   int region;                        // clear and cloudy regions (ip_cloud_mix_max / mix_random)
   int solver_hogan;                  // regions solved by solver_mix_direct_hogan, else solver_mix_direct
-  int corr_mode;                     // like regions at an interface: 0 random, 1 maximal, 2 exp(dp / dp_corr)
-  double dp_corr[3];                 // decorrelation scales [Pa] of the clear, stratiform, convective regions
-  int triple;                        // three regions: clear, stratiform and convective (ip_cloud_triple)
-  int type_region[4];                // the region (2 stratiform, 3 convective) of each 0-based cloud type
   int l_continuum, l_mixing_ratio, i_water;   // i_water: 0-based species of water vapour
   // sizes
   int n_profile, n_layer, nd_profile, nd_layer, id_ct;  // id_ct 0-based first cloudy layer
@@ -234,6 +230,11 @@ struct FluxParams {
   int wenyi_n4, wenyi_n6;
   const double *wenyi;
   const float *wenyi_f;
+  // cloud regions: overlap of like regions and the three-region types
+  int corr_mode;                     // like regions at an interface: 0 random, 1 maximal, 2 exp(dp / dp_corr)
+  double dp_corr[3];                 // decorrelation scales [Pa] of the clear, stratiform, convective regions
+  int triple;                        // three regions: clear, stratiform and convective (ip_cloud_triple)
+  int type_region[4];                // the region (2 stratiform, 3 convective) of each 0-based cloud type
 };
 
 // Launch configuration chosen by the tuner.
