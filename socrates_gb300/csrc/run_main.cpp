@@ -11,6 +11,8 @@
 //               -m <condensate relative std. deviation> +m <sampling> -dp <decorrelation scale>]
 //              [-C 6 -K 3|4 -d <droplet type> -i <ice type> +d <convective droplet type>
 //               +i <convective ice type>]
+//              [-C 7 | -C 8 (partially correlated regions) -dp <stratiform decorrelation scale>
+//               +dp <convective decorrelation scale>]
 //              [-a [+A]]
 //   socgpu_run --convert <in> <out.cdf|out.cdl>
 //
@@ -258,7 +260,7 @@ int main(int argc, char **argv) {
   int representation = 0, drop_type = 0, ice_type = 0, sampling = 2;
   int conv_drop_type = 0, conv_ice_type = 0;   // +d, +i: convective particles (three regions)
   bool aerosol = false, overlay = false;   // -a: classic aerosols; +A: overlay of optical properties
-  double mcica_sigma = 0.0, dp_corr_strat = 0.0;
+  double mcica_sigma = 0.0, dp_corr_strat = 0.0, dp_corr_conv = 0.0;
   for (size_t i = 0; i < a.size(); ++i) {
     const std::string &o = a[i];
     auto need = [&](size_t n) { return i + n < a.size(); };
@@ -288,6 +290,7 @@ int main(int argc, char **argv) {
     else if (o == "-m" && need(1)) mcica_sigma = std::atof(a[++i].c_str());
     else if (o == "+m" && need(1)) sampling = std::atoi(a[++i].c_str());
     else if (o == "-dp" && need(1)) dp_corr_strat = std::atof(a[++i].c_str());
+    else if (o == "+dp" && need(1)) dp_corr_conv = std::atof(a[++i].c_str());
     else if (o == "-P" && need(1)) {
       std::string p = a[++i];
       precision = (p == "mixed") ? SOCGPU_PRECISION_MIXED : SOCGPU_PRECISION_FP64;
@@ -298,11 +301,12 @@ int main(int argc, char **argv) {
   if (!isolir) return die("Spectral region not set.");
   if (first < 1 || last < first) return die("Range of bands not set");
   if (overlay && !aerosol) return die("+A overlays aerosol optical properties: it needs -a");
-  const bool triple = cloud == SOCGPU_IP_CLOUD_TRIPLE;
-  const bool region = cloud == SOCGPU_IP_CLOUD_MIX_MAX || cloud == SOCGPU_IP_CLOUD_MIX_RANDOM || triple;
+  const bool triple = cloud == SOCGPU_IP_CLOUD_TRIPLE || cloud == SOCGPU_IP_CLOUD_PART_CORR_CNV;
+  const bool region = cloud == SOCGPU_IP_CLOUD_MIX_MAX || cloud == SOCGPU_IP_CLOUD_MIX_RANDOM ||
+                      cloud == SOCGPU_IP_CLOUD_PART_CORR || triple;
   if (cloud != SOCGPU_IP_CLOUD_CLEAR && cloud != SOCGPU_IP_CLOUD_MCICA && !region)
     return die("cloud scheme " + std::to_string(cloud) +
-               " is not driven (clear sky -C 5, cloud regions -C 2 or 4, three regions -C 6, McICA -C 10)");
+               " is not driven (clear sky -C 5, cloud regions -C 2, 4 or 7, three regions -C 6 or 8, McICA -C 10)");
   const bool mcica = cloud == SOCGPU_IP_CLOUD_MCICA;
   const bool clouds = mcica || region;
   const bool conv = representation == SOCGPU_IP_CLOUD_CONV_STRAT || representation == SOCGPU_IP_CLOUD_CSIW;
@@ -752,6 +756,9 @@ int main(int argc, char **argv) {
     cld.n_cloud_type = n_cloud_type;
     cld.w_cloud = w_cloud.data();
     cld.frac_cloud = frac_cloud.data();
+    // decorrelation scales of like regions (l_run_cdf.F90:984-996: -dp, +dp)
+    cld.dp_corr_strat = dp_corr_strat;
+    cld.dp_corr_conv = dp_corr_conv;
   }
   if (mcica) mst.attach(cld);
   const auto t0 = std::chrono::steady_clock::now();

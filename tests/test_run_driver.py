@@ -404,9 +404,11 @@ def test_driver_reproduces_circ6_sw_aerosol(gpu_lib, tmp_path, to_cdf):
 
 
 @pytest.mark.gpu
-def test_driver_three_regions(gpu_lib, tmp_path):
+@pytest.mark.parametrize("scheme", ["triple", "part_corr_cnv"])
+def test_driver_three_regions(gpu_lib, tmp_path, scheme):
     """Three regions through the column driver (-C 6 -K 3, solver 17 by
-    default): the 7460_28 long-wave column with 40 % of its cloud made
+    default; -C 8 with -dp 3000 +dp 1000 for partially correlated like
+    regions): the 7460_28 long-wave column with 40 % of its cloud made
     convective (.ccfr) and denser convective water (.lwmcv), .clfr holding
     the stratiform rest.  The written heating rates match the oracle on the
     same clouds (set up as input_cloud_cdf.f does: stratiform water and ice
@@ -430,6 +432,9 @@ def test_driver_three_regions(gpu_lib, tmp_path):
         text = (tmp_path / f"7460_28.{src}").read_text().replace(f"7460_28.{src}", f"7460_28.{dst}")
         (tmp_path / f"7460_28.{dst}").write_text(text)
     opts = "-R 1 9 -I -t 12 +R -g 2 -c -C 6 -K 3 -d 1 -i 1 +d 1 +i 1".split()
+    if scheme == "part_corr_cnv":
+        opts[opts.index("-C") + 1] = "8"
+        opts += "-dp 3000 +dp 1000".split()
     r = subprocess.run([tool, "-s", str(sp_path)] + opts + ["-B", str(base)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     _, got = field(str(base) + ".hrts")
@@ -443,7 +448,8 @@ def test_driver_three_regions(gpu_lib, tmp_path):
                    condensed_dim_char=np.asfortranarray(np.concatenate([dc, dc], axis=2)),
                    frac_cloud=np.asfortranarray(np.stack([np.where(w > 0, 0.6, 0.0), np.where(w > 0, 0.4, 0.0)],
                                                          axis=2)))
-    ctl = replace(ctl, i_cloud=abi.IP_CLOUD_TRIPLE, i_solver=abi.IP_SOLVER_TRIPLE_HOGAN,
-                  i_cloud_representation=abi.IP_CLOUD_CONV_STRAT)
+    ctl = replace(ctl, i_cloud=abi.IP_CLOUD_TRIPLE if scheme == "triple" else abi.IP_CLOUD_PART_CORR_CNV,
+                  i_solver=abi.IP_SOLVER_TRIPLE_HOGAN, i_cloud_representation=abi.IP_CLOUD_CONV_STRAT)
+    col.cld.update(dp_corr_strat=3000.0, dp_corr_conv=1000.0)
     ref = K.printed(O.radiance_calc(ctl, sp, col), col, "hrts")[0]
     assert K.half_units(got, ref).max() <= 1.05
